@@ -1,0 +1,163 @@
+"""Run set-up: switches, seeded soundings and initial states of the benchmark workloads.
+
+The switches mirror the model defaults of ``AtmosphereModel`` (src/core/model.ts:747-844) with the SUMMER_DAY
+configuration (src/core/fixtures.ts:6-12): WENO transport, ice microphysics (one-moment), anisotropic Smagorinsky
+width, explicit vertical mixing, theta-e moist stability, pressure in the RK3 stages, wind relaxation 1e-4 1/s,
+sponge 0.06 1/s. The single-storm mode (``single``: no sun, no surface pattern, src/core/config.ts:147-152) is the
+only surface mode the device step supports.
+
+Initial state: the ``ellipsoid`` start (src/core/model.ts:94, :431-437) with the amplitude as a parameter, plus
+seeded uniform noise below a height, drawn with ``mulberry32`` (src/core/math.ts:7-14) in node order.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field, asdict
+from typing import Dict, List, Optional, Tuple
+
+import numpy as np
+
+from .environment import (CP, G, OMEGA, Environment, EnvironmentProfile, SliderConfig, tanh_shear, weisman_klemp)
+from .grid import Grid
+
+#: The transported fields in the order the step carries them (src/core/model.ts:1319-1335, ice on, no lightning).
+CARRIED = ("rain", "snow", "graupel", "hail", "u", "v", "w", "theta", "q", "cloud", "ice", "iceNumber", "cold")
+#: The fields the subgrid turbulence mixes (src/core/model.ts:1338-1344).
+MIXED = ("u", "v", "w", "theta", "q", "cloud", "ice", "iceNumber")
+SMAGORINSKY = 0.18
+SURFACE_ROUGHNESS = {"grass": 0.03, "dry": 0.01, "water": 0.0002, "urban": 1.0}
+
+
+def mulberry32(seed: int):
+    """The reference's seeded generator (src/core/math.ts:7-14), 32-bit integer semantics of JS."""
+    state = [seed & 0xFFFFFFFF]
+
+    def imul(a: int, b: int) -> int:
+        return (a * b) & 0xFFFFFFFF
+
+    def nxt() -> float:
+        s = (state[0] + 0x6D2B79F5) & 0xFFFFFFFF
+        state[0] = s
+        t = imul(s ^ (s >> 15), 1 | s)
+        t = ((t + imul(t ^ (t >> 7), 61 | t)) & 0xFFFFFFFF) ^ t
+        return ((t ^ (t >> 14)) & 0xFFFFFFFF) / 4294967296.0
+
+    return nxt
+
+
+def drag_coefficient(surface: str, dz: float) -> float:
+    """Neutral drag coefficient of the ground node (src/core/surface.ts:9)."""
+    return (0.4 / math.log(dz / 4 / SURFACE_ROUGHNESS[surface])) ** 2
+
+
+@dataclass
+class Switches:
+    """Scalar settings of a run: the POD ``sg_switches`` of the C ABI (field for field)."""
+    dt: float = 3.0
+    coriolis: float = 2 * OMEGA * math.sin(45 * math.pi / 180)  # f at SUMMER_DAY's latitude 45
+    wind_relaxation: float = 1e-4
+    sponge_rate: float = 0.06
+    sponge_start: float = 14_000.0  # max(tropopause*1000 + 2500, 14 km) with tropopause 11 km
+    cs: float = SMAGORINSKY         # SMAGORINSKY * turbulence / .55 with the default slider .55
+    drag: float = 1.0               # 1: surface drag on (coefficient from the surface type), 0: off
+    surface: str = "grass"
+    frame_u: float = 0.0
+    frame_v: float = 0.0
+    loading: int = 1
+    evaporation: int = 1
+    rain_formation: int = 1
+    anisotropic: int = 1
+    vertical_dz: int = 0
+    durran_klemp: int = 0
+    pressure_in_stages: int = 1
+
+    def drag_cd(self, grid: Grid) -> float:
+        return drag_coefficient(self.surface, 2 * float(grid.hz[0])) if self.drag else 0.0
+
+
+@dataclass
+class RunSpec:
+    """Everything that defines one run: its grid, environment, switches and initial fields."""
+    grid: Grid
+    env: Environment
+    switches: Switches
+    fields: Dict[str, np.ndarray]
+    seed: int = 0
+    label: str = ""
+
+    @property
+    def cells(self) -> int:
+        return self.grid.n
+
+
+def baseline_profile(qv_max: float = 0.014, shear: float = 20.0, veer: float = 0.0) -> EnvironmentProfile:
+    """The analytic benchmark sounding: Weisman-Klemp theta and RH, qv capped, wind ``shear * tanh(z / 3 km)``."""
+    return weisman_klemp(qv_max=qv_max, wind=tanh_shear(shear, 3000.0, veer))
+
+
+def initial_fields(grid: Grid, env: Environment, seed: int, bubble: float = 2.0, noise: float = 0.1,
+                   noise_top: float = 1000.0, frame: Tuple[float, float] = (0.0, 0.0),
+                   across: float = 1 / 3) -> Dict[str, np.ndarray]:
+    """Initial fields: environment profile, a cos^2 ellipsoid bubble (radii 10 km / 1.4 km at 1.4 km, a third of the
+    way in from the west, src/core/model.ts:94), uniform noise of +-``noise`` K below ``noise_top``; FP32 like the
+    reference's ``Float32Array`` fields."""
+    nx, ny, nz = grid.nx, grid.ny, grid.nz
+    zs = grid.zs
+    rng = mulberry32(seed)
+    theta = np.empty((nz, ny, nx))
+    q = np.empty((nz, ny, nx))
+    u = np.empty((nz, ny, nx))
+    v = np.empty((nz, ny, nx))
+    for z in range(nz):
+        theta[z] = env.theta[z]
+        q[z] = env.q[z]
+        u[z] = env.u[z] - frame[0]
+        v[z] = env.v[z] - frame[1]
+        if zs[z] < noise_top and noise > 0:
+            draws = np.array([rng() for _ in range(nx * ny)]).reshape(ny, nx)
+            theta[z] += (draws - 0.5) * 2 * noise
+    theta32 = theta.astype(np.float32)
+    if bubble:
+        radius, depth, height = 10_000.0, 1400.0, 1400.0
+        x = np.arange(nx) * grid.dx - grid.width * across
+        y = np.arange(ny) * grid.dy - grid.depth / 2
+        for z in range(nz):
+            beta = np.sqrt((x[None, :] / radius) ** 2 + (y[:, None] / radius) ** 2 + ((zs[z] - height) / depth) ** 2)
+            inside = beta < 1
+            if inside.any():
+                add = bubble * np.cos(np.pi * beta / 2) ** 2
+                layer = theta32[z].astype(np.float64)
+                layer[inside] += add[inside]
+                theta32[z] = layer.astype(np.float32)
+    zero = np.zeros(grid.n, dtype=np.float32)
+    out = {name: zero.copy() for name in CARRIED}
+    out["u"] = u.astype(np.float32).ravel()
+    out["v"] = v.astype(np.float32).ravel()
+    out["theta"] = theta32.ravel()
+    out["q"] = q.astype(np.float32).ravel()
+    return out
+
+
+def baseline_run(grid: Grid, seed: int = 42, bubble: float = 2.0, qv_max: float = 0.014, shear: float = 20.0,
+                 veer: float = 0.0, switches: Optional[Switches] = None, label: str = "") -> RunSpec:
+    """One run of the benchmark configuration on ``grid`` (analytic sounding, single-storm mode)."""
+    env = Environment(SliderConfig(), grid, baseline_profile(qv_max, shear, veer))
+    sw = switches or Switches()
+    fields = initial_fields(grid, env, seed, bubble, frame=(sw.frame_u, sw.frame_v))
+    return RunSpec(grid, env, sw, fields, seed, label)
+
+
+def ensemble_members(grid: Grid, count: int, seed: int = 2026) -> List[RunSpec]:
+    """Seeded ensemble members: surface qv U[11, 16] g/kg, 0-6 km shear U[0, 30] m/s with a veering of U[0, 90] deg,
+    bubble amplitude U[1, 3] K; each member's own noise seed."""
+    rng = np.random.default_rng(seed)
+    runs = []
+    for k in range(count):
+        qv = rng.uniform(0.011, 0.016)
+        shear6 = rng.uniform(0.0, 30.0)
+        veer = rng.uniform(0.0, 90.0)
+        bubble = rng.uniform(1.0, 3.0)
+        # tanh(z / 3 km) reaches tanh(2) at 6 km: scale so that the 0-6 km difference is shear6.
+        runs.append(baseline_run(grid, seed=seed * 1000 + k, bubble=bubble, qv_max=qv,
+                                 shear=shear6 / math.tanh(2.0), veer=veer, label=f"member{k}"))
+    return runs

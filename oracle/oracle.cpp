@@ -1,0 +1,183 @@
+// TEST INFRASTRUCTURE ONLY — C entry points of the oracle (a CPU restatement of the reference's StormLab step,
+// see oracle_core.h). Loaded by oracle/pyoracle.py for tests/, __graft_entry__.smoke() and bench.py's CPU legs.
+#include "oracle_model.h"
+
+using namespace orc;
+
+namespace {
+struct Handle {
+  bool fp64;
+  Model<float>* m32 = nullptr;
+  Model<double>* m64 = nullptr;
+};
+
+GridSpec makeGrid(int nx, int ny, int nz, double dx, double dy, double dz, double height, const double* zs, const double* dzs, const double* hz) {
+  GridSpec g; g.nx = nx; g.ny = ny; g.nz = nz; g.dx = dx; g.dy = dy; g.dz = dz; g.width = dx * nx; g.depth = dy * ny; g.height = height;
+  g.zs.assign(zs, zs + nz); g.dzs.assign(dzs, dzs + nz - 1); g.hz.assign(hz, hz + nz); g.finish();
+  return g;
+}
+
+Switches makeSwitches(const double* s) {
+  Switches w;
+  w.coriolis = s[0]; w.windRelaxation = s[1]; w.spongeRate = s[2]; w.spongeStart = s[3]; w.cs = s[4]; w.dragCd = s[5];
+  w.frameU = s[6]; w.frameV = s[7]; w.loading = s[8] != 0; w.evaporation = s[9] != 0; w.rainFormation = s[10] != 0;
+  w.anisotropic = s[11] != 0; w.verticalDz = s[12] != 0; w.durranKlemp = s[13] != 0; w.pressureInStages = s[14] != 0;
+  w.ice = s[15] != 0; w.sensible = s[16]; w.latent = s[17]; w.surfaceOn = s[18] != 0; w.slabs = (int)s[19];
+  return w;
+}
+
+template <class S> std::vector<S>* extraField(Model<S>* m, int id) {
+  switch (id) {
+    case 100: return &m->precipitation; case 101: return &m->hailGround; case 102: return &m->hailSize;
+    case 103: return &m->fallRain; case 104: return &m->fallSnow; case 105: return &m->fallGraupel; case 106: return &m->fallHail;
+    case 107: return &m->condensate;
+  }
+  return (id >= 0 && id < N_CARRIED) ? &m->f[id] : nullptr;
+}
+}  // namespace
+
+extern "C" {
+
+// Model. env7 = p, exner, theta, q, u, v, rho (each nz, FP64). sw = 20 switches (makeSwitches).
+void* orc_create(int fp64, int nx, int ny, int nz, double dx, double dy, double dz, double height, const double* zs, const double* dzs,
+                 const double* hz, const double* env7, const double* sw, int threads) {
+  Handle* h = new Handle; h->fp64 = fp64 != 0;
+  GridSpec g = makeGrid(nx, ny, nz, dx, dy, dz, height, zs, dzs, hz); Switches s = makeSwitches(sw);
+  if (h->fp64) h->m64 = new Model<double>(g, env7, s, threads); else h->m32 = new Model<float>(g, env7, s, threads);
+  return h;
+}
+void orc_destroy(void* p) { Handle* h = (Handle*)p; delete h->m32; delete h->m64; delete h; }
+void orc_set_threads(void* p, int threads) {
+  Handle* h = (Handle*)p;
+  if (h->m32) h->m32->nthreads = std::min(threads, (int)h->m32->dscr.size());
+  if (h->m64) h->m64->nthreads = std::min(threads, (int)h->m64->dscr.size());
+}
+// Field ids: 0..12 carried (rain, snow, graupel, hail, u, v, w, theta, q, cloud, ice, iceNumber, cold); 100 precipitation,
+// 101 hailGround, 102 hailSize, 103-106 fall speeds, 107 condensate.
+int orc_set_field(void* p, int id, const double* src, long count) {
+  Handle* h = (Handle*)p;
+  if (h->m32) { auto* v = extraField(h->m32, id); if (!v || (long)v->size() != count) return -1; for (long i = 0; i < count; i++) (*v)[i] = (float)src[i]; }
+  else { auto* v = extraField(h->m64, id); if (!v || (long)v->size() != count) return -1; for (long i = 0; i < count; i++) (*v)[i] = src[i]; }
+  return 0;
+}
+int orc_get_field(void* p, int id, double* dst, long count) {
+  Handle* h = (Handle*)p;
+  if (h->m32) { auto* v = extraField(h->m32, id); if (!v || (long)v->size() != count) return -1; for (long i = 0; i < count; i++) dst[i] = (*v)[i]; }
+  else { auto* v = extraField(h->m64, id); if (!v || (long)v->size() != count) return -1; for (long i = 0; i < count; i++) dst[i] = (*v)[i]; }
+  return 0;
+}
+// Steps with time += dt after each (src/core/fixtures.ts:28-30).
+void orc_step(void* p, double dt, int steps) {
+  Handle* h = (Handle*)p;
+  for (int s = 0; s < steps; s++) {
+    if (h->m32) { h->m32->step(dt); h->m32->time += dt; } else { h->m64->step(dt); h->m64->time += dt; }
+  }
+}
+// Stages of one step, for stage-wise parity: 1 = beginStep, 2 = dynamics, 3 = physicsStep, 4 = mixStep, 5 = final project.
+void orc_step_part(void* p, double dt, int part) {
+  Handle* h = (Handle*)p;
+  auto go = [&](auto* m) {
+    switch (part) {
+      case 1: m->beginStep(dt); break; case 2: m->dynamics(dt); break; case 3: m->physicsStep(dt); break;
+      case 4: m->mixStep(dt); break; case 5: m->project(dt, true); m->time += dt; break;
+    }
+  };
+  if (h->m32) go(h->m32); else go(h->m64);
+}
+int orc_get_pressure(void* p, double* dst, long count) {
+  Handle* h = (Handle*)p; auto& v = h->m32 ? h->m32->pressure : h->m64->pressure;
+  if ((long)v.size() != count) return -1; std::memcpy(dst, v.data(), count * sizeof(double)); return 0;
+}
+int orc_get_faces(void* p, double* mx, double* my, double* mz, double* dv, long count) {
+  Handle* h = (Handle*)p; FluxTransport& f = h->m32 ? h->m32->flux : h->m64->flux;
+  if ((long)f.mx.size() != count) return -1;
+  std::memcpy(mx, f.mx.data(), count * 8); std::memcpy(my, f.my.data(), count * 8); std::memcpy(mz, f.mz.data(), count * 8); std::memcpy(dv, f.div.data(), count * 8);
+  return 0;
+}
+// counters: clipped, negativeFilled, water condensed, evaporated, rainEvaporated, surface, time.
+void orc_counters(void* p, double* out) {
+  Handle* h = (Handle*)p;
+  auto fill = [&](auto* m) { out[0] = m->clipped; out[1] = m->negativeFilled; for (int k = 0; k < 4; k++) out[2 + k] = m->water[k]; out[6] = m->time; };
+  if (h->m32) fill(h->m32); else fill(h->m64);
+}
+
+// ---------------------------------------------------------------- known-answer hooks (reference unit tests)
+double orc_weno(double a, double b, double c, double d, double e) { return weno(a, b, c, d, e); }
+double orc_upwind5(double a, double b, double c, double d, double e) { return upwind5(a, b, c, d, e); }
+double orc_qsat(double t, double p) { return qsatP(t, p); }
+double orc_qsat_ice(double t, double p) { return qsatIce(t, p); }
+double orc_fall_speed(double rain, double rho, double rhoGround) { return fallSpeed(rain, rho, rhoGround); }
+double orc_snow_fall_speed(double snow, double rho, double rhoGround) { return snowFallSpeed(snow, rho, rhoGround); }
+double orc_graupel_fall_speed(double x, double rho) { return graupelFallSpeed(x, rho); }
+double orc_hail_fall_speed(double x, double rho) { return hailFallSpeed(x, rho); }
+double orc_hail_max_diameter(double x, double rho) { return hailMaxDiameter(x, rho); }
+double orc_cooper(double tc) { return cooperCrystals(tc); }
+double orc_splintering(double tc) { return splintering(tc); }
+double orc_fragments(double lambda) { return fragmentsPerKg(lambda); }
+double orc_koenig(double tc, double m) { return koenigGrowth(tc, m); }
+double orc_plate_size(double m) { return plateSize(m); }
+double orc_crystal_size(double qi, double n, double rho) { return crystalSize(qi, n, rho); }
+
+// Cell processes on float32 cells (the reference tests use Float32Array.of): v = [theta, q, cloud, ice, snow, rain, graupel, hail, number].
+double orc_cell(int which, float* v, double exner, double p, double rho, double dt, double aux) {
+  Arr<float> th = (Arr<float>)&v[0], q = (Arr<float>)&v[1], cl = (Arr<float>)&v[2], ic = (Arr<float>)&v[3], sn = (Arr<float>)&v[4];
+  Arr<float> rn = (Arr<float>)&v[5], gr = (Arr<float>)&v[6], ha = (Arr<float>)&v[7], nb = (Arr<float>)&v[8];
+  switch (which) {
+    case 0: return rainProcesses<float>(q, cl, rn, 0, aux, p, rho, dt, true);          // aux = tk
+    case 1: return saturationAdjust<float>(th, q, cl, 0, exner, p);
+    case 2: return saturationAdjustMixed<float>(th, q, cl, ic, 0, exner, p, aux != 0 ? nb : nullptr);
+    case 3: freezeRain<float>(th, rn, gr, 0, exner); return 0;
+    case 4: return iceProcesses<float>(th, q, ic, sn, nb, 0, exner, p, rho, dt);
+    case 5: return snowProcesses<float>(th, q, cl, ic, sn, rn, 0, exner, p, rho, aux, dt);  // aux = rhoGround
+    case 6: return graupelProcesses<float>(th, q, cl, ic, sn, rn, gr, 0, exner, p, rho, dt);
+    case 7: return hailProcesses<float>(th, q, cl, ic, sn, rn, gr, ha, 0, exner, p, rho, dt);
+    case 8: settleCrystals<float>(ic, nb, 0); return 0;
+  }
+  return NAN;
+}
+
+// FFT of length n in place (sign -1 forward, +1 unnormalised inverse).
+void orc_fft(int n, double* re, double* im, int sign) { FFT f(n); f.transform(re, im, sign); }
+// HorizontalDFT forward of `layers` layers of src; spectra into re/im (nx*ny*layers); then inverse into out.
+void orc_hdft(int nx, int ny, int layers, const double* src, double* re, double* im, double* out) {
+  HorizontalDFT d(nx, ny, layers); DftScratch s(nx, ny);
+  d.forwardLayers([src](size_t i) { return src[i]; }, 0, layers, s);
+  std::memcpy(re, d.re.data(), d.re.size() * 8); std::memcpy(im, d.im.data(), d.im.size() * 8);
+  d.inverseLayers([out](size_t i, double v) { out[i] = v; }, 0, layers, s);
+}
+// Pressure projection on float velocities: divergence before/after into div0/div1 (cells), pressure into p.
+void orc_pressure_project(int nx, int ny, int nz, double dx, double dy, double dz, double height, const double* zs, const double* dzs, const double* hz,
+                          const double* rho, float* u, float* v, float* w, double dt, double* div0, double* div1, double* pOut) {
+  GridSpec g = makeGrid(nx, ny, nz, dx, dy, dz, height, zs, dzs, hz);
+  PressureSolver s(g, rho); DftScratch ds(nx, ny); ModeScratch ms(nz);
+  Arr<float> U = (Arr<float>)u, V = (Arr<float>)v, W = (Arr<float>)w;
+  s.divergence<float>(U, V, W, dt, div0, 0, nz - 1);
+  s.transform(div0, 0, nz - 1, ds); s.modes(0, ny, ms); s.back(pOut, 0, nz - 1, ds);
+  s.correct<float>(pOut, U, V, W, dt, 0, nz);
+  s.divergence<float>(U, V, W, dt, div1, 0, nz - 1);
+}
+// Transport: face fluxes of (u, v, w) projected, then `steps` advect() calls on q (float) with dt. Faces out (may be null).
+void orc_transport(int nx, int ny, int nz, double dx, double dy, double dz, double height, const double* zs, const double* dzs, const double* hz,
+                   const double* rho, const float* u, const float* v, const float* w, float* q, double dt, int steps, int monotone,
+                   double* mx, double* my, double* mz, double* div) {
+  GridSpec g = makeGrid(nx, ny, nz, dx, dy, dz, height, zs, dzs, hz);
+  FluxTransport t(g, rho); DftScratch ds(nx, ny); ModeScratch ms(nz); TendScratch ts(g.n, nz * ny); std::vector<double> tend(g.n);
+  t.setVelocity<float>((Arr<float>)u, (Arr<float>)v, (Arr<float>)w, ds, ms);
+  if (mx) { std::memcpy(mx, t.mx.data(), g.n * 8); std::memcpy(my, t.my.data(), g.n * 8); std::memcpy(mz, t.mz.data(), g.n * 8); std::memcpy(div, t.div.data(), g.n * 8); }
+  for (int s = 0; s < steps; s++) t.advect<float>((Arr<float>)q, dt, monotone != 0, ts, tend);
+}
+// Turbulence: viscosity into km/kh (dry when q null), then `steps` mix() calls on a with base/factor when a is not null.
+void orc_turbulence(int nx, int ny, int nz, double dx, double dy, double dz, double height, const double* zs, const double* dzs, const double* hz,
+                    const double* rho, const float* u, const float* v, const float* w, const float* theta, const double* thetaEnv, double cs, double dt,
+                    const float* q, const float* cond, const double* exner, int anisotropic, int verticalDz, int implicitV, int durranKlemp,
+                    const double* kmIn, const double* khIn, double* km, double* kh, float* a, const double* base, double factor, int steps) {
+  GridSpec g = makeGrid(nx, ny, nz, dx, dy, dz, height, zs, dzs, hz);
+  Turbulence t(g, rho); t.anisotropic = anisotropic; t.verticalDz = verticalDz; t.implicitVertical = implicitV; t.durranKlemp = durranKlemp;
+  if (kmIn) { std::memcpy(t.km.data(), kmIn, g.n * 8); std::memcpy(t.kh.data(), khIn, g.n * 8); }
+  else t.viscosity<float>((Arr<float>)u, (Arr<float>)v, (Arr<float>)w, (Arr<float>)theta, thetaEnv, cs, dt, (Arr<float>)q, (Arr<float>)cond, exner, 0, nz);
+  if (km) { std::memcpy(km, t.km.data(), g.n * 8); std::memcpy(kh, t.kh.data(), g.n * 8); }
+  std::vector<float> tmp(g.n);
+  if (a) for (int s = 0; s < steps; s++) t.mix<float>((Arr<float>)a, base, factor, dt, tmp);
+}
+
+}  // extern "C"

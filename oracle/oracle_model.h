@@ -1,0 +1,322 @@
+// TEST INFRASTRUCTURE ONLY — the oracle's model step (see oracle_core.h).
+// Restates AtmosphereModel.step (src/core/model.ts:873-877) for the configuration of the device path: flat ground,
+// WENO transport with the pressure and buoyancy in the RK3 stages, one-moment microphysics (ice or warm), no
+// lightning, no budget tracers, no zones/fronts/large-scale forcing, no nudging, periodic edges. Phases run on
+// OpenMP threads over the reference's own task split (src/core/threads.ts:44-48): every task writes only its own
+// outputs and every sum is taken in task order afterwards, so results are bit-identical for any thread count.
+#pragma once
+#include <omp.h>
+#include "oracle_solvers.h"
+
+namespace orc {
+
+struct Switches {
+  double coriolis = 0, windRelaxation = 1e-4, spongeRate = .06, spongeStart = 14000, cs = SMAGORINSKY, dragCd = 0;
+  double frameU = 0, frameV = 0, sensible = 0, latent = 0;
+  bool loading = true, evaporation = true, rainFormation = true, anisotropic = true, verticalDz = false, durranKlemp = false;
+  bool pressureInStages = true, ice = true, surfaceOn = true;
+  int slabs = 1;
+};
+
+enum FieldId { F_RAIN, F_SNOW, F_GRAUPEL, F_HAIL, F_U, F_V, F_W, F_THETA, F_Q, F_CLOUD, F_ICE, F_ICENUMBER, F_COLD, N_CARRIED };
+
+template <class S> struct Model {
+  GridSpec g;
+  std::vector<double> p, exner, thetaEnv, qEnv, uGround, vGround, rho, uEnv, vEnv, levelWeight, surfaceShare;
+  Switches sw;
+  std::vector<S> f[N_CARRIED];
+  std::vector<S> fallRain, fallSnow, fallGraupel, fallHail, condensate, precipitation, hailGround, hailSize, levelWater;
+  std::vector<S> stageStart[N_CARRIED]; std::vector<double> stageTend[N_CARRIED];
+  FluxTransport flux; PressureSolver solver; Turbulence turb;
+  std::vector<double> pressure, divergence;
+  double negativeFilled = 0, time = 0; double clipped = 0;
+  double water[4] = {0, 0, 0, 0};
+  double taskNegative[N_CARRIED] = {0};
+  std::vector<int> groundCell; std::vector<double> groundWeight;
+  int nthreads;
+  std::vector<DftScratch> dscr; std::vector<ModeScratch> mscr; std::vector<TendScratch> tscr; std::vector<std::vector<S>> mixTmp;
+
+  Arr<S> F(int k) { return reinterpret_cast<Arr<S>>(f[k].data()); }
+  static Arr<S> A(std::vector<S>& v) { return reinterpret_cast<Arr<S>>(v.data()); }
+
+  Model(const GridSpec& grid, const double* env7, const Switches& s, int threads) : g(grid), sw(s), nthreads(threads) {
+    int nz = g.nz, n = g.n, layer = g.layer;
+    auto lvl = [&](int k) { return std::vector<double>(env7 + k * nz, env7 + (k + 1) * nz); };
+    p = lvl(0); exner = lvl(1); thetaEnv = lvl(2); qEnv = lvl(3); uGround = lvl(4); vGround = lvl(5); rho = lvl(6);
+    uEnv.resize(nz); vEnv.resize(nz);
+    for (int z = 0; z < nz; z++) { uEnv[z] = uGround[z] - sw.frameU; vEnv[z] = vGround[z] - sw.frameV; }
+    for (int k = 0; k < N_CARRIED; k++) { f[k].assign(n, 0); stageStart[k].assign(n, 0); stageTend[k].assign(n, 0); }
+    fallRain.assign(n, 0); fallSnow.assign(n, 0); fallGraupel.assign(n, 0); fallHail.assign(n, 0); condensate.assign(n, 0);
+    precipitation.assign(layer, 0); hailGround.assign(layer, 0); hailSize.assign(layer, 0); levelWater.assign(nz * 4, 0);
+    flux = FluxTransport(g, rho.data()); solver = PressureSolver(g, rho.data()); turb = Turbulence(g, rho.data());
+    flux.g = &g; solver.g = &g; turb.g = &g;
+    turb.anisotropic = sw.anisotropic; turb.verticalDz = sw.verticalDz; turb.durranKlemp = sw.durranKlemp;
+    pressure.assign(solver.cells, 0); divergence.assign(solver.cells, 0);
+    levelWeight.resize(nz);
+    for (int z = 0; z < nz; z++) levelWeight[z] = g.hz[z] / g.dz * rho[z];  // src/core/model.ts:386
+    // sharesAbove(0) (src/core/model.ts:762-767)
+    int first500 = -1; for (int z = 0; z < nz; z++) if (g.zs[z] - g.zs[0] >= 500) { first500 = z; break; }
+    int low = std::max(2, first500); double total = 0; surfaceShare.assign(low, 0);
+    for (int z = 0; z < low; z++) { surfaceShare[z] = std::exp(-(g.zs[z] - g.zs[0]) / 300); total += surfaceShare[z] * g.hz[z]; }
+    for (int z = 0; z < low; z++) surfaceShare[z] /= total;
+    groundCell.assign(layer * 4, 0); groundWeight.assign(layer * 4, 0);
+    dscr.resize(threads); mscr.resize(threads); tscr.resize(threads); mixTmp.resize(threads);
+    for (int t = 0; t < threads; t++) { dscr[t] = DftScratch(g.nx, g.ny); mscr[t] = ModeScratch(nz); tscr[t] = TendScratch(n, nz * g.ny); mixTmp[t].assign(n, 0); }
+  }
+
+  template <class Fn> void run(int tasks, Fn fn) {
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+    for (int k = 0; k < tasks; k++) fn(k, omp_get_thread_num());
+  }
+
+  struct Carried { int k; bool monotone, conserve; double decay; };
+  std::vector<Carried> carried() const {  // src/core/model.ts:1319-1335
+    std::vector<Carried> c;
+    c.push_back({F_RAIN, true, true, 1});
+    if (sw.ice) { c.push_back({F_SNOW, true, true, 1}); c.push_back({F_GRAUPEL, true, true, 1}); c.push_back({F_HAIL, true, true, 1}); }
+    for (int k : {F_U, F_V, F_W, F_THETA}) c.push_back({k, false, false, 1});
+    c.push_back({F_Q, true, true, 1}); c.push_back({F_CLOUD, true, true, 1});
+    if (sw.ice) { c.push_back({F_ICE, true, true, 1}); c.push_back({F_ICENUMBER, true, false, 1}); }
+    c.push_back({F_COLD, true, false, .9992});
+    return c;
+  }
+
+  // ---------------------------------------------------------- beginStep (src/core/model.ts:893-902)
+  void updateGround() {  // :644-657 (the surface pattern, city and zones are zero in the device's configuration)
+    int nx = g.nx, ny = g.ny; double ox = sw.frameU * time, oy = sw.frameV * time;
+    double sx = jmod(ox / g.dx, nx), sy = jmod(oy / g.dy, ny);
+    int x0 = (int)std::floor(sx), y0 = (int)std::floor(sy); double fx = sx - x0, fy = sy - y0;
+    for (int y = 0; y < ny; y++) for (int x = 0; x < nx; x++) {
+      int i = x + nx * y, ax = (x + x0) % nx, bx = (ax + 1) % nx, ay = (y + y0) % ny * nx, by = (ay / nx + 1) % ny * nx, k = i * 4;
+      groundCell[k] = ax + ay; groundCell[k + 1] = bx + ay; groundCell[k + 2] = ax + by; groundCell[k + 3] = bx + by;
+      groundWeight[k] = (1 - fx) * (1 - fy); groundWeight[k + 1] = fx * (1 - fy); groundWeight[k + 2] = (1 - fx) * fy; groundWeight[k + 3] = fx * fy;
+    }
+  }
+  void deposit(int i, double mm, std::vector<S>& target) {  // :691-694
+    Arr<S> t = A(target); int k = i * 4;
+    for (int j = 0; j < 4; j++) if (groundWeight[k + j] > 0) t[groundCell[k + j]] += groundWeight[k + j] * mm;
+  }
+  void fall(int k) {  // 'fall' task (:1220-1235), one-moment
+    int layer = g.layer; Arr<S> rain = F(F_RAIN), snow = F(F_SNOW), graupel = F(F_GRAUPEL), hail = F(F_HAIL);
+    Arr<S> fr = A(fallRain), fs = A(fallSnow), fg = A(fallGraupel), fh = A(fallHail);
+    for (int i = k * layer, end = i + layer; i < end; i++) {
+      fr[i] = fallSpeed(rain[i], rho[k], rho[0]); fs[i] = snowFallSpeed(snow[i], rho[k], rho[0]);
+      fg[i] = graupelFallSpeed(graupel[i], rho[k]); fh[i] = hailFallSpeed(hail[i], rho[k]);
+    }
+  }
+  void collectHail(double dt) {  // :697-706
+    int layer = g.layer; Arr<S> hail = F(F_HAIL), fh = A(fallHail), hs = A(hailSize);
+    for (int b = 0; b < layer; b++) {
+      int i = b; double h = hail[i];
+      if (!(h > 1e-9)) continue;
+      deposit(b, rho[0] * h * (double)fh[i] * dt, hailGround);
+      double size = hailMaxDiameter(hail[i], rho[0]) * 1000;
+      for (int j = 0; j < 4; j++) if (groundWeight[b * 4 + j] > 0) { int c = groundCell[b * 4 + j]; hs[c] = jmax(hs[c], size); }
+    }
+  }
+  int fallParts(Arr<S> rain, Arr<S> vt, double dt) {  // :575-580
+    int nz = g.nz, layer = g.layer; double courant = 0;
+    for (int z = 0; z < nz; z++) { double c = dt * rho[z] / (levelWeight[z] * g.dz); for (int i = z * layer; i < (z + 1) * layer; i++) if ((double)rain[i] != 0) courant = jmax(courant, c * (double)vt[i] / 1); }
+    return (int)jmax(1, std::ceil(courant / .8));
+  }
+  void sedimentPart(Arr<S> rain, Arr<S> vt, double dt) {  // :582-598 (flat ground, water deposited)
+    int nz = g.nz, layer = g.layer;
+    for (int c = 0; c < layer; c++) deposit(c, rho[0] * (double)rain[c] * (double)vt[c] * dt, precipitation);
+    run(64, [&](int part, int) {
+      int c0 = (int)((long)part * layer / 64), c1 = (int)((long)(part + 1) * layer / 64);
+      for (int z = 0; z < nz; z++) {
+        int l = z * layer; double inflow = z < nz - 1 ? rho[z + 1] : 0;
+        for (int i = l + c0; i < l + c1; i++)
+          rain[i] += dt * (inflow * (z < nz - 1 ? (double)rain[i + layer] * (double)vt[i + layer] : 0) - rho[z] * (double)rain[i] * (double)vt[i]) / (levelWeight[z] * g.dz * 1);
+      }
+    });
+  }
+  void sedimentStep(double dt) {  // :928-932
+    std::pair<int, std::vector<S>*> falls[4] = {{F_RAIN, &fallRain}, {F_SNOW, &fallSnow}, {F_GRAUPEL, &fallGraupel}, {F_HAIL, &fallHail}};
+    for (int j = 0; j < (sw.ice ? 4 : 1); j++) {
+      Arr<S> field = F(falls[j].first), vt = A(*falls[j].second);
+      int parts = fallParts(field, vt, dt);
+      for (int q = 0; q < parts; q++) sedimentPart(field, vt, dt / parts);
+    }
+  }
+  void beginStep(double dt) {
+    updateGround();
+    run(g.nz, [&](int k, int) { fall(k); });
+    if (sw.ice) collectHail(dt);
+    sedimentStep(dt);
+  }
+
+  // ---------------------------------------------------------- dynamics (src/core/model.ts:1029-1051)
+  void stageBuoyancy(double* tend, int z0, int z1) {  // :1204-1214 (no zones)
+    int layer = g.layer; Arr<S> theta = F(F_THETA), q = F(F_Q), cloud = F(F_CLOUD), ice = F(F_ICE), rain = F(F_RAIN), snow = F(F_SNOW), graupel = F(F_GRAUPEL), hail = F(F_HAIL);
+    for (int z = z0; z < z1; z++) {
+      double thEnv = thetaEnv[z], qE = qEnv[z], thvEnv = thEnv * (1 + .61 * qE);
+      for (int i = z * layer, c = 0; c < layer; i++, c++) {
+        double ref = thvEnv;
+        double loaded = (double)cloud[i] + (double)ice[i] + (sw.loading ? (double)rain[i] + (double)snow[i] + (double)graupel[i] + (double)hail[i] : 0);
+        tend[i] += G * (((double)theta[i] * (1 + .61 * (double)q[i]) - ref) / ref - loaded);
+      }
+    }
+  }
+  void project(double dt, bool limit) {  // :1575-1583
+    int nz = g.nz, ny = g.ny;
+    Arr<S> u = F(F_U), v = F(F_V), w = F(F_W);
+    run(nz - 1, [&](int k, int) { solver.divergence<S>(u, v, w, dt, divergence.data(), k, k + 1); });
+    run(nz - 1, [&](int k, int t) { solver.transform(divergence.data(), k, k + 1, dscr[t]); });
+    run(ny, [&](int n, int t) { solver.modes(n, n + 1, mscr[t]); });
+    run(nz - 1, [&](int k, int t) { solver.back(pressure.data(), k, k + 1, dscr[t]); });
+    run(nz, [&](int k, int) { solver.correct<S>(pressure.data(), u, v, w, dt, k, k + 1); });
+    if (limit) clipWind();
+  }
+  void clipWind() {  // :1586-1595
+    Arr<S> u = F(F_U), v = F(F_V), w = F(F_W); double c = 0;
+    for (int i = 0; i < g.n; i++) {
+      if ((double)u[i] < -U_LIMIT || (double)u[i] > U_LIMIT) { u[i] = clamp(u[i], -U_LIMIT, U_LIMIT); c++; }
+      if ((double)v[i] < -U_LIMIT || (double)v[i] > U_LIMIT) { v[i] = clamp(v[i], -U_LIMIT, U_LIMIT); c++; }
+      if ((double)w[i] < -W_LIMIT || (double)w[i] > W_LIMIT) { w[i] = clamp(w[i], -W_LIMIT, W_LIMIT); c++; }
+    }
+    clipped += c;
+  }
+  void faceProjection() {  // the 'faces' .. 'faceDivergence' phases (:1039)
+    int nz = g.nz, ny = g.ny; Arr<S> u = F(F_U), v = F(F_V), w = F(F_W);
+    run(nz, [&](int k, int) { flux.faces<S>(u, v, w, k, k + 1); });
+    run(nz, [&](int k, int) { flux.divergence(k, k + 1); });
+    run(nz, [&](int k, int t) { flux.forward(k, k + 1, dscr[t]); });
+    run(ny, [&](int n, int t) { flux.modes(n, n + 1, mscr[t]); });
+    run(nz, [&](int k, int t) { flux.inverse(k, k + 1, dscr[t]); });
+    run(nz, [&](int k, int) { flux.correctFaces(k, k + 1); });
+    run(nz, [&](int k, int) { flux.divergence(k, k + 1); });
+  }
+  void dynamics(double dt) {
+    int nz = g.nz, layer = g.layer;
+    faceProjection();
+    std::vector<Carried> c = carried(); int slabs = std::max(1, std::min(sw.slabs, nz)); int tasks = (int)c.size() * slabs;
+    for (int stage = 0; stage < 3; stage++) {
+      run(tasks, [&](int k, int t) {  // 'tendency{s}' (:1237-1249)
+        int fi = k / slabs, j = k % slabs; const Carried& cc = c[fi];
+        int z0 = (int)std::floor((double)j * nz / slabs), z1 = (int)std::floor((double)(j + 1) * nz / slabs);
+        Arr<S> a = F(cc.k);
+        if (stage == 0) for (size_t i = (size_t)z0 * layer; i < (size_t)z1 * layer; i++) stageStart[cc.k][i] = f[cc.k][i];
+        flux.tendency<S>(a, stageTend[cc.k].data(), z0, z1, cc.monotone, tscr[t]);
+        if (cc.k == F_W && sw.pressureInStages) stageBuoyancy(stageTend[cc.k].data(), z0, z1);
+      });
+      double fraction = RK3[stage] * dt;
+      run(tasks, [&](int k, int) {  // 'update{s}' (:1250)
+        int fi = k / slabs, j = k % slabs; const Carried& cc = c[fi];
+        int z0 = (int)std::floor((double)j * nz / slabs), z1 = (int)std::floor((double)(j + 1) * nz / slabs);
+        Arr<S> a = F(cc.k); const S* start = stageStart[cc.k].data(); const double* tend = stageTend[cc.k].data();
+        for (size_t i = (size_t)z0 * layer; i < (size_t)z1 * layer; i++) a[i] = (double)start[i] + fraction * tend[i];
+      });
+      if (sw.pressureInStages && stage < 2) {
+        Arr<S> w = F(F_W); int top = (nz - 1) * layer;
+        for (int b = 0; b < layer; b++) { w[b] = 0.0; w[b + top] = 0.0; }
+        project(dt, false);
+      }
+    }
+  }
+
+  // ---------------------------------------------------------- endStep (src/core/model.ts:1103-1195)
+  double fillNegative(Arr<S> a) {  // :606-617 (flat ground)
+    int nz = g.nz, layer = g.layer; double removed = 0, kept = 0, negative = 0;
+    for (int z = 0, i = 0; z < nz; z++) {
+      double level = levelWeight[z];
+      for (int e = i + layer; i < e; i++) { double x = a[i], wz = level; if (x < TINY_WATER) { if (x != 0) { removed += wz * x; if (x < 0) negative -= wz * x; } } else kept += wz * x; }
+    }
+    if (removed == 0 && negative == 0) return 0;
+    double scale = kept > 0 ? jmax(0, 1 + removed / kept) : 0;
+    for (int i = 0; i < g.n; i++) a[i] = (double)a[i] < TINY_WATER ? 0 : (double)a[i] * scale;
+    return negative;
+  }
+  void physics(int z, double dt) {  // :1347-1531 for the device configuration
+    int nx = g.nx, ny = g.ny, layer = g.layer;
+    double nodeMass = g.dx * g.dy * g.hz[z] * rho[z]; double wCond = 0, wEvap = 0, wRain = 0, wSurf = 0;
+    Arr<S> u = F(F_U), v = F(F_V), w = F(F_W), theta = F(F_THETA), q = F(F_Q), cloud = F(F_CLOUD), rain = F(F_RAIN), cold = F(F_COLD);
+    Arr<S> ice = F(F_ICE), iceNumber = F(F_ICENUMBER), snow = F(F_SNOW), graupel = F(F_GRAUPEL), hail = F(F_HAIL);
+    double rhoGround = rho[0], f = sw.coriolis, keep = std::exp(-sw.windRelaxation * dt), H = g.height;
+    double alt = g.zs[z], pz = p[z], rhoZ = rho[z], ex = exner[z], ue = uEnv[z], ve = vEnv[z], thEnv = thetaEnv[z];
+    for (int y = 0; y < ny; y++) for (int x = 0, i = z * layer + y * nx; x < nx; x++, i++) {
+      double q0 = q[i];
+      double evap = !sw.rainFormation ? 0 : rainProcesses<S>(q, cloud, rain, i, (double)theta[i] * ex, pz, rhoZ, dt, sw.evaporation);
+      if (evap > 0) { double cool = LV / CP / ex * evap; theta[i] -= cool; cold[i] += cool; }
+      double cond;
+      if (sw.ice) {
+        freezeRain<S>(theta, rain, graupel, i, ex);
+        settleCrystals<S>(ice, iceNumber, i);
+        cold[i] += iceProcesses<S>(theta, q, ice, snow, iceNumber, i, ex, pz, rhoZ, dt);
+        double iceBefore = ice[i], cloudBefore = cloud[i];
+        cold[i] += snowProcesses<S>(theta, q, cloud, ice, snow, rain, i, ex, pz, rhoZ, rhoGround, dt);
+        double rainBefore = rain[i];
+        cold[i] += graupelProcesses<S>(theta, q, cloud, ice, snow, rain, graupel, i, ex, pz, rhoZ, dt);
+        double rainFrozen = (double)theta[i] * ex < 273.15 ? jmax(0, rainBefore - (double)rain[i]) : 0;
+        cold[i] += hailProcesses<S>(theta, q, cloud, ice, snow, rain, graupel, hail, i, ex, pz, rhoZ, dt);
+        if (iceBefore > 0) iceNumber[i] *= (double)ice[i] / iceBefore;
+        double splinters = splintering((double)theta[i] * ex - 273.15) * SPLINTERS * jmax(0, cloudBefore - (double)cloud[i])
+          + (rainFrozen > 0 ? fragmentsPerKg(std::pow(PI * RHO_W * N0R / (rhoZ * rainBefore), .25)) * rainFrozen : 0);
+        if (splinters > 0) {
+          double fromG = jmin(graupel[i], splinters * CRYSTAL_MASS), fromS = jmin(snow[i], splinters * CRYSTAL_MASS - fromG);
+          graupel[i] -= fromG; snow[i] -= fromS; ice[i] += fromG + fromS; iceNumber[i] += (fromG + fromS) / CRYSTAL_MASS;
+        }
+        cond = saturationAdjustMixed<S>(theta, q, cloud, ice, i, ex, pz, iceNumber);
+        settleCrystals<S>(ice, iceNumber, i);
+      } else cond = saturationAdjust<S>(theta, q, cloud, i, ex, pz);
+      if (cond < 0) cold[i] -= LV / CP / ex * cond * .14;
+      if (!sw.pressureInStages) {
+        double thvEnv = thEnv * (1 + .61 * qEnv[z]);
+        double buoy = ((double)theta[i] * (1 + .61 * (double)q[i]) - thvEnv) / thvEnv - (double)cloud[i] - (double)ice[i] - (sw.loading ? (double)rain[i] + (double)snow[i] + (double)graupel[i] + (double)hail[i] : 0);
+        w[i] += G * buoy * dt;
+      }
+      double du = ((double)u[i] - ue) * keep, dv = ((double)v[i] - ve) * keep; u[i] = ue + du + f * dv * dt; v[i] = ve + dv - f * du * dt;
+      { double dq = (double)q[i] - q0; if (dq < 0) wCond -= dq; else wEvap += dq; if (evap > 0) wRain += evap; }
+      double share = z < (int)surfaceShare.size() ? surfaceShare[z] : 0;
+      if (sw.surfaceOn && share > 0) {
+        double per = 1 * share * dt / rhoZ;
+        double heat = sw.sensible * per / (CP * ex), vapour = sw.latent * per / LV;
+        theta[i] += heat; q[i] += vapour; wSurf += vapour;
+      }
+      cold[i] = (double)cold[i] < 1e-3 ? 0 : jmin(cold[i], 15);
+      if (alt > sw.spongeStart) {
+        double s = clamp((alt - sw.spongeStart) / (H - sw.spongeStart)) * sw.spongeRate * dt;
+        w[i] *= 1 - s; u[i] = lerp(u[i], ue, s); v[i] = lerp(v[i], ve, s); theta[i] = lerp(theta[i], thEnv, s);
+      }
+    }
+    Arr<S> cnd = A(condensate);
+    if (sw.ice) for (int i = z * layer, e = i + layer; i < e; i++) cnd[i] = (double)cloud[i] + (double)ice[i];
+    Arr<S> lw = A(levelWater); int l4 = z * 4;
+    lw[l4] = wCond * nodeMass; lw[l4 + 1] = wEvap * nodeMass; lw[l4 + 2] = wRain * nodeMass; lw[l4 + 3] = wSurf * nodeMass;
+  }
+  void physicsStep(double dt) {  // :1116-1127
+    std::vector<Carried> c = carried();
+    run((int)c.size(), [&](int k, int) {
+      const Carried& cc = c[k]; Arr<S> a = F(cc.k);
+      taskNegative[k] = cc.conserve ? fillNegative(a) : 0;
+      if (cc.decay != 1) { double keep = std::pow(cc.decay, dt); for (int i = 0; i < g.n; i++) a[i] *= keep; }
+    });
+    for (size_t k = 0; k < c.size(); k++) if (c[k].conserve) negativeFilled += taskNegative[k];
+    run(g.nz, [&](int z, int) { physics(z, dt); });
+    for (int k = 0; k < g.nz * 4; k += 4) { water[0] += (double)levelWater[k]; water[1] += (double)levelWater[k + 1]; water[2] += (double)levelWater[k + 2]; water[3] += (double)levelWater[k + 3]; }
+  }
+  void mixStep(double dt) {  // :1161-1195 (flat ground)
+    int nz = g.nz, layer = g.layer;
+    Arr<S> u = F(F_U), v = F(F_V), w = F(F_W);
+    Arr<S> moistCond = sw.ice ? A(condensate) : F(F_CLOUD);
+    run(nz, [&](int k, int) { turb.viscosity<S>(u, v, w, F(F_THETA), thetaEnv.data(), sw.cs, dt, F(F_Q), moistCond, exner.data(), k, k + 1); });
+    struct Mixed { int k; const double* base; double factor; };
+    std::vector<Mixed> mixed = {{F_U, uEnv.data(), 1}, {F_V, vEnv.data(), 1}, {F_W, nullptr, 1}, {F_THETA, thetaEnv.data(), 3}, {F_Q, qEnv.data(), 3}, {F_CLOUD, nullptr, 3}};
+    if (sw.ice) { mixed.push_back({F_ICE, nullptr, 3}); mixed.push_back({F_ICENUMBER, nullptr, 3}); }
+    run((int)mixed.size(), [&](int k, int t) { turb.mix<S>(F(mixed[k].k), mixed[k].base, mixed[k].factor, dt, mixTmp[t]); });
+    double cd = sw.dragCd * dt, drag = cd / g.hz[0], ue0 = uGround[0], ve0 = vGround[0], envSpeed = std::hypot(ue0, ve0), fu = sw.frameU, fv = sw.frameV;
+    for (int b = 0; b < layer; b++) {
+      double ug = (double)u[b] + fu, vg = (double)v[b] + fv, speed = std::hypot(ug, vg);
+      u[b] -= drag * (speed * ug - envSpeed * ue0); v[b] -= drag * (speed * vg - envSpeed * ve0);
+      w[b] = 0.0; w[b + (nz - 1) * layer] = 0.0;
+    }
+  }
+  void endStep(double dt) {
+    physicsStep(dt);
+    mixStep(dt);
+    project(dt, true);
+  }
+  void step(double dt) { beginStep(dt); dynamics(dt); endStep(dt); }
+};
+
+}  // namespace orc
