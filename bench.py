@@ -1,0 +1,281 @@
+#!/usr/bin/env python3
+"""Benchmark of the StormLab model step on GB300: batched / served cell-steps/s beside the plain single-run step.
+
+One JSON line on rank 0. A "step" is one model time step (dt = 3 s) of every run in the workload.
+Headline (`value`): the batched ensemble of BASELINE config 3 — 64 members on the standard 40x32x50 grid, seeded
+soundings, advanced together through one CUDA graph per step; inputs resident in HBM (213 MB per field set, larger
+than the 129 MB L2, so no flush is needed between steps). `e2e`: the same metric through the C ABI with host
+buffers: every step writes all members' fields from pinned host memory, steps, and reads them back.
+Beside it: the plain single-run step on the standard, large (80x64x50) and stress (320x256x80) grids.
+`--impl reference`: the reference's algorithm on the host cores (the oracle port, OpenMP, all host threads) on a
+bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-steps/s batched vs plain GPU step at <=1e-5 rel-L2; serve p50/p99 s/run"
+MEMBERS = 64
+TRANSPORT_BYTES_PER_CELL = (30 * 4 + 43 * 4 + 43 * 4) / 3  # mean algorithmic bytes per cell of one RK3 transport launch
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--members", type=int, default=MEMBERS)
+    p.add_argument("--quick", action="store_true", help="skip the serving and stress-grid legs")
+    return p.parse_args()
+
+
+def dist_setup(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        pg = dist
+    return rank, world, local, pg
+
+
+def barrier(pg):
+    if pg:
+        pg.barrier()
+
+
+def allmax(pg, x: float) -> float:
+    if not pg:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device, self.proc, self.lines = device, None, []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.reader = threading.Thread(target=lambda: self.lines.extend(self.proc.stdout), daemon=True)
+            self.reader.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except Exception:
+                self.proc.kill()
+            self.reader.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1])); mx = float(f[2])
+            except ValueError:
+                continue
+            for k, n in enumerate(names):
+                if f[5 + k].lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_per_cell():
+    """DRAM bytes per cell of one transport launch from the committed ncu summary, if there is one."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "transport_traffic.json")) as f:
+            return float(json.load(f)["dram_bytes_per_cell"])
+    except Exception:
+        return None
+
+
+def cpu_baseline(seconds: float = 10.0):
+    """The reference's algorithm (the oracle port) on the host cores, all threads, one standard-grid member."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    from meteolab_gb300.grid import DEFAULT_GRID, create_grid
+    from meteolab_gb300.scenarios import baseline_run
+    spec = baseline_run(create_grid(DEFAULT_GRID), seed=1)
+    threads = os.cpu_count() or 1
+    m = pyoracle.OracleModel(spec, threads=threads)
+    m.step(3.0, 2)  # warm-up
+    n, t0 = 0, time.perf_counter()
+    while True:
+        m.step(3.0, 1)
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or n >= 2000:
+            break
+    return {"value": spec.grid.n * n / el, "unit": "cell-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{n} steps of one 40x32x50 member ({el:.1f} s), reference algorithm restated in C++ (oracle), OpenMP"}
+
+
+def reference_arm(args, rank, pg):
+    """--impl reference: the CPU port of the reference on the same workload, bounded sample per step."""
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    from meteolab_gb300.grid import DEFAULT_GRID, create_grid
+    from meteolab_gb300.scenarios import ensemble_members
+    grid = create_grid(DEFAULT_GRID)
+    members = ensemble_members(grid, 2)
+    threads = os.cpu_count() or 1
+    ms = [pyoracle.OracleModel(s, threads=threads) for s in members]
+    for _ in range(args.warmup):
+        ms[0].step(3.0, 1)
+    times = []
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        ms[k % 2].step(3.0, 1)  # one member's step stands for the batch's per-member cost
+        times.append(time.perf_counter() - t0)
+    per_member = sum(times) / len(times)
+    value = grid.n / per_member
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": per_member * 1e3 * args.members, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded soundings, ellipsoid bubble)",
+            "config": {"workload": f"ensemble {args.members} x 40x32x50 (sampled: one member per step)", "cores": threads},
+            "cpu_baseline": {"value": value, "unit": "cell-steps/s", "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} single-member steps of 40x32x50 (reference algorithm restated in C++, OpenMP)"},
+            "e2e": {"value": value, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local, pg = dist_setup(args)
+    if args.impl == "reference":
+        reference_arm(args, rank, pg)
+        return
+    from meteolab_gb300 import build
+    build.build()
+    import numpy as np
+    import torch
+    from meteolab_gb300.grid import DEFAULT_GRID, LARGE_GRID, STRESS_GRID, create_grid
+    from meteolab_gb300.runtime import Context
+    from meteolab_gb300.scenarios import CARRIED, baseline_run, ensemble_members
+
+    ctx = Context(local)
+    grid = create_grid(DEFAULT_GRID)
+    members = ensemble_members(grid, args.members, seed=2026 + rank)
+    runs = [ctx.create(s) for s in members]
+    cells = sum(r.grid.n for r in runs)
+
+    # ---- headline: the batched ensemble from its CUDA graph, device time, inputs resident
+    ctx.time_steps(runs, max(3, args.warmup))
+    barrier(pg)
+    with Clocks(local) as clk:
+        ms = ctx.time_steps(runs, args.steps)
+    ms = allmax(pg, ms)
+    value = cells * world * args.steps / (ms * 1e-3)
+
+    # ---- kernel profile (eager, CUDA events per launch) and the roofline of the transport
+    prof = ctx.profile(runs, 2)
+    hbm, peak_kind = peaks()
+    tr_ms = prof.get("transport", (None, 0))[0]
+    achieved = cells * TRANSPORT_BYTES_PER_CELL / (tr_ms * 1e-3) / 1e9 if tr_ms else None
+    tpc = traffic_per_cell()
+    launches_per_step = sum(v[1] for v in prof.values())
+
+    # ---- e2e through the C ABI with pinned host buffers: write all fields, step, read all fields, every step
+    pinned = [{k: torch.empty(r.grid.n, dtype=torch.float32, pin_memory=True).numpy() for k in CARRIED} for r in runs]
+    for r, buf in zip(runs, pinned):
+        r.read(out=buf)
+    def e2e_step():
+        for r, buf in zip(runs, pinned):
+            r.write(buf)
+        ctx.batch_step(runs, 1)
+        for r, buf in zip(runs, pinned):
+            r.read(out=buf)
+    for _ in range(2):
+        e2e_step()
+    e2e_n = max(3, args.steps // 4)
+    barrier(pg)
+    t0 = time.perf_counter()
+    for _ in range(e2e_n):
+        e2e_step()
+    e2e_s = allmax(pg, time.perf_counter() - t0)
+    e2e_value = cells * world * e2e_n / e2e_s
+    bytes_io = cells * 4 * len(CARRIED)
+
+    # ---- plain single-run steps (eager launches and from a graph) on the standard, large and stress grids
+    plain = {}
+    for name, opts in (("standard", DEFAULT_GRID), ("large", LARGE_GRID)) + ((("stress", STRESS_GRID),) if not args.quick else ()):
+        spec = baseline_run(create_grid(opts), seed=3)
+        r = ctx.create(spec)
+        ctx.time_steps([r], 3, graph=False)
+        n = max(5, args.steps // 2)
+        eager = ctx.time_steps([r], n, graph=False)
+        ctx.time_steps([r], 3)
+        graphed = ctx.time_steps([r], n)
+        plain[name] = {"cells": spec.grid.n, "eager_cell_steps_s": spec.grid.n * n / (eager * 1e-3),
+                       "graph_cell_steps_s": spec.grid.n * n / (graphed * 1e-3), "graph_ms_per_step": graphed / n}
+        r.retire()
+
+    cpu = cpu_baseline(10.0) if rank == 0 else None
+    for r in runs:
+        r.retire()
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded Weisman-Klemp-type soundings (surface qv 11-16 g/kg, 0-6 km shear 0-30 m/s, veering 0-90 deg), "
+                "1-3 K ellipsoid bubble, +-0.1 K noise below 1 km",
+        "config": {"workload": f"ensemble {args.members} x 40x32x50 per GPU, one CUDA graph per step", "cells_per_gpu": cells,
+                   "l2": "inputs larger than L2 (213 MB per field set)", "parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e_value, "unit": "cell-steps/s", "h2d_bytes_per_step": bytes_io, "d2h_bytes_per_step": bytes_io},
+        "gpu_launches": launches_per_step * args.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm if achieved else None,
+                     "traffic": tpc * cells if tpc else None, "kernel": "transport", "peak_kind": peak_kind,
+                     "bytes_per_cell_per_launch": TRANSPORT_BYTES_PER_CELL},
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+        "plain_single_run": plain,
+        "batched_vs_plain_standard": value / world / plain["standard"]["graph_cell_steps_s"],
+        "kernels_ms_per_launch": {k: round(v[0], 5) for k, v in prof.items()},
+    }
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,150 @@
+/*
+ * stormgpu — the StormLab model time step on one GB300 (sm_103a), behind a plain C ABI.
+ *
+ * The step replaces AtmosphereModel.step (src/core/model.ts:873-877 of Bandananor/MeteoLAB) for the reference's
+ * GPU-eligible configuration (AtmosphereModel.gpuDynamics/gpuMixing, src/core/model.ts:882, :1136: WENO transport with
+ * the pressure and buoyancy in the RK3 stages, flat ground, explicit Smagorinsky mixing), with the one-moment ice
+ * microphysics, no lightning, single-storm surface (no sun). The whole step runs on the device; a run's state stays
+ * resident in HBM between calls. Many independent runs of uneven sizes advance together in one set of launches
+ * (sg_batch_step), and a serving loop admits, steps and retires runs (sg_server_*).
+ *
+ * Conventions: every call returns an sg_status (0 = ok); no exception crosses the ABI. Host buffers belong to the
+ * caller; device state belongs to the library; handles are opaque. Fields are FP32 arrays of n = nx*ny*nz values,
+ * node i = x + nx*(y + ny*z) (x fastest), as the reference's Float32Array fields. One context per host thread, or
+ * serialise calls on a context.
+ */
+#ifndef STORMGPU_H
+#define STORMGPU_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum sg_status {
+  SG_OK = 0,
+  SG_ERR_INVALID = 1,      /* a bad argument or configuration */
+  SG_ERR_BUDGET = 2,       /* the run does not fit the context's HBM budget */
+  SG_ERR_DEVICE = 3,       /* a CUDA error (sg_last_error says which) */
+  SG_ERR_TIMEOUT = 4,      /* a bounded wait ran out */
+  SG_ERR_NONFINITE = 5,    /* the run's state went non-finite; the run is marked failed */
+  SG_ERR_NOT_FOUND = 6,    /* no such run */
+  SG_ERR_UNSUPPORTED = 7   /* a configuration the device step does not implement */
+} sg_status;
+
+/* The carried fields in the reference's transport order (src/core/model.ts:1319-1335, ice, no lightning). */
+enum sg_field {
+  SG_RAIN = 0, SG_SNOW, SG_GRAUPEL, SG_HAIL, SG_U, SG_V, SG_W, SG_THETA, SG_Q, SG_CLOUD, SG_ICE, SG_ICE_NUMBER, SG_COLD,
+  SG_NFIELDS
+};
+#define SG_ALL_FIELDS ((1u << SG_NFIELDS) - 1u)
+
+typedef struct sg_context sg_context;
+typedef int32_t sg_run;
+
+/* A grid as createGrid builds it (src/core/grid.ts:99-121): levels zs[nz], spacings dzs[nz-1], control volumes hz[nz]. */
+typedef struct sg_grid {
+  int32_t nx, ny, nz, reserved;
+  double dx, dy, height;
+  const double* zs;
+  const double* dzs;
+  const double* hz;
+} sg_grid;
+
+/* The base state per level, FP64 (Environment, src/core/environment.ts:34-37): ground-relative wind u, v. */
+typedef struct sg_base_state {
+  const double* p;
+  const double* exner;
+  const double* theta;
+  const double* q;
+  const double* u;
+  const double* v;
+  const double* rho;
+} sg_base_state;
+
+/* Scalar settings of a run (AtmosphereModel's switches, src/core/model.ts:747-844, and SimConfig). */
+typedef struct sg_switches {
+  double dt;               /* step length, s (DT = 3, src/core/constants.ts:6) */
+  double coriolis;         /* f = 2 Omega sin(latitude), 1/s; 0 switches it off */
+  double wind_relaxation;  /* 1/s (windRelaxation, 1e-4) */
+  double sponge_rate;      /* 1/s (spongeRate, .06) */
+  double sponge_start;     /* m: max(tropopause + 2.5 km, 14 km) */
+  double cs;               /* Smagorinsky constant times the turbulence slider (SMAGORINSKY * turbulence / .55) */
+  double drag_cd;          /* neutral drag coefficient of the ground node (dragCoefficient), 0 = no drag */
+  double frame_u, frame_v; /* velocity of the domain over the ground, m/s */
+  int32_t loading, evaporation, rain_formation, anisotropic, vertical_dz, durran_klemp, pressure_in_stages, ice;
+} sg_switches;
+
+/* Per-run counters (AtmosphereModel.clipped, negativeFilled, water, src/core/model.ts:236, :269-271). */
+typedef struct sg_run_counters {
+  int64_t steps;
+  int64_t clipped;
+  double negative_filled;
+  double water_condensed, water_evaporated, water_rain_evaporated, water_surface;
+  int32_t failed;          /* 1: the state went non-finite (the run is skipped by later steps) */
+  int32_t reserved;
+} sg_run_counters;
+
+/* ---- context (replaces GpuDynamics.create / destroy / errors, src/gpu/dynamics.ts:250-282, :404) */
+int sg_context_create(int device, uint64_t hbm_budget_bytes, sg_context** out);
+int sg_context_destroy(sg_context* ctx);
+const char* sg_last_error(sg_context* ctx);
+/* Bytes of HBM one run of this grid takes (state, scratch, solver tables). */
+uint64_t sg_run_bytes(const sg_grid* grid);
+
+/* ---- runs (replace `new AtmosphereModel(config, grid, profile)`, src/core/model.ts:329; fields as its arrays) */
+/* init[SG_NFIELDS] host arrays in sg_field order (theta is the full potential temperature, K). */
+int sg_run_create(sg_context* ctx, const sg_grid* grid, const sg_base_state* base, const sg_switches* sw,
+                  const float* const* init, sg_run* out);
+int sg_run_write_fields(sg_context* ctx, sg_run run, uint32_t mask, const float* const* host);
+int sg_run_read_fields(sg_context* ctx, sg_run run, uint32_t mask, float* const* host);
+/* precipitation, hailGround, hailSize: nx*ny each (nullable); src/core/model.ts:253, :262. */
+int sg_run_read_columns(sg_context* ctx, sg_run run, float* precipitation, float* hail_ground, float* hail_size);
+/* The projection pressure of the last final projection, nx*ny*(nz-1) values (AtmosphereModel.pressure, :247). */
+int sg_run_read_pressure(sg_context* ctx, sg_run run, double* p);
+int sg_run_status(sg_context* ctx, sg_run run, sg_run_counters* out);
+int sg_run_retire(sg_context* ctx, sg_run run);
+
+/* ---- stepping (replaces AtmosphereModel.step(dt) + time += dt, src/core/model.ts:873; gpuStep, src/gpu/step.ts:12) */
+int sg_run_step(sg_context* ctx, sg_run run, int nsteps);
+/* All runs advance together, one set of launches per stage for the whole batch, replayed from a CUDA graph. */
+int sg_batch_step(sg_context* ctx, const sg_run* runs, int n, int nsteps);
+/* Enqueue without waiting; sg_synchronize waits for the context's stream. */
+int sg_batch_step_async(sg_context* ctx, const sg_run* runs, int n, int nsteps);
+int sg_synchronize(sg_context* ctx);
+
+/* ---- measurement: mean device time (ms) per launch of each kernel class over `nsteps` eager steps of a batch.
+ * names[k] receives a static string; returns the number of classes written (<= cap). */
+int sg_profile_kernels(sg_context* ctx, const sg_run* runs, int n, int nsteps, const char** names, double* ms_per_launch,
+                       int64_t* launches, int cap);
+/* Advance a batch `nsteps` steps (from its CUDA graph, or eagerly) between two CUDA events on the context's stream;
+ * *ms receives the device time. */
+int sg_time_steps(sg_context* ctx, const sg_run* runs, int n, int nsteps, int use_graph, double* ms);
+/* Max |D R u| of the run's current velocities (FP64 on the device), for the divergence check. */
+int sg_run_divergence(sg_context* ctx, sg_run run, double* max_abs_div);
+
+/* ---- diagnostics: one part of the step (1 beginStep, 2 dynamics, 3 physicsStep, 4 mixStep, 5 final projection),
+ * and the raw device buffers (set 0 = state, 1 and 2 = stage scratch; theta of a set is its departure from the base
+ * profile; faces4 = mx, my, mz, div). For stage-wise parity tests against the oracle. */
+int sg_debug_step_part(sg_context* ctx, sg_run run, int part);
+int sg_debug_read_set(sg_context* ctx, sg_run run, int set, int field, float* host);
+int sg_debug_read_faces(sg_context* ctx, sg_run run, float* faces4);
+
+/* ---- serving: a request loop with HBM-budget admission, device-resident runs and mid-batch retirement ---- */
+typedef struct sg_server sg_server;
+int sg_server_create(sg_context* ctx, int max_active, sg_server** out);
+int sg_server_destroy(sg_server* srv);
+/* Queue a request: the run (created by sg_run_create or queued lazily) and its number of steps. */
+int sg_server_submit(sg_server* srv, const sg_grid* grid, const sg_base_state* base, const sg_switches* sw,
+                     const float* const* init, int64_t steps, int64_t tag);
+/* One iteration: admit what fits, advance every active run one step in one batch, retire finished runs.
+ * done_tags/done_count receive the tags of runs finished in this iteration (cap entries). */
+int sg_server_iterate(sg_server* srv, int64_t* done_tags, int* done_count, int cap, int* active, int* queued);
+/* Read a finished run's fields (mask/host as sg_run_read_fields; precipitation nullable) and retire it. Finished runs
+ * stay resident, and are no longer stepped, until collected. */
+int sg_server_collect(sg_server* srv, int64_t tag, uint32_t mask, float* const* host, float* precipitation);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* STORMGPU_H */

@@ -1,0 +1,108 @@
+// Complex FFTs of short rows held in shared memory: the horizontal transforms of the two elliptic solves
+// (lengths 40, 32, 80, 64, 320, 256 in the benchmark grids; any length whose prime factors are handled below).
+// Self-sorting Stockham stages (no bit reversal): stage s with radix r reads src[j + q*n/r] and writes
+// dst[(j / Ns) * Ns * r + j % Ns + q * Ns], the inputs turned by exp(-2 pi i q (j % Ns) / (Ns r)); Ns is the product
+// of the radices already applied. Radix 4, 2, 3, 5 butterflies are written out; any other prime p uses a direct
+// p-point sum. Twiddles exp(-2 pi i t / n) come from a per-length FP32 table computed in FP64 on the host.
+#pragma once
+#include "sg_common.cuh"
+
+namespace sg {
+
+struct FftPlan { int n, nf; const int* rad; const float2* tw; };
+
+SG_HD float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+SG_HD float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+SG_HD float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+
+// One butterfly group: j in [0, n/r) of one row, from x (stage input) into y (stage output).
+SG_HD void fft_butterfly(const float2* x, float2* y, int n, int r, int Ns, int j, const float2* tw) {
+  const int nb = n / r, k = j % Ns, t = k * (n / (Ns * r)), out = (j / Ns) * Ns * r + k;
+  if (r == 4) {
+    float2 v0 = x[j], v1 = cmul(x[j + nb], tw[t]), v2 = cmul(x[j + 2 * nb], tw[2 * t]), v3 = cmul(x[j + 3 * nb], tw[3 * t]);
+    float2 a0 = cadd(v0, v2), a1 = csub(v0, v2), b0 = cadd(v1, v3), b1 = csub(v1, v3);
+    y[out] = cadd(a0, b0);
+    y[out + Ns] = make_float2(a1.x + b1.y, a1.y - b1.x);
+    y[out + 2 * Ns] = csub(a0, b0);
+    y[out + 3 * Ns] = make_float2(a1.x - b1.y, a1.y + b1.x);
+  } else if (r == 2) {
+    float2 v0 = x[j], v1 = cmul(x[j + nb], tw[t]);
+    y[out] = cadd(v0, v1); y[out + Ns] = csub(v0, v1);
+  } else if (r == 3) {
+    const float s3 = 0.86602540378443865f;
+    float2 v0 = x[j], v1 = cmul(x[j + nb], tw[t]), v2 = cmul(x[j + 2 * nb], tw[2 * t]);
+    float2 s = cadd(v1, v2), d = csub(v1, v2);
+    float2 m = make_float2(v0.x - .5f * s.x, v0.y - .5f * s.y);
+    y[out] = cadd(v0, s);
+    y[out + Ns] = make_float2(m.x + s3 * d.y, m.y - s3 * d.x);
+    y[out + 2 * Ns] = make_float2(m.x - s3 * d.y, m.y + s3 * d.x);
+  } else if (r == 5) {
+    const float c1 = 0.30901699437494742f, s1 = 0.95105651629515357f, c2 = -0.80901699437494742f, s2 = 0.58778525229247313f;
+    float2 v0 = x[j], v1 = cmul(x[j + nb], tw[t]), v2 = cmul(x[j + 2 * nb], tw[2 * t]), v3 = cmul(x[j + 3 * nb], tw[3 * t]), v4 = cmul(x[j + 4 * nb], tw[4 * t]);
+    float2 t1 = cadd(v1, v4), t2 = cadd(v2, v3), d1 = csub(v1, v4), d2 = csub(v2, v3);
+    float2 a = make_float2(v0.x + c1 * t1.x + c2 * t2.x, v0.y + c1 * t1.y + c2 * t2.y);
+    float2 b = make_float2(v0.x + c2 * t1.x + c1 * t2.x, v0.y + c2 * t1.y + c1 * t2.y);
+    float2 e = make_float2(s1 * d1.x + s2 * d2.x, s1 * d1.y + s2 * d2.y);   // -i e goes to X1, +i e to X4
+    float2 f = make_float2(s2 * d1.x - s1 * d2.x, s2 * d1.y - s1 * d2.y);   // -i f goes to X2, +i f to X3
+    y[out] = make_float2(v0.x + t1.x + t2.x, v0.y + t1.y + t2.y);
+    y[out + Ns] = make_float2(a.x + e.y, a.y - e.x);
+    y[out + 4 * Ns] = make_float2(a.x - e.y, a.y + e.x);
+    y[out + 2 * Ns] = make_float2(b.x + f.y, b.y - f.x);
+    y[out + 3 * Ns] = make_float2(b.x - f.y, b.y + f.x);
+  } else {
+    const int base = n / r;  // exp(-2 pi i / r) = tw[n / r]
+    for (int q1 = 0; q1 < r; q1++) {
+      float2 acc = make_float2(0.f, 0.f);
+      for (int q = 0; q < r; q++) {
+        float2 v = q ? cmul(x[j + q * nb], tw[q * t]) : x[j];
+        acc = cadd(acc, cmul(v, tw[((q * q1) % r) * base]));
+      }
+      y[out + q1 * Ns] = acc;
+    }
+  }
+}
+
+#ifdef __CUDACC__
+// Forward transform (exp(-i)) of `rows` rows of length P.n, row stride `stride`, in place in `a`, with scratch `b`
+// (same shape). All threads of the block take part; ends with the block synchronised.
+__device__ inline void fft_rows(float2* a, float2* b, int stride, int rows, const FftPlan& P) {
+  const int tid = threadIdx.x, nth = blockDim.x, n = P.n;
+  float2 *src = a, *dst = b;
+  int Ns = 1;
+  for (int s = 0; s < P.nf; s++) {
+    const int r = P.rad[s], nb = n / r, total = rows * nb;
+    for (int u = tid; u < total; u += nth) {
+      int row = u / nb, j = u - row * nb;
+      fft_butterfly(src + row * stride, dst + row * stride, n, r, Ns, j, P.tw);
+    }
+    __syncthreads();
+    float2* t = src; src = dst; dst = t; Ns *= r;
+  }
+  if (src != a) {
+    for (int u = tid; u < rows * n; u += nth) { int row = u / n, i = u - row * n; a[row * stride + i] = src[row * stride + i]; }
+    __syncthreads();
+  }
+}
+// Unnormalised inverse (exp(+i)): conj, forward, conj.
+__device__ inline void ifft_rows(float2* a, float2* b, int stride, int rows, const FftPlan& P) {
+  const int tid = threadIdx.x, nth = blockDim.x, n = P.n;
+  for (int u = tid; u < rows * n; u += nth) { int row = u / n, i = u - row * n; a[row * stride + i].y = -a[row * stride + i].y; }
+  __syncthreads();
+  fft_rows(a, b, stride, rows, P);
+  for (int u = tid; u < rows * n; u += nth) { int row = u / n, i = u - row * n; a[row * stride + i].y = -a[row * stride + i].y; }
+  __syncthreads();
+}
+#endif
+
+// Host reference of the same stages (used to build plans and by the CPU tests of the plan).
+inline int fft_plan_factors(int n, int* rad) {
+  int nf = 0, rest = n;
+  while (rest % 4 == 0 && rest > 1) { rad[nf++] = 4; rest /= 4; }
+  while (rest % 2 == 0) { rad[nf++] = 2; rest /= 2; }
+  while (rest % 3 == 0) { rad[nf++] = 3; rest /= 3; }
+  while (rest % 5 == 0) { rad[nf++] = 5; rest /= 5; }
+  for (int p = 7; rest > 1; p += 2) while (rest % p == 0) { if (nf >= 8) return -1; rad[nf++] = p; rest /= p; }
+  return nf <= 8 ? nf : -1;
+}
+
+}  // namespace sg

@@ -1,0 +1,761 @@
+// The StormLab step as sm_103a kernels. Every kernel is a grid-stride loop over a list of work items
+// (run slot, a, b, c): one launch advances every run of a batch, whatever its size, and the same launch sequence
+// captured once replays as a CUDA graph. No kernel waits on another block, so nothing here can spin.
+//
+// Step order (AtmosphereModel.step, src/core/model.ts:873-877, with the reference's phases):
+//   fall_courant  -> sediment                     beginStep: fall speeds, hail swath, CFL-split sedimentation (:893-932)
+//   face projection (div+xfft, modes, xifft, correct)   FluxTransport.setVelocity in phases (:1039, advection.ts:190-255)
+//   3 x transport stage (+ pressure projection after stages 0, 1)  RK3 with buoyancy and rigid w (:1042-1049)
+//   fill_partial -> fill_final                    positivity fix sums (:1116-1121, :606-617)
+//   physics                                       per-node physics (:1347-1531) + fill apply + cold decay
+//   viscosity -> mix                              Turbulence.viscosity / mix, drag, rigid walls (:1161-1195)
+//   final pressure projection with the wind clip  project(dt) (:1575-1595)
+//   step_end                                      budgets and counters
+#include <cuda_runtime.h>
+#include <math.h>
+#include "sg_common.cuh"
+#include "sg_fft.cuh"
+#include "sg_physics.cuh"
+#include "sg_kernels.h"
+
+namespace sg {
+
+#define FOR_ITEMS for (int it = blockIdx.x; it < nitems; it += gridDim.x)
+
+__device__ __forceinline__ void atomicMaxPos(float* addr, float v) {
+  // Non-negative floats order like their bit patterns.
+  atomicMax(reinterpret_cast<int*>(addr), __float_as_int(v));
+}
+
+template <class T>
+__device__ __forceinline__ T warpSum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float warpMax(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+// Block sum of `count` doubles per thread into out[] (fixed order: warp shuffles, then warps in order).
+template <int COUNT>
+__device__ void blockSums(double (&v)[COUNT], double* out, double* sh /* >= 32*COUNT */) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int c = 0; c < COUNT; c++) v[c] = warpSum(v[c]);
+  __syncthreads();
+  if (lane == 0)
+    for (int c = 0; c < COUNT; c++) sh[warp * COUNT + c] = v[c];
+  __syncthreads();
+  if (threadIdx.x < COUNT) {
+    double s = 0;
+    for (int w = 0; w < nw; w++) s += sh[w * COUNT + threadIdx.x];
+    out[threadIdx.x] = s;
+  }
+  __syncthreads();
+}
+
+// ==================================================================== conversion at the ABI boundary
+// theta' = theta - theta_b(z) (FP64 difference) and back.
+__global__ void k_theta_in(const RunDesc* runs, const int4* items, int nitems, const float* src) {
+  FOR_ITEMS {
+    const RunDesc& R = runs[items[it].x];
+    int i0 = items[it].y * CHUNK, i1 = min(R.n, i0 + CHUNK);
+    float* th = field(R, 0, THETA);
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) th[i] = (float)((double)src[i] - R.lv64[D_THB * R.nz + i / R.layer]);
+  }
+}
+__global__ void k_theta_out(const RunDesc* runs, const int4* items, int nitems, float* dst) {
+  FOR_ITEMS {
+    const RunDesc& R = runs[items[it].x];
+    int i0 = items[it].y * CHUNK, i1 = min(R.n, i0 + CHUNK);
+    const float* th = field(R, 0, THETA);
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) dst[i] = (float)((double)th[i] + R.lv64[D_THB * R.nz + i / R.layer]);
+  }
+}
+
+// ==================================================================== beginStep
+// Fall speeds of the four falling fields and the largest Courant number dt Vt / h of each over its non-zero nodes
+// (fallParts, src/core/model.ts:575-580): the sedimentation's sub-step count.
+__global__ void k_fall_courant(const RunDesc* runs, const int4* items, int nitems) {
+  FOR_ITEMS {
+    const RunDesc& R = runs[items[it].x];
+    if (R.cnt[C_FAILED]) continue;
+    int i0 = items[it].y * CHUNK, i1 = min(R.n, i0 + CHUNK);
+    float c[4] = {0.f, 0.f, 0.f, 0.f};
+    const float *rain = field(R, 0, RAIN), *snow = field(R, 0, SNOW), *graupel = field(R, 0, GRAUPEL), *hail = field(R, 0, HAIL);
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+      int z = i / R.layer;
+      float rho = lvl(R, L_RHO, z), fsq = lvl(R, L_FALLSQ, z), k = R.dt * lvl(R, L_INV_HZ, z);
+      float a = rain[i], b = snow[i], g = graupel[i], h = hail[i];
+      if (a != 0.f) c[0] = fmaxf(c[0], k * phys::rainFall(a, rho, fsq));
+      if (b != 0.f) c[1] = fmaxf(c[1], k * phys::snowFall(b, rho, fsq));
+      if (g != 0.f) c[2] = fmaxf(c[2], k * phys::graupelFall(g, rho));
+      if (h != 0.f) c[3] = fmaxf(c[3], k * phys::hailFall(h, rho));
+    }
+    for (int f = 0; f < 4; f++) {
+      float m = warpMax(c[f]);
+      if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMaxPos(R.scr + S_COURANT + f, m);
+    }
+  }
+}
+
+// One thread per column: the hail swath (collectHail, :697-706), then for rain, snow, graupel and hail the upwind
+// flux-form fall in ceil(courant / 0.8) sub-steps (sediment/sedimentPart, :565-598), bottom-up so each face uses the
+// values above from before the sub-step, the ground flux into the rain gauge. Fall speeds are those of the step's
+// start. Columns stay in shared memory.
+constexpr int SED_COLS = 64;
+__global__ void k_sediment(const RunDesc* runs, const int4* items, int nitems) {
+  extern __shared__ float sm[];
+  FOR_ITEMS {
+    const RunDesc& R = runs[items[it].x];
+    if (R.cnt[C_FAILED]) continue;
+    const int nz = R.nz, layer = R.layer, t = threadIdx.x;
+    float* sq = sm;                     // [nz][SED_COLS]
+    float* sv = sm + nz * SED_COLS;     // [nz][SED_COLS]
+    const int c = items[it].y * SED_COLS + t;
+    const bool on = t < SED_COLS && c < layer;
+    const float rho0 = R.rho0;
+    float* precip = R.cols;
+    float* hailGround = R.cols + layer;
+    float* hailSize = R.cols + 2 * layer;
+    for (int f = 0; f < 4; f++) {
+      float* a = field(R, 0, f);
+      float courant = R.scr[S_COURANT + f];
+      int parts = max(1, (int)ceilf(courant / .8f));
+      if (on) {
+        for (int z = 0; z < nz; z++) {
+          float q = a[c + z * layer], rho = lvl(R, L_RHO, z), fsq = lvl(R, L_FALLSQ, z);
+          float v = f == 0 ? phys::rainFall(q, rho, fsq) : f == 1 ? phys::snowFall(q, rho, fsq) : f == 2 ? phys::graupelFall(q, rho) : phys::hailFall(q, rho);
+          sq[z * SED_COLS + t] = q; sv[z * SED_COLS + t] = v;
+        }
+        if (f == HAIL && (R.flags & RF_ICE)) {
+          float h = sq[t];
+          if (h > 1e-9f) {
+            hailGround[c] += rho0 * h * sv[t] * R.dt;
+            hailSize[c] = fmaxf(hailSize[c], phys::hailMaxDiameter(h, rho0) * 1000.f);
+          }
+        }
+        if (f == RAIN || (R.flags & RF_ICE)) {
+          float dts = R.dt / (float)parts;
+          for (int p = 0; p < parts; p++) {
+            precip[c] += rho0 * sq[t] * sv[t] * dts;
+            for (int z = 0; z < nz; z++) {
+              float inflow = z < nz - 1 ? lvl(R, L_RHO, z + 1) * sq[(z + 1) * SED_COLS + t] * sv[(z + 1) * SED_COLS + t] : 0.f;
+              float q = sq[z * SED_COLS + t];
+              sq[z * SED_COLS + t] = q + dts * (inflow - lvl(R, L_RHO, z) * q * sv[z * SED_COLS + t]) * lvl(R, L_INV_RHO, z) * lvl(R, L_INV_HZ, z);
+            }
+          }
+          for (int z = 0; z < nz; z++) a[c + z * layer] = sq[z * SED_COLS + t];
+        }
+      }
+    }
+  }
+}
+
+// ==================================================================== elliptic solves
+// Divergence rows of one layer and their forward x-transform (real rows paired into complex ones, the reference's
+// trick, src/core/spectral.ts:246-255), written m-major: spec[(m * nzc + k) * ny + y].
+//  FACE: node divergence of the unprojected face mass fluxes rho0 * mean(u) (src/core/advection.ts:190-211).
+//  PRES: dual-cell divergence of rho0 u from the 8 corner nodes, over dt (src/core/pressure.ts:50-66).
+__global__ void k_proj_div_xfft(const RunDesc* runs, const int4* items, int nitems, int mode, int set, int yc) {
+  extern __shared__ float2 smc[];
+  FOR_ITEMS {
+    const RunDesc& R = runs[items[it].x];
+    if (R.cnt[C_FAILED]) continue;
+    const int k = items[it].y, y0 = items[it].z, nx = R.nx, ny = R.ny, layer = R.layer, nz = R.nz;
+    const int rows = min(yc, ny - y0), pairs = (rows + 1) / 2, nzc = mode == PROJ_FACE ? nz : nz - 1;
+    float2* Z = smc;                   // [pairs][nx]
+    float2* T = smc + pairs * nx;      // scratch
+    const float *u = field(R, set, U), *v = field(R, set, V), *w = field(R, set, W);
+    for (int e = threadIdx.x; e < pairs * 2 * nx; e += blockDim.x) {
+      int r = e / nx, x = e - r * nx, y = y0 + r;
+      float d = 0.f;
+      if (r < rows) {
+        if (mode == PROJ_FACE) {
+          const int l = k * layer, i = x + y * nx + l;
+          const int xe = wrap(x + 1, nx), xw = wrap(x - 1, nx), yn = wrap(y + 1, ny), ys = wrap(y - 1, ny);
+          float rho = lvl(R, L_RHO, k);
+          float ddx = .5f * rho * (u[xe + y * nx + l] - u[xw + y * nx + l]);
+          float ddy = .5f * rho * (v[x + yn * nx + l] - v[x + ys * nx + l]);
+          float up = k < nz - 1 ? .5f * lvl(R, L_RUP, k) * (w[i] + w[i + layer]) : 0.f;
+          float dn = k > 0 ? .5f * lvl(R, L_RUP, k - 1) * (w[i - layer] + w[i]) : 0.f;
+          d = ddx * R.inv_dx + ddy * R.inv_dy + (up - dn) * lvl(R, L_INV_HZ, k);
+        } else {
+          const int l0 = k * layer, x1 = wrap(x + 1, nx), y1 = wrap(y + 1, ny);
+          const int a = x + y * nx + l0, b = x1 + y * nx + l0, ee = x + y1 * nx + l0, f = x1 + y1 * nx + l0;
+          const int g = a + layer, h = b + layer, s = ee + layer, tt = f + layer;
+          float r0 = .25f * lvl(R, L_RHO, k), r1 = .25f * lvl(R, L_RHO, k + 1);
+          float ddx = (r0 * ((u[b] - u[a]) + (u[f] - u[ee])) + r1 * ((u[h] - u[g]) + (u[tt] - u[s]))) * R.inv_dx;
+          float ddy = (r0 * ((v[ee] - v[a]) + (v[f] - v[b])) + r1 * ((v[s] - v[g]) + (v[tt] - v[h]))) * R.inv_dy;
+          float ddz = (r1 * ((w[g] + w[h]) + (w[s] + w[tt])) - r0 * ((w[a] + w[b]) + (w[ee] + w[f]))) * lvl(R, L_INV_DZS, k);
+          d = (ddx + ddy + ddz) / R.dt;
+        }
+      }
+      float* zf = reinterpret_cast<float*>(&Z[(r >> 1) * nx + x]);
+      zf[r & 1] = d;
+    }
+    __syncthreads();
+    FftPlan P{nx, R.fx_nf, R.fx_rad, R.twx};
+    fft_rows(Z, T, nx, pairs, P);
+    const int nm = R.nm;
+    for (int e = threadIdx.x; e < nm * rows; e += blockDim.x) {
+      int m = e / rows, r = e - m * rows, pr = r >> 1, c = m ? nx - m : 0;
+      float2 zm = Z[pr * nx + m], zc = Z[pr * nx + c], out;
+      if ((r & 1) == 0) out = make_float2(.5f * (zm.x + zc.x), .5f * (zm.y - zc.y));
+      else out = make_float2(.5f * (zm.y + zc.y), .5f * (zc.x - zm.x));
+      R.spec[((size_t)m * nzc + k) * ny + y0 + r] = out;
+    }
+    __syncthreads();
+  }
+}
+
+// One x-wavenumber m per item: the y-transform of every layer, one tridiagonal solve per y-wavenumber n along the
+// vertical in FP64 (Thomas, factorised on the host in FP64: the k = 0 uniform mode pinned at the ground, the null
+// modes zero), the inverse y-transform. FACE: rows -rho h lambda + vertical faces (src/core/advection.ts:222-241);
+// PRES: the density-weighted consistent Laplacian (src/core/pressure.ts:104-140).
+constexpr int MAXNZ = 128;
+constexpr int MODE_GROUP = 8;
+__global__ void k_proj_modes(const RunDesc* runs, const int4* items, int nitems, int mode) {
+  extern __shared__ float2 smc[];
+  FOR_ITEMS {
+    const RunDesc& R = runs[items[it].x];
+    if (R.cnt[C_FAILED]) continue;
+    const int m = items[it].y, ny = R.ny, nz = R.nz, nzc = mode == PROJ_FACE ? nz : nz - 1;
+    float2* S = smc;                   // [nzc][ny]
+    float2* T = smc + nzc * ny;        // [MODE_GROUP][ny] scratch
+    float2* g = R.spec + (size_t)m * nzc * ny;
+    for (int e = threadIdx.x; e < nzc * ny; e += blockDim.x) S[e] = g[e];
+    __syncthreads();
+    FftPlan P{ny, R.fy_nf, R.fy_rad, R.twy};
+    for (int k0 = 0; k0 < nzc; k0 += MODE_GROUP) {
+      int rows = min(MODE_GROUP, nzc - k0);
+      // fft_rows ping-pongs between the slab rows and T; rows stay within this group.
+      fft_rows(S + k0 * ny, T, ny, rows, P);
+    }
+    const double2* tri = (mode == PROJ_FACE ? R.tri_face : R.tri_pres) + (size_t)m * nzc * ny;
+    const double* lv64 = R.lv64;
+    for (int n = threadIdx.x; n < ny; n += blockDim.x) {
+      double2 d[MAXNZ];
+      double a = 0, b = 0;
+      if (mode == PROJ_PRES) { double2 ab = R.ab[m * ny + n]; a = ab.x; b = ab.y; }
+      double pr = 0, pi = 0;
+      for (int k = 0; k < nzc; k++) {
+        double2 f = tri[(size_t)k * ny + n];                         // (1/pivot, cp)
+        float2 r = S[k * ny + n];
+        double rr = r.x, ri = r.y, lo;
+        if (mode == PROJ_FACE) { double h = lv64[D_FHZ * nz + k]; rr *= h; ri *= h; lo = lv64[D_FLO * nz + k]; }
+        else lo = a * lv64[D_PL1 * nz + k] + b * lv64[D_PL2 * nz + k];
+        double dr = (rr - lo * pr) * f.x, di = (ri - lo * pi) * f.x;
+        d[k] = make_double2(dr, di); pr = dr; pi = di;
+      }
+      double xr = 0, xi = 0;
+      for (int k = nzc - 1; k >= 0; k--) {
+        double cp = tri[(size_t)k * ny + n].y;
+        xr = d[k].x - (k < nzc - 1 ? cp * xr : 0.0);
+        xi = d[k].y - (k < nzc - 1 ? cp * xi : 0.0);
+        S[k * ny + n] = make_float2((float)xr, (float)xi);
+      }
+    }
+    __syncthreads();
+    for (int k0 = 0; k0 < nzc; k0 += MODE_GROUP) ifft_rows(S + k0 * ny, T, ny, min(MODE_GROUP, nzc - k0), P);
+    for (int e = threadIdx.x; e < nzc * ny; e += blockDim.x) g[e] = S[e];
+    __syncthreads();
+  }
+}
+
+// Inverse x-transform of one layer's rows (Hermitian rows rebuilt from the half spectrum, two real rows per complex
+// transform, src/core/spectral.ts:281-290), normalised by nx*ny, into phi (FACE) or the pressure (PRES).
+__global__ void k_proj_xifft(const RunDesc* runs, const int4* items, int nitems, int mode, int yc) {
+  extern __shared__ float2 smc[];
+  FOR_ITEMS {
+    const RunDesc& R = runs[items[it].x];
+    if (R.cnt[C_FAILED]) continue;
+    const int k = items[it].y, y0 = items[it].z, nx = R.nx, ny = R.ny, nz = R.nz, mh = R.mh, nm = R.nm;
+    const int rows = min(yc, ny - y0), pairs = (rows + 1) / 2, nzc = mode == PROJ_FACE ? nz : nz - 1;
+    float2* H = smc;                    // [rows][nm] half spectra
+    float2* Z = smc + yc * nm;          // [pairs][nx]
+    float2* T = Z + pairs * nx;
+    for (int e = threadIdx.x; e < nm * rows; e += blockDim.x) {
+      int m = e / rows, r = e - m * rows;
+      H[r * nm + m] = R.spec[((size_t)m * nzc + k) * ny + y0 + r];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < pairs * nx; e += blockDim.x) {
+      int pr = e / nx, m = e - pr * nx, c = m <= mh ? m : nx - m;
+      float sg = m <= mh ? 1.f : -1.f; bool real = c == 0 || 2 * c == nx, pair = 2 * pr + 1 < rows;
+      float2 A = H[(2 * pr) * nm + c];
+      float ar = A.x, ai = real ? 0.f : sg * A.y, br = 0.f, bi = 0.f;
+      if (pair) { float2 B = H[(2 * pr + 1) * nm + c]; br = B.x; bi = real ? 0.f : sg * B.y; }
+      Z[pr * nx + m] = make_float2(ar - bi, ai + br);
+    }
+    __syncthreads();
+    FftPlan P{nx, R.fx_nf, R.fx_rad, R.twx};
+    ifft_rows(Z, T, nx, pairs, P);
+    const float norm = 1.f / (float)(nx * ny);
+    float* out = (mode == PROJ_FACE ? R.phi : R.pres) + (size_t)k * nx * ny;
+    for (int e = threadIdx.x; e < rows * nx; e += blockDim.x) {
+      int r = e / nx, x = e - r * nx;
+      float2 z = Z[(r >> 1) * nx + x];
+      out[(y0 + r) * nx + x] = ((r & 1) ? z.y : z.x) * norm;
+    }
+    __syncthreads();
+  }
+}
+
+// Projected face mass fluxes and their divergence (FluxTransport.correctFaces + divergence, advection.ts:203-255):
+// mx = rho (u + u_e)/2 - rho (phi_e - phi)/dx, and so on; div of the corrected faces at the node.
+__global__ void k_face_correct(const RunDesc* runs, const int4* items, int nitems, int set) {
+  FOR_ITEMS {
+    const RunDesc& R = runs[items[it].x];
+    if (R.cnt[C_FAILED]) continue;
+    const int nx = R.nx, ny = R.ny, nz = R.nz, layer = R.layer, i0 = items[it].y * CHUNK, i1 = min(R.n, i0 + CHUNK);
+    const float *u = field(R, set, U), *v = field(R, set, V), *w = field(R, set, W), *phi = R.phi;
+    float *mx = R.faces, *my = R.faces + R.n, *mz = R.faces + 2 * R.n, *dv = R.faces + 3 * R.n;
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+      int z = i / layer, c = i - z * layer, y = c / nx, x = c - y * nx, l = z * layer;
+      int ie = wrap(x + 1, nx) + y * nx + l, iw = wrap(x - 1, nx) + y * nx + l, in = x + wrap(y + 1, ny) * nx + l, is = x + wrap(y - 1, ny) * nx + l;
+      float rho = lvl(R, L_RHO, z), p0 = phi[i];
+      float fxE = rho * (.5f * (u[i] + u[ie]) - (phi[ie] - p0) * R.inv_dx);
+      float fxW = rho * (.5f * (u[iw] + u[i]) - (p0 - phi[iw]) * R.inv_dx);
+      float fyN = rho * (.5f * (v[i] + v[in]) - (phi[in] - p0) * R.inv_dy);
+      float fyS = rho * (.5f * (v[is] + v[i]) - (p0 - phi[is]) * R.inv_dy);
+      float fzU = z < nz - 1 ? lvl(R, L_RUP, z) * (.5f * (w[i] + w[i + layer]) - (phi[i + layer] - p0) * lvl(R, L_INV_DZS, z)) : 0.f;
+      float fzD = z > 0 ? lvl(R, L_RUP, z - 1) * (.5f * (w[i - layer] + w[i]) - (p0 - phi[i - layer]) * lvl(R, L_INV_DZS, z - 1)) : 0.f;
+      mx[i] = fxE; my[i] = fyN; mz[i] = fzU;
+      dv[i] = (fxE - fxW) * R.inv_dx + (fyN - fyS) * R.inv_dy + (fzU - fzD) * lvl(R, L_INV_HZ, z);
+    }
+  }
+}
+
+// u -= dt G p at the nodes of one set (PressureSolver.correct, src/core/pressure.ts:69-92); with `final` the wind
+// limits act and count (clipWind, src/core/model.ts:1586-1595).
+__global__ void k_pres_correct(const RunDesc* runs, const int4* items, int nitems, int set, int final_) {
+  FOR_ITEMS {
+    const RunDesc& R = runs[items[it].x];
+    if (R.cnt[C_FAILED]) continue;
+    const int nx = R.nx, ny = R.ny, nz = R.nz, layer = R.layer, i0 = items[it].y * CHUNK, i1 = min(R.n, i0 + CHUNK);
+    float *u = field(R, set, U), *v = field(R, set, V), *w = field(R, set, W);
+    const float* p = R.pres;
+    const float dt = R.dt;
+    int clipped = 0;
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+      int k = i / layer, c = i - k * layer, j = c / nx, x = c - j * nx;
+      int im = wrap(x - 1, nx), jm = wrap(j - 1, ny) * nx, j0 = j * nx;
+      const float* lo = p + (size_t)max(0, k - 1) * layer;
+      const float* hi = p + (size_t)min(nz - 2, k) * layer;
+      float hz = lvl(R, L_HZ, k);
+      float wLo = k > 0 ? lvl(R, L_DZS, k - 1) / hz : 0.f, wHi = k < nz - 1 ? lvl(R, L_DZS, k) / hz : 0.f;
+      float gx = (wLo * ((lo[x + jm] - lo[im + jm]) + (lo[x + j0] - lo[im + j0])) + wHi * ((hi[x + jm] - hi[im + jm]) + (hi[x + j0] - hi[im + j0]))) * (.25f * R.inv_dx);
+      float gy = (wLo * ((lo[im + j0] - lo[im + jm]) + (lo[x + j0] - lo[x + jm])) + wHi * ((hi[im + j0] - hi[im + jm]) + (hi[x + j0] - hi[x + jm]))) * (.25f * R.inv_dy);
+      float uu = u[i] - dt * gx, vv = v[i] - dt * gy, ww = w[i];
+      if (k > 0 && k < nz - 1) {
+        const float* ab = p + (size_t)k * layer;
+        const float* be = p + (size_t)(k - 1) * layer;
+        float gz = ((ab[im + jm] - be[im + jm]) + (ab[x + jm] - be[x + jm]) + (ab[im + j0] - be[im + j0]) + (ab[x + j0] - be[x + j0])) * (.25f * lvl(R, L_INV_HZ, k));
+        ww -= dt * gz;
+      }
+      if (final_) {
+        const float UL = 120.f, WL = 100.f;
+        if (uu < -UL || uu > UL) { uu = fmaxf(-UL, fminf(UL, uu)); clipped++; }
+        if (vv < -UL || vv > UL) { vv = fmaxf(-UL, fminf(UL, vv)); clipped++; }
+        if (ww < -WL || ww > WL) { ww = fmaxf(-WL, fminf(WL, ww)); clipped++; }
+      }
+      u[i] = uu; v[i] = vv; w[i] = ww;
+    }
+    if (final_) {
+      clipped = warpSum(clipped);
+      if ((threadIdx.x & 31) == 0 && clipped) atomicAdd(&R.cnt[C_CLIPPED], (unsigned long long)clipped);
+    }
+  }
+}
+
+// ==================================================================== RK3 transport
+// One field of one run on a TX x TY tile of columns, marching up the column: the tendency -(div F - q div)/rho0 of
+// the flux-form WENO5 (monotone fields) or linear fifth-order upwind reconstruction on the projected face fluxes
+// (FluxTransport.tendency, src/core/advection.ts:274-378), w with the stage buoyancy (stageBuoyancy, model.ts:1204),
+// theta' with the base profile's own vertical flux tendency, then the RK3 update a = start + f dt tend (:1250) and,
+// before a stage projection, w = 0 on the ground and the top (:1045). The column's own values z-3..z+3 live in
+// registers; the current plane with a 3-node halo in shared memory; each x and y face is reconstructed once.
+__device__ __forceinline__ float recon(bool mono, float a, float b, float c, float d, float e) {
+  return mono ? weno5(a, b, c, d, e) : upwind5(a, b, c, d, e);
+}
+__global__ void __launch_bounds__(512) k_transport(const RunDesc* runs, const int4* items, int nitems, int in_set, int out_set,
+                                                    float frac, int stage, int TX, int TY) {
+  extern __shared__ float sm[];
+  const int PW = TX + 6, PH = TY + 6;
+  float* plane = sm;                       // [PH][PW]
+  float* fxs = sm + PW * PH;               // [TY][TX + 1]
+  float* fys = fxs + TY * (TX + 1);        // [TY + 1][TX]
+  const int t = threadIdx.x, lx = t % TX, ly = t / TX;
+  FOR_ITEMS {
+    const RunDesc& R = runs[items[it].x];
+    if (R.cnt[C_FAILED]) continue;
+    const int f = items[it].y, tile = items[it].z;
+    const int nx = R.nx, ny = R.ny, nz = R.nz, layer = R.layer;
+    const int tilesX = (nx + TX - 1) / TX, x0 = (tile % tilesX) * TX, y0 = (tile / tilesX) * TY;
+    const int x = x0 + lx, y = y0 + ly;
+    const bool on = x < nx && y < ny;
+    const bool mono = monotone(f);
+    const float* q = field(R, in_set, f);
+    const float* st = field(R, 0, f);
+    float* out = field(R, out_set, f);
+    const float *mx = R.faces, *my = R.faces + R.n, *mz = R.faces + 2 * R.n, *dv = R.faces + 3 * R.n;
+    const int col = (on ? x + y * nx : 0);
+    float win[7];
+#pragma unroll
+    for (int j = 0; j < 7; j++) win[j] = on ? q[col + clampi(j - 3, 0, nz - 1) * layer] : 0.f;
+    float fzD = 0.f, mzD = 0.f;
+    for (int z = 0; z < nz; z++) {
+      const int l = z * layer;
+      // the plane with its halo, periodic in x and y
+      for (int e = t; e < PW * PH; e += blockDim.x) {
+        int hy = e / PW, hx = e - hy * PW;
+        int gx = wrap(x0 + hx - 3, nx), gy = wrap(y0 + hy - 3, ny);
+        gx = gx < 0 ? gx + nx : (gx >= nx ? gx - nx : gx);  // tiles wider than nx wrap twice at most
+        gy = gy < 0 ? gy + ny : (gy >= ny ? gy - ny : gy);
+        plane[e] = q[gx + gy * nx + l];
+      }
+      __syncthreads();
+      float fzU = 0.f, m3 = 0.f;
+      if (on) {
+        const int i = col + l;
+        const float* P = plane + (ly + 3) * PW + (lx + 3);
+        float m1 = mx[i];
+        float fe = m1 >= 0.f ? m1 * recon(mono, P[-2], P[-1], P[0], P[1], P[2]) : m1 * recon(mono, P[3], P[2], P[1], P[0], P[-1]);
+        fxs[ly * (TX + 1) + lx + 1] = fe;
+        if (lx == 0) {
+          float mw = mx[wrap(x - 1, nx) + y * nx + l];
+          fxs[ly * (TX + 1)] = mw >= 0.f ? mw * recon(mono, P[-3], P[-2], P[-1], P[0], P[1]) : mw * recon(mono, P[2], P[1], P[0], P[-1], P[-2]);
+        }
+        float m2 = my[i];
+        fys[(ly + 1) * TX + lx] = m2 >= 0.f ? m2 * recon(mono, P[-2 * PW], P[-PW], P[0], P[PW], P[2 * PW]) : m2 * recon(mono, P[3 * PW], P[2 * PW], P[PW], P[0], P[-PW]);
+        if (ly == 0) {
+          float ms = my[x + wrap(y - 1, ny) * nx + l];
+          fys[lx] = ms >= 0.f ? ms * recon(mono, P[-3 * PW], P[-2 * PW], P[-PW], P[0], P[PW]) : ms * recon(mono, P[2 * PW], P[PW], P[0], P[-PW], P[-2 * PW]);
+        }
+        m3 = mz[i];
+        if (z < nz - 1) fzU = m3 >= 0.f ? m3 * recon(mono, win[1], win[2], win[3], win[4], win[5]) : m3 * recon(mono, win[6], win[5], win[4], win[3], win[2]);
+      }
+      __syncthreads();
+      if (on) {
+        const int i = col + l;
+        const float qc = win[3];
+        float flux = (fxs[ly * (TX + 1) + lx + 1] - fxs[ly * (TX + 1) + lx]) * R.inv_dx + (fys[(ly + 1) * TX + lx] - fys[ly * TX + lx]) * R.inv_dy +
+                     (fzU - fzD) * lvl(R, L_INV_HZ, z);
+        float tend = -(flux - qc * dv[i]) * lvl(R, L_INV_RHO, z);
+        if (f == THETA) {
+          float up = m3 * (m3 >= 0.f ? lvl(R, L_TH_UP_POS, z) : lvl(R, L_TH_UP_NEG, z));
+          float dn = mzD * (mzD >= 0.f ? lvl(R, L_TH_DN_POS, z) : lvl(R, L_TH_DN_NEG, z));
+          tend -= (up - dn) * lvl(R, L_INV_HZ, z) * lvl(R, L_INV_RHO, z);
+        } else if (f == W && (R.flags & RF_STAGES)) {
+          // g B with theta' and the base state (stageBuoyancy): theta_v - theta_v,env from small differences.
+          const float* th = field(R, in_set, THETA);
+          float dth = th[i], qq = field(R, in_set, Q)[i], Rb = lvl(R, L_THB, z), Qb = lvl(R, L_QB, z);
+          float num = dth + .61f * ((Rb + dth) * (qq - Qb) + Qb * dth);
+          float loaded = field(R, in_set, CLOUD)[i] + field(R, in_set, ICE)[i];
+          if (R.flags & RF_LOADING) loaded += field(R, in_set, RAIN)[i] + field(R, in_set, SNOW)[i] + field(R, in_set, GRAUPEL)[i] + field(R, in_set, HAIL)[i];
+          tend += 9.81f * (num / lvl(R, L_THVENV, z) - loaded);
+        }
+        float s0 = stage == 0 ? qc : st[i];
+        float a = s0 + (frac * R.dt) * tend;
+        if (f == W && stage < 2 && (R.flags & RF_STAGES) && (z == 0 || z == nz - 1)) a = 0.f;
+        out[i] = a;
+      }
+      fzD = fzU; mzD = m3;
+#pragma unroll
+      for (int j = 0; j < 6; j++) win[j] = win[j + 1];
+      if (on) win[6] = q[col + min(z + 4, nz - 1) * layer];
+    }
+    __syncthreads();
+  }
+}
+
+// ==================================================================== endStep
+// Sums of the positivity fix over one chunk of the final RK3 values (fillNegative, src/core/model.ts:606-617):
+// per conserve field, (removed, kept, negative) weighted by the level weight, FP64, in a fixed order.
+__global__ void k_fill_partial(const RunDesc* runs, const int4* items, int nitems, int set) {
+  __shared__ double sh[32 * 3];
+  FOR_ITEMS {
+    const RunDesc& R = runs[items[it].x];
+    if (R.cnt[C_FAILED]) continue;
+    const int chunk = items[it].y, i0 = chunk * CHUNK, i1 = min(R.n, i0 + CHUNK);
+    for (int k = 0; k < NCONS; k++) {
+      const float* a = field(R, set, cons_field(k));
+      double v[3] = {0, 0, 0};
+      for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+        float x = a[i];
+        double wz = lvl(R, L_LW, i / R.layer);
+        if (x < 1e-10f) { if (x != 0.f) { v[0] += wz * x; if (x < 0.f) v[2] -= wz * x; } }
+        else v[1] += wz * x;
+      }
+      blockSums<3>(v, R.part + ((size_t)chunk * NCONS + k) * 3, sh);
+    }
+  }
+}
+// Per run: the scale of each conserve field, kept as delta = scale - 1 so a * scale rounds once (fma).
+__global__ void k_fill_final(const RunDesc* runs, const int4* items, int nitems) {
+  FOR_ITEMS {
+    const RunDesc& R = runs[items[it].x];
+    if (R.cnt[C_FAILED]) continue;
+    if (threadIdx.x != 0) continue;
+    const int nch = (R.n + CHUNK - 1) / CHUNK;
+    double neg = 0;
+    for (int k = 0; k < NCONS; k++) {
+      double removed = 0, kept = 0, negative = 0;
+      for (int c = 0; c < nch; c++) {
+        const double* p = R.part + ((size_t)c * NCONS + k) * 3;
+        removed += p[0]; kept += p[1]; negative += p[2];
+      }
+      double delta = 0;
+      if (!(removed == 0 && negative == 0)) delta = kept > 0 ? fmax(-1.0, removed / kept) : -1.0;
+      R.scr[S_FILL + k] = (float)delta;
+      neg += negative;
+    }
+    R.acc[A_NEG] += neg;
+  }
+}
+
+// Per node: the positivity fix and the cold decay ('finish', :1253-1258), then physics(z) (:1347-1531): microphysics,
+// Coriolis and wind relaxation, surface fluxes (none in the single-storm mode), cold clamp, Rayleigh sponge.
+// In: set `in` (final RK3 values). Out: rain, snow, graupel, hail, cold -> set A; the mixed fields -> set `mid`.
+__global__ void k_physics(const RunDesc* runs, const int4* items, int nitems, int in, int mid) {
+  __shared__ double sh[32 * 3];
+  FOR_ITEMS {
+    const RunDesc& R = runs[items[it].x];
+    const int chunk = items[it].y, i0 = chunk * CHUNK, i1 = min(R.n, i0 + CHUNK);
+    const float dt = R.dt, keepCold = __powf(.9992f, dt);
+    float fill[NCONS];
+#pragma unroll
+    for (int k = 0; k < NCONS; k++) fill[k] = R.scr[S_FILL + k];
+    double wsum[3] = {0, 0, 0};
+    bool bad = false;
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+      const int z = i / R.layer;
+      auto fixed = [&](int kc, float x) { return x < 1e-10f ? 0.f : fmaf(x, fill[kc], x); };
+      phys::Node s;
+      s.rain = fixed(0, field(R, in, RAIN)[i]); s.snow = fixed(1, field(R, in, SNOW)[i]);
+      s.graupel = fixed(2, field(R, in, GRAUPEL)[i]); s.hail = fixed(3, field(R, in, HAIL)[i]);
+      s.q = fixed(4, field(R, in, Q)[i]); s.cloud = fixed(5, field(R, in, CLOUD)[i]); s.ice = fixed(6, field(R, in, ICE)[i]);
+      s.inum = field(R, in, ICENUM)[i];
+      s.cold = field(R, in, COLD)[i] * keepCold;
+      s.thp = field(R, in, THETA)[i]; s.thb = lvl(R, L_THB, z);
+      float u = field(R, in, U)[i], v = field(R, in, V)[i], w = field(R, in, W)[i];
+      const float exner = lvl(R, L_EXNER, z), p = lvl(R, L_P, z), rho = lvl(R, L_RHO, z);
+      const float q0 = s.q;
+      float evap;
+      phys::microphysics(s, exner, p, rho, lvl(R, L_FALLSQ, z), dt, R.flags, evap);
+      if (!(R.flags & RF_STAGES)) {
+        float num = s.thp + .61f * ((s.thb + s.thp) * (s.q - lvl(R, L_QB, z)) + lvl(R, L_QB, z) * s.thp);
+        float loaded = s.cloud + s.ice + ((R.flags & RF_LOADING) ? s.rain + s.snow + s.graupel + s.hail : 0.f);
+        w += 9.81f * (num / lvl(R, L_THVENV, z) - loaded) * dt;
+      }
+      // Coriolis on the departure from the environmental wind, relaxed towards it (:1478).
+      const float ue = lvl(R, L_UENV, z), ve = lvl(R, L_VENV, z);
+      float du = (u - ue) * R.keep, dvv = (v - ve) * R.keep;
+      u = ue + du + R.coriolis * dvv * dt; v = ve + dvv - R.coriolis * du * dt;
+      const double nm = lvl(R, L_NODEMASS, z);
+      { float dq = s.q - q0; if (dq < 0.f) wsum[0] -= nm * dq; else wsum[1] += nm * dq; if (evap > 0.f) wsum[2] += nm * evap; }
+      s.cold = s.cold < 1e-3f ? 0.f : fminf(s.cold, 15.f);
+      const float sp = lvl(R, L_SPONGE, z);
+      if (sp > 0.f) { w *= 1.f - sp; u += (ue - u) * sp; v += (ve - v) * sp; s.thp += (0.f - s.thp) * sp; }
+      bad |= !(isfinite(s.thp) && isfinite(s.q) && isfinite(u) && isfinite(v) && isfinite(w) && isfinite(s.rain) && isfinite(s.cloud));
+      field(R, 0, RAIN)[i] = s.rain; field(R, 0, SNOW)[i] = s.snow; field(R, 0, GRAUPEL)[i] = s.graupel; field(R, 0, HAIL)[i] = s.hail;
+      field(R, 0, COLD)[i] = s.cold;
+      field(R, mid, U)[i] = u; field(R, mid, V)[i] = v; field(R, mid, W)[i] = w; field(R, mid, THETA)[i] = s.thp;
+      field(R, mid, Q)[i] = s.q; field(R, mid, CLOUD)[i] = s.cloud; field(R, mid, ICE)[i] = s.ice; field(R, mid, ICENUM)[i] = s.inum;
+    }
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicExch(&R.cnt[C_FAILED], 1ull);
+    size_t nch = (R.n + CHUNK - 1) / CHUNK;
+    blockSums<3>(wsum, R.part + nch * NCONS * 3 + (size_t)chunk * 4, sh);
+  }
+}
+
+// Smagorinsky-Lilly eddy viscosities (Turbulence.viscosity, src/core/turbulence.ts:87-137): anisotropic horizontal
+// width, cube-root (or dz) vertical width with the per-level explicit cap, dry N^2 or the saturated one in cloud
+// (theta-e form; Durran-Klemp when switched on).
+__global__ void k_viscosity(const RunDesc* runs, const int4* items, int nitems, int set) {
+  FOR_ITEMS {
+    const RunDesc& R = runs[items[it].x];
+    if (R.cnt[C_FAILED]) continue;
+    const int nx = R.nx, ny = R.ny, nz = R.nz, layer = R.layer, i0 = items[it].y * CHUNK, i1 = min(R.n, i0 + CHUNK);
+    const float *u = field(R, set, U), *v = field(R, set, V), *w = field(R, set, W), *th = field(R, set, THETA);
+    const float *qv = field(R, set, Q), *cl = field(R, set, CLOUD), *ic = field(R, set, ICE);
+    float *km = R.kmkh, *kh = R.kmkh + R.n;
+    const bool ice = R.flags & RF_ICE;
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+      int z = i / layer, c = i - z * layer, y = c / nx, x = c - y * nx, l = z * layer;
+      int e = wrap(x + 1, nx) + y * nx + l, wst = wrap(x - 1, nx) + y * nx + l, n = x + wrap(y + 1, ny) * nx + l, s = x + wrap(y - 1, ny) * nx + l;
+      int up = z < nz - 1 ? layer : 0, dn = z > 0 ? -layer : 0;
+      float ihx = .5f * R.inv_dx, ihy = .5f * R.inv_dy, isp = lvl(R, L_INV_SPAN, z);
+      float dudx = (u[e] - u[wst]) * ihx, dvdy = (v[n] - v[s]) * ihy, dwdz = (w[i + up] - w[i + dn]) * isp;
+      float dudy = (u[n] - u[s]) * ihy, dvdx = (v[e] - v[wst]) * ihx;
+      float dudz = (u[i + up] - u[i + dn]) * isp, dwdx = (w[e] - w[wst]) * ihx;
+      float dvdz = (v[i + up] - v[i + dn]) * isp, dwdy = (w[n] - w[s]) * ihy;
+      float a1 = dudy + dvdx, a2 = dudz + dwdx, a3 = dvdz + dwdy;
+      float s2 = 2.f * (dudx * dudx + dvdy * dvdy + dwdz * dwdz) + a1 * a1 + a2 * a2 + a3 * a3;
+      float n2 = lvl(R, L_G_OVER_THB, z) * ((th[i + up] - th[i + dn]) + lvl(R, L_DTHB, z)) * isp;
+      float cond = ice ? cl[i] + ic[i] : cl[i];
+      if (cond > 1e-5f) {
+        const int zu = z + (up ? 1 : 0), zd = z - (dn ? 1 : 0);
+        float condU = ice ? cl[i + up] + ic[i + up] : cl[i + up], condD = ice ? cl[i + dn] + ic[i + dn] : cl[i + dn];
+        float Ti = lvl(R, L_THB, z) + th[i], Tu = lvl(R, L_THB, zu) + th[i + up], Td = lvl(R, L_THB, zd) + th[i + dn];
+        if ((R.flags & RF_DK) && condU > 1e-5f && condD > 1e-5f) {
+          const float LV = 2.5e6f, RD = 287.05f, CP = 1004.f, EPS = .622f;
+          float t = Ti * lvl(R, L_EXNER, z), qs = qv[i];
+          float factor = (1.f + LV * qs / (RD * t)) / (1.f + EPS * LV * LV * qs / (CP * RD * t * t));
+          n2 = 9.81f * (factor * ((Tu - Td) / Ti + LV / (CP * t) * (qv[i + up] - qv[i + dn])) - (qv[i + up] + condU - qv[i + dn] - condD)) * isp;
+        } else {
+          const float L_CP = 2.5e6f / 1004.f;
+          float ti = Ti * expf(L_CP * qv[i] / (Ti * lvl(R, L_EXNER, z)));
+          float tu = Tu * expf(L_CP * qv[i + up] / (Tu * lvl(R, L_EXNER, zu)));
+          float td = Td * expf(L_CP * qv[i + dn] / (Td * lvl(R, L_EXNER, zd)));
+          n2 = 9.81f / ti * (tu - td) * isp;
+        }
+      }
+      float rate = sqrtf(fmaxf(0.f, s2 - 3.f * n2));
+      float kmv = fminf(lvl(R, L_CAP, z), lvl(R, L_LEN2, z) * rate);
+      km[i] = kmv;
+      kh[i] = (R.flags & RF_ANISO) ? fminf(R.capH, R.lenH2 * rate) : kmv;
+    }
+  }
+}
+
+// Explicit flux-form diffusion of each mixed field's departure (Turbulence.mix, src/core/turbulence.ts:143-185),
+// then the ground drag balanced against the environment's own and rigid w at the ground and top (mixStep, :1179-1194).
+// In: set `in`; out: set A.
+__global__ void k_mix(const RunDesc* runs, const int4* items, int nitems, int in) {
+  FOR_ITEMS {
+    const RunDesc& R = runs[items[it].x];
+    if (R.cnt[C_FAILED]) continue;
+    const int nx = R.nx, ny = R.ny, nz = R.nz, layer = R.layer, i0 = items[it].y * CHUNK, i1 = min(R.n, i0 + CHUNK);
+    const float *km = R.kmkh, *kh = R.kmkh + R.n;
+    const int nmix = (R.flags & RF_ICE) ? NMIX : 6;
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+      int z = i / layer, c = i - z * layer, y = c / nx, x = c - y * nx, l = z * layer;
+      int e = wrap(x + 1, nx) + y * nx + l, wst = wrap(x - 1, nx) + y * nx + l, n = x + wrap(y + 1, ny) * nx + l, s = x + wrap(y - 1, ny) * nx + l;
+      float khi = kh[i], kmi = km[i];
+      float hE = .5f * (khi + kh[e]), hW = .5f * (kh[wst] + khi), hN = .5f * (khi + kh[n]), hS = .5f * (kh[s] + khi);
+      float vU = z < nz - 1 ? .5f * (kmi + km[i + layer]) * lvl(R, L_MIXUP, z) * lvl(R, L_INV_DZS, z) : 0.f;
+      float vD = z > 0 ? .5f * (km[i - layer] + kmi) * lvl(R, L_MIXDN, z) * lvl(R, L_INV_DZS, z - 1) : 0.f;
+      float ix2 = R.inv_dx * R.inv_dx, iy2 = R.inv_dy * R.inv_dy;
+      float uu = 0.f, vv = 0.f;
+      for (int k = 0; k < nmix; k++) {
+        const int f = mix_field(k);
+        const float factor = k < 3 ? 1.f : 3.f;
+        const float* a = field(R, in, f);
+        float ai = a[i];
+        // vertical departures: the base differences to the level above / below (u, v, q carry a base profile;
+        // theta' is already a departure; w, cloud, ice, number have none)
+        float bu = 0.f, bd = 0.f;
+        if (f == U) { bu = z < nz - 1 ? lvl(R, L_DUENV, z) : 0.f; bd = z > 0 ? lvl(R, L_DUENV, z - 1) : 0.f; }
+        else if (f == V) { bu = z < nz - 1 ? lvl(R, L_DVENV, z) : 0.f; bd = z > 0 ? lvl(R, L_DVENV, z - 1) : 0.f; }
+        else if (f == Q) { bu = z < nz - 1 ? lvl(R, L_DQB, z) : 0.f; bd = z > 0 ? lvl(R, L_DQB, z - 1) : 0.f; }
+        float tx = (hE * (a[e] - ai) - hW * (ai - a[wst])) * ix2;
+        float ty = (hN * (a[n] - ai) - hS * (ai - a[s])) * iy2;
+        float tz = (z < nz - 1 ? vU * ((a[i + layer] - ai) - bu) : 0.f) - (z > 0 ? vD * ((ai - a[i - layer]) - bd) : 0.f);
+        float out = ai + R.dt * factor * (tx + ty + tz);
+        if (f == U) uu = out;
+        else if (f == V) vv = out;
+        else {
+          if (f == W && (z == 0 || z == nz - 1)) out = 0.f;
+          field(R, 0, f)[i] = out;
+        }
+      }
+      if (z == 0 && R.drag != 0.f) {
+        float ug = uu + R.frame_u, vg = vv + R.frame_v, speed = sqrtf(ug * ug + vg * vg);
+        uu -= R.drag * (speed * ug - R.env_speed * R.ue0);
+        vv -= R.drag * (speed * vg - R.env_speed * R.ve0);
+      }
+      field(R, 0, U)[i] = uu; field(R, 0, V)[i] = vv;
+    }
+  }
+}
+
+// Per run, once a step: the water budget and negative mass of this step added in a fixed order, the step count,
+// the scratch reset for the next step.
+__global__ void k_step_end(const RunDesc* runs, const int4* items, int nitems) {
+  FOR_ITEMS {
+    const RunDesc& R = runs[items[it].x];
+    if (threadIdx.x == 0 && !R.cnt[C_FAILED]) {
+      const size_t nch = (R.n + CHUNK - 1) / CHUNK;
+      double w[3] = {0, 0, 0};
+      for (size_t c = 0; c < nch; c++) for (int j = 0; j < 3; j++) w[j] += R.part[nch * NCONS * 3 + c * 4 + j];
+      for (int j = 0; j < 3; j++) R.acc[A_WATER + j] += w[j];
+      R.cnt[C_STEPS] += 1;
+    }
+    __syncthreads();
+    if (threadIdx.x < S_COUNT + 16) R.scr[threadIdx.x] = 0.f;
+    __syncthreads();
+  }
+}
+
+// FP64 max |D R u| over the dual cells of a set (the divergence check).
+__global__ void k_divergence_max(const RunDesc* runs, const int4* items, int nitems, int set, double* out) {
+  FOR_ITEMS {
+    const RunDesc& R = runs[items[it].x];
+    const int nx = R.nx, ny = R.ny, layer = R.layer, i0 = items[it].y * CHUNK, i1 = min(R.ncells, i0 + CHUNK);
+    const float *u = field(R, set, U), *v = field(R, set, V), *w = field(R, set, W);
+    double m = 0;
+    for (int cidx = i0 + threadIdx.x; cidx < i1; cidx += blockDim.x) {
+      int k = cidx / layer, c = cidx - k * layer, y = c / nx, x = c - y * nx;
+      int l0 = k * layer, x1 = wrap(x + 1, nx), y1 = wrap(y + 1, ny);
+      int a = x + y * nx + l0, b = x1 + y * nx + l0, ee = x + y1 * nx + l0, f = x1 + y1 * nx + l0, g = a + layer, h = b + layer, s = ee + layer, tt = f + layer;
+      double r0 = lvl(R, L_RHO, k) / 4.0, r1 = lvl(R, L_RHO, k + 1) / 4.0;
+      double ddx = (r0 * ((double)u[b] + u[f] - u[a] - u[ee]) + r1 * ((double)u[h] + u[tt] - u[g] - u[s])) / R.dx;
+      double ddy = (r0 * ((double)v[ee] + v[f] - v[a] - v[b]) + r1 * ((double)v[s] + v[tt] - v[g] - v[h])) / R.dy;
+      double ddz = (r1 * ((double)w[g] + w[h] + w[s] + w[tt]) - r0 * ((double)w[a] + w[b] + w[ee] + w[f])) / lvl(R, L_DZS, k);
+      m = fmax(m, fabs(ddx + ddy + ddz));
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<unsigned long long*>(out), (unsigned long long)__double_as_longlong(m));
+  }
+}
+
+// ==================================================================== launchers
+#define GRID(n, cap) dim3(max(1, min((n), (cap))))
+
+void launch_theta_in(const Launch& L, const float* src) { k_theta_in<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, src); }
+void launch_theta_out(const Launch& L, float* dst) { k_theta_out<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, dst); }
+void launch_fall_courant(const Launch& L) { k_fall_courant<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n); }
+void launch_sediment(const Launch& L, int maxnz) {
+  k_sediment<<<GRID(L.n, L.cap), SED_COLS, 2 * maxnz * SED_COLS * sizeof(float), L.stream>>>(L.runs, L.items, L.n);
+}
+void launch_proj_div_xfft(const Launch& L, int mode, int set, int yc, int maxnx) {
+  size_t smem = (size_t)2 * ((yc + 1) / 2) * maxnx * sizeof(float2);
+  k_proj_div_xfft<<<GRID(L.n, L.cap), 256, smem, L.stream>>>(L.runs, L.items, L.n, mode, set, yc);
+}
+void launch_proj_modes(const Launch& L, int mode, int maxnz, int maxny, int threads) {
+  size_t smem = (size_t)(maxnz + MODE_GROUP) * maxny * sizeof(float2);
+  k_proj_modes<<<GRID(L.n, L.cap), threads, smem, L.stream>>>(L.runs, L.items, L.n, mode);
+}
+void launch_proj_xifft(const Launch& L, int mode, int yc, int maxnx) {
+  size_t smem = ((size_t)yc * (maxnx / 2 + 1) + (size_t)2 * ((yc + 1) / 2) * maxnx) * sizeof(float2);
+  k_proj_xifft<<<GRID(L.n, L.cap), 256, smem, L.stream>>>(L.runs, L.items, L.n, mode, yc);
+}
+void launch_face_correct(const Launch& L, int set) { k_face_correct<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set); }
+void launch_pres_correct(const Launch& L, int set, int final_) { k_pres_correct<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set, final_); }
+void launch_transport(const Launch& L, int in_set, int out_set, float frac, int stage, int TX, int TY) {
+  size_t smem = ((size_t)(TX + 6) * (TY + 6) + (size_t)TY * (TX + 1) + (size_t)(TY + 1) * TX) * sizeof(float);
+  k_transport<<<GRID(L.n, L.cap), TX * TY, smem, L.stream>>>(L.runs, L.items, L.n, in_set, out_set, frac, stage, TX, TY);
+}
+void launch_fill_partial(const Launch& L, int set) { k_fill_partial<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set); }
+void launch_fill_final(const Launch& L) { k_fill_final<<<GRID(L.n, L.cap), 32, 0, L.stream>>>(L.runs, L.items, L.n); }
+void launch_physics(const Launch& L, int in, int mid) { k_physics<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, in, mid); }
+void launch_viscosity(const Launch& L, int set) { k_viscosity<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set); }
+void launch_mix(const Launch& L, int in) { k_mix<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, in); }
+void launch_step_end(const Launch& L) { k_step_end<<<GRID(L.n, L.cap), 64, 0, L.stream>>>(L.runs, L.items, L.n); }
+void launch_divergence_max(const Launch& L, int set, double* out) { k_divergence_max<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set, out); }
+
+cudaError_t set_smem_limits(int bytes) {
+  cudaError_t e;
+  if ((e = cudaFuncSetAttribute(k_proj_modes, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(k_proj_div_xfft, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(k_proj_xifft, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(k_sediment, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(k_transport, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
+  return cudaSuccess;
+}
+
+}  // namespace sg

@@ -1,0 +1,37 @@
+// Host-side launchers of the step's kernels (sg_kernels.cu). Each launch covers a list of work items of a batch.
+#pragma once
+#include <cuda_runtime.h>
+#include "sg_common.cuh"
+
+namespace sg {
+
+enum ProjMode { PROJ_FACE = 0, PROJ_PRES = 1 };
+
+struct Launch {
+  const RunDesc* runs;   // device array of run descriptors
+  const int4* items;     // device work items (slot, a, b, c)
+  int n;                 // number of items
+  int cap;               // grid cap (blocks)
+  cudaStream_t stream;
+};
+
+void launch_theta_in(const Launch& L, const float* src);
+void launch_theta_out(const Launch& L, float* dst);
+void launch_fall_courant(const Launch& L);
+void launch_sediment(const Launch& L, int maxnz);
+void launch_proj_div_xfft(const Launch& L, int mode, int set, int yc, int maxnx);
+void launch_proj_modes(const Launch& L, int mode, int maxnz, int maxny, int threads);
+void launch_proj_xifft(const Launch& L, int mode, int yc, int maxnx);
+void launch_face_correct(const Launch& L, int set);
+void launch_pres_correct(const Launch& L, int set, int final_);
+void launch_transport(const Launch& L, int in_set, int out_set, float frac, int stage, int TX, int TY);
+void launch_fill_partial(const Launch& L, int set);
+void launch_fill_final(const Launch& L);
+void launch_physics(const Launch& L, int in, int mid);
+void launch_viscosity(const Launch& L, int set);
+void launch_mix(const Launch& L, int in);
+void launch_step_end(const Launch& L);
+void launch_divergence_max(const Launch& L, int set, double* out);
+cudaError_t set_smem_limits(int bytes);
+
+}  // namespace sg

@@ -1,0 +1,302 @@
+// Bulk microphysics of one node in FP32: warm rain (Kessler), one-moment Lin ice, snow, graupel and hail, the
+// saturation adjustment, secondary ice; each function follows the reference routine it names (file:line) and
+// updates the node in the reference's order. theta is held as its departure `thp` from the level's base value `thb`;
+// a temperature is formed as (thb + thp) * exner where the reference reads theta * exner.
+#pragma once
+#include <math.h>
+#include "sg_common.cuh"
+
+namespace sg {
+namespace phys {
+
+constexpr float G = 9.81f, CP = 1004.f, LV = 2.5e6f, RD = 287.05f, RV = 461.5f, EPS = .622f;
+constexpr float LF = 3.34e5f, LS = 2.5e6f + 3.34e5f, T0 = 273.15f, T_HOM = 235.15f, CW = 4187.f;
+constexpr float CRYSTAL_MASS = 1e-12f, MAX_CRYSTAL_MASS = 9.4e-10f, SPLINTERS = 3.5e8f, MAX_NUCLEATED = 250e3f;
+constexpr float KA = 2.43e-2f, PSI = 2.26e-5f, NU = 1.51e-5f;
+constexpr float N0S = 3e6f, RHO_S = 100.f, N0G = 4e4f, RHO_G = 400.f, N0R = 8e6f, RHO_W = 1000.f, N0H = 4e4f, RHO_H = 900.f;
+constexpr float PI = 3.14159265358979f;
+constexpr float GAMMA_3D = 2.5493f, GAMMA_4D = 8.2850f, GAMMA_5D2 = 1.4569f, GAMMA_45 = 11.6317f, GAMMA_35 = 3.3234f, GAMMA_275 = 1.6084f;
+// C_S = 152.93 * 0.01^0.75 (src/core/ice.ts:122) and the droplet mass pi/6 * 1000 * (20 um)^3 (:102), evaluated in FP64.
+constexpr float C_S = 4.8360712f;
+constexpr float SQRT_C_S = 2.1991069f;
+constexpr float DROPLET_MASS = 4.18879020e-12f;
+constexpr float SC13 = 0.84343267f;  // 0.6^(1/3)
+
+SG_HD float fclamp(float x, float a, float b) { return fmaxf(a, fminf(b, x)); }
+
+struct Node { float thp, thb, q, cloud, rain, ice, inum, snow, graupel, hail, cold; };
+
+SG_HD float qsatP(float t, float p) {  // src/core/microphysics.ts:5
+  float es = 611.2f * expf(17.67f * t / (t + 243.5f));
+  return fclamp(EPS * es / fmaxf(1000.f, p - es), 0.f, .045f);
+}
+SG_HD float qsatIce(float t, float p) {  // src/core/ice.ts:130-134
+  if (t >= 0.f) return qsatP(t, p);
+  float es = 611.21f * expf(22.587f * t / (t + 273.86f));
+  return fclamp(EPS * es / fmaxf(1000.f, p - es), 0.f, .045f);
+}
+// Fall speeds (src/core/microphysics.ts:37, ice.ts:143, graupel.ts:21, hail.ts:102); fallsq = sqrt(rho_ground / rho).
+SG_HD float rainFall(float rain, float rho, float fallsq) { return rain > 0.f ? 36.34f * powf(.001f * rho * rain, .1364f) * fallsq : 0.f; }
+SG_HD float snowFall(float snow, float rho, float fallsq) {
+  return snow > 1e-9f ? C_S * GAMMA_4D / 6.f * powf(PI * RHO_S * N0S / (rho * snow), -.0625f) * fallsq : 0.f;
+}
+SG_HD float fallCoef(float rho, float rhoX) { return sqrtf(4.f * G * rhoX / (3.f * .6f * rho)); }
+SG_HD float graupelFall(float x, float rho) { return x > 1e-9f ? fallCoef(rho, RHO_G) * GAMMA_45 / 6.f * powf(PI * RHO_G * N0G / (rho * x), -.125f) : 0.f; }
+SG_HD float hailFall(float x, float rho) { return x > 1e-9f ? fallCoef(rho, RHO_H) * GAMMA_45 / 6.f * powf(PI * RHO_H * N0H / (rho * x), -.125f) : 0.f; }
+SG_HD float hailMaxDiameter(float hail, float rho) {  // src/core/hail.ts:107-111
+  if (!(hail > 1e-9f)) return 0.f;
+  float lambda = powf(PI * RHO_H * N0H / (rho * hail), .25f);
+  return fmaxf(0.f, logf(N0H * 10.f / lambda) / lambda);
+}
+
+// src/core/microphysics.ts:48-60 (Marshall-Palmer intercept). Returns the evaporated rain.
+SG_HD float rainProcesses(Node& s, float tk, float p, float rho, float dt, bool evaporate) {
+  float qc = s.cloud, qr = s.rain;
+  float rate = .001f * fmaxf(0.f, qc - .001f) + (qr > 0.f ? 2.2f * qc * powf(qr, .875f) : 0.f);
+  float production = fminf(qc, rate * dt);
+  s.cloud -= production; s.rain += production;
+  float qs = qsatP(tk - 273.15f, p);
+  if (!evaporate || s.rain <= 0.f || s.q >= qs) return 0.f;
+  float rq = .001f * rho * s.rain, vent = 1.6f + 124.9f * powf(rq, .2046f);
+  float er = (1.f - s.q / qs) * vent * powf(rq, .525f) / (.001f * rho * (5.4e5f + 2.55e6f / (p / 100.f * qs)));
+  float ev = fminf(fminf(s.rain, er * dt), (qs - s.q) / (1.f + LV * LV * qs / (CP * RV * tk * tk)));
+  s.rain -= ev; s.q += ev;
+  return ev;
+}
+// src/core/microphysics.ts:67-77
+SG_HD float saturationAdjust(Node& s, float exner, float p) {
+  float total = 0.f;
+  for (int k = 0; k < 2; k++) {
+    float tk = (s.thb + s.thp) * exner, qs = qsatP(tk - 273.15f, p);
+    float d = (s.q - qs) / (1.f + LV * LV * qs / (CP * RV * tk * tk));
+    if (d < 0.f) d = fmaxf(d, -s.cloud);
+    if (d == 0.f) break;
+    s.q -= d; s.cloud += d; s.thp += LV / (CP * exner) * d; total += d;
+  }
+  return total;
+}
+SG_HD float cooperCrystals(float tc) { return tc >= -5.f ? 0.f : fminf(MAX_NUCLEATED, 5.f * expf(.304f * -tc)); }  // src/core/ice.ts:137
+// src/core/ice.ts:154-176 (number = the crystal count)
+SG_HD float saturationAdjustMixed(Node& s, float exner, float p) {
+  float heat = LF / (CP * exner);
+  if ((s.thb + s.thp) * exner >= T_HOM) {
+    if (s.ice > 0.f && (s.thb + s.thp) * exner > T0) {
+      float melt = fminf(s.ice, ((s.thb + s.thp) * exner - T0) * CP / LF);
+      s.inum *= 1.f - melt / s.ice;
+      s.ice -= melt; s.cloud += melt; s.thp -= heat * melt;
+    }
+    return saturationAdjust(s, exner, p);
+  }
+  if (s.cloud > 0.f) { s.inum += s.cloud / DROPLET_MASS; s.ice += s.cloud; s.thp += heat * s.cloud; s.cloud = 0.f; }
+  float total = 0.f;
+  for (int k = 0; k < 2; k++) {
+    float tk = (s.thb + s.thp) * exner, qs = qsatIce(tk - T0, p);
+    float d = (s.q - qs) / (1.f + LS * LS * qs / (CP * RV * tk * tk));
+    if (d < 0.f) d = fmaxf(d, -s.ice);
+    if (d == 0.f) break;
+    s.q -= d; s.ice += d; s.thp += LS / (CP * exner) * d; total += d;
+  }
+  return total;
+}
+SG_HD void freezeRain(Node& s, float exner) {  // src/core/ice.ts:179-183
+  float r = s.rain;
+  if (r <= 0.f || (s.thb + s.thp) * exner >= T_HOM) return;
+  s.rain = 0.f; s.graupel += r; s.thp += LF / (CP * exner) * r;
+}
+SG_HD void settleCrystals(Node& s) {  // src/core/ice.ts:245-248
+  float qi = s.ice;
+  s.inum = qi > 1e-12f ? fminf(qi / CRYSTAL_MASS, fmaxf(qi / MAX_CRYSTAL_MASS, s.inum)) : 0.f;
+}
+// Koenig (1971) crystal growth table of the reference (src/core/ice.ts:197-200), as coded there; a device copy in
+// constant memory and a host copy for the CPU build of these functions.
+#define SG_KOENIG_A1 {.7939e-7f, .7841e-6f, .3369e-5f, .4336e-5f, .5285e-5f, .3728e-5f, .1852e-5f, .2991e-6f, .4248e-6f, .7434e-6f, .1812e-5f, .4394e-5f, .9145e-5f, .1725e-4f, .3348e-4f, \
+  .1725e-4f, .9175e-5f, .4412e-5f, .2252e-5f, .9115e-6f, .4876e-6f, .3473e-6f, .4758e-6f, .6306e-6f, .8573e-6f, .7868e-6f, .7192e-6f, .6513e-6f, .5956e-6f, .5333e-6f, .4834e-6f}
+#define SG_KOENIG_A2 {.4006f, .4831f, .5320f, .5307f, .5319f, .5249f, .4888f, .3894f, .4047f, .4318f, .4771f, .5183f, .5463f, .5651f, .5813f, \
+  .5655f, .5478f, .5203f, .4906f, .4447f, .4126f, .3960f, .4149f, .4320f, .4506f, .4483f, .4460f, .4433f, .4413f, .4382f, .4361f}
+#ifdef __CUDACC__
+__constant__ float KOENIG_A1_D[31] = SG_KOENIG_A1;
+__constant__ float KOENIG_A2_D[31] = SG_KOENIG_A2;
+#endif
+static const float KOENIG_A1_H[31] = SG_KOENIG_A1;
+static const float KOENIG_A2_H[31] = SG_KOENIG_A2;
+#ifdef __CUDA_ARCH__
+#define KOENIG_A1 KOENIG_A1_D
+#define KOENIG_A2 KOENIG_A2_D
+#else
+#define KOENIG_A1 KOENIG_A1_H
+#define KOENIG_A2 KOENIG_A2_H
+#endif
+SG_HD float koenigGrowth(float tc, float m) {  // src/core/ice.ts:203-206
+  float x = fclamp(-tc, 1.f, 31.f) - 1.f; int k = (int)fminf(29.f, floorf(x)); float f = x - (float)k, g = m * 1000.f;
+  return 1e-3f * ((1.f - f) * KOENIG_A1[k] * powf(g, KOENIG_A2[k]) + f * KOENIG_A1[k + 1] * powf(g, KOENIG_A2[k + 1]));
+}
+// src/core/ice.ts:223-242
+SG_HD float iceProcesses(Node& s, float exner, float p, float rho, float dt) {
+  float tk = (s.thb + s.thp) * exner, tc = tk - T0;
+  if (tc >= 0.f || tk < T_HOM) return 0.f;
+  float qsi = qsatIce(tc, p), limit = (s.q - qsi) / (1.f + LS * LS * qsi / (CP * RV * tk * tk)), heat = LS / (CP * exner), lacking = cooperCrystals(tc) / rho - s.inum;
+  float change = 0.f;
+  if (limit > 0.f && lacking > 0.f) { change = fminf(limit, lacking * CRYSTAL_MASS); s.inum += change / CRYSTAL_MASS; }
+  float qi = s.ice + change, n = s.inum;
+  if (qi > 1e-12f && n > 0.f) {
+    if (s.q > qsi) change += fminf(n * koenigGrowth(tc, qi / n) * (s.q - qsi) / (qsatP(tc, p) - qsi) * dt, limit - change);
+    else {
+      float a = LS * LS / (KA * RV * tk * tk), b = 1.f / (rho * qsi * PSI);
+      float size = cbrtf(6.f * rho * qi / (PI * 900.f * (n * rho)));
+      float lost = fminf(qi, n * 2.f * PI * size * (1.f - s.q / qsi) / (a + b) * dt);
+      change -= lost; s.inum *= 1.f - lost / qi;
+    }
+  }
+  s.ice += change; s.q -= change; s.thp += heat * change;
+  float excess = s.ice - s.inum * MAX_CRYSTAL_MASS;
+  if (excess > 0.f) { s.ice -= excess; s.snow += excess; }
+  return change < 0.f ? -heat * change : 0.f;
+}
+// src/core/ice.ts:266-303 (riming of snow into graupel off, the reference default)
+SG_HD float snowProcesses(Node& s, float exner, float p, float rho, float fallsq, float dt) {
+  float tk = (s.thb + s.thp) * exner, tc = tk - T0, qs = s.snow;
+  if (tc < 0.f && s.ice > 0.f) {
+    float aut = 1e-3f * expf(.025f * tc) * fmaxf(0.f, s.ice - .001f);
+    float moved = fminf(s.ice, aut * dt); s.ice -= moved; s.snow += moved;
+  }
+  if (qs <= 1e-9f) return 0.f;
+  float lambda = powf(PI * RHO_S * N0S / (rho * qs), .25f);
+  float sweep = PI * N0S * C_S * GAMMA_3D / (4.f * powf(lambda, 3.25f)) * fallsq;
+  float vent = N0S * (.78f / (lambda * lambda) + .31f * SC13 * GAMMA_5D2 * SQRT_C_S * sqrtf(fallsq) / sqrtf(NU) * powf(lambda, -2.625f));
+  float cooling = 0.f;
+  if (tc < 0.f) {
+    float saci = fminf(s.ice, sweep * expf(.025f * tc) * s.ice * dt); s.ice -= saci; s.snow += saci;
+    float sacw = fminf(s.cloud, sweep * s.cloud * dt); s.cloud -= sacw; s.snow += sacw;
+    s.thp += LF / (CP * exner) * sacw;
+    float qsi = qsatIce(tc, p), a = LS * LS / (KA * RV * tk * tk), b = 1.f / (rho * qsi * PSI);
+    float rate = 2.f * PI * (s.q / qsi - 1.f) * vent / (rho * (a + b));
+    float dep = rate > 0.f ? fminf(rate * dt, (s.q - qsi) / (1.f + LS * LS * qsi / (CP * RV * tk * tk))) : -fminf(s.snow, -rate * dt);
+    s.snow += dep; s.q -= dep; s.thp += LS / (CP * exner) * dep;
+    if (dep < 0.f) cooling -= LS / (CP * exner) * dep;
+  } else {
+    float sacw = fminf(s.cloud, sweep * s.cloud * dt); s.cloud -= sacw; s.rain += sacw;
+    float rate = 2.f * PI * KA * tc * vent / (rho * LF) + CW * tc / LF * sweep * s.cloud;
+    float melt = fminf(fminf(s.snow, rate * dt), CP * tc / LF);
+    s.snow -= melt; s.rain += melt; s.thp -= LF / (CP * exner) * melt; cooling += LF / (CP * exner) * melt;
+  }
+  return cooling;
+}
+// src/core/graupel.ts:34-72
+SG_HD float graupelProcesses(Node& s, float exner, float p, float rho, float dt) {
+  float tk = (s.thb + s.thp) * exner, tc = tk - T0, heat = 1.f / (CP * exner);
+  float cooling = 0.f;
+  if (tc < 0.f) {
+    if (s.rain > 1e-9f) {
+      float lambdaR = powf(PI * RHO_W * N0R / (rho * s.rain), .25f);
+      float l2 = lambdaR * lambdaR, l7 = l2 * l2 * l2 * lambdaR;
+      float rate = 20.f * PI * PI * 100.f * N0R * RHO_W / rho * (expf(-.66f * tc) - 1.f) / l7;
+      float frozen = fminf(s.rain, rate * dt); s.rain -= frozen; s.graupel += frozen; s.thp += LF * heat * frozen;
+    }
+    float aut = fminf(s.snow, 1e-3f * expf(.09f * tc) * fmaxf(0.f, s.snow - 6e-4f) * dt);
+    s.snow -= aut; s.graupel += aut;
+  }
+  float qg = s.graupel;
+  if (qg <= 1e-9f) return 0.f;
+  float lambda = powf(PI * RHO_G * N0G / (rho * qg), .25f), a = fallCoef(rho, RHO_G);
+  float sweep = PI * N0G * a * GAMMA_35 / (4.f * powf(lambda, 3.5f));
+  float vent = N0G * (.78f / (lambda * lambda) + .31f * SC13 * GAMMA_275 * sqrtf(a / NU) * powf(lambda, -2.75f));
+  if (tc < 0.f) {
+    float gacw = fminf(s.cloud, sweep * s.cloud * dt), gacr = fminf(s.rain, sweep * s.rain * dt);
+    float gaci = fminf(s.ice, sweep * .1f * s.ice * dt), gacs = fminf(s.snow, sweep * expf(.09f * tc) * s.snow * dt);
+    s.cloud -= gacw; s.rain -= gacr; s.ice -= gaci; s.snow -= gacs; s.graupel += gacw + gacr + gaci + gacs;
+    s.thp += LF * heat * (gacw + gacr);
+    float qsi = qsatIce(tc, p);
+    if (s.q < qsi) {
+      float aa = LS * LS / (KA * RV * tk * tk), b = 1.f / (rho * qsi * PSI);
+      float sub = fminf(fminf(s.graupel, 2.f * PI * (1.f - s.q / qsi) * vent / (rho * (aa + b)) * dt), (qsi - s.q) / (1.f + LS * LS * qsi / (CP * RV * tk * tk)));
+      s.graupel -= sub; s.q += sub; s.thp -= LS * heat * sub; cooling += LS * heat * sub;
+    }
+  } else {
+    float gacw = fminf(s.cloud, sweep * s.cloud * dt); s.cloud -= gacw; s.rain += gacw;
+    float rate = 2.f * PI * KA * tc * vent / (rho * LF) + CW * tc / LF * sweep * (s.cloud + s.rain);
+    float melt = fminf(fminf(s.graupel, rate * dt), CP * tc / LF);
+    s.graupel -= melt; s.rain += melt; s.thp -= LF * heat * melt; cooling += LF * heat * melt;
+  }
+  return cooling;
+}
+// src/core/hail.ts:99, :118-131
+SG_HD float ventilationOf(float lambda, float a, float n0) { return n0 * (.78f / (lambda * lambda) + .31f * SC13 * GAMMA_275 * sqrtf(a / NU) * powf(lambda, -2.75f)); }
+SG_HD float wetGrowth(float lambda, float a, float n0, float tc, float qv, float p, float rho, float iceRate) {
+  float heat = KA * -tc + LV * PSI * rho * (qsatP(0.f, p) - qv);
+  return fmaxf(0.f, 2.f * PI * ventilationOf(lambda, a, n0) * heat / (rho * (LF + CW * tc))) + iceRate * (1.f - 2106.f * tc / (LF + CW * tc));
+}
+// src/core/hail.ts:140-175
+SG_HD float hailProcesses(Node& s, float exner, float p, float rho, float dt) {
+  float tk = (s.thb + s.thp) * exner, tc = tk - T0, heat = 1.f / (CP * exner);
+  float cooling = 0.f;
+  // wetGrowing(graupel, N0G, RHO_G, ...) (src/core/hail.ts:127-131)
+  if (tc < 0.f && s.graupel > 1e-9f) {
+    float lambda = powf(PI * RHO_G * N0G / (rho * s.graupel), .25f), a = fallCoef(rho, RHO_G);
+    float k = PI * N0G * a * GAMMA_35 / (4.f * powf(lambda, 3.5f));
+    if (k * (s.cloud + s.rain + .1f * s.ice + expf(.09f * tc) * s.snow) > wetGrowth(lambda, a, N0G, tc, s.q, p, rho, k * (s.ice + s.snow))) {
+      float turned = s.graupel * (1.f - expf(-dt / 60.f)); s.graupel -= turned; s.hail += turned;
+    }
+  }
+  float qh = s.hail;
+  if (qh <= 1e-9f) return 0.f;
+  float lambda = powf(PI * RHO_H * N0H / (rho * qh), .25f), a = fallCoef(rho, RHO_H);
+  float k = PI * N0H * a * GAMMA_35 / (4.f * powf(lambda, 3.5f)), vent = ventilationOf(lambda, a, N0H);
+  if (tc < 0.f) {
+    float hacw = fminf(s.cloud, k * s.cloud * dt), hacr = fminf(s.rain, k * s.rain * dt), liquid = hacw + hacr;
+    float haci = fminf(s.ice, k * .1f * s.ice * dt), hacs = fminf(s.snow, k * expf(.09f * tc) * s.snow * dt), frozen = liquid;
+    float wet = wetGrowth(lambda, a, N0H, tc, s.q, p, rho, k * (s.ice + s.snow)) * dt;
+    if (liquid + haci + hacs > wet) {
+      haci = fminf(s.ice, k * s.ice * dt); hacs = fminf(s.snow, k * s.snow * dt);
+      frozen = fminf(liquid, fmaxf(0.f, wet - haci - hacs));
+    }
+    s.cloud -= hacw; s.rain += liquid - frozen - hacr; s.ice -= haci; s.snow -= hacs; s.hail += frozen + haci + hacs;
+    s.thp += LF * heat * frozen;
+    float qsi = qsatIce(tc, p);
+    if (s.q < qsi) {
+      float aa = LS * LS / (KA * RV * tk * tk), b = 1.f / (rho * qsi * PSI);
+      float sub = fminf(fminf(s.hail, 2.f * PI * (1.f - s.q / qsi) * vent / (rho * (aa + b)) * dt), (qsi - s.q) / (1.f + LS * LS * qsi / (CP * RV * tk * tk)));
+      s.hail -= sub; s.q += sub; s.thp -= LS * heat * sub; cooling += LS * heat * sub;
+    }
+  } else {
+    float hacw = fminf(s.cloud, k * s.cloud * dt); s.cloud -= hacw; s.rain += hacw;
+    float rate = 2.f * PI * KA * tc * vent / (rho * LF) + CW * tc / LF * k * (s.cloud + s.rain);
+    float melt = fminf(fminf(s.hail, rate * dt), CP * tc / LF);
+    s.hail -= melt; s.rain += melt; s.thp -= LF * heat * melt; cooling += LF * heat * melt;
+  }
+  return cooling;
+}
+SG_HD float splintering(float tc) { return tc >= -3.f || tc <= -8.f ? 0.f : tc > -5.f ? (-3.f - tc) * .5f : (tc + 8.f) * (1.f / 3.f); }
+SG_HD float fragmentsPerKg(float lambda) { return 2.5e13f * 7.f / (lambda * 1000.f * PI / 6.f); }
+
+// The microphysics part of physics(z) (src/core/model.ts:1384-1471), ice or warm. Returns evap (for the water
+// budget) through `evapOut`.
+SG_HD void microphysics(Node& s, float exner, float p, float rho, float fallsq, float dt, int flags, float& evapOut) {
+  float evap = (flags & RF_RAINFORM) ? rainProcesses(s, (s.thb + s.thp) * exner, p, rho, dt, (flags & RF_EVAP) != 0) : 0.f;
+  if (evap > 0.f) { float cool = LV / CP / exner * evap; s.thp -= cool; s.cold += cool; }
+  float cond;
+  if (flags & RF_ICE) {
+    freezeRain(s, exner);
+    settleCrystals(s);
+    s.cold += iceProcesses(s, exner, p, rho, dt);
+    float iceBefore = s.ice, cloudBefore = s.cloud;
+    s.cold += snowProcesses(s, exner, p, rho, fallsq, dt);
+    float rainBefore = s.rain;
+    s.cold += graupelProcesses(s, exner, p, rho, dt);
+    float rainFrozen = (s.thb + s.thp) * exner < 273.15f ? fmaxf(0.f, rainBefore - s.rain) : 0.f;
+    s.cold += hailProcesses(s, exner, p, rho, dt);
+    if (iceBefore > 0.f) s.inum *= s.ice / iceBefore;
+    float splinters = splintering((s.thb + s.thp) * exner - 273.15f) * SPLINTERS * fmaxf(0.f, cloudBefore - s.cloud)
+      + (rainFrozen > 0.f ? fragmentsPerKg(powf(PI * RHO_W * N0R / (rho * rainBefore), .25f)) * rainFrozen : 0.f);
+    if (splinters > 0.f) {
+      float fromG = fminf(s.graupel, splinters * CRYSTAL_MASS), fromS = fminf(s.snow, splinters * CRYSTAL_MASS - fromG);
+      s.graupel -= fromG; s.snow -= fromS; s.ice += fromG + fromS; s.inum += (fromG + fromS) / CRYSTAL_MASS;
+    }
+    cond = saturationAdjustMixed(s, exner, p);
+    settleCrystals(s);
+  } else cond = saturationAdjust(s, exner, p);
+  if (cond < 0.f) s.cold -= LV / CP / exner * cond * .14f;
+  evapOut = evap;
+}
+
+}  // namespace phys
+}  // namespace sg

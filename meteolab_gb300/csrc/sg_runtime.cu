@@ -1,0 +1,791 @@
+// Host runtime of the device step: context, runs, batch plans, CUDA graphs, the C ABI (include/stormgpu.h) and the
+// serving loop. Everything a run needs beyond its fields is precomputed here in FP64 when the run is created: the
+// per-level constants, the FP64 LU factorisations of the two vertical tridiagonal families (face projection,
+// src/core/advection.ts:222-241; pressure, src/core/pressure.ts:104-140), the FFT twiddles and radix plans.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+#include "../../include/stormgpu.h"
+#include "sg_common.cuh"
+#include "sg_fft.cuh"
+#include "sg_kernels.h"
+
+using namespace sg;
+
+namespace {
+
+constexpr int MAX_SLOTS = 4096;
+constexpr int YC = 16;            // rows per x-transform work item
+constexpr size_t ALIGN = 256;
+const double RK3[3] = {1.0 / 3, 1.0 / 2, 1.0};
+
+size_t align(size_t x) { return (x + ALIGN - 1) / ALIGN * ALIGN; }
+
+struct Layout {
+  size_t fld, faces, kmkh, phi, pres, spec, cols, lv, lv64, triF, triP, ab, twx, twy, scr, part, acc, cnt, total;
+};
+Layout layout(int nx, int ny, int nz) {
+  Layout L; size_t n = (size_t)nx * ny * nz, layer = (size_t)nx * ny, nm = nx / 2 + 1, nch = (n + CHUNK - 1) / CHUNK, o = 0;
+  auto take = [&](size_t bytes) { size_t at = o; o += align(bytes); return at; };
+  L.fld = take(3 * NF * n * 4); L.faces = take(4 * n * 4); L.kmkh = take(2 * n * 4); L.phi = take(n * 4);
+  L.pres = take(layer * (nz - 1) * 4); L.spec = take(nm * nz * ny * 8); L.cols = take(3 * layer * 4);
+  L.lv = take((size_t)L_COUNT * nz * 4); L.lv64 = take((size_t)D_COUNT * nz * 8);
+  L.triF = take(nm * nz * ny * 16); L.triP = take(nm * (nz - 1) * ny * 16); L.ab = take(nm * ny * 16);
+  L.twx = take(nx * 8); L.twy = take(ny * 8); L.scr = take(64 * 4); L.part = take((nch * NCONS * 3 + nch * 4) * 8);
+  L.acc = take(A_COUNT * 8); L.cnt = take(C_COUNT * 8); L.total = o;
+  return L;
+}
+
+struct Run {
+  bool live = false;
+  int slot = -1;
+  int nx = 0, ny = 0, nz = 0;
+  size_t bytes = 0;
+  char* mem = nullptr;
+  RunDesc desc{};
+};
+
+struct Plan {
+  std::vector<int> slots;
+  int4* items = nullptr;  // device
+  int off[8] = {0}, cnt[8] = {0};
+  int maxnx = 0, maxny = 0, maxnz = 0, TX = 40, TY = 8;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  ~Plan() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (items) cudaFree(items);
+  }
+};
+enum Family { FAM_NODE, FAM_COLS, FAM_ROWS_FACE, FAM_ROWS_PRES, FAM_MODES, FAM_TILES, FAM_RUNS, FAM_CELLS, FAM_COUNT };
+
+}  // namespace
+
+struct sg_context {
+  int device = 0, sms = 0, maxSmem = 0;
+  uint64_t budget = 0, used = 0;
+  cudaStream_t stream = nullptr;
+  RunDesc* d_runs = nullptr;
+  std::vector<Run> runs;
+  std::vector<int> freeSlots;
+  std::map<std::vector<int>, std::unique_ptr<Plan>> plans;
+  std::multimap<size_t, char*> pool;   // retired run allocations kept for reuse
+  uint64_t pooled = 0;
+  std::string error;
+  double* d_scalar = nullptr;           // scratch for reductions read back by the host
+};
+
+namespace {
+
+int fail(sg_context* ctx, int code, const std::string& msg) { if (ctx) ctx->error = msg; return code; }
+int cudaFail(sg_context* ctx, cudaError_t e, const char* where) {
+  return fail(ctx, SG_ERR_DEVICE, std::string(where) + ": " + cudaGetErrorString(e));
+}
+#define CK(call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) return cudaFail(ctx, e_, #call); } while (0)
+
+// ------------------------------------------------------------------ host precomputation
+struct HostTables { std::vector<float> lv; std::vector<double> lv64; std::vector<double2> triF, triP, ab; std::vector<float2> twx, twy; };
+
+void twiddles(int n, std::vector<float2>& tw) {
+  tw.resize(n);
+  for (int t = 0; t < n; t++) { double a = -2 * M_PI * t / n; tw[t] = make_float2((float)std::cos(a), (float)std::sin(a)); }
+}
+
+// Per-level constants (FP64 -> FP32), the turbulence widths and caps (src/core/turbulence.ts:91-99), the base-theta
+// face values for the profile tendency, the mixing coefficients, sponge shares (src/core/model.ts:1369, :1495).
+void build_tables(const sg_grid* g, const sg_base_state* b, const sg_switches* sw, HostTables& T, RunDesc& d) {
+  const int nx = g->nx, ny = g->ny, nz = g->nz, nm = nx / 2 + 1;
+  const double dx = g->dx, dy = g->dy, dt = sw->dt;
+  const double* zs = g->zs; const double* dzs = g->dzs; const double* hz = g->hz; const double* rho = b->rho;
+  T.lv.assign((size_t)L_COUNT * nz, 0.f); T.lv64.assign((size_t)D_COUNT * nz, 0.0);
+  auto L = [&](int w, int z, double v) { T.lv[(size_t)w * nz + z] = (float)v; };
+  auto D = [&](int w, int z, double v) { T.lv64[(size_t)w * nz + z] = v; };
+  const double G = 9.81, dzMean = g->height / (nz - 1);
+  const double* thb = b->theta;
+  auto thc = [&](int k) { return thb[std::max(0, std::min(nz - 1, k))]; };
+  auto up5 = [](double a, double bb, double c, double dd, double e) { return (2 * a - 13 * bb + 47 * c + 27 * dd - 3 * e) / 60; };
+  double cs = sw->cs;
+  for (int z = 0; z < nz; z++) {
+    double rUp = z < nz - 1 ? (rho[z] + rho[z + 1]) / 2 : 0;
+    L(L_RHO, z, rho[z]); L(L_INV_RHO, z, 1 / rho[z]); L(L_HZ, z, hz[z]); L(L_INV_HZ, z, 1 / hz[z]);
+    L(L_DZS, z, z < nz - 1 ? dzs[z] : 0); L(L_INV_DZS, z, z < nz - 1 ? 1 / dzs[z] : 0); L(L_RUP, z, rUp);
+    L(L_EXNER, z, b->exner[z]); L(L_P, z, b->p[z]); L(L_THB, z, thb[z]); L(L_QB, z, b->q[z]);
+    double ue = b->u[z] - sw->frame_u, ve = b->v[z] - sw->frame_v;
+    L(L_UENV, z, ue); L(L_VENV, z, ve); L(L_THVENV, z, thb[z] * (1 + .61 * b->q[z])); L(L_ZS, z, zs[z]);
+    // The base profile's vertical faces minus theta_b(z): the face above (k = z) and below (k = z - 1), each for
+    // both flow directions, with the reference's clamped stencils (src/core/advection.ts:356, :366).
+    double r0 = thb[z];
+    L(L_TH_UP_POS, z, up5(thc(z - 2), thc(z - 1), thc(z), thc(z + 1), thc(z + 2)) - r0);
+    L(L_TH_UP_NEG, z, up5(thc(z + 3), thc(z + 2), thc(z + 1), thc(z), thc(z - 1)) - r0);
+    L(L_TH_DN_POS, z, up5(thc(z - 3), thc(z - 2), thc(z - 1), thc(z), thc(z + 1)) - r0);
+    L(L_TH_DN_NEG, z, up5(thc(z + 2), thc(z + 1), thc(z), thc(z - 1), thc(z - 2)) - r0);
+    double local = z == 0 ? dzs[0] : z == nz - 1 ? dzs[nz - 2] : hz[z];
+    double len = sw->anisotropic && sw->vertical_dz ? local : std::cbrt(dx * dy * local);
+    L(L_LEN2, z, (cs * len) * (cs * len));
+    double mn = std::min(dx, dy);
+    if (z > 0) mn = std::min(mn, dzs[z - 1]);
+    if (z < nz - 1) mn = std::min(mn, dzs[z]);
+    L(L_CAP, z, .05 * mn * mn / dt);
+    int zu = z < nz - 1 ? z + 1 : z, zd = z > 0 ? z - 1 : z;
+    L(L_INV_SPAN, z, 1 / (zs[zu] - zs[zd]));
+    L(L_DTHB, z, thb[zu] - thb[zd]);
+    L(L_G_OVER_THB, z, G / thb[z]);
+    L(L_MIXUP, z, z < nz - 1 ? rUp / (rho[z] * hz[z]) : 0);
+    L(L_MIXDN, z, z > 0 ? (rho[z - 1] + rho[z]) / 2 / (rho[z] * hz[z]) : 0);
+    L(L_DUENV, z, z < nz - 1 ? (b->u[z + 1] - sw->frame_u) - ue : 0);
+    L(L_DVENV, z, z < nz - 1 ? (b->v[z + 1] - sw->frame_v) - ve : 0);
+    L(L_DQB, z, z < nz - 1 ? b->q[z + 1] - b->q[z] : 0);
+    L(L_FALLSQ, z, std::sqrt(rho[0] / rho[z]));
+    double alt = zs[z], H = g->height;
+    double sp = alt > sw->sponge_start ? std::max(0.0, std::min(1.0, (alt - sw->sponge_start) / (H - sw->sponge_start))) * sw->sponge_rate * dt : 0;
+    L(L_SPONGE, z, sp);
+    L(L_NODEMASS, z, dx * dy * hz[z] * rho[z]);
+    L(L_LW, z, hz[z] / dzMean * rho[z]);
+    L(L_SURF, z, 0);
+    double face = z > 0 ? (rho[z - 1] + rho[z]) / 2 : 0;
+    D(D_FLO, z, z > 0 ? face / dzs[z - 1] : 0);
+    D(D_FHZ, z, hz[z]);
+    D(D_PL1, z, z > 0 && z < nz - 1 ? -rho[z] * dzs[z - 1] / (4 * hz[z]) : 0);
+    D(D_PL2, z, z > 0 && z < nz - 1 ? rho[z] / (hz[z] * dzs[z]) : 0);
+    D(D_THB, z, thb[z]);
+  }
+  // Face projection factorisation [m][k][n] (src/core/advection.ts:222-241): rows -rho h lambda - lo - up.
+  T.triF.assign((size_t)nm * nz * ny, make_double2(0, 0));
+  std::vector<double> cp(nz);
+  auto faceRho = [&](int k) { return k < 0 || k >= nz - 1 ? 0.0 : (rho[k] + rho[k + 1]) / 2; };
+  for (int m = 0; m < nm; m++) for (int n = 0; n < ny; n++) {
+    double lam = (m == 0 && n == 0) ? 0 : 4 * std::pow(std::sin(M_PI * m / nx), 2) / (dx * dx) + 4 * std::pow(std::sin(M_PI * n / ny), 2) / (dy * dy);
+    bool pinned = lam == 0;
+    for (int k = 0; k < nz; k++) {
+      double lo = k > 0 ? faceRho(k - 1) / dzs[k - 1] : 0, up = k < nz - 1 ? faceRho(k) / dzs[k] : 0, di = -rho[k] * hz[k] * lam - lo - up;
+      if (pinned && k == 0) { lo = 0; di = 1; up = 0; }
+      if (pinned && k == 1) lo = 0;
+      double piv = k == 0 ? di : di - lo * cp[k - 1];
+      cp[k] = up / piv;
+      T.triF[((size_t)m * nz + k) * ny + n] = make_double2(pinned && k == 0 ? 0.0 : 1 / piv, cp[k]);
+    }
+  }
+  // Pressure factorisation [m][k][n] (src/core/pressure.ts:37-44, :104-140), the symbols snapped as there.
+  const int nc = nz - 1;
+  T.triP.assign((size_t)nm * nc * ny, make_double2(0, 0)); T.ab.assign((size_t)nm * ny, make_double2(0, 0));
+  auto exact = [](double x) { return x < 1e-12 ? 0 : x > 1 - 1e-12 ? 1 : x; };
+  for (int m = 0; m < nm; m++) for (int n = 0; n < ny; n++) {
+    double sx = exact(std::pow(std::sin(M_PI * m / nx), 2)), cx = exact(std::pow(std::cos(M_PI * m / nx), 2));
+    double sy = exact(std::pow(std::sin(M_PI * n / ny), 2)), cy = exact(std::pow(std::cos(M_PI * n / ny), 2));
+    double a = 4 * (sx * cy / (dx * dx) + cx * sy / (dy * dy)), bb = cx * cy;
+    T.ab[(size_t)m * ny + n] = make_double2(a, bb);
+    if ((a == 0 && bb == 0) || (nc == 1 && a == 0)) continue;  // null modes: zero
+    bool pinned = a == 0;
+    for (int k = 0; k < nc; k++) {
+      double di = -a / 2 * (rho[k] * dzs[k] / (2 * hz[k]) + rho[k + 1] * dzs[k] / (2 * hz[k + 1])), lo = 0, up = 0;
+      if (k > 0) { lo = a * T.lv64[(size_t)D_PL1 * nz + k] + bb * T.lv64[(size_t)D_PL2 * nz + k]; di -= bb * rho[k] / (hz[k] * dzs[k]); }
+      if (k < nc - 1) { up = -a / 2 * rho[k + 1] * dzs[k + 1] / (2 * hz[k + 1]); double v = bb * rho[k + 1] / (hz[k + 1] * dzs[k]); up += v; di -= v; }
+      if (pinned && k == 0) { lo = 0; di = 1; up = 0; }
+      if (pinned && k == 1) lo = 0;
+      double piv = k == 0 ? di : di - lo * cp[k - 1];
+      cp[k] = up / piv;
+      T.triP[((size_t)m * nc + k) * ny + n] = make_double2(pinned && k == 0 ? 0.0 : 1 / piv, cp[k]);
+    }
+  }
+  twiddles(nx, T.twx); twiddles(ny, T.twy);
+  d.nx = nx; d.ny = ny; d.nz = nz; d.layer = nx * ny; d.n = nx * ny * nz; d.nm = nm; d.mh = nx / 2; d.ncells = nx * ny * (nz - 1);
+  d.fx_nf = fft_plan_factors(nx, d.fx_rad); d.fy_nf = fft_plan_factors(ny, d.fy_rad);
+  d.dx = (float)dx; d.dy = (float)dy; d.inv_dx = (float)(1 / dx); d.inv_dy = (float)(1 / dy); d.dt = (float)dt; d.height = (float)g->height;
+  d.coriolis = (float)sw->coriolis; d.keep = (float)std::exp(-sw->wind_relaxation * dt); d.sponge_start = (float)sw->sponge_start; d.cs = (float)cs;
+  d.drag = (float)(sw->drag_cd * dt / hz[0]); d.frame_u = (float)sw->frame_u; d.frame_v = (float)sw->frame_v;
+  d.ue0 = (float)b->u[0]; d.ve0 = (float)b->v[0]; d.env_speed = (float)std::hypot(b->u[0], b->v[0]);
+  d.lenH2 = (float)std::pow(cs * std::sqrt(dx * dy), 2); d.capH = (float)(.05 * std::pow(std::min(dx, dy), 2) / dt); d.rho0 = (float)rho[0];
+  d.flags = (sw->loading ? RF_LOADING : 0) | (sw->evaporation ? RF_EVAP : 0) | (sw->rain_formation ? RF_RAINFORM : 0) | (sw->anisotropic ? RF_ANISO : 0) |
+            (sw->vertical_dz ? RF_VDZ : 0) | (sw->durran_klemp ? RF_DK : 0) | (sw->pressure_in_stages ? RF_STAGES : 0) | (sw->ice ? RF_ICE : 0);
+}
+
+int validate(sg_context* ctx, const sg_grid* g, const sg_base_state* b, const sg_switches* sw) {
+  if (!g || !b || !sw) return fail(ctx, SG_ERR_INVALID, "null grid, base state or switches");
+  if (g->nx < 1 || g->ny < 1 || g->nz < 3) return fail(ctx, SG_ERR_INVALID, "grid needs nx, ny >= 1 and nz >= 3");
+  if (g->nz > 128) return fail(ctx, SG_ERR_UNSUPPORTED, "nz > 128 levels");
+  if (g->nx > 4096 || g->ny > 4096) return fail(ctx, SG_ERR_UNSUPPORTED, "nx or ny > 4096");
+  int rad[8];
+  if (fft_plan_factors(g->nx, rad) < 0 || fft_plan_factors(g->ny, rad) < 0) return fail(ctx, SG_ERR_UNSUPPORTED, "nx or ny has more than 8 prime factors");
+  if (!(g->dx > 0 && g->dy > 0 && g->height > 0) || !g->zs || !g->dzs || !g->hz) return fail(ctx, SG_ERR_INVALID, "bad grid spacing or levels");
+  if (!b->p || !b->exner || !b->theta || !b->q || !b->u || !b->v || !b->rho) return fail(ctx, SG_ERR_INVALID, "null base-state array");
+  for (int z = 0; z < g->nz; z++) if (!(b->rho[z] > 0) || !(b->theta[z] > 0) || !(g->hz[z] > 0)) return fail(ctx, SG_ERR_INVALID, "non-positive rho, theta or hz");
+  if (!(sw->dt > 0)) return fail(ctx, SG_ERR_INVALID, "dt must be positive");
+  if (!sw->pressure_in_stages) return fail(ctx, SG_ERR_UNSUPPORTED, "the device step needs the pressure in the RK3 stages");
+  // The shared memory of the mode kernel: (nz + 8) * ny complex values.
+  size_t smem = (size_t)(g->nz + 8) * g->ny * 8;
+  if ((int)smem > ctx->maxSmem) return fail(ctx, SG_ERR_UNSUPPORTED, "(nz + 8) * ny too large for one block's shared memory");
+  return SG_OK;
+}
+
+Run* find(sg_context* ctx, sg_run run) {
+  if (run < 0 || run >= (int)ctx->runs.size() || !ctx->runs[run].live) return nullptr;
+  return &ctx->runs[run];
+}
+
+// ------------------------------------------------------------------ plans
+int build_plan(sg_context* ctx, const std::vector<int>& slots, Plan& P) {
+  P.slots = slots;
+  std::vector<int4> all[FAM_COUNT];
+  bool all40 = true, all8 = true;
+  for (int s : slots) {
+    const Run& r = ctx->runs[s];
+    P.maxnx = std::max(P.maxnx, r.nx); P.maxny = std::max(P.maxny, r.ny); P.maxnz = std::max(P.maxnz, r.nz);
+    if (r.nx % 40) all40 = false;
+    if (r.ny % 8) all8 = false;
+  }
+  // Tile of the transport: 40 x 8 columns on the benchmark grids (40, 80, 320 wide), else 32 x 8.
+  P.TX = all40 ? 40 : std::min(32, P.maxnx);
+  P.TY = all8 ? 8 : std::min(8, P.maxny);
+  for (int s : slots) {
+    const Run& r = ctx->runs[s];
+    int n = r.nx * r.ny * r.nz, nch = (n + CHUNK - 1) / CHUNK, layer = r.nx * r.ny;
+    for (int c = 0; c < nch; c++) all[FAM_NODE].push_back(make_int4(s, c, 0, 0));
+    int ncc = (r.nx * r.ny * (r.nz - 1) + CHUNK - 1) / CHUNK;
+    for (int c = 0; c < ncc; c++) all[FAM_CELLS].push_back(make_int4(s, c, 0, 0));
+    for (int c = 0; c < (layer + 63) / 64; c++) all[FAM_COLS].push_back(make_int4(s, c, 0, 0));
+    for (int k = 0; k < r.nz; k++) for (int y = 0; y < r.ny; y += YC) all[FAM_ROWS_FACE].push_back(make_int4(s, k, y, 0));
+    for (int k = 0; k < r.nz - 1; k++) for (int y = 0; y < r.ny; y += YC) all[FAM_ROWS_PRES].push_back(make_int4(s, k, y, 0));
+    for (int m = 0; m < r.nx / 2 + 1; m++) all[FAM_MODES].push_back(make_int4(s, m, 0, 0));
+    int tiles = ((r.nx + P.TX - 1) / P.TX) * ((r.ny + P.TY - 1) / P.TY);
+    for (int f = 0; f < NF; f++) for (int t = 0; t < tiles; t++) all[FAM_TILES].push_back(make_int4(s, f, t, 0));
+    all[FAM_RUNS].push_back(make_int4(s, 0, 0, 0));
+  }
+  std::vector<int4> flat;
+  for (int f = 0; f < FAM_COUNT; f++) { P.off[f] = (int)flat.size(); P.cnt[f] = (int)all[f].size(); flat.insert(flat.end(), all[f].begin(), all[f].end()); }
+  CK(cudaMalloc(&P.items, flat.size() * sizeof(int4)));
+  CK(cudaMemcpy(P.items, flat.data(), flat.size() * sizeof(int4), cudaMemcpyHostToDevice));
+  return SG_OK;
+}
+
+Launch lx(sg_context* ctx, const Plan& P, int fam, int capPerSm = 8) {
+  return Launch{ctx->d_runs, P.items + P.off[fam], P.cnt[fam], ctx->sms * capPerSm, ctx->stream};
+}
+
+// The step's launch sequence for a plan in five parts (the oracle's partition of AtmosphereModel.step):
+// 1 beginStep (fall speeds, sedimentation), 2 dynamics (face projection, RK3 stages with their projections),
+// 3 physicsStep (positivity fix, physics), 4 mixStep (viscosity, mixing, drag), 5 the final projection and the
+// end-of-step counters. `hook(k)` is called after each launch (profiling).
+template <class Hook>
+void enqueue_part(sg_context* ctx, const Plan& P, int part, Hook hook) {
+  const int A = 0, B = 1, C = 2;
+  Launch node = lx(ctx, P, FAM_NODE), cols = lx(ctx, P, FAM_COLS), rf = lx(ctx, P, FAM_ROWS_FACE), rp = lx(ctx, P, FAM_ROWS_PRES);
+  Launch modes = lx(ctx, P, FAM_MODES, 2), tiles = lx(ctx, P, FAM_TILES, 4), runs = lx(ctx, P, FAM_RUNS);
+  const int mthreads = std::min(512, std::max(128, P.maxny));
+  auto project = [&](int set, int final_) {
+    launch_proj_div_xfft(rp, PROJ_PRES, set, YC, P.maxnx); hook(7);
+    launch_proj_modes(modes, PROJ_PRES, P.maxnz, P.maxny, mthreads); hook(8);
+    launch_proj_xifft(rp, PROJ_PRES, YC, P.maxnx); hook(9);
+    launch_pres_correct(node, set, final_); hook(final_ ? 16 : 10);
+  };
+  if (part == 1) {
+    launch_fall_courant(node); hook(0);
+    launch_sediment(cols, P.maxnz); hook(1);
+  } else if (part == 2) {
+    launch_proj_div_xfft(rf, PROJ_FACE, A, YC, P.maxnx); hook(2);
+    launch_proj_modes(modes, PROJ_FACE, P.maxnz, P.maxny, mthreads); hook(3);
+    launch_proj_xifft(rf, PROJ_FACE, YC, P.maxnx); hook(4);
+    launch_face_correct(node, A); hook(5);
+    const int in[3] = {A, B, C}, out[3] = {B, C, B};
+    for (int s = 0; s < 3; s++) {
+      launch_transport(tiles, in[s], out[s], (float)RK3[s], s, P.TX, P.TY); hook(6);
+      if (s < 2) project(out[s], 0);
+    }
+  } else if (part == 3) {
+    launch_fill_partial(node, B); hook(11);
+    launch_fill_final(runs); hook(12);
+    launch_physics(node, B, C); hook(13);
+  } else if (part == 4) {
+    launch_viscosity(node, C); hook(14);
+    launch_mix(node, C); hook(15);
+  } else if (part == 5) {
+    project(A, 1);
+    launch_step_end(runs); hook(17);
+  }
+}
+template <class Hook>
+void enqueue_step(sg_context* ctx, const Plan& P, Hook hook) {
+  for (int part = 1; part <= 5; part++) enqueue_part(ctx, P, part, hook);
+}
+const char* KERNEL_NAMES[18] = {"fall_courant", "sediment", "face_div_xfft", "face_modes", "face_xifft", "face_correct", "transport",
+                                "pres_div_xfft", "pres_modes", "pres_xifft", "pres_correct", "fill_partial", "fill_final", "physics",
+                                "viscosity", "mix", "pres_correct_final", "step_end"};
+
+Plan* get_plan(sg_context* ctx, const std::vector<int>& slots, int* status) {
+  auto it = ctx->plans.find(slots);
+  if (it != ctx->plans.end()) { *status = SG_OK; return it->second.get(); }
+  if (ctx->plans.size() > 64) ctx->plans.clear();
+  auto P = std::make_unique<Plan>();
+  *status = build_plan(ctx, slots, *P);
+  if (*status != SG_OK) return nullptr;
+  Plan* raw = P.get();
+  ctx->plans[slots] = std::move(P);
+  return raw;
+}
+
+int ensure_graph(sg_context* ctx, Plan& P) {
+  if (P.exec) return SG_OK;
+  CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  enqueue_step(ctx, P, [](int) {});
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &P.graph);
+  if (e != cudaSuccess) return cudaFail(ctx, e, "cudaStreamEndCapture");
+  CK(cudaGraphInstantiate(&P.exec, P.graph, 0));
+  return SG_OK;
+}
+
+void drop_plans_with(sg_context* ctx, int slot) {
+  for (auto it = ctx->plans.begin(); it != ctx->plans.end();) {
+    if (std::find(it->first.begin(), it->first.end(), slot) != it->first.end()) it = ctx->plans.erase(it);
+    else ++it;
+  }
+}
+
+int slots_of(sg_context* ctx, const sg_run* runs, int n, std::vector<int>& slots) {
+  if (n < 1 || !runs) return fail(ctx, SG_ERR_INVALID, "empty batch");
+  for (int k = 0; k < n; k++) {
+    if (!find(ctx, runs[k])) return fail(ctx, SG_ERR_NOT_FOUND, "no run " + std::to_string(runs[k]));
+    slots.push_back(runs[k]);
+  }
+  std::vector<int> s = slots; std::sort(s.begin(), s.end());
+  if (std::adjacent_find(s.begin(), s.end()) != s.end()) return fail(ctx, SG_ERR_INVALID, "a run appears twice in the batch");
+  return SG_OK;
+}
+
+int batch_step(sg_context* ctx, const sg_run* runs, int n, int nsteps, bool wait) {
+  if (nsteps < 0) return fail(ctx, SG_ERR_INVALID, "negative step count");
+  std::vector<int> slots;
+  int st = slots_of(ctx, runs, n, slots);
+  if (st) return st;
+  Plan* P = get_plan(ctx, slots, &st);
+  if (!P) return st;
+  if ((st = ensure_graph(ctx, *P))) return st;
+  for (int s = 0; s < nsteps; s++) CK(cudaGraphLaunch(P->exec, ctx->stream));
+  if (wait) CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaGetLastError());
+  return SG_OK;
+}
+
+// A plan over one run for the boundary kernels (theta conversion).
+Plan* single_plan(sg_context* ctx, int slot, int* st) { return get_plan(ctx, std::vector<int>{slot}, st); }
+
+}  // namespace
+
+// ==================================================================== C ABI
+extern "C" {
+
+int sg_context_create(int device, uint64_t hbm_budget_bytes, sg_context** out) {
+  if (!out) return SG_ERR_INVALID;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return SG_ERR_DEVICE;
+  if (device < 0 || device >= count) return SG_ERR_INVALID;
+  auto* ctx = new sg_context;
+  ctx->device = device;
+  cudaError_t e;
+  if ((e = cudaSetDevice(device)) != cudaSuccess) { delete ctx; return SG_ERR_DEVICE; }
+  cudaDeviceProp prop;
+  cudaGetDeviceProperties(&prop, device);
+  ctx->sms = prop.multiProcessorCount; ctx->maxSmem = (int)prop.sharedMemPerBlockOptin;
+  size_t freeB = 0, totalB = 0; cudaMemGetInfo(&freeB, &totalB);
+  ctx->budget = hbm_budget_bytes ? hbm_budget_bytes : (uint64_t)(freeB * 0.9);
+  if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaMalloc(&ctx->d_runs, MAX_SLOTS * sizeof(RunDesc))) != cudaSuccess ||
+      (e = cudaMalloc(&ctx->d_scalar, 64 * sizeof(double))) != cudaSuccess ||
+      (e = set_smem_limits(ctx->maxSmem)) != cudaSuccess) {
+    delete ctx; return SG_ERR_DEVICE;
+  }
+  *out = ctx;
+  return SG_OK;
+}
+
+int sg_context_destroy(sg_context* ctx) {
+  if (!ctx) return SG_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  ctx->plans.clear();
+  for (auto& r : ctx->runs) if (r.live) cudaFree(r.mem);
+  for (auto& p : ctx->pool) cudaFree(p.second);
+  cudaFree(ctx->d_runs); cudaFree(ctx->d_scalar);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return SG_OK;
+}
+
+const char* sg_last_error(sg_context* ctx) { return ctx ? ctx->error.c_str() : "no context"; }
+
+uint64_t sg_run_bytes(const sg_grid* grid) { return grid ? layout(grid->nx, grid->ny, grid->nz).total : 0; }
+
+int sg_run_create(sg_context* ctx, const sg_grid* g, const sg_base_state* b, const sg_switches* sw, const float* const* init, sg_run* out) {
+  if (!ctx || !out) return SG_ERR_INVALID;
+  int st = validate(ctx, g, b, sw);
+  if (st) return st;
+  cudaSetDevice(ctx->device);
+  Layout Lo = layout(g->nx, g->ny, g->nz);
+  // Admission by the HBM budget (pooled allocations of a retired run count as free).
+  char* mem = nullptr;
+  auto pit = ctx->pool.find(Lo.total);
+  if (pit != ctx->pool.end()) { mem = pit->second; ctx->pool.erase(pit); ctx->pooled -= Lo.total; }
+  else {
+    while (ctx->used + ctx->pooled + Lo.total > ctx->budget && !ctx->pool.empty()) {
+      auto last = std::prev(ctx->pool.end()); cudaFree(last->second); ctx->pooled -= last->first; ctx->pool.erase(last);
+    }
+    if (ctx->used + Lo.total > ctx->budget) return fail(ctx, SG_ERR_BUDGET, "run needs " + std::to_string(Lo.total) + " bytes beyond the HBM budget");
+    cudaError_t e = cudaMalloc(&mem, Lo.total);
+    if (e != cudaSuccess) { cudaGetLastError(); return fail(ctx, SG_ERR_BUDGET, std::string("cudaMalloc: ") + cudaGetErrorString(e)); }
+  }
+  ctx->used += Lo.total;
+  int slot;
+  if (!ctx->freeSlots.empty()) { slot = ctx->freeSlots.back(); ctx->freeSlots.pop_back(); }
+  else {
+    slot = (int)ctx->runs.size();
+    if (slot >= MAX_SLOTS) { cudaFree(mem); ctx->used -= Lo.total; return fail(ctx, SG_ERR_BUDGET, "too many runs"); }
+    ctx->runs.emplace_back();
+  }
+  Run& r = ctx->runs[slot];
+  r.live = true; r.slot = slot; r.nx = g->nx; r.ny = g->ny; r.nz = g->nz; r.bytes = Lo.total; r.mem = mem;
+  HostTables T; RunDesc& d = r.desc; d = RunDesc{};
+  build_tables(g, b, sw, T, d);
+  d.slot = slot;
+  d.fld = (float*)(mem + Lo.fld); d.faces = (float*)(mem + Lo.faces); d.kmkh = (float*)(mem + Lo.kmkh); d.phi = (float*)(mem + Lo.phi);
+  d.pres = (float*)(mem + Lo.pres); d.spec = (float2*)(mem + Lo.spec); d.cols = (float*)(mem + Lo.cols);
+  d.lv = (const float*)(mem + Lo.lv); d.lv64 = (const double*)(mem + Lo.lv64); d.tri_face = (const double2*)(mem + Lo.triF);
+  d.tri_pres = (const double2*)(mem + Lo.triP); d.ab = (const double2*)(mem + Lo.ab); d.twx = (const float2*)(mem + Lo.twx);
+  d.twy = (const float2*)(mem + Lo.twy); d.scr = (float*)(mem + Lo.scr); d.part = (double*)(mem + Lo.part); d.acc = (double*)(mem + Lo.acc);
+  d.cnt = (unsigned long long*)(mem + Lo.cnt);
+  auto H2D = [&](size_t off, const void* src, size_t bytes) { return cudaMemcpyAsync(mem + off, src, bytes, cudaMemcpyHostToDevice, ctx->stream); };
+  CK(cudaMemsetAsync(mem, 0, Lo.total, ctx->stream));
+  CK(H2D(Lo.lv, T.lv.data(), T.lv.size() * 4)); CK(H2D(Lo.lv64, T.lv64.data(), T.lv64.size() * 8));
+  CK(H2D(Lo.triF, T.triF.data(), T.triF.size() * 16)); CK(H2D(Lo.triP, T.triP.data(), T.triP.size() * 16));
+  CK(H2D(Lo.ab, T.ab.data(), T.ab.size() * 16)); CK(H2D(Lo.twx, T.twx.data(), T.twx.size() * 8)); CK(H2D(Lo.twy, T.twy.data(), T.twy.size() * 8));
+  CK(cudaMemcpyAsync(ctx->d_runs + slot, &d, sizeof(RunDesc), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  *out = slot;
+  if (init) {
+    int s2 = sg_run_write_fields(ctx, slot, SG_ALL_FIELDS, init);
+    if (s2) { sg_run_retire(ctx, slot); return s2; }
+  }
+  return SG_OK;
+}
+
+int sg_run_write_fields(sg_context* ctx, sg_run run, uint32_t mask, const float* const* host) {
+  if (!ctx || !host) return SG_ERR_INVALID;
+  Run* r = find(ctx, run);
+  if (!r) return fail(ctx, SG_ERR_NOT_FOUND, "no run " + std::to_string(run));
+  cudaSetDevice(ctx->device);
+  size_t n = (size_t)r->nx * r->ny * r->nz;
+  for (int f = 0; f < NF; f++) {
+    if (!(mask & (1u << f))) continue;
+    if (!host[f]) return fail(ctx, SG_ERR_INVALID, "null field pointer");
+    // theta arrives full; it is staged in set B and converted to its departure in set A.
+    float* dst = r->desc.fld + (size_t)(f == THETA ? NF + THETA : f) * n;
+    CK(cudaMemcpyAsync(dst, host[f], n * 4, cudaMemcpyHostToDevice, ctx->stream));
+  }
+  if (mask & (1u << THETA)) {
+    int st; Plan* P = single_plan(ctx, run, &st);
+    if (!P) return st;
+    launch_theta_in(lx(ctx, *P, FAM_NODE), r->desc.fld + (size_t)(NF + THETA) * n);
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  return SG_OK;
+}
+
+int sg_run_read_fields(sg_context* ctx, sg_run run, uint32_t mask, float* const* host) {
+  if (!ctx || !host) return SG_ERR_INVALID;
+  Run* r = find(ctx, run);
+  if (!r) return fail(ctx, SG_ERR_NOT_FOUND, "no run " + std::to_string(run));
+  cudaSetDevice(ctx->device);
+  size_t n = (size_t)r->nx * r->ny * r->nz;
+  if (mask & (1u << THETA)) {
+    int st; Plan* P = single_plan(ctx, run, &st);
+    if (!P) return st;
+    launch_theta_out(lx(ctx, *P, FAM_NODE), r->desc.fld + (size_t)(NF + THETA) * n);
+  }
+  for (int f = 0; f < NF; f++) {
+    if (!(mask & (1u << f))) continue;
+    if (!host[f]) return fail(ctx, SG_ERR_INVALID, "null field pointer");
+    const float* src = r->desc.fld + (size_t)(f == THETA ? NF + THETA : f) * n;
+    CK(cudaMemcpyAsync(host[f], src, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  return SG_OK;
+}
+
+int sg_run_read_columns(sg_context* ctx, sg_run run, float* precipitation, float* hail_ground, float* hail_size) {
+  if (!ctx) return SG_ERR_INVALID;
+  Run* r = find(ctx, run);
+  if (!r) return fail(ctx, SG_ERR_NOT_FOUND, "no run " + std::to_string(run));
+  size_t layer = (size_t)r->nx * r->ny;
+  float* dst[3] = {precipitation, hail_ground, hail_size};
+  for (int k = 0; k < 3; k++) if (dst[k]) CK(cudaMemcpyAsync(dst[k], r->desc.cols + k * layer, layer * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return SG_OK;
+}
+
+int sg_run_read_pressure(sg_context* ctx, sg_run run, double* p) {
+  if (!ctx || !p) return SG_ERR_INVALID;
+  Run* r = find(ctx, run);
+  if (!r) return fail(ctx, SG_ERR_NOT_FOUND, "no run " + std::to_string(run));
+  size_t cells = (size_t)r->nx * r->ny * (r->nz - 1);
+  std::vector<float> tmp(cells);
+  CK(cudaMemcpyAsync(tmp.data(), r->desc.pres, cells * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (size_t i = 0; i < cells; i++) p[i] = tmp[i];
+  return SG_OK;
+}
+
+int sg_run_status(sg_context* ctx, sg_run run, sg_run_counters* out) {
+  if (!ctx || !out) return SG_ERR_INVALID;
+  Run* r = find(ctx, run);
+  if (!r) return fail(ctx, SG_ERR_NOT_FOUND, "no run " + std::to_string(run));
+  double acc[A_COUNT]; unsigned long long cnt[C_COUNT];
+  CK(cudaMemcpyAsync(acc, r->desc.acc, sizeof(acc), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(cnt, r->desc.cnt, sizeof(cnt), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  out->steps = (int64_t)cnt[C_STEPS]; out->clipped = (int64_t)cnt[C_CLIPPED]; out->failed = cnt[C_FAILED] ? 1 : 0; out->reserved = 0;
+  out->negative_filled = acc[A_NEG]; out->water_condensed = acc[A_WATER]; out->water_evaporated = acc[A_WATER + 1];
+  out->water_rain_evaporated = acc[A_WATER + 2]; out->water_surface = 0;
+  return out->failed ? SG_ERR_NONFINITE : SG_OK;
+}
+
+int sg_run_retire(sg_context* ctx, sg_run run) {
+  if (!ctx) return SG_ERR_INVALID;
+  Run* r = find(ctx, run);
+  if (!r) return fail(ctx, SG_ERR_NOT_FOUND, "no run " + std::to_string(run));
+  cudaStreamSynchronize(ctx->stream);
+  drop_plans_with(ctx, run);
+  ctx->used -= r->bytes;
+  ctx->pool.emplace(r->bytes, r->mem); ctx->pooled += r->bytes;
+  r->live = false; r->mem = nullptr;
+  ctx->freeSlots.push_back(run);
+  return SG_OK;
+}
+
+int sg_run_step(sg_context* ctx, sg_run run, int nsteps) { return sg_batch_step(ctx, &run, 1, nsteps); }
+
+int sg_batch_step(sg_context* ctx, const sg_run* runs, int n, int nsteps) {
+  if (!ctx) return SG_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  return batch_step(ctx, runs, n, nsteps, true);
+}
+int sg_batch_step_async(sg_context* ctx, const sg_run* runs, int n, int nsteps) {
+  if (!ctx) return SG_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  return batch_step(ctx, runs, n, nsteps, false);
+}
+int sg_synchronize(sg_context* ctx) {
+  if (!ctx) return SG_ERR_INVALID;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return SG_OK;
+}
+
+int sg_time_steps(sg_context* ctx, const sg_run* runs, int n, int nsteps, int use_graph, double* ms) {
+  if (!ctx || !ms || nsteps < 1) return SG_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  std::vector<int> slots;
+  int st = slots_of(ctx, runs, n, slots);
+  if (st) return st;
+  Plan* P = get_plan(ctx, slots, &st);
+  if (!P) return st;
+  if (use_graph && (st = ensure_graph(ctx, *P))) return st;
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a)); CK(cudaEventCreate(&b));
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaEventRecord(a, ctx->stream));
+  for (int s = 0; s < nsteps; s++) {
+    if (use_graph) CK(cudaGraphLaunch(P->exec, ctx->stream));
+    else enqueue_step(ctx, *P, [](int) {});
+  }
+  CK(cudaEventRecord(b, ctx->stream));
+  CK(cudaEventSynchronize(b));
+  float t = 0; CK(cudaEventElapsedTime(&t, a, b));
+  cudaEventDestroy(a); cudaEventDestroy(b);
+  CK(cudaGetLastError());
+  *ms = t;
+  return SG_OK;
+}
+
+int sg_profile_kernels(sg_context* ctx, const sg_run* runs, int n, int nsteps, const char** names, double* ms, int64_t* launches, int cap) {
+  if (!ctx || !names || !ms || !launches) return SG_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  std::vector<int> slots;
+  int st = slots_of(ctx, runs, n, slots);
+  if (st) return -st;
+  Plan* P = get_plan(ctx, slots, &st);
+  if (!P) return -st;
+  const int K = 18;
+  std::vector<double> total(K, 0); std::vector<int64_t> count(K, 0);
+  cudaEvent_t ev[64];
+  for (int e = 0; e < 64; e++) cudaEventCreate(&ev[e]);
+  for (int s = 0; s < nsteps; s++) {
+    int k = 0; int which[64];
+    cudaEventRecord(ev[k++], ctx->stream);
+    enqueue_step(ctx, *P, [&](int id) { which[k] = id; cudaEventRecord(ev[k++], ctx->stream); });
+    cudaStreamSynchronize(ctx->stream);
+    for (int e = 1; e < k; e++) { float t; cudaEventElapsedTime(&t, ev[e - 1], ev[e]); total[which[e]] += t; count[which[e]]++; }
+  }
+  for (int e = 0; e < 64; e++) cudaEventDestroy(ev[e]);
+  if (cudaGetLastError() != cudaSuccess) return -SG_ERR_DEVICE;
+  int w = 0;
+  for (int k = 0; k < K && w < cap; k++) if (count[k]) { names[w] = KERNEL_NAMES[k]; ms[w] = total[k] / count[k]; launches[w] = count[k]; w++; }
+  return w;
+}
+
+int sg_run_divergence(sg_context* ctx, sg_run run, double* max_abs_div) {
+  if (!ctx || !max_abs_div) return SG_ERR_INVALID;
+  Run* r = find(ctx, run);
+  if (!r) return fail(ctx, SG_ERR_NOT_FOUND, "no run " + std::to_string(run));
+  int st; Plan* P = single_plan(ctx, run, &st);
+  if (!P) return st;
+  CK(cudaMemsetAsync(ctx->d_scalar, 0, 8, ctx->stream));
+  launch_divergence_max(lx(ctx, *P, FAM_CELLS), 0, ctx->d_scalar);
+  CK(cudaMemcpyAsync(max_abs_div, ctx->d_scalar, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return SG_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ diagnostics
+extern "C" {
+int sg_debug_step_part(sg_context* ctx, sg_run run, int part) {
+  if (!ctx || part < 1 || part > 5) return SG_ERR_INVALID;
+  if (!find(ctx, run)) return fail(ctx, SG_ERR_NOT_FOUND, "no run");
+  int st; Plan* P = single_plan(ctx, run, &st);
+  if (!P) return st;
+  enqueue_part(ctx, *P, part, [](int) {});
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaGetLastError());
+  return SG_OK;
+}
+int sg_debug_read_set(sg_context* ctx, sg_run run, int set, int field, float* host) {
+  if (!ctx || !host || set < 0 || set > 2 || field < 0 || field >= NF) return SG_ERR_INVALID;
+  Run* r = find(ctx, run);
+  if (!r) return fail(ctx, SG_ERR_NOT_FOUND, "no run");
+  size_t n = (size_t)r->nx * r->ny * r->nz;
+  CK(cudaMemcpyAsync(host, r->desc.fld + ((size_t)set * NF + field) * n, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return SG_OK;
+}
+int sg_debug_read_faces(sg_context* ctx, sg_run run, float* faces4) {
+  if (!ctx || !faces4) return SG_ERR_INVALID;
+  Run* r = find(ctx, run);
+  if (!r) return fail(ctx, SG_ERR_NOT_FOUND, "no run");
+  size_t n = (size_t)r->nx * r->ny * r->nz;
+  CK(cudaMemcpyAsync(faces4, r->desc.faces, 4 * n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return SG_OK;
+}
+}  // extern "C"
+
+// ==================================================================== serving
+namespace {
+struct Request {
+  sg_grid grid; std::vector<double> zs, dzs, hz;
+  std::vector<double> base[7]; sg_switches sw;
+  std::vector<std::vector<float>> init;
+  int64_t steps, tag;
+};
+struct Active { sg_run run; int64_t left, tag; };
+}  // namespace
+
+struct sg_server {
+  sg_context* ctx;
+  int maxActive;
+  std::deque<Request> queue;
+  std::vector<Active> active;
+  std::map<int64_t, sg_run> finished;  // done, resident until collected
+};
+
+extern "C" {
+
+int sg_server_create(sg_context* ctx, int max_active, sg_server** out) {
+  if (!ctx || !out || max_active < 1) return SG_ERR_INVALID;
+  *out = new sg_server{ctx, max_active, {}, {}};
+  return SG_OK;
+}
+
+int sg_server_destroy(sg_server* srv) {
+  if (!srv) return SG_ERR_INVALID;
+  for (auto& a : srv->active) sg_run_retire(srv->ctx, a.run);
+  for (auto& f : srv->finished) sg_run_retire(srv->ctx, f.second);
+  delete srv;
+  return SG_OK;
+}
+
+int sg_server_submit(sg_server* srv, const sg_grid* grid, const sg_base_state* base, const sg_switches* sw, const float* const* init, int64_t steps, int64_t tag) {
+  if (!srv || !grid || !base || !sw || !init || steps < 1) return SG_ERR_INVALID;
+  int st = validate(srv->ctx, grid, base, sw);
+  if (st) return st;
+  Request r; r.grid = *grid; int nz = grid->nz;
+  r.zs.assign(grid->zs, grid->zs + nz); r.dzs.assign(grid->dzs, grid->dzs + nz - 1); r.hz.assign(grid->hz, grid->hz + nz);
+  const double* src[7] = {base->p, base->exner, base->theta, base->q, base->u, base->v, base->rho};
+  for (int k = 0; k < 7; k++) r.base[k].assign(src[k], src[k] + nz);
+  r.sw = *sw;
+  size_t n = (size_t)grid->nx * grid->ny * nz;
+  r.init.resize(NF);
+  for (int f = 0; f < NF; f++) r.init[f].assign(init[f], init[f] + n);
+  r.steps = steps; r.tag = tag;
+  srv->queue.push_back(std::move(r));
+  return SG_OK;
+}
+
+int sg_server_iterate(sg_server* srv, int64_t* done_tags, int* done_count, int cap, int* active, int* queued) {
+  if (!srv) return SG_ERR_INVALID;
+  sg_context* ctx = srv->ctx;
+  // Admit in arrival order while slots and HBM allow.
+  while (!srv->queue.empty() && (int)srv->active.size() < srv->maxActive) {
+    Request& q = srv->queue.front();
+    q.grid.zs = q.zs.data(); q.grid.dzs = q.dzs.data(); q.grid.hz = q.hz.data();
+    sg_base_state b{q.base[0].data(), q.base[1].data(), q.base[2].data(), q.base[3].data(), q.base[4].data(), q.base[5].data(), q.base[6].data()};
+    std::vector<const float*> init(NF);
+    for (int f = 0; f < NF; f++) init[f] = q.init[f].data();
+    sg_run run;
+    int st = sg_run_create(ctx, &q.grid, &b, &q.sw, init.data(), &run);
+    if (st == SG_ERR_BUDGET) break;  // wait for a retirement
+    if (st) return st;
+    srv->active.push_back(Active{run, q.steps, q.tag});
+    srv->queue.pop_front();
+  }
+  int done = 0;
+  if (!srv->active.empty()) {
+    std::vector<sg_run> ids;
+    for (auto& a : srv->active) ids.push_back(a.run);
+    int st = sg_batch_step(ctx, ids.data(), (int)ids.size(), 1);
+    if (st) return st;
+    std::vector<Active> keep;
+    for (auto& a : srv->active) {
+      if (--a.left > 0) { keep.push_back(a); continue; }
+      if (done < cap && done_tags) done_tags[done] = a.tag;
+      done++;
+      srv->finished[a.tag] = a.run;
+    }
+    srv->active.swap(keep);
+  }
+  if (done_count) *done_count = std::min(done, cap);
+  if (active) *active = (int)srv->active.size();
+  if (queued) *queued = (int)srv->queue.size();
+  return SG_OK;
+}
+
+
+int sg_server_collect(sg_server* srv, int64_t tag, uint32_t mask, float* const* host, float* precipitation) {
+  if (!srv) return SG_ERR_INVALID;
+  auto it = srv->finished.find(tag);
+  if (it == srv->finished.end()) return fail(srv->ctx, SG_ERR_NOT_FOUND, "no finished run with tag " + std::to_string(tag));
+  int st = SG_OK;
+  if (mask && host) st = sg_run_read_fields(srv->ctx, it->second, mask, host);
+  if (!st && precipitation) st = sg_run_read_columns(srv->ctx, it->second, precipitation, nullptr, nullptr);
+  if (st) return st;
+  sg_run_retire(srv->ctx, it->second);
+  srv->finished.erase(it);
+  return SG_OK;
+}
+}  // extern "C"

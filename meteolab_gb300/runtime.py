@@ -1,0 +1,337 @@
+"""Python host side over the C ABI of libstormgpu.so (include/stormgpu.h).
+
+Mirrors the reference's interface for the step: ``AtmosphereModel(config, grid, profile)`` with ``step(dt)`` and the
+model's fields as arrays (src/core/model.ts:183-210, :329, :873), here backed by a device-resident run. There is no
+CPU fallback: without the built library or a CUDA device every call raises ``StormGpuError``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+from typing import Dict, Iterable, List, Optional, Sequence
+
+import numpy as np
+
+from .scenarios import CARRIED, RunSpec
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libstormgpu.so")
+
+STATUS = {0: "ok", 1: "invalid", 2: "budget", 3: "device", 4: "timeout", 5: "non-finite", 6: "not found", 7: "unsupported"}
+
+
+class StormGpuError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"stormgpu {STATUS.get(code, code)}: {message}")
+        self.code = code
+
+
+class SgGrid(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("reserved", C.c_int32),
+                ("dx", C.c_double), ("dy", C.c_double), ("height", C.c_double),
+                ("zs", C.POINTER(C.c_double)), ("dzs", C.POINTER(C.c_double)), ("hz", C.POINTER(C.c_double))]
+
+
+class SgBase(C.Structure):
+    _fields_ = [(k, C.POINTER(C.c_double)) for k in ("p", "exner", "theta", "q", "u", "v", "rho")]
+
+
+class SgSwitches(C.Structure):
+    _fields_ = [("dt", C.c_double), ("coriolis", C.c_double), ("wind_relaxation", C.c_double), ("sponge_rate", C.c_double),
+                ("sponge_start", C.c_double), ("cs", C.c_double), ("drag_cd", C.c_double), ("frame_u", C.c_double),
+                ("frame_v", C.c_double)] + [(k, C.c_int32) for k in ("loading", "evaporation", "rain_formation",
+                                                                         "anisotropic", "vertical_dz", "durran_klemp",
+                                                                         "pressure_in_stages", "ice")]
+
+
+class SgCounters(C.Structure):
+    _fields_ = [("steps", C.c_int64), ("clipped", C.c_int64), ("negative_filled", C.c_double),
+                ("water_condensed", C.c_double), ("water_evaporated", C.c_double), ("water_rain_evaporated", C.c_double),
+                ("water_surface", C.c_double), ("failed", C.c_int32), ("reserved", C.c_int32)]
+
+
+_lib = None
+_lock = threading.Lock()
+_FP = C.POINTER(C.c_float)
+
+
+def load():
+    """Load the in-tree libstormgpu.so (build it first with meteolab_gb300.build.build())."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise StormGpuError(3, f"{LIB_PATH} is not built; run meteolab_gb300.build.build()")
+            L = C.CDLL(LIB_PATH)
+            vp, i32, u64, i64 = C.c_void_p, C.c_int, C.c_uint64, C.c_int64
+            L.sg_context_create.argtypes = [i32, u64, C.POINTER(vp)]
+            L.sg_context_destroy.argtypes = [vp]
+            L.sg_last_error.restype = C.c_char_p
+            L.sg_last_error.argtypes = [vp]
+            L.sg_run_bytes.restype = u64
+            L.sg_run_bytes.argtypes = [C.POINTER(SgGrid)]
+            L.sg_run_create.argtypes = [vp, C.POINTER(SgGrid), C.POINTER(SgBase), C.POINTER(SgSwitches), C.POINTER(_FP), C.POINTER(C.c_int32)]
+            L.sg_run_write_fields.argtypes = [vp, C.c_int32, C.c_uint32, C.POINTER(_FP)]
+            L.sg_run_read_fields.argtypes = [vp, C.c_int32, C.c_uint32, C.POINTER(_FP)]
+            L.sg_run_read_columns.argtypes = [vp, C.c_int32, _FP, _FP, _FP]
+            L.sg_run_read_pressure.argtypes = [vp, C.c_int32, C.POINTER(C.c_double)]
+            L.sg_run_status.argtypes = [vp, C.c_int32, C.POINTER(SgCounters)]
+            L.sg_run_retire.argtypes = [vp, C.c_int32]
+            L.sg_run_step.argtypes = [vp, C.c_int32, i32]
+            L.sg_batch_step.argtypes = [vp, C.POINTER(C.c_int32), i32, i32]
+            L.sg_batch_step_async.argtypes = [vp, C.POINTER(C.c_int32), i32, i32]
+            L.sg_synchronize.argtypes = [vp]
+            L.sg_profile_kernels.argtypes = [vp, C.POINTER(C.c_int32), i32, i32, C.POINTER(C.c_char_p), C.POINTER(C.c_double),
+                                             C.POINTER(C.c_int64), i32]
+            L.sg_run_divergence.argtypes = [vp, C.c_int32, C.POINTER(C.c_double)]
+            L.sg_time_steps.argtypes = [vp, C.POINTER(C.c_int32), i32, i32, i32, C.POINTER(C.c_double)]
+            L.sg_debug_step_part.argtypes = [vp, C.c_int32, i32]
+            L.sg_debug_read_set.argtypes = [vp, C.c_int32, i32, i32, _FP]
+            L.sg_debug_read_faces.argtypes = [vp, C.c_int32, _FP]
+            L.sg_server_create.argtypes = [vp, i32, C.POINTER(vp)]
+            L.sg_server_destroy.argtypes = [vp]
+            L.sg_server_submit.argtypes = [vp, C.POINTER(SgGrid), C.POINTER(SgBase), C.POINTER(SgSwitches), C.POINTER(_FP), i64, i64]
+            L.sg_server_iterate.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int), i32, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+            L.sg_server_collect.argtypes = [vp, i64, C.c_uint32, C.POINTER(_FP), _FP]
+            _lib = L
+    return _lib
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class _Packed:
+    """The C structs of one run spec with the arrays they point to kept alive."""
+
+    def __init__(self, spec: RunSpec):
+        g, env, sw = spec.grid, spec.env, spec.switches
+        self.keep = [_f64(g.zs), _f64(g.dzs), _f64(g.hz)] + [_f64(getattr(env, k)) for k in ("p", "exner", "theta", "q", "u", "v", "rho")]
+        dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+        self.grid = SgGrid(g.nx, g.ny, g.nz, 0, g.dx, g.dy, g.height, dp(self.keep[0]), dp(self.keep[1]), dp(self.keep[2]))
+        self.base = SgBase(*[dp(a) for a in self.keep[3:]])
+        self.switches = SgSwitches(sw.dt, sw.coriolis, sw.wind_relaxation, sw.sponge_rate, sw.sponge_start, sw.cs, sw.drag_cd(g),
+                                   sw.frame_u, sw.frame_v, sw.loading, sw.evaporation, sw.rain_formation, sw.anisotropic,
+                                   sw.vertical_dz, sw.durran_klemp, sw.pressure_in_stages, 1)
+        self.fields = [np.ascontiguousarray(spec.fields[k], dtype=np.float32).ravel() for k in CARRIED]
+        self.ptrs = (_FP * len(CARRIED))(*[a.ctypes.data_as(_FP) for a in self.fields])
+
+
+class Context:
+    """One device context (one CUDA stream, an HBM budget, the runs it owns)."""
+
+    def __init__(self, device: int = 0, hbm_budget: int = 0):
+        L = load()
+        h = C.c_void_p()
+        rc = L.sg_context_create(device, hbm_budget, C.byref(h))
+        if rc:
+            raise StormGpuError(rc, "sg_context_create failed (is a CUDA device visible?)")
+        self.h = h
+
+    def check(self, rc: int, what: str = ""):
+        if rc:
+            raise StormGpuError(rc, f"{what}: {load().sg_last_error(self.h).decode()}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().sg_context_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def create(self, spec: RunSpec) -> "Run":
+        return Run(self, spec)
+
+    def batch_step(self, runs: Sequence["Run"], steps: int = 1, wait: bool = True):
+        ids = (C.c_int32 * len(runs))(*[r.id for r in runs])
+        fn = load().sg_batch_step if wait else load().sg_batch_step_async
+        self.check(fn(self.h, ids, len(runs), steps), "batch step")
+        for r in runs:
+            r.time += steps * r.spec.switches.dt
+
+    def time_steps(self, runs: Sequence["Run"], steps: int, graph: bool = True) -> float:
+        """Device time (ms, CUDA events on the library's stream) of `steps` batch steps."""
+        ids = (C.c_int32 * len(runs))(*[r.id for r in runs])
+        ms = C.c_double()
+        self.check(load().sg_time_steps(self.h, ids, len(runs), steps, 1 if graph else 0, C.byref(ms)), "time steps")
+        for r in runs:
+            r.time += steps * r.spec.switches.dt
+        return ms.value
+
+    def synchronize(self):
+        self.check(load().sg_synchronize(self.h), "synchronize")
+
+    def profile(self, runs: Sequence["Run"], steps: int = 2) -> Dict[str, tuple]:
+        """Mean device ms per launch of each kernel class over `steps` eager steps."""
+        ids = (C.c_int32 * len(runs))(*[r.id for r in runs])
+        cap = 32
+        names = (C.c_char_p * cap)()
+        ms = (C.c_double * cap)()
+        launches = (C.c_int64 * cap)()
+        n = load().sg_profile_kernels(self.h, ids, len(runs), steps, names, ms, launches, cap)
+        if n < 0:
+            self.check(-n, "profile")
+        return {names[k].decode(): (ms[k], launches[k] // max(1, steps)) for k in range(n)}
+
+
+class Run:
+    """A device-resident run (the state of one model)."""
+
+    def __init__(self, ctx: Context, spec: RunSpec):
+        self.ctx, self.spec, self.grid = ctx, spec, spec.grid
+        packed = _Packed(spec)
+        rid = C.c_int32()
+        ctx.check(load().sg_run_create(ctx.h, C.byref(packed.grid), C.byref(packed.base), C.byref(packed.switches), packed.ptrs,
+                                       C.byref(rid)), "run create")
+        self.id = rid.value
+        self.time = 0.0
+        self.live = True
+
+    def retire(self):
+        if self.live:
+            self.ctx.check(load().sg_run_retire(self.ctx.h, self.id), "retire")
+            self.live = False
+
+    def step(self, steps: int = 1):
+        self.ctx.check(load().sg_run_step(self.ctx.h, self.id, steps), "step")
+        self.time += steps * self.spec.switches.dt
+
+    def read(self, names: Iterable[str] = CARRIED, out: Optional[Dict[str, np.ndarray]] = None) -> Dict[str, np.ndarray]:
+        names = list(names)
+        out = out if out is not None else {k: np.empty(self.grid.n, np.float32) for k in names}
+        mask = 0
+        ptrs = (_FP * len(CARRIED))()
+        for k in names:
+            j = CARRIED.index(k)
+            mask |= 1 << j
+            ptrs[j] = out[k].ctypes.data_as(_FP)
+        self.ctx.check(load().sg_run_read_fields(self.ctx.h, self.id, mask, ptrs), "read fields")
+        return out
+
+    def write(self, fields: Dict[str, np.ndarray]):
+        mask = 0
+        ptrs = (_FP * len(CARRIED))()
+        keep = []
+        for k, a in fields.items():
+            j = CARRIED.index(k)
+            a = np.ascontiguousarray(a, dtype=np.float32).ravel()
+            keep.append(a)
+            mask |= 1 << j
+            ptrs[j] = a.ctypes.data_as(_FP)
+        self.ctx.check(load().sg_run_write_fields(self.ctx.h, self.id, mask, ptrs), "write fields")
+
+    def columns(self) -> Dict[str, np.ndarray]:
+        layer = self.grid.layer
+        out = {k: np.empty(layer, np.float32) for k in ("precipitation", "hailGround", "hailSize")}
+        self.ctx.check(load().sg_run_read_columns(self.ctx.h, self.id, *[out[k].ctypes.data_as(_FP) for k in ("precipitation", "hailGround", "hailSize")]),
+                       "read columns")
+        return out
+
+    def pressure(self) -> np.ndarray:
+        out = np.empty(self.grid.nx * self.grid.ny * (self.grid.nz - 1))
+        self.ctx.check(load().sg_run_read_pressure(self.ctx.h, self.id, out.ctypes.data_as(C.POINTER(C.c_double))), "read pressure")
+        return out
+
+    def status(self) -> dict:
+        c = SgCounters()
+        rc = load().sg_run_status(self.ctx.h, self.id, C.byref(c))
+        if rc not in (0, 5):
+            self.ctx.check(rc, "status")
+        return {k: getattr(c, k) for k, _ in SgCounters._fields_ if k != "reserved"}
+
+    def debug_part(self, part: int):
+        """Run one part of the step (1 beginStep, 2 dynamics, 3 physicsStep, 4 mixStep, 5 final projection)."""
+        self.ctx.check(load().sg_debug_step_part(self.ctx.h, self.id, part), f"step part {part}")
+
+    def debug_read_set(self, set_: int, name: str) -> np.ndarray:
+        """A raw device buffer (theta of a set is its departure from the base profile)."""
+        out = np.empty(self.grid.n, np.float32)
+        self.ctx.check(load().sg_debug_read_set(self.ctx.h, self.id, set_, CARRIED.index(name), out.ctypes.data_as(_FP)), "read set")
+        return out
+
+    def debug_faces(self) -> np.ndarray:
+        out = np.empty((4, self.grid.n), np.float32)
+        self.ctx.check(load().sg_debug_read_faces(self.ctx.h, self.id, out.ctypes.data_as(_FP)), "read faces")
+        return out
+
+    def divergence(self) -> float:
+        out = C.c_double()
+        self.ctx.check(load().sg_run_divergence(self.ctx.h, self.id, C.byref(out)), "divergence")
+        return out.value
+
+
+class AtmosphereModel:
+    """The reference's model interface (src/core/model.ts:183-210, :873) over one device run: ``step(dt)`` advances
+    by one model step and moves ``time`` (the reference's callers add dt themselves, src/core/fixtures.ts:28-30);
+    the fields read back as FP32 arrays in node order."""
+
+    def __init__(self, spec: RunSpec, context: Optional[Context] = None):
+        self.context = context or Context()
+        self.spec, self.grid, self.env = spec, spec.grid, spec.env
+        self.run = self.context.create(spec)
+        self.time = 0.0
+
+    def step(self, dt: Optional[float] = None):
+        if dt is not None and abs(dt - self.spec.switches.dt) > 1e-12:
+            raise StormGpuError(1, f"the run was set up for dt = {self.spec.switches.dt}")
+        self.run.step(1)
+        self.time += self.spec.switches.dt
+
+    def __getattr__(self, name):
+        if name in CARRIED:
+            return self.run.read([name])[name]
+        if name in ("precipitation", "hailGround", "hailSize"):
+            return self.run.columns()[name]
+        if name == "pressure":
+            return self.run.pressure()
+        raise AttributeError(name)
+
+    @property
+    def clipped(self) -> int:
+        return self.run.status()["clipped"]
+
+    @property
+    def negativeFilled(self) -> float:
+        return self.run.status()["negative_filled"]
+
+
+class Server:
+    """The serving loop (sg_server_*): submit requests, iterate; each iteration admits by HBM budget, advances every
+    active run one step in one batch and retires finished runs."""
+
+    def __init__(self, ctx: Context, max_active: int = 256):
+        h = C.c_void_p()
+        ctx.check(load().sg_server_create(ctx.h, max_active, C.byref(h)), "server create")
+        self.ctx, self.h = ctx, h
+
+    def submit(self, spec: RunSpec, steps: int, tag: int):
+        p = _Packed(spec)
+        self.ctx.check(load().sg_server_submit(self.h, C.byref(p.grid), C.byref(p.base), C.byref(p.switches), p.ptrs, steps, tag), "submit")
+
+    def iterate(self, cap: int = 1024):
+        tags = (C.c_int64 * cap)()
+        done, active, queued = C.c_int(), C.c_int(), C.c_int()
+        self.ctx.check(load().sg_server_iterate(self.h, tags, C.byref(done), cap, C.byref(active), C.byref(queued)), "iterate")
+        return [tags[k] for k in range(done.value)], active.value, queued.value
+
+    def collect(self, tag: int, n: int, names: Iterable[str] = CARRIED) -> Dict[str, np.ndarray]:
+        """Read a finished run's fields (n nodes each) and retire it."""
+        names = list(names)
+        out = {k: np.empty(n, np.float32) for k in names}
+        ptrs = (_FP * len(CARRIED))()
+        mask = 0
+        for k in names:
+            mask |= 1 << CARRIED.index(k)
+            ptrs[CARRIED.index(k)] = out[k].ctypes.data_as(_FP)
+        self.ctx.check(load().sg_server_collect(self.h, tag, mask, ptrs, None), "collect")
+        return out
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().sg_server_destroy(self.h)
+            self.h = None

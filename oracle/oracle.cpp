@@ -136,6 +136,14 @@ double orc_cell(int which, float* v, double exner, double p, double rho, double 
   return NAN;
 }
 
+// The per-node microphysics sequence of physics(z) on float32 cells: v = [theta, q, cloud, rain, ice, iceNumber,
+// snow, graupel, hail, cold]; flags bit 0 ice, bit 1 evaporation, bit 2 rain formation. Returns the evaporated rain.
+double orc_microphysics(float* v, double exner, double p, double rho, double rhoGround, double dt, int flags) {
+  Switches sw; sw.ice = flags & 1; sw.evaporation = (flags & 2) != 0; sw.rainFormation = (flags & 4) != 0;
+  Arr<float> a = (Arr<float>)v;
+  return microphysicsNode<float>(a, a + 1, a + 2, a + 3, a + 9, a + 4, a + 5, a + 6, a + 7, a + 8, 0, exner, p, rho, rhoGround, dt, sw);
+}
+
 // FFT of length n in place (sign -1 forward, +1 unnormalised inverse).
 void orc_fft(int n, double* re, double* im, int sign) { FFT f(n); f.transform(re, im, sign); }
 // HorizontalDFT forward of `layers` layers of src; spectra into re/im (nx*ny*layers); then inverse into out.

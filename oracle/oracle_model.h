@@ -20,6 +20,39 @@ struct Switches {
 
 enum FieldId { F_RAIN, F_SNOW, F_GRAUPEL, F_HAIL, F_U, F_V, F_W, F_THETA, F_Q, F_CLOUD, F_ICE, F_ICENUMBER, F_COLD, N_CARRIED };
 
+// The microphysics part of physics(z) for node i (src/core/model.ts:1391-1471): Kessler rain, then with ice the
+// freezing, crystals, snow, graupel, hail, secondary ice and the mixed-phase saturation adjustment, else the warm
+// adjustment; the cold-pool indicator's share of the cooling. Returns the evaporated rain.
+template <class S>
+double microphysicsNode(Arr<S> theta, Arr<S> q, Arr<S> cloud, Arr<S> rain, Arr<S> cold, Arr<S> ice, Arr<S> iceNumber, Arr<S> snow, Arr<S> graupel,
+                        Arr<S> hail, int i, double ex, double pz, double rhoZ, double rhoGround, double dt, const Switches& sw) {
+  double evap = !sw.rainFormation ? 0 : rainProcesses<S>(q, cloud, rain, i, (double)theta[i] * ex, pz, rhoZ, dt, sw.evaporation);
+  if (evap > 0) { double cool = LV / CP / ex * evap; theta[i] -= cool; cold[i] += cool; }
+  double cond;
+  if (sw.ice) {
+    freezeRain<S>(theta, rain, graupel, i, ex);
+    settleCrystals<S>(ice, iceNumber, i);
+    cold[i] += iceProcesses<S>(theta, q, ice, snow, iceNumber, i, ex, pz, rhoZ, dt);
+    double iceBefore = ice[i], cloudBefore = cloud[i];
+    cold[i] += snowProcesses<S>(theta, q, cloud, ice, snow, rain, i, ex, pz, rhoZ, rhoGround, dt);
+    double rainBefore = rain[i];
+    cold[i] += graupelProcesses<S>(theta, q, cloud, ice, snow, rain, graupel, i, ex, pz, rhoZ, dt);
+    double rainFrozen = (double)theta[i] * ex < 273.15 ? jmax(0, rainBefore - (double)rain[i]) : 0;
+    cold[i] += hailProcesses<S>(theta, q, cloud, ice, snow, rain, graupel, hail, i, ex, pz, rhoZ, dt);
+    if (iceBefore > 0) iceNumber[i] *= (double)ice[i] / iceBefore;
+    double splinters = splintering((double)theta[i] * ex - 273.15) * SPLINTERS * jmax(0, cloudBefore - (double)cloud[i])
+      + (rainFrozen > 0 ? fragmentsPerKg(std::pow(PI * RHO_W * N0R / (rhoZ * rainBefore), .25)) * rainFrozen : 0);
+    if (splinters > 0) {
+      double fromG = jmin(graupel[i], splinters * CRYSTAL_MASS), fromS = jmin(snow[i], splinters * CRYSTAL_MASS - fromG);
+      graupel[i] -= fromG; snow[i] -= fromS; ice[i] += fromG + fromS; iceNumber[i] += (fromG + fromS) / CRYSTAL_MASS;
+    }
+    cond = saturationAdjustMixed<S>(theta, q, cloud, ice, i, ex, pz, iceNumber);
+    settleCrystals<S>(ice, iceNumber, i);
+  } else cond = saturationAdjust<S>(theta, q, cloud, i, ex, pz);
+  if (cond < 0) cold[i] -= LV / CP / ex * cond * .14;
+  return evap;
+}
+
 template <class S> struct Model {
   GridSpec g;
   std::vector<double> p, exner, thetaEnv, qEnv, uGround, vGround, rho, uEnv, vEnv, levelWeight, surfaceShare;
@@ -236,30 +269,7 @@ template <class S> struct Model {
     double alt = g.zs[z], pz = p[z], rhoZ = rho[z], ex = exner[z], ue = uEnv[z], ve = vEnv[z], thEnv = thetaEnv[z];
     for (int y = 0; y < ny; y++) for (int x = 0, i = z * layer + y * nx; x < nx; x++, i++) {
       double q0 = q[i];
-      double evap = !sw.rainFormation ? 0 : rainProcesses<S>(q, cloud, rain, i, (double)theta[i] * ex, pz, rhoZ, dt, sw.evaporation);
-      if (evap > 0) { double cool = LV / CP / ex * evap; theta[i] -= cool; cold[i] += cool; }
-      double cond;
-      if (sw.ice) {
-        freezeRain<S>(theta, rain, graupel, i, ex);
-        settleCrystals<S>(ice, iceNumber, i);
-        cold[i] += iceProcesses<S>(theta, q, ice, snow, iceNumber, i, ex, pz, rhoZ, dt);
-        double iceBefore = ice[i], cloudBefore = cloud[i];
-        cold[i] += snowProcesses<S>(theta, q, cloud, ice, snow, rain, i, ex, pz, rhoZ, rhoGround, dt);
-        double rainBefore = rain[i];
-        cold[i] += graupelProcesses<S>(theta, q, cloud, ice, snow, rain, graupel, i, ex, pz, rhoZ, dt);
-        double rainFrozen = (double)theta[i] * ex < 273.15 ? jmax(0, rainBefore - (double)rain[i]) : 0;
-        cold[i] += hailProcesses<S>(theta, q, cloud, ice, snow, rain, graupel, hail, i, ex, pz, rhoZ, dt);
-        if (iceBefore > 0) iceNumber[i] *= (double)ice[i] / iceBefore;
-        double splinters = splintering((double)theta[i] * ex - 273.15) * SPLINTERS * jmax(0, cloudBefore - (double)cloud[i])
-          + (rainFrozen > 0 ? fragmentsPerKg(std::pow(PI * RHO_W * N0R / (rhoZ * rainBefore), .25)) * rainFrozen : 0);
-        if (splinters > 0) {
-          double fromG = jmin(graupel[i], splinters * CRYSTAL_MASS), fromS = jmin(snow[i], splinters * CRYSTAL_MASS - fromG);
-          graupel[i] -= fromG; snow[i] -= fromS; ice[i] += fromG + fromS; iceNumber[i] += (fromG + fromS) / CRYSTAL_MASS;
-        }
-        cond = saturationAdjustMixed<S>(theta, q, cloud, ice, i, ex, pz, iceNumber);
-        settleCrystals<S>(ice, iceNumber, i);
-      } else cond = saturationAdjust<S>(theta, q, cloud, i, ex, pz);
-      if (cond < 0) cold[i] -= LV / CP / ex * cond * .14;
+      double evap = microphysicsNode<S>(theta, q, cloud, rain, cold, ice, iceNumber, snow, graupel, hail, i, ex, pz, rhoZ, rhoGround, dt, sw);
       if (!sw.pressureInStages) {
         double thvEnv = thEnv * (1 + .61 * qEnv[z]);
         double buoy = ((double)theta[i] * (1 + .61 * (double)q[i]) - thvEnv) / thvEnv - (double)cloud[i] - (double)ice[i] - (sw.loading ? (double)rain[i] + (double)snow[i] + (double)graupel[i] + (double)hail[i] : 0);

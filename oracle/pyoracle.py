@@ -61,6 +61,8 @@ def lib():
                 getattr(L, name).argtypes = [C.c_double] * nargs
             L.orc_cell.restype = C.c_double
             L.orc_cell.argtypes = [C.c_int, _f, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double]
+            L.orc_microphysics.restype = C.c_double
+            L.orc_microphysics.argtypes = [_f, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int]
             L.orc_fft.argtypes = [C.c_int, _d, _d, C.c_int]
             L.orc_hdft.argtypes = [C.c_int, C.c_int, C.c_int, _d, _d, _d, _d]
             grid_args = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, _d, _d, _d]

@@ -1,0 +1,49 @@
+// Test harness: the device step's per-node functions (meteolab_gb300/csrc/sg_physics.cuh, sg_common.cuh,
+// sg_fft.cuh) compiled for the host, so their logic can be checked against the oracle on the CPU. Built by
+// tests/test_device_code_on_cpu.py with g++; not part of the library.
+#include <vector_types.h>
+#include <vector_functions.h>
+#include <cmath>
+#include <vector>
+#include "../../meteolab_gb300/csrc/sg_common.cuh"
+#include "../../meteolab_gb300/csrc/sg_fft.cuh"
+#include "../../meteolab_gb300/csrc/sg_physics.cuh"
+
+using namespace sg;
+
+extern "C" {
+
+float ht_weno(float a, float b, float c, float d, float e) { return weno5(a, b, c, d, e); }
+float ht_upwind(float a, float b, float c, float d, float e) { return upwind5(a, b, c, d, e); }
+
+// v = [thp, thb, q, cloud, rain, ice, inum, snow, graupel, hail, cold] in/out; returns evap.
+float ht_microphysics(float* v, float exner, float p, float rho, float fallsq, float dt, int flags) {
+  phys::Node s{v[0], v[1], v[2], v[3], v[4], v[5], v[6], v[7], v[8], v[9], v[10]};
+  float evap = 0;
+  phys::microphysics(s, exner, p, rho, fallsq, dt, flags, evap);
+  v[0] = s.thp; v[2] = s.q; v[3] = s.cloud; v[4] = s.rain; v[5] = s.ice; v[6] = s.inum; v[7] = s.snow; v[8] = s.graupel; v[9] = s.hail; v[10] = s.cold;
+  return evap;
+}
+void ht_fall(float rain, float snow, float graupel, float hail, float rho, float fallsq, float* out) {
+  out[0] = phys::rainFall(rain, rho, fallsq); out[1] = phys::snowFall(snow, rho, fallsq);
+  out[2] = phys::graupelFall(graupel, rho); out[3] = phys::hailFall(hail, rho);
+}
+// Forward FFT of one row with the device's Stockham stages (x in/out as interleaved re, im).
+int ht_fft(int n, float* x) {
+  int rad[8]; int nf = fft_plan_factors(n, rad);
+  if (nf < 0) return -1;
+  std::vector<float2> tw(n), a(n), b(n);
+  for (int t = 0; t < n; t++) { double ang = -2 * M_PI * t / n; tw[t] = make_float2((float)cos(ang), (float)sin(ang)); }
+  for (int i = 0; i < n; i++) a[i] = make_float2(x[2 * i], x[2 * i + 1]);
+  float2 *src = a.data(), *dst = b.data();
+  int Ns = 1;
+  for (int s = 0; s < nf; s++) {
+    int r = rad[s];
+    for (int j = 0; j < n / r; j++) fft_butterfly(src, dst, n, r, Ns, j, tw.data());
+    std::swap(src, dst); Ns *= r;
+  }
+  for (int i = 0; i < n; i++) { x[2 * i] = src[i].x; x[2 * i + 1] = src[i].y; }
+  return nf;
+}
+
+}  // extern "C"

@@ -1,0 +1,128 @@
+"""The device step's per-node code compiled for the host and checked against the oracle on the CPU.
+
+The microphysics (sg_physics.cuh), the WENO5/upwind reconstructions (sg_common.cuh) and the Stockham FFT stages
+(sg_fft.cuh) are __host__ __device__ functions; tests/native/hosttest.cpp builds them with g++ so their logic is
+tested here without a GPU. The GPU tests (test_gpu_*.py) check the same code as the device runs it.
+"""
+import ctypes as C
+import math
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import pyoracle as O
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "native", "hosttest.cpp")
+LIB = os.path.join(HERE, "native", "libhosttest.so")
+
+
+def _cuda_include():
+    for d in ("/usr/local/cuda/include", "/usr/local/cuda/targets/x86_64-linux/include", "/usr/local/cuda/targets/sbsa-linux/include"):
+        if os.path.exists(os.path.join(d, "vector_types.h")):
+            return d
+    pytest.skip("CUDA headers (vector_types.h) not found")
+
+
+@pytest.fixture(scope="module")
+def ht():
+    deps = [SRC] + [os.path.join(HERE, "..", "meteolab_gb300", "csrc", f) for f in ("sg_common.cuh", "sg_fft.cuh", "sg_physics.cuh")]
+    if not os.path.exists(LIB) or any(os.path.getmtime(d) > os.path.getmtime(LIB) for d in deps):
+        subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-I", _cuda_include(), "-o", LIB, SRC], check=True)
+    L = C.CDLL(LIB)
+    L.ht_weno.restype = C.c_float
+    L.ht_weno.argtypes = [C.c_float] * 5
+    L.ht_upwind.restype = C.c_float
+    L.ht_upwind.argtypes = [C.c_float] * 5
+    L.ht_microphysics.restype = C.c_float
+    L.ht_microphysics.argtypes = [C.POINTER(C.c_float), C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int]
+    L.ht_fft.restype = C.c_int
+    L.ht_fft.argtypes = [C.c_int, C.POINTER(C.c_float)]
+    L.ht_fall.argtypes = [C.c_float] * 6 + [C.POINTER(C.c_float)]
+    return L
+
+
+def test_weno_matches_oracle_over_scales(ht):
+    rng = np.random.default_rng(3)
+    L = O.lib()
+    for scale in (1e-9, 1e-6, 1e-3, 1.0, 300.0, 1e6):
+        for _ in range(200):
+            v = (rng.random(5) * scale).astype(np.float32)
+            if rng.random() < 0.3:
+                v[rng.integers(0, 5, 2)] = 0
+            ref = L.orc_weno(*[float(x) for x in v])
+            got = ht.ht_weno(*[float(x) for x in v])
+            assert abs(got - ref) <= 4e-7 * float(np.max(np.abs(v))) + 2e-6 * abs(ref), (scale, v, got, ref)
+    assert ht.ht_weno(0, 0, 0, 0, 0) == 0.0
+    assert ht.ht_weno(0.25, 0.25, 0.25, 0.25, 0.25) == np.float32(0.25)
+
+
+def test_upwind_matches_oracle(ht):
+    rng = np.random.default_rng(4)
+    for _ in range(100):
+        v = (rng.random(5) * 40 - 20).astype(np.float32)
+        assert abs(ht.ht_upwind(*map(float, v)) - O.lib().orc_upwind5(*map(float, v))) < 1e-5
+
+
+@pytest.mark.parametrize("n", list(range(1, 18)) + [20, 21, 32, 40, 49, 64, 80, 256, 320])
+def test_stockham_fft_matches_numpy(ht, n):
+    rng = np.random.default_rng(n)
+    z = (rng.random(n) - 0.5) + 1j * (rng.random(n) - 0.5)
+    x = np.empty(2 * n, np.float32)
+    x[0::2], x[1::2] = z.real, z.imag
+    assert ht.ht_fft(n, x.ctypes.data_as(C.POINTER(C.c_float))) >= 0
+    got = x[0::2] + 1j * x[1::2]
+    ref = np.fft.fft(z)
+    assert np.max(np.abs(got - ref)) < 2e-6 * max(1.0, np.max(np.abs(ref))) * math.log2(max(n, 2))
+
+
+def test_fall_speeds_match_oracle(ht):
+    L = O.lib()
+    out = np.empty(4, np.float32)
+    for q in (1e-8, 1e-6, 1e-4, 1e-3, 5e-3):
+        for rho in (1.16, 0.7, 0.3):
+            fsq = math.sqrt(1.16 / rho)
+            ht.ht_fall(q, q, q, q, rho, fsq, out.ctypes.data_as(C.POINTER(C.c_float)))
+            ref = [L.orc_fall_speed(q, rho, 1.16), L.orc_snow_fall_speed(q, rho, 1.16), L.orc_graupel_fall_speed(q, rho), L.orc_hail_fall_speed(q, rho)]
+            assert np.allclose(out, ref, rtol=2e-6, atol=1e-7)
+
+
+KAPPA = 0.286
+# Representative cells: (T K, p Pa, rho, species dict) away from the branch thresholds of the scheme.
+CELLS = [
+    (295.0, 95000, 1.12, dict(q=0.018, cloud=2e-3, rain=1e-3)),            # warm, supersaturated, autoconversion
+    (290.0, 90000, 1.08, dict(q=0.006, rain=2e-3)),                        # warm, dry: rain evaporates
+    (285.0, 85000, 1.04, dict(q=0.0105, cloud=5e-4, rain=3e-4, graupel=1e-3, hail=2e-3, snow=5e-4)),  # melting
+    (268.0, 60000, 0.78, dict(q=3.2e-3, cloud=1.5e-3, rain=1e-3, ice=1e-5, snow=1e-3, graupel=2e-3, iceNumber=2e4)),  # riming, splinters
+    (255.0, 45000, 0.62, dict(q=1.2e-3, cloud=5e-4, ice=2e-4, snow=8e-4, graupel=1e-3, hail=3e-3, iceNumber=5e5, rain=2e-4)),
+    (240.0, 33000, 0.48, dict(q=3e-4, cloud=1e-4, ice=5e-4, snow=2e-4, iceNumber=1e6)),
+    (228.0, 25000, 0.38, dict(q=1e-4, cloud=3e-4, rain=1e-4, ice=1e-4, iceNumber=1e5)),  # below -38: droplets freeze
+    (262.0, 55000, 0.73, dict(q=2.0e-3, ice=1e-3, snow=3e-3, iceNumber=1e5)),  # subsaturated: sublimation
+    (265.15, 55000, 0.75, dict(q=4e-3, cloud=4e-3, rain=4e-3, graupel=4e-3)),   # wet growth: hail forms
+]
+
+
+@pytest.mark.parametrize("k", range(len(CELLS)))
+@pytest.mark.parametrize("ice", [1, 0])
+def test_microphysics_matches_oracle(ht, k, ice):
+    tk, p, rho, sp = CELLS[k]
+    exner = (p / 1e5) ** KAPPA
+    theta = tk / exner
+    thb = np.float32(theta - 0.7)
+    dt = 3.0
+    names = ("theta", "q", "cloud", "rain", "ice", "iceNumber", "snow", "graupel", "hail", "cold")
+    ov = np.array([theta] + [sp.get(n, 0.0) for n in names[1:]], np.float32)
+    dv = np.array([np.float32(ov[0]) - thb, thb, ov[1], ov[2], ov[3], ov[4], ov[5], ov[6], ov[7], ov[8], ov[9]], np.float32)
+    flags = (1 if ice else 0) | 2 | 4
+    evo = O.lib().orc_microphysics(O.fp(ov), exner, p, rho, 1.16, dt, flags)
+    dflags = (128 if ice else 0) | 2 | 4
+    evd = ht.ht_microphysics(dv.ctypes.data_as(C.POINTER(C.c_float)), exner, p, rho, math.sqrt(1.16 / rho), dt, dflags)
+    got = dict(theta=float(dv[0]) + float(dv[1]), q=dv[2], cloud=dv[3], rain=dv[4], ice=dv[5], iceNumber=dv[6], snow=dv[7], graupel=dv[8], hail=dv[9], cold=dv[10])
+    ref = {n: float(ov[j]) for j, n in enumerate(names)}
+    assert abs(got["theta"] - ref["theta"]) < 2e-4, (got["theta"], ref["theta"])
+    for n in names[1:]:
+        tol = {"iceNumber": 1e-3 * max(1.0, abs(ref[n])), "cold": 2e-4}.get(n, 1e-4 * abs(ref[n]) + 2e-9)
+        assert abs(float(got[n]) - ref[n]) <= tol, (n, float(got[n]), ref[n])
+    assert abs(evd - evo) <= 1e-4 * abs(evo) + 1e-10

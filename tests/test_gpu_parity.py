@@ -1,0 +1,184 @@
+"""Parity of the device step with the oracle, through the C ABI (GPU).
+
+Tolerances: the device computes the fields and all stencil arithmetic in FP32 (FP64 only in the tridiagonal
+solves and the budget sums); the oracle is the reference's algorithm in FP64 arithmetic. Per field after one step
+the relative L2 error is held to 1e-5 (with the absolute floors of tests/parity.py for fields that are near zero);
+stage by stage within a step to 2e-5; over 100 steps of a growing storm to 2e-3 (FP32 rounding amplified by the
+convective instability the storm grows from).
+"""
+import numpy as np
+import pytest
+
+import pyoracle as O
+from parity import FLOOR, developed_state, field_errors, rel_l2, threads
+from meteolab_gb300.grid import DEFAULT_GRID, LARGE_GRID, GridOptions, create_grid
+from meteolab_gb300.scenarios import CARRIED, baseline_run
+
+pytestmark = pytest.mark.gpu
+DT = 3.0
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from meteolab_gb300 import build
+    build.build()
+    from meteolab_gb300.runtime import Context
+    c = Context()
+    yield c
+    c.close()
+
+
+@pytest.fixture(scope="module")
+def storm():
+    """A developed storm on the standard grid: 300 oracle steps (15 min) from the benchmark initial state."""
+    spec = baseline_run(create_grid(DEFAULT_GRID), seed=42)
+    return developed_state(spec, 300)
+
+
+def _report(title, errs):
+    print(f"\n{title}: " + ", ".join(f"{k} {v:.2e}" for k, v in errs.items()))
+
+
+def test_step_parts_match_oracle(ctx, storm):
+    """Part by part within one step (beginStep, dynamics, physicsStep, mixStep, final projection)."""
+    o = O.OracleModel(storm, threads=threads())
+    r = ctx.create(storm)
+    thb = np.repeat(storm.env.theta, storm.grid.layer)
+    # where each field lives on the device after each part (set index)
+    where = {1: {k: 0 for k in CARRIED}, 2: {k: 1 for k in CARRIED},
+             3: {k: (0 if k in ("rain", "snow", "graupel", "hail", "cold") else 2) for k in CARRIED},
+             4: {k: 0 for k in CARRIED}, 5: {k: 0 for k in CARRIED}}
+    worst = {}
+    for part in (1, 2, 3, 4, 5):
+        o.step_part(DT, part)
+        r.debug_part(part)
+        got = {k: r.debug_read_set(where[part][k], k) for k in CARRIED}
+        got["theta"] = got["theta"].astype(np.float64) + thb
+        ref = o.fields()
+        errs = field_errors(got, ref)
+        errs["theta'"] = rel_l2(got["theta"] - thb, ref["theta"] - thb, FLOOR["theta'"])
+        _report(f"part {part}", errs)
+        worst[part] = errs
+    for part, errs in worst.items():
+        bad = {k: v for k, v in errs.items() if v > 2e-5}
+        assert not bad, f"part {part}: {bad}"
+    r.retire()
+
+
+def test_one_step_against_fp64_oracle(ctx, storm):
+    """Every field within 1e-5 relative L2 of the FP64 oracle after one step (from the developed storm)."""
+    o64 = O.OracleModel(storm, fp64=True, threads=threads())
+    o64.step(DT, 1)
+    ref = o64.fields()
+    r = ctx.create(storm)
+    r.step(1)
+    got = r.read()
+    errs = field_errors(got, ref)
+    thb = np.repeat(storm.env.theta, storm.grid.layer)
+    errs["theta'"] = rel_l2(got["theta"] - thb, ref["theta"] - thb, FLOOR["theta'"])
+    _report("one step vs FP64", errs)
+    col = r.columns()
+    errs_c = {"precipitation": rel_l2(col["precipitation"], o64.get("precipitation"), 1e-9)}
+    _report("columns", errs_c)
+    assert max(errs.values()) <= 1e-5, errs
+    assert errs_c["precipitation"] <= 1e-5
+    r.retire()
+
+
+def test_hundred_steps_from_rest(ctx):
+    """100 steps from the initial state on the standard grid against the FP64 oracle."""
+    spec = baseline_run(create_grid(DEFAULT_GRID), seed=7)
+    o64 = O.OracleModel(spec, fp64=True, threads=threads())
+    o64.step(DT, 100)
+    r = ctx.create(spec)
+    r.step(100)
+    got, ref = r.read(), o64.fields()
+    errs = field_errors(got, ref)
+    thb = np.repeat(spec.env.theta, spec.grid.layer)
+    errs["theta'"] = rel_l2(got["theta"] - thb, ref["theta"] - thb, FLOOR["theta'"])
+    _report("100 steps vs FP64", errs)
+    st = r.status()
+    assert st["steps"] == 100 and st["clipped"] == 0 and not st["failed"]
+    assert max(errs.values()) <= 2e-3, errs
+    r.retire()
+
+
+def test_projection_leaves_no_divergence(ctx, storm):
+    """After a step the dual-cell divergence of the stored FP32 velocities is at FP32 rounding level."""
+    r = ctx.create(storm)
+    before = r.divergence()
+    r.step(1)
+    after = r.divergence()
+    u = r.read(["u", "v", "w"])
+    scale = max(float(np.abs(u[k]).max()) for k in ("u", "v", "w")) * 1.2 / 100.0  # |rho u| / dz at the ground
+    print(f"\nmax |D R u|: before {before:.3e}, after {after:.3e}, rounding scale {scale:.3e}")
+    assert after < 1e-5 * scale and after < before
+    r.retire()
+
+
+def test_runs_are_deterministic_and_batch_independent(ctx, storm):
+    """A run alone and the same run inside an uneven batch (standard + large) give bitwise equal fields."""
+    alone = ctx.create(storm)
+    alone.step(3)
+    a = alone.read()
+    big = baseline_run(create_grid(LARGE_GRID), seed=5)
+    x, y = ctx.create(storm), ctx.create(big)
+    ctx.batch_step([x, y], 3)
+    b = x.read()
+    for k in CARRIED:
+        assert np.array_equal(a[k], b[k]), k
+    z = ctx.create(big)
+    z.step(3)
+    c, d = y.read(), z.read()
+    for k in CARRIED:
+        assert np.array_equal(c[k], d[k]), k
+    for run in (alone, x, y, z):
+        run.retire()
+
+
+def test_serving_gives_the_same_result_alone_and_in_the_mix(ctx, storm):
+    """Requests admitted while others are on the device finish with the fields they get when stepped alone."""
+    from meteolab_gb300.runtime import Server
+    specs = [storm, baseline_run(create_grid(LARGE_GRID), seed=11), baseline_run(create_grid(DEFAULT_GRID), seed=12)]
+    steps = [6, 4, 5]
+    ref = []
+    for s, n in zip(specs, steps):
+        r = ctx.create(s)
+        r.step(n)
+        ref.append(r.read())
+        r.retire()
+    srv = Server(ctx, max_active=2)
+    srv.submit(specs[0], steps[0], 0)
+    srv.submit(specs[1], steps[1], 1)
+    got, it = {}, 0
+    while len(got) < 3 and it < 50:
+        done, active, queued = srv.iterate()
+        for tag in done:
+            got[tag] = srv.collect(tag, specs[tag].grid.n)
+        if it == 1:
+            srv.submit(specs[2], steps[2], 2)  # arrives while two others are stepping; waits for a slot
+        it += 1
+    srv.close()
+    assert sorted(got) == [0, 1, 2]
+    for tag in range(3):
+        for k in CARRIED:
+            assert np.array_equal(got[tag][k], ref[tag][k]), (tag, k)
+
+
+def test_nonfinite_run_fails_alone(ctx, storm):
+    """A NaN put into one run's state marks that run failed; the run batched with it is untouched."""
+    bad = {k: v.copy() for k, v in storm.fields.items()}
+    bad["theta"][12345] = np.nan
+    from meteolab_gb300.scenarios import RunSpec
+    sick = ctx.create(RunSpec(storm.grid, storm.env, storm.switches, bad))
+    well = ctx.create(storm)
+    ctx.batch_step([sick, well], 2)
+    assert sick.status()["failed"] == 1
+    assert well.status()["failed"] == 0
+    ref = ctx.create(storm)
+    ref.step(2)
+    a, b = well.read(), ref.read()
+    for k in CARRIED:
+        assert np.array_equal(a[k], b[k]), k
+    for r in (sick, well, ref):
+        r.retire()
