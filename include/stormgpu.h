@@ -125,7 +125,7 @@ int sg_run_divergence(sg_context* ctx, sg_run run, double* max_abs_div);
 
 /* ---- diagnostics: one part of the step (1 beginStep, 2 dynamics, 3 physicsStep, 4 mixStep, 5 final projection),
  * and the raw device buffers (set 0 = state, 1 and 2 = stage scratch; theta of a set is its departure from the base
- * profile; faces4 = mx, my, mz, div). For stage-wise parity tests against the oracle. */
+ * profile; faces4 = (mx, my, mz, div) per node, interleaved). For stage-wise parity tests against the oracle. */
 int sg_debug_step_part(sg_context* ctx, sg_run run, int part);
 int sg_debug_read_set(sg_context* ctx, sg_run run, int set, int field, float* host);
 int sg_debug_read_faces(sg_context* ctx, sg_run run, float* faces4);

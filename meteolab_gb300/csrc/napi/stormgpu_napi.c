@@ -1,0 +1,199 @@
+/*
+ * N-API addon over the stormgpu C ABI, for the reference's Node host (its physics worker, src/simulation.worker.ts,
+ * and the ensemble/series runners). Each stepping call runs on the libuv thread pool (napi_async_work) and resolves
+ * a Promise, as the reference awaits GpuDynamics.step (src/gpu/step.ts:16). Build where node_api.h exists:
+ *   cc -O2 -shared -fPIC -I<node>/include/node stormgpu_napi.c -L.. -lstormgpu -o stormgpu.node
+ *
+ * JS surface:
+ *   createContext(device = 0, hbmBudget = 0) -> ctx
+ *   createRun(ctx, grid, base, switches, fields) -> run      grid {nx, ny, nz, dx, dy, height, zs, dzs, hz: Float64Array}
+ *                                                             base {p, exner, theta, q, u, v, rho: Float64Array}
+ *                                                             switches {dt, coriolis, ...}, fields: Float32Array[13]
+ *   step(ctx, runs: Int32Array, steps) -> Promise<void>
+ *   readFields(ctx, run, fields: Float32Array[13]) / writeFields(ctx, run, fields)
+ *   status(ctx, run) -> {steps, clipped, negativeFilled, failed}
+ *   retire(ctx, run), destroyContext(ctx)
+ */
+#include <node_api.h>
+#include <stdlib.h>
+#include <string.h>
+#include "../../../include/stormgpu.h"
+
+#define CHECK(env, call)                                                    \
+  do {                                                                      \
+    if ((call) != napi_ok) { napi_throw_error(env, NULL, #call); return NULL; } \
+  } while (0)
+
+static napi_value throw_status(napi_env env, sg_context* ctx, int st) {
+  char msg[256];
+  snprintf(msg, sizeof msg, "stormgpu error %d: %s", st, ctx ? sg_last_error(ctx) : "");
+  napi_throw_error(env, NULL, msg);
+  return NULL;
+}
+
+static double get_num(napi_env env, napi_value obj, const char* key) {
+  napi_value v; double d = 0;
+  if (napi_get_named_property(env, obj, key, &v) == napi_ok) napi_get_value_double(env, v, &d);
+  return d;
+}
+
+static void* typed_data(napi_env env, napi_value obj, const char* key, size_t* length) {
+  napi_value v; napi_typedarray_type type; size_t len; void* data; napi_value buf; size_t off;
+  if (napi_get_named_property(env, obj, key, &v) != napi_ok) return NULL;
+  if (napi_get_typedarray_info(env, v, &type, &len, &data, &buf, &off) != napi_ok) return NULL;
+  if (length) *length = len;
+  return data;
+}
+
+static napi_value create_context(napi_env env, napi_callback_info info) {
+  size_t argc = 2; napi_value argv[2]; int32_t device = 0; double budget = 0;
+  CHECK(env, napi_get_cb_info(env, info, &argc, argv, NULL, NULL));
+  if (argc > 0) napi_get_value_int32(env, argv[0], &device);
+  if (argc > 1) napi_get_value_double(env, argv[1], &budget);
+  sg_context* ctx = NULL;
+  int st = sg_context_create(device, (uint64_t)budget, &ctx);
+  if (st) return throw_status(env, NULL, st);
+  napi_value ext;
+  CHECK(env, napi_create_external(env, ctx, NULL, NULL, &ext));
+  return ext;
+}
+
+static sg_context* ctx_of(napi_env env, napi_value v) { void* p = NULL; napi_get_value_external(env, v, &p); return (sg_context*)p; }
+
+static int fields_of(napi_env env, napi_value arr, float** out) {
+  for (uint32_t k = 0; k < SG_NFIELDS; k++) {
+    napi_value el; napi_typedarray_type type; size_t len; void* data; napi_value buf; size_t off;
+    if (napi_get_element(env, arr, k, &el) != napi_ok) return 0;
+    if (napi_get_typedarray_info(env, el, &type, &len, &data, &buf, &off) != napi_ok || type != napi_float32_array) return 0;
+    out[k] = (float*)data;
+  }
+  return 1;
+}
+
+static napi_value create_run(napi_env env, napi_callback_info info) {
+  size_t argc = 5; napi_value argv[5];
+  CHECK(env, napi_get_cb_info(env, info, &argc, argv, NULL, NULL));
+  sg_context* ctx = ctx_of(env, argv[0]);
+  sg_grid g; memset(&g, 0, sizeof g);
+  g.nx = (int32_t)get_num(env, argv[1], "nx"); g.ny = (int32_t)get_num(env, argv[1], "ny"); g.nz = (int32_t)get_num(env, argv[1], "nz");
+  g.dx = get_num(env, argv[1], "dx"); g.dy = get_num(env, argv[1], "dy"); g.height = get_num(env, argv[1], "height");
+  g.zs = typed_data(env, argv[1], "zs", NULL); g.dzs = typed_data(env, argv[1], "dzs", NULL); g.hz = typed_data(env, argv[1], "hz", NULL);
+  sg_base_state b = {typed_data(env, argv[2], "p", NULL), typed_data(env, argv[2], "exner", NULL), typed_data(env, argv[2], "theta", NULL),
+                     typed_data(env, argv[2], "q", NULL), typed_data(env, argv[2], "u", NULL), typed_data(env, argv[2], "v", NULL),
+                     typed_data(env, argv[2], "rho", NULL)};
+  sg_switches s; memset(&s, 0, sizeof s);
+  s.dt = get_num(env, argv[3], "dt"); s.coriolis = get_num(env, argv[3], "coriolis"); s.wind_relaxation = get_num(env, argv[3], "windRelaxation");
+  s.sponge_rate = get_num(env, argv[3], "spongeRate"); s.sponge_start = get_num(env, argv[3], "spongeStart"); s.cs = get_num(env, argv[3], "cs");
+  s.drag_cd = get_num(env, argv[3], "dragCd"); s.frame_u = get_num(env, argv[3], "frameU"); s.frame_v = get_num(env, argv[3], "frameV");
+  s.loading = (int32_t)get_num(env, argv[3], "loading"); s.evaporation = (int32_t)get_num(env, argv[3], "evaporation");
+  s.rain_formation = (int32_t)get_num(env, argv[3], "rainFormation"); s.anisotropic = (int32_t)get_num(env, argv[3], "anisotropic");
+  s.vertical_dz = (int32_t)get_num(env, argv[3], "verticalDz"); s.durran_klemp = (int32_t)get_num(env, argv[3], "durranKlemp");
+  s.pressure_in_stages = (int32_t)get_num(env, argv[3], "pressureInStages"); s.ice = (int32_t)get_num(env, argv[3], "ice");
+  float* init[SG_NFIELDS];
+  if (!fields_of(env, argv[4], init)) { napi_throw_type_error(env, NULL, "fields: 13 Float32Array"); return NULL; }
+  sg_run run;
+  int st = sg_run_create(ctx, &g, &b, &s, (const float* const*)init, &run);
+  if (st) return throw_status(env, ctx, st);
+  napi_value out;
+  CHECK(env, napi_create_int32(env, run, &out));
+  return out;
+}
+
+typedef struct { sg_context* ctx; sg_run* runs; int n, steps, status; napi_deferred deferred; napi_async_work work; } StepJob;
+
+static void step_execute(napi_env env, void* data) {
+  StepJob* j = (StepJob*)data;
+  j->status = sg_batch_step(j->ctx, j->runs, j->n, j->steps);
+}
+static void step_complete(napi_env env, napi_status status, void* data) {
+  StepJob* j = (StepJob*)data;
+  if (j->status == SG_OK) { napi_value u; napi_get_undefined(env, &u); napi_resolve_deferred(env, j->deferred, u); }
+  else {
+    napi_value msg, err; char text[256];
+    snprintf(text, sizeof text, "stormgpu error %d: %s", j->status, sg_last_error(j->ctx));
+    napi_create_string_utf8(env, text, NAPI_AUTO_LENGTH, &msg); napi_create_error(env, NULL, msg, &err);
+    napi_reject_deferred(env, j->deferred, err);
+  }
+  napi_delete_async_work(env, j->work);
+  free(j->runs); free(j);
+}
+
+static napi_value step(napi_env env, napi_callback_info info) {
+  size_t argc = 3; napi_value argv[3];
+  CHECK(env, napi_get_cb_info(env, info, &argc, argv, NULL, NULL));
+  StepJob* j = (StepJob*)calloc(1, sizeof(StepJob));
+  j->ctx = ctx_of(env, argv[0]);
+  napi_typedarray_type type; size_t len; void* data; napi_value buf; size_t off;
+  if (napi_get_typedarray_info(env, argv[1], &type, &len, &data, &buf, &off) != napi_ok || type != napi_int32_array) {
+    free(j); napi_throw_type_error(env, NULL, "runs: Int32Array"); return NULL;
+  }
+  j->n = (int)len; j->runs = (sg_run*)malloc(len * sizeof(sg_run)); memcpy(j->runs, data, len * sizeof(sg_run));
+  napi_get_value_int32(env, argv[2], &j->steps);
+  napi_value promise, name;
+  CHECK(env, napi_create_promise(env, &j->deferred, &promise));
+  CHECK(env, napi_create_string_utf8(env, "stormgpu.step", NAPI_AUTO_LENGTH, &name));
+  CHECK(env, napi_create_async_work(env, NULL, name, step_execute, step_complete, j, &j->work));
+  CHECK(env, napi_queue_async_work(env, j->work));
+  return promise;
+}
+
+static napi_value fields_io(napi_env env, napi_callback_info info, int write) {
+  size_t argc = 3; napi_value argv[3]; int32_t run;
+  CHECK(env, napi_get_cb_info(env, info, &argc, argv, NULL, NULL));
+  sg_context* ctx = ctx_of(env, argv[0]);
+  napi_get_value_int32(env, argv[1], &run);
+  float* f[SG_NFIELDS];
+  if (!fields_of(env, argv[2], f)) { napi_throw_type_error(env, NULL, "fields: 13 Float32Array"); return NULL; }
+  int st = write ? sg_run_write_fields(ctx, run, SG_ALL_FIELDS, (const float* const*)f) : sg_run_read_fields(ctx, run, SG_ALL_FIELDS, f);
+  if (st) return throw_status(env, ctx, st);
+  return NULL;
+}
+static napi_value read_fields(napi_env env, napi_callback_info info) { return fields_io(env, info, 0); }
+static napi_value write_fields(napi_env env, napi_callback_info info) { return fields_io(env, info, 1); }
+
+static napi_value status(napi_env env, napi_callback_info info) {
+  size_t argc = 2; napi_value argv[2]; int32_t run;
+  CHECK(env, napi_get_cb_info(env, info, &argc, argv, NULL, NULL));
+  sg_context* ctx = ctx_of(env, argv[0]);
+  napi_get_value_int32(env, argv[1], &run);
+  sg_run_counters c;
+  int st = sg_run_status(ctx, run, &c);
+  if (st && st != SG_ERR_NONFINITE) return throw_status(env, ctx, st);
+  napi_value o, v;
+  CHECK(env, napi_create_object(env, &o));
+  napi_create_double(env, (double)c.steps, &v); napi_set_named_property(env, o, "steps", v);
+  napi_create_double(env, (double)c.clipped, &v); napi_set_named_property(env, o, "clipped", v);
+  napi_create_double(env, c.negative_filled, &v); napi_set_named_property(env, o, "negativeFilled", v);
+  napi_get_boolean(env, c.failed != 0, &v); napi_set_named_property(env, o, "failed", v);
+  return o;
+}
+
+static napi_value retire(napi_env env, napi_callback_info info) {
+  size_t argc = 2; napi_value argv[2]; int32_t run;
+  CHECK(env, napi_get_cb_info(env, info, &argc, argv, NULL, NULL));
+  sg_context* ctx = ctx_of(env, argv[0]);
+  napi_get_value_int32(env, argv[1], &run);
+  int st = sg_run_retire(ctx, run);
+  if (st) return throw_status(env, ctx, st);
+  return NULL;
+}
+
+static napi_value destroy_context(napi_env env, napi_callback_info info) {
+  size_t argc = 1; napi_value argv[1];
+  CHECK(env, napi_get_cb_info(env, info, &argc, argv, NULL, NULL));
+  sg_context_destroy(ctx_of(env, argv[0]));
+  return NULL;
+}
+
+static napi_value init(napi_env env, napi_value exports) {
+  napi_property_descriptor d[] = {
+    {"createContext", 0, create_context, 0, 0, 0, napi_default, 0}, {"createRun", 0, create_run, 0, 0, 0, napi_default, 0},
+    {"step", 0, step, 0, 0, 0, napi_default, 0}, {"readFields", 0, read_fields, 0, 0, 0, napi_default, 0},
+    {"writeFields", 0, write_fields, 0, 0, 0, napi_default, 0}, {"status", 0, status, 0, 0, 0, napi_default, 0},
+    {"retire", 0, retire, 0, 0, 0, napi_default, 0}, {"destroyContext", 0, destroy_context, 0, 0, 0, napi_default, 0},
+  };
+  napi_define_properties(env, exports, sizeof d / sizeof d[0], d);
+  return exports;
+}
+
+NAPI_MODULE(NODE_GYP_MODULE_NAME, init)

@@ -312,7 +312,7 @@ __global__ void k_face_correct(const RunDesc* runs, const int4* items, int nitem
     if (R.cnt[C_FAILED]) continue;
     const int nx = R.nx, ny = R.ny, nz = R.nz, layer = R.layer, i0 = items[it].y * CHUNK, i1 = min(R.n, i0 + CHUNK);
     const float *u = field(R, set, U), *v = field(R, set, V), *w = field(R, set, W), *phi = R.phi;
-    float *mx = R.faces, *my = R.faces + R.n, *mz = R.faces + 2 * R.n, *dv = R.faces + 3 * R.n;
+    float4* F4 = reinterpret_cast<float4*>(R.faces);
     for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
       int z = i / layer, c = i - z * layer, y = c / nx, x = c - y * nx, l = z * layer;
       int ie = wrap(x + 1, nx) + y * nx + l, iw = wrap(x - 1, nx) + y * nx + l, in = x + wrap(y + 1, ny) * nx + l, is = x + wrap(y - 1, ny) * nx + l;
@@ -323,8 +323,7 @@ __global__ void k_face_correct(const RunDesc* runs, const int4* items, int nitem
       float fyS = rho * (.5f * (v[is] + v[i]) - (p0 - phi[is]) * R.inv_dy);
       float fzU = z < nz - 1 ? lvl(R, L_RUP, z) * (.5f * (w[i] + w[i + layer]) - (phi[i + layer] - p0) * lvl(R, L_INV_DZS, z)) : 0.f;
       float fzD = z > 0 ? lvl(R, L_RUP, z - 1) * (.5f * (w[i - layer] + w[i]) - (p0 - phi[i - layer]) * lvl(R, L_INV_DZS, z - 1)) : 0.f;
-      mx[i] = fxE; my[i] = fyN; mz[i] = fzU;
-      dv[i] = (fxE - fxW) * R.inv_dx + (fyN - fyS) * R.inv_dy + (fzU - fzD) * lvl(R, L_INV_HZ, z);
+      F4[i] = make_float4(fxE, fyN, fzU, (fxE - fxW) * R.inv_dx + (fyN - fyS) * R.inv_dy + (fzU - fzD) * lvl(R, L_INV_HZ, z));
     }
   }
 }
@@ -376,99 +375,164 @@ __global__ void k_pres_correct(const RunDesc* runs, const int4* items, int nitem
 // the flux-form WENO5 (monotone fields) or linear fifth-order upwind reconstruction on the projected face fluxes
 // (FluxTransport.tendency, src/core/advection.ts:274-378), w with the stage buoyancy (stageBuoyancy, model.ts:1204),
 // theta' with the base profile's own vertical flux tendency, then the RK3 update a = start + f dt tend (:1250) and,
-// before a stage projection, w = 0 on the ground and the top (:1045). The column's own values z-3..z+3 live in
-// registers; the current plane with a 3-node halo in shared memory; each x and y face is reconstructed once.
-__device__ __forceinline__ float recon(bool mono, float a, float b, float c, float d, float e) {
-  return mono ? weno5(a, b, c, d, e) : upwind5(a, b, c, d, e);
+// before a stage projection, w = 0 on the ground and the top (:1045).
+// Layout of the march: the column's own values z-3..z+3 live in registers (the vertical faces); the current plane
+// with a 3-node halo in shared memory (the x and y faces, each reconstructed once and exchanged through shared
+// memory); the next level's plane, faces, start value and (w) buoyancy inputs are loaded while the current level
+// computes; one barrier per level (double-buffered plane and face arrays); per-level constants staged once per item.
+enum TKind { TK_WENO = 0, TK_LIN = 1, TK_W = 2, TK_TH = 3 };
+constexpr int TMAXC = 4;  // halo-plane cells per thread: (TX + 6)(TY + 6) <= TMAXC * TX * TY
+constexpr int TLV = 9;    // per-level constants staged: 1/hz, 1/rho, theta faces x4, thb, qb, thv_env
+
+template <int KIND>
+__device__ __forceinline__ float trecon(float a, float b, float c, float d, float e) {
+  if (KIND == TK_WENO) return weno5(a, b, c, d, e);
+  return upwind5(a, b, c, d, e);
 }
+
+template <int KIND>
+__device__ __forceinline__ void transport_item(const RunDesc& Rg, int f, int tile, int in_set, int out_set, float frac, int stage,
+                                               int TX, int TY, float* sm) {
+  const int nx = Rg.nx, ny = Rg.ny, nz = Rg.nz, layer = Rg.layer;
+  const size_t n = Rg.n;
+  const float inv_dx = Rg.inv_dx, inv_dy = Rg.inv_dy, fdt = frac * Rg.dt;
+  const int flags = Rg.flags;
+  const float* __restrict__ q = Rg.fld + ((size_t)in_set * NF + f) * n;
+  const float* __restrict__ st = Rg.fld + (size_t)f * n;
+  float* __restrict__ out = Rg.fld + ((size_t)out_set * NF + f) * n;
+  const float4* __restrict__ F4 = reinterpret_cast<const float4*>(Rg.faces);
+  const float* __restrict__ inb = Rg.fld + (size_t)in_set * NF * n;  // the input set's fields (buoyancy)
+  const int PW = TX + 6, PH = TY + 6, NCELL = PW * PH, NT = TX * TY;
+  float* lv = sm;                                  // [TLV][MAXNZ]
+  float* plane = lv + TLV * MAXNZ;                 // [2][PH][PW]
+  float* fxs = plane + 2 * NCELL;                  // [2][TY][TX + 1]
+  float* fys = fxs + 2 * TY * (TX + 1);            // [2][TY + 1][TX]
+  const int t = threadIdx.x, lx = t % TX, ly = t / TX;
+  const int tilesX = (nx + TX - 1) / TX, x0 = (tile % tilesX) * TX, y0 = (tile / tilesX) * TY;
+  const int x = x0 + lx, y = y0 + ly;
+  const bool on = t < NT && x < nx && y < ny;
+  const int col = on ? x + y * nx : 0;
+  for (int z = t; z < nz; z += blockDim.x) {
+    lv[0 * MAXNZ + z] = lvl(Rg, L_INV_HZ, z);
+    lv[1 * MAXNZ + z] = lvl(Rg, L_INV_RHO, z);
+    if (KIND == TK_TH) {
+      lv[2 * MAXNZ + z] = lvl(Rg, L_TH_UP_POS, z); lv[3 * MAXNZ + z] = lvl(Rg, L_TH_UP_NEG, z);
+      lv[4 * MAXNZ + z] = lvl(Rg, L_TH_DN_POS, z); lv[5 * MAXNZ + z] = lvl(Rg, L_TH_DN_NEG, z);
+    }
+    if (KIND == TK_W) { lv[6 * MAXNZ + z] = lvl(Rg, L_THB, z); lv[7 * MAXNZ + z] = lvl(Rg, L_QB, z); lv[8 * MAXNZ + z] = lvl(Rg, L_THVENV, z); }
+  }
+  // halo-plane cells of this thread, as column offsets (periodic)
+  int off[TMAXC], cell[TMAXC];
+#pragma unroll
+  for (int j = 0; j < TMAXC; j++) {
+    int e = t + j * blockDim.x;
+    cell[j] = e < NCELL ? e : -1;
+    int hy = e / PW, hx = e - hy * PW;
+    int gx = x0 + hx - 3, gy = y0 + hy - 3;
+    gx = ((gx % nx) + nx) % nx; gy = ((gy % ny) + ny) % ny;
+    off[j] = e < NCELL ? gx + gy * nx : 0;
+  }
+  const int offW = on ? wrap(x - 1, nx) + y * nx : 0, offS = on ? x + wrap(y - 1, ny) * nx : 0;
+  const bool loadBuoy = KIND == TK_W && (flags & RF_STAGES);
+  const bool loading = flags & RF_LOADING;
+  // prologue: plane 0, the column window, level 0's inputs
+  float win[7];
+#pragma unroll
+  for (int j = 0; j < 7; j++) win[j] = on ? q[col + clampi(j - 3, 0, nz - 1) * layer] : 0.f;
+#pragma unroll
+  for (int j = 0; j < TMAXC; j++) if (cell[j] >= 0) plane[cell[j]] = q[off[j]];
+  float4 fc = on ? F4[col] : make_float4(0.f, 0.f, 0.f, 0.f);
+  float mw = on && lx == 0 ? F4[offW].x : 0.f, ms = on && ly == 0 ? F4[offS].y : 0.f;
+  float s0 = on && stage > 0 ? st[col] : 0.f;
+  float b[8];
+#pragma unroll
+  for (int j = 0; j < 8; j++) b[j] = 0.f;
+  if (loadBuoy && on) { b[0] = inb[THETA * n + col]; b[1] = inb[Q * n + col]; b[2] = inb[CLOUD * n + col]; b[3] = inb[ICE * n + col];
+    if (loading) { b[4] = inb[RAIN * n + col]; b[5] = inb[SNOW * n + col]; b[6] = inb[GRAUPEL * n + col]; b[7] = inb[HAIL * n + col]; } }
+  __syncthreads();
+  float fzD = 0.f, mzD = 0.f;
+  for (int z = 0; z < nz; z++) {
+    const int buf = z & 1, l = z * layer;
+    const bool more = z + 1 < nz;
+    const int ln = l + layer;
+    // loads for level z + 1 (issued before this level's arithmetic)
+    float pn[TMAXC];
+#pragma unroll
+    for (int j = 0; j < TMAXC; j++) pn[j] = (more && cell[j] >= 0) ? q[off[j] + ln] : 0.f;
+    float4 fcn = make_float4(0.f, 0.f, 0.f, 0.f);
+    float mwn = 0.f, msn = 0.f, s0n = 0.f, qn = 0.f, bn[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) bn[j] = 0.f;
+    if (on) {
+      qn = q[col + min(z + 4, nz - 1) * layer];
+      if (more) {
+        fcn = F4[col + ln];
+        if (lx == 0) mwn = F4[offW + ln].x;
+        if (ly == 0) msn = F4[offS + ln].y;
+        if (stage > 0) s0n = st[col + ln];
+        if (loadBuoy) { bn[0] = inb[THETA * n + col + ln]; bn[1] = inb[Q * n + col + ln]; bn[2] = inb[CLOUD * n + col + ln]; bn[3] = inb[ICE * n + col + ln];
+          if (loading) { bn[4] = inb[RAIN * n + col + ln]; bn[5] = inb[SNOW * n + col + ln]; bn[6] = inb[GRAUPEL * n + col + ln]; bn[7] = inb[HAIL * n + col + ln]; } }
+      }
+    }
+    // faces of level z
+    float fzU = 0.f;
+    const float m3 = fc.z;
+    if (on) {
+      const float* P = plane + buf * NCELL + (ly + 3) * PW + (lx + 3);
+      float* FX = fxs + buf * TY * (TX + 1) + ly * (TX + 1) + lx;
+      float* FY = fys + buf * (TY + 1) * TX + ly * TX + lx;
+      const float m1 = fc.x, m2 = fc.y;
+      FX[1] = m1 >= 0.f ? m1 * trecon<KIND>(P[-2], P[-1], P[0], P[1], P[2]) : m1 * trecon<KIND>(P[3], P[2], P[1], P[0], P[-1]);
+      if (lx == 0) FX[0] = mw >= 0.f ? mw * trecon<KIND>(P[-3], P[-2], P[-1], P[0], P[1]) : mw * trecon<KIND>(P[2], P[1], P[0], P[-1], P[-2]);
+      FY[TX] = m2 >= 0.f ? m2 * trecon<KIND>(P[-2 * PW], P[-PW], P[0], P[PW], P[2 * PW]) : m2 * trecon<KIND>(P[3 * PW], P[2 * PW], P[PW], P[0], P[-PW]);
+      if (ly == 0) FY[0] = ms >= 0.f ? ms * trecon<KIND>(P[-3 * PW], P[-2 * PW], P[-PW], P[0], P[PW]) : ms * trecon<KIND>(P[2 * PW], P[PW], P[0], P[-PW], P[-2 * PW]);
+      if (z < nz - 1) fzU = m3 >= 0.f ? m3 * trecon<KIND>(win[1], win[2], win[3], win[4], win[5]) : m3 * trecon<KIND>(win[6], win[5], win[4], win[3], win[2]);
+    }
+    if (more) {
+#pragma unroll
+      for (int j = 0; j < TMAXC; j++) if (cell[j] >= 0) plane[(buf ^ 1) * NCELL + cell[j]] = pn[j];
+    }
+    __syncthreads();
+    if (on) {
+      const float* FX = fxs + buf * TY * (TX + 1) + ly * (TX + 1) + lx;
+      const float* FY = fys + buf * (TY + 1) * TX + ly * TX + lx;
+      const float qc = win[3], ihz = lv[z], irho = lv[MAXNZ + z];
+      float flux = (FX[1] - FX[0]) * inv_dx + (FY[TX] - FY[0]) * inv_dy + (fzU - fzD) * ihz;
+      float tend = -(flux - qc * fc.w) * irho;
+      if (KIND == TK_TH) {
+        float up = m3 * (m3 >= 0.f ? lv[2 * MAXNZ + z] : lv[3 * MAXNZ + z]);
+        float dn = mzD * (mzD >= 0.f ? lv[4 * MAXNZ + z] : lv[5 * MAXNZ + z]);
+        tend -= (up - dn) * ihz * irho;
+      }
+      if (KIND == TK_W && loadBuoy) {
+        // g B with theta' and the base state (stageBuoyancy): theta_v - theta_v,env from small differences.
+        const float Rb = lv[6 * MAXNZ + z], Qb = lv[7 * MAXNZ + z];
+        float dth = b[0], num = dth + .61f * ((Rb + dth) * (b[1] - Qb) + Qb * dth);
+        float loaded = b[2] + b[3] + (loading ? (b[4] + b[5]) + (b[6] + b[7]) : 0.f);
+        tend += 9.81f * (num / lv[8 * MAXNZ + z] - loaded);
+      }
+      float a = (stage == 0 ? qc : s0) + fdt * tend;
+      if (KIND == TK_W && stage < 2 && (flags & RF_STAGES) && (z == 0 || z == nz - 1)) a = 0.f;
+      out[col + l] = a;
+    }
+    fzD = fzU; mzD = m3;
+#pragma unroll
+    for (int j = 0; j < 6; j++) win[j] = win[j + 1];
+    win[6] = qn; fc = fcn; mw = mwn; ms = msn; s0 = s0n;
+#pragma unroll
+    for (int j = 0; j < 8; j++) b[j] = bn[j];
+  }
+  __syncthreads();
+}
+
+template <int KIND>
 __global__ void __launch_bounds__(512) k_transport(const RunDesc* runs, const int4* items, int nitems, int in_set, int out_set,
                                                     float frac, int stage, int TX, int TY) {
   extern __shared__ float sm[];
-  const int PW = TX + 6, PH = TY + 6;
-  float* plane = sm;                       // [PH][PW]
-  float* fxs = sm + PW * PH;               // [TY][TX + 1]
-  float* fys = fxs + TY * (TX + 1);        // [TY + 1][TX]
-  const int t = threadIdx.x, lx = t % TX, ly = t / TX;
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
     if (R.cnt[C_FAILED]) continue;
-    const int f = items[it].y, tile = items[it].z;
-    const int nx = R.nx, ny = R.ny, nz = R.nz, layer = R.layer;
-    const int tilesX = (nx + TX - 1) / TX, x0 = (tile % tilesX) * TX, y0 = (tile / tilesX) * TY;
-    const int x = x0 + lx, y = y0 + ly;
-    const bool on = x < nx && y < ny;
-    const bool mono = monotone(f);
-    const float* q = field(R, in_set, f);
-    const float* st = field(R, 0, f);
-    float* out = field(R, out_set, f);
-    const float *mx = R.faces, *my = R.faces + R.n, *mz = R.faces + 2 * R.n, *dv = R.faces + 3 * R.n;
-    const int col = (on ? x + y * nx : 0);
-    float win[7];
-#pragma unroll
-    for (int j = 0; j < 7; j++) win[j] = on ? q[col + clampi(j - 3, 0, nz - 1) * layer] : 0.f;
-    float fzD = 0.f, mzD = 0.f;
-    for (int z = 0; z < nz; z++) {
-      const int l = z * layer;
-      // the plane with its halo, periodic in x and y
-      for (int e = t; e < PW * PH; e += blockDim.x) {
-        int hy = e / PW, hx = e - hy * PW;
-        int gx = wrap(x0 + hx - 3, nx), gy = wrap(y0 + hy - 3, ny);
-        gx = gx < 0 ? gx + nx : (gx >= nx ? gx - nx : gx);  // tiles wider than nx wrap twice at most
-        gy = gy < 0 ? gy + ny : (gy >= ny ? gy - ny : gy);
-        plane[e] = q[gx + gy * nx + l];
-      }
-      __syncthreads();
-      float fzU = 0.f, m3 = 0.f;
-      if (on) {
-        const int i = col + l;
-        const float* P = plane + (ly + 3) * PW + (lx + 3);
-        float m1 = mx[i];
-        float fe = m1 >= 0.f ? m1 * recon(mono, P[-2], P[-1], P[0], P[1], P[2]) : m1 * recon(mono, P[3], P[2], P[1], P[0], P[-1]);
-        fxs[ly * (TX + 1) + lx + 1] = fe;
-        if (lx == 0) {
-          float mw = mx[wrap(x - 1, nx) + y * nx + l];
-          fxs[ly * (TX + 1)] = mw >= 0.f ? mw * recon(mono, P[-3], P[-2], P[-1], P[0], P[1]) : mw * recon(mono, P[2], P[1], P[0], P[-1], P[-2]);
-        }
-        float m2 = my[i];
-        fys[(ly + 1) * TX + lx] = m2 >= 0.f ? m2 * recon(mono, P[-2 * PW], P[-PW], P[0], P[PW], P[2 * PW]) : m2 * recon(mono, P[3 * PW], P[2 * PW], P[PW], P[0], P[-PW]);
-        if (ly == 0) {
-          float ms = my[x + wrap(y - 1, ny) * nx + l];
-          fys[lx] = ms >= 0.f ? ms * recon(mono, P[-3 * PW], P[-2 * PW], P[-PW], P[0], P[PW]) : ms * recon(mono, P[2 * PW], P[PW], P[0], P[-PW], P[-2 * PW]);
-        }
-        m3 = mz[i];
-        if (z < nz - 1) fzU = m3 >= 0.f ? m3 * recon(mono, win[1], win[2], win[3], win[4], win[5]) : m3 * recon(mono, win[6], win[5], win[4], win[3], win[2]);
-      }
-      __syncthreads();
-      if (on) {
-        const int i = col + l;
-        const float qc = win[3];
-        float flux = (fxs[ly * (TX + 1) + lx + 1] - fxs[ly * (TX + 1) + lx]) * R.inv_dx + (fys[(ly + 1) * TX + lx] - fys[ly * TX + lx]) * R.inv_dy +
-                     (fzU - fzD) * lvl(R, L_INV_HZ, z);
-        float tend = -(flux - qc * dv[i]) * lvl(R, L_INV_RHO, z);
-        if (f == THETA) {
-          float up = m3 * (m3 >= 0.f ? lvl(R, L_TH_UP_POS, z) : lvl(R, L_TH_UP_NEG, z));
-          float dn = mzD * (mzD >= 0.f ? lvl(R, L_TH_DN_POS, z) : lvl(R, L_TH_DN_NEG, z));
-          tend -= (up - dn) * lvl(R, L_INV_HZ, z) * lvl(R, L_INV_RHO, z);
-        } else if (f == W && (R.flags & RF_STAGES)) {
-          // g B with theta' and the base state (stageBuoyancy): theta_v - theta_v,env from small differences.
-          const float* th = field(R, in_set, THETA);
-          float dth = th[i], qq = field(R, in_set, Q)[i], Rb = lvl(R, L_THB, z), Qb = lvl(R, L_QB, z);
-          float num = dth + .61f * ((Rb + dth) * (qq - Qb) + Qb * dth);
-          float loaded = field(R, in_set, CLOUD)[i] + field(R, in_set, ICE)[i];
-          if (R.flags & RF_LOADING) loaded += field(R, in_set, RAIN)[i] + field(R, in_set, SNOW)[i] + field(R, in_set, GRAUPEL)[i] + field(R, in_set, HAIL)[i];
-          tend += 9.81f * (num / lvl(R, L_THVENV, z) - loaded);
-        }
-        float s0 = stage == 0 ? qc : st[i];
-        float a = s0 + (frac * R.dt) * tend;
-        if (f == W && stage < 2 && (R.flags & RF_STAGES) && (z == 0 || z == nz - 1)) a = 0.f;
-        out[i] = a;
-      }
-      fzD = fzU; mzD = m3;
-#pragma unroll
-      for (int j = 0; j < 6; j++) win[j] = win[j + 1];
-      if (on) win[6] = q[col + min(z + 4, nz - 1) * layer];
-    }
-    __syncthreads();
+    transport_item<KIND>(R, items[it].y, items[it].z, in_set, out_set, frac, stage, TX, TY, sm);
   }
 }
 
@@ -605,13 +669,20 @@ __global__ void k_viscosity(const RunDesc* runs, const int4* items, int nitems, 
           const float LV = 2.5e6f, RD = 287.05f, CP = 1004.f, EPS = .622f;
           float t = Ti * lvl(R, L_EXNER, z), qs = qv[i];
           float factor = (1.f + LV * qs / (RD * t)) / (1.f + EPS * LV * LV * qs / (CP * RD * t * t));
-          n2 = 9.81f * (factor * ((Tu - Td) / Ti + LV / (CP * t) * (qv[i + up] - qv[i + dn])) - (qv[i + up] + condU - qv[i + dn] - condD)) * isp;
+          float dT = (th[i + up] - th[i + dn]) + lvl(R, L_DTHB, z);
+          n2 = 9.81f * (factor * (dT / Ti + LV / (CP * t) * (qv[i + up] - qv[i + dn])) - ((qv[i + up] - qv[i + dn]) + (condU - condD))) * isp;
         } else {
+          // g / theta_e d theta_e / dz with theta_e = theta exp(L q / (cp theta pi)). The difference of the two
+          // theta_e values (~330 K) is formed without cancellation: (theta_u - theta_d) e^xu + theta_d e^xd expm1(xu - xd),
+          // theta_u - theta_d from the departures and the base profile's own difference.
           const float L_CP = 2.5e6f / 1004.f;
-          float ti = Ti * expf(L_CP * qv[i] / (Ti * lvl(R, L_EXNER, z)));
-          float tu = Tu * expf(L_CP * qv[i + up] / (Tu * lvl(R, L_EXNER, zu)));
-          float td = Td * expf(L_CP * qv[i + dn] / (Td * lvl(R, L_EXNER, zd)));
-          n2 = 9.81f / ti * (tu - td) * isp;
+          float xi = L_CP * qv[i] / (Ti * lvl(R, L_EXNER, z));
+          float xu = L_CP * qv[i + up] / (Tu * lvl(R, L_EXNER, zu));
+          float xd = L_CP * qv[i + dn] / (Td * lvl(R, L_EXNER, zd));
+          float dT = (th[i + up] - th[i + dn]) + lvl(R, L_DTHB, z);
+          float eu = expf(xu), ed = expf(xd);
+          float dte = dT * eu + Td * ed * expm1f(xu - xd);
+          n2 = 9.81f / (Ti * expf(xi)) * dte * isp;
         }
       }
       float rate = sqrtf(fmaxf(0.f, s2 - 3.f * n2));
@@ -736,9 +807,16 @@ void launch_proj_xifft(const Launch& L, int mode, int yc, int maxnx) {
 }
 void launch_face_correct(const Launch& L, int set) { k_face_correct<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set); }
 void launch_pres_correct(const Launch& L, int set, int final_) { k_pres_correct<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set, final_); }
-void launch_transport(const Launch& L, int in_set, int out_set, float frac, int stage, int TX, int TY) {
-  size_t smem = ((size_t)(TX + 6) * (TY + 6) + (size_t)TY * (TX + 1) + (size_t)(TY + 1) * TX) * sizeof(float);
-  k_transport<<<GRID(L.n, L.cap), TX * TY, smem, L.stream>>>(L.runs, L.items, L.n, in_set, out_set, frac, stage, TX, TY);
+void launch_transport(const Launch& L, int kind, int in_set, int out_set, float frac, int stage, int TX, int TY) {
+  if (L.n == 0) return;
+  size_t smem = ((size_t)TLV * MAXNZ + 2 * (size_t)(TX + 6) * (TY + 6) + 2 * (size_t)TY * (TX + 1) + 2 * (size_t)(TY + 1) * TX) * sizeof(float);
+  dim3 g = GRID(L.n, L.cap);
+  switch (kind) {
+    case TK_WENO: k_transport<TK_WENO><<<g, TX * TY, smem, L.stream>>>(L.runs, L.items, L.n, in_set, out_set, frac, stage, TX, TY); break;
+    case TK_LIN: k_transport<TK_LIN><<<g, TX * TY, smem, L.stream>>>(L.runs, L.items, L.n, in_set, out_set, frac, stage, TX, TY); break;
+    case TK_W: k_transport<TK_W><<<g, TX * TY, smem, L.stream>>>(L.runs, L.items, L.n, in_set, out_set, frac, stage, TX, TY); break;
+    default: k_transport<TK_TH><<<g, TX * TY, smem, L.stream>>>(L.runs, L.items, L.n, in_set, out_set, frac, stage, TX, TY); break;
+  }
 }
 void launch_fill_partial(const Launch& L, int set) { k_fill_partial<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set); }
 void launch_fill_final(const Launch& L) { k_fill_final<<<GRID(L.n, L.cap), 32, 0, L.stream>>>(L.runs, L.items, L.n); }
@@ -754,7 +832,10 @@ cudaError_t set_smem_limits(int bytes) {
   if ((e = cudaFuncSetAttribute(k_proj_div_xfft, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
   if ((e = cudaFuncSetAttribute(k_proj_xifft, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
   if ((e = cudaFuncSetAttribute(k_sediment, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(k_transport, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(k_transport<TK_WENO>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(k_transport<TK_LIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(k_transport<TK_W>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(k_transport<TK_TH>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
   return cudaSuccess;
 }
 

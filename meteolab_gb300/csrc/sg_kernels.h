@@ -24,7 +24,8 @@ void launch_proj_modes(const Launch& L, int mode, int maxnz, int maxny, int thre
 void launch_proj_xifft(const Launch& L, int mode, int yc, int maxnx);
 void launch_face_correct(const Launch& L, int set);
 void launch_pres_correct(const Launch& L, int set, int final_);
-void launch_transport(const Launch& L, int in_set, int out_set, float frac, int stage, int TX, int TY);
+// kind: 0 WENO fields, 1 u and v, 2 w, 3 theta (the item list of that kind)
+void launch_transport(const Launch& L, int kind, int in_set, int out_set, float frac, int stage, int TX, int TY);
 void launch_fill_partial(const Launch& L, int set);
 void launch_fill_final(const Launch& L);
 void launch_physics(const Launch& L, int in, int mid);

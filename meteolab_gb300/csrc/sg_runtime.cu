@@ -56,7 +56,7 @@ struct Run {
 struct Plan {
   std::vector<int> slots;
   int4* items = nullptr;  // device
-  int off[8] = {0}, cnt[8] = {0};
+  int off[16] = {0}, cnt[16] = {0};
   int maxnx = 0, maxny = 0, maxnz = 0, TX = 40, TY = 8;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -66,7 +66,7 @@ struct Plan {
     if (items) cudaFree(items);
   }
 };
-enum Family { FAM_NODE, FAM_COLS, FAM_ROWS_FACE, FAM_ROWS_PRES, FAM_MODES, FAM_TILES, FAM_RUNS, FAM_CELLS, FAM_COUNT };
+enum Family { FAM_NODE, FAM_COLS, FAM_ROWS_FACE, FAM_ROWS_PRES, FAM_MODES, FAM_RUNS, FAM_CELLS, FAM_T_WENO, FAM_T_LIN, FAM_T_W, FAM_T_TH, FAM_COUNT };
 
 }  // namespace
 
@@ -242,9 +242,11 @@ int build_plan(sg_context* ctx, const std::vector<int>& slots, Plan& P) {
     if (r.nx % 40) all40 = false;
     if (r.ny % 8) all8 = false;
   }
-  // Tile of the transport: 40 x 8 columns on the benchmark grids (40, 80, 320 wide), else 32 x 8.
-  P.TX = all40 ? 40 : std::min(32, P.maxnx);
-  P.TY = all8 ? 8 : std::min(8, P.maxny);
+  // Tile of the transport: 40 x 8 columns on the benchmark grids (40, 80, 320 wide), else 32 x 8 (a tile may be wider
+  // than a small grid: its halo wraps periodically and the threads beyond the grid only load).
+  (void)all8;
+  P.TX = all40 ? 40 : 32;
+  P.TY = 8;
   for (int s : slots) {
     const Run& r = ctx->runs[s];
     int n = r.nx * r.ny * r.nz, nch = (n + CHUNK - 1) / CHUNK, layer = r.nx * r.ny;
@@ -256,7 +258,10 @@ int build_plan(sg_context* ctx, const std::vector<int>& slots, Plan& P) {
     for (int k = 0; k < r.nz - 1; k++) for (int y = 0; y < r.ny; y += YC) all[FAM_ROWS_PRES].push_back(make_int4(s, k, y, 0));
     for (int m = 0; m < r.nx / 2 + 1; m++) all[FAM_MODES].push_back(make_int4(s, m, 0, 0));
     int tiles = ((r.nx + P.TX - 1) / P.TX) * ((r.ny + P.TY - 1) / P.TY);
-    for (int f = 0; f < NF; f++) for (int t = 0; t < tiles; t++) all[FAM_TILES].push_back(make_int4(s, f, t, 0));
+    for (int f = 0; f < NF; f++) {
+      int fam = f == W ? FAM_T_W : f == THETA ? FAM_T_TH : (f == U || f == V) ? FAM_T_LIN : FAM_T_WENO;
+      for (int t = 0; t < tiles; t++) all[fam].push_back(make_int4(s, f, t, 0));
+    }
     all[FAM_RUNS].push_back(make_int4(s, 0, 0, 0));
   }
   std::vector<int4> flat;
@@ -278,7 +283,8 @@ template <class Hook>
 void enqueue_part(sg_context* ctx, const Plan& P, int part, Hook hook) {
   const int A = 0, B = 1, C = 2;
   Launch node = lx(ctx, P, FAM_NODE), cols = lx(ctx, P, FAM_COLS), rf = lx(ctx, P, FAM_ROWS_FACE), rp = lx(ctx, P, FAM_ROWS_PRES);
-  Launch modes = lx(ctx, P, FAM_MODES, 2), tiles = lx(ctx, P, FAM_TILES, 4), runs = lx(ctx, P, FAM_RUNS);
+  Launch modes = lx(ctx, P, FAM_MODES, 2), runs = lx(ctx, P, FAM_RUNS);
+  Launch tk[4] = {lx(ctx, P, FAM_T_WENO, 4), lx(ctx, P, FAM_T_LIN, 4), lx(ctx, P, FAM_T_W, 4), lx(ctx, P, FAM_T_TH, 4)};
   const int mthreads = std::min(512, std::max(128, P.maxny));
   auto project = [&](int set, int final_) {
     launch_proj_div_xfft(rp, PROJ_PRES, set, YC, P.maxnx); hook(7);
@@ -296,7 +302,7 @@ void enqueue_part(sg_context* ctx, const Plan& P, int part, Hook hook) {
     launch_face_correct(node, A); hook(5);
     const int in[3] = {A, B, C}, out[3] = {B, C, B};
     for (int s = 0; s < 3; s++) {
-      launch_transport(tiles, in[s], out[s], (float)RK3[s], s, P.TX, P.TY); hook(6);
+      for (int k = 0; k < 4; k++) if (tk[k].n) { launch_transport(tk[k], k, in[s], out[s], (float)RK3[s], s, P.TX, P.TY); hook(6); }
       if (s < 2) project(out[s], 0);
     }
   } else if (part == 3) {

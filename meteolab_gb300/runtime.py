@@ -255,9 +255,9 @@ class Run:
         return out
 
     def debug_faces(self) -> np.ndarray:
-        out = np.empty((4, self.grid.n), np.float32)
+        out = np.empty((self.grid.n, 4), np.float32)
         self.ctx.check(load().sg_debug_read_faces(self.ctx.h, self.id, out.ctypes.data_as(_FP)), "read faces")
-        return out
+        return out.T.copy()  # mx, my, mz, div
 
     def divergence(self) -> float:
         out = C.c_double()
