@@ -26,7 +26,11 @@ sys.path.insert(0, ROOT)
 
 METRIC = "cell-steps/s batched vs plain GPU step at <=1e-5 rel-L2; serve p50/p99 s/run"
 MEMBERS = 64
-TRANSPORT_BYTES_PER_CELL = (30 * 4 + 43 * 4 + 43 * 4) / 3  # mean algorithmic bytes per cell of one RK3 transport launch
+# The dominant kernel: the WENO5 transport of the 9 monotone fields (rain, snow, graupel, hail, q, cloud, ice,
+# iceNumber, cold), one launch per RK3 stage. Algorithmic bytes per cell and launch: each field read once and written
+# once (4 + 4 B), the step-start value read in stages 2 and 3 (4 B), the projected face fluxes (mx, my, mz, div: 16 B);
+# mean over the three stages = (9 * 8 + 16 + 2 * (9 * 12 + 16)) / 3.
+TRANSPORT_BYTES_PER_CELL = (9 * 8 + 16 + 2 * (9 * 12 + 16)) / 3
 
 
 def parse():
@@ -211,7 +215,7 @@ def main():
     # ---- kernel profile (eager, CUDA events per launch) and the roofline of the transport
     prof = ctx.profile(runs, 2)
     hbm, peak_kind = peaks()
-    tr_ms = prof.get("transport", (None, 0))[0]
+    tr_ms = prof.get("transport_weno", (None, 0))[0]
     achieved = cells * TRANSPORT_BYTES_PER_CELL / (tr_ms * 1e-3) / 1e9 if tr_ms else None
     tpc = traffic_per_cell()
     launches_per_step = sum(v[1] for v in prof.values())
@@ -266,7 +270,7 @@ def main():
         "e2e": {"value": e2e_value, "unit": "cell-steps/s", "h2d_bytes_per_step": bytes_io, "d2h_bytes_per_step": bytes_io},
         "gpu_launches": launches_per_step * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm if achieved else None,
-                     "traffic": tpc * cells if tpc else None, "kernel": "transport", "peak_kind": peak_kind,
+                     "traffic": tpc * cells if tpc else None, "kernel": "k_transport<WENO> (9 fields, one RK3 stage)", "peak_kind": peak_kind,
                      "bytes_per_cell_per_launch": TRANSPORT_BYTES_PER_CELL},
         "cpu_baseline": cpu,
         "clocks": clk.summary(),

@@ -48,6 +48,8 @@ enum Level {
   L_NODEMASS,                                           // dx dy hz rho (water budget)
   L_LW,                                                 // level weight hz/dz rho (positivity fix)
   L_SURF,                                               // surface flux share per metre (sharesAbove)
+  L_TCB,                                                // theta_b exner - 273.15 (Celsius base temperature)
+  L_QW_HI, L_QW_LO, L_BW, L_QI_HI, L_QI_LO, L_BI, L_Q0_HI, L_Q0_LO,  // saturation bases (sg_physics.cuh Level)
   L_COUNT
 };
 // Per-level FP64 constants.

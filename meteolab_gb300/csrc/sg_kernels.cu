@@ -13,6 +13,7 @@
 //   step_end                                      budgets and counters
 #include <cuda_runtime.h>
 #include <math.h>
+#include <algorithm>
 #include "sg_common.cuh"
 #include "sg_fft.cuh"
 #include "sg_physics.cuh"
@@ -216,50 +217,46 @@ __global__ void k_proj_div_xfft(const RunDesc* runs, const int4* items, int nite
 // modes zero), the inverse y-transform. FACE: rows -rho h lambda + vertical faces (src/core/advection.ts:222-241);
 // PRES: the density-weighted consistent Laplacian (src/core/pressure.ts:104-140).
 constexpr int MAXNZ = 128;
-constexpr int MODE_GROUP = 8;
-__global__ void k_proj_modes(const RunDesc* runs, const int4* items, int nitems, int mode) {
+// `group`: layers per y-transform pass (all of them when the scratch fits in shared memory).
+__global__ void k_proj_modes(const RunDesc* runs, const int4* items, int nitems, int mode, int group) {
   extern __shared__ float2 smc[];
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
     if (R.cnt[C_FAILED]) continue;
     const int m = items[it].y, ny = R.ny, nz = R.nz, nzc = mode == PROJ_FACE ? nz : nz - 1;
     float2* S = smc;                   // [nzc][ny]
-    float2* T = smc + nzc * ny;        // [MODE_GROUP][ny] scratch
+    float2* T = smc + nzc * ny;        // [group][ny] scratch
     float2* g = R.spec + (size_t)m * nzc * ny;
     for (int e = threadIdx.x; e < nzc * ny; e += blockDim.x) S[e] = g[e];
     __syncthreads();
     FftPlan P{ny, R.fy_nf, R.fy_rad, R.twy};
-    for (int k0 = 0; k0 < nzc; k0 += MODE_GROUP) {
-      int rows = min(MODE_GROUP, nzc - k0);
-      // fft_rows ping-pongs between the slab rows and T; rows stay within this group.
-      fft_rows(S + k0 * ny, T, ny, rows, P);
-    }
+    for (int k0 = 0; k0 < nzc; k0 += group) fft_rows(S + k0 * ny, T, ny, min(group, nzc - k0), P);
+    // One real recurrence per (n, component): the real and imaginary parts share the coefficients.
     const double2* tri = (mode == PROJ_FACE ? R.tri_face : R.tri_pres) + (size_t)m * nzc * ny;
     const double* lv64 = R.lv64;
-    for (int n = threadIdx.x; n < ny; n += blockDim.x) {
-      double2 d[MAXNZ];
+    float* Sf = reinterpret_cast<float*>(S);
+    for (int u = threadIdx.x; u < 2 * ny; u += blockDim.x) {
+      const int n = u >> 1, c = u & 1;
+      double d[MAXNZ];
       double a = 0, b = 0;
       if (mode == PROJ_PRES) { double2 ab = R.ab[m * ny + n]; a = ab.x; b = ab.y; }
-      double pr = 0, pi = 0;
+      double prev = 0;
       for (int k = 0; k < nzc; k++) {
-        double2 f = tri[(size_t)k * ny + n];                         // (1/pivot, cp)
-        float2 r = S[k * ny + n];
-        double rr = r.x, ri = r.y, lo;
-        if (mode == PROJ_FACE) { double h = lv64[D_FHZ * nz + k]; rr *= h; ri *= h; lo = lv64[D_FLO * nz + k]; }
+        const double ip = tri[(size_t)k * ny + n].x;                  // 1 / pivot
+        double r = Sf[2 * (k * ny + n) + c], lo;
+        if (mode == PROJ_FACE) { r *= lv64[D_FHZ * nz + k]; lo = lv64[D_FLO * nz + k]; }
         else lo = a * lv64[D_PL1 * nz + k] + b * lv64[D_PL2 * nz + k];
-        double dr = (rr - lo * pr) * f.x, di = (ri - lo * pi) * f.x;
-        d[k] = make_double2(dr, di); pr = dr; pi = di;
+        prev = (r - lo * prev) * ip;
+        d[k] = prev;
       }
-      double xr = 0, xi = 0;
+      double x = 0;
       for (int k = nzc - 1; k >= 0; k--) {
-        double cp = tri[(size_t)k * ny + n].y;
-        xr = d[k].x - (k < nzc - 1 ? cp * xr : 0.0);
-        xi = d[k].y - (k < nzc - 1 ? cp * xi : 0.0);
-        S[k * ny + n] = make_float2((float)xr, (float)xi);
+        x = k < nzc - 1 ? d[k] - tri[(size_t)k * ny + n].y * x : d[k];
+        Sf[2 * (k * ny + n) + c] = (float)x;
       }
     }
     __syncthreads();
-    for (int k0 = 0; k0 < nzc; k0 += MODE_GROUP) ifft_rows(S + k0 * ny, T, ny, min(MODE_GROUP, nzc - k0), P);
+    for (int k0 = 0; k0 < nzc; k0 += group) ifft_rows(S + k0 * ny, T, ny, min(group, nzc - k0), P);
     for (int e = threadIdx.x; e < nzc * ny; e += blockDim.x) g[e] = S[e];
     __syncthreads();
   }
@@ -540,22 +537,24 @@ __global__ void __launch_bounds__(512) k_transport(const RunDesc* runs, const in
 // Sums of the positivity fix over one chunk of the final RK3 values (fillNegative, src/core/model.ts:606-617):
 // per conserve field, (removed, kept, negative) weighted by the level weight, FP64, in a fixed order.
 __global__ void k_fill_partial(const RunDesc* runs, const int4* items, int nitems, int set) {
-  __shared__ double sh[32 * 3];
+  __shared__ double sh[32 * NCONS * 3];
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
     if (R.cnt[C_FAILED]) continue;
     const int chunk = items[it].y, i0 = chunk * CHUNK, i1 = min(R.n, i0 + CHUNK);
-    for (int k = 0; k < NCONS; k++) {
-      const float* a = field(R, set, cons_field(k));
-      double v[3] = {0, 0, 0};
-      for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-        float x = a[i];
-        double wz = lvl(R, L_LW, i / R.layer);
-        if (x < 1e-10f) { if (x != 0.f) { v[0] += wz * x; if (x < 0.f) v[2] -= wz * x; } }
-        else v[1] += wz * x;
+    double v[NCONS * 3];
+#pragma unroll
+    for (int k = 0; k < NCONS * 3; k++) v[k] = 0;
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+      const double wz = lvl(R, L_LW, i / R.layer);
+#pragma unroll
+      for (int k = 0; k < NCONS; k++) {
+        float x = field(R, set, cons_field(k))[i];
+        if (x < 1e-10f) { if (x != 0.f) { v[3 * k] += wz * x; if (x < 0.f) v[3 * k + 2] -= wz * x; } }
+        else v[3 * k + 1] += wz * x;
       }
-      blockSums<3>(v, R.part + ((size_t)chunk * NCONS + k) * 3, sh);
     }
+    blockSums<NCONS * 3>(v, R.part + (size_t)chunk * NCONS * 3, sh);
   }
 }
 // Per run: the scale of each conserve field, kept as delta = scale - 1 so a * scale rounds once (fma).
@@ -604,12 +603,16 @@ __global__ void k_physics(const RunDesc* runs, const int4* items, int nitems, in
       s.q = fixed(4, field(R, in, Q)[i]); s.cloud = fixed(5, field(R, in, CLOUD)[i]); s.ice = fixed(6, field(R, in, ICE)[i]);
       s.inum = field(R, in, ICENUM)[i];
       s.cold = field(R, in, COLD)[i] * keepCold;
-      s.thp = field(R, in, THETA)[i]; s.thb = lvl(R, L_THB, z);
+      s.thp = field(R, in, THETA)[i]; s.thb = lvl(R, L_THB, z); s.tcb = lvl(R, L_TCB, z);
       float u = field(R, in, U)[i], v = field(R, in, V)[i], w = field(R, in, W)[i];
-      const float exner = lvl(R, L_EXNER, z), p = lvl(R, L_P, z), rho = lvl(R, L_RHO, z);
+      phys::Level pl;
+      pl.exner = lvl(R, L_EXNER, z); pl.p = lvl(R, L_P, z); pl.rho = lvl(R, L_RHO, z); pl.fallsq = lvl(R, L_FALLSQ, z); pl.tcb = s.tcb;
+      pl.qw_hi = lvl(R, L_QW_HI, z); pl.qw_lo = lvl(R, L_QW_LO, z); pl.bw = lvl(R, L_BW, z);
+      pl.qi_hi = lvl(R, L_QI_HI, z); pl.qi_lo = lvl(R, L_QI_LO, z); pl.bi = lvl(R, L_BI, z);
+      pl.q0_hi = lvl(R, L_Q0_HI, z); pl.q0_lo = lvl(R, L_Q0_LO, z);
       const float q0 = s.q;
       float evap;
-      phys::microphysics(s, exner, p, rho, lvl(R, L_FALLSQ, z), dt, R.flags, evap);
+      phys::microphysics(s, pl, dt, R.flags, evap);
       if (!(R.flags & RF_STAGES)) {
         float num = s.thp + .61f * ((s.thb + s.thp) * (s.q - lvl(R, L_QB, z)) + lvl(R, L_QB, z) * s.thp);
         float loaded = s.cloud + s.ice + ((R.flags & RF_LOADING) ? s.rain + s.snow + s.graupel + s.hail : 0.f);
@@ -797,9 +800,13 @@ void launch_proj_div_xfft(const Launch& L, int mode, int set, int yc, int maxnx)
   size_t smem = (size_t)2 * ((yc + 1) / 2) * maxnx * sizeof(float2);
   k_proj_div_xfft<<<GRID(L.n, L.cap), 256, smem, L.stream>>>(L.runs, L.items, L.n, mode, set, yc);
 }
-void launch_proj_modes(const Launch& L, int mode, int maxnz, int maxny, int threads) {
-  size_t smem = (size_t)(maxnz + MODE_GROUP) * maxny * sizeof(float2);
-  k_proj_modes<<<GRID(L.n, L.cap), threads, smem, L.stream>>>(L.runs, L.items, L.n, mode);
+void launch_proj_modes(const Launch& L, int mode, int maxnz, int maxny, int threads, int smem_budget) {
+  // the slab [nz][ny] plus a scratch of `group` layers, all layers at once when they fit
+  size_t slab = (size_t)maxnz * maxny * sizeof(float2);
+  int group = (int)std::min<size_t>(maxnz, (smem_budget - slab) / ((size_t)maxny * sizeof(float2)));
+  group = std::max(group, 1);
+  size_t smem = slab + (size_t)group * maxny * sizeof(float2);
+  k_proj_modes<<<GRID(L.n, L.cap), threads, smem, L.stream>>>(L.runs, L.items, L.n, mode, group);
 }
 void launch_proj_xifft(const Launch& L, int mode, int yc, int maxnx) {
   size_t smem = ((size_t)yc * (maxnx / 2 + 1) + (size_t)2 * ((yc + 1) / 2) * maxnx) * sizeof(float2);

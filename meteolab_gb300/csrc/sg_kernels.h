@@ -20,7 +20,7 @@ void launch_theta_out(const Launch& L, float* dst);
 void launch_fall_courant(const Launch& L);
 void launch_sediment(const Launch& L, int maxnz);
 void launch_proj_div_xfft(const Launch& L, int mode, int set, int yc, int maxnx);
-void launch_proj_modes(const Launch& L, int mode, int maxnz, int maxny, int threads);
+void launch_proj_modes(const Launch& L, int mode, int maxnz, int maxny, int threads, int smem_budget);
 void launch_proj_xifft(const Launch& L, int mode, int yc, int maxnx);
 void launch_face_correct(const Launch& L, int set);
 void launch_pres_correct(const Launch& L, int set, int final_);

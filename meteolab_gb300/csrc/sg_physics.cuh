@@ -1,9 +1,13 @@
 // Bulk microphysics of one node in FP32: warm rain (Kessler), one-moment Lin ice, snow, graupel and hail, the
 // saturation adjustment, secondary ice; each function follows the reference routine it names (file:line) and
-// updates the node in the reference's order. theta is held as its departure `thp` from the level's base value `thb`;
-// a temperature is formed as (thb + thp) * exner where the reference reads theta * exner.
+// updates the node in the reference's order. theta is held as its departure `thp` from the level's base value `thb`.
+// Where the reference reads theta * exner, the Celsius temperature is formed as tcb + thp * exner, tcb = thb * exner
+// - 273.15 of the level from FP64: FP32 resolves it to ~1e-6 K (an FP32 kelvin value near 290 K only to 3e-5 K,
+// which moves the saturation mixing ratio by ~2e-6 of itself and small condensation amounts by up to a percent).
 #pragma once
 #include <math.h>
+#include <algorithm>
+#include <cmath>
 #include "sg_common.cuh"
 
 namespace sg {
@@ -24,7 +28,20 @@ constexpr float SC13 = 0.84343267f;  // 0.6^(1/3)
 
 SG_HD float fclamp(float x, float a, float b) { return fmaxf(a, fminf(b, x)); }
 
-struct Node { float thp, thb, q, cloud, rain, ice, inum, snow, graupel, hail, cold; };
+struct Node { float thp, thb, tcb, q, cloud, rain, ice, inum, snow, graupel, hail, cold; };
+SG_HD float tcOf(const Node& s, float exner) { return s.tcb + s.thp * exner; }
+
+// Saturation about the level's base state. With t = tb + t' (tb = theta_b exner - 273.15 of the level in FP64,
+// t' = theta' exner at the node), es(t) = es(tb) (1 + x), x = expm1(A (t - tb) / ((t + B)(tb + B))) for the Bolton
+// (A = 17.67 * 243.5, B = 243.5) and Alduchov-Eskridge (A = 22.587 * 273.86, B = 273.86) fits, and
+// qs(t) = eps es / (p - es) = qs(tb) (1 + g), g = x (1 + beta) / (1 - beta x), beta = es(tb) / (p - es(tb)): exact
+// identities of the reference's formulas. qs(tb) is an FP32 pair hi + lo from FP64, so q - qs = (q - hi) - (lo + hi g)
+// keeps the digits that matter near saturation (q - qs ~ 1e-6 of q ~ 1e-2) without FP64 on the device.
+struct Level { float exner, p, rho, fallsq, tcb, qw_hi, qw_lo, bw, qi_hi, qi_lo, bi, q0_hi, q0_lo; };
+struct Sat { float hi, corr; };                 // qs = hi + corr
+SG_HD float satv(Sat a) { return a.hi + a.corr; }
+SG_HD float excess(float q, Sat a) { return (q - a.hi) - a.corr; }  // q - qs
+SG_HD float satDiff(Sat a, Sat b) { return (a.hi - b.hi) + (a.corr - b.corr); }  // qs_a - qs_b
 
 SG_HD float qsatP(float t, float p) {  // src/core/microphysics.ts:5
   float es = 611.2f * expf(17.67f * t / (t + 243.5f));
@@ -35,6 +52,27 @@ SG_HD float qsatIce(float t, float p) {  // src/core/ice.ts:130-134
   float es = 611.21f * expf(22.587f * t / (t + 273.86f));
   return fclamp(EPS * es / fmaxf(1000.f, p - es), 0.f, .045f);
 }
+SG_HD Sat satExpand(float hi, float lo, float beta, float A, float B, float dT, float t, float tcb) {
+  const float x = expm1f(A * dT / ((t + B) * (tcb + B)));
+  const float g = x * (1.f + beta) / (1.f - beta * x);
+  const float v = hi + (lo + hi * g);
+  if (!(v < .045f)) return Sat{.045f, 0.f};   // the reference's upper clamp
+  return Sat{hi, lo + hi * g};
+}
+// Water saturation at the node (qsatP of its temperature); the level's base must be valid (hi >= 0), else direct.
+SG_HD Sat satWater(const Node& s, const Level& L) {
+  const float dT = s.thp * L.exner, t = L.tcb + dT;
+  if (!(L.qw_hi >= 0.f)) return Sat{qsatP(t, L.p), 0.f};
+  return satExpand(L.qw_hi, L.qw_lo, L.bw, 17.67f * 243.5f, 243.5f, dT, t, L.tcb);
+}
+// Ice saturation (qsatIce: over water at and above 0 C).
+SG_HD Sat satIce(const Node& s, const Level& L) {
+  const float dT = s.thp * L.exner, t = L.tcb + dT;
+  if (t >= 0.f) return satWater(s, L);
+  if (!(L.qi_hi >= 0.f)) return Sat{qsatIce(t, L.p), 0.f};
+  return satExpand(L.qi_hi, L.qi_lo, L.bi, 22.587f * 273.86f, 273.86f, dT, t, L.tcb);
+}
+
 // Fall speeds (src/core/microphysics.ts:37, ice.ts:143, graupel.ts:21, hail.ts:102); fallsq = sqrt(rho_ground / rho).
 SG_HD float rainFall(float rain, float rho, float fallsq) { return rain > 0.f ? 36.34f * powf(.001f * rho * rain, .1364f) * fallsq : 0.f; }
 SG_HD float snowFall(float snow, float rho, float fallsq) {
@@ -50,48 +88,52 @@ SG_HD float hailMaxDiameter(float hail, float rho) {  // src/core/hail.ts:107-11
 }
 
 // src/core/microphysics.ts:48-60 (Marshall-Palmer intercept). Returns the evaporated rain.
-SG_HD float rainProcesses(Node& s, float tk, float p, float rho, float dt, bool evaporate) {
+SG_HD float rainProcesses(Node& s, const Level& L, float dt, bool evaporate) {
+  const float tk = tcOf(s, L.exner) + 273.15f, rho = L.rho, p = L.p;
   float qc = s.cloud, qr = s.rain;
   float rate = .001f * fmaxf(0.f, qc - .001f) + (qr > 0.f ? 2.2f * qc * powf(qr, .875f) : 0.f);
   float production = fminf(qc, rate * dt);
   s.cloud -= production; s.rain += production;
-  float qs = qsatP(tk - 273.15f, p);
-  if (!evaporate || s.rain <= 0.f || s.q >= qs) return 0.f;
+  const Sat sw = satWater(s, L);
+  const float qs = satv(sw), ex = excess(s.q, sw);     // ex = q - qs
+  if (!evaporate || s.rain <= 0.f || ex >= 0.f) return 0.f;
   float rq = .001f * rho * s.rain, vent = 1.6f + 124.9f * powf(rq, .2046f);
-  float er = (1.f - s.q / qs) * vent * powf(rq, .525f) / (.001f * rho * (5.4e5f + 2.55e6f / (p / 100.f * qs)));
-  float ev = fminf(fminf(s.rain, er * dt), (qs - s.q) / (1.f + LV * LV * qs / (CP * RV * tk * tk)));
+  float er = (-ex / qs) * vent * powf(rq, .525f) / (.001f * rho * (5.4e5f + 2.55e6f / (p / 100.f * qs)));
+  float ev = fminf(fminf(s.rain, er * dt), -ex / (1.f + LV * LV * qs / (CP * RV * tk * tk)));
   s.rain -= ev; s.q += ev;
   return ev;
 }
 // src/core/microphysics.ts:67-77
-SG_HD float saturationAdjust(Node& s, float exner, float p) {
+SG_HD float saturationAdjust(Node& s, const Level& L) {
   float total = 0.f;
   for (int k = 0; k < 2; k++) {
-    float tk = (s.thb + s.thp) * exner, qs = qsatP(tk - 273.15f, p);
-    float d = (s.q - qs) / (1.f + LV * LV * qs / (CP * RV * tk * tk));
+    const float tk = tcOf(s, L.exner) + 273.15f;
+    const Sat sw = satWater(s, L);
+    float d = excess(s.q, sw) / (1.f + LV * LV * satv(sw) / (CP * RV * tk * tk));
     if (d < 0.f) d = fmaxf(d, -s.cloud);
     if (d == 0.f) break;
-    s.q -= d; s.cloud += d; s.thp += LV / (CP * exner) * d; total += d;
+    s.q -= d; s.cloud += d; s.thp += LV / (CP * L.exner) * d; total += d;
   }
   return total;
 }
 SG_HD float cooperCrystals(float tc) { return tc >= -5.f ? 0.f : fminf(MAX_NUCLEATED, 5.f * expf(.304f * -tc)); }  // src/core/ice.ts:137
 // src/core/ice.ts:154-176 (number = the crystal count)
-SG_HD float saturationAdjustMixed(Node& s, float exner, float p) {
-  float heat = LF / (CP * exner);
-  if ((s.thb + s.thp) * exner >= T_HOM) {
-    if (s.ice > 0.f && (s.thb + s.thp) * exner > T0) {
-      float melt = fminf(s.ice, ((s.thb + s.thp) * exner - T0) * CP / LF);
+SG_HD float saturationAdjustMixed(Node& s, const Level& L) {
+  const float exner = L.exner, heat = LF / (CP * exner);
+  if (tcOf(s, exner) >= T_HOM - T0) {
+    if (s.ice > 0.f && tcOf(s, exner) > 0.f) {
+      float melt = fminf(s.ice, tcOf(s, exner) * CP / LF);
       s.inum *= 1.f - melt / s.ice;
       s.ice -= melt; s.cloud += melt; s.thp -= heat * melt;
     }
-    return saturationAdjust(s, exner, p);
+    return saturationAdjust(s, L);
   }
   if (s.cloud > 0.f) { s.inum += s.cloud / DROPLET_MASS; s.ice += s.cloud; s.thp += heat * s.cloud; s.cloud = 0.f; }
   float total = 0.f;
   for (int k = 0; k < 2; k++) {
-    float tk = (s.thb + s.thp) * exner, qs = qsatIce(tk - T0, p);
-    float d = (s.q - qs) / (1.f + LS * LS * qs / (CP * RV * tk * tk));
+    const float tk = tcOf(s, exner) + T0;
+    const Sat si = satIce(s, L);
+    float d = excess(s.q, si) / (1.f + LS * LS * satv(si) / (CP * RV * tk * tk));
     if (d < 0.f) d = fmaxf(d, -s.ice);
     if (d == 0.f) break;
     s.q -= d; s.ice += d; s.thp += LS / (CP * exner) * d; total += d;
@@ -100,7 +142,7 @@ SG_HD float saturationAdjustMixed(Node& s, float exner, float p) {
 }
 SG_HD void freezeRain(Node& s, float exner) {  // src/core/ice.ts:179-183
   float r = s.rain;
-  if (r <= 0.f || (s.thb + s.thp) * exner >= T_HOM) return;
+  if (r <= 0.f || tcOf(s, exner) >= T_HOM - T0) return;
   s.rain = 0.f; s.graupel += r; s.thp += LF / (CP * exner) * r;
 }
 SG_HD void settleCrystals(Node& s) {  // src/core/ice.ts:245-248
@@ -131,30 +173,35 @@ SG_HD float koenigGrowth(float tc, float m) {  // src/core/ice.ts:203-206
   return 1e-3f * ((1.f - f) * KOENIG_A1[k] * powf(g, KOENIG_A2[k]) + f * KOENIG_A1[k + 1] * powf(g, KOENIG_A2[k + 1]));
 }
 // src/core/ice.ts:223-242
-SG_HD float iceProcesses(Node& s, float exner, float p, float rho, float dt) {
-  float tk = (s.thb + s.thp) * exner, tc = tk - T0;
-  if (tc >= 0.f || tk < T_HOM) return 0.f;
-  float qsi = qsatIce(tc, p), limit = (s.q - qsi) / (1.f + LS * LS * qsi / (CP * RV * tk * tk)), heat = LS / (CP * exner), lacking = cooperCrystals(tc) / rho - s.inum;
+SG_HD float iceProcesses(Node& s, const Level& L, float dt) {
+  const float exner = L.exner, rho = L.rho;
+  float tc = tcOf(s, exner), tk = tc + T0;
+  if (tc >= 0.f || tc < T_HOM - T0) return 0.f;
+  const Sat si = satIce(s, L);
+  const float qsi = satv(si), exi = excess(s.q, si);
+  float limit = exi / (1.f + LS * LS * qsi / (CP * RV * tk * tk)), heat = LS / (CP * exner), lacking = cooperCrystals(tc) / rho - s.inum;
   float change = 0.f;
   if (limit > 0.f && lacking > 0.f) { change = fminf(limit, lacking * CRYSTAL_MASS); s.inum += change / CRYSTAL_MASS; }
   float qi = s.ice + change, n = s.inum;
   if (qi > 1e-12f && n > 0.f) {
-    if (s.q > qsi) change += fminf(n * koenigGrowth(tc, qi / n) * (s.q - qsi) / (qsatP(tc, p) - qsi) * dt, limit - change);
+    if (exi > 0.f) change += fminf(n * koenigGrowth(tc, qi / n) * exi / satDiff(satWater(s, L), si) * dt, limit - change);
     else {
       float a = LS * LS / (KA * RV * tk * tk), b = 1.f / (rho * qsi * PSI);
       float size = cbrtf(6.f * rho * qi / (PI * 900.f * (n * rho)));
-      float lost = fminf(qi, n * 2.f * PI * size * (1.f - s.q / qsi) / (a + b) * dt);
+      float lost = fminf(qi, n * 2.f * PI * size * (-exi / qsi) / (a + b) * dt);
       change -= lost; s.inum *= 1.f - lost / qi;
     }
   }
   s.ice += change; s.q -= change; s.thp += heat * change;
-  float excess = s.ice - s.inum * MAX_CRYSTAL_MASS;
-  if (excess > 0.f) { s.ice -= excess; s.snow += excess; }
+  float excessIce = s.ice - s.inum * MAX_CRYSTAL_MASS;
+  if (excessIce > 0.f) { s.ice -= excessIce; s.snow += excessIce; }
   return change < 0.f ? -heat * change : 0.f;
 }
 // src/core/ice.ts:266-303 (riming of snow into graupel off, the reference default)
-SG_HD float snowProcesses(Node& s, float exner, float p, float rho, float fallsq, float dt) {
-  float tk = (s.thb + s.thp) * exner, tc = tk - T0, qs = s.snow;
+SG_HD float snowProcesses(Node& s, const Level& L, float dt) {
+  const float exner = L.exner, rho = L.rho, fallsq = L.fallsq;
+  const float tc = tcOf(s, exner), tk = tc + T0, qs = s.snow;
+  const Sat si = satIce(s, L);   // at the temperature the routine starts with, as the reference evaluates it
   if (tc < 0.f && s.ice > 0.f) {
     float aut = 1e-3f * expf(.025f * tc) * fmaxf(0.f, s.ice - .001f);
     float moved = fminf(s.ice, aut * dt); s.ice -= moved; s.snow += moved;
@@ -168,9 +215,10 @@ SG_HD float snowProcesses(Node& s, float exner, float p, float rho, float fallsq
     float saci = fminf(s.ice, sweep * expf(.025f * tc) * s.ice * dt); s.ice -= saci; s.snow += saci;
     float sacw = fminf(s.cloud, sweep * s.cloud * dt); s.cloud -= sacw; s.snow += sacw;
     s.thp += LF / (CP * exner) * sacw;
-    float qsi = qsatIce(tc, p), a = LS * LS / (KA * RV * tk * tk), b = 1.f / (rho * qsi * PSI);
-    float rate = 2.f * PI * (s.q / qsi - 1.f) * vent / (rho * (a + b));
-    float dep = rate > 0.f ? fminf(rate * dt, (s.q - qsi) / (1.f + LS * LS * qsi / (CP * RV * tk * tk))) : -fminf(s.snow, -rate * dt);
+    const float qsi = satv(si), exi = excess(s.q, si);
+    float a = LS * LS / (KA * RV * tk * tk), b = 1.f / (rho * qsi * PSI);
+    float rate = 2.f * PI * (exi / qsi) * vent / (rho * (a + b));
+    float dep = rate > 0.f ? fminf(rate * dt, exi / (1.f + LS * LS * qsi / (CP * RV * tk * tk))) : -fminf(s.snow, -rate * dt);
     s.snow += dep; s.q -= dep; s.thp += LS / (CP * exner) * dep;
     if (dep < 0.f) cooling -= LS / (CP * exner) * dep;
   } else {
@@ -182,8 +230,10 @@ SG_HD float snowProcesses(Node& s, float exner, float p, float rho, float fallsq
   return cooling;
 }
 // src/core/graupel.ts:34-72
-SG_HD float graupelProcesses(Node& s, float exner, float p, float rho, float dt) {
-  float tk = (s.thb + s.thp) * exner, tc = tk - T0, heat = 1.f / (CP * exner);
+SG_HD float graupelProcesses(Node& s, const Level& L, float dt) {
+  const float exner = L.exner, rho = L.rho;
+  const float tc = tcOf(s, exner), tk = tc + T0, heat = 1.f / (CP * exner);
+  const Sat si = satIce(s, L);   // at the starting temperature (the reference's qsatIce(tc, p))
   float cooling = 0.f;
   if (tc < 0.f) {
     if (s.rain > 1e-9f) {
@@ -205,10 +255,10 @@ SG_HD float graupelProcesses(Node& s, float exner, float p, float rho, float dt)
     float gaci = fminf(s.ice, sweep * .1f * s.ice * dt), gacs = fminf(s.snow, sweep * expf(.09f * tc) * s.snow * dt);
     s.cloud -= gacw; s.rain -= gacr; s.ice -= gaci; s.snow -= gacs; s.graupel += gacw + gacr + gaci + gacs;
     s.thp += LF * heat * (gacw + gacr);
-    float qsi = qsatIce(tc, p);
-    if (s.q < qsi) {
+    const float qsi = satv(si), exi = excess(s.q, si);
+    if (exi < 0.f) {
       float aa = LS * LS / (KA * RV * tk * tk), b = 1.f / (rho * qsi * PSI);
-      float sub = fminf(fminf(s.graupel, 2.f * PI * (1.f - s.q / qsi) * vent / (rho * (aa + b)) * dt), (qsi - s.q) / (1.f + LS * LS * qsi / (CP * RV * tk * tk)));
+      float sub = fminf(fminf(s.graupel, 2.f * PI * (-exi / qsi) * vent / (rho * (aa + b)) * dt), -exi / (1.f + LS * LS * qsi / (CP * RV * tk * tk)));
       s.graupel -= sub; s.q += sub; s.thp -= LS * heat * sub; cooling += LS * heat * sub;
     }
   } else {
@@ -221,19 +271,22 @@ SG_HD float graupelProcesses(Node& s, float exner, float p, float rho, float dt)
 }
 // src/core/hail.ts:99, :118-131
 SG_HD float ventilationOf(float lambda, float a, float n0) { return n0 * (.78f / (lambda * lambda) + .31f * SC13 * GAMMA_275 * sqrtf(a / NU) * powf(lambda, -2.75f)); }
-SG_HD float wetGrowth(float lambda, float a, float n0, float tc, float qv, float p, float rho, float iceRate) {
-  float heat = KA * -tc + LV * PSI * rho * (qsatP(0.f, p) - qv);
+SG_HD float wetGrowth(float lambda, float a, float n0, float tc, float qv, const Level& L, float iceRate) {
+  const float rho = L.rho;
+  float heat = KA * -tc + LV * PSI * rho * ((L.q0_hi - qv) + L.q0_lo);   // qsatP(0, p) - qv
   return fmaxf(0.f, 2.f * PI * ventilationOf(lambda, a, n0) * heat / (rho * (LF + CW * tc))) + iceRate * (1.f - 2106.f * tc / (LF + CW * tc));
 }
 // src/core/hail.ts:140-175
-SG_HD float hailProcesses(Node& s, float exner, float p, float rho, float dt) {
-  float tk = (s.thb + s.thp) * exner, tc = tk - T0, heat = 1.f / (CP * exner);
+SG_HD float hailProcesses(Node& s, const Level& L, float dt) {
+  const float exner = L.exner, rho = L.rho;
+  const float tc = tcOf(s, exner), tk = tc + T0, heat = 1.f / (CP * exner);
+  const Sat si = satIce(s, L);   // at the starting temperature (the reference's qsatIce(tc, p))
   float cooling = 0.f;
   // wetGrowing(graupel, N0G, RHO_G, ...) (src/core/hail.ts:127-131)
   if (tc < 0.f && s.graupel > 1e-9f) {
     float lambda = powf(PI * RHO_G * N0G / (rho * s.graupel), .25f), a = fallCoef(rho, RHO_G);
     float k = PI * N0G * a * GAMMA_35 / (4.f * powf(lambda, 3.5f));
-    if (k * (s.cloud + s.rain + .1f * s.ice + expf(.09f * tc) * s.snow) > wetGrowth(lambda, a, N0G, tc, s.q, p, rho, k * (s.ice + s.snow))) {
+    if (k * (s.cloud + s.rain + .1f * s.ice + expf(.09f * tc) * s.snow) > wetGrowth(lambda, a, N0G, tc, s.q, L, k * (s.ice + s.snow))) {
       float turned = s.graupel * (1.f - expf(-dt / 60.f)); s.graupel -= turned; s.hail += turned;
     }
   }
@@ -244,17 +297,17 @@ SG_HD float hailProcesses(Node& s, float exner, float p, float rho, float dt) {
   if (tc < 0.f) {
     float hacw = fminf(s.cloud, k * s.cloud * dt), hacr = fminf(s.rain, k * s.rain * dt), liquid = hacw + hacr;
     float haci = fminf(s.ice, k * .1f * s.ice * dt), hacs = fminf(s.snow, k * expf(.09f * tc) * s.snow * dt), frozen = liquid;
-    float wet = wetGrowth(lambda, a, N0H, tc, s.q, p, rho, k * (s.ice + s.snow)) * dt;
+    float wet = wetGrowth(lambda, a, N0H, tc, s.q, L, k * (s.ice + s.snow)) * dt;
     if (liquid + haci + hacs > wet) {
       haci = fminf(s.ice, k * s.ice * dt); hacs = fminf(s.snow, k * s.snow * dt);
       frozen = fminf(liquid, fmaxf(0.f, wet - haci - hacs));
     }
     s.cloud -= hacw; s.rain += liquid - frozen - hacr; s.ice -= haci; s.snow -= hacs; s.hail += frozen + haci + hacs;
     s.thp += LF * heat * frozen;
-    float qsi = qsatIce(tc, p);
-    if (s.q < qsi) {
+    const float qsi = satv(si), exi = excess(s.q, si);
+    if (exi < 0.f) {
       float aa = LS * LS / (KA * RV * tk * tk), b = 1.f / (rho * qsi * PSI);
-      float sub = fminf(fminf(s.hail, 2.f * PI * (1.f - s.q / qsi) * vent / (rho * (aa + b)) * dt), (qsi - s.q) / (1.f + LS * LS * qsi / (CP * RV * tk * tk)));
+      float sub = fminf(fminf(s.hail, 2.f * PI * (-exi / qsi) * vent / (rho * (aa + b)) * dt), -exi / (1.f + LS * LS * qsi / (CP * RV * tk * tk)));
       s.hail -= sub; s.q += sub; s.thp -= LS * heat * sub; cooling += LS * heat * sub;
     }
   } else {
@@ -270,32 +323,54 @@ SG_HD float fragmentsPerKg(float lambda) { return 2.5e13f * 7.f / (lambda * 1000
 
 // The microphysics part of physics(z) (src/core/model.ts:1384-1471), ice or warm. Returns evap (for the water
 // budget) through `evapOut`.
-SG_HD void microphysics(Node& s, float exner, float p, float rho, float fallsq, float dt, int flags, float& evapOut) {
-  float evap = (flags & RF_RAINFORM) ? rainProcesses(s, (s.thb + s.thp) * exner, p, rho, dt, (flags & RF_EVAP) != 0) : 0.f;
+SG_HD void microphysics(Node& s, const Level& L, float dt, int flags, float& evapOut) {
+  const float exner = L.exner, rho = L.rho;
+  float evap = (flags & RF_RAINFORM) ? rainProcesses(s, L, dt, (flags & RF_EVAP) != 0) : 0.f;
   if (evap > 0.f) { float cool = LV / CP / exner * evap; s.thp -= cool; s.cold += cool; }
   float cond;
   if (flags & RF_ICE) {
     freezeRain(s, exner);
     settleCrystals(s);
-    s.cold += iceProcesses(s, exner, p, rho, dt);
+    s.cold += iceProcesses(s, L, dt);
     float iceBefore = s.ice, cloudBefore = s.cloud;
-    s.cold += snowProcesses(s, exner, p, rho, fallsq, dt);
+    s.cold += snowProcesses(s, L, dt);
     float rainBefore = s.rain;
-    s.cold += graupelProcesses(s, exner, p, rho, dt);
-    float rainFrozen = (s.thb + s.thp) * exner < 273.15f ? fmaxf(0.f, rainBefore - s.rain) : 0.f;
-    s.cold += hailProcesses(s, exner, p, rho, dt);
+    s.cold += graupelProcesses(s, L, dt);
+    float rainFrozen = tcOf(s, exner) < 0.f ? fmaxf(0.f, rainBefore - s.rain) : 0.f;
+    s.cold += hailProcesses(s, L, dt);
     if (iceBefore > 0.f) s.inum *= s.ice / iceBefore;
-    float splinters = splintering((s.thb + s.thp) * exner - 273.15f) * SPLINTERS * fmaxf(0.f, cloudBefore - s.cloud)
+    float splinters = splintering(tcOf(s, exner)) * SPLINTERS * fmaxf(0.f, cloudBefore - s.cloud)
       + (rainFrozen > 0.f ? fragmentsPerKg(powf(PI * RHO_W * N0R / (rho * rainBefore), .25f)) * rainFrozen : 0.f);
     if (splinters > 0.f) {
       float fromG = fminf(s.graupel, splinters * CRYSTAL_MASS), fromS = fminf(s.snow, splinters * CRYSTAL_MASS - fromG);
       s.graupel -= fromG; s.snow -= fromS; s.ice += fromG + fromS; s.inum += (fromG + fromS) / CRYSTAL_MASS;
     }
-    cond = saturationAdjustMixed(s, exner, p);
+    cond = saturationAdjustMixed(s, L);
     settleCrystals(s);
-  } else cond = saturationAdjust(s, exner, p);
+  } else cond = saturationAdjust(s, L);
   if (cond < 0.f) s.cold -= LV / CP / exner * cond * .14f;
   evapOut = evap;
+}
+
+// The per-level saturation bases in FP64 (host side, when a run is created; the CPU tests use the same).
+inline Level makeLevel(double thb, double exner, double p, double rho, double rho0) {
+  auto split = [](double x, float& hi, float& lo) { hi = (float)x; lo = (float)(x - (double)hi); };
+  Level L{};
+  L.exner = (float)exner; L.p = (float)p; L.rho = (float)rho; L.fallsq = (float)std::sqrt(rho0 / rho);
+  const double tb = thb * exner - 273.15;
+  L.tcb = (float)tb;
+  auto base = [&](double es, float& hi, float& lo, float& beta) {
+    double den = p - es;
+    if (!(den > 1000.0)) { hi = -1.f; lo = 0.f; beta = 0.f; return; }   // the reference's floor binds: direct formula
+    double qs = .622 * es / den;
+    if (!(qs < .045 * 0.999)) { hi = -1.f; lo = 0.f; beta = 0.f; return; }
+    split(qs, hi, lo); beta = (float)(es / den);
+  };
+  base(611.2 * std::exp(17.67 * tb / (tb + 243.5)), L.qw_hi, L.qw_lo, L.bw);
+  base(611.21 * std::exp(22.587 * tb / (tb + 273.86)), L.qi_hi, L.qi_lo, L.bi);
+  const double es0 = 611.2, q0 = std::min(.045, std::max(0.0, .622 * es0 / std::max(1000.0, p - es0)));
+  split(q0, L.q0_hi, L.q0_lo);
+  return L;
 }
 
 }  // namespace phys

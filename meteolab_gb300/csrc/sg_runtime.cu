@@ -17,6 +17,7 @@
 #include "sg_common.cuh"
 #include "sg_fft.cuh"
 #include "sg_kernels.h"
+#include "sg_physics.cuh"
 
 using namespace sg;
 
@@ -151,6 +152,14 @@ void build_tables(const sg_grid* g, const sg_base_state* b, const sg_switches* s
     L(L_NODEMASS, z, dx * dy * hz[z] * rho[z]);
     L(L_LW, z, hz[z] / dzMean * rho[z]);
     L(L_SURF, z, 0);
+    L(L_TCB, z, thb[z] * b->exner[z] - 273.15);
+    {
+      phys::Level pl = phys::makeLevel(thb[z], b->exner[z], b->p[z], rho[z], rho[0]);
+      T.lv[(size_t)L_QW_HI * nz + z] = pl.qw_hi; T.lv[(size_t)L_QW_LO * nz + z] = pl.qw_lo; T.lv[(size_t)L_BW * nz + z] = pl.bw;
+      T.lv[(size_t)L_QI_HI * nz + z] = pl.qi_hi; T.lv[(size_t)L_QI_LO * nz + z] = pl.qi_lo; T.lv[(size_t)L_BI * nz + z] = pl.bi;
+      T.lv[(size_t)L_Q0_HI * nz + z] = pl.q0_hi; T.lv[(size_t)L_Q0_LO * nz + z] = pl.q0_lo;
+      T.lv[(size_t)L_TCB * nz + z] = pl.tcb;
+    }
     double face = z > 0 ? (rho[z - 1] + rho[z]) / 2 : 0;
     D(D_FLO, z, z > 0 ? face / dzs[z - 1] : 0);
     D(D_FHZ, z, hz[z]);
@@ -285,10 +294,11 @@ void enqueue_part(sg_context* ctx, const Plan& P, int part, Hook hook) {
   Launch node = lx(ctx, P, FAM_NODE), cols = lx(ctx, P, FAM_COLS), rf = lx(ctx, P, FAM_ROWS_FACE), rp = lx(ctx, P, FAM_ROWS_PRES);
   Launch modes = lx(ctx, P, FAM_MODES, 2), runs = lx(ctx, P, FAM_RUNS);
   Launch tk[4] = {lx(ctx, P, FAM_T_WENO, 4), lx(ctx, P, FAM_T_LIN, 4), lx(ctx, P, FAM_T_W, 4), lx(ctx, P, FAM_T_TH, 4)};
-  const int mthreads = std::min(512, std::max(128, P.maxny));
+  const int mthreads = std::min(512, std::max(256, 2 * P.maxny));
+  const int mbudget = std::min(ctx->maxSmem, 200 * 1024);
   auto project = [&](int set, int final_) {
     launch_proj_div_xfft(rp, PROJ_PRES, set, YC, P.maxnx); hook(7);
-    launch_proj_modes(modes, PROJ_PRES, P.maxnz, P.maxny, mthreads); hook(8);
+    launch_proj_modes(modes, PROJ_PRES, P.maxnz, P.maxny, mthreads, mbudget); hook(8);
     launch_proj_xifft(rp, PROJ_PRES, YC, P.maxnx); hook(9);
     launch_pres_correct(node, set, final_); hook(final_ ? 16 : 10);
   };
@@ -297,12 +307,12 @@ void enqueue_part(sg_context* ctx, const Plan& P, int part, Hook hook) {
     launch_sediment(cols, P.maxnz); hook(1);
   } else if (part == 2) {
     launch_proj_div_xfft(rf, PROJ_FACE, A, YC, P.maxnx); hook(2);
-    launch_proj_modes(modes, PROJ_FACE, P.maxnz, P.maxny, mthreads); hook(3);
+    launch_proj_modes(modes, PROJ_FACE, P.maxnz, P.maxny, mthreads, mbudget); hook(3);
     launch_proj_xifft(rf, PROJ_FACE, YC, P.maxnx); hook(4);
     launch_face_correct(node, A); hook(5);
     const int in[3] = {A, B, C}, out[3] = {B, C, B};
     for (int s = 0; s < 3; s++) {
-      for (int k = 0; k < 4; k++) if (tk[k].n) { launch_transport(tk[k], k, in[s], out[s], (float)RK3[s], s, P.TX, P.TY); hook(6); }
+      for (int k = 0; k < 4; k++) if (tk[k].n) { launch_transport(tk[k], k, in[s], out[s], (float)RK3[s], s, P.TX, P.TY); hook(18 + k); }
       if (s < 2) project(out[s], 0);
     }
   } else if (part == 3) {
@@ -321,9 +331,11 @@ template <class Hook>
 void enqueue_step(sg_context* ctx, const Plan& P, Hook hook) {
   for (int part = 1; part <= 5; part++) enqueue_part(ctx, P, part, hook);
 }
-const char* KERNEL_NAMES[18] = {"fall_courant", "sediment", "face_div_xfft", "face_modes", "face_xifft", "face_correct", "transport",
-                                "pres_div_xfft", "pres_modes", "pres_xifft", "pres_correct", "fill_partial", "fill_final", "physics",
-                                "viscosity", "mix", "pres_correct_final", "step_end"};
+const int NKERNELS = 22;
+const char* KERNEL_NAMES[NKERNELS] = {"fall_courant", "sediment", "face_div_xfft", "face_modes", "face_xifft", "face_correct", "transport",
+                                      "pres_div_xfft", "pres_modes", "pres_xifft", "pres_correct", "fill_partial", "fill_final", "physics",
+                                      "viscosity", "mix", "pres_correct_final", "step_end", "transport_weno", "transport_uv",
+                                      "transport_w", "transport_theta"};
 
 Plan* get_plan(sg_context* ctx, const std::vector<int>& slots, int* status) {
   auto it = ctx->plans.find(slots);
@@ -626,7 +638,7 @@ int sg_profile_kernels(sg_context* ctx, const sg_run* runs, int n, int nsteps, c
   if (st) return -st;
   Plan* P = get_plan(ctx, slots, &st);
   if (!P) return -st;
-  const int K = 18;
+  const int K = NKERNELS;
   std::vector<double> total(K, 0); std::vector<int64_t> count(K, 0);
   cudaEvent_t ev[64];
   for (int e = 0; e < 64; e++) cudaEventCreate(&ev[e]);

@@ -144,6 +144,13 @@ double orc_microphysics(float* v, double exner, double p, double rho, double rho
   return microphysicsNode<float>(a, a + 1, a + 2, a + 3, a + 9, a + 4, a + 5, a + 6, a + 7, a + 8, 0, exner, p, rho, rhoGround, dt, sw);
 }
 
+// The same on FP64 cells (the pure FP64 oracle's arithmetic and storage).
+double orc_microphysics64(double* v, double exner, double p, double rho, double rhoGround, double dt, int flags) {
+  Switches sw; sw.ice = flags & 1; sw.evaporation = (flags & 2) != 0; sw.rainFormation = (flags & 4) != 0;
+  Arr<double> a = (Arr<double>)v;
+  return microphysicsNode<double>(a, a + 1, a + 2, a + 3, a + 9, a + 4, a + 5, a + 6, a + 7, a + 8, 0, exner, p, rho, rhoGround, dt, sw);
+}
+
 // FFT of length n in place (sign -1 forward, +1 unnormalised inverse).
 void orc_fft(int n, double* re, double* im, int sign) { FFT f(n); f.transform(re, im, sign); }
 // HorizontalDFT forward of `layers` layers of src; spectra into re/im (nx*ny*layers); then inverse into out.

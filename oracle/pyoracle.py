@@ -63,6 +63,8 @@ def lib():
             L.orc_cell.argtypes = [C.c_int, _f, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double]
             L.orc_microphysics.restype = C.c_double
             L.orc_microphysics.argtypes = [_f, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int]
+            L.orc_microphysics64.restype = C.c_double
+            L.orc_microphysics64.argtypes = [_d, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int]
             L.orc_fft.argtypes = [C.c_int, _d, _d, C.c_int]
             L.orc_hdft.argtypes = [C.c_int, C.c_int, C.c_int, _d, _d, _d, _d]
             grid_args = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, _d, _d, _d]

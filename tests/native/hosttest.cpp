@@ -16,11 +16,13 @@ extern "C" {
 float ht_weno(float a, float b, float c, float d, float e) { return weno5(a, b, c, d, e); }
 float ht_upwind(float a, float b, float c, float d, float e) { return upwind5(a, b, c, d, e); }
 
-// v = [thp, thb, q, cloud, rain, ice, inum, snow, graupel, hail, cold] in/out; returns evap.
-float ht_microphysics(float* v, float exner, float p, float rho, float fallsq, float dt, int flags) {
-  phys::Node s{v[0], v[1], v[2], v[3], v[4], v[5], v[6], v[7], v[8], v[9], v[10]};
+// v = [thp, thb, q, cloud, rain, ice, inum, snow, graupel, hail, cold] in/out; returns evap. The level's constants
+// (the Celsius base temperature, the saturation bases) come from thb, exner, p, rho in FP64, as when a run is created.
+float ht_microphysics(float* v, double exner, double p, double rho, double rho0, float dt, int flags) {
+  phys::Level L = phys::makeLevel((double)v[1], exner, p, rho, rho0);
+  phys::Node s{v[0], v[1], L.tcb, v[2], v[3], v[4], v[5], v[6], v[7], v[8], v[9], v[10]};
   float evap = 0;
-  phys::microphysics(s, exner, p, rho, fallsq, dt, flags, evap);
+  phys::microphysics(s, L, dt, flags, evap);
   v[0] = s.thp; v[2] = s.q; v[3] = s.cloud; v[4] = s.rain; v[5] = s.ice; v[6] = s.inum; v[7] = s.snow; v[8] = s.graupel; v[9] = s.hail; v[10] = s.cold;
   return evap;
 }

@@ -37,7 +37,7 @@ def ht():
     L.ht_upwind.restype = C.c_float
     L.ht_upwind.argtypes = [C.c_float] * 5
     L.ht_microphysics.restype = C.c_float
-    L.ht_microphysics.argtypes = [C.POINTER(C.c_float), C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int]
+    L.ht_microphysics.argtypes = [C.POINTER(C.c_float), C.c_double, C.c_double, C.c_double, C.c_double, C.c_float, C.c_int]
     L.ht_fft.restype = C.c_int
     L.ht_fft.argtypes = [C.c_int, C.POINTER(C.c_float)]
     L.ht_fall.argtypes = [C.c_float] * 6 + [C.POINTER(C.c_float)]
@@ -118,7 +118,7 @@ def test_microphysics_matches_oracle(ht, k, ice):
     flags = (1 if ice else 0) | 2 | 4
     evo = O.lib().orc_microphysics(O.fp(ov), exner, p, rho, 1.16, dt, flags)
     dflags = (128 if ice else 0) | 2 | 4
-    evd = ht.ht_microphysics(dv.ctypes.data_as(C.POINTER(C.c_float)), exner, p, rho, math.sqrt(1.16 / rho), dt, dflags)
+    evd = ht.ht_microphysics(dv.ctypes.data_as(C.POINTER(C.c_float)), exner, p, rho, 1.16, dt, dflags)
     got = dict(theta=float(dv[0]) + float(dv[1]), q=dv[2], cloud=dv[3], rain=dv[4], ice=dv[5], iceNumber=dv[6], snow=dv[7], graupel=dv[8], hail=dv[9], cold=dv[10])
     ref = {n: float(ov[j]) for j, n in enumerate(names)}
     assert abs(got["theta"] - ref["theta"]) < 2e-4, (got["theta"], ref["theta"])
