@@ -368,42 +368,66 @@ __global__ void k_pres_correct(const RunDesc* runs, const int4* items, int nitem
 }
 
 // ==================================================================== RK3 transport
-// One field of one run on a TX x TY tile of columns, marching up the column: the tendency -(div F - q div)/rho0 of
-// the flux-form WENO5 (monotone fields) or linear fifth-order upwind reconstruction on the projected face fluxes
-// (FluxTransport.tendency, src/core/advection.ts:274-378), w with the stage buoyancy (stageBuoyancy, model.ts:1204),
-// theta' with the base profile's own vertical flux tendency, then the RK3 update a = start + f dt tend (:1250) and,
-// before a stage projection, w = 0 on the ground and the top (:1045).
-// Layout of the march: the column's own values z-3..z+3 live in registers (the vertical faces); the current plane
-// with a 3-node halo in shared memory (the x and y faces, each reconstructed once and exchanged through shared
-// memory); the next level's plane, faces, start value and (w) buoyancy inputs are loaded while the current level
-// computes; one barrier per level (double-buffered plane and face arrays); per-level constants staged once per item.
+// A group of G fields of one run on a TX x TY tile of columns, marching up the column: the tendency
+// -(div F - q div)/rho0 of the flux-form WENO5 (monotone fields) or linear fifth-order upwind reconstruction on the
+// projected face fluxes (FluxTransport.tendency, src/core/advection.ts:274-378), w with the stage buoyancy
+// (stageBuoyancy, model.ts:1204), theta' with the base profile's own vertical flux tendency, then the RK3 update
+// a = start + f dt tend (:1250) and, before a stage projection, w = 0 on the ground and the top (:1045).
+// Each field's planes z-3..z+3 (clamped at the ground and top, with a 3-node halo, periodic) sit in a 7-slot ring in
+// shared memory; per level one new plane per field is loaded (issued before the level's arithmetic, stored after it),
+// each x and y face is reconstructed once and exchanged through shared memory (double-buffered), the vertical faces
+// come from the ring, and one barrier separates the levels. The group shares the face-flux loads.
 enum TKind { TK_WENO = 0, TK_LIN = 1, TK_W = 2, TK_TH = 3 };
-constexpr int TMAXC = 4;  // halo-plane cells per thread: (TX + 6)(TY + 6) <= TMAXC * TX * TY
+constexpr int TMAXC = 4;  // plane cells per thread: (TX + 6)(TY + 6) <= TMAXC * TX * TY
 constexpr int TLV = 9;    // per-level constants staged: 1/hz, 1/rho, theta faces x4, thb, qb, thv_env
+// Field groups of the transport work items: WENO {rain, snow, graupel}, {hail, q, cloud}, {ice, number, cold};
+// linear {u, v}; {w}; {theta}.
+__constant__ int TGROUP[6][3] = {{RAIN, SNOW, GRAUPEL}, {HAIL, Q, CLOUD}, {ICE, ICENUM, COLD}, {U, V, -1}, {W, -1, -1}, {THETA, -1, -1}};
 
 template <int KIND>
 __device__ __forceinline__ float trecon(float a, float b, float c, float d, float e) {
-  if (KIND == TK_WENO) return weno5(a, b, c, d, e);
+  if (KIND == TK_WENO) {
+    // WENO of five zeros is zero: precipitation and ice are zero over most of a domain (the reference skips such
+    // rows, FluxTransport.markActiveRows, advection.ts), and a warp whose stencils are all zero skips the weights.
+    if (((__float_as_uint(a) | __float_as_uint(b) | __float_as_uint(c) | __float_as_uint(d) | __float_as_uint(e)) << 1) == 0u) return 0.f;
+    return weno5(a, b, c, d, e);
+  }
   return upwind5(a, b, c, d, e);
 }
 
-template <int KIND>
-__device__ __forceinline__ void transport_item(const RunDesc& Rg, int f, int tile, int in_set, int out_set, float frac, int stage,
+// 4-byte asynchronous copy global -> shared (lands without passing through registers), and the wait for all of
+// this thread's copies; other threads see the data after the next barrier.
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+template <int KIND, int G>
+__device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int tile, int in_set, int out_set, float frac, int stage,
                                                int TX, int TY, float* sm) {
   const int nx = Rg.nx, ny = Rg.ny, nz = Rg.nz, layer = Rg.layer;
   const size_t n = Rg.n;
   const float inv_dx = Rg.inv_dx, inv_dy = Rg.inv_dy, fdt = frac * Rg.dt;
   const int flags = Rg.flags;
-  const float* __restrict__ q = Rg.fld + ((size_t)in_set * NF + f) * n;
-  const float* __restrict__ st = Rg.fld + (size_t)f * n;
-  float* __restrict__ out = Rg.fld + ((size_t)out_set * NF + f) * n;
   const float4* __restrict__ F4 = reinterpret_cast<const float4*>(Rg.faces);
-  const float* __restrict__ inb = Rg.fld + (size_t)in_set * NF * n;  // the input set's fields (buoyancy)
+  const float* __restrict__ inb = Rg.fld + (size_t)in_set * NF * n;   // the input set (buoyancy)
+  const float* q[G];
+  const float* st[G];
+  float* out[G];
+#pragma unroll
+  for (int g = 0; g < G; g++) {
+    const int f = TGROUP[group][g];
+    q[g] = Rg.fld + ((size_t)in_set * NF + f) * n;
+    st[g] = Rg.fld + (size_t)f * n;
+    out[g] = Rg.fld + ((size_t)out_set * NF + f) * n;
+  }
   const int PW = TX + 6, PH = TY + 6, NCELL = PW * PH, NT = TX * TY;
-  float* lv = sm;                                  // [TLV][MAXNZ]
-  float* plane = lv + TLV * MAXNZ;                 // [2][PH][PW]
-  float* fxs = plane + 2 * NCELL;                  // [2][TY][TX + 1]
-  float* fys = fxs + 2 * TY * (TX + 1);            // [2][TY + 1][TX]
+  float* lv = sm;                                   // [TLV][MAXNZ]
+  float* ring = lv + TLV * MAXNZ;                   // [G][7][NCELL]
+  float* fxs = ring + G * 7 * NCELL;                // [2][G][TY][TX + 1]
+  float* fys = fxs + 2 * G * TY * (TX + 1);         // [2][G][TY + 1][TX]
+  const int FXS = TY * (TX + 1), FYS = (TY + 1) * TX;
   const int t = threadIdx.x, lx = t % TX, ly = t / TX;
   const int tilesX = (nx + TX - 1) / TX, x0 = (tile % tilesX) * TX, y0 = (tile / tilesX) * TY;
   const int x = x0 + lx, y = y0 + ly;
@@ -418,7 +442,7 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int f, int til
     }
     if (KIND == TK_W) { lv[6 * MAXNZ + z] = lvl(Rg, L_THB, z); lv[7 * MAXNZ + z] = lvl(Rg, L_QB, z); lv[8 * MAXNZ + z] = lvl(Rg, L_THVENV, z); }
   }
-  // halo-plane cells of this thread, as column offsets (periodic)
+  // plane cells of this thread as column offsets (periodic)
   int off[TMAXC], cell[TMAXC];
 #pragma unroll
   for (int j = 0; j < TMAXC; j++) {
@@ -432,104 +456,128 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int f, int til
   const int offW = on ? wrap(x - 1, nx) + y * nx : 0, offS = on ? x + wrap(y - 1, ny) * nx : 0;
   const bool loadBuoy = KIND == TK_W && (flags & RF_STAGES);
   const bool loading = flags & RF_LOADING;
-  // prologue: plane 0, the column window, level 0's inputs
-  float win[7];
+  // prologue: ring slots of the virtual levels -3..3 (clamped), level 0's inputs
+  for (int v = -3; v <= 3; v++) {
+    const int lev = clampi(v, 0, nz - 1), slot = (v + 7) % 7;
 #pragma unroll
-  for (int j = 0; j < 7; j++) win[j] = on ? q[col + clampi(j - 3, 0, nz - 1) * layer] : 0.f;
+    for (int g = 0; g < G; g++)
 #pragma unroll
-  for (int j = 0; j < TMAXC; j++) if (cell[j] >= 0) plane[cell[j]] = q[off[j]];
+      for (int j = 0; j < TMAXC; j++) if (cell[j] >= 0) ring[(g * 7 + slot) * NCELL + cell[j]] = q[g][off[j] + lev * layer];
+  }
   float4 fc = on ? F4[col] : make_float4(0.f, 0.f, 0.f, 0.f);
   float mw = on && lx == 0 ? F4[offW].x : 0.f, ms = on && ly == 0 ? F4[offS].y : 0.f;
-  float s0 = on && stage > 0 ? st[col] : 0.f;
+  float s0[G];
+#pragma unroll
+  for (int g = 0; g < G; g++) s0[g] = on && stage > 0 ? st[g][col] : 0.f;
   float b[8];
 #pragma unroll
   for (int j = 0; j < 8; j++) b[j] = 0.f;
   if (loadBuoy && on) { b[0] = inb[THETA * n + col]; b[1] = inb[Q * n + col]; b[2] = inb[CLOUD * n + col]; b[3] = inb[ICE * n + col];
     if (loading) { b[4] = inb[RAIN * n + col]; b[5] = inb[SNOW * n + col]; b[6] = inb[GRAUPEL * n + col]; b[7] = inb[HAIL * n + col]; } }
   __syncthreads();
-  float fzD = 0.f, mzD = 0.f;
+  float fzD[G];
+#pragma unroll
+  for (int g = 0; g < G; g++) fzD[g] = 0.f;
+  float mzD = 0.f;
+  const int cidx = (ly + 3) * PW + (lx + 3);
   for (int z = 0; z < nz; z++) {
     const int buf = z & 1, l = z * layer;
     const bool more = z + 1 < nz;
     const int ln = l + layer;
-    // loads for level z + 1 (issued before this level's arithmetic)
-    float pn[TMAXC];
+    // loads for later levels (issued before this level's arithmetic): the plane z + 4 into the freed ring slot
+    // (asynchronous copies), and level z + 1's faces, start values and buoyancy inputs
+    // (slot of z - 3, read last by the previous level before its barrier)
+    const int levNext = min(z + 4, nz - 1) * layer, s_new = (z + 4) % 7;
 #pragma unroll
-    for (int j = 0; j < TMAXC; j++) pn[j] = (more && cell[j] >= 0) ? q[off[j] + ln] : 0.f;
+    for (int g = 0; g < G; g++)
+#pragma unroll
+      for (int j = 0; j < TMAXC; j++) if (cell[j] >= 0) cp_async4(ring + (g * 7 + s_new) * NCELL + cell[j], q[g] + off[j] + levNext);
     float4 fcn = make_float4(0.f, 0.f, 0.f, 0.f);
-    float mwn = 0.f, msn = 0.f, s0n = 0.f, qn = 0.f, bn[8];
+    float mwn = 0.f, msn = 0.f, s0n[G], bn[8];
+#pragma unroll
+    for (int g = 0; g < G; g++) s0n[g] = 0.f;
 #pragma unroll
     for (int j = 0; j < 8; j++) bn[j] = 0.f;
-    if (on) {
-      qn = q[col + min(z + 4, nz - 1) * layer];
-      if (more) {
-        fcn = F4[col + ln];
-        if (lx == 0) mwn = F4[offW + ln].x;
-        if (ly == 0) msn = F4[offS + ln].y;
-        if (stage > 0) s0n = st[col + ln];
-        if (loadBuoy) { bn[0] = inb[THETA * n + col + ln]; bn[1] = inb[Q * n + col + ln]; bn[2] = inb[CLOUD * n + col + ln]; bn[3] = inb[ICE * n + col + ln];
-          if (loading) { bn[4] = inb[RAIN * n + col + ln]; bn[5] = inb[SNOW * n + col + ln]; bn[6] = inb[GRAUPEL * n + col + ln]; bn[7] = inb[HAIL * n + col + ln]; } }
+    if (on && more) {
+      fcn = F4[col + ln];
+      if (lx == 0) mwn = F4[offW + ln].x;
+      if (ly == 0) msn = F4[offS + ln].y;
+      if (stage > 0) {
+#pragma unroll
+        for (int g = 0; g < G; g++) s0n[g] = st[g][col + ln];
+      }
+      if (loadBuoy) { bn[0] = inb[THETA * n + col + ln]; bn[1] = inb[Q * n + col + ln]; bn[2] = inb[CLOUD * n + col + ln]; bn[3] = inb[ICE * n + col + ln];
+        if (loading) { bn[4] = inb[RAIN * n + col + ln]; bn[5] = inb[SNOW * n + col + ln]; bn[6] = inb[GRAUPEL * n + col + ln]; bn[7] = inb[HAIL * n + col + ln]; } }
+    }
+    // faces of level z for each field
+    const float m1 = fc.x, m2 = fc.y, m3 = fc.z;
+    float fzU[G], qc[G];
+    const int s_m2 = (z + 5) % 7, s_m1 = (z + 6) % 7, s_0 = z % 7, s_p1 = (z + 1) % 7, s_p2 = (z + 2) % 7, s_p3 = (z + 3) % 7;
+#pragma unroll
+    for (int g = 0; g < G; g++) {
+      const float* R = ring + g * 7 * NCELL;
+      const float* P = R + s_0 * NCELL + cidx;
+      qc[g] = P[0];
+      fzU[g] = 0.f;
+      if (on) {
+        float* FX = fxs + (buf * G + g) * FXS + ly * (TX + 1) + lx;
+        float* FY = fys + (buf * G + g) * FYS + ly * TX + lx;
+        FX[1] = m1 >= 0.f ? m1 * trecon<KIND>(P[-2], P[-1], P[0], P[1], P[2]) : m1 * trecon<KIND>(P[3], P[2], P[1], P[0], P[-1]);
+        if (lx == 0) FX[0] = mw >= 0.f ? mw * trecon<KIND>(P[-3], P[-2], P[-1], P[0], P[1]) : mw * trecon<KIND>(P[2], P[1], P[0], P[-1], P[-2]);
+        FY[TX] = m2 >= 0.f ? m2 * trecon<KIND>(P[-2 * PW], P[-PW], P[0], P[PW], P[2 * PW]) : m2 * trecon<KIND>(P[3 * PW], P[2 * PW], P[PW], P[0], P[-PW]);
+        if (ly == 0) FY[0] = ms >= 0.f ? ms * trecon<KIND>(P[-3 * PW], P[-2 * PW], P[-PW], P[0], P[PW]) : ms * trecon<KIND>(P[2 * PW], P[PW], P[0], P[-PW], P[-2 * PW]);
+        if (z < nz - 1) {
+          const float a2 = R[s_m2 * NCELL + cidx], a1 = R[s_m1 * NCELL + cidx], b1 = R[s_p1 * NCELL + cidx], b2 = R[s_p2 * NCELL + cidx], b3 = R[s_p3 * NCELL + cidx];
+          fzU[g] = m3 >= 0.f ? m3 * trecon<KIND>(a2, a1, qc[g], b1, b2) : m3 * trecon<KIND>(b3, b2, b1, qc[g], a1);
+        }
       }
     }
-    // faces of level z
-    float fzU = 0.f;
-    const float m3 = fc.z;
-    if (on) {
-      const float* P = plane + buf * NCELL + (ly + 3) * PW + (lx + 3);
-      float* FX = fxs + buf * TY * (TX + 1) + ly * (TX + 1) + lx;
-      float* FY = fys + buf * (TY + 1) * TX + ly * TX + lx;
-      const float m1 = fc.x, m2 = fc.y;
-      FX[1] = m1 >= 0.f ? m1 * trecon<KIND>(P[-2], P[-1], P[0], P[1], P[2]) : m1 * trecon<KIND>(P[3], P[2], P[1], P[0], P[-1]);
-      if (lx == 0) FX[0] = mw >= 0.f ? mw * trecon<KIND>(P[-3], P[-2], P[-1], P[0], P[1]) : mw * trecon<KIND>(P[2], P[1], P[0], P[-1], P[-2]);
-      FY[TX] = m2 >= 0.f ? m2 * trecon<KIND>(P[-2 * PW], P[-PW], P[0], P[PW], P[2 * PW]) : m2 * trecon<KIND>(P[3 * PW], P[2 * PW], P[PW], P[0], P[-PW]);
-      if (ly == 0) FY[0] = ms >= 0.f ? ms * trecon<KIND>(P[-3 * PW], P[-2 * PW], P[-PW], P[0], P[PW]) : ms * trecon<KIND>(P[2 * PW], P[PW], P[0], P[-PW], P[-2 * PW]);
-      if (z < nz - 1) fzU = m3 >= 0.f ? m3 * trecon<KIND>(win[1], win[2], win[3], win[4], win[5]) : m3 * trecon<KIND>(win[6], win[5], win[4], win[3], win[2]);
-    }
-    if (more) {
-#pragma unroll
-      for (int j = 0; j < TMAXC; j++) if (cell[j] >= 0) plane[(buf ^ 1) * NCELL + cell[j]] = pn[j];
-    }
+    cp_async_wait_all();
     __syncthreads();
     if (on) {
-      const float* FX = fxs + buf * TY * (TX + 1) + ly * (TX + 1) + lx;
-      const float* FY = fys + buf * (TY + 1) * TX + ly * TX + lx;
-      const float qc = win[3], ihz = lv[z], irho = lv[MAXNZ + z];
-      float flux = (FX[1] - FX[0]) * inv_dx + (FY[TX] - FY[0]) * inv_dy + (fzU - fzD) * ihz;
-      float tend = -(flux - qc * fc.w) * irho;
-      if (KIND == TK_TH) {
-        float up = m3 * (m3 >= 0.f ? lv[2 * MAXNZ + z] : lv[3 * MAXNZ + z]);
-        float dn = mzD * (mzD >= 0.f ? lv[4 * MAXNZ + z] : lv[5 * MAXNZ + z]);
-        tend -= (up - dn) * ihz * irho;
-      }
-      if (KIND == TK_W && loadBuoy) {
-        // g B with theta' and the base state (stageBuoyancy): theta_v - theta_v,env from small differences.
-        const float Rb = lv[6 * MAXNZ + z], Qb = lv[7 * MAXNZ + z];
-        float dth = b[0], num = dth + .61f * ((Rb + dth) * (b[1] - Qb) + Qb * dth);
-        float loaded = b[2] + b[3] + (loading ? (b[4] + b[5]) + (b[6] + b[7]) : 0.f);
-        tend += 9.81f * (num / lv[8 * MAXNZ + z] - loaded);
-      }
-      float a = (stage == 0 ? qc : s0) + fdt * tend;
-      if (KIND == TK_W && stage < 2 && (flags & RF_STAGES) && (z == 0 || z == nz - 1)) a = 0.f;
-      out[col + l] = a;
-    }
-    fzD = fzU; mzD = m3;
+      const float ihz = lv[z], irho = lv[MAXNZ + z];
 #pragma unroll
-    for (int j = 0; j < 6; j++) win[j] = win[j + 1];
-    win[6] = qn; fc = fcn; mw = mwn; ms = msn; s0 = s0n;
+      for (int g = 0; g < G; g++) {
+        const float* FX = fxs + (buf * G + g) * FXS + ly * (TX + 1) + lx;
+        const float* FY = fys + (buf * G + g) * FYS + ly * TX + lx;
+        float flux = (FX[1] - FX[0]) * inv_dx + (FY[TX] - FY[0]) * inv_dy + (fzU[g] - fzD[g]) * ihz;
+        float tend = -(flux - qc[g] * fc.w) * irho;
+        if (KIND == TK_TH) {
+          float up = m3 * (m3 >= 0.f ? lv[2 * MAXNZ + z] : lv[3 * MAXNZ + z]);
+          float dn = mzD * (mzD >= 0.f ? lv[4 * MAXNZ + z] : lv[5 * MAXNZ + z]);
+          tend -= (up - dn) * ihz * irho;
+        }
+        if (KIND == TK_W && loadBuoy) {
+          // g B with theta' and the base state (stageBuoyancy): theta_v - theta_v,env from small differences.
+          const float Rb = lv[6 * MAXNZ + z], Qb = lv[7 * MAXNZ + z];
+          float dth = b[0], num = dth + .61f * ((Rb + dth) * (b[1] - Qb) + Qb * dth);
+          float loaded = b[2] + b[3] + (loading ? (b[4] + b[5]) + (b[6] + b[7]) : 0.f);
+          tend += 9.81f * (num / lv[8 * MAXNZ + z] - loaded);
+        }
+        float a = (stage == 0 ? qc[g] : s0[g]) + fdt * tend;
+        if (KIND == TK_W && stage < 2 && (flags & RF_STAGES) && (z == 0 || z == nz - 1)) a = 0.f;
+        out[g][col + l] = a;
+        fzD[g] = fzU[g];
+      }
+    }
+    mzD = m3;
+    fc = fcn; mw = mwn; ms = msn;
+#pragma unroll
+    for (int g = 0; g < G; g++) s0[g] = s0n[g];
 #pragma unroll
     for (int j = 0; j < 8; j++) b[j] = bn[j];
   }
   __syncthreads();
 }
 
-template <int KIND>
-__global__ void __launch_bounds__(512) k_transport(const RunDesc* runs, const int4* items, int nitems, int in_set, int out_set,
-                                                    float frac, int stage, int TX, int TY) {
+template <int KIND, int G>
+__global__ void __launch_bounds__(320, 2) k_transport(const RunDesc* runs, const int4* items, int nitems, int in_set, int out_set,
+                                                       float frac, int stage, int TX, int TY) {
   extern __shared__ float sm[];
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
     if (R.cnt[C_FAILED]) continue;
-    transport_item<KIND>(R, items[it].y, items[it].z, in_set, out_set, frac, stage, TX, TY, sm);
+    transport_item<KIND, G>(R, items[it].y, items[it].z, in_set, out_set, frac, stage, TX, TY, sm);
   }
 }
 
@@ -814,15 +862,17 @@ void launch_proj_xifft(const Launch& L, int mode, int yc, int maxnx) {
 }
 void launch_face_correct(const Launch& L, int set) { k_face_correct<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set); }
 void launch_pres_correct(const Launch& L, int set, int final_) { k_pres_correct<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set, final_); }
+size_t transport_smem(int G, int TX, int TY) {
+  return ((size_t)TLV * MAXNZ + (size_t)G * 7 * (TX + 6) * (TY + 6) + 2 * (size_t)G * TY * (TX + 1) + 2 * (size_t)G * (TY + 1) * TX) * sizeof(float);
+}
 void launch_transport(const Launch& L, int kind, int in_set, int out_set, float frac, int stage, int TX, int TY) {
   if (L.n == 0) return;
-  size_t smem = ((size_t)TLV * MAXNZ + 2 * (size_t)(TX + 6) * (TY + 6) + 2 * (size_t)TY * (TX + 1) + 2 * (size_t)(TY + 1) * TX) * sizeof(float);
   dim3 g = GRID(L.n, L.cap);
   switch (kind) {
-    case TK_WENO: k_transport<TK_WENO><<<g, TX * TY, smem, L.stream>>>(L.runs, L.items, L.n, in_set, out_set, frac, stage, TX, TY); break;
-    case TK_LIN: k_transport<TK_LIN><<<g, TX * TY, smem, L.stream>>>(L.runs, L.items, L.n, in_set, out_set, frac, stage, TX, TY); break;
-    case TK_W: k_transport<TK_W><<<g, TX * TY, smem, L.stream>>>(L.runs, L.items, L.n, in_set, out_set, frac, stage, TX, TY); break;
-    default: k_transport<TK_TH><<<g, TX * TY, smem, L.stream>>>(L.runs, L.items, L.n, in_set, out_set, frac, stage, TX, TY); break;
+    case TK_WENO: k_transport<TK_WENO, 3><<<g, TX * TY, transport_smem(3, TX, TY), L.stream>>>(L.runs, L.items, L.n, in_set, out_set, frac, stage, TX, TY); break;
+    case TK_LIN: k_transport<TK_LIN, 2><<<g, TX * TY, transport_smem(2, TX, TY), L.stream>>>(L.runs, L.items, L.n, in_set, out_set, frac, stage, TX, TY); break;
+    case TK_W: k_transport<TK_W, 1><<<g, TX * TY, transport_smem(1, TX, TY), L.stream>>>(L.runs, L.items, L.n, in_set, out_set, frac, stage, TX, TY); break;
+    default: k_transport<TK_TH, 1><<<g, TX * TY, transport_smem(1, TX, TY), L.stream>>>(L.runs, L.items, L.n, in_set, out_set, frac, stage, TX, TY); break;
   }
 }
 void launch_fill_partial(const Launch& L, int set) { k_fill_partial<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set); }
@@ -839,10 +889,10 @@ cudaError_t set_smem_limits(int bytes) {
   if ((e = cudaFuncSetAttribute(k_proj_div_xfft, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
   if ((e = cudaFuncSetAttribute(k_proj_xifft, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
   if ((e = cudaFuncSetAttribute(k_sediment, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(k_transport<TK_WENO>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(k_transport<TK_LIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(k_transport<TK_W>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(k_transport<TK_TH>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(k_transport<TK_WENO, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(k_transport<TK_LIN, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(k_transport<TK_W, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(k_transport<TK_TH, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
   return cudaSuccess;
 }
 

@@ -267,9 +267,10 @@ int build_plan(sg_context* ctx, const std::vector<int>& slots, Plan& P) {
     for (int k = 0; k < r.nz - 1; k++) for (int y = 0; y < r.ny; y += YC) all[FAM_ROWS_PRES].push_back(make_int4(s, k, y, 0));
     for (int m = 0; m < r.nx / 2 + 1; m++) all[FAM_MODES].push_back(make_int4(s, m, 0, 0));
     int tiles = ((r.nx + P.TX - 1) / P.TX) * ((r.ny + P.TY - 1) / P.TY);
-    for (int f = 0; f < NF; f++) {
-      int fam = f == W ? FAM_T_W : f == THETA ? FAM_T_TH : (f == U || f == V) ? FAM_T_LIN : FAM_T_WENO;
-      for (int t = 0; t < tiles; t++) all[fam].push_back(make_int4(s, f, t, 0));
+    // transport items: (run, field group, tile); groups 0-2 WENO fields in threes, 3 {u, v}, 4 {w}, 5 {theta}
+    for (int grp = 0; grp < 6; grp++) {
+      int fam = grp < 3 ? FAM_T_WENO : grp == 3 ? FAM_T_LIN : grp == 4 ? FAM_T_W : FAM_T_TH;
+      for (int t = 0; t < tiles; t++) all[fam].push_back(make_int4(s, grp, t, 0));
     }
     all[FAM_RUNS].push_back(make_int4(s, 0, 0, 0));
   }
