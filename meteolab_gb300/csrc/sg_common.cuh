@@ -13,6 +13,7 @@
 // theta is carried as its departure from the base profile theta_b(z) (the full value only at the ABI boundary).
 #pragma once
 #include <stdint.h>
+#include <cmath>
 
 #ifdef __CUDACC__
 #define SG_HD __host__ __device__ __forceinline__
@@ -47,6 +48,7 @@ enum Level {
   L_SPONGE,                                             // sponge rate * dt share (0 below the sponge)
   L_NODEMASS,                                           // dx dy hz rho (water budget)
   L_LW,                                                 // level weight hz/dz rho (positivity fix)
+  L_NODEMASS_LO, L_LW_LO,                               // their FP32 rounding errors (compensated sums)
   L_SURF,                                               // surface flux share per metre (sharesAbove)
   L_TCB,                                                // theta_b exner - 273.15 (Celsius base temperature)
   L_QW_HI, L_QW_LO, L_BW, L_QI_HI, L_QI_LO, L_BI, L_Q0_HI, L_Q0_LO,  // saturation bases (sg_physics.cuh Level)
@@ -93,46 +95,98 @@ constexpr int CHUNK = 4096;   // nodes per pointwise work item
 SG_HD float lvl(const RunDesc& R, int which, int z) { return R.lv[which * R.nz + z]; }
 SG_HD float* field(const RunDesc& R, int set, int f) { return R.fld + ((size_t)set * NF + f) * R.n; }
 
-// ---------------------------------------------------------------- reconstructions (src/core/advection.ts:385-399)
-// Linear fifth-order upwind value at the face between c and d for flow from a towards e.
-SG_HD float upwind5(float a, float b, float c, float d, float e) {
-  return (2.f * a - 13.f * b + 47.f * c + 27.f * d - 3.f * e) * (1.f / 60.f);
+// ---- face reconstruction. Every operation is an explicitly rounded one (no contraction left to the compiler), so
+// a face gets the same bits whether it is computed alone (Op1, here and on the host) or paired with another face on
+// Blackwell's packed FP32 pipes (Op2, in the transport kernel).
+struct Op1 {
+  using T = float;
+#ifdef __CUDA_ARCH__
+  static __device__ __forceinline__ T mul(T a, T b) { return __fmul_rn(a, b); }
+  static __device__ __forceinline__ T fma(T a, T b, T c) { return __fmaf_rn(a, b, c); }
+  static __device__ __forceinline__ T add(T a, T b) { return __fadd_rn(a, b); }
+#else
+  static T mul(T a, T b) { return a * b; }
+  static T fma(T a, T b, T c) { return std::fma(a, b, c); }
+  static T add(T a, T b) { return a + b; }
+#endif
+  SG_HD static T k(float v) { return v; }
+};
+
+// WENO5 on values already scaled so the largest is in [1, 2) (the Jiang-Shu weights with the reference's scale-aware
+// epsilon 2e-7 sum q^2, src/core/advection.ts:388-399), written about the centre value c: the face value is
+// c + num / den, where num / den is the weighted average of the three candidates' departures from c. In exact
+// arithmetic this is the reference's sum w_k p_k / sum w_k; in FP32 a uniform stencil gives c exactly (all departures
+// are 0) and smooth data keep the rounding of the small correction only. alpha_k = d_k / beta_k^2 is multiplied
+// through by the three beta^2, so one division remains.
+template <class O>
+SG_HD void weno_core(typename O::T a, typename O::T b, typename O::T c, typename O::T d, typename O::T e, typename O::T& num,
+                     typename O::T& den) {
+  using T = typename O::T;
+  const T m1 = O::k(-1.f), two = O::k(2.f), m2 = O::k(-2.f), m4 = O::k(-4.f);
+  const T da = O::fma(c, m1, a), db = O::fma(c, m1, b), dd = O::fma(c, m1, d), de = O::fma(c, m1, e);
+  // six times the candidates' departures from c: p0 = (2a - 7b + 11c)/6, p1 = (-b + 5c + 2d)/6, p2 = (2c + 5d - e)/6
+  const T p0 = O::fma(O::k(-7.f), db, O::mul(two, da));
+  const T p1 = O::fma(two, dd, O::mul(m1, db));
+  const T p2 = O::fma(m1, de, O::mul(O::k(5.f), dd));
+  // smoothness: s0 = a - 2b + c, t0 = a - 4b + 3c, s1 = b - 2c + d, t1 = b - d, s2 = c - 2d + e, t2 = 3c - 4d + e
+  const T s0 = O::fma(m2, db, da), t0 = O::fma(m4, db, da);
+  const T s1 = O::add(db, dd), t1 = O::fma(m1, dd, db);
+  const T s2 = O::fma(m2, dd, de), t2 = O::fma(m4, dd, de);
+  const T eps = O::mul(O::k(2e-7f), O::fma(e, e, O::fma(d, d, O::fma(c, c, O::fma(b, b, O::mul(a, a))))));
+  const T k13 = O::k(13.f / 12.f), q4 = O::k(.25f);
+  const T b0 = O::fma(O::mul(k13, s0), s0, O::fma(O::mul(q4, t0), t0, eps));
+  const T b1 = O::fma(O::mul(k13, s1), s1, O::fma(O::mul(q4, t1), t1, eps));
+  const T b2 = O::fma(O::mul(k13, s2), s2, O::fma(O::mul(q4, t2), t2, eps));
+  const T c0 = O::mul(b0, b0), c1 = O::mul(b1, b1), c2 = O::mul(b2, b2);
+  const T w0 = O::mul(O::mul(O::k(.1f), c1), c2), w1 = O::mul(O::mul(O::k(.6f), c0), c2), w2 = O::mul(O::mul(O::k(.3f), c0), c1);
+  num = O::fma(w2, p2, O::fma(w1, p1, O::mul(w0, p0)));
+  den = O::mul(O::k(6.f), O::add(O::add(w0, w1), w2));
 }
 
-// WENO5 (Jiang & Shu weights with the reference's scale-aware epsilon 2e-7 * sum q^2). The five values are first
-// scaled by an exact power of two that brings the largest to [1, 2): the weights are scale-free, so this changes
-// nothing in exact arithmetic, and in FP32 it keeps the squared products of water contents of 1e-6 kg/kg away from
-// underflow. All-zero input gives 0 exactly (the reference's early return).
-SG_HD float weno5(float a, float b, float c, float d, float e) {
-  float s = fmaxf(fmaxf(fabsf(a), fabsf(b)), fmaxf(fmaxf(fabsf(c), fabsf(d)), fabsf(e)));
+SG_HD int float_bits(float v) {
 #ifdef __CUDA_ARCH__
-  int ex = (__float_as_int(s) >> 23) & 0xff;
+  return __float_as_int(v);
 #else
-  int ex; { union { float f; int i; } u; u.f = s; ex = (u.i >> 23) & 0xff; }
-#endif
-  if (ex == 0) return 0.f;  // all zero (or below 1.2e-38)
-  float down, up;
-#ifdef __CUDA_ARCH__
-  down = __int_as_float((254 - ex) << 23); up = __int_as_float(ex << 23);
-#else
-  { union { float f; int i; } u; u.i = (254 - ex) << 23; down = u.f; u.i = ex << 23; up = u.f; }
-#endif
-  a *= down; b *= down; c *= down; d *= down; e *= down;
-  const float sixth = 1.f / 6.f;
-  float p0 = (2.f * a - 7.f * b + 11.f * c) * sixth, p1 = (-b + 5.f * c + 2.f * d) * sixth, p2 = (2.f * c + 5.f * d - e) * sixth;
-  float s0 = a - 2.f * b + c, t0 = a - 4.f * b + 3.f * c, s1 = b - 2.f * c + d, t1 = b - d, s2 = c - 2.f * d + e, t2 = 3.f * c - 4.f * d + e;
-  float eps = 2e-7f * (a * a + b * b + c * c + d * d + e * e);
-  const float k13 = 13.f / 12.f;
-  float b0 = eps + k13 * s0 * s0 + .25f * t0 * t0, b1 = eps + k13 * s1 * s1 + .25f * t1 * t1, b2 = eps + k13 * s2 * s2 + .25f * t2 * t2;
-  float c0 = b0 * b0, c1 = b1 * b1, c2 = b2 * b2;
-  float w0 = .1f * c1 * c2, w1 = .6f * c0 * c2, w2 = .3f * c0 * c1;
-  float num = w0 * p0 + w1 * p1 + w2 * p2, den = w0 + w1 + w2;
-#ifdef __CUDA_ARCH__
-  return __fdividef(num, den) * up;
-#else
-  return num / den * up;
+  union { float f; int i; } u; u.f = v; return u.i;
 #endif
 }
+SG_HD float bits_float(int v) {
+#ifdef __CUDA_ARCH__
+  return __int_as_float(v);
+#else
+  union { float f; int i; } u; u.i = v; return u.f;
+#endif
+}
+SG_HD float div_fast(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fdividef(a, b);
+#else
+  return a / b;
+#endif
+}
+// Biased exponent of the largest magnitude of a stencil; the values are scaled by the exact power of two that brings
+// it to [1, 2). The weights are scale-free, so this changes nothing in exact arithmetic, and in FP32 it keeps the
+// eighth powers inside the weights away from underflow for water contents of 1e-6 kg/kg.
+SG_HD int weno_exponent(float a, float b, float c, float d, float e) {
+  const float s = fmaxf(fmaxf(fabsf(a), fabsf(b)), fmaxf(fmaxf(fabsf(c), fabsf(d)), fabsf(e)));
+  return (float_bits(s) >> 23) & 0xff;
+}
+// WENO5 of one face. All-zero input (or all below 1.2e-38) gives 0, the reference's early return.
+SG_HD float weno5(float a, float b, float c, float d, float e) {
+  const int ex = weno_exponent(a, b, c, d, e);
+  if (ex == 0) return 0.f;
+  const float down = bits_float((254 - ex) << 23), up = bits_float(ex << 23);
+  float num, den;
+  weno_core<Op1>(Op1::mul(a, down), Op1::mul(b, down), Op1::mul(c, down), Op1::mul(d, down), Op1::mul(e, down), num, den);
+  return Op1::fma(div_fast(num, den), up, c);
+}
+// Linear fifth-order upwind (advection.ts:385): (2a - 13b + 47c + 27d - 3e) / 60.
+template <class O>
+SG_HD typename O::T upwind_core(typename O::T a, typename O::T b, typename O::T c, typename O::T d, typename O::T e) {
+  return O::mul(O::fma(O::k(-3.f), e, O::fma(O::k(27.f), d, O::fma(O::k(47.f), c, O::fma(O::k(-13.f), b, O::mul(O::k(2.f), a))))),
+                O::k(1.f / 60.f));
+}
+SG_HD float upwind5(float a, float b, float c, float d, float e) { return upwind_core<Op1>(a, b, c, d, e); }
 
 SG_HD int wrap(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 SG_HD int clampi(int i, int lo, int hi) { return i < lo ? lo : (i > hi ? hi : i); }

@@ -57,6 +57,53 @@ __device__ void blockSums(double (&v)[COUNT], double* out, double* sh /* >= 32*C
   __syncthreads();
 }
 
+// Compensated FP32 sums: a partial sum is kept as hi + lo (two FP32 words, about 48 significant bits) and terms are
+// added with TwoSum (Knuth), so the per-thread sums of the positivity fix and the water budget keep FP64-like accuracy
+// on the FP32 pipes (GB300 runs FP64 at a small fraction of its FP32 rate); warps combine them the same way and the
+// sums across warps and blocks are FP64. Every step is an explicitly rounded operation, and the xor-butterfly gives
+// every lane the same bits (TwoSum's error term does not depend on the operand order).
+__device__ __forceinline__ void df_add(float& hi, float& lo, float a) {
+  const float s = __fadd_rn(hi, a), bp = __fsub_rn(s, hi);
+  const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(a, bp));
+  hi = s; lo = __fadd_rn(lo, e);
+}
+// (hi, lo) += (whi + wlo) x, the product's rounding error included.
+__device__ __forceinline__ void df_add_prod(float& hi, float& lo, float whi, float wlo, float x) {
+  const float p = __fmul_rn(whi, x);
+  const float pe = __fmaf_rn(wlo, x, __fmaf_rn(whi, x, -p));
+  df_add(hi, lo, p);
+  lo = __fadd_rn(lo, pe);
+}
+__device__ __forceinline__ void df_norm(float& hi, float& lo) {
+  const float s = __fadd_rn(hi, lo);
+  lo = __fsub_rn(lo, __fsub_rn(s, hi)); hi = s;
+}
+template <int COUNT>
+__device__ void blockSumsDF(float (&hi)[COUNT], float (&lo)[COUNT], double* out, double* sh /* >= 32*COUNT */) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int c = 0; c < COUNT; c++) {
+    df_norm(hi[c], lo[c]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float h2 = __shfl_xor_sync(0xffffffffu, hi[c], o), l2 = __shfl_xor_sync(0xffffffffu, lo[c], o);
+      df_add(hi[c], lo[c], h2);
+      lo[c] = __fadd_rn(lo[c], l2);
+      df_norm(hi[c], lo[c]);
+    }
+  }
+  __syncthreads();
+  if (lane == 0)
+    for (int c = 0; c < COUNT; c++) sh[warp * COUNT + c] = (double)hi[c] + (double)lo[c];
+  __syncthreads();
+  if (threadIdx.x < COUNT) {
+    double s = 0;
+    for (int w = 0; w < nw; w++) s += sh[w * COUNT + threadIdx.x];
+    out[threadIdx.x] = s;
+  }
+  __syncthreads();
+}
+
 // ==================================================================== conversion at the ABI boundary
 // theta' = theta - theta_b(z) (FP64 difference) and back.
 __global__ void k_theta_in(const RunDesc* runs, const int4* items, int nitems, const float* src) {
@@ -373,26 +420,47 @@ __global__ void k_pres_correct(const RunDesc* runs, const int4* items, int nitem
 // projected face fluxes (FluxTransport.tendency, src/core/advection.ts:274-378), w with the stage buoyancy
 // (stageBuoyancy, model.ts:1204), theta' with the base profile's own vertical flux tendency, then the RK3 update
 // a = start + f dt tend (:1250) and, before a stage projection, w = 0 on the ground and the top (:1045).
-// Each field's planes z-3..z+3 (clamped at the ground and top, with a 3-node halo, periodic) sit in a 7-slot ring in
-// shared memory; per level one new plane per field is loaded (issued before the level's arithmetic, stored after it),
-// each x and y face is reconstructed once and exchanged through shared memory (double-buffered), the vertical faces
-// come from the ring, and one barrier separates the levels. The group shares the face-flux loads.
+// Each field's planes z-3..z+3 (clamped at the ground and top, with a 3-node periodic halo) sit in a 7-slot ring in
+// shared memory; per level one new plane per field arrives by asynchronous copies issued before the level's
+// arithmetic, every thread reconstructs the east and north faces of its own cell (as one packed pair) and the top face,
+// threads 0..TY-1 and TY..TY+TX-1 reconstruct the tile's west and south edge faces, the x and y faces are exchanged
+// through shared memory (double-buffered), and one barrier separates the levels. The group shares the face-flux loads.
 enum TKind { TK_WENO = 0, TK_LIN = 1, TK_W = 2, TK_TH = 3 };
 constexpr int TMAXC = 4;  // plane cells per thread: (TX + 6)(TY + 6) <= TMAXC * TX * TY
 constexpr int TLV = 9;    // per-level constants staged: 1/hz, 1/rho, theta faces x4, thb, qb, thv_env
-// Field groups of the transport work items: WENO {rain, snow, graupel}, {hail, q, cloud}, {ice, number, cold};
-// linear {u, v}; {w}; {theta}.
-__constant__ int TGROUP[6][3] = {{RAIN, SNOW, GRAUPEL}, {HAIL, Q, CLOUD}, {ICE, ICENUM, COLD}, {U, V, -1}, {W, -1, -1}, {THETA, -1, -1}};
+// Field groups of the transport work items: 0-2 the WENO fields in threes, 3 {u, v}, 4 {w}, 5 {theta}, 6-14 the WENO
+// fields one by one.
+constexpr int TGROUPS = 15;
+__constant__ int TGROUP[TGROUPS][3] = {{RAIN, SNOW, GRAUPEL}, {HAIL, Q, CLOUD}, {ICE, ICENUM, COLD}, {U, V, -1}, {W, -1, -1},
+                                       {THETA, -1, -1}, {RAIN, -1, -1}, {SNOW, -1, -1}, {GRAUPEL, -1, -1}, {HAIL, -1, -1},
+                                       {Q, -1, -1}, {CLOUD, -1, -1}, {ICE, -1, -1}, {ICENUM, -1, -1}, {COLD, -1, -1}};
 
+// Two faces at once on the packed FP32 pipes (bit-identical per face to the scalar weno5 / upwind5).
+struct Op2 {
+  using T = float2;
+  static __device__ __forceinline__ T mul(T a, T b) { return __fmul2_rn(a, b); }
+  static __device__ __forceinline__ T fma(T a, T b, T c) { return __ffma2_rn(a, b, c); }
+  static __device__ __forceinline__ T add(T a, T b) { return __fadd2_rn(a, b); }
+  static __device__ __forceinline__ T k(float v) { return make_float2(v, v); }
+};
+__device__ __forceinline__ float2 weno2(float2 a, float2 b, float2 c, float2 d, float2 e) {
+  const int ex = weno_exponent(a.x, b.x, c.x, d.x, e.x), ey = weno_exponent(a.y, b.y, c.y, d.y, e.y);
+  if ((ex | ey) == 0) return make_float2(0.f, 0.f);  // a warp of empty stencils skips the weights
+  const float2 down = make_float2(__int_as_float((254 - ex) << 23), __int_as_float((254 - ey) << 23));
+  float2 num, den;
+  weno_core<Op2>(__fmul2_rn(a, down), __fmul2_rn(b, down), __fmul2_rn(c, down), __fmul2_rn(d, down), __fmul2_rn(e, down), num, den);
+  return make_float2(ex ? __fmaf_rn(__fdividef(num.x, den.x), __int_as_float(ex << 23), c.x) : 0.f,
+                     ey ? __fmaf_rn(__fdividef(num.y, den.y), __int_as_float(ey << 23), c.y) : 0.f);
+}
 template <int KIND>
-__device__ __forceinline__ float trecon(float a, float b, float c, float d, float e) {
-  if (KIND == TK_WENO) {
-    // WENO of five zeros is zero: precipitation and ice are zero over most of a domain (the reference skips such
-    // rows, FluxTransport.markActiveRows, advection.ts), and a warp whose stencils are all zero skips the weights.
-    if (((__float_as_uint(a) | __float_as_uint(b) | __float_as_uint(c) | __float_as_uint(d) | __float_as_uint(e)) << 1) == 0u) return 0.f;
-    return weno5(a, b, c, d, e);
-  }
+__device__ __forceinline__ float recon1(float a, float b, float c, float d, float e) {
+  if (KIND == TK_WENO) return weno5(a, b, c, d, e);
   return upwind5(a, b, c, d, e);
+}
+template <int KIND>
+__device__ __forceinline__ float2 recon2(float2 a, float2 b, float2 c, float2 d, float2 e) {
+  if (KIND == TK_WENO) return weno2(a, b, c, d, e);
+  return upwind_core<Op2>(a, b, c, d, e);
 }
 
 // 4-byte asynchronous copy global -> shared (lands without passing through registers), and the wait for all of
@@ -402,6 +470,13 @@ __device__ __forceinline__ void cp_async4(float* dst, const float* src) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// The upwind stencil of a face along one axis (stride s) whose low-side cell is at P[-1] and high-side cell at P[0]:
+// for flow towards +axis the cells -3..1, else 2..-2 (mirrored).
+__device__ __forceinline__ void face_stencil(const float* P, int s, bool pos, float& a, float& b, float& c, float& d, float& e) {
+  if (pos) { a = P[-3 * s]; b = P[-2 * s]; c = P[-s]; d = P[0]; e = P[s]; }
+  else { a = P[2 * s]; b = P[s]; c = P[0]; d = P[-s]; e = P[-2 * s]; }
+}
 
 template <int KIND, int G>
 __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int tile, int in_set, int out_set, float frac, int stage,
@@ -422,17 +497,23 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
     st[g] = Rg.fld + (size_t)f * n;
     out[g] = Rg.fld + ((size_t)out_set * NF + f) * n;
   }
-  const int PW = TX + 6, PH = TY + 6, NCELL = PW * PH, NT = TX * TY;
+  const int PW = TX + 6, PH = TY + 6, NCELL = PW * PH;
   float* lv = sm;                                   // [TLV][MAXNZ]
   float* ring = lv + TLV * MAXNZ;                   // [G][7][NCELL]
-  float* fxs = ring + G * 7 * NCELL;                // [2][G][TY][TX + 1]
-  float* fys = fxs + 2 * G * TY * (TX + 1);         // [2][G][TY + 1][TX]
+  float* fxs = ring + G * 7 * NCELL;                // [2][G][TY][TX + 1]: x faces, west edge at column 0
+  float* fys = fxs + 2 * G * TY * (TX + 1);         // [2][G][TY + 1][TX]: y faces, south edge at row 0
   const int FXS = TY * (TX + 1), FYS = (TY + 1) * TX;
   const int t = threadIdx.x, lx = t % TX, ly = t / TX;
   const int tilesX = (nx + TX - 1) / TX, x0 = (tile % tilesX) * TX, y0 = (tile / tilesX) * TY;
   const int x = x0 + lx, y = y0 + ly;
-  const bool on = t < NT && x < nx && y < ny;
+  const bool on = x < nx && y < ny;
   const int col = on ? x + y * nx : 0;
+  // edge lanes: t < TY the west face of row t, TY <= t < TY + TX the south face of column t - TY
+  const bool edgeW = t < TY && y0 + t < ny, edgeS = t >= TY && t < TY + TX && x0 + t - TY < nx;
+  const int eoff = edgeW ? wrap(x0 - 1, nx) + (y0 + t) * nx : edgeS ? (x0 + t - TY) + wrap(y0 - 1, ny) * nx : 0;
+  const int ecell = edgeW ? (t + 3) * PW + 3 : (3 * PW + t - TY + 3);  // plane index of the cell on the edge's high side
+  const int estride = edgeW ? 1 : PW;
+  float* const edst = edgeW ? fxs + t * (TX + 1) : fys + (t - TY);
   for (int z = t; z < nz; z += blockDim.x) {
     lv[0 * MAXNZ + z] = lvl(Rg, L_INV_HZ, z);
     lv[1 * MAXNZ + z] = lvl(Rg, L_INV_RHO, z);
@@ -453,7 +534,6 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
     gx = ((gx % nx) + nx) % nx; gy = ((gy % ny) + ny) % ny;
     off[j] = e < NCELL ? gx + gy * nx : 0;
   }
-  const int offW = on ? wrap(x - 1, nx) + y * nx : 0, offS = on ? x + wrap(y - 1, ny) * nx : 0;
   const bool loadBuoy = KIND == TK_W && (flags & RF_STAGES);
   const bool loading = flags & RF_LOADING;
   // prologue: ring slots of the virtual levels -3..3 (clamped), level 0's inputs
@@ -465,7 +545,7 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
       for (int j = 0; j < TMAXC; j++) if (cell[j] >= 0) ring[(g * 7 + slot) * NCELL + cell[j]] = q[g][off[j] + lev * layer];
   }
   float4 fc = on ? F4[col] : make_float4(0.f, 0.f, 0.f, 0.f);
-  float mw = on && lx == 0 ? F4[offW].x : 0.f, ms = on && ly == 0 ? F4[offS].y : 0.f;
+  float me = edgeW ? F4[eoff].x : edgeS ? F4[eoff].y : 0.f;
   float s0[G];
 #pragma unroll
   for (int g = 0; g < G; g++) s0[g] = on && stage > 0 ? st[g][col] : 0.f;
@@ -484,52 +564,77 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
     const int buf = z & 1, l = z * layer;
     const bool more = z + 1 < nz;
     const int ln = l + layer;
-    // loads for later levels (issued before this level's arithmetic): the plane z + 4 into the freed ring slot
-    // (asynchronous copies), and level z + 1's faces, start values and buoyancy inputs
-    // (slot of z - 3, read last by the previous level before its barrier)
+    // loads for later levels, issued before this level's arithmetic: the plane z + 4 into the ring slot of z - 3
+    // (read last by the previous level, before its barrier) by asynchronous copies; level z + 1's faces, start values
+    // and buoyancy inputs into registers
     const int levNext = min(z + 4, nz - 1) * layer, s_new = (z + 4) % 7;
 #pragma unroll
     for (int g = 0; g < G; g++)
 #pragma unroll
       for (int j = 0; j < TMAXC; j++) if (cell[j] >= 0) cp_async4(ring + (g * 7 + s_new) * NCELL + cell[j], q[g] + off[j] + levNext);
     float4 fcn = make_float4(0.f, 0.f, 0.f, 0.f);
-    float mwn = 0.f, msn = 0.f, s0n[G], bn[8];
+    float men = 0.f, s0n[G], bn[8];
 #pragma unroll
     for (int g = 0; g < G; g++) s0n[g] = 0.f;
 #pragma unroll
     for (int j = 0; j < 8; j++) bn[j] = 0.f;
-    if (on && more) {
-      fcn = F4[col + ln];
-      if (lx == 0) mwn = F4[offW + ln].x;
-      if (ly == 0) msn = F4[offS + ln].y;
-      if (stage > 0) {
-#pragma unroll
-        for (int g = 0; g < G; g++) s0n[g] = st[g][col + ln];
-      }
-      if (loadBuoy) { bn[0] = inb[THETA * n + col + ln]; bn[1] = inb[Q * n + col + ln]; bn[2] = inb[CLOUD * n + col + ln]; bn[3] = inb[ICE * n + col + ln];
-        if (loading) { bn[4] = inb[RAIN * n + col + ln]; bn[5] = inb[SNOW * n + col + ln]; bn[6] = inb[GRAUPEL * n + col + ln]; bn[7] = inb[HAIL * n + col + ln]; } }
-    }
-    // faces of level z for each field
-    const float m1 = fc.x, m2 = fc.y, m3 = fc.z;
-    float fzU[G], qc[G];
-    const int s_m2 = (z + 5) % 7, s_m1 = (z + 6) % 7, s_0 = z % 7, s_p1 = (z + 1) % 7, s_p2 = (z + 2) % 7, s_p3 = (z + 3) % 7;
-#pragma unroll
-    for (int g = 0; g < G; g++) {
-      const float* R = ring + g * 7 * NCELL;
-      const float* P = R + s_0 * NCELL + cidx;
-      qc[g] = P[0];
-      fzU[g] = 0.f;
+    if (more) {
+      if (edgeW) men = F4[eoff + ln].x;
+      if (edgeS) men = F4[eoff + ln].y;
       if (on) {
-        float* FX = fxs + (buf * G + g) * FXS + ly * (TX + 1) + lx;
-        float* FY = fys + (buf * G + g) * FYS + ly * TX + lx;
-        FX[1] = m1 >= 0.f ? m1 * trecon<KIND>(P[-2], P[-1], P[0], P[1], P[2]) : m1 * trecon<KIND>(P[3], P[2], P[1], P[0], P[-1]);
-        if (lx == 0) FX[0] = mw >= 0.f ? mw * trecon<KIND>(P[-3], P[-2], P[-1], P[0], P[1]) : mw * trecon<KIND>(P[2], P[1], P[0], P[-1], P[-2]);
-        FY[TX] = m2 >= 0.f ? m2 * trecon<KIND>(P[-2 * PW], P[-PW], P[0], P[PW], P[2 * PW]) : m2 * trecon<KIND>(P[3 * PW], P[2 * PW], P[PW], P[0], P[-PW]);
-        if (ly == 0) FY[0] = ms >= 0.f ? ms * trecon<KIND>(P[-3 * PW], P[-2 * PW], P[-PW], P[0], P[PW]) : ms * trecon<KIND>(P[2 * PW], P[PW], P[0], P[-PW], P[-2 * PW]);
-        if (z < nz - 1) {
-          const float a2 = R[s_m2 * NCELL + cidx], a1 = R[s_m1 * NCELL + cidx], b1 = R[s_p1 * NCELL + cidx], b2 = R[s_p2 * NCELL + cidx], b3 = R[s_p3 * NCELL + cidx];
-          fzU[g] = m3 >= 0.f ? m3 * trecon<KIND>(a2, a1, qc[g], b1, b2) : m3 * trecon<KIND>(b3, b2, b1, qc[g], a1);
+        fcn = F4[col + ln];
+        if (stage > 0) {
+#pragma unroll
+          for (int g = 0; g < G; g++) s0n[g] = st[g][col + ln];
         }
+        if (loadBuoy) { bn[0] = inb[THETA * n + col + ln]; bn[1] = inb[Q * n + col + ln]; bn[2] = inb[CLOUD * n + col + ln]; bn[3] = inb[ICE * n + col + ln];
+          if (loading) { bn[4] = inb[RAIN * n + col + ln]; bn[5] = inb[SNOW * n + col + ln]; bn[6] = inb[GRAUPEL * n + col + ln]; bn[7] = inb[HAIL * n + col + ln]; } }
+      }
+    }
+    // faces of level z
+    const float m1 = fc.x, m2 = fc.y, m3 = fc.z;
+    const bool px = m1 >= 0.f, py = m2 >= 0.f, pz = m3 >= 0.f, top = z == nz - 1;
+    const int s_m2 = (z + 5) % 7, s_m1 = (z + 6) % 7, s_0 = z % 7, s_p1 = (z + 1) % 7, s_p2 = (z + 2) % 7, s_p3 = (z + 3) % 7;
+    float fzU[G], qc[G];
+    if (on) {
+#pragma unroll
+      for (int g = 0; g < G; g++) {
+        // east and north faces of this cell as one pair
+        const float* P = ring + (g * 7 + s_0) * NCELL + cidx;
+        qc[g] = P[0];
+        float2 A, B, C, D, E;
+        face_stencil(P + 1, 1, px, A.x, B.x, C.x, D.x, E.x);
+        face_stencil(P + PW, PW, py, A.y, B.y, C.y, D.y, E.y);
+        const float2 r = recon2<KIND>(A, B, C, D, E);
+        fxs[(buf * G + g) * FXS + ly * (TX + 1) + lx + 1] = m1 * r.x;
+        fys[(buf * G + g) * FYS + (ly + 1) * TX + lx] = m2 * r.y;
+      }
+      // top faces, fields in pairs
+#pragma unroll
+      for (int g = 0; g < G; g += 2) {
+        const int g2 = g + 1 < G ? g + 1 : g;
+        const float* R = ring + g * 7 * NCELL + cidx;
+        const float* S = ring + g2 * 7 * NCELL + cidx;
+        const float2 a2 = make_float2(R[s_m2 * NCELL], S[s_m2 * NCELL]), a1 = make_float2(R[s_m1 * NCELL], S[s_m1 * NCELL]);
+        const float2 c0 = make_float2(qc[g], qc[g2]), b1 = make_float2(R[s_p1 * NCELL], S[s_p1 * NCELL]);
+        const float2 b2 = make_float2(R[s_p2 * NCELL], S[s_p2 * NCELL]), b3 = make_float2(R[s_p3 * NCELL], S[s_p3 * NCELL]);
+        const float2 A = pz ? a2 : b3, B = pz ? a1 : b2, C = pz ? c0 : b1, D = pz ? b1 : c0, E = pz ? b2 : a1;
+        if (g + 1 < G) {
+          const float2 r = recon2<KIND>(A, B, C, D, E);
+          fzU[g] = top ? 0.f : m3 * r.x;
+          fzU[g + 1] = top ? 0.f : m3 * r.y;
+        } else {
+          fzU[g] = top ? 0.f : m3 * recon1<KIND>(A.x, B.x, C.x, D.x, E.x);
+        }
+      }
+    }
+    // the tile's west and south edge faces
+    if (edgeW || edgeS) {
+#pragma unroll
+      for (int g = 0; g < G; g++) {
+        float a, bb, c, d, e;
+        face_stencil(ring + (g * 7 + s_0) * NCELL + ecell, estride, me >= 0.f, a, bb, c, d, e);
+        edst[(buf * G + g) * (edgeW ? FXS : FYS)] = me * recon1<KIND>(a, bb, c, d, e);
       }
     }
     cp_async_wait_all();
@@ -561,7 +666,7 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
       }
     }
     mzD = m3;
-    fc = fcn; mw = mwn; ms = msn;
+    fc = fcn; me = men;
 #pragma unroll
     for (int g = 0; g < G; g++) s0[g] = s0n[g];
 #pragma unroll
@@ -590,30 +695,38 @@ __global__ void k_fill_partial(const RunDesc* runs, const int4* items, int nitem
     const RunDesc& R = runs[items[it].x];
     if (R.cnt[C_FAILED]) continue;
     const int chunk = items[it].y, i0 = chunk * CHUNK, i1 = min(R.n, i0 + CHUNK);
-    double v[NCONS * 3];
+    // per conserve field: removed (the tiny values the fix zeroes), kept (the rest), negative (-sum of the negatives)
+    float hi[NCONS * 3], lo[NCONS * 3];
 #pragma unroll
-    for (int k = 0; k < NCONS * 3; k++) v[k] = 0;
+    for (int k = 0; k < NCONS * 3; k++) hi[k] = lo[k] = 0.f;
     for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-      const double wz = lvl(R, L_LW, i / R.layer);
+      const int z = i / R.layer;
+      const float whi = lvl(R, L_LW, z), wlo = lvl(R, L_LW_LO, z);
 #pragma unroll
       for (int k = 0; k < NCONS; k++) {
-        float x = field(R, set, cons_field(k))[i];
-        if (x < 1e-10f) { if (x != 0.f) { v[3 * k] += wz * x; if (x < 0.f) v[3 * k + 2] -= wz * x; } }
-        else v[3 * k + 1] += wz * x;
+        const float x = field(R, set, cons_field(k))[i];
+        if (x < 1e-10f) {
+          if (x != 0.f) {
+            df_add_prod(hi[3 * k], lo[3 * k], whi, wlo, x);
+            if (x < 0.f) df_add_prod(hi[3 * k + 2], lo[3 * k + 2], whi, wlo, -x);
+          }
+        } else {
+          df_add_prod(hi[3 * k + 1], lo[3 * k + 1], whi, wlo, x);
+        }
       }
     }
-    blockSums<NCONS * 3>(v, R.part + (size_t)chunk * NCONS * 3, sh);
+    blockSumsDF<NCONS * 3>(hi, lo, R.part + (size_t)chunk * NCONS * 3, sh);
   }
 }
-// Per run: the scale of each conserve field, kept as delta = scale - 1 so a * scale rounds once (fma).
+// Per run: the scale of each conserve field, kept as delta = scale - 1 so a * scale rounds once (fma). Thread k sums
+// field k's block partials (FP64, in chunk order).
 __global__ void k_fill_final(const RunDesc* runs, const int4* items, int nitems) {
+  __shared__ double negs[NCONS];
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
     if (R.cnt[C_FAILED]) continue;
-    if (threadIdx.x != 0) continue;
-    const int nch = (R.n + CHUNK - 1) / CHUNK;
-    double neg = 0;
-    for (int k = 0; k < NCONS; k++) {
+    const int nch = (R.n + CHUNK - 1) / CHUNK, k = threadIdx.x;
+    if (k < NCONS) {
       double removed = 0, kept = 0, negative = 0;
       for (int c = 0; c < nch; c++) {
         const double* p = R.part + ((size_t)c * NCONS + k) * 3;
@@ -622,9 +735,15 @@ __global__ void k_fill_final(const RunDesc* runs, const int4* items, int nitems)
       double delta = 0;
       if (!(removed == 0 && negative == 0)) delta = kept > 0 ? fmax(-1.0, removed / kept) : -1.0;
       R.scr[S_FILL + k] = (float)delta;
-      neg += negative;
+      negs[k] = negative;
     }
-    R.acc[A_NEG] += neg;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double neg = 0;
+      for (int j = 0; j < NCONS; j++) neg += negs[j];
+      R.acc[A_NEG] += neg;
+    }
+    __syncthreads();
   }
 }
 
@@ -640,7 +759,7 @@ __global__ void k_physics(const RunDesc* runs, const int4* items, int nitems, in
     float fill[NCONS];
 #pragma unroll
     for (int k = 0; k < NCONS; k++) fill[k] = R.scr[S_FILL + k];
-    double wsum[3] = {0, 0, 0};
+    float whi[3] = {0.f, 0.f, 0.f}, wlo[3] = {0.f, 0.f, 0.f};
     bool bad = false;
     for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
       const int z = i / R.layer;
@@ -670,8 +789,12 @@ __global__ void k_physics(const RunDesc* runs, const int4* items, int nitems, in
       const float ue = lvl(R, L_UENV, z), ve = lvl(R, L_VENV, z);
       float du = (u - ue) * R.keep, dvv = (v - ve) * R.keep;
       u = ue + du + R.coriolis * dvv * dt; v = ve + dvv - R.coriolis * du * dt;
-      const double nm = lvl(R, L_NODEMASS, z);
-      { float dq = s.q - q0; if (dq < 0.f) wsum[0] -= nm * dq; else wsum[1] += nm * dq; if (evap > 0.f) wsum[2] += nm * evap; }
+      const float nmh = lvl(R, L_NODEMASS, z), nml = lvl(R, L_NODEMASS_LO, z);
+      {
+        const float dq = s.q - q0;
+        if (dq < 0.f) df_add_prod(whi[0], wlo[0], nmh, nml, -dq); else df_add_prod(whi[1], wlo[1], nmh, nml, dq);
+        if (evap > 0.f) df_add_prod(whi[2], wlo[2], nmh, nml, evap);
+      }
       s.cold = s.cold < 1e-3f ? 0.f : fminf(s.cold, 15.f);
       const float sp = lvl(R, L_SPONGE, z);
       if (sp > 0.f) { w *= 1.f - sp; u += (ue - u) * sp; v += (ve - v) * sp; s.thp += (0.f - s.thp) * sp; }
@@ -683,7 +806,7 @@ __global__ void k_physics(const RunDesc* runs, const int4* items, int nitems, in
     }
     if (__syncthreads_or(bad) && threadIdx.x == 0) atomicExch(&R.cnt[C_FAILED], 1ull);
     size_t nch = (R.n + CHUNK - 1) / CHUNK;
-    blockSums<3>(wsum, R.part + nch * NCONS * 3 + (size_t)chunk * 4, sh);
+    blockSumsDF<3>(whi, wlo, R.part + nch * NCONS * 3 + (size_t)chunk * 4, sh);
   }
 }
 
@@ -865,16 +988,20 @@ void launch_pres_correct(const Launch& L, int set, int final_) { k_pres_correct<
 size_t transport_smem(int G, int TX, int TY) {
   return ((size_t)TLV * MAXNZ + (size_t)G * 7 * (TX + 6) * (TY + 6) + 2 * (size_t)G * TY * (TX + 1) + 2 * (size_t)G * (TY + 1) * TX) * sizeof(float);
 }
-void launch_transport(const Launch& L, int kind, int in_set, int out_set, float frac, int stage, int TX, int TY) {
+void launch_transport(const Launch& L, int kind, int group, int in_set, int out_set, float frac, int stage, int TX, int TY) {
   if (L.n == 0) return;
   dim3 g = GRID(L.n, L.cap);
   switch (kind) {
-    case TK_WENO: k_transport<TK_WENO, 3><<<g, TX * TY, transport_smem(3, TX, TY), L.stream>>>(L.runs, L.items, L.n, in_set, out_set, frac, stage, TX, TY); break;
+    case TK_WENO:
+      if (group == 3) k_transport<TK_WENO, 3><<<g, TX * TY, transport_smem(3, TX, TY), L.stream>>>(L.runs, L.items, L.n, in_set, out_set, frac, stage, TX, TY);
+      else k_transport<TK_WENO, 1><<<g, TX * TY, transport_smem(1, TX, TY), L.stream>>>(L.runs, L.items, L.n, in_set, out_set, frac, stage, TX, TY);
+      break;
     case TK_LIN: k_transport<TK_LIN, 2><<<g, TX * TY, transport_smem(2, TX, TY), L.stream>>>(L.runs, L.items, L.n, in_set, out_set, frac, stage, TX, TY); break;
     case TK_W: k_transport<TK_W, 1><<<g, TX * TY, transport_smem(1, TX, TY), L.stream>>>(L.runs, L.items, L.n, in_set, out_set, frac, stage, TX, TY); break;
     default: k_transport<TK_TH, 1><<<g, TX * TY, transport_smem(1, TX, TY), L.stream>>>(L.runs, L.items, L.n, in_set, out_set, frac, stage, TX, TY); break;
   }
 }
+
 void launch_fill_partial(const Launch& L, int set) { k_fill_partial<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set); }
 void launch_fill_final(const Launch& L) { k_fill_final<<<GRID(L.n, L.cap), 32, 0, L.stream>>>(L.runs, L.items, L.n); }
 void launch_physics(const Launch& L, int in, int mid) { k_physics<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, in, mid); }
@@ -890,6 +1017,7 @@ cudaError_t set_smem_limits(int bytes) {
   if ((e = cudaFuncSetAttribute(k_proj_xifft, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
   if ((e = cudaFuncSetAttribute(k_sediment, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
   if ((e = cudaFuncSetAttribute(k_transport<TK_WENO, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(k_transport<TK_WENO, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
   if ((e = cudaFuncSetAttribute(k_transport<TK_LIN, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
   if ((e = cudaFuncSetAttribute(k_transport<TK_W, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
   if ((e = cudaFuncSetAttribute(k_transport<TK_TH, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;

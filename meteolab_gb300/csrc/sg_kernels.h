@@ -25,7 +25,9 @@ void launch_proj_xifft(const Launch& L, int mode, int yc, int maxnx);
 void launch_face_correct(const Launch& L, int set);
 void launch_pres_correct(const Launch& L, int set, int final_);
 // kind: 0 WENO fields, 1 u and v, 2 w, 3 theta (the item list of that kind)
-void launch_transport(const Launch& L, int kind, int in_set, int out_set, float frac, int stage, int TX, int TY);
+// Transport of one field kind (0 WENO, 1 {u, v}, 2 w, 3 theta); for WENO `group` is the fields per item (1 or 3).
+void launch_transport(const Launch& L, int kind, int group, int in_set, int out_set, float frac, int stage, int TX, int TY);
+size_t transport_smem(int G, int TX, int TY);
 void launch_fill_partial(const Launch& L, int set);
 void launch_fill_final(const Launch& L);
 void launch_physics(const Launch& L, int in, int mid);

@@ -9,6 +9,8 @@
 #include <cstdio>
 #include <cstring>
 #include <deque>
+#include <array>
+#include <functional>
 #include <map>
 #include <memory>
 #include <string>
@@ -31,7 +33,7 @@ const double RK3[3] = {1.0 / 3, 1.0 / 2, 1.0};
 size_t align(size_t x) { return (x + ALIGN - 1) / ALIGN * ALIGN; }
 
 struct Layout {
-  size_t fld, faces, kmkh, phi, pres, spec, cols, lv, lv64, triF, triP, ab, twx, twy, scr, part, acc, cnt, total;
+  size_t fld, faces, kmkh, phi, pres, spec, cols, lv, lv64, triF, triP, ab, twx, twy, scr, part, acc, cnt, items, total;
 };
 Layout layout(int nx, int ny, int nz) {
   Layout L; size_t n = (size_t)nx * ny * nz, layer = (size_t)nx * ny, nm = nx / 2 + 1, nch = (n + CHUNK - 1) / CHUNK, o = 0;
@@ -41,7 +43,9 @@ Layout layout(int nx, int ny, int nz) {
   L.lv = take((size_t)L_COUNT * nz * 4); L.lv64 = take((size_t)D_COUNT * nz * 8);
   L.triF = take(nm * nz * ny * 16); L.triP = take(nm * (nz - 1) * ny * 16); L.ab = take(nm * ny * 16);
   L.twx = take(nx * 8); L.twy = take(ny * 8); L.scr = take(64 * 4); L.part = take((nch * NCONS * 3 + nch * 4) * 8);
-  L.acc = take(A_COUNT * 8); L.cnt = take(C_COUNT * 8); L.total = o;
+  L.acc = take(A_COUNT * 8); L.cnt = take(C_COUNT * 8);
+  L.items = take(nch * 16);  // the run's own per-node work items (field conversions outside a batch plan)
+  L.total = o;
   return L;
 }
 
@@ -52,13 +56,16 @@ struct Run {
   size_t bytes = 0;
   char* mem = nullptr;
   RunDesc desc{};
+  int4* nodeItems = nullptr;  // inside mem
+  int nNode = 0;
 };
 
 struct Plan {
   std::vector<int> slots;
   int4* items = nullptr;  // device
   int off[16] = {0}, cnt[16] = {0};
-  int maxnx = 0, maxny = 0, maxnz = 0, TX = 40, TY = 8;
+  int maxnx = 0, maxny = 0, maxnz = 0, TX = 40, TY = 8, wenoG = 3;  // transport tile and WENO fields per item
+  bool tuned = false;                                                 // TX, TY, wenoG chosen by timing
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   ~Plan() {
@@ -83,6 +90,13 @@ struct sg_context {
   uint64_t pooled = 0;
   std::string error;
   double* d_scalar = nullptr;           // scratch for reductions read back by the host
+  // The four transport kinds of an RK3 stage run as parallel branches of the step's graph.
+  cudaStream_t side[3] = {nullptr, nullptr, nullptr};
+  cudaEvent_t fork = nullptr, join[3] = {nullptr, nullptr, nullptr};
+  bool forking = false;                 // set while a step is captured into a graph
+  bool autotune = true;
+  int pinned[3] = {0, 0, 0};            // transport tile and WENO group fixed by the caller (TX = 0: tune)
+  std::map<std::vector<int>, std::array<int, 3>> tuning;  // batch signature -> (TX, TY, wenoG)
 };
 
 namespace {
@@ -151,6 +165,8 @@ void build_tables(const sg_grid* g, const sg_base_state* b, const sg_switches* s
     L(L_SPONGE, z, sp);
     L(L_NODEMASS, z, dx * dy * hz[z] * rho[z]);
     L(L_LW, z, hz[z] / dzMean * rho[z]);
+    L(L_NODEMASS_LO, z, dx * dy * hz[z] * rho[z] - (double)(float)(dx * dy * hz[z] * rho[z]));
+    L(L_LW_LO, z, hz[z] / dzMean * rho[z] - (double)(float)(hz[z] / dzMean * rho[z]));
     L(L_SURF, z, 0);
     L(L_TCB, z, thb[z] * b->exner[z] - 273.15);
     {
@@ -241,21 +257,44 @@ Run* find(sg_context* ctx, sg_run run) {
 }
 
 // ------------------------------------------------------------------ plans
+// Transport work items (run, field group, tile) of a plan for a tile shape and WENO group size: groups 0-2 are the
+// WENO fields in threes, 6-14 one by one, 3 {u, v}, 4 {w}, 5 {theta}.
+void transport_items(sg_context* ctx, const std::vector<int>& slots, int TX, int TY, int wenoG, std::vector<int4>* fam) {
+  for (int s : slots) {
+    const Run& r = ctx->runs[s];
+    const int tiles = ((r.nx + TX - 1) / TX) * ((r.ny + TY - 1) / TY);
+    const int grp0 = wenoG == 3 ? 0 : 6, ngrp = wenoG == 3 ? 3 : 9;
+    for (int g = grp0; g < grp0 + ngrp; g++) for (int t = 0; t < tiles; t++) fam[0].push_back(make_int4(s, g, t, 0));
+    for (int k = 1; k < 4; k++) for (int t = 0; t < tiles; t++) fam[k].push_back(make_int4(s, 2 + k, t, 0));
+  }
+}
+
+int upload_items(sg_context* ctx, Plan& P, std::vector<int4>* all) {
+  std::vector<int4> flat;
+  for (int f = 0; f < FAM_COUNT; f++) { P.off[f] = (int)flat.size(); P.cnt[f] = (int)all[f].size(); flat.insert(flat.end(), all[f].begin(), all[f].end()); }
+  if (P.items) { cudaFree(P.items); P.items = nullptr; }
+  CK(cudaMalloc(&P.items, flat.size() * sizeof(int4)));
+  CK(cudaMemcpy(P.items, flat.data(), flat.size() * sizeof(int4), cudaMemcpyHostToDevice));
+  return SG_OK;
+}
+
+int autotune_transport(sg_context* ctx, Plan& P);
+
 int build_plan(sg_context* ctx, const std::vector<int>& slots, Plan& P) {
   P.slots = slots;
   std::vector<int4> all[FAM_COUNT];
-  bool all40 = true, all8 = true;
+  bool all40 = true;
   for (int s : slots) {
     const Run& r = ctx->runs[s];
     P.maxnx = std::max(P.maxnx, r.nx); P.maxny = std::max(P.maxny, r.ny); P.maxnz = std::max(P.maxnz, r.nz);
     if (r.nx % 40) all40 = false;
-    if (r.ny % 8) all8 = false;
   }
-  // Tile of the transport: 40 x 8 columns on the benchmark grids (40, 80, 320 wide), else 32 x 8 (a tile may be wider
-  // than a small grid: its halo wraps periodically and the threads beyond the grid only load).
-  (void)all8;
+  // Default transport tile: 40 x 8 columns when every grid is a multiple of 40 wide, else 32 x 8 (a tile may be
+  // wider than a small grid: its halo wraps periodically and the threads beyond the grid only load); the WENO fields
+  // in threes. The autotuner below replaces these by the fastest measured shape.
   P.TX = all40 ? 40 : 32;
   P.TY = 8;
+  P.wenoG = 3;
   for (int s : slots) {
     const Run& r = ctx->runs[s];
     int n = r.nx * r.ny * r.nz, nch = (n + CHUNK - 1) / CHUNK, layer = r.nx * r.ny;
@@ -266,23 +305,99 @@ int build_plan(sg_context* ctx, const std::vector<int>& slots, Plan& P) {
     for (int k = 0; k < r.nz; k++) for (int y = 0; y < r.ny; y += YC) all[FAM_ROWS_FACE].push_back(make_int4(s, k, y, 0));
     for (int k = 0; k < r.nz - 1; k++) for (int y = 0; y < r.ny; y += YC) all[FAM_ROWS_PRES].push_back(make_int4(s, k, y, 0));
     for (int m = 0; m < r.nx / 2 + 1; m++) all[FAM_MODES].push_back(make_int4(s, m, 0, 0));
-    int tiles = ((r.nx + P.TX - 1) / P.TX) * ((r.ny + P.TY - 1) / P.TY);
-    // transport items: (run, field group, tile); groups 0-2 WENO fields in threes, 3 {u, v}, 4 {w}, 5 {theta}
-    for (int grp = 0; grp < 6; grp++) {
-      int fam = grp < 3 ? FAM_T_WENO : grp == 3 ? FAM_T_LIN : grp == 4 ? FAM_T_W : FAM_T_TH;
-      for (int t = 0; t < tiles; t++) all[fam].push_back(make_int4(s, grp, t, 0));
-    }
     all[FAM_RUNS].push_back(make_int4(s, 0, 0, 0));
   }
-  std::vector<int4> flat;
-  for (int f = 0; f < FAM_COUNT; f++) { P.off[f] = (int)flat.size(); P.cnt[f] = (int)all[f].size(); flat.insert(flat.end(), all[f].begin(), all[f].end()); }
-  CK(cudaMalloc(&P.items, flat.size() * sizeof(int4)));
-  CK(cudaMemcpy(P.items, flat.data(), flat.size() * sizeof(int4), cudaMemcpyHostToDevice));
-  return SG_OK;
+  if (ctx->pinned[0]) { P.TX = ctx->pinned[0]; P.TY = ctx->pinned[1]; P.wenoG = ctx->pinned[2]; }
+  transport_items(ctx, slots, P.TX, P.TY, P.wenoG, all + FAM_T_WENO);
+  int st = upload_items(ctx, P, all);
+  if (st != SG_OK) return st;
+  return ctx->autotune && !ctx->pinned[0] ? autotune_transport(ctx, P) : SG_OK;
 }
 
 Launch lx(sg_context* ctx, const Plan& P, int fam, int capPerSm = 8) {
   return Launch{ctx->d_runs, P.items + P.off[fam], P.cnt[fam], ctx->sms * capPerSm, ctx->stream};
+}
+
+// Transport launches: one block per item, so the hardware block scheduler balances items of uneven cost (tiles of
+// empty air skip their WENO weights) across the SMs.
+void launch_transport_kinds(sg_context* ctx, const Plan& P, int in, int out, float frac, int stage, bool fork, int hookBase,
+                            const std::function<void(int)>& hook) {
+  const int fams[4] = {FAM_T_WENO, FAM_T_LIN, FAM_T_W, FAM_T_TH};
+  if (fork) cudaEventRecord(ctx->fork, ctx->stream);
+  for (int k = 0; k < 4; k++) {
+    Launch L = lx(ctx, P, fams[k]);
+    L.cap = L.n;
+    if (fork && k > 0) { cudaStreamWaitEvent(ctx->side[k - 1], ctx->fork, 0); L.stream = ctx->side[k - 1]; }
+    if (L.n) launch_transport(L, k, P.wenoG, in, out, frac, stage, P.TX, P.TY);
+    if (fork && k > 0) cudaEventRecord(ctx->join[k - 1], ctx->side[k - 1]);
+    hook(hookBase + k);
+  }
+  if (fork) for (int k = 0; k < 3; k++) cudaStreamWaitEvent(ctx->stream, ctx->join[k], 0);
+}
+
+// Picks the transport tile (TX x TY columns) and WENO fields per item by timing every candidate on the plan's own
+// runs: the four transport kinds of one RK3 stage (set A in, set C out; C is scratch between steps), best of three
+// after a warm-up. Results are cached per batch signature (the sorted grid shapes, and the run count to a power of
+// two), so a serving loop whose batch changes run by run tunes each kind of batch once.
+int autotune_transport(sg_context* ctx, Plan& P) {
+  std::vector<int> sig;
+  for (int s : P.slots) { const Run& r = ctx->runs[s]; sig.push_back(r.nx); sig.push_back(r.ny); sig.push_back(r.nz); }
+  {
+    std::vector<std::array<int, 3>> dims;
+    for (size_t i = 0; i < sig.size(); i += 3) dims.push_back({sig[i], sig[i + 1], sig[i + 2]});
+    std::sort(dims.begin(), dims.end());
+    dims.erase(std::unique(dims.begin(), dims.end()), dims.end());
+    sig.clear();
+    for (auto& d : dims) sig.insert(sig.end(), d.begin(), d.end());
+    int c = 1; while (c < (int)P.slots.size()) c *= 2;
+    sig.push_back(c);
+  }
+  std::array<int, 3> best{P.TX, P.TY, P.wenoG};
+  auto it = ctx->tuning.find(sig);
+  if (it != ctx->tuning.end()) {
+    best = it->second;
+  } else {
+    static const int shapes[][2] = {{40, 8}, {32, 8}, {20, 8}, {16, 16}, {16, 8}, {40, 4}, {32, 4}, {8, 8}};
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
+    float bestMs = 1e30f;
+    Plan T;  // candidate items only
+    T.slots = P.slots; T.maxnx = P.maxnx; T.maxny = P.maxny; T.maxnz = P.maxnz;
+    for (auto& sh : shapes) {
+      const int TX = sh[0], TY = sh[1];
+      if (TX > 2 * P.maxnx || TY > 2 * P.maxny) continue;
+      for (int G : {3, 1}) {
+        if (transport_smem(G, TX, TY) > (size_t)ctx->maxSmem) continue;
+        std::vector<int4> all[FAM_COUNT];
+        transport_items(ctx, P.slots, TX, TY, G, all + FAM_T_WENO);
+        int st = upload_items(ctx, T, all);
+        if (st != SG_OK) { cudaEventDestroy(e0); cudaEventDestroy(e1); return st; }
+        T.TX = TX; T.TY = TY; T.wenoG = G;
+        float ms = 1e30f;
+        for (int rep = 0; rep < 4; rep++) {
+          cudaEventRecord(e0, ctx->stream);
+          launch_transport_kinds(ctx, T, 0, 2, 1.f / 3.f, 0, false, 0, [](int) {});
+          cudaEventRecord(e1, ctx->stream);
+          CK(cudaEventSynchronize(e1));
+          float t = 0; cudaEventElapsedTime(&t, e0, e1);
+          if (rep) ms = std::min(ms, t);
+        }
+        CK(cudaGetLastError());
+        if (ms < bestMs) { bestMs = ms; best = {TX, TY, G}; }
+      }
+    }
+    cudaEventDestroy(e0); cudaEventDestroy(e1);
+    ctx->tuning[sig] = best;
+  }
+  P.TX = best[0]; P.TY = best[1]; P.wenoG = best[2]; P.tuned = true;
+  std::vector<int4> all[FAM_COUNT];
+  for (int f = 0; f < FAM_COUNT; f++) {  // keep the other families, rebuild the transport ones
+    if (f >= FAM_T_WENO && f <= FAM_T_TH) continue;
+    all[f].resize(P.cnt[f]);
+    if (P.cnt[f]) CK(cudaMemcpy(all[f].data(), P.items + P.off[f], P.cnt[f] * sizeof(int4), cudaMemcpyDeviceToHost));
+  }
+  transport_items(ctx, P.slots, P.TX, P.TY, P.wenoG, all + FAM_T_WENO);
+  return upload_items(ctx, P, all);
 }
 
 // The step's launch sequence for a plan in five parts (the oracle's partition of AtmosphereModel.step):
@@ -294,7 +409,6 @@ void enqueue_part(sg_context* ctx, const Plan& P, int part, Hook hook) {
   const int A = 0, B = 1, C = 2;
   Launch node = lx(ctx, P, FAM_NODE), cols = lx(ctx, P, FAM_COLS), rf = lx(ctx, P, FAM_ROWS_FACE), rp = lx(ctx, P, FAM_ROWS_PRES);
   Launch modes = lx(ctx, P, FAM_MODES, 2), runs = lx(ctx, P, FAM_RUNS);
-  Launch tk[4] = {lx(ctx, P, FAM_T_WENO, 4), lx(ctx, P, FAM_T_LIN, 4), lx(ctx, P, FAM_T_W, 4), lx(ctx, P, FAM_T_TH, 4)};
   const int mthreads = std::min(512, std::max(256, 2 * P.maxny));
   const int mbudget = std::min(ctx->maxSmem, 200 * 1024);
   auto project = [&](int set, int final_) {
@@ -313,7 +427,7 @@ void enqueue_part(sg_context* ctx, const Plan& P, int part, Hook hook) {
     launch_face_correct(node, A); hook(5);
     const int in[3] = {A, B, C}, out[3] = {B, C, B};
     for (int s = 0; s < 3; s++) {
-      for (int k = 0; k < 4; k++) if (tk[k].n) { launch_transport(tk[k], k, in[s], out[s], (float)RK3[s], s, P.TX, P.TY); hook(18 + k); }
+      launch_transport_kinds(ctx, P, in[s], out[s], (float)RK3[s], s, ctx->forking, 18, hook);
       if (s < 2) project(out[s], 0);
     }
   } else if (part == 3) {
@@ -341,7 +455,7 @@ const char* KERNEL_NAMES[NKERNELS] = {"fall_courant", "sediment", "face_div_xfft
 Plan* get_plan(sg_context* ctx, const std::vector<int>& slots, int* status) {
   auto it = ctx->plans.find(slots);
   if (it != ctx->plans.end()) { *status = SG_OK; return it->second.get(); }
-  if (ctx->plans.size() > 64) ctx->plans.clear();
+  if (ctx->plans.size() > 256) ctx->plans.clear();
   auto P = std::make_unique<Plan>();
   *status = build_plan(ctx, slots, *P);
   if (*status != SG_OK) return nullptr;
@@ -353,7 +467,9 @@ Plan* get_plan(sg_context* ctx, const std::vector<int>& slots, int* status) {
 int ensure_graph(sg_context* ctx, Plan& P) {
   if (P.exec) return SG_OK;
   CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  ctx->forking = true;
   enqueue_step(ctx, P, [](int) {});
+  ctx->forking = false;
   cudaError_t e = cudaStreamEndCapture(ctx->stream, &P.graph);
   if (e != cudaSuccess) return cudaFail(ctx, e, "cudaStreamEndCapture");
   CK(cudaGraphInstantiate(&P.exec, P.graph, 0));
@@ -393,6 +509,7 @@ int batch_step(sg_context* ctx, const sg_run* runs, int n, int nsteps, bool wait
 }
 
 // A plan over one run for the boundary kernels (theta conversion).
+Launch node_launch(sg_context* ctx, const Run& r) { return Launch{ctx->d_runs, r.nodeItems, r.nNode, ctx->sms * 8, ctx->stream}; }
 Plan* single_plan(sg_context* ctx, int slot, int* st) { return get_plan(ctx, std::vector<int>{slot}, st); }
 
 }  // namespace
@@ -408,7 +525,7 @@ int sg_context_create(int device, uint64_t hbm_budget_bytes, sg_context** out) {
   if (device < 0 || device >= count) return SG_ERR_INVALID;
   auto* ctx = new sg_context;
   ctx->device = device;
-  cudaError_t e;
+  cudaError_t e = cudaSuccess;
   if ((e = cudaSetDevice(device)) != cudaSuccess) { delete ctx; return SG_ERR_DEVICE; }
   cudaDeviceProp prop;
   cudaGetDeviceProperties(&prop, device);
@@ -418,9 +535,14 @@ int sg_context_create(int device, uint64_t hbm_budget_bytes, sg_context** out) {
   if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess ||
       (e = cudaMalloc(&ctx->d_runs, MAX_SLOTS * sizeof(RunDesc))) != cudaSuccess ||
       (e = cudaMalloc(&ctx->d_scalar, 64 * sizeof(double))) != cudaSuccess ||
-      (e = set_smem_limits(ctx->maxSmem)) != cudaSuccess) {
+      (e = set_smem_limits(ctx->maxSmem)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming)) != cudaSuccess) {
     delete ctx; return SG_ERR_DEVICE;
   }
+  for (int k = 0; k < 3; k++)
+    if ((e = cudaStreamCreateWithFlags(&ctx->side[k], cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&ctx->join[k], cudaEventDisableTiming)) != cudaSuccess) { delete ctx; return SG_ERR_DEVICE; }
+  if (const char* a = getenv("SG_AUTOTUNE")) ctx->autotune = atoi(a) != 0;
   *out = ctx;
   return SG_OK;
 }
@@ -434,6 +556,8 @@ int sg_context_destroy(sg_context* ctx) {
   for (auto& p : ctx->pool) cudaFree(p.second);
   cudaFree(ctx->d_runs); cudaFree(ctx->d_scalar);
   cudaStreamDestroy(ctx->stream);
+  for (int k = 0; k < 3; k++) { cudaStreamDestroy(ctx->side[k]); cudaEventDestroy(ctx->join[k]); }
+  cudaEventDestroy(ctx->fork);
   delete ctx;
   return SG_OK;
 }
@@ -485,6 +609,14 @@ int sg_run_create(sg_context* ctx, const sg_grid* g, const sg_base_state* b, con
   CK(H2D(Lo.triF, T.triF.data(), T.triF.size() * 16)); CK(H2D(Lo.triP, T.triP.data(), T.triP.size() * 16));
   CK(H2D(Lo.ab, T.ab.data(), T.ab.size() * 16)); CK(H2D(Lo.twx, T.twx.data(), T.twx.size() * 8)); CK(H2D(Lo.twy, T.twy.data(), T.twy.size() * 8));
   CK(cudaMemcpyAsync(ctx->d_runs + slot, &d, sizeof(RunDesc), cudaMemcpyHostToDevice, ctx->stream));
+  {
+    const size_t n = (size_t)g->nx * g->ny * g->nz;
+    r.nNode = (int)((n + CHUNK - 1) / CHUNK);
+    std::vector<int4> items(r.nNode);
+    for (int c = 0; c < r.nNode; c++) items[c] = make_int4(slot, c, 0, 0);
+    r.nodeItems = (int4*)(mem + Lo.items);
+    CK(H2D(Lo.items, items.data(), items.size() * sizeof(int4)));
+  }
   CK(cudaStreamSynchronize(ctx->stream));
   *out = slot;
   if (init) {
@@ -507,11 +639,7 @@ int sg_run_write_fields(sg_context* ctx, sg_run run, uint32_t mask, const float*
     float* dst = r->desc.fld + (size_t)(f == THETA ? NF + THETA : f) * n;
     CK(cudaMemcpyAsync(dst, host[f], n * 4, cudaMemcpyHostToDevice, ctx->stream));
   }
-  if (mask & (1u << THETA)) {
-    int st; Plan* P = single_plan(ctx, run, &st);
-    if (!P) return st;
-    launch_theta_in(lx(ctx, *P, FAM_NODE), r->desc.fld + (size_t)(NF + THETA) * n);
-  }
+  if (mask & (1u << THETA)) launch_theta_in(node_launch(ctx, *r), r->desc.fld + (size_t)(NF + THETA) * n);
   CK(cudaStreamSynchronize(ctx->stream));
   return SG_OK;
 }
@@ -522,11 +650,7 @@ int sg_run_read_fields(sg_context* ctx, sg_run run, uint32_t mask, float* const*
   if (!r) return fail(ctx, SG_ERR_NOT_FOUND, "no run " + std::to_string(run));
   cudaSetDevice(ctx->device);
   size_t n = (size_t)r->nx * r->ny * r->nz;
-  if (mask & (1u << THETA)) {
-    int st; Plan* P = single_plan(ctx, run, &st);
-    if (!P) return st;
-    launch_theta_out(lx(ctx, *P, FAM_NODE), r->desc.fld + (size_t)(NF + THETA) * n);
-  }
+  if (mask & (1u << THETA)) launch_theta_out(node_launch(ctx, *r), r->desc.fld + (size_t)(NF + THETA) * n);
   for (int f = 0; f < NF; f++) {
     if (!(mask & (1u << f))) continue;
     if (!host[f]) return fail(ctx, SG_ERR_INVALID, "null field pointer");
@@ -674,6 +798,30 @@ int sg_run_divergence(sg_context* ctx, sg_run run, double* max_abs_div) {
 
 // ------------------------------------------------------------------ diagnostics
 extern "C" {
+int sg_set_transport_shape(sg_context* ctx, int tile_x, int tile_y, int weno_group) {
+  if (!ctx) return SG_ERR_INVALID;
+  if (tile_x == 0) { ctx->pinned[0] = 0; }
+  else {
+    if (tile_x < 1 || tile_y < 1 || tile_x * tile_y > 320 || tile_x * tile_y < tile_x + tile_y ||
+        (tile_x + 6) * (tile_y + 6) > 4 * tile_x * tile_y || (weno_group != 1 && weno_group != 3) ||
+        transport_smem(weno_group, tile_x, tile_y) > (size_t)ctx->maxSmem)
+      return fail(ctx, SG_ERR_INVALID, "transport shape out of range");
+    ctx->pinned[0] = tile_x; ctx->pinned[1] = tile_y; ctx->pinned[2] = weno_group;
+  }
+  cudaStreamSynchronize(ctx->stream);
+  ctx->plans.clear();
+  return SG_OK;
+}
+int sg_batch_transport_shape(sg_context* ctx, const sg_run* runs, int n, int* shape3) {
+  if (!ctx || !shape3) return SG_ERR_INVALID;
+  std::vector<int> slots;
+  int st = slots_of(ctx, runs, n, slots);
+  if (st != SG_OK) return st;
+  Plan* P = get_plan(ctx, slots, &st);
+  if (!P) return st;
+  shape3[0] = P->TX; shape3[1] = P->TY; shape3[2] = P->wenoG;
+  return SG_OK;
+}
 int sg_debug_step_part(sg_context* ctx, sg_run run, int part) {
   if (!ctx || part < 1 || part > 5) return SG_ERR_INVALID;
   if (!find(ctx, run)) return fail(ctx, SG_ERR_NOT_FOUND, "no run");

@@ -89,6 +89,8 @@ def load():
             L.sg_debug_step_part.argtypes = [vp, C.c_int32, i32]
             L.sg_debug_read_set.argtypes = [vp, C.c_int32, i32, i32, _FP]
             L.sg_debug_read_faces.argtypes = [vp, C.c_int32, _FP]
+            L.sg_set_transport_shape.argtypes = [vp, i32, i32, i32]
+            L.sg_batch_transport_shape.argtypes = [vp, C.POINTER(C.c_int32), i32, C.POINTER(C.c_int)]
             L.sg_server_create.argtypes = [vp, i32, C.POINTER(vp)]
             L.sg_server_destroy.argtypes = [vp]
             L.sg_server_submit.argtypes = [vp, C.POINTER(SgGrid), C.POINTER(SgBase), C.POINTER(SgSwitches), C.POINTER(_FP), i64, i64]
@@ -162,6 +164,17 @@ class Context:
         for r in runs:
             r.time += steps * r.spec.switches.dt
         return ms.value
+
+    def set_transport_shape(self, tile_x: int = 0, tile_y: int = 0, weno_group: int = 3):
+        """Pin the transport tile (tile_x x tile_y columns, 1 or 3 WENO fields per item); tile_x = 0 returns to tuning."""
+        self.check(load().sg_set_transport_shape(self.h, tile_x, tile_y, weno_group), "transport shape")
+
+    def transport_shape(self, runs: Sequence["Run"]) -> tuple:
+        """(tile_x, tile_y, weno_group) the batch of `runs` is stepped with."""
+        ids = (C.c_int32 * len(runs))(*[r.id for r in runs])
+        out = (C.c_int * 3)()
+        self.check(load().sg_batch_transport_shape(self.h, ids, len(runs), out), "transport shape")
+        return tuple(out)
 
     def synchronize(self):
         self.check(load().sg_synchronize(self.h), "synchronize")

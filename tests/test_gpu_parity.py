@@ -140,6 +140,33 @@ def test_runs_are_deterministic_and_batch_independent(ctx, storm):
         run.retire()
 
 
+@pytest.mark.parametrize("shape", [(40, 8, 3), (40, 8, 1), (32, 8, 3), (16, 16, 1), (8, 8, 3), (40, 4, 1)])
+def test_transport_tiles_give_the_same_bits(ctx, storm, shape):
+    """Every transport tile shape and WENO grouping (faces computed alone or as packed pairs) gives bitwise equal
+    fields; the autotuner may pick any of them."""
+    ctx.set_transport_shape(40, 8, 3)
+    ref = ctx.create(storm)
+    ref.step(2)
+    a = ref.read()
+    ctx.set_transport_shape(*shape)
+    r = ctx.create(storm)
+    r.step(2)
+    assert ctx.transport_shape([r]) == shape
+    b = r.read()
+    ctx.set_transport_shape(0)
+    for k in CARRIED:
+        assert np.array_equal(a[k], b[k]), (shape, k)
+    ref.retire(); r.retire()
+
+
+def test_autotuner_picks_a_valid_shape(ctx, storm):
+    runs = [ctx.create(storm) for _ in range(4)]
+    tx, ty, g = ctx.transport_shape(runs)
+    assert tx * ty <= 320 and g in (1, 3)
+    for r in runs:
+        r.retire()
+
+
 def test_serving_gives_the_same_result_alone_and_in_the_mix(ctx, storm):
     """Requests admitted while others are on the device finish with the fields they get when stepped alone."""
     from meteolab_gb300.runtime import Server
