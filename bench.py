@@ -43,6 +43,9 @@ def parse():
     p.add_argument("--spinup", type=int, default=300, help="untimed steps before the warm-up (15 simulated minutes), so the "
                    "timed steps see a developed storm with cloud and precipitation rather than the quiescent start")
     p.add_argument("--quick", action="store_true", help="skip the serving and stress-grid legs")
+    p.add_argument("--ncu-window", action="store_true",
+                   help="profiling driver: set up and spin up the ensemble, then run --steps eager steps between "
+                        "cudaProfilerStart/Stop (for ncu --profile-from-start off) and exit without timing")
     return p.parse_args()
 
 
@@ -56,6 +59,17 @@ def dist_setup(args):
         dist.init_process_group("gloo")
         pg = dist
     return rank, world, local, pg
+
+
+def rank_members(grid, members: int, rank: int):
+    """Replicas only: each rank steps its own ensemble, seeded by its rank; no data crosses ranks."""
+    from meteolab_gb300.scenarios import ensemble_members
+    return ensemble_members(grid, members, seed=2026 + rank)
+
+
+def job_value(cells_per_rank: int, world: int, steps: int, ms_max: float) -> float:
+    """Whole-job cell-steps/s: every rank's cells over the slowest rank's time."""
+    return cells_per_rank * world * steps / (ms_max * 1e-3)
 
 
 def barrier(pg):
@@ -202,19 +216,27 @@ def main():
 
     ctx = Context(local)
     grid = create_grid(DEFAULT_GRID)
-    members = ensemble_members(grid, args.members, seed=2026 + rank)
+    members = rank_members(grid, args.members, rank)
     runs = [ctx.create(s) for s in members]
     cells = sum(r.grid.n for r in runs)
 
     # ---- headline: the batched ensemble from its CUDA graph, device time, inputs resident
     if args.spinup:
         ctx.time_steps(runs, args.spinup)
+    if args.ncu_window:
+        ctx.time_steps(runs, 1, graph=False)  # plans and tuning outside the window
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        ctx.time_steps(runs, args.steps, graph=False)
+        torch.cuda.profiler.stop()
+        print(json.dumps({"ncu_window": True, "members": args.members, "steps": args.steps, "transport_tile": ctx.transport_shape(runs)}))
+        return
     ctx.time_steps(runs, max(3, args.warmup))
     barrier(pg)
     with Clocks(local) as clk:
         ms = ctx.time_steps(runs, args.steps)
     ms = allmax(pg, ms)
-    value = cells * world * args.steps / (ms * 1e-3)
+    value = job_value(cells, world, args.steps, ms)
 
     tile = ctx.transport_shape(runs)
     # ---- kernel profile (eager, CUDA events per launch) and the roofline of the transport

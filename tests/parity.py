@@ -36,3 +36,41 @@ def developed_state(spec: RunSpec, steps: int) -> RunSpec:
     m.step(spec.switches.dt, steps)
     fields = {k: m.get(k).astype(np.float32) for k in CARRIED}
     return RunSpec(spec.grid, spec.env, spec.switches, fields, spec.seed, spec.label + f"+{steps}")
+
+
+# ---- invariants of the reference's tests (src/core/fixtures.ts, src/core/pressure.ts)
+WATER = ("q", "cloud", "ice", "rain", "snow", "graupel", "hail")
+
+
+def level_mean(a, grid, z):
+    """Horizontal mean of a field at level z (levelMean, src/core/fixtures.ts:33-38)."""
+    return float(np.mean(np.asarray(a[z * grid.layer:(z + 1) * grid.layer], np.float64)))
+
+
+def water_total(fields, precipitation, spec):
+    """Total water in the air (mixing ratios weighted by rho0 h) plus what reached the ground, kg per m2 of ground
+    (totalWater, src/core/fixtures.ts:44-56)."""
+    g = spec.grid
+    total = 0.0
+    for z in range(g.nz):
+        sl = slice(z * g.layer, (z + 1) * g.layer)
+        level = sum(float(np.sum(np.asarray(fields[k][sl], np.float64))) for k in WATER)
+        total += g.hz[z] * spec.env.rho[z] * level / g.layer
+    return total + float(np.sum(np.asarray(precipitation, np.float64))) / g.layer
+
+
+def dual_divergence(u, v, w, grid, rho):
+    """Dual-cell divergence of rho0 u from the 8 corner nodes, FP64 (PressureSolver.divergence with dt = 1,
+    src/core/pressure.ts:50-66)."""
+    nx, ny, nz = grid.nx, grid.ny, grid.nz
+    U, V, W = (np.asarray(a, np.float64).reshape(nz, ny, nx) for a in (u, v, w))
+    sx = lambda a: np.roll(a, -1, axis=2)
+    sy = lambda a: np.roll(a, -1, axis=1)
+    lo, hi = slice(0, nz - 1), slice(1, nz)
+    r0 = (np.asarray(rho[:-1], np.float64) / 4)[:, None, None]
+    r1 = (np.asarray(rho[1:], np.float64) / 4)[:, None, None]
+    dz = np.asarray(grid.dzs[:nz - 1], np.float64)[:, None, None]
+    ddx = (r0 * (sx(U)[lo] + sx(sy(U))[lo] - U[lo] - sy(U)[lo]) + r1 * (sx(U)[hi] + sx(sy(U))[hi] - U[hi] - sy(U)[hi])) / grid.dx
+    ddy = (r0 * (sy(V)[lo] + sx(sy(V))[lo] - V[lo] - sx(V)[lo]) + r1 * (sy(V)[hi] + sx(sy(V))[hi] - V[hi] - sx(V)[hi])) / grid.dy
+    ddz = (r1 * (W[hi] + sx(W)[hi] + sy(W)[hi] + sx(sy(W))[hi]) - r0 * (W[lo] + sx(W)[lo] + sy(W)[lo] + sx(sy(W))[lo])) / dz
+    return ddx + ddy + ddz

@@ -1,0 +1,53 @@
+"""The C ABI library: it builds for sm_103a here, loads without a GPU, and exports every function include/stormgpu.h
+declares; the Python host mirror binds each of them. No compute call is made (no GPU on this machine)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "stormgpu.h")
+
+
+def declared():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(sg_\w+)\s*\(", src, flags=re.M)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from meteolab_gb300 import build
+    build.build()
+    return ctypes.CDLL(os.path.join(ROOT, "meteolab_gb300", "libstormgpu.so"))
+
+
+def test_header_declares_the_entry_points():
+    names = declared()
+    for must in ("sg_context_create", "sg_run_create", "sg_run_step", "sg_batch_step", "sg_run_read_fields",
+                 "sg_run_write_fields", "sg_run_read_columns", "sg_run_status", "sg_run_retire", "sg_last_error",
+                 "sg_context_destroy", "sg_server_submit", "sg_server_iterate", "sg_server_collect"):
+        assert must in names
+
+
+def test_library_exports_every_declared_function(lib):
+    missing = [n for n in declared() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_mirror_binds_every_declared_function(lib):
+    from meteolab_gb300 import runtime
+    src = open(runtime.__file__).read()
+    unbound = [n for n in declared() if n not in src]
+    assert not unbound, unbound
+
+
+def test_context_create_fails_cleanly_without_a_device(lib):
+    lib.sg_context_create.argtypes = [ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(ctypes.c_void_p)]
+    h = ctypes.c_void_p()
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a device is visible")
+    assert lib.sg_context_create(0, 0, ctypes.byref(h)) != 0
+    assert not h.value
