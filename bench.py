@@ -200,6 +200,72 @@ def reference_arm(args, rank, pg):
     print(json.dumps(line), flush=True)
 
 
+def serving_leg(ctx, rate: float, count: int, quantum: int):
+    """The serving configuration: an open Poisson stream of requests (seeded soundings, standard or large grid 3:1,
+    400-1200 steps) through the continuous-batching loop. Time-to-completion runs from a request's arrival to its
+    collected result; per-step latency is an iteration's wall time over the steps it advanced."""
+    import numpy as np
+    from meteolab_gb300.grid import DEFAULT_GRID, LARGE_GRID, create_grid
+    from meteolab_gb300.runtime import Server
+    from meteolab_gb300.scenarios import serving_requests
+    reqs = serving_requests(create_grid(DEFAULT_GRID), create_grid(LARGE_GRID), count, rate)
+    srv = Server(ctx, max_active=256)
+    srv.set_quantum(quantum)
+    done_at, step_ms, cells_steps = {}, [], 0
+    nxt, active, queued = 0, 0, 0
+    t0 = time.perf_counter()
+    while len(done_at) < count:
+        now = time.perf_counter() - t0
+        while nxt < count and reqs[nxt][0] <= now:
+            _, spec, steps = reqs[nxt]
+            srv.submit(spec, steps, nxt)
+            nxt += 1
+        if active or queued or nxt > len(done_at) + active:
+            ts = time.perf_counter()
+            tags, active, queued = srv.iterate()
+            te = time.perf_counter()
+            k = srv.last_steps
+            if k:
+                step_ms.append((te - ts) * 1e3 / k)
+            for t in tags:
+                srv.collect(t, reqs[t][1].grid.n)
+                done_at[t] = time.perf_counter() - t0
+                cells_steps += reqs[t][1].grid.n * reqs[t][2]
+        else:
+            time.sleep(max(0.0, min(0.01, reqs[nxt][0] - now)))
+    wall = time.perf_counter() - t0
+    srv.close()
+    ttc = np.array([done_at[t] - reqs[t][0] for t in range(count)])
+    return {"rate_per_s": rate, "requests": count, "quantum_steps": quantum, "wall_s": wall,
+            "p50_s": float(np.percentile(ttc, 50)), "p99_s": float(np.percentile(ttc, 99)),
+            "step_latency_p50_ms": float(np.percentile(step_ms, 50)), "step_latency_p99_ms": float(np.percentile(step_ms, 99)),
+            "cell_steps_s": cells_steps / wall}
+
+
+def uneven_leg(ctx, steps: int, spinup: int):
+    """48 standard + 16 large runs of a CAPE x shear regime grid in the same launches."""
+    from meteolab_gb300.grid import DEFAULT_GRID, LARGE_GRID, create_grid
+    from meteolab_gb300.scenarios import regime_runs
+    specs = regime_runs(create_grid(DEFAULT_GRID), create_grid(LARGE_GRID))
+    runs = [ctx.create(s) for s in specs]
+    if spinup:
+        ctx.time_steps(runs, spinup)
+    ctx.time_steps(runs, 3)
+    ms = ctx.time_steps(runs, steps)
+    cells = sum(r.grid.n for r in runs)
+    small = sum(r.grid.n for r in runs if r.grid.nx == 40)
+    tile = ctx.transport_shape(runs)
+    for r in runs:
+        r.retire()
+    v = cells * steps / (ms * 1e-3)
+    # Work items are per run, so no run is padded to another's size; the transport tiles overhang no grid edge
+    # when the tile width divides the grid widths.
+    waste = 0.0 if all(nx % tile[0] == 0 and ny % tile[1] == 0 for nx, ny in ((40, 32), (80, 64))) else None
+    return {"runs": "48 x 40x32x50 + 16 x 80x64x50", "cell_steps_s": v, "ms_per_step": ms / steps,
+            "standard_share_cell_steps_s": v * small / cells, "large_share_cell_steps_s": v * (cells - small) / cells,
+            "padding_waste": waste, "transport_tile": list(tile)}
+
+
 def main():
     args = parse()
     rank, world, local, pg = dist_setup(args)
@@ -252,11 +318,9 @@ def main():
     for r, buf in zip(runs, pinned):
         r.read(out=buf)
     def e2e_step():
-        for r, buf in zip(runs, pinned):
-            r.write(buf)
-        ctx.batch_step(runs, 1)
-        for r, buf in zip(runs, pinned):
-            r.read(out=buf)
+        ctx.write_fields(runs, pinned)
+        ctx.batch_step(runs, 1, wait=False)
+        ctx.read_fields(runs, pinned)
     for _ in range(2):
         e2e_step()
     e2e_n = max(3, args.steps // 4)
@@ -284,6 +348,8 @@ def main():
                        "graph_cell_steps_s": spec.grid.n * n / (graphed * 1e-3), "graph_ms_per_step": graphed / n}
         r.retire()
 
+    uneven = uneven_leg(ctx, max(5, args.steps // 2), args.spinup)
+    serving = None if args.quick else serving_leg(ctx, rate=4.0, count=32, quantum=10)
     cpu = cpu_baseline(10.0) if rank == 0 else None
     for r in runs:
         r.retire()
@@ -306,6 +372,8 @@ def main():
         "clocks": clk.summary(),
         "plain_single_run": plain,
         "batched_vs_plain_standard": value / world / plain["standard"]["graph_cell_steps_s"],
+        "uneven_batch": uneven,
+        "serving": serving,
         "kernels_ms_per_launch": {k: round(v[0], 5) for k, v in prof.items()},
     }
     print(json.dumps(line), flush=True)

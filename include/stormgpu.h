@@ -98,6 +98,11 @@ int sg_run_create(sg_context* ctx, const sg_grid* grid, const sg_base_state* bas
                   const float* const* init, sg_run* out);
 int sg_run_write_fields(sg_context* ctx, sg_run run, uint32_t mask, const float* const* host);
 int sg_run_read_fields(sg_context* ctx, sg_run run, uint32_t mask, float* const* host);
+/* The same for n runs at once (host[k * SG_NFIELDS + f] is run k's field f): all copies queued on the library's
+ * stream, one synchronisation at the end, so pinned host buffers move at full link speed. The batch of an ensemble
+ * runner that reads every member between samples (src/ensemble/member.ts:101-107). */
+int sg_batch_write_fields(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, const float* const* host);
+int sg_batch_read_fields(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, float* const* host);
 /* precipitation, hailGround, hailSize: nx*ny each (nullable); src/core/model.ts:253, :262. */
 int sg_run_read_columns(sg_context* ctx, sg_run run, float* precipitation, float* hail_ground, float* hail_size);
 /* The projection pressure of the last final projection, nx*ny*(nz-1) values (AtmosphereModel.pressure, :247). */
@@ -149,6 +154,11 @@ int sg_server_submit(sg_server* srv, const sg_grid* grid, const sg_base_state* b
 /* One iteration: admit what fits, advance every active run one step in one batch, retire finished runs.
  * done_tags/done_count receive the tags of runs finished in this iteration (cap entries). */
 int sg_server_iterate(sg_server* srv, int64_t* done_tags, int* done_count, int cap, int* active, int* queued);
+/* Steps an iteration may advance (default 1): each iteration advances every active run by min(quantum, the fewest
+ * steps any active run has left), so no run overshoots and new requests join at the next iteration boundary. */
+int sg_server_set_quantum(sg_server* srv, int steps);
+/* Steps the last sg_server_iterate advanced. */
+int sg_server_last_steps(sg_server* srv);
 /* Read a finished run's fields (mask/host as sg_run_read_fields; precipitation nullable) and retire it. Finished runs
  * stay resident, and are no longer stepped, until collected. */
 int sg_server_collect(sg_server* srv, int64_t tag, uint32_t mask, float* const* host, float* precipitation);

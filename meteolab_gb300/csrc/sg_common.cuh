@@ -14,6 +14,7 @@
 #pragma once
 #include <stdint.h>
 #include <cmath>
+#include <cstring>
 
 #ifdef __CUDACC__
 #define SG_HD __host__ __device__ __forceinline__
@@ -164,6 +165,47 @@ SG_HD float div_fast(float a, float b) {
   return a / b;
 #endif
 }
+// FP32 <-> FP64 conversions on the integer pipes (GB300 runs FP64, conversions included, at a small fraction of its
+// FP32 rate; the tridiagonal solves convert every value in and out). Bit manipulation of the IEEE 754 formats:
+// exact widening, and narrowing with round-to-nearest-even, for normal FP32 values and zeros; anything else (FP32
+// subnormals, out-of-range, Inf, NaN) takes the hardware conversion.
+SG_HD uint32_t dbl_hi(double d) {
+#ifdef __CUDA_ARCH__
+  return (uint32_t)__double2hiint(d);
+#else
+  uint64_t u; std::memcpy(&u, &d, 8); return (uint32_t)(u >> 32);
+#endif
+}
+SG_HD uint32_t dbl_lo(double d) {
+#ifdef __CUDA_ARCH__
+  return (uint32_t)__double2loint(d);
+#else
+  uint64_t u; std::memcpy(&u, &d, 8); return (uint32_t)u;
+#endif
+}
+SG_HD double dbl_make(uint32_t hi, uint32_t lo) {
+#ifdef __CUDA_ARCH__
+  return __hiloint2double((int)hi, (int)lo);
+#else
+  uint64_t u = ((uint64_t)hi << 32) | lo; double d; std::memcpy(&d, &u, 8); return d;
+#endif
+}
+SG_HD double widen(float f) {
+  const uint32_t b = (uint32_t)float_bits(f), mag = b & 0x7fffffffu;
+  if (mag == 0) return dbl_make(b, 0);                                    // signed zero
+  if (mag - 0x00800000u >= 0x7f000000u) return (double)f;                 // subnormal, Inf, NaN
+  return dbl_make((b & 0x80000000u) | ((mag >> 3) + (896u << 20)), mag << 29);  // exponent rebias 127 -> 1023
+}
+SG_HD float narrow(double d) {
+  const uint32_t hi = dbl_hi(d), lo = dbl_lo(d), e = (hi >> 20) & 0x7ffu;
+  if (((hi & 0x7fffffffu) | lo) == 0) return bits_float((int)(hi & 0x80000000u));  // signed zero
+  if (e - 897u > 253u) return (float)d;                                   // outside the normal FP32 range
+  const uint32_t m = ((hi & 0xfffffu) << 3) | (lo >> 29), rest = lo & 0x1fffffffu;
+  uint32_t bits = (hi & 0x80000000u) | ((e - 896u) << 23) | m;
+  if (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) bits += 1;  // a carry moves into the exponent
+  return bits_float((int)bits);
+}
+
 // Biased exponent of the largest magnitude of a stencil; the values are scaled by the exact power of two that brings
 // it to [1, 2). The weights are scale-free, so this changes nothing in exact arithmetic, and in FP32 it keeps the
 // eighth powers inside the weights away from underflow for water contents of 1e-6 kg/kg.

@@ -62,7 +62,42 @@ SG_HD void fft_butterfly(const float2* x, float2* y, int n, int r, int Ns, int j
   }
 }
 
+// The radix sequence of a length, known at compile time (the same order as fft_plan_factors below).
+constexpr int fft_count(int n) {
+  int nf = 0;
+  while (n % 4 == 0 && n > 1) { nf++; n /= 4; }
+  while (n % 2 == 0) { nf++; n /= 2; }
+  while (n % 3 == 0) { nf++; n /= 3; }
+  while (n % 5 == 0) { nf++; n /= 5; }
+  return n == 1 ? nf : -1;
+}
+constexpr int fft_radix_at(int n, int s) {
+  int nf = 0;
+  while (n % 4 == 0 && n > 1) { if (nf++ == s) return 4; n /= 4; }
+  while (n % 2 == 0) { if (nf++ == s) return 2; n /= 2; }
+  while (n % 3 == 0) { if (nf++ == s) return 3; n /= 3; }
+  while (n % 5 == 0) { if (nf++ == s) return 5; n /= 5; }
+  return 0;
+}
+
 #ifdef __CUDACC__
+// Forward transform of `rows` rows of a compile-time length N (stride `stride`), ping-ponging between `src` and `dst`:
+// every index division is by a constant. Returns the buffer that holds the result. Ends with the block synchronised.
+template <int N, int S = 0, int NS = 1>
+__device__ __forceinline__ float2* fft_rows_t(float2* src, float2* dst, int stride, int rows, const float2* tw) {
+  if constexpr (S >= fft_count(N)) {
+    return src;
+  } else {
+    constexpr int R = fft_radix_at(N, S), NB = N / R;
+    for (int u = threadIdx.x; u < rows * NB; u += blockDim.x) {
+      const int row = u / NB, j = u - row * NB;
+      fft_butterfly(src + row * stride, dst + row * stride, N, R, NS, j, tw);
+    }
+    __syncthreads();
+    return fft_rows_t<N, S + 1, NS * R>(dst, src, stride, rows, tw);
+  }
+}
+
 // Forward transform (exp(-i)) of `rows` rows of length P.n, row stride `stride`, in place in `a`, with scratch `b`
 // (same shape). All threads of the block take part; ends with the block synchronised.
 __device__ inline void fft_rows(float2* a, float2* b, int stride, int rows, const FftPlan& P) {
@@ -81,6 +116,21 @@ __device__ inline void fft_rows(float2* a, float2* b, int stride, int rows, cons
   if (src != a) {
     for (int u = tid; u < rows * n; u += nth) { int row = u / n, i = u - row * n; a[row * stride + i] = src[row * stride + i]; }
     __syncthreads();
+  }
+}
+// Forward transform of rows of any supported length: the compile-time path for the grid widths in use (32, 40, 64,
+// 80, 128, 160, 256, 320), the runtime plan for the others. Returns the buffer that holds the result (a or b).
+__device__ inline float2* fft_rows_any(float2* a, float2* b, int stride, int rows, const FftPlan& P) {
+  switch (P.n) {
+    case 32: return fft_rows_t<32>(a, b, stride, rows, P.tw);
+    case 40: return fft_rows_t<40>(a, b, stride, rows, P.tw);
+    case 64: return fft_rows_t<64>(a, b, stride, rows, P.tw);
+    case 80: return fft_rows_t<80>(a, b, stride, rows, P.tw);
+    case 128: return fft_rows_t<128>(a, b, stride, rows, P.tw);
+    case 160: return fft_rows_t<160>(a, b, stride, rows, P.tw);
+    case 256: return fft_rows_t<256>(a, b, stride, rows, P.tw);
+    case 320: return fft_rows_t<320>(a, b, stride, rows, P.tw);
+    default: fft_rows(a, b, stride, rows, P); return a;
   }
 }
 // Unnormalised inverse (exp(+i)): conj, forward, conj.

@@ -106,27 +106,29 @@ __device__ void blockSumsDF(float (&hi)[COUNT], float (&lo)[COUNT], double* out,
 
 // ==================================================================== conversion at the ABI boundary
 // theta' = theta - theta_b(z) (FP64 difference) and back.
-__global__ void k_theta_in(const RunDesc* runs, const int4* items, int nitems, const float* src) {
+__global__ void k_theta_in(const RunDesc* __restrict__ runs, const int4* items, int nitems, const float* src) {
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
     int i0 = items[it].y * CHUNK, i1 = min(R.n, i0 + CHUNK);
     float* th = field(R, 0, THETA);
-    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) th[i] = (float)((double)src[i] - R.lv64[D_THB * R.nz + i / R.layer]);
+    const float* s = src ? src : field(R, 1, THETA);  // null: each run's own staging slot (set B)
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) th[i] = (float)((double)s[i] - R.lv64[D_THB * R.nz + i / R.layer]);
   }
 }
-__global__ void k_theta_out(const RunDesc* runs, const int4* items, int nitems, float* dst) {
+__global__ void k_theta_out(const RunDesc* __restrict__ runs, const int4* items, int nitems, float* dst) {
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
     int i0 = items[it].y * CHUNK, i1 = min(R.n, i0 + CHUNK);
     const float* th = field(R, 0, THETA);
-    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) dst[i] = (float)((double)th[i] + R.lv64[D_THB * R.nz + i / R.layer]);
+    float* d = dst ? dst : field(R, 1, THETA);
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) d[i] = (float)((double)th[i] + R.lv64[D_THB * R.nz + i / R.layer]);
   }
 }
 
 // ==================================================================== beginStep
 // Fall speeds of the four falling fields and the largest Courant number dt Vt / h of each over its non-zero nodes
 // (fallParts, src/core/model.ts:575-580): the sedimentation's sub-step count.
-__global__ void k_fall_courant(const RunDesc* runs, const int4* items, int nitems) {
+__global__ void k_fall_courant(const RunDesc* __restrict__ runs, const int4* items, int nitems) {
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
     if (R.cnt[C_FAILED]) continue;
@@ -154,7 +156,7 @@ __global__ void k_fall_courant(const RunDesc* runs, const int4* items, int nitem
 // values above from before the sub-step, the ground flux into the rain gauge. Fall speeds are those of the step's
 // start. Columns stay in shared memory.
 constexpr int SED_COLS = 64;
-__global__ void k_sediment(const RunDesc* runs, const int4* items, int nitems) {
+__global__ void k_sediment(const RunDesc* __restrict__ runs, const int4* items, int nitems) {
   extern __shared__ float sm[];
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
@@ -203,54 +205,73 @@ __global__ void k_sediment(const RunDesc* runs, const int4* items, int nitems) {
 }
 
 // ==================================================================== elliptic solves
+// Exact row index of element e of a row-major block with rows of length `len` (e < 2^16): one multiply by the
+// reciprocal instead of an integer division.
+__device__ __forceinline__ int row_of(int e, float inv_len) { return __float2int_rz(((float)e + .5f) * inv_len); }
+
 // Divergence rows of one layer and their forward x-transform (real rows paired into complex ones, the reference's
 // trick, src/core/spectral.ts:246-255), written m-major: spec[(m * nzc + k) * ny + y].
 //  FACE: node divergence of the unprojected face mass fluxes rho0 * mean(u) (src/core/advection.ts:190-211).
 //  PRES: dual-cell divergence of rho0 u from the 8 corner nodes, over dt (src/core/pressure.ts:50-66).
-__global__ void k_proj_div_xfft(const RunDesc* runs, const int4* items, int nitems, int mode, int set, int yc) {
+__global__ void k_proj_div_xfft(const RunDesc* __restrict__ runs, const int4* items, int nitems, int mode, int set, int yc) {
   extern __shared__ float2 smc[];
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
     if (R.cnt[C_FAILED]) continue;
     const int k = items[it].y, y0 = items[it].z, nx = R.nx, ny = R.ny, layer = R.layer, nz = R.nz;
     const int rows = min(yc, ny - y0), pairs = (rows + 1) / 2, nzc = mode == PROJ_FACE ? nz : nz - 1;
+    const float inv_nx = 1.f / (float)nx;
     float2* Z = smc;                   // [pairs][nx]
     float2* T = smc + pairs * nx;      // scratch
     const float *u = field(R, set, U), *v = field(R, set, V), *w = field(R, set, W);
-    for (int e = threadIdx.x; e < pairs * 2 * nx; e += blockDim.x) {
-      int r = e / nx, x = e - r * nx, y = y0 + r;
-      float d = 0.f;
-      if (r < rows) {
-        if (mode == PROJ_FACE) {
-          const int l = k * layer, i = x + y * nx + l;
-          const int xe = wrap(x + 1, nx), xw = wrap(x - 1, nx), yn = wrap(y + 1, ny), ys = wrap(y - 1, ny);
-          float rho = lvl(R, L_RHO, k);
-          float ddx = .5f * rho * (u[xe + y * nx + l] - u[xw + y * nx + l]);
-          float ddy = .5f * rho * (v[x + yn * nx + l] - v[x + ys * nx + l]);
-          float up = k < nz - 1 ? .5f * lvl(R, L_RUP, k) * (w[i] + w[i + layer]) : 0.f;
-          float dn = k > 0 ? .5f * lvl(R, L_RUP, k - 1) * (w[i - layer] + w[i]) : 0.f;
-          d = ddx * R.inv_dx + ddy * R.inv_dy + (up - dn) * lvl(R, L_INV_HZ, k);
-        } else {
-          const int l0 = k * layer, x1 = wrap(x + 1, nx), y1 = wrap(y + 1, ny);
-          const int a = x + y * nx + l0, b = x1 + y * nx + l0, ee = x + y1 * nx + l0, f = x1 + y1 * nx + l0;
-          const int g = a + layer, h = b + layer, s = ee + layer, tt = f + layer;
-          float r0 = .25f * lvl(R, L_RHO, k), r1 = .25f * lvl(R, L_RHO, k + 1);
-          float ddx = (r0 * ((u[b] - u[a]) + (u[f] - u[ee])) + r1 * ((u[h] - u[g]) + (u[tt] - u[s]))) * R.inv_dx;
-          float ddy = (r0 * ((v[ee] - v[a]) + (v[f] - v[b])) + r1 * ((v[s] - v[g]) + (v[tt] - v[h]))) * R.inv_dy;
-          float ddz = (r1 * ((w[g] + w[h]) + (w[s] + w[tt])) - r0 * ((w[a] + w[b]) + (w[ee] + w[f]))) * lvl(R, L_INV_DZS, k);
-          d = (ddx + ddy + ddz) / R.dt;
+    const float idx = R.inv_dx, idy = R.inv_dy;
+    if (mode == PROJ_FACE) {
+      const float rho = lvl(R, L_RHO, k), ihz = lvl(R, L_INV_HZ, k);
+      const float rup = k < nz - 1 ? .5f * lvl(R, L_RUP, k) : 0.f, rdn = k > 0 ? .5f * lvl(R, L_RUP, k - 1) : 0.f;
+      const int l = k * layer, lu = k < nz - 1 ? l + layer : l, ld = k > 0 ? l - layer : l;
+#pragma unroll 4
+      for (int e = threadIdx.x; e < pairs * 2 * nx; e += blockDim.x) {
+        const int r = row_of(e, inv_nx), x = e - r * nx, y = y0 + r;
+        float d = 0.f;
+        if (r < rows) {
+          const int c = x + y * nx;
+          const int ce = (x + 1 == nx ? 0 : x + 1) + y * nx, cw = (x == 0 ? nx - 1 : x - 1) + y * nx;
+          const int cn = x + (y + 1 == ny ? 0 : y + 1) * nx, cs = x + (y == 0 ? ny - 1 : y - 1) * nx;
+          const float ddx = .5f * rho * (u[ce + l] - u[cw + l]);
+          const float ddy = .5f * rho * (v[cn + l] - v[cs + l]);
+          const float wc = w[c + l];
+          const float up = rup * (wc + w[c + lu]), dn = rdn * (w[c + ld] + wc);
+          d = ddx * idx + ddy * idy + (up - dn) * ihz;
         }
+        reinterpret_cast<float*>(&Z[(r >> 1) * nx + x])[r & 1] = d;
       }
-      float* zf = reinterpret_cast<float*>(&Z[(r >> 1) * nx + x]);
-      zf[r & 1] = d;
+    } else {
+      const float r0 = .25f * lvl(R, L_RHO, k), r1 = .25f * lvl(R, L_RHO, k + 1), idz = lvl(R, L_INV_DZS, k), idt = 1.f / R.dt;
+      const int l0 = k * layer, l1 = l0 + layer;
+#pragma unroll 4
+      for (int e = threadIdx.x; e < pairs * 2 * nx; e += blockDim.x) {
+        const int r = row_of(e, inv_nx), x = e - r * nx, y = y0 + r;
+        float d = 0.f;
+        if (r < rows) {
+          const int x1 = x + 1 == nx ? 0 : x + 1, y1 = (y + 1 == ny ? 0 : y + 1) * nx, yy = y * nx;
+          const int a = x + yy, b = x1 + yy, ee = x + y1, f = x1 + y1;
+          const float ddx = (r0 * ((u[b + l0] - u[a + l0]) + (u[f + l0] - u[ee + l0])) + r1 * ((u[b + l1] - u[a + l1]) + (u[f + l1] - u[ee + l1]))) * idx;
+          const float ddy = (r0 * ((v[ee + l0] - v[a + l0]) + (v[f + l0] - v[b + l0])) + r1 * ((v[ee + l1] - v[a + l1]) + (v[f + l1] - v[b + l1]))) * idy;
+          const float ddz = (r1 * ((w[a + l1] + w[b + l1]) + (w[ee + l1] + w[f + l1])) - r0 * ((w[a + l0] + w[b + l0]) + (w[ee + l0] + w[f + l0]))) * idz;
+          d = (ddx + ddy + ddz) * idt;
+        }
+        reinterpret_cast<float*>(&Z[(r >> 1) * nx + x])[r & 1] = d;
+      }
     }
     __syncthreads();
     FftPlan P{nx, R.fx_nf, R.fx_rad, R.twx};
-    fft_rows(Z, T, nx, pairs, P);
+    const float2* Zf = fft_rows_any(Z, T, nx, pairs, P);
     const int nm = R.nm;
+    const float inv_rows = 1.f / (float)rows;
     for (int e = threadIdx.x; e < nm * rows; e += blockDim.x) {
-      int m = e / rows, r = e - m * rows, pr = r >> 1, c = m ? nx - m : 0;
-      float2 zm = Z[pr * nx + m], zc = Z[pr * nx + c], out;
+      const int m = row_of(e, inv_rows), r = e - m * rows, pr = r >> 1, c = m ? nx - m : 0;
+      const float2 zm = Zf[pr * nx + m], zc = Zf[pr * nx + c];
+      float2 out;
       if ((r & 1) == 0) out = make_float2(.5f * (zm.x + zc.x), .5f * (zm.y - zc.y));
       else out = make_float2(.5f * (zm.y + zc.y), .5f * (zc.x - zm.x));
       R.spec[((size_t)m * nzc + k) * ny + y0 + r] = out;
@@ -260,58 +281,82 @@ __global__ void k_proj_div_xfft(const RunDesc* runs, const int4* items, int nite
 }
 
 // One x-wavenumber m per item: the y-transform of every layer, one tridiagonal solve per y-wavenumber n along the
-// vertical in FP64 (Thomas, factorised on the host in FP64: the k = 0 uniform mode pinned at the ground, the null
-// modes zero), the inverse y-transform. FACE: rows -rho h lambda + vertical faces (src/core/advection.ts:222-241);
-// PRES: the density-weighted consistent Laplacian (src/core/pressure.ts:104-140).
+// vertical in FP64, the inverse y-transform. The solve is Thomas' algorithm with the LU factors made on the host in
+// FP64 (the k = 0 uniform mode pinned at the ground, the null modes zero): per level the forward sweep
+// d_k = A_k r_k - B_k d_(k-1) and the back substitution x_k = d_k - C_k x_(k+1), for the real and the imaginary
+// part of each y-wavenumber n (they share the coefficients). FACE: rows -rho h lambda + vertical faces
+// (src/core/advection.ts:222-241); PRES: the density-weighted consistent Laplacian (src/core/pressure.ts:104-140).
+// The inverse transform is the forward one of the conjugate, conjugated: the back substitution stores conj(x).
 constexpr int MAXNZ = 128;
-// `group`: layers per y-transform pass (all of them when the scratch fits in shared memory).
-__global__ void k_proj_modes(const RunDesc* runs, const int4* items, int nitems, int mode, int group) {
+// Transform of `rows` rows at S (stride n) with a scratch of `cap` rows; the result ends in S.
+__device__ void fft_rows_grouped(float2* S, float2* T, int n, int rows, int cap, const FftPlan& P) {
+  for (int k0 = 0; k0 < rows; k0 += cap) {
+    const int g = min(cap, rows - k0);
+    float2* r = fft_rows_any(S + k0 * n, T, n, g, P);
+    if (r != S + k0 * n) {
+      for (int e = threadIdx.x; e < g * n; e += blockDim.x) S[k0 * n + e] = r[e];
+      __syncthreads();
+    }
+  }
+}
+
+// `group`: layers the scratch holds (all of them: the transforms ping-pong between the two buffers; fewer, for tall
+// or wide grids: the layers go through the scratch in groups).
+__global__ void k_proj_modes(const RunDesc* __restrict__ runs, const int4* items, int nitems, int mode, int group) {
   extern __shared__ float2 smc[];
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
     if (R.cnt[C_FAILED]) continue;
     const int m = items[it].y, ny = R.ny, nz = R.nz, nzc = mode == PROJ_FACE ? nz : nz - 1;
+    const bool whole = group >= nzc;
     float2* S = smc;                   // [nzc][ny]
     float2* T = smc + nzc * ny;        // [group][ny] scratch
     float2* g = R.spec + (size_t)m * nzc * ny;
     for (int e = threadIdx.x; e < nzc * ny; e += blockDim.x) S[e] = g[e];
     __syncthreads();
     FftPlan P{ny, R.fy_nf, R.fy_rad, R.twy};
-    for (int k0 = 0; k0 < nzc; k0 += group) fft_rows(S + k0 * ny, T, ny, min(group, nzc - k0), P);
-    // One real recurrence per (n, component): the real and imaginary parts share the coefficients.
-    const double2* tri = (mode == PROJ_FACE ? R.tri_face : R.tri_pres) + (size_t)m * nzc * ny;
-    const double* lv64 = R.lv64;
-    float* Sf = reinterpret_cast<float*>(S);
-    for (int u = threadIdx.x; u < 2 * ny; u += blockDim.x) {
-      const int n = u >> 1, c = u & 1;
-      double d[MAXNZ];
-      double a = 0, b = 0;
-      if (mode == PROJ_PRES) { double2 ab = R.ab[m * ny + n]; a = ab.x; b = ab.y; }
-      double prev = 0;
+    float2* F = S;
+    if (whole) F = fft_rows_any(S, T, ny, nzc, P);
+    else fft_rows_grouped(S, T, ny, nzc, group, P);
+    float2* Fo = F == S ? T : S;       // the other buffer (whole slab case)
+    const double2* AB = (mode == PROJ_FACE ? R.tri_face : R.tri_pres) + (size_t)m * nzc * ny;
+    const double* Cc = reinterpret_cast<const double*>((mode == PROJ_FACE ? R.tri_face : R.tri_pres) + (size_t)R.nm * nzc * ny) + (size_t)m * nzc * ny;
+    // one thread per y-wavenumber n carries the real and the imaginary recurrence (shared coefficients, two
+    // independent FP64 chains); values enter and leave FP64 through the integer-pipe conversions
+    for (int n = threadIdx.x; n < ny; n += blockDim.x) {
+      double dr[MAXNZ], di[MAXNZ];
+      double pr = 0, pi = 0;
+#pragma unroll 4
       for (int k = 0; k < nzc; k++) {
-        const double ip = tri[(size_t)k * ny + n].x;                  // 1 / pivot
-        double r = Sf[2 * (k * ny + n) + c], lo;
-        if (mode == PROJ_FACE) { r *= lv64[D_FHZ * nz + k]; lo = lv64[D_FLO * nz + k]; }
-        else lo = a * lv64[D_PL1 * nz + k] + b * lv64[D_PL2 * nz + k];
-        prev = (r - lo * prev) * ip;
-        d[k] = prev;
+        const double2 ab = AB[(size_t)k * ny + n];
+        const float2 v = F[k * ny + n];
+        pr = fma(-ab.y, pr, ab.x * widen(v.x));
+        pi = fma(-ab.y, pi, ab.x * widen(v.y));
+        dr[k] = pr; di[k] = pi;
       }
-      double x = 0;
-      for (int k = nzc - 1; k >= 0; k--) {
-        x = k < nzc - 1 ? d[k] - tri[(size_t)k * ny + n].y * x : d[k];
-        Sf[2 * (k * ny + n) + c] = (float)x;
+      double xr = dr[nzc - 1], xi = di[nzc - 1];
+      F[(nzc - 1) * ny + n] = make_float2(narrow(xr), -narrow(xi));
+#pragma unroll 4
+      for (int k = nzc - 2; k >= 0; k--) {
+        const double c = Cc[(size_t)k * ny + n];
+        xr = fma(-c, xr, dr[k]);
+        xi = fma(-c, xi, di[k]);
+        F[k * ny + n] = make_float2(narrow(xr), -narrow(xi));
       }
     }
     __syncthreads();
-    for (int k0 = 0; k0 < nzc; k0 += group) ifft_rows(S + k0 * ny, T, ny, min(group, nzc - k0), P);
-    for (int e = threadIdx.x; e < nzc * ny; e += blockDim.x) g[e] = S[e];
+    const float2* G = F;
+    if (whole) G = fft_rows_any(F, Fo, ny, nzc, P);
+    else fft_rows_grouped(S, T, ny, nzc, group, P);
+    for (int e = threadIdx.x; e < nzc * ny; e += blockDim.x) { const float2 z = G[e]; g[e] = make_float2(z.x, -z.y); }
     __syncthreads();
   }
 }
 
 // Inverse x-transform of one layer's rows (Hermitian rows rebuilt from the half spectrum, two real rows per complex
-// transform, src/core/spectral.ts:281-290), normalised by nx*ny, into phi (FACE) or the pressure (PRES).
-__global__ void k_proj_xifft(const RunDesc* runs, const int4* items, int nitems, int mode, int yc) {
+// transform, src/core/spectral.ts:281-290; the inverse as the conjugate of the forward transform of the conjugate),
+// normalised by nx*ny, into phi (FACE) or the pressure (PRES).
+__global__ void k_proj_xifft(const RunDesc* __restrict__ runs, const int4* items, int nitems, int mode, int yc) {
   extern __shared__ float2 smc[];
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
@@ -321,28 +366,32 @@ __global__ void k_proj_xifft(const RunDesc* runs, const int4* items, int nitems,
     float2* H = smc;                    // [rows][nm] half spectra
     float2* Z = smc + yc * nm;          // [pairs][nx]
     float2* T = Z + pairs * nx;
+    const float inv_rows = 1.f / (float)rows, inv_nx = 1.f / (float)nx;
+#pragma unroll 4
     for (int e = threadIdx.x; e < nm * rows; e += blockDim.x) {
-      int m = e / rows, r = e - m * rows;
+      const int m = row_of(e, inv_rows), r = e - m * rows;
       H[r * nm + m] = R.spec[((size_t)m * nzc + k) * ny + y0 + r];
     }
     __syncthreads();
     for (int e = threadIdx.x; e < pairs * nx; e += blockDim.x) {
-      int pr = e / nx, m = e - pr * nx, c = m <= mh ? m : nx - m;
-      float sg = m <= mh ? 1.f : -1.f; bool real = c == 0 || 2 * c == nx, pair = 2 * pr + 1 < rows;
-      float2 A = H[(2 * pr) * nm + c];
-      float ar = A.x, ai = real ? 0.f : sg * A.y, br = 0.f, bi = 0.f;
-      if (pair) { float2 B = H[(2 * pr + 1) * nm + c]; br = B.x; bi = real ? 0.f : sg * B.y; }
-      Z[pr * nx + m] = make_float2(ar - bi, ai + br);
+      const int pr = row_of(e, inv_nx), m = e - pr * nx, c = m <= mh ? m : nx - m;
+      const float sg = m <= mh ? 1.f : -1.f;
+      const bool real = c == 0 || 2 * c == nx, pair = 2 * pr + 1 < rows;
+      const float2 A = H[(2 * pr) * nm + c];
+      const float ar = A.x, ai = real ? 0.f : sg * A.y;
+      float br = 0.f, bi = 0.f;
+      if (pair) { const float2 B = H[(2 * pr + 1) * nm + c]; br = B.x; bi = real ? 0.f : sg * B.y; }
+      Z[pr * nx + m] = make_float2(ar - bi, -(ai + br));  // conj(A + iB)
     }
     __syncthreads();
     FftPlan P{nx, R.fx_nf, R.fx_rad, R.twx};
-    ifft_rows(Z, T, nx, pairs, P);
+    const float2* Zf = fft_rows_any(Z, T, nx, pairs, P);
     const float norm = 1.f / (float)(nx * ny);
     float* out = (mode == PROJ_FACE ? R.phi : R.pres) + (size_t)k * nx * ny;
     for (int e = threadIdx.x; e < rows * nx; e += blockDim.x) {
-      int r = e / nx, x = e - r * nx;
-      float2 z = Z[(r >> 1) * nx + x];
-      out[(y0 + r) * nx + x] = ((r & 1) ? z.y : z.x) * norm;
+      const int r = row_of(e, inv_nx), x = e - r * nx;
+      const float2 z = Zf[(r >> 1) * nx + x];
+      out[(y0 + r) * nx + x] = ((r & 1) ? -z.y : z.x) * norm;
     }
     __syncthreads();
   }
@@ -350,7 +399,7 @@ __global__ void k_proj_xifft(const RunDesc* runs, const int4* items, int nitems,
 
 // Projected face mass fluxes and their divergence (FluxTransport.correctFaces + divergence, advection.ts:203-255):
 // mx = rho (u + u_e)/2 - rho (phi_e - phi)/dx, and so on; div of the corrected faces at the node.
-__global__ void k_face_correct(const RunDesc* runs, const int4* items, int nitems, int set) {
+__global__ void k_face_correct(const RunDesc* __restrict__ runs, const int4* items, int nitems, int set) {
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
     if (R.cnt[C_FAILED]) continue;
@@ -374,7 +423,7 @@ __global__ void k_face_correct(const RunDesc* runs, const int4* items, int nitem
 
 // u -= dt G p at the nodes of one set (PressureSolver.correct, src/core/pressure.ts:69-92); with `final` the wind
 // limits act and count (clipWind, src/core/model.ts:1586-1595).
-__global__ void k_pres_correct(const RunDesc* runs, const int4* items, int nitems, int set, int final_) {
+__global__ void k_pres_correct(const RunDesc* __restrict__ runs, const int4* items, int nitems, int set, int final_) {
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
     if (R.cnt[C_FAILED]) continue;
@@ -676,7 +725,7 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
 }
 
 template <int KIND, int G>
-__global__ void __launch_bounds__(320, 2) k_transport(const RunDesc* runs, const int4* items, int nitems, int in_set, int out_set,
+__global__ void __launch_bounds__(320, 2) k_transport(const RunDesc* __restrict__ runs, const int4* items, int nitems, int in_set, int out_set,
                                                        float frac, int stage, int TX, int TY) {
   extern __shared__ float sm[];
   FOR_ITEMS {
@@ -689,7 +738,7 @@ __global__ void __launch_bounds__(320, 2) k_transport(const RunDesc* runs, const
 // ==================================================================== endStep
 // Sums of the positivity fix over one chunk of the final RK3 values (fillNegative, src/core/model.ts:606-617):
 // per conserve field, (removed, kept, negative) weighted by the level weight, FP64, in a fixed order.
-__global__ void k_fill_partial(const RunDesc* runs, const int4* items, int nitems, int set) {
+__global__ void k_fill_partial(const RunDesc* __restrict__ runs, const int4* items, int nitems, int set) {
   __shared__ double sh[32 * NCONS * 3];
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
@@ -720,7 +769,7 @@ __global__ void k_fill_partial(const RunDesc* runs, const int4* items, int nitem
 }
 // Per run: the scale of each conserve field, kept as delta = scale - 1 so a * scale rounds once (fma). Thread k sums
 // field k's block partials (FP64, in chunk order).
-__global__ void k_fill_final(const RunDesc* runs, const int4* items, int nitems) {
+__global__ void k_fill_final(const RunDesc* __restrict__ runs, const int4* items, int nitems) {
   __shared__ double negs[NCONS];
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
@@ -750,7 +799,7 @@ __global__ void k_fill_final(const RunDesc* runs, const int4* items, int nitems)
 // Per node: the positivity fix and the cold decay ('finish', :1253-1258), then physics(z) (:1347-1531): microphysics,
 // Coriolis and wind relaxation, surface fluxes (none in the single-storm mode), cold clamp, Rayleigh sponge.
 // In: set `in` (final RK3 values). Out: rain, snow, graupel, hail, cold -> set A; the mixed fields -> set `mid`.
-__global__ void k_physics(const RunDesc* runs, const int4* items, int nitems, int in, int mid) {
+__global__ void k_physics(const RunDesc* __restrict__ runs, const int4* items, int nitems, int in, int mid) {
   __shared__ double sh[32 * 3];
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
@@ -813,7 +862,7 @@ __global__ void k_physics(const RunDesc* runs, const int4* items, int nitems, in
 // Smagorinsky-Lilly eddy viscosities (Turbulence.viscosity, src/core/turbulence.ts:87-137): anisotropic horizontal
 // width, cube-root (or dz) vertical width with the per-level explicit cap, dry N^2 or the saturated one in cloud
 // (theta-e form; Durran-Klemp when switched on).
-__global__ void k_viscosity(const RunDesc* runs, const int4* items, int nitems, int set) {
+__global__ void k_viscosity(const RunDesc* __restrict__ runs, const int4* items, int nitems, int set) {
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
     if (R.cnt[C_FAILED]) continue;
@@ -870,7 +919,7 @@ __global__ void k_viscosity(const RunDesc* runs, const int4* items, int nitems, 
 // Explicit flux-form diffusion of each mixed field's departure (Turbulence.mix, src/core/turbulence.ts:143-185),
 // then the ground drag balanced against the environment's own and rigid w at the ground and top (mixStep, :1179-1194).
 // In: set `in`; out: set A.
-__global__ void k_mix(const RunDesc* runs, const int4* items, int nitems, int in) {
+__global__ void k_mix(const RunDesc* __restrict__ runs, const int4* items, int nitems, int in) {
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
     if (R.cnt[C_FAILED]) continue;
@@ -920,7 +969,7 @@ __global__ void k_mix(const RunDesc* runs, const int4* items, int nitems, int in
 
 // Per run, once a step: the water budget and negative mass of this step added in a fixed order, the step count,
 // the scratch reset for the next step.
-__global__ void k_step_end(const RunDesc* runs, const int4* items, int nitems) {
+__global__ void k_step_end(const RunDesc* __restrict__ runs, const int4* items, int nitems) {
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
     if (threadIdx.x == 0 && !R.cnt[C_FAILED]) {
@@ -937,7 +986,7 @@ __global__ void k_step_end(const RunDesc* runs, const int4* items, int nitems) {
 }
 
 // FP64 max |D R u| over the dual cells of a set (the divergence check).
-__global__ void k_divergence_max(const RunDesc* runs, const int4* items, int nitems, int set, double* out) {
+__global__ void k_divergence_max(const RunDesc* __restrict__ runs, const int4* items, int nitems, int set, double* out) {
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
     const int nx = R.nx, ny = R.ny, layer = R.layer, i0 = items[it].y * CHUNK, i1 = min(R.ncells, i0 + CHUNK);
@@ -972,11 +1021,11 @@ void launch_proj_div_xfft(const Launch& L, int mode, int set, int yc, int maxnx)
   k_proj_div_xfft<<<GRID(L.n, L.cap), 256, smem, L.stream>>>(L.runs, L.items, L.n, mode, set, yc);
 }
 void launch_proj_modes(const Launch& L, int mode, int maxnz, int maxny, int threads, int smem_budget) {
-  // the slab [nz][ny] plus a scratch of `group` layers, all layers at once when they fit
-  size_t slab = (size_t)maxnz * maxny * sizeof(float2);
+  // the column slab [nz][ny] plus a scratch of `group` layers, all of them when they fit
+  const size_t slab = (size_t)maxnz * maxny * sizeof(float2);
   int group = (int)std::min<size_t>(maxnz, (smem_budget - slab) / ((size_t)maxny * sizeof(float2)));
   group = std::max(group, 1);
-  size_t smem = slab + (size_t)group * maxny * sizeof(float2);
+  const size_t smem = slab + (size_t)group * maxny * sizeof(float2);
   k_proj_modes<<<GRID(L.n, L.cap), threads, smem, L.stream>>>(L.runs, L.items, L.n, mode, group);
 }
 void launch_proj_xifft(const Launch& L, int mode, int yc, int maxnx) {

@@ -26,7 +26,6 @@ using namespace sg;
 namespace {
 
 constexpr int MAX_SLOTS = 4096;
-constexpr int YC = 16;            // rows per x-transform work item
 constexpr size_t ALIGN = 256;
 const double RK3[3] = {1.0 / 3, 1.0 / 2, 1.0};
 
@@ -41,7 +40,7 @@ Layout layout(int nx, int ny, int nz) {
   L.fld = take(3 * NF * n * 4); L.faces = take(4 * n * 4); L.kmkh = take(2 * n * 4); L.phi = take(n * 4);
   L.pres = take(layer * (nz - 1) * 4); L.spec = take(nm * nz * ny * 8); L.cols = take(3 * layer * 4);
   L.lv = take((size_t)L_COUNT * nz * 4); L.lv64 = take((size_t)D_COUNT * nz * 8);
-  L.triF = take(nm * nz * ny * 16); L.triP = take(nm * (nz - 1) * ny * 16); L.ab = take(nm * ny * 16);
+  L.triF = take(nm * nz * ny * 24); L.triP = take(nm * (nz - 1) * ny * 24); L.ab = take(nm * ny * 16);
   L.twx = take(nx * 8); L.twy = take(ny * 8); L.scr = take(64 * 4); L.part = take((nch * NCONS * 3 + nch * 4) * 8);
   L.acc = take(A_COUNT * 8); L.cnt = take(C_COUNT * 8);
   L.items = take(nch * 16);  // the run's own per-node work items (field conversions outside a batch plan)
@@ -65,6 +64,7 @@ struct Plan {
   int4* items = nullptr;  // device
   int off[16] = {0}, cnt[16] = {0};
   int maxnx = 0, maxny = 0, maxnz = 0, TX = 40, TY = 8, wenoG = 3;  // transport tile and WENO fields per item
+  int yc = 32;                                                        // layer rows per x-transform item
   bool tuned = false;                                                 // TX, TY, wenoG chosen by timing
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -108,7 +108,8 @@ int cudaFail(sg_context* ctx, cudaError_t e, const char* where) {
 #define CK(call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) return cudaFail(ctx, e_, #call); } while (0)
 
 // ------------------------------------------------------------------ host precomputation
-struct HostTables { std::vector<float> lv; std::vector<double> lv64; std::vector<double2> triF, triP, ab; std::vector<float2> twx, twy; };
+// triF / triP: the Thomas coefficients of every mode, [m][k][n] (A, B) pairs followed by [m][k][n] C values.
+struct HostTables { std::vector<float> lv; std::vector<double> lv64; std::vector<double2> triF, triP, ab; std::vector<double> triFc, triPc; std::vector<float2> twx, twy; };
 
 void twiddles(int n, std::vector<float2>& tw) {
   tw.resize(n);
@@ -184,7 +185,7 @@ void build_tables(const sg_grid* g, const sg_base_state* b, const sg_switches* s
     D(D_THB, z, thb[z]);
   }
   // Face projection factorisation [m][k][n] (src/core/advection.ts:222-241): rows -rho h lambda - lo - up.
-  T.triF.assign((size_t)nm * nz * ny, make_double2(0, 0));
+  T.triF.assign((size_t)nm * nz * ny, make_double2(0, 0)); T.triFc.assign((size_t)nm * nz * ny, 0.0);
   std::vector<double> cp(nz);
   auto faceRho = [&](int k) { return k < 0 || k >= nz - 1 ? 0.0 : (rho[k] + rho[k + 1]) / 2; };
   for (int m = 0; m < nm; m++) for (int n = 0; n < ny; n++) {
@@ -196,12 +197,16 @@ void build_tables(const sg_grid* g, const sg_base_state* b, const sg_switches* s
       if (pinned && k == 1) lo = 0;
       double piv = k == 0 ? di : di - lo * cp[k - 1];
       cp[k] = up / piv;
-      T.triF[((size_t)m * nz + k) * ny + n] = make_double2(pinned && k == 0 ? 0.0 : 1 / piv, cp[k]);
+      // forward sweep d_k = A r_k - B d_(k-1) with A = h_k / pivot (the rows are scaled by h), B = lower / pivot
+      const double ip = pinned && k == 0 ? 0.0 : 1 / piv, lower = k > 0 ? faceRho(k - 1) / dzs[k - 1] : 0;
+      T.triF[((size_t)m * nz + k) * ny + n] = make_double2(ip * hz[k], ip * lower);
+      T.triFc[((size_t)m * nz + k) * ny + n] = cp[k];
     }
   }
   // Pressure factorisation [m][k][n] (src/core/pressure.ts:37-44, :104-140), the symbols snapped as there.
   const int nc = nz - 1;
-  T.triP.assign((size_t)nm * nc * ny, make_double2(0, 0)); T.ab.assign((size_t)nm * ny, make_double2(0, 0));
+  T.triP.assign((size_t)nm * nc * ny, make_double2(0, 0)); T.triPc.assign((size_t)nm * nc * ny, 0.0);
+  T.ab.assign((size_t)nm * ny, make_double2(0, 0));
   auto exact = [](double x) { return x < 1e-12 ? 0 : x > 1 - 1e-12 ? 1 : x; };
   for (int m = 0; m < nm; m++) for (int n = 0; n < ny; n++) {
     double sx = exact(std::pow(std::sin(M_PI * m / nx), 2)), cx = exact(std::pow(std::cos(M_PI * m / nx), 2));
@@ -218,7 +223,9 @@ void build_tables(const sg_grid* g, const sg_base_state* b, const sg_switches* s
       if (pinned && k == 1) lo = 0;
       double piv = k == 0 ? di : di - lo * cp[k - 1];
       cp[k] = up / piv;
-      T.triP[((size_t)m * nc + k) * ny + n] = make_double2(pinned && k == 0 ? 0.0 : 1 / piv, cp[k]);
+      const double ip = pinned && k == 0 ? 0.0 : 1 / piv;
+      T.triP[((size_t)m * nc + k) * ny + n] = make_double2(ip, ip * lo);
+      T.triPc[((size_t)m * nc + k) * ny + n] = cp[k];
     }
   }
   twiddles(nx, T.twx); twiddles(ny, T.twy);
@@ -295,6 +302,8 @@ int build_plan(sg_context* ctx, const std::vector<int>& slots, Plan& P) {
   P.TX = all40 ? 40 : 32;
   P.TY = 8;
   P.wenoG = 3;
+  // x-transform items: a whole layer of the benchmark grids (up to 32 rows), 16 rows for grids wider than 128
+  P.yc = std::min(P.maxnx > 128 ? 16 : 32, (P.maxny + 1) / 2 * 2);
   for (int s : slots) {
     const Run& r = ctx->runs[s];
     int n = r.nx * r.ny * r.nz, nch = (n + CHUNK - 1) / CHUNK, layer = r.nx * r.ny;
@@ -302,8 +311,8 @@ int build_plan(sg_context* ctx, const std::vector<int>& slots, Plan& P) {
     int ncc = (r.nx * r.ny * (r.nz - 1) + CHUNK - 1) / CHUNK;
     for (int c = 0; c < ncc; c++) all[FAM_CELLS].push_back(make_int4(s, c, 0, 0));
     for (int c = 0; c < (layer + 63) / 64; c++) all[FAM_COLS].push_back(make_int4(s, c, 0, 0));
-    for (int k = 0; k < r.nz; k++) for (int y = 0; y < r.ny; y += YC) all[FAM_ROWS_FACE].push_back(make_int4(s, k, y, 0));
-    for (int k = 0; k < r.nz - 1; k++) for (int y = 0; y < r.ny; y += YC) all[FAM_ROWS_PRES].push_back(make_int4(s, k, y, 0));
+    for (int k = 0; k < r.nz; k++) for (int y = 0; y < r.ny; y += P.yc) all[FAM_ROWS_FACE].push_back(make_int4(s, k, y, 0));
+    for (int k = 0; k < r.nz - 1; k++) for (int y = 0; y < r.ny; y += P.yc) all[FAM_ROWS_PRES].push_back(make_int4(s, k, y, 0));
     for (int m = 0; m < r.nx / 2 + 1; m++) all[FAM_MODES].push_back(make_int4(s, m, 0, 0));
     all[FAM_RUNS].push_back(make_int4(s, 0, 0, 0));
   }
@@ -408,22 +417,24 @@ template <class Hook>
 void enqueue_part(sg_context* ctx, const Plan& P, int part, Hook hook) {
   const int A = 0, B = 1, C = 2;
   Launch node = lx(ctx, P, FAM_NODE), cols = lx(ctx, P, FAM_COLS), rf = lx(ctx, P, FAM_ROWS_FACE), rp = lx(ctx, P, FAM_ROWS_PRES);
-  Launch modes = lx(ctx, P, FAM_MODES, 2), runs = lx(ctx, P, FAM_RUNS);
-  const int mthreads = std::min(512, std::max(256, 2 * P.maxny));
+  Launch modes = lx(ctx, P, FAM_MODES), runs = lx(ctx, P, FAM_RUNS);
+  modes.cap = modes.n;  // one block per wavenumber: its column solves are serial in z, so spread them over the SMs
+  rf.cap = rf.n; rp.cap = rp.n;
+  const int mthreads = std::min(256, std::max(64, (P.maxny + 31) / 32 * 32));
   const int mbudget = std::min(ctx->maxSmem, 200 * 1024);
   auto project = [&](int set, int final_) {
-    launch_proj_div_xfft(rp, PROJ_PRES, set, YC, P.maxnx); hook(7);
+    launch_proj_div_xfft(rp, PROJ_PRES, set, P.yc, P.maxnx); hook(7);
     launch_proj_modes(modes, PROJ_PRES, P.maxnz, P.maxny, mthreads, mbudget); hook(8);
-    launch_proj_xifft(rp, PROJ_PRES, YC, P.maxnx); hook(9);
+    launch_proj_xifft(rp, PROJ_PRES, P.yc, P.maxnx); hook(9);
     launch_pres_correct(node, set, final_); hook(final_ ? 16 : 10);
   };
   if (part == 1) {
     launch_fall_courant(node); hook(0);
     launch_sediment(cols, P.maxnz); hook(1);
   } else if (part == 2) {
-    launch_proj_div_xfft(rf, PROJ_FACE, A, YC, P.maxnx); hook(2);
+    launch_proj_div_xfft(rf, PROJ_FACE, A, P.yc, P.maxnx); hook(2);
     launch_proj_modes(modes, PROJ_FACE, P.maxnz, P.maxny, mthreads, mbudget); hook(3);
-    launch_proj_xifft(rf, PROJ_FACE, YC, P.maxnx); hook(4);
+    launch_proj_xifft(rf, PROJ_FACE, P.yc, P.maxnx); hook(4);
     launch_face_correct(node, A); hook(5);
     const int in[3] = {A, B, C}, out[3] = {B, C, B};
     for (int s = 0; s < 3; s++) {
@@ -606,7 +617,8 @@ int sg_run_create(sg_context* ctx, const sg_grid* g, const sg_base_state* b, con
   auto H2D = [&](size_t off, const void* src, size_t bytes) { return cudaMemcpyAsync(mem + off, src, bytes, cudaMemcpyHostToDevice, ctx->stream); };
   CK(cudaMemsetAsync(mem, 0, Lo.total, ctx->stream));
   CK(H2D(Lo.lv, T.lv.data(), T.lv.size() * 4)); CK(H2D(Lo.lv64, T.lv64.data(), T.lv64.size() * 8));
-  CK(H2D(Lo.triF, T.triF.data(), T.triF.size() * 16)); CK(H2D(Lo.triP, T.triP.data(), T.triP.size() * 16));
+  CK(H2D(Lo.triF, T.triF.data(), T.triF.size() * 16)); CK(H2D(Lo.triF + T.triF.size() * 16, T.triFc.data(), T.triFc.size() * 8));
+  CK(H2D(Lo.triP, T.triP.data(), T.triP.size() * 16)); CK(H2D(Lo.triP + T.triP.size() * 16, T.triPc.data(), T.triPc.size() * 8));
   CK(H2D(Lo.ab, T.ab.data(), T.ab.size() * 16)); CK(H2D(Lo.twx, T.twx.data(), T.twx.size() * 8)); CK(H2D(Lo.twy, T.twy.data(), T.twy.size() * 8));
   CK(cudaMemcpyAsync(ctx->d_runs + slot, &d, sizeof(RunDesc), cudaMemcpyHostToDevice, ctx->stream));
   {
@@ -661,6 +673,35 @@ int sg_run_read_fields(sg_context* ctx, sg_run run, uint32_t mask, float* const*
   return SG_OK;
 }
 
+// Fields of many runs in one call: all copies on the library's stream, one theta conversion launch for the batch,
+// one synchronisation at the end. host[k * 13 + f] is run k's field f (by the mask).
+int batch_fields(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, float* const* host, bool write) {
+  if (!ctx || !host) return SG_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  std::vector<int> slots;
+  int st = slots_of(ctx, runs, n, slots);
+  if (st != SG_OK) return st;
+  Plan* P = nullptr;
+  if (mask & (1u << THETA)) { P = get_plan(ctx, slots, &st); if (!P) return st; }
+  if (!write && P) launch_theta_out(lx(ctx, *P, FAM_NODE), nullptr);
+  for (int k = 0; k < n; k++) {
+    Run* r = find(ctx, runs[k]);
+    const size_t nn = (size_t)r->nx * r->ny * r->nz;
+    for (int f = 0; f < NF; f++) {
+      if (!(mask & (1u << f))) continue;
+      float* h = host[(size_t)k * NF + f];
+      if (!h) return fail(ctx, SG_ERR_INVALID, "null field pointer");
+      float* dev = r->desc.fld + (size_t)(f == THETA ? NF + THETA : f) * nn;  // theta staged in set B
+      if (write) CK(cudaMemcpyAsync(dev, h, nn * 4, cudaMemcpyHostToDevice, ctx->stream));
+      else CK(cudaMemcpyAsync(h, dev, nn * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+  }
+  if (write && P) launch_theta_in(lx(ctx, *P, FAM_NODE), nullptr);
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaGetLastError());
+  return SG_OK;
+}
+
 int sg_run_read_columns(sg_context* ctx, sg_run run, float* precipitation, float* hail_ground, float* hail_size) {
   if (!ctx) return SG_ERR_INVALID;
   Run* r = find(ctx, run);
@@ -696,6 +737,13 @@ int sg_run_status(sg_context* ctx, sg_run run, sg_run_counters* out) {
   out->negative_filled = acc[A_NEG]; out->water_condensed = acc[A_WATER]; out->water_evaporated = acc[A_WATER + 1];
   out->water_rain_evaporated = acc[A_WATER + 2]; out->water_surface = 0;
   return out->failed ? SG_ERR_NONFINITE : SG_OK;
+}
+
+int sg_batch_write_fields(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, const float* const* host) {
+  return batch_fields(ctx, runs, n, mask, const_cast<float* const*>(host), true);
+}
+int sg_batch_read_fields(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, float* const* host) {
+  return batch_fields(ctx, runs, n, mask, host, false);
 }
 
 int sg_run_retire(sg_context* ctx, sg_run run) {
@@ -866,6 +914,8 @@ struct Active { sg_run run; int64_t left, tag; };
 struct sg_server {
   sg_context* ctx;
   int maxActive;
+  int quantum = 1;      // steps per iteration at most (an iteration stops where the first active run finishes)
+  int lastSteps = 0;
   std::deque<Request> queue;
   std::vector<Active> active;
   std::map<int64_t, sg_run> finished;  // done, resident until collected
@@ -875,7 +925,7 @@ extern "C" {
 
 int sg_server_create(sg_context* ctx, int max_active, sg_server** out) {
   if (!ctx || !out || max_active < 1) return SG_ERR_INVALID;
-  *out = new sg_server{ctx, max_active, {}, {}};
+  *out = new sg_server{ctx, max_active};
   return SG_OK;
 }
 
@@ -922,14 +972,17 @@ int sg_server_iterate(sg_server* srv, int64_t* done_tags, int* done_count, int c
     srv->queue.pop_front();
   }
   int done = 0;
+  srv->lastSteps = 0;
   if (!srv->active.empty()) {
     std::vector<sg_run> ids;
-    for (auto& a : srv->active) ids.push_back(a.run);
-    int st = sg_batch_step(ctx, ids.data(), (int)ids.size(), 1);
+    int64_t q = srv->quantum;
+    for (auto& a : srv->active) { ids.push_back(a.run); q = std::min(q, a.left); }
+    int st = sg_batch_step(ctx, ids.data(), (int)ids.size(), (int)q);
     if (st) return st;
+    srv->lastSteps = (int)q;
     std::vector<Active> keep;
     for (auto& a : srv->active) {
-      if (--a.left > 0) { keep.push_back(a); continue; }
+      if ((a.left -= q) > 0) { keep.push_back(a); continue; }
       if (done < cap && done_tags) done_tags[done] = a.tag;
       done++;
       srv->finished[a.tag] = a.run;
@@ -942,6 +995,13 @@ int sg_server_iterate(sg_server* srv, int64_t* done_tags, int* done_count, int c
   return SG_OK;
 }
 
+
+int sg_server_set_quantum(sg_server* srv, int steps) {
+  if (!srv || steps < 1) return SG_ERR_INVALID;
+  srv->quantum = steps;
+  return SG_OK;
+}
+int sg_server_last_steps(sg_server* srv) { return srv ? srv->lastSteps : 0; }
 
 int sg_server_collect(sg_server* srv, int64_t tag, uint32_t mask, float* const* host, float* precipitation) {
   if (!srv) return SG_ERR_INVALID;

@@ -89,6 +89,8 @@ def load():
             L.sg_debug_step_part.argtypes = [vp, C.c_int32, i32]
             L.sg_debug_read_set.argtypes = [vp, C.c_int32, i32, i32, _FP]
             L.sg_debug_read_faces.argtypes = [vp, C.c_int32, _FP]
+            L.sg_batch_write_fields.argtypes = [vp, C.POINTER(C.c_int32), i32, C.c_uint32, C.POINTER(_FP)]
+            L.sg_batch_read_fields.argtypes = [vp, C.POINTER(C.c_int32), i32, C.c_uint32, C.POINTER(_FP)]
             L.sg_set_transport_shape.argtypes = [vp, i32, i32, i32]
             L.sg_batch_transport_shape.argtypes = [vp, C.POINTER(C.c_int32), i32, C.POINTER(C.c_int)]
             L.sg_server_create.argtypes = [vp, i32, C.POINTER(vp)]
@@ -96,6 +98,8 @@ def load():
             L.sg_server_submit.argtypes = [vp, C.POINTER(SgGrid), C.POINTER(SgBase), C.POINTER(SgSwitches), C.POINTER(_FP), i64, i64]
             L.sg_server_iterate.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int), i32, C.POINTER(C.c_int), C.POINTER(C.c_int)]
             L.sg_server_collect.argtypes = [vp, i64, C.c_uint32, C.POINTER(_FP), _FP]
+            L.sg_server_set_quantum.argtypes = [vp, i32]
+            L.sg_server_last_steps.argtypes = [vp]
             _lib = L
     return _lib
 
@@ -164,6 +168,34 @@ class Context:
         for r in runs:
             r.time += steps * r.spec.switches.dt
         return ms.value
+
+    def _batch_io(self, runs, bufs, names, write: bool):
+        names = list(names)
+        mask = 0
+        for k in names:
+            mask |= 1 << CARRIED.index(k)
+        ptrs = (_FP * (len(runs) * len(CARRIED)))()
+        keep = []
+        for j, (r, b) in enumerate(zip(runs, bufs)):
+            for k in names:
+                a = b[k]
+                if write:
+                    a = np.ascontiguousarray(a, dtype=np.float32).ravel()
+                    keep.append(a)
+                elif a.dtype != np.float32 or not a.flags.c_contiguous or a.size != r.grid.n:
+                    raise ValueError(f"output buffer for {k} must be a contiguous float32 array of {r.grid.n}")
+                ptrs[j * len(CARRIED) + CARRIED.index(k)] = a.ctypes.data_as(_FP)
+        ids = (C.c_int32 * len(runs))(*[r.id for r in runs])
+        fn = load().sg_batch_write_fields if write else load().sg_batch_read_fields
+        self.check(fn(self.h, ids, len(runs), mask, ptrs), "batch fields")
+
+    def write_fields(self, runs: Sequence["Run"], fields: Sequence[Dict[str, np.ndarray]], names: Iterable[str] = CARRIED):
+        """Write the fields of many runs in one call (one synchronisation)."""
+        self._batch_io(runs, fields, names, True)
+
+    def read_fields(self, runs: Sequence["Run"], out: Sequence[Dict[str, np.ndarray]], names: Iterable[str] = CARRIED):
+        """Read the fields of many runs into the caller's float32 arrays in one call."""
+        self._batch_io(runs, out, names, False)
 
     def set_transport_shape(self, tile_x: int = 0, tile_y: int = 0, weno_group: int = 3):
         """Pin the transport tile (tile_x x tile_y columns, 1 or 3 WENO fields per item); tile_x = 0 returns to tuning."""
@@ -321,6 +353,14 @@ class Server:
         h = C.c_void_p()
         ctx.check(load().sg_server_create(ctx.h, max_active, C.byref(h)), "server create")
         self.ctx, self.h = ctx, h
+
+    def set_quantum(self, steps: int):
+        """Advance up to `steps` steps per iteration (stopping where the first active run finishes)."""
+        self.ctx.check(load().sg_server_set_quantum(self.h, steps), "quantum")
+
+    @property
+    def last_steps(self) -> int:
+        return load().sg_server_last_steps(self.h)
 
     def submit(self, spec: RunSpec, steps: int, tag: int):
         p = _Packed(spec)

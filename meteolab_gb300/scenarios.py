@@ -161,3 +161,36 @@ def ensemble_members(grid: Grid, count: int, seed: int = 2026) -> List[RunSpec]:
         runs.append(baseline_run(grid, seed=seed * 1000 + k, bubble=bubble, qv_max=qv,
                                  shear=shear6 / math.tanh(2.0), veer=veer, label=f"member{k}"))
     return runs
+
+
+def regime_runs(small: Grid, large: Grid, n_small: int = 48, n_large: int = 16, seed: int = 88) -> List[RunSpec]:
+    """An 8 x 8 CAPE x shear regime grid (src/regime/grid.ts) split over two domain sizes: CAPE levels from the
+    surface moisture (qv cap 10.5-17 g/kg spans roughly 500-4000 J/kg on this sounding), 0-6 km shear 0-40 m/s, a
+    seeded veering and bubble per point; a seeded shuffle puts n_small points on the small grid and n_large on the
+    large one."""
+    rng = np.random.default_rng(seed)
+    points = [(i, j) for i in range(8) for j in range(8)]
+    order = rng.permutation(len(points))
+    runs = []
+    for slot, p in enumerate(order[:n_small + n_large]):
+        i, j = points[p]
+        qv = 0.0105 + (0.017 - 0.0105) * i / 7
+        shear6 = 40.0 * j / 7
+        grid = small if slot < n_small else large
+        runs.append(baseline_run(grid, seed=seed * 1000 + slot, bubble=float(rng.uniform(1.0, 3.0)), qv_max=qv,
+                                 shear=shear6 / math.tanh(2.0), veer=float(rng.uniform(0.0, 90.0)),
+                                 label=f"cape{i}-shear{j}"))
+    return runs
+
+
+def serving_requests(small: Grid, large: Grid, count: int, rate: float, seed: int = 5):
+    """An open Poisson request stream: arrival times (s) at `rate` runs/s, each request a seeded sounding as the
+    ensemble's on the small or the large grid with 3:1 odds, for 20-60 simulated minutes (400-1200 steps of 3 s)."""
+    rng = np.random.default_rng(seed)
+    t, out = 0.0, []
+    for k in range(count):
+        t += float(rng.exponential(1.0 / rate))
+        grid = small if rng.random() < 0.75 else large
+        spec = ensemble_members(grid, 1, seed=seed * 100 + k)[0]
+        out.append((t, spec, int(rng.integers(400, 1201))))
+    return out

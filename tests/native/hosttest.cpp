@@ -48,4 +48,10 @@ int ht_fft(int n, float* x) {
   return nf;
 }
 
+double ht_widen(float f) { return widen(f); }
+float ht_narrow(double d) { return narrow(d); }
+int ht_fft_factors(int n, int* rad) { return fft_plan_factors(n, rad); }
+int ht_fft_count(int n) { return fft_count(n); }
+int ht_fft_radix(int n, int s) { return fft_radix_at(n, s); }
+
 }  // extern "C"

@@ -38,6 +38,10 @@ def ht():
     L.ht_upwind.argtypes = [C.c_float] * 5
     L.ht_microphysics.restype = C.c_float
     L.ht_microphysics.argtypes = [C.POINTER(C.c_float), C.c_double, C.c_double, C.c_double, C.c_double, C.c_float, C.c_int]
+    L.ht_widen.restype = C.c_double
+    L.ht_widen.argtypes = [C.c_float]
+    L.ht_narrow.restype = C.c_float
+    L.ht_narrow.argtypes = [C.c_double]
     L.ht_fft.restype = C.c_int
     L.ht_fft.argtypes = [C.c_int, C.POINTER(C.c_float)]
     L.ht_fall.argtypes = [C.c_float] * 6 + [C.POINTER(C.c_float)]
@@ -126,3 +130,34 @@ def test_microphysics_matches_oracle(ht, k, ice):
         tol = {"iceNumber": 1e-3 * max(1.0, abs(ref[n])), "cold": 2e-4}.get(n, 1e-4 * abs(ref[n]) + 2e-9)
         assert abs(float(got[n]) - ref[n]) <= tol, (n, float(got[n]), ref[n])
     assert abs(evd - evo) <= 1e-4 * abs(evo) + 1e-10
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 8, 12, 16, 20, 24, 30, 32, 40, 48, 60, 64, 80, 96, 100, 128, 160, 256, 320, 7, 14, 49])
+def test_compile_time_radices_match_the_runtime_plan(ht, n):
+    """The kernels' compile-time FFT stages (fft_count / fft_radix_at) are the runtime plan's (fft_plan_factors)."""
+    rad = (C.c_int * 8)()
+    nf = ht.ht_fft_factors(n, rad)
+    if nf < 0 or any(rad[s] not in (2, 3, 4, 5) for s in range(nf)):
+        assert ht.ht_fft_count(n) == -1 or n % 7 != 0
+        return
+    assert ht.ht_fft_count(n) == nf
+    assert [ht.ht_fft_radix(n, s) for s in range(nf)] == [rad[s] for s in range(nf)]
+
+
+def test_integer_conversions(ht):
+    """widen / narrow (FP32 <-> FP64 on the integer pipes) against the IEEE conversions, halfway cases included."""
+    rng = np.random.default_rng(9)
+    f = np.concatenate([(rng.standard_normal(20000) * 10.0 ** rng.integers(-40, 39, 20000)).astype(np.float32),
+                        np.array([0.0, -0.0, 1.0, -1.0, 1e-45, -1e-40, 1.17549435e-38, 3.4028235e38, np.inf, -np.inf], np.float32)])
+    for x in f:
+        got = ht.ht_widen(float(x))
+        assert got == float(x) and math.copysign(1, got) == math.copysign(1, float(x))
+    d = np.concatenate([rng.standard_normal(20000) * 10.0 ** rng.integers(-45, 40, 20000),
+                        np.array([0.0, -0.0, 1.0 + 2.0 ** -24, 1.0 + 3 * 2.0 ** -24, 1.0 + 2.0 ** -24 + 2.0 ** -50,
+                                  -(1.0 + 2.0 ** -24), 3.4028235e38 * (1 + 2.0 ** -25), 1.1754942e-38, 1e-39, 1e300, np.inf])])
+    for x in d:
+        got = np.float32(ht.ht_narrow(float(x)))
+        want = np.float32(x)
+        assert got == want or (np.isnan(got) and np.isnan(want)), (x, got, want)
+        assert math.copysign(1, got) == math.copysign(1, want)
+    assert np.isnan(ht.ht_narrow(float("nan")))

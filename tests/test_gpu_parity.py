@@ -159,6 +159,28 @@ def test_transport_tiles_give_the_same_bits(ctx, storm, shape):
     ref.retire(); r.retire()
 
 
+def test_batch_field_io_matches_per_run_calls(ctx, storm):
+    runs = [ctx.create(storm), ctx.create(baseline_run(create_grid(LARGE_GRID), seed=8))]
+    ctx.batch_step(runs, 2)
+    new = []
+    for r in runs:
+        f = r.read()
+        f["u"] = f["u"] + np.float32(1.5)
+        f["theta"] = f["theta"] + np.float32(0.25)
+        new.append(f)
+    ctx.write_fields(runs, new)
+    out = [{k: np.empty(r.grid.n, np.float32) for k in CARRIED} for r in runs]
+    ctx.read_fields(runs, out)
+    for r, f, o in zip(runs, new, out):
+        single = r.read()
+        for k in CARRIED:
+            assert np.array_equal(o[k], single[k]), k
+        assert np.array_equal(o["u"], f["u"])
+        assert np.max(np.abs(o["theta"] - f["theta"])) < 1e-4  # theta goes through its departure from the base profile
+    for r in runs:
+        r.retire()
+
+
 def test_autotuner_picks_a_valid_shape(ctx, storm):
     runs = [ctx.create(storm) for _ in range(4)]
     tx, ty, g = ctx.transport_shape(runs)
@@ -167,8 +189,10 @@ def test_autotuner_picks_a_valid_shape(ctx, storm):
         r.retire()
 
 
-def test_serving_gives_the_same_result_alone_and_in_the_mix(ctx, storm):
-    """Requests admitted while others are on the device finish with the fields they get when stepped alone."""
+@pytest.mark.parametrize("quantum", [1, 3])
+def test_serving_gives_the_same_result_alone_and_in_the_mix(ctx, storm, quantum):
+    """Requests admitted while others are on the device finish with the fields they get when stepped alone, whether
+    an iteration advances one step or several."""
     from meteolab_gb300.runtime import Server
     specs = [storm, baseline_run(create_grid(LARGE_GRID), seed=11), baseline_run(create_grid(DEFAULT_GRID), seed=12)]
     steps = [6, 4, 5]
@@ -179,11 +203,13 @@ def test_serving_gives_the_same_result_alone_and_in_the_mix(ctx, storm):
         ref.append(r.read())
         r.retire()
     srv = Server(ctx, max_active=2)
+    srv.set_quantum(quantum)
     srv.submit(specs[0], steps[0], 0)
     srv.submit(specs[1], steps[1], 1)
     got, it = {}, 0
     while len(got) < 3 and it < 50:
         done, active, queued = srv.iterate()
+        assert 1 <= srv.last_steps <= quantum or not (active or done)
         for tag in done:
             got[tag] = srv.collect(tag, specs[tag].grid.n)
         if it == 1:
