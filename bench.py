@@ -361,7 +361,7 @@ def main():
         "data": "synthetic: seeded Weisman-Klemp-type soundings (surface qv 11-16 g/kg, 0-6 km shear 0-30 m/s, veering 0-90 deg), "
                 "1-3 K ellipsoid bubble, +-0.1 K noise below 1 km",
         "config": {"workload": f"ensemble {args.members} x 40x32x50 per GPU, one CUDA graph per step", "cells_per_gpu": cells,
-                   "spinup_steps": args.spinup, "transport_tile": {"x": tile[0], "y": tile[1], "weno_fields_per_item": tile[2]},
+                   "spinup_steps": args.spinup, "transport_tile": {"x": tile[0], "y": tile[1], "weno_fields_per_item": tile[2], "weno_blocks_per_sm": tile[3]},
                    "l2": "inputs larger than L2 (213 MB per field set)", "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": "cell-steps/s", "h2d_bytes_per_step": bytes_io, "d2h_bytes_per_step": bytes_io},
         "gpu_launches": launches_per_step * args.steps,

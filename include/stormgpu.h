@@ -131,11 +131,13 @@ int sg_run_divergence(sg_context* ctx, sg_run run, double* max_abs_div);
 /* ---- transport tile: the RK3 transport works on tiles of tile_x x tile_y columns, each work item carrying 1 or 3 of
  * the nine WENO fields (weno_group). By default a batch's shape is picked by timing the candidates on the batch itself
  * when its plan is first built (the autotuner; SG_AUTOTUNE=0 in the environment keeps the default 40x8 or 32x8, 3).
- * sg_set_transport_shape pins one shape for every later plan (tile_x = 0 returns to tuning); results are the same bits
+ * The tuner also picks the WENO kernel's register budget. sg_set_transport_shape pins one shape for every later plan
+ * (tile_x = 0 returns to tuning; register budget for 2 blocks per SM); results are the same bits
  * for every shape. sg_batch_transport_shape reports the shape a batch runs with. No counterpart in the reference (its
  * CPU transport has no tiles). */
 int sg_set_transport_shape(sg_context* ctx, int tile_x, int tile_y, int weno_group);
-int sg_batch_transport_shape(sg_context* ctx, const sg_run* runs, int n, int* shape3);
+/* shape4 = (tile_x, tile_y, weno_group, blocks per SM the WENO kernel's register budget is cut for: 2 or 3). */
+int sg_batch_transport_shape(sg_context* ctx, const sg_run* runs, int n, int* shape4);
 
 /* ---- diagnostics: one part of the step (1 beginStep, 2 dynamics, 3 physicsStep, 4 mixStep, 5 final projection),
  * and the raw device buffers (set 0 = state, 1 and 2 = stage scratch; theta of a set is its departure from the base

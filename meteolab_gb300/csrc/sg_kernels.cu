@@ -283,8 +283,8 @@ __global__ void k_proj_div_xfft(const RunDesc* __restrict__ runs, const int4* it
 // One x-wavenumber m per item: the y-transform of every layer, one tridiagonal solve per y-wavenumber n along the
 // vertical in FP64, the inverse y-transform. The solve is Thomas' algorithm with the LU factors made on the host in
 // FP64 (the k = 0 uniform mode pinned at the ground, the null modes zero): per level the forward sweep
-// d_k = A_k r_k - B_k d_(k-1) and the back substitution x_k = d_k - C_k x_(k+1), for the real and the imaginary
-// part of each y-wavenumber n (they share the coefficients). FACE: rows -rho h lambda + vertical faces
+// d_k = A_k r_k - B_k d_(k-1) and the back substitution x_k = d_k - C_k x_(k+1), one real recurrence per
+// (n, real/imaginary part), the two parts sharing the coefficients. FACE: rows -rho h lambda + vertical faces
 // (src/core/advection.ts:222-241); PRES: the density-weighted consistent Laplacian (src/core/pressure.ts:104-140).
 // The inverse transform is the forward one of the conjugate, conjugated: the back substitution stores conj(x).
 constexpr int MAXNZ = 128;
@@ -321,27 +321,25 @@ __global__ void k_proj_modes(const RunDesc* __restrict__ runs, const int4* items
     float2* Fo = F == S ? T : S;       // the other buffer (whole slab case)
     const double2* AB = (mode == PROJ_FACE ? R.tri_face : R.tri_pres) + (size_t)m * nzc * ny;
     const double* Cc = reinterpret_cast<const double*>((mode == PROJ_FACE ? R.tri_face : R.tri_pres) + (size_t)R.nm * nzc * ny) + (size_t)m * nzc * ny;
-    // one thread per y-wavenumber n carries the real and the imaginary recurrence (shared coefficients, two
-    // independent FP64 chains); values enter and leave FP64 through the integer-pipe conversions
-    for (int n = threadIdx.x; n < ny; n += blockDim.x) {
-      double dr[MAXNZ], di[MAXNZ];
-      double pr = 0, pi = 0;
+    // one FP64 recurrence per (n, real/imaginary part); values enter and leave FP64 through the integer-pipe
+    // conversions
+    float* Ff = reinterpret_cast<float*>(F);
+    for (int u = threadIdx.x; u < 2 * ny; u += blockDim.x) {
+      const int n = u >> 1, c = u & 1;
+      double d[MAXNZ];
+      double prev = 0;
 #pragma unroll 4
       for (int k = 0; k < nzc; k++) {
         const double2 ab = AB[(size_t)k * ny + n];
-        const float2 v = F[k * ny + n];
-        pr = fma(-ab.y, pr, ab.x * widen(v.x));
-        pi = fma(-ab.y, pi, ab.x * widen(v.y));
-        dr[k] = pr; di[k] = pi;
+        prev = fma(-ab.y, prev, ab.x * widen(Ff[2 * (k * ny + n) + c]));
+        d[k] = prev;
       }
-      double xr = dr[nzc - 1], xi = di[nzc - 1];
-      F[(nzc - 1) * ny + n] = make_float2(narrow(xr), -narrow(xi));
+      double x = d[nzc - 1];
+      Ff[2 * ((nzc - 1) * ny + n) + c] = c ? -narrow(x) : narrow(x);
 #pragma unroll 4
       for (int k = nzc - 2; k >= 0; k--) {
-        const double c = Cc[(size_t)k * ny + n];
-        xr = fma(-c, xr, dr[k]);
-        xi = fma(-c, xi, di[k]);
-        F[k * ny + n] = make_float2(narrow(xr), -narrow(xi));
+        x = fma(-Cc[(size_t)k * ny + n], x, d[k]);
+        Ff[2 * (k * ny + n) + c] = c ? -narrow(x) : narrow(x);
       }
     }
     __syncthreads();
@@ -474,9 +472,10 @@ __global__ void k_pres_correct(const RunDesc* __restrict__ runs, const int4* ite
 // arithmetic, every thread reconstructs the east and north faces of its own cell (as one packed pair) and the top face,
 // threads 0..TY-1 and TY..TY+TX-1 reconstruct the tile's west and south edge faces, the x and y faces are exchanged
 // through shared memory (double-buffered), and one barrier separates the levels. The group shares the face-flux loads.
-enum TKind { TK_WENO = 0, TK_LIN = 1, TK_W = 2, TK_TH = 3 };
 constexpr int TMAXC = 4;  // plane cells per thread: (TX + 6)(TY + 6) <= TMAXC * TX * TY
-constexpr int TLV = 9;    // per-level constants staged: 1/hz, 1/rho, theta faces x4, thb, qb, thv_env
+// Per-level constants staged in shared memory, rows of MAXNZ: 1/hz, 1/rho (all kinds), theta's four base-profile
+// face values (theta), thb, qb, thv_env (w).
+constexpr int tlv_rows(int kind) { return kind == 2 ? 9 : kind == 3 ? 6 : 2; }
 // Field groups of the transport work items: 0-2 the WENO fields in threes, 3 {u, v}, 4 {w}, 5 {theta}, 6-14 the WENO
 // fields one by one.
 constexpr int TGROUPS = 15;
@@ -547,8 +546,8 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
     out[g] = Rg.fld + ((size_t)out_set * NF + f) * n;
   }
   const int PW = TX + 6, PH = TY + 6, NCELL = PW * PH;
-  float* lv = sm;                                   // [TLV][MAXNZ]
-  float* ring = lv + TLV * MAXNZ;                   // [G][7][NCELL]
+  float* lv = sm;                                   // [tlv_rows][MAXNZ]
+  float* ring = lv + tlv_rows(KIND) * MAXNZ;        // [G][7][NCELL]
   float* fxs = ring + G * 7 * NCELL;                // [2][G][TY][TX + 1]: x faces, west edge at column 0
   float* fys = fxs + 2 * G * TY * (TX + 1);         // [2][G][TY + 1][TX]: y faces, south edge at row 0
   const int FXS = TY * (TX + 1), FYS = (TY + 1) * TX;
@@ -724,9 +723,10 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
   __syncthreads();
 }
 
-template <int KIND, int G>
-__global__ void __launch_bounds__(320, 2) k_transport(const RunDesc* __restrict__ runs, const int4* items, int nitems, int in_set, int out_set,
-                                                       float frac, int stage, int TX, int TY) {
+// MINB: resident blocks per SM the register budget is cut for (2: up to 96 registers a thread, 3: 64).
+template <int KIND, int G, int MINB>
+__global__ void __launch_bounds__(320, MINB) k_transport(const RunDesc* __restrict__ runs, const int4* items, int nitems, int in_set, int out_set,
+                                                          float frac, int stage, int TX, int TY) {
   extern __shared__ float sm[];
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
@@ -1034,22 +1034,24 @@ void launch_proj_xifft(const Launch& L, int mode, int yc, int maxnx) {
 }
 void launch_face_correct(const Launch& L, int set) { k_face_correct<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set); }
 void launch_pres_correct(const Launch& L, int set, int final_) { k_pres_correct<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set, final_); }
-size_t transport_smem(int G, int TX, int TY) {
-  return ((size_t)TLV * MAXNZ + (size_t)G * 7 * (TX + 6) * (TY + 6) + 2 * (size_t)G * TY * (TX + 1) + 2 * (size_t)G * (TY + 1) * TX) * sizeof(float);
+size_t transport_smem(int kind, int G, int TX, int TY) {
+  return ((size_t)tlv_rows(kind) * MAXNZ + (size_t)G * 7 * (TX + 6) * (TY + 6) + 2 * (size_t)G * TY * (TX + 1) + 2 * (size_t)G * (TY + 1) * TX) * sizeof(float);
 }
-void launch_transport(const Launch& L, int kind, int group, int in_set, int out_set, float frac, int stage, int TX, int TY) {
+#define TLAUNCH(K, G, M) k_transport<K, G, M><<<g, TX * TY, transport_smem(K, G, TX, TY), L.stream>>>(L.runs, L.items, L.n, in_set, out_set, frac, stage, TX, TY)
+void launch_transport(const Launch& L, int kind, int group, int minb, int in_set, int out_set, float frac, int stage, int TX, int TY) {
   if (L.n == 0) return;
   dim3 g = GRID(L.n, L.cap);
   switch (kind) {
     case TK_WENO:
-      if (group == 3) k_transport<TK_WENO, 3><<<g, TX * TY, transport_smem(3, TX, TY), L.stream>>>(L.runs, L.items, L.n, in_set, out_set, frac, stage, TX, TY);
-      else k_transport<TK_WENO, 1><<<g, TX * TY, transport_smem(1, TX, TY), L.stream>>>(L.runs, L.items, L.n, in_set, out_set, frac, stage, TX, TY);
+      if (group == 3) { if (minb == 3) TLAUNCH(TK_WENO, 3, 3); else TLAUNCH(TK_WENO, 3, 2); }
+      else { if (minb == 3) TLAUNCH(TK_WENO, 1, 3); else TLAUNCH(TK_WENO, 1, 2); }
       break;
-    case TK_LIN: k_transport<TK_LIN, 2><<<g, TX * TY, transport_smem(2, TX, TY), L.stream>>>(L.runs, L.items, L.n, in_set, out_set, frac, stage, TX, TY); break;
-    case TK_W: k_transport<TK_W, 1><<<g, TX * TY, transport_smem(1, TX, TY), L.stream>>>(L.runs, L.items, L.n, in_set, out_set, frac, stage, TX, TY); break;
-    default: k_transport<TK_TH, 1><<<g, TX * TY, transport_smem(1, TX, TY), L.stream>>>(L.runs, L.items, L.n, in_set, out_set, frac, stage, TX, TY); break;
+    case TK_LIN: TLAUNCH(TK_LIN, 2, 2); break;
+    case TK_W: TLAUNCH(TK_W, 1, 2); break;
+    default: TLAUNCH(TK_TH, 1, 2); break;
   }
 }
+#undef TLAUNCH
 
 void launch_fill_partial(const Launch& L, int set) { k_fill_partial<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set); }
 void launch_fill_final(const Launch& L) { k_fill_final<<<GRID(L.n, L.cap), 32, 0, L.stream>>>(L.runs, L.items, L.n); }
@@ -1065,11 +1067,13 @@ cudaError_t set_smem_limits(int bytes) {
   if ((e = cudaFuncSetAttribute(k_proj_div_xfft, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
   if ((e = cudaFuncSetAttribute(k_proj_xifft, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
   if ((e = cudaFuncSetAttribute(k_sediment, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(k_transport<TK_WENO, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(k_transport<TK_WENO, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(k_transport<TK_LIN, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(k_transport<TK_W, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(k_transport<TK_TH, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(k_transport<TK_WENO, 3, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(k_transport<TK_WENO, 3, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(k_transport<TK_WENO, 1, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(k_transport<TK_WENO, 1, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(k_transport<TK_LIN, 2, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(k_transport<TK_W, 1, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(k_transport<TK_TH, 1, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
   return cudaSuccess;
 }
 

@@ -64,6 +64,7 @@ struct Plan {
   int4* items = nullptr;  // device
   int off[16] = {0}, cnt[16] = {0};
   int maxnx = 0, maxny = 0, maxnz = 0, TX = 40, TY = 8, wenoG = 3;  // transport tile and WENO fields per item
+  int minb = 2;                                                       // WENO transport blocks per SM (register budget)
   int yc = 32;                                                        // layer rows per x-transform item
   bool tuned = false;                                                 // TX, TY, wenoG chosen by timing
   cudaGraph_t graph = nullptr;
@@ -95,8 +96,8 @@ struct sg_context {
   cudaEvent_t fork = nullptr, join[3] = {nullptr, nullptr, nullptr};
   bool forking = false;                 // set while a step is captured into a graph
   bool autotune = true;
-  int pinned[3] = {0, 0, 0};            // transport tile and WENO group fixed by the caller (TX = 0: tune)
-  std::map<std::vector<int>, std::array<int, 3>> tuning;  // batch signature -> (TX, TY, wenoG)
+  int pinned[4] = {0, 0, 0, 2};         // transport tile, WENO group, blocks per SM fixed by the caller (TX = 0: tune)
+  std::map<std::vector<int>, std::array<int, 4>> tuning;  // batch signature -> (TX, TY, wenoG, minb)
 };
 
 namespace {
@@ -316,7 +317,7 @@ int build_plan(sg_context* ctx, const std::vector<int>& slots, Plan& P) {
     for (int m = 0; m < r.nx / 2 + 1; m++) all[FAM_MODES].push_back(make_int4(s, m, 0, 0));
     all[FAM_RUNS].push_back(make_int4(s, 0, 0, 0));
   }
-  if (ctx->pinned[0]) { P.TX = ctx->pinned[0]; P.TY = ctx->pinned[1]; P.wenoG = ctx->pinned[2]; }
+  if (ctx->pinned[0]) { P.TX = ctx->pinned[0]; P.TY = ctx->pinned[1]; P.wenoG = ctx->pinned[2]; P.minb = ctx->pinned[3]; }
   transport_items(ctx, slots, P.TX, P.TY, P.wenoG, all + FAM_T_WENO);
   int st = upload_items(ctx, P, all);
   if (st != SG_OK) return st;
@@ -337,7 +338,7 @@ void launch_transport_kinds(sg_context* ctx, const Plan& P, int in, int out, flo
     Launch L = lx(ctx, P, fams[k]);
     L.cap = L.n;
     if (fork && k > 0) { cudaStreamWaitEvent(ctx->side[k - 1], ctx->fork, 0); L.stream = ctx->side[k - 1]; }
-    if (L.n) launch_transport(L, k, P.wenoG, in, out, frac, stage, P.TX, P.TY);
+    if (L.n) launch_transport(L, k, P.wenoG, P.minb, in, out, frac, stage, P.TX, P.TY);
     if (fork && k > 0) cudaEventRecord(ctx->join[k - 1], ctx->side[k - 1]);
     hook(hookBase + k);
   }
@@ -361,7 +362,7 @@ int autotune_transport(sg_context* ctx, Plan& P) {
     int c = 1; while (c < (int)P.slots.size()) c *= 2;
     sig.push_back(c);
   }
-  std::array<int, 3> best{P.TX, P.TY, P.wenoG};
+  std::array<int, 4> best{P.TX, P.TY, P.wenoG, P.minb};
   auto it = ctx->tuning.find(sig);
   if (it != ctx->tuning.end()) {
     best = it->second;
@@ -375,13 +376,13 @@ int autotune_transport(sg_context* ctx, Plan& P) {
     for (auto& sh : shapes) {
       const int TX = sh[0], TY = sh[1];
       if (TX > 2 * P.maxnx || TY > 2 * P.maxny) continue;
-      for (int G : {3, 1}) {
-        if (transport_smem(G, TX, TY) > (size_t)ctx->maxSmem) continue;
+      for (int G : {3, 1}) for (int MB : {2, 3}) {
+        if (transport_smem(TK_WENO, G, TX, TY) > (size_t)ctx->maxSmem) continue;
         std::vector<int4> all[FAM_COUNT];
         transport_items(ctx, P.slots, TX, TY, G, all + FAM_T_WENO);
         int st = upload_items(ctx, T, all);
         if (st != SG_OK) { cudaEventDestroy(e0); cudaEventDestroy(e1); return st; }
-        T.TX = TX; T.TY = TY; T.wenoG = G;
+        T.TX = TX; T.TY = TY; T.wenoG = G; T.minb = MB;
         float ms = 1e30f;
         for (int rep = 0; rep < 4; rep++) {
           cudaEventRecord(e0, ctx->stream);
@@ -392,13 +393,13 @@ int autotune_transport(sg_context* ctx, Plan& P) {
           if (rep) ms = std::min(ms, t);
         }
         CK(cudaGetLastError());
-        if (ms < bestMs) { bestMs = ms; best = {TX, TY, G}; }
+        if (ms < bestMs) { bestMs = ms; best = {TX, TY, G, MB}; }
       }
     }
     cudaEventDestroy(e0); cudaEventDestroy(e1);
     ctx->tuning[sig] = best;
   }
-  P.TX = best[0]; P.TY = best[1]; P.wenoG = best[2]; P.tuned = true;
+  P.TX = best[0]; P.TY = best[1]; P.wenoG = best[2]; P.minb = best[3]; P.tuned = true;
   std::vector<int4> all[FAM_COUNT];
   for (int f = 0; f < FAM_COUNT; f++) {  // keep the other families, rebuild the transport ones
     if (f >= FAM_T_WENO && f <= FAM_T_TH) continue;
@@ -420,7 +421,7 @@ void enqueue_part(sg_context* ctx, const Plan& P, int part, Hook hook) {
   Launch modes = lx(ctx, P, FAM_MODES), runs = lx(ctx, P, FAM_RUNS);
   modes.cap = modes.n;  // one block per wavenumber: its column solves are serial in z, so spread them over the SMs
   rf.cap = rf.n; rp.cap = rp.n;
-  const int mthreads = std::min(256, std::max(64, (P.maxny + 31) / 32 * 32));
+  const int mthreads = std::min(512, std::max(64, (2 * P.maxny + 31) / 32 * 32));
   const int mbudget = std::min(ctx->maxSmem, 200 * 1024);
   auto project = [&](int set, int final_) {
     launch_proj_div_xfft(rp, PROJ_PRES, set, P.yc, P.maxnx); hook(7);
@@ -852,7 +853,7 @@ int sg_set_transport_shape(sg_context* ctx, int tile_x, int tile_y, int weno_gro
   else {
     if (tile_x < 1 || tile_y < 1 || tile_x * tile_y > 320 || tile_x * tile_y < tile_x + tile_y ||
         (tile_x + 6) * (tile_y + 6) > 4 * tile_x * tile_y || (weno_group != 1 && weno_group != 3) ||
-        transport_smem(weno_group, tile_x, tile_y) > (size_t)ctx->maxSmem)
+        transport_smem(TK_WENO, weno_group, tile_x, tile_y) > (size_t)ctx->maxSmem)
       return fail(ctx, SG_ERR_INVALID, "transport shape out of range");
     ctx->pinned[0] = tile_x; ctx->pinned[1] = tile_y; ctx->pinned[2] = weno_group;
   }
@@ -860,14 +861,15 @@ int sg_set_transport_shape(sg_context* ctx, int tile_x, int tile_y, int weno_gro
   ctx->plans.clear();
   return SG_OK;
 }
-int sg_batch_transport_shape(sg_context* ctx, const sg_run* runs, int n, int* shape3) {
+int sg_batch_transport_shape(sg_context* ctx, const sg_run* runs, int n, int* shape4) {
+  int* shape3 = shape4;
   if (!ctx || !shape3) return SG_ERR_INVALID;
   std::vector<int> slots;
   int st = slots_of(ctx, runs, n, slots);
   if (st != SG_OK) return st;
   Plan* P = get_plan(ctx, slots, &st);
   if (!P) return st;
-  shape3[0] = P->TX; shape3[1] = P->TY; shape3[2] = P->wenoG;
+  shape3[0] = P->TX; shape3[1] = P->TY; shape3[2] = P->wenoG; shape3[3] = P->minb;
   return SG_OK;
 }
 int sg_debug_step_part(sg_context* ctx, sg_run run, int part) {

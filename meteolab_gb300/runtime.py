@@ -202,9 +202,9 @@ class Context:
         self.check(load().sg_set_transport_shape(self.h, tile_x, tile_y, weno_group), "transport shape")
 
     def transport_shape(self, runs: Sequence["Run"]) -> tuple:
-        """(tile_x, tile_y, weno_group) the batch of `runs` is stepped with."""
+        """(tile_x, tile_y, weno_group, blocks per SM of the WENO kernel) the batch of `runs` is stepped with."""
         ids = (C.c_int32 * len(runs))(*[r.id for r in runs])
-        out = (C.c_int * 3)()
+        out = (C.c_int * 4)()
         self.check(load().sg_batch_transport_shape(self.h, ids, len(runs), out), "transport shape")
         return tuple(out)
 
