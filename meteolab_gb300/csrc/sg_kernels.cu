@@ -154,7 +154,7 @@ __global__ void k_fall_courant(const RunDesc* __restrict__ runs, const int4* ite
 // One thread per column: the hail swath (collectHail, :697-706), then for rain, snow, graupel and hail the upwind
 // flux-form fall in ceil(courant / 0.8) sub-steps (sediment/sedimentPart, :565-598), bottom-up so each face uses the
 // values above from before the sub-step, the ground flux into the rain gauge. Fall speeds are those of the step's
-// start. Columns stay in shared memory.
+// start. Columns stay in shared memory; a column of zeros stays zero and is left alone.
 constexpr int SED_COLS = 64;
 __global__ void k_sediment(const RunDesc* __restrict__ runs, const int4* items, int nitems) {
   extern __shared__ float sm[];
@@ -163,7 +163,14 @@ __global__ void k_sediment(const RunDesc* __restrict__ runs, const int4* items, 
     if (R.cnt[C_FAILED]) continue;
     const int nz = R.nz, layer = R.layer, t = threadIdx.x;
     float* sq = sm;                     // [nz][SED_COLS]
-    float* sv = sm + nz * SED_COLS;     // [nz][SED_COLS]
+    float* sv = sq + nz * SED_COLS;     // [nz][SED_COLS]
+    float* lrho = sv + nz * SED_COLS;   // [nz] rho0, 1/(rho0 h), fall-speed density factor
+    float* lk = lrho + nz;
+    float* lfs = lk + nz;
+    for (int z = t; z < nz; z += blockDim.x) {
+      lrho[z] = lvl(R, L_RHO, z); lk[z] = lvl(R, L_INV_RHO, z) * lvl(R, L_INV_HZ, z); lfs[z] = lvl(R, L_FALLSQ, z);
+    }
+    __syncthreads();
     const int c = items[it].y * SED_COLS + t;
     const bool on = t < SED_COLS && c < layer;
     const float rho0 = R.rho0;
@@ -172,35 +179,43 @@ __global__ void k_sediment(const RunDesc* __restrict__ runs, const int4* items, 
     float* hailSize = R.cols + 2 * layer;
     for (int f = 0; f < 4; f++) {
       float* a = field(R, 0, f);
-      float courant = R.scr[S_COURANT + f];
-      int parts = max(1, (int)ceilf(courant / .8f));
-      if (on) {
-        for (int z = 0; z < nz; z++) {
-          float q = a[c + z * layer], rho = lvl(R, L_RHO, z), fsq = lvl(R, L_FALLSQ, z);
-          float v = f == 0 ? phys::rainFall(q, rho, fsq) : f == 1 ? phys::snowFall(q, rho, fsq) : f == 2 ? phys::graupelFall(q, rho) : phys::hailFall(q, rho);
-          sq[z * SED_COLS + t] = q; sv[z * SED_COLS + t] = v;
-        }
-        if (f == HAIL && (R.flags & RF_ICE)) {
-          float h = sq[t];
-          if (h > 1e-9f) {
-            hailGround[c] += rho0 * h * sv[t] * R.dt;
-            hailSize[c] = fmaxf(hailSize[c], phys::hailMaxDiameter(h, rho0) * 1000.f);
-          }
-        }
-        if (f == RAIN || (R.flags & RF_ICE)) {
-          float dts = R.dt / (float)parts;
-          for (int p = 0; p < parts; p++) {
-            precip[c] += rho0 * sq[t] * sv[t] * dts;
-            for (int z = 0; z < nz; z++) {
-              float inflow = z < nz - 1 ? lvl(R, L_RHO, z + 1) * sq[(z + 1) * SED_COLS + t] * sv[(z + 1) * SED_COLS + t] : 0.f;
-              float q = sq[z * SED_COLS + t];
-              sq[z * SED_COLS + t] = q + dts * (inflow - lvl(R, L_RHO, z) * q * sv[z * SED_COLS + t]) * lvl(R, L_INV_RHO, z) * lvl(R, L_INV_HZ, z);
-            }
-          }
-          for (int z = 0; z < nz; z++) a[c + z * layer] = sq[z * SED_COLS + t];
+      const float courant = R.scr[S_COURANT + f];
+      const int parts = max(1, (int)ceilf(courant / .8f));
+      if (!on) continue;
+      bool any = false;
+#pragma unroll 8
+      for (int z = 0; z < nz; z++) {
+        const float q = a[c + z * layer];
+        sq[z * SED_COLS + t] = q;
+        any |= q != 0.f;
+      }
+      if (!any) continue;
+      for (int z = 0; z < nz; z++) {
+        const float q = sq[z * SED_COLS + t], rho = lrho[z], fsq = lfs[z];
+        sv[z * SED_COLS + t] = f == 0 ? phys::rainFall(q, rho, fsq) : f == 1 ? phys::snowFall(q, rho, fsq) : f == 2 ? phys::graupelFall(q, rho) : phys::hailFall(q, rho);
+      }
+      if (f == HAIL && (R.flags & RF_ICE)) {
+        const float h = sq[t];
+        if (h > 1e-9f) {
+          hailGround[c] += rho0 * h * sv[t] * R.dt;
+          hailSize[c] = fmaxf(hailSize[c], phys::hailMaxDiameter(h, rho0) * 1000.f);
         }
       }
+      if (f == RAIN || (R.flags & RF_ICE)) {
+        const float dts = R.dt / (float)parts;
+        for (int p = 0; p < parts; p++) {
+          precip[c] += rho0 * sq[t] * sv[t] * dts;
+          float inflowAbove = 0.f;  // the flux into level z from above, from the values before this sub-step
+          for (int z = nz - 1; z >= 0; z--) {
+            const float q = sq[z * SED_COLS + t], out = lrho[z] * q * sv[z * SED_COLS + t];
+            sq[z * SED_COLS + t] = q + dts * (inflowAbove - out) * lk[z];
+            inflowAbove = out;
+          }
+        }
+        for (int z = 0; z < nz; z++) a[c + z * layer] = sq[z * SED_COLS + t];
+      }
     }
+    __syncthreads();  // the level tables are restaged for the block's next item
   }
 }
 
@@ -390,6 +405,182 @@ __global__ void k_proj_xifft(const RunDesc* __restrict__ runs, const int4* items
       const int r = row_of(e, inv_nx), x = e - r * nx;
       const float2 z = Zf[(r >> 1) * nx + x];
       out[(y0 + r) * nx + x] = ((r & 1) ? -z.y : z.x) * norm;
+    }
+    __syncthreads();
+  }
+}
+
+
+// ---- the whole-layer path (grids whose layer spectrum fits in shared memory: the benchmark's 40x32 and 80x64):
+// the divergence kernel transforms each layer along x and y, the mode kernel is a pure FP64 sweep without
+// transforms or barriers, and the inverse kernel transforms back along y and x.
+
+// Builds the half spectrum X[m][y] (m <= nx/2) of the real rows held in pairs in Zf (spectral.ts:246-255).
+__device__ __forceinline__ void unpack_rows(const float2* Zf, float2* X, int nx, int ny, int rows, int nm) {
+  for (int e = threadIdx.x; e < nm * rows; e += blockDim.x) {
+    const int m = e / rows, r = e - m * rows, pr = r >> 1, c = m ? nx - m : 0;
+    const float2 zm = Zf[pr * nx + m], zc = Zf[pr * nx + c];
+    X[m * ny + r] = (r & 1) == 0 ? make_float2(.5f * (zm.x + zc.x), .5f * (zm.y - zc.y))
+                                 : make_float2(.5f * (zm.y + zc.y), .5f * (zc.x - zm.x));
+  }
+  __syncthreads();
+}
+
+// Divergence of one layer (FACE or PRES, as k_proj_div_xfft) and its 2-D forward transform, written
+// spec[(m * nzc + k) * ny + n].
+__global__ void k_proj_div_fft2(const RunDesc* __restrict__ runs, const int4* items, int nitems, int mode, int set) {
+  extern __shared__ float2 smc[];
+  FOR_ITEMS {
+    const RunDesc& R = runs[items[it].x];
+    if (R.cnt[C_FAILED]) continue;
+    const int k = items[it].y, nx = R.nx, ny = R.ny, layer = R.layer, nz = R.nz, nm = R.nm;
+    const int pairs = (ny + 1) / 2, nzc = mode == PROJ_FACE ? nz : nz - 1;
+    const float inv_nx = 1.f / (float)nx;
+    float2* Z = smc;                        // [pairs][nx]
+    float2* T = Z + pairs * nx;
+    float2* X = T + pairs * nx;             // [nm][ny]
+    float2* Xs = X + nm * ny;
+    const float *u = field(R, set, U), *v = field(R, set, V), *w = field(R, set, W);
+    const float idx = R.inv_dx, idy = R.inv_dy;
+    if (mode == PROJ_FACE) {
+      const float rho = lvl(R, L_RHO, k), ihz = lvl(R, L_INV_HZ, k);
+      const float rup = k < nz - 1 ? .5f * lvl(R, L_RUP, k) : 0.f, rdn = k > 0 ? .5f * lvl(R, L_RUP, k - 1) : 0.f;
+      const int l = k * layer, lu = k < nz - 1 ? l + layer : l, ld = k > 0 ? l - layer : l;
+#pragma unroll 4
+      for (int e = threadIdx.x; e < pairs * 2 * nx; e += blockDim.x) {
+        const int r = row_of(e, inv_nx), x = e - r * nx, y = r;
+        float d = 0.f;
+        if (r < ny) {
+          const int c = x + y * nx;
+          const int ce = (x + 1 == nx ? 0 : x + 1) + y * nx, cw = (x == 0 ? nx - 1 : x - 1) + y * nx;
+          const int cn = x + (y + 1 == ny ? 0 : y + 1) * nx, cs = x + (y == 0 ? ny - 1 : y - 1) * nx;
+          const float ddx = .5f * rho * (u[ce + l] - u[cw + l]);
+          const float ddy = .5f * rho * (v[cn + l] - v[cs + l]);
+          const float wc = w[c + l];
+          const float up = rup * (wc + w[c + lu]), dn = rdn * (w[c + ld] + wc);
+          d = ddx * idx + ddy * idy + (up - dn) * ihz;
+        }
+        reinterpret_cast<float*>(&Z[(r >> 1) * nx + x])[r & 1] = d;
+      }
+    } else {
+      const float r0 = .25f * lvl(R, L_RHO, k), r1 = .25f * lvl(R, L_RHO, k + 1), idz = lvl(R, L_INV_DZS, k), idt = 1.f / R.dt;
+      const int l0 = k * layer, l1 = l0 + layer;
+#pragma unroll 4
+      for (int e = threadIdx.x; e < pairs * 2 * nx; e += blockDim.x) {
+        const int r = row_of(e, inv_nx), x = e - r * nx, y = r;
+        float d = 0.f;
+        if (r < ny) {
+          const int x1 = x + 1 == nx ? 0 : x + 1, y1 = (y + 1 == ny ? 0 : y + 1) * nx, yy = y * nx;
+          const int a = x + yy, b = x1 + yy, ee = x + y1, f = x1 + y1;
+          const float ddx = (r0 * ((u[b + l0] - u[a + l0]) + (u[f + l0] - u[ee + l0])) + r1 * ((u[b + l1] - u[a + l1]) + (u[f + l1] - u[ee + l1]))) * idx;
+          const float ddy = (r0 * ((v[ee + l0] - v[a + l0]) + (v[f + l0] - v[b + l0])) + r1 * ((v[ee + l1] - v[a + l1]) + (v[f + l1] - v[b + l1]))) * idy;
+          const float ddz = (r1 * ((w[a + l1] + w[b + l1]) + (w[ee + l1] + w[f + l1])) - r0 * ((w[a + l0] + w[b + l0]) + (w[ee + l0] + w[f + l0]))) * idz;
+          d = (ddx + ddy + ddz) * idt;
+        }
+        reinterpret_cast<float*>(&Z[(r >> 1) * nx + x])[r & 1] = d;
+      }
+    }
+    __syncthreads();
+    FftPlan Px{nx, R.fx_nf, R.fx_rad, R.twx}, Py{ny, R.fy_nf, R.fy_rad, R.twy};
+    const float2* Zf = fft_rows_any(Z, T, nx, pairs, Px);
+    unpack_rows(Zf, X, nx, ny, ny, nm);
+    const float2* Xf = fft_rows_any(X, Xs, ny, nm, Py);
+    float2* g = R.spec + (size_t)k * ny;
+    for (int e = threadIdx.x; e < nm * ny; e += blockDim.x) {
+      const int m = e / ny, n = e - m * ny;
+      g[(size_t)m * nzc * ny + n] = Xf[e];
+    }
+    __syncthreads();
+  }
+}
+
+// One x-wavenumber m of one run per block, thread (n, real/imaginary): the FP64 sweeps of k_proj_modes on the 2-D
+// spectrum in place (the input and the output stay in global memory; no transform, no barrier).
+__global__ void k_proj_sweep(const RunDesc* __restrict__ runs, const int4* items, int nitems, int mode) {
+  FOR_ITEMS {
+    const RunDesc& R = runs[items[it].x];
+    if (R.cnt[C_FAILED]) continue;
+    const int m = items[it].y, ny = R.ny, nz = R.nz, nzc = mode == PROJ_FACE ? nz : nz - 1;
+    const int u = threadIdx.x;
+    if (u >= 2 * ny) continue;
+    const int n = u >> 1, c = u & 1;
+    float* g = reinterpret_cast<float*>(R.spec + (size_t)m * nzc * ny) + c;
+    const double2* AB = (mode == PROJ_FACE ? R.tri_face : R.tri_pres) + (size_t)m * nzc * ny;
+    const double* Cc = reinterpret_cast<const double*>((mode == PROJ_FACE ? R.tri_face : R.tri_pres) + (size_t)R.nm * nzc * ny) + (size_t)m * nzc * ny;
+    double d[MAXNZ];
+    double prev = 0;
+    // levels in blocks of 8: the block's coefficients and values are loaded before its recurrence steps
+    for (int k0 = 0; k0 < nzc; k0 += 8) {
+      double2 ab[8];
+      float r[8];
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        const int k = min(k0 + j, nzc - 1);
+        ab[j] = AB[(size_t)k * ny + n];
+        r[j] = g[2 * ((size_t)k * ny + n)];
+      }
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        if (k0 + j < nzc) { prev = fma(-ab[j].y, prev, ab[j].x * widen(r[j])); d[k0 + j] = prev; }
+      }
+    }
+    double x = d[nzc - 1];
+    g[2 * ((size_t)(nzc - 1) * ny + n)] = narrow(x);
+    for (int k1 = nzc - 2; k1 >= 0; k1 -= 8) {
+      double cc[8];
+#pragma unroll
+      for (int j = 0; j < 8; j++) cc[j] = Cc[(size_t)max(k1 - j, 0) * ny + n];
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        const int k = k1 - j;
+        if (k >= 0) { x = fma(-cc[j], x, d[k]); g[2 * ((size_t)k * ny + n)] = narrow(x); }
+      }
+    }
+  }
+}
+
+// The 2-D inverse transform of one layer (y, then x with the Hermitian rows rebuilt two real rows per complex
+// transform), normalised by nx*ny, into phi (FACE) or the pressure (PRES). Each inverse is the conjugate of the
+// forward transform of the conjugate.
+__global__ void k_proj_ifft2(const RunDesc* __restrict__ runs, const int4* items, int nitems, int mode) {
+  extern __shared__ float2 smc[];
+  FOR_ITEMS {
+    const RunDesc& R = runs[items[it].x];
+    if (R.cnt[C_FAILED]) continue;
+    const int k = items[it].y, nx = R.nx, ny = R.ny, nz = R.nz, mh = R.mh, nm = R.nm;
+    const int pairs = (ny + 1) / 2, nzc = mode == PROJ_FACE ? nz : nz - 1;
+    float2* X = smc;                        // [nm][ny]
+    float2* Xs = X + nm * ny;
+    float2* Z = Xs + nm * ny;               // [pairs][nx]
+    float2* T = Z + pairs * nx;
+    const float2* g = R.spec + (size_t)k * ny;
+    for (int e = threadIdx.x; e < nm * ny; e += blockDim.x) {
+      const int m = e / ny, n = e - m * ny;
+      const float2 v = g[(size_t)m * nzc * ny + n];
+      X[e] = make_float2(v.x, -v.y);
+    }
+    __syncthreads();
+    FftPlan Px{nx, R.fx_nf, R.fx_rad, R.twx}, Py{ny, R.fy_nf, R.fy_rad, R.twy};
+    const float2* G = fft_rows_any(X, Xs, ny, nm, Py);   // conj of the y-inverse: H[m][y] = conj(G[m][y])
+    const float inv_nx = 1.f / (float)nx;
+    for (int e = threadIdx.x; e < pairs * nx; e += blockDim.x) {
+      const int pr = row_of(e, inv_nx), m = e - pr * nx, c = m <= mh ? m : nx - m;
+      const float sg = m <= mh ? 1.f : -1.f;
+      const bool real = c == 0 || 2 * c == nx, pair = 2 * pr + 1 < ny;
+      const float2 A = G[c * ny + 2 * pr];
+      const float ar = A.x, ai = real ? 0.f : -sg * A.y;
+      float br = 0.f, bi = 0.f;
+      if (pair) { const float2 B = G[c * ny + 2 * pr + 1]; br = B.x; bi = real ? 0.f : -sg * B.y; }
+      Z[pr * nx + m] = make_float2(ar - bi, -(ai + br));  // conj(A + iB)
+    }
+    __syncthreads();
+    const float2* Zf = fft_rows_any(Z, T, nx, pairs, Px);
+    const float norm = 1.f / (float)(nx * ny);
+    float* out = (mode == PROJ_FACE ? R.phi : R.pres) + (size_t)k * nx * ny;
+    for (int e = threadIdx.x; e < ny * nx; e += blockDim.x) {
+      const int r = row_of(e, inv_nx), x = e - r * nx;
+      const float2 z = Zf[(r >> 1) * nx + x];
+      out[r * nx + x] = ((r & 1) ? -z.y : z.x) * norm;
     }
     __syncthreads();
   }
@@ -678,11 +869,20 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
     }
     // the tile's west and south edge faces
     if (edgeW || edgeS) {
+      const bool pe = me >= 0.f;
+      const int es = edgeW ? FXS : FYS;
 #pragma unroll
-      for (int g = 0; g < G; g++) {
-        float a, bb, c, d, e;
-        face_stencil(ring + (g * 7 + s_0) * NCELL + ecell, estride, me >= 0.f, a, bb, c, d, e);
-        edst[(buf * G + g) * (edgeW ? FXS : FYS)] = me * recon1<KIND>(a, bb, c, d, e);
+      for (int g = 0; g < G; g += 2) {  // fields in pairs, as the top faces
+        float2 A, B, C, D, E;
+        face_stencil(ring + (g * 7 + s_0) * NCELL + ecell, estride, pe, A.x, B.x, C.x, D.x, E.x);
+        if (g + 1 < G) {
+          face_stencil(ring + ((g + 1) * 7 + s_0) * NCELL + ecell, estride, pe, A.y, B.y, C.y, D.y, E.y);
+          const float2 r = recon2<KIND>(A, B, C, D, E);
+          edst[(buf * G + g) * es] = me * r.x;
+          edst[(buf * G + g + 1) * es] = me * r.y;
+        } else {
+          edst[(buf * G + g) * es] = me * recon1<KIND>(A.x, B.x, C.x, D.x, E.x);
+        }
       }
     }
     cp_async_wait_all();
@@ -748,19 +948,36 @@ __global__ void k_fill_partial(const RunDesc* __restrict__ runs, const int4* ite
     float hi[NCONS * 3], lo[NCONS * 3];
 #pragma unroll
     for (int k = 0; k < NCONS * 3; k++) hi[k] = lo[k] = 0.f;
-    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-      const int z = i / R.layer;
-      const float whi = lvl(R, L_LW, z), wlo = lvl(R, L_LW_LO, z);
+    const float* fp[NCONS];
 #pragma unroll
-      for (int k = 0; k < NCONS; k++) {
-        const float x = field(R, set, cons_field(k))[i];
-        if (x < 1e-10f) {
-          if (x != 0.f) {
-            df_add_prod(hi[3 * k], lo[3 * k], whi, wlo, x);
-            if (x < 0.f) df_add_prod(hi[3 * k + 2], lo[3 * k + 2], whi, wlo, -x);
+    for (int k = 0; k < NCONS; k++) fp[k] = field(R, set, cons_field(k));
+    const int layer = R.layer, B = blockDim.x;
+    int z = (i0 + threadIdx.x) / layer;
+    // four nodes per pass: their 28 loads are issued together
+    for (int base = i0 + threadIdx.x; base < i1; base += 4 * B) {
+      float x[4][NCONS];
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const int i = base + j * B;
+#pragma unroll
+        for (int k = 0; k < NCONS; k++) x[j][k] = i < i1 ? fp[k][i] : 0.f;
+      }
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const int i = base + j * B;
+        while (i >= (z + 1) * layer) z++;
+        const float whi = lvl(R, L_LW, z), wlo = lvl(R, L_LW_LO, z);
+#pragma unroll
+        for (int k = 0; k < NCONS; k++) {
+          const float v = x[j][k];
+          if (v < 1e-10f) {
+            if (v != 0.f) {
+              df_add_prod(hi[3 * k], lo[3 * k], whi, wlo, v);
+              if (v < 0.f) df_add_prod(hi[3 * k + 2], lo[3 * k + 2], whi, wlo, -v);
+            }
+          } else {
+            df_add_prod(hi[3 * k + 1], lo[3 * k + 1], whi, wlo, v);
           }
-        } else {
-          df_add_prod(hi[3 * k + 1], lo[3 * k + 1], whi, wlo, x);
         }
       }
     }
@@ -1014,7 +1231,7 @@ void launch_theta_in(const Launch& L, const float* src) { k_theta_in<<<GRID(L.n,
 void launch_theta_out(const Launch& L, float* dst) { k_theta_out<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, dst); }
 void launch_fall_courant(const Launch& L) { k_fall_courant<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n); }
 void launch_sediment(const Launch& L, int maxnz) {
-  k_sediment<<<GRID(L.n, L.cap), SED_COLS, 2 * maxnz * SED_COLS * sizeof(float), L.stream>>>(L.runs, L.items, L.n);
+  k_sediment<<<GRID(L.n, L.cap), SED_COLS, (2 * maxnz * SED_COLS + 3 * maxnz) * sizeof(float), L.stream>>>(L.runs, L.items, L.n);
 }
 void launch_proj_div_xfft(const Launch& L, int mode, int set, int yc, int maxnx) {
   size_t smem = (size_t)2 * ((yc + 1) / 2) * maxnx * sizeof(float2);
@@ -1027,6 +1244,18 @@ void launch_proj_modes(const Launch& L, int mode, int maxnz, int maxny, int thre
   group = std::max(group, 1);
   const size_t smem = slab + (size_t)group * maxny * sizeof(float2);
   k_proj_modes<<<GRID(L.n, L.cap), threads, smem, L.stream>>>(L.runs, L.items, L.n, mode, group);
+}
+size_t layer_fft_smem(int maxnx, int maxny) {
+  return ((size_t)2 * ((maxny + 1) / 2) * maxnx + (size_t)2 * (maxnx / 2 + 1) * maxny) * sizeof(float2);
+}
+void launch_proj_div_fft2(const Launch& L, int mode, int set, int maxnx, int maxny) {
+  k_proj_div_fft2<<<GRID(L.n, L.cap), 256, layer_fft_smem(maxnx, maxny), L.stream>>>(L.runs, L.items, L.n, mode, set);
+}
+void launch_proj_sweep(const Launch& L, int mode, int maxny) {
+  k_proj_sweep<<<GRID(L.n, L.cap), (2 * maxny + 31) / 32 * 32, 0, L.stream>>>(L.runs, L.items, L.n, mode);
+}
+void launch_proj_ifft2(const Launch& L, int mode, int maxnx, int maxny) {
+  k_proj_ifft2<<<GRID(L.n, L.cap), 256, layer_fft_smem(maxnx, maxny), L.stream>>>(L.runs, L.items, L.n, mode);
 }
 void launch_proj_xifft(const Launch& L, int mode, int yc, int maxnx) {
   size_t smem = ((size_t)yc * (maxnx / 2 + 1) + (size_t)2 * ((yc + 1) / 2) * maxnx) * sizeof(float2);
@@ -1067,6 +1296,8 @@ cudaError_t set_smem_limits(int bytes) {
   if ((e = cudaFuncSetAttribute(k_proj_div_xfft, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
   if ((e = cudaFuncSetAttribute(k_proj_xifft, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
   if ((e = cudaFuncSetAttribute(k_sediment, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(k_proj_div_fft2, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(k_proj_ifft2, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
   if ((e = cudaFuncSetAttribute(k_transport<TK_WENO, 3, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
   if ((e = cudaFuncSetAttribute(k_transport<TK_WENO, 3, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
   if ((e = cudaFuncSetAttribute(k_transport<TK_WENO, 1, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;

@@ -21,6 +21,11 @@ void launch_fall_courant(const Launch& L);
 void launch_sediment(const Launch& L, int maxnz);
 void launch_proj_div_xfft(const Launch& L, int mode, int set, int yc, int maxnx);
 void launch_proj_modes(const Launch& L, int mode, int maxnz, int maxny, int threads, int smem_budget);
+// The whole-layer path: 2-D transforms per layer, FP64 sweeps per (m, n) in global memory.
+size_t layer_fft_smem(int maxnx, int maxny);
+void launch_proj_div_fft2(const Launch& L, int mode, int set, int maxnx, int maxny);
+void launch_proj_sweep(const Launch& L, int mode, int maxny);
+void launch_proj_ifft2(const Launch& L, int mode, int maxnx, int maxny);
 void launch_proj_xifft(const Launch& L, int mode, int yc, int maxnx);
 void launch_face_correct(const Launch& L, int set);
 void launch_pres_correct(const Launch& L, int set, int final_);

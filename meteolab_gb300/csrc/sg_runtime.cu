@@ -66,6 +66,7 @@ struct Plan {
   int maxnx = 0, maxny = 0, maxnz = 0, TX = 40, TY = 8, wenoG = 3;  // transport tile and WENO fields per item
   int minb = 2;                                                       // WENO transport blocks per SM (register budget)
   int yc = 32;                                                        // layer rows per x-transform item
+  bool layerfft = false;                                              // 2-D transforms per layer (see enqueue_part)
   bool tuned = false;                                                 // TX, TY, wenoG chosen by timing
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -96,6 +97,7 @@ struct sg_context {
   cudaEvent_t fork = nullptr, join[3] = {nullptr, nullptr, nullptr};
   bool forking = false;                 // set while a step is captured into a graph
   bool autotune = true;
+  bool rowsOnly = false;                // row-transform spectral path for every grid (SG_SPECTRAL_ROWS=1)
   int pinned[4] = {0, 0, 0, 2};         // transport tile, WENO group, blocks per SM fixed by the caller (TX = 0: tune)
   std::map<std::vector<int>, std::array<int, 4>> tuning;  // batch signature -> (TX, TY, wenoG, minb)
 };
@@ -303,8 +305,11 @@ int build_plan(sg_context* ctx, const std::vector<int>& slots, Plan& P) {
   P.TX = all40 ? 40 : 32;
   P.TY = 8;
   P.wenoG = 3;
-  // x-transform items: a whole layer of the benchmark grids (up to 32 rows), 16 rows for grids wider than 128
-  P.yc = std::min(P.maxnx > 128 ? 16 : 32, (P.maxny + 1) / 2 * 2);
+  // Spectral solves: when a layer's spectrum fits in shared memory (the 40x32 and 80x64 grids), whole layers are
+  // transformed in 2-D and the mode kernel is a pure FP64 sweep; otherwise rows of 16 or 32 are x-transformed and
+  // the mode kernel transforms along y around its sweep.
+  P.layerfft = !ctx->rowsOnly && layer_fft_smem(P.maxnx, P.maxny) <= (size_t)std::min(ctx->maxSmem, 100 * 1024);
+  P.yc = P.layerfft ? P.maxny : std::min(P.maxnx > 128 ? 16 : 32, (P.maxny + 1) / 2 * 2);
   for (int s : slots) {
     const Run& r = ctx->runs[s];
     int n = r.nx * r.ny * r.nz, nch = (n + CHUNK - 1) / CHUNK, layer = r.nx * r.ny;
@@ -423,19 +428,27 @@ void enqueue_part(sg_context* ctx, const Plan& P, int part, Hook hook) {
   rf.cap = rf.n; rp.cap = rp.n;
   const int mthreads = std::min(512, std::max(64, (2 * P.maxny + 31) / 32 * 32));
   const int mbudget = std::min(ctx->maxSmem, 200 * 1024);
+  // the three stages of a spectral solve: divergence and forward transform, mode solves, inverse transform
+  auto solve = [&](const Launch& rows, int mode, int set) {
+    if (P.layerfft) {
+      launch_proj_div_fft2(rows, mode, set, P.maxnx, P.maxny); hook(mode == PROJ_FACE ? 2 : 7);
+      launch_proj_sweep(modes, mode, P.maxny); hook(mode == PROJ_FACE ? 3 : 8);
+      launch_proj_ifft2(rows, mode, P.maxnx, P.maxny); hook(mode == PROJ_FACE ? 4 : 9);
+    } else {
+      launch_proj_div_xfft(rows, mode, set, P.yc, P.maxnx); hook(mode == PROJ_FACE ? 2 : 7);
+      launch_proj_modes(modes, mode, P.maxnz, P.maxny, mthreads, mbudget); hook(mode == PROJ_FACE ? 3 : 8);
+      launch_proj_xifft(rows, mode, P.yc, P.maxnx); hook(mode == PROJ_FACE ? 4 : 9);
+    }
+  };
   auto project = [&](int set, int final_) {
-    launch_proj_div_xfft(rp, PROJ_PRES, set, P.yc, P.maxnx); hook(7);
-    launch_proj_modes(modes, PROJ_PRES, P.maxnz, P.maxny, mthreads, mbudget); hook(8);
-    launch_proj_xifft(rp, PROJ_PRES, P.yc, P.maxnx); hook(9);
+    solve(rp, PROJ_PRES, set);
     launch_pres_correct(node, set, final_); hook(final_ ? 16 : 10);
   };
   if (part == 1) {
     launch_fall_courant(node); hook(0);
     launch_sediment(cols, P.maxnz); hook(1);
   } else if (part == 2) {
-    launch_proj_div_xfft(rf, PROJ_FACE, A, P.yc, P.maxnx); hook(2);
-    launch_proj_modes(modes, PROJ_FACE, P.maxnz, P.maxny, mthreads, mbudget); hook(3);
-    launch_proj_xifft(rf, PROJ_FACE, P.yc, P.maxnx); hook(4);
+    solve(rf, PROJ_FACE, A);
     launch_face_correct(node, A); hook(5);
     const int in[3] = {A, B, C}, out[3] = {B, C, B};
     for (int s = 0; s < 3; s++) {
@@ -555,6 +568,7 @@ int sg_context_create(int device, uint64_t hbm_budget_bytes, sg_context** out) {
     if ((e = cudaStreamCreateWithFlags(&ctx->side[k], cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&ctx->join[k], cudaEventDisableTiming)) != cudaSuccess) { delete ctx; return SG_ERR_DEVICE; }
   if (const char* a = getenv("SG_AUTOTUNE")) ctx->autotune = atoi(a) != 0;
+  if (const char* a = getenv("SG_SPECTRAL_ROWS")) ctx->rowsOnly = atoi(a) != 0;
   *out = ctx;
   return SG_OK;
 }

@@ -140,6 +140,30 @@ def test_runs_are_deterministic_and_batch_independent(ctx, storm):
         run.retire()
 
 
+def test_row_transform_path_matches_fp64_oracle(storm, monkeypatch):
+    """The row-transform path of the spectral solves (x-transforms of row blocks, y-transforms inside the mode
+    kernel; what grids too wide for the whole-layer path take, e.g. 320x256) forced on the standard grid: one step
+    from the developed storm against the FP64 oracle, every field within 1e-5."""
+    from meteolab_gb300.runtime import Context
+    monkeypatch.setenv("SG_SPECTRAL_ROWS", "1")
+    c = Context(0)
+    r = c.create(storm)
+    r.step(1)
+    got = r.read()
+    got_thp = r.debug_read_set(0, "theta")
+    m = O.OracleModel(storm, fp64=True, threads=threads())
+    m.step(storm.switches.dt, 1)
+    ref = {k: m.get(k) for k in CARRIED}
+    errs = {k: rel_l2(got[k], ref[k], FLOOR.get(k, 0.0)) for k in CARRIED}
+    thb = np.repeat(storm.env.theta, storm.grid.layer)
+    errs["theta'"] = rel_l2(got_thp, ref["theta"] - thb, FLOOR["theta'"])
+    print("row path:", ", ".join(f"{k} {v:.2e}" for k, v in errs.items()))
+    bad = {k: v for k, v in errs.items() if not v <= 1e-5}
+    r.retire()
+    c.close()
+    assert not bad, bad
+
+
 @pytest.mark.parametrize("shape", [(40, 8, 3), (40, 8, 1), (32, 8, 3), (16, 16, 1), (8, 8, 3), (40, 4, 1)])
 def test_transport_tiles_give_the_same_bits(ctx, storm, shape):
     """Every transport tile shape and WENO grouping (faces computed alone or as packed pairs) gives bitwise equal
