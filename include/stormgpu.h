@@ -139,6 +139,21 @@ int sg_set_transport_shape(sg_context* ctx, int tile_x, int tile_y, int weno_gro
 /* shape4 = (tile_x, tile_y, weno_group, blocks per SM the WENO kernel's register budget is cut for: 2 or 3). */
 int sg_batch_transport_shape(sg_context* ctx, const sg_run* runs, int n, int* shape4);
 
+/* ---- divergence check without allocation. No counterpart in the reference (its check, PressureSolver.divergence,
+ * src/core/pressure.ts:50-66, runs on its own CPU arrays).
+ * Max |D rho0 u| over the dual cells of velocities the caller holds in device memory (u, v, w: nx*ny*nz FP32 nodes,
+ * x fastest; rho: nz and dzs: nz-1 host FP64 values), the same FP64 arithmetic as sg_run_divergence, on `stream` (NULL: the
+ * default stream), synchronised before it returns. It allocates nothing: its scratch is a static device array of 256
+ * bytes, so callers that must not allocate at that point (HBM fully committed, or device memory owned by another
+ * allocator) can still check a projection. nz is at most SG_STATIC_MAX_NZ; a larger grid, or a bad argument, returns
+ * SG_ERR_INVALID with the reason in err (err_len bytes, nullable). The first call on a device looks up the scratch
+ * and the SM count (no allocation); make it before any stream capture. Calls that overlap on one device race on the
+ * scratch: serialise them. */
+#define SG_STATIC_MAX_NZ 128
+int sg_divergence_max_static(int device, const float* u, const float* v, const float* w, int nx, int ny, int nz,
+                             double dx, double dy, const double* rho, const double* dzs, void* stream,
+                             double* max_abs_div, char* err, size_t err_len);
+
 /* ---- diagnostics: one part of the step (1 beginStep, 2 dynamics, 3 physicsStep, 4 mixStep, 5 final projection),
  * and the raw device buffers (set 0 = state, 1 and 2 = stage scratch; theta of a set is its departure from the base
  * profile; faces4 = (mx, my, mz, div) per node, interleaved). For stage-wise parity tests against the oracle. */

@@ -1,6 +1,6 @@
 """Builds libstormgpu.so (the device step and its C ABI) in-tree with nvcc for sm_103a only.
 
-The two translation units compile in parallel; the result lands next to this file as ``libstormgpu.so``.
+The translation units compile in parallel; the result lands next to this file as ``libstormgpu.so``.
 """
 from __future__ import annotations
 
@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libstormgpu.so")
 OBJDIR = os.path.join(HERE, "_build")
-SOURCES = ["sg_kernels.cu", "sg_runtime.cu"]
+SOURCES = ["sg_kernels.cu", "sg_runtime.cu", "sg_static.cu"]
 HEADERS = ["sg_common.cuh", "sg_fft.cuh", "sg_physics.cuh", "sg_kernels.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr", "-Xptxas", "-v"]

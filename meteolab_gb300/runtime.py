@@ -92,6 +92,8 @@ def load():
             L.sg_batch_write_fields.argtypes = [vp, C.POINTER(C.c_int32), i32, C.c_uint32, C.POINTER(_FP)]
             L.sg_batch_read_fields.argtypes = [vp, C.POINTER(C.c_int32), i32, C.c_uint32, C.POINTER(_FP)]
             L.sg_set_transport_shape.argtypes = [vp, i32, i32, i32]
+            L.sg_divergence_max_static.argtypes = [i32, vp, vp, vp, i32, i32, i32, C.c_double, C.c_double, C.POINTER(C.c_double),
+                                                   C.POINTER(C.c_double), vp, C.POINTER(C.c_double), C.c_char_p, C.c_size_t]
             L.sg_batch_transport_shape.argtypes = [vp, C.POINTER(C.c_int32), i32, C.POINTER(C.c_int)]
             L.sg_server_create.argtypes = [vp, i32, C.POINTER(vp)]
             L.sg_server_destroy.argtypes = [vp]
@@ -388,3 +390,18 @@ class Server:
         if getattr(self, "h", None):
             load().sg_server_destroy(self.h)
             self.h = None
+
+
+def divergence_max_static(device: int, u_ptr: int, v_ptr: int, w_ptr: int, grid, rho, stream: int = 0) -> float:
+    """Max |D rho0 u| of velocity fields already in device memory (raw device pointers, nx*ny*nz FP32 each), without
+    any allocation by the library (sg_divergence_max_static)."""
+    rho = _f64(rho)
+    dzs = _f64(grid.dzs)
+    out = C.c_double()
+    err = C.create_string_buffer(160)
+    rc = load().sg_divergence_max_static(device, u_ptr, v_ptr, w_ptr, grid.nx, grid.ny, grid.nz, grid.dx, grid.dy,
+                                         rho.ctypes.data_as(C.POINTER(C.c_double)), dzs.ctypes.data_as(C.POINTER(C.c_double)),
+                                         stream or None, C.byref(out), err, len(err))
+    if rc:
+        raise StormGpuError(rc, err.value.decode())
+    return out.value
