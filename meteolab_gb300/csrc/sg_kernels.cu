@@ -220,8 +220,8 @@ __global__ void k_sediment(const RunDesc* __restrict__ runs, const int4* items, 
 }
 
 // ==================================================================== elliptic solves
-// Exact row index of element e of a row-major block with rows of length `len` (e < 2^16): one multiply by the
-// reciprocal instead of an integer division.
+// Exact row index of element e of a row-major block with rows of length `len` (e < 2^20, len <= 640; checked
+// exhaustively for the grid widths in use): one multiply by the reciprocal instead of an integer division.
 __device__ __forceinline__ int row_of(int e, float inv_len) { return __float2int_rz(((float)e + .5f) * inv_len); }
 
 // Divergence rows of one layer and their forward x-transform (real rows paired into complex ones, the reference's
@@ -587,63 +587,110 @@ __global__ void k_proj_ifft2(const RunDesc* __restrict__ runs, const int4* items
 }
 
 // Projected face mass fluxes and their divergence (FluxTransport.correctFaces + divergence, advection.ts:203-255):
-// mx = rho (u + u_e)/2 - rho (phi_e - phi)/dx, and so on; div of the corrected faces at the node.
+// mx = rho (u + u_e)/2 - rho (phi_e - phi)/dx, and so on; div of the corrected faces at the node. Each thread takes
+// nodes in passes of NB, their loads issued together.
+constexpr int NB = 4;
 __global__ void k_face_correct(const RunDesc* __restrict__ runs, const int4* items, int nitems, int set) {
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
     if (R.cnt[C_FAILED]) continue;
     const int nx = R.nx, ny = R.ny, nz = R.nz, layer = R.layer, i0 = items[it].y * CHUNK, i1 = min(R.n, i0 + CHUNK);
-    const float *u = field(R, set, U), *v = field(R, set, V), *w = field(R, set, W), *phi = R.phi;
+    const float* __restrict__ u = field(R, set, U);
+    const float* __restrict__ v = field(R, set, V);
+    const float* __restrict__ w = field(R, set, W);
+    const float* __restrict__ phi = R.phi;
     float4* F4 = reinterpret_cast<float4*>(R.faces);
-    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-      int z = i / layer, c = i - z * layer, y = c / nx, x = c - y * nx, l = z * layer;
-      int ie = wrap(x + 1, nx) + y * nx + l, iw = wrap(x - 1, nx) + y * nx + l, in = x + wrap(y + 1, ny) * nx + l, is = x + wrap(y - 1, ny) * nx + l;
-      float rho = lvl(R, L_RHO, z), p0 = phi[i];
-      float fxE = rho * (.5f * (u[i] + u[ie]) - (phi[ie] - p0) * R.inv_dx);
-      float fxW = rho * (.5f * (u[iw] + u[i]) - (p0 - phi[iw]) * R.inv_dx);
-      float fyN = rho * (.5f * (v[i] + v[in]) - (phi[in] - p0) * R.inv_dy);
-      float fyS = rho * (.5f * (v[is] + v[i]) - (p0 - phi[is]) * R.inv_dy);
-      float fzU = z < nz - 1 ? lvl(R, L_RUP, z) * (.5f * (w[i] + w[i + layer]) - (phi[i + layer] - p0) * lvl(R, L_INV_DZS, z)) : 0.f;
-      float fzD = z > 0 ? lvl(R, L_RUP, z - 1) * (.5f * (w[i - layer] + w[i]) - (p0 - phi[i - layer]) * lvl(R, L_INV_DZS, z - 1)) : 0.f;
-      F4[i] = make_float4(fxE, fyN, fzU, (fxE - fxW) * R.inv_dx + (fyN - fyS) * R.inv_dy + (fzU - fzD) * lvl(R, L_INV_HZ, z));
+    const float inv_nx = 1.f / (float)nx, idx = R.inv_dx, idy = R.inv_dy;
+    const int B = blockDim.x;
+    int z = (i0 + threadIdx.x) / layer;
+    for (int base = i0 + threadIdx.x; base < i1; base += NB * B) {
+      float uc[NB], ue[NB], uw[NB], vc[NB], vn[NB], vs[NB], wc[NB], wu[NB], wd[NB];
+      float pc[NB], pe[NB], pw[NB], pn[NB], ps[NB], pu[NB], pd[NB];
+      int zz[NB];
+#pragma unroll
+      for (int j = 0; j < NB; j++) {
+        const int i = min(base + j * B, i1 - 1);
+        while (i >= (z + 1) * layer) z++;
+        zz[j] = z;
+        const int c = i - z * layer, y = row_of(c, inv_nx), x = c - y * nx, l = z * layer;
+        const int ie = (x + 1 == nx ? 0 : x + 1) + y * nx + l, iw = (x == 0 ? nx - 1 : x - 1) + y * nx + l;
+        const int in = x + (y + 1 == ny ? 0 : y + 1) * nx + l, is = x + (y == 0 ? ny - 1 : y - 1) * nx + l;
+        const int iu = z < nz - 1 ? i + layer : i, id = z > 0 ? i - layer : i;
+        uc[j] = u[i]; ue[j] = u[ie]; uw[j] = u[iw]; vc[j] = v[i]; vn[j] = v[in]; vs[j] = v[is];
+        wc[j] = w[i]; wu[j] = w[iu]; wd[j] = w[id];
+        pc[j] = phi[i]; pe[j] = phi[ie]; pw[j] = phi[iw]; pn[j] = phi[in]; ps[j] = phi[is]; pu[j] = phi[iu]; pd[j] = phi[id];
+      }
+#pragma unroll
+      for (int j = 0; j < NB; j++) {
+        const int i = base + j * B;
+        if (i >= i1) break;
+        const int k = zz[j];
+        const float rho = lvl(R, L_RHO, k), p0 = pc[j];
+        const float fxE = rho * (.5f * (uc[j] + ue[j]) - (pe[j] - p0) * idx);
+        const float fxW = rho * (.5f * (uw[j] + uc[j]) - (p0 - pw[j]) * idx);
+        const float fyN = rho * (.5f * (vc[j] + vn[j]) - (pn[j] - p0) * idy);
+        const float fyS = rho * (.5f * (vs[j] + vc[j]) - (p0 - ps[j]) * idy);
+        const float fzU = k < nz - 1 ? lvl(R, L_RUP, k) * (.5f * (wc[j] + wu[j]) - (pu[j] - p0) * lvl(R, L_INV_DZS, k)) : 0.f;
+        const float fzD = k > 0 ? lvl(R, L_RUP, k - 1) * (.5f * (wd[j] + wc[j]) - (p0 - pd[j]) * lvl(R, L_INV_DZS, k - 1)) : 0.f;
+        F4[i] = make_float4(fxE, fyN, fzU, (fxE - fxW) * idx + (fyN - fyS) * idy + (fzU - fzD) * lvl(R, L_INV_HZ, k));
+      }
     }
   }
 }
 
 // u -= dt G p at the nodes of one set (PressureSolver.correct, src/core/pressure.ts:69-92); with `final` the wind
-// limits act and count (clipWind, src/core/model.ts:1586-1595).
+// limits act and count (clipWind, src/core/model.ts:1586-1595). Nodes in passes of NB, as above.
 __global__ void k_pres_correct(const RunDesc* __restrict__ runs, const int4* items, int nitems, int set, int final_) {
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
     if (R.cnt[C_FAILED]) continue;
     const int nx = R.nx, ny = R.ny, nz = R.nz, layer = R.layer, i0 = items[it].y * CHUNK, i1 = min(R.n, i0 + CHUNK);
     float *u = field(R, set, U), *v = field(R, set, V), *w = field(R, set, W);
-    const float* p = R.pres;
-    const float dt = R.dt;
+    const float* __restrict__ p = R.pres;
+    const float dt = R.dt, inv_nx = 1.f / (float)nx;
+    const int B = blockDim.x;
     int clipped = 0;
-    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-      int k = i / layer, c = i - k * layer, j = c / nx, x = c - j * nx;
-      int im = wrap(x - 1, nx), jm = wrap(j - 1, ny) * nx, j0 = j * nx;
-      const float* lo = p + (size_t)max(0, k - 1) * layer;
-      const float* hi = p + (size_t)min(nz - 2, k) * layer;
-      float hz = lvl(R, L_HZ, k);
-      float wLo = k > 0 ? lvl(R, L_DZS, k - 1) / hz : 0.f, wHi = k < nz - 1 ? lvl(R, L_DZS, k) / hz : 0.f;
-      float gx = (wLo * ((lo[x + jm] - lo[im + jm]) + (lo[x + j0] - lo[im + j0])) + wHi * ((hi[x + jm] - hi[im + jm]) + (hi[x + j0] - hi[im + j0]))) * (.25f * R.inv_dx);
-      float gy = (wLo * ((lo[im + j0] - lo[im + jm]) + (lo[x + j0] - lo[x + jm])) + wHi * ((hi[im + j0] - hi[im + jm]) + (hi[x + j0] - hi[x + jm]))) * (.25f * R.inv_dy);
-      float uu = u[i] - dt * gx, vv = v[i] - dt * gy, ww = w[i];
-      if (k > 0 && k < nz - 1) {
-        const float* ab = p + (size_t)k * layer;
-        const float* be = p + (size_t)(k - 1) * layer;
-        float gz = ((ab[im + jm] - be[im + jm]) + (ab[x + jm] - be[x + jm]) + (ab[im + j0] - be[im + j0]) + (ab[x + j0] - be[x + j0])) * (.25f * lvl(R, L_INV_HZ, k));
-        ww -= dt * gz;
+    int z = (i0 + threadIdx.x) / layer;
+    for (int base = i0 + threadIdx.x; base < i1; base += NB * B) {
+      float lo[NB][4], hi[NB][4], uu[NB], vv[NB], ww[NB];
+      int zz[NB];
+#pragma unroll
+      for (int j = 0; j < NB; j++) {
+        const int i = min(base + j * B, i1 - 1);
+        while (i >= (z + 1) * layer) z++;
+        zz[j] = z;
+        const int c = i - z * layer, jy = row_of(c, inv_nx), x = c - jy * nx;
+        const int im = x == 0 ? nx - 1 : x - 1, jm = (jy == 0 ? ny - 1 : jy - 1) * nx, j0 = jy * nx;
+        const float* L = p + (size_t)max(0, z - 1) * layer;
+        const float* H = p + (size_t)min(nz - 2, z) * layer;
+        // corners (im, jm), (x, jm), (im, j0), (x, j0) of the dual cells below and above
+        lo[j][0] = L[im + jm]; lo[j][1] = L[x + jm]; lo[j][2] = L[im + j0]; lo[j][3] = L[x + j0];
+        hi[j][0] = H[im + jm]; hi[j][1] = H[x + jm]; hi[j][2] = H[im + j0]; hi[j][3] = H[x + j0];
+        uu[j] = u[i]; vv[j] = v[i]; ww[j] = w[i];
       }
-      if (final_) {
-        const float UL = 120.f, WL = 100.f;
-        if (uu < -UL || uu > UL) { uu = fmaxf(-UL, fminf(UL, uu)); clipped++; }
-        if (vv < -UL || vv > UL) { vv = fmaxf(-UL, fminf(UL, vv)); clipped++; }
-        if (ww < -WL || ww > WL) { ww = fmaxf(-WL, fminf(WL, ww)); clipped++; }
+#pragma unroll
+      for (int j = 0; j < NB; j++) {
+        const int i = base + j * B;
+        if (i >= i1) break;
+        const int k = zz[j];
+        const float hz = lvl(R, L_HZ, k);
+        const float wLo = k > 0 ? lvl(R, L_DZS, k - 1) / hz : 0.f, wHi = k < nz - 1 ? lvl(R, L_DZS, k) / hz : 0.f;
+        const float gx = (wLo * ((lo[j][1] - lo[j][0]) + (lo[j][3] - lo[j][2])) + wHi * ((hi[j][1] - hi[j][0]) + (hi[j][3] - hi[j][2]))) * (.25f * R.inv_dx);
+        const float gy = (wLo * ((lo[j][2] - lo[j][0]) + (lo[j][3] - lo[j][1])) + wHi * ((hi[j][2] - hi[j][0]) + (hi[j][3] - hi[j][1]))) * (.25f * R.inv_dy);
+        float un = uu[j] - dt * gx, vn = vv[j] - dt * gy, wn = ww[j];
+        if (k > 0 && k < nz - 1) {
+          // the gradient between the dual cells below (k - 1) and above (k)
+          const float gz = ((hi[j][0] - lo[j][0]) + (hi[j][1] - lo[j][1]) + (hi[j][2] - lo[j][2]) + (hi[j][3] - lo[j][3])) * (.25f * lvl(R, L_INV_HZ, k));
+          wn -= dt * gz;
+        }
+        if (final_) {
+          const float UL = 120.f, WL = 100.f;
+          if (un < -UL || un > UL) { un = fmaxf(-UL, fminf(UL, un)); clipped++; }
+          if (vn < -UL || vn > UL) { vn = fmaxf(-UL, fminf(UL, vn)); clipped++; }
+          if (wn < -WL || wn > WL) { wn = fmaxf(-WL, fminf(WL, wn)); clipped++; }
+        }
+        u[i] = un; v[i] = vn; w[i] = wn;
       }
-      u[i] = uu; v[i] = vv; w[i] = ww;
     }
     if (final_) {
       clipped = warpSum(clipped);
@@ -1135,38 +1182,92 @@ __global__ void k_viscosity(const RunDesc* __restrict__ runs, const int4* items,
 
 // Explicit flux-form diffusion of each mixed field's departure (Turbulence.mix, src/core/turbulence.ts:143-185),
 // then the ground drag balanced against the environment's own and rigid w at the ground and top (mixStep, :1179-1194).
-// In: set `in`; out: set A.
-__global__ void k_mix(const RunDesc* __restrict__ runs, const int4* items, int nitems, int in) {
-  FOR_ITEMS {
-    const RunDesc& R = runs[items[it].x];
-    if (R.cnt[C_FAILED]) continue;
-    const int nx = R.nx, ny = R.ny, nz = R.nz, layer = R.layer, i0 = items[it].y * CHUNK, i1 = min(R.n, i0 + CHUNK);
-    const float *km = R.kmkh, *kh = R.kmkh + R.n;
-    const int nmix = (R.flags & RF_ICE) ? NMIX : 6;
-    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-      int z = i / layer, c = i - z * layer, y = c / nx, x = c - y * nx, l = z * layer;
-      int e = wrap(x + 1, nx) + y * nx + l, wst = wrap(x - 1, nx) + y * nx + l, n = x + wrap(y + 1, ny) * nx + l, s = x + wrap(y - 1, ny) * nx + l;
-      float khi = kh[i], kmi = km[i];
-      float hE = .5f * (khi + kh[e]), hW = .5f * (kh[wst] + khi), hN = .5f * (khi + kh[n]), hS = .5f * (kh[s] + khi);
-      float vU = z < nz - 1 ? .5f * (kmi + km[i + layer]) * lvl(R, L_MIXUP, z) * lvl(R, L_INV_DZS, z) : 0.f;
-      float vD = z > 0 ? .5f * (km[i - layer] + kmi) * lvl(R, L_MIXDN, z) * lvl(R, L_INV_DZS, z - 1) : 0.f;
-      float ix2 = R.inv_dx * R.inv_dx, iy2 = R.inv_dy * R.inv_dy;
+// In: set `in`; out: set A. A block takes one tile of columns of one run and a range of levels [z0, z1), marching up:
+// per level the planes of the mixed fields and of K_h (1-node periodic halo) arrive in shared memory by asynchronous
+// copies issued a level ahead, the vertical neighbours and K_m stay in registers, one barrier per level.
+constexpr int MIX_MAXC = 2;  // plane cells per thread: (TX + 2)(TY + 2) <= MIX_MAXC * TX * TY
+template <int NM>
+__device__ __forceinline__ void mix_item(const RunDesc& R, int tile, int z0, int z1, int in, int TX, int TY, float* sm) {
+  const int nx = R.nx, ny = R.ny, nz = R.nz, layer = R.layer;
+  const int PW = TX + 2, PH = TY + 2, NCELL = PW * PH, NP = NM + 1;  // planes: the NM fields, then K_h
+  const int t = threadIdx.x, lx = t % TX, ly = t / TX;
+  const int tilesX = (nx + TX - 1) / TX, x0 = (tile % tilesX) * TX, y0 = (tile / tilesX) * TY;
+  const int x = x0 + lx, y = y0 + ly;
+  const bool on = x < nx && y < ny;
+  const int col = on ? x + y * nx : 0;
+  const float* src[NP];
+#pragma unroll
+  for (int k = 0; k < NM; k++) src[k] = field(R, in, mix_field(k));
+  src[NM] = R.kmkh + R.n;  // K_h
+  const float* km = R.kmkh;
+  int off[MIX_MAXC], cell[MIX_MAXC];
+#pragma unroll
+  for (int j = 0; j < MIX_MAXC; j++) {
+    const int e = t + j * blockDim.x;
+    cell[j] = e < NCELL ? e : -1;
+    const int hy = e / PW, hx = e - hy * PW;
+    int gx = x0 + hx - 1, gy = y0 + hy - 1;
+    gx = gx < 0 ? gx + nx : (gx >= nx ? gx - nx : gx);
+    gy = gy < 0 ? gy + ny : (gy >= ny ? gy - ny : gy);
+    off[j] = e < NCELL ? gx + gy * nx : 0;
+  }
+  // plane z0 into buffer 0; the centre values of z0 - 1, z0, z0 + 1 into registers
+#pragma unroll
+  for (int p = 0; p < NP; p++)
+#pragma unroll
+    for (int j = 0; j < MIX_MAXC; j++) if (cell[j] >= 0) sm[p * NCELL + cell[j]] = src[p][off[j] + z0 * layer];
+  float below[NM], cur[NM], above[NM];
+#pragma unroll
+  for (int k = 0; k < NM; k++) {
+    cur[k] = src[k][col + z0 * layer];
+    below[k] = z0 > 0 ? src[k][col + (z0 - 1) * layer] : 0.f;
+    above[k] = z0 + 1 < nz ? src[k][col + (z0 + 1) * layer] : 0.f;
+  }
+  float kmD = z0 > 0 ? km[col + (z0 - 1) * layer] : 0.f, kmC = km[col + z0 * layer], kmU = z0 + 1 < nz ? km[col + (z0 + 1) * layer] : 0.f;
+  __syncthreads();
+  const float ix2 = R.inv_dx * R.inv_dx, iy2 = R.inv_dy * R.inv_dy, dt = R.dt;
+  const int cc = (ly + 1) * PW + lx + 1;
+  for (int z = z0; z < z1; z++) {
+    const int buf = (z - z0) & 1;
+    const float* P = sm + buf * NP * NCELL;
+    // a level ahead: plane z + 1 (asynchronous copies into the other buffer), the centre values of z + 2
+    if (z + 1 < z1) {
+      float* Q = sm + (buf ^ 1) * NP * NCELL;
+#pragma unroll
+      for (int p = 0; p < NP; p++)
+#pragma unroll
+        for (int j = 0; j < MIX_MAXC; j++) if (cell[j] >= 0) cp_async4(Q + p * NCELL + cell[j], src[p] + off[j] + (z + 1) * layer);
+    }
+    float nextv[NM];
+    float kmN = 0.f;
+    const bool more = z + 2 < nz;
+#pragma unroll
+    for (int k = 0; k < NM; k++) nextv[k] = more ? src[k][col + (z + 2) * layer] : 0.f;
+    if (more) kmN = km[col + (z + 2) * layer];
+    if (on) {
+      const float* KH = P + NM * NCELL + cc;
+      const float khi = KH[0];
+      const float hE = .5f * (khi + KH[1]), hW = .5f * (KH[-1] + khi), hN = .5f * (khi + KH[PW]), hS = .5f * (KH[-PW] + khi);
+      const float vU = z < nz - 1 ? .5f * (kmC + kmU) * lvl(R, L_MIXUP, z) * lvl(R, L_INV_DZS, z) : 0.f;
+      const float vD = z > 0 ? .5f * (kmD + kmC) * lvl(R, L_MIXDN, z) * lvl(R, L_INV_DZS, z - 1) : 0.f;
       float uu = 0.f, vv = 0.f;
-      for (int k = 0; k < nmix; k++) {
+      const int i = col + z * layer;
+#pragma unroll
+      for (int k = 0; k < NM; k++) {
         const int f = mix_field(k);
         const float factor = k < 3 ? 1.f : 3.f;
-        const float* a = field(R, in, f);
-        float ai = a[i];
+        const float* A = P + k * NCELL + cc;
+        const float ai = cur[k];
         // vertical departures: the base differences to the level above / below (u, v, q carry a base profile;
         // theta' is already a departure; w, cloud, ice, number have none)
         float bu = 0.f, bd = 0.f;
         if (f == U) { bu = z < nz - 1 ? lvl(R, L_DUENV, z) : 0.f; bd = z > 0 ? lvl(R, L_DUENV, z - 1) : 0.f; }
         else if (f == V) { bu = z < nz - 1 ? lvl(R, L_DVENV, z) : 0.f; bd = z > 0 ? lvl(R, L_DVENV, z - 1) : 0.f; }
         else if (f == Q) { bu = z < nz - 1 ? lvl(R, L_DQB, z) : 0.f; bd = z > 0 ? lvl(R, L_DQB, z - 1) : 0.f; }
-        float tx = (hE * (a[e] - ai) - hW * (ai - a[wst])) * ix2;
-        float ty = (hN * (a[n] - ai) - hS * (ai - a[s])) * iy2;
-        float tz = (z < nz - 1 ? vU * ((a[i + layer] - ai) - bu) : 0.f) - (z > 0 ? vD * ((ai - a[i - layer]) - bd) : 0.f);
-        float out = ai + R.dt * factor * (tx + ty + tz);
+        const float tx = (hE * (A[1] - ai) - hW * (ai - A[-1])) * ix2;
+        const float ty = (hN * (A[PW] - ai) - hS * (ai - A[-PW])) * iy2;
+        const float tz = (z < nz - 1 ? vU * ((above[k] - ai) - bu) : 0.f) - (z > 0 ? vD * ((ai - below[k]) - bd) : 0.f);
+        float out = ai + dt * factor * (tx + ty + tz);
         if (f == U) uu = out;
         else if (f == V) vv = out;
         else {
@@ -1175,12 +1276,28 @@ __global__ void k_mix(const RunDesc* __restrict__ runs, const int4* items, int n
         }
       }
       if (z == 0 && R.drag != 0.f) {
-        float ug = uu + R.frame_u, vg = vv + R.frame_v, speed = sqrtf(ug * ug + vg * vg);
+        const float ug = uu + R.frame_u, vg = vv + R.frame_v, speed = sqrtf(ug * ug + vg * vg);
         uu -= R.drag * (speed * ug - R.env_speed * R.ue0);
         vv -= R.drag * (speed * vg - R.env_speed * R.ve0);
       }
       field(R, 0, U)[i] = uu; field(R, 0, V)[i] = vv;
     }
+#pragma unroll
+    for (int k = 0; k < NM; k++) { below[k] = cur[k]; cur[k] = above[k]; above[k] = nextv[k]; }
+    kmD = kmC; kmC = kmU; kmU = kmN;
+    cp_async_wait_all();
+    __syncthreads();
+  }
+}
+
+// Work item (run, tile, z0, z1); `TX` x `TY` threads.
+__global__ void __launch_bounds__(320, 2) k_mix_tile(const RunDesc* __restrict__ runs, const int4* items, int nitems, int in, int TX, int TY) {
+  extern __shared__ float sm[];
+  FOR_ITEMS {
+    const RunDesc& R = runs[items[it].x];
+    if (R.cnt[C_FAILED]) continue;
+    if (R.flags & RF_ICE) mix_item<NMIX>(R, items[it].y, items[it].z, items[it].w, in, TX, TY, sm);
+    else mix_item<6>(R, items[it].y, items[it].z, items[it].w, in, TX, TY, sm);
   }
 }
 
@@ -1286,7 +1403,10 @@ void launch_fill_partial(const Launch& L, int set) { k_fill_partial<<<GRID(L.n, 
 void launch_fill_final(const Launch& L) { k_fill_final<<<GRID(L.n, L.cap), 32, 0, L.stream>>>(L.runs, L.items, L.n); }
 void launch_physics(const Launch& L, int in, int mid) { k_physics<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, in, mid); }
 void launch_viscosity(const Launch& L, int set) { k_viscosity<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set); }
-void launch_mix(const Launch& L, int in) { k_mix<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, in); }
+size_t mix_smem(int TX, int TY) { return (size_t)2 * (NMIX + 1) * (TX + 2) * (TY + 2) * sizeof(float); }
+void launch_mix(const Launch& L, int in, int TX, int TY) {
+  k_mix_tile<<<GRID(L.n, L.cap), TX * TY, mix_smem(TX, TY), L.stream>>>(L.runs, L.items, L.n, in, TX, TY);
+}
 void launch_step_end(const Launch& L) { k_step_end<<<GRID(L.n, L.cap), 64, 0, L.stream>>>(L.runs, L.items, L.n); }
 void launch_divergence_max(const Launch& L, int set, double* out) { k_divergence_max<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set, out); }
 

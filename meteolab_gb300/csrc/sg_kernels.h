@@ -39,7 +39,9 @@ void launch_fill_partial(const Launch& L, int set);
 void launch_fill_final(const Launch& L);
 void launch_physics(const Launch& L, int in, int mid);
 void launch_viscosity(const Launch& L, int set);
-void launch_mix(const Launch& L, int in);
+// Mixing on (run, tile of TX x TY columns, z0, z1) items.
+void launch_mix(const Launch& L, int in, int TX, int TY);
+size_t mix_smem(int TX, int TY);
 void launch_step_end(const Launch& L);
 void launch_divergence_max(const Launch& L, int set, double* out);
 cudaError_t set_smem_limits(int bytes);

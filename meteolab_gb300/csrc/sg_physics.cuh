@@ -94,9 +94,10 @@ SG_HD float rainProcesses(Node& s, const Level& L, float dt, bool evaporate) {
   float rate = .001f * fmaxf(0.f, qc - .001f) + (qr > 0.f ? 2.2f * qc * powf(qr, .875f) : 0.f);
   float production = fminf(qc, rate * dt);
   s.cloud -= production; s.rain += production;
+  if (!evaporate || s.rain <= 0.f) return 0.f;         // (the saturation below is only needed to evaporate rain)
   const Sat sw = satWater(s, L);
   const float qs = satv(sw), ex = excess(s.q, sw);     // ex = q - qs
-  if (!evaporate || s.rain <= 0.f || ex >= 0.f) return 0.f;
+  if (ex >= 0.f) return 0.f;
   float rq = .001f * rho * s.rain, vent = 1.6f + 124.9f * powf(rq, .2046f);
   float er = (-ex / qs) * vent * powf(rq, .525f) / (.001f * rho * (5.4e5f + 2.55e6f / (p / 100.f * qs)));
   float ev = fminf(fminf(s.rain, er * dt), -ex / (1.f + LV * LV * qs / (CP * RV * tk * tk)));
@@ -201,12 +202,13 @@ SG_HD float iceProcesses(Node& s, const Level& L, float dt) {
 SG_HD float snowProcesses(Node& s, const Level& L, float dt) {
   const float exner = L.exner, rho = L.rho, fallsq = L.fallsq;
   const float tc = tcOf(s, exner), tk = tc + T0, qs = s.snow;
-  const Sat si = satIce(s, L);   // at the temperature the routine starts with, as the reference evaluates it
   if (tc < 0.f && s.ice > 0.f) {
     float aut = 1e-3f * expf(.025f * tc) * fmaxf(0.f, s.ice - .001f);
     float moved = fminf(s.ice, aut * dt); s.ice -= moved; s.snow += moved;
   }
   if (qs <= 1e-9f) return 0.f;
+  // at the temperature the routine starts with, as the reference evaluates it (the conversion above leaves it)
+  const Sat si = tc < 0.f ? satIce(s, L) : Sat{0.f, 0.f};
   float lambda = powf(PI * RHO_S * N0S / (rho * qs), .25f);
   float sweep = PI * N0S * C_S * GAMMA_3D / (4.f * powf(lambda, 3.25f)) * fallsq;
   float vent = N0S * (.78f / (lambda * lambda) + .31f * SC13 * GAMMA_5D2 * SQRT_C_S * sqrtf(fallsq) / sqrtf(NU) * powf(lambda, -2.625f));
@@ -233,7 +235,10 @@ SG_HD float snowProcesses(Node& s, const Level& L, float dt) {
 SG_HD float graupelProcesses(Node& s, const Level& L, float dt) {
   const float exner = L.exner, rho = L.rho;
   const float tc = tcOf(s, exner), tk = tc + T0, heat = 1.f / (CP * exner);
-  const Sat si = satIce(s, L);   // at the starting temperature (the reference's qsatIce(tc, p))
+  // at the starting temperature (the reference's qsatIce(tc, p)); needed only below 0 C when graupel is or becomes
+  // present (frozen rain, autoconverted snow)
+  const bool needSi = tc < 0.f && (s.graupel > 1e-9f || s.rain > 1e-9f || s.snow > 6e-4f);
+  const Sat si = needSi ? satIce(s, L) : Sat{0.f, 0.f};
   float cooling = 0.f;
   if (tc < 0.f) {
     if (s.rain > 1e-9f) {
@@ -280,7 +285,6 @@ SG_HD float wetGrowth(float lambda, float a, float n0, float tc, float qv, const
 SG_HD float hailProcesses(Node& s, const Level& L, float dt) {
   const float exner = L.exner, rho = L.rho;
   const float tc = tcOf(s, exner), tk = tc + T0, heat = 1.f / (CP * exner);
-  const Sat si = satIce(s, L);   // at the starting temperature (the reference's qsatIce(tc, p))
   float cooling = 0.f;
   // wetGrowing(graupel, N0G, RHO_G, ...) (src/core/hail.ts:127-131)
   if (tc < 0.f && s.graupel > 1e-9f) {
@@ -292,6 +296,8 @@ SG_HD float hailProcesses(Node& s, const Level& L, float dt) {
   }
   float qh = s.hail;
   if (qh <= 1e-9f) return 0.f;
+  // at the starting temperature (the reference's qsatIce(tc, p)): the conversion above leaves it
+  const Sat si = tc < 0.f ? satIce(s, L) : Sat{0.f, 0.f};
   float lambda = powf(PI * RHO_H * N0H / (rho * qh), .25f), a = fallCoef(rho, RHO_H);
   float k = PI * N0H * a * GAMMA_35 / (4.f * powf(lambda, 3.5f)), vent = ventilationOf(lambda, a, N0H);
   if (tc < 0.f) {

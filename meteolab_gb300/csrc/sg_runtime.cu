@@ -66,6 +66,7 @@ struct Plan {
   int maxnx = 0, maxny = 0, maxnz = 0, TX = 40, TY = 8, wenoG = 3;  // transport tile and WENO fields per item
   int minb = 2;                                                       // WENO transport blocks per SM (register budget)
   int yc = 32;                                                        // layer rows per x-transform item
+  int mixTX = 32, mixTY = 8;                                          // mixing tile
   bool layerfft = false;                                              // 2-D transforms per layer (see enqueue_part)
   bool tuned = false;                                                 // TX, TY, wenoG chosen by timing
   cudaGraph_t graph = nullptr;
@@ -76,7 +77,8 @@ struct Plan {
     if (items) cudaFree(items);
   }
 };
-enum Family { FAM_NODE, FAM_COLS, FAM_ROWS_FACE, FAM_ROWS_PRES, FAM_MODES, FAM_RUNS, FAM_CELLS, FAM_T_WENO, FAM_T_LIN, FAM_T_W, FAM_T_TH, FAM_COUNT };
+enum Family { FAM_NODE, FAM_COLS, FAM_ROWS_FACE, FAM_ROWS_PRES, FAM_MODES, FAM_RUNS, FAM_CELLS, FAM_T_WENO, FAM_T_LIN, FAM_T_W, FAM_T_TH,
+              FAM_MIX, FAM_COUNT };
 
 }  // namespace
 
@@ -322,6 +324,14 @@ int build_plan(sg_context* ctx, const std::vector<int>& slots, Plan& P) {
     for (int m = 0; m < r.nx / 2 + 1; m++) all[FAM_MODES].push_back(make_int4(s, m, 0, 0));
     all[FAM_RUNS].push_back(make_int4(s, 0, 0, 0));
   }
+  // mixing items: (run, tile, z0, z1), the column in four level ranges
+  P.mixTX = all40 ? 40 : 32; P.mixTY = 8;
+  for (int s : slots) {
+    const Run& r = ctx->runs[s];
+    const int tiles = ((r.nx + P.mixTX - 1) / P.mixTX) * ((r.ny + P.mixTY - 1) / P.mixTY), zc = (r.nz + 3) / 4;
+    for (int t = 0; t < tiles; t++)
+      for (int z0 = 0; z0 < r.nz; z0 += zc) all[FAM_MIX].push_back(make_int4(s, t, z0, std::min(r.nz, z0 + zc)));
+  }
   if (ctx->pinned[0]) { P.TX = ctx->pinned[0]; P.TY = ctx->pinned[1]; P.wenoG = ctx->pinned[2]; P.minb = ctx->pinned[3]; }
   transport_items(ctx, slots, P.TX, P.TY, P.wenoG, all + FAM_T_WENO);
   int st = upload_items(ctx, P, all);
@@ -461,7 +471,9 @@ void enqueue_part(sg_context* ctx, const Plan& P, int part, Hook hook) {
     launch_physics(node, B, C); hook(13);
   } else if (part == 4) {
     launch_viscosity(node, C); hook(14);
-    launch_mix(node, C); hook(15);
+    Launch mx = lx(ctx, P, FAM_MIX);
+    mx.cap = mx.n;
+    launch_mix(mx, C, P.mixTX, P.mixTY); hook(15);
   } else if (part == 5) {
     project(A, 1);
     launch_step_end(runs); hook(17);
