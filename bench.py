@@ -31,6 +31,20 @@ MEMBERS = 64
 # once (4 + 4 B), the step-start value read in stages 2 and 3 (4 B), the projected face fluxes (mx, my, mz, div: 16 B);
 # mean over the three stages = (9 * 8 + 16 + 2 * (9 * 12 + 16)) / 3.
 TRANSPORT_BYTES_PER_CELL = (9 * 8 + 16 + 2 * (9 * 12 + 16)) / 3
+# Algorithmic bytes per cell and launch of every kernel (FP32 fields 4 B; inputs read once, outputs written once):
+# the denominators of the per-kernel HBM roofline. Spectra and solver factors per cell of the 40-wide grid: a half
+# spectrum is (nx/2 + 1)/nx complex values per node (4.2 B), the sweep's FP64 factors 3 x 8 B per mode (12.6 B).
+KERNEL_BYTES_PER_CELL = {
+    "fall_courant": 16, "sediment": 32,                                   # 4 falling fields in (and out)
+    "face_div_xfft": 12 + 4.2, "pres_div_xfft": 12 + 4.2,                 # u, v, w in; half spectrum out
+    "face_modes": 8.4 + 12.6, "pres_modes": 8.4 + 12.6,                   # spectrum in and out, FP64 factors
+    "face_xifft": 4.2 + 4, "pres_xifft": 4.2 + 4,                         # spectrum in, potential / pressure out
+    "face_correct": 16 + 16,                                              # u, v, w, phi in; float4 faces out
+    "pres_correct": 16 + 12, "pres_correct_final": 16 + 12,               # p, u, v, w in; u, v, w out
+    "transport_weno": TRANSPORT_BYTES_PER_CELL,
+    "transport_dynamics": (80 + 96 + 96) / 3,                             # u, v, w, theta' r/w, faces, buoyancy inputs, start values
+    "fill_partial": 28, "physics": 104, "viscosity": 36, "mix": 72,
+}
 
 
 def parse():
@@ -375,6 +389,8 @@ def main():
         "uneven_batch": uneven,
         "serving": serving,
         "kernels_ms_per_launch": {k: round(v[0], 5) for k, v in prof.items()},
+        "kernels_hbm_gbs": {k: round(cells * KERNEL_BYTES_PER_CELL[k] / (v[0] * 1e-3) / 1e9, 1)
+                            for k, v in prof.items() if k in KERNEL_BYTES_PER_CELL and v[0] > 0},
     }
     print(json.dumps(line), flush=True)
 

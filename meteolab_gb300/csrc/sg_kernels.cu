@@ -711,15 +711,15 @@ __global__ void k_pres_correct(const RunDesc* __restrict__ runs, const int4* ite
 // threads 0..TY-1 and TY..TY+TX-1 reconstruct the tile's west and south edge faces, the x and y faces are exchanged
 // through shared memory (double-buffered), and one barrier separates the levels. The group shares the face-flux loads.
 constexpr int TMAXC = 4;  // plane cells per thread: (TX + 6)(TY + 6) <= TMAXC * TX * TY
-// Per-level constants staged in shared memory, rows of MAXNZ: 1/hz, 1/rho (all kinds), theta's four base-profile
-// face values (theta), thb, qb, thv_env (w).
-constexpr int tlv_rows(int kind) { return kind == 2 ? 9 : kind == 3 ? 6 : 2; }
-// Field groups of the transport work items: 0-2 the WENO fields in threes, 3 {u, v}, 4 {w}, 5 {theta}, 6-14 the WENO
-// fields one by one.
-constexpr int TGROUPS = 15;
-__constant__ int TGROUP[TGROUPS][3] = {{RAIN, SNOW, GRAUPEL}, {HAIL, Q, CLOUD}, {ICE, ICENUM, COLD}, {U, V, -1}, {W, -1, -1},
-                                       {THETA, -1, -1}, {RAIN, -1, -1}, {SNOW, -1, -1}, {GRAUPEL, -1, -1}, {HAIL, -1, -1},
-                                       {Q, -1, -1}, {CLOUD, -1, -1}, {ICE, -1, -1}, {ICENUM, -1, -1}, {COLD, -1, -1}};
+// Per-level constants staged in shared memory, rows of MAXNZ: 1/hz, 1/rho (both kinds), theta's four base-profile
+// face values, thb, qb, thv_env (dynamics).
+constexpr int tlv_rows(int kind) { return kind == TK_DYN ? 9 : 2; }
+// Field groups of the transport work items: 0-2 the WENO fields in threes, 3 the dynamics {u, v, w, theta'}, 4-12
+// the WENO fields one by one.
+constexpr int TGROUPS = 13;
+__constant__ int TGROUP[TGROUPS][4] = {{RAIN, SNOW, GRAUPEL, -1}, {HAIL, Q, CLOUD, -1}, {ICE, ICENUM, COLD, -1}, {U, V, W, THETA},
+                                       {RAIN, -1, -1, -1}, {SNOW, -1, -1, -1}, {GRAUPEL, -1, -1, -1}, {HAIL, -1, -1, -1},
+                                       {Q, -1, -1, -1}, {CLOUD, -1, -1, -1}, {ICE, -1, -1, -1}, {ICENUM, -1, -1, -1}, {COLD, -1, -1, -1}};
 
 // Two faces at once on the packed FP32 pipes (bit-identical per face to the scalar weno5 / upwind5).
 struct Op2 {
@@ -803,11 +803,11 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
   for (int z = t; z < nz; z += blockDim.x) {
     lv[0 * MAXNZ + z] = lvl(Rg, L_INV_HZ, z);
     lv[1 * MAXNZ + z] = lvl(Rg, L_INV_RHO, z);
-    if (KIND == TK_TH) {
+    if (KIND == TK_DYN) {
       lv[2 * MAXNZ + z] = lvl(Rg, L_TH_UP_POS, z); lv[3 * MAXNZ + z] = lvl(Rg, L_TH_UP_NEG, z);
       lv[4 * MAXNZ + z] = lvl(Rg, L_TH_DN_POS, z); lv[5 * MAXNZ + z] = lvl(Rg, L_TH_DN_NEG, z);
+      lv[6 * MAXNZ + z] = lvl(Rg, L_THB, z); lv[7 * MAXNZ + z] = lvl(Rg, L_QB, z); lv[8 * MAXNZ + z] = lvl(Rg, L_THVENV, z);
     }
-    if (KIND == TK_W) { lv[6 * MAXNZ + z] = lvl(Rg, L_THB, z); lv[7 * MAXNZ + z] = lvl(Rg, L_QB, z); lv[8 * MAXNZ + z] = lvl(Rg, L_THVENV, z); }
   }
   // plane cells of this thread as column offsets (periodic)
   int off[TMAXC], cell[TMAXC];
@@ -820,7 +820,7 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
     gx = ((gx % nx) + nx) % nx; gy = ((gy % ny) + ny) % ny;
     off[j] = e < NCELL ? gx + gy * nx : 0;
   }
-  const bool loadBuoy = KIND == TK_W && (flags & RF_STAGES);
+  const bool loadBuoy = KIND == TK_DYN && (flags & RF_STAGES);
   const bool loading = flags & RF_LOADING;
   // prologue: ring slots of the virtual levels -3..3 (clamped), level 0's inputs
   for (int v = -3; v <= 3; v++) {
@@ -942,12 +942,12 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
         const float* FY = fys + (buf * G + g) * FYS + ly * TX + lx;
         float flux = (FX[1] - FX[0]) * inv_dx + (FY[TX] - FY[0]) * inv_dy + (fzU[g] - fzD[g]) * ihz;
         float tend = -(flux - qc[g] * fc.w) * irho;
-        if (KIND == TK_TH) {
+        if (KIND == TK_DYN && g == 3) {  // theta': the base profile's own vertical flux
           float up = m3 * (m3 >= 0.f ? lv[2 * MAXNZ + z] : lv[3 * MAXNZ + z]);
           float dn = mzD * (mzD >= 0.f ? lv[4 * MAXNZ + z] : lv[5 * MAXNZ + z]);
           tend -= (up - dn) * ihz * irho;
         }
-        if (KIND == TK_W && loadBuoy) {
+        if (KIND == TK_DYN && g == 2 && loadBuoy) {
           // g B with theta' and the base state (stageBuoyancy): theta_v - theta_v,env from small differences.
           const float Rb = lv[6 * MAXNZ + z], Qb = lv[7 * MAXNZ + z];
           float dth = b[0], num = dth + .61f * ((Rb + dth) * (b[1] - Qb) + Qb * dth);
@@ -955,7 +955,7 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
           tend += 9.81f * (num / lv[8 * MAXNZ + z] - loaded);
         }
         float a = (stage == 0 ? qc[g] : s0[g]) + fdt * tend;
-        if (KIND == TK_W && stage < 2 && (flags & RF_STAGES) && (z == 0 || z == nz - 1)) a = 0.f;
+        if (KIND == TK_DYN && g == 2 && stage < 2 && (flags & RF_STAGES) && (z == 0 || z == nz - 1)) a = 0.f;
         out[g][col + l] = a;
         fzD[g] = fzU[g];
       }
@@ -1392,9 +1392,7 @@ void launch_transport(const Launch& L, int kind, int group, int minb, int in_set
       if (group == 3) { if (minb == 3) TLAUNCH(TK_WENO, 3, 3); else TLAUNCH(TK_WENO, 3, 2); }
       else { if (minb == 3) TLAUNCH(TK_WENO, 1, 3); else TLAUNCH(TK_WENO, 1, 2); }
       break;
-    case TK_LIN: TLAUNCH(TK_LIN, 2, 2); break;
-    case TK_W: TLAUNCH(TK_W, 1, 2); break;
-    default: TLAUNCH(TK_TH, 1, 2); break;
+    default: TLAUNCH(TK_DYN, 4, 2); break;
   }
 }
 #undef TLAUNCH
@@ -1422,9 +1420,7 @@ cudaError_t set_smem_limits(int bytes) {
   if ((e = cudaFuncSetAttribute(k_transport<TK_WENO, 3, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
   if ((e = cudaFuncSetAttribute(k_transport<TK_WENO, 1, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
   if ((e = cudaFuncSetAttribute(k_transport<TK_WENO, 1, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(k_transport<TK_LIN, 2, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(k_transport<TK_W, 1, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(k_transport<TK_TH, 1, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(k_transport<TK_DYN, 4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
   return cudaSuccess;
 }
 

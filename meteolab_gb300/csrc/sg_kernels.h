@@ -30,8 +30,9 @@ void launch_proj_xifft(const Launch& L, int mode, int yc, int maxnx);
 void launch_face_correct(const Launch& L, int set);
 void launch_pres_correct(const Launch& L, int set, int final_);
 // kind: 0 WENO fields, 1 u and v, 2 w, 3 theta (the item list of that kind)
-enum TKind { TK_WENO = 0, TK_LIN = 1, TK_W = 2, TK_TH = 3 };
-// Transport of one field kind (0 WENO, 1 {u, v}, 2 w, 3 theta); for WENO `group` is the fields per item (1 or 3)
+enum TKind { TK_WENO = 0, TK_DYN = 1 };
+// Transport of one field kind (0: the WENO fields, 1: the dynamics u, v, w, theta'); for WENO `group` is the fields
+// per item (1 or 3)
 // and `minb` the blocks per SM its register budget is cut for (2 or 3).
 void launch_transport(const Launch& L, int kind, int group, int minb, int in_set, int out_set, float frac, int stage, int TX, int TY);
 size_t transport_smem(int kind, int G, int TX, int TY);

@@ -77,8 +77,8 @@ struct Plan {
     if (items) cudaFree(items);
   }
 };
-enum Family { FAM_NODE, FAM_COLS, FAM_ROWS_FACE, FAM_ROWS_PRES, FAM_MODES, FAM_RUNS, FAM_CELLS, FAM_T_WENO, FAM_T_LIN, FAM_T_W, FAM_T_TH,
-              FAM_MIX, FAM_COUNT };
+enum Family { FAM_NODE, FAM_COLS, FAM_ROWS_FACE, FAM_ROWS_PRES, FAM_MODES, FAM_RUNS, FAM_CELLS, FAM_T_WENO, FAM_T_DYN, FAM_MIX,
+              FAM_COUNT };
 
 }  // namespace
 
@@ -94,7 +94,7 @@ struct sg_context {
   uint64_t pooled = 0;
   std::string error;
   double* d_scalar = nullptr;           // scratch for reductions read back by the host
-  // The four transport kinds of an RK3 stage run as parallel branches of the step's graph.
+  // The two transport kinds of an RK3 stage (WENO fields, dynamics) run as parallel branches of the step's graph.
   cudaStream_t side[3] = {nullptr, nullptr, nullptr};
   cudaEvent_t fork = nullptr, join[3] = {nullptr, nullptr, nullptr};
   bool forking = false;                 // set while a step is captured into a graph
@@ -270,14 +270,14 @@ Run* find(sg_context* ctx, sg_run run) {
 
 // ------------------------------------------------------------------ plans
 // Transport work items (run, field group, tile) of a plan for a tile shape and WENO group size: groups 0-2 are the
-// WENO fields in threes, 6-14 one by one, 3 {u, v}, 4 {w}, 5 {theta}.
+// WENO fields in threes, 4-12 one by one, 3 the dynamics {u, v, w, theta'}.
 void transport_items(sg_context* ctx, const std::vector<int>& slots, int TX, int TY, int wenoG, std::vector<int4>* fam) {
   for (int s : slots) {
     const Run& r = ctx->runs[s];
     const int tiles = ((r.nx + TX - 1) / TX) * ((r.ny + TY - 1) / TY);
-    const int grp0 = wenoG == 3 ? 0 : 6, ngrp = wenoG == 3 ? 3 : 9;
+    const int grp0 = wenoG == 3 ? 0 : 4, ngrp = wenoG == 3 ? 3 : 9;
     for (int g = grp0; g < grp0 + ngrp; g++) for (int t = 0; t < tiles; t++) fam[0].push_back(make_int4(s, g, t, 0));
-    for (int k = 1; k < 4; k++) for (int t = 0; t < tiles; t++) fam[k].push_back(make_int4(s, 2 + k, t, 0));
+    for (int t = 0; t < tiles; t++) fam[1].push_back(make_int4(s, 3, t, 0));
   }
 }
 
@@ -347,21 +347,21 @@ Launch lx(sg_context* ctx, const Plan& P, int fam, int capPerSm = 8) {
 // empty air skip their WENO weights) across the SMs.
 void launch_transport_kinds(sg_context* ctx, const Plan& P, int in, int out, float frac, int stage, bool fork, int hookBase,
                             const std::function<void(int)>& hook) {
-  const int fams[4] = {FAM_T_WENO, FAM_T_LIN, FAM_T_W, FAM_T_TH};
+  const int fams[2] = {FAM_T_WENO, FAM_T_DYN};
   if (fork) cudaEventRecord(ctx->fork, ctx->stream);
-  for (int k = 0; k < 4; k++) {
+  for (int k = 0; k < 2; k++) {
     Launch L = lx(ctx, P, fams[k]);
     L.cap = L.n;
-    if (fork && k > 0) { cudaStreamWaitEvent(ctx->side[k - 1], ctx->fork, 0); L.stream = ctx->side[k - 1]; }
+    if (fork && k > 0) { cudaStreamWaitEvent(ctx->side[0], ctx->fork, 0); L.stream = ctx->side[0]; }
     if (L.n) launch_transport(L, k, P.wenoG, P.minb, in, out, frac, stage, P.TX, P.TY);
-    if (fork && k > 0) cudaEventRecord(ctx->join[k - 1], ctx->side[k - 1]);
+    if (fork && k > 0) cudaEventRecord(ctx->join[0], ctx->side[0]);
     hook(hookBase + k);
   }
-  if (fork) for (int k = 0; k < 3; k++) cudaStreamWaitEvent(ctx->stream, ctx->join[k], 0);
+  if (fork) cudaStreamWaitEvent(ctx->stream, ctx->join[0], 0);
 }
 
 // Picks the transport tile (TX x TY columns) and WENO fields per item by timing every candidate on the plan's own
-// runs: the four transport kinds of one RK3 stage (set A in, set C out; C is scratch between steps), best of three
+// runs: the two transport kinds of one RK3 stage (set A in, set C out; C is scratch between steps), best of three
 // after a warm-up. Results are cached per batch signature (the sorted grid shapes, and the run count to a power of
 // two), so a serving loop whose batch changes run by run tunes each kind of batch once.
 int autotune_transport(sg_context* ctx, Plan& P) {
@@ -417,7 +417,7 @@ int autotune_transport(sg_context* ctx, Plan& P) {
   P.TX = best[0]; P.TY = best[1]; P.wenoG = best[2]; P.minb = best[3]; P.tuned = true;
   std::vector<int4> all[FAM_COUNT];
   for (int f = 0; f < FAM_COUNT; f++) {  // keep the other families, rebuild the transport ones
-    if (f >= FAM_T_WENO && f <= FAM_T_TH) continue;
+    if (f == FAM_T_WENO || f == FAM_T_DYN) continue;
     all[f].resize(P.cnt[f]);
     if (P.cnt[f]) CK(cudaMemcpy(all[f].data(), P.items + P.off[f], P.cnt[f] * sizeof(int4), cudaMemcpyDeviceToHost));
   }
@@ -483,11 +483,10 @@ template <class Hook>
 void enqueue_step(sg_context* ctx, const Plan& P, Hook hook) {
   for (int part = 1; part <= 5; part++) enqueue_part(ctx, P, part, hook);
 }
-const int NKERNELS = 22;
+const int NKERNELS = 20;
 const char* KERNEL_NAMES[NKERNELS] = {"fall_courant", "sediment", "face_div_xfft", "face_modes", "face_xifft", "face_correct", "transport",
                                       "pres_div_xfft", "pres_modes", "pres_xifft", "pres_correct", "fill_partial", "fill_final", "physics",
-                                      "viscosity", "mix", "pres_correct_final", "step_end", "transport_weno", "transport_uv",
-                                      "transport_w", "transport_theta"};
+                                      "viscosity", "mix", "pres_correct_final", "step_end", "transport_weno", "transport_dynamics"};
 
 Plan* get_plan(sg_context* ctx, const std::vector<int>& slots, int* status) {
   auto it = ctx->plans.find(slots);
