@@ -73,6 +73,10 @@ typedef struct sg_switches {
   double drag_cd;          /* neutral drag coefficient of the ground node (dragCoefficient), 0 = no drag */
   double frame_u, frame_v; /* velocity of the domain over the ground, m/s */
   int32_t loading, evaporation, rain_formation, anisotropic, vertical_dz, durran_klemp, pressure_in_stages, ice;
+  /* 1: the final projection is refined once (the residual divergence formed in double-FP32 and solved again), so the
+   * projected velocity's divergence before its FP32 rounding is at rounding level as with the reference's FP64 solve;
+   * 0: one FP32-transform solve (residual a few 1e-6 of the divergence removed). No counterpart switch in the reference. */
+  int32_t refine_projection;
 } sg_switches;
 
 /* Per-run counters (AtmosphereModel.clipped, negativeFilled, water, src/core/model.ts:236, :269-271). */

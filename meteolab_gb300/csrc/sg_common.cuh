@@ -53,6 +53,8 @@ enum Level {
   L_SURF,                                               // surface flux share per metre (sharesAbove)
   L_TCB,                                                // theta_b exner - 273.15 (Celsius base temperature)
   L_QW_HI, L_QW_LO, L_BW, L_QI_HI, L_QI_LO, L_BI, L_Q0_HI, L_Q0_LO,  // saturation bases (sg_physics.cuh Level)
+  L_RHO_LO, L_INV_DZS_LO, L_INV_HZ_LO,                 // FP32 rounding errors of rho, 1/dzs, 1/hz (refinement)
+  L_WLO, L_WLO_LO, L_WHI, L_WHI_LO,                     // dzs(k-1)/hz, dzs(k)/hz as FP32 pairs (refinement)
   L_COUNT
 };
 // Per-level FP64 constants.
@@ -63,12 +65,14 @@ struct RunDesc {
   int fx_nf, fy_nf, fx_rad[8], fy_rad[8];  // FFT radix plans of nx and ny
   int slot, flags, pad0, pad1;
   float dx, dy, inv_dx, inv_dy, dt, height;
+  float inv_dx_lo, inv_dy_lo, inv_dt, inv_dt_lo;      // FP32 rounding errors of 1/dx, 1/dy; 1/dt as a pair
   float coriolis, keep, sponge_start, cs, drag, frame_u, frame_v, ue0, ve0, env_speed, lenH2, capH, rho0;
   float* fld;
   float* faces;
   float* kmkh;
   float* phi;
   float* pres;
+  float* pres2;            // the refinement's pressure correction (the projection's pressure is pres + pres2)
   float2* spec;
   float* cols;
   const float* lv;
@@ -83,7 +87,8 @@ struct RunDesc {
   double* acc;             // FP64 running totals: negativeFilled, water[4]
   unsigned long long* cnt; // counters: clipped, steps, failed flag
 };
-enum RunFlags { RF_LOADING = 1, RF_EVAP = 2, RF_RAINFORM = 4, RF_ANISO = 8, RF_VDZ = 16, RF_DK = 32, RF_STAGES = 64, RF_ICE = 128 };
+enum RunFlags { RF_LOADING = 1, RF_EVAP = 2, RF_RAINFORM = 4, RF_ANISO = 8, RF_VDZ = 16, RF_DK = 32, RF_STAGES = 64, RF_ICE = 128,
+                RF_REFINE = 256 };
 // scr layout
 enum Scratch { S_COURANT = 0, S_FILL = 4, S_COUNT = 16 };
 // cnt layout

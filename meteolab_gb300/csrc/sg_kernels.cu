@@ -260,6 +260,12 @@ __global__ void k_proj_div_xfft(const RunDesc* __restrict__ runs, const int4* it
         }
         reinterpret_cast<float*>(&Z[(r >> 1) * nx + x])[r & 1] = d;
       }
+    } else if (mode == PROJ_GIVEN) {
+      const float* rhs = R.phi + (size_t)k * layer;
+      for (int e = threadIdx.x; e < pairs * 2 * nx; e += blockDim.x) {
+        const int r = row_of(e, inv_nx), x = e - r * nx, y = y0 + r;
+        reinterpret_cast<float*>(&Z[(r >> 1) * nx + x])[r & 1] = r < rows ? rhs[x + y * nx] : 0.f;
+      }
     } else {
       const float r0 = .25f * lvl(R, L_RHO, k), r1 = .25f * lvl(R, L_RHO, k + 1), idz = lvl(R, L_INV_DZS, k), idt = 1.f / R.dt;
       const int l0 = k * layer, l1 = l0 + layer;
@@ -400,7 +406,7 @@ __global__ void k_proj_xifft(const RunDesc* __restrict__ runs, const int4* items
     FftPlan P{nx, R.fx_nf, R.fx_rad, R.twx};
     const float2* Zf = fft_rows_any(Z, T, nx, pairs, P);
     const float norm = 1.f / (float)(nx * ny);
-    float* out = (mode == PROJ_FACE ? R.phi : R.pres) + (size_t)k * nx * ny;
+    float* out = (mode == PROJ_FACE ? R.phi : mode == PROJ_GIVEN ? R.pres2 : R.pres) + (size_t)k * nx * ny;
     for (int e = threadIdx.x; e < rows * nx; e += blockDim.x) {
       const int r = row_of(e, inv_nx), x = e - r * nx;
       const float2 z = Zf[(r >> 1) * nx + x];
@@ -461,6 +467,12 @@ __global__ void k_proj_div_fft2(const RunDesc* __restrict__ runs, const int4* it
           d = ddx * idx + ddy * idy + (up - dn) * ihz;
         }
         reinterpret_cast<float*>(&Z[(r >> 1) * nx + x])[r & 1] = d;
+      }
+    } else if (mode == PROJ_GIVEN) {
+      const float* rhs = R.phi + (size_t)k * layer;
+      for (int e = threadIdx.x; e < pairs * 2 * nx; e += blockDim.x) {
+        const int r = row_of(e, inv_nx), x = e - r * nx, y = r;
+        reinterpret_cast<float*>(&Z[(r >> 1) * nx + x])[r & 1] = r < ny ? rhs[x + y * nx] : 0.f;
       }
     } else {
       const float r0 = .25f * lvl(R, L_RHO, k), r1 = .25f * lvl(R, L_RHO, k + 1), idz = lvl(R, L_INV_DZS, k), idt = 1.f / R.dt;
@@ -576,7 +588,7 @@ __global__ void k_proj_ifft2(const RunDesc* __restrict__ runs, const int4* items
     __syncthreads();
     const float2* Zf = fft_rows_any(Z, T, nx, pairs, Px);
     const float norm = 1.f / (float)(nx * ny);
-    float* out = (mode == PROJ_FACE ? R.phi : R.pres) + (size_t)k * nx * ny;
+    float* out = (mode == PROJ_FACE ? R.phi : mode == PROJ_GIVEN ? R.pres2 : R.pres) + (size_t)k * nx * ny;
     for (int e = threadIdx.x; e < ny * nx; e += blockDim.x) {
       const int r = row_of(e, inv_nx), x = e - r * nx;
       const float2 z = Zf[(r >> 1) * nx + x];
@@ -644,6 +656,7 @@ __global__ void k_pres_correct(const RunDesc* __restrict__ runs, const int4* ite
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
     if (R.cnt[C_FAILED]) continue;
+    if (final_ && (R.flags & RF_REFINE)) continue;  // these runs finish in k_refine_correct
     const int nx = R.nx, ny = R.ny, nz = R.nz, layer = R.layer, i0 = items[it].y * CHUNK, i1 = min(R.n, i0 + CHUNK);
     float *u = field(R, set, U), *v = field(R, set, V), *w = field(R, set, W);
     const float* __restrict__ p = R.pres;
@@ -696,6 +709,150 @@ __global__ void k_pres_correct(const RunDesc* __restrict__ runs, const int4* ite
       clipped = warpSum(clipped);
       if ((threadIdx.x & 31) == 0 && clipped) atomicAdd(&R.cnt[C_CLIPPED], (unsigned long long)clipped);
     }
+  }
+}
+
+// ---- refinement of the final projection (runs with RF_REFINE). The solve above works in FP32 transforms and an FP32
+// pressure, which leaves a residual divergence of a few 1e-6 of the one it removed. One refinement step brings it to
+// rounding level: the projected velocity v = u - dt G p1 and its divergence are formed in double-FP32 arithmetic
+// (hi + lo pairs, error-free sums and products: about 44 significant bits on the FP32 pipes), the residual r = D v / dt
+// is solved again (p2) and the velocity becomes v - dt G p2, rounded to FP32 once. The projection's pressure is
+// p1 + p2.
+struct DF { float hi, lo; };
+__device__ __forceinline__ DF df_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b), bp = __fsub_rn(s, a);
+  return DF{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp))};
+}
+__device__ __forceinline__ DF df_fast(float s, float e) {  // |s| >= |e|
+  const float h = __fadd_rn(s, e);
+  return DF{h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+  const DF s = df_two_sum(a.hi, b.hi);
+  return df_fast(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ DF df_sub(DF a, DF b) { return df_add(a, DF{-b.hi, -b.lo}); }
+__device__ __forceinline__ DF df_mul(DF a, DF b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  const float e = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, __fmaf_rn(a.hi, b.hi, -p)));
+  return df_fast(p, e);
+}
+__device__ __forceinline__ DF df_diff(float a, float b) { return df_two_sum(a, -b); }  // a - b exactly
+
+// G p1 at a node in double-FP32 (the gradient of k_pres_correct).
+__device__ __forceinline__ void df_gradient(const RunDesc& R, const float* p, int i, int k, DF& gx, DF& gy, DF& gz) {
+  const int nx = R.nx, ny = R.ny, nz = R.nz, layer = R.layer;
+  const int c = i - k * layer, jy = row_of(c, 1.f / (float)nx), x = c - jy * nx;
+  const int im = x == 0 ? nx - 1 : x - 1, jm = (jy == 0 ? ny - 1 : jy - 1) * nx, j0 = jy * nx;
+  const float* L = p + (size_t)max(0, k - 1) * layer;
+  const float* H = p + (size_t)min(nz - 2, k) * layer;
+  const float l0 = L[im + jm], l1 = L[x + jm], l2 = L[im + j0], l3 = L[x + j0];
+  const float h0 = H[im + jm], h1 = H[x + jm], h2 = H[im + j0], h3 = H[x + j0];
+  const DF wlo = k > 0 ? DF{lvl(R, L_WLO, k), lvl(R, L_WLO_LO, k)} : DF{0.f, 0.f};
+  const DF whi = k < nz - 1 ? DF{lvl(R, L_WHI, k), lvl(R, L_WHI_LO, k)} : DF{0.f, 0.f};
+  const DF qx{.25f * R.inv_dx, .25f * R.inv_dx_lo}, qy{.25f * R.inv_dy, .25f * R.inv_dy_lo};
+  gx = df_mul(df_add(df_mul(wlo, df_add(df_diff(l1, l0), df_diff(l3, l2))), df_mul(whi, df_add(df_diff(h1, h0), df_diff(h3, h2)))), qx);
+  gy = df_mul(df_add(df_mul(wlo, df_add(df_diff(l2, l0), df_diff(l3, l1))), df_mul(whi, df_add(df_diff(h2, h0), df_diff(h3, h1)))), qy);
+  gz = DF{0.f, 0.f};
+  if (k > 0 && k < nz - 1) {
+    const DF s = df_add(df_add(df_diff(h0, l0), df_diff(h1, l1)), df_add(df_diff(h2, l2), df_diff(h3, l3)));
+    gz = df_mul(s, DF{.25f * lvl(R, L_INV_HZ, k), .25f * lvl(R, L_INV_HZ_LO, k)});
+  }
+}
+
+// v = u - dt G p1 at every node of set `set` as hi + lo: hi into set B, lo into set C (u, v, w).
+__global__ void k_refine_nodes(const RunDesc* __restrict__ runs, const int4* items, int nitems, int set) {
+  FOR_ITEMS {
+    const RunDesc& R = runs[items[it].x];
+    if (R.cnt[C_FAILED] || !(R.flags & RF_REFINE)) continue;
+    const int layer = R.layer, i0 = items[it].y * CHUNK, i1 = min(R.n, i0 + CHUNK);
+    const DF dt{R.dt, 0.f};
+    int k = (i0 + threadIdx.x) / layer;
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+      while (i >= (k + 1) * layer) k++;
+      DF g[3];
+      df_gradient(R, R.pres, i, k, g[0], g[1], g[2]);
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        const DF v = df_sub(DF{field(R, set, U + d)[i], 0.f}, df_mul(dt, g[d]));
+        field(R, 1, U + d)[i] = v.hi;
+        field(R, 2, U + d)[i] = v.lo;
+      }
+    }
+  }
+}
+
+// r = D v / dt per dual cell from the pairs of k_refine_nodes, rounded once into phi: D of the hi parts in
+// double-FP32 (their differences are exact), D of the lo parts (a few 1e-8 of them) in FP32.
+__global__ void k_refine_div(const RunDesc* __restrict__ runs, const int4* items, int nitems) {
+  FOR_ITEMS {
+    const RunDesc& R = runs[items[it].x];
+    if (R.cnt[C_FAILED] || !(R.flags & RF_REFINE)) continue;
+    const int nx = R.nx, ny = R.ny, layer = R.layer, i0 = items[it].y * CHUNK, i1 = min(R.ncells, i0 + CHUNK);
+    const DF idx{R.inv_dx, R.inv_dx_lo}, idy{R.inv_dy, R.inv_dy_lo}, idt{R.inv_dt, R.inv_dt_lo};
+    const float* __restrict__ H[3] = {field(R, 1, U), field(R, 1, V), field(R, 1, W)};
+    const float* __restrict__ Lo[3] = {field(R, 2, U), field(R, 2, V), field(R, 2, W)};
+    const float inv_nx = 1.f / (float)nx;
+    int k = (i0 + threadIdx.x) / layer;
+    for (int cidx = i0 + threadIdx.x; cidx < i1; cidx += blockDim.x) {
+      while (cidx >= (k + 1) * layer) k++;
+      const int c = cidx - k * layer, y = row_of(c, inv_nx), x = c - y * nx;
+      const int l0 = k * layer, l1 = l0 + layer, x1 = x + 1 == nx ? 0 : x + 1, y1 = (y + 1 == ny ? 0 : y + 1) * nx, yy = y * nx;
+      const int a = x + yy, b = x1 + yy, e = x + y1, f = x1 + y1;
+      const DF r0{.25f * lvl(R, L_RHO, k), .25f * lvl(R, L_RHO_LO, k)}, r1{.25f * lvl(R, L_RHO, k + 1), .25f * lvl(R, L_RHO_LO, k + 1)};
+      const DF idz{lvl(R, L_INV_DZS, k), lvl(R, L_INV_DZS_LO, k)};
+      const float* hu = H[0]; const float* hv = H[1]; const float* hw = H[2];
+      const DF ddx = df_mul(df_add(df_mul(r0, df_add(df_diff(hu[b + l0], hu[a + l0]), df_diff(hu[f + l0], hu[e + l0]))),
+                                   df_mul(r1, df_add(df_diff(hu[b + l1], hu[a + l1]), df_diff(hu[f + l1], hu[e + l1])))), idx);
+      const DF ddy = df_mul(df_add(df_mul(r0, df_add(df_diff(hv[e + l0], hv[a + l0]), df_diff(hv[f + l0], hv[b + l0]))),
+                                   df_mul(r1, df_add(df_diff(hv[e + l1], hv[a + l1]), df_diff(hv[f + l1], hv[b + l1])))), idy);
+      const DF up = df_add(df_add(DF{hw[a + l1], 0.f}, DF{hw[b + l1], 0.f}), df_add(DF{hw[e + l1], 0.f}, DF{hw[f + l1], 0.f}));
+      const DF dn = df_add(df_add(DF{hw[a + l0], 0.f}, DF{hw[b + l0], 0.f}), df_add(DF{hw[e + l0], 0.f}, DF{hw[f + l0], 0.f}));
+      const DF ddz = df_mul(df_sub(df_mul(r1, up), df_mul(r0, dn)), idz);
+      const float* lu = Lo[0]; const float* lv_ = Lo[1]; const float* lw = Lo[2];
+      const float rr0 = r0.hi, rr1 = r1.hi;
+      const float lox = (rr0 * ((lu[b + l0] - lu[a + l0]) + (lu[f + l0] - lu[e + l0])) + rr1 * ((lu[b + l1] - lu[a + l1]) + (lu[f + l1] - lu[e + l1]))) * idx.hi;
+      const float loy = (rr0 * ((lv_[e + l0] - lv_[a + l0]) + (lv_[f + l0] - lv_[b + l0])) + rr1 * ((lv_[e + l1] - lv_[a + l1]) + (lv_[f + l1] - lv_[b + l1]))) * idy.hi;
+      const float loz = (rr1 * ((lw[a + l1] + lw[b + l1]) + (lw[e + l1] + lw[f + l1])) - rr0 * ((lw[a + l0] + lw[b + l0]) + (lw[e + l0] + lw[f + l0]))) * idz.hi;
+      const DF d = df_mul(df_add(df_add(df_add(ddx, ddy), ddz), DF{(lox + loy) + loz, 0.f}), idt);
+      R.phi[cidx] = d.hi + d.lo;
+    }
+  }
+}
+
+// The final velocity v - dt G p2 (p2 from the refinement's solve, its gradient in FP32: it is a correction of a few
+// 1e-6), rounded once to FP32, with the wind limits and their count (clipWind, src/core/model.ts:1586-1595).
+__global__ void k_refine_correct(const RunDesc* __restrict__ runs, const int4* items, int nitems, int set) {
+  FOR_ITEMS {
+    const RunDesc& R = runs[items[it].x];
+    if (R.cnt[C_FAILED] || !(R.flags & RF_REFINE)) continue;
+    const int nx = R.nx, ny = R.ny, nz = R.nz, layer = R.layer, i0 = items[it].y * CHUNK, i1 = min(R.n, i0 + CHUNK);
+    const float* p = R.pres2;
+    const float dt = R.dt;
+    int clipped = 0;
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+      const int k = i / layer, c = i - k * layer, jy = c / nx, x = c - jy * nx;
+      const int im = x == 0 ? nx - 1 : x - 1, jm = (jy == 0 ? ny - 1 : jy - 1) * nx, j0 = jy * nx;
+      const float* L = p + (size_t)max(0, k - 1) * layer;
+      const float* H = p + (size_t)min(nz - 2, k) * layer;
+      const float hz = lvl(R, L_HZ, k);
+      const float wLo = k > 0 ? lvl(R, L_DZS, k - 1) / hz : 0.f, wHi = k < nz - 1 ? lvl(R, L_DZS, k) / hz : 0.f;
+      const float g[3] = {
+        (wLo * ((L[x + jm] - L[im + jm]) + (L[x + j0] - L[im + j0])) + wHi * ((H[x + jm] - H[im + jm]) + (H[x + j0] - H[im + j0]))) * (.25f * R.inv_dx),
+        (wLo * ((L[im + j0] - L[im + jm]) + (L[x + j0] - L[x + jm])) + wHi * ((H[im + j0] - H[im + jm]) + (H[x + j0] - H[x + jm]))) * (.25f * R.inv_dy),
+        k > 0 && k < nz - 1 ? ((H[im + jm] - L[im + jm]) + (H[x + jm] - L[x + jm]) + (H[im + j0] - L[im + j0]) + (H[x + j0] - L[x + j0])) * (.25f * lvl(R, L_INV_HZ, k)) : 0.f};
+      float out[3];
+#pragma unroll
+      for (int d = 0; d < 3; d++) out[d] = __fadd_rn(__fmaf_rn(-dt, g[d], field(R, 1, U + d)[i]), field(R, 2, U + d)[i]);
+      const float UL = 120.f, WL = 100.f;
+      if (out[0] < -UL || out[0] > UL) { out[0] = fmaxf(-UL, fminf(UL, out[0])); clipped++; }
+      if (out[1] < -UL || out[1] > UL) { out[1] = fmaxf(-UL, fminf(UL, out[1])); clipped++; }
+      if (out[2] < -WL || out[2] > WL) { out[2] = fmaxf(-WL, fminf(WL, out[2])); clipped++; }
+#pragma unroll
+      for (int d = 0; d < 3; d++) field(R, set, U + d)[i] = out[d];
+    }
+    clipped = warpSum(clipped);
+    if ((threadIdx.x & 31) == 0 && clipped) atomicAdd(&R.cnt[C_CLIPPED], (unsigned long long)clipped);
   }
 }
 
@@ -810,15 +967,16 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
     }
   }
   // plane cells of this thread as column offsets (periodic)
-  int off[TMAXC], cell[TMAXC];
+  // plane cell t + j * NT of this thread: its column offset (periodic), -1 past the plane
+  const int NT = blockDim.x;
+  int off[TMAXC];
 #pragma unroll
   for (int j = 0; j < TMAXC; j++) {
-    int e = t + j * blockDim.x;
-    cell[j] = e < NCELL ? e : -1;
+    int e = t + j * NT;
     int hy = e / PW, hx = e - hy * PW;
     int gx = x0 + hx - 3, gy = y0 + hy - 3;
     gx = ((gx % nx) + nx) % nx; gy = ((gy % ny) + ny) % ny;
-    off[j] = e < NCELL ? gx + gy * nx : 0;
+    off[j] = e < NCELL ? gx + gy * nx : -1;
   }
   const bool loadBuoy = KIND == TK_DYN && (flags & RF_STAGES);
   const bool loading = flags & RF_LOADING;
@@ -828,7 +986,7 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
 #pragma unroll
     for (int g = 0; g < G; g++)
 #pragma unroll
-      for (int j = 0; j < TMAXC; j++) if (cell[j] >= 0) ring[(g * 7 + slot) * NCELL + cell[j]] = q[g][off[j] + lev * layer];
+      for (int j = 0; j < TMAXC; j++) if (off[j] >= 0) ring[(g * 7 + slot) * NCELL + t + j * NT] = q[g][off[j] + lev * layer];
   }
   float4 fc = on ? F4[col] : make_float4(0.f, 0.f, 0.f, 0.f);
   float me = edgeW ? F4[eoff].x : edgeS ? F4[eoff].y : 0.f;
@@ -857,7 +1015,7 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
 #pragma unroll
     for (int g = 0; g < G; g++)
 #pragma unroll
-      for (int j = 0; j < TMAXC; j++) if (cell[j] >= 0) cp_async4(ring + (g * 7 + s_new) * NCELL + cell[j], q[g] + off[j] + levNext);
+      for (int j = 0; j < TMAXC; j++) if (off[j] >= 0) cp_async4(ring + (g * 7 + s_new) * NCELL + t + j * NT, q[g] + off[j] + levNext);
     float4 fcn = make_float4(0.f, 0.f, 0.f, 0.f);
     float men = 0.f, s0n[G], bn[8];
 #pragma unroll
@@ -1379,6 +1537,9 @@ void launch_proj_xifft(const Launch& L, int mode, int yc, int maxnx) {
   k_proj_xifft<<<GRID(L.n, L.cap), 256, smem, L.stream>>>(L.runs, L.items, L.n, mode, yc);
 }
 void launch_face_correct(const Launch& L, int set) { k_face_correct<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set); }
+void launch_refine_nodes(const Launch& L, int set) { k_refine_nodes<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set); }
+void launch_refine_div(const Launch& L) { k_refine_div<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n); }
+void launch_refine_correct(const Launch& L, int set) { k_refine_correct<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set); }
 void launch_pres_correct(const Launch& L, int set, int final_) { k_pres_correct<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set, final_); }
 size_t transport_smem(int kind, int G, int TX, int TY) {
   return ((size_t)tlv_rows(kind) * MAXNZ + (size_t)G * 7 * (TX + 6) * (TY + 6) + 2 * (size_t)G * TY * (TX + 1) + 2 * (size_t)G * (TY + 1) * TX) * sizeof(float);

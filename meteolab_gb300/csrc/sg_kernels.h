@@ -5,7 +5,9 @@
 
 namespace sg {
 
-enum ProjMode { PROJ_FACE = 0, PROJ_PRES = 1 };
+// FACE: the face projection; PRES: the pressure projection of a set's velocities; GIVEN: the pressure solve of the
+// right-hand side held in phi (the refinement), its result into pres2.
+enum ProjMode { PROJ_FACE = 0, PROJ_PRES = 1, PROJ_GIVEN = 2 };
 
 struct Launch {
   const RunDesc* runs;   // device array of run descriptors
@@ -28,6 +30,11 @@ void launch_proj_sweep(const Launch& L, int mode, int maxny);
 void launch_proj_ifft2(const Launch& L, int mode, int maxnx, int maxny);
 void launch_proj_xifft(const Launch& L, int mode, int yc, int maxnx);
 void launch_face_correct(const Launch& L, int set);
+// Refinement of the final projection: node pairs v = u - dt G p1 (nodes), their divergence into phi (cells), and
+// the corrected velocity from pres2 (nodes).
+void launch_refine_nodes(const Launch& L, int set);
+void launch_refine_div(const Launch& L);
+void launch_refine_correct(const Launch& L, int set);
 void launch_pres_correct(const Launch& L, int set, int final_);
 // kind: 0 WENO fields, 1 u and v, 2 w, 3 theta (the item list of that kind)
 enum TKind { TK_WENO = 0, TK_DYN = 1 };

@@ -32,13 +32,13 @@ const double RK3[3] = {1.0 / 3, 1.0 / 2, 1.0};
 size_t align(size_t x) { return (x + ALIGN - 1) / ALIGN * ALIGN; }
 
 struct Layout {
-  size_t fld, faces, kmkh, phi, pres, spec, cols, lv, lv64, triF, triP, ab, twx, twy, scr, part, acc, cnt, items, total;
+  size_t fld, faces, kmkh, phi, pres, pres2, spec, cols, lv, lv64, triF, triP, ab, twx, twy, scr, part, acc, cnt, items, total;
 };
 Layout layout(int nx, int ny, int nz) {
   Layout L; size_t n = (size_t)nx * ny * nz, layer = (size_t)nx * ny, nm = nx / 2 + 1, nch = (n + CHUNK - 1) / CHUNK, o = 0;
   auto take = [&](size_t bytes) { size_t at = o; o += align(bytes); return at; };
   L.fld = take(3 * NF * n * 4); L.faces = take(4 * n * 4); L.kmkh = take(2 * n * 4); L.phi = take(n * 4);
-  L.pres = take(layer * (nz - 1) * 4); L.spec = take(nm * nz * ny * 8); L.cols = take(3 * layer * 4);
+  L.pres = take(layer * (nz - 1) * 4); L.pres2 = take(layer * (nz - 1) * 4); L.spec = take(nm * nz * ny * 8); L.cols = take(3 * layer * 4);
   L.lv = take((size_t)L_COUNT * nz * 4); L.lv64 = take((size_t)D_COUNT * nz * 8);
   L.triF = take(nm * nz * ny * 24); L.triP = take(nm * (nz - 1) * ny * 24); L.ab = take(nm * ny * 16);
   L.twx = take(nx * 8); L.twy = take(ny * 8); L.scr = take(64 * 4); L.part = take((nch * NCONS * 3 + nch * 4) * 8);
@@ -68,6 +68,7 @@ struct Plan {
   int yc = 32;                                                        // layer rows per x-transform item
   int mixTX = 32, mixTY = 8;                                          // mixing tile
   bool layerfft = false;                                              // 2-D transforms per layer (see enqueue_part)
+  bool refine = false;                                                // some run refines its final projection
   bool tuned = false;                                                 // TX, TY, wenoG chosen by timing
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -139,6 +140,11 @@ void build_tables(const sg_grid* g, const sg_base_state* b, const sg_switches* s
     double rUp = z < nz - 1 ? (rho[z] + rho[z + 1]) / 2 : 0;
     L(L_RHO, z, rho[z]); L(L_INV_RHO, z, 1 / rho[z]); L(L_HZ, z, hz[z]); L(L_INV_HZ, z, 1 / hz[z]);
     L(L_DZS, z, z < nz - 1 ? dzs[z] : 0); L(L_INV_DZS, z, z < nz - 1 ? 1 / dzs[z] : 0); L(L_RUP, z, rUp);
+    // FP32 pairs (value and rounding error) for the refinement's double-FP32 arithmetic
+    auto lo = [](double v) { return v - (double)(float)v; };
+    L(L_RHO_LO, z, lo(rho[z])); L(L_INV_HZ_LO, z, lo(1 / hz[z])); L(L_INV_DZS_LO, z, z < nz - 1 ? lo(1 / dzs[z]) : 0);
+    const double wlo = z > 0 ? dzs[z - 1] / hz[z] : 0, whi = z < nz - 1 ? dzs[z] / hz[z] : 0;
+    L(L_WLO, z, wlo); L(L_WLO_LO, z, lo(wlo)); L(L_WHI, z, whi); L(L_WHI_LO, z, lo(whi));
     L(L_EXNER, z, b->exner[z]); L(L_P, z, b->p[z]); L(L_THB, z, thb[z]); L(L_QB, z, b->q[z]);
     double ue = b->u[z] - sw->frame_u, ve = b->v[z] - sw->frame_v;
     L(L_UENV, z, ue); L(L_VENV, z, ve); L(L_THVENV, z, thb[z] * (1 + .61 * b->q[z])); L(L_ZS, z, zs[z]);
@@ -237,12 +243,15 @@ void build_tables(const sg_grid* g, const sg_base_state* b, const sg_switches* s
   d.nx = nx; d.ny = ny; d.nz = nz; d.layer = nx * ny; d.n = nx * ny * nz; d.nm = nm; d.mh = nx / 2; d.ncells = nx * ny * (nz - 1);
   d.fx_nf = fft_plan_factors(nx, d.fx_rad); d.fy_nf = fft_plan_factors(ny, d.fy_rad);
   d.dx = (float)dx; d.dy = (float)dy; d.inv_dx = (float)(1 / dx); d.inv_dy = (float)(1 / dy); d.dt = (float)dt; d.height = (float)g->height;
+  d.inv_dx_lo = (float)(1 / dx - (double)d.inv_dx); d.inv_dy_lo = (float)(1 / dy - (double)d.inv_dy);
+  d.inv_dt = (float)(1 / (double)d.dt); d.inv_dt_lo = (float)(1 / (double)d.dt - (double)d.inv_dt);
   d.coriolis = (float)sw->coriolis; d.keep = (float)std::exp(-sw->wind_relaxation * dt); d.sponge_start = (float)sw->sponge_start; d.cs = (float)cs;
   d.drag = (float)(sw->drag_cd * dt / hz[0]); d.frame_u = (float)sw->frame_u; d.frame_v = (float)sw->frame_v;
   d.ue0 = (float)b->u[0]; d.ve0 = (float)b->v[0]; d.env_speed = (float)std::hypot(b->u[0], b->v[0]);
   d.lenH2 = (float)std::pow(cs * std::sqrt(dx * dy), 2); d.capH = (float)(.05 * std::pow(std::min(dx, dy), 2) / dt); d.rho0 = (float)rho[0];
   d.flags = (sw->loading ? RF_LOADING : 0) | (sw->evaporation ? RF_EVAP : 0) | (sw->rain_formation ? RF_RAINFORM : 0) | (sw->anisotropic ? RF_ANISO : 0) |
-            (sw->vertical_dz ? RF_VDZ : 0) | (sw->durran_klemp ? RF_DK : 0) | (sw->pressure_in_stages ? RF_STAGES : 0) | (sw->ice ? RF_ICE : 0);
+            (sw->vertical_dz ? RF_VDZ : 0) | (sw->durran_klemp ? RF_DK : 0) | (sw->pressure_in_stages ? RF_STAGES : 0) | (sw->ice ? RF_ICE : 0) |
+            (sw->refine_projection ? RF_REFINE : 0);
 }
 
 int validate(sg_context* ctx, const sg_grid* g, const sg_base_state* b, const sg_switches* sw) {
@@ -323,6 +332,7 @@ int build_plan(sg_context* ctx, const std::vector<int>& slots, Plan& P) {
     for (int k = 0; k < r.nz - 1; k++) for (int y = 0; y < r.ny; y += P.yc) all[FAM_ROWS_PRES].push_back(make_int4(s, k, y, 0));
     for (int m = 0; m < r.nx / 2 + 1; m++) all[FAM_MODES].push_back(make_int4(s, m, 0, 0));
     all[FAM_RUNS].push_back(make_int4(s, 0, 0, 0));
+    if (r.desc.flags & RF_REFINE) P.refine = true;
   }
   // mixing items: (run, tile, z0, z1), the column in four level ranges
   P.mixTX = all40 ? 40 : 32; P.mixTY = 8;
@@ -440,19 +450,26 @@ void enqueue_part(sg_context* ctx, const Plan& P, int part, Hook hook) {
   const int mbudget = std::min(ctx->maxSmem, 200 * 1024);
   // the three stages of a spectral solve: divergence and forward transform, mode solves, inverse transform
   auto solve = [&](const Launch& rows, int mode, int set) {
+    const int h = mode == PROJ_FACE ? 2 : mode == PROJ_PRES ? 7 : 22;  // profile ids of the three stages
     if (P.layerfft) {
-      launch_proj_div_fft2(rows, mode, set, P.maxnx, P.maxny); hook(mode == PROJ_FACE ? 2 : 7);
-      launch_proj_sweep(modes, mode, P.maxny); hook(mode == PROJ_FACE ? 3 : 8);
-      launch_proj_ifft2(rows, mode, P.maxnx, P.maxny); hook(mode == PROJ_FACE ? 4 : 9);
+      launch_proj_div_fft2(rows, mode, set, P.maxnx, P.maxny); hook(h);
+      launch_proj_sweep(modes, mode, P.maxny); hook(h + 1);
+      launch_proj_ifft2(rows, mode, P.maxnx, P.maxny); hook(h + 2);
     } else {
-      launch_proj_div_xfft(rows, mode, set, P.yc, P.maxnx); hook(mode == PROJ_FACE ? 2 : 7);
-      launch_proj_modes(modes, mode, P.maxnz, P.maxny, mthreads, mbudget); hook(mode == PROJ_FACE ? 3 : 8);
-      launch_proj_xifft(rows, mode, P.yc, P.maxnx); hook(mode == PROJ_FACE ? 4 : 9);
+      launch_proj_div_xfft(rows, mode, set, P.yc, P.maxnx); hook(h);
+      launch_proj_modes(modes, mode, P.maxnz, P.maxny, mthreads, mbudget); hook(h + 1);
+      launch_proj_xifft(rows, mode, P.yc, P.maxnx); hook(h + 2);
     }
   };
   auto project = [&](int set, int final_) {
     solve(rp, PROJ_PRES, set);
-    launch_pres_correct(node, set, final_); hook(final_ ? 16 : 10);
+    launch_pres_correct(node, set, final_); hook(final_ ? 16 : 10);  // (the final one skips refined runs)
+    if (final_ && P.refine) {
+      launch_refine_nodes(node, set); hook(20);
+      launch_refine_div(lx(ctx, P, FAM_CELLS)); hook(21);
+      solve(rp, PROJ_GIVEN, set);
+      launch_refine_correct(node, set); hook(25);
+    }
   };
   if (part == 1) {
     launch_fall_courant(node); hook(0);
@@ -483,10 +500,11 @@ template <class Hook>
 void enqueue_step(sg_context* ctx, const Plan& P, Hook hook) {
   for (int part = 1; part <= 5; part++) enqueue_part(ctx, P, part, hook);
 }
-const int NKERNELS = 20;
+const int NKERNELS = 26;
 const char* KERNEL_NAMES[NKERNELS] = {"fall_courant", "sediment", "face_div_xfft", "face_modes", "face_xifft", "face_correct", "transport",
                                       "pres_div_xfft", "pres_modes", "pres_xifft", "pres_correct", "fill_partial", "fill_final", "physics",
-                                      "viscosity", "mix", "pres_correct_final", "step_end", "transport_weno", "transport_dynamics"};
+                                      "viscosity", "mix", "pres_correct_final", "step_end", "transport_weno", "transport_dynamics",
+                                      "refine_nodes", "refine_div", "refine_div_xfft", "refine_modes", "refine_xifft", "refine_correct"};
 
 Plan* get_plan(sg_context* ctx, const std::vector<int>& slots, int* status) {
   auto it = ctx->plans.find(slots);
@@ -635,7 +653,7 @@ int sg_run_create(sg_context* ctx, const sg_grid* g, const sg_base_state* b, con
   build_tables(g, b, sw, T, d);
   d.slot = slot;
   d.fld = (float*)(mem + Lo.fld); d.faces = (float*)(mem + Lo.faces); d.kmkh = (float*)(mem + Lo.kmkh); d.phi = (float*)(mem + Lo.phi);
-  d.pres = (float*)(mem + Lo.pres); d.spec = (float2*)(mem + Lo.spec); d.cols = (float*)(mem + Lo.cols);
+  d.pres = (float*)(mem + Lo.pres); d.pres2 = (float*)(mem + Lo.pres2); d.spec = (float2*)(mem + Lo.spec); d.cols = (float*)(mem + Lo.cols);
   d.lv = (const float*)(mem + Lo.lv); d.lv64 = (const double*)(mem + Lo.lv64); d.tri_face = (const double2*)(mem + Lo.triF);
   d.tri_pres = (const double2*)(mem + Lo.triP); d.ab = (const double2*)(mem + Lo.ab); d.twx = (const float2*)(mem + Lo.twx);
   d.twy = (const float2*)(mem + Lo.twy); d.scr = (float*)(mem + Lo.scr); d.part = (double*)(mem + Lo.part); d.acc = (double*)(mem + Lo.acc);
@@ -744,10 +762,11 @@ int sg_run_read_pressure(sg_context* ctx, sg_run run, double* p) {
   Run* r = find(ctx, run);
   if (!r) return fail(ctx, SG_ERR_NOT_FOUND, "no run " + std::to_string(run));
   size_t cells = (size_t)r->nx * r->ny * (r->nz - 1);
-  std::vector<float> tmp(cells);
+  std::vector<float> tmp(cells), tmp2(cells, 0.f);
   CK(cudaMemcpyAsync(tmp.data(), r->desc.pres, cells * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  if (r->desc.flags & RF_REFINE) CK(cudaMemcpyAsync(tmp2.data(), r->desc.pres2, cells * 4, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
-  for (size_t i = 0; i < cells; i++) p[i] = tmp[i];
+  for (size_t i = 0; i < cells; i++) p[i] = (double)tmp[i] + (double)tmp2[i];  // p1 + p2 of a refined projection
   return SG_OK;
 }
 

@@ -42,7 +42,7 @@ class SgSwitches(C.Structure):
                 ("sponge_start", C.c_double), ("cs", C.c_double), ("drag_cd", C.c_double), ("frame_u", C.c_double),
                 ("frame_v", C.c_double)] + [(k, C.c_int32) for k in ("loading", "evaporation", "rain_formation",
                                                                          "anisotropic", "vertical_dz", "durran_klemp",
-                                                                         "pressure_in_stages", "ice")]
+                                                                         "pressure_in_stages", "ice", "refine_projection")]
 
 
 class SgCounters(C.Structure):
@@ -121,7 +121,7 @@ class _Packed:
         self.base = SgBase(*[dp(a) for a in self.keep[3:]])
         self.switches = SgSwitches(sw.dt, sw.coriolis, sw.wind_relaxation, sw.sponge_rate, sw.sponge_start, sw.cs, sw.drag_cd(g),
                                    sw.frame_u, sw.frame_v, sw.loading, sw.evaporation, sw.rain_formation, sw.anisotropic,
-                                   sw.vertical_dz, sw.durran_klemp, sw.pressure_in_stages, 1)
+                                   sw.vertical_dz, sw.durran_klemp, sw.pressure_in_stages, 1, sw.refine_projection)
         self.fields = [np.ascontiguousarray(spec.fields[k], dtype=np.float32).ravel() for k in CARRIED]
         self.ptrs = (_FP * len(CARRIED))(*[a.ctypes.data_as(_FP) for a in self.fields])
 

@@ -70,6 +70,9 @@ class Switches:
     vertical_dz: int = 0
     durran_klemp: int = 0
     pressure_in_stages: int = 1
+    # the device refines its final projection once (FP32-transform residual solved again); the oracle's FP64 solve
+    # needs no refinement and ignores it
+    refine_projection: int = 1
 
     def drag_cd(self, grid: Grid) -> float:
         return drag_coefficient(self.surface, 2 * float(grid.hz[0])) if self.drag else 0.0

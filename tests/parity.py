@@ -74,3 +74,28 @@ def dual_divergence(u, v, w, grid, rho):
     ddy = (r0 * (sy(V)[lo] + sx(sy(V))[lo] - V[lo] - sx(V)[lo]) + r1 * (sy(V)[hi] + sx(sy(V))[hi] - V[hi] - sx(V)[hi])) / grid.dy
     ddz = (r1 * (W[hi] + sx(W)[hi] + sy(W)[hi] + sx(sy(W))[hi]) - r0 * (W[lo] + sx(W)[lo] + sy(W)[lo] + sx(sy(W))[lo])) / dz
     return ddx + ddy + ddz
+
+
+def pressure_gradient(p, grid):
+    """G p at the nodes from the dual-cell pressure (nx*ny*(nz-1), cell k between nodes k and k+1), FP64: the
+    gradient of PressureSolver.correct (src/core/pressure.ts:69-92) - x and y from the four cells around each of the
+    two neighbouring layers weighted by the spacings, z between the cell layers below and above; none at the ground and
+    the top for z."""
+    nx, ny, nz = grid.nx, grid.ny, grid.nz
+    P = np.asarray(p, np.float64).reshape(nz - 1, ny, nx)
+    hz, dzs = np.asarray(grid.hz, np.float64), np.asarray(grid.dzs, np.float64)
+    sx = lambda a: np.roll(a, 1, axis=2)   # the cell at x - 1
+    sy = lambda a: np.roll(a, 1, axis=1)   # at y - 1
+    k = np.arange(nz)
+    lo, hi = P[np.maximum(0, k - 1)], P[np.minimum(nz - 2, k)]
+    wlo = np.where(k > 0, dzs[np.maximum(0, k - 1)] / hz, 0.0)[:, None, None]
+    whi = np.where(k < nz - 1, dzs[np.minimum(nz - 2, k)] / hz, 0.0)[:, None, None]
+    dx4 = lambda a: (sy(a) - sx(sy(a))) + (a - sx(a))      # (x, jm) - (im, jm) + (x, j0) - (im, j0)
+    dy4 = lambda a: (sx(a) - sx(sy(a))) + (a - sy(a))      # (im, j0) - (im, jm) + (x, j0) - (x, jm)
+    gx = (wlo * dx4(lo) + whi * dx4(hi)) * (0.25 / grid.dx)
+    gy = (wlo * dy4(lo) + whi * dy4(hi)) * (0.25 / grid.dy)
+    c4 = lambda a: a + sx(a) + sy(a) + sx(sy(a))
+    gz = np.zeros((nz, ny, nx))
+    kk = np.arange(1, nz - 1)
+    gz[kk] = (c4(P[kk]) - c4(P[kk - 1])) * (0.25 / hz[kk])[:, None, None]
+    return gx.ravel(), gy.ravel(), gz.ravel()

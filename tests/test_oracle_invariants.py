@@ -103,3 +103,24 @@ def test_water_is_conserved_within_001_percent_in_a_30_minute_storm_with_ice(sto
     assert float(np.max(m.get("ice"))) > 1e-6
     assert float(np.max(m.get("graupel"))) > 1e-4
     assert abs(total_water(m, spec) / before - 1) < 1e-4
+
+
+def test_numpy_gradient_and_divergence_restate_the_projection():
+    """The FP64 operators the divergence checks use (parity.dual_divergence, parity.pressure_gradient) are the
+    projection's own: applied to the oracle's pressure they leave the oracle's velocities divergence-free."""
+    from parity import pressure_gradient
+    grid = create_grid(GridOptions(16, 12, 20, 16 * 1200.0, 12 * 1125.0, 15_000.0, 100.0))
+    rho = O.f64(quiet_run(grid).env.rho)
+    rng = np.random.default_rng(5)
+    u, v, w = ((rng.random(grid.n) - 0.5).astype(np.float32) * 10 for _ in range(3))
+    w[:grid.layer] = 0; w[grid.n - grid.layer:] = 0
+    u0, v0, w0 = u.copy(), v.copy(), w.copy()
+    cells = grid.layer * (grid.nz - 1)
+    d0, d1, p = np.empty(cells), np.empty(cells), np.empty(cells)
+    args, keep = O.grid_args(grid)
+    dt = 1.0
+    O.lib().orc_pressure_project(*args, O.dp(rho), O.fp(u), O.fp(v), O.fp(w), dt, O.dp(d0), O.dp(d1), O.dp(p))
+    gx, gy, gz = pressure_gradient(p, grid)
+    div0 = dual_divergence(u0, v0, w0, grid, rho)
+    div = dual_divergence(u0 - dt * gx, v0 - dt * gy, w0 - dt * gz, grid, rho)
+    assert np.max(np.abs(div)) < 1e-10 * np.max(np.abs(div0))
