@@ -54,7 +54,7 @@ KERNEL_BYTES_PER_CELL = {
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--steps", type=int, default=100)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--members", type=int, default=MEMBERS)
@@ -331,14 +331,14 @@ def main():
     tpc = traffic_per_cell()
     launches_per_step = sum(v[1] for v in prof.values())
 
-    # ---- e2e through the C ABI with pinned host buffers: write all fields, step, read all fields, every step
-    pinned = [{k: torch.empty(r.grid.n, dtype=torch.float32, pin_memory=True).numpy() for k in CARRIED} for r in runs]
-    for r, buf in zip(runs, pinned):
-        r.read(out=buf)
+    # ---- e2e through the C ABI with a pinned host buffer: write all fields of all runs, step, read them all back,
+    # every step (the packed batch transfer: one copy each way)
+    packed = torch.empty(cells * len(CARRIED), dtype=torch.float32, pin_memory=True).numpy()
+    ctx.read_packed(runs, packed)
     def e2e_step():
-        ctx.write_fields(runs, pinned)
+        ctx.write_packed(runs, packed)
         ctx.batch_step(runs, 1, wait=False)
-        ctx.read_fields(runs, pinned)
+        ctx.read_packed(runs, packed)
     for _ in range(2):
         e2e_step()
     e2e_n = max(3, args.steps // 4)

@@ -107,6 +107,12 @@ int sg_run_read_fields(sg_context* ctx, sg_run run, uint32_t mask, float* const*
  * runner that reads every member between samples (src/ensemble/member.ts:101-107). */
 int sg_batch_write_fields(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, const float* const* host);
 int sg_batch_read_fields(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, float* const* host);
+/* The same with one host buffer: `host` holds, run after run in the order of `runs`, the mask's fields in sg_field
+ * order, nx*ny*nz FP32 values each (theta as the full potential temperature). One host<->device copy of the whole
+ * buffer through a device staging buffer the context keeps, one kernel placing or gathering the fields, one
+ * synchronisation: the fastest way to move a batch's state (pinned host memory moves at link speed). */
+int sg_batch_write_packed(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, const float* host);
+int sg_batch_read_packed(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, float* host);
 /* precipitation, hailGround, hailSize: nx*ny each (nullable); src/core/model.ts:253, :262. */
 int sg_run_read_columns(sg_context* ctx, sg_run run, float* precipitation, float* hail_ground, float* hail_size);
 /* The projection pressure of the last final projection, nx*ny*(nz-1) values (AtmosphereModel.pressure, :247). */

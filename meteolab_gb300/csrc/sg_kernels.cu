@@ -966,7 +966,6 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
       lv[6 * MAXNZ + z] = lvl(Rg, L_THB, z); lv[7 * MAXNZ + z] = lvl(Rg, L_QB, z); lv[8 * MAXNZ + z] = lvl(Rg, L_THVENV, z);
     }
   }
-  // plane cells of this thread as column offsets (periodic)
   // plane cell t + j * NT of this thread: its column offset (periodic), -1 past the plane
   const int NT = blockDim.x;
   int off[TMAXC];
@@ -1499,9 +1498,32 @@ __global__ void k_divergence_max(const RunDesc* __restrict__ runs, const int4* i
   }
 }
 
+// ==================================================================== packed field transfer
+// Moves fields between the runs and one staging buffer that holds, run after run, the selected fields in field
+// order (the host copies the whole buffer at once). Item (slot, field, chunk, staging offset of the chunk); theta
+// crosses as the full potential temperature (FP64 difference with the base profile).
+__global__ void k_pack(const RunDesc* __restrict__ runs, const int4* items, int nitems, float* staging, int write) {
+  FOR_ITEMS {
+    const int4 w = items[it];
+    const RunDesc& R = runs[w.x];
+    const int i0 = w.z * CHUNK, i1 = min(R.n, i0 + CHUNK);
+    float* f = field(R, 0, w.y);
+    float* s = staging + (size_t)(unsigned)w.w;
+    const double* thb = R.lv64 + (size_t)D_THB * R.nz;
+    if (write) {
+      if (w.y == THETA) for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) f[i] = (float)((double)s[i - i0] - thb[i / R.layer]);
+      else for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) f[i] = s[i - i0];
+    } else {
+      if (w.y == THETA) for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) s[i - i0] = (float)((double)f[i] + thb[i / R.layer]);
+      else for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) s[i - i0] = f[i];
+    }
+  }
+}
+
 // ==================================================================== launchers
 #define GRID(n, cap) dim3(max(1, min((n), (cap))))
 
+void launch_pack(const Launch& L, float* staging, int write) { k_pack<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, staging, write); }
 void launch_theta_in(const Launch& L, const float* src) { k_theta_in<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, src); }
 void launch_theta_out(const Launch& L, float* dst) { k_theta_out<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, dst); }
 void launch_fall_courant(const Launch& L) { k_fall_courant<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n); }
@@ -1569,19 +1591,27 @@ void launch_mix(const Launch& L, int in, int TX, int TY) {
 void launch_step_end(const Launch& L) { k_step_end<<<GRID(L.n, L.cap), 64, 0, L.stream>>>(L.runs, L.items, L.n); }
 void launch_divergence_max(const Launch& L, int set, double* out) { k_divergence_max<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set, out); }
 
+// Opt every kernel with dynamic shared memory in to the device's per-block maximum, less its static shared memory.
+template <class K>
+cudaError_t smem_limit(K kernel, int bytes) {
+  cudaFuncAttributes attr;
+  cudaError_t e = cudaFuncGetAttributes(&attr, kernel);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes - (int)attr.sharedSizeBytes);
+}
 cudaError_t set_smem_limits(int bytes) {
   cudaError_t e;
-  if ((e = cudaFuncSetAttribute(k_proj_modes, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(k_proj_div_xfft, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(k_proj_xifft, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(k_sediment, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(k_proj_div_fft2, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(k_proj_ifft2, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(k_transport<TK_WENO, 3, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(k_transport<TK_WENO, 3, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(k_transport<TK_WENO, 1, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(k_transport<TK_WENO, 1, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(k_transport<TK_DYN, 4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess) return e;
+  if ((e = smem_limit(k_proj_modes, bytes)) != cudaSuccess) return e;
+  if ((e = smem_limit(k_proj_div_xfft, bytes)) != cudaSuccess) return e;
+  if ((e = smem_limit(k_proj_xifft, bytes)) != cudaSuccess) return e;
+  if ((e = smem_limit(k_sediment, bytes)) != cudaSuccess) return e;
+  if ((e = smem_limit(k_proj_div_fft2, bytes)) != cudaSuccess) return e;
+  if ((e = smem_limit(k_proj_ifft2, bytes)) != cudaSuccess) return e;
+  if ((e = smem_limit(k_transport<TK_WENO, 3, 2>, bytes)) != cudaSuccess) return e;
+  if ((e = smem_limit(k_transport<TK_WENO, 3, 3>, bytes)) != cudaSuccess) return e;
+  if ((e = smem_limit(k_transport<TK_WENO, 1, 2>, bytes)) != cudaSuccess) return e;
+  if ((e = smem_limit(k_transport<TK_WENO, 1, 3>, bytes)) != cudaSuccess) return e;
+  if ((e = smem_limit(k_transport<TK_DYN, 4, 2>, bytes)) != cudaSuccess) return e;
   return cudaSuccess;
 }
 

@@ -17,6 +17,9 @@ struct Launch {
   cudaStream_t stream;
 };
 
+// Packed field transfer between the runs and a staging buffer (write = 1: staging -> runs); items (slot, field, chunk,
+// staging offset).
+void launch_pack(const Launch& L, float* staging, int write);
 void launch_theta_in(const Launch& L, const float* src);
 void launch_theta_out(const Launch& L, float* dst);
 void launch_fall_courant(const Launch& L);

@@ -103,6 +103,10 @@ struct sg_context {
   bool rowsOnly = false;                // row-transform spectral path for every grid (SG_SPECTRAL_ROWS=1)
   int pinned[4] = {0, 0, 0, 2};         // transport tile, WENO group, blocks per SM fixed by the caller (TX = 0: tune)
   std::map<std::vector<int>, std::array<int, 4>> tuning;  // batch signature -> (TX, TY, wenoG, minb)
+  // packed transfers: a device staging buffer (grown on demand) and the item lists per (runs, mask)
+  float* staging = nullptr;
+  size_t stagingBytes = 0;
+  std::map<std::vector<int>, std::pair<int4*, int>> packs;
 };
 
 namespace {
@@ -530,6 +534,13 @@ int ensure_graph(sg_context* ctx, Plan& P) {
   return SG_OK;
 }
 
+void drop_packs_with(sg_context* ctx, int slot) {
+  for (auto it = ctx->packs.begin(); it != ctx->packs.end();) {
+    if (std::find(it->first.begin(), it->first.end() - 1, slot) != it->first.end() - 1) { cudaFree(it->second.first); it = ctx->packs.erase(it); }
+    else ++it;
+  }
+}
+
 void drop_plans_with(sg_context* ctx, int slot) {
   for (auto it = ctx->plans.begin(); it != ctx->plans.end();) {
     if (std::find(it->first.begin(), it->first.end(), slot) != it->first.end()) it = ctx->plans.erase(it);
@@ -612,6 +623,8 @@ int sg_context_destroy(sg_context* ctx) {
   cudaFree(ctx->d_runs); cudaFree(ctx->d_scalar);
   cudaStreamDestroy(ctx->stream);
   for (int k = 0; k < 3; k++) { cudaStreamDestroy(ctx->side[k]); cudaEventDestroy(ctx->join[k]); }
+  for (auto& p : ctx->packs) cudaFree(p.second.first);
+  if (ctx->staging) cudaFree(ctx->staging);
   cudaEventDestroy(ctx->fork);
   delete ctx;
   return SG_OK;
@@ -746,6 +759,59 @@ int batch_fields(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, floa
   return SG_OK;
 }
 
+// Fields of many runs packed run after run (the mask's fields in field order, n nodes each) through one staging
+// buffer: one host copy, one kernel, one synchronisation. The packing follows the caller's order of the runs.
+int batch_packed(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, float* host, bool write) {
+  if (!ctx || !host) return SG_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  std::vector<int> key;
+  int st = slots_of(ctx, runs, n, key);
+  if (st != SG_OK) return st;
+  key.push_back((int)mask);
+  size_t total = 0;
+  for (int k = 0; k < n; k++) {
+    const Run* r = find(ctx, runs[k]);
+    for (int f = 0; f < NF; f++) if (mask & (1u << f)) total += (size_t)r->nx * r->ny * r->nz;
+  }
+  if (total >= (1ull << 31)) return fail(ctx, SG_ERR_INVALID, "packed batch too large");
+  auto it = ctx->packs.find(key);
+  if (it == ctx->packs.end()) {
+    std::vector<int4> items;
+    size_t off = 0;
+    for (int k = 0; k < n; k++) {
+      const Run* r = find(ctx, runs[k]);
+      const int nn = r->nx * r->ny * r->nz;
+      for (int f = 0; f < NF; f++) {
+        if (!(mask & (1u << f))) continue;
+        for (int c = 0; c * CHUNK < nn; c++) items.push_back(make_int4(runs[k], f, c, (int)(off + (size_t)c * CHUNK)));
+        off += nn;
+      }
+    }
+    int4* d = nullptr;
+    CK(cudaMalloc(&d, items.size() * sizeof(int4)));
+    CK(cudaMemcpy(d, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    if (ctx->packs.size() > 64) { for (auto& p : ctx->packs) cudaFree(p.second.first); ctx->packs.clear(); }
+    it = ctx->packs.emplace(key, std::make_pair(d, (int)items.size())).first;
+  }
+  if (ctx->stagingBytes < total * 4) {
+    if (ctx->staging) cudaFree(ctx->staging);
+    ctx->staging = nullptr; ctx->stagingBytes = 0;
+    CK(cudaMalloc(&ctx->staging, total * 4));
+    ctx->stagingBytes = total * 4;
+  }
+  Launch L{ctx->d_runs, it->second.first, it->second.second, ctx->sms * 8, ctx->stream};
+  if (write) {
+    CK(cudaMemcpyAsync(ctx->staging, host, total * 4, cudaMemcpyHostToDevice, ctx->stream));
+    launch_pack(L, ctx->staging, 1);
+  } else {
+    launch_pack(L, ctx->staging, 0);
+    CK(cudaMemcpyAsync(host, ctx->staging, total * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaGetLastError());
+  return SG_OK;
+}
+
 int sg_run_read_columns(sg_context* ctx, sg_run run, float* precipitation, float* hail_ground, float* hail_size) {
   if (!ctx) return SG_ERR_INVALID;
   Run* r = find(ctx, run);
@@ -790,6 +856,12 @@ int sg_batch_write_fields(sg_context* ctx, const sg_run* runs, int n, uint32_t m
 int sg_batch_read_fields(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, float* const* host) {
   return batch_fields(ctx, runs, n, mask, host, false);
 }
+int sg_batch_write_packed(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, const float* host) {
+  return batch_packed(ctx, runs, n, mask, const_cast<float*>(host), true);
+}
+int sg_batch_read_packed(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, float* host) {
+  return batch_packed(ctx, runs, n, mask, host, false);
+}
 
 int sg_run_retire(sg_context* ctx, sg_run run) {
   if (!ctx) return SG_ERR_INVALID;
@@ -797,6 +869,7 @@ int sg_run_retire(sg_context* ctx, sg_run run) {
   if (!r) return fail(ctx, SG_ERR_NOT_FOUND, "no run " + std::to_string(run));
   cudaStreamSynchronize(ctx->stream);
   drop_plans_with(ctx, run);
+  drop_packs_with(ctx, run);
   ctx->used -= r->bytes;
   ctx->pool.emplace(r->bytes, r->mem); ctx->pooled += r->bytes;
   r->live = false; r->mem = nullptr;

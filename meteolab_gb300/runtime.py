@@ -91,6 +91,8 @@ def load():
             L.sg_debug_read_faces.argtypes = [vp, C.c_int32, _FP]
             L.sg_batch_write_fields.argtypes = [vp, C.POINTER(C.c_int32), i32, C.c_uint32, C.POINTER(_FP)]
             L.sg_batch_read_fields.argtypes = [vp, C.POINTER(C.c_int32), i32, C.c_uint32, C.POINTER(_FP)]
+            L.sg_batch_write_packed.argtypes = [vp, C.POINTER(C.c_int32), i32, C.c_uint32, _FP]
+            L.sg_batch_read_packed.argtypes = [vp, C.POINTER(C.c_int32), i32, C.c_uint32, _FP]
             L.sg_set_transport_shape.argtypes = [vp, i32, i32, i32]
             L.sg_divergence_max_static.argtypes = [i32, vp, vp, vp, i32, i32, i32, C.c_double, C.c_double, C.POINTER(C.c_double),
                                                    C.POINTER(C.c_double), vp, C.POINTER(C.c_double), C.c_char_p, C.c_size_t]
@@ -198,6 +200,26 @@ class Context:
     def read_fields(self, runs: Sequence["Run"], out: Sequence[Dict[str, np.ndarray]], names: Iterable[str] = CARRIED):
         """Read the fields of many runs into the caller's float32 arrays in one call."""
         self._batch_io(runs, out, names, False)
+
+    def _mask(self, names) -> int:
+        m = 0
+        for k in names:
+            m |= 1 << CARRIED.index(k)
+        return m
+
+    def write_packed(self, runs: Sequence["Run"], packed: np.ndarray, names: Iterable[str] = CARRIED):
+        """Write the fields of many runs from one buffer: run after run, the named fields in field order."""
+        if packed.dtype != np.float32 or not packed.flags.c_contiguous:
+            raise ValueError("packed buffer must be contiguous float32")
+        ids = (C.c_int32 * len(runs))(*[r.id for r in runs])
+        self.check(load().sg_batch_write_packed(self.h, ids, len(runs), self._mask(names), packed.ctypes.data_as(_FP)), "write packed")
+
+    def read_packed(self, runs: Sequence["Run"], packed: np.ndarray, names: Iterable[str] = CARRIED):
+        """Read the fields of many runs into one buffer (the layout of write_packed)."""
+        if packed.dtype != np.float32 or not packed.flags.c_contiguous:
+            raise ValueError("packed buffer must be contiguous float32")
+        ids = (C.c_int32 * len(runs))(*[r.id for r in runs])
+        self.check(load().sg_batch_read_packed(self.h, ids, len(runs), self._mask(names), packed.ctypes.data_as(_FP)), "read packed")
 
     def set_transport_shape(self, tile_x: int = 0, tile_y: int = 0, weno_group: int = 3):
         """Pin the transport tile (tile_x x tile_y columns, 1 or 3 WENO fields per item); tile_x = 0 returns to tuning."""

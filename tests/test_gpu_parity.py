@@ -218,6 +218,38 @@ def test_batch_field_io_matches_per_run_calls(ctx, storm):
         r.retire()
 
 
+def test_packed_transfer_matches_per_run_calls(ctx, storm):
+    runs = [ctx.create(storm), ctx.create(baseline_run(create_grid(LARGE_GRID), seed=9))]
+    ctx.batch_step(runs, 2)
+    total = sum(r.grid.n for r in runs) * len(CARRIED)
+    packed = np.empty(total, np.float32)
+    ctx.read_packed(runs, packed)
+    o = 0
+    for r in runs:
+        f = r.read()
+        for k in CARRIED:
+            assert np.array_equal(packed[o:o + r.grid.n], f[k]), k
+            o += r.grid.n
+    # write a changed state packed, read it back per run (theta through its departure: FP32-close)
+    packed2 = packed.copy()
+    packed2[:runs[0].grid.n] += np.float32(1e-4)  # the first run's rain
+    ctx.write_packed(runs, packed2)
+    back = np.empty_like(packed2)
+    ctx.read_packed(runs, back)
+    th = [i for i, k in enumerate(CARRIED) if k == "theta"][0]
+    o = 0
+    for r in runs:
+        for j, k in enumerate(CARRIED):
+            a, b = back[o:o + r.grid.n], packed2[o:o + r.grid.n]
+            if j == th:
+                assert np.max(np.abs(a - b)) < 1e-4
+            else:
+                assert np.array_equal(a, b), k
+            o += r.grid.n
+    for r in runs:
+        r.retire()
+
+
 def test_autotuner_picks_a_valid_shape(ctx, storm):
     runs = [ctx.create(storm) for _ in range(4)]
     tx, ty, g, mb = ctx.transport_shape(runs)
