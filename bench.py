@@ -49,6 +49,10 @@ KERNEL_BYTES_PER_CELL = {
     "refine_nodes": 16 + 24, "refine_div": 24 + 4, "refine_div_xfft": 4 + 4.2, "refine_modes": 8.4 + 12.6,
     "refine_xifft": 4.2 + 4, "refine_correct": 28 + 12,
 }
+# Algorithmic bytes of one whole step per cell, pass by pass (each global pass reads its inputs once and writes its
+# outputs once, FP32 4 B): sedimentation 32, face projection 72, RK3 transport 464, three pressure projections 252,
+# positivity rescale 64, physics 104, viscosity 36, mixing and drag 72.
+STEP_BYTES_PER_CELL = 32 + 72 + 464 + 252 + 64 + 104 + 36 + 72
 
 
 def parse():
@@ -386,6 +390,8 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm if achieved else None,
                      "traffic": tpc * cells if tpc else None, "kernel": "k_transport<WENO> (9 fields, one RK3 stage)", "peak_kind": peak_kind,
                      "bytes_per_cell_per_launch": TRANSPORT_BYTES_PER_CELL},
+        "step_roofline": {"bytes_per_cell_step": STEP_BYTES_PER_CELL, "achieved": value / world * STEP_BYTES_PER_CELL / 1e9,
+                          "peak": hbm, "unit": "GB/s", "frac": value / world * STEP_BYTES_PER_CELL / 1e9 / hbm},
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
         "plain_single_run": plain,

@@ -912,6 +912,11 @@ __device__ __forceinline__ void cp_async4(float* dst, const float* src) {
   const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
 }
+// 16-byte asynchronous copy (both addresses 16-byte aligned), not cached in L1
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 // The upwind stencil of a face along one axis (stride s) whose low-side cell is at P[-1] and high-side cell at P[0]:
@@ -930,19 +935,21 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
   const int flags = Rg.flags;
   const float4* __restrict__ F4 = reinterpret_cast<const float4*>(Rg.faces);
   const float* __restrict__ inb = Rg.fld + (size_t)in_set * NF * n;   // the input set (buoyancy)
-  const float* q[G];
-  const float* st[G];
-  float* out[G];
+  // the group's fields as 32-bit element offsets from the run's field block (input set, step-start set A, output
+  // set): fewer live registers than a pointer per field and set
+  float* const fld = Rg.fld;
+  int fo[G];
 #pragma unroll
-  for (int g = 0; g < G; g++) {
-    const int f = TGROUP[group][g];
-    q[g] = Rg.fld + ((size_t)in_set * NF + f) * n;
-    st[g] = Rg.fld + (size_t)f * n;
-    out[g] = Rg.fld + ((size_t)out_set * NF + f) * n;
-  }
+  for (int g = 0; g < G; g++) fo[g] = TGROUP[group][g] * (int)n;
+  const int qo = in_set * NF * (int)n, oo = out_set * NF * (int)n;
+#define QP(g) (fld + qo + fo[g])
+#define SP(g) (fld + fo[g])
+#define OP(g) (fld + oo + fo[g])
   const int PW = TX + 6, PH = TY + 6, NCELL = PW * PH;
+  const int NT = blockDim.x;
   float* lv = sm;                                   // [tlv_rows][MAXNZ]
-  float* ring = lv + tlv_rows(KIND) * MAXNZ;        // [G][7][NCELL]
+  float4* fcs = reinterpret_cast<float4*>(lv + tlv_rows(KIND) * MAXNZ);  // [2][NT]: the face fluxes of levels z, z + 1
+  float* ring = reinterpret_cast<float*>(fcs + 2 * NT);  // [G][7][NCELL]
   float* fxs = ring + G * 7 * NCELL;                // [2][G][TY][TX + 1]: x faces, west edge at column 0
   float* fys = fxs + 2 * G * TY * (TX + 1);         // [2][G][TY + 1][TX]: y faces, south edge at row 0
   const int FXS = TY * (TX + 1), FYS = (TY + 1) * TX;
@@ -967,7 +974,6 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
     }
   }
   // plane cell t + j * NT of this thread: its column offset (periodic), -1 past the plane
-  const int NT = blockDim.x;
   int off[TMAXC];
 #pragma unroll
   for (int j = 0; j < TMAXC; j++) {
@@ -985,18 +991,21 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
 #pragma unroll
     for (int g = 0; g < G; g++)
 #pragma unroll
-      for (int j = 0; j < TMAXC; j++) if (off[j] >= 0) ring[(g * 7 + slot) * NCELL + t + j * NT] = q[g][off[j] + lev * layer];
+      for (int j = 0; j < TMAXC; j++) if (off[j] >= 0) ring[(g * 7 + slot) * NCELL + t + j * NT] = QP(g)[off[j] + lev * layer];
   }
-  float4 fc = on ? F4[col] : make_float4(0.f, 0.f, 0.f, 0.f);
+  if (on) cp_async16(fcs + t, F4 + col);
   float me = edgeW ? F4[eoff].x : edgeS ? F4[eoff].y : 0.f;
   float s0[G];
 #pragma unroll
-  for (int g = 0; g < G; g++) s0[g] = on && stage > 0 ? st[g][col] : 0.f;
-  float b[8];
-#pragma unroll
-  for (int j = 0; j < 8; j++) b[j] = 0.f;
-  if (loadBuoy && on) { b[0] = inb[THETA * n + col]; b[1] = inb[Q * n + col]; b[2] = inb[CLOUD * n + col]; b[3] = inb[ICE * n + col];
-    if (loading) { b[4] = inb[RAIN * n + col]; b[5] = inb[SNOW * n + col]; b[6] = inb[GRAUPEL * n + col]; b[7] = inb[HAIL * n + col]; } }
+  for (int g = 0; g < G; g++) s0[g] = on && stage > 0 ? SP(g)[col] : 0.f;
+  // buoyancy inputs of the level (dynamics): the vapour and the condensate load (theta' is the ring's centre value)
+  float bQ = 0.f, bL = 0.f;
+  if (loadBuoy && on) {
+    bQ = inb[Q * n + col];
+    bL = inb[CLOUD * n + col] + inb[ICE * n + col] +
+         (loading ? (inb[RAIN * n + col] + inb[SNOW * n + col]) + (inb[GRAUPEL * n + col] + inb[HAIL * n + col]) : 0.f);
+  }
+  cp_async_wait_all();
   __syncthreads();
   float fzD[G];
 #pragma unroll
@@ -1014,27 +1023,28 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
 #pragma unroll
     for (int g = 0; g < G; g++)
 #pragma unroll
-      for (int j = 0; j < TMAXC; j++) if (off[j] >= 0) cp_async4(ring + (g * 7 + s_new) * NCELL + t + j * NT, q[g] + off[j] + levNext);
-    float4 fcn = make_float4(0.f, 0.f, 0.f, 0.f);
-    float men = 0.f, s0n[G], bn[8];
+      for (int j = 0; j < TMAXC; j++) if (off[j] >= 0) cp_async4(ring + (g * 7 + s_new) * NCELL + t + j * NT, QP(g) + off[j] + levNext);
+    float men = 0.f, s0n[G], bn[7];
 #pragma unroll
     for (int g = 0; g < G; g++) s0n[g] = 0.f;
 #pragma unroll
-    for (int j = 0; j < 8; j++) bn[j] = 0.f;
+    for (int j = 0; j < 7; j++) bn[j] = 0.f;
     if (more) {
       if (edgeW) men = F4[eoff + ln].x;
       if (edgeS) men = F4[eoff + ln].y;
       if (on) {
-        fcn = F4[col + ln];
+        cp_async16(fcs + (buf ^ 1) * NT + t, F4 + col + ln);
         if (stage > 0) {
 #pragma unroll
-          for (int g = 0; g < G; g++) s0n[g] = st[g][col + ln];
+          for (int g = 0; g < G; g++) s0n[g] = SP(g)[col + ln];
         }
-        if (loadBuoy) { bn[0] = inb[THETA * n + col + ln]; bn[1] = inb[Q * n + col + ln]; bn[2] = inb[CLOUD * n + col + ln]; bn[3] = inb[ICE * n + col + ln];
-          if (loading) { bn[4] = inb[RAIN * n + col + ln]; bn[5] = inb[SNOW * n + col + ln]; bn[6] = inb[GRAUPEL * n + col + ln]; bn[7] = inb[HAIL * n + col + ln]; } }
+        if (loadBuoy) { bn[0] = inb[Q * n + col + ln]; bn[1] = inb[CLOUD * n + col + ln]; bn[2] = inb[ICE * n + col + ln];
+          if (loading) { bn[3] = inb[RAIN * n + col + ln]; bn[4] = inb[SNOW * n + col + ln]; bn[5] = inb[GRAUPEL * n + col + ln]; bn[6] = inb[HAIL * n + col + ln]; } }
       }
     }
-    // faces of level z
+    // faces of level z (slot buf is read only before this level's barrier and rewritten after it, by the next
+    // level's copies)
+    const float4 fc = on ? fcs[buf * NT + t] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float m1 = fc.x, m2 = fc.y, m3 = fc.z;
     const bool px = m1 >= 0.f, py = m2 >= 0.f, pz = m3 >= 0.f, top = z == nz - 1;
     const int s_m2 = (z + 5) % 7, s_m1 = (z + 6) % 7, s_0 = z % 7, s_p1 = (z + 1) % 7, s_p2 = (z + 2) % 7, s_p3 = (z + 3) % 7;
@@ -1089,6 +1099,8 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
         }
       }
     }
+    // the next level's buoyancy inputs reduced to two values before the barrier
+    const float bnQ = bn[0], bnL = bn[1] + bn[2] + (loading ? (bn[3] + bn[4]) + (bn[5] + bn[6]) : 0.f);
     cp_async_wait_all();
     __syncthreads();
     if (on) {
@@ -1107,24 +1119,25 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
         if (KIND == TK_DYN && g == 2 && loadBuoy) {
           // g B with theta' and the base state (stageBuoyancy): theta_v - theta_v,env from small differences.
           const float Rb = lv[6 * MAXNZ + z], Qb = lv[7 * MAXNZ + z];
-          float dth = b[0], num = dth + .61f * ((Rb + dth) * (b[1] - Qb) + Qb * dth);
-          float loaded = b[2] + b[3] + (loading ? (b[4] + b[5]) + (b[6] + b[7]) : 0.f);
-          tend += 9.81f * (num / lv[8 * MAXNZ + z] - loaded);
+          float dth = qc[3], num = dth + .61f * ((Rb + dth) * (bQ - Qb) + Qb * dth);
+          tend += 9.81f * (num / lv[8 * MAXNZ + z] - bL);
         }
         float a = (stage == 0 ? qc[g] : s0[g]) + fdt * tend;
         if (KIND == TK_DYN && g == 2 && stage < 2 && (flags & RF_STAGES) && (z == 0 || z == nz - 1)) a = 0.f;
-        out[g][col + l] = a;
+        OP(g)[col + l] = a;
         fzD[g] = fzU[g];
       }
     }
     mzD = m3;
-    fc = fcn; me = men;
+    me = men;
 #pragma unroll
     for (int g = 0; g < G; g++) s0[g] = s0n[g];
-#pragma unroll
-    for (int j = 0; j < 8; j++) b[j] = bn[j];
+    bQ = bnQ; bL = bnL;
   }
   __syncthreads();
+#undef QP
+#undef SP
+#undef OP
 }
 
 // MINB: resident blocks per SM the register budget is cut for (2: up to 96 registers a thread, 3: 64).
@@ -1564,7 +1577,7 @@ void launch_refine_div(const Launch& L) { k_refine_div<<<GRID(L.n, L.cap), 256, 
 void launch_refine_correct(const Launch& L, int set) { k_refine_correct<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set); }
 void launch_pres_correct(const Launch& L, int set, int final_) { k_pres_correct<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set, final_); }
 size_t transport_smem(int kind, int G, int TX, int TY) {
-  return ((size_t)tlv_rows(kind) * MAXNZ + (size_t)G * 7 * (TX + 6) * (TY + 6) + 2 * (size_t)G * TY * (TX + 1) + 2 * (size_t)G * (TY + 1) * TX) * sizeof(float);
+  return ((size_t)tlv_rows(kind) * MAXNZ + 2 * 4 * (size_t)TX * TY + (size_t)G * 7 * (TX + 6) * (TY + 6) + 2 * (size_t)G * TY * (TX + 1) + 2 * (size_t)G * (TY + 1) * TX) * sizeof(float);
 }
 #define TLAUNCH(K, G, M) k_transport<K, G, M><<<g, TX * TY, transport_smem(K, G, TX, TY), L.stream>>>(L.runs, L.items, L.n, in_set, out_set, frac, stage, TX, TY)
 void launch_transport(const Launch& L, int kind, int group, int minb, int in_set, int out_set, float frac, int stage, int TX, int TY) {

@@ -263,6 +263,8 @@ int validate(sg_context* ctx, const sg_grid* g, const sg_base_state* b, const sg
   if (g->nx < 1 || g->ny < 1 || g->nz < 3) return fail(ctx, SG_ERR_INVALID, "grid needs nx, ny >= 1 and nz >= 3");
   if (g->nz > 128) return fail(ctx, SG_ERR_UNSUPPORTED, "nz > 128 levels");
   if (g->nx > 4096 || g->ny > 4096) return fail(ctx, SG_ERR_UNSUPPORTED, "nx or ny > 4096");
+  // the kernels index a run's field sets with 32-bit element offsets
+  if ((size_t)g->nx * g->ny * g->nz * 3 * NF >= (1ull << 31)) return fail(ctx, SG_ERR_UNSUPPORTED, "grid beyond 55 million nodes");
   int rad[8];
   if (fft_plan_factors(g->nx, rad) < 0 || fft_plan_factors(g->ny, rad) < 0) return fail(ctx, SG_ERR_UNSUPPORTED, "nx or ny has more than 8 prime factors");
   if (!(g->dx > 0 && g->dy > 0 && g->height > 0) || !g->zs || !g->dzs || !g->hz) return fail(ctx, SG_ERR_INVALID, "bad grid spacing or levels");
