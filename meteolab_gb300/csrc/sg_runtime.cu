@@ -95,10 +95,10 @@ struct sg_context {
   uint64_t pooled = 0;
   std::string error;
   double* d_scalar = nullptr;           // scratch for reductions read back by the host
-  // The two transport kinds of an RK3 stage (WENO fields, dynamics) run as parallel branches of the step's graph.
-  cudaStream_t side[3] = {nullptr, nullptr, nullptr};
-  cudaEvent_t fork = nullptr, join[3] = {nullptr, nullptr, nullptr};
-  bool forking = false;                 // set while a step is captured into a graph
+  // Independent chains of the step (sedimentation, the WENO transport) run on a side stream as parallel branches
+  // of the step's graph; dep[] are the events between the branches.
+  cudaStream_t side[2] = {nullptr, nullptr};
+  cudaEvent_t dep[8] = {};
   bool autotune = true;
   bool rowsOnly = false;                // row-transform spectral path for every grid (SG_SPECTRAL_ROWS=1)
   int pinned[4] = {0, 0, 0, 2};         // transport tile, WENO group, blocks per SM fixed by the caller (TX = 0: tune)
@@ -361,19 +361,15 @@ Launch lx(sg_context* ctx, const Plan& P, int fam, int capPerSm = 8) {
 
 // Transport launches: one block per item, so the hardware block scheduler balances items of uneven cost (tiles of
 // empty air skip their WENO weights) across the SMs.
-void launch_transport_kinds(sg_context* ctx, const Plan& P, int in, int out, float frac, int stage, bool fork, int hookBase,
+void launch_transport_kinds(sg_context* ctx, const Plan& P, int in, int out, float frac, int stage, int hookBase,
                             const std::function<void(int)>& hook) {
   const int fams[2] = {FAM_T_WENO, FAM_T_DYN};
-  if (fork) cudaEventRecord(ctx->fork, ctx->stream);
   for (int k = 0; k < 2; k++) {
     Launch L = lx(ctx, P, fams[k]);
     L.cap = L.n;
-    if (fork && k > 0) { cudaStreamWaitEvent(ctx->side[0], ctx->fork, 0); L.stream = ctx->side[0]; }
     if (L.n) launch_transport(L, k, P.wenoG, P.minb, in, out, frac, stage, P.TX, P.TY);
-    if (fork && k > 0) cudaEventRecord(ctx->join[0], ctx->side[0]);
     hook(hookBase + k);
   }
-  if (fork) cudaStreamWaitEvent(ctx->stream, ctx->join[0], 0);
 }
 
 // Picks the transport tile (TX x TY columns) and WENO fields per item by timing every candidate on the plan's own
@@ -417,7 +413,7 @@ int autotune_transport(sg_context* ctx, Plan& P) {
         float ms = 1e30f;
         for (int rep = 0; rep < 4; rep++) {
           cudaEventRecord(e0, ctx->stream);
-          launch_transport_kinds(ctx, T, 0, 2, 1.f / 3.f, 0, false, 0, [](int) {});
+          launch_transport_kinds(ctx, T, 0, 2, 1.f / 3.f, 0, 0, [](int) {});
           cudaEventRecord(e1, ctx->stream);
           CK(cudaEventSynchronize(e1));
           float t = 0; cudaEventElapsedTime(&t, e0, e1);
@@ -441,52 +437,64 @@ int autotune_transport(sg_context* ctx, Plan& P) {
   return upload_items(ctx, P, all);
 }
 
+// The three stages of a spectral solve (divergence and forward transform, mode solves, inverse transform) on the
+// plan's rows and modes, on the stream of `rows`.
+template <class Hook>
+void enqueue_solve(sg_context* ctx, const Plan& P, int mode, int set, cudaStream_t stream, Hook hook) {
+  Launch rows = lx(ctx, P, mode == PROJ_FACE ? FAM_ROWS_FACE : FAM_ROWS_PRES), modes = lx(ctx, P, FAM_MODES);
+  rows.cap = rows.n;
+  modes.cap = modes.n;  // one block per wavenumber: its column solves are serial in z, so spread them over the SMs
+  rows.stream = modes.stream = stream;
+  const int h = mode == PROJ_FACE ? 2 : mode == PROJ_PRES ? 7 : 22;  // profile ids of the three stages
+  if (P.layerfft) {
+    launch_proj_div_fft2(rows, mode, set, P.maxnx, P.maxny); hook(h);
+    launch_proj_sweep(modes, mode, P.maxny); hook(h + 1);
+    launch_proj_ifft2(rows, mode, P.maxnx, P.maxny); hook(h + 2);
+  } else {
+    const int mthreads = std::min(512, std::max(64, (2 * P.maxny + 31) / 32 * 32));
+    const int mbudget = std::min(ctx->maxSmem, 200 * 1024);
+    launch_proj_div_xfft(rows, mode, set, P.yc, P.maxnx); hook(h);
+    launch_proj_modes(modes, mode, P.maxnz, P.maxny, mthreads, mbudget); hook(h + 1);
+    launch_proj_xifft(rows, mode, P.yc, P.maxnx); hook(h + 2);
+  }
+}
+
+// The pressure projection of one set (a stage projection, or the final one with the wind limits and, for refined
+// runs, the refinement pass).
+template <class Hook>
+void enqueue_project(sg_context* ctx, const Plan& P, int set, int final_, cudaStream_t stream, Hook hook) {
+  Launch node = lx(ctx, P, FAM_NODE), cells = lx(ctx, P, FAM_CELLS);
+  node.stream = cells.stream = stream;
+  enqueue_solve(ctx, P, PROJ_PRES, set, stream, hook);
+  launch_pres_correct(node, set, final_); hook(final_ ? 16 : 10);  // (the final one skips refined runs)
+  if (final_ && P.refine) {
+    launch_refine_nodes(node, set); hook(20);
+    launch_refine_div(cells); hook(21);
+    enqueue_solve(ctx, P, PROJ_GIVEN, set, stream, hook);
+    launch_refine_correct(node, set); hook(25);
+  }
+}
+
 // The step's launch sequence for a plan in five parts (the oracle's partition of AtmosphereModel.step):
 // 1 beginStep (fall speeds, sedimentation), 2 dynamics (face projection, RK3 stages with their projections),
 // 3 physicsStep (positivity fix, physics), 4 mixStep (viscosity, mixing, drag), 5 the final projection and the
-// end-of-step counters. `hook(k)` is called after each launch (profiling).
+// end-of-step counters. `hook(k)` is called after each launch (profiling). Everything runs in order on the context's
+// stream.
 template <class Hook>
 void enqueue_part(sg_context* ctx, const Plan& P, int part, Hook hook) {
   const int A = 0, B = 1, C = 2;
-  Launch node = lx(ctx, P, FAM_NODE), cols = lx(ctx, P, FAM_COLS), rf = lx(ctx, P, FAM_ROWS_FACE), rp = lx(ctx, P, FAM_ROWS_PRES);
-  Launch modes = lx(ctx, P, FAM_MODES), runs = lx(ctx, P, FAM_RUNS);
-  modes.cap = modes.n;  // one block per wavenumber: its column solves are serial in z, so spread them over the SMs
-  rf.cap = rf.n; rp.cap = rp.n;
-  const int mthreads = std::min(512, std::max(64, (2 * P.maxny + 31) / 32 * 32));
-  const int mbudget = std::min(ctx->maxSmem, 200 * 1024);
-  // the three stages of a spectral solve: divergence and forward transform, mode solves, inverse transform
-  auto solve = [&](const Launch& rows, int mode, int set) {
-    const int h = mode == PROJ_FACE ? 2 : mode == PROJ_PRES ? 7 : 22;  // profile ids of the three stages
-    if (P.layerfft) {
-      launch_proj_div_fft2(rows, mode, set, P.maxnx, P.maxny); hook(h);
-      launch_proj_sweep(modes, mode, P.maxny); hook(h + 1);
-      launch_proj_ifft2(rows, mode, P.maxnx, P.maxny); hook(h + 2);
-    } else {
-      launch_proj_div_xfft(rows, mode, set, P.yc, P.maxnx); hook(h);
-      launch_proj_modes(modes, mode, P.maxnz, P.maxny, mthreads, mbudget); hook(h + 1);
-      launch_proj_xifft(rows, mode, P.yc, P.maxnx); hook(h + 2);
-    }
-  };
-  auto project = [&](int set, int final_) {
-    solve(rp, PROJ_PRES, set);
-    launch_pres_correct(node, set, final_); hook(final_ ? 16 : 10);  // (the final one skips refined runs)
-    if (final_ && P.refine) {
-      launch_refine_nodes(node, set); hook(20);
-      launch_refine_div(lx(ctx, P, FAM_CELLS)); hook(21);
-      solve(rp, PROJ_GIVEN, set);
-      launch_refine_correct(node, set); hook(25);
-    }
-  };
+  cudaStream_t st = ctx->stream;
+  Launch node = lx(ctx, P, FAM_NODE), cols = lx(ctx, P, FAM_COLS), runs = lx(ctx, P, FAM_RUNS);
   if (part == 1) {
     launch_fall_courant(node); hook(0);
     launch_sediment(cols, P.maxnz); hook(1);
   } else if (part == 2) {
-    solve(rf, PROJ_FACE, A);
+    enqueue_solve(ctx, P, PROJ_FACE, A, st, hook);
     launch_face_correct(node, A); hook(5);
     const int in[3] = {A, B, C}, out[3] = {B, C, B};
     for (int s = 0; s < 3; s++) {
-      launch_transport_kinds(ctx, P, in[s], out[s], (float)RK3[s], s, ctx->forking, 18, hook);
-      if (s < 2) project(out[s], 0);
+      launch_transport_kinds(ctx, P, in[s], out[s], (float)RK3[s], s, 18, hook);
+      if (s < 2) enqueue_project(ctx, P, out[s], 0, st, hook);
     }
   } else if (part == 3) {
     launch_fill_partial(node, B); hook(11);
@@ -498,13 +506,59 @@ void enqueue_part(sg_context* ctx, const Plan& P, int part, Hook hook) {
     mx.cap = mx.n;
     launch_mix(mx, C, P.mixTX, P.mixTY); hook(15);
   } else if (part == 5) {
-    project(A, 1);
+    enqueue_project(ctx, P, A, 1, st, hook);
     launch_step_end(runs); hook(17);
   }
 }
+
+// Parts 1 and 2 for a graph, with their independent chains on parallel branches (the same launches and the same
+// results as the serial order):
+//  * sedimentation (the falling fields of set A) alongside the face projection (u, v, w of set A);
+//  * the WENO transport of the three RK3 stages as one chain, alongside the chain of the dynamics transport
+//    (u, v, w, theta') and the stage projections. A WENO stage needs only the face fluxes, the step-start values and
+//    its input scalars; the dynamics stage s > 0 reads the scalars WENO stage s - 1 wrote (buoyancy), and WENO stage 2
+//    overwrites the scalars of set B only after dynamics stage 1 has read them.
+void enqueue_dynamics_graph(sg_context* ctx, const Plan& P) {
+  const int A = 0, B = 1, C = 2;
+  auto none = [](int) {};
+  cudaStream_t main = ctx->stream, side = ctx->side[1];
+  cudaEvent_t* ev = ctx->dep;
+  Launch node = lx(ctx, P, FAM_NODE), cols = lx(ctx, P, FAM_COLS);
+  Launch nodeS = node, colsS = cols;
+  nodeS.stream = colsS.stream = side;
+  cudaEventRecord(ev[0], main);
+  cudaStreamWaitEvent(side, ev[0], 0);
+  launch_fall_courant(nodeS);
+  launch_sediment(colsS, P.maxnz);
+  enqueue_solve(ctx, P, PROJ_FACE, A, main, none);
+  launch_face_correct(node, A);
+  cudaEventRecord(ev[1], main);
+  cudaStreamWaitEvent(side, ev[1], 0);  // the face fluxes
+  Launch W = lx(ctx, P, FAM_T_WENO), D = lx(ctx, P, FAM_T_DYN);
+  W.cap = W.n; D.cap = D.n; W.stream = side;
+  const int in[3] = {A, B, C}, out[3] = {B, C, B};
+  // ev[2 + s]: WENO stage s done; ev[5]: dynamics stage 1 done
+  for (int s = 0; s < 3; s++) {
+    if (s == 2) cudaStreamWaitEvent(side, ev[5], 0);     // dynamics stage 1 has read set B's scalars
+    if (W.n) launch_transport(W, TK_WENO, P.wenoG, P.minb, in[s], out[s], (float)RK3[s], s, P.TX, P.TY);
+    cudaEventRecord(ev[2 + s], side);
+    if (s > 0) cudaStreamWaitEvent(main, ev[1 + s], 0);  // the stage's input scalars
+    if (D.n) launch_transport(D, TK_DYN, P.wenoG, P.minb, in[s], out[s], (float)RK3[s], s, P.TX, P.TY);
+    if (s == 1) cudaEventRecord(ev[5], main);
+    if (s < 2) enqueue_project(ctx, P, out[s], 0, main, none);
+  }
+  cudaStreamWaitEvent(main, ev[4], 0);
+}
+
 template <class Hook>
 void enqueue_step(sg_context* ctx, const Plan& P, Hook hook) {
   for (int part = 1; part <= 5; part++) enqueue_part(ctx, P, part, hook);
+}
+// The same step with parallel branches, for graph capture.
+void enqueue_step_graph(sg_context* ctx, const Plan& P) {
+  auto none = [](int) {};
+  enqueue_dynamics_graph(ctx, P);
+  for (int part = 3; part <= 5; part++) enqueue_part(ctx, P, part, none);
 }
 const int NKERNELS = 26;
 const char* KERNEL_NAMES[NKERNELS] = {"fall_courant", "sediment", "face_div_xfft", "face_modes", "face_xifft", "face_correct", "transport",
@@ -527,9 +581,7 @@ Plan* get_plan(sg_context* ctx, const std::vector<int>& slots, int* status) {
 int ensure_graph(sg_context* ctx, Plan& P) {
   if (P.exec) return SG_OK;
   CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-  ctx->forking = true;
-  enqueue_step(ctx, P, [](int) {});
-  ctx->forking = false;
+  enqueue_step_graph(ctx, P);
   cudaError_t e = cudaStreamEndCapture(ctx->stream, &P.graph);
   if (e != cudaSuccess) return cudaFail(ctx, e, "cudaStreamEndCapture");
   CK(cudaGraphInstantiate(&P.exec, P.graph, 0));
@@ -602,13 +654,13 @@ int sg_context_create(int device, uint64_t hbm_budget_bytes, sg_context** out) {
   if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess ||
       (e = cudaMalloc(&ctx->d_runs, MAX_SLOTS * sizeof(RunDesc))) != cudaSuccess ||
       (e = cudaMalloc(&ctx->d_scalar, 64 * sizeof(double))) != cudaSuccess ||
-      (e = set_smem_limits(ctx->maxSmem)) != cudaSuccess ||
-      (e = cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming)) != cudaSuccess) {
+      (e = set_smem_limits(ctx->maxSmem)) != cudaSuccess) {
     delete ctx; return SG_ERR_DEVICE;
   }
-  for (int k = 0; k < 3; k++)
-    if ((e = cudaStreamCreateWithFlags(&ctx->side[k], cudaStreamNonBlocking)) != cudaSuccess ||
-        (e = cudaEventCreateWithFlags(&ctx->join[k], cudaEventDisableTiming)) != cudaSuccess) { delete ctx; return SG_ERR_DEVICE; }
+  for (int k = 0; k < 2; k++)
+    if ((e = cudaStreamCreateWithFlags(&ctx->side[k], cudaStreamNonBlocking)) != cudaSuccess) { delete ctx; return SG_ERR_DEVICE; }
+  for (int k = 0; k < 8; k++)
+    if ((e = cudaEventCreateWithFlags(&ctx->dep[k], cudaEventDisableTiming)) != cudaSuccess) { delete ctx; return SG_ERR_DEVICE; }
   if (const char* a = getenv("SG_AUTOTUNE")) ctx->autotune = atoi(a) != 0;
   if (const char* a = getenv("SG_SPECTRAL_ROWS")) ctx->rowsOnly = atoi(a) != 0;
   *out = ctx;
@@ -624,10 +676,10 @@ int sg_context_destroy(sg_context* ctx) {
   for (auto& p : ctx->pool) cudaFree(p.second);
   cudaFree(ctx->d_runs); cudaFree(ctx->d_scalar);
   cudaStreamDestroy(ctx->stream);
-  for (int k = 0; k < 3; k++) { cudaStreamDestroy(ctx->side[k]); cudaEventDestroy(ctx->join[k]); }
+  for (int k = 0; k < 2; k++) cudaStreamDestroy(ctx->side[k]);
+  for (int k = 0; k < 8; k++) cudaEventDestroy(ctx->dep[k]);
   for (auto& p : ctx->packs) cudaFree(p.second.first);
   if (ctx->staging) cudaFree(ctx->staging);
-  cudaEventDestroy(ctx->fork);
   delete ctx;
   return SG_OK;
 }

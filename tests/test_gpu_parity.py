@@ -153,6 +153,23 @@ def test_runs_are_deterministic_and_batch_independent(ctx, storm):
         run.retire()
 
 
+def test_graph_branches_match_the_serial_order(ctx, storm):
+    """The captured step runs independent chains on parallel branches (sedimentation beside the face projection, the
+    WENO transport of the three stages beside the dynamics transport and the stage projections); launched eagerly the
+    same kernels run one after another on one stream. Both orders give bitwise equal fields, for a batch of runs."""
+    specs = [storm, baseline_run(create_grid(DEFAULT_GRID), seed=11), baseline_run(create_grid(LARGE_GRID), seed=12)]
+    serial = [ctx.create(s) for s in specs]
+    ctx.time_steps(serial, 3, graph=False)
+    branched = [ctx.create(s) for s in specs]
+    ctx.time_steps(branched, 3, graph=True)
+    for a, b in zip(serial, branched):
+        x, y = a.read(), b.read()
+        for k in CARRIED:
+            assert np.array_equal(x[k], y[k]), k
+    for r in serial + branched:
+        r.retire()
+
+
 def test_row_transform_path_matches_fp64_oracle(storm, monkeypatch):
     """The row-transform path of the spectral solves (x-transforms of row blocks, y-transforms inside the mode
     kernel; what grids too wide for the whole-layer path take, e.g. 320x256) forced on the standard grid: one step
