@@ -23,6 +23,19 @@ namespace sg {
 
 #define FOR_ITEMS for (int it = blockIdx.x; it < nitems; it += gridDim.x)
 
+// 4-byte asynchronous copy global -> shared (lands without passing through registers), and the wait for all of
+// this thread's copies; other threads see the data after the next barrier.
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+// 16-byte asynchronous copy (both addresses 16-byte aligned), not cached in L1
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 __device__ __forceinline__ void atomicMaxPos(float* addr, float v) {
   // Non-negative floats order like their bit patterns.
   atomicMax(reinterpret_cast<int*>(addr), __float_as_int(v));
@@ -60,8 +73,8 @@ __device__ void blockSums(double (&v)[COUNT], double* out, double* sh /* >= 32*C
 // Compensated FP32 sums: a partial sum is kept as hi + lo (two FP32 words, about 48 significant bits) and terms are
 // added with TwoSum (Knuth), so the per-thread sums of the positivity fix and the water budget keep FP64-like accuracy
 // on the FP32 pipes (GB300 runs FP64 at a small fraction of its FP32 rate); warps combine them the same way and the
-// sums across warps and blocks are FP64. Every step is an explicitly rounded operation, and the xor-butterfly gives
-// every lane the same bits (TwoSum's error term does not depend on the operand order).
+// sums across warps and blocks are FP64. Every step is an explicitly rounded operation, so the sums do not depend on
+// compiler contraction.
 __device__ __forceinline__ void df_add(float& hi, float& lo, float a) {
   const float s = __fadd_rn(hi, a), bp = __fsub_rn(s, hi);
   const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(a, bp));
@@ -78,23 +91,46 @@ __device__ __forceinline__ void df_norm(float& hi, float& lo) {
   const float s = __fadd_rn(hi, lo);
   lo = __fsub_rn(lo, __fsub_rn(s, hi)); hi = s;
 }
+// Block sums of `count` compensated sums per thread into out[] (FP64, a fixed order). Within a warp the sums are
+// reduced by halving exchanges: partner lanes swap halves of their (zero-padded) value lists and each keeps the sum of
+// one half, so after log2(P) exchanges lane v * 32 / P holds value v; the offsets left over add the one value per lane
+// as a plain butterfly. Then the warps' sums are added in warp order.
 template <int COUNT>
 __device__ void blockSumsDF(float (&hi)[COUNT], float (&lo)[COUNT], double* out, double* sh /* >= 32*COUNT */) {
+  static_assert(COUNT >= 1 && COUNT <= 32, "at most 32 sums");
+  constexpr int P = COUNT <= 1 ? 1 : COUNT <= 2 ? 2 : COUNT <= 4 ? 4 : COUNT <= 8 ? 8 : COUNT <= 16 ? 16 : 32;
+  constexpr int LOGP = P == 1 ? 0 : P == 2 ? 1 : P == 4 ? 2 : P == 8 ? 3 : P == 16 ? 4 : 5;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  float h[P], l[P];
 #pragma unroll
-  for (int c = 0; c < COUNT; c++) {
-    df_norm(hi[c], lo[c]);
+  for (int i = 0; i < P; i++) {
+    h[i] = i < COUNT ? hi[i] : 0.f; l[i] = i < COUNT ? lo[i] : 0.f;
+    df_norm(h[i], l[i]);
+  }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const float h2 = __shfl_xor_sync(0xffffffffu, hi[c], o), l2 = __shfl_xor_sync(0xffffffffu, lo[c], o);
-      df_add(hi[c], lo[c], h2);
-      lo[c] = __fadd_rn(lo[c], l2);
-      df_norm(hi[c], lo[c]);
+  for (int j = 0; j < LOGP; j++) {
+    const int m = P >> j, o = 16 >> j;
+    const bool up = lane & o;
+#pragma unroll
+    for (int i = 0; i < m / 2; i++) {
+      const float sendH = up ? h[i] : h[i + m / 2], sendL = up ? l[i] : l[i + m / 2];
+      float kh = up ? h[i + m / 2] : h[i], kl = up ? l[i + m / 2] : l[i];
+      const float rh = __shfl_xor_sync(0xffffffffu, sendH, o), rl = __shfl_xor_sync(0xffffffffu, sendL, o);
+      df_add(kh, kl, rh);
+      kl = __fadd_rn(kl, rl);
+      df_norm(kh, kl);
+      h[i] = kh; l[i] = kl;
     }
   }
+#pragma unroll
+  for (int o = 16 >> LOGP; o > 0; o >>= 1) {
+    const float h2 = __shfl_xor_sync(0xffffffffu, h[0], o), l2 = __shfl_xor_sync(0xffffffffu, l[0], o);
+    df_add(h[0], l[0], h2);
+    l[0] = __fadd_rn(l[0], l2);
+    df_norm(h[0], l[0]);
+  }
   __syncthreads();
-  if (lane == 0)
-    for (int c = 0; c < COUNT; c++) sh[warp * COUNT + c] = (double)hi[c] + (double)lo[c];
+  if ((lane & (32 / P - 1)) == 0 && lane / (32 / P) < COUNT) sh[warp * COUNT + lane / (32 / P)] = (double)h[0] + (double)l[0];
   __syncthreads();
   if (threadIdx.x < COUNT) {
     double s = 0;
@@ -739,15 +775,11 @@ __device__ __forceinline__ DF df_mul(DF a, DF b) {
 }
 __device__ __forceinline__ DF df_diff(float a, float b) { return df_two_sum(a, -b); }  // a - b exactly
 
-// G p1 at a node in double-FP32 (the gradient of k_pres_correct).
-__device__ __forceinline__ void df_gradient(const RunDesc& R, const float* p, int i, int k, DF& gx, DF& gy, DF& gz) {
-  const int nx = R.nx, ny = R.ny, nz = R.nz, layer = R.layer;
-  const int c = i - k * layer, jy = row_of(c, 1.f / (float)nx), x = c - jy * nx;
-  const int im = x == 0 ? nx - 1 : x - 1, jm = (jy == 0 ? ny - 1 : jy - 1) * nx, j0 = jy * nx;
-  const float* L = p + (size_t)max(0, k - 1) * layer;
-  const float* H = p + (size_t)min(nz - 2, k) * layer;
-  const float l0 = L[im + jm], l1 = L[x + jm], l2 = L[im + j0], l3 = L[x + j0];
-  const float h0 = H[im + jm], h1 = H[x + jm], h2 = H[im + j0], h3 = H[x + j0];
+// G p1 at a node of level k in double-FP32 (the gradient of k_pres_correct) from the pressure of the four dual cells
+// around it below (l: (x-1, y-1), (x, y-1), (x-1, y), (x, y)) and above (h, the same order).
+__device__ __forceinline__ void df_gradient_of(const RunDesc& R, int k, float l0, float l1, float l2, float l3, float h0, float h1,
+                                               float h2, float h3, DF& gx, DF& gy, DF& gz) {
+  const int nz = R.nz;
   const DF wlo = k > 0 ? DF{lvl(R, L_WLO, k), lvl(R, L_WLO_LO, k)} : DF{0.f, 0.f};
   const DF whi = k < nz - 1 ? DF{lvl(R, L_WHI, k), lvl(R, L_WHI_LO, k)} : DF{0.f, 0.f};
   const DF qx{.25f * R.inv_dx, .25f * R.inv_dx_lo}, qy{.25f * R.inv_dy, .25f * R.inv_dy_lo};
@@ -760,63 +792,100 @@ __device__ __forceinline__ void df_gradient(const RunDesc& R, const float* p, in
   }
 }
 
-// v = u - dt G p1 at every node of set `set` as hi + lo: hi into set B, lo into set C (u, v, w).
-__global__ void k_refine_nodes(const RunDesc* __restrict__ runs, const int4* items, int nitems, int set) {
+// The residual of the refined runs' final projection in one tiled march over the item's levels (run, tile, z0, z1),
+// a thread per node of the tile and its halo:
+// per node level, v = u - dt G p1 in double-FP32 for the tile's nodes and a one-node halo on the high x and y sides
+// (into a pair of shared-memory planes), the tile's own nodes' (hi, lo) written to sets B and C for the final
+// correction; per dual layer, r = D v / dt rounded once into phi: D of the hi parts in double-FP32 (their differences
+// are exact), D of the lo parts (a few 1e-8 of them) in FP32. The pressure planes (dual levels k - 1 and k, with a
+// one-cell halo on the low sides) arrive by asynchronous copies a level ahead.
+__global__ void __launch_bounds__(320) k_refine_residual(const RunDesc* __restrict__ runs, const int4* items, int nitems, int set,
+                                                         int TX, int TY) {
+  extern __shared__ float rsm[];
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
     if (R.cnt[C_FAILED] || !(R.flags & RF_REFINE)) continue;
-    const int layer = R.layer, i0 = items[it].y * CHUNK, i1 = min(R.n, i0 + CHUNK);
+    const int tile = items[it].y, z0 = items[it].z, z1 = items[it].w;
+    const int nx = R.nx, ny = R.ny, nz = R.nz, layer = R.layer;
+    const int PW = TX + 2, PP = PW * (TY + 2), NW = TX + 1, NN = NW * (TY + 1), NT = blockDim.x, t = threadIdx.x;
+    float* pp = rsm;                 // [2][PP]: p1 of dual level d in slot d & 1, columns x0 - 1 .. x0 + TX
+    float* nv = rsm + 2 * PP;        // [2][6][NN]: node level k in slot k & 1; u hi, u lo, v hi, v lo, w hi, w lo
+    const int tilesX = (nx + TX - 1) / TX, x0 = (tile % tilesX) * TX, y0 = (tile / tilesX) * TY;
+    const float* __restrict__ u = field(R, set, U);
+    const float* __restrict__ v = field(R, set, V);
+    const float* __restrict__ w = field(R, set, W);
+    const float* __restrict__ p = R.pres;
     const DF dt{R.dt, 0.f};
-    int k = (i0 + threadIdx.x) / layer;
-    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-      while (i >= (k + 1) * layer) k++;
-      DF g[3];
-      df_gradient(R, R.pres, i, k, g[0], g[1], g[2]);
+    const int kTop = min(z1, nz - 1);  // node levels z0 .. kTop; dual layers z0 .. kTop - 1
+    auto load_plane = [&](int d, bool async) {
+      float* dst = pp + (d & 1) * PP;
+      const float* src = p + (size_t)d * layer;
+      for (int e = t; e < PP; e += NT) {
+        const int hy = e / PW, hx = e - hy * PW;
+        const int gx = wrap(x0 - 1 + hx, nx), gy = wrap(y0 - 1 + hy, ny);
+        if (async) cp_async4(dst + e, src + gx + gy * nx); else dst[e] = src[gx + gy * nx];
+      }
+    };
+    load_plane(max(0, z0 - 1), false);
+    load_plane(min(nz - 2, z0), false);
+    const int lx = t % TX, ly = t / TX, cx = x0 + lx, cy = y0 + ly;  // the dual cell of thread t < TX * TY
+    const bool on = t < TX * TY && cx < nx && cy < ny;
+    const DF idx{R.inv_dx, R.inv_dx_lo}, idy{R.inv_dy, R.inv_dy_lo}, idt{R.inv_dt, R.inv_dt_lo};
+    for (int k = z0; k <= kTop; k++) {
+      cp_async_wait_all();
+      __syncthreads();
+      // node velocities of level k
+      const float* L = pp + (max(0, k - 1) & 1) * PP;
+      const float* H = pp + (min(nz - 2, k) & 1) * PP;
+      float* V = nv + (k & 1) * 6 * NN;
+      for (int e = t; e < NN; e += NT) {
+        const int ny_ = e / NW, nx_ = e - ny_ * NW;
+        if (x0 + nx_ > nx || y0 + ny_ > ny) continue;  // past the last cell of a partial tile
+        const int gx = x0 + nx_ == nx ? 0 : x0 + nx_, gy = y0 + ny_ == ny ? 0 : y0 + ny_;
+        const int a = ny_ * PW + nx_;  // p plane cell (x - 1, y - 1)
+        DF g[3];
+        df_gradient_of(R, k, L[a], L[a + 1], L[a + PW], L[a + PW + 1], H[a], H[a + 1], H[a + PW], H[a + PW + 1], g[0], g[1], g[2]);
+        const size_t i = (size_t)k * layer + gx + gy * nx;
+        const float uin[3] = {u[i], v[i], w[i]};
+        const bool own = nx_ < TX && ny_ < TY && k < z1;
 #pragma unroll
-      for (int d = 0; d < 3; d++) {
-        const DF v = df_sub(DF{field(R, set, U + d)[i], 0.f}, df_mul(dt, g[d]));
-        field(R, 1, U + d)[i] = v.hi;
-        field(R, 2, U + d)[i] = v.lo;
+        for (int d = 0; d < 3; d++) {
+          const DF r = df_sub(DF{uin[d], 0.f}, df_mul(dt, g[d]));
+          V[(2 * d) * NN + e] = r.hi;
+          V[(2 * d + 1) * NN + e] = r.lo;
+          if (own) { field(R, 1, U + d)[i] = r.hi; field(R, 2, U + d)[i] = r.lo; }
+        }
+      }
+      __syncthreads();
+      // the pressure of dual level k + 1 for the next node level (its slot held dual level k - 1, read above)
+      if (k + 1 <= kTop && k + 1 <= nz - 2) load_plane(k + 1, true);
+      // the residual of dual layer k - 1 (node levels k - 1 and k)
+      if (k > z0 && on) {
+        const int kc = k - 1;
+        const float* B0 = nv + (kc & 1) * 6 * NN;
+        const float* B1 = V;
+        const int a = ly * NW + lx, b = a + 1, e = a + NW, f = e + 1;
+        const DF r0{.25f * lvl(R, L_RHO, kc), .25f * lvl(R, L_RHO_LO, kc)}, r1{.25f * lvl(R, L_RHO, kc + 1), .25f * lvl(R, L_RHO_LO, kc + 1)};
+        const DF idz{lvl(R, L_INV_DZS, kc), lvl(R, L_INV_DZS_LO, kc)};
+        const float *hu0 = B0, *hv0 = B0 + 2 * NN, *hw0 = B0 + 4 * NN, *hu1 = B1, *hv1 = B1 + 2 * NN, *hw1 = B1 + 4 * NN;
+        const DF ddx = df_mul(df_add(df_mul(r0, df_add(df_diff(hu0[b], hu0[a]), df_diff(hu0[f], hu0[e]))),
+                                     df_mul(r1, df_add(df_diff(hu1[b], hu1[a]), df_diff(hu1[f], hu1[e])))), idx);
+        const DF ddy = df_mul(df_add(df_mul(r0, df_add(df_diff(hv0[e], hv0[a]), df_diff(hv0[f], hv0[b]))),
+                                     df_mul(r1, df_add(df_diff(hv1[e], hv1[a]), df_diff(hv1[f], hv1[b])))), idy);
+        const DF up = df_add(df_add(DF{hw1[a], 0.f}, DF{hw1[b], 0.f}), df_add(DF{hw1[e], 0.f}, DF{hw1[f], 0.f}));
+        const DF dn = df_add(df_add(DF{hw0[a], 0.f}, DF{hw0[b], 0.f}), df_add(DF{hw0[e], 0.f}, DF{hw0[f], 0.f}));
+        const DF ddz = df_mul(df_sub(df_mul(r1, up), df_mul(r0, dn)), idz);
+        const float *lu0 = B0 + NN, *lv0 = B0 + 3 * NN, *lw0 = B0 + 5 * NN, *lu1 = B1 + NN, *lv1 = B1 + 3 * NN, *lw1 = B1 + 5 * NN;
+        const float rr0 = r0.hi, rr1 = r1.hi;
+        const float lox = (rr0 * ((lu0[b] - lu0[a]) + (lu0[f] - lu0[e])) + rr1 * ((lu1[b] - lu1[a]) + (lu1[f] - lu1[e]))) * idx.hi;
+        const float loy = (rr0 * ((lv0[e] - lv0[a]) + (lv0[f] - lv0[b])) + rr1 * ((lv1[e] - lv1[a]) + (lv1[f] - lv1[b]))) * idy.hi;
+        const float loz = (rr1 * ((lw1[a] + lw1[b]) + (lw1[e] + lw1[f])) - rr0 * ((lw0[a] + lw0[b]) + (lw0[e] + lw0[f]))) * idz.hi;
+        const DF dd = df_mul(df_add(df_add(df_add(ddx, ddy), ddz), DF{(lox + loy) + loz, 0.f}), idt);
+        R.phi[(size_t)kc * layer + cx + cy * nx] = dd.hi + dd.lo;
       }
     }
-  }
-}
-
-// r = D v / dt per dual cell from the pairs of k_refine_nodes, rounded once into phi: D of the hi parts in
-// double-FP32 (their differences are exact), D of the lo parts (a few 1e-8 of them) in FP32.
-__global__ void k_refine_div(const RunDesc* __restrict__ runs, const int4* items, int nitems) {
-  FOR_ITEMS {
-    const RunDesc& R = runs[items[it].x];
-    if (R.cnt[C_FAILED] || !(R.flags & RF_REFINE)) continue;
-    const int nx = R.nx, ny = R.ny, layer = R.layer, i0 = items[it].y * CHUNK, i1 = min(R.ncells, i0 + CHUNK);
-    const DF idx{R.inv_dx, R.inv_dx_lo}, idy{R.inv_dy, R.inv_dy_lo}, idt{R.inv_dt, R.inv_dt_lo};
-    const float* __restrict__ H[3] = {field(R, 1, U), field(R, 1, V), field(R, 1, W)};
-    const float* __restrict__ Lo[3] = {field(R, 2, U), field(R, 2, V), field(R, 2, W)};
-    const float inv_nx = 1.f / (float)nx;
-    int k = (i0 + threadIdx.x) / layer;
-    for (int cidx = i0 + threadIdx.x; cidx < i1; cidx += blockDim.x) {
-      while (cidx >= (k + 1) * layer) k++;
-      const int c = cidx - k * layer, y = row_of(c, inv_nx), x = c - y * nx;
-      const int l0 = k * layer, l1 = l0 + layer, x1 = x + 1 == nx ? 0 : x + 1, y1 = (y + 1 == ny ? 0 : y + 1) * nx, yy = y * nx;
-      const int a = x + yy, b = x1 + yy, e = x + y1, f = x1 + y1;
-      const DF r0{.25f * lvl(R, L_RHO, k), .25f * lvl(R, L_RHO_LO, k)}, r1{.25f * lvl(R, L_RHO, k + 1), .25f * lvl(R, L_RHO_LO, k + 1)};
-      const DF idz{lvl(R, L_INV_DZS, k), lvl(R, L_INV_DZS_LO, k)};
-      const float* hu = H[0]; const float* hv = H[1]; const float* hw = H[2];
-      const DF ddx = df_mul(df_add(df_mul(r0, df_add(df_diff(hu[b + l0], hu[a + l0]), df_diff(hu[f + l0], hu[e + l0]))),
-                                   df_mul(r1, df_add(df_diff(hu[b + l1], hu[a + l1]), df_diff(hu[f + l1], hu[e + l1])))), idx);
-      const DF ddy = df_mul(df_add(df_mul(r0, df_add(df_diff(hv[e + l0], hv[a + l0]), df_diff(hv[f + l0], hv[b + l0]))),
-                                   df_mul(r1, df_add(df_diff(hv[e + l1], hv[a + l1]), df_diff(hv[f + l1], hv[b + l1])))), idy);
-      const DF up = df_add(df_add(DF{hw[a + l1], 0.f}, DF{hw[b + l1], 0.f}), df_add(DF{hw[e + l1], 0.f}, DF{hw[f + l1], 0.f}));
-      const DF dn = df_add(df_add(DF{hw[a + l0], 0.f}, DF{hw[b + l0], 0.f}), df_add(DF{hw[e + l0], 0.f}, DF{hw[f + l0], 0.f}));
-      const DF ddz = df_mul(df_sub(df_mul(r1, up), df_mul(r0, dn)), idz);
-      const float* lu = Lo[0]; const float* lv_ = Lo[1]; const float* lw = Lo[2];
-      const float rr0 = r0.hi, rr1 = r1.hi;
-      const float lox = (rr0 * ((lu[b + l0] - lu[a + l0]) + (lu[f + l0] - lu[e + l0])) + rr1 * ((lu[b + l1] - lu[a + l1]) + (lu[f + l1] - lu[e + l1]))) * idx.hi;
-      const float loy = (rr0 * ((lv_[e + l0] - lv_[a + l0]) + (lv_[f + l0] - lv_[b + l0])) + rr1 * ((lv_[e + l1] - lv_[a + l1]) + (lv_[f + l1] - lv_[b + l1]))) * idy.hi;
-      const float loz = (rr1 * ((lw[a + l1] + lw[b + l1]) + (lw[e + l1] + lw[f + l1])) - rr0 * ((lw[a + l0] + lw[b + l0]) + (lw[e + l0] + lw[f + l0]))) * idz.hi;
-      const DF d = df_mul(df_add(df_add(df_add(ddx, ddy), ddz), DF{(lox + loy) + loz, 0.f}), idt);
-      R.phi[cidx] = d.hi + d.lo;
-    }
+    cp_async_wait_all();
+    __syncthreads();
   }
 }
 
@@ -905,19 +974,6 @@ __device__ __forceinline__ float2 recon2(float2 a, float2 b, float2 c, float2 d,
   if (KIND == TK_WENO) return weno2(a, b, c, d, e);
   return upwind_core<Op2>(a, b, c, d, e);
 }
-
-// 4-byte asynchronous copy global -> shared (lands without passing through registers), and the wait for all of
-// this thread's copies; other threads see the data after the next barrier.
-__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
-  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
-}
-// 16-byte asynchronous copy (both addresses 16-byte aligned), not cached in L1
-__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
-  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 // The upwind stencil of a face along one axis (stride s) whose low-side cell is at P[-1] and high-side cell at P[0]:
 // for flow towards +axis the cells -3..1, else 2..-2 (mirrored).
@@ -1365,10 +1421,14 @@ __device__ __forceinline__ void mix_item(const RunDesc& R, int tile, int z0, int
   const int x = x0 + lx, y = y0 + ly;
   const bool on = x < nx && y < ny;
   const int col = on ? x + y * nx : 0;
-  const float* src[NP];
+  // the fields as 32-bit element offsets from the run's field block (fewer live registers than pointers); plane NM
+  // is K_h
+  const float* const fld = R.fld;
+  const float* const kh = R.kmkh + R.n;
+  int so[NM];
 #pragma unroll
-  for (int k = 0; k < NM; k++) src[k] = field(R, in, mix_field(k));
-  src[NM] = R.kmkh + R.n;  // K_h
+  for (int k = 0; k < NM; k++) so[k] = (in * NF + mix_field(k)) * (int)R.n;
+#define SRC(p) ((p) < NM ? fld + so[(p) < NM ? (p) : 0] : kh)
   const float* km = R.kmkh;
   int off[MIX_MAXC], cell[MIX_MAXC];
 #pragma unroll
@@ -1385,13 +1445,13 @@ __device__ __forceinline__ void mix_item(const RunDesc& R, int tile, int z0, int
 #pragma unroll
   for (int p = 0; p < NP; p++)
 #pragma unroll
-    for (int j = 0; j < MIX_MAXC; j++) if (cell[j] >= 0) sm[p * NCELL + cell[j]] = src[p][off[j] + z0 * layer];
+    for (int j = 0; j < MIX_MAXC; j++) if (cell[j] >= 0) sm[p * NCELL + cell[j]] = SRC(p)[off[j] + z0 * layer];
   float below[NM], cur[NM], above[NM];
 #pragma unroll
   for (int k = 0; k < NM; k++) {
-    cur[k] = src[k][col + z0 * layer];
-    below[k] = z0 > 0 ? src[k][col + (z0 - 1) * layer] : 0.f;
-    above[k] = z0 + 1 < nz ? src[k][col + (z0 + 1) * layer] : 0.f;
+    cur[k] = SRC(k)[col + z0 * layer];
+    below[k] = z0 > 0 ? SRC(k)[col + (z0 - 1) * layer] : 0.f;
+    above[k] = z0 + 1 < nz ? SRC(k)[col + (z0 + 1) * layer] : 0.f;
   }
   float kmD = z0 > 0 ? km[col + (z0 - 1) * layer] : 0.f, kmC = km[col + z0 * layer], kmU = z0 + 1 < nz ? km[col + (z0 + 1) * layer] : 0.f;
   __syncthreads();
@@ -1406,13 +1466,13 @@ __device__ __forceinline__ void mix_item(const RunDesc& R, int tile, int z0, int
 #pragma unroll
       for (int p = 0; p < NP; p++)
 #pragma unroll
-        for (int j = 0; j < MIX_MAXC; j++) if (cell[j] >= 0) cp_async4(Q + p * NCELL + cell[j], src[p] + off[j] + (z + 1) * layer);
+        for (int j = 0; j < MIX_MAXC; j++) if (cell[j] >= 0) cp_async4(Q + p * NCELL + cell[j], SRC(p) + off[j] + (z + 1) * layer);
     }
     float nextv[NM];
     float kmN = 0.f;
     const bool more = z + 2 < nz;
 #pragma unroll
-    for (int k = 0; k < NM; k++) nextv[k] = more ? src[k][col + (z + 2) * layer] : 0.f;
+    for (int k = 0; k < NM; k++) nextv[k] = more ? SRC(k)[col + (z + 2) * layer] : 0.f;
     if (more) kmN = km[col + (z + 2) * layer];
     if (on) {
       const float* KH = P + NM * NCELL + cc;
@@ -1458,6 +1518,7 @@ __device__ __forceinline__ void mix_item(const RunDesc& R, int tile, int z0, int
     cp_async_wait_all();
     __syncthreads();
   }
+#undef SRC
 }
 
 // Work item (run, tile, z0, z1); `TX` x `TY` threads.
@@ -1572,8 +1633,12 @@ void launch_proj_xifft(const Launch& L, int mode, int yc, int maxnx) {
   k_proj_xifft<<<GRID(L.n, L.cap), 256, smem, L.stream>>>(L.runs, L.items, L.n, mode, yc);
 }
 void launch_face_correct(const Launch& L, int set) { k_face_correct<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set); }
-void launch_refine_nodes(const Launch& L, int set) { k_refine_nodes<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set); }
-void launch_refine_div(const Launch& L) { k_refine_div<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n); }
+size_t refine_smem(int TX, int TY) { return ((size_t)2 * (TX + 2) * (TY + 2) + (size_t)12 * (TX + 1) * (TY + 1)) * sizeof(float); }
+void launch_refine_residual(const Launch& L, int set, int TX, int TY) {
+  if (L.n == 0) return;
+  const int threads = ((TX + 1) * (TY + 1) + 31) / 32 * 32;  // a thread per node of the tile and its halo
+  k_refine_residual<<<GRID(L.n, L.cap), threads, refine_smem(TX, TY), L.stream>>>(L.runs, L.items, L.n, set, TX, TY);
+}
 void launch_refine_correct(const Launch& L, int set) { k_refine_correct<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set); }
 void launch_pres_correct(const Launch& L, int set, int final_) { k_pres_correct<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set, final_); }
 size_t transport_smem(int kind, int G, int TX, int TY) {
@@ -1593,7 +1658,7 @@ void launch_transport(const Launch& L, int kind, int group, int minb, int in_set
 }
 #undef TLAUNCH
 
-void launch_fill_partial(const Launch& L, int set) { k_fill_partial<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set); }
+void launch_fill_partial(const Launch& L, int set) { k_fill_partial<<<GRID(L.n, L.cap), 128, 0, L.stream>>>(L.runs, L.items, L.n, set); }
 void launch_fill_final(const Launch& L) { k_fill_final<<<GRID(L.n, L.cap), 32, 0, L.stream>>>(L.runs, L.items, L.n); }
 void launch_physics(const Launch& L, int in, int mid) { k_physics<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, in, mid); }
 void launch_viscosity(const Launch& L, int set) { k_viscosity<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set); }
@@ -1620,6 +1685,7 @@ cudaError_t set_smem_limits(int bytes) {
   if ((e = smem_limit(k_sediment, bytes)) != cudaSuccess) return e;
   if ((e = smem_limit(k_proj_div_fft2, bytes)) != cudaSuccess) return e;
   if ((e = smem_limit(k_proj_ifft2, bytes)) != cudaSuccess) return e;
+  if ((e = smem_limit(k_refine_residual, bytes)) != cudaSuccess) return e;
   if ((e = smem_limit(k_transport<TK_WENO, 3, 2>, bytes)) != cudaSuccess) return e;
   if ((e = smem_limit(k_transport<TK_WENO, 3, 3>, bytes)) != cudaSuccess) return e;
   if ((e = smem_limit(k_transport<TK_WENO, 1, 2>, bytes)) != cudaSuccess) return e;

@@ -35,8 +35,7 @@ void launch_proj_xifft(const Launch& L, int mode, int yc, int maxnx);
 void launch_face_correct(const Launch& L, int set);
 // Refinement of the final projection: node pairs v = u - dt G p1 (nodes), their divergence into phi (cells), and
 // the corrected velocity from pres2 (nodes).
-void launch_refine_nodes(const Launch& L, int set);
-void launch_refine_div(const Launch& L);
+void launch_refine_residual(const Launch& L, int set, int TX, int TY);
 void launch_refine_correct(const Launch& L, int set);
 void launch_pres_correct(const Launch& L, int set, int final_);
 // kind: 0 WENO fields, 1 u and v, 2 w, 3 theta (the item list of that kind)

@@ -67,6 +67,7 @@ struct Plan {
   int minb = 2;                                                       // WENO transport blocks per SM (register budget)
   int yc = 32;                                                        // layer rows per x-transform item
   int mixTX = 32, mixTY = 8;                                          // mixing tile
+  int refTX = 16, refTY = 8;                                          // refinement tile
   bool layerfft = false;                                              // 2-D transforms per layer (see enqueue_part)
   bool refine = false;                                                // some run refines its final projection
   bool tuned = false;                                                 // TX, TY, wenoG chosen by timing
@@ -79,7 +80,7 @@ struct Plan {
   }
 };
 enum Family { FAM_NODE, FAM_COLS, FAM_ROWS_FACE, FAM_ROWS_PRES, FAM_MODES, FAM_RUNS, FAM_CELLS, FAM_T_WENO, FAM_T_DYN, FAM_MIX,
-              FAM_COUNT };
+              FAM_REFINE, FAM_COUNT };
 
 }  // namespace
 
@@ -348,6 +349,15 @@ int build_plan(sg_context* ctx, const std::vector<int>& slots, Plan& P) {
     for (int t = 0; t < tiles; t++)
       for (int z0 = 0; z0 < r.nz; z0 += zc) all[FAM_MIX].push_back(make_int4(s, t, z0, std::min(r.nz, z0 + zc)));
   }
+  // refinement items (refined runs only): (run, tile, z0, z1) on tiles whose nodes, halo included, fit one block
+  P.refTX = all40 ? 20 : 16; P.refTY = 8;
+  for (int s : slots) {
+    const Run& r = ctx->runs[s];
+    if (!(r.desc.flags & RF_REFINE)) continue;
+    const int tiles = ((r.nx + P.refTX - 1) / P.refTX) * ((r.ny + P.refTY - 1) / P.refTY), zc = (r.nz + 3) / 4;
+    for (int t = 0; t < tiles; t++)
+      for (int z0 = 0; z0 < r.nz; z0 += zc) all[FAM_REFINE].push_back(make_int4(s, t, z0, std::min(r.nz, z0 + zc)));
+  }
   if (ctx->pinned[0]) { P.TX = ctx->pinned[0]; P.TY = ctx->pinned[1]; P.wenoG = ctx->pinned[2]; P.minb = ctx->pinned[3]; }
   transport_items(ctx, slots, P.TX, P.TY, P.wenoG, all + FAM_T_WENO);
   int st = upload_items(ctx, P, all);
@@ -468,8 +478,9 @@ void enqueue_project(sg_context* ctx, const Plan& P, int set, int final_, cudaSt
   enqueue_solve(ctx, P, PROJ_PRES, set, stream, hook);
   launch_pres_correct(node, set, final_); hook(final_ ? 16 : 10);  // (the final one skips refined runs)
   if (final_ && P.refine) {
-    launch_refine_nodes(node, set); hook(20);
-    launch_refine_div(cells); hook(21);
+    Launch rr = lx(ctx, P, FAM_REFINE);
+    rr.cap = rr.n; rr.stream = stream;
+    launch_refine_residual(rr, set, P.refTX, P.refTY); hook(20);
     enqueue_solve(ctx, P, PROJ_GIVEN, set, stream, hook);
     launch_refine_correct(node, set); hook(25);
   }
@@ -564,7 +575,7 @@ const int NKERNELS = 26;
 const char* KERNEL_NAMES[NKERNELS] = {"fall_courant", "sediment", "face_div_xfft", "face_modes", "face_xifft", "face_correct", "transport",
                                       "pres_div_xfft", "pres_modes", "pres_xifft", "pres_correct", "fill_partial", "fill_final", "physics",
                                       "viscosity", "mix", "pres_correct_final", "step_end", "transport_weno", "transport_dynamics",
-                                      "refine_nodes", "refine_div", "refine_div_xfft", "refine_modes", "refine_xifft", "refine_correct"};
+                                      "refine_residual", "refine_unused", "refine_div_xfft", "refine_modes", "refine_xifft", "refine_correct"};
 
 Plan* get_plan(sg_context* ctx, const std::vector<int>& slots, int* status) {
   auto it = ctx->plans.find(slots);
