@@ -55,5 +55,6 @@ size_t mix_smem(int TX, int TY);
 void launch_step_end(const Launch& L);
 void launch_divergence_max(const Launch& L, int set, double* out);
 cudaError_t set_smem_limits(int bytes);
+cudaError_t set_transport_smem_limits(int bytes);  // (sg_transport.cu)
 
 }  // namespace sg
