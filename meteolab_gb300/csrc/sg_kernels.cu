@@ -760,6 +760,32 @@ __device__ __forceinline__ DF df_mul(DF a, DF b) {
 }
 __device__ __forceinline__ DF df_diff(float a, float b) { return df_two_sum(a, -b); }  // a - b exactly
 
+// The same operations on two independent values at once (the x and y lanes) on the packed FP32 pipes: per lane the
+// bits of the scalar functions above (a - b is formed as fma(b, -1, a), the same rounded difference).
+struct DF2 { float2 hi, lo; };
+__device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.f, -1.f), a); }
+__device__ __forceinline__ DF2 df2_two_sum(float2 a, float2 b) {
+  const float2 s = add2(a, b), bp = sub2(s, a);
+  return DF2{s, add2(sub2(a, sub2(s, bp)), sub2(b, bp))};
+}
+__device__ __forceinline__ DF2 df2_fast(float2 s, float2 e) {
+  const float2 h = add2(s, e);
+  return DF2{h, sub2(e, sub2(h, s))};
+}
+__device__ __forceinline__ DF2 df2_add(DF2 a, DF2 b) {
+  const DF2 s = df2_two_sum(a.hi, b.hi);
+  return df2_fast(s.hi, add2(s.lo, add2(a.lo, b.lo)));
+}
+__device__ __forceinline__ DF2 df2_mul(DF2 a, DF2 b) {
+  const float2 p = __fmul2_rn(a.hi, b.hi);
+  const float2 e = __ffma2_rn(a.hi, b.lo, __ffma2_rn(a.lo, b.hi, __ffma2_rn(a.hi, b.hi, f2(-p.x, -p.y))));
+  return df2_fast(p, e);
+}
+__device__ __forceinline__ DF2 df2_diff(float2 a, float2 b) { return df2_two_sum(a, f2(-b.x, -b.y)); }
+__device__ __forceinline__ DF2 df2_splat(DF a) { return DF2{f2(a.hi, a.hi), f2(a.lo, a.lo)}; }
+
 // G p1 at a node of level k in double-FP32 (the gradient of k_pres_correct) from the pressure of the four dual cells
 // around it below (l: (x-1, y-1), (x, y-1), (x-1, y), (x, y)) and above (h, the same order).
 __device__ __forceinline__ void df_gradient_of(const RunDesc& R, int k, float l0, float l1, float l2, float l3, float h0, float h1,
@@ -768,8 +794,12 @@ __device__ __forceinline__ void df_gradient_of(const RunDesc& R, int k, float l0
   const DF wlo = k > 0 ? DF{lvl(R, L_WLO, k), lvl(R, L_WLO_LO, k)} : DF{0.f, 0.f};
   const DF whi = k < nz - 1 ? DF{lvl(R, L_WHI, k), lvl(R, L_WHI_LO, k)} : DF{0.f, 0.f};
   const DF qx{.25f * R.inv_dx, .25f * R.inv_dx_lo}, qy{.25f * R.inv_dy, .25f * R.inv_dy_lo};
-  gx = df_mul(df_add(df_mul(wlo, df_add(df_diff(l1, l0), df_diff(l3, l2))), df_mul(whi, df_add(df_diff(h1, h0), df_diff(h3, h2)))), qx);
-  gy = df_mul(df_add(df_mul(wlo, df_add(df_diff(l2, l0), df_diff(l3, l1))), df_mul(whi, df_add(df_diff(h2, h0), df_diff(h3, h1)))), qy);
+  // gx and gy as the two lanes of one packed evaluation
+  const DF2 W0 = df2_splat(wlo), W1 = df2_splat(whi), Q{f2(qx.hi, qy.hi), f2(qx.lo, qy.lo)};
+  const DF2 g = df2_mul(df2_add(df2_mul(W0, df2_add(df2_diff(f2(l1, l2), f2(l0, l0)), df2_diff(f2(l3, l3), f2(l2, l1)))),
+                                df2_mul(W1, df2_add(df2_diff(f2(h1, h2), f2(h0, h0)), df2_diff(f2(h3, h3), f2(h2, h1))))), Q);
+  gx = DF{g.hi.x, g.lo.x};
+  gy = DF{g.hi.y, g.lo.y};
   gz = DF{0.f, 0.f};
   if (k > 0 && k < nz - 1) {
     const DF s = df_add(df_add(df_diff(h0, l0), df_diff(h1, l1)), df_add(df_diff(h2, l2), df_diff(h3, l3)));
@@ -833,12 +863,18 @@ __global__ void __launch_bounds__(320) k_refine_residual(const RunDesc* __restri
         const size_t i = (size_t)k * layer + gx + gy * nx;
         const float uin[3] = {u[i], v[i], w[i]};
         const bool own = nx_ < TX && ny_ < TY && k < z1;
+        DF r[3];
+        {  // u and v as the lanes of one packed evaluation (df_sub(a, b) = df_add(a, -b))
+          const DF2 m = df2_mul(df2_splat(dt), DF2{f2(g[0].hi, g[1].hi), f2(g[0].lo, g[1].lo)});
+          const DF2 uv = df2_add(DF2{f2(uin[0], uin[1]), f2(0.f, 0.f)}, DF2{f2(-m.hi.x, -m.hi.y), f2(-m.lo.x, -m.lo.y)});
+          r[0] = DF{uv.hi.x, uv.lo.x}; r[1] = DF{uv.hi.y, uv.lo.y};
+        }
+        r[2] = df_sub(DF{uin[2], 0.f}, df_mul(dt, g[2]));
 #pragma unroll
         for (int d = 0; d < 3; d++) {
-          const DF r = df_sub(DF{uin[d], 0.f}, df_mul(dt, g[d]));
-          V[(2 * d) * NN + e] = r.hi;
-          V[(2 * d + 1) * NN + e] = r.lo;
-          if (own) { field(R, 1, U + d)[i] = r.hi; field(R, 2, U + d)[i] = r.lo; }
+          V[(2 * d) * NN + e] = r[d].hi;
+          V[(2 * d + 1) * NN + e] = r[d].lo;
+          if (own) { field(R, 1, U + d)[i] = r[d].hi; field(R, 2, U + d)[i] = r[d].lo; }
         }
       }
       __syncthreads();
@@ -853,10 +889,11 @@ __global__ void __launch_bounds__(320) k_refine_residual(const RunDesc* __restri
         const DF r0{.25f * lvl(R, L_RHO, kc), .25f * lvl(R, L_RHO_LO, kc)}, r1{.25f * lvl(R, L_RHO, kc + 1), .25f * lvl(R, L_RHO_LO, kc + 1)};
         const DF idz{lvl(R, L_INV_DZS, kc), lvl(R, L_INV_DZS_LO, kc)};
         const float *hu0 = B0, *hv0 = B0 + 2 * NN, *hw0 = B0 + 4 * NN, *hu1 = B1, *hv1 = B1 + 2 * NN, *hw1 = B1 + 4 * NN;
-        const DF ddx = df_mul(df_add(df_mul(r0, df_add(df_diff(hu0[b], hu0[a]), df_diff(hu0[f], hu0[e]))),
-                                     df_mul(r1, df_add(df_diff(hu1[b], hu1[a]), df_diff(hu1[f], hu1[e])))), idx);
-        const DF ddy = df_mul(df_add(df_mul(r0, df_add(df_diff(hv0[e], hv0[a]), df_diff(hv0[f], hv0[b]))),
-                                     df_mul(r1, df_add(df_diff(hv1[e], hv1[a]), df_diff(hv1[f], hv1[b])))), idy);
+        // ddx and ddy as the two lanes of one packed evaluation
+        const DF2 dxy = df2_mul(df2_add(df2_mul(df2_splat(r0), df2_add(df2_diff(f2(hu0[b], hv0[e]), f2(hu0[a], hv0[a])), df2_diff(f2(hu0[f], hv0[f]), f2(hu0[e], hv0[b])))),
+                                        df2_mul(df2_splat(r1), df2_add(df2_diff(f2(hu1[b], hv1[e]), f2(hu1[a], hv1[a])), df2_diff(f2(hu1[f], hv1[f]), f2(hu1[e], hv1[b]))))),
+                                DF2{f2(idx.hi, idy.hi), f2(idx.lo, idy.lo)});
+        const DF ddx{dxy.hi.x, dxy.lo.x}, ddy{dxy.hi.y, dxy.lo.y};
         const DF up = df_add(df_add(DF{hw1[a], 0.f}, DF{hw1[b], 0.f}), df_add(DF{hw1[e], 0.f}, DF{hw1[f], 0.f}));
         const DF dn = df_add(df_add(DF{hw0[a], 0.f}, DF{hw0[b], 0.f}), df_add(DF{hw0[e], 0.f}, DF{hw0[f], 0.f}));
         const DF ddz = df_mul(df_sub(df_mul(r1, up), df_mul(r0, dn)), idz);
@@ -881,7 +918,10 @@ __global__ void k_refine_correct(const RunDesc* __restrict__ runs, const int4* i
     const RunDesc& R = runs[items[it].x];
     if (R.cnt[C_FAILED] || !(R.flags & RF_REFINE)) continue;
     const int nx = R.nx, ny = R.ny, nz = R.nz, layer = R.layer, i0 = items[it].y * CHUNK, i1 = min(R.n, i0 + CHUNK);
-    const float* p = R.pres2;
+    const float* __restrict__ p = R.pres2;
+    const float* __restrict__ hi[3] = {field(R, 1, U), field(R, 1, V), field(R, 1, W)};
+    const float* __restrict__ lo[3] = {field(R, 2, U), field(R, 2, V), field(R, 2, W)};
+    float* __restrict__ out3[3] = {field(R, set, U), field(R, set, V), field(R, set, W)};
     const float dt = R.dt;
     int clipped = 0;
     for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
@@ -897,13 +937,13 @@ __global__ void k_refine_correct(const RunDesc* __restrict__ runs, const int4* i
         k > 0 && k < nz - 1 ? ((H[im + jm] - L[im + jm]) + (H[x + jm] - L[x + jm]) + (H[im + j0] - L[im + j0]) + (H[x + j0] - L[x + j0])) * (.25f * lvl(R, L_INV_HZ, k)) : 0.f};
       float out[3];
 #pragma unroll
-      for (int d = 0; d < 3; d++) out[d] = __fadd_rn(__fmaf_rn(-dt, g[d], field(R, 1, U + d)[i]), field(R, 2, U + d)[i]);
+      for (int d = 0; d < 3; d++) out[d] = __fadd_rn(__fmaf_rn(-dt, g[d], hi[d][i]), lo[d][i]);
       const float UL = 120.f, WL = 100.f;
       if (out[0] < -UL || out[0] > UL) { out[0] = fmaxf(-UL, fminf(UL, out[0])); clipped++; }
       if (out[1] < -UL || out[1] > UL) { out[1] = fmaxf(-UL, fminf(UL, out[1])); clipped++; }
       if (out[2] < -WL || out[2] > WL) { out[2] = fmaxf(-WL, fminf(WL, out[2])); clipped++; }
 #pragma unroll
-      for (int d = 0; d < 3; d++) field(R, set, U + d)[i] = out[d];
+      for (int d = 0; d < 3; d++) out3[d][i] = out[d];
     }
     clipped = warpSum(clipped);
     if ((threadIdx.x & 31) == 0 && clipped) atomicAdd(&R.cnt[C_CLIPPED], (unsigned long long)clipped);
@@ -1059,10 +1099,18 @@ __global__ void k_viscosity(const RunDesc* __restrict__ runs, const int4* items,
     const RunDesc& R = runs[items[it].x];
     if (R.cnt[C_FAILED]) continue;
     const int nx = R.nx, ny = R.ny, nz = R.nz, layer = R.layer, i0 = items[it].y * CHUNK, i1 = min(R.n, i0 + CHUNK);
-    const float *u = field(R, set, U), *v = field(R, set, V), *w = field(R, set, W), *th = field(R, set, THETA);
-    const float *qv = field(R, set, Q), *cl = field(R, set, CLOUD), *ic = field(R, set, ICE);
-    float *km = R.kmkh, *kh = R.kmkh + R.n;
+    const float* __restrict__ u = field(R, set, U);
+    const float* __restrict__ v = field(R, set, V);
+    const float* __restrict__ w = field(R, set, W);
+    const float* __restrict__ th = field(R, set, THETA);
+    const float* __restrict__ qv = field(R, set, Q);
+    const float* __restrict__ cl = field(R, set, CLOUD);
+    const float* __restrict__ ic = field(R, set, ICE);
+    float* __restrict__ km = R.kmkh;
+    float* __restrict__ kh = R.kmkh + R.n;
     const bool ice = R.flags & RF_ICE;
+    // (the outputs do not alias the inputs, so the loads of two nodes can be issued together)
+#pragma unroll 2
     for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
       int z = i / layer, c = i - z * layer, y = c / nx, x = c - y * nx, l = z * layer;
       int e = wrap(x + 1, nx) + y * nx + l, wst = wrap(x - 1, nx) + y * nx + l, n = x + wrap(y + 1, ny) * nx + l, s = x + wrap(y - 1, ny) * nx + l;
