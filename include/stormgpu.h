@@ -15,6 +15,7 @@
  */
 #ifndef STORMGPU_H
 #define STORMGPU_H
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -115,6 +116,34 @@ int sg_batch_write_packed(sg_context* ctx, const sg_run* runs, int n, uint32_t m
 int sg_batch_read_packed(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, float* host);
 /* precipitation, hailGround, hailSize: nx*ny each (nullable); src/core/model.ts:253, :262. */
 int sg_run_read_columns(sg_context* ctx, sg_run run, float* precipitation, float* hail_ground, float* hail_size);
+/* The same columns written (each pointer nullable: that column is left as it is). */
+int sg_run_write_columns(sg_context* ctx, sg_run run, const float* precipitation, const float* hail_ground, const float* hail_size);
+/* The run's grid size. */
+int sg_run_shape(sg_context* ctx, sg_run run, int32_t* nx, int32_t* ny, int32_t* nz);
+
+/* ---- saved state (.meteolab files: saveState / readState / applyState, src/core/state.ts:43-83). The image is 'MLAB',
+ * the JSON header's length (uint32 LE), the JSON header, zero padding to 4 bytes, the fields as float32 in the file's
+ * STATE_FIELDS order (state.ts:9; the charge fields and two-moment moments, which the configured step does not carry,
+ * are written as zeros and ignored on loading) and the ground columns (precipitation, hailGround, hailSize). */
+typedef struct sg_state_info {
+  int32_t version, nx, ny, nz, nfields, reserved;
+  double time, persisted;
+  uint64_t data_offset;
+} sg_state_info;
+/* readState's checks alone (no context, no device): SG_OK and the header's values, or SG_ERR_INVALID with the
+ * reference's message in err ("this is not a MeteoLab state file", "the file is truncated", "the file's header is
+ * damaged", "unknown file format or version", "the file's size does not match the grid"). */
+int sg_state_parse(const uint8_t* image, size_t len, sg_state_info* out, char* err, size_t err_len);
+/* saveState of one run (version 5): config_json is the run's SimConfig as JSON text (nullable), time the model time
+ * and persisted how long the rotation has held (the host keeps both). out == NULL or cap too small: *size gets the
+ * bytes needed and nothing is written (SG_OK, or SG_ERR_INVALID when cap is too small). One gather on the device and
+ * one copy to the host. */
+int sg_run_save_state(sg_context* ctx, sg_run run, const char* config_json, double time, double persisted, uint8_t* out,
+                      size_t cap, size_t* size);
+/* readState + applyState into a run of the same grid: the fields a file of its version holds (the others zero, as
+ * the reference fills them) and the columns, one copy to the device and one scatter; info gets the header's values
+ * (time, persisted: the host's to keep). A different grid: SG_ERR_INVALID, "the file's grid is AxBxC, the run's DxExF". */
+int sg_run_load_state(sg_context* ctx, sg_run run, const uint8_t* image, size_t len, sg_state_info* info);
 /* The projection pressure of the last final projection, nx*ny*(nz-1) values (AtmosphereModel.pressure, :247). */
 int sg_run_read_pressure(sg_context* ctx, sg_run run, double* p);
 int sg_run_status(sg_context* ctx, sg_run run, sg_run_counters* out);

@@ -13,8 +13,11 @@
  *   readFields(ctx, run, fields: Float32Array[13]) / writeFields(ctx, run, fields)
  *   status(ctx, run) -> {steps, clipped, negativeFilled, failed}
  *   retire(ctx, run), destroyContext(ctx)
+ *   saveState(ctx, run, configJson: string, time, persisted) -> ArrayBuffer      (saveState, src/core/state.ts:43)
+ *   loadState(ctx, run, image: ArrayBuffer) -> {version, time, persisted}        (readState + applyState, :55-83)
  */
 #include <node_api.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #include "../../../include/stormgpu.h"
@@ -179,6 +182,43 @@ static napi_value retire(napi_env env, napi_callback_info info) {
   return NULL;
 }
 
+static napi_value save_state(napi_env env, napi_callback_info info) {
+  size_t argc = 5; napi_value argv[5]; int32_t run; double time = 0, persisted = 0; size_t jl = 0, size = 0;
+  CHECK(env, napi_get_cb_info(env, info, &argc, argv, NULL, NULL));
+  sg_context* ctx = ctx_of(env, argv[0]);
+  napi_get_value_int32(env, argv[1], &run);
+  CHECK(env, napi_get_value_string_utf8(env, argv[2], NULL, 0, &jl));
+  char* config = (char*)malloc(jl + 1);
+  if (!config) { napi_throw_error(env, NULL, "out of memory"); return NULL; }
+  napi_get_value_string_utf8(env, argv[2], config, jl + 1, &jl);
+  if (argc > 3) napi_get_value_double(env, argv[3], &time);
+  if (argc > 4) napi_get_value_double(env, argv[4], &persisted);
+  int st = sg_run_save_state(ctx, run, config, time, persisted, NULL, 0, &size);
+  napi_value ab; void* data = NULL;
+  if (!st && napi_create_arraybuffer(env, size, &data, &ab) != napi_ok) { free(config); napi_throw_error(env, NULL, "arraybuffer"); return NULL; }
+  if (!st) st = sg_run_save_state(ctx, run, config, time, persisted, (uint8_t*)data, size, &size);
+  free(config);
+  if (st) return throw_status(env, ctx, st);
+  return ab;
+}
+
+static napi_value load_state(napi_env env, napi_callback_info info) {
+  size_t argc = 3; napi_value argv[3]; int32_t run; void* data; size_t len;
+  CHECK(env, napi_get_cb_info(env, info, &argc, argv, NULL, NULL));
+  sg_context* ctx = ctx_of(env, argv[0]);
+  napi_get_value_int32(env, argv[1], &run);
+  CHECK(env, napi_get_arraybuffer_info(env, argv[2], &data, &len));
+  sg_state_info h;
+  int st = sg_run_load_state(ctx, run, (const uint8_t*)data, len, &h);
+  if (st) return throw_status(env, ctx, st);
+  napi_value o, v;
+  CHECK(env, napi_create_object(env, &o));
+  napi_create_int32(env, h.version, &v); napi_set_named_property(env, o, "version", v);
+  napi_create_double(env, h.time, &v); napi_set_named_property(env, o, "time", v);
+  napi_create_double(env, h.persisted, &v); napi_set_named_property(env, o, "persisted", v);
+  return o;
+}
+
 static napi_value destroy_context(napi_env env, napi_callback_info info) {
   size_t argc = 1; napi_value argv[1];
   CHECK(env, napi_get_cb_info(env, info, &argc, argv, NULL, NULL));
@@ -192,6 +232,7 @@ static napi_value init(napi_env env, napi_value exports) {
     {"step", 0, step, 0, 0, 0, napi_default, 0}, {"readFields", 0, read_fields, 0, 0, 0, napi_default, 0},
     {"writeFields", 0, write_fields, 0, 0, 0, napi_default, 0}, {"status", 0, status, 0, 0, 0, napi_default, 0},
     {"retire", 0, retire, 0, 0, 0, napi_default, 0}, {"destroyContext", 0, destroy_context, 0, 0, 0, napi_default, 0},
+    {"saveState", 0, save_state, 0, 0, 0, napi_default, 0}, {"loadState", 0, load_state, 0, 0, 0, napi_default, 0},
   };
   napi_define_properties(env, exports, sizeof d / sizeof d[0], d);
   return exports;

@@ -19,6 +19,7 @@
 #include "sg_common.cuh"
 #include "sg_fft.cuh"
 #include "sg_kernels.h"
+#include "sg_state.h"
 #include "sg_physics.cuh"
 
 using namespace sg;
@@ -885,6 +886,95 @@ int sg_run_read_columns(sg_context* ctx, sg_run run, float* precipitation, float
   float* dst[3] = {precipitation, hail_ground, hail_size};
   for (int k = 0; k < 3; k++) if (dst[k]) CK(cudaMemcpyAsync(dst[k], r->desc.cols + k * layer, layer * 4, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  return SG_OK;
+}
+
+int sg_run_write_columns(sg_context* ctx, sg_run run, const float* precipitation, const float* hail_ground, const float* hail_size) {
+  if (!ctx) return SG_ERR_INVALID;
+  Run* r = find(ctx, run);
+  if (!r) return fail(ctx, SG_ERR_NOT_FOUND, "no run " + std::to_string(run));
+  size_t layer = (size_t)r->nx * r->ny;
+  const float* src[3] = {precipitation, hail_ground, hail_size};
+  for (int k = 0; k < 3; k++) if (src[k]) CK(cudaMemcpyAsync(r->desc.cols + k * layer, src[k], layer * 4, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return SG_OK;
+}
+
+int sg_run_shape(sg_context* ctx, sg_run run, int32_t* nx, int32_t* ny, int32_t* nz) {
+  if (!ctx) return SG_ERR_INVALID;
+  Run* r = find(ctx, run);
+  if (!r) return fail(ctx, SG_ERR_NOT_FOUND, "no run " + std::to_string(run));
+  if (nx) *nx = r->nx;
+  if (ny) *ny = r->ny;
+  if (nz) *nz = r->nz;
+  return SG_OK;
+}
+
+// saveState (src/core/state.ts:43-53): the carried fields gathered by the packed transfer (one kernel, one copy),
+// placed in STATE_FIELDS order on the host, the fields the step does not carry written as zeros.
+int sg_run_save_state(sg_context* ctx, sg_run run, const char* config_json, double time, double persisted, uint8_t* out,
+                      size_t cap, size_t* size) {
+  if (!ctx || !size) return SG_ERR_INVALID;
+  Run* r = find(ctx, run);
+  if (!r) return fail(ctx, SG_ERR_NOT_FOUND, "no run " + std::to_string(run));
+  if (!state::json_valid(config_json)) return fail(ctx, SG_ERR_INVALID, "config_json is not one JSON value");
+  sg_run_counters c;
+  int st = sg_run_status(ctx, run, &c);
+  if (st != SG_OK && st != SG_ERR_NONFINITE) return st;
+  const double water[4] = {c.water_condensed, c.water_evaporated, c.water_rain_evaporated, c.water_surface};
+  const std::string json = state::header_json(config_json, time, persisted, r->nx, r->ny, r->nz, water);
+  const size_t need = state::image_bytes(json.size(), state::VERSION, r->nx, r->ny, r->nz);
+  *size = need;
+  if (!out) return SG_OK;
+  if (cap < need) return fail(ctx, SG_ERR_INVALID, "the buffer holds " + std::to_string(cap) + " bytes, the image needs " + std::to_string(need));
+  const size_t n = (size_t)r->nx * r->ny * r->nz, layer = (size_t)r->nx * r->ny, off = state::data_offset(json.size());
+  std::vector<float> fields((size_t)SG_NFIELDS * n), cols(3 * layer);
+  if ((st = sg_batch_read_packed(ctx, &run, 1, SG_ALL_FIELDS, fields.data())) != SG_OK) return st;
+  if ((st = sg_run_read_columns(ctx, run, cols.data(), cols.data() + layer, cols.data() + 2 * layer)) != SG_OK) return st;
+  std::memset(out, 0, off);
+  std::memcpy(out, "MLAB", 4);
+  const uint32_t jl = (uint32_t)json.size();
+  const uint8_t len4[4] = {(uint8_t)jl, (uint8_t)(jl >> 8), (uint8_t)(jl >> 16), (uint8_t)(jl >> 24)};
+  std::memcpy(out + 4, len4, 4);
+  std::memcpy(out + 8, json.data(), json.size());
+  for (int k = 0; k < state::NSTATE; k++) {
+    uint8_t* dst = out + off + (size_t)k * n * 4;
+    const int f = state::carried_of(k);
+    if (f >= 0) std::memcpy(dst, fields.data() + (size_t)f * n, n * 4); else std::memset(dst, 0, n * 4);
+  }
+  std::memcpy(out + off + (size_t)state::NSTATE * n * 4, cols.data(), 3 * layer * 4);
+  return SG_OK;
+}
+
+// readState + applyState (src/core/state.ts:55-83) into a run of the same grid: the file's fields (those an older
+// version lacks as zeros, state.ts:70), the columns; the packed transfer scatters them (one copy, one kernel).
+int sg_run_load_state(sg_context* ctx, sg_run run, const uint8_t* image, size_t len, sg_state_info* info) {
+  if (!ctx) return SG_ERR_INVALID;
+  Run* r = find(ctx, run);
+  if (!r) return fail(ctx, SG_ERR_NOT_FOUND, "no run " + std::to_string(run));
+  state::Info h;
+  const std::string msg = state::parse(image, len, h);
+  if (!msg.empty()) return fail(ctx, SG_ERR_INVALID, msg);
+  if (h.nx != r->nx || h.ny != r->ny || h.nz != r->nz)
+    return fail(ctx, SG_ERR_INVALID, "the file's grid is " + std::to_string(h.nx) + "x" + std::to_string(h.ny) + "x" + std::to_string(h.nz) +
+                                         ", the run's " + std::to_string(r->nx) + "x" + std::to_string(r->ny) + "x" + std::to_string(r->nz));
+  const size_t n = (size_t)r->nx * r->ny * r->nz, layer = (size_t)r->nx * r->ny;
+  std::vector<float> fields((size_t)SG_NFIELDS * n, 0.f), cols(3 * layer);
+  for (int k = 0; k < h.nfields; k++) {
+    const int f = state::carried_of(k);
+    if (f >= 0) std::memcpy(fields.data() + (size_t)f * n, image + h.data_offset + (size_t)k * n * 4, n * 4);
+  }
+  std::memcpy(cols.data(), image + h.data_offset + (size_t)h.nfields * n * 4, 3 * layer * 4);
+  int st = sg_batch_write_packed(ctx, &run, 1, SG_ALL_FIELDS, fields.data());
+  if (st != SG_OK) return st;
+  if ((st = sg_run_write_columns(ctx, run, cols.data(), cols.data() + layer, cols.data() + 2 * layer)) != SG_OK) return st;
+  // the water budget goes on from the file's flows (state.ts:77)
+  CK(cudaMemcpyAsync(r->desc.acc + A_WATER, h.water, 3 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (info) {
+    info->version = h.version; info->nx = h.nx; info->ny = h.ny; info->nz = h.nz; info->nfields = h.nfields;
+    info->time = h.time; info->persisted = h.persisted; info->data_offset = (uint64_t)h.data_offset;
+  }
   return SG_OK;
 }
 

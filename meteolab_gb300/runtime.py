@@ -7,6 +7,7 @@ CPU fallback: without the built library or a CUDA device every call raises ``Sto
 from __future__ import annotations
 
 import ctypes as C
+import json
 import os
 import threading
 from typing import Dict, Iterable, List, Optional, Sequence
@@ -43,6 +44,11 @@ class SgSwitches(C.Structure):
                 ("frame_v", C.c_double)] + [(k, C.c_int32) for k in ("loading", "evaporation", "rain_formation",
                                                                          "anisotropic", "vertical_dz", "durran_klemp",
                                                                          "pressure_in_stages", "ice", "refine_projection")]
+
+
+class SgStateInfo(C.Structure):
+    _fields_ = [("version", C.c_int32), ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("nfields", C.c_int32),
+                ("reserved", C.c_int32), ("time", C.c_double), ("persisted", C.c_double), ("data_offset", C.c_uint64)]
 
 
 class SgCounters(C.Structure):
@@ -104,6 +110,12 @@ def load():
             L.sg_server_collect.argtypes = [vp, i64, C.c_uint32, C.POINTER(_FP), _FP]
             L.sg_server_set_quantum.argtypes = [vp, i32]
             L.sg_server_last_steps.argtypes = [vp]
+            L.sg_run_write_columns.argtypes = [vp, C.c_int32, _FP, _FP, _FP]
+            L.sg_run_shape.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+            L.sg_state_parse.argtypes = [C.c_char_p, C.c_size_t, C.POINTER(SgStateInfo), C.c_char_p, C.c_size_t]
+            L.sg_run_save_state.argtypes = [vp, C.c_int32, C.c_char_p, C.c_double, C.c_double, C.c_char_p, C.c_size_t,
+                                            C.POINTER(C.c_size_t)]
+            L.sg_run_load_state.argtypes = [vp, C.c_int32, C.c_char_p, C.c_size_t, C.POINTER(SgStateInfo)]
             _lib = L
     return _lib
 
@@ -332,6 +344,44 @@ class Run:
         out = C.c_double()
         self.ctx.check(load().sg_run_divergence(self.ctx.h, self.id, C.byref(out)), "divergence")
         return out.value
+
+    def write_columns(self, cols: Dict[str, np.ndarray]):
+        keep = [np.ascontiguousarray(cols[k], dtype=np.float32) if k in cols else None for k in ("precipitation", "hailGround", "hailSize")]
+        ptrs = [a.ctypes.data_as(_FP) if a is not None else None for a in keep]
+        self.ctx.check(load().sg_run_write_columns(self.ctx.h, self.id, *ptrs), "write columns")
+
+    def save_state(self, config: Optional[dict] = None, persisted: float = 0.0) -> bytes:
+        """saveState (src/core/state.ts:43-53): the run as a .meteolab image, at this run's model time."""
+        cfg = json.dumps(config, separators=(",", ":")).encode() if config is not None else None
+        size = C.c_size_t()
+        self.ctx.check(load().sg_run_save_state(self.ctx.h, self.id, cfg, self.time, persisted, None, 0, C.byref(size)), "save state")
+        buf = C.create_string_buffer(size.value)
+        self.ctx.check(load().sg_run_save_state(self.ctx.h, self.id, cfg, self.time, persisted, buf, size.value, C.byref(size)),
+                       "save state")
+        return buf.raw[:size.value]
+
+    def load_state(self, image: bytes) -> dict:
+        """readState + applyState (src/core/state.ts:55-83): the image's fields and columns into this run; the run's
+        model time becomes the file's."""
+        info = SgStateInfo()
+        self.ctx.check(load().sg_run_load_state(self.ctx.h, self.id, image, len(image), C.byref(info)), "load state")
+        self.time = info.time
+        return _info_dict(info)
+
+
+def _info_dict(info: "SgStateInfo") -> dict:
+    return {k: getattr(info, k) for k, _ in SgStateInfo._fields_ if k != "reserved"}
+
+
+def parse_state(image: bytes) -> dict:
+    """readState's checks alone (sg_state_parse; no context, no device): the header's values, or StormGpuError with
+    the reference's message."""
+    info = SgStateInfo()
+    err = C.create_string_buffer(200)
+    rc = load().sg_state_parse(image, len(image), C.byref(info), err, len(err))
+    if rc:
+        raise StormGpuError(rc, err.value.decode())
+    return _info_dict(info)
 
 
 class AtmosphereModel:
