@@ -78,6 +78,10 @@ typedef struct sg_switches {
    * projected velocity's divergence before its FP32 rounding is at rounding level as with the reference's FP64 solve;
    * 0: one FP32-transform solve (residual a few 1e-6 of the divergence removed). No counterpart switch in the reference. */
   int32_t refine_projection;
+  /* 1: after every step the rotation tracking (updateRotation, src/core/model.ts:1609-1648, which the reference's step
+   * runs in afterStep) and the run's swaths (addSwaths, src/ensemble/member.ts:71-89) on the device; read with
+   * sg_run_rotation / sg_run_read_swaths. 0: neither (two launches a step fewer). */
+  int32_t rotation;
 } sg_switches;
 
 /* Per-run counters (AtmosphereModel.clipped, negativeFilled, water, src/core/model.ts:236, :269-271). */
@@ -120,6 +124,29 @@ int sg_run_read_columns(sg_context* ctx, sg_run run, float* precipitation, float
 int sg_run_write_columns(sg_context* ctx, sg_run run, const float* precipitation, const float* hail_ground, const float* hail_size);
 /* The run's grid size. */
 int sg_run_shape(sg_context* ctx, sg_run run, int32_t* nx, int32_t* ny, int32_t* nz);
+
+/* ---- per-run diagnostics (runs with switches.rotation). The rotation state after the last step (RotationState,
+ * src/core/model.ts:263; the reference's field names) and the model time the device keeps for the swaths' ground shift. */
+typedef struct sg_rotation {
+  double uh, x, y, anticyclonic, persisted, uh01, uh03, low, core_zeta, core_uh, core_anti, time;
+} sg_rotation;
+/* uh_column: nx*ny floats (nullable), the 2-5 km updraught helicity of every column (model.uhColumn). */
+int sg_run_rotation(sg_context* ctx, sg_run run, sg_rotation* out, float* uh_column);
+/* refreshRotation (src/core/model.ts:1607): the rotation state from the fields as they are (after fields were written
+ * or a state loaded), the time the rotation has held and the model time kept, the swaths untouched. */
+int sg_run_refresh_rotation(sg_context* ctx, sg_run run);
+/* The swaths since the run began or since the last reset (MemberResult.gustMax / uhMax, src/ensemble/member.ts:20-21):
+ * per ground column the strongest surface wind (m/s) and the strongest UH 2-5 km (m2/s2); nullable outputs. */
+int sg_run_read_swaths(sg_context* ctx, sg_run run, float* gust_max, float* uh_max);
+int sg_run_reset_swaths(sg_context* ctx, sg_run run);
+/* diagnostics() (src/core/model.ts:1672-1696) without shear06 (a property of the sounding the host has): the domain
+ * maxima on the device, then on the host the cores (countCores, 4-connected) and the outflow deficit (rkw.ts:72-90) from
+ * five ground columns copied once. */
+typedef struct sg_diagnostics {
+  double updraft, downdraft, rain_rate, rain_total, cloud_top, thermal_top, max_cloud, cold_max, cores, outflow, outflow_low, gust,
+      hail, clipped;
+} sg_diagnostics;
+int sg_run_diagnostics(sg_context* ctx, sg_run run, sg_diagnostics* out);
 
 /* ---- saved state (.meteolab files: saveState / readState / applyState, src/core/state.ts:43-83). The image is 'MLAB',
  * the JSON header's length (uint32 LE), the JSON header, zero padding to 4 bytes, the fields as float32 in the file's

@@ -93,6 +93,7 @@ static napi_value create_run(napi_env env, napi_callback_info info) {
   s.vertical_dz = (int32_t)get_num(env, argv[3], "verticalDz"); s.durran_klemp = (int32_t)get_num(env, argv[3], "durranKlemp");
   s.pressure_in_stages = (int32_t)get_num(env, argv[3], "pressureInStages"); s.ice = (int32_t)get_num(env, argv[3], "ice");
   s.refine_projection = (int32_t)get_num(env, argv[3], "refineProjection");
+  s.rotation = (int32_t)get_num(env, argv[3], "rotation");
   float* init[SG_NFIELDS];
   if (!fields_of(env, argv[4], init)) { napi_throw_type_error(env, NULL, "fields: 13 Float32Array"); return NULL; }
   sg_run run;

@@ -86,9 +86,23 @@ struct RunDesc {
   double* part;            // FP64 partial sums (positivity fix, water budget)
   double* acc;             // FP64 running totals: negativeFilled, water[4]
   unsigned long long* cnt; // counters: clipped, steps, failed flag
+  // per-run diagnostics (RF_ROTATION): columns [DG_COUNT][layer] and the rotation state and accumulators
+  float* diag;
+  double* rot;
+  int uh_z0, uh_z1, uh_top1, uh_top3;  // 2-5 km levels, the last levels at or below 1 and 3 km (src/core/model.ts:389, :1612)
+  int core_lo, core_hi;                // the cloudy-core levels of countCores (:1653)
+  float meso_zeta;                     // mesoCoreZeta(dx) (:129)
+  float pad2;
 };
 enum RunFlags { RF_LOADING = 1, RF_EVAP = 2, RF_RAINFORM = 4, RF_ANISO = 8, RF_VDZ = 16, RF_DK = 32, RF_STAGES = 64, RF_ICE = 128,
-                RF_REFINE = 256 };
+                RF_REFINE = 256, RF_ROTATION = 512 };
+// diag columns: the UH column, the core sums, the swaths, the core labels; then the ground columns of a sample
+enum DiagColumn { DG_UH = 0, DG_COREW, DG_COREWZ, DG_GUST_MAX, DG_UH_MAX, DG_LABEL, DG_RATE, DG_HAIL, DG_GUST, DG_THV, DG_MASK, DG_COUNT };
+// rot layout (doubles): the rotation state (src/core/model.ts:263), the run's model time, then the step's keys and the
+// sample's maxima (stored as 64-bit keys: non-negative values order as their bits)
+enum RotSlot { R_UH = 0, R_X, R_Y, R_ANTI, R_PERSISTED, R_UH01, R_UH03, R_LOW, R_CZETA, R_CUH, R_CANTI, R_TIME,
+               K_UH = 12, K_01, K_MIN, K_03,
+               M_UP = 16, M_DOWN, M_CLOUD, M_TOP, M_THERMAL, M_COLD, R_COUNT = 24 };
 // scr layout
 enum Scratch { S_COURANT = 0, S_FILL = 4, S_COUNT = 16 };
 // cnt layout

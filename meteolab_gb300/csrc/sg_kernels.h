@@ -54,6 +54,11 @@ void launch_mix(const Launch& L, int in, int TX, int TY);
 size_t mix_smem(int TX, int TY);
 void launch_step_end(const Launch& L);
 void launch_divergence_max(const Launch& L, int set, double* out);
+// Per-run diagnostics (sg_diag.cu): the rotation tracking after a step (or a refresh that keeps the held time and the
+// model time) on COLS and RUNS items; a sample's domain maxima and ground columns on node items of one run.
+void launch_rotation_columns(const Launch& cols, int refresh);
+void launch_rotation_summary(const Launch& runs, int refresh);
+void launch_diag_sample(const Launch& L);
 cudaError_t set_smem_limits(int bytes);
 cudaError_t set_transport_smem_limits(int bytes);  // (sg_transport.cu)
 

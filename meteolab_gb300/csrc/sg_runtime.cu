@@ -33,7 +33,7 @@ const double RK3[3] = {1.0 / 3, 1.0 / 2, 1.0};
 size_t align(size_t x) { return (x + ALIGN - 1) / ALIGN * ALIGN; }
 
 struct Layout {
-  size_t fld, faces, kmkh, phi, pres, pres2, spec, cols, lv, lv64, triF, triP, ab, twx, twy, scr, part, acc, cnt, items, total;
+  size_t fld, faces, kmkh, phi, pres, pres2, spec, cols, lv, lv64, triF, triP, ab, twx, twy, scr, part, acc, cnt, items, diag, rot, total;
 };
 Layout layout(int nx, int ny, int nz) {
   Layout L; size_t n = (size_t)nx * ny * nz, layer = (size_t)nx * ny, nm = nx / 2 + 1, nch = (n + CHUNK - 1) / CHUNK, o = 0;
@@ -45,6 +45,7 @@ Layout layout(int nx, int ny, int nz) {
   L.twx = take(nx * 8); L.twy = take(ny * 8); L.scr = take(64 * 4); L.part = take((nch * NCONS * 3 + nch * 4) * 8);
   L.acc = take(A_COUNT * 8); L.cnt = take(C_COUNT * 8);
   L.items = take(nch * 16);  // the run's own per-node work items (field conversions outside a batch plan)
+  L.diag = take((size_t)DG_COUNT * layer * 4); L.rot = take(R_COUNT * 8);
   L.total = o;
   return L;
 }
@@ -71,6 +72,7 @@ struct Plan {
   int refTX = 16, refTY = 8;                                          // refinement tile
   bool layerfft = false;                                              // 2-D transforms per layer (see enqueue_part)
   bool refine = false;                                                // some run refines its final projection
+  bool rotation = false;                                              // some run tracks its rotation and swaths
   bool tuned = false;                                                 // TX, TY, wenoG chosen by timing
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -257,7 +259,21 @@ void build_tables(const sg_grid* g, const sg_base_state* b, const sg_switches* s
   d.lenH2 = (float)std::pow(cs * std::sqrt(dx * dy), 2); d.capH = (float)(.05 * std::pow(std::min(dx, dy), 2) / dt); d.rho0 = (float)rho[0];
   d.flags = (sw->loading ? RF_LOADING : 0) | (sw->evaporation ? RF_EVAP : 0) | (sw->rain_formation ? RF_RAINFORM : 0) | (sw->anisotropic ? RF_ANISO : 0) |
             (sw->vertical_dz ? RF_VDZ : 0) | (sw->durran_klemp ? RF_DK : 0) | (sw->pressure_in_stages ? RF_STAGES : 0) | (sw->ice ? RF_ICE : 0) |
-            (sw->refine_projection ? RF_REFINE : 0);
+            (sw->refine_projection ? RF_REFINE : 0) | (sw->rotation ? RF_ROTATION : 0);
+  // the rotation tracking's levels (src/core/model.ts:389, :1612) and countCores' (:1653), its threshold (:129)
+  const double* zl = g->zs;
+  d.uh_z0 = -1; d.uh_z1 = -1; d.uh_top1 = -1; d.uh_top3 = -1; d.core_lo = -1;
+  int coreLast = -1;
+  for (int z = 0; z < nz; z++) {
+    if (d.uh_z0 < 0 && zl[z] >= 2000) d.uh_z0 = z;
+    if (zl[z] <= 5000) d.uh_z1 = z;
+    if (zl[z] <= 1000) d.uh_top1 = z;
+    if (zl[z] <= 3000) d.uh_top3 = z;
+    if (d.core_lo < 0 && zl[z] >= 1900) d.core_lo = z;
+    if (zl[z] <= 6600) coreLast = z;
+  }
+  d.core_hi = std::min(nz - 3, coreLast);
+  d.meso_zeta = (float)(3e-3 * std::max(1.0, 1200.0 / dx));
 }
 
 int validate(sg_context* ctx, const sg_grid* g, const sg_base_state* b, const sg_switches* sw) {
@@ -341,6 +357,7 @@ int build_plan(sg_context* ctx, const std::vector<int>& slots, Plan& P) {
     for (int m = 0; m < r.nx / 2 + 1; m++) all[FAM_MODES].push_back(make_int4(s, m, 0, 0));
     all[FAM_RUNS].push_back(make_int4(s, 0, 0, 0));
     if (r.desc.flags & RF_REFINE) P.refine = true;
+    if (r.desc.flags & RF_ROTATION) P.rotation = true;
   }
   // mixing items: (run, tile, z0, z1), the column in four level ranges
   P.mixTX = all40 ? 40 : 32; P.mixTY = 8;
@@ -520,6 +537,10 @@ void enqueue_part(sg_context* ctx, const Plan& P, int part, Hook hook) {
   } else if (part == 5) {
     enqueue_project(ctx, P, A, 1, st, hook);
     launch_step_end(runs); hook(17);
+    if (P.rotation) {  // afterStep (src/core/model.ts:1130-1131): the rotation tracking, and the swaths
+      launch_rotation_columns(cols, 0); hook(26);
+      launch_rotation_summary(runs, 0); hook(27);
+    }
   }
 }
 
@@ -572,11 +593,12 @@ void enqueue_step_graph(sg_context* ctx, const Plan& P) {
   enqueue_dynamics_graph(ctx, P);
   for (int part = 3; part <= 5; part++) enqueue_part(ctx, P, part, none);
 }
-const int NKERNELS = 26;
+const int NKERNELS = 28;
 const char* KERNEL_NAMES[NKERNELS] = {"fall_courant", "sediment", "face_div_xfft", "face_modes", "face_xifft", "face_correct", "transport",
                                       "pres_div_xfft", "pres_modes", "pres_xifft", "pres_correct", "fill_partial", "fill_final", "physics",
                                       "viscosity", "mix", "pres_correct_final", "step_end", "transport_weno", "transport_dynamics",
-                                      "refine_residual", "refine_unused", "refine_div_xfft", "refine_modes", "refine_xifft", "refine_correct"};
+                                      "refine_residual", "refine_unused", "refine_div_xfft", "refine_modes", "refine_xifft", "refine_correct",
+                                      "rotation_columns", "rotation_summary"};
 
 Plan* get_plan(sg_context* ctx, const std::vector<int>& slots, int* status) {
   auto it = ctx->plans.find(slots);
@@ -737,6 +759,7 @@ int sg_run_create(sg_context* ctx, const sg_grid* g, const sg_base_state* b, con
   d.tri_pres = (const double2*)(mem + Lo.triP); d.ab = (const double2*)(mem + Lo.ab); d.twx = (const float2*)(mem + Lo.twx);
   d.twy = (const float2*)(mem + Lo.twy); d.scr = (float*)(mem + Lo.scr); d.part = (double*)(mem + Lo.part); d.acc = (double*)(mem + Lo.acc);
   d.cnt = (unsigned long long*)(mem + Lo.cnt);
+  d.diag = (float*)(mem + Lo.diag); d.rot = (double*)(mem + Lo.rot);
   auto H2D = [&](size_t off, const void* src, size_t bytes) { return cudaMemcpyAsync(mem + off, src, bytes, cudaMemcpyHostToDevice, ctx->stream); };
   CK(cudaMemsetAsync(mem, 0, Lo.total, ctx->stream));
   CK(H2D(Lo.lv, T.lv.data(), T.lv.size() * 4)); CK(H2D(Lo.lv64, T.lv64.data(), T.lv64.size() * 8));
@@ -970,11 +993,132 @@ int sg_run_load_state(sg_context* ctx, sg_run run, const uint8_t* image, size_t 
   if ((st = sg_run_write_columns(ctx, run, cols.data(), cols.data() + layer, cols.data() + 2 * layer)) != SG_OK) return st;
   // the water budget goes on from the file's flows (state.ts:77)
   CK(cudaMemcpyAsync(r->desc.acc + A_WATER, h.water, 3 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  // the model time and the time the rotation has held; the rotation recomputed from the fields (state.ts:74-76)
+  const double tp[2] = {h.time, h.persisted};
+  CK(cudaMemcpyAsync(r->desc.rot + R_TIME, &tp[0], sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(r->desc.rot + R_PERSISTED, &tp[1], sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  if ((r->desc.flags & RF_ROTATION) && (st = sg_run_refresh_rotation(ctx, run)) != SG_OK) return st;
   if (info) {
     info->version = h.version; info->nx = h.nx; info->ny = h.ny; info->nz = h.nz; info->nfields = h.nfields;
     info->time = h.time; info->persisted = h.persisted; info->data_offset = (uint64_t)h.data_offset;
   }
+  return SG_OK;
+}
+
+int sg_run_rotation(sg_context* ctx, sg_run run, sg_rotation* out, float* uh_column) {
+  if (!ctx || !out) return SG_ERR_INVALID;
+  Run* r = find(ctx, run);
+  if (!r) return fail(ctx, SG_ERR_NOT_FOUND, "no run " + std::to_string(run));
+  if (!(r->desc.flags & RF_ROTATION)) return fail(ctx, SG_ERR_INVALID, "the run does not track its rotation (switches.rotation = 0)");
+  double rot[R_COUNT];
+  CK(cudaMemcpyAsync(rot, r->desc.rot, sizeof rot, cudaMemcpyDeviceToHost, ctx->stream));
+  if (uh_column) CK(cudaMemcpyAsync(uh_column, r->desc.diag + (size_t)DG_UH * r->nx * r->ny, (size_t)r->nx * r->ny * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  out->uh = rot[R_UH]; out->x = rot[R_X]; out->y = rot[R_Y]; out->anticyclonic = rot[R_ANTI]; out->persisted = rot[R_PERSISTED];
+  out->uh01 = rot[R_UH01]; out->uh03 = rot[R_UH03]; out->low = rot[R_LOW]; out->core_zeta = rot[R_CZETA]; out->core_uh = rot[R_CUH];
+  out->core_anti = rot[R_CANTI]; out->time = rot[R_TIME];
+  return SG_OK;
+}
+
+int sg_run_refresh_rotation(sg_context* ctx, sg_run run) {
+  if (!ctx) return SG_ERR_INVALID;
+  Run* r = find(ctx, run);
+  if (!r) return fail(ctx, SG_ERR_NOT_FOUND, "no run " + std::to_string(run));
+  if (!(r->desc.flags & RF_ROTATION)) return fail(ctx, SG_ERR_INVALID, "the run does not track its rotation (switches.rotation = 0)");
+  int st;
+  Plan* P = single_plan(ctx, run, &st);
+  if (!P) return st;
+  launch_rotation_columns(lx(ctx, *P, FAM_COLS), 1);
+  launch_rotation_summary(lx(ctx, *P, FAM_RUNS), 1);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  return SG_OK;
+}
+
+int sg_run_read_swaths(sg_context* ctx, sg_run run, float* gust_max, float* uh_max) {
+  if (!ctx) return SG_ERR_INVALID;
+  Run* r = find(ctx, run);
+  if (!r) return fail(ctx, SG_ERR_NOT_FOUND, "no run " + std::to_string(run));
+  const size_t layer = (size_t)r->nx * r->ny;
+  if (gust_max) CK(cudaMemcpyAsync(gust_max, r->desc.diag + DG_GUST_MAX * layer, layer * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  if (uh_max) CK(cudaMemcpyAsync(uh_max, r->desc.diag + DG_UH_MAX * layer, layer * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return SG_OK;
+}
+
+int sg_run_reset_swaths(sg_context* ctx, sg_run run) {
+  if (!ctx) return SG_ERR_INVALID;
+  Run* r = find(ctx, run);
+  if (!r) return fail(ctx, SG_ERR_NOT_FOUND, "no run " + std::to_string(run));
+  const size_t layer = (size_t)r->nx * r->ny;
+  CK(cudaMemsetAsync(r->desc.diag + DG_GUST_MAX * layer, 0, 2 * layer * 4, ctx->stream));  // gustMax, uhMax
+  CK(cudaStreamSynchronize(ctx->stream));
+  return SG_OK;
+}
+
+// diagnostics() (src/core/model.ts:1672-1696): the device's maxima and ground columns, then countCores (:1650-1670,
+// 4-connected), outflowDeficit and deficitNear (src/core/rkw.ts:72-90) on the host, from those columns.
+int sg_run_diagnostics(sg_context* ctx, sg_run run, sg_diagnostics* out) {
+  if (!ctx || !out) return SG_ERR_INVALID;
+  Run* r = find(ctx, run);
+  if (!r) return fail(ctx, SG_ERR_NOT_FOUND, "no run " + std::to_string(run));
+  if (!(r->desc.flags & RF_ROTATION)) return fail(ctx, SG_ERR_INVALID, "the run does not track its rotation (switches.rotation = 0)");
+  const int nx = r->nx, ny = r->ny;
+  const size_t layer = (size_t)nx * ny;
+  CK(cudaMemsetAsync(r->desc.rot + M_UP, 0, 6 * sizeof(double), ctx->stream));
+  launch_diag_sample(node_launch(ctx, *r));
+  CK(cudaGetLastError());
+  double rot[R_COUNT];
+  std::vector<float> cols(5 * layer);
+  CK(cudaMemcpyAsync(rot, r->desc.rot, sizeof rot, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(cols.data(), r->desc.diag + DG_RATE * layer, 5 * layer * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  std::vector<float> precip(layer);
+  CK(cudaMemcpyAsync(precip.data(), r->desc.cols, layer * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  sg_run_counters c;
+  int st = sg_run_status(ctx, run, &c);  // (synchronises the stream)
+  if (st != SG_OK && st != SG_ERR_NONFINITE) return st;
+  auto keyed = [&](int slot) { uint64_t k; std::memcpy(&k, &rot[slot], 8); uint32_t b = (uint32_t)k; float v; std::memcpy(&v, &b, 4); return (double)v; };
+  const float *rate = cols.data(), *hail = rate + layer, *gust = hail + layer, *thv = gust + layer, *mask = thv + layer;
+  double rainRate = 0, rainTotal = 0, gmax = 0, hmax = 0;
+  for (size_t k = 0; k < layer; k++) {
+    rainRate = std::max(rainRate, (double)rate[k]); rainTotal = std::max(rainTotal, (double)precip[k]);
+    gmax = std::max(gmax, (double)gust[k]); hmax = std::max(hmax, (double)hail[k]);
+  }
+  // countCores: 4-connected components of the flagged columns, periodic
+  std::vector<unsigned char> m(layer);
+  for (size_t k = 0; k < layer; k++) m[k] = mask[k] > 0.f ? 1 : 0;
+  int cores = 0;
+  std::vector<int> stack;
+  for (size_t i = 0; i < layer; i++) {
+    if (m[i] != 1) continue;
+    cores++; m[i] = 2; stack.push_back((int)i);
+    while (!stack.empty()) {
+      const int a = stack.back(); stack.pop_back();
+      const int x = a % nx, y = a / nx;
+      const int nb[4] = {(x + 1) % nx + nx * y, (x - 1 + nx) % nx + nx * y, x + nx * ((y + 1) % ny), x + nx * ((y - 1 + ny) % ny)};
+      for (int b : nb) if (m[b] == 1) { m[b] = 2; stack.push_back(b); }
+    }
+  }
+  // outflowDeficit: theta_v of the ground columns below their 75th percentile; deficitNear around the low-level rotation
+  std::vector<float> sorted(thv, thv + layer);
+  std::sort(sorted.begin(), sorted.end());
+  const double warm = sorted[(size_t)std::floor((layer - 1) * .75)];
+  std::vector<float> deficit(layer);
+  double omax = 0;
+  for (size_t k = 0; k < layer; k++) { deficit[k] = (float)std::max(0.0, warm - (double)thv[k]); omax = std::max(omax, (double)deficit[k]); }
+  const int c0 = (int)rot[R_LOW], x0 = c0 % nx, y0 = c0 / nx;
+  const double dx = r->desc.dx, dy = r->desc.dy, radius = 2000;
+  const int rx = (int)std::floor(radius / dx), ry = (int)std::floor(radius / dy);
+  double near = 0;
+  for (int j = -ry; j <= ry; j++) for (int i = -rx; i <= rx; i++) {
+    if ((i * dx) * (i * dx) + (j * dy) * (j * dy) > radius * radius) continue;
+    near = std::max(near, (double)deficit[((x0 + i) % nx + nx) % nx + nx * (((y0 + j) % ny + ny) % ny)]);
+  }
+  out->updraft = keyed(M_UP); out->downdraft = keyed(M_DOWN); out->max_cloud = keyed(M_CLOUD); out->cloud_top = keyed(M_TOP);
+  out->thermal_top = keyed(M_THERMAL); out->cold_max = keyed(M_COLD);
+  out->rain_rate = rainRate; out->rain_total = rainTotal; out->gust = gmax; out->hail = hmax; out->cores = cores;
+  out->outflow = omax; out->outflow_low = near; out->clipped = (double)c.clipped;
   return SG_OK;
 }
 

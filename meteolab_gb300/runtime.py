@@ -43,12 +43,23 @@ class SgSwitches(C.Structure):
                 ("sponge_start", C.c_double), ("cs", C.c_double), ("drag_cd", C.c_double), ("frame_u", C.c_double),
                 ("frame_v", C.c_double)] + [(k, C.c_int32) for k in ("loading", "evaporation", "rain_formation",
                                                                          "anisotropic", "vertical_dz", "durran_klemp",
-                                                                         "pressure_in_stages", "ice", "refine_projection")]
+                                                                         "pressure_in_stages", "ice", "refine_projection",
+                                                                         "rotation")]
 
 
 class SgStateInfo(C.Structure):
     _fields_ = [("version", C.c_int32), ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("nfields", C.c_int32),
                 ("reserved", C.c_int32), ("time", C.c_double), ("persisted", C.c_double), ("data_offset", C.c_uint64)]
+
+
+class SgRotation(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("uh", "x", "y", "anticyclonic", "persisted", "uh01", "uh03", "low", "coreZeta", "coreUH",
+                                          "coreAnti", "time")]
+
+
+class SgDiagnostics(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("updraft", "downdraft", "rainRate", "rainTotal", "cloudTop", "thermalTop", "maxCloud",
+                                          "coldMax", "cores", "outflow", "outflowLow", "gust", "hail", "clipped")]
 
 
 class SgCounters(C.Structure):
@@ -116,6 +127,11 @@ def load():
             L.sg_run_save_state.argtypes = [vp, C.c_int32, C.c_char_p, C.c_double, C.c_double, C.c_char_p, C.c_size_t,
                                             C.POINTER(C.c_size_t)]
             L.sg_run_load_state.argtypes = [vp, C.c_int32, C.c_char_p, C.c_size_t, C.POINTER(SgStateInfo)]
+            L.sg_run_rotation.argtypes = [vp, C.c_int32, C.POINTER(SgRotation), _FP]
+            L.sg_run_refresh_rotation.argtypes = [vp, C.c_int32]
+            L.sg_run_read_swaths.argtypes = [vp, C.c_int32, _FP, _FP]
+            L.sg_run_reset_swaths.argtypes = [vp, C.c_int32]
+            L.sg_run_diagnostics.argtypes = [vp, C.c_int32, C.POINTER(SgDiagnostics)]
             _lib = L
     return _lib
 
@@ -135,7 +151,8 @@ class _Packed:
         self.base = SgBase(*[dp(a) for a in self.keep[3:]])
         self.switches = SgSwitches(sw.dt, sw.coriolis, sw.wind_relaxation, sw.sponge_rate, sw.sponge_start, sw.cs, sw.drag_cd(g),
                                    sw.frame_u, sw.frame_v, sw.loading, sw.evaporation, sw.rain_formation, sw.anisotropic,
-                                   sw.vertical_dz, sw.durran_klemp, sw.pressure_in_stages, 1, sw.refine_projection)
+                                   sw.vertical_dz, sw.durran_klemp, sw.pressure_in_stages, 1, sw.refine_projection,
+                                   sw.rotation)
         self.fields = [np.ascontiguousarray(spec.fields[k], dtype=np.float32).ravel() for k in CARRIED]
         self.ptrs = (_FP * len(CARRIED))(*[a.ctypes.data_as(_FP) for a in self.fields])
 
@@ -350,8 +367,39 @@ class Run:
         ptrs = [a.ctypes.data_as(_FP) if a is not None else None for a in keep]
         self.ctx.check(load().sg_run_write_columns(self.ctx.h, self.id, *ptrs), "write columns")
 
-    def save_state(self, config: Optional[dict] = None, persisted: float = 0.0) -> bytes:
-        """saveState (src/core/state.ts:43-53): the run as a .meteolab image, at this run's model time."""
+    def rotation(self, column: bool = False):
+        """The rotation state after the last step (model.rotation, src/core/model.ts:263) and, with column=True, the
+        2-5 km UH column (model.uhColumn)."""
+        r = SgRotation()
+        col = np.empty(self.grid.layer, np.float32) if column else None
+        self.ctx.check(load().sg_run_rotation(self.ctx.h, self.id, C.byref(r), col.ctypes.data_as(_FP) if column else None), "rotation")
+        out = {k: getattr(r, k) for k, _ in SgRotation._fields_}
+        return (out, col) if column else out
+
+    def refresh_rotation(self):
+        """refreshRotation (src/core/model.ts:1607): the rotation from the fields as they are."""
+        self.ctx.check(load().sg_run_refresh_rotation(self.ctx.h, self.id), "refresh rotation")
+
+    def swaths(self) -> Dict[str, np.ndarray]:
+        """The run's swaths (MemberResult.gustMax, uhMax, src/ensemble/member.ts:20-21)."""
+        g, u = np.empty(self.grid.layer, np.float32), np.empty(self.grid.layer, np.float32)
+        self.ctx.check(load().sg_run_read_swaths(self.ctx.h, self.id, g.ctypes.data_as(_FP), u.ctypes.data_as(_FP)), "swaths")
+        return {"gustMax": g, "uhMax": u}
+
+    def reset_swaths(self):
+        self.ctx.check(load().sg_run_reset_swaths(self.ctx.h, self.id), "reset swaths")
+
+    def diagnostics(self) -> dict:
+        """diagnostics() (src/core/model.ts:1672-1696) without shear06."""
+        d = SgDiagnostics()
+        self.ctx.check(load().sg_run_diagnostics(self.ctx.h, self.id, C.byref(d)), "diagnostics")
+        return {k: getattr(d, k) for k, _ in SgDiagnostics._fields_}
+
+    def save_state(self, config: Optional[dict] = None, persisted: Optional[float] = None) -> bytes:
+        """saveState (src/core/state.ts:43-53): the run as a .meteolab image, at this run's model time; `persisted`
+        defaults to the device's own count when the run tracks its rotation (else 0)."""
+        if persisted is None:
+            persisted = self.rotation()["persisted"] if self.spec.switches.rotation else 0.0
         cfg = json.dumps(config, separators=(",", ":")).encode() if config is not None else None
         size = C.c_size_t()
         self.ctx.check(load().sg_run_save_state(self.ctx.h, self.id, cfg, self.time, persisted, None, 0, C.byref(size)), "save state")

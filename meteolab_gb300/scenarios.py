@@ -73,6 +73,7 @@ class Switches:
     # the device refines its final projection once (FP32-transform residual solved again); the oracle's FP64 solve
     # needs no refinement and ignores it
     refine_projection: int = 1
+    rotation: int = 1   # the rotation tracking after every step (afterStep) and the swaths, on the device
 
     def drag_cd(self, grid: Grid) -> float:
         return drag_coefficient(self.surface, 2 * float(grid.hz[0])) if self.drag else 0.0

@@ -1,6 +1,7 @@
 // TEST INFRASTRUCTURE ONLY — C entry points of the oracle (a CPU restatement of the reference's StormLab step,
 // see oracle_core.h). Loaded by oracle/pyoracle.py for tests/, __graft_entry__.smoke() and bench.py's CPU legs.
 #include "oracle_model.h"
+#include "oracle_diag.h"
 
 using namespace orc;
 
@@ -9,6 +10,10 @@ struct Handle {
   bool fp64;
   Model<float>* m32 = nullptr;
   Model<double>* m64 = nullptr;
+  // afterStep's rotation tracking (src/core/model.ts:1130-1131) and runMember's swaths (src/ensemble/member.ts:103)
+  Rotation rot;
+  std::vector<double> uhColumn;
+  std::vector<float> gustMax, uhMax;
 };
 
 GridSpec makeGrid(int nx, int ny, int nz, double dx, double dy, double dz, double height, const double* zs, const double* dzs, const double* hz) {
@@ -44,6 +49,7 @@ void* orc_create(int fp64, int nx, int ny, int nz, double dx, double dy, double 
   Handle* h = new Handle; h->fp64 = fp64 != 0;
   GridSpec g = makeGrid(nx, ny, nz, dx, dy, dz, height, zs, dzs, hz); Switches s = makeSwitches(sw);
   if (h->fp64) h->m64 = new Model<double>(g, env7, s, threads); else h->m32 = new Model<float>(g, env7, s, threads);
+  h->uhColumn.assign(g.layer, 0); h->gustMax.assign(g.layer, 0); h->uhMax.assign(g.layer, 0);
   return h;
 }
 void orc_destroy(void* p) { Handle* h = (Handle*)p; delete h->m32; delete h->m64; delete h; }
@@ -66,12 +72,50 @@ int orc_get_field(void* p, int id, double* dst, long count) {
   else { auto* v = extraField(h->m64, id); if (!v || (long)v->size() != count) return -1; for (long i = 0; i < count; i++) dst[i] = (*v)[i]; }
   return 0;
 }
-// Steps with time += dt after each (src/core/fixtures.ts:28-30).
+// Steps with time += dt after each (src/core/fixtures.ts:28-30); each step ends with the rotation tracking
+// (afterStep, src/core/model.ts:1130-1131) and, after the time moves, the swaths (runMember, src/ensemble/member.ts:102-103).
 void orc_step(void* p, double dt, int steps) {
   Handle* h = (Handle*)p;
-  for (int s = 0; s < steps; s++) {
-    if (h->m32) { h->m32->step(dt); h->m32->time += dt; } else { h->m64->step(dt); h->m64->time += dt; }
-  }
+  auto go = [&](auto* m) {
+    m->step(dt);
+    updateRotation(*m, dt, h->rot, h->uhColumn);
+    m->time += dt;
+    addSwaths(*m, m->time, h->uhColumn, h->gustMax, h->uhMax);
+  };
+  for (int s = 0; s < steps; s++) { if (h->m32) go(h->m32); else go(h->m64); }
+}
+// The rotation tracking on the fields as they are (refreshRotation with dt, src/core/model.ts:1607-1609).
+void orc_update_rotation(void* p, double dt) {
+  Handle* h = (Handle*)p;
+  if (h->m32) updateRotation(*h->m32, dt, h->rot, h->uhColumn); else updateRotation(*h->m64, dt, h->rot, h->uhColumn);
+}
+// out[11]: uh, x, y, anticyclonic, persisted, uh01, uh03, low, coreZeta, coreUH, coreAnti; uhColumn[layer] (nullable).
+void orc_rotation(void* p, double* out, double* uhColumn) {
+  Handle* h = (Handle*)p;
+  const Rotation& r = h->rot;
+  const double v[11] = {r.uh, r.x, r.y, r.anticyclonic, r.persisted, r.uh01, r.uh03, r.low, r.coreZeta, r.coreUH, r.coreAnti};
+  for (int k = 0; k < 11; k++) out[k] = v[k];
+  if (uhColumn) for (size_t c = 0; c < h->uhColumn.size(); c++) uhColumn[c] = h->uhColumn[c];
+}
+void orc_set_persisted(void* p, double persisted) { ((Handle*)p)->rot.persisted = persisted; }
+// out[14]: updraft, downdraft, rainRate, rainTotal, cloudTop, thermalTop, maxCloud, coldMax, cores, outflow, outflowLow,
+// gust, hail, clipped (diagnostics, src/core/model.ts:1672-1696, without shear06).
+void orc_diagnostics(void* p, double* out) {
+  Handle* h = (Handle*)p;
+  const Diagnostics d = h->m32 ? diagnostics(*h->m32, h->rot) : diagnostics(*h->m64, h->rot);
+  const double v[14] = {d.updraft, d.downdraft, d.rainRate, d.rainTotal, d.cloudTop, d.thermalTop, d.maxCloud, d.coldMax, d.cores,
+                        d.outflow, d.outflowLow, d.gust, d.hail, d.clipped};
+  for (int k = 0; k < 14; k++) out[k] = v[k];
+}
+// addSwaths on the fields as they are, at model time `time`, with the given UH column (member.ts:71-89).
+void orc_add_swaths(void* p, double time, const double* uhColumn) {
+  Handle* h = (Handle*)p;
+  std::vector<double> col(uhColumn, uhColumn + h->uhColumn.size());
+  if (h->m32) addSwaths(*h->m32, time, col, h->gustMax, h->uhMax); else addSwaths(*h->m64, time, col, h->gustMax, h->uhMax);
+}
+void orc_swaths(void* p, float* gustMax, float* uhMax) {
+  Handle* h = (Handle*)p;
+  for (size_t c = 0; c < h->gustMax.size(); c++) { gustMax[c] = h->gustMax[c]; uhMax[c] = h->uhMax[c]; }
 }
 // Stages of one step, for stage-wise parity: 1 = beginStep, 2 = dynamics, 3 = physicsStep, 4 = mixStep, 5 = final project.
 void orc_step_part(void* p, double dt, int part) {

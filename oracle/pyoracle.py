@@ -26,7 +26,7 @@ _f = C.POINTER(C.c_float)
 
 def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (plain g++/OpenMP)."""
-    sources = [os.path.join(HERE, n) for n in ("oracle.cpp", "oracle_core.h", "oracle_solvers.h", "oracle_model.h")]
+    sources = [os.path.join(HERE, n) for n in ("oracle.cpp", "oracle_core.h", "oracle_solvers.h", "oracle_model.h", "oracle_diag.h")]
     if force or not os.path.exists(LIB_PATH) or any(os.path.getmtime(s) > os.path.getmtime(LIB_PATH) for s in sources):
         subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
     return LIB_PATH
@@ -50,6 +50,12 @@ def lib():
             L.orc_get_pressure.argtypes = [C.c_void_p, _d, C.c_long]
             L.orc_get_faces.argtypes = [C.c_void_p, _d, _d, _d, _d, C.c_long]
             L.orc_counters.argtypes = [C.c_void_p, _d]
+            L.orc_update_rotation.argtypes = [C.c_void_p, C.c_double]
+            L.orc_rotation.argtypes = [C.c_void_p, _d, _d]
+            L.orc_set_persisted.argtypes = [C.c_void_p, C.c_double]
+            L.orc_diagnostics.argtypes = [C.c_void_p, _d]
+            L.orc_swaths.argtypes = [C.c_void_p, _f, _f]
+            L.orc_add_swaths.argtypes = [C.c_void_p, C.c_double, _d]
             for name in ("orc_weno", "orc_upwind5"):
                 getattr(L, name).restype = C.c_double
                 getattr(L, name).argtypes = [C.c_double] * 5
@@ -166,6 +172,45 @@ class OracleModel:
         lib().orc_counters(self.h, dp(out))
         return dict(clipped=out[0], negativeFilled=out[1], condensed=out[2], evaporated=out[3],
                     rainEvaporated=out[4], surface=out[5], time=out[6])
+
+
+ROTATION = ("uh", "x", "y", "anticyclonic", "persisted", "uh01", "uh03", "low", "coreZeta", "coreUH", "coreAnti")
+DIAGNOSTICS = ("updraft", "downdraft", "rainRate", "rainTotal", "cloudTop", "thermalTop", "maxCloud", "coldMax", "cores",
+               "outflow", "outflowLow", "gust", "hail", "clipped")
+
+
+def _rotation(self):
+    """The rotation tracking's state after the last step (updateRotation) and the UH column."""
+    out, col = np.empty(len(ROTATION)), np.empty(self.grid.layer)
+    lib().orc_rotation(self.h, dp(out), dp(col))
+    return dict(zip(ROTATION, out)), col
+
+
+def _update_rotation(self, dt: float):
+    lib().orc_update_rotation(self.h, dt)
+
+
+def _diagnostics(self):
+    out = np.empty(len(DIAGNOSTICS))
+    lib().orc_diagnostics(self.h, dp(out))
+    return dict(zip(DIAGNOSTICS, out))
+
+
+def _swaths(self):
+    g, u = np.empty(self.grid.layer, np.float32), np.empty(self.grid.layer, np.float32)
+    lib().orc_swaths(self.h, g.ctypes.data_as(_f), u.ctypes.data_as(_f))
+    return g, u
+
+
+OracleModel.rotation = _rotation
+OracleModel.update_rotation = _update_rotation
+OracleModel.diagnostics = _diagnostics
+def _add_swaths(self, time: float, uh_column):
+    lib().orc_add_swaths(self.h, time, dp(np.ascontiguousarray(uh_column, np.float64)))
+
+
+OracleModel.swaths = _swaths
+OracleModel.add_swaths = _add_swaths
 
 
 def cell(which: str, values: Dict[str, float], exner=1.0, p=1e5, rho=1.0, dt=1.0, aux=0.0):
