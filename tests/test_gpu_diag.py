@@ -146,3 +146,18 @@ def test_a_loaded_state_keeps_the_rotation_time(ctx, storm):
     assert after["persisted"] == before["persisted"] and after["time"] == before["time"]
     assert after["uh"] == before["uh"] and after["coreZeta"] == before["coreZeta"]
     r.retire(); s.retire()
+
+
+def test_members_sample_every_minute_and_a_batch_gives_each_members_own_result(ctx):
+    # ensemble.test.ts:16-21: a member runs for 3 minutes: samples at 0, 1, 2, 3 minutes and a surface wind swath
+    from meteolab_gb300.ensemble import SAMPLE_EVERY, run_members
+    from meteolab_gb300.scenarios import ensemble_members
+    specs = ensemble_members(create_grid(DEFAULT_GRID), 3, seed=11)
+    res = run_members(ctx, specs, 3)
+    for r in res:
+        assert [s["t"] for s in r["samples"]] == [k * SAMPLE_EVERY for k in range(4)]
+        assert r["gustMax"].shape == (r["nx"] * r["ny"],) and r["gustMax"].max() > 0
+    alone = run_members(ctx, specs[1:2], 3)[0]
+    assert alone["samples"] == res[1]["samples"]
+    for k in ("rainTotal", "hailSize", "gustMax", "uhMax"):
+        assert np.array_equal(alone[k], res[1][k]), k
