@@ -228,15 +228,18 @@ SG_HD float narrow(double d) {
 // Biased exponent of the largest magnitude of a stencil; the values are scaled by the exact power of two that brings
 // it to [1, 2). The weights are scale-free, so this changes nothing in exact arithmetic, and in FP32 it keeps the
 // eighth powers inside the weights away from underflow for water contents of 1e-6 kg/kg.
+// The exponent is kept in place (the bits of 2^(e - 127)): the scale down is 2^(127 - e) = bits 0x7f000000 - those, the
+// scale back up those bits themselves.
 SG_HD int weno_exponent(float a, float b, float c, float d, float e) {
   const float s = fmaxf(fmaxf(fabsf(a), fabsf(b)), fmaxf(fmaxf(fabsf(c), fabsf(d)), fabsf(e)));
-  return (float_bits(s) >> 23) & 0xff;
+  return float_bits(s) & 0x7f800000;
 }
+SG_HD float weno_down(int m) { return bits_float((int)(0x7f000000u - (uint32_t)m)); }
 // WENO5 of one face. All-zero input (or all below 1.2e-38) gives 0, the reference's early return.
 SG_HD float weno5(float a, float b, float c, float d, float e) {
   const int ex = weno_exponent(a, b, c, d, e);
   if (ex == 0) return 0.f;
-  const float down = bits_float((254 - ex) << 23), up = bits_float(ex << 23);
+  const float down = weno_down(ex), up = bits_float(ex);
   float num, den;
   weno_core<Op1>(Op1::mul(a, down), Op1::mul(b, down), Op1::mul(c, down), Op1::mul(d, down), Op1::mul(e, down), num, den);
   return Op1::fma(div_fast(num, den), up, c);

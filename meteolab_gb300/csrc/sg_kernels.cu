@@ -1031,7 +1031,7 @@ __global__ void k_fill_final(const RunDesc* __restrict__ runs, const int4* items
 // Per node: the positivity fix and the cold decay ('finish', :1253-1258), then physics(z) (:1347-1531): microphysics,
 // Coriolis and wind relaxation, surface fluxes (none in the single-storm mode), cold clamp, Rayleigh sponge.
 // In: set `in` (final RK3 values). Out: rain, snow, graupel, hail, cold -> set A; the mixed fields -> set `mid`.
-__global__ void k_physics(const RunDesc* __restrict__ runs, const int4* items, int nitems, int in, int mid) {
+__global__ void __launch_bounds__(256, 3) k_physics(const RunDesc* __restrict__ runs, const int4* items, int nitems, int in, int mid) {
   __shared__ double sh[32 * 3];
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];

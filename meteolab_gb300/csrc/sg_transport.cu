@@ -42,11 +42,11 @@ struct Op2 {
 __device__ __forceinline__ float2 weno2(float2 a, float2 b, float2 c, float2 d, float2 e) {
   const int ex = weno_exponent(a.x, b.x, c.x, d.x, e.x), ey = weno_exponent(a.y, b.y, c.y, d.y, e.y);
   if ((ex | ey) == 0) return make_float2(0.f, 0.f);  // a warp of empty stencils skips the weights
-  const float2 down = make_float2(__int_as_float((254 - ex) << 23), __int_as_float((254 - ey) << 23));
+  const float2 down = make_float2(weno_down(ex), weno_down(ey));
   float2 num, den;
   weno_core<Op2>(__fmul2_rn(a, down), __fmul2_rn(b, down), __fmul2_rn(c, down), __fmul2_rn(d, down), __fmul2_rn(e, down), num, den);
-  return make_float2(ex ? __fmaf_rn(__fdividef(num.x, den.x), __int_as_float(ex << 23), c.x) : 0.f,
-                     ey ? __fmaf_rn(__fdividef(num.y, den.y), __int_as_float(ey << 23), c.y) : 0.f);
+  return make_float2(ex ? __fmaf_rn(__fdividef(num.x, den.x), __int_as_float(ex), c.x) : 0.f,
+                     ey ? __fmaf_rn(__fdividef(num.y, den.y), __int_as_float(ey), c.y) : 0.f);
 }
 template <int KIND>
 __device__ __forceinline__ float recon1(float a, float b, float c, float d, float e) {
