@@ -467,6 +467,8 @@ __global__ void k_proj_div_fft2(const RunDesc* __restrict__ runs, const int4* it
     float2* T = Z + pairs * nx;
     float2* X = T + pairs * nx;             // [nm][ny]
     float2* Xs = X + nm * ny;
+    float2* TW = Xs + nm * ny;              // the twiddles of x then y, staged once per layer
+    for (int e = threadIdx.x; e < nx + ny; e += blockDim.x) TW[e] = e < nx ? R.twx[e] : R.twy[e - nx];
     const float *u = field(R, set, U), *v = field(R, set, V), *w = field(R, set, W);
     const float idx = R.inv_dx, idy = R.inv_dy;
     if (mode == PROJ_FACE) {
@@ -514,7 +516,7 @@ __global__ void k_proj_div_fft2(const RunDesc* __restrict__ runs, const int4* it
       }
     }
     __syncthreads();
-    FftPlan Px{nx, R.fx_nf, R.fx_rad, R.twx}, Py{ny, R.fy_nf, R.fy_rad, R.twy};
+    FftPlan Px{nx, R.fx_nf, R.fx_rad, TW}, Py{ny, R.fy_nf, R.fy_rad, TW + nx};
     const float2* Zf = fft_rows_any(Z, T, nx, pairs, Px);
     unpack_rows(Zf, X, nx, ny, ny, nm);
     const float2* Xf = fft_rows_any(X, Xs, ny, nm, Py);
@@ -586,6 +588,8 @@ __global__ void k_proj_ifft2(const RunDesc* __restrict__ runs, const int4* items
     float2* Xs = X + nm * ny;
     float2* Z = Xs + nm * ny;               // [pairs][nx]
     float2* T = Z + pairs * nx;
+    float2* TW = T + pairs * nx;            // the twiddles of x then y, staged once per layer
+    for (int e = threadIdx.x; e < nx + ny; e += blockDim.x) TW[e] = e < nx ? R.twx[e] : R.twy[e - nx];
     const float2* g = R.spec + (size_t)k * ny;
     for (int e = threadIdx.x; e < nm * ny; e += blockDim.x) {
       const int m = e / ny, n = e - m * ny;
@@ -593,7 +597,7 @@ __global__ void k_proj_ifft2(const RunDesc* __restrict__ runs, const int4* items
       X[e] = make_float2(v.x, -v.y);
     }
     __syncthreads();
-    FftPlan Px{nx, R.fx_nf, R.fx_rad, R.twx}, Py{ny, R.fy_nf, R.fy_rad, R.twy};
+    FftPlan Px{nx, R.fx_nf, R.fx_rad, TW}, Py{ny, R.fy_nf, R.fy_rad, TW + nx};
     const float2* G = fft_rows_any(X, Xs, ny, nm, Py);   // conj of the y-inverse: H[m][y] = conj(G[m][y])
     const float inv_nx = 1.f / (float)nx;
     for (int e = threadIdx.x; e < pairs * nx; e += blockDim.x) {
@@ -1366,7 +1370,7 @@ void launch_proj_modes(const Launch& L, int mode, int maxnz, int maxny, int thre
   k_proj_modes<<<GRID(L.n, L.cap), threads, smem, L.stream>>>(L.runs, L.items, L.n, mode, group);
 }
 size_t layer_fft_smem(int maxnx, int maxny) {
-  return ((size_t)2 * ((maxny + 1) / 2) * maxnx + (size_t)2 * (maxnx / 2 + 1) * maxny) * sizeof(float2);
+  return ((size_t)2 * ((maxny + 1) / 2) * maxnx + (size_t)2 * (maxnx / 2 + 1) * maxny + maxnx + maxny) * sizeof(float2);
 }
 void launch_proj_div_fft2(const Launch& L, int mode, int set, int maxnx, int maxny) {
   k_proj_div_fft2<<<GRID(L.n, L.cap), 256, layer_fft_smem(maxnx, maxny), L.stream>>>(L.runs, L.items, L.n, mode, set);
