@@ -44,10 +44,10 @@ KERNEL_BYTES_PER_CELL = {
     "transport_weno": TRANSPORT_BYTES_PER_CELL,
     "transport_dynamics": (80 + 96 + 96) / 3,                             # u, v, w, theta' r/w, faces, buoyancy inputs, start values
     "fill_partial": 28, "physics": 104, "viscosity": 36, "mix": 72,
-    # the final projection's refinement: the residual (u, v, w, p in; node pairs hi, lo and the residual out), the
-    # second solve (right-hand side in), the correction (pairs, p2 in; u, v, w out)
-    "refine_residual": 16 + 24 + 4, "refine_div_xfft": 4 + 4.2, "refine_modes": 8.4 + 12.6,
-    "refine_xifft": 4.2 + 4, "refine_correct": 28 + 12,
+    # the final projection's refinement: the residual (u, v, w, p in; the residual out), the second solve (right-hand
+    # side in), the correction (u, v, w, p1, p2 in; u, v, w out)
+    "refine_residual": 16 + 4, "refine_div_xfft": 4 + 4.2, "refine_modes": 8.4 + 12.6,
+    "refine_xifft": 4.2 + 4, "refine_correct": 20 + 12,
 }
 # Algorithmic bytes of one whole step per cell, pass by pass (each global pass reads its inputs once and writes its
 # outputs once, FP32 4 B): sedimentation 32, face projection 72, RK3 transport 464, three pressure projections 252,

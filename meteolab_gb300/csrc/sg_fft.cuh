@@ -144,6 +144,83 @@ __device__ inline void ifft_rows(float2* a, float2* b, int stride, int rows, con
 }
 #endif
 
+#ifdef __CUDACC__
+// ---- Warp-level transforms (no block barrier inside): the layer transforms of the grids 40 x 32 and 80 x 64.
+// A length N = 5 G row (G = 8 or 16 lanes) is one 5-point DFT in registers per lane (its elements l + G q, q = 0..4),
+// a turn by exp(-2 pi i l k2 / N), then a G-point DFT across the lanes for each register k2 (the index map
+// n = l + G q, k = 5 k1 + k2); a length 32 or 64 column is a 32-point DFT across the lanes (after one radix-2 stage in
+// registers for 64). The lane DFTs are decimation in frequency: lane l ends with output bitrev(l).
+
+// The forward 5-point DFT of five values (the radix-5 butterfly above without its turns).
+__device__ __forceinline__ void dft5(float2& v0, float2& v1, float2& v2, float2& v3, float2& v4) {
+  const float c1 = 0.30901699437494742f, s1 = 0.95105651629515357f, c2 = -0.80901699437494742f, s2 = 0.58778525229247313f;
+  const float2 t1 = cadd(v1, v4), t2 = cadd(v2, v3), d1 = csub(v1, v4), d2 = csub(v2, v3);
+  const float2 a = make_float2(v0.x + c1 * t1.x + c2 * t2.x, v0.y + c1 * t1.y + c2 * t2.y);
+  const float2 b = make_float2(v0.x + c2 * t1.x + c1 * t2.x, v0.y + c2 * t1.y + c1 * t2.y);
+  const float2 e = make_float2(s1 * d1.x + s2 * d2.x, s1 * d1.y + s2 * d2.y);
+  const float2 f = make_float2(s2 * d1.x - s1 * d2.x, s2 * d1.y - s1 * d2.y);
+  v0 = make_float2(v0.x + t1.x + t2.x, v0.y + t1.y + t2.y);
+  v1 = make_float2(a.x + e.y, a.y - e.x);
+  v4 = make_float2(a.x - e.y, a.y + e.x);
+  v2 = make_float2(b.x + f.y, b.y - f.x);
+  v3 = make_float2(b.x - f.y, b.y + f.x);
+}
+// G-point forward DFT across the aligned group of G lanes holding one value each (l = lane within the group), the
+// twiddles exp(-2 pi i t / T) in tw with T = G * tstep. All 32 lanes of the warp take part.
+template <int G>
+__device__ __forceinline__ float2 lane_dft(float2 a, const float2* tw, int tstep, int l) {
+#pragma unroll
+  for (int h = G / 2; h >= 1; h >>= 1) {
+    const float2 b = make_float2(__shfl_xor_sync(0xffffffffu, a.x, h), __shfl_xor_sync(0xffffffffu, a.y, h));
+    if (l & h) a = cmul(csub(b, a), tw[(l & (h - 1)) * (G / (2 * h)) * tstep]);
+    else a = cadd(a, b);
+  }
+  return a;
+}
+template <int BITS>
+__device__ __forceinline__ int bitrev(int l) { return (int)(__brev((unsigned)l) >> (32 - BITS)); }
+constexpr int ilog2(int v) { return v <= 1 ? 0 : 1 + ilog2(v / 2); }
+
+// Forward transform of the length-NX rows of Z (row stride ZS) in place, by warps of the block.
+template <int NX, int ZS>
+__device__ __forceinline__ void warp_rows_fft(float2* Z, int rows, const float2* twx) {
+  constexpr int G = NX / 5, RPW = 32 / G;
+  static_assert(G * 5 == NX && (G == 8 || G == 16), "rows of 40 or 80");
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, l = lane % G, gi = lane / G, nw = blockDim.x >> 5;
+  for (int rw = warp; rw * RPW < rows; rw += nw) {
+    const int row = rw * RPW + gi;
+    float2* Zr = Z + (row < rows ? row : rows - 1) * ZS;
+    float2 v[5];
+#pragma unroll
+    for (int q = 0; q < 5; q++) v[q] = Zr[l + G * q];
+    dft5(v[0], v[1], v[2], v[3], v[4]);
+#pragma unroll
+    for (int q = 1; q < 5; q++) v[q] = cmul(v[q], twx[l * q]);
+#pragma unroll
+    for (int q = 0; q < 5; q++) v[q] = lane_dft<G>(v[q], twx, 5, l);
+    __syncwarp();
+    if (row < rows) {
+      const int k1 = bitrev<ilog2(G)>(l);
+#pragma unroll
+      for (int q = 0; q < 5; q++) Zr[5 * k1 + q] = v[q];
+    }
+  }
+}
+// Forward transform of one length-NY column held one value a lane (NY = 32) or two (NY = 64: x0 = element lane,
+// x1 = element lane + 32); out[s] is the output 2 * bitrev(lane) + s (NY = 64) or bitrev(lane) (NY = 32, s = 0).
+template <int NY>
+__device__ __forceinline__ void warp_column_fft(float2 x0, float2 x1, const float2* twy, int lane, float2 out[2]) {
+  static_assert(NY == 32 || NY == 64, "columns of 32 or 64");
+  if constexpr (NY == 32) {
+    out[0] = lane_dft<32>(x0, twy, 1, lane);
+  } else {
+    const float2 top = cadd(x0, x1), bot = cmul(csub(x0, x1), twy[lane]);
+    out[0] = lane_dft<32>(top, twy, 2, lane);
+    out[1] = lane_dft<32>(bot, twy, 2, lane);
+  }
+}
+#endif
+
 // Host reference of the same stages (used to build plans and by the CPU tests of the plan).
 inline int fft_plan_factors(int n, int* rad) {
   int nf = 0, rest = n;

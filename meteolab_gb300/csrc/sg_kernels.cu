@@ -453,9 +453,90 @@ __device__ __forceinline__ void unpack_rows(const float2* Zf, float2* X, int nx,
   __syncthreads();
 }
 
+// The layer transforms done by warps (sg_fft.cuh): 1 for the 40 x 32 grid, 2 for 80 x 64, 0 the block-wide stages.
+__device__ __forceinline__ int layer_fast(int nx, int ny) { return nx == 40 && ny == 32 ? 1 : nx == 80 && ny == 64 ? 2 : 0; }
+
+// The 2-D forward transform of one layer whose pair rows (real rows 2p and 2p + 1 as one complex row) are in Z (row
+// stride NX + 1; the block synchronised): the rows by warps in place, then per x-wavenumber m a warp unpacks the two
+// real rows' spectra (from Z[m] and conj Z[NX - m]) for every y and transforms the column, into
+// spec[(m * nzc + k) * NY + n].
+template <int NX, int NY>
+__device__ __forceinline__ void layer_forward_fast(const RunDesc& R, float2* Z, const float2* TW, int k, int nzc) {
+  constexpr int PAIRS = NY / 2, NM = NX / 2 + 1, ZS = NX + 1;
+  warp_rows_fft<NX, ZS>(Z, PAIRS, TW);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const float2* twy = TW + NX;
+  for (int m = warp; m < NM; m += nw) {
+    const int c = m ? NX - m : 0;
+    float2 x[2];
+#pragma unroll
+    for (int s = 0; s < NY / 32; s++) {
+      const int r = lane + 32 * s;
+      const float2 zm = Z[(r >> 1) * ZS + m], zc = Z[(r >> 1) * ZS + c];
+      x[s] = (r & 1) == 0 ? make_float2(.5f * (zm.x + zc.x), .5f * (zm.y - zc.y)) : make_float2(.5f * (zm.y + zc.y), .5f * (zc.x - zm.x));
+    }
+    float2 out[2];
+    warp_column_fft<NY>(x[0], x[NY / 32 - 1], twy, lane, out);
+    float2* gm = R.spec + ((size_t)m * nzc + k) * NY;
+    const int b = bitrev<5>(lane);
+    if (NY == 32) gm[b] = out[0];
+    else { gm[2 * b] = out[0]; gm[2 * b + 1] = out[1]; }
+  }
+  __syncthreads();
+}
+
+// The 2-D inverse of one layer by warps: per x-wavenumber m a warp transforms the conjugated column
+// (G[m][y] = conj of the y-inverse) into X (row stride NY + 1); then each pair row is rebuilt from the Hermitian half
+// spectrum, transformed along x, and its conjugate gives the two real rows, normalised, into out.
+template <int NX, int NY>
+__device__ __forceinline__ void layer_inverse_fast(const RunDesc& R, float2* X, const float2* TW, int k, int nzc, float* out) {
+  constexpr int PAIRS = NY / 2, NM = NX / 2 + 1, MH = NX / 2, XS = NY + 1, G = NX / 5, RPW = 32 / G;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const float2* twy = TW + NX;
+  for (int m = warp; m < NM; m += nw) {
+    const float2* gm = R.spec + ((size_t)m * nzc + k) * NY;
+    float2 x[2];
+#pragma unroll
+    for (int s = 0; s < NY / 32; s++) { const float2 v = gm[lane + 32 * s]; x[s] = make_float2(v.x, -v.y); }
+    float2 o[2];
+    warp_column_fft<NY>(x[0], x[NY / 32 - 1], twy, lane, o);
+    const int b = bitrev<5>(lane);
+    if (NY == 32) X[m * XS + b] = o[0];
+    else { X[m * XS + 2 * b] = o[0]; X[m * XS + 2 * b + 1] = o[1]; }
+  }
+  __syncthreads();
+  const int l = lane % G, gi = lane / G;
+  const float norm = 1.f / (float)(NX * NY);
+  for (int rw = warp; rw * RPW < PAIRS; rw += nw) {
+    const int pr = rw * RPW + gi;
+    float2 v[5];
+#pragma unroll
+    for (int q = 0; q < 5; q++) {
+      const int j = l + G * q, c = j <= MH ? j : NX - j;
+      const float sg = j <= MH ? 1.f : -1.f;
+      const bool real = c == 0 || 2 * c == NX;
+      const float2 A = X[c * XS + 2 * pr], B = X[c * XS + 2 * pr + 1];
+      const float ar = A.x, ai = real ? 0.f : -sg * A.y, br = B.x, bi = real ? 0.f : -sg * B.y;
+      v[q] = make_float2(ar - bi, -(ai + br));  // conj(A + iB)
+    }
+    dft5(v[0], v[1], v[2], v[3], v[4]);
+#pragma unroll
+    for (int q = 1; q < 5; q++) v[q] = cmul(v[q], TW[l * q]);
+#pragma unroll
+    for (int q = 0; q < 5; q++) v[q] = lane_dft<G>(v[q], TW, 5, l);
+    const int x0 = 5 * bitrev<ilog2(G)>(l);
+    float* o0 = out + (size_t)(2 * pr) * NX + x0;
+    float* o1 = o0 + NX;
+#pragma unroll
+    for (int q = 0; q < 5; q++) { o0[q] = v[q].x * norm; o1[q] = -v[q].y * norm; }
+  }
+  __syncthreads();
+}
+
 // Divergence of one layer (FACE or PRES, as k_proj_div_xfft) and its 2-D forward transform, written
 // spec[(m * nzc + k) * ny + n].
-__global__ void k_proj_div_fft2(const RunDesc* __restrict__ runs, const int4* items, int nitems, int mode, int set) {
+__global__ void __launch_bounds__(256, 4) k_proj_div_fft2(const RunDesc* __restrict__ runs, const int4* items, int nitems, int mode, int set) {
   extern __shared__ float2 smc[];
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
@@ -463,11 +544,9 @@ __global__ void k_proj_div_fft2(const RunDesc* __restrict__ runs, const int4* it
     const int k = items[it].y, nx = R.nx, ny = R.ny, layer = R.layer, nz = R.nz, nm = R.nm;
     const int pairs = (ny + 1) / 2, nzc = mode == PROJ_FACE ? nz : nz - 1;
     const float inv_nx = 1.f / (float)nx;
-    float2* Z = smc;                        // [pairs][nx]
-    float2* T = Z + pairs * nx;
-    float2* X = T + pairs * nx;             // [nm][ny]
-    float2* Xs = X + nm * ny;
-    float2* TW = Xs + nm * ny;              // the twiddles of x then y, staged once per layer
+    const int fast = layer_fast(nx, ny), zs = fast ? nx + 1 : nx;  // Z's row stride (padded for the warp transforms)
+    float2* TW = smc;                       // the twiddles of x then y, staged once per layer
+    float2* Z = TW + nx + ny;               // [pairs][zs]
     for (int e = threadIdx.x; e < nx + ny; e += blockDim.x) TW[e] = e < nx ? R.twx[e] : R.twy[e - nx];
     const float *u = field(R, set, U), *v = field(R, set, V), *w = field(R, set, W);
     const float idx = R.inv_dx, idy = R.inv_dy;
@@ -489,13 +568,13 @@ __global__ void k_proj_div_fft2(const RunDesc* __restrict__ runs, const int4* it
           const float up = rup * (wc + w[c + lu]), dn = rdn * (w[c + ld] + wc);
           d = ddx * idx + ddy * idy + (up - dn) * ihz;
         }
-        reinterpret_cast<float*>(&Z[(r >> 1) * nx + x])[r & 1] = d;
+        reinterpret_cast<float*>(&Z[(r >> 1) * zs + x])[r & 1] = d;
       }
     } else if (mode == PROJ_GIVEN) {
       const float* rhs = R.phi + (size_t)k * layer;
       for (int e = threadIdx.x; e < pairs * 2 * nx; e += blockDim.x) {
         const int r = row_of(e, inv_nx), x = e - r * nx, y = r;
-        reinterpret_cast<float*>(&Z[(r >> 1) * nx + x])[r & 1] = r < ny ? rhs[x + y * nx] : 0.f;
+        reinterpret_cast<float*>(&Z[(r >> 1) * zs + x])[r & 1] = r < ny ? rhs[x + y * nx] : 0.f;
       }
     } else {
       const float r0 = .25f * lvl(R, L_RHO, k), r1 = .25f * lvl(R, L_RHO, k + 1), idz = lvl(R, L_INV_DZS, k), idt = 1.f / R.dt;
@@ -512,10 +591,15 @@ __global__ void k_proj_div_fft2(const RunDesc* __restrict__ runs, const int4* it
           const float ddz = (r1 * ((w[a + l1] + w[b + l1]) + (w[ee + l1] + w[f + l1])) - r0 * ((w[a + l0] + w[b + l0]) + (w[ee + l0] + w[f + l0]))) * idz;
           d = (ddx + ddy + ddz) * idt;
         }
-        reinterpret_cast<float*>(&Z[(r >> 1) * nx + x])[r & 1] = d;
+        reinterpret_cast<float*>(&Z[(r >> 1) * zs + x])[r & 1] = d;
       }
     }
     __syncthreads();
+    if (fast == 1) { layer_forward_fast<40, 32>(R, Z, TW, k, nzc); continue; }
+    if (fast == 2) { layer_forward_fast<80, 64>(R, Z, TW, k, nzc); continue; }
+    float2* T = Z + pairs * nx;
+    float2* X = T + pairs * nx;             // [nm][ny]
+    float2* Xs = X + nm * ny;
     FftPlan Px{nx, R.fx_nf, R.fx_rad, TW}, Py{ny, R.fy_nf, R.fy_rad, TW + nx};
     const float2* Zf = fft_rows_any(Z, T, nx, pairs, Px);
     unpack_rows(Zf, X, nx, ny, ny, nm);
@@ -577,19 +661,26 @@ __global__ void k_proj_sweep(const RunDesc* __restrict__ runs, const int4* items
 // The 2-D inverse transform of one layer (y, then x with the Hermitian rows rebuilt two real rows per complex
 // transform), normalised by nx*ny, into phi (FACE) or the pressure (PRES). Each inverse is the conjugate of the
 // forward transform of the conjugate.
-__global__ void k_proj_ifft2(const RunDesc* __restrict__ runs, const int4* items, int nitems, int mode) {
+__global__ void __launch_bounds__(256, 4) k_proj_ifft2(const RunDesc* __restrict__ runs, const int4* items, int nitems, int mode) {
   extern __shared__ float2 smc[];
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
     if (R.cnt[C_FAILED]) continue;
     const int k = items[it].y, nx = R.nx, ny = R.ny, nz = R.nz, mh = R.mh, nm = R.nm;
     const int pairs = (ny + 1) / 2, nzc = mode == PROJ_FACE ? nz : nz - 1;
-    float2* X = smc;                        // [nm][ny]
+    float2* TW = smc;                       // the twiddles of x then y, staged once per layer
+    for (int e = threadIdx.x; e < nx + ny; e += blockDim.x) TW[e] = e < nx ? R.twx[e] : R.twy[e - nx];
+    float* out = (mode == PROJ_FACE ? R.phi : mode == PROJ_GIVEN ? R.pres2 : R.pres) + (size_t)k * nx * ny;
+    if (const int fast = layer_fast(nx, ny)) {
+      __syncthreads();
+      if (fast == 1) layer_inverse_fast<40, 32>(R, TW + nx + ny, TW, k, nzc, out);
+      else layer_inverse_fast<80, 64>(R, TW + nx + ny, TW, k, nzc, out);
+      continue;
+    }
+    float2* X = TW + nx + ny;               // [nm][ny]
     float2* Xs = X + nm * ny;
     float2* Z = Xs + nm * ny;               // [pairs][nx]
     float2* T = Z + pairs * nx;
-    float2* TW = T + pairs * nx;            // the twiddles of x then y, staged once per layer
-    for (int e = threadIdx.x; e < nx + ny; e += blockDim.x) TW[e] = e < nx ? R.twx[e] : R.twy[e - nx];
     const float2* g = R.spec + (size_t)k * ny;
     for (int e = threadIdx.x; e < nm * ny; e += blockDim.x) {
       const int m = e / ny, n = e - m * ny;
@@ -613,7 +704,6 @@ __global__ void k_proj_ifft2(const RunDesc* __restrict__ runs, const int4* items
     __syncthreads();
     const float2* Zf = fft_rows_any(Z, T, nx, pairs, Px);
     const float norm = 1.f / (float)(nx * ny);
-    float* out = (mode == PROJ_FACE ? R.phi : mode == PROJ_GIVEN ? R.pres2 : R.pres) + (size_t)k * nx * ny;
     for (int e = threadIdx.x; e < ny * nx; e += blockDim.x) {
       const int r = row_of(e, inv_nx), x = e - r * nx;
       const float2 z = Zf[(r >> 1) * nx + x];
@@ -675,51 +765,73 @@ __global__ void k_face_correct(const RunDesc* __restrict__ runs, const int4* ite
   }
 }
 
-// u -= dt G p at the nodes of one set (PressureSolver.correct, src/core/pressure.ts:69-92); with `final` the wind
-// limits act and count (clipWind, src/core/model.ts:1586-1595). Nodes in passes of NB, as above.
-__global__ void k_pres_correct(const RunDesc* __restrict__ runs, const int4* items, int nitems, int set, int final_) {
+// u -= dt G p at the nodes of one set (PressureSolver.correct, src/core/pressure.ts:69-92); in the final projection
+// the wind limits act and count (clipWind, src/core/model.ts:1586-1595). Nodes in passes of NB, as above.
+// MODE: 0 a stage projection; 1 the final projection of the runs without its refinement (the refined runs are skipped);
+// 2 the final velocity of the refined runs, u - dt G p1 - dt G p2 in FP32 (p2 from the refinement's solve: the
+// correction of mode 1, then that of p2, a few 1e-6 of it).
+template <int MODE>
+__global__ void k_pres_correct(const RunDesc* __restrict__ runs, const int4* items, int nitems, int set) {
+  constexpr bool final_ = MODE > 0, two = MODE == 2;
+  constexpr int nb = two ? 2 : NB;  // two pressures: fewer nodes a pass
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
     if (R.cnt[C_FAILED]) continue;
-    if (final_ && (R.flags & RF_REFINE)) continue;  // these runs finish in k_refine_correct
+    if (final_ && (bool)(R.flags & RF_REFINE) != two) continue;
     const int nx = R.nx, ny = R.ny, nz = R.nz, layer = R.layer, i0 = items[it].y * CHUNK, i1 = min(R.n, i0 + CHUNK);
     float *u = field(R, set, U), *v = field(R, set, V), *w = field(R, set, W);
     const float* __restrict__ p = R.pres;
+    const float* __restrict__ p2 = R.pres2;
     const float dt = R.dt, inv_nx = 1.f / (float)nx;
     const int B = blockDim.x;
     int clipped = 0;
     int z = (i0 + threadIdx.x) / layer;
-    for (int base = i0 + threadIdx.x; base < i1; base += NB * B) {
-      float lo[NB][4], hi[NB][4], uu[NB], vv[NB], ww[NB];
-      int zz[NB];
+    for (int base = i0 + threadIdx.x; base < i1; base += nb * B) {
+      float lo[nb][4], hi[nb][4], lo2[two ? nb : 1][4], hi2[two ? nb : 1][4], uu[nb], vv[nb], ww[nb];
+      int zz[nb];
 #pragma unroll
-      for (int j = 0; j < NB; j++) {
+      for (int j = 0; j < nb; j++) {
         const int i = min(base + j * B, i1 - 1);
         while (i >= (z + 1) * layer) z++;
         zz[j] = z;
         const int c = i - z * layer, jy = row_of(c, inv_nx), x = c - jy * nx;
         const int im = x == 0 ? nx - 1 : x - 1, jm = (jy == 0 ? ny - 1 : jy - 1) * nx, j0 = jy * nx;
-        const float* L = p + (size_t)max(0, z - 1) * layer;
-        const float* H = p + (size_t)min(nz - 2, z) * layer;
+        const size_t lz = (size_t)max(0, z - 1) * layer, hz_ = (size_t)min(nz - 2, z) * layer;
+        const float* L = p + lz;
+        const float* H = p + hz_;
         // corners (im, jm), (x, jm), (im, j0), (x, j0) of the dual cells below and above
         lo[j][0] = L[im + jm]; lo[j][1] = L[x + jm]; lo[j][2] = L[im + j0]; lo[j][3] = L[x + j0];
         hi[j][0] = H[im + jm]; hi[j][1] = H[x + jm]; hi[j][2] = H[im + j0]; hi[j][3] = H[x + j0];
+        if (two) {
+          const float* L2 = p2 + lz;
+          const float* H2 = p2 + hz_;
+          lo2[j][0] = L2[im + jm]; lo2[j][1] = L2[x + jm]; lo2[j][2] = L2[im + j0]; lo2[j][3] = L2[x + j0];
+          hi2[j][0] = H2[im + jm]; hi2[j][1] = H2[x + jm]; hi2[j][2] = H2[im + j0]; hi2[j][3] = H2[x + j0];
+        }
         uu[j] = u[i]; vv[j] = v[i]; ww[j] = w[i];
       }
 #pragma unroll
-      for (int j = 0; j < NB; j++) {
+      for (int j = 0; j < nb; j++) {
         const int i = base + j * B;
         if (i >= i1) break;
         const int k = zz[j];
         const float hz = lvl(R, L_HZ, k);
         const float wLo = k > 0 ? lvl(R, L_DZS, k - 1) / hz : 0.f, wHi = k < nz - 1 ? lvl(R, L_DZS, k) / hz : 0.f;
-        const float gx = (wLo * ((lo[j][1] - lo[j][0]) + (lo[j][3] - lo[j][2])) + wHi * ((hi[j][1] - hi[j][0]) + (hi[j][3] - hi[j][2]))) * (.25f * R.inv_dx);
-        const float gy = (wLo * ((lo[j][2] - lo[j][0]) + (lo[j][3] - lo[j][1])) + wHi * ((hi[j][2] - hi[j][0]) + (hi[j][3] - hi[j][1]))) * (.25f * R.inv_dy);
-        float un = uu[j] - dt * gx, vn = vv[j] - dt * gy, wn = ww[j];
-        if (k > 0 && k < nz - 1) {
+        const float qx = .25f * R.inv_dx, qy = .25f * R.inv_dy, qz = .25f * lvl(R, L_INV_HZ, k);
+        const bool inner = k > 0 && k < nz - 1;
+        auto grad = [&](const float* l, const float* h, float& gx, float& gy, float& gz) {
+          gx = (wLo * ((l[1] - l[0]) + (l[3] - l[2])) + wHi * ((h[1] - h[0]) + (h[3] - h[2]))) * qx;
+          gy = (wLo * ((l[2] - l[0]) + (l[3] - l[1])) + wHi * ((h[2] - h[0]) + (h[3] - h[1]))) * qy;
           // the gradient between the dual cells below (k - 1) and above (k)
-          const float gz = ((hi[j][0] - lo[j][0]) + (hi[j][1] - lo[j][1]) + (hi[j][2] - lo[j][2]) + (hi[j][3] - lo[j][3])) * (.25f * lvl(R, L_INV_HZ, k));
-          wn -= dt * gz;
+          gz = ((h[0] - l[0]) + (h[1] - l[1]) + (h[2] - l[2]) + (h[3] - l[3])) * qz;
+        };
+        float gx, gy, gz;
+        grad(lo[j], hi[j], gx, gy, gz);
+        float un = __fmaf_rn(-dt, gx, uu[j]), vn = __fmaf_rn(-dt, gy, vv[j]), wn = inner ? __fmaf_rn(-dt, gz, ww[j]) : ww[j];
+        if (two) {
+          grad(lo2[j], hi2[j], gx, gy, gz);
+          un = __fmaf_rn(-dt, gx, un); vn = __fmaf_rn(-dt, gy, vn);
+          if (inner) wn = __fmaf_rn(-dt, gz, wn);
         }
         if (final_) {
           const float UL = 120.f, WL = 100.f;
@@ -741,8 +853,8 @@ __global__ void k_pres_correct(const RunDesc* __restrict__ runs, const int4* ite
 // pressure, which leaves a residual divergence of a few 1e-6 of the one it removed. One refinement step brings it to
 // rounding level: the projected velocity v = u - dt G p1 and its divergence are formed in double-FP32 arithmetic
 // (hi + lo pairs, error-free sums and products: about 44 significant bits on the FP32 pipes), the residual r = D v / dt
-// is solved again (p2) and the velocity becomes v - dt G p2, rounded to FP32 once. The projection's pressure is
-// p1 + p2.
+// is solved again (p2) and the velocity becomes u - dt G p1 - dt G p2 in FP32 (two corrections of a few rounding
+// errors of v each: the storage of v in FP32 bounds its divergence either way). The projection's pressure is p1 + p2.
 struct DF { float hi, lo; };
 __device__ __forceinline__ DF df_two_sum(float a, float b) {
   const float s = __fadd_rn(a, b), bp = __fsub_rn(s, a);
@@ -814,11 +926,10 @@ __device__ __forceinline__ void df_gradient_of(const RunDesc& R, int k, float l0
 // The residual of the refined runs' final projection in one tiled march over the item's levels (run, tile, z0, z1),
 // a thread per node of the tile and its halo:
 // per node level, v = u - dt G p1 in double-FP32 for the tile's nodes and a one-node halo on the high x and y sides
-// (into a pair of shared-memory planes), the tile's own nodes' (hi, lo) written to sets B and C for the final
-// correction; per dual layer, r = D v / dt rounded once into phi: D of the hi parts in double-FP32 (their differences
+// (into a pair of shared-memory planes); per dual layer, r = D v / dt rounded once into phi: D of the hi parts in double-FP32 (their differences
 // are exact), D of the lo parts (a few 1e-8 of them) in FP32. The pressure planes (dual levels k - 1 and k, with a
 // one-cell halo on the low sides) arrive by asynchronous copies a level ahead.
-__global__ void __launch_bounds__(320) k_refine_residual(const RunDesc* __restrict__ runs, const int4* items, int nitems, int set,
+__global__ void __launch_bounds__(192, 4) k_refine_residual(const RunDesc* __restrict__ runs, const int4* items, int nitems, int set,
                                                          int TX, int TY) {
   extern __shared__ float rsm[];
   FOR_ITEMS {
@@ -866,7 +977,6 @@ __global__ void __launch_bounds__(320) k_refine_residual(const RunDesc* __restri
         df_gradient_of(R, k, L[a], L[a + 1], L[a + PW], L[a + PW + 1], H[a], H[a + 1], H[a + PW], H[a + PW + 1], g[0], g[1], g[2]);
         const size_t i = (size_t)k * layer + gx + gy * nx;
         const float uin[3] = {u[i], v[i], w[i]};
-        const bool own = nx_ < TX && ny_ < TY && k < z1;
         DF r[3];
         {  // u and v as the lanes of one packed evaluation (df_sub(a, b) = df_add(a, -b))
           const DF2 m = df2_mul(df2_splat(dt), DF2{f2(g[0].hi, g[1].hi), f2(g[0].lo, g[1].lo)});
@@ -878,7 +988,6 @@ __global__ void __launch_bounds__(320) k_refine_residual(const RunDesc* __restri
         for (int d = 0; d < 3; d++) {
           V[(2 * d) * NN + e] = r[d].hi;
           V[(2 * d + 1) * NN + e] = r[d].lo;
-          if (own) { field(R, 1, U + d)[i] = r[d].hi; field(R, 2, U + d)[i] = r[d].lo; }
         }
       }
       __syncthreads();
@@ -912,45 +1021,6 @@ __global__ void __launch_bounds__(320) k_refine_residual(const RunDesc* __restri
     }
     cp_async_wait_all();
     __syncthreads();
-  }
-}
-
-// The final velocity v - dt G p2 (p2 from the refinement's solve, its gradient in FP32: it is a correction of a few
-// 1e-6), rounded once to FP32, with the wind limits and their count (clipWind, src/core/model.ts:1586-1595).
-__global__ void k_refine_correct(const RunDesc* __restrict__ runs, const int4* items, int nitems, int set) {
-  FOR_ITEMS {
-    const RunDesc& R = runs[items[it].x];
-    if (R.cnt[C_FAILED] || !(R.flags & RF_REFINE)) continue;
-    const int nx = R.nx, ny = R.ny, nz = R.nz, layer = R.layer, i0 = items[it].y * CHUNK, i1 = min(R.n, i0 + CHUNK);
-    const float* __restrict__ p = R.pres2;
-    const float* __restrict__ hi[3] = {field(R, 1, U), field(R, 1, V), field(R, 1, W)};
-    const float* __restrict__ lo[3] = {field(R, 2, U), field(R, 2, V), field(R, 2, W)};
-    float* __restrict__ out3[3] = {field(R, set, U), field(R, set, V), field(R, set, W)};
-    const float dt = R.dt;
-    int clipped = 0;
-    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-      const int k = i / layer, c = i - k * layer, jy = c / nx, x = c - jy * nx;
-      const int im = x == 0 ? nx - 1 : x - 1, jm = (jy == 0 ? ny - 1 : jy - 1) * nx, j0 = jy * nx;
-      const float* L = p + (size_t)max(0, k - 1) * layer;
-      const float* H = p + (size_t)min(nz - 2, k) * layer;
-      const float hz = lvl(R, L_HZ, k);
-      const float wLo = k > 0 ? lvl(R, L_DZS, k - 1) / hz : 0.f, wHi = k < nz - 1 ? lvl(R, L_DZS, k) / hz : 0.f;
-      const float g[3] = {
-        (wLo * ((L[x + jm] - L[im + jm]) + (L[x + j0] - L[im + j0])) + wHi * ((H[x + jm] - H[im + jm]) + (H[x + j0] - H[im + j0]))) * (.25f * R.inv_dx),
-        (wLo * ((L[im + j0] - L[im + jm]) + (L[x + j0] - L[x + jm])) + wHi * ((H[im + j0] - H[im + jm]) + (H[x + j0] - H[x + jm]))) * (.25f * R.inv_dy),
-        k > 0 && k < nz - 1 ? ((H[im + jm] - L[im + jm]) + (H[x + jm] - L[x + jm]) + (H[im + j0] - L[im + j0]) + (H[x + j0] - L[x + j0])) * (.25f * lvl(R, L_INV_HZ, k)) : 0.f};
-      float out[3];
-#pragma unroll
-      for (int d = 0; d < 3; d++) out[d] = __fadd_rn(__fmaf_rn(-dt, g[d], hi[d][i]), lo[d][i]);
-      const float UL = 120.f, WL = 100.f;
-      if (out[0] < -UL || out[0] > UL) { out[0] = fmaxf(-UL, fminf(UL, out[0])); clipped++; }
-      if (out[1] < -UL || out[1] > UL) { out[1] = fmaxf(-UL, fminf(UL, out[1])); clipped++; }
-      if (out[2] < -WL || out[2] > WL) { out[2] = fmaxf(-WL, fminf(WL, out[2])); clipped++; }
-#pragma unroll
-      for (int d = 0; d < 3; d++) out3[d][i] = out[d];
-    }
-    clipped = warpSum(clipped);
-    if ((threadIdx.x & 31) == 0 && clipped) atomicAdd(&R.cnt[C_CLIPPED], (unsigned long long)clipped);
   }
 }
 
@@ -1372,14 +1442,20 @@ void launch_proj_modes(const Launch& L, int mode, int maxnz, int maxny, int thre
 size_t layer_fft_smem(int maxnx, int maxny) {
   return ((size_t)2 * ((maxny + 1) / 2) * maxnx + (size_t)2 * (maxnx / 2 + 1) * maxny + maxnx + maxny) * sizeof(float2);
 }
-void launch_proj_div_fft2(const Launch& L, int mode, int set, int maxnx, int maxny) {
-  k_proj_div_fft2<<<GRID(L.n, L.cap), 256, layer_fft_smem(maxnx, maxny), L.stream>>>(L.runs, L.items, L.n, mode, set);
+size_t layer_fft_smem_run(int nx, int ny) {
+  const bool fast = (nx == 40 && ny == 32) || (nx == 80 && ny == 64);
+  if (!fast) return layer_fft_smem(nx, ny);
+  const size_t fwd = (size_t)(ny / 2) * (nx + 1), inv = (size_t)(nx / 2 + 1) * (ny + 1);
+  return ((size_t)nx + ny + std::max(fwd, inv)) * sizeof(float2);
+}
+void launch_proj_div_fft2(const Launch& L, int mode, int set, size_t smem) {
+  k_proj_div_fft2<<<GRID(L.n, L.cap), 256, smem, L.stream>>>(L.runs, L.items, L.n, mode, set);
 }
 void launch_proj_sweep(const Launch& L, int mode, int maxny) {
   k_proj_sweep<<<GRID(L.n, L.cap), (2 * maxny + 31) / 32 * 32, 0, L.stream>>>(L.runs, L.items, L.n, mode);
 }
-void launch_proj_ifft2(const Launch& L, int mode, int maxnx, int maxny) {
-  k_proj_ifft2<<<GRID(L.n, L.cap), 256, layer_fft_smem(maxnx, maxny), L.stream>>>(L.runs, L.items, L.n, mode);
+void launch_proj_ifft2(const Launch& L, int mode, size_t smem) {
+  k_proj_ifft2<<<GRID(L.n, L.cap), 256, smem, L.stream>>>(L.runs, L.items, L.n, mode);
 }
 void launch_proj_xifft(const Launch& L, int mode, int yc, int maxnx) {
   size_t smem = ((size_t)yc * (maxnx / 2 + 1) + (size_t)2 * ((yc + 1) / 2) * maxnx) * sizeof(float2);
@@ -1392,8 +1468,11 @@ void launch_refine_residual(const Launch& L, int set, int TX, int TY) {
   const int threads = ((TX + 1) * (TY + 1) + 31) / 32 * 32;  // a thread per node of the tile and its halo
   k_refine_residual<<<GRID(L.n, L.cap), threads, refine_smem(TX, TY), L.stream>>>(L.runs, L.items, L.n, set, TX, TY);
 }
-void launch_refine_correct(const Launch& L, int set) { k_refine_correct<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set); }
-void launch_pres_correct(const Launch& L, int set, int final_) { k_pres_correct<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set, final_); }
+void launch_refine_correct(const Launch& L, int set) { k_pres_correct<2><<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set); }
+void launch_pres_correct(const Launch& L, int set, int final_) {
+  if (final_) k_pres_correct<1><<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set);
+  else k_pres_correct<0><<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set);
+}
 
 void launch_fill_partial(const Launch& L, int set) { k_fill_partial<<<GRID(L.n, L.cap), 128, 0, L.stream>>>(L.runs, L.items, L.n, set); }
 void launch_fill_final(const Launch& L) { k_fill_final<<<GRID(L.n, L.cap), 32, 0, L.stream>>>(L.runs, L.items, L.n); }

@@ -28,9 +28,10 @@ void launch_proj_div_xfft(const Launch& L, int mode, int set, int yc, int maxnx)
 void launch_proj_modes(const Launch& L, int mode, int maxnz, int maxny, int threads, int smem_budget);
 // The whole-layer path: 2-D transforms per layer, FP64 sweeps per (m, n) in global memory.
 size_t layer_fft_smem(int maxnx, int maxny);
-void launch_proj_div_fft2(const Launch& L, int mode, int set, int maxnx, int maxny);
+size_t layer_fft_smem_run(int nx, int ny);  // the layer transforms' shared memory for one run's grid
+void launch_proj_div_fft2(const Launch& L, int mode, int set, size_t smem);
 void launch_proj_sweep(const Launch& L, int mode, int maxny);
-void launch_proj_ifft2(const Launch& L, int mode, int maxnx, int maxny);
+void launch_proj_ifft2(const Launch& L, int mode, size_t smem);
 void launch_proj_xifft(const Launch& L, int mode, int yc, int maxnx);
 void launch_face_correct(const Launch& L, int set);
 // Refinement of the final projection: node pairs v = u - dt G p1 (nodes), their divergence into phi (cells), and

@@ -71,6 +71,7 @@ struct Plan {
   int mixTX = 32, mixTY = 8;                                          // mixing tile
   int refTX = 16, refTY = 8;                                          // refinement tile
   bool layerfft = false;                                              // 2-D transforms per layer (see enqueue_part)
+  size_t fftSmem = 0;                                                 // their shared memory: the largest over the runs
   bool refine = false;                                                // some run refines its final projection
   bool rotation = false;                                              // some run tracks its rotation and swaths
   bool tuned = false;                                                 // TX, TY, wenoG chosen by timing
@@ -345,6 +346,7 @@ int build_plan(sg_context* ctx, const std::vector<int>& slots, Plan& P) {
   // the mode kernel transforms along y around its sweep.
   P.layerfft = !ctx->rowsOnly && layer_fft_smem(P.maxnx, P.maxny) <= (size_t)std::min(ctx->maxSmem, 100 * 1024);
   P.yc = P.layerfft ? P.maxny : std::min(P.maxnx > 128 ? 16 : 32, (P.maxny + 1) / 2 * 2);
+  for (int s : slots) P.fftSmem = std::max(P.fftSmem, layer_fft_smem_run(ctx->runs[s].nx, ctx->runs[s].ny));
   for (int s : slots) {
     const Run& r = ctx->runs[s];
     int n = r.nx * r.ny * r.nz, nch = (n + CHUNK - 1) / CHUNK, layer = r.nx * r.ny;
@@ -475,9 +477,9 @@ void enqueue_solve(sg_context* ctx, const Plan& P, int mode, int set, cudaStream
   rows.stream = modes.stream = stream;
   const int h = mode == PROJ_FACE ? 2 : mode == PROJ_PRES ? 7 : 22;  // profile ids of the three stages
   if (P.layerfft) {
-    launch_proj_div_fft2(rows, mode, set, P.maxnx, P.maxny); hook(h);
+    launch_proj_div_fft2(rows, mode, set, P.fftSmem); hook(h);
     launch_proj_sweep(modes, mode, P.maxny); hook(h + 1);
-    launch_proj_ifft2(rows, mode, P.maxnx, P.maxny); hook(h + 2);
+    launch_proj_ifft2(rows, mode, P.fftSmem); hook(h + 2);
   } else {
     const int mthreads = std::min(512, std::max(64, (2 * P.maxny + 31) / 32 * 32));
     const int mbudget = std::min(ctx->maxSmem, 200 * 1024);
