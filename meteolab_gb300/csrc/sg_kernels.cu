@@ -456,6 +456,75 @@ __device__ __forceinline__ void unpack_rows(const float2* Zf, float2* X, int nx,
 // The layer transforms done by warps (sg_fft.cuh): 1 for the 40 x 32 grid, 2 for 80 x 64, 0 the block-wide stages.
 __device__ __forceinline__ int layer_fast(int nx, int ny) { return nx == 40 && ny == 32 ? 1 : nx == 80 && ny == 64 ? 2 : 0; }
 
+// The source of one layer's forward transform on a grid of NX * NY = 256 * PER nodes (the 40 x 32 grid), by a block of
+// 256 threads: the level planes it needs are read once, coalesced, and combined per node into three staged planes P
+// (FACE: u, v and the vertical flux difference; PRES: u, v and w weighted by the levels' densities), then each node's
+// divergence takes its horizontal neighbours from P; into the pair rows of Z (row stride NX + 1). The same
+// divergences as the block-wide path, summed in another order. Ends with the block synchronised.
+template <int NX, int NY>
+__device__ __forceinline__ void layer_source_staged(const RunDesc& R, int mode, int set, int k, float2* Z, float* P) {
+  constexpr int N = NX * NY, PER = N / 256, ZS = NX + 1;
+  static_assert(PER * 256 == N, "a whole number of nodes a thread");
+  const int t = threadIdx.x, nz = R.nz;
+  float* Zf = reinterpret_cast<float*>(Z);
+  auto put = [&](int e, float d) { const int r = e / NX, x = e - r * NX; Zf[2 * ((r >> 1) * ZS + x) + (r & 1)] = d; };
+  if (mode == PROJ_GIVEN) {
+    const float* rhs = R.phi + (size_t)k * N;
+    float d[PER];
+#pragma unroll
+    for (int j = 0; j < PER; j++) d[j] = rhs[t + 256 * j];
+#pragma unroll
+    for (int j = 0; j < PER; j++) put(t + 256 * j, d[j]);
+    __syncthreads();
+    return;
+  }
+  const float *u = field(R, set, U), *v = field(R, set, V), *w = field(R, set, W);
+  const float idx = R.inv_dx, idy = R.inv_dy;
+  if (mode == PROJ_FACE) {
+    const float rho = lvl(R, L_RHO, k), ihz = lvl(R, L_INV_HZ, k);
+    const float rup = k < nz - 1 ? .5f * lvl(R, L_RUP, k) : 0.f, rdn = k > 0 ? .5f * lvl(R, L_RUP, k - 1) : 0.f;
+    const int l = k * N, lu = k < nz - 1 ? l + N : l, ld = k > 0 ? l - N : l;
+#pragma unroll
+    for (int j = 0; j < PER; j++) {
+      const int e = t + 256 * j;
+      const float wc = w[l + e];
+      P[e] = u[l + e]; P[N + e] = v[l + e];
+      P[2 * N + e] = (rup * (wc + w[lu + e]) - rdn * (w[ld + e] + wc)) * ihz;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < PER; j++) {
+      const int e = t + 256 * j, y = e / NX, x = e - y * NX, row = y * NX;
+      const int ce = (x + 1 == NX ? 0 : x + 1) + row, cw = (x == 0 ? NX - 1 : x - 1) + row;
+      const int cn = x + (y + 1 == NY ? 0 : y + 1) * NX, cs = x + (y == 0 ? NY - 1 : y - 1) * NX;
+      const float ddx = .5f * rho * (P[ce] - P[cw]), ddy = .5f * rho * (P[N + cn] - P[N + cs]);
+      put(e, ddx * idx + ddy * idy + P[2 * N + e]);
+    }
+  } else {
+    const float r0 = .25f * lvl(R, L_RHO, k), r1 = .25f * lvl(R, L_RHO, k + 1), idz = lvl(R, L_INV_DZS, k), idt = 1.f / R.dt;
+    const int l0 = k * N, l1 = l0 + N;
+#pragma unroll
+    for (int j = 0; j < PER; j++) {
+      const int e = t + 256 * j;
+      P[e] = r0 * u[l0 + e] + r1 * u[l1 + e];
+      P[N + e] = r0 * v[l0 + e] + r1 * v[l1 + e];
+      P[2 * N + e] = r1 * w[l1 + e] - r0 * w[l0 + e];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < PER; j++) {
+      const int e = t + 256 * j, y = e / NX, x = e - y * NX;
+      const int x1 = x + 1 == NX ? 0 : x + 1, y1 = (y + 1 == NY ? 0 : y + 1) * NX, yy = y * NX;
+      const int a = x + yy, b = x1 + yy, c = x + y1, f = x1 + y1;
+      const float ddx = ((P[b] - P[a]) + (P[f] - P[c])) * idx;
+      const float ddy = ((P[N + c] - P[N + a]) + (P[N + f] - P[N + b])) * idy;
+      const float ddz = ((P[2 * N + a] + P[2 * N + b]) + (P[2 * N + c] + P[2 * N + f])) * idz;
+      put(e, (ddx + ddy + ddz) * idt);
+    }
+  }
+  __syncthreads();
+}
+
 // The 2-D forward transform of one layer whose pair rows (real rows 2p and 2p + 1 as one complex row) are in Z (row
 // stride NX + 1; the block synchronised): the rows by warps in place, then per x-wavenumber m a warp unpacks the two
 // real rows' spectra (from Z[m] and conj Z[NX - m]) for every y and transforms the column, into
@@ -489,16 +558,28 @@ __device__ __forceinline__ void layer_forward_fast(const RunDesc& R, float2* Z, 
 // The 2-D inverse of one layer by warps: per x-wavenumber m a warp transforms the conjugated column
 // (G[m][y] = conj of the y-inverse) into X (row stride NY + 1); then each pair row is rebuilt from the Hermitian half
 // spectrum, transformed along x, and its conjugate gives the two real rows, normalised, into out.
+// A block of 256 threads; the twiddles' staging in TW is synchronised here (after the spectrum's loads are issued).
 template <int NX, int NY>
 __device__ __forceinline__ void layer_inverse_fast(const RunDesc& R, float2* X, const float2* TW, int k, int nzc, float* out) {
-  constexpr int PAIRS = NY / 2, NM = NX / 2 + 1, MH = NX / 2, XS = NY + 1, G = NX / 5, RPW = 32 / G;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  constexpr int PAIRS = NY / 2, NM = NX / 2 + 1, MH = NX / 2, XS = NY + 1, G = NX / 5, RPW = 32 / G, NW = 8, ROUNDS = (NM + NW - 1) / NW;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = NW;
   const float2* twy = TW + NX;
-  for (int m = warp; m < NM; m += nw) {
-    const float2* gm = R.spec + ((size_t)m * nzc + k) * NY;
+  float2 sp[ROUNDS][NY / 32];  // every column of this warp, loaded before any is transformed
+#pragma unroll
+  for (int q = 0; q < ROUNDS; q++) {
+    const int m = warp + NW * q;
+    const float2* gm = R.spec + ((size_t)(m < NM ? m : 0) * nzc + k) * NY;
+#pragma unroll
+    for (int s = 0; s < NY / 32; s++) sp[q][s] = gm[lane + 32 * s];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < ROUNDS; q++) {
+    const int m = warp + NW * q;
+    if (m >= NM) break;
     float2 x[2];
 #pragma unroll
-    for (int s = 0; s < NY / 32; s++) { const float2 v = gm[lane + 32 * s]; x[s] = make_float2(v.x, -v.y); }
+    for (int s = 0; s < NY / 32; s++) x[s] = make_float2(sp[q][s].x, -sp[q][s].y);
     float2 o[2];
     warp_column_fft<NY>(x[0], x[NY / 32 - 1], twy, lane, o);
     const int b = bitrev<5>(lane);
@@ -548,6 +629,11 @@ __global__ void __launch_bounds__(256, 4) k_proj_div_fft2(const RunDesc* __restr
     float2* TW = smc;                       // the twiddles of x then y, staged once per layer
     float2* Z = TW + nx + ny;               // [pairs][zs]
     for (int e = threadIdx.x; e < nx + ny; e += blockDim.x) TW[e] = e < nx ? R.twx[e] : R.twy[e - nx];
+    if (fast == 1) {  // the 40 x 32 grid: staged source, warp transforms
+      layer_source_staged<40, 32>(R, mode, set, k, Z, reinterpret_cast<float*>(Z + pairs * zs));
+      layer_forward_fast<40, 32>(R, Z, TW, k, nzc);
+      continue;
+    }
     const float *u = field(R, set, U), *v = field(R, set, V), *w = field(R, set, W);
     const float idx = R.inv_dx, idy = R.inv_dy;
     if (mode == PROJ_FACE) {
@@ -595,7 +681,6 @@ __global__ void __launch_bounds__(256, 4) k_proj_div_fft2(const RunDesc* __restr
       }
     }
     __syncthreads();
-    if (fast == 1) { layer_forward_fast<40, 32>(R, Z, TW, k, nzc); continue; }
     if (fast == 2) { layer_forward_fast<80, 64>(R, Z, TW, k, nzc); continue; }
     float2* T = Z + pairs * nx;
     float2* X = T + pairs * nx;             // [nm][ny]
@@ -672,7 +757,6 @@ __global__ void __launch_bounds__(256, 4) k_proj_ifft2(const RunDesc* __restrict
     for (int e = threadIdx.x; e < nx + ny; e += blockDim.x) TW[e] = e < nx ? R.twx[e] : R.twy[e - nx];
     float* out = (mode == PROJ_FACE ? R.phi : mode == PROJ_GIVEN ? R.pres2 : R.pres) + (size_t)k * nx * ny;
     if (const int fast = layer_fast(nx, ny)) {
-      __syncthreads();
       if (fast == 1) layer_inverse_fast<40, 32>(R, TW + nx + ny, TW, k, nzc, out);
       else layer_inverse_fast<80, 64>(R, TW + nx + ny, TW, k, nzc, out);
       continue;
@@ -1445,7 +1529,8 @@ size_t layer_fft_smem(int maxnx, int maxny) {
 size_t layer_fft_smem_run(int nx, int ny) {
   const bool fast = (nx == 40 && ny == 32) || (nx == 80 && ny == 64);
   if (!fast) return layer_fft_smem(nx, ny);
-  const size_t fwd = (size_t)(ny / 2) * (nx + 1), inv = (size_t)(nx / 2 + 1) * (ny + 1);
+  // the forward's pair rows (and on 40 x 32 its three staged planes, 1.5 complex words a node), the inverse's columns
+  const size_t fwd = (size_t)(ny / 2) * (nx + 1) + (nx == 40 ? (size_t)3 * nx * ny / 2 : 0), inv = (size_t)(nx / 2 + 1) * (ny + 1);
   return ((size_t)nx + ny + std::max(fwd, inv)) * sizeof(float2);
 }
 void launch_proj_div_fft2(const Launch& L, int mode, int set, size_t smem) {
