@@ -9,7 +9,7 @@
 //   spec  (nx/2+1) x nzc x ny complex x-spectrum of one projection, m-major so a mode slab is contiguous
 //   cols  3 x nx*ny                   precipitation, hail on the ground, largest hail
 //   lv    L_COUNT x nz                per-level constants (FP32); lv64: per-level FP64 (tridiagonal coefficients)
-//   tri_face/tri_pres  (invpiv, cp) FP64 per (m, k, n) of the two tridiagonal factorisations
+//   tri_face/tri_pres  (TriAB, then cp in FP64) per (m, k, n) of the two tridiagonal factorisations
 // theta is carried as its departure from the base profile theta_b(z) (the full value only at the ABI boundary).
 #pragma once
 #include <stdint.h>
@@ -60,6 +60,11 @@ enum Level {
 // Per-level FP64 constants.
 enum Level64 { D_FLO, D_FHZ, D_PL1, D_PL2, D_THB, D_COUNT };
 
+// One mode's forward-sweep coefficients at one level: d_k = a r_k - b d_(k-1), a = (row scale) / pivot in FP32 (it
+// multiplies the FP32 right-hand side, rounded once like that value itself), b = lower / pivot in FP64.
+struct TriAB { double b; float a; float pad; };
+static_assert(sizeof(TriAB) == 16, "one 16-byte load a level");
+
 struct RunDesc {
   int nx, ny, nz, layer, n, nm, mh, ncells;
   int fx_nf, fy_nf, fx_rad[8], fy_rad[8];  // FFT radix plans of nx and ny
@@ -77,8 +82,8 @@ struct RunDesc {
   float* cols;
   const float* lv;
   const double* lv64;
-  const double2* tri_face;
-  const double2* tri_pres;
+  const TriAB* tri_face;
+  const TriAB* tri_pres;
   const double2* ab;       // pressure symbols (alpha, beta) per mode [m][n]
   const float2* twx;       // exp(-2 pi i t / nx), t < nx
   const float2* twy;       // exp(-2 pi i t / ny)

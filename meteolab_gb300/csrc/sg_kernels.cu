@@ -361,7 +361,7 @@ __global__ void k_proj_modes(const RunDesc* __restrict__ runs, const int4* items
     if (whole) F = fft_rows_any(S, T, ny, nzc, P);
     else fft_rows_grouped(S, T, ny, nzc, group, P);
     float2* Fo = F == S ? T : S;       // the other buffer (whole slab case)
-    const double2* AB = (mode == PROJ_FACE ? R.tri_face : R.tri_pres) + (size_t)m * nzc * ny;
+    const TriAB* AB = (mode == PROJ_FACE ? R.tri_face : R.tri_pres) + (size_t)m * nzc * ny;
     const double* Cc = reinterpret_cast<const double*>((mode == PROJ_FACE ? R.tri_face : R.tri_pres) + (size_t)R.nm * nzc * ny) + (size_t)m * nzc * ny;
     // one FP64 recurrence per (n, real/imaginary part); values enter and leave FP64 through the integer-pipe
     // conversions
@@ -372,8 +372,8 @@ __global__ void k_proj_modes(const RunDesc* __restrict__ runs, const int4* items
       double prev = 0;
 #pragma unroll 4
       for (int k = 0; k < nzc; k++) {
-        const double2 ab = AB[(size_t)k * ny + n];
-        prev = fma(-ab.y, prev, ab.x * widen(Ff[2 * (k * ny + n) + c]));
+        const TriAB ab = AB[(size_t)k * ny + n];
+        prev = fma(-ab.b, prev, widen(__fmul_rn(ab.a, Ff[2 * (k * ny + n) + c])));
         d[k] = prev;
       }
       double x = d[nzc - 1];
@@ -709,13 +709,13 @@ __global__ void k_proj_sweep(const RunDesc* __restrict__ runs, const int4* items
     if (u >= 2 * ny) continue;
     const int n = u >> 1, c = u & 1;
     float* g = reinterpret_cast<float*>(R.spec + (size_t)m * nzc * ny) + c;
-    const double2* AB = (mode == PROJ_FACE ? R.tri_face : R.tri_pres) + (size_t)m * nzc * ny;
+    const TriAB* AB = (mode == PROJ_FACE ? R.tri_face : R.tri_pres) + (size_t)m * nzc * ny;
     const double* Cc = reinterpret_cast<const double*>((mode == PROJ_FACE ? R.tri_face : R.tri_pres) + (size_t)R.nm * nzc * ny) + (size_t)m * nzc * ny;
     double d[MAXNZ];
     double prev = 0;
     // levels in blocks of 8: the block's coefficients and values are loaded before its recurrence steps
     for (int k0 = 0; k0 < nzc; k0 += 8) {
-      double2 ab[8];
+      TriAB ab[8];
       float r[8];
 #pragma unroll
       for (int j = 0; j < 8; j++) {
@@ -725,7 +725,7 @@ __global__ void k_proj_sweep(const RunDesc* __restrict__ runs, const int4* items
       }
 #pragma unroll
       for (int j = 0; j < 8; j++) {
-        if (k0 + j < nzc) { prev = fma(-ab[j].y, prev, ab[j].x * widen(r[j])); d[k0 + j] = prev; }
+        if (k0 + j < nzc) { prev = fma(-ab[j].b, prev, widen(__fmul_rn(ab[j].a, r[j]))); d[k0 + j] = prev; }
       }
     }
     double x = d[nzc - 1];

@@ -123,8 +123,8 @@ int cudaFail(sg_context* ctx, cudaError_t e, const char* where) {
 #define CK(call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) return cudaFail(ctx, e_, #call); } while (0)
 
 // ------------------------------------------------------------------ host precomputation
-// triF / triP: the Thomas coefficients of every mode, [m][k][n] (A, B) pairs followed by [m][k][n] C values.
-struct HostTables { std::vector<float> lv; std::vector<double> lv64; std::vector<double2> triF, triP, ab; std::vector<double> triFc, triPc; std::vector<float2> twx, twy; };
+// triF / triP: the Thomas coefficients of every mode, [m][k][n] TriAB (b, a) followed by [m][k][n] C values.
+struct HostTables { std::vector<float> lv; std::vector<double> lv64; std::vector<TriAB> triF, triP; std::vector<double2> ab; std::vector<double> triFc, triPc; std::vector<float2> twx, twy; };
 
 void twiddles(int n, std::vector<float2>& tw) {
   tw.resize(n);
@@ -205,7 +205,7 @@ void build_tables(const sg_grid* g, const sg_base_state* b, const sg_switches* s
     D(D_THB, z, thb[z]);
   }
   // Face projection factorisation [m][k][n] (src/core/advection.ts:222-241): rows -rho h lambda - lo - up.
-  T.triF.assign((size_t)nm * nz * ny, make_double2(0, 0)); T.triFc.assign((size_t)nm * nz * ny, 0.0);
+  T.triF.assign((size_t)nm * nz * ny, TriAB{0, 0.f, 0.f}); T.triFc.assign((size_t)nm * nz * ny, 0.0);
   std::vector<double> cp(nz);
   auto faceRho = [&](int k) { return k < 0 || k >= nz - 1 ? 0.0 : (rho[k] + rho[k + 1]) / 2; };
   for (int m = 0; m < nm; m++) for (int n = 0; n < ny; n++) {
@@ -217,15 +217,15 @@ void build_tables(const sg_grid* g, const sg_base_state* b, const sg_switches* s
       if (pinned && k == 1) lo = 0;
       double piv = k == 0 ? di : di - lo * cp[k - 1];
       cp[k] = up / piv;
-      // forward sweep d_k = A r_k - B d_(k-1) with A = h_k / pivot (the rows are scaled by h), B = lower / pivot
+      // forward sweep d_k = a r_k - b d_(k-1) with a = h_k / pivot (the rows are scaled by h), b = lower / pivot
       const double ip = pinned && k == 0 ? 0.0 : 1 / piv, lower = k > 0 ? faceRho(k - 1) / dzs[k - 1] : 0;
-      T.triF[((size_t)m * nz + k) * ny + n] = make_double2(ip * hz[k], ip * lower);
+      T.triF[((size_t)m * nz + k) * ny + n] = TriAB{ip * lower, (float)(ip * hz[k]), 0.f};
       T.triFc[((size_t)m * nz + k) * ny + n] = cp[k];
     }
   }
   // Pressure factorisation [m][k][n] (src/core/pressure.ts:37-44, :104-140), the symbols snapped as there.
   const int nc = nz - 1;
-  T.triP.assign((size_t)nm * nc * ny, make_double2(0, 0)); T.triPc.assign((size_t)nm * nc * ny, 0.0);
+  T.triP.assign((size_t)nm * nc * ny, TriAB{0, 0.f, 0.f}); T.triPc.assign((size_t)nm * nc * ny, 0.0);
   T.ab.assign((size_t)nm * ny, make_double2(0, 0));
   auto exact = [](double x) { return x < 1e-12 ? 0 : x > 1 - 1e-12 ? 1 : x; };
   for (int m = 0; m < nm; m++) for (int n = 0; n < ny; n++) {
@@ -244,7 +244,7 @@ void build_tables(const sg_grid* g, const sg_base_state* b, const sg_switches* s
       double piv = k == 0 ? di : di - lo * cp[k - 1];
       cp[k] = up / piv;
       const double ip = pinned && k == 0 ? 0.0 : 1 / piv;
-      T.triP[((size_t)m * nc + k) * ny + n] = make_double2(ip, ip * lo);
+      T.triP[((size_t)m * nc + k) * ny + n] = TriAB{ip * lo, (float)ip, 0.f};
       T.triPc[((size_t)m * nc + k) * ny + n] = cp[k];
     }
   }
@@ -757,8 +757,8 @@ int sg_run_create(sg_context* ctx, const sg_grid* g, const sg_base_state* b, con
   d.slot = slot;
   d.fld = (float*)(mem + Lo.fld); d.faces = (float*)(mem + Lo.faces); d.kmkh = (float*)(mem + Lo.kmkh); d.phi = (float*)(mem + Lo.phi);
   d.pres = (float*)(mem + Lo.pres); d.pres2 = (float*)(mem + Lo.pres2); d.spec = (float2*)(mem + Lo.spec); d.cols = (float*)(mem + Lo.cols);
-  d.lv = (const float*)(mem + Lo.lv); d.lv64 = (const double*)(mem + Lo.lv64); d.tri_face = (const double2*)(mem + Lo.triF);
-  d.tri_pres = (const double2*)(mem + Lo.triP); d.ab = (const double2*)(mem + Lo.ab); d.twx = (const float2*)(mem + Lo.twx);
+  d.lv = (const float*)(mem + Lo.lv); d.lv64 = (const double*)(mem + Lo.lv64); d.tri_face = (const TriAB*)(mem + Lo.triF);
+  d.tri_pres = (const TriAB*)(mem + Lo.triP); d.ab = (const double2*)(mem + Lo.ab); d.twx = (const float2*)(mem + Lo.twx);
   d.twy = (const float2*)(mem + Lo.twy); d.scr = (float*)(mem + Lo.scr); d.part = (double*)(mem + Lo.part); d.acc = (double*)(mem + Lo.acc);
   d.cnt = (unsigned long long*)(mem + Lo.cnt);
   d.diag = (float*)(mem + Lo.diag); d.rot = (double*)(mem + Lo.rot);
