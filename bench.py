@@ -275,8 +275,16 @@ def uneven_leg(ctx, steps: int, spinup: int):
     ctx.time_steps(runs, 3)
     ms = ctx.time_steps(runs, steps)
     cells = sum(r.grid.n for r in runs)
-    small = sum(r.grid.n for r in runs if r.grid.nx == 40)
     tile = ctx.transport_shape(runs)
+    # each size alone (its own plan, graph and tuned tile), from the same states: the per-size throughput, and what
+    # mixing the sizes in one launch costs or saves
+    alone = {}
+    for name, nx in (("standard", 40), ("large", 80)):
+        part = [r for r in runs if r.grid.nx == nx]
+        ctx.time_steps(part, 3)
+        pms = ctx.time_steps(part, steps)
+        alone[name] = {"runs": len(part), "cell_steps_s": sum(r.grid.n for r in part) * steps / (pms * 1e-3),
+                       "ms_per_step": pms / steps}
     for r in runs:
         r.retire()
     v = cells * steps / (ms * 1e-3)
@@ -284,7 +292,7 @@ def uneven_leg(ctx, steps: int, spinup: int):
     # when the tile width divides the grid widths.
     waste = 0.0 if all(nx % tile[0] == 0 and ny % tile[1] == 0 for nx, ny in ((40, 32), (80, 64))) else None
     return {"runs": "48 x 40x32x50 + 16 x 80x64x50", "cell_steps_s": v, "ms_per_step": ms / steps,
-            "standard_share_cell_steps_s": v * small / cells, "large_share_cell_steps_s": v * (cells - small) / cells,
+            "alone": alone, "mixed_vs_sizes_alone": (alone["standard"]["ms_per_step"] + alone["large"]["ms_per_step"]) / (ms / steps),
             "padding_waste": waste, "transport_tile": list(tile)}
 
 
@@ -372,6 +380,8 @@ def main():
 
     uneven = uneven_leg(ctx, max(5, args.steps // 2), args.spinup)
     serving = None if args.quick else serving_leg(ctx, rate=4.0, count=32, quantum=10)
+    # the serving configuration's range of arrival rates (0.5 to 8 runs/s), each with about 8-12 s of arrivals
+    serving_rates = None if args.quick else [serving_leg(ctx, rate=r, count=c, quantum=10) for r, c in ((0.5, 6), (2.0, 16), (8.0, 64))]
     cpu = cpu_baseline(10.0) if rank == 0 else None
     for r in runs:
         r.retire()
@@ -398,6 +408,7 @@ def main():
         "batched_vs_plain_standard": value / world / plain["standard"]["graph_cell_steps_s"],
         "uneven_batch": uneven,
         "serving": serving,
+        "serving_rates": serving_rates,
         "kernels_ms_per_launch": {k: round(v[0], 5) for k, v in prof.items()},
         "kernels_hbm_gbs": {k: round(cells * KERNEL_BYTES_PER_CELL[k] / (v[0] * 1e-3) / 1e9, 1)
                             for k, v in prof.items() if k in KERNEL_BYTES_PER_CELL and v[0] > 0},
