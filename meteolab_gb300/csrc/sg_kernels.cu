@@ -617,7 +617,7 @@ __device__ __forceinline__ void layer_inverse_fast(const RunDesc& R, float2* X, 
 
 // Divergence of one layer (FACE or PRES, as k_proj_div_xfft) and its 2-D forward transform, written
 // spec[(m * nzc + k) * ny + n].
-__global__ void __launch_bounds__(256, 4) k_proj_div_fft2(const RunDesc* __restrict__ runs, const int4* items, int nitems, int mode, int set) {
+__global__ void __launch_bounds__(256, 5) k_proj_div_fft2(const RunDesc* __restrict__ runs, const int4* items, int nitems, int mode, int set) {
   extern __shared__ float2 smc[];
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
@@ -746,7 +746,7 @@ __global__ void k_proj_sweep(const RunDesc* __restrict__ runs, const int4* items
 // The 2-D inverse transform of one layer (y, then x with the Hermitian rows rebuilt two real rows per complex
 // transform), normalised by nx*ny, into phi (FACE) or the pressure (PRES). Each inverse is the conjugate of the
 // forward transform of the conjugate.
-__global__ void __launch_bounds__(256, 4) k_proj_ifft2(const RunDesc* __restrict__ runs, const int4* items, int nitems, int mode) {
+__global__ void __launch_bounds__(256, 5) k_proj_ifft2(const RunDesc* __restrict__ runs, const int4* items, int nitems, int mode) {
   extern __shared__ float2 smc[];
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
