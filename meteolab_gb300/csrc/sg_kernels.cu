@@ -899,8 +899,8 @@ __global__ void k_pres_correct(const RunDesc* __restrict__ runs, const int4* ite
         const int i = base + j * B;
         if (i >= i1) break;
         const int k = zz[j];
-        const float hz = lvl(R, L_HZ, k);
-        const float wLo = k > 0 ? lvl(R, L_DZS, k - 1) / hz : 0.f, wHi = k < nz - 1 ? lvl(R, L_DZS, k) / hz : 0.f;
+        // dzs(k-1)/hz and dzs(k)/hz, rounded once from FP64 (zero at the ground and the top)
+        const float wLo = lvl(R, L_WLO, k), wHi = lvl(R, L_WHI, k);
         const float qx = .25f * R.inv_dx, qy = .25f * R.inv_dy, qz = .25f * lvl(R, L_INV_HZ, k);
         const bool inner = k > 0 && k < nz - 1;
         auto grad = [&](const float* l, const float* h, float& gx, float& gy, float& gz) {
