@@ -89,7 +89,10 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
 #define SP(g) (fld + fo[g])
 #define OP(g) (fld + oo + fo[g])
   const int PW = TX + 6, PH = TY + 6, NCELL = PW * PH;
-  const int NT = blockDim.x;
+  const int NT = CTX ? CTX * CTY : blockDim.x;  // the block is one thread a column of the tile
+  // plane cells a thread copies: exact for a compile-time tile, the bound TMAXC otherwise
+  constexpr int CJ = CTX ? ((CTX + 6) * (CTY + 6) + CTX * CTY - 1) / (CTX * CTY) : TMAXC;
+  static_assert(CJ <= TMAXC, "the tile's halo plane fits in TMAXC cells a thread");
   float* lv = sm;                                   // [tlv_rows][MAXNZ]
   float4* fcs = reinterpret_cast<float4*>(lv + tlv_rows(KIND) * MAXNZ);  // [2][NT]: the face fluxes of levels z, z + 1
   float* ring = reinterpret_cast<float*>(fcs + 2 * NT);  // [G][7][NCELL]
@@ -117,9 +120,9 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
     }
   }
   // plane cell t + j * NT of this thread: its column offset (periodic), -1 past the plane
-  int off[TMAXC];
+  int off[CJ];
 #pragma unroll
-  for (int j = 0; j < TMAXC; j++) {
+  for (int j = 0; j < CJ; j++) {
     int e = t + j * NT;
     int hy = e / PW, hx = e - hy * PW;
     int gx = x0 + hx - 3, gy = y0 + hy - 3;
@@ -134,7 +137,7 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
 #pragma unroll
     for (int g = 0; g < G; g++)
 #pragma unroll
-      for (int j = 0; j < TMAXC; j++) if (off[j] >= 0) ring[(g * 7 + slot) * NCELL + t + j * NT] = QP(g)[off[j] + lev * layer];
+      for (int j = 0; j < CJ; j++) if (off[j] >= 0) ring[(g * 7 + slot) * NCELL + t + j * NT] = QP(g)[off[j] + lev * layer];
   }
   if (on) cp_async16(fcs + t, F4 + col);
   float me = edgeW ? F4[eoff].x : edgeS ? F4[eoff].y : 0.f;
@@ -166,7 +169,7 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
 #pragma unroll
     for (int g = 0; g < G; g++)
 #pragma unroll
-      for (int j = 0; j < TMAXC; j++) if (off[j] >= 0) cp_async4(ring + (g * 7 + s_new) * NCELL + t + j * NT, QP(g) + off[j] + levNext);
+      for (int j = 0; j < CJ; j++) if (off[j] >= 0) cp_async4(ring + (g * 7 + s_new) * NCELL + t + j * NT, QP(g) + off[j] + levNext);
     float men = 0.f, s0n[G], bn[7];
 #pragma unroll
     for (int g = 0; g < G; g++) s0n[g] = 0.f;
