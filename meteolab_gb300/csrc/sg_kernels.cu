@@ -1013,15 +1013,20 @@ __device__ __forceinline__ void df_gradient_of(const RunDesc& R, int k, float l0
 // (into a pair of shared-memory planes); per dual layer, r = D v / dt rounded once into phi: D of the hi parts in double-FP32 (their differences
 // are exact), D of the lo parts (a few 1e-8 of them) in FP32. The pressure planes (dual levels k - 1 and k, with a
 // one-cell halo on the low sides) arrive by asynchronous copies a level ahead.
+// CTX x CTY: the tile as compile-time constants (20 x 8, the refinement tile of grids 40 wide), or 0 x 0 for a tile
+// given at run time.
+template <int CTX, int CTY>
 __global__ void __launch_bounds__(192, 4) k_refine_residual(const RunDesc* __restrict__ runs, const int4* items, int nitems, int set,
-                                                         int TX, int TY) {
+                                                         int TXr, int TYr) {
   extern __shared__ float rsm[];
+  const int TX = CTX ? CTX : TXr, TY = CTY ? CTY : TYr;
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
     if (R.cnt[C_FAILED] || !(R.flags & RF_REFINE)) continue;
     const int tile = items[it].y, z0 = items[it].z, z1 = items[it].w;
     const int nx = R.nx, ny = R.ny, nz = R.nz, layer = R.layer;
-    const int PW = TX + 2, PP = PW * (TY + 2), NW = TX + 1, NN = NW * (TY + 1), NT = blockDim.x, t = threadIdx.x;
+    const int PW = TX + 2, PP = PW * (TY + 2), NW = TX + 1, NN = NW * (TY + 1), t = threadIdx.x;
+    const int NT = CTX ? ((CTX + 1) * (CTY + 1) + 31) / 32 * 32 : (int)blockDim.x;
     float* pp = rsm;                 // [2][PP]: p1 of dual level d in slot d & 1, columns x0 - 1 .. x0 + TX
     float* nv = rsm + 2 * PP;        // [2][6][NN]: node level k in slot k & 1; u hi, u lo, v hi, v lo, w hi, w lo
     const int tilesX = (nx + TX - 1) / TX, x0 = (tile % tilesX) * TX, y0 = (tile / tilesX) * TY;
@@ -1551,7 +1556,8 @@ size_t refine_smem(int TX, int TY) { return ((size_t)2 * (TX + 2) * (TY + 2) + (
 void launch_refine_residual(const Launch& L, int set, int TX, int TY) {
   if (L.n == 0) return;
   const int threads = ((TX + 1) * (TY + 1) + 31) / 32 * 32;  // a thread per node of the tile and its halo
-  k_refine_residual<<<GRID(L.n, L.cap), threads, refine_smem(TX, TY), L.stream>>>(L.runs, L.items, L.n, set, TX, TY);
+  if (TX == 20 && TY == 8) k_refine_residual<20, 8><<<GRID(L.n, L.cap), threads, refine_smem(TX, TY), L.stream>>>(L.runs, L.items, L.n, set, TX, TY);
+  else k_refine_residual<0, 0><<<GRID(L.n, L.cap), threads, refine_smem(TX, TY), L.stream>>>(L.runs, L.items, L.n, set, TX, TY);
 }
 void launch_refine_correct(const Launch& L, int set) { k_pres_correct<2><<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set); }
 void launch_pres_correct(const Launch& L, int set, int final_) {
@@ -1578,7 +1584,8 @@ cudaError_t set_smem_limits(int bytes) {
   if ((e = smem_limit(k_sediment, bytes)) != cudaSuccess) return e;
   if ((e = smem_limit(k_proj_div_fft2, bytes)) != cudaSuccess) return e;
   if ((e = smem_limit(k_proj_ifft2, bytes)) != cudaSuccess) return e;
-  if ((e = smem_limit(k_refine_residual, bytes)) != cudaSuccess) return e;
+  if ((e = smem_limit(k_refine_residual<0, 0>, bytes)) != cudaSuccess) return e;
+  if ((e = smem_limit(k_refine_residual<20, 8>, bytes)) != cudaSuccess) return e;
   return set_transport_smem_limits(bytes);
 }
 
