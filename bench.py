@@ -5,7 +5,8 @@ One JSON line on rank 0. A "step" is one model time step (dt = 3 s) of every run
 Headline (`value`): the batched ensemble of BASELINE config 3 — 64 members on the standard 40x32x50 grid, seeded
 soundings, advanced together through one CUDA graph per step; inputs resident in HBM (213 MB per field set, larger
 than the 129 MB L2, so no flush is needed between steps). `e2e`: the same metric through the C ABI with host
-buffers: every step writes all members' fields from pinned host memory, steps, and reads them back.
+buffers: every step writes all members' fields from pinned host memory, steps, and reads them back (one
+sg_batch_step_io call a step, the members in four groups whose copies overlap the other groups' steps).
 Beside it: the plain single-run step on the standard, large (80x64x50) and stress (320x256x80) grids.
 `--impl reference`: the reference's algorithm on the host cores (the oracle port, OpenMP, all host threads) on a
 bounded sample of the same workload.
@@ -26,6 +27,8 @@ sys.path.insert(0, ROOT)
 
 METRIC = "cell-steps/s batched vs plain GPU step at <=1e-5 rel-L2; serve p50/p99 s/run"
 MEMBERS = 64
+# Groups of the e2e leg's sg_batch_step_io call (16 members each): the fastest of 1, 2, 4 and 8 on GB300.
+E2E_GROUPS = 4
 # The dominant kernel: the WENO5 transport of the 9 monotone fields (rain, snow, graupel, hail, q, cloud, ice,
 # iceNumber, cold), one launch per RK3 stage. Algorithmic bytes per cell and launch: each field read once and written
 # once (4 + 4 B), the step-start value read in stages 2 and 3 (4 B), the projected face fluxes (mx, my, mz, div: 16 B);
@@ -343,23 +346,29 @@ def main():
     tpc = traffic_per_cell()
     launches_per_step = sum(v[1] for v in prof.values())
 
-    # ---- e2e through the C ABI with a pinned host buffer: write all fields of all runs, step, read them all back,
-    # every step (the packed batch transfer: one copy each way)
+    # ---- e2e through the C ABI with a pinned host buffer: all fields of all runs written from it, one step, all read
+    # back into it, every step. Headline: one sg_batch_step_io call a step (the runs in E2E_GROUPS groups whose copies
+    # overlap the other groups' steps); beside it the same round trip as three separate calls (write, step, read).
     packed = torch.empty(cells * len(CARRIED), dtype=torch.float32, pin_memory=True).numpy()
     ctx.read_packed(runs, packed)
-    def e2e_step():
+    def e2e_serial():
         ctx.write_packed(runs, packed)
         ctx.batch_step(runs, 1, wait=False)
         ctx.read_packed(runs, packed)
-    for _ in range(2):
-        e2e_step()
+    def e2e_io():
+        ctx.batch_step_io(runs, packed, steps=1, groups=E2E_GROUPS)
     e2e_n = max(3, args.steps // 4)
-    barrier(pg)
-    t0 = time.perf_counter()
-    for _ in range(e2e_n):
-        e2e_step()
-    e2e_s = allmax(pg, time.perf_counter() - t0)
-    e2e_value = cells * world * e2e_n / e2e_s
+    e2e_values = {}
+    for name, fn in (("io", e2e_io), ("serial", e2e_serial)):
+        for _ in range(2):
+            fn()
+        barrier(pg)
+        t0 = time.perf_counter()
+        for _ in range(e2e_n):
+            fn()
+        e2e_s = allmax(pg, time.perf_counter() - t0)
+        e2e_values[name] = cells * world * e2e_n / e2e_s
+    e2e_value = e2e_values["io"]
     bytes_io = cells * 4 * len(CARRIED)
 
     # ---- plain single-run steps (eager launches and from a graph) on the standard, large and stress grids
@@ -395,7 +404,8 @@ def main():
         "config": {"workload": f"ensemble {args.members} x 40x32x50 per GPU, one CUDA graph per step", "cells_per_gpu": cells,
                    "spinup_steps": args.spinup, "transport_tile": {"x": tile[0], "y": tile[1], "weno_fields_per_item": tile[2], "weno_blocks_per_sm": tile[3]},
                    "l2": "inputs larger than L2 (213 MB per field set)", "parallelism": f"replicas x{world}"},
-        "e2e": {"value": e2e_value, "unit": "cell-steps/s", "h2d_bytes_per_step": bytes_io, "d2h_bytes_per_step": bytes_io},
+        "e2e": {"value": e2e_value, "unit": "cell-steps/s", "h2d_bytes_per_step": bytes_io, "d2h_bytes_per_step": bytes_io,
+                "call": f"sg_batch_step_io, {E2E_GROUPS} groups", "serial_calls_value": e2e_values["serial"]},
         "gpu_launches": launches_per_step * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm if achieved else None,
                      "traffic": tpc * cells if tpc else None, "kernel": "k_transport<WENO> (9 fields, one RK3 stage)", "peak_kind": peak_kind,

@@ -118,6 +118,13 @@ int sg_batch_read_fields(sg_context* ctx, const sg_run* runs, int n, uint32_t ma
  * synchronisation: the fastest way to move a batch's state (pinned host memory moves at link speed). */
 int sg_batch_write_packed(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, const float* host);
 int sg_batch_read_packed(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, float* host);
+/* Steps with the state moved through host memory around them, as the reference's GPU engine moves all fields in and
+ * out every step (src/gpu/dynamics.ts:446-450, :488-497; GpuDynamics.step, :404): the mask's fields of every run are
+ * written from `host` (the layout of sg_batch_write_packed), the runs advance `nsteps`, and the fields are read back
+ * into `host`. The runs are cut into `groups` (1..8, at most n) consecutive groups with a stream, a part of the staging
+ * buffer and a CUDA graph each, so one group's host copies overlap the other groups' steps; a run's results are the
+ * same as with sg_batch_write_packed, sg_batch_step and sg_batch_read_packed. Returns when every group is done. */
+int sg_batch_step_io(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, float* host, int nsteps, int groups);
 /* precipitation, hailGround, hailSize: nx*ny each (nullable); src/core/model.ts:253, :262. */
 int sg_run_read_columns(sg_context* ctx, sg_run run, float* precipitation, float* hail_ground, float* hail_size);
 /* The same columns written (each pointer nullable: that column is left as it is). */

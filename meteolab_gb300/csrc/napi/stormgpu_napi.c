@@ -104,11 +104,13 @@ static napi_value create_run(napi_env env, napi_callback_info info) {
   return out;
 }
 
-typedef struct { sg_context* ctx; sg_run* runs; int n, steps, status; napi_deferred deferred; napi_async_work work; } StepJob;
+/* host: the packed buffer of stepIo (NULL for step), held by `keep` while the work runs. */
+typedef struct { sg_context* ctx; sg_run* runs; int n, steps, groups, status; float* host; napi_ref keep; napi_deferred deferred; napi_async_work work; } StepJob;
 
 static void step_execute(napi_env env, void* data) {
   StepJob* j = (StepJob*)data;
-  j->status = sg_batch_step(j->ctx, j->runs, j->n, j->steps);
+  j->status = j->host ? sg_batch_step_io(j->ctx, j->runs, j->n, SG_ALL_FIELDS, j->host, j->steps, j->groups)
+                      : sg_batch_step(j->ctx, j->runs, j->n, j->steps);
 }
 static void step_complete(napi_env env, napi_status status, void* data) {
   StepJob* j = (StepJob*)data;
@@ -120,6 +122,7 @@ static void step_complete(napi_env env, napi_status status, void* data) {
     napi_reject_deferred(env, j->deferred, err);
   }
   napi_delete_async_work(env, j->work);
+  if (j->keep) napi_delete_reference(env, j->keep);
   free(j->runs); free(j);
 }
 
@@ -137,6 +140,35 @@ static napi_value step(napi_env env, napi_callback_info info) {
   napi_value promise, name;
   CHECK(env, napi_create_promise(env, &j->deferred, &promise));
   CHECK(env, napi_create_string_utf8(env, "stormgpu.step", NAPI_AUTO_LENGTH, &name));
+  CHECK(env, napi_create_async_work(env, NULL, name, step_execute, step_complete, j, &j->work));
+  CHECK(env, napi_queue_async_work(env, j->work));
+  return promise;
+}
+
+/* stepIo(ctx, runs: Int32Array, packed: Float32Array, steps, groups) -> Promise: every run's fields written from
+ * `packed` (run after run, the 13 fields in sg_field order), `steps` steps, the fields read back into `packed`
+ * (sg_batch_step_io) -- the per-step round trip of GpuDynamics.step (src/gpu/dynamics.ts:446-450, :488-497) for a
+ * whole batch, its copies overlapping the steps of the other groups. */
+static napi_value step_io(napi_env env, napi_callback_info info) {
+  size_t argc = 5; napi_value argv[5];
+  CHECK(env, napi_get_cb_info(env, info, &argc, argv, NULL, NULL));
+  StepJob* j = (StepJob*)calloc(1, sizeof(StepJob));
+  j->ctx = ctx_of(env, argv[0]);
+  napi_typedarray_type type; size_t len; void* data; napi_value buf; size_t off;
+  if (napi_get_typedarray_info(env, argv[1], &type, &len, &data, &buf, &off) != napi_ok || type != napi_int32_array) {
+    free(j); napi_throw_type_error(env, NULL, "runs: Int32Array"); return NULL;
+  }
+  j->n = (int)len; j->runs = (sg_run*)malloc(len * sizeof(sg_run)); memcpy(j->runs, data, len * sizeof(sg_run));
+  if (napi_get_typedarray_info(env, argv[2], &type, &len, &data, &buf, &off) != napi_ok || type != napi_float32_array) {
+    free(j->runs); free(j); napi_throw_type_error(env, NULL, "packed: Float32Array"); return NULL;
+  }
+  j->host = (float*)data;
+  napi_get_value_int32(env, argv[3], &j->steps);
+  napi_get_value_int32(env, argv[4], &j->groups);
+  CHECK(env, napi_create_reference(env, argv[2], 1, &j->keep));
+  napi_value promise, name;
+  CHECK(env, napi_create_promise(env, &j->deferred, &promise));
+  CHECK(env, napi_create_string_utf8(env, "stormgpu.stepIo", NAPI_AUTO_LENGTH, &name));
   CHECK(env, napi_create_async_work(env, NULL, name, step_execute, step_complete, j, &j->work));
   CHECK(env, napi_queue_async_work(env, j->work));
   return promise;
@@ -234,6 +266,7 @@ static napi_value init(napi_env env, napi_value exports) {
     {"writeFields", 0, write_fields, 0, 0, 0, napi_default, 0}, {"status", 0, status, 0, 0, 0, napi_default, 0},
     {"retire", 0, retire, 0, 0, 0, napi_default, 0}, {"destroyContext", 0, destroy_context, 0, 0, 0, napi_default, 0},
     {"saveState", 0, save_state, 0, 0, 0, napi_default, 0}, {"loadState", 0, load_state, 0, 0, 0, napi_default, 0},
+    {"stepIo", 0, step_io, 0, 0, 0, napi_default, 0},
   };
   napi_define_properties(env, exports, sizeof d / sizeof d[0], d);
   return exports;

@@ -112,6 +112,11 @@ struct sg_context {
   float* staging = nullptr;
   size_t stagingBytes = 0;
   std::map<std::vector<int>, std::pair<int4*, int>> packs;
+  // the groups of sg_batch_step_io: a stream each, the event that ends each group's work, and the event their work
+  // starts after (created on first use)
+  static constexpr int IO_GROUPS = 8;
+  cudaStream_t io[IO_GROUPS] = {};
+  cudaEvent_t ioEv[IO_GROUPS + 1] = {};
 };
 
 namespace {
@@ -714,6 +719,8 @@ int sg_context_destroy(sg_context* ctx) {
   cudaStreamDestroy(ctx->stream);
   for (int k = 0; k < 2; k++) cudaStreamDestroy(ctx->side[k]);
   for (int k = 0; k < 8; k++) cudaEventDestroy(ctx->dep[k]);
+  for (int k = 0; k < sg_context::IO_GROUPS; k++) if (ctx->io[k]) cudaStreamDestroy(ctx->io[k]);
+  for (int k = 0; k <= sg_context::IO_GROUPS; k++) if (ctx->ioEv[k]) cudaEventDestroy(ctx->ioEv[k]);
   for (auto& p : ctx->packs) cudaFree(p.second.first);
   if (ctx->staging) cudaFree(ctx->staging);
   delete ctx;
@@ -850,16 +857,15 @@ int batch_fields(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, floa
   return SG_OK;
 }
 
-// Fields of many runs packed run after run (the mask's fields in field order, n nodes each) through one staging
-// buffer: one host copy, one kernel, one synchronisation. The packing follows the caller's order of the runs.
-int batch_packed(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, float* host, bool write) {
-  if (!ctx || !host) return SG_ERR_INVALID;
-  cudaSetDevice(ctx->device);
+// The placing items of a packed batch (run after run in the caller's order, the mask's fields in field order, n
+// nodes each; item w = the chunk's offset in the packed buffer) and the buffer's length in floats, cached per
+// (runs, mask).
+static int pack_items(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, std::pair<int4*, int>& out, size_t& total) {
   std::vector<int> key;
   int st = slots_of(ctx, runs, n, key);
   if (st != SG_OK) return st;
   key.push_back((int)mask);
-  size_t total = 0;
+  total = 0;
   for (int k = 0; k < n; k++) {
     const Run* r = find(ctx, runs[k]);
     for (int f = 0; f < NF; f++) if (mask & (1u << f)) total += (size_t)r->nx * r->ny * r->nz;
@@ -884,19 +890,98 @@ int batch_packed(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, floa
     if (ctx->packs.size() > 64) { for (auto& p : ctx->packs) cudaFree(p.second.first); ctx->packs.clear(); }
     it = ctx->packs.emplace(key, std::make_pair(d, (int)items.size())).first;
   }
-  if (ctx->stagingBytes < total * 4) {
+  out = it->second;
+  return SG_OK;
+}
+
+// The context's staging buffer, grown to at least `floats` values.
+static int ensure_staging(sg_context* ctx, size_t floats) {
+  if (ctx->stagingBytes < floats * 4) {
     if (ctx->staging) cudaFree(ctx->staging);
     ctx->staging = nullptr; ctx->stagingBytes = 0;
-    CK(cudaMalloc(&ctx->staging, total * 4));
-    ctx->stagingBytes = total * 4;
+    CK(cudaMalloc(&ctx->staging, floats * 4));
+    ctx->stagingBytes = floats * 4;
   }
-  Launch L{ctx->d_runs, it->second.first, it->second.second, ctx->sms * 8, ctx->stream};
+  return SG_OK;
+}
+
+// Fields of many runs packed run after run (the mask's fields in field order, n nodes each) through one staging
+// buffer: one host copy, one kernel, one synchronisation. The packing follows the caller's order of the runs.
+static int batch_packed(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, float* host, bool write) {
+  if (!ctx || !host) return SG_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  std::pair<int4*, int> items;
+  size_t total = 0;
+  int st = pack_items(ctx, runs, n, mask, items, total);
+  if (st != SG_OK) return st;
+  if ((st = ensure_staging(ctx, total)) != SG_OK) return st;
+  Launch L{ctx->d_runs, items.first, items.second, ctx->sms * 8, ctx->stream};
   if (write) {
     CK(cudaMemcpyAsync(ctx->staging, host, total * 4, cudaMemcpyHostToDevice, ctx->stream));
     launch_pack(L, ctx->staging, 1);
   } else {
     launch_pack(L, ctx->staging, 0);
     CK(cudaMemcpyAsync(host, ctx->staging, total * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaGetLastError());
+  return SG_OK;
+}
+
+// Steps with the state moved through host memory around them, as the reference's GPU engine moves it every step
+// (src/gpu/dynamics.ts:446-450, :488-497): the mask's fields of every run are written from `host` (the packed layout),
+// the runs advance `nsteps`, and the fields are read back into `host`. The runs are cut into `groups` consecutive
+// groups, each with a stream, a part of the staging buffer and a graph of its own, so one group's copies overlap the
+// other groups' steps. Each group's runs step exactly as in any other batch (a run's results do not depend on the
+// runs beside it).
+static int batch_step_io(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, float* host, int nsteps, int groups) {
+  if (!ctx || !host) return SG_ERR_INVALID;
+  if (nsteps < 0) return fail(ctx, SG_ERR_INVALID, "negative step count");
+  cudaSetDevice(ctx->device);
+  std::vector<int> all;
+  int st = slots_of(ctx, runs, n, all);
+  if (st != SG_OK) return st;
+  groups = std::max(1, std::min(std::min(groups, n), sg_context::IO_GROUPS));
+  // the plan and item-list caches drop everything when full: make room first, so no group's plan or items are dropped
+  // while the others are set up
+  if (ctx->plans.size() + groups > 256) ctx->plans.clear();
+  if (ctx->packs.size() + groups > 64) { for (auto& p : ctx->packs) cudaFree(p.second.first); ctx->packs.clear(); }
+  // set-up before any group's work is queued: plans, graphs (captured on the context's stream), item lists, staging
+  struct Group { int first = 0, count = 0; Plan* P = nullptr; std::pair<int4*, int> items; size_t off = 0, total = 0; };
+  std::vector<Group> gs(groups);
+  size_t total = 0;
+  for (int g = 0; g < groups; g++) {
+    Group& x = gs[g];
+    x.first = (int)((int64_t)n * g / groups);
+    x.count = (int)((int64_t)n * (g + 1) / groups) - x.first;
+    const std::vector<int> slots(all.begin() + x.first, all.begin() + x.first + x.count);
+    if (!(x.P = get_plan(ctx, slots, &st))) return st;
+    if ((st = ensure_graph(ctx, *x.P)) != SG_OK) return st;
+    if ((st = pack_items(ctx, runs + x.first, x.count, mask, x.items, x.total)) != SG_OK) return st;
+    x.off = total;
+    total += x.total;
+  }
+  if ((st = ensure_staging(ctx, total)) != SG_OK) return st;
+  for (int g = 0; g <= groups; g++) {
+    if (g < groups && !ctx->io[g]) CK(cudaStreamCreateWithFlags(&ctx->io[g], cudaStreamNonBlocking));
+    const int e = g < groups ? g : sg_context::IO_GROUPS;
+    if (!ctx->ioEv[e]) CK(cudaEventCreateWithFlags(&ctx->ioEv[e], cudaEventDisableTiming));
+  }
+  // the groups start after the work already on the context's stream; the stream's later work waits for them all
+  CK(cudaEventRecord(ctx->ioEv[sg_context::IO_GROUPS], ctx->stream));
+  for (int g = 0; g < groups; g++) {
+    const Group& x = gs[g];
+    cudaStream_t s = ctx->io[g];
+    float* dev = ctx->staging + x.off;
+    const Launch L{ctx->d_runs, x.items.first, x.items.second, ctx->sms * 8, s};
+    CK(cudaStreamWaitEvent(s, ctx->ioEv[sg_context::IO_GROUPS], 0));
+    CK(cudaMemcpyAsync(dev, host + x.off, x.total * 4, cudaMemcpyHostToDevice, s));
+    launch_pack(L, dev, 1);
+    for (int k = 0; k < nsteps; k++) CK(cudaGraphLaunch(x.P->exec, s));
+    launch_pack(L, dev, 0);
+    CK(cudaMemcpyAsync(host + x.off, dev, x.total * 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaEventRecord(ctx->ioEv[g], s));
+    CK(cudaStreamWaitEvent(ctx->stream, ctx->ioEv[g], 0));
   }
   CK(cudaStreamSynchronize(ctx->stream));
   CK(cudaGetLastError());
@@ -1162,6 +1247,9 @@ int sg_batch_write_packed(sg_context* ctx, const sg_run* runs, int n, uint32_t m
 }
 int sg_batch_read_packed(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, float* host) {
   return batch_packed(ctx, runs, n, mask, host, false);
+}
+int sg_batch_step_io(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, float* host, int nsteps, int groups) {
+  return batch_step_io(ctx, runs, n, mask, host, nsteps, groups);
 }
 
 int sg_run_retire(sg_context* ctx, sg_run run) {

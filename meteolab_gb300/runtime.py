@@ -110,6 +110,7 @@ def load():
             L.sg_batch_read_fields.argtypes = [vp, C.POINTER(C.c_int32), i32, C.c_uint32, C.POINTER(_FP)]
             L.sg_batch_write_packed.argtypes = [vp, C.POINTER(C.c_int32), i32, C.c_uint32, _FP]
             L.sg_batch_read_packed.argtypes = [vp, C.POINTER(C.c_int32), i32, C.c_uint32, _FP]
+            L.sg_batch_step_io.argtypes = [vp, C.POINTER(C.c_int32), i32, C.c_uint32, _FP, i32, i32]
             L.sg_set_transport_shape.argtypes = [vp, i32, i32, i32]
             L.sg_divergence_max_static.argtypes = [i32, vp, vp, vp, i32, i32, i32, C.c_double, C.c_double, C.POINTER(C.c_double),
                                                    C.POINTER(C.c_double), vp, C.POINTER(C.c_double), C.c_char_p, C.c_size_t]
@@ -249,6 +250,19 @@ class Context:
             raise ValueError("packed buffer must be contiguous float32")
         ids = (C.c_int32 * len(runs))(*[r.id for r in runs])
         self.check(load().sg_batch_read_packed(self.h, ids, len(runs), self._mask(names), packed.ctypes.data_as(_FP)), "read packed")
+
+    def batch_step_io(self, runs: Sequence["Run"], packed: np.ndarray, steps: int = 1, groups: int = 4,
+                      names: Iterable[str] = CARRIED):
+        """Write the runs' fields from `packed` (the layout of write_packed), advance them `steps`, read them back into
+        `packed`: the reference engine's per-step host round trip, with the runs cut into `groups` groups whose copies
+        overlap the other groups' steps."""
+        if packed.dtype != np.float32 or not packed.flags.c_contiguous:
+            raise ValueError("packed buffer must be contiguous float32")
+        ids = (C.c_int32 * len(runs))(*[r.id for r in runs])
+        self.check(load().sg_batch_step_io(self.h, ids, len(runs), self._mask(names), packed.ctypes.data_as(_FP), steps, groups),
+                   "batch step io")
+        for r in runs:
+            r.time += steps * r.spec.switches.dt
 
     def set_transport_shape(self, tile_x: int = 0, tile_y: int = 0, weno_group: int = 3):
         """Pin the transport tile (tile_x x tile_y columns, 1 or 3 WENO fields per item); tile_x = 0 returns to tuning."""

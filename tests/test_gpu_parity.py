@@ -267,6 +267,36 @@ def test_packed_transfer_matches_per_run_calls(ctx, storm):
         r.retire()
 
 
+@pytest.mark.parametrize("groups,pinned", [(1, False), (3, False), (1, True), (3, True)])
+def test_step_with_host_io_matches_separate_calls(ctx, storm, groups, pinned):
+    """sg_batch_step_io (write packed, step, read packed; the runs in groups whose copies overlap the other groups'
+    steps) gives the bits of the three separate calls, over an uneven batch and two rounds, from pageable and from
+    pinned host memory."""
+    large = baseline_run(create_grid(LARGE_GRID), seed=11)
+    specs = [storm, storm, large, storm, large]
+    a = [ctx.create(s) for s in specs]
+    b = [ctx.create(s) for s in specs]
+    ctx.batch_step(a + b, 3)
+    total = sum(r.grid.n for r in a) * len(CARRIED)
+    pa = np.empty(total, np.float32)
+    ctx.read_packed(a, pa)
+    pa[:a[0].grid.n] += np.float32(2e-4)  # a change the host makes between steps (the first run's rain)
+    if pinned:
+        import torch
+        pb = torch.empty(total, dtype=torch.float32, pin_memory=True).numpy()
+        pb[:] = pa
+    else:
+        pb = pa.copy()
+    for _ in range(2):
+        ctx.write_packed(a, pa)
+        ctx.batch_step(a, 1)
+        ctx.read_packed(a, pa)
+        ctx.batch_step_io(b, pb, steps=1, groups=groups)
+        assert np.array_equal(pa, pb)
+    for r in a + b:
+        r.retire()
+
+
 def test_autotuner_picks_a_valid_shape(ctx, storm):
     runs = [ctx.create(storm) for _ in range(4)]
     tx, ty, g, mb = ctx.transport_shape(runs)
