@@ -132,6 +132,17 @@ int sg_run_write_columns(sg_context* ctx, sg_run run, const float* precipitation
 /* The run's grid size. */
 int sg_run_shape(sg_context* ctx, sg_run run, int32_t* nx, int32_t* ny, int32_t* nz);
 
+/* ---- the storm's electric potential (ElectricSolver, src/core/electric.ts:15-60; re-solved by Lightning.discharge for
+ * every flash, src/core/lightning.ts:231). Laplacian(phi) = -rho/eps0 at the nodes of `grid`, phi = 0 on the ground and
+ * top levels, periodic in x and y; FP64 throughout (the reference's tests hold it to 1e-9 of the discrete equation).
+ * sg_electric_create replaces `new ElectricSolver(grid)` ("the electric solver needs an interior level" for nz < 3;
+ * nx, ny <= 2048); sg_electric_solve replaces `solve(rho, phi)`: rho (C/m^3) and phi (V) are host arrays of
+ * nx*ny*nz doubles, node x + nx*(y + ny*z). Errors are reported on the context (sg_last_error). */
+typedef struct sg_electric sg_electric;
+int sg_electric_create(sg_context* ctx, const sg_grid* grid, sg_electric** out);
+int sg_electric_solve(sg_electric* solver, const double* rho, double* phi);
+int sg_electric_destroy(sg_electric* solver);
+
 /* ---- per-run diagnostics (runs with switches.rotation). The rotation state after the last step (RotationState,
  * src/core/model.ts:263; the reference's field names) and the model time the device keeps for the swaths' ground shift. */
 typedef struct sg_rotation {

@@ -174,6 +174,48 @@ static napi_value step_io(napi_env env, napi_callback_info info) {
   return promise;
 }
 
+/* electricCreate(ctx, grid) -> solver: `new ElectricSolver(grid)` (src/core/electric.ts:24) on the device. */
+static napi_value electric_create(napi_env env, napi_callback_info info) {
+  size_t argc = 2; napi_value argv[2];
+  CHECK(env, napi_get_cb_info(env, info, &argc, argv, NULL, NULL));
+  sg_context* ctx = ctx_of(env, argv[0]);
+  sg_grid g; memset(&g, 0, sizeof g);
+  g.nx = (int32_t)get_num(env, argv[1], "nx"); g.ny = (int32_t)get_num(env, argv[1], "ny"); g.nz = (int32_t)get_num(env, argv[1], "nz");
+  g.dx = get_num(env, argv[1], "dx"); g.dy = get_num(env, argv[1], "dy"); g.height = get_num(env, argv[1], "height");
+  g.zs = typed_data(env, argv[1], "zs", NULL); g.dzs = typed_data(env, argv[1], "dzs", NULL); g.hz = typed_data(env, argv[1], "hz", NULL);
+  sg_electric* solver = NULL;
+  int st = sg_electric_create(ctx, &g, &solver);
+  if (st) return throw_status(env, ctx, st);
+  napi_value ext;
+  CHECK(env, napi_create_external(env, solver, NULL, NULL, &ext));
+  return ext;
+}
+
+/* electricSolve(ctx, solver, rho: Float64Array, phi: Float64Array): ElectricSolver.solve(rho, phi) (:33-60), synchronous
+ * (a solve is a fraction of a millisecond), as the reference's Lightning calls it for each flash. */
+static napi_value electric_solve(napi_env env, napi_callback_info info) {
+  size_t argc = 4; napi_value argv[4];
+  CHECK(env, napi_get_cb_info(env, info, &argc, argv, NULL, NULL));
+  sg_context* ctx = ctx_of(env, argv[0]);
+  void* solver = NULL; napi_get_value_external(env, argv[1], &solver);
+  napi_typedarray_type type; size_t len; void* rho; void* phi; napi_value buf; size_t off;
+  if (napi_get_typedarray_info(env, argv[2], &type, &len, &rho, &buf, &off) != napi_ok || type != napi_float64_array ||
+      napi_get_typedarray_info(env, argv[3], &type, &len, &phi, &buf, &off) != napi_ok || type != napi_float64_array) {
+    napi_throw_type_error(env, NULL, "rho, phi: Float64Array"); return NULL;
+  }
+  int st = sg_electric_solve((sg_electric*)solver, (const double*)rho, (double*)phi);
+  if (st) return throw_status(env, ctx, st);
+  return NULL;
+}
+
+static napi_value electric_destroy(napi_env env, napi_callback_info info) {
+  size_t argc = 1; napi_value argv[1];
+  CHECK(env, napi_get_cb_info(env, info, &argc, argv, NULL, NULL));
+  void* solver = NULL; napi_get_value_external(env, argv[0], &solver);
+  sg_electric_destroy((sg_electric*)solver);
+  return NULL;
+}
+
 static napi_value fields_io(napi_env env, napi_callback_info info, int write) {
   size_t argc = 3; napi_value argv[3]; int32_t run;
   CHECK(env, napi_get_cb_info(env, info, &argc, argv, NULL, NULL));
@@ -267,6 +309,8 @@ static napi_value init(napi_env env, napi_value exports) {
     {"retire", 0, retire, 0, 0, 0, napi_default, 0}, {"destroyContext", 0, destroy_context, 0, 0, 0, napi_default, 0},
     {"saveState", 0, save_state, 0, 0, 0, napi_default, 0}, {"loadState", 0, load_state, 0, 0, 0, napi_default, 0},
     {"stepIo", 0, step_io, 0, 0, 0, napi_default, 0},
+    {"electricCreate", 0, electric_create, 0, 0, 0, napi_default, 0}, {"electricSolve", 0, electric_solve, 0, 0, 0, napi_default, 0},
+    {"electricDestroy", 0, electric_destroy, 0, 0, 0, napi_default, 0},
   };
   napi_define_properties(env, exports, sizeof d / sizeof d[0], d);
   return exports;

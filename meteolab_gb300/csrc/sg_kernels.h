@@ -64,3 +64,9 @@ cudaError_t set_smem_limits(int bytes);
 cudaError_t set_transport_smem_limits(int bytes);  // (sg_transport.cu)
 
 }  // namespace sg
+
+// The context's device, stream and error message, for the entry points in other translation units (sg_runtime.cu).
+struct sg_context;
+int sg_context_device(sg_context* ctx);
+cudaStream_t sg_context_stream(sg_context* ctx);
+int sg_context_fail(sg_context* ctx, int code, const char* message);

@@ -729,6 +729,12 @@ int sg_context_destroy(sg_context* ctx) {
 
 const char* sg_last_error(sg_context* ctx) { return ctx ? ctx->error.c_str() : "no context"; }
 
+}  // extern "C"
+int sg_context_device(sg_context* ctx) { return ctx->device; }
+cudaStream_t sg_context_stream(sg_context* ctx) { return ctx->stream; }
+int sg_context_fail(sg_context* ctx, int code, const char* message) { return fail(ctx, code, message); }
+extern "C" {
+
 uint64_t sg_run_bytes(const sg_grid* grid) { return grid ? layout(grid->nx, grid->ny, grid->nz).total : 0; }
 
 int sg_run_create(sg_context* ctx, const sg_grid* g, const sg_base_state* b, const sg_switches* sw, const float* const* init, sg_run* out) {

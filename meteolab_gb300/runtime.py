@@ -109,6 +109,9 @@ def load():
             L.sg_batch_write_fields.argtypes = [vp, C.POINTER(C.c_int32), i32, C.c_uint32, C.POINTER(_FP)]
             L.sg_batch_read_fields.argtypes = [vp, C.POINTER(C.c_int32), i32, C.c_uint32, C.POINTER(_FP)]
             L.sg_batch_write_packed.argtypes = [vp, C.POINTER(C.c_int32), i32, C.c_uint32, _FP]
+            L.sg_electric_create.argtypes = [vp, C.POINTER(SgGrid), C.POINTER(vp)]
+            L.sg_electric_solve.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+            L.sg_electric_destroy.argtypes = [vp]
             L.sg_batch_read_packed.argtypes = [vp, C.POINTER(C.c_int32), i32, C.c_uint32, _FP]
             L.sg_batch_step_io.argtypes = [vp, C.POINTER(C.c_int32), i32, C.c_uint32, _FP, i32, i32]
             L.sg_set_transport_shape.argtypes = [vp, i32, i32, i32]
@@ -524,6 +527,55 @@ class Server:
         if getattr(self, "h", None):
             load().sg_server_destroy(self.h)
             self.h = None
+
+
+class ElectricSolver:
+    """The storm's electric potential on the device, the reference's ElectricSolver (src/core/electric.ts:15-72):
+    ``solve(rho)`` returns phi (V) with Laplacian(phi) = -rho/eps0 at the nodes (rho in C/m3, nx*ny*nz values), phi = 0
+    on the ground and top levels, periodic in x and y; ``field(phi, x, y, z)`` is E = -grad(phi) at a node."""
+
+    def __init__(self, ctx: Context, grid):
+        self.ctx, self.grid = ctx, grid
+        self._keep = [_f64(grid.zs), _f64(grid.dzs), _f64(grid.hz)]
+        dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+        g = SgGrid(grid.nx, grid.ny, grid.nz, 0, grid.dx, grid.dy, grid.height, dp(self._keep[0]), dp(self._keep[1]), dp(self._keep[2]))
+        h = C.c_void_p()
+        ctx.check(load().sg_electric_create(ctx.h, C.byref(g), C.byref(h)), "electric solver")
+        self.h = h
+
+    def solve(self, rho: np.ndarray, out: Optional[np.ndarray] = None) -> np.ndarray:
+        n = self.grid.nx * self.grid.ny * self.grid.nz
+        rho = np.ascontiguousarray(rho, dtype=np.float64).ravel()
+        if rho.size != n:
+            raise ValueError(f"rho must hold {n} values")
+        phi = out if out is not None else np.empty(n, np.float64)
+        if phi.dtype != np.float64 or not phi.flags.c_contiguous or phi.size != n:
+            raise ValueError(f"phi must be a contiguous float64 array of {n}")
+        self.ctx.check(load().sg_electric_solve(self.h, rho.ctypes.data_as(C.POINTER(C.c_double)), phi.ctypes.data_as(C.POINTER(C.c_double))),
+                       "electric solve")
+        return phi
+
+    def field(self, phi: np.ndarray, x: int, y: int, z: int):
+        """E = -grad(phi) (V/m) at node (x, y, z): centred, periodic in x and y, one-sided at the ground and top (:64-71)."""
+        g = self.grid
+        nx, ny, nz, layer = g.nx, g.ny, g.nz, g.nx * g.ny
+
+        def at(i, j, k):
+            return phi[((i + nx) % nx) + ((j + ny) % ny) * nx + k * layer]
+        lo, hi = max(0, z - 1), min(nz - 1, z + 1)
+        return (-(at(x + 1, y, z) - at(x - 1, y, z)) / (2 * g.dx), -(at(x, y + 1, z) - at(x, y - 1, z)) / (2 * g.dy),
+                -(at(x, y, hi) - at(x, y, lo)) / (g.zs[hi] - g.zs[lo]))
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().sg_electric_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def divergence_max_static(device: int, u_ptr: int, v_ptr: int, w_ptr: int, grid, rho, stream: int = 0) -> float:
