@@ -73,17 +73,23 @@ SG_HD Sat satIce(const Node& s, const Level& L) {
   return satExpand(L.qi_hi, L.qi_lo, L.bi, 22.587f * 273.86f, 273.86f, dT, t, L.tcb);
 }
 
+// Powers with dyadic exponents from correctly rounded square roots and products: within a few ulp of powf at a fraction
+// of its cost (the processes below evaluate several a node). x^(1/4), x^(1/8), x^(1/16).
+SG_HD float root4(float x) { return sqrtf(sqrtf(x)); }
+SG_HD float root8(float x) { return sqrtf(root4(x)); }
+SG_HD float root16(float x) { return sqrtf(root8(x)); }
+
 // Fall speeds (src/core/microphysics.ts:37, ice.ts:143, graupel.ts:21, hail.ts:102); fallsq = sqrt(rho_ground / rho).
 SG_HD float rainFall(float rain, float rho, float fallsq) { return rain > 0.f ? 36.34f * powf(.001f * rho * rain, .1364f) * fallsq : 0.f; }
 SG_HD float snowFall(float snow, float rho, float fallsq) {
-  return snow > 1e-9f ? C_S * GAMMA_4D / 6.f * powf(PI * RHO_S * N0S / (rho * snow), -.0625f) * fallsq : 0.f;
+  return snow > 1e-9f ? C_S * GAMMA_4D / 6.f * (1.f / root16(PI * RHO_S * N0S / (rho * snow))) * fallsq : 0.f;
 }
 SG_HD float fallCoef(float rho, float rhoX) { return sqrtf(4.f * G * rhoX / (3.f * .6f * rho)); }
-SG_HD float graupelFall(float x, float rho) { return x > 1e-9f ? fallCoef(rho, RHO_G) * GAMMA_45 / 6.f * powf(PI * RHO_G * N0G / (rho * x), -.125f) : 0.f; }
-SG_HD float hailFall(float x, float rho) { return x > 1e-9f ? fallCoef(rho, RHO_H) * GAMMA_45 / 6.f * powf(PI * RHO_H * N0H / (rho * x), -.125f) : 0.f; }
+SG_HD float graupelFall(float x, float rho) { return x > 1e-9f ? fallCoef(rho, RHO_G) * GAMMA_45 / 6.f * (1.f / root8(PI * RHO_G * N0G / (rho * x))) : 0.f; }
+SG_HD float hailFall(float x, float rho) { return x > 1e-9f ? fallCoef(rho, RHO_H) * GAMMA_45 / 6.f * (1.f / root8(PI * RHO_H * N0H / (rho * x))) : 0.f; }
 SG_HD float hailMaxDiameter(float hail, float rho) {  // src/core/hail.ts:107-111
   if (!(hail > 1e-9f)) return 0.f;
-  float lambda = powf(PI * RHO_H * N0H / (rho * hail), .25f);
+  float lambda = root4(PI * RHO_H * N0H / (rho * hail));
   return fmaxf(0.f, logf(N0H * 10.f / lambda) / lambda);
 }
 
@@ -91,7 +97,7 @@ SG_HD float hailMaxDiameter(float hail, float rho) {  // src/core/hail.ts:107-11
 SG_HD float rainProcesses(Node& s, const Level& L, float dt, bool evaporate) {
   const float tk = tcOf(s, L.exner) + 273.15f, rho = L.rho, p = L.p;
   float qc = s.cloud, qr = s.rain;
-  float rate = .001f * fmaxf(0.f, qc - .001f) + (qr > 0.f ? 2.2f * qc * powf(qr, .875f) : 0.f);
+  float rate = .001f * fmaxf(0.f, qc - .001f) + (qr > 0.f ? 2.2f * qc * (qr / root8(qr)) : 0.f);
   float production = fminf(qc, rate * dt);
   s.cloud -= production; s.rain += production;
   if (!evaporate || s.rain <= 0.f) return 0.f;         // (the saturation below is only needed to evaporate rain)
@@ -209,9 +215,9 @@ SG_HD float snowProcesses(Node& s, const Level& L, float dt) {
   if (qs <= 1e-9f) return 0.f;
   // at the temperature the routine starts with, as the reference evaluates it (the conversion above leaves it)
   const Sat si = tc < 0.f ? satIce(s, L) : Sat{0.f, 0.f};
-  float lambda = powf(PI * RHO_S * N0S / (rho * qs), .25f);
-  float sweep = PI * N0S * C_S * GAMMA_3D / (4.f * powf(lambda, 3.25f)) * fallsq;
-  float vent = N0S * (.78f / (lambda * lambda) + .31f * SC13 * GAMMA_5D2 * SQRT_C_S * sqrtf(fallsq) / sqrtf(NU) * powf(lambda, -2.625f));
+  float lambda = root4(PI * RHO_S * N0S / (rho * qs));
+  float sweep = PI * N0S * C_S * GAMMA_3D / (4.f * (lambda * lambda * lambda * root4(lambda))) * fallsq;
+  float vent = N0S * (.78f / (lambda * lambda) + .31f * SC13 * GAMMA_5D2 * SQRT_C_S * sqrtf(fallsq) / sqrtf(NU) * (1.f / (lambda * lambda * sqrtf(lambda) * root8(lambda))));
   float cooling = 0.f;
   if (tc < 0.f) {
     float saci = fminf(s.ice, sweep * expf(.025f * tc) * s.ice * dt); s.ice -= saci; s.snow += saci;
@@ -242,7 +248,7 @@ SG_HD float graupelProcesses(Node& s, const Level& L, float dt) {
   float cooling = 0.f;
   if (tc < 0.f) {
     if (s.rain > 1e-9f) {
-      float lambdaR = powf(PI * RHO_W * N0R / (rho * s.rain), .25f);
+      float lambdaR = root4(PI * RHO_W * N0R / (rho * s.rain));
       float l2 = lambdaR * lambdaR, l7 = l2 * l2 * l2 * lambdaR;
       float rate = 20.f * PI * PI * 100.f * N0R * RHO_W / rho * (expf(-.66f * tc) - 1.f) / l7;
       float frozen = fminf(s.rain, rate * dt); s.rain -= frozen; s.graupel += frozen; s.thp += LF * heat * frozen;
@@ -252,9 +258,9 @@ SG_HD float graupelProcesses(Node& s, const Level& L, float dt) {
   }
   float qg = s.graupel;
   if (qg <= 1e-9f) return 0.f;
-  float lambda = powf(PI * RHO_G * N0G / (rho * qg), .25f), a = fallCoef(rho, RHO_G);
-  float sweep = PI * N0G * a * GAMMA_35 / (4.f * powf(lambda, 3.5f));
-  float vent = N0G * (.78f / (lambda * lambda) + .31f * SC13 * GAMMA_275 * sqrtf(a / NU) * powf(lambda, -2.75f));
+  float lambda = root4(PI * RHO_G * N0G / (rho * qg)), a = fallCoef(rho, RHO_G);
+  float sweep = PI * N0G * a * GAMMA_35 / (4.f * (lambda * lambda * lambda * sqrtf(lambda)));
+  float vent = N0G * (.78f / (lambda * lambda) + .31f * SC13 * GAMMA_275 * sqrtf(a / NU) * (1.f / (lambda * lambda * sqrtf(lambda) * root4(lambda))));
   if (tc < 0.f) {
     float gacw = fminf(s.cloud, sweep * s.cloud * dt), gacr = fminf(s.rain, sweep * s.rain * dt);
     float gaci = fminf(s.ice, sweep * .1f * s.ice * dt), gacs = fminf(s.snow, sweep * expf(.09f * tc) * s.snow * dt);
@@ -275,7 +281,7 @@ SG_HD float graupelProcesses(Node& s, const Level& L, float dt) {
   return cooling;
 }
 // src/core/hail.ts:99, :118-131
-SG_HD float ventilationOf(float lambda, float a, float n0) { return n0 * (.78f / (lambda * lambda) + .31f * SC13 * GAMMA_275 * sqrtf(a / NU) * powf(lambda, -2.75f)); }
+SG_HD float ventilationOf(float lambda, float a, float n0) { return n0 * (.78f / (lambda * lambda) + .31f * SC13 * GAMMA_275 * sqrtf(a / NU) * (1.f / (lambda * lambda * sqrtf(lambda) * root4(lambda)))); }
 SG_HD float wetGrowth(float lambda, float a, float n0, float tc, float qv, const Level& L, float iceRate) {
   const float rho = L.rho;
   float heat = KA * -tc + LV * PSI * rho * ((L.q0_hi - qv) + L.q0_lo);   // qsatP(0, p) - qv
@@ -288,8 +294,8 @@ SG_HD float hailProcesses(Node& s, const Level& L, float dt) {
   float cooling = 0.f;
   // wetGrowing(graupel, N0G, RHO_G, ...) (src/core/hail.ts:127-131)
   if (tc < 0.f && s.graupel > 1e-9f) {
-    float lambda = powf(PI * RHO_G * N0G / (rho * s.graupel), .25f), a = fallCoef(rho, RHO_G);
-    float k = PI * N0G * a * GAMMA_35 / (4.f * powf(lambda, 3.5f));
+    float lambda = root4(PI * RHO_G * N0G / (rho * s.graupel)), a = fallCoef(rho, RHO_G);
+    float k = PI * N0G * a * GAMMA_35 / (4.f * (lambda * lambda * lambda * sqrtf(lambda)));
     if (k * (s.cloud + s.rain + .1f * s.ice + expf(.09f * tc) * s.snow) > wetGrowth(lambda, a, N0G, tc, s.q, L, k * (s.ice + s.snow))) {
       float turned = s.graupel * (1.f - expf(-dt / 60.f)); s.graupel -= turned; s.hail += turned;
     }
@@ -298,8 +304,8 @@ SG_HD float hailProcesses(Node& s, const Level& L, float dt) {
   if (qh <= 1e-9f) return 0.f;
   // at the starting temperature (the reference's qsatIce(tc, p)): the conversion above leaves it
   const Sat si = tc < 0.f ? satIce(s, L) : Sat{0.f, 0.f};
-  float lambda = powf(PI * RHO_H * N0H / (rho * qh), .25f), a = fallCoef(rho, RHO_H);
-  float k = PI * N0H * a * GAMMA_35 / (4.f * powf(lambda, 3.5f)), vent = ventilationOf(lambda, a, N0H);
+  float lambda = root4(PI * RHO_H * N0H / (rho * qh)), a = fallCoef(rho, RHO_H);
+  float k = PI * N0H * a * GAMMA_35 / (4.f * (lambda * lambda * lambda * sqrtf(lambda))), vent = ventilationOf(lambda, a, N0H);
   if (tc < 0.f) {
     float hacw = fminf(s.cloud, k * s.cloud * dt), hacr = fminf(s.rain, k * s.rain * dt), liquid = hacw + hacr;
     float haci = fminf(s.ice, k * .1f * s.ice * dt), hacs = fminf(s.snow, k * expf(.09f * tc) * s.snow * dt), frozen = liquid;
@@ -346,7 +352,7 @@ SG_HD void microphysics(Node& s, const Level& L, float dt, int flags, float& eva
     s.cold += hailProcesses(s, L, dt);
     if (iceBefore > 0.f) s.inum *= s.ice / iceBefore;
     float splinters = splintering(tcOf(s, exner)) * SPLINTERS * fmaxf(0.f, cloudBefore - s.cloud)
-      + (rainFrozen > 0.f ? fragmentsPerKg(powf(PI * RHO_W * N0R / (rho * rainBefore), .25f)) * rainFrozen : 0.f);
+      + (rainFrozen > 0.f ? fragmentsPerKg(root4(PI * RHO_W * N0R / (rho * rainBefore))) * rainFrozen : 0.f);
     if (splinters > 0.f) {
       float fromG = fminf(s.graupel, splinters * CRYSTAL_MASS), fromS = fminf(s.snow, splinters * CRYSTAL_MASS - fromG);
       s.graupel -= fromG; s.snow -= fromS; s.ice += fromG + fromS; s.inum += (fromG + fromS) / CRYSTAL_MASS;
