@@ -190,8 +190,18 @@ def cpu_baseline(seconds: float = 10.0):
         el = time.perf_counter() - t0
         if el >= seconds or n >= 2000:
             break
+    # the lightning's field solve (ElectricSolver.solve) restated with numpy's FFT, one thread, on the same grid
+    import electric
+    import numpy as np
+    rho = np.random.default_rng(1).standard_normal(spec.grid.n) * 1e-10
+    electric.solve(spec.grid, rho)
+    k, t1 = 0, time.perf_counter()
+    while time.perf_counter() - t1 < .5:
+        electric.solve(spec.grid, rho)
+        k += 1
     return {"value": spec.grid.n * n / el, "unit": "cell-steps/s", "cores": threads, "kind": "port",
-            "sample": f"{n} steps of one 40x32x50 member ({el:.1f} s), reference algorithm restated in C++ (oracle), OpenMP"}
+            "sample": f"{n} steps of one 40x32x50 member ({el:.1f} s), reference algorithm restated in C++ (oracle), OpenMP",
+            "electric_solve_ms": (time.perf_counter() - t1) / k * 1e3}
 
 
 def reference_arm(args, rank, pg):
@@ -387,6 +397,20 @@ def main():
                        "graph_cell_steps_s": spec.grid.n * n / (graphed * 1e-3), "graph_ms_per_step": graphed / n}
         r.retire()
 
+    # ---- the lightning's field solve (ElectricSolver) on the standard grid: one call with its host copies (FP64 in,
+    # FP64 out), wall time per solve
+    from meteolab_gb300.runtime import ElectricSolver
+    es = ElectricSolver(ctx, grid)
+    rho = np.random.default_rng(1).standard_normal(grid.n) * 1e-10
+    phi = np.empty_like(rho)
+    for _ in range(5):
+        es.solve(rho, phi)
+    t0, k = time.perf_counter(), 100
+    for _ in range(k):
+        es.solve(rho, phi)
+    electric_ms = (time.perf_counter() - t0) / k * 1e3
+    es.close()
+
     uneven = uneven_leg(ctx, max(5, args.steps // 2), args.spinup)
     serving = None if args.quick else serving_leg(ctx, rate=4.0, count=32, quantum=10)
     # the serving configuration's range of arrival rates (0.5 to 8 runs/s), each with about 8-12 s of arrivals
@@ -417,6 +441,7 @@ def main():
         "plain_single_run": plain,
         "batched_vs_plain_standard": value / world / plain["standard"]["graph_cell_steps_s"],
         "uneven_batch": uneven,
+        "electric_solve": {"grid": "40x32x50", "ms_per_solve": electric_ms, "host_io_bytes": 2 * grid.n * 8},
         "serving": serving,
         "serving_rates": serving_rates,
         "kernels_ms_per_launch": {k: round(v[0], 5) for k, v in prof.items()},
