@@ -78,9 +78,12 @@ SG_HD Sat satIce(const Node& s, const Level& L) {
 SG_HD float root4(float x) { return sqrtf(sqrtf(x)); }
 SG_HD float root8(float x) { return sqrtf(root4(x)); }
 SG_HD float root16(float x) { return sqrtf(root8(x)); }
+// x^y for x > 0 and a small exponent |y| < 1 (the rain laws): exp2(y log2 x). log2f's error (1 ulp of log2 x) enters
+// scaled by |y|, so the result stays within ~3e-7 of x^y, at a fraction of powf's cost.
+SG_HD float pow_small(float x, float y) { return exp2f(y * log2f(x)); }
 
 // Fall speeds (src/core/microphysics.ts:37, ice.ts:143, graupel.ts:21, hail.ts:102); fallsq = sqrt(rho_ground / rho).
-SG_HD float rainFall(float rain, float rho, float fallsq) { return rain > 0.f ? 36.34f * powf(.001f * rho * rain, .1364f) * fallsq : 0.f; }
+SG_HD float rainFall(float rain, float rho, float fallsq) { return rain > 0.f ? 36.34f * pow_small(.001f * rho * rain, .1364f) * fallsq : 0.f; }
 SG_HD float snowFall(float snow, float rho, float fallsq) {
   return snow > 1e-9f ? C_S * GAMMA_4D / 6.f * (1.f / root16(PI * RHO_S * N0S / (rho * snow))) * fallsq : 0.f;
 }
@@ -104,8 +107,8 @@ SG_HD float rainProcesses(Node& s, const Level& L, float dt, bool evaporate) {
   const Sat sw = satWater(s, L);
   const float qs = satv(sw), ex = excess(s.q, sw);     // ex = q - qs
   if (ex >= 0.f) return 0.f;
-  float rq = .001f * rho * s.rain, vent = 1.6f + 124.9f * powf(rq, .2046f);
-  float er = (-ex / qs) * vent * powf(rq, .525f) / (.001f * rho * (5.4e5f + 2.55e6f / (p / 100.f * qs)));
+  float rq = .001f * rho * s.rain, vent = 1.6f + 124.9f * pow_small(rq, .2046f);
+  float er = (-ex / qs) * vent * pow_small(rq, .525f) / (.001f * rho * (5.4e5f + 2.55e6f / (p / 100.f * qs)));
   float ev = fminf(fminf(s.rain, er * dt), -ex / (1.f + LV * LV * qs / (CP * RV * tk * tk)));
   s.rain -= ev; s.q += ev;
   return ev;
