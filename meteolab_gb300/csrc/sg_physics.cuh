@@ -78,7 +78,7 @@ SG_HD Sat satIce(const Node& s, const Level& L) {
 SG_HD float root4(float x) { return sqrtf(sqrtf(x)); }
 SG_HD float root8(float x) { return sqrtf(root4(x)); }
 SG_HD float root16(float x) { return sqrtf(root8(x)); }
-// x^y for x > 0 and a small exponent |y| < 1 (the rain laws): exp2(y log2 x). log2f's error (1 ulp of log2 x) enters
+// x^y for x > 0 and a small exponent |y| < 1 (the rain laws, Koenig's growth): exp2(y log2 x). log2f's error (1 ulp of log2 x) enters
 // scaled by |y|, so the result stays within ~3e-7 of x^y, at a fraction of powf's cost.
 SG_HD float pow_small(float x, float y) { return exp2f(y * log2f(x)); }
 
@@ -180,7 +180,7 @@ static const float KOENIG_A2_H[31] = SG_KOENIG_A2;
 #endif
 SG_HD float koenigGrowth(float tc, float m) {  // src/core/ice.ts:203-206
   float x = fclamp(-tc, 1.f, 31.f) - 1.f; int k = (int)fminf(29.f, floorf(x)); float f = x - (float)k, g = m * 1000.f;
-  return 1e-3f * ((1.f - f) * KOENIG_A1[k] * powf(g, KOENIG_A2[k]) + f * KOENIG_A1[k + 1] * powf(g, KOENIG_A2[k + 1]));
+  return 1e-3f * ((1.f - f) * KOENIG_A1[k] * pow_small(g, KOENIG_A2[k]) + f * KOENIG_A1[k + 1] * pow_small(g, KOENIG_A2[k + 1]));
 }
 // src/core/ice.ts:223-242
 SG_HD float iceProcesses(Node& s, const Level& L, float dt) {
