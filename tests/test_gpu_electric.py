@@ -82,3 +82,16 @@ def test_a_grid_without_interior_levels_is_refused(ctx):
     grid = create_grid(GridOptions(8, 8, 2, 8000.0, 8000.0, 1000.0, None))
     with pytest.raises(StormGpuError, match="needs an interior level"):
         solver(ctx, grid)
+
+
+@pytest.mark.parametrize("shape", [(5, 4, 3, None), (4, 3, 7, 120.0), (7, 6, 9, 80.0), (1, 1, 6, None), (9, 2, 5, None)])
+def test_small_and_odd_grids_match_the_oracle(ctx, shape):
+    """Odd widths (no Nyquist column), a single interior level, a single column and two-row grids."""
+    nx, ny, nz, bottom = shape
+    grid = create_grid(GridOptions(nx, ny, nz, nx * 900.0, ny * 1000.0, 4000.0, bottom))
+    rho = np.random.default_rng(nx * 100 + nz).standard_normal(nx * ny * nz) * 1e-9
+    s = solver(ctx, grid)
+    got = s.solve(rho)
+    s.close()
+    want = E.solve(grid, rho)
+    assert np.max(np.abs(got - want)) <= 1e-10 * np.max(np.abs(want))

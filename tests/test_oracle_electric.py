@@ -9,6 +9,7 @@ import os
 import sys
 
 import numpy as np
+import pytest
 
 sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "oracle"))
 import electric as E  # noqa: E402
@@ -115,3 +116,33 @@ def test_a_charged_layer_gives_the_parallel_plate_field():
 def test_a_point_charge_gives_coulomb_with_its_images():
     grid = point_grid()
     check_point(grid, E.solve(grid, point_charge(grid)), E.field)
+
+
+@pytest.mark.parametrize("shape", [(4, 3, 7, 120.0), (5, 4, 3, None), (6, 5, 9, 80.0)])
+def test_matches_a_dense_solve_of_the_same_equations(shape):
+    """The oracle against a direct dense solve of the discrete equations it restates (electric.ts:13-19): the periodic
+    5-point horizontal Laplacian plus the stretched vertical one at every interior node, phi = 0 on the ground and top."""
+    nx, ny, nz, bottom = shape
+    grid = create_grid(GridOptions(nx, ny, nz, nx * 900.0, ny * 1000.0, 4000.0, bottom))
+    rng = np.random.default_rng(nx * 100 + nz)
+    rho = rng.standard_normal(nx * ny * nz) * 1e-9
+    layer, ni = nx * ny, nz - 2
+    dzs, hz = np.asarray(grid.dzs), np.asarray(grid.hz)
+    A = np.zeros((ni * layer, ni * layer))
+    idx = lambda x, y, k: ((x % nx) + (y % ny) * nx) + (k - 1) * layer
+    for k in range(1, nz - 1):
+        lo, up = 1 / (hz[k] * dzs[k - 1]), 1 / (hz[k] * dzs[k])
+        for y in range(ny):
+            for x in range(nx):
+                r = idx(x, y, k)
+                for (xx, yy, c) in ((x + 1, y, 1 / grid.dx ** 2), (x - 1, y, 1 / grid.dx ** 2), (x, y + 1, 1 / grid.dy ** 2), (x, y - 1, 1 / grid.dy ** 2)):
+                    A[r, idx(xx, yy, k)] += c
+                A[r, r] -= 2 / grid.dx ** 2 + 2 / grid.dy ** 2 + lo + up
+                if k - 1 >= 1:
+                    A[r, idx(x, y, k - 1)] += lo
+                if k + 1 <= nz - 2:
+                    A[r, idx(x, y, k + 1)] += up
+    b = -rho[layer:(nz - 1) * layer] / E.EPSILON0
+    want = np.linalg.solve(A, b)
+    got = E.solve(grid, rho)[layer:(nz - 1) * layer]
+    assert np.max(np.abs(got - want)) <= 1e-12 * np.max(np.abs(want))
