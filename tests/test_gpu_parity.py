@@ -355,3 +355,23 @@ def test_nonfinite_run_fails_alone(ctx, storm):
         assert np.array_equal(a[k], b[k]), k
     for r in (sick, well, ref):
         r.retire()
+
+
+def test_step_with_host_io_refuses_bad_arguments(ctx, storm):
+    """sg_batch_step_io: an empty batch, a run named twice and a negative step count are refused with a message; a
+    group count out of 1..8 is brought into it."""
+    from meteolab_gb300.runtime import StormGpuError
+    r = ctx.create(storm)
+    buf = np.empty(r.grid.n * len(CARRIED), np.float32)
+    ctx.read_packed([r], buf)
+    with pytest.raises(StormGpuError, match="empty batch"):
+        ctx.batch_step_io([], buf)
+    with pytest.raises(StormGpuError, match="twice"):
+        ctx.batch_step_io([r, r], np.empty(2 * buf.size, np.float32))
+    with pytest.raises(StormGpuError, match="negative step count"):
+        ctx.batch_step_io([r], buf, steps=-1)
+    before = buf.copy()
+    ctx.batch_step_io([r], buf, steps=1, groups=0)
+    ctx.batch_step_io([r], buf, steps=0, groups=99)
+    assert not np.array_equal(before, buf) and np.all(np.isfinite(buf))
+    r.retire()
