@@ -63,34 +63,49 @@ __global__ void k_elec_ydft(const double2* __restrict__ in, double2* __restrict_
 }
 
 // One horizontal mode (thread) over the interior levels, in place in S2[j][mode]: row j is node level k = j + 1,
-// lo phi_{k-1} + di phi_k + up phi_{k+1} = rhs with phi = 0 at both ends (src/core/electric.ts:41-56).
-__global__ void k_elec_thomas(double2* __restrict__ S2, double* __restrict__ cp, const double* __restrict__ lam, const double* __restrict__ lo_,
-                              const double* __restrict__ up_, int ni, int modes) {
+// lo phi_{k-1} + di phi_k + up phi_{k+1} = rhs with phi = 0 at both ends (src/core/electric.ts:41-56). The pivots
+// depend on the grid alone: cp = up / pivot and 1 / pivot come from the host (FP64), so a level costs two FMAs a lane.
+// The right-hand sides arrive eight levels ahead of the recurrence; the forward values wait in a per-thread column.
+constexpr int ELEC_MAXNI = 128;
+__global__ void k_elec_thomas(double2* __restrict__ S2, const double* __restrict__ cp, const double* __restrict__ ipiv,
+                              const double* __restrict__ lo_, int ni, int modes) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= modes) return;
-  const double l = lam[g];
-  double cprev = 0, dre = 0, dim = 0;
-  for (int j = 0; j < ni; j++) {
-    const int k = j + 1;
-    const double lo = lo_[k], up = up_[k], di = -lo - up - l;
-    const double a = j > 0 ? lo : 0, c = j < ni - 1 ? up : 0;
-    const double piv = j == 0 ? di : di - a * cprev;
-    const size_t e = (size_t)j * modes + g;
-    const double2 r = S2[e];
-    cprev = c / piv;
-    dre = (r.x - (j == 0 ? 0 : a * dre)) / piv;
-    dim = (r.y - (j == 0 ? 0 : a * dim)) / piv;
-    cp[e] = cprev;
-    S2[e] = make_double2(dre, dim);
+  double2 col[ELEC_MAXNI];
+  double2 d = make_double2(0, 0);
+  for (int j0 = 0; j0 < ni; j0 += 8) {
+    double2 r[8];
+    double ip[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const int j = min(j0 + q, ni - 1);
+      r[q] = S2[(size_t)j * modes + g];
+      ip[q] = ipiv[(size_t)j * modes + g];
+    }
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const int j = j0 + q;
+      if (j < ni) {
+        const double a = j > 0 ? lo_[j + 1] : 0;
+        d = make_double2((r[q].x - a * d.x) * ip[q], (r[q].y - a * d.y) * ip[q]);
+        col[j] = d;
+      }
+    }
   }
-  for (int j = ni - 2; j >= 0; j--) {
-    const size_t e = (size_t)j * modes + g;
-    const double c = cp[e];
-    double2 d = S2[e];
-    d.x -= c * dre;
-    d.y -= c * dim;
-    S2[e] = d;
-    dre = d.x; dim = d.y;
+  S2[(size_t)(ni - 1) * modes + g] = d;
+  for (int j1 = ni - 2; j1 >= 0; j1 -= 8) {
+    double c[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) c[q] = cp[(size_t)max(j1 - q, 0) * modes + g];
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const int j = j1 - q;
+      if (j >= 0) {
+        const double2 v = col[j];
+        d = make_double2(v.x - c[q] * d.x, v.y - c[q] * d.y);
+        S2[(size_t)j * modes + g] = d;
+      }
+    }
   }
 }
 
@@ -121,7 +136,7 @@ struct sg_electric {
   sg_context* ctx = nullptr;
   int nx = 0, ny = 0, nz = 0, mh = 0;
   char* mem = nullptr;
-  double *rho = nullptr, *phi = nullptr, *cp = nullptr, *lam = nullptr, *lo = nullptr, *up = nullptr;
+  double *rho = nullptr, *phi = nullptr, *cp = nullptr, *ipiv = nullptr, *lo = nullptr;
   double2 *S1 = nullptr, *S2 = nullptr, *twx = nullptr, *twy = nullptr;
 };
 
@@ -133,6 +148,7 @@ int sg_electric_create(sg_context* ctx, const sg_grid* g, sg_electric** out) {
   if (!g || !g->dzs || !g->hz || g->nx < 1 || g->ny < 1 || !(g->dx > 0) || !(g->dy > 0))
     return sg_context_fail(ctx, SG_ERR_INVALID, "electric solver: a grid with nx, ny >= 1, dx, dy > 0 and its level arrays");
   if (g->nz < 3) return sg_context_fail(ctx, SG_ERR_INVALID, "the electric solver needs an interior level");
+  if (g->nz - 2 > ELEC_MAXNI) return sg_context_fail(ctx, SG_ERR_INVALID, "electric solver: at most 130 levels");
   // (a row, a column and a half spectrum in shared memory: at most 32 KB)
   if (g->nx > 2048 || g->ny > 2048) return sg_context_fail(ctx, SG_ERR_INVALID, "electric solver: nx and ny at most 2048");
   const int nx = g->nx, ny = g->ny, nz = g->nz, mh = nx / 2, ni = nz - 2, modes = (mh + 1) * ny;
@@ -140,32 +156,44 @@ int sg_electric_create(sg_context* ctx, const sg_grid* g, sg_electric** out) {
     if (!(g->hz[k] > 0) || (k < nz - 1 && !(g->dzs[k] > 0))) return sg_context_fail(ctx, SG_ERR_INVALID, "electric solver: level spacings must be positive");
   if (cudaSetDevice(sg_context_device(ctx)) != cudaSuccess) return sg_context_fail(ctx, SG_ERR_DEVICE, "electric solver: cudaSetDevice");
   const size_t n = (size_t)nx * ny * nz, spec = (size_t)ni * modes;
-  // one allocation: rho, phi [n]; S1, S2 [ni][mh + 1][ny] complex; cp [ni][modes]; lam [modes]; lo, up [nz]; twiddles
+  // one allocation: rho, phi [n]; S1, S2 [ni][mh + 1][ny] complex; cp, 1/pivot [ni][modes]; lo [nz]; twiddles
   auto al = [](size_t b) { return (b + 255) / 256 * 256; };
   const size_t oRho = 0, oPhi = oRho + al(n * 8), oS1 = oPhi + al(n * 8), oS2 = oS1 + al(spec * 16), oCp = oS2 + al(spec * 16),
-               oLam = oCp + al(spec * 8), oLo = oLam + al((size_t)modes * 8), oUp = oLo + al((size_t)nz * 8), oTx = oUp + al((size_t)nz * 8),
-               oTy = oTx + al((size_t)nx * 16), total = oTy + al((size_t)ny * 16);
+               oIp = oCp + al(spec * 8), oLo = oIp + al(spec * 8), oTx = oLo + al((size_t)nz * 8), oTy = oTx + al((size_t)nx * 16),
+               total = oTy + al((size_t)ny * 16);
   auto* s = new sg_electric;
   s->ctx = ctx; s->nx = nx; s->ny = ny; s->nz = nz; s->mh = mh;
   cudaError_t e = cudaMalloc(&s->mem, total);
   if (e != cudaSuccess) { delete s; cudaGetLastError(); return sg_context_fail(ctx, SG_ERR_BUDGET, "electric solver: device memory"); }
   s->rho = (double*)(s->mem + oRho); s->phi = (double*)(s->mem + oPhi); s->S1 = (double2*)(s->mem + oS1); s->S2 = (double2*)(s->mem + oS2);
-  s->cp = (double*)(s->mem + oCp); s->lam = (double*)(s->mem + oLam); s->lo = (double*)(s->mem + oLo); s->up = (double*)(s->mem + oUp);
+  s->cp = (double*)(s->mem + oCp); s->ipiv = (double*)(s->mem + oIp); s->lo = (double*)(s->mem + oLo);
   s->twx = (double2*)(s->mem + oTx); s->twy = (double2*)(s->mem + oTy);
-  // minus the eigenvalue of the 5-point horizontal Laplacian per mode (src/core/electric.ts:29), the rows' off-diagonals
-  // 1/(hz dzs) below and above each level (:45), the twiddles e^{2 pi i t / N}
-  std::vector<double> lam(modes), lo(nz, 0.0), up(nz, 0.0);
-  for (int m = 0; m <= mh; m++)
-    for (int q = 0; q < ny; q++)
-      lam[(size_t)m * ny + q] = 4 * std::pow(std::sin(PI * m / nx), 2) / (g->dx * g->dx) + 4 * std::pow(std::sin(PI * q / ny), 2) / (g->dy * g->dy);
+  // minus the eigenvalue of the 5-point horizontal Laplacian per mode (src/core/electric.ts:29), the rows'
+  // off-diagonals 1/(hz dzs) below and above each level (:45), and every mode's elimination in the reference's order
+  // (:46-48): piv = di - lo cp_{j-1}, cp = up / piv
+  std::vector<double> lo(nz, 0.0), up(nz, 0.0), cpv(spec), ipv(spec);
   for (int k = 1; k < nz - 1; k++) { lo[k] = 1 / (g->hz[k] * g->dzs[k - 1]); up[k] = 1 / (g->hz[k] * g->dzs[k]); }
+  for (int m = 0; m <= mh; m++)
+    for (int q = 0; q < ny; q++) {
+      const double lam = 4 * std::pow(std::sin(PI * m / nx), 2) / (g->dx * g->dx) + 4 * std::pow(std::sin(PI * q / ny), 2) / (g->dy * g->dy);
+      const size_t mode = (size_t)m * ny + q;
+      double cprev = 0;
+      for (int j = 0; j < ni; j++) {
+        const int k = j + 1;
+        const double di = -lo[k] - up[k] - lam, a = j > 0 ? lo[k] : 0, c = j < ni - 1 ? up[k] : 0;
+        const double piv = j == 0 ? di : di - a * cprev;
+        cprev = c / piv;
+        cpv[(size_t)j * modes + mode] = cprev;
+        ipv[(size_t)j * modes + mode] = 1 / piv;
+      }
+    }
   std::vector<double2> tx(nx), ty(ny);
   for (int t = 0; t < nx; t++) tx[t] = make_double2(std::cos(2 * PI * t / nx), std::sin(2 * PI * t / nx));
   for (int t = 0; t < ny; t++) ty[t] = make_double2(std::cos(2 * PI * t / ny), std::sin(2 * PI * t / ny));
   cudaStream_t st = sg_context_stream(ctx);
-  if ((e = cudaMemcpyAsync(s->lam, lam.data(), lam.size() * 8, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+  if ((e = cudaMemcpyAsync(s->cp, cpv.data(), cpv.size() * 8, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(s->ipiv, ipv.data(), ipv.size() * 8, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
       (e = cudaMemcpyAsync(s->lo, lo.data(), lo.size() * 8, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
-      (e = cudaMemcpyAsync(s->up, up.data(), up.size() * 8, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
       (e = cudaMemcpyAsync(s->twx, tx.data(), tx.size() * 16, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
       (e = cudaMemcpyAsync(s->twy, ty.data(), ty.size() * 16, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
       (e = cudaStreamSynchronize(st)) != cudaSuccess) {
@@ -191,7 +219,7 @@ int sg_electric_solve(sg_electric* s, const double* rho, double* phi) {
   const int txi = std::min(256, std::max(32, (nx + 31) / 32 * 32));
   k_elec_xdft<<<dim3(ny, ni), tx, (size_t)nx * 8, st>>>(s->rho, s->S1, s->twx, nx, ny, mh);
   k_elec_ydft<<<dim3(mh + 1, ni), tyb, (size_t)ny * 16, st>>>(s->S1, s->S2, s->twy, ny, mh, -1.0);
-  k_elec_thomas<<<(modes + 127) / 128, 128, 0, st>>>(s->S2, s->cp, s->lam, s->lo, s->up, ni, modes);
+  k_elec_thomas<<<(modes + 31) / 32, 32, 0, st>>>(s->S2, s->cp, s->ipiv, s->lo, ni, modes);
   k_elec_ydft<<<dim3(mh + 1, ni), tyb, (size_t)ny * 16, st>>>(s->S2, s->S1, s->twy, ny, mh, 1.0);
   k_elec_xidft<<<dim3(ny, ni), txi, (size_t)(mh + 1) * 16, st>>>(s->S1, s->phi, s->twx, nx, ny, mh);
   if ((e = cudaMemcpyAsync(phi, s->phi, n * 8, cudaMemcpyDeviceToHost, st)) != cudaSuccess || (e = cudaStreamSynchronize(st)) != cudaSuccess ||
