@@ -2,7 +2,7 @@
 """Benchmark of the StormLab model step on GB300: batched / served cell-steps/s beside the plain single-run step.
 
 One JSON line on rank 0. A "step" is one model time step (dt = 3 s) of every run in the workload.
-Headline (`value`): the batched ensemble of BASELINE config 3 — 64 members on the standard 40x32x50 grid, seeded
+Headline (`value`): the batched ensemble — 64 members on the standard 40x32x50 grid, seeded
 soundings, advanced together through one CUDA graph per step; inputs resident in HBM (213 MB per field set, larger
 than the 129 MB L2, so no flush is needed between steps). `e2e`: the same metric through the C ABI with host
 buffers: every step writes all members' fields from pinned host memory, steps, and reads them back (one
