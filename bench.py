@@ -8,8 +8,9 @@ than the 129 MB L2, so no flush is needed between steps). `e2e`: the same metric
 buffers: every step writes all members' fields from pinned host memory, steps, and reads them back (one
 sg_batch_step_io call a step, the members in four groups whose copies overlap the other groups' steps).
 Beside it: the plain single-run step on the standard, large (80x64x50) and stress (320x256x80) grids.
-`--impl reference`: the reference's algorithm on the host cores (the oracle port, OpenMP, all host threads) on a
-bounded sample of the same workload.
+`--impl reference`: the reference's algorithm on the host cores (the oracle port) on a bounded sample of the same
+workload (one member per host core, spun up like the GPU arm's), timed two ways (every step split over all threads;
+one member per thread) and reported as the faster.
 """
 from __future__ import annotations
 
@@ -173,64 +174,102 @@ def traffic_per_cell():
         return None
 
 
-def cpu_baseline(seconds: float = 10.0):
-    """The reference's algorithm (the oracle port) on the host cores, all threads, one standard-grid member."""
+def cpu_strategies(specs, steps: int, threads: int):
+    """The reference's algorithm (the oracle port: FP32 fields, FP64 arithmetic, the reference's task order) on the host
+    cores, two ways over the same member states, wall-clock measured:
+      * "openmp": the members one after another, each step split over all threads (the reference's in-step tasks,
+        src/core/threads.ts; its `npm run bench` times one run this way);
+      * "pool": one member per worker thread, all at once, each single-threaded (the reference's ensemble runner,
+        runPool, src/ensemble/pool.ts:19-47: one run per worker).
+    Returns {strategy: (cell-steps/s, ms per step of the whole sample)}."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
-    from meteolab_gb300.grid import DEFAULT_GRID, create_grid
-    from meteolab_gb300.scenarios import baseline_run
-    spec = baseline_run(create_grid(DEFAULT_GRID), seed=1)
-    threads = os.cpu_count() or 1
-    m = pyoracle.OracleModel(spec, threads=threads)
-    m.step(3.0, 2)  # warm-up
-    n, t0 = 0, time.perf_counter()
-    while True:
-        m.step(3.0, 1)
-        n += 1
+    from concurrent.futures import ThreadPoolExecutor
+    cells = sum(s.grid.n for s in specs)
+    out = {}
+    models = [pyoracle.OracleModel(s, threads=threads) for s in specs]
+    for m in models:
+        m.step(3.0, 1)  # warm-up
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for m in models:
+            m.step(3.0, 1)
+    el = time.perf_counter() - t0
+    out["openmp"] = (cells * steps / el, el * 1e3 / steps)
+    models = [pyoracle.OracleModel(s, threads=1) for s in specs]
+    with ThreadPoolExecutor(max_workers=len(models)) as ex:  # ctypes calls run without the GIL
+        list(ex.map(lambda m: m.step(3.0, 1), models))
+        t0 = time.perf_counter()
+        list(ex.map(lambda m: m.step(3.0, steps), models))
         el = time.perf_counter() - t0
-        if el >= seconds or n >= 2000:
-            break
-    # the lightning's field solve (ElectricSolver.solve) restated with numpy's FFT, one thread, on the same grid
-    import electric
+    out["pool"] = (cells * steps / el, el * 1e3 / steps)
+    return out
+
+
+def cpu_summary(strategies, threads: int, sample: str) -> dict:
+    best = max(strategies, key=lambda k: strategies[k][0])
+    return {"value": strategies[best][0], "unit": "cell-steps/s", "cores": threads, "kind": "port", "strategy": best,
+            "strategies": {k: {"cell_steps_s": v[0], "ms_per_step": v[1]} for k, v in strategies.items()},
+            "sample": sample}
+
+
+def cpu_baseline(states, steps: int = 30):
+    """The CPU baseline beside the GPU figures: both strategies of cpu_strategies on the GPU arm's own spun-up member
+    states (the first `threads` members), `steps` steps each; and the lightning's field solve restated with numpy."""
     import numpy as np
-    rho = np.random.default_rng(1).standard_normal(spec.grid.n) * 1e-10
-    electric.solve(spec.grid, rho)
+    threads = os.cpu_count() or 1
+    specs = states[:threads]
+    st = cpu_strategies(specs, steps, threads)
+    out = cpu_summary(st, threads, f"{len(specs)} of the ensemble's 40x32x50 members from the GPU arm's spun-up states, {steps} "
+                                   f"steps per strategy; reference algorithm restated in C++ (oracle)")
+    # the lightning's field solve (ElectricSolver.solve) restated with numpy's FFT, one thread, on the same grid
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import electric
+    grid = specs[0].grid
+    rho = np.random.default_rng(1).standard_normal(grid.n) * 1e-10
+    electric.solve(grid, rho)
     k, t1 = 0, time.perf_counter()
     while time.perf_counter() - t1 < .5:
-        electric.solve(spec.grid, rho)
+        electric.solve(grid, rho)
         k += 1
-    return {"value": spec.grid.n * n / el, "unit": "cell-steps/s", "cores": threads, "kind": "port",
-            "sample": f"{n} steps of one 40x32x50 member ({el:.1f} s), reference algorithm restated in C++ (oracle), OpenMP",
-            "electric_solve_ms": (time.perf_counter() - t1) / k * 1e3}
+    out["electric_solve_ms"] = (time.perf_counter() - t1) / k * 1e3
+    return out
 
 
 def reference_arm(args, rank, pg):
-    """--impl reference: the CPU port of the reference on the same workload, bounded sample per step."""
+    """--impl reference: the reference's algorithm on the host cores (the oracle port; no GPU, none of this package's
+    device code) on a bounded sample of the workload: the first `threads` members of the same seeded 64-member ensemble,
+    spun up --spinup steps in the pool strategy (untimed), then W warm-up and K timed steps in each strategy of
+    cpu_strategies; the faster is the line's value. ms_per_step is the measured wall time of one step of the sample."""
     if rank != 0:
         return
+    from meteolab_gb300.grid import DEFAULT_GRID, create_grid
+    from meteolab_gb300.scenarios import CARRIED, RunSpec, ensemble_members
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
-    from meteolab_gb300.grid import DEFAULT_GRID, create_grid
-    from meteolab_gb300.scenarios import ensemble_members
-    grid = create_grid(DEFAULT_GRID)
-    members = ensemble_members(grid, 2)
+    from concurrent.futures import ThreadPoolExecutor
     threads = os.cpu_count() or 1
-    ms = [pyoracle.OracleModel(s, threads=threads) for s in members]
-    for _ in range(args.warmup):
-        ms[0].step(3.0, 1)
-    times = []
-    for k in range(args.steps):
-        t0 = time.perf_counter()
-        ms[k % 2].step(3.0, 1)  # one member's step stands for the batch's per-member cost
-        times.append(time.perf_counter() - t0)
-    per_member = sum(times) / len(times)
-    value = grid.n / per_member
+    grid = create_grid(DEFAULT_GRID)
+    members = ensemble_members(grid, args.members, seed=2026)[:min(threads, args.members)]
+    if args.spinup:  # the GPU arm's spun-up state: storms with cloud and precipitation
+        models = [pyoracle.OracleModel(s, threads=1) for s in members]
+        with ThreadPoolExecutor(max_workers=len(models)) as ex:
+            list(ex.map(lambda m: m.step(3.0, args.spinup), models))
+        members = [RunSpec(s.grid, s.env, s.switches, {k: m.get(k).astype("float32") for k in CARRIED}, s.seed, s.label)
+                   for s, m in zip(members, models)]
+        del models
+    if args.warmup:
+        cpu_strategies(members, max(1, args.warmup // 2), threads)
+    st = cpu_strategies(members, args.steps, threads)
+    cpu = cpu_summary(st, threads, f"{len(members)} of the {args.members} ensemble members (40x32x50), spun up {args.spinup} steps, "
+                                   f"{args.steps} timed steps per strategy; reference algorithm restated in C++ (oracle)")
+    value = cpu["value"]
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": per_member * 1e3 * args.members, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded soundings, ellipsoid bubble)",
-            "config": {"workload": f"ensemble {args.members} x 40x32x50 (sampled: one member per step)", "cores": threads},
-            "cpu_baseline": {"value": value, "unit": "cell-steps/s", "cores": threads, "kind": "port",
-                             "sample": f"{args.steps} single-member steps of 40x32x50 (reference algorithm restated in C++, OpenMP)"},
+            "warmup": args.warmup, "ms_per_step": cpu["strategies"][cpu["strategy"]]["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded soundings, ellipsoid bubble)",
+            "config": {"workload": f"ensemble {args.members} x 40x32x50, sampled: the first {len(members)} members, "
+                                   f"all of them every timed step", "cores": threads, "spinup_steps": args.spinup},
+            "cpu_baseline": cpu,
             "e2e": {"value": value, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -415,7 +454,13 @@ def main():
     serving = None if args.quick else serving_leg(ctx, rate=4.0, count=32, quantum=10)
     # the serving configuration's range of arrival rates (0.5 to 8 runs/s), each with about 8-12 s of arrivals
     serving_rates = None if args.quick else [serving_leg(ctx, rate=r, count=c, quantum=10) for r, c in ((0.5, 6), (2.0, 16), (8.0, 64))]
-    cpu = cpu_baseline(10.0) if rank == 0 else None
+    # the CPU baseline on the ensemble's states as the timed GPU steps left them (developed storms)
+    cpu = None
+    if rank == 0:
+        from meteolab_gb300.scenarios import RunSpec
+        k = min(os.cpu_count() or 1, len(runs))
+        states = [RunSpec(m.grid, m.env, m.switches, r.read(), m.seed, m.label) for m, r in zip(members[:k], runs[:k])]
+        cpu = cpu_baseline(states)
     for r in runs:
         r.retire()
     if rank != 0:

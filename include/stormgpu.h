@@ -209,7 +209,8 @@ int sg_profile_kernels(sg_context* ctx, const sg_run* runs, int n, int nsteps, c
 /* Advance a batch `nsteps` steps (from its CUDA graph, or eagerly) between two CUDA events on the context's stream;
  * *ms receives the device time. */
 int sg_time_steps(sg_context* ctx, const sg_run* runs, int n, int nsteps, int use_graph, double* ms);
-/* Max |D R u| of the run's current velocities (FP64 on the device), for the divergence check. */
+/* Max |D R u| of the run's current velocities (FP64 on the device), for the divergence check. A NaN or infinite
+ * velocity gives a non-finite maximum and SG_ERR_NONFINITE. */
 int sg_run_divergence(sg_context* ctx, sg_run run, double* max_abs_div);
 
 /* ---- transport tile: the RK3 transport works on tiles of tile_x x tile_y columns, each work item carrying 1 or 3 of
@@ -227,12 +228,15 @@ int sg_batch_transport_shape(sg_context* ctx, const sg_run* runs, int n, int* sh
  * src/core/pressure.ts:50-66, runs on its own CPU arrays).
  * Max |D rho0 u| over the dual cells of velocities the caller holds in device memory (u, v, w: nx*ny*nz FP32 nodes,
  * x fastest; rho: nz and dzs: nz-1 host FP64 values), the same FP64 arithmetic as sg_run_divergence, on `stream` (NULL: the
- * default stream), synchronised before it returns. It allocates nothing: its scratch is a static device array of 256
- * bytes, so callers that must not allocate at that point (HBM fully committed, or device memory owned by another
- * allocator) can still check a projection. nz is at most SG_STATIC_MAX_NZ; a larger grid, or a bad argument, returns
- * SG_ERR_INVALID with the reason in err (err_len bytes, nullable). The first call on a device looks up the scratch
- * and the SM count (no allocation); make it before any stream capture. Calls that overlap on one device race on the
- * scratch: serialise them. */
+ * default stream; a stream of another device is refused), synchronised before it returns. The call allocates nothing:
+ * its scratch is a static device array of 256 bytes, so callers that must not allocate at that point (HBM fully
+ * committed, or device memory owned by another allocator) can still check a projection. The array and the kernel
+ * belong to the library's module: sg_context_create loads them for its device; without a context on the device, the
+ * first call loads them (under lazy module loading, the default, that takes a little device memory), so make that
+ * first call before HBM is committed or set CUDA_MODULE_LOADING=EAGER, and before any stream capture. nz is at most
+ * SG_STATIC_MAX_NZ; a larger grid, or a bad argument, returns SG_ERR_INVALID with the reason in err (err_len bytes,
+ * nullable). A NaN or infinite velocity returns SG_ERR_NONFINITE (*max_abs_div non-finite). Calls that overlap on one
+ * device race on the scratch: serialise them. The calling thread's current device is the same after the call. */
 #define SG_STATIC_MAX_NZ 128
 int sg_divergence_max_static(int device, const float* u, const float* v, const float* w, int nx, int ny, int nz,
                              double dx, double dy, const double* rho, const double* dzs, void* stream,

@@ -1478,10 +1478,13 @@ __global__ void k_divergence_max(const RunDesc* __restrict__ runs, const int4* i
       double ddx = (r0 * ((double)u[b] + u[f] - u[a] - u[ee]) + r1 * ((double)u[h] + u[tt] - u[g] - u[s])) / R.dx;
       double ddy = (r0 * ((double)v[ee] + v[f] - v[a] - v[b]) + r1 * ((double)v[s] + v[tt] - v[g] - v[h])) / R.dy;
       double ddz = (r1 * ((double)w[g] + w[h] + w[s] + w[tt]) - r0 * ((double)w[a] + w[b] + w[ee] + w[f])) / lvl(R, L_DZS, k);
-      m = fmax(m, fabs(ddx + ddy + ddz));
+      const double d = fabs(ddx + ddy + ddz);
+      m = (d > m || d != d) ? d : m;  // a NaN wins (fmax would drop it)
     }
-    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<unsigned long long*>(out), (unsigned long long)__double_as_longlong(m));
+    for (int o = 16; o > 0; o >>= 1) { const double a = __shfl_xor_sync(0xffffffffu, m, o); m = (a > m || a != a) ? a : m; }
+    // the bits of a non-negative double order as unsigned integers; a NaN with its sign cleared orders above +inf
+    if ((threadIdx.x & 31) == 0)
+      atomicMax(reinterpret_cast<unsigned long long*>(out), (unsigned long long)__double_as_longlong(m) & 0x7fffffffffffffffull);
   }
 }
 

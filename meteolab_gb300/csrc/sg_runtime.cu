@@ -59,6 +59,7 @@ struct Run {
   RunDesc desc{};
   int4* nodeItems = nullptr;  // inside mem
   int nNode = 0;
+  double waterStart = 0;      // the water reservoirs' sum when the run began (AtmosphereModel.water.start), kg
 };
 
 struct Plan {
@@ -73,6 +74,7 @@ struct Plan {
   bool layerfft = false;                                              // 2-D transforms per layer (see enqueue_part)
   size_t fftSmem = 0;                                                 // their shared memory: the largest over the runs
   bool refine = false;                                                // some run refines its final projection
+  bool unrefined = false;                                             // some run does not (k_pres_correct<1> has work)
   bool rotation = false;                                              // some run tracks its rotation and swaths
   bool tuned = false;                                                 // TX, TY, wenoG chosen by timing
   cudaGraph_t graph = nullptr;
@@ -363,7 +365,7 @@ int build_plan(sg_context* ctx, const std::vector<int>& slots, Plan& P) {
     for (int k = 0; k < r.nz - 1; k++) for (int y = 0; y < r.ny; y += P.yc) all[FAM_ROWS_PRES].push_back(make_int4(s, k, y, 0));
     for (int m = 0; m < r.nx / 2 + 1; m++) all[FAM_MODES].push_back(make_int4(s, m, 0, 0));
     all[FAM_RUNS].push_back(make_int4(s, 0, 0, 0));
-    if (r.desc.flags & RF_REFINE) P.refine = true;
+    if (r.desc.flags & RF_REFINE) P.refine = true; else P.unrefined = true;
     if (r.desc.flags & RF_ROTATION) P.rotation = true;
   }
   // mixing items: (run, tile, z0, z1), the column in four level ranges
@@ -501,7 +503,9 @@ void enqueue_project(sg_context* ctx, const Plan& P, int set, int final_, cudaSt
   Launch node = lx(ctx, P, FAM_NODE), cells = lx(ctx, P, FAM_CELLS);
   node.stream = cells.stream = stream;
   enqueue_solve(ctx, P, PROJ_PRES, set, stream, hook);
-  launch_pres_correct(node, set, final_); hook(final_ ? 16 : 10);  // (the final one skips refined runs)
+  // the final correction of unrefined runs (refined runs take theirs from both pressures below): not launched when
+  // every run of the plan refines
+  if (!final_ || P.unrefined) { launch_pres_correct(node, set, final_); hook(final_ ? 16 : 10); }
   if (final_ && P.refine) {
     Launch rr = lx(ctx, P, FAM_REFINE);
     rr.cap = rr.n; rr.stream = stream;
@@ -674,6 +678,25 @@ Plan* single_plan(sg_context* ctx, int slot, int* st) { return get_plan(ctx, std
 
 }  // namespace
 
+// waterReservoirs (src/core/water.ts:27-46) of initial fields on the host, FP64 in the reference's order: per level the
+// vapour above the environment's profile, the condensate (cloud water, ice) and the precipitation aloft, each weighted
+// by the level's air mass; nothing on the ground yet.
+static double water_reservoirs(const sg_grid* g, const sg_base_state* b, const float* const* f) {
+  const size_t layer = (size_t)g->nx * g->ny;
+  double vapour = 0, condensate = 0, aloft = 0;
+  for (int z = 0; z < g->nz; z++) {
+    const double mass = b->rho[z] * g->dx * g->dy * g->hz[z], q0 = b->q[z];
+    double v = 0, c = 0, a = 0;
+    for (size_t i = z * layer, e = i + layer; i < e; i++) {
+      v += f[Q][i] - q0;
+      c += (double)f[CLOUD][i] + f[ICE][i];
+      a += (double)f[RAIN][i] + f[SNOW][i] + f[GRAUPEL][i] + f[HAIL][i];
+    }
+    vapour += v * mass; condensate += c * mass; aloft += a * mass;
+  }
+  return vapour + condensate + aloft;
+}
+
 // ==================================================================== C ABI
 extern "C" {
 
@@ -702,6 +725,8 @@ int sg_context_create(int device, uint64_t hbm_budget_bytes, sg_context** out) {
     if ((e = cudaStreamCreateWithFlags(&ctx->side[k], cudaStreamNonBlocking)) != cudaSuccess) { delete ctx; return SG_ERR_DEVICE; }
   for (int k = 0; k < 8; k++)
     if ((e = cudaEventCreateWithFlags(&ctx->dep[k], cudaEventDisableTiming)) != cudaSuccess) { delete ctx; return SG_ERR_DEVICE; }
+  // the no-allocation divergence check's module (its code and static scratch) loads now, while the context is made
+  if (static_prepare(device) != 0) { cudaGetLastError(); delete ctx; return SG_ERR_DEVICE; }
   if (const char* a = getenv("SG_AUTOTUNE")) ctx->autotune = atoi(a) != 0;
   if (const char* a = getenv("SG_SPECTRAL_ROWS")) ctx->rowsOnly = atoi(a) != 0;
   *out = ctx;
@@ -795,6 +820,7 @@ int sg_run_create(sg_context* ctx, const sg_grid* g, const sg_base_state* b, con
   if (init) {
     int s2 = sg_run_write_fields(ctx, slot, SG_ALL_FIELDS, init);
     if (s2) { sg_run_retire(ctx, slot); return s2; }
+    r.waterStart = water_reservoirs(g, b, init);
   }
   return SG_OK;
 }
@@ -1037,7 +1063,7 @@ int sg_run_save_state(sg_context* ctx, sg_run run, const char* config_json, doub
   sg_run_counters c;
   int st = sg_run_status(ctx, run, &c);
   if (st != SG_OK && st != SG_ERR_NONFINITE) return st;
-  const double water[4] = {c.water_condensed, c.water_evaporated, c.water_rain_evaporated, c.water_surface};
+  const double water[5] = {c.water_condensed, c.water_evaporated, c.water_rain_evaporated, c.water_surface, r->waterStart};
   const std::string json = state::header_json(config_json, time, persisted, r->nx, r->ny, r->nz, water);
   const size_t need = state::image_bytes(json.size(), state::VERSION, r->nx, r->ny, r->nz);
   *size = need;
@@ -1084,8 +1110,9 @@ int sg_run_load_state(sg_context* ctx, sg_run run, const uint8_t* image, size_t 
   int st = sg_batch_write_packed(ctx, &run, 1, SG_ALL_FIELDS, fields.data());
   if (st != SG_OK) return st;
   if ((st = sg_run_write_columns(ctx, run, cols.data(), cols.data() + layer, cols.data() + 2 * layer)) != SG_OK) return st;
-  // the water budget goes on from the file's flows (state.ts:77)
+  // the water budget goes on from the file's flows and start (state.ts:77)
   CK(cudaMemcpyAsync(r->desc.acc + A_WATER, h.water, 3 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  r->waterStart = h.water[4];
   // the model time and the time the rotation has held; the rotation recomputed from the fields (state.ts:74-76)
   const double tp[2] = {h.time, h.persisted};
   CK(cudaMemcpyAsync(r->desc.rot + R_TIME, &tp[0], sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
@@ -1352,6 +1379,7 @@ int sg_run_divergence(sg_context* ctx, sg_run run, double* max_abs_div) {
   launch_divergence_max(lx(ctx, *P, FAM_CELLS), 0, ctx->d_scalar);
   CK(cudaMemcpyAsync(max_abs_div, ctx->d_scalar, 8, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  if (!std::isfinite(*max_abs_div)) return fail(ctx, SG_ERR_NONFINITE, "the run's velocities hold a non-finite value");
   return SG_OK;
 }
 

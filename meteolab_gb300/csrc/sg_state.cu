@@ -93,11 +93,11 @@ struct Reader {
     bool format_is_string = false;
     double num[6];
     bool is_num[6] = {};
-    double water[4] = {0, 0, 0, 0};  // the budget's condensed, evaporated, rainEvaporated, surface (absent: 0)
+    double water[5] = {0, 0, 0, 0, 0};  // the budget's condensed, evaporated, rainEvaporated, surface, start (absent: 0)
   };
-  // The header's "water" object: its four flows when they are numbers.
+  // The header's "water" object: its four flows and its start when they are numbers.
   bool water(int depth, Top* top) {
-    static const char* keys[4] = {"condensed", "evaporated", "rainEvaporated", "surface"};
+    static const char* keys[5] = {"condensed", "evaporated", "rainEvaporated", "surface", "start"};
     p++; ws();
     if (p < e && *p == '}') { p++; return true; }
     for (;;) {
@@ -108,7 +108,7 @@ struct Reader {
       if (p >= e || *p != ':') return false;
       p++; ws();
       bool done = false;
-      for (int k = 0; k < 4 && !done; k++)
+      for (int k = 0; k < 5 && !done; k++)
         if (key == keys[k] && p < e && (*p == '-' || std::isdigit((unsigned char)*p))) { if (!num(&top->water[k])) return false; done = true; }
       if (!done && !value(depth + 1)) return false;
       ws();
@@ -202,20 +202,20 @@ std::string parse(const uint8_t* buf, size_t len, Info& info) {
   info.time = top.num[1]; info.persisted = top.num[2];
   info.nx = (int)top.num[3]; info.ny = (int)top.num[4]; info.nz = (int)top.num[5];
   info.nfields = fields_of(info.version);
-  for (int k = 0; k < 4; k++) info.water[k] = top.water[k];
+  for (int k = 0; k < 5; k++) info.water[k] = top.water[k];
   info.data_offset = data_offset(length);
   if (len != image_bytes(length, info.version, info.nx, info.ny, info.nz)) return "the file's size does not match the grid";
   return "";
 }
 
-std::string header_json(const char* config, double time, double persisted, int nx, int ny, int nz, const double water[4]) {
+std::string header_json(const char* config, double time, double persisted, int nx, int ny, int nz, const double water[5]) {
   std::string j = "{\"format\":\"meteolab-state\",\"version\":" + std::to_string(VERSION) + ",\"config\":";
   j += config && *config ? config : "null";
   j += ",\"time\":" + js_number(time) + ",\"persisted\":" + js_number(persisted);
   j += ",\"nx\":" + std::to_string(nx) + ",\"ny\":" + std::to_string(ny) + ",\"nz\":" + std::to_string(nz);
   j += ",\"chargeGround\":0,\"flashCount\":{\"ic\":0,\"cg\":0}";
   j += ",\"water\":{\"condensed\":" + js_number(water[0]) + ",\"evaporated\":" + js_number(water[1]) + ",\"rainEvaporated\":" +
-       js_number(water[2]) + ",\"surface\":" + js_number(water[3]) + ",\"start\":0}";
+       js_number(water[2]) + ",\"surface\":" + js_number(water[3]) + ",\"start\":" + js_number(water[4]) + "}";
   j += ",\"added\":{\"heat\":0,\"vapour\":0,\"count\":0}";
   j += ",\"charge\":{\"separated\":0,\"ic\":0,\"cgNegative\":0,\"cgPositive\":0,\"precipitation\":0,\"conduction\":0}}";
   return j;

@@ -23,7 +23,7 @@ int carried_of(int k);
 struct Info {
   int version = 0, nx = 0, ny = 0, nz = 0, nfields = 0;
   double time = 0, persisted = 0;
-  double water[4] = {0, 0, 0, 0};  // the water budget's flows (condensed, evaporated, rainEvaporated, surface)
+  double water[5] = {0, 0, 0, 0, 0};  // the water budget's flows (condensed, evaporated, rainEvaporated, surface) and start
   size_t data_offset = 0;   // first float of the fields
 };
 
@@ -32,8 +32,9 @@ struct Info {
 std::string parse(const uint8_t* buf, size_t len, Info& info);
 
 // The version-5 header of saveState (state.ts:43-53) for a run of this grid; `config` is the caller's SimConfig as
-// JSON text (null when absent), `water` the budget's condensed, evaporated, rainEvaporated and surface flows.
-std::string header_json(const char* config, double time, double persisted, int nx, int ny, int nz, const double water[4]);
+// JSON text (null when absent), `water` the budget's condensed, evaporated, rainEvaporated and surface flows and its
+// start (the reservoirs' sum when the run began, AtmosphereModel.water.start).
+std::string header_json(const char* config, double time, double persisted, int nx, int ny, int nz, const double water[5]);
 
 // Whether `text` (null-terminated; null counts as valid) is one JSON value.
 bool json_valid(const char* text);

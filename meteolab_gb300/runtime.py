@@ -161,6 +161,14 @@ class _Packed:
         self.ptrs = (_FP * len(CARRIED))(*[a.ctypes.data_as(_FP) for a in self.fields])
 
 
+def run_bytes(grid) -> int:
+    """Bytes of HBM one run of this grid takes in a context (sg_run_bytes): what admission by budget counts."""
+    zs, dzs, hz = _f64(grid.zs), _f64(grid.dzs), _f64(grid.hz)
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    g = SgGrid(grid.nx, grid.ny, grid.nz, 0, grid.dx, grid.dy, grid.height, dp(zs), dp(dzs), dp(hz))
+    return int(load().sg_run_bytes(C.byref(g)))
+
+
 class Context:
     """One device context (one CUDA stream, an HBM budget, the runs it owns)."""
 
@@ -583,6 +591,8 @@ def divergence_max_static(device: int, u_ptr: int, v_ptr: int, w_ptr: int, grid,
     any allocation by the library (sg_divergence_max_static)."""
     rho = _f64(rho)
     dzs = _f64(grid.dzs)
+    if rho.size < grid.nz or dzs.size < grid.nz - 1:
+        raise ValueError(f"rho needs {grid.nz} levels and dzs {grid.nz - 1} spacings (got {rho.size}, {dzs.size})")
     out = C.c_double()
     err = C.create_string_buffer(160)
     rc = load().sg_divergence_max_static(device, u_ptr, v_ptr, w_ptr, grid.nx, grid.ny, grid.nz, grid.dx, grid.dy,

@@ -51,3 +51,26 @@ def test_context_create_fails_cleanly_without_a_device(lib):
         pytest.skip("a device is visible")
     assert lib.sg_context_create(0, 0, ctypes.byref(h)) != 0
     assert not h.value
+
+
+def test_napi_addon_compiles_against_the_documented_api():
+    """The N-API addon (meteolab_gb300/csrc/napi/stormgpu_napi.c) compiles without a warning against declarations of
+    the Node-API calls it makes (tests/napi_stub/node_api.h; no Node here to provide its own header)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("cc") or shutil.which("gcc")
+    if not cc:
+        pytest.skip("no C compiler")
+    src = os.path.join(ROOT, "meteolab_gb300", "csrc", "napi", "stormgpu_napi.c")
+    r = subprocess.run([cc, "-std=c11", "-fsyntax-only", "-Wall", "-Wextra", "-Werror", "-Wno-unused-parameter",
+                        "-I", os.path.join(ROOT, "tests", "napi_stub"), src], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
+def test_static_check_refuses_short_level_arrays():
+    """The Python mirror of sg_divergence_max_static checks the level arrays' lengths before the C side reads them."""
+    from meteolab_gb300.grid import DEFAULT_GRID, create_grid
+    from meteolab_gb300.runtime import divergence_max_static
+    g = create_grid(DEFAULT_GRID)
+    with pytest.raises(ValueError, match="levels"):
+        divergence_max_static(0, 0, 0, 0, g, [1.0] * (g.nz - 1))

@@ -1,4 +1,6 @@
-"""The device step at the benchmark's full sizes (GPU), through size-independent properties: the large 80x64x50
+"""The device step at the benchmark's full sizes (GPU). Per field against the FP64 oracle: one step on the large and the
+stress grid, and the two switches no other parity case exercises, the wind limits (clipWind) and a moving frame.
+Through size-independent properties: the large 80x64x50
 domain and the 320x256x80 stress grid (its layer spectrum too wide for shared memory: the row-transform path of the
 spectral solves), each grown from a warm bubble for 100 steps (the scope of the large and stress configurations):
 every field finite, no wind clipped, the post-projection divergence before its FP32 rounding at rounding level (the
@@ -7,8 +9,9 @@ rain gauge to the reference's 1e-4 (src/core/invariants.test.ts:84-94), and the 
 import numpy as np
 import pytest
 
-from parity import WATER, dual_divergence, pressure_gradient, water_total
-from meteolab_gb300.grid import LARGE_GRID, STRESS_GRID, create_grid
+import pyoracle as O
+from parity import FLOOR, WATER, developed_state, dual_divergence, field_errors, pressure_gradient, rel_l2, threads, water_total
+from meteolab_gb300.grid import DEFAULT_GRID, LARGE_GRID, STRESS_GRID, create_grid
 from meteolab_gb300.scenarios import CARRIED, baseline_run
 
 pytestmark = pytest.mark.gpu
@@ -71,3 +74,75 @@ def test_the_stress_grid_is_the_same_alone_and_in_a_batch(ctx):
         assert np.array_equal(fa[k], fx[k]), k
     for run in (a, x, y):
         run.retire()
+
+
+# ---- per field against the FP64 oracle at full size: one step from a state the faithful oracle grew
+def _one_step_parity(ctx, state, label, bound=1e-5):
+    o64 = O.OracleModel(state, fp64=True, threads=threads())
+    o64.step(state.switches.dt, 1)
+    ref = o64.fields()
+    r = ctx.create(state)
+    r.step(1)
+    got = r.read()
+    errs = field_errors(got, ref)
+    thb = np.repeat(state.env.theta, state.grid.layer)
+    errs["theta'"] = rel_l2(r.debug_read_set(0, "theta"), ref["theta"] - thb, FLOOR["theta'"])
+    errs["precipitation"] = rel_l2(r.columns()["precipitation"], o64.get("precipitation"), 1e-9)
+    st, oc = r.status(), o64.counters()
+    print(f"\n{label}, one step vs FP64: " + ", ".join(f"{k} {v:.2e}" for k, v in errs.items()) +
+          f"; clipped {st['clipped']} (oracle {int(oc['clipped'])})")
+    r.retire()
+    bad = {k: v for k, v in errs.items() if not v <= bound}
+    assert not bad, (label, bad)
+    return st, oc, got, ref
+
+
+def test_large_grid_one_step_per_field_against_fp64_oracle(ctx):
+    """The large 80x64x50 grid (its layer spectrum in shared memory: the whole-layer 80-point warp transforms), a storm
+    the faithful oracle grew for 300 steps from a 3 K bubble, one step on the device against the FP64 oracle: every
+    field within 1e-5 relative L2."""
+    state = developed_state(baseline_run(create_grid(LARGE_GRID), seed=5, bubble=3.0), 300)
+    _one_step_parity(ctx, state, "large 80x64x50 after 300 steps")
+
+
+def test_stress_grid_one_step_per_field_against_fp64_oracle(ctx):
+    """The 320x256x80 stress grid (the row-transform path of the spectral solves at its real size), 25 faithful-oracle
+    steps from a 3 K bubble, one step on the device against the FP64 oracle: every field within 1e-5 relative L2."""
+    state = developed_state(baseline_run(create_grid(STRESS_GRID), seed=6, bubble=3.0), 25)
+    _one_step_parity(ctx, state, "stress 320x256x80 after 25 steps")
+
+
+def test_wind_limits_clip_like_the_oracle(ctx):
+    """clipWind (src/core/model.ts:1586-1595): jets beyond the limits planted in a developed storm (u = 200 m/s on two
+    whole x rows, v = -170 m/s on a whole y column, both uniform along their own axis so the projection keeps them; w =
+    150 m/s in a 4x4 column over the layers between 8 and 13.5 km), one step: every field within 1e-5 of the FP64 oracle, the
+    clamped nodes at exactly +-120 / +-100, and the same clipped count as the oracle's."""
+    state = developed_state(baseline_run(create_grid(DEFAULT_GRID), seed=42), 300)
+    g = state.grid
+    f = {k: v.copy() for k, v in state.fields.items()}
+    zu = int(np.searchsorted(g.zs, 2000.0))
+    for y in (5, 6):
+        f["u"][zu * g.layer + y * g.nx: zu * g.layer + (y + 1) * g.nx] = 200.0
+    zv = int(np.searchsorted(g.zs, 3000.0))
+    f["v"][zv * g.layer + 30 + g.nx * np.arange(g.ny)] = -170.0
+    levels = [z for z in range(g.nz) if 8000.0 <= g.zs[z] <= 13500.0]  # layers of 500-730 m: Courant below 1
+    for z in levels:
+        for y in range(12, 16):
+            f["w"][z * g.layer + y * g.nx + 20: z * g.layer + y * g.nx + 24] = 150.0
+    from meteolab_gb300.scenarios import RunSpec
+    jets = RunSpec(g, state.env, state.switches, f, state.seed, "jets")
+    st, oc, got, ref = _one_step_parity(ctx, jets, "planted jets")
+    assert st["clipped"] > 0 and st["clipped"] == int(oc["clipped"])
+    for k, lim in (("u", 120.0), ("v", 120.0), ("w", 100.0)):
+        assert float(np.max(np.abs(got[k]))) == lim
+        assert np.array_equal(np.abs(got[k]) == lim, np.abs(ref[k]) == lim), k
+
+
+def test_moving_frame_one_step_against_fp64_oracle(ctx):
+    """A domain moving over the ground (frame_u = 10, frame_v = -4 m/s): the wind relaxation and the sponge act on
+    uEnv = env.u - frame and the surface drag on the ground-relative wind (src/core/model.ts:1179-1194, :1478, :1495).
+    A storm grown 300 steps in that frame by the faithful oracle, one step on the device against the FP64 oracle."""
+    from meteolab_gb300.scenarios import Switches
+    sw = Switches(frame_u=10.0, frame_v=-4.0)
+    state = developed_state(baseline_run(create_grid(DEFAULT_GRID), seed=43, switches=sw), 300)
+    _one_step_parity(ctx, state, "moving frame (10, -4) m/s")

@@ -3,8 +3,8 @@
 Tolerances: the device computes the fields and all stencil arithmetic in FP32 (FP64 only in the tridiagonal
 solves and the budget sums); the oracle is the reference's algorithm in FP64 arithmetic. Per field after one step
 the relative L2 error is held to 1e-5 (with the absolute floors of tests/parity.py for fields that are near zero);
-stage by stage within a step (FP64 oracle) to 1e-5; over 100 steps of a growing storm to 2e-3 (FP32 rounding amplified by the
-convective instability the storm grows from).
+stage by stage within a step (FP64 oracle) to 1e-5; over 100 steps of a growing storm to 1e-4 (measured 2.1e-5: FP32
+rounding amplified by the convective instability the storm grows from).
 """
 import numpy as np
 import pytest
@@ -102,7 +102,7 @@ def test_hundred_steps_from_rest(ctx):
     _report("100 steps vs FP64", errs)
     st = r.status()
     assert st["steps"] == 100 and st["clipped"] == 0 and not st["failed"]
-    assert max(errs.values()) <= 2e-3, errs
+    assert max(errs.values()) <= 1e-4, errs
     r.retire()
 
 

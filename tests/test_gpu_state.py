@@ -116,3 +116,27 @@ def test_refuses_a_file_of_another_grid_and_a_damaged_one(ctx, saved):
     with pytest.raises(StormGpuError, match="this is not a MeteoLab state file"):
         r.load_state(b"hello world, not a state")
     other.retire()
+
+
+def test_the_saved_water_start_is_the_initial_reservoirs(ctx, saved):
+    """water.start in the saved header is waterReservoirs of the run's initial fields (src/core/model.ts:450,
+    src/core/water.ts:27-46: vapour above the profile, condensate and precipitation aloft, each by the level's air
+    mass), FP64; a run loaded from the file saves the same start again."""
+    spec, r, img = saved
+    header, _, _ = SF.read_state(img)
+    g, env, f = spec.grid, spec.env, spec.fields
+    want = 0.0
+    for z in range(g.nz):
+        sl = slice(z * g.layer, (z + 1) * g.layer)
+        mass = env.rho[z] * g.dx * g.dy * g.hz[z]
+        v = np.sum(f["q"][sl].astype(np.float64) - env.q[z])
+        c = np.sum(f["cloud"][sl].astype(np.float64) + f["ice"][sl])
+        a = np.sum(f["rain"][sl].astype(np.float64) + f["snow"][sl] + f["graupel"][sl] + f["hail"][sl])
+        want += (v + c + a) * mass
+    start = header["water"]["start"]
+    assert abs(start - want) <= 1e-9 * max(1.0, abs(want)), (start, want)
+    other = ctx.create(spec)
+    other.load_state(img)
+    again, _, _ = SF.read_state(other.save_state(CONFIG, persisted=12.0))
+    assert again["water"]["start"] == start
+    other.retire()

@@ -37,6 +37,17 @@ def test_static_scratch_divergence_matches_the_run_entry_point():
     third = divergence_max_static(0, *args)
     assert third == ref2 and ref2 != ref
 
+    # a NaN in the velocities: a non-finite maximum and SG_ERR_NONFINITE, not a finite number that passes a check
+    dev["w"][777] = float("nan")
+    torch.cuda.synchronize()
+    with pytest.raises(StormGpuError, match="non-finite") as e:
+        divergence_max_static(0, *args)
+    assert e.value.code == 5
+    assert torch.cuda.current_device() == 0
+    dev["w"].copy_(torch.from_numpy(w2))
+    torch.cuda.synchronize()
+    assert divergence_max_static(0, *args) == ref2  # the scratch holds no NaN into the next call
+
     # beyond the static level table: rejected with a message
     tall = create_grid(GridOptions(8, 8, 200, 9600.0, 9000.0, 18900.0, 50.0))
     with pytest.raises(StormGpuError, match="static level table"):
