@@ -90,7 +90,8 @@ typedef struct sg_run_counters {
   int64_t clipped;
   double negative_filled;
   double water_condensed, water_evaporated, water_rain_evaporated, water_surface;
-  int32_t failed;          /* 1: the state went non-finite (the run is skipped by later steps) */
+  int32_t failed;          /* 1: the state went non-finite; 2: a bounded device wait ran out (SG_ERR_TIMEOUT); either
+                            * way the run is skipped by later steps */
   int32_t reserved;
 } sg_run_counters;
 

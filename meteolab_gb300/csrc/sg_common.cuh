@@ -111,7 +111,8 @@ enum RotSlot { R_UH = 0, R_X, R_Y, R_ANTI, R_PERSISTED, R_UH01, R_UH03, R_LOW, R
 // scr layout
 enum Scratch { S_COURANT = 0, S_FILL = 4, S_COUNT = 16 };
 // cnt layout
-enum Counter { C_CLIPPED = 0, C_STEPS = 1, C_FAILED = 2, C_COUNT = 4 };
+// C_TIMEOUT: a kernel's bounded wait for its own asynchronous copies ran out (the run is then failed too)
+enum Counter { C_CLIPPED = 0, C_STEPS = 1, C_FAILED = 2, C_TIMEOUT = 3, C_COUNT = 4 };
 // acc layout
 enum Acc { A_NEG = 0, A_WATER = 1, A_COUNT = 8 };
 // partial-sum layout (per run): fill partials [chunk][7][3], then water partials [chunk][4].

@@ -44,8 +44,15 @@ enum TKind { TK_WENO = 0, TK_DYN = 1 };
 // Transport of one field kind (0: the WENO fields, 1: the dynamics u, v, w, theta'); for WENO `group` is the fields
 // per item (1 or 3)
 // and `minb` the blocks per SM its register budget is cut for (2 or 3).
-void launch_transport(const Launch& L, int kind, int group, int minb, int in_set, int out_set, float frac, int stage, int TX, int TY);
+// bulk: the bulk-copy kernels (a producer warp moves each level's inputs with TMA bulk copies; only with minb 2 and
+// when transport_bulk_ok holds for the plan), else the kernels whose threads copy their own plane cells.
+void launch_transport(const Launch& L, int kind, int group, int minb, int in_set, int out_set, float frac, int stage, int TX, int TY,
+                      bool bulk);
 size_t transport_smem(int kind, int G, int TX, int TY);
+size_t transport_smem_bulk(int kind, int G, int TX, int TY);
+// Whether a tile shape can take the bulk-copy kernels on a plan whose narrowest grid is min_nx wide (all_nx4: every
+// grid width a multiple of 4).
+bool transport_bulk_ok(int TX, int TY, int min_nx, bool all_nx4);
 void launch_fill_partial(const Launch& L, int set);
 void launch_fill_final(const Launch& L);
 void launch_physics(const Launch& L, int in, int mid);

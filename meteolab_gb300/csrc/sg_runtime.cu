@@ -68,6 +68,9 @@ struct Plan {
   int off[16] = {0}, cnt[16] = {0};
   int maxnx = 0, maxny = 0, maxnz = 0, TX = 40, TY = 8, wenoG = 3;  // transport tile and WENO fields per item
   int minb = 2;                                                       // WENO transport blocks per SM (register budget)
+  int minnx = 1 << 30;                                                // the narrowest grid of the plan
+  bool nx4 = true;                                                    // every grid width a multiple of 4
+  bool bulk = false;                                                  // transport inputs by TMA bulk copies (producer warp)
   int yc = 32;                                                        // layer rows per x-transform item
   int mixTX = 32, mixTY = 8;                                          // mixing tile
   int refTX = 16, refTY = 8;                                          // refinement tile
@@ -107,6 +110,7 @@ struct sg_context {
   cudaStream_t side[2] = {nullptr, nullptr};
   cudaEvent_t dep[8] = {};
   bool autotune = true;
+  bool bulk = true;                     // the bulk-copy transport kernels where a plan allows them (SG_TRANSPORT_BULK=0: never)
   bool rowsOnly = false;                // row-transform spectral path for every grid (SG_SPECTRAL_ROWS=1)
   int pinned[4] = {0, 0, 0, 2};         // transport tile, WENO group, blocks per SM fixed by the caller (TX = 0: tune)
   std::map<std::vector<int>, std::array<int, 4>> tuning;  // batch signature -> (TX, TY, wenoG, minb)
@@ -340,6 +344,7 @@ int build_plan(sg_context* ctx, const std::vector<int>& slots, Plan& P) {
   for (int s : slots) {
     const Run& r = ctx->runs[s];
     P.maxnx = std::max(P.maxnx, r.nx); P.maxny = std::max(P.maxny, r.ny); P.maxnz = std::max(P.maxnz, r.nz);
+    P.minnx = std::min(P.minnx, r.nx); P.nx4 = P.nx4 && r.nx % 4 == 0;
     if (r.nx % 40) all40 = false;
   }
   // Default transport tile: 40 x 8 columns when every grid is a multiple of 40 wide, else 32 x 8 (a tile may be
@@ -386,6 +391,8 @@ int build_plan(sg_context* ctx, const std::vector<int>& slots, Plan& P) {
       for (int z0 = 0; z0 < r.nz; z0 += zc) all[FAM_REFINE].push_back(make_int4(s, t, z0, std::min(r.nz, z0 + zc)));
   }
   if (ctx->pinned[0]) { P.TX = ctx->pinned[0]; P.TY = ctx->pinned[1]; P.wenoG = ctx->pinned[2]; P.minb = ctx->pinned[3]; }
+  P.bulk = P.minb == 2 && ctx->bulk && transport_bulk_ok(P.TX, P.TY, P.minnx, P.nx4) &&
+           std::max(transport_smem_bulk(TK_WENO, P.wenoG, P.TX, P.TY), transport_smem_bulk(TK_DYN, 4, P.TX, P.TY)) <= (size_t)ctx->maxSmem;
   transport_items(ctx, slots, P.TX, P.TY, P.wenoG, all + FAM_T_WENO);
   int st = upload_items(ctx, P, all);
   if (st != SG_OK) return st;
@@ -404,7 +411,7 @@ void launch_transport_kinds(sg_context* ctx, const Plan& P, int in, int out, flo
   for (int k = 0; k < 2; k++) {
     Launch L = lx(ctx, P, fams[k]);
     L.cap = L.n;
-    if (L.n) launch_transport(L, k, P.wenoG, P.minb, in, out, frac, stage, P.TX, P.TY);
+    if (L.n) launch_transport(L, k, P.wenoG, P.minb, in, out, frac, stage, P.TX, P.TY, P.bulk);
     hook(hookBase + k);
   }
 }
@@ -436,17 +443,21 @@ int autotune_transport(sg_context* ctx, Plan& P) {
     CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
     float bestMs = 1e30f;
     Plan T;  // candidate items only
-    T.slots = P.slots; T.maxnx = P.maxnx; T.maxny = P.maxny; T.maxnz = P.maxnz;
+    T.slots = P.slots; T.maxnx = P.maxnx; T.maxny = P.maxny; T.maxnz = P.maxnz; T.minnx = P.minnx; T.nx4 = P.nx4;
     for (auto& sh : shapes) {
       const int TX = sh[0], TY = sh[1];
       if (TX > 2 * P.maxnx || TY > 2 * P.maxny) continue;
       for (int G : {3, 1}) for (int MB : {2, 3}) {
-        if (transport_smem(TK_WENO, G, TX, TY) > (size_t)ctx->maxSmem) continue;
+        // with 2 blocks an SM the bulk-copy kernels where the shape allows them, else the per-thread copies
+        const bool bulk = MB == 2 && ctx->bulk && transport_bulk_ok(TX, TY, P.minnx, P.nx4);
+        const size_t need = bulk ? std::max(transport_smem_bulk(TK_WENO, G, TX, TY), transport_smem_bulk(TK_DYN, 4, TX, TY))
+                                 : transport_smem(TK_WENO, G, TX, TY);
+        if (need > (size_t)ctx->maxSmem) continue;
         std::vector<int4> all[FAM_COUNT];
         transport_items(ctx, P.slots, TX, TY, G, all + FAM_T_WENO);
         int st = upload_items(ctx, T, all);
         if (st != SG_OK) { cudaEventDestroy(e0); cudaEventDestroy(e1); return st; }
-        T.TX = TX; T.TY = TY; T.wenoG = G; T.minb = MB;
+        T.TX = TX; T.TY = TY; T.wenoG = G; T.minb = MB; T.bulk = bulk;
         float ms = 1e30f;
         for (int rep = 0; rep < 4; rep++) {
           cudaEventRecord(e0, ctx->stream);
@@ -464,6 +475,7 @@ int autotune_transport(sg_context* ctx, Plan& P) {
     ctx->tuning[sig] = best;
   }
   P.TX = best[0]; P.TY = best[1]; P.wenoG = best[2]; P.minb = best[3]; P.tuned = true;
+  P.bulk = P.minb == 2 && ctx->bulk && transport_bulk_ok(P.TX, P.TY, P.minnx, P.nx4);
   std::vector<int4> all[FAM_COUNT];
   for (int f = 0; f < FAM_COUNT; f++) {  // keep the other families, rebuild the transport ones
     if (f == FAM_T_WENO || f == FAM_T_DYN) continue;
@@ -584,10 +596,10 @@ void enqueue_dynamics_graph(sg_context* ctx, const Plan& P) {
   // ev[2 + s]: WENO stage s done; ev[5]: dynamics stage 1 done
   for (int s = 0; s < 3; s++) {
     if (s == 2) cudaStreamWaitEvent(side, ev[5], 0);     // dynamics stage 1 has read set B's scalars
-    if (W.n) launch_transport(W, TK_WENO, P.wenoG, P.minb, in[s], out[s], (float)RK3[s], s, P.TX, P.TY);
+    if (W.n) launch_transport(W, TK_WENO, P.wenoG, P.minb, in[s], out[s], (float)RK3[s], s, P.TX, P.TY, P.bulk);
     cudaEventRecord(ev[2 + s], side);
     if (s > 0) cudaStreamWaitEvent(main, ev[1 + s], 0);  // the stage's input scalars
-    if (D.n) launch_transport(D, TK_DYN, P.wenoG, P.minb, in[s], out[s], (float)RK3[s], s, P.TX, P.TY);
+    if (D.n) launch_transport(D, TK_DYN, P.wenoG, P.minb, in[s], out[s], (float)RK3[s], s, P.TX, P.TY, P.bulk);
     if (s == 1) cudaEventRecord(ev[5], main);
     if (s < 2) enqueue_project(ctx, P, out[s], 0, main, none);
   }
@@ -729,6 +741,7 @@ int sg_context_create(int device, uint64_t hbm_budget_bytes, sg_context** out) {
   if (static_prepare(device) != 0) { cudaGetLastError(); delete ctx; return SG_ERR_DEVICE; }
   if (const char* a = getenv("SG_AUTOTUNE")) ctx->autotune = atoi(a) != 0;
   if (const char* a = getenv("SG_SPECTRAL_ROWS")) ctx->rowsOnly = atoi(a) != 0;
+  if (const char* a = getenv("SG_TRANSPORT_BULK")) ctx->bulk = atoi(a) != 0;
   *out = ctx;
   return SG_OK;
 }
@@ -1263,9 +1276,11 @@ int sg_run_status(sg_context* ctx, sg_run run, sg_run_counters* out) {
   CK(cudaMemcpyAsync(acc, r->desc.acc, sizeof(acc), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(cnt, r->desc.cnt, sizeof(cnt), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
-  out->steps = (int64_t)cnt[C_STEPS]; out->clipped = (int64_t)cnt[C_CLIPPED]; out->failed = cnt[C_FAILED] ? 1 : 0; out->reserved = 0;
+  out->steps = (int64_t)cnt[C_STEPS]; out->clipped = (int64_t)cnt[C_CLIPPED]; out->reserved = 0;
+  out->failed = cnt[C_TIMEOUT] ? 2 : cnt[C_FAILED] ? 1 : 0;
   out->negative_filled = acc[A_NEG]; out->water_condensed = acc[A_WATER]; out->water_evaporated = acc[A_WATER + 1];
   out->water_rain_evaporated = acc[A_WATER + 2]; out->water_surface = 0;
+  if (out->failed == 2) return fail(ctx, SG_ERR_TIMEOUT, "a bounded device wait for the transport's copies ran out; the run is failed");
   return out->failed ? SG_ERR_NONFINITE : SG_OK;
 }
 

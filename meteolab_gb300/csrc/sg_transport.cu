@@ -6,6 +6,7 @@
 #include "sg_common.cuh"
 #include "sg_kernels.h"
 #include "sg_device.cuh"
+#include "sg_tile_copies.cuh"
 
 namespace sg {
 
@@ -298,9 +299,281 @@ __global__ void __launch_bounds__(320, MINB) k_transport(const RunDesc* __restri
   }
 }
 
+// ==================================================================== RK3 transport, bulk-copy tiles
+// The same arithmetic as transport_item (the same bits for every face), with the tile's inputs moved by the TMA
+// engine: the block is TX x TY consumer threads (one per column) and one producer warp. Per level the producer warp
+// issues cp.async.bulk row copies of the next input packet into shared memory - the G field planes of level z + 4
+// (rows of the periodic window [x0 - 4, x0 + TX + 4) x [y0 - 3, y0 + TY + 3), one copy per piece of a row between
+// wraps, so the halo needs no wrapped index arithmetic), the tile's face fluxes of level z + 1 (one row copy per tile
+// row), the face fluxes of the west and south edges and, for the WENO fields, their step-start values - completing on
+// one of two mbarriers (the packet of level L on barrier L & 1); it then reconstructs the tile's west and south edge
+// faces. The consumer threads wait on the packet's mbarrier, reconstruct the east, north and top faces of their own
+// cells, and after the level's block barrier form the tendency and the RK3 update. The edge faces, which made two
+// warps of every block do 40% more reconstructions than the rest, are all on the producer warp.
+// Needs nx and TX multiples of 4 (16-byte rows and pieces) and TX <= nx (at most three pieces a row).
+constexpr int TPROD = 32;  // producer threads per block
+
+template <int KIND, int G>
+__host__ __device__ constexpr int aux_floats(int TX, int TY) {
+  // per buffer: faces [TY][TX] float4, edges [TY + TX] float4, step-start values [G][TY][TX] (WENO)
+  return 4 * (TY * TX + TY + TX) + (KIND == TK_WENO ? G * TY * TX : 0);
+}
+
+template <int KIND, int G, int CTX, int CTY>
+__device__ __forceinline__ void transport_item_bulk(const RunDesc& Rg, int group, int tile, int in_set, int out_set, float frac, int stage,
+                                                    int TXr, int TYr, float* sm, unsigned long long* bars, unsigned& phase,
+                                                    bool& timed_out) {
+  const int TX = CTX ? CTX : TXr, TY = CTY ? CTY : TYr;
+  const int nx = Rg.nx, ny = Rg.ny, nz = Rg.nz, layer = Rg.layer;
+  const size_t n = Rg.n;
+  const float inv_dx = Rg.inv_dx, inv_dy = Rg.inv_dy, fdt = frac * Rg.dt;
+  const int flags = Rg.flags;
+  const float4* __restrict__ F4 = reinterpret_cast<const float4*>(Rg.faces);
+  const float* __restrict__ inb = Rg.fld + (size_t)in_set * NF * n;
+  float* const fld = Rg.fld;
+  int fo[G];
+#pragma unroll
+  for (int g = 0; g < G; g++) fo[g] = TGROUP[group][g] * (int)n;
+  const int qo = in_set * NF * (int)n, oo = out_set * NF * (int)n;
+  constexpr bool AUX_S0 = KIND == TK_WENO;
+  const int PW = TX + 8, PH = TY + 6, NCELL = PW * PH;
+  const int NT = CTX ? CTX * CTY : TXr * TYr;
+  const int AUXF = aux_floats<KIND, G>(TX, TY);
+  float* lv = sm;                                     // [tlv_rows][MAXNZ]
+  float* ring = lv + tlv_rows(KIND) * MAXNZ;          // [G][7][PH][PW], cell (x0 - 4 + c, y0 - 3 + r) at r PW + c
+  float* aux = ring + G * 7 * NCELL;                  // [2][AUXF]
+  float* fxs = aux + 2 * AUXF;                        // [2][G][TY][TX + 1]: x faces, west edge at column 0
+  float* fys = fxs + 2 * G * TY * (TX + 1);           // [2][G][TY + 1][TX]: y faces, south edge at row 0
+  const int FXS = TY * (TX + 1), FYS = (TY + 1) * TX;
+  const int t = threadIdx.x;
+  const bool producer = t >= NT;
+  const int lane = t - NT;
+  const int tilesX = (nx + TX - 1) / TX, x0 = (tile % tilesX) * TX, y0 = (tile / tilesX) * TY;
+  const int rows_on = min(TY, ny - y0), ncols = min(TX, nx - x0);  // tile rows and columns inside the grid
+  const int lx = producer ? 0 : t % TX, ly = producer ? 0 : t / TX;
+  const int x = x0 + lx, y = y0 + ly;
+  const bool on = !producer && x < nx && y < ny;
+  const int col = on ? x + y * nx : 0;
+  const TileCopies TC{nx, ny, layer, TX, TY, x0, y0, G, AUX_S0 && stage > 0};
+  // The packet of level L (issued by the producer warp): the planes L + 3 (all seven ring slots, virtual levels -3..3
+  // clamped, for L = 0) and the level's faces, edges and step-start values; its bytes announced on barrier L & 1 first.
+  auto issue = [&](int L) {
+    unsigned long long* bar = bars + (L & 1);
+    const int v0 = L == 0 ? -3 : L + 3, v1 = L + 3;
+    if (lane == 0) mbar_arrive_expect_tx(bar, TC.bytes(v1 - v0 + 1));
+    __syncwarp();
+    int covered;
+    const int nseg = TC.pieces(covered), nrs = PH * nseg;
+    for (int v = v0; v <= v1; v++) {
+      const int lev = clampi(v, 0, nz - 1), slot = (v + 7) % 7;
+      for (int j = lane; j < nrs; j += TPROD) {
+        int soff, goff, len;
+        TC.ring(j, nseg, soff, goff, len);
+#pragma unroll
+        for (int g = 0; g < G; g++)
+          bulk_g2s(ring + (g * 7 + slot) * NCELL + soff, fld + qo + fo[g] + lev * layer + goff, (unsigned)(4 * len), bar);
+      }
+    }
+    float* A = aux + (L & 1) * AUXF;
+    const int l = L * layer, na = TC.naux();
+    for (int j = lane; j < na; j += TPROD) {
+      int soff, src, which, bytes;
+      TC.aux(j, soff, src, which, bytes);
+      const void* from = which == 0 ? static_cast<const void*>(F4 + l + src)
+                                    : static_cast<const void*>(fld + TGROUP[group][which - 1] * (int)n + l + src);
+      bulk_g2s(A + soff, from, (unsigned)bytes, bar);
+    }
+  };
+  // the packet of level L has landed (all threads); a wait that runs out is recorded and ends the item
+  auto await = [&](int L) {
+    const int b = L & 1;
+    if (!mbar_wait(bars + b, (phase >> b) & 1u)) timed_out = true;
+    phase ^= 1u << b;
+  };
+  __syncthreads();  // the level table; the previous item's reads of the ring and the packets are done
+  if (producer) { fence_proxy_async(); issue(0); }
+  // edge faces: producer lanes e = lane, lane + 32 (e < TY: the west face of tile row e; TY <= e < TY + TX: the south
+  // face of tile column e - TY)
+  constexpr int EROUNDS = 2;
+  const bool loadBuoy = KIND == TK_DYN && (flags & RF_STAGES);
+  const bool loading = flags & RF_LOADING;
+  float s0[G];
+#pragma unroll
+  for (int g = 0; g < G; g++) s0[g] = !AUX_S0 && on && stage > 0 ? fld[fo[g] + col] : 0.f;
+  float bQ = 0.f, bL = 0.f;
+  if (loadBuoy && on) {
+    bQ = inb[Q * n + col];
+    bL = inb[CLOUD * n + col] + inb[ICE * n + col] +
+         (loading ? (inb[RAIN * n + col] + inb[SNOW * n + col]) + (inb[GRAUPEL * n + col] + inb[HAIL * n + col]) : 0.f);
+  }
+  float fzD[G];
+#pragma unroll
+  for (int g = 0; g < G; g++) fzD[g] = 0.f;
+  float mzD = 0.f;
+  const int cidx = (ly + 3) * PW + (lx + 4);
+  for (int z = 0; z < nz; z++) {
+    const int buf = z & 1, l = z * layer;
+    const bool more = z + 1 < nz;
+    const int ln = l + layer;
+    if (producer && more) { fence_proxy_async(); issue(z + 1); }
+    // the next level's start values (dynamics) and buoyancy inputs into registers, a level ahead
+    float s0n[G], bn[7];
+#pragma unroll
+    for (int g = 0; g < G; g++) s0n[g] = 0.f;
+#pragma unroll
+    for (int j = 0; j < 7; j++) bn[j] = 0.f;
+    if (more && on) {
+      if (!AUX_S0 && stage > 0) {
+#pragma unroll
+        for (int g = 0; g < G; g++) s0n[g] = fld[fo[g] + col + ln];
+      }
+      if (loadBuoy) { bn[0] = inb[Q * n + col + ln]; bn[1] = inb[CLOUD * n + col + ln]; bn[2] = inb[ICE * n + col + ln];
+        if (loading) { bn[3] = inb[RAIN * n + col + ln]; bn[4] = inb[SNOW * n + col + ln]; bn[5] = inb[GRAUPEL * n + col + ln]; bn[6] = inb[HAIL * n + col + ln]; } }
+    }
+    await(z);
+    const float* A = aux + buf * AUXF;
+    const int s_m2 = (z + 5) % 7, s_m1 = (z + 6) % 7, s_0 = z % 7, s_p1 = (z + 1) % 7, s_p2 = (z + 2) % 7, s_p3 = (z + 3) % 7;
+    const bool top = z == nz - 1;
+    float4 fc = make_float4(0.f, 0.f, 0.f, 0.f);
+    float fzU[G], qc[G];
+    if (on) {
+      fc = reinterpret_cast<const float4*>(A)[ly * TX + lx];
+      if (AUX_S0 && stage > 0) {
+#pragma unroll
+        for (int g = 0; g < G; g++) s0[g] = A[4 * (TY * TX + TY + TX) + (g * TY + ly) * TX + lx];
+      }
+      const float m1 = fc.x, m2 = fc.y, m3 = fc.z;
+      const bool px = m1 >= 0.f, py = m2 >= 0.f, pz = m3 >= 0.f;
+#pragma unroll
+      for (int g = 0; g < G; g++) {
+        // east and north faces of this cell as one pair
+        const float* P = ring + (g * 7 + s_0) * NCELL + cidx;
+        qc[g] = P[0];
+        float2 Av, Bv, Cv, Dv, Ev;
+        face_stencil(P + 1, 1, px, Av.x, Bv.x, Cv.x, Dv.x, Ev.x);
+        face_stencil(P + PW, PW, py, Av.y, Bv.y, Cv.y, Dv.y, Ev.y);
+        const float2 r = recon2<KIND>(Av, Bv, Cv, Dv, Ev);
+        fxs[(buf * G + g) * FXS + ly * (TX + 1) + lx + 1] = m1 * r.x;
+        fys[(buf * G + g) * FYS + (ly + 1) * TX + lx] = m2 * r.y;
+      }
+      // top faces, fields in pairs
+#pragma unroll
+      for (int g = 0; g < G; g += 2) {
+        const int g2 = g + 1 < G ? g + 1 : g;
+        const float* R = ring + g * 7 * NCELL + cidx;
+        const float* S = ring + g2 * 7 * NCELL + cidx;
+        const float2 a2 = make_float2(R[s_m2 * NCELL], S[s_m2 * NCELL]), a1 = make_float2(R[s_m1 * NCELL], S[s_m1 * NCELL]);
+        const float2 c0v = make_float2(qc[g], qc[g2]), b1 = make_float2(R[s_p1 * NCELL], S[s_p1 * NCELL]);
+        const float2 b2 = make_float2(R[s_p2 * NCELL], S[s_p2 * NCELL]), b3 = make_float2(R[s_p3 * NCELL], S[s_p3 * NCELL]);
+        const float2 Av = pz ? a2 : b3, Bv = pz ? a1 : b2, Cv = pz ? c0v : b1, Dv = pz ? b1 : c0v, Ev = pz ? b2 : a1;
+        if (g + 1 < G) {
+          const float2 r = recon2<KIND>(Av, Bv, Cv, Dv, Ev);
+          fzU[g] = top ? 0.f : m3 * r.x;
+          fzU[g + 1] = top ? 0.f : m3 * r.y;
+        } else {
+          fzU[g] = top ? 0.f : m3 * recon1<KIND>(Av.x, Bv.x, Cv.x, Dv.x, Ev.x);
+        }
+      }
+    }
+    if (producer) {
+#pragma unroll
+      for (int rd = 0; rd < EROUNDS; rd++) {
+        const int e = lane + rd * TPROD;
+        const bool edgeW = e < TY && e < rows_on, edgeS = e >= TY && e < TY + ncols;
+        if (!(edgeW || edgeS)) continue;
+        const float4 ef = reinterpret_cast<const float4*>(A)[TY * TX + e];  // west faces, then the south ones
+        const float me = edgeW ? ef.x : ef.y;
+        const bool pe = me >= 0.f;
+        const int ecell = edgeW ? (e + 3) * PW + 4 : 3 * PW + (e - TY) + 4;  // the cell on the edge's high side
+        const int estride = edgeW ? 1 : PW, es = edgeW ? FXS : FYS;
+        float* const edst = edgeW ? fxs + e * (TX + 1) : fys + (e - TY);
+#pragma unroll
+        for (int g = 0; g < G; g += 2) {  // fields in pairs, as the top faces
+          float2 Av, Bv, Cv, Dv, Ev;
+          face_stencil(ring + (g * 7 + s_0) * NCELL + ecell, estride, pe, Av.x, Bv.x, Cv.x, Dv.x, Ev.x);
+          if (g + 1 < G) {
+            face_stencil(ring + ((g + 1) * 7 + s_0) * NCELL + ecell, estride, pe, Av.y, Bv.y, Cv.y, Dv.y, Ev.y);
+            const float2 r = recon2<KIND>(Av, Bv, Cv, Dv, Ev);
+            edst[(buf * G + g) * es] = me * r.x;
+            edst[(buf * G + g + 1) * es] = me * r.y;
+          } else {
+            edst[(buf * G + g) * es] = me * recon1<KIND>(Av.x, Bv.x, Cv.x, Dv.x, Ev.x);
+          }
+        }
+      }
+    }
+    const float bnQ = bn[0], bnL = bn[1] + bn[2] + (loading ? (bn[3] + bn[4]) + (bn[5] + bn[6]) : 0.f);
+    if (__syncthreads_or(timed_out)) {
+      // a packet never landed: record it on the run, give the copies in flight a last bounded wait (this level's
+      // packet, whose phase bit await has already flipped, and the next one's), and end the item and the kernel
+      timed_out = true;
+      if (t == 0) { atomicAdd(Rg.cnt + C_TIMEOUT, 1ull); atomicExch(Rg.cnt + C_FAILED, 1ull); }
+      mbar_wait(bars + (z & 1), ((phase >> (z & 1)) & 1u) ^ 1u);
+      if (more) mbar_wait(bars + ((z + 1) & 1), (phase >> ((z + 1) & 1)) & 1u);
+      return;
+    }
+    if (on) {
+      const float ihz = lv[z], irho = lv[MAXNZ + z];
+#pragma unroll
+      for (int g = 0; g < G; g++) {
+        const float* FX = fxs + (buf * G + g) * FXS + ly * (TX + 1) + lx;
+        const float* FY = fys + (buf * G + g) * FYS + ly * TX + lx;
+        float flux = (FX[1] - FX[0]) * inv_dx + (FY[TX] - FY[0]) * inv_dy + (fzU[g] - fzD[g]) * ihz;
+        float tend = -(flux - qc[g] * fc.w) * irho;
+        if (KIND == TK_DYN && g == 3) {  // theta': the base profile's own vertical flux
+          const float m3 = fc.z;
+          float up = m3 * (m3 >= 0.f ? lv[2 * MAXNZ + z] : lv[3 * MAXNZ + z]);
+          float dn = mzD * (mzD >= 0.f ? lv[4 * MAXNZ + z] : lv[5 * MAXNZ + z]);
+          tend -= (up - dn) * ihz * irho;
+        }
+        if (KIND == TK_DYN && g == 2 && loadBuoy) {
+          const float Rb = lv[6 * MAXNZ + z], Qb = lv[7 * MAXNZ + z];
+          float dth = qc[3], num = dth + .61f * ((Rb + dth) * (bQ - Qb) + Qb * dth);
+          tend += 9.81f * (num / lv[8 * MAXNZ + z] - bL);
+        }
+        float a = (stage == 0 ? qc[g] : s0[g]) + fdt * tend;
+        if (KIND == TK_DYN && g == 2 && stage < 2 && (flags & RF_STAGES) && (z == 0 || z == nz - 1)) a = 0.f;
+        fld[oo + fo[g] + col + l] = a;
+        fzD[g] = fzU[g];
+      }
+    }
+    mzD = fc.z;
+    if (!AUX_S0) {
+#pragma unroll
+      for (int g = 0; g < G; g++) s0[g] = s0n[g];
+    }
+    bQ = bnQ; bL = bnL;
+  }
+  __syncthreads();
+}
+
+template <int KIND, int G, int MINB, int CTX, int CTY>
+__global__ void __launch_bounds__(320 + TPROD, MINB) k_transport_bulk(const RunDesc* __restrict__ runs, const int4* items, int nitems, int in_set,
+                                                                       int out_set, float frac, int stage, int TX, int TY) {
+  extern __shared__ __align__(16) float sm[];
+  __shared__ __align__(8) unsigned long long bars[2];
+  if (threadIdx.x == 0) { mbar_init(bars, 1); mbar_init(bars + 1, 1); fence_mbar_init(); fence_proxy_async(); }
+  __syncthreads();
+  unsigned phase = 0;
+  bool timed_out = false;
+  FOR_ITEMS {
+    const RunDesc& R = runs[items[it].x];
+    if (R.cnt[C_FAILED]) continue;
+    transport_item_bulk<KIND, G, CTX, CTY>(R, items[it].y, items[it].z, in_set, out_set, frac, stage, TX, TY, sm, bars, phase, timed_out);
+    if (timed_out) return;
+  }
+}
+
 // ==================================================================== launchers
 size_t transport_smem(int kind, int G, int TX, int TY) {
   return ((size_t)tlv_rows(kind) * MAXNZ + 2 * 4 * (size_t)TX * TY + (size_t)G * 7 * (TX + 6) * (TY + 6) + 2 * (size_t)G * TY * (TX + 1) + 2 * (size_t)G * (TY + 1) * TX) * sizeof(float);
+}
+size_t transport_smem_bulk(int kind, int G, int TX, int TY) {
+  const size_t auxf = kind == TK_WENO ? (G == 3 ? aux_floats<TK_WENO, 3>(TX, TY) : aux_floats<TK_WENO, 1>(TX, TY)) : aux_floats<TK_DYN, 4>(TX, TY);
+  return ((size_t)tlv_rows(kind) * MAXNZ + (size_t)G * 7 * (TX + 8) * (TY + 6) + 2 * auxf + 2 * (size_t)G * TY * (TX + 1) + 2 * (size_t)G * (TY + 1) * TX) * sizeof(float);
+}
+bool transport_bulk_ok(int TX, int TY, int min_nx, bool all_nx4) {
+  return all_nx4 && TX % 4 == 0 && TX <= min_nx && (TX * TY) % 32 == 0 && TX * TY <= 320 && TX + TY <= 2 * TPROD;
 }
 
 namespace {
@@ -309,6 +582,30 @@ template <int KIND, int G, int MINB, int CTX, int CTY>
 void tlaunch(const Launch& L, int in_set, int out_set, float frac, int stage, int TX, int TY) {
   k_transport<KIND, G, MINB, CTX, CTY><<<GRID(L.n, L.cap), TX * TY, transport_smem(KIND, G, TX, TY), L.stream>>>(
       L.runs, L.items, L.n, in_set, out_set, frac, stage, TX, TY);
+}
+template <int KIND, int G, int CTX, int CTY>
+void tlaunch_bulk(const Launch& L, int in_set, int out_set, float frac, int stage, int TX, int TY) {
+  k_transport_bulk<KIND, G, 2, CTX, CTY><<<GRID(L.n, L.cap), TX * TY + TPROD, transport_smem_bulk(KIND, G, TX, TY), L.stream>>>(
+      L.runs, L.items, L.n, in_set, out_set, frac, stage, TX, TY);
+}
+template <int KIND, int G>
+void tlaunch_tile_bulk(const Launch& L, int in_set, int out_set, float frac, int stage, int TX, int TY) {
+  if (TX == 40 && TY == 8) return tlaunch_bulk<KIND, G, 40, 8>(L, in_set, out_set, frac, stage, TX, TY);
+  if (TX == 32 && TY == 8) return tlaunch_bulk<KIND, G, 32, 8>(L, in_set, out_set, frac, stage, TX, TY);
+  if (TX == 20 && TY == 8) return tlaunch_bulk<KIND, G, 20, 8>(L, in_set, out_set, frac, stage, TX, TY);
+  if (TX == 16 && TY == 16) return tlaunch_bulk<KIND, G, 16, 16>(L, in_set, out_set, frac, stage, TX, TY);
+  if (TX == 40 && TY == 4) return tlaunch_bulk<KIND, G, 40, 4>(L, in_set, out_set, frac, stage, TX, TY);
+  tlaunch_bulk<KIND, G, 0, 0>(L, in_set, out_set, frac, stage, TX, TY);
+}
+template <int KIND, int G>
+cudaError_t tlimits_bulk(int bytes) {
+  cudaError_t e;
+  if ((e = smem_limit(k_transport_bulk<KIND, G, 2, 0, 0>, bytes)) != cudaSuccess) return e;
+  if ((e = smem_limit(k_transport_bulk<KIND, G, 2, 40, 8>, bytes)) != cudaSuccess) return e;
+  if ((e = smem_limit(k_transport_bulk<KIND, G, 2, 32, 8>, bytes)) != cudaSuccess) return e;
+  if ((e = smem_limit(k_transport_bulk<KIND, G, 2, 20, 8>, bytes)) != cudaSuccess) return e;
+  if ((e = smem_limit(k_transport_bulk<KIND, G, 2, 16, 16>, bytes)) != cudaSuccess) return e;
+  return smem_limit(k_transport_bulk<KIND, G, 2, 40, 4>, bytes);
 }
 template <int KIND, int G, int MINB>
 void tlaunch_tile(const Launch& L, int in_set, int out_set, float frac, int stage, int TX, int TY) {
@@ -336,8 +633,18 @@ cudaError_t tlimits(int bytes) {
 }
 }  // namespace
 
-void launch_transport(const Launch& L, int kind, int group, int minb, int in_set, int out_set, float frac, int stage, int TX, int TY) {
+void launch_transport(const Launch& L, int kind, int group, int minb, int in_set, int out_set, float frac, int stage, int TX, int TY,
+                      bool bulk) {
   if (L.n == 0) return;
+  if (bulk && minb == 2) {
+    if (kind == TK_WENO) {
+      if (group == 3) tlaunch_tile_bulk<TK_WENO, 3>(L, in_set, out_set, frac, stage, TX, TY);
+      else tlaunch_tile_bulk<TK_WENO, 1>(L, in_set, out_set, frac, stage, TX, TY);
+    } else {
+      tlaunch_tile_bulk<TK_DYN, 4>(L, in_set, out_set, frac, stage, TX, TY);
+    }
+    return;
+  }
   switch (kind) {
     case TK_WENO:
       if (group == 3) { if (minb == 3) tlaunch_tile<TK_WENO, 3, 3>(L, in_set, out_set, frac, stage, TX, TY); else tlaunch_tile<TK_WENO, 3, 2>(L, in_set, out_set, frac, stage, TX, TY); }
@@ -353,6 +660,9 @@ cudaError_t set_transport_smem_limits(int bytes) {
   if ((e = tlimits<TK_WENO, 3, 3>(bytes)) != cudaSuccess) return e;
   if ((e = tlimits<TK_WENO, 1, 2>(bytes)) != cudaSuccess) return e;
   if ((e = tlimits<TK_WENO, 1, 3>(bytes)) != cudaSuccess) return e;
+  if ((e = tlimits_bulk<TK_WENO, 3>(bytes)) != cudaSuccess) return e;
+  if ((e = tlimits_bulk<TK_WENO, 1>(bytes)) != cudaSuccess) return e;
+  if ((e = tlimits_bulk<TK_DYN, 4>(bytes)) != cudaSuccess) return e;
   return tlimits<TK_DYN, 4, 2>(bytes);
 }
 

@@ -8,6 +8,7 @@
 #include "../../meteolab_gb300/csrc/sg_common.cuh"
 #include "../../meteolab_gb300/csrc/sg_fft.cuh"
 #include "../../meteolab_gb300/csrc/sg_physics.cuh"
+#include "../../meteolab_gb300/csrc/sg_tile_copies.cuh"
 
 using namespace sg;
 
@@ -54,4 +55,29 @@ int ht_fft_factors(int n, int* rad) { return fft_plan_factors(n, rad); }
 int ht_fft_count(int n) { return fft_count(n); }
 int ht_fft_radix(int n, int s) { return fft_radix_at(n, s); }
 
+
+// The bulk-copy transport's packet plan of one tile (sg_tile_copies.cuh): every ring copy of one plane and every
+// auxiliary copy, as rows (kind, smem float offset, source offset, bytes): kind 0 a ring piece (source: float offset
+// in a field's level), 1 a face-flux copy (float4 offset in the level), 2 + g a step-start row of field g (float
+// offset). Returns the number of rows (at most cap); *bytes gets the announced bytes of a one-plane packet, *covered
+// the window columns the pieces fill.
+int ht_tile_copies(int nx, int ny, int TX, int TY, int x0, int y0, int G, int s0, int* out, int cap, unsigned* bytes, int* covered) {
+  TileCopies T{nx, ny, nx * ny, TX, TY, x0, y0, G, s0 != 0};
+  int cov = 0;
+  const int nseg = T.pieces(cov);
+  int k = 0;
+  for (int j = 0; j < T.PH() * nseg && k < cap; j++, k++) {
+    int soff, goff, len;
+    T.ring(j, nseg, soff, goff, len);
+    out[4 * k] = 0; out[4 * k + 1] = soff; out[4 * k + 2] = goff; out[4 * k + 3] = 4 * len;
+  }
+  for (int j = 0; j < T.naux() && k < cap; j++, k++) {
+    int soff, src, which, b;
+    T.aux(j, soff, src, which, b);
+    out[4 * k] = which == 0 ? 1 : 1 + which; out[4 * k + 1] = soff; out[4 * k + 2] = src; out[4 * k + 3] = b;
+  }
+  *bytes = T.bytes(1);
+  *covered = cov;
+  return k;
+}
 }  // extern "C"

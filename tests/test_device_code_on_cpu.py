@@ -28,7 +28,8 @@ def _cuda_include():
 
 @pytest.fixture(scope="module")
 def ht():
-    deps = [SRC] + [os.path.join(HERE, "..", "meteolab_gb300", "csrc", f) for f in ("sg_common.cuh", "sg_fft.cuh", "sg_physics.cuh")]
+    deps = [SRC] + [os.path.join(HERE, "..", "meteolab_gb300", "csrc", f) for f in ("sg_common.cuh", "sg_fft.cuh", "sg_physics.cuh",
+                                                                                    "sg_tile_copies.cuh")]
     if not os.path.exists(LIB) or any(os.path.getmtime(d) > os.path.getmtime(LIB) for d in deps):
         subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-I", _cuda_include(), "-o", LIB, SRC], check=True)
     L = C.CDLL(LIB)
@@ -45,6 +46,8 @@ def ht():
     L.ht_fft.restype = C.c_int
     L.ht_fft.argtypes = [C.c_int, C.POINTER(C.c_float)]
     L.ht_fall.argtypes = [C.c_float] * 6 + [C.POINTER(C.c_float)]
+    L.ht_tile_copies.restype = C.c_int
+    L.ht_tile_copies.argtypes = [C.c_int] * 8 + [C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_uint), C.POINTER(C.c_int)]
     return L
 
 
@@ -161,3 +164,64 @@ def test_integer_conversions(ht):
         assert got == want or (np.isnan(got) and np.isnan(want)), (x, got, want)
         assert math.copysign(1, got) == math.copysign(1, want)
     assert np.isnan(ht.ht_narrow(float("nan")))
+
+
+# ---- the bulk-copy transport's packet plan (sg_tile_copies.cuh), for every tile of the grids the device runs
+TILE_SHAPES = [(40, 8), (32, 8), (20, 8), (16, 16), (40, 4), (8, 8), (16, 8), (32, 4)]
+GRIDS = [(40, 32), (80, 64), (320, 256), (12, 10), (16, 12)]
+
+
+def _bulk_ok(TX, TY, nx):
+    return nx % 4 == 0 and TX % 4 == 0 and TX <= nx and (TX * TY) % 32 == 0 and TX * TY <= 320 and TX + TY <= 64
+
+
+@pytest.mark.parametrize("nx,ny", GRIDS)
+def test_bulk_tile_copies_cover_the_window_in_bounds(ht, nx, ny):
+    """Every copy the producer warp issues for a packet stays inside its source level and its shared-memory buffer,
+    starts and ends on 16-byte boundaries, the ring pieces fill the periodic window exactly once with the right
+    global cells, the auxiliary rows do not overlap, and the announced bytes equal the bytes copied: a wrong count
+    would leave the mbarrier waiting, a wrong address would read out of bounds."""
+    layer = nx * ny
+    cap = 4096
+    buf = (C.c_int * (4 * cap))()
+    for TX, TY in TILE_SHAPES:
+        if not _bulk_ok(TX, TY, nx):
+            continue
+        PW, PH = TX + 8, TY + 6
+        for G, s0 in ((3, 1), (3, 0), (1, 1), (4, 0)):
+            for y0 in range(0, ny, TY):
+                for x0 in range(0, nx, TX):
+                    nb, cov = C.c_uint(), C.c_int()
+                    k = ht.ht_tile_copies(nx, ny, TX, TY, x0, y0, G, s0, buf, cap, C.byref(nb), C.byref(cov))
+                    assert 0 < k < cap
+                    rows = np.frombuffer(buf, dtype=np.int32, count=4 * k).reshape(k, 4)
+                    assert cov.value == PW
+                    ring = rows[rows[:, 0] == 0]
+                    seen = np.zeros(PH * PW, np.int32)
+                    for _, soff, goff, b in ring:
+                        assert b > 0 and b % 16 == 0 and (4 * soff) % 16 == 0 and (4 * goff) % 16 == 0
+                        assert 0 <= goff and goff + b // 4 <= layer
+                        for q in range(b // 4):
+                            c = (soff + q) % PW
+                            r = (soff + q) // PW
+                            assert r < PH and (soff + q) // PW == soff // PW  # a piece stays in its row
+                            want = ((x0 - 4 + c) % nx) + ((y0 - 3 + r) % ny) * nx
+                            assert goff + q == want, (TX, TY, x0, y0, c, r)
+                        seen[soff: soff + b // 4] += 1
+                    assert np.all(seen == 1), (TX, TY, x0, y0)
+                    aux = rows[rows[:, 0] != 0]
+                    rows_on, ncols = min(TY, ny - y0), min(TX, nx - x0)
+                    aux_len = 4 * (TY * TX + TY + TX) + (G * TY * TX if s0 else 0)
+                    used = np.zeros(aux_len, np.int32)
+                    for kind, soff, src, b in aux:
+                        assert b > 0 and b % 16 == 0 and (4 * soff) % 16 == 0
+                        assert 0 <= soff and soff + b // 4 <= aux_len
+                        used[soff: soff + b // 4] += 1
+                        if kind == 1:   # float4 face fluxes of the level
+                            assert 0 <= src and src + b // 16 <= layer
+                        else:           # a step-start row of field kind - 2
+                            assert s0 and 0 <= kind - 2 < G and (4 * src) % 16 == 0 and 0 <= src and src + b // 4 <= layer
+                    assert used.max() == 1
+                    assert len(aux) == 2 * rows_on + 1 + (G * rows_on if s0 else 0)
+                    total = G * int(ring[:, 3].sum()) + int(aux[:, 3].sum())
+                    assert total == nb.value, (TX, TY, x0, y0, G, s0, total, nb.value)

@@ -213,6 +213,28 @@ def test_transport_tiles_give_the_same_bits(ctx, storm, shape):
     ref.retire(); r.retire()
 
 
+def test_bulk_copy_transport_gives_the_bits_of_per_thread_copies(storm, monkeypatch):
+    """The transport kernels whose producer warp moves each level's inputs with TMA bulk copies (the default where the
+    grid allows) and the kernels whose threads copy their own plane cells (SG_TRANSPORT_BULK=0) give bitwise equal
+    fields, on an uneven batch (standard and large grid) over three steps."""
+    from meteolab_gb300.runtime import Context
+    specs = [storm, baseline_run(create_grid(LARGE_GRID), seed=14)]
+    out = {}
+    for flag in ("1", "0"):
+        monkeypatch.setenv("SG_TRANSPORT_BULK", flag)
+        c = Context(0)
+        c.set_transport_shape(40, 8, 3)
+        runs = [c.create(s) for s in specs]
+        c.batch_step(runs, 3)
+        out[flag] = [r.read() for r in runs]
+        for r in runs:
+            r.retire()
+        c.close()
+    for a, b in zip(out["1"], out["0"]):
+        for k in CARRIED:
+            assert np.array_equal(a[k], b[k]), k
+
+
 def test_batch_field_io_matches_per_run_calls(ctx, storm):
     runs = [ctx.create(storm), ctx.create(baseline_run(create_grid(LARGE_GRID), seed=8))]
     ctx.batch_step(runs, 2)
