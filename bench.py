@@ -343,7 +343,12 @@ def uneven_leg(ctx, steps: int, spinup: int):
     # Work items are per run, so no run is padded to another's size; the transport tiles overhang no grid edge
     # when the tile width divides the grid widths.
     waste = 0.0 if all(nx % tile[0] == 0 and ny % tile[1] == 0 for nx, ny in ((40, 32), (80, 64))) else None
+    capes = [s.meta["cape"] for s in specs]
     return {"runs": "48 x 40x32x50 + 16 x 80x64x50", "cell_steps_s": v, "ms_per_step": ms / steps,
+            "regime": {"ml_cape_j_per_kg": {"min": min(capes), "max": max(capes)},
+                       "points": [[s.label, s.grid.nx, round(s.meta["cape"]), round(s.meta["shear"], 1), round(s.meta["lid_k"], 2),
+                                   round(s.meta["lid_km"], 2)] for s in specs],
+                       "point_fields": ["label", "nx", "ml_cape", "shear06", "lid_K", "lid_km"]},
             "alone": alone, "mixed_vs_sizes_alone": (alone["standard"]["ms_per_step"] + alone["large"]["ms_per_step"]) / (ms / steps),
             "padding_waste": waste, "transport_tile": list(tile)}
 

@@ -355,11 +355,13 @@ __device__ __forceinline__ void transport_item_bulk(const RunDesc& Rg, int group
   const bool on = !producer && x < nx && y < ny;
   const int col = on ? x + y * nx : 0;
   const TileCopies TC{nx, ny, layer, TX, TY, x0, y0, G, AUX_S0 && stage > 0};
-  // The packet of level L (issued by the producer warp): the planes L + 3 (all seven ring slots, virtual levels -3..3
-  // clamped, for L = 0) and the level's faces, edges and step-start values; its bytes announced on barrier L & 1 first.
+  // The packet of level L (issued by the producer warp): the plane L + 3 (for L = 0 the six planes of virtual levels
+  // -2..3, clamped, that level 0 reads; the seventh slot is the one the packet of level 1, issued before this one has
+  // landed, fills with plane 4, so no two packets in flight write the same slot) and the level's faces, edges and
+  // step-start values; its bytes announced on barrier L & 1 first.
   auto issue = [&](int L) {
     unsigned long long* bar = bars + (L & 1);
-    const int v0 = L == 0 ? -3 : L + 3, v1 = L + 3;
+    const int v0 = L == 0 ? -2 : L + 3, v1 = L + 3;
     if (lane == 0) mbar_arrive_expect_tx(bar, TC.bytes(v1 - v0 + 1));
     __syncwarp();
     int covered;

@@ -145,6 +145,13 @@ class Environment:
             self.u[z], self.v[z] = u, v
             self.rho[z] = self.p[z] / (RD * self.theta[z] * self.exner[z] * (1 + 0.61 * self.q[z]))
 
+    @classmethod
+    def winds_only(cls, config: SliderConfig) -> "Environment":
+        """An environment that answers only for its wind (the slider's nodes), without the base state's integration."""
+        e = cls.__new__(cls)
+        e.config, e.profile, e.neutral = config, None, None
+        return e
+
     # -- hydrostatic pressure (src/core/environment.ts:64-78)
     def _integrate_hydrostatic(self, top: float) -> np.ndarray:
         n = math.ceil(top / PRESSURE_STEP) + 1
@@ -304,6 +311,22 @@ class Environment:
         s = self._wind_at(z, 1)
         a = (270 - self._wind_at(z, 2)) * math.pi / 180
         return (s * math.cos(a), s * math.sin(a))
+
+    def wind_scalar(self, z: float) -> float:
+        return self._wind_at(z, 1)
+
+    def wind_direction(self, z: float) -> float:
+        """Direction the wind blows from, turning along the shorter arc between the nodes (environment.ts:201)."""
+        return self._wind_at(z, 2)
+
+    def qsat(self, t: float, z: float) -> float:
+        return qsat_p(t, self.pressure_at(z))
+
+    def dewpoint(self, q: float, z: float) -> float:
+        """Dew point, C, of mixing ratio q at height z (environment.ts:214)."""
+        e = max(1.0, q * self.pressure_at(z) / (EPS + q))
+        lg = math.log(e / 611.2)
+        return 243.5 * lg / (17.67 - lg)
 
     def base_state(self) -> dict:
         """The per-level arrays the device needs (FP64)."""

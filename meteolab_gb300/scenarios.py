@@ -88,6 +88,7 @@ class RunSpec:
     fields: Dict[str, np.ndarray]
     seed: int = 0
     label: str = ""
+    meta: Dict[str, float] = field(default_factory=dict)   # what a workload records about the run (CAPE, shear, lid)
 
     @property
     def cells(self) -> int:
@@ -167,23 +168,90 @@ def ensemble_members(grid: Grid, count: int, seed: int = 2026) -> List[RunSpec]:
     return runs
 
 
-def regime_runs(small: Grid, large: Grid, n_small: int = 48, n_large: int = 16, seed: int = 88) -> List[RunSpec]:
-    """An 8 x 8 CAPE x shear regime grid (src/regime/grid.ts) split over two domain sizes: CAPE levels from the
-    surface moisture (qv cap 10.5-17 g/kg spans roughly 500-4000 J/kg on this sounding), 0-6 km shear 0-40 m/s, a
-    seeded veering and bubble per point; a seeded shuffle puts n_small points on the small grid and n_large on the
-    large one."""
+# The regime grid's base settings: the SUMMER_DAY slider profile (src/core/fixtures.ts:6-12) with a well-mixed lowest
+# kilometre and the light veering wind of the quiet scenarios (src/core/scenarios.ts:31); its CAPE is set through the
+# pair (surface moisture, low-level lapse rate) and its shear by scaling the hodograph about the ground wind.
+REGIME_BASE = dict(moistLayer=1.0, wind0=2, wind3=5, wind6=9, wind10=14, windDir0=200, windDir3=230, windDir6=250, windDir10=260)
+CAPE_LEVELS = tuple(500.0 + 500.0 * i for i in range(8))   # J/kg, the grid's rows
+SHEAR_LEVELS = tuple(40.0 * j / 7 for j in range(8))       # m/s over 0-6 km, the grid's columns
+
+
+def moisture_lapse(s: float) -> Dict[str, float]:
+    """The CAPE knob: s in [0, 1] raises the surface relative humidity (so the boundary layer's vapour) and the
+    0-3 km lapse rate together."""
+    rh = 40.0 + 25.0 * s
+    return dict(rhSurface=rh, rhLow=rh - 5.0, lapseLow=6.0 + 2.0 * s)
+
+
+def with_shear(values: Dict[str, float], grid: Grid, shear: float) -> Dict[str, float]:
+    """The slider hodograph scaled about the ground wind so that the 0-6 km difference is `shear` m/s, its shape kept
+    (withShear, src/regime/grid.ts:67-92); a calm hodograph (difference below 2 m/s) gets a straight westerly shear
+    added instead."""
+    from .environment import SliderConfig
+    env = Environment.winds_only(SliderConfig(**values))
+    (u0, v0), (u6, v6) = env.wind_uv(0.0), env.wind_uv(6000.0)
+    now = math.hypot(u6 - u0, v6 - v0)
+    f, added = (shear / now, 0.0) if now > 2 else (1.0, shear)
+    out = dict(values)
+    for key, z in (("0", 0), ("05", 500), ("1", 1000), ("3", 3000), ("6", 6000), ("10", 10000)):
+        speed, direction = values.get(f"wind{key}"), values.get(f"windDir{key}")
+        if speed is None or direction is None:
+            continue
+        a = math.radians(270 - direction)
+        u, v = speed * math.cos(a), speed * math.sin(a)
+        u, v = u0 + (u - u0) * f + added * min(z, 6000) / 6000, v0 + (v - v0) * f
+        out[f"wind{key}"] = math.hypot(u, v)
+        if out[f"wind{key}"] > .05:
+            out[f"windDir{key}"] = (270 - math.degrees(math.atan2(v, u))) % 360
+    return out
+
+
+def _cape_knob(grid: Grid) -> List[Tuple[float, float]]:
+    """Mixed-layer CAPE of the lid-free base profile along the moisture / lapse-rate knob, 11 points."""
+    from .environment import SliderConfig
+    from .sounding import lift_parcel
+    table = []
+    for k in range(11):
+        env = Environment(SliderConfig(**dict(REGIME_BASE, **moisture_lapse(k / 10))), grid)
+        table.append((k / 10, lift_parcel(env, grid.height, "ml").cape))
+    return table
+
+
+def regime_runs(small: Grid, large: Grid, n_small: int = 48, n_large: int = 16, seed: int = 88,
+                lid: bool = True) -> List[RunSpec]:
+    """An 8 x 8 CAPE x shear regime grid (src/regime/grid.ts) split over two domain sizes.
+
+    Rows: mixed-layer CAPE levels of 500-4000 J/kg, set through the (surface moisture, low-level lapse rate) pair of
+    the slider profile (moisture_lapse; the knob's value for each level interpolated from an 11-point table of the
+    lid-free profile's CAPE). Columns: 0-6 km shear 0-40 m/s (with_shear). With `lid`, a seeded half of the points
+    carries an elevated mixed layer's lid: capStrength U[0, 4] K across the cap law's 300 m at capHeight U[1.5, 3] km
+    (src/core/environment.ts:131-138). Each point's own mixed-layer CAPE (lid included) and shear are computed (FP64,
+    sounding.py) and kept in its RunSpec's ``meta``. A seeded shuffle puts n_small points on the
+    small grid and n_large on the large one; each point has its own bubble amplitude U[1, 3] K and noise seed."""
+    from .environment import SliderConfig
+    from .sounding import lift_parcel
     rng = np.random.default_rng(seed)
+    table = _cape_knob(small)
+    ss, cs = [t[0] for t in table], [t[1] for t in table]
     points = [(i, j) for i in range(8) for j in range(8)]
     order = rng.permutation(len(points))
     runs = []
     for slot, p in enumerate(order[:n_small + n_large]):
         i, j = points[p]
-        qv = 0.0105 + (0.017 - 0.0105) * i / 7
-        shear6 = 40.0 * j / 7
+        knob = float(np.interp(CAPE_LEVELS[i], cs, ss))
         grid = small if slot < n_small else large
-        runs.append(baseline_run(grid, seed=seed * 1000 + slot, bubble=float(rng.uniform(1.0, 3.0)), qv_max=qv,
-                                 shear=shear6 / math.tanh(2.0), veer=float(rng.uniform(0.0, 90.0)),
-                                 label=f"cape{i}-shear{j}"))
+        values = with_shear(dict(REGIME_BASE, **moisture_lapse(knob)), grid, SHEAR_LEVELS[j])
+        strength = height = 0.0
+        if lid and rng.random() < 0.5:
+            strength, height = float(rng.uniform(0.0, 4.0)), float(rng.uniform(1.5, 3.0))
+            values.update(capStrength=strength, capHeight=height)
+        env = Environment(SliderConfig(**values), grid)
+        bubble = float(rng.uniform(1.0, 3.0))
+        sd = seed * 1000 + slot
+        (u0, v0), (u6, v6) = env.wind_uv(0.0), env.wind_uv(6000.0)
+        meta = dict(cape=lift_parcel(env, grid.height, "ml").cape, cape_level=CAPE_LEVELS[i], shear=math.hypot(u6 - u0, v6 - v0),
+                    lid_k=strength, lid_km=height)
+        runs.append(RunSpec(grid, env, Switches(), initial_fields(grid, env, sd, bubble), sd, f"cape{i}-shear{j}", meta))
     return runs
 
 

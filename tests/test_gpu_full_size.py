@@ -146,3 +146,17 @@ def test_moving_frame_one_step_against_fp64_oracle(ctx):
     sw = Switches(frame_u=10.0, frame_v=-4.0)
     state = developed_state(baseline_run(create_grid(DEFAULT_GRID), seed=43, switches=sw), 300)
     _one_step_parity(ctx, state, "moving frame (10, -4) m/s")
+
+
+def test_regime_point_with_a_lid_one_step_against_fp64_oracle(ctx):
+    """A point of the uneven batch's regime grid (a slider-profile sounding: the moisture / lapse-rate knob, the
+    hodograph scaled to its shear, an elevated mixed layer's lid), grown 200 steps by the faithful oracle, one step on
+    the device against the FP64 oracle."""
+    from meteolab_gb300.scenarios import regime_runs
+    specs = [s for s in regime_runs(create_grid(DEFAULT_GRID), create_grid(LARGE_GRID), n_small=8, n_large=0, seed=88)
+             if s.meta["lid_k"] > 0 and s.meta["cape"] > 1500]
+    assert specs, "no lidded point with CAPE above 1500 J/kg among the eight"
+    spec = max(specs, key=lambda s: s.meta["shear"])
+    state = developed_state(spec, 200)
+    _one_step_parity(ctx, state, f"regime point {spec.label} (ML CAPE {spec.meta['cape']:.0f} J/kg, shear {spec.meta['shear']:.0f} m/s, "
+                                 f"lid {spec.meta['lid_k']:.1f} K at {spec.meta['lid_km']:.1f} km)")
