@@ -35,12 +35,22 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned 
                : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
   return ok != 0;
 }
-// Waits for the phase of `parity` to complete, at most MBAR_POLLS polls (each try_wait may suspend the thread for a
-// while); false when it did not complete in that time.
-constexpr int MBAR_POLLS = 1 << 16;
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+  return t;
+}
+// Waits for the phase of `parity` to complete, at most MBAR_WAIT_NS of the global timer (and at most 2^24 rounds of
+// polls, should the timer not advance); false when it did not complete in that time.
+constexpr unsigned long long MBAR_WAIT_NS = 200000000ull;
 __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
-  for (int i = 0; i < MBAR_POLLS; i++)
-    if (mbar_try_wait(bar, parity)) return true;
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  for (int round = 0; round < (1 << 24); round++) {
+    for (int i = 0; i < 32; i++)
+      if (mbar_try_wait(bar, parity)) return true;
+    if (global_ns() - t0 > MBAR_WAIT_NS) return false;
+  }
   return false;
 }
 __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {

@@ -572,8 +572,9 @@ void enqueue_part(sg_context* ctx, const Plan& P, int part, Hook hook) {
 //  * sedimentation (the falling fields of set A) alongside the face projection (u, v, w of set A);
 //  * the WENO transport of the three RK3 stages as one chain, alongside the chain of the dynamics transport
 //    (u, v, w, theta') and the stage projections. A WENO stage needs only the face fluxes, the step-start values and
-//    its input scalars; the dynamics stage s > 0 reads the scalars WENO stage s - 1 wrote (buoyancy), and WENO stage 2
-//    overwrites the scalars of set B only after dynamics stage 1 has read them.
+//    its input scalars; the dynamics stage 0 reads the step-start precipitation after the sedimentation (its
+//    buoyancy's condensate load), stage s > 0 the scalars WENO stage s - 1 wrote, and WENO stage 2 overwrites the
+//    scalars of set B only after dynamics stage 1 has read them.
 void enqueue_dynamics_graph(sg_context* ctx, const Plan& P) {
   const int A = 0, B = 1, C = 2;
   auto none = [](int) {};
@@ -586,6 +587,7 @@ void enqueue_dynamics_graph(sg_context* ctx, const Plan& P) {
   cudaStreamWaitEvent(side, ev[0], 0);
   launch_fall_courant(nodeS);
   launch_sediment(colsS, P.maxnz);
+  cudaEventRecord(ev[6], side);  // the sedimented precipitation (the dynamics' stage-0 buoyancy loads it)
   enqueue_solve(ctx, P, PROJ_FACE, A, main, none);
   launch_face_correct(node, A);
   cudaEventRecord(ev[1], main);
@@ -593,12 +595,13 @@ void enqueue_dynamics_graph(sg_context* ctx, const Plan& P) {
   Launch W = lx(ctx, P, FAM_T_WENO), D = lx(ctx, P, FAM_T_DYN);
   W.cap = W.n; D.cap = D.n; W.stream = side;
   const int in[3] = {A, B, C}, out[3] = {B, C, B};
-  // ev[2 + s]: WENO stage s done; ev[5]: dynamics stage 1 done
+  // ev[2 + s]: WENO stage s done; ev[5]: dynamics stage 1 done; ev[6]: the sedimentation done
   for (int s = 0; s < 3; s++) {
     if (s == 2) cudaStreamWaitEvent(side, ev[5], 0);     // dynamics stage 1 has read set B's scalars
     if (W.n) launch_transport(W, TK_WENO, P.wenoG, P.minb, in[s], out[s], (float)RK3[s], s, P.TX, P.TY, P.bulk);
     cudaEventRecord(ev[2 + s], side);
-    if (s > 0) cudaStreamWaitEvent(main, ev[1 + s], 0);  // the stage's input scalars
+    // the stage's input scalars: for stage 0 the step-start fields after the sedimentation, later the WENO stage's
+    cudaStreamWaitEvent(main, s == 0 ? ev[6] : ev[1 + s], 0);
     if (D.n) launch_transport(D, TK_DYN, P.wenoG, P.minb, in[s], out[s], (float)RK3[s], s, P.TX, P.TY, P.bulk);
     if (s == 1) cudaEventRecord(ev[5], main);
     if (s < 2) enqueue_project(ctx, P, out[s], 0, main, none);

@@ -208,6 +208,7 @@ def test_transport_tiles_give_the_same_bits(ctx, storm, shape):
     assert ctx.transport_shape([r])[:3] == shape
     b = r.read()
     ctx.set_transport_shape(0)
+    assert ref.status()["failed"] == 0 and r.status()["failed"] == 0
     for k in CARRIED:
         assert np.array_equal(a[k], b[k]), (shape, k)
     ref.retire(); r.retire()
@@ -227,6 +228,7 @@ def test_bulk_copy_transport_gives_the_bits_of_per_thread_copies(storm, monkeypa
         runs = [c.create(s) for s in specs]
         c.batch_step(runs, 3)
         out[flag] = [r.read() for r in runs]
+        assert all(r.status()["failed"] == 0 for r in runs)
         for r in runs:
             r.retire()
         c.close()
