@@ -354,6 +354,15 @@ __device__ __forceinline__ void transport_item_bulk(const RunDesc& Rg, int group
   const int x = x0 + lx, y = y0 + ly;
   const bool on = !producer && x < nx && y < ny;
   const int col = on ? x + y * nx : 0;
+  for (int z = t; z < nz; z += blockDim.x) {
+    lv[0 * MAXNZ + z] = lvl(Rg, L_INV_HZ, z);
+    lv[1 * MAXNZ + z] = lvl(Rg, L_INV_RHO, z);
+    if (KIND == TK_DYN) {
+      lv[2 * MAXNZ + z] = lvl(Rg, L_TH_UP_POS, z); lv[3 * MAXNZ + z] = lvl(Rg, L_TH_UP_NEG, z);
+      lv[4 * MAXNZ + z] = lvl(Rg, L_TH_DN_POS, z); lv[5 * MAXNZ + z] = lvl(Rg, L_TH_DN_NEG, z);
+      lv[6 * MAXNZ + z] = lvl(Rg, L_THB, z); lv[7 * MAXNZ + z] = lvl(Rg, L_QB, z); lv[8 * MAXNZ + z] = lvl(Rg, L_THVENV, z);
+    }
+  }
   const TileCopies TC{nx, ny, layer, TX, TY, x0, y0, G, AUX_S0 && stage > 0};
   // The packet of level L (issued by the producer warp): the plane L + 3 (for L = 0 the six planes of virtual levels
   // -2..3, clamped, that level 0 reads; the seventh slot is the one the packet of level 1, issued before this one has
