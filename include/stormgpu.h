@@ -218,7 +218,8 @@ int sg_run_divergence(sg_context* ctx, sg_run run, double* max_abs_div);
  * the nine WENO fields (weno_group). By default a batch's shape is picked by timing the candidates on the batch itself
  * when its plan is first built (the autotuner; SG_AUTOTUNE=0 in the environment keeps the default 40x8 or 32x8, 3).
  * The tuner also picks the WENO kernel's register budget. sg_set_transport_shape pins one shape for every later plan
- * (tile_x = 0 returns to tuning; register budget for 2 blocks per SM); results are the same bits
+ * (tile_x = 0 returns to tuning and forgets earlier results, so the next plan of a batch is tuned on its runs as they are
+ * then, e.g. developed storms after a spin-up; register budget for 2 blocks per SM); results are the same bits
  * for every shape. sg_batch_transport_shape reports the shape a batch runs with. No counterpart in the reference (its
  * CPU transport has no tiles). */
 int sg_set_transport_shape(sg_context* ctx, int tile_x, int tile_y, int weno_group);

@@ -110,6 +110,7 @@ struct sg_context {
   cudaStream_t side[2] = {nullptr, nullptr};
   cudaEvent_t dep[8] = {};
   bool autotune = true;
+  bool tuneLog = false;                 // SG_AUTOTUNE_LOG=1: the tuner prints every candidate's time to stderr
   bool bulk = true;                     // the bulk-copy transport kernels where a plan allows them (SG_TRANSPORT_BULK=0: never)
   bool rowsOnly = false;                // row-transform spectral path for every grid (SG_SPECTRAL_ROWS=1)
   int pinned[4] = {0, 0, 0, 2};         // transport tile, WENO group, blocks per SM fixed by the caller (TX = 0: tune)
@@ -468,6 +469,8 @@ int autotune_transport(sg_context* ctx, Plan& P) {
           if (rep) ms = std::min(ms, t);
         }
         CK(cudaGetLastError());
+        if (ctx->tuneLog) fprintf(stderr, "stormgpu tuner: tile %dx%d, %d WENO fields an item, %d blocks an SM, %s: %.4f ms\n", TX, TY, G, MB,
+                                  bulk ? "bulk copies" : "per-thread copies", ms);
         if (ms < bestMs) { bestMs = ms; best = {TX, TY, G, MB}; }
       }
     }
@@ -745,6 +748,7 @@ int sg_context_create(int device, uint64_t hbm_budget_bytes, sg_context** out) {
   if (const char* a = getenv("SG_AUTOTUNE")) ctx->autotune = atoi(a) != 0;
   if (const char* a = getenv("SG_SPECTRAL_ROWS")) ctx->rowsOnly = atoi(a) != 0;
   if (const char* a = getenv("SG_TRANSPORT_BULK")) ctx->bulk = atoi(a) != 0;
+  if (const char* a = getenv("SG_AUTOTUNE_LOG")) ctx->tuneLog = atoi(a) != 0;
   *out = ctx;
   return SG_OK;
 }
@@ -1407,7 +1411,7 @@ int sg_run_divergence(sg_context* ctx, sg_run run, double* max_abs_div) {
 extern "C" {
 int sg_set_transport_shape(sg_context* ctx, int tile_x, int tile_y, int weno_group) {
   if (!ctx) return SG_ERR_INVALID;
-  if (tile_x == 0) { ctx->pinned[0] = 0; }
+  if (tile_x == 0) { ctx->pinned[0] = 0; ctx->tuning.clear(); }  // back to tuning, on the runs as they are from now on
   else {
     if (tile_x < 1 || tile_y < 1 || tile_x * tile_y > 320 || tile_x * tile_y < tile_x + tile_y ||
         (tile_x + 6) * (tile_y + 6) > 4 * tile_x * tile_y || (weno_group != 1 && weno_group != 3) ||
