@@ -394,6 +394,7 @@ def main():
     value = job_value(cells, world, args.steps, ms)
 
     tile = ctx.transport_shape(runs)
+    bulk = ctx.transport_bulk(runs)
     # ---- kernel profile (eager, CUDA events per launch) and the roofline of the transport
     prof = ctx.profile(runs, 2)
     hbm, peak_kind = peaks()
@@ -480,8 +481,7 @@ def main():
                 "1-3 K ellipsoid bubble, +-0.1 K noise below 1 km",
         "config": {"workload": f"ensemble {args.members} x 40x32x50 per GPU, one CUDA graph per step", "cells_per_gpu": cells,
                    "spinup_steps": args.spinup, "transport_tile": {"x": tile[0], "y": tile[1], "weno_fields_per_item": tile[2], "weno_blocks_per_sm": tile[3]},
-                   "transport_copies": ("TMA bulk copies by a producer warp" if tile[3] == 2 and os.environ.get("SG_TRANSPORT_BULK", "1") != "0"
-                                        and tile[0] % 4 == 0 and tile[0] <= 40 else "per-thread cp.async"),
+                   "transport_copies": "TMA bulk copies by two producer warps" if bulk else "per-thread cp.async",
                    "l2": "inputs larger than L2 (213 MB per field set)", "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": "cell-steps/s", "h2d_bytes_per_step": bytes_io, "d2h_bytes_per_step": bytes_io,
                 "call": f"sg_batch_step_io, {E2E_GROUPS} groups", "serial_calls_value": e2e_values["serial"]},

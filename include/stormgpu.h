@@ -225,6 +225,10 @@ int sg_run_divergence(sg_context* ctx, sg_run run, double* max_abs_div);
 int sg_set_transport_shape(sg_context* ctx, int tile_x, int tile_y, int weno_group);
 /* shape4 = (tile_x, tile_y, weno_group, blocks per SM the WENO kernel's register budget is cut for: 2 or 3). */
 int sg_batch_transport_shape(sg_context* ctx, const sg_run* runs, int n, int* shape4);
+/* *bulk = 1 when the batch's transport tiles get their inputs by TMA bulk copies that two producer warps issue, 0 when
+ * every thread copies its own plane cells (the tuner times both; SG_TRANSPORT_BULK=0 keeps the bulk copies out). No
+ * counterpart in the reference. */
+int sg_batch_transport_copies(sg_context* ctx, const sg_run* runs, int n, int* bulk);
 
 /* ---- divergence check without allocation. No counterpart in the reference (its check, PressureSolver.divergence,
  * src/core/pressure.ts:50-66, runs on its own CPU arrays).

@@ -114,7 +114,7 @@ struct sg_context {
   bool bulk = true;                     // the bulk-copy transport kernels where a plan allows them (SG_TRANSPORT_BULK=0: never)
   bool rowsOnly = false;                // row-transform spectral path for every grid (SG_SPECTRAL_ROWS=1)
   int pinned[4] = {0, 0, 0, 2};         // transport tile, WENO group, blocks per SM fixed by the caller (TX = 0: tune)
-  std::map<std::vector<int>, std::array<int, 4>> tuning;  // batch signature -> (TX, TY, wenoG, minb)
+  std::map<std::vector<int>, std::array<int, 5>> tuning;  // batch signature -> (TX, TY, wenoG, minb, bulk)
   // packed transfers: a device staging buffer (grown on demand) and the item lists per (runs, mask)
   float* staging = nullptr;
   size_t stagingBytes = 0;
@@ -434,7 +434,7 @@ int autotune_transport(sg_context* ctx, Plan& P) {
     int c = 1; while (c < (int)P.slots.size()) c *= 2;
     sig.push_back(c);
   }
-  std::array<int, 4> best{P.TX, P.TY, P.wenoG, P.minb};
+  std::array<int, 5> best{P.TX, P.TY, P.wenoG, P.minb, P.bulk ? 1 : 0};
   auto it = ctx->tuning.find(sig);
   if (it != ctx->tuning.end()) {
     best = it->second;
@@ -448,9 +448,11 @@ int autotune_transport(sg_context* ctx, Plan& P) {
     for (auto& sh : shapes) {
       const int TX = sh[0], TY = sh[1];
       if (TX > 2 * P.maxnx || TY > 2 * P.maxny) continue;
-      for (int G : {3, 1}) for (int MB : {2, 3}) {
-        // with 2 blocks an SM the bulk-copy kernels where the shape allows them, else the per-thread copies
-        const bool bulk = MB == 2 && ctx->bulk && transport_bulk_ok(TX, TY, P.minnx, P.nx4);
+      // variants: per-thread copies at 2 or 3 blocks an SM, and (where the shape allows them) the bulk copies at 2
+      for (int G : {3, 1}) for (int V : {0, 1, 2}) {
+        const int MB = V == 1 ? 3 : 2;
+        const bool bulk = V == 2;
+        if (bulk && !(ctx->bulk && transport_bulk_ok(TX, TY, P.minnx, P.nx4))) continue;
         const size_t need = bulk ? std::max(transport_smem_bulk(TK_WENO, G, TX, TY), transport_smem_bulk(TK_DYN, 4, TX, TY))
                                  : transport_smem(TK_WENO, G, TX, TY);
         if (need > (size_t)ctx->maxSmem) continue;
@@ -471,14 +473,13 @@ int autotune_transport(sg_context* ctx, Plan& P) {
         CK(cudaGetLastError());
         if (ctx->tuneLog) fprintf(stderr, "stormgpu tuner: tile %dx%d, %d WENO fields an item, %d blocks an SM, %s: %.4f ms\n", TX, TY, G, MB,
                                   bulk ? "bulk copies" : "per-thread copies", ms);
-        if (ms < bestMs) { bestMs = ms; best = {TX, TY, G, MB}; }
+        if (ms < bestMs) { bestMs = ms; best = {TX, TY, G, MB, bulk ? 1 : 0}; }
       }
     }
     cudaEventDestroy(e0); cudaEventDestroy(e1);
     ctx->tuning[sig] = best;
   }
-  P.TX = best[0]; P.TY = best[1]; P.wenoG = best[2]; P.minb = best[3]; P.tuned = true;
-  P.bulk = P.minb == 2 && ctx->bulk && transport_bulk_ok(P.TX, P.TY, P.minnx, P.nx4);
+  P.TX = best[0]; P.TY = best[1]; P.wenoG = best[2]; P.minb = best[3]; P.bulk = best[4] != 0; P.tuned = true;
   std::vector<int4> all[FAM_COUNT];
   for (int f = 0; f < FAM_COUNT; f++) {  // keep the other families, rebuild the transport ones
     if (f == FAM_T_WENO || f == FAM_T_DYN) continue;
@@ -1432,6 +1433,16 @@ int sg_batch_transport_shape(sg_context* ctx, const sg_run* runs, int n, int* sh
   Plan* P = get_plan(ctx, slots, &st);
   if (!P) return st;
   shape3[0] = P->TX; shape3[1] = P->TY; shape3[2] = P->wenoG; shape3[3] = P->minb;
+  return SG_OK;
+}
+int sg_batch_transport_copies(sg_context* ctx, const sg_run* runs, int n, int* bulk) {
+  if (!ctx || !bulk) return SG_ERR_INVALID;
+  std::vector<int> slots;
+  int st = slots_of(ctx, runs, n, slots);
+  if (st != SG_OK) return st;
+  Plan* P = get_plan(ctx, slots, &st);
+  if (!P) return st;
+  *bulk = P->bulk ? 1 : 0;
   return SG_OK;
 }
 int sg_debug_step_part(sg_context* ctx, sg_run run, int part) {

@@ -301,17 +301,23 @@ __global__ void __launch_bounds__(320, MINB) k_transport(const RunDesc* __restri
 
 // ==================================================================== RK3 transport, bulk-copy tiles
 // The same arithmetic as transport_item (the same bits for every face), with the tile's inputs moved by the TMA
-// engine: the block is TX x TY consumer threads (one per column) and one producer warp. Per level the producer warp
-// issues cp.async.bulk row copies of the next input packet into shared memory - the G field planes of level z + 4
+// engine: the block is TX x TY consumer threads (one per column) and two producer warps. Per level the producer warps
+// issue cp.async.bulk row copies of the next input packet into shared memory - the G field planes of level z + 4
 // (rows of the periodic window [x0 - 4, x0 + TX + 4) x [y0 - 3, y0 + TY + 3), one copy per piece of a row between
 // wraps, so the halo needs no wrapped index arithmetic), the tile's face fluxes of level z + 1 (one row copy per tile
 // row), the face fluxes of the west and south edges and, for the WENO fields, their step-start values - completing on
-// one of two mbarriers (the packet of level L on barrier L & 1); it then reconstructs the tile's west and south edge
-// faces. The consumer threads wait on the packet's mbarrier, reconstruct the east, north and top faces of their own
-// cells, and after the level's block barrier form the tendency and the RK3 update. The edge faces, which made two
-// warps of every block do 40% more reconstructions than the rest, are all on the producer warp.
-// Needs nx and TX multiples of 4 (16-byte rows and pieces) and TX <= nx (at most three pieces a row).
-constexpr int TPROD = 32;  // producer threads per block
+// one of two mbarriers (the packet of level L on barrier L & 1), from a table of copy descriptors made once per tile;
+// they then reconstruct the tile's west and south edge faces, one a lane. The consumer threads wait on the packet's
+// mbarrier, reconstruct the east, north and top faces of their own cells, and after the level's block barrier form
+// the tendency and the RK3 update. The edge faces, which made two warps of every block do 40% more reconstructions
+// than the rest, are all on the producer warps.
+// Needs nx and TX multiples of 4 (16-byte rows and pieces), TX <= nx (at most three pieces a row), TX + TY <= 64.
+constexpr int TPROD = 64;  // producer threads per block (two warps; named barrier 1 is theirs)
+
+// Entries of the copy-descriptor table of a tile (ring pieces, at most three a window row, then auxiliary rows).
+__host__ __device__ constexpr int copy_table_entries(int kind, int G, int TY) {
+  return (TY + 6) * 3 + 2 * TY + 1 + (kind == TK_WENO ? G * TY : 0);
+}
 
 template <int KIND, int G>
 __host__ __device__ constexpr int aux_floats(int TX, int TY) {
@@ -344,6 +350,9 @@ __device__ __forceinline__ void transport_item_bulk(const RunDesc& Rg, int group
   float* aux = ring + G * 7 * NCELL;                  // [2][AUXF]
   float* fxs = aux + 2 * AUXF;                        // [2][G][TY][TX + 1]: x faces, west edge at column 0
   float* fys = fxs + 2 * G * TY * (TX + 1);           // [2][G][TY + 1][TX]: y faces, south edge at row 0
+  // the copy descriptors: ring pieces (smem offset, global offset, bytes), then auxiliary rows (smem offset, source
+  // offset, source, bytes); each producer lane fills and reads only its own entries
+  int4* const tab = reinterpret_cast<int4*>(sm + (((fys + 2 * G * (TY + 1) * TX) - sm + 3) & ~3));
   const int FXS = TY * (TX + 1), FYS = (TY + 1) * TX;
   const int t = threadIdx.x;
   const bool producer = t >= NT;
@@ -364,6 +373,15 @@ __device__ __forceinline__ void transport_item_bulk(const RunDesc& Rg, int group
     }
   }
   const TileCopies TC{nx, ny, layer, TX, TY, x0, y0, G, AUX_S0 && stage > 0};
+  int covered;
+  const int nseg = TC.pieces(covered), nrs = PH * nseg, na = TC.naux();
+  const unsigned auxBytes = TC.bytes(0), planeBytes = TC.bytes(1) - auxBytes;
+  int4* const rtab = tab;
+  int4* const atab = tab + nrs;
+  if (producer) {
+    for (int j = lane; j < nrs; j += TPROD) { int so, go, len; TC.ring(j, nseg, so, go, len); rtab[j] = make_int4(so, go, 4 * len, 0); }
+    for (int j = lane; j < na; j += TPROD) { int so, src, which, b; TC.aux(j, so, src, which, b); atab[j] = make_int4(so, src, which, b); }
+  }
   // The packet of level L (issued by the producer warp): the plane L + 3 (for L = 0 the six planes of virtual levels
   // -2..3, clamped, that level 0 reads; the seventh slot is the one the packet of level 1, issued before this one has
   // landed, fills with plane 4, so no two packets in flight write the same slot) and the level's faces, edges and
@@ -371,28 +389,25 @@ __device__ __forceinline__ void transport_item_bulk(const RunDesc& Rg, int group
   auto issue = [&](int L) {
     unsigned long long* bar = bars + (L & 1);
     const int v0 = L == 0 ? -2 : L + 3, v1 = L + 3;
-    if (lane == 0) mbar_arrive_expect_tx(bar, TC.bytes(v1 - v0 + 1));
-    __syncwarp();
-    int covered;
-    const int nseg = TC.pieces(covered), nrs = PH * nseg;
+    if (lane == 0) mbar_arrive_expect_tx(bar, auxBytes + (unsigned)(v1 - v0 + 1) * planeBytes);
+    asm volatile("bar.sync 1, %0;\n" ::"n"(TPROD) : "memory");  // the bytes are announced before any copy lands
     for (int v = v0; v <= v1; v++) {
       const int lev = clampi(v, 0, nz - 1), slot = (v + 7) % 7;
+      float* const rs = ring + slot * NCELL;
+      const float* const gs = fld + qo + lev * layer;
       for (int j = lane; j < nrs; j += TPROD) {
-        int soff, goff, len;
-        TC.ring(j, nseg, soff, goff, len);
+        const int4 d = rtab[j];
 #pragma unroll
-        for (int g = 0; g < G; g++)
-          bulk_g2s(ring + (g * 7 + slot) * NCELL + soff, fld + qo + fo[g] + lev * layer + goff, (unsigned)(4 * len), bar);
+        for (int g = 0; g < G; g++) bulk_g2s(rs + g * 7 * NCELL + d.x, gs + fo[g] + d.y, (unsigned)d.z, bar);
       }
     }
     float* A = aux + (L & 1) * AUXF;
-    const int l = L * layer, na = TC.naux();
+    const int l = L * layer;
     for (int j = lane; j < na; j += TPROD) {
-      int soff, src, which, bytes;
-      TC.aux(j, soff, src, which, bytes);
-      const void* from = which == 0 ? static_cast<const void*>(F4 + l + src)
-                                    : static_cast<const void*>(fld + TGROUP[group][which - 1] * (int)n + l + src);
-      bulk_g2s(A + soff, from, (unsigned)bytes, bar);
+      const int4 d = atab[j];
+      const void* from = d.z == 0 ? static_cast<const void*>(F4 + l + d.y)
+                                  : static_cast<const void*>(fld + TGROUP[group][d.z - 1] * (int)n + l + d.y);
+      bulk_g2s(A + d.x, from, (unsigned)d.w, bar);
     }
   };
   // the packet of level L has landed (all threads); a wait that runs out is recorded and ends the item
@@ -403,9 +418,9 @@ __device__ __forceinline__ void transport_item_bulk(const RunDesc& Rg, int group
   };
   __syncthreads();  // the level table; the previous item's reads of the ring and the packets are done
   if (producer) { fence_proxy_async(); issue(0); }
-  // edge faces: producer lanes e = lane, lane + 32 (e < TY: the west face of tile row e; TY <= e < TY + TX: the south
-  // face of tile column e - TY)
-  constexpr int EROUNDS = 2;
+  // edge faces: producer lane e (e < TY: the west face of tile row e; TY <= e < TY + TX: the south face of tile column
+  // e - TY)
+  constexpr int EROUNDS = 1;
   const bool loadBuoy = KIND == TK_DYN && (flags & RF_STAGES);
   const bool loading = flags & RF_LOADING;
   float s0[G];
@@ -581,10 +596,12 @@ size_t transport_smem(int kind, int G, int TX, int TY) {
 }
 size_t transport_smem_bulk(int kind, int G, int TX, int TY) {
   const size_t auxf = kind == TK_WENO ? (G == 3 ? aux_floats<TK_WENO, 3>(TX, TY) : aux_floats<TK_WENO, 1>(TX, TY)) : aux_floats<TK_DYN, 4>(TX, TY);
-  return ((size_t)tlv_rows(kind) * MAXNZ + (size_t)G * 7 * (TX + 8) * (TY + 6) + 2 * auxf + 2 * (size_t)G * TY * (TX + 1) + 2 * (size_t)G * (TY + 1) * TX) * sizeof(float);
+  const size_t floats = (size_t)tlv_rows(kind) * MAXNZ + (size_t)G * 7 * (TX + 8) * (TY + 6) + 2 * auxf + 2 * (size_t)G * TY * (TX + 1) +
+                        2 * (size_t)G * (TY + 1) * TX;
+  return ((floats + 3) / 4 * 4 + 4 * (size_t)copy_table_entries(kind, G, TY)) * sizeof(float);
 }
 bool transport_bulk_ok(int TX, int TY, int min_nx, bool all_nx4) {
-  return all_nx4 && TX % 4 == 0 && TX <= min_nx && (TX * TY) % 32 == 0 && TX * TY <= 320 && TX + TY <= 2 * TPROD;
+  return all_nx4 && TX % 4 == 0 && TX <= min_nx && (TX * TY) % 32 == 0 && TX * TY <= 320 && TX + TY <= TPROD;
 }
 
 namespace {

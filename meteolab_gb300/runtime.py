@@ -118,6 +118,7 @@ def load():
             L.sg_divergence_max_static.argtypes = [i32, vp, vp, vp, i32, i32, i32, C.c_double, C.c_double, C.POINTER(C.c_double),
                                                    C.POINTER(C.c_double), vp, C.POINTER(C.c_double), C.c_char_p, C.c_size_t]
             L.sg_batch_transport_shape.argtypes = [vp, C.POINTER(C.c_int32), i32, C.POINTER(C.c_int)]
+            L.sg_batch_transport_copies.argtypes = [vp, C.POINTER(C.c_int32), i32, C.POINTER(C.c_int)]
             L.sg_server_create.argtypes = [vp, i32, C.POINTER(vp)]
             L.sg_server_destroy.argtypes = [vp]
             L.sg_server_submit.argtypes = [vp, C.POINTER(SgGrid), C.POINTER(SgBase), C.POINTER(SgSwitches), C.POINTER(_FP), i64, i64]
@@ -285,6 +286,13 @@ class Context:
         out = (C.c_int * 4)()
         self.check(load().sg_batch_transport_shape(self.h, ids, len(runs), out), "transport shape")
         return tuple(out)
+
+    def transport_bulk(self, runs: Sequence["Run"]) -> bool:
+        """Whether the batch's transport tiles move their inputs by TMA bulk copies (sg_batch_transport_copies)."""
+        ids = (C.c_int32 * len(runs))(*[r.id for r in runs])
+        out = C.c_int()
+        self.check(load().sg_batch_transport_copies(self.h, ids, len(runs), C.byref(out)), "transport copies")
+        return bool(out.value)
 
     def synchronize(self):
         self.check(load().sg_synchronize(self.h), "synchronize")
