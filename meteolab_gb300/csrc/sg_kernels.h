@@ -44,10 +44,11 @@ enum TKind { TK_WENO = 0, TK_DYN = 1 };
 // Transport of one field kind (0: the WENO fields, 1: the dynamics u, v, w, theta'); for WENO `group` is the fields
 // per item (1 or 3)
 // and `minb` the blocks per SM its register budget is cut for (2 or 3).
-// bulk: the bulk-copy kernels (a producer warp moves each level's inputs with TMA bulk copies; only with minb 2 and
-// when transport_bulk_ok holds for the plan), else the kernels whose threads copy their own plane cells.
+// bulk: the bulk-copy kernels (two producer warps move each level's inputs with TMA bulk copies; only with minb 2 and
+// when transport_bulk_ok holds for the plan), else the kernels whose threads copy their own plane cells; ew: those
+// with two edge warps that take the tile's edge faces (minb 2, the compile-time tiles).
 void launch_transport(const Launch& L, int kind, int group, int minb, int in_set, int out_set, float frac, int stage, int TX, int TY,
-                      bool bulk);
+                      bool bulk, bool ew);
 size_t transport_smem(int kind, int G, int TX, int TY);
 size_t transport_smem_bulk(int kind, int G, int TX, int TY);
 // Whether a tile shape can take the bulk-copy kernels on a plan whose narrowest grid is min_nx wide (all_nx4: every

@@ -112,6 +112,7 @@ struct sg_context {
   bool autotune = true;
   bool tuneLog = false;                 // SG_AUTOTUNE_LOG=1: the tuner prints every candidate's time to stderr
   bool bulk = true;                     // the bulk-copy transport kernels where a plan allows them (SG_TRANSPORT_BULK=0: never)
+  bool edgeWarps = true;                // per-thread transport with two edge warps (SG_TRANSPORT_EDGE_WARPS=0: the column threads take the edges)
   bool rowsOnly = false;                // row-transform spectral path for every grid (SG_SPECTRAL_ROWS=1)
   int pinned[4] = {0, 0, 0, 2};         // transport tile, WENO group, blocks per SM fixed by the caller (TX = 0: tune)
   std::map<std::vector<int>, std::array<int, 5>> tuning;  // batch signature -> (TX, TY, wenoG, minb, bulk)
@@ -412,7 +413,7 @@ void launch_transport_kinds(sg_context* ctx, const Plan& P, int in, int out, flo
   for (int k = 0; k < 2; k++) {
     Launch L = lx(ctx, P, fams[k]);
     L.cap = L.n;
-    if (L.n) launch_transport(L, k, P.wenoG, P.minb, in, out, frac, stage, P.TX, P.TY, P.bulk);
+    if (L.n) launch_transport(L, k, P.wenoG, P.minb, in, out, frac, stage, P.TX, P.TY, P.bulk, ctx->edgeWarps);
     hook(hookBase + k);
   }
 }
@@ -602,11 +603,11 @@ void enqueue_dynamics_graph(sg_context* ctx, const Plan& P) {
   // ev[2 + s]: WENO stage s done; ev[5]: dynamics stage 1 done; ev[6]: the sedimentation done
   for (int s = 0; s < 3; s++) {
     if (s == 2) cudaStreamWaitEvent(side, ev[5], 0);     // dynamics stage 1 has read set B's scalars
-    if (W.n) launch_transport(W, TK_WENO, P.wenoG, P.minb, in[s], out[s], (float)RK3[s], s, P.TX, P.TY, P.bulk);
+    if (W.n) launch_transport(W, TK_WENO, P.wenoG, P.minb, in[s], out[s], (float)RK3[s], s, P.TX, P.TY, P.bulk, ctx->edgeWarps);
     cudaEventRecord(ev[2 + s], side);
     // the stage's input scalars: for stage 0 the step-start fields after the sedimentation, later the WENO stage's
     cudaStreamWaitEvent(main, s == 0 ? ev[6] : ev[1 + s], 0);
-    if (D.n) launch_transport(D, TK_DYN, P.wenoG, P.minb, in[s], out[s], (float)RK3[s], s, P.TX, P.TY, P.bulk);
+    if (D.n) launch_transport(D, TK_DYN, P.wenoG, P.minb, in[s], out[s], (float)RK3[s], s, P.TX, P.TY, P.bulk, ctx->edgeWarps);
     if (s == 1) cudaEventRecord(ev[5], main);
     if (s < 2) enqueue_project(ctx, P, out[s], 0, main, none);
   }
@@ -750,6 +751,7 @@ int sg_context_create(int device, uint64_t hbm_budget_bytes, sg_context** out) {
   if (const char* a = getenv("SG_SPECTRAL_ROWS")) ctx->rowsOnly = atoi(a) != 0;
   if (const char* a = getenv("SG_TRANSPORT_BULK")) ctx->bulk = atoi(a) != 0;
   if (const char* a = getenv("SG_AUTOTUNE_LOG")) ctx->tuneLog = atoi(a) != 0;
+  if (const char* a = getenv("SG_TRANSPORT_EDGE_WARPS")) ctx->edgeWarps = atoi(a) != 0;
   *out = ctx;
   return SG_OK;
 }

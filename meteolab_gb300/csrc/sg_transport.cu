@@ -68,8 +68,12 @@ __device__ __forceinline__ void face_stencil(const float* P, int s, bool pos, fl
 }
 
 // CTX x CTY: the tile as compile-time constants (every plane stride and stencil offset an immediate), or 0 x 0 for a
-// tile given at run time (TXr x TYr).
-template <int KIND, int G, int CTX, int CTY>
+// tile given at run time (TXr x TYr). EW: the block has two more warps, whose 64 lanes take the tile's west and south
+// edge faces (one face a lane) while the TX x TY column threads take only their own cells' faces; without it the
+// first TY + TX column threads take the edges too, and their warps do up to 40% more reconstructions than the rest
+// of the block waits for at every level's barrier.
+constexpr int TEDGE = 64;  // edge threads of an EW block
+template <int KIND, int G, int CTX, int CTY, bool EW>
 __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int tile, int in_set, int out_set, float frac, int stage,
                                                int TXr, int TYr, float* sm) {
   const int TX = CTX ? CTX : TXr, TY = CTY ? CTY : TYr;
@@ -90,7 +94,7 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
 #define SP(g) (fld + fo[g])
 #define OP(g) (fld + oo + fo[g])
   const int PW = TX + 6, PH = TY + 6, NCELL = PW * PH;
-  const int NT = CTX ? CTX * CTY : blockDim.x;  // the block is one thread a column of the tile
+  const int NT = CTX ? CTX * CTY : (EW ? (int)blockDim.x - TEDGE : (int)blockDim.x);  // one thread a column of the tile
   // plane cells a thread copies: exact for a compile-time tile, the bound TMAXC otherwise
   constexpr int CJ = CTX ? ((CTX + 6) * (CTY + 6) + CTX * CTY - 1) / (CTX * CTY) : TMAXC;
   static_assert(CJ <= TMAXC, "the tile's halo plane fits in TMAXC cells a thread");
@@ -101,16 +105,19 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
   float* fys = fxs + 2 * G * TY * (TX + 1);         // [2][G][TY + 1][TX]: y faces, south edge at row 0
   const int FXS = TY * (TX + 1), FYS = (TY + 1) * TX;
   const int t = threadIdx.x, lx = t % TX, ly = t / TX;
+  const bool column = !EW || t < NT;  // a column thread (else an edge thread of an EW block)
   const int tilesX = (nx + TX - 1) / TX, x0 = (tile % tilesX) * TX, y0 = (tile / tilesX) * TY;
   const int x = x0 + lx, y = y0 + ly;
-  const bool on = x < nx && y < ny;
+  const bool on = column && x < nx && y < ny;
   const int col = on ? x + y * nx : 0;
-  // edge lanes: t < TY the west face of row t, TY <= t < TY + TX the south face of column t - TY
-  const bool edgeW = t < TY && y0 + t < ny, edgeS = t >= TY && t < TY + TX && x0 + t - TY < nx;
-  const int eoff = edgeW ? wrap(x0 - 1, nx) + (y0 + t) * nx : edgeS ? (x0 + t - TY) + wrap(y0 - 1, ny) * nx : 0;
-  const int ecell = edgeW ? (t + 3) * PW + 3 : (3 * PW + t - TY + 3);  // plane index of the cell on the edge's high side
+  // edge lanes: e < TY the west face of row e, TY <= e < TY + TX the south face of column e - TY (e = t, or the edge
+  // thread's index in an EW block)
+  const int e = EW ? t - NT : t;
+  const bool edgeW = e >= 0 && e < TY && y0 + e < ny, edgeS = e >= TY && e < TY + TX && x0 + e - TY < nx;
+  const int eoff = edgeW ? wrap(x0 - 1, nx) + (y0 + e) * nx : edgeS ? (x0 + e - TY) + wrap(y0 - 1, ny) * nx : 0;
+  const int ecell = edgeW ? (e + 3) * PW + 3 : (3 * PW + e - TY + 3);  // plane index of the cell on the edge's high side
   const int estride = edgeW ? 1 : PW;
-  float* const edst = edgeW ? fxs + t * (TX + 1) : fys + (t - TY);
+  float* const edst = edgeW ? fxs + e * (TX + 1) : fys + (e - TY);
   for (int z = t; z < nz; z += blockDim.x) {
     lv[0 * MAXNZ + z] = lvl(Rg, L_INV_HZ, z);
     lv[1 * MAXNZ + z] = lvl(Rg, L_INV_RHO, z);
@@ -124,11 +131,11 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
   int off[CJ];
 #pragma unroll
   for (int j = 0; j < CJ; j++) {
-    int e = t + j * NT;
-    int hy = e / PW, hx = e - hy * PW;
+    int c = t + j * NT;
+    int hy = c / PW, hx = c - hy * PW;
     int gx = x0 + hx - 3, gy = y0 + hy - 3;
     gx = ((gx % nx) + nx) % nx; gy = ((gy % ny) + ny) % ny;
-    off[j] = e < NCELL ? gx + gy * nx : -1;
+    off[j] = column && c < NCELL ? gx + gy * nx : -1;
   }
   const bool loadBuoy = KIND == TK_DYN && (flags & RF_STAGES);
   const bool loading = flags & RF_LOADING;
@@ -287,15 +294,16 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
 #undef OP
 }
 
-// MINB: resident blocks per SM the register budget is cut for (2: up to 96 registers a thread, 3: 64).
-template <int KIND, int G, int MINB, int CTX, int CTY>
-__global__ void __launch_bounds__(320, MINB) k_transport(const RunDesc* __restrict__ runs, const int4* items, int nitems, int in_set, int out_set,
-                                                          float frac, int stage, int TX, int TY) {
+// MINB: resident blocks per SM the register budget is cut for (2: up to 96 registers a thread, 80 with the edge warps;
+// 3: 64).
+template <int KIND, int G, int MINB, int CTX, int CTY, bool EW>
+__global__ void __launch_bounds__(EW ? 320 + TEDGE : 320, MINB) k_transport(const RunDesc* __restrict__ runs, const int4* items, int nitems,
+                                                                             int in_set, int out_set, float frac, int stage, int TX, int TY) {
   extern __shared__ float sm[];
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
     if (R.cnt[C_FAILED]) continue;
-    transport_item<KIND, G, CTX, CTY>(R, items[it].y, items[it].z, in_set, out_set, frac, stage, TX, TY, sm);
+    transport_item<KIND, G, CTX, CTY, EW>(R, items[it].y, items[it].z, in_set, out_set, frac, stage, TX, TY, sm);
   }
 }
 
@@ -606,10 +614,15 @@ bool transport_bulk_ok(int TX, int TY, int min_nx, bool all_nx4) {
 
 namespace {
 // The tiles compiled with constant strides (the autotuner's candidates); any other tile takes the run-time variant.
-template <int KIND, int G, int MINB, int CTX, int CTY>
+template <int KIND, int G, int MINB, int CTX, int CTY, bool EW>
 void tlaunch(const Launch& L, int in_set, int out_set, float frac, int stage, int TX, int TY) {
-  k_transport<KIND, G, MINB, CTX, CTY><<<GRID(L.n, L.cap), TX * TY, transport_smem(KIND, G, TX, TY), L.stream>>>(
+  k_transport<KIND, G, MINB, CTX, CTY, EW><<<GRID(L.n, L.cap), TX * TY + (EW ? TEDGE : 0), transport_smem(KIND, G, TX, TY), L.stream>>>(
       L.runs, L.items, L.n, in_set, out_set, frac, stage, TX, TY);
+}
+template <int KIND, int G, int CTX, int CTY>
+void tlaunch_ew(const Launch& L, int in_set, int out_set, float frac, int stage, int TX, int TY, bool ew) {
+  if (ew) tlaunch<KIND, G, 2, CTX, CTY, true>(L, in_set, out_set, frac, stage, TX, TY);
+  else tlaunch<KIND, G, 2, CTX, CTY, false>(L, in_set, out_set, frac, stage, TX, TY);
 }
 template <int KIND, int G, int CTX, int CTY>
 void tlaunch_bulk(const Launch& L, int in_set, int out_set, float frac, int stage, int TX, int TY) {
@@ -635,34 +648,41 @@ cudaError_t tlimits_bulk(int bytes) {
   if ((e = smem_limit(k_transport_bulk<KIND, G, 2, 16, 16>, bytes)) != cudaSuccess) return e;
   return smem_limit(k_transport_bulk<KIND, G, 2, 40, 4>, bytes);
 }
+// ew: the compile-time tiles (all with a multiple of 32 columns) with the two edge warps
 template <int KIND, int G, int MINB>
-void tlaunch_tile(const Launch& L, int in_set, int out_set, float frac, int stage, int TX, int TY) {
+void tlaunch_tile(const Launch& L, int in_set, int out_set, float frac, int stage, int TX, int TY, bool ew) {
   if constexpr (MINB == 2) {
-    if (TX == 40 && TY == 8) return tlaunch<KIND, G, MINB, 40, 8>(L, in_set, out_set, frac, stage, TX, TY);
-    if (TX == 32 && TY == 8) return tlaunch<KIND, G, MINB, 32, 8>(L, in_set, out_set, frac, stage, TX, TY);
-    if (TX == 20 && TY == 8) return tlaunch<KIND, G, MINB, 20, 8>(L, in_set, out_set, frac, stage, TX, TY);
-    if (TX == 16 && TY == 16) return tlaunch<KIND, G, MINB, 16, 16>(L, in_set, out_set, frac, stage, TX, TY);
-    if (TX == 40 && TY == 4) return tlaunch<KIND, G, MINB, 40, 4>(L, in_set, out_set, frac, stage, TX, TY);
+    if (TX == 40 && TY == 8) return tlaunch_ew<KIND, G, 40, 8>(L, in_set, out_set, frac, stage, TX, TY, ew);
+    if (TX == 32 && TY == 8) return tlaunch_ew<KIND, G, 32, 8>(L, in_set, out_set, frac, stage, TX, TY, ew);
+    if (TX == 20 && TY == 8) return tlaunch_ew<KIND, G, 20, 8>(L, in_set, out_set, frac, stage, TX, TY, ew);
+    if (TX == 16 && TY == 16) return tlaunch_ew<KIND, G, 16, 16>(L, in_set, out_set, frac, stage, TX, TY, ew);
+    if (TX == 40 && TY == 4) return tlaunch_ew<KIND, G, 40, 4>(L, in_set, out_set, frac, stage, TX, TY, ew);
   }
-  tlaunch<KIND, G, MINB, 0, 0>(L, in_set, out_set, frac, stage, TX, TY);
+  tlaunch<KIND, G, MINB, 0, 0, false>(L, in_set, out_set, frac, stage, TX, TY);
+}
+template <int KIND, int G, int CTX, int CTY>
+cudaError_t tlimits_ew(int bytes) {
+  cudaError_t e;
+  if ((e = smem_limit(k_transport<KIND, G, 2, CTX, CTY, false>, bytes)) != cudaSuccess) return e;
+  return smem_limit(k_transport<KIND, G, 2, CTX, CTY, true>, bytes);
 }
 template <int KIND, int G, int MINB>
 cudaError_t tlimits(int bytes) {
   cudaError_t e;
-  if ((e = smem_limit(k_transport<KIND, G, MINB, 0, 0>, bytes)) != cudaSuccess) return e;
+  if ((e = smem_limit(k_transport<KIND, G, MINB, 0, 0, false>, bytes)) != cudaSuccess) return e;
   if constexpr (MINB == 2) {
-    if ((e = smem_limit(k_transport<KIND, G, MINB, 40, 8>, bytes)) != cudaSuccess) return e;
-    if ((e = smem_limit(k_transport<KIND, G, MINB, 32, 8>, bytes)) != cudaSuccess) return e;
-    if ((e = smem_limit(k_transport<KIND, G, MINB, 20, 8>, bytes)) != cudaSuccess) return e;
-    if ((e = smem_limit(k_transport<KIND, G, MINB, 16, 16>, bytes)) != cudaSuccess) return e;
-    if ((e = smem_limit(k_transport<KIND, G, MINB, 40, 4>, bytes)) != cudaSuccess) return e;
+    if ((e = tlimits_ew<KIND, G, 40, 8>(bytes)) != cudaSuccess) return e;
+    if ((e = tlimits_ew<KIND, G, 32, 8>(bytes)) != cudaSuccess) return e;
+    if ((e = tlimits_ew<KIND, G, 20, 8>(bytes)) != cudaSuccess) return e;
+    if ((e = tlimits_ew<KIND, G, 16, 16>(bytes)) != cudaSuccess) return e;
+    if ((e = tlimits_ew<KIND, G, 40, 4>(bytes)) != cudaSuccess) return e;
   }
   return cudaSuccess;
 }
 }  // namespace
 
 void launch_transport(const Launch& L, int kind, int group, int minb, int in_set, int out_set, float frac, int stage, int TX, int TY,
-                      bool bulk) {
+                      bool bulk, bool ew) {
   if (L.n == 0) return;
   if (bulk && minb == 2) {
     if (kind == TK_WENO) {
@@ -675,10 +695,10 @@ void launch_transport(const Launch& L, int kind, int group, int minb, int in_set
   }
   switch (kind) {
     case TK_WENO:
-      if (group == 3) { if (minb == 3) tlaunch_tile<TK_WENO, 3, 3>(L, in_set, out_set, frac, stage, TX, TY); else tlaunch_tile<TK_WENO, 3, 2>(L, in_set, out_set, frac, stage, TX, TY); }
-      else { if (minb == 3) tlaunch_tile<TK_WENO, 1, 3>(L, in_set, out_set, frac, stage, TX, TY); else tlaunch_tile<TK_WENO, 1, 2>(L, in_set, out_set, frac, stage, TX, TY); }
+      if (group == 3) { if (minb == 3) tlaunch_tile<TK_WENO, 3, 3>(L, in_set, out_set, frac, stage, TX, TY, false); else tlaunch_tile<TK_WENO, 3, 2>(L, in_set, out_set, frac, stage, TX, TY, ew); }
+      else { if (minb == 3) tlaunch_tile<TK_WENO, 1, 3>(L, in_set, out_set, frac, stage, TX, TY, false); else tlaunch_tile<TK_WENO, 1, 2>(L, in_set, out_set, frac, stage, TX, TY, ew); }
       break;
-    default: tlaunch_tile<TK_DYN, 4, 2>(L, in_set, out_set, frac, stage, TX, TY); break;
+    default: tlaunch_tile<TK_DYN, 4, 2>(L, in_set, out_set, frac, stage, TX, TY, ew); break;
   }
 }
 

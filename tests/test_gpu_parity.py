@@ -214,27 +214,32 @@ def test_transport_tiles_give_the_same_bits(ctx, storm, shape):
     ref.retire(); r.retire()
 
 
-def test_bulk_copy_transport_gives_the_bits_of_per_thread_copies(storm, monkeypatch):
-    """The transport kernels whose producer warp moves each level's inputs with TMA bulk copies (the default where the
-    grid allows) and the kernels whose threads copy their own plane cells (SG_TRANSPORT_BULK=0) give bitwise equal
-    fields, on an uneven batch (standard and large grid) over three steps."""
+@pytest.mark.parametrize("shape", [(40, 8, 3), (20, 8, 1)])
+def test_transport_variants_give_the_same_bits(storm, monkeypatch, shape):
+    """The three transport variants give bitwise equal fields, on an uneven batch (standard and large grid) over
+    three steps: the tiles whose producer warps move each level's inputs with TMA bulk copies, the per-thread copies
+    with two edge warps taking the tile's edge faces, and the per-thread copies with the column threads taking them
+    (SG_TRANSPORT_BULK, SG_TRANSPORT_EDGE_WARPS)."""
     from meteolab_gb300.runtime import Context
     specs = [storm, baseline_run(create_grid(LARGE_GRID), seed=14)]
     out = {}
-    for flag in ("1", "0"):
-        monkeypatch.setenv("SG_TRANSPORT_BULK", flag)
+    for bulk, edge in (("1", "1"), ("0", "1"), ("0", "0")):
+        monkeypatch.setenv("SG_TRANSPORT_BULK", bulk)
+        monkeypatch.setenv("SG_TRANSPORT_EDGE_WARPS", edge)
         c = Context(0)
-        c.set_transport_shape(40, 8, 3)
+        c.set_transport_shape(*shape)
         runs = [c.create(s) for s in specs]
+        assert c.transport_bulk(runs) == (bulk == "1")
         c.batch_step(runs, 3)
-        out[flag] = [r.read() for r in runs]
+        out[bulk + edge] = [r.read() for r in runs]
         assert all(r.status()["failed"] == 0 for r in runs)
         for r in runs:
             r.retire()
         c.close()
-    for a, b in zip(out["1"], out["0"]):
-        for k in CARRIED:
-            assert np.array_equal(a[k], b[k]), k
+    for variant in ("01", "00"):
+        for a, b in zip(out["11"], out[variant]):
+            for k in CARRIED:
+                assert np.array_equal(a[k], b[k]), (variant, k)
 
 
 def test_batch_field_io_matches_per_run_calls(ctx, storm):
