@@ -698,7 +698,8 @@ void launch_transport(const Launch& L, int kind, int group, int minb, int in_set
       if (group == 3) { if (minb == 3) tlaunch_tile<TK_WENO, 3, 3>(L, in_set, out_set, frac, stage, TX, TY, false); else tlaunch_tile<TK_WENO, 3, 2>(L, in_set, out_set, frac, stage, TX, TY, ew); }
       else { if (minb == 3) tlaunch_tile<TK_WENO, 1, 3>(L, in_set, out_set, frac, stage, TX, TY, false); else tlaunch_tile<TK_WENO, 1, 2>(L, in_set, out_set, frac, stage, TX, TY, ew); }
       break;
-    default: tlaunch_tile<TK_DYN, 4, 2>(L, in_set, out_set, frac, stage, TX, TY, ew); break;
+    // the dynamics kernel without the edge warps: at their 80-register budget it spills, and measured slower
+    default: tlaunch_tile<TK_DYN, 4, 2>(L, in_set, out_set, frac, stage, TX, TY, false); break;
   }
 }
 
