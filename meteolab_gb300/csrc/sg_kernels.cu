@@ -701,9 +701,6 @@ __global__ void __launch_bounds__(256, 5) k_proj_div_fft2(const RunDesc* __restr
 // One x-wavenumber m of one run per block, thread (n, real/imaginary): the FP64 sweeps of k_proj_modes on the 2-D
 // spectrum in place (the input and the output stay in global memory; no transform, no barrier).
 __global__ void k_proj_sweep(const RunDesc* __restrict__ runs, const int4* items, int nitems, int mode) {
-  // the forward elimination's FP64 values of every thread's column, [level][thread] (shared memory rather than a
-  // per-thread array, which the compiler puts in local memory: the back substitution read it back through L1/L2)
-  extern __shared__ double sweep_d[];
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
     if (R.cnt[C_FAILED]) continue;
@@ -714,8 +711,7 @@ __global__ void k_proj_sweep(const RunDesc* __restrict__ runs, const int4* items
     float* g = reinterpret_cast<float*>(R.spec + (size_t)m * nzc * ny) + c;
     const TriAB* AB = (mode == PROJ_FACE ? R.tri_face : R.tri_pres) + (size_t)m * nzc * ny;
     const double* Cc = reinterpret_cast<const double*>((mode == PROJ_FACE ? R.tri_face : R.tri_pres) + (size_t)R.nm * nzc * ny) + (size_t)m * nzc * ny;
-    double* const d = sweep_d + u;  // level k at d[k * blockDim.x]
-    const int ds = blockDim.x;
+    double d[MAXNZ];
     double prev = 0;
     // levels in blocks of 8: the block's coefficients and values are loaded before its recurrence steps
     for (int k0 = 0; k0 < nzc; k0 += 8) {
@@ -729,10 +725,10 @@ __global__ void k_proj_sweep(const RunDesc* __restrict__ runs, const int4* items
       }
 #pragma unroll
       for (int j = 0; j < 8; j++) {
-        if (k0 + j < nzc) { prev = fma(-ab[j].b, prev, widen(__fmul_rn(ab[j].a, r[j]))); d[(k0 + j) * ds] = prev; }
+        if (k0 + j < nzc) { prev = fma(-ab[j].b, prev, widen(__fmul_rn(ab[j].a, r[j]))); d[k0 + j] = prev; }
       }
     }
-    double x = d[(nzc - 1) * ds];
+    double x = d[nzc - 1];
     g[2 * ((size_t)(nzc - 1) * ny + n)] = narrow(x);
     for (int k1 = nzc - 2; k1 >= 0; k1 -= 8) {
       double cc[8];
@@ -741,7 +737,7 @@ __global__ void k_proj_sweep(const RunDesc* __restrict__ runs, const int4* items
 #pragma unroll
       for (int j = 0; j < 8; j++) {
         const int k = k1 - j;
-        if (k >= 0) { x = fma(-cc[j], x, d[k * ds]); g[2 * ((size_t)k * ny + n)] = narrow(x); }
+        if (k >= 0) { x = fma(-cc[j], x, d[k]); g[2 * ((size_t)k * ny + n)] = narrow(x); }
       }
     }
   }
@@ -1548,9 +1544,8 @@ size_t layer_fft_smem_run(int nx, int ny) {
 void launch_proj_div_fft2(const Launch& L, int mode, int set, size_t smem) {
   k_proj_div_fft2<<<GRID(L.n, L.cap), 256, smem, L.stream>>>(L.runs, L.items, L.n, mode, set);
 }
-void launch_proj_sweep(const Launch& L, int mode, int maxny, int maxnz) {
-  const int threads = (2 * maxny + 31) / 32 * 32;
-  k_proj_sweep<<<GRID(L.n, L.cap), threads, (size_t)maxnz * threads * sizeof(double), L.stream>>>(L.runs, L.items, L.n, mode);
+void launch_proj_sweep(const Launch& L, int mode, int maxny) {
+  k_proj_sweep<<<GRID(L.n, L.cap), (2 * maxny + 31) / 32 * 32, 0, L.stream>>>(L.runs, L.items, L.n, mode);
 }
 void launch_proj_ifft2(const Launch& L, int mode, size_t smem) {
   k_proj_ifft2<<<GRID(L.n, L.cap), 256, smem, L.stream>>>(L.runs, L.items, L.n, mode);
@@ -1591,7 +1586,6 @@ cudaError_t set_smem_limits(int bytes) {
   if ((e = smem_limit(k_proj_xifft, bytes)) != cudaSuccess) return e;
   if ((e = smem_limit(k_sediment, bytes)) != cudaSuccess) return e;
   if ((e = smem_limit(k_proj_div_fft2, bytes)) != cudaSuccess) return e;
-  if ((e = smem_limit(k_proj_sweep, bytes)) != cudaSuccess) return e;
   if ((e = smem_limit(k_proj_ifft2, bytes)) != cudaSuccess) return e;
   if ((e = smem_limit(k_refine_residual<0, 0>, bytes)) != cudaSuccess) return e;
   if ((e = smem_limit(k_refine_residual<20, 8>, bytes)) != cudaSuccess) return e;

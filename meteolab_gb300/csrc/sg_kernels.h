@@ -30,7 +30,7 @@ void launch_proj_modes(const Launch& L, int mode, int maxnz, int maxny, int thre
 size_t layer_fft_smem(int maxnx, int maxny);
 size_t layer_fft_smem_run(int nx, int ny);  // the layer transforms' shared memory for one run's grid
 void launch_proj_div_fft2(const Launch& L, int mode, int set, size_t smem);
-void launch_proj_sweep(const Launch& L, int mode, int maxny, int maxnz);
+void launch_proj_sweep(const Launch& L, int mode, int maxny);
 void launch_proj_ifft2(const Launch& L, int mode, size_t smem);
 void launch_proj_xifft(const Launch& L, int mode, int yc, int maxnx);
 void launch_face_correct(const Launch& L, int set);

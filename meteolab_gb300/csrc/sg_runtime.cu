@@ -502,7 +502,7 @@ void enqueue_solve(sg_context* ctx, const Plan& P, int mode, int set, cudaStream
   const int h = mode == PROJ_FACE ? 2 : mode == PROJ_PRES ? 7 : 22;  // profile ids of the three stages
   if (P.layerfft) {
     launch_proj_div_fft2(rows, mode, set, P.fftSmem); hook(h);
-    launch_proj_sweep(modes, mode, P.maxny, P.maxnz); hook(h + 1);
+    launch_proj_sweep(modes, mode, P.maxny); hook(h + 1);
     launch_proj_ifft2(rows, mode, P.fftSmem); hook(h + 2);
   } else {
     const int mthreads = std::min(512, std::max(64, (2 * P.maxny + 31) / 32 * 32));
