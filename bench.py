@@ -5,8 +5,9 @@ One JSON line on rank 0. A "step" is one model time step (dt = 3 s) of every run
 Headline (`value`): the batched ensemble — 64 members on the standard 40x32x50 grid, seeded
 soundings, advanced together through one CUDA graph per step; inputs resident in HBM (213 MB per field set, larger
 than the 129 MB L2, so no flush is needed between steps). `e2e`: the same metric through the C ABI with host
-buffers: every step writes all members' fields from pinned host memory, steps, and reads them back (one
-sg_batch_step_io call a step, the members in four groups whose copies overlap the other groups' steps).
+buffers: every step writes all members' fields from pinned host memory, steps, and reads them back
+(sg_batch_step_round_trips over the timed steps, the members in four groups whose copies overlap the other groups'
+steps; beside it one sg_batch_step_io call a step, and separate write / step / read calls).
 Beside it: the plain single-run step on the standard, large (80x64x50) and stress (320x256x80) grids.
 `--impl reference`: the reference's algorithm on the host cores (the oracle port) on a bounded sample of the same
 workload (one member per host core, spun up like the GPU arm's), timed two ways (every step split over all threads;
@@ -163,6 +164,15 @@ def peaks():
         return float(p["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+def dram_profile():
+    """Per-kernel DRAM bytes and GB/s of one step from the committed ncu launch list, if there is one."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "step_dram_ensemble64.json")) as f:
+            return json.load(f)["kernels"]
+    except Exception:
+        return None
 
 
 def traffic_per_cell():
@@ -404,8 +414,9 @@ def main():
     launches_per_step = sum(v[1] for v in prof.values())
 
     # ---- e2e through the C ABI with a pinned host buffer: all fields of all runs written from it, one step, all read
-    # back into it, every step. Headline: one sg_batch_step_io call a step (the runs in E2E_GROUPS groups whose copies
-    # overlap the other groups' steps); beside it the same round trip as three separate calls (write, step, read).
+    # back into it, every step. Headline: sg_batch_step_round_trips over the timed steps (the runs in E2E_GROUPS groups
+    # whose copies overlap the other groups' steps, pipelined across steps); beside it one sg_batch_step_io call a step
+    # and the same round trip as three separate calls (write, step, read).
     packed = torch.empty(cells * len(CARRIED), dtype=torch.float32, pin_memory=True).numpy()
     ctx.read_packed(runs, packed)
     def e2e_serial():
@@ -425,7 +436,14 @@ def main():
             fn()
         e2e_s = allmax(pg, time.perf_counter() - t0)
         e2e_values[name] = cells * world * e2e_n / e2e_s
-    e2e_value = e2e_values["io"]
+    # the same round trip every step, e2e_n steps in one call: the groups pipeline across steps
+    ctx.batch_round_trips(runs, packed, steps=2, groups=E2E_GROUPS)
+    barrier(pg)
+    t0 = time.perf_counter()
+    ctx.batch_round_trips(runs, packed, steps=e2e_n, groups=E2E_GROUPS)
+    e2e_s = allmax(pg, time.perf_counter() - t0)
+    e2e_values["round_trips"] = cells * world * e2e_n / e2e_s
+    e2e_value = e2e_values["round_trips"]
     bytes_io = cells * 4 * len(CARRIED)
 
     # ---- plain single-run steps (eager launches and from a graph) on the standard, large and stress grids
@@ -484,7 +502,9 @@ def main():
                    "transport_copies": "TMA bulk copies by two producer warps" if bulk else "per-thread cp.async",
                    "l2": "inputs larger than L2 (213 MB per field set)", "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": "cell-steps/s", "h2d_bytes_per_step": bytes_io, "d2h_bytes_per_step": bytes_io,
-                "call": f"sg_batch_step_io, {E2E_GROUPS} groups", "serial_calls_value": e2e_values["serial"]},
+                "call": f"sg_batch_step_round_trips, {e2e_n} steps a call, every step's fields written from and read back to "
+                        f"pinned host memory, {E2E_GROUPS} groups", "call_a_step_value": e2e_values["io"],
+                "serial_calls_value": e2e_values["serial"]},
         "gpu_launches": launches_per_step * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm if achieved else None,
                      "traffic": tpc * cells if tpc else None, "kernel": "k_transport<WENO> (9 fields, one RK3 stage)", "peak_kind": peak_kind,
@@ -500,8 +520,11 @@ def main():
         "serving": serving,
         "serving_rates": serving_rates,
         "kernels_ms_per_launch": {k: round(v[0], 5) for k, v in prof.items()},
-        "kernels_hbm_gbs": {k: round(cells * KERNEL_BYTES_PER_CELL[k] / (v[0] * 1e-3) / 1e9, 1)
-                            for k, v in prof.items() if k in KERNEL_BYTES_PER_CELL and v[0] > 0},
+        # each kernel's algorithmic bytes over its event-timed launch (L2 hits can put a kernel above its DRAM rate)
+        "kernels_algorithmic_gbs": {k: round(cells * KERNEL_BYTES_PER_CELL[k] / (v[0] * 1e-3) / 1e9, 1)
+                                    for k, v in prof.items() if k in KERNEL_BYTES_PER_CELL and v[0] > 0},
+        # the measured DRAM bytes and GB/s of every kernel (ncu, profiles/step_launches_ensemble64.md)
+        "kernels_dram_ncu": dram_profile(),
     }
     print(json.dumps(line), flush=True)
 

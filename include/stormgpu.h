@@ -126,6 +126,13 @@ int sg_batch_read_packed(sg_context* ctx, const sg_run* runs, int n, uint32_t ma
  * buffer and a CUDA graph each, so one group's host copies overlap the other groups' steps; a run's results are the
  * same as with sg_batch_write_packed, sg_batch_step and sg_batch_read_packed. Returns when every group is done. */
 int sg_batch_step_io(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, float* host, int nsteps, int groups);
+/* The engine's round trip every step for nsteps steps in one call: each step writes the mask's fields of every run from
+ * `host`, advances one step and reads them back into `host`, so a step's inputs are the host buffer as the previous
+ * step left it (GpuDynamics.step, src/gpu/dynamics.ts:446-450, :488-497, called nsteps times). The groups (as in
+ * sg_batch_step_io) run as independent pipelines: one group's copies overlap the other groups' steps within and across
+ * steps, and the call pays its first write and last read once instead of every step. The same bits as nsteps calls
+ * of sg_batch_step_io with one step each. */
+int sg_batch_step_round_trips(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, float* host, int nsteps, int groups);
 /* precipitation, hailGround, hailSize: nx*ny each (nullable); src/core/model.ts:253, :262. */
 int sg_run_read_columns(sg_context* ctx, sg_run run, float* precipitation, float* hail_ground, float* hail_size);
 /* The same columns written (each pointer nullable: that column is left as it is). */

@@ -989,7 +989,10 @@ static int batch_packed(sg_context* ctx, const sg_run* runs, int n, uint32_t mas
 // groups, each with a stream, a part of the staging buffer and a graph of its own, so one group's copies overlap the
 // other groups' steps. Each group's runs step exactly as in any other batch (a run's results do not depend on the
 // runs beside it).
-static int batch_step_io(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, float* host, int nsteps, int groups) {
+// each_step: nsteps round trips (every step written from host, stepped once, read back into host; a group's next
+// write reads what its last read wrote), else one round trip around nsteps steps.
+static int batch_step_io(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, float* host, int nsteps, int groups,
+                         bool each_step = false) {
   if (!ctx || !host) return SG_ERR_INVALID;
   if (nsteps < 0) return fail(ctx, SG_ERR_INVALID, "negative step count");
   cudaSetDevice(ctx->device);
@@ -1030,11 +1033,14 @@ static int batch_step_io(sg_context* ctx, const sg_run* runs, int n, uint32_t ma
     float* dev = ctx->staging + x.off;
     const Launch L{ctx->d_runs, x.items.first, x.items.second, ctx->sms * 8, s};
     CK(cudaStreamWaitEvent(s, ctx->ioEv[sg_context::IO_GROUPS], 0));
-    CK(cudaMemcpyAsync(dev, host + x.off, x.total * 4, cudaMemcpyHostToDevice, s));
-    launch_pack(L, dev, 1);
-    for (int k = 0; k < nsteps; k++) CK(cudaGraphLaunch(x.P->exec, s));
-    launch_pack(L, dev, 0);
-    CK(cudaMemcpyAsync(host + x.off, dev, x.total * 4, cudaMemcpyDeviceToHost, s));
+    const int trips = each_step ? nsteps : 1, inner = each_step ? 1 : nsteps;
+    for (int r = 0; r < trips; r++) {
+      CK(cudaMemcpyAsync(dev, host + x.off, x.total * 4, cudaMemcpyHostToDevice, s));
+      launch_pack(L, dev, 1);
+      for (int k = 0; k < inner; k++) CK(cudaGraphLaunch(x.P->exec, s));
+      launch_pack(L, dev, 0);
+      CK(cudaMemcpyAsync(host + x.off, dev, x.total * 4, cudaMemcpyDeviceToHost, s));
+    }
     CK(cudaEventRecord(ctx->ioEv[g], s));
     CK(cudaStreamWaitEvent(ctx->stream, ctx->ioEv[g], 0));
   }
@@ -1308,6 +1314,9 @@ int sg_batch_read_packed(sg_context* ctx, const sg_run* runs, int n, uint32_t ma
 }
 int sg_batch_step_io(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, float* host, int nsteps, int groups) {
   return batch_step_io(ctx, runs, n, mask, host, nsteps, groups);
+}
+int sg_batch_step_round_trips(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, float* host, int nsteps, int groups) {
+  return batch_step_io(ctx, runs, n, mask, host, nsteps, groups, true);
 }
 
 int sg_run_retire(sg_context* ctx, sg_run run) {

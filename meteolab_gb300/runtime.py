@@ -114,6 +114,7 @@ def load():
             L.sg_electric_destroy.argtypes = [vp]
             L.sg_batch_read_packed.argtypes = [vp, C.POINTER(C.c_int32), i32, C.c_uint32, _FP]
             L.sg_batch_step_io.argtypes = [vp, C.POINTER(C.c_int32), i32, C.c_uint32, _FP, i32, i32]
+            L.sg_batch_step_round_trips.argtypes = [vp, C.POINTER(C.c_int32), i32, C.c_uint32, _FP, i32, i32]
             L.sg_set_transport_shape.argtypes = [vp, i32, i32, i32]
             L.sg_divergence_max_static.argtypes = [i32, vp, vp, vp, i32, i32, i32, C.c_double, C.c_double, C.POINTER(C.c_double),
                                                    C.POINTER(C.c_double), vp, C.POINTER(C.c_double), C.c_char_p, C.c_size_t]
@@ -273,6 +274,18 @@ class Context:
         ids = (C.c_int32 * len(runs))(*[r.id for r in runs])
         self.check(load().sg_batch_step_io(self.h, ids, len(runs), self._mask(names), packed.ctypes.data_as(_FP), steps, groups),
                    "batch step io")
+        for r in runs:
+            r.time += steps * r.spec.switches.dt
+
+    def batch_round_trips(self, runs: Sequence["Run"], packed: np.ndarray, steps: int = 1, groups: int = 4,
+                          names: Iterable[str] = CARRIED):
+        """`steps` steps with the round trip every step (sg_batch_step_round_trips): each step writes the runs' fields
+        from `packed`, advances one step and reads them back into it; the groups pipeline independently."""
+        if packed.dtype != np.float32 or not packed.flags.c_contiguous:
+            raise ValueError("packed buffer must be contiguous float32")
+        ids = (C.c_int32 * len(runs))(*[r.id for r in runs])
+        self.check(load().sg_batch_step_round_trips(self.h, ids, len(runs), self._mask(names), packed.ctypes.data_as(_FP), steps,
+                                                    groups), "batch round trips")
         for r in runs:
             r.time += steps * r.spec.switches.dt
 

@@ -326,6 +326,28 @@ def test_step_with_host_io_matches_separate_calls(ctx, storm, groups, pinned):
         r.retire()
 
 
+@pytest.mark.parametrize("groups", [1, 3])
+def test_round_trips_every_step_match_one_call_a_step(ctx, storm, groups):
+    """sg_batch_step_round_trips (a round trip through the host buffer every step, the groups pipelined across steps)
+    gives the bits of one sg_batch_step_io call a step, over three steps of an uneven batch."""
+    large = baseline_run(create_grid(LARGE_GRID), seed=13)
+    specs = [storm, large, storm, large, storm]
+    a = [ctx.create(s) for s in specs]
+    b = [ctx.create(s) for s in specs]
+    total = sum(r.grid.n for r in a) * len(CARRIED)
+    pa = np.empty(total, np.float32)
+    ctx.read_packed(a, pa)
+    pb = pa.copy()
+    for _ in range(3):
+        ctx.batch_step_io(a, pa, steps=1, groups=groups)
+    ctx.batch_round_trips(b, pb, steps=3, groups=groups)
+    assert np.array_equal(pa, pb)
+    for x, y in zip(a, b):
+        assert x.status()["steps"] == y.status()["steps"] == 3
+    for r in a + b:
+        r.retire()
+
+
 def test_autotuner_picks_a_valid_shape(ctx, storm):
     runs = [ctx.create(storm) for _ in range(4)]
     tx, ty, g, mb = ctx.transport_shape(runs)
