@@ -74,6 +74,13 @@ class Switches:
     # needs no refinement and ignores it
     refine_projection: int = 1
     rotation: int = 1   # the rotation tracking after every step (afterStep) and the swaths, on the device
+    ice: int = 1        # the ice microphysics (the warm scheme when 0)
+    # electrification and lightning (SimConfig.lightning; with the ice microphysics only, src/core/model.ts:1316): the
+    # four charge carriers, the charging in the physics and the flashes after every step; corona from the ground (over
+    # land, not over water); the lightning's seed (config.seed + 1, :1538)
+    lightning: int = 0
+    corona: int = 1
+    lightning_seed: int = 43
 
     def drag_cd(self, grid: Grid) -> float:
         return drag_coefficient(self.surface, 2 * float(grid.hz[0])) if self.drag else 0.0

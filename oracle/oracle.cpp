@@ -6,6 +6,17 @@
 using namespace orc;
 
 namespace {
+struct LightningHandle {
+  GridSpec g; std::unique_ptr<Lightning> l; std::vector<Flash> flashes;
+};
+
+void copyFlash(const Flash& f, double* out, int* nodes, int* parent, int* polarity, double* strokes, int cap) {
+  const double v[9] = {f.time, f.cg ? 1.0 : 0.0, (double)f.start, (double)f.ground, f.potential, f.charge, f.moment, (double)f.nodes.size(), (double)f.strokes.size()};
+  for (int k = 0; k < 9; k++) out[k] = v[k];
+  for (int c = 0; c < (int)f.nodes.size() && c < cap; c++) { if (nodes) nodes[c] = f.nodes[c]; if (parent) parent[c] = f.parent[c]; if (polarity) polarity[c] = f.polarity[c]; }
+  if (strokes) for (size_t k = 0; k < f.strokes.size() && k < 8; k++) strokes[k] = f.strokes[k];
+}
+
 struct Handle {
   bool fp64;
   Model<float>* m32 = nullptr;
@@ -36,6 +47,7 @@ template <class S> std::vector<S>* extraField(Model<S>* m, int id) {
     case 100: return &m->precipitation; case 101: return &m->hailGround; case 102: return &m->hailSize;
     case 103: return &m->fallRain; case 104: return &m->fallSnow; case 105: return &m->fallGraupel; case 106: return &m->fallHail;
     case 107: return &m->condensate;
+    case 108: return &m->fallChargeIce; case 109: return &m->fallChargeGraupel; case 110: return &m->fieldZ;
   }
   return (id >= 0 && id < N_CARRIED) ? &m->f[id] : nullptr;
 }
@@ -58,8 +70,9 @@ void orc_set_threads(void* p, int threads) {
   if (h->m32) h->m32->nthreads = std::min(threads, (int)h->m32->dscr.size());
   if (h->m64) h->m64->nthreads = std::min(threads, (int)h->m64->dscr.size());
 }
-// Field ids: 0..12 carried (rain, snow, graupel, hail, u, v, w, theta, q, cloud, ice, iceNumber, cold); 100 precipitation,
-// 101 hailGround, 102 hailSize, 103-106 fall speeds, 107 condensate.
+// Field ids: 0..16 carried (rain, snow, graupel, hail, u, v, w, theta, q, cloud, ice, iceNumber, cold, chargeIce,
+// chargeGraupel, chargeRain, chargeAir); 100 precipitation, 101 hailGround, 102 hailSize, 103-106 fall speeds,
+// 107 condensate, 108-109 the charge carriers' fall speeds, 110 the vertical field (fieldZ).
 int orc_set_field(void* p, int id, const double* src, long count) {
   Handle* h = (Handle*)p;
   if (h->m32) { auto* v = extraField(h->m32, id); if (!v || (long)v->size() != count) return -1; for (long i = 0; i < count; i++) (*v)[i] = (float)src[i]; }
@@ -130,7 +143,9 @@ void orc_step_part(void* p, double dt, int part) {
 }
 int orc_get_pressure(void* p, double* dst, long count) {
   Handle* h = (Handle*)p; auto& v = h->m32 ? h->m32->pressure : h->m64->pressure;
-  if ((long)v.size() != count) return -1; std::memcpy(dst, v.data(), count * sizeof(double)); return 0;
+  if ((long)v.size() != count) return -1;
+  std::memcpy(dst, v.data(), count * sizeof(double));
+  return 0;
 }
 int orc_get_faces(void* p, double* mx, double* my, double* mz, double* dv, long count) {
   Handle* h = (Handle*)p; FluxTransport& f = h->m32 ? h->m32->flux : h->m64->flux;
@@ -144,6 +159,91 @@ void orc_counters(void* p, double* out) {
   auto fill = [&](auto* m) { out[0] = m->clipped; out[1] = m->negativeFilled; for (int k = 0; k < 4; k++) out[2 + k] = m->water[k]; out[6] = m->time; };
   if (h->m32) fill(h->m32); else fill(h->m64);
 }
+
+// Electrification and lightning (SimConfig.lightning; with ice only). seed: the lightning's (config.seed + 1).
+void orc_set_lightning(void* p, int on, int corona, int seed) {
+  Handle* h = (Handle*)p;
+  auto set = [&](auto* m) { m->sw.lightning = on != 0; m->sw.corona = corona != 0; m->sw.lightningSeed = seed; };
+  if (h->m32) set(h->m32); else set(h->m64);
+}
+// out[11]: chargeGround, separated, ic, cgNegative, cgPositive, precipitation, conduction, flashes IC, flashes CG,
+// totalCharge, flashes of the last step.
+void orc_charge_state(void* p, double* out) {
+  Handle* h = (Handle*)p;
+  auto fill = [&](auto* m) {
+    const double v[11] = {m->chargeGround, m->chargeSeparated, m->chargeIC, m->chargeCgNegative, m->chargeCgPositive, m->chargePrecipitation,
+                          m->chargeConduction, (double)m->flashesIC, (double)m->flashesCG, m->totalCharge(), (double)m->lastFlashes.size()};
+    for (int k = 0; k < 11; k++) out[k] = v[k];
+  };
+  if (h->m32) fill(h->m32); else fill(h->m64);
+}
+// Flash k of the last step: out[9] = time, cg, start, ground, potential, charge, moment, nodes, strokes; the channel
+// (nodes, parent, polarity; up to cap) and the strokes' charges (up to 8). Returns -1 past the end.
+int orc_flash(void* p, int k, double* out, int* nodes, int* parent, int* polarity, double* strokes, int cap) {
+  Handle* h = (Handle*)p;
+  const std::vector<Flash>& f = h->m32 ? h->m32->lastFlashes : h->m64->lastFlashes;
+  if (k < 0 || k >= (int)f.size()) return -1;
+  copyFlash(f[k], out, nodes, parent, polarity, strokes, cap);
+  return 0;
+}
+
+// ---------------------------------------------------------------- Lightning on its own (src/core/lightning.test.ts)
+void* orc_lightning_create(int nx, int ny, int nz, double dx, double dy, double dz, double height, const double* zs, const double* dzs, const double* hz,
+                           const double* air, int seed) {
+  auto* L = new LightningHandle;
+  L->g = makeGrid(nx, ny, nz, dx, dy, dz, height, zs, dzs, hz);
+  L->l = std::make_unique<Lightning>(L->g, air, seed);
+  return L;
+}
+void orc_lightning_destroy(void* p) { delete (LightningHandle*)p; }
+void orc_lightning_set_corona(void* p, int on) { ((LightningHandle*)p)->l->corona = on != 0; }
+// cloud(): the sum of `count` FP32 fields of n nodes each (fields[k] points to field k).
+void orc_lightning_cloud(void* p, float** fields, int count) {
+  auto* L = (LightningHandle*)p; std::vector<Arr<float>> a(count);
+  for (int k = 0; k < count; k++) a[k] = (Arr<float>)fields[k];
+  L->l->cloud(a.data(), count);
+}
+void orc_lightning_solve(void* p, float** carriers) {
+  auto* L = (LightningHandle*)p; Arr<float> a[4] = {(Arr<float>)carriers[0], (Arr<float>)carriers[1], (Arr<float>)carriers[2], (Arr<float>)carriers[3]};
+  L->l->solve(a, 4);
+}
+int orc_lightning_strongest(void* p, int stamp, double* ratio) { auto r = ((LightningHandle*)p)->l->strongest(stamp); *ratio = r.second; return r.first; }
+int orc_lightning_discharge(void* p, float** carriers, double time, int limit) {
+  auto* L = (LightningHandle*)p; Arr<float> a[4] = {(Arr<float>)carriers[0], (Arr<float>)carriers[1], (Arr<float>)carriers[2], (Arr<float>)carriers[3]};
+  L->flashes = L->l->discharge(a, 4, time, limit);
+  return (int)L->flashes.size();
+}
+int orc_lightning_flash(void* p, int k, double* out, int* nodes, int* parent, int* polarity, double* strokes, int cap) {
+  auto* L = (LightningHandle*)p;
+  if (k < 0 || k >= (int)L->flashes.size()) return -1;
+  copyFlash(L->flashes[k], out, nodes, parent, polarity, strokes, cap);
+  return 0;
+}
+double orc_lightning_conduct(void* p, float* ions, double dt) { return ((LightningHandle*)p)->l->conduct((Arr<float>)ions, dt); }
+// phi (n), rho (n) of the last solve; state[2] = fromGround, conducted.
+void orc_lightning_fields(void* p, double* phi, double* rho, double* state) {
+  auto* L = (LightningHandle*)p;
+  if (phi) std::memcpy(phi, L->l->phi.data(), L->l->phi.size() * 8);
+  if (rho) std::memcpy(rho, L->l->rho.data(), L->l->rho.size() * 8);
+  if (state) { state[0] = L->l->fromGround; state[1] = L->l->conducted; }
+}
+int orc_flash_limit(double dt) { return flashLimit(dt); }
+
+// ---------------------------------------------------------------- charging (src/core/charge.test.ts)
+double orc_critical_rar(double tc) { return criticalRar(tc); }
+double orc_collision_charge(double tc, double rar, double d, double v, int signedCoefficients) { return collisionCharge(tc, rar, d, v, signedCoefficients != 0); }
+double orc_crystal_number(double tc, double qi, double rho) { return crystalNumber(tc, qi, rho); }
+double orc_crystal_diameter(double qi, double rho, double tc) { return crystalDiameter(qi, rho, tc); }
+double orc_takahashi(double tc, double lwc) { return takahashiCharge(tc, lwc); }
+// crystals < 0: not given (estimated from the mass); tak 1: the Takahashi scheme, 0: Saunders-Peck.
+double orc_charging_rate(double tc, double rho, double cloud, double ice, double snow, double graupel, double hail, double snowFall, int wetG, int wetH,
+                         double crystals, int tak) {
+  return chargingRate(tc, rho, cloud, ice, snow, graupel, hail, snowFall, wetG != 0, wetH != 0, crystals, tak != 0);
+}
+double orc_inductive_rate(double tc, double rho, double cloud, double graupel, double hail, double ez, double rimerCharge, int wetG, int wetH) {
+  return inductiveRate(tc, rho, cloud, graupel, hail, ez, rimerCharge, wetG != 0, wetH != 0);
+}
+void orc_transfer_charge(double* charge, const double* before, const double* after) { transferCharge(charge, before, after); }
 
 // ---------------------------------------------------------------- known-answer hooks (reference unit tests)
 double orc_weno(double a, double b, double c, double d, double e) { return weno(a, b, c, d, e); }

@@ -7,6 +7,7 @@
 #pragma once
 #include <omp.h>
 #include "oracle_solvers.h"
+#include "oracle_elec.h"
 
 namespace orc {
 
@@ -16,9 +17,14 @@ struct Switches {
   bool loading = true, evaporation = true, rainFormation = true, anisotropic = true, verticalDz = false, durranKlemp = false;
   bool pressureInStages = true, ice = true, surfaceOn = true;
   int slabs = 1;
+  // Electrification and lightning (SimConfig.lightning, with the ice microphysics only: electrified(), model.ts:1316);
+  // the lightning's random numbers are seeded with config.seed + 1 (:1538); corona over land (:1539).
+  bool lightning = false, corona = true;
+  int lightningSeed = 43;
 };
 
-enum FieldId { F_RAIN, F_SNOW, F_GRAUPEL, F_HAIL, F_U, F_V, F_W, F_THETA, F_Q, F_CLOUD, F_ICE, F_ICENUMBER, F_COLD, N_CARRIED };
+enum FieldId { F_RAIN, F_SNOW, F_GRAUPEL, F_HAIL, F_U, F_V, F_W, F_THETA, F_Q, F_CLOUD, F_ICE, F_ICENUMBER, F_COLD,
+               F_CHARGE_ICE, F_CHARGE_GRAUPEL, F_CHARGE_RAIN, F_CHARGE_AIR, N_CARRIED };  // charges: src/core/model.ts:210
 
 // The microphysics part of physics(z) for node i (src/core/model.ts:1391-1471): Kessler rain, then with ice the
 // freezing, crystals, snow, graupel, hail, secondary ice and the mixed-phase saturation adjustment, else the warm
@@ -59,6 +65,13 @@ template <class S> struct Model {
   Switches sw;
   std::vector<S> f[N_CARRIED];
   std::vector<S> fallRain, fallSnow, fallGraupel, fallHail, condensate, precipitation, hailGround, hailSize, levelWater;
+  // electrification (src/core/model.ts:205-245): the carriers' fall speeds, the vertical field of the last solve, the
+  // charge separated per level; the ground's charge, the budget, the flash counts and this step's flashes
+  std::vector<S> fallChargeIce, fallChargeGraupel, fieldZ, levelCharge;
+  double chargeGround = 0, chargeSeparated = 0, chargeIC = 0, chargeCgNegative = 0, chargeCgPositive = 0, chargePrecipitation = 0, chargeConduction = 0;
+  long flashesIC = 0, flashesCG = 0;
+  std::vector<Flash> lastFlashes;
+  std::unique_ptr<Lightning> lightning;
   std::vector<S> stageStart[N_CARRIED]; std::vector<double> stageTend[N_CARRIED];
   FluxTransport flux; PressureSolver solver; Turbulence turb;
   std::vector<double> pressure, divergence;
@@ -81,6 +94,7 @@ template <class S> struct Model {
     for (int k = 0; k < N_CARRIED; k++) { f[k].assign(n, 0); stageStart[k].assign(n, 0); stageTend[k].assign(n, 0); }
     fallRain.assign(n, 0); fallSnow.assign(n, 0); fallGraupel.assign(n, 0); fallHail.assign(n, 0); condensate.assign(n, 0);
     precipitation.assign(layer, 0); hailGround.assign(layer, 0); hailSize.assign(layer, 0); levelWater.assign(nz * 4, 0);
+    fallChargeIce.assign(n, 0); fallChargeGraupel.assign(n, 0); fieldZ.assign(n, 0); levelCharge.assign(nz, 0);
     flux = FluxTransport(g, rho.data()); solver = PressureSolver(g, rho.data()); turb = Turbulence(g, rho.data());
     flux.g = &g; solver.g = &g; turb.g = &g;
     turb.anisotropic = sw.anisotropic; turb.verticalDz = sw.verticalDz; turb.durranKlemp = sw.durranKlemp;
@@ -111,8 +125,10 @@ template <class S> struct Model {
     c.push_back({F_Q, true, true, 1}); c.push_back({F_CLOUD, true, true, 1});
     if (sw.ice) { c.push_back({F_ICE, true, true, 1}); c.push_back({F_ICENUMBER, true, false, 1}); }
     c.push_back({F_COLD, true, false, .9992});
+    if (electrified()) for (int k : {F_CHARGE_ICE, F_CHARGE_GRAUPEL, F_CHARGE_RAIN, F_CHARGE_AIR}) c.push_back({k, true, false, 1});  // :1331
     return c;
   }
+  bool electrified() const { return sw.ice && sw.lightning; }  // :1316
 
   // ---------------------------------------------------------- beginStep (src/core/model.ts:893-902)
   void updateGround() {  // :644-657 (the surface pattern, city and zones are zero in the device's configuration)
@@ -136,6 +152,14 @@ template <class S> struct Model {
       fr[i] = fallSpeed(rain[i], rho[k], rho[0]); fs[i] = snowFallSpeed(snow[i], rho[k], rho[0]);
       fg[i] = graupelFallSpeed(graupel[i], rho[k]); fh[i] = hailFallSpeed(hail[i], rho[k]);
     }
+    if (electrified()) {  // :1230-1234
+      Arr<S> ice = F(F_ICE), ci = A(fallChargeIce), cg = A(fallChargeGraupel);
+      for (int i = k * layer, end = i + layer; i < end; i++) {
+        double is = (double)ice[i] + (double)snow[i], gh = (double)graupel[i] + (double)hail[i];
+        ci[i] = is > 0 ? (double)snow[i] * (double)fs[i] / is : 0;
+        cg[i] = gh > 0 ? ((double)graupel[i] * (double)fg[i] + (double)hail[i] * (double)fh[i]) / gh : 0;
+      }
+    }
   }
   void collectHail(double dt) {  // :697-706
     int layer = g.layer; Arr<S> hail = F(F_HAIL), fh = A(fallHail), hs = A(hailSize);
@@ -152,9 +176,15 @@ template <class S> struct Model {
     for (int z = 0; z < nz; z++) { double c = dt * rho[z] / (levelWeight[z] * g.dz); for (int i = z * layer; i < (z + 1) * layer; i++) if ((double)rain[i] != 0) courant = jmax(courant, c * (double)vt[i] / 1); }
     return (int)jmax(1, std::ceil(courant / .8));
   }
-  void sedimentPart(Arr<S> rain, Arr<S> vt, double dt) {  // :582-598 (flat ground, water deposited)
+  void sedimentPart(Arr<S> rain, Arr<S> vt, double dt, bool water = true) {  // :582-598 (flat ground)
     int nz = g.nz, layer = g.layer;
-    for (int c = 0; c < layer; c++) deposit(c, rho[0] * (double)rain[c] * (double)vt[c] * dt, precipitation);
+    if (water) for (int c = 0; c < layer; c++) deposit(c, rho[0] * (double)rain[c] * (double)vt[c] * dt, precipitation);
+    else {  // a charge carrier: what falls through the ground goes to the ground's charge (:588-591)
+      double out = 0;
+      for (int i = 0; i < layer; i++) out += (double)rain[i] * (double)vt[i];
+      out *= rho[0];
+      double q = out * dt * g.dx * g.dy; chargeGround += q; chargePrecipitation += q;
+    }
     run(64, [&](int part, int) {
       int c0 = (int)((long)part * layer / 64), c1 = (int)((long)(part + 1) * layer / 64);
       for (int z = 0; z < nz; z++) {
@@ -170,6 +200,14 @@ template <class S> struct Model {
       Arr<S> field = F(falls[j].first), vt = A(*falls[j].second);
       int parts = fallParts(field, vt, dt);
       for (int q = 0; q < parts; q++) sedimentPart(field, vt, dt / parts);
+    }
+    if (electrified()) {  // chargeFalls (:562), :931
+      std::pair<int, std::vector<S>*> charges[3] = {{F_CHARGE_ICE, &fallChargeIce}, {F_CHARGE_GRAUPEL, &fallChargeGraupel}, {F_CHARGE_RAIN, &fallRain}};
+      for (auto& cf : charges) {
+        Arr<S> field = F(cf.first), vt = A(*cf.second);
+        int parts = fallParts(field, vt, dt);
+        for (int q = 0; q < parts; q++) sedimentPart(field, vt, dt / parts, false);
+      }
     }
   }
   void beginStep(double dt) {
@@ -267,9 +305,25 @@ template <class S> struct Model {
     Arr<S> ice = F(F_ICE), iceNumber = F(F_ICENUMBER), snow = F(F_SNOW), graupel = F(F_GRAUPEL), hail = F(F_HAIL);
     double rhoGround = rho[0], f = sw.coriolis, keep = std::exp(-sw.windRelaxation * dt), H = g.height;
     double alt = g.zs[z], pz = p[z], rhoZ = rho[z], ex = exner[z], ue = uEnv[z], ve = vEnv[z], thEnv = thetaEnv[z];
+    const bool electric = electrified(); double wCharge = 0;
+    Arr<S> cI = F(F_CHARGE_ICE), cG = F(F_CHARGE_GRAUPEL), cR = F(F_CHARGE_RAIN), cA = F(F_CHARGE_AIR), snowFall = A(fallSnow), ez = A(fieldZ);
     for (int y = 0; y < ny; y++) for (int x = 0, i = z * layer + y * nx; x < nx; x++, i++) {
       double q0 = q[i];
+      double before[4] = {0, 0, 0, 0};
+      if (electric) { before[0] = (double)ice[i] + (double)snow[i]; before[1] = (double)graupel[i] + (double)hail[i]; before[2] = rain[i]; before[3] = cloud[i]; }
       double evap = microphysicsNode<S>(theta, q, cloud, rain, cold, ice, iceNumber, snow, graupel, hail, i, ex, pz, rhoZ, rhoGround, dt, sw);
+      if (electric) {  // :1454-1469 (after the microphysics' last change to the carriers; only cold changes after it there)
+        double after[4] = {(double)ice[i] + (double)snow[i], (double)graupel[i] + (double)hail[i], (double)rain[i], (double)cloud[i]};
+        double now[4] = {cI[i], cG[i], cR[i], cA[i]};
+        if (now[0] != 0 || now[1] != 0 || now[2] != 0 || now[3] != 0) transferCharge(now, before, after);
+        double tc = (double)theta[i] * ex - 273.15;
+        bool wetG = wetGrowing(graupel[i], N0G, RHO_G, tc, q[i], pz, rhoZ, cloud[i], rain[i], ice[i], snow[i]);
+        bool wetH = wetGrowing(hail[i], N0H, RHO_H, tc, q[i], pz, rhoZ, cloud[i], rain[i], ice[i], snow[i]);
+        double separated = chargingRate(tc, rhoZ, cloud[i], ice[i], snow[i], graupel[i], hail[i], snowFall[i], wetG, wetH, (double)iceNumber[i] * rhoZ, true) * dt / rhoZ;
+        double induced = inductiveRate(tc, rhoZ, cloud[i], graupel[i], hail[i], ez[i], (now[1] + separated) * rhoZ, wetG, wetH) * dt / rhoZ;
+        cI[i] = now[0] - separated; cG[i] = now[1] + separated + induced; cR[i] = now[2]; cA[i] = now[3] - induced;
+        wCharge += std::fabs(separated) + std::fabs(induced);
+      }
       if (!sw.pressureInStages) {
         double thvEnv = thEnv * (1 + .61 * qEnv[z]);
         double buoy = ((double)theta[i] * (1 + .61 * (double)q[i]) - thvEnv) / thvEnv - (double)cloud[i] - (double)ice[i] - (sw.loading ? (double)rain[i] + (double)snow[i] + (double)graupel[i] + (double)hail[i] : 0);
@@ -293,6 +347,7 @@ template <class S> struct Model {
     if (sw.ice) for (int i = z * layer, e = i + layer; i < e; i++) cnd[i] = (double)cloud[i] + (double)ice[i];
     Arr<S> lw = A(levelWater); int l4 = z * 4;
     lw[l4] = wCond * nodeMass; lw[l4 + 1] = wEvap * nodeMass; lw[l4 + 2] = wRain * nodeMass; lw[l4 + 3] = wSurf * nodeMass;
+    A(levelCharge)[z] = wCharge * nodeMass;
   }
   void physicsStep(double dt) {  // :1116-1127
     std::vector<Carried> c = carried();
@@ -304,6 +359,7 @@ template <class S> struct Model {
     for (size_t k = 0; k < c.size(); k++) if (c[k].conserve) negativeFilled += taskNegative[k];
     run(g.nz, [&](int z, int) { physics(z, dt); });
     for (int k = 0; k < g.nz * 4; k += 4) { water[0] += (double)levelWater[k]; water[1] += (double)levelWater[k + 1]; water[2] += (double)levelWater[k + 2]; water[3] += (double)levelWater[k + 3]; }
+    for (int z = 0; z < g.nz; z++) chargeSeparated += (double)levelCharge[z];  // :1126
   }
   void mixStep(double dt) {  // :1161-1195 (flat ground)
     int nz = g.nz, layer = g.layer;
@@ -325,6 +381,39 @@ template <class S> struct Model {
     physicsStep(dt);
     mixStep(dt);
     project(dt, true);
+    if (electrified()) discharge(dt);  // afterStep (:1130-1133): the rotation tracking there changes no field
+  }
+  // :1537-1552: flashes where the field exceeds the breakdown threshold, then the ion conduction and the corona, then
+  // the vertical field of the last solve for the next step's inductive charging.
+  void discharge(double dt) {
+    if (!lightning) lightning = std::make_unique<Lightning>(g, rho.data(), sw.lightningSeed);
+    lightning->corona = sw.corona;
+    Arr<S> clouds[3] = {F(F_CLOUD), F(F_ICE), F(F_SNOW)};
+    lightning->cloud(clouds, 3);
+    Arr<S> carriers[4] = {F(F_CHARGE_ICE), F(F_CHARGE_GRAUPEL), F(F_CHARGE_RAIN), F(F_CHARGE_AIR)};
+    lastFlashes = lightning->discharge(carriers, 4, time + dt, flashLimit(dt));
+    for (const Flash& f : lastFlashes) {
+      if (f.cg) { chargeGround += f.charge; flashesCG++; if (f.charge < 0) chargeCgNegative += f.charge; else chargeCgPositive += f.charge; }
+      else { flashesIC++; chargeIC += std::fabs(f.charge); }
+    }
+    double conducted = lightning->conduct(F(F_CHARGE_AIR), dt);
+    chargeGround += conducted; chargeConduction += conducted;
+    int nz = g.nz, layer = g.layer; Arr<S> ez = A(fieldZ); const double* phi = lightning->phi.data();
+    for (int z = 1; z < nz - 1; z++) {
+      double h = g.zs[z + 1] - g.zs[z - 1];
+      for (int c = 0, i = z * layer; c < layer; c++, i++) ez[i] = -(phi[i + layer] - phi[i - layer]) / h;
+    }
+  }
+  // Total charge, C (:1555-1560): the four carriers summed with each node's air mass.
+  double totalCharge() {
+    int nz = g.nz, layer = g.layer; double total = 0;
+    Arr<S> a = F(F_CHARGE_ICE), b = F(F_CHARGE_GRAUPEL), c = F(F_CHARGE_RAIN), d = F(F_CHARGE_AIR);
+    for (int z = 0, i = 0; z < nz; z++) {
+      double s = 0;
+      for (int e = i + layer; i < e; i++) s += (double)a[i] + (double)b[i] + (double)c[i] + (double)d[i];
+      total += s * rho[z] * g.dx * g.dy * g.hz[z];
+    }
+    return total;
   }
   void step(double dt) { beginStep(dt); dynamics(dt); endStep(dt); }
 };

@@ -17,8 +17,10 @@ _lock = threading.Lock()
 _lib = None
 
 CARRIED = ("rain", "snow", "graupel", "hail", "u", "v", "w", "theta", "q", "cloud", "ice", "iceNumber", "cold")
+CHARGES = ("chargeIce", "chargeGraupel", "chargeRain", "chargeAir")
 EXTRA = {"precipitation": 100, "hailGround": 101, "hailSize": 102, "fallSpeed": 103, "snowFall": 104,
-         "graupelFall": 105, "hailFall": 106, "condensate": 107}
+         "graupelFall": 105, "hailFall": 106, "condensate": 107, "chargeFallIce": 108, "chargeFallGraupel": 109,
+         "fieldZ": 110}
 
 _d = C.POINTER(C.c_double)
 _f = C.POINTER(C.c_float)
@@ -26,7 +28,8 @@ _f = C.POINTER(C.c_float)
 
 def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (plain g++/OpenMP)."""
-    sources = [os.path.join(HERE, n) for n in ("oracle.cpp", "oracle_core.h", "oracle_solvers.h", "oracle_model.h", "oracle_diag.h")]
+    sources = [os.path.join(HERE, n) for n in ("oracle.cpp", "oracle_core.h", "oracle_solvers.h", "oracle_model.h", "oracle_diag.h",
+                                               "oracle_elec.h", os.path.join("..", "meteolab_gb300", "csrc", "sg_takahashi.h"))]
     if force or not os.path.exists(LIB_PATH) or any(os.path.getmtime(s) > os.path.getmtime(LIB_PATH) for s in sources):
         subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
     return LIB_PATH
@@ -78,6 +81,33 @@ def lib():
             L.orc_transport.argtypes = grid_args + [_d, _f, _f, _f, _f, C.c_double, C.c_int, C.c_int, _d, _d, _d, _d]
             L.orc_turbulence.argtypes = grid_args + [_d, _f, _f, _f, _f, _d, C.c_double, C.c_double, _f, _f, _d, C.c_int,
                                                      C.c_int, C.c_int, C.c_int, _d, _d, _d, _d, _f, _d, C.c_double, C.c_int]
+            L.orc_set_lightning.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
+            L.orc_charge_state.argtypes = [C.c_void_p, _d]
+            _i = C.POINTER(C.c_int)
+            L.orc_flash.argtypes = [C.c_void_p, C.c_int, _d, _i, _i, _i, _d, C.c_int]
+            L.orc_lightning_create.restype = C.c_void_p
+            L.orc_lightning_create.argtypes = grid_args + [_d, C.c_int]
+            L.orc_lightning_destroy.argtypes = [C.c_void_p]
+            L.orc_lightning_set_corona.argtypes = [C.c_void_p, C.c_int]
+            L.orc_lightning_cloud.argtypes = [C.c_void_p, C.POINTER(_f), C.c_int]
+            L.orc_lightning_solve.argtypes = [C.c_void_p, C.POINTER(_f)]
+            L.orc_lightning_strongest.argtypes = [C.c_void_p, C.c_int, _d]
+            L.orc_lightning_discharge.argtypes = [C.c_void_p, C.POINTER(_f), C.c_double, C.c_int]
+            L.orc_lightning_flash.argtypes = [C.c_void_p, C.c_int, _d, _i, _i, _i, _d, C.c_int]
+            L.orc_lightning_conduct.restype = C.c_double
+            L.orc_lightning_conduct.argtypes = [C.c_void_p, _f, C.c_double]
+            L.orc_lightning_fields.argtypes = [C.c_void_p, _d, _d, _d]
+            L.orc_flash_limit.argtypes = [C.c_double]
+            for name, nargs in (("orc_critical_rar", 1), ("orc_crystal_number", 3), ("orc_crystal_diameter", 3), ("orc_takahashi", 2)):
+                getattr(L, name).restype = C.c_double
+                getattr(L, name).argtypes = [C.c_double] * nargs
+            L.orc_collision_charge.restype = C.c_double
+            L.orc_collision_charge.argtypes = [C.c_double] * 4 + [C.c_int]
+            L.orc_charging_rate.restype = C.c_double
+            L.orc_charging_rate.argtypes = [C.c_double] * 8 + [C.c_int, C.c_int, C.c_double, C.c_int]
+            L.orc_inductive_rate.restype = C.c_double
+            L.orc_inductive_rate.argtypes = [C.c_double] * 7 + [C.c_int, C.c_int]
+            L.orc_transfer_charge.argtypes = [_d, _d, _d]
             _lib = L
     return _lib
 
@@ -103,7 +133,8 @@ def switch_vector(sw, grid, slabs: int = 1) -> np.ndarray:
     """The oracle's 20 switches from a ``meteolab_gb300.scenarios.Switches``."""
     return np.array([sw.coriolis, sw.wind_relaxation, sw.sponge_rate, sw.sponge_start, sw.cs, sw.drag_cd(grid),
                      sw.frame_u, sw.frame_v, sw.loading, sw.evaporation, sw.rain_formation, sw.anisotropic,
-                     sw.vertical_dz, sw.durran_klemp, sw.pressure_in_stages, 1, 0.0, 0.0, 1, slabs], dtype=np.float64)
+                     sw.vertical_dz, sw.durran_klemp, sw.pressure_in_stages, getattr(sw, "ice", 1), 0.0, 0.0, 1, slabs],
+                    dtype=np.float64)
 
 
 class OracleModel:
@@ -120,6 +151,9 @@ class OracleModel:
         threads = threads or os.cpu_count() or 1
         self.h = L.orc_create(1 if fp64 else 0, *args[:7], args[7], args[8], args[9], dp(env7), dp(sw), threads)
         self._keep = (keep, env7, sw)
+        sw_ = spec.switches
+        if getattr(sw_, "lightning", False):
+            L.orc_set_lightning(self.h, 1, 1 if getattr(sw_, "corona", True) else 0, int(getattr(sw_, "lightning_seed", 43)))
         for name, arr in spec.fields.items():
             self.set(name, arr)
 
@@ -133,7 +167,11 @@ class OracleModel:
         lib().orc_set_threads(self.h, threads)
 
     def _id(self, name: str) -> int:
-        return CARRIED.index(name) if name in CARRIED else EXTRA[name]
+        if name in CARRIED:
+            return CARRIED.index(name)
+        if name in CHARGES:
+            return len(CARRIED) + CHARGES.index(name)
+        return EXTRA[name]
 
     def set(self, name: str, values: np.ndarray):
         a = f64(values).ravel()
@@ -221,3 +259,132 @@ def cell(which: str, values: Dict[str, float], exner=1.0, p=1e5, rho=1.0, dt=1.0
             "settle": 8}[which]
     r = lib().orc_cell(code, fp(v), exner, p, rho, dt, aux)
     return r, {n: v[k] for k, n in enumerate(names)}
+
+
+CHARGE_STATE = ("chargeGround", "separated", "ic", "cgNegative", "cgPositive", "precipitation", "conduction", "flashesIC",
+                "flashesCG", "totalCharge", "lastFlashes")
+
+
+def _flash_record(read, k: int, cap: int = 3000):
+    out, strokes = np.empty(9), np.zeros(8)
+    nodes, parent, polarity = (np.empty(cap, np.int32) for _ in range(3))
+    ip = C.POINTER(C.c_int)
+    if read(k, dp(out), nodes.ctypes.data_as(ip), parent.ctypes.data_as(ip), polarity.ctypes.data_as(ip), dp(strokes), cap):
+        return None
+    m = int(out[7])
+    return dict(time=out[0], kind="CG" if out[1] else "IC", start=int(out[2]), ground=int(out[3]), potential=out[4],
+                charge=out[5], moment=out[6], nodes=nodes[:m].copy(), parent=parent[:m].copy(),
+                polarity=polarity[:m].copy(), strokes=strokes[:int(out[8])].copy())
+
+
+def _charge_state(self):
+    out = np.empty(len(CHARGE_STATE))
+    lib().orc_charge_state(self.h, dp(out))
+    return dict(zip(CHARGE_STATE, out))
+
+
+def _last_flashes(self):
+    n = int(self.charge_state()["lastFlashes"])
+    return [_flash_record(lambda *a: lib().orc_flash(self.h, *a), k) for k in range(n)]
+
+
+OracleModel.charge_state = _charge_state
+OracleModel.last_flashes = _last_flashes
+
+
+def _float_ptrs(arrays):
+    ptrs = (_f * len(arrays))(*[a.ctypes.data_as(_f) for a in arrays])
+    return ptrs
+
+
+class OracleLightning:
+    """Lightning (src/core/lightning.ts:135-420) on a grid with the air density of each level: FP32 carriers (C/kg)
+    changed in place, as the reference's Float32Arrays."""
+
+    def __init__(self, grid, air, seed: int = 1):
+        args, keep = grid_args(grid)
+        self.grid, self.air = grid, f64(air)
+        self.h = lib().orc_lightning_create(*args, dp(self.air), seed)
+        self._keep = keep
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            lib().orc_lightning_destroy(h)
+            self.h = None
+
+    @staticmethod
+    def _check(carriers):
+        for c in carriers:
+            assert c.dtype == np.float32 and c.flags.c_contiguous
+
+    def set_corona(self, on: bool):
+        lib().orc_lightning_set_corona(self.h, 1 if on else 0)
+
+    def cloud(self, fields):
+        self._check(fields)
+        lib().orc_lightning_cloud(self.h, _float_ptrs(fields), len(fields))
+
+    def solve(self, carriers):
+        self._check(carriers)
+        lib().orc_lightning_solve(self.h, _float_ptrs(carriers))
+
+    def strongest(self, stamp: int = -1):
+        r = C.c_double()
+        best = lib().orc_lightning_strongest(self.h, stamp, C.byref(r))
+        return best, r.value
+
+    def discharge(self, carriers, time: float, limit: int = 10):
+        self._check(carriers)
+        n = lib().orc_lightning_discharge(self.h, _float_ptrs(carriers), time, limit)
+        return [_flash_record(lambda *a: lib().orc_lightning_flash(self.h, *a), k) for k in range(n)]
+
+    def conduct(self, ions, dt: float) -> float:
+        self._check([ions])
+        return lib().orc_lightning_conduct(self.h, ions.ctypes.data_as(_f), dt)
+
+    def fields(self):
+        n = self.grid.nx * self.grid.ny * self.grid.nz
+        phi, rho, st = np.empty(n), np.empty(n), np.empty(2)
+        lib().orc_lightning_fields(self.h, dp(phi), dp(rho), dp(st))
+        return phi, rho, dict(fromGround=st[0], conducted=st[1])
+
+
+def flash_limit(dt: float) -> int:
+    return lib().orc_flash_limit(dt)
+
+
+def critical_rar(tc):
+    return lib().orc_critical_rar(tc)
+
+
+def collision_charge(tc, rar, d, v, signed=False):
+    return lib().orc_collision_charge(tc, rar, d, v, 1 if signed else 0)
+
+
+def crystal_number(tc, qi=0.0, rho=1.0):
+    return lib().orc_crystal_number(tc, qi, rho)
+
+
+def crystal_diameter(qi, rho, tc):
+    return lib().orc_crystal_diameter(qi, rho, tc)
+
+
+def takahashi(tc, lwc):
+    return lib().orc_takahashi(tc, lwc)
+
+
+def charging_rate(tc, rho, cloud, ice, snow, graupel, hail, snow_fall, wet_graupel=False, wet_hail=False, crystals=None,
+                  scheme="tak"):
+    return lib().orc_charging_rate(tc, rho, cloud, ice, snow, graupel, hail, snow_fall, int(wet_graupel), int(wet_hail),
+                                   -1.0 if crystals is None else crystals, 1 if scheme == "tak" else 0)
+
+
+def inductive_rate(tc, rho, cloud, graupel, hail, ez, rimer_charge, wet_graupel=False, wet_hail=False):
+    return lib().orc_inductive_rate(tc, rho, cloud, graupel, hail, ez, rimer_charge, int(wet_graupel), int(wet_hail))
+
+
+def transfer_charge(charge, before, after):
+    c, b, a = f64(charge).copy(), f64(before), f64(after)
+    lib().orc_transfer_charge(dp(c), dp(b), dp(a))
+    return c
