@@ -39,6 +39,11 @@ enum sg_field {
   SG_NFIELDS
 };
 #define SG_ALL_FIELDS ((1u << SG_NFIELDS) - 1u)
+/* An electrified run (sg_switches.lightning with ice) also carries the charge on the ice-snow, graupel-hail, rain and
+ * droplet-ion carriers, C per kg of air (AtmosphereModel.chargeIce, chargeGraupel, chargeRain, chargeAir,
+ * src/core/model.ts:210), fields 13-16 of sg_run_read_fields / sg_run_write_fields (host[f] by field id). */
+enum sg_charge_field { SG_CHARGE_ICE = 13, SG_CHARGE_GRAUPEL, SG_CHARGE_RAIN, SG_CHARGE_AIR, SG_NFIELDS_ELECTRIFIED };
+#define SG_CHARGE_FIELDS (0xFu << SG_CHARGE_ICE)
 
 typedef struct sg_context sg_context;
 typedef int32_t sg_run;
@@ -82,7 +87,43 @@ typedef struct sg_switches {
    * runs in afterStep) and the run's swaths (addSwaths, src/ensemble/member.ts:71-89) on the device; read with
    * sg_run_rotation / sg_run_read_swaths. 0: neither (two launches a step fewer). */
   int32_t rotation;
+  /* 1 with ice: electrification and lightning (SimConfig.lightning; electrified(), src/core/model.ts:1316): the four
+   * charge carriers transported and sedimented with their carriers, the non-inductive (Takahashi) and inductive
+   * charging and the charge transfer in the physics, and after every step the flashes (Lightning.discharge,
+   * src/core/lightning.ts:259-275), the ion conduction and the corona. 0: none of it (the step of the configurations
+   * the throughput is quoted on). */
+  int32_t lightning;
+  int32_t corona;          /* 1: the ground gives corona (over land; surfaceType 'water': 0, :1539) */
+  int32_t lightning_seed;  /* the lightning's random numbers: config.seed + 1 (:1538) */
+  int32_t reserved2;
 } sg_switches;
+
+/* The charge budget of an electrified run since it began (AtmosphereModel.chargeGround, .charge, .flashCount,
+ * src/core/model.ts:218-241), C and counts. */
+typedef struct sg_charge_state {
+  double ground;           /* chargeGround: what the precipitation, the flashes and the conduction gave the ground */
+  double separated;        /* charge separated by the charging (both signs, |non-inductive| + |inductive|) */
+  double ic;               /* neutralized by IC flashes (each sign) */
+  double cg_negative, cg_positive;  /* lowered to the ground by -CG and +CG flashes */
+  double precipitation;    /* carried to the ground by the falling carriers */
+  double conduction;       /* lost to the ground and the top by the ion current and the corona */
+  int64_t flashes_ic, flashes_cg;
+  int32_t last_flashes;    /* flashes of the last step (sg_run_flashes) */
+  int32_t electrified;
+} sg_charge_state;
+
+/* One flash of the last step (Flash, src/core/lightning.ts:69-106, without its drawing and transient event). */
+typedef struct sg_flash {
+  double time;             /* model time of the step's end, s */
+  double potential;        /* the channel's potential when it stopped growing (a CG's before its ground contact), V */
+  double charge;           /* IC: charge neutralized of each sign (> 0); CG: charge lowered to the ground, signed */
+  double moment;           /* CG: charge moment change, C m */
+  double stroke_charge[4]; /* CG: each stroke's charge (at most 4) */
+  int32_t cg;              /* 1: a cloud-to-ground flash */
+  int32_t start, ground;   /* initiation node; the ground contact node (-1 for IC) */
+  int32_t nodes, strokes;  /* channel nodes; CG strokes */
+  int32_t reserved;
+} sg_flash;
 
 /* Per-run counters (AtmosphereModel.clipped, negativeFilled, water, src/core/model.ts:236, :269-271). */
 typedef struct sg_run_counters {
@@ -99,8 +140,10 @@ typedef struct sg_run_counters {
 int sg_context_create(int device, uint64_t hbm_budget_bytes, sg_context** out);
 int sg_context_destroy(sg_context* ctx);
 const char* sg_last_error(sg_context* ctx);
-/* Bytes of HBM one run of this grid takes (state, scratch, solver tables). */
+/* Bytes of HBM one run of this grid takes (state, scratch, solver tables); an electrified run's (with its charge
+ * carriers and lightning buffers). */
 uint64_t sg_run_bytes(const sg_grid* grid);
+uint64_t sg_run_bytes_electrified(const sg_grid* grid);
 
 /* ---- runs (replace `new AtmosphereModel(config, grid, profile)`, src/core/model.ts:329; fields as its arrays) */
 /* init[SG_NFIELDS] host arrays in sg_field order (theta is the full potential temperature, K). */
@@ -201,6 +244,19 @@ int sg_run_load_state(sg_context* ctx, sg_run run, const uint8_t* image, size_t 
 int sg_run_read_pressure(sg_context* ctx, sg_run run, double* p);
 int sg_run_status(sg_context* ctx, sg_run run, sg_run_counters* out);
 int sg_run_retire(sg_context* ctx, sg_run run);
+
+/* ---- electrification and lightning (an electrified run; replace AtmosphereModel.chargeGround / charge / flashCount /
+ * flashes, src/core/model.ts:218-241, and Lightning, src/core/lightning.ts:135) */
+int sg_run_charge(sg_context* ctx, sg_run run, sg_charge_state* out);
+/* The flashes of the run's last step, oldest first: up to cap records, *count = how many there were. */
+int sg_run_flashes(sg_context* ctx, sg_run run, sg_flash* out, int cap, int* count);
+/* Flash k's channel: nodes in growth order, the index of the node each grew from (-1 for the first), the leader
+ * polarity (+1, -1, 0), up to cap each (a flash has at most 3000 nodes). */
+int sg_run_flash_channel(sg_context* ctx, sg_run run, int k, int32_t* nodes, int32_t* parent, int32_t* polarity, int cap);
+/* The discharge of the run's charge as it stands (AtmosphereModel.discharge, src/core/model.ts:1537-1552: the flashes
+ * at model time `time`, at most flashLimit(dt) of them, then the conduction and corona over dt and the vertical field),
+ * without a step: the seam of a caller that orders the step itself. The run's own time is not moved. */
+int sg_run_discharge(sg_context* ctx, sg_run run, double time, double dt);
 
 /* ---- stepping (replaces AtmosphereModel.step(dt) + time += dt, src/core/model.ts:873; gpuStep, src/gpu/step.ts:12) */
 int sg_run_step(sg_context* ctx, sg_run run, int nsteps);

@@ -1,7 +1,8 @@
 // Device data layout of the step and the small numerical building blocks shared by the kernels.
 //
 // HBM layout of one run (all FP32 unless noted, n = nx*ny*nz nodes, node i = x + nx*(y + ny*z)):
-//   fld   3 sets x 13 fields x n      set A = the state between steps, B and C = RK3 stage / mixing scratch
+//   fld   3 sets x 13 fields x n      set A = the state between steps, B and C = RK3 stage / mixing scratch; an
+//                                     electrified run's 3 sets x 4 charge carriers x n after them
 //   faces 4 x n                       projected face mass fluxes mx, my, mz and their divergence
 //   kmkh  2 x n                       eddy viscosities (vertical km, horizontal kh)
 //   phi   n                           face-projection potential
@@ -28,6 +29,10 @@ namespace sg {
 
 constexpr int NF = 13;  // carried fields
 enum Field { RAIN = 0, SNOW, GRAUPEL, HAIL, U, V, W, THETA, Q, CLOUD, ICE, ICENUM, COLD };
+// An electrified run also carries the charge on the ice-snow, graupel-hail, rain and droplet-ion carriers (C/kg,
+// src/core/model.ts:210): WENO fields without the positivity fix, not mixed (:1331, :1338-1344).
+constexpr int NFE = 17;
+enum ChargeField { CHARGE_ICE = 13, CHARGE_GRAUPEL, CHARGE_RAIN, CHARGE_AIR };
 // WENO5 for the water species and the cold-pool indicator, linear fifth-order upwind for u, v, w, theta
 // (src/core/model.ts:1320-1328).
 SG_HD bool monotone(int f) { return !(f == U || f == V || f == W || f == THETA); }
@@ -68,7 +73,7 @@ static_assert(sizeof(TriAB) == 16, "one 16-byte load a level");
 struct RunDesc {
   int nx, ny, nz, layer, n, nm, mh, ncells;
   int fx_nf, fy_nf, fx_rad[8], fy_rad[8];  // FFT radix plans of nx and ny
-  int slot, flags, pad0, pad1;
+  int slot, flags, nf, pad1;  // nf: fields a set (NF, or NFE for an electrified run)
   float dx, dy, inv_dx, inv_dy, dt, height;
   float inv_dx_lo, inv_dy_lo, inv_dt, inv_dt_lo;      // FP32 rounding errors of 1/dx, 1/dy; 1/dt as a pair
   float coriolis, keep, sponge_start, cs, drag, frame_u, frame_v, ue0, ve0, env_speed, lenH2, capH, rho0;
@@ -98,9 +103,15 @@ struct RunDesc {
   int core_lo, core_hi;                // the cloudy-core levels of countCores (:1653)
   float meso_zeta;                     // mesoCoreZeta(dx) (:129)
   float pad2;
+  // electrified runs (RF_ELEC): the step-start fall speeds [4][n] (ice-snow and graupel-hail charge carriers, rain,
+  // snow), the vertical field of the last solve [n] (V/m, for the inductive charging), the sedimentation's charge
+  // reaching the ground per work item
+  float* vfall;
+  float* ez;
+  double* cpart;
 };
 enum RunFlags { RF_LOADING = 1, RF_EVAP = 2, RF_RAINFORM = 4, RF_ANISO = 8, RF_VDZ = 16, RF_DK = 32, RF_STAGES = 64, RF_ICE = 128,
-                RF_REFINE = 256, RF_ROTATION = 512 };
+                RF_REFINE = 256, RF_ROTATION = 512, RF_ELEC = 1024 };
 // diag columns: the UH column, the core sums, the swaths, the core labels; then the ground columns of a sample
 enum DiagColumn { DG_UH = 0, DG_COREW, DG_COREWZ, DG_GUST_MAX, DG_UH_MAX, DG_LABEL, DG_RATE, DG_HAIL, DG_GUST, DG_THV, DG_MASK, DG_COUNT };
 // rot layout (doubles): the rotation state (src/core/model.ts:263), the run's model time, then the step's keys and the
@@ -109,17 +120,23 @@ enum RotSlot { R_UH = 0, R_X, R_Y, R_ANTI, R_PERSISTED, R_UH01, R_UH03, R_LOW, R
                K_UH = 12, K_01, K_MIN, K_03,
                M_UP = 16, M_DOWN, M_CLOUD, M_TOP, M_THERMAL, M_COLD, R_COUNT = 24 };
 // scr layout
-enum Scratch { S_COURANT = 0, S_FILL = 4, S_COUNT = 16 };
+enum Scratch { S_COURANT = 0, S_FILL = 4, S_CCOURANT = 11, S_COUNT = 16 };  // S_CCOURANT: the three falling charges
 // cnt layout
 // C_TIMEOUT: a kernel's bounded wait for its own asynchronous copies ran out (the run is then failed too)
 enum Counter { C_CLIPPED = 0, C_STEPS = 1, C_FAILED = 2, C_TIMEOUT = 3, C_COUNT = 4 };
 // acc layout
-enum Acc { A_NEG = 0, A_WATER = 1, A_COUNT = 8 };
+// A_CHG_*: the charge budget (AtmosphereModel.chargeGround and .charge, src/core/model.ts:218-224), C; A_FLASH_*: counts
+enum Acc { A_NEG = 0, A_WATER = 1, A_CHG_GROUND = 8, A_CHG_SEPARATED, A_CHG_IC, A_CHG_CG_NEG, A_CHG_CG_POS, A_CHG_PRECIP, A_CHG_CONDUCTION,
+           A_FLASH_IC, A_FLASH_CG, A_COUNT = 24 };
 // partial-sum layout (per run): fill partials [chunk][7][3], then water partials [chunk][4].
 constexpr int CHUNK = 4096;   // nodes per pointwise work item
 
 SG_HD float lvl(const RunDesc& R, int which, int z) { return R.lv[which * R.nz + z]; }
-SG_HD float* field(const RunDesc& R, int set, int f) { return R.fld + ((size_t)set * NF + f) * R.n; }
+// Set s of the 13 base fields is fld[s * 13 n ...]; an electrified run's charge carriers follow the three sets,
+// four fields a set, so the base fields keep their offsets (and the hot kernels their constant strides).
+SG_HD float* field(const RunDesc& R, int set, int f) {
+  return f < NF ? R.fld + ((size_t)set * NF + f) * R.n : R.fld + ((size_t)3 * NF + (size_t)set * (NFE - NF) + (f - NF)) * R.n;
+}
 
 // ---- face reconstruction. Every operation is an explicitly rounded one (no contraction left to the compiler), so
 // a face gets the same bits whether it is computed alone (Op1, here and on the host) or paired with another face on

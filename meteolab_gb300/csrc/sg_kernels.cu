@@ -17,6 +17,7 @@
 #include "sg_common.cuh"
 #include "sg_fft.cuh"
 #include "sg_physics.cuh"
+#include "sg_charge.cuh"
 #include "sg_kernels.h"
 #include "sg_device.cuh"
 
@@ -170,6 +171,29 @@ __global__ void k_fall_courant(const RunDesc* __restrict__ runs, const int4* ite
       float m = warpMax(c[f]);
       if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMaxPos(R.scr + S_COURANT + f, m);
     }
+    if (R.flags & RF_ELEC) {
+      // the charge carriers' fall speeds (:1230-1234) from the step-start water, with rain's and snow's own (the
+      // charge on rain falls with it; the charging reads the snow's), and the charges' Courant numbers
+      const size_t n = R.n;
+      const float *ice = field(R, 0, ICE), *cI = field(R, 0, CHARGE_ICE), *cG = field(R, 0, CHARGE_GRAUPEL), *cR = field(R, 0, CHARGE_RAIN);
+      float cc[3] = {0.f, 0.f, 0.f};
+      for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+        const int z = i / R.layer;
+        const float rho = lvl(R, L_RHO, z), fsq = lvl(R, L_FALLSQ, z), k = R.dt * lvl(R, L_INV_HZ, z);
+        const float a = rain[i], b = snow[i], g = graupel[i], h = hail[i], ic = ice[i];
+        const float vr = phys::rainFall(a, rho, fsq), vs = phys::snowFall(b, rho, fsq), vg = phys::graupelFall(g, rho), vh = phys::hailFall(h, rho);
+        const float is = ic + b, gh = g + h;
+        const float vi = is > 0.f ? b * vs / is : 0.f, vgh = gh > 0.f ? (g * vg + h * vh) / gh : 0.f;
+        R.vfall[i] = vi; R.vfall[n + i] = vgh; R.vfall[2 * n + i] = vr; R.vfall[3 * n + i] = vs;
+        if (cI[i] != 0.f) cc[0] = fmaxf(cc[0], k * vi);
+        if (cG[i] != 0.f) cc[1] = fmaxf(cc[1], k * vgh);
+        if (cR[i] != 0.f) cc[2] = fmaxf(cc[2], k * vr);
+      }
+      for (int f = 0; f < 3; f++) {
+        float m = warpMax(cc[f]);
+        if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMaxPos(R.scr + S_CCOURANT + f, m);
+      }
+    }
   }
 }
 
@@ -235,6 +259,44 @@ __global__ void k_sediment(const RunDesc* __restrict__ runs, const int4* items, 
           }
         }
         for (int z = 0; z < nz; z++) a[c + z * layer] = sq[z * SED_COLS + t];
+      }
+    }
+    if (R.flags & RF_ELEC) {
+      // The charge on the falling carriers (sediment(field, vt, dt, false), :931, :582-598) with the carriers' step-start
+      // fall speeds: what falls through the ground is the ground's charge, C (:588-591), summed per work item.
+      __shared__ double gsum[SED_COLS];
+      double ground = 0;
+      const float dxy = R.dx * R.dy;
+      for (int j = 0; j < 3; j++) {
+        float* a = field(R, 0, CHARGE_ICE + j);
+        const float* vt = R.vfall + (size_t)j * R.n;
+        const int parts = max(1, (int)ceilf(R.scr[S_CCOURANT + j] / .8f));
+        if (!on) continue;
+        bool any = false;
+        for (int z = 0; z < nz; z++) {
+          const float q = a[c + z * layer];
+          sq[z * SED_COLS + t] = q; sv[z * SED_COLS + t] = vt[c + z * layer];
+          any |= q != 0.f;
+        }
+        if (!any) continue;
+        const float dts = R.dt / (float)parts;
+        for (int p = 0; p < parts; p++) {
+          ground += (double)rho0 * (double)(sq[t] * sv[t]) * (double)dts * (double)dxy;
+          float inflowAbove = 0.f;
+          for (int z = nz - 1; z >= 0; z--) {
+            const float q = sq[z * SED_COLS + t], out = lrho[z] * q * sv[z * SED_COLS + t];
+            sq[z * SED_COLS + t] = q + dts * (inflowAbove - out) * lk[z];
+            inflowAbove = out;
+          }
+        }
+        for (int z = 0; z < nz; z++) a[c + z * layer] = sq[z * SED_COLS + t];
+      }
+      gsum[t] = ground;
+      __syncthreads();
+      if (t == 0) {
+        double s = 0;
+        for (int k = 0; k < SED_COLS; k++) s += gsum[k];
+        R.cpart[items[it].y] = s;
       }
     }
     __syncthreads();  // the level tables are restaged for the block's next item
@@ -1194,8 +1256,11 @@ __global__ void k_fill_final(const RunDesc* __restrict__ runs, const int4* items
 // Per node: the positivity fix and the cold decay ('finish', :1253-1258), then physics(z) (:1347-1531): microphysics,
 // Coriolis and wind relaxation, surface fluxes (none in the single-storm mode), cold clamp, Rayleigh sponge.
 // In: set `in` (final RK3 values). Out: rain, snow, graupel, hail, cold -> set A; the mixed fields -> set `mid`.
+// ELEC: the kernel of a batch with electrified runs, which also moves their charge with the water and charges the
+// graupel and crystals after the microphysics (:1454-1469); the charges go to set A (they are not mixed).
+template <bool ELEC>
 __global__ void __launch_bounds__(256, 3) k_physics(const RunDesc* __restrict__ runs, const int4* items, int nitems, int in, int mid) {
-  __shared__ double sh[32 * 3];
+  __shared__ double sh[32 * 4];
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
     const int chunk = items[it].y, i0 = chunk * CHUNK, i1 = min(R.n, i0 + CHUNK);
@@ -1203,8 +1268,12 @@ __global__ void __launch_bounds__(256, 3) k_physics(const RunDesc* __restrict__ 
     float fill[NCONS];
 #pragma unroll
     for (int k = 0; k < NCONS; k++) fill[k] = R.scr[S_FILL + k];
-    float whi[3] = {0.f, 0.f, 0.f}, wlo[3] = {0.f, 0.f, 0.f};
+    constexpr int NW = ELEC ? 4 : 3;  // the water budget's three sums, and the charge separated
+    float whi[NW], wlo[NW];
+#pragma unroll
+    for (int k = 0; k < NW; k++) whi[k] = wlo[k] = 0.f;
     bool bad = false;
+    const bool elec = ELEC && (R.flags & RF_ELEC);
     for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
       const int z = i / R.layer;
       auto fixed = [&](int kc, float x) { return x < 1e-10f ? 0.f : fmaf(x, fill[kc], x); };
@@ -1222,8 +1291,22 @@ __global__ void __launch_bounds__(256, 3) k_physics(const RunDesc* __restrict__ 
       pl.qi_hi = lvl(R, L_QI_HI, z); pl.qi_lo = lvl(R, L_QI_LO, z); pl.bi = lvl(R, L_BI, z);
       pl.q0_hi = lvl(R, L_Q0_HI, z); pl.q0_lo = lvl(R, L_Q0_LO, z);
       const float q0 = s.q;
+      float before[4];
+      if constexpr (ELEC) if (elec) { before[0] = s.ice + s.snow; before[1] = s.graupel + s.hail; before[2] = s.rain; before[3] = s.cloud; }
       float evap;
       phys::microphysics(s, pl, dt, R.flags, evap);
+      if constexpr (ELEC) if (elec) {
+        const float after[4] = {s.ice + s.snow, s.graupel + s.hail, s.rain, s.cloud};
+        float c[4] = {field(R, in, CHARGE_ICE)[i], field(R, in, CHARGE_GRAUPEL)[i], field(R, in, CHARGE_RAIN)[i], field(R, in, CHARGE_AIR)[i]};
+        if (c[0] != 0.f || c[1] != 0.f || c[2] != 0.f || c[3] != 0.f) charge::transferCharge(c, before, after);
+        const float tc = phys::tcOf(s, pl.exner), rho = pl.rho;
+        const bool wetG = charge::wetGrowing(s.graupel, phys::N0G, phys::RHO_G, tc, s, pl), wetH = charge::wetGrowing(s.hail, phys::N0H, phys::RHO_H, tc, s, pl);
+        const float separated = charge::chargingRate(tc, rho, s.cloud, s.ice, s.snow, s.graupel, s.hail, R.vfall[3 * (size_t)R.n + i], wetG, wetH, s.inum * rho) * dt / rho;
+        const float induced = charge::inductiveRate(tc, rho, s.cloud, s.graupel, s.hail, R.ez[i], (c[1] + separated) * rho, wetG, wetH) * dt / rho;
+        field(R, 0, CHARGE_ICE)[i] = c[0] - separated; field(R, 0, CHARGE_GRAUPEL)[i] = c[1] + separated + induced;
+        field(R, 0, CHARGE_RAIN)[i] = c[2]; field(R, 0, CHARGE_AIR)[i] = c[3] - induced;
+        df_add_prod(whi[NW - 1], wlo[NW - 1], lvl(R, L_NODEMASS, z), lvl(R, L_NODEMASS_LO, z), fabsf(separated) + fabsf(induced));
+      }
       if (!(R.flags & RF_STAGES)) {
         float num = s.thp + .61f * ((s.thb + s.thp) * (s.q - lvl(R, L_QB, z)) + lvl(R, L_QB, z) * s.thp);
         float loaded = s.cloud + s.ice + ((R.flags & RF_LOADING) ? s.rain + s.snow + s.graupel + s.hail : 0.f);
@@ -1250,7 +1333,7 @@ __global__ void __launch_bounds__(256, 3) k_physics(const RunDesc* __restrict__ 
     }
     if (__syncthreads_or(bad) && threadIdx.x == 0) atomicExch(&R.cnt[C_FAILED], 1ull);
     size_t nch = (R.n + CHUNK - 1) / CHUNK;
-    blockSumsDF<3>(whi, wlo, R.part + nch * NCONS * 3 + (size_t)chunk * 4, sh);
+    blockSumsDF<NW>(whi, wlo, R.part + nch * NCONS * 3 + (size_t)chunk * 4, sh);
   }
 }
 
@@ -1455,6 +1538,14 @@ __global__ void k_step_end(const RunDesc* __restrict__ runs, const int4* items, 
       double w[3] = {0, 0, 0};
       for (size_t c = 0; c < nch; c++) for (int j = 0; j < 3; j++) w[j] += R.part[nch * NCONS * 3 + c * 4 + j];
       for (int j = 0; j < 3; j++) R.acc[A_WATER + j] += w[j];
+      if (R.flags & RF_ELEC) {
+        // the charge separated this step (:1126), and the sedimentation's charge reaching the ground (:590)
+        double sep = 0, ground = 0;
+        for (size_t c = 0; c < nch; c++) sep += R.part[nch * NCONS * 3 + c * 4 + 3];
+        const int sedItems = (R.layer + SED_COLS - 1) / SED_COLS;
+        for (int c = 0; c < sedItems; c++) ground += R.cpart[c];
+        R.acc[A_CHG_SEPARATED] += sep; R.acc[A_CHG_GROUND] += ground; R.acc[A_CHG_PRECIP] += ground;
+      }
       R.cnt[C_STEPS] += 1;
     }
     __syncthreads();
@@ -1570,7 +1661,10 @@ void launch_pres_correct(const Launch& L, int set, int final_) {
 
 void launch_fill_partial(const Launch& L, int set) { k_fill_partial<<<GRID(L.n, L.cap), 128, 0, L.stream>>>(L.runs, L.items, L.n, set); }
 void launch_fill_final(const Launch& L) { k_fill_final<<<GRID(L.n, L.cap), 32, 0, L.stream>>>(L.runs, L.items, L.n); }
-void launch_physics(const Launch& L, int in, int mid) { k_physics<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, in, mid); }
+void launch_physics(const Launch& L, int in, int mid, bool elec) {
+  if (elec) k_physics<true><<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, in, mid);
+  else k_physics<false><<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, in, mid);
+}
 void launch_viscosity(const Launch& L, int set) { k_viscosity<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set); }
 size_t mix_smem(int TX, int TY) { return (size_t)2 * (NMIX + 1) * (TX + 2) * (TY + 2) * sizeof(float); }
 void launch_mix(const Launch& L, int in, int TX, int TY) {

@@ -21,6 +21,7 @@
 #include "sg_kernels.h"
 #include "sg_state.h"
 #include "sg_physics.cuh"
+#include "sg_lightning.h"
 
 using namespace sg;
 
@@ -33,12 +34,15 @@ const double RK3[3] = {1.0 / 3, 1.0 / 2, 1.0};
 size_t align(size_t x) { return (x + ALIGN - 1) / ALIGN * ALIGN; }
 
 struct Layout {
-  size_t fld, faces, kmkh, phi, pres, pres2, spec, cols, lv, lv64, triF, triP, ab, twx, twy, scr, part, acc, cnt, items, diag, rot, total;
+  size_t fld, faces, kmkh, phi, pres, pres2, spec, cols, lv, lv64, triF, triP, ab, twx, twy, scr, part, acc, cnt, items, diag, rot;
+  size_t vfall = 0, ez = 0, cpart = 0, lgt = 0, total;  // electrified runs only
 };
-Layout layout(int nx, int ny, int nz) {
+// One run's allocation; an electrified run's sets hold the four charge carriers too, and it has its fall speeds, the
+// vertical field and the lightning's buffers (sg_lightning.cu) after the rest.
+Layout layout(int nx, int ny, int nz, bool elec = false) {
   Layout L; size_t n = (size_t)nx * ny * nz, layer = (size_t)nx * ny, nm = nx / 2 + 1, nch = (n + CHUNK - 1) / CHUNK, o = 0;
   auto take = [&](size_t bytes) { size_t at = o; o += align(bytes); return at; };
-  L.fld = take(3 * NF * n * 4); L.faces = take(4 * n * 4); L.kmkh = take(2 * n * 4); L.phi = take(n * 4);
+  L.fld = take(3 * (size_t)(elec ? NFE : NF) * n * 4); L.faces = take(4 * n * 4); L.kmkh = take(2 * n * 4); L.phi = take(n * 4);
   L.pres = take(layer * (nz - 1) * 4); L.pres2 = take(layer * (nz - 1) * 4); L.spec = take(nm * nz * ny * 8); L.cols = take(3 * layer * 4);
   L.lv = take((size_t)L_COUNT * nz * 4); L.lv64 = take((size_t)D_COUNT * nz * 8);
   L.triF = take(nm * nz * ny * 24); L.triP = take(nm * (nz - 1) * ny * 24); L.ab = take(nm * ny * 16);
@@ -46,6 +50,10 @@ Layout layout(int nx, int ny, int nz) {
   L.acc = take(A_COUNT * 8); L.cnt = take(C_COUNT * 8);
   L.items = take(nch * 16);  // the run's own per-node work items (field conversions outside a batch plan)
   L.diag = take((size_t)DG_COUNT * layer * 4); L.rot = take(R_COUNT * 8);
+  if (elec) {
+    L.vfall = take(4 * n * 4); L.ez = take(n * 4); L.cpart = take(((layer + 63) / 64) * 8);
+    L.lgt = take(lightning_bytes(nx, ny, nz));
+  }
   L.total = o;
   return L;
 }
@@ -60,6 +68,12 @@ struct Run {
   int4* nodeItems = nullptr;  // inside mem
   int nNode = 0;
   double waterStart = 0;      // the water reservoirs' sum when the run began (AtmosphereModel.water.start), kg
+  // an electrified run: its lightning, the model time it has reached (the flashes' time and random numbers), its step
+  // length, and its grid (the lightning's tables and solve)
+  std::unique_ptr<LgtHost> lgt;
+  double time = 0, dt = 0;
+  std::vector<double> zs, dzs, hz;
+  sg_grid grid{};
 };
 
 struct Plan {
@@ -79,6 +93,7 @@ struct Plan {
   bool refine = false;                                                // some run refines its final projection
   bool unrefined = false;                                             // some run does not (k_pres_correct<1> has work)
   bool rotation = false;                                              // some run tracks its rotation and swaths
+  bool elec = false;                                                  // some run is electrified (charges, lightning)
   bool tuned = false;                                                 // TX, TY, wenoG chosen by timing
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -89,7 +104,7 @@ struct Plan {
   }
 };
 enum Family { FAM_NODE, FAM_COLS, FAM_ROWS_FACE, FAM_ROWS_PRES, FAM_MODES, FAM_RUNS, FAM_CELLS, FAM_T_WENO, FAM_T_DYN, FAM_MIX,
-              FAM_REFINE, FAM_COUNT };
+              FAM_REFINE, FAM_T_CHG, FAM_COUNT };
 
 }  // namespace
 
@@ -296,7 +311,7 @@ int validate(sg_context* ctx, const sg_grid* g, const sg_base_state* b, const sg
   if (g->nz > 128) return fail(ctx, SG_ERR_UNSUPPORTED, "nz > 128 levels");
   if (g->nx > 4096 || g->ny > 4096) return fail(ctx, SG_ERR_UNSUPPORTED, "nx or ny > 4096");
   // the kernels index a run's field sets with 32-bit element offsets
-  if ((size_t)g->nx * g->ny * g->nz * 3 * NF >= (1ull << 31)) return fail(ctx, SG_ERR_UNSUPPORTED, "grid beyond 55 million nodes");
+  if ((size_t)g->nx * g->ny * g->nz * 3 * (sw->lightning ? NFE : NF) >= (1ull << 31)) return fail(ctx, SG_ERR_UNSUPPORTED, "grid beyond 55 million nodes");
   int rad[8];
   if (fft_plan_factors(g->nx, rad) < 0 || fft_plan_factors(g->ny, rad) < 0) return fail(ctx, SG_ERR_UNSUPPORTED, "nx or ny has more than 8 prime factors");
   if (!(g->dx > 0 && g->dy > 0 && g->height > 0) || !g->zs || !g->dzs || !g->hz) return fail(ctx, SG_ERR_INVALID, "bad grid spacing or levels");
@@ -304,6 +319,8 @@ int validate(sg_context* ctx, const sg_grid* g, const sg_base_state* b, const sg
   for (int z = 0; z < g->nz; z++) if (!(b->rho[z] > 0) || !(b->theta[z] > 0) || !(g->hz[z] > 0)) return fail(ctx, SG_ERR_INVALID, "non-positive rho, theta or hz");
   if (!(sw->dt > 0)) return fail(ctx, SG_ERR_INVALID, "dt must be positive");
   if (!sw->pressure_in_stages) return fail(ctx, SG_ERR_UNSUPPORTED, "the device step needs the pressure in the RK3 stages");
+  // the lightning's potential solve holds a row, a column and a half spectrum of a level in shared memory
+  if (sw->lightning && sw->ice && (g->nx > 2048 || g->ny > 2048)) return fail(ctx, SG_ERR_UNSUPPORTED, "lightning: nx and ny at most 2048");
   // The shared memory of the mode kernel: (nz + 8) * ny complex values.
   size_t smem = (size_t)(g->nz + 8) * g->ny * 8;
   if ((int)smem > ctx->maxSmem) return fail(ctx, SG_ERR_UNSUPPORTED, "(nz + 8) * ny too large for one block's shared memory");
@@ -325,6 +342,17 @@ void transport_items(sg_context* ctx, const std::vector<int>& slots, int TX, int
     const int grp0 = wenoG == 3 ? 0 : 4, ngrp = wenoG == 3 ? 3 : 9;
     for (int g = grp0; g < grp0 + ngrp; g++) for (int t = 0; t < tiles; t++) fam[0].push_back(make_int4(s, g, t, 0));
     for (int t = 0; t < tiles; t++) fam[1].push_back(make_int4(s, 3, t, 0));
+  }
+}
+
+// The charge carriers of the electrified runs, one WENO field an item (groups 13-16), on the plan's tile.
+void charge_items(sg_context* ctx, const std::vector<int>& slots, int TX, int TY, std::vector<int4>& out) {
+  out.clear();
+  for (int s : slots) {
+    const Run& r = ctx->runs[s];
+    if (!(r.desc.flags & RF_ELEC)) continue;
+    const int tiles = ((r.nx + TX - 1) / TX) * ((r.ny + TY - 1) / TY);
+    for (int g = 13; g < 17; g++) for (int t = 0; t < tiles; t++) out.push_back(make_int4(s, g, t, 0));
   }
 }
 
@@ -374,6 +402,7 @@ int build_plan(sg_context* ctx, const std::vector<int>& slots, Plan& P) {
     all[FAM_RUNS].push_back(make_int4(s, 0, 0, 0));
     if (r.desc.flags & RF_REFINE) P.refine = true; else P.unrefined = true;
     if (r.desc.flags & RF_ROTATION) P.rotation = true;
+    if (r.desc.flags & RF_ELEC) P.elec = true;
   }
   // mixing items: (run, tile, z0, z1), the column in four level ranges
   P.mixTX = all40 ? 40 : 32; P.mixTY = 8;
@@ -396,6 +425,7 @@ int build_plan(sg_context* ctx, const std::vector<int>& slots, Plan& P) {
   P.bulk = P.minb == 2 && ctx->bulk && transport_bulk_ok(P.TX, P.TY, P.minnx, P.nx4) &&
            std::max(transport_smem_bulk(TK_WENO, P.wenoG, P.TX, P.TY), transport_smem_bulk(TK_DYN, 4, P.TX, P.TY)) <= (size_t)ctx->maxSmem;
   transport_items(ctx, slots, P.TX, P.TY, P.wenoG, all + FAM_T_WENO);
+  charge_items(ctx, slots, P.TX, P.TY, all[FAM_T_CHG]);
   int st = upload_items(ctx, P, all);
   if (st != SG_OK) return st;
   return ctx->autotune && !ctx->pinned[0] ? autotune_transport(ctx, P) : SG_OK;
@@ -403,6 +433,13 @@ int build_plan(sg_context* ctx, const std::vector<int>& slots, Plan& P) {
 
 Launch lx(sg_context* ctx, const Plan& P, int fam, int capPerSm = 8) {
   return Launch{ctx->d_runs, P.items + P.off[fam], P.cnt[fam], ctx->sms * capPerSm, ctx->stream};
+}
+
+// The charge carriers' WENO transport of one RK3 stage (electrified runs; per-thread copies, one field an item).
+void launch_charges(sg_context* ctx, const Plan& P, int in, int out, float frac, int stage, cudaStream_t stream) {
+  Launch C = lx(ctx, P, FAM_T_CHG);
+  C.cap = C.n; C.stream = stream;
+  if (C.n) launch_transport(C, TK_WENO, 1, P.minb, in, out, frac, stage, P.TX, P.TY, false, ctx->edgeWarps);
 }
 
 // Transport launches: one block per item, so the hardware block scheduler balances items of uneven cost (tiles of
@@ -414,6 +451,7 @@ void launch_transport_kinds(sg_context* ctx, const Plan& P, int in, int out, flo
     Launch L = lx(ctx, P, fams[k]);
     L.cap = L.n;
     if (L.n) launch_transport(L, k, P.wenoG, P.minb, in, out, frac, stage, P.TX, P.TY, P.bulk, ctx->edgeWarps);
+    if (k == 0) launch_charges(ctx, P, in, out, frac, stage, ctx->stream);
     hook(hookBase + k);
   }
 }
@@ -483,11 +521,12 @@ int autotune_transport(sg_context* ctx, Plan& P) {
   P.TX = best[0]; P.TY = best[1]; P.wenoG = best[2]; P.minb = best[3]; P.bulk = best[4] != 0; P.tuned = true;
   std::vector<int4> all[FAM_COUNT];
   for (int f = 0; f < FAM_COUNT; f++) {  // keep the other families, rebuild the transport ones
-    if (f == FAM_T_WENO || f == FAM_T_DYN) continue;
+    if (f == FAM_T_WENO || f == FAM_T_DYN || f == FAM_T_CHG) continue;
     all[f].resize(P.cnt[f]);
     if (P.cnt[f]) CK(cudaMemcpy(all[f].data(), P.items + P.off[f], P.cnt[f] * sizeof(int4), cudaMemcpyDeviceToHost));
   }
   transport_items(ctx, P.slots, P.TX, P.TY, P.wenoG, all + FAM_T_WENO);
+  charge_items(ctx, P.slots, P.TX, P.TY, all[FAM_T_CHG]);
   return upload_items(ctx, P, all);
 }
 
@@ -556,7 +595,7 @@ void enqueue_part(sg_context* ctx, const Plan& P, int part, Hook hook) {
   } else if (part == 3) {
     launch_fill_partial(node, B); hook(11);
     launch_fill_final(runs); hook(12);
-    launch_physics(node, B, C); hook(13);
+    launch_physics(node, B, C, P.elec); hook(13);
   } else if (part == 4) {
     launch_viscosity(node, C); hook(14);
     Launch mx = lx(ctx, P, FAM_MIX);
@@ -604,6 +643,7 @@ void enqueue_dynamics_graph(sg_context* ctx, const Plan& P) {
   for (int s = 0; s < 3; s++) {
     if (s == 2) cudaStreamWaitEvent(side, ev[5], 0);     // dynamics stage 1 has read set B's scalars
     if (W.n) launch_transport(W, TK_WENO, P.wenoG, P.minb, in[s], out[s], (float)RK3[s], s, P.TX, P.TY, P.bulk, ctx->edgeWarps);
+    launch_charges(ctx, P, in[s], out[s], (float)RK3[s], s, side);
     cudaEventRecord(ev[2 + s], side);
     // the stage's input scalars: for stage 0 the step-start fields after the sedimentation, later the WENO stage's
     cudaStreamWaitEvent(main, s == 0 ? ev[6] : ev[1 + s], 0);
@@ -678,6 +718,21 @@ int slots_of(sg_context* ctx, const sg_run* runs, int n, std::vector<int>& slots
   return SG_OK;
 }
 
+// The lightning of an electrified run after its step: the flash time is the step's end (time + dt, src/core/model.ts:1542);
+// `advance`: the step moved the run's time by dt. Runs that failed or are not electrified are left alone.
+int discharge_run(sg_context* ctx, Run& r, bool advance) {
+  if (!r.lgt) return SG_OK;
+  if (advance) r.time += r.dt;
+  unsigned long long failed = 0;
+  CK(cudaMemcpyAsync(&failed, r.desc.cnt + C_FAILED, sizeof(failed), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (failed) return SG_OK;
+  std::string err;
+  const int st = lightning_discharge(ctx->stream, &r.grid, r.desc, *r.lgt, r.time, r.dt, flash_limit(r.dt), &err);
+  if (st != SG_OK) return fail(ctx, st, "lightning: " + err);
+  return SG_OK;
+}
+
 int batch_step(sg_context* ctx, const sg_run* runs, int n, int nsteps, bool wait) {
   if (nsteps < 0) return fail(ctx, SG_ERR_INVALID, "negative step count");
   std::vector<int> slots;
@@ -686,7 +741,15 @@ int batch_step(sg_context* ctx, const sg_run* runs, int n, int nsteps, bool wait
   Plan* P = get_plan(ctx, slots, &st);
   if (!P) return st;
   if ((st = ensure_graph(ctx, *P))) return st;
-  for (int s = 0; s < nsteps; s++) CK(cudaGraphLaunch(P->exec, ctx->stream));
+  if (P->elec) {
+    // electrified runs: after each step their lightning (host-stepped flash stages, src/core/model.ts:1130-1133)
+    for (int s = 0; s < nsteps; s++) {
+      CK(cudaGraphLaunch(P->exec, ctx->stream));
+      for (int slot : P->slots) if ((st = discharge_run(ctx, ctx->runs[slot], true)) != SG_OK) return st;
+    }
+  } else {
+    for (int s = 0; s < nsteps; s++) CK(cudaGraphLaunch(P->exec, ctx->stream));
+  }
   if (wait) CK(cudaStreamSynchronize(ctx->stream));
   CK(cudaGetLastError());
   return SG_OK;
@@ -784,13 +847,15 @@ int sg_context_fail(sg_context* ctx, int code, const char* message) { return fai
 extern "C" {
 
 uint64_t sg_run_bytes(const sg_grid* grid) { return grid ? layout(grid->nx, grid->ny, grid->nz).total : 0; }
+uint64_t sg_run_bytes_electrified(const sg_grid* grid) { return grid ? layout(grid->nx, grid->ny, grid->nz, true).total : 0; }
 
 int sg_run_create(sg_context* ctx, const sg_grid* g, const sg_base_state* b, const sg_switches* sw, const float* const* init, sg_run* out) {
   if (!ctx || !out) return SG_ERR_INVALID;
   int st = validate(ctx, g, b, sw);
   if (st) return st;
   cudaSetDevice(ctx->device);
-  Layout Lo = layout(g->nx, g->ny, g->nz);
+  const bool elec = sw->lightning && sw->ice;  // electrified() (src/core/model.ts:1316)
+  Layout Lo = layout(g->nx, g->ny, g->nz, elec);
   // Admission by the HBM budget (pooled allocations of a retired run count as free).
   char* mem = nullptr;
   auto pit = ctx->pool.find(Lo.total);
@@ -816,6 +881,8 @@ int sg_run_create(sg_context* ctx, const sg_grid* g, const sg_base_state* b, con
   HostTables T; RunDesc& d = r.desc; d = RunDesc{};
   build_tables(g, b, sw, T, d);
   d.slot = slot;
+  d.nf = elec ? NFE : NF;
+  if (elec) d.flags |= RF_ELEC;
   d.fld = (float*)(mem + Lo.fld); d.faces = (float*)(mem + Lo.faces); d.kmkh = (float*)(mem + Lo.kmkh); d.phi = (float*)(mem + Lo.phi);
   d.pres = (float*)(mem + Lo.pres); d.pres2 = (float*)(mem + Lo.pres2); d.spec = (float2*)(mem + Lo.spec); d.cols = (float*)(mem + Lo.cols);
   d.lv = (const float*)(mem + Lo.lv); d.lv64 = (const double*)(mem + Lo.lv64); d.tri_face = (const TriAB*)(mem + Lo.triF);
@@ -823,6 +890,16 @@ int sg_run_create(sg_context* ctx, const sg_grid* g, const sg_base_state* b, con
   d.twy = (const float2*)(mem + Lo.twy); d.scr = (float*)(mem + Lo.scr); d.part = (double*)(mem + Lo.part); d.acc = (double*)(mem + Lo.acc);
   d.cnt = (unsigned long long*)(mem + Lo.cnt);
   d.diag = (float*)(mem + Lo.diag); d.rot = (double*)(mem + Lo.rot);
+  r.lgt.reset();
+  if (elec) {
+    d.vfall = (float*)(mem + Lo.vfall); d.ez = (float*)(mem + Lo.ez); d.cpart = (double*)(mem + Lo.cpart);
+    r.lgt = std::make_unique<LgtHost>();
+    lightning_bind(mem + Lo.lgt, g->nx, g->ny, g->nz, r.lgt->dev);
+    r.lgt->seed = (uint32_t)sw->lightning_seed; r.lgt->corona = sw->corona != 0;
+    r.zs.assign(g->zs, g->zs + g->nz); r.dzs.assign(g->dzs, g->dzs + g->nz - 1); r.hz.assign(g->hz, g->hz + g->nz);
+    r.grid = *g; r.grid.zs = r.zs.data(); r.grid.dzs = r.dzs.data(); r.grid.hz = r.hz.data();
+  }
+  r.time = 0; r.dt = sw->dt;
   auto H2D = [&](size_t off, const void* src, size_t bytes) { return cudaMemcpyAsync(mem + off, src, bytes, cudaMemcpyHostToDevice, ctx->stream); };
   CK(cudaMemsetAsync(mem, 0, Lo.total, ctx->stream));
   CK(H2D(Lo.lv, T.lv.data(), T.lv.size() * 4)); CK(H2D(Lo.lv64, T.lv64.data(), T.lv64.size() * 8));
@@ -830,6 +907,10 @@ int sg_run_create(sg_context* ctx, const sg_grid* g, const sg_base_state* b, con
   CK(H2D(Lo.triP, T.triP.data(), T.triP.size() * 16)); CK(H2D(Lo.triP + T.triP.size() * 16, T.triPc.data(), T.triPc.size() * 8));
   CK(H2D(Lo.ab, T.ab.data(), T.ab.size() * 16)); CK(H2D(Lo.twx, T.twx.data(), T.twx.size() * 8)); CK(H2D(Lo.twy, T.twy.data(), T.twy.size() * 8));
   CK(cudaMemcpyAsync(ctx->d_runs + slot, &d, sizeof(RunDesc), cudaMemcpyHostToDevice, ctx->stream));
+  if (elec) {
+    const int e = lightning_init(ctx->stream, &r.grid, b->rho, *r.lgt);
+    if (e) return fail(ctx, SG_ERR_DEVICE, std::string("lightning tables: ") + cudaGetErrorString((cudaError_t)e));
+  }
   {
     const size_t n = (size_t)g->nx * g->ny * g->nz;
     r.nNode = (int)((n + CHUNK - 1) / CHUNK);
@@ -854,14 +935,16 @@ int sg_run_write_fields(sg_context* ctx, sg_run run, uint32_t mask, const float*
   if (!r) return fail(ctx, SG_ERR_NOT_FOUND, "no run " + std::to_string(run));
   cudaSetDevice(ctx->device);
   size_t n = (size_t)r->nx * r->ny * r->nz;
-  for (int f = 0; f < NF; f++) {
+  const int nf = r->desc.nf;
+  if (mask >> nf) return fail(ctx, SG_ERR_INVALID, "field mask beyond the run's fields (the charges need an electrified run)");
+  for (int f = 0; f < nf; f++) {
     if (!(mask & (1u << f))) continue;
     if (!host[f]) return fail(ctx, SG_ERR_INVALID, "null field pointer");
     // theta arrives full; it is staged in set B and converted to its departure in set A.
-    float* dst = r->desc.fld + (size_t)(f == THETA ? NF + THETA : f) * n;
+    float* dst = field(r->desc, f == THETA ? 1 : 0, f);
     CK(cudaMemcpyAsync(dst, host[f], n * 4, cudaMemcpyHostToDevice, ctx->stream));
   }
-  if (mask & (1u << THETA)) launch_theta_in(node_launch(ctx, *r), r->desc.fld + (size_t)(NF + THETA) * n);
+  if (mask & (1u << THETA)) launch_theta_in(node_launch(ctx, *r), field(r->desc, 1, THETA));
   CK(cudaStreamSynchronize(ctx->stream));
   return SG_OK;
 }
@@ -872,11 +955,13 @@ int sg_run_read_fields(sg_context* ctx, sg_run run, uint32_t mask, float* const*
   if (!r) return fail(ctx, SG_ERR_NOT_FOUND, "no run " + std::to_string(run));
   cudaSetDevice(ctx->device);
   size_t n = (size_t)r->nx * r->ny * r->nz;
-  if (mask & (1u << THETA)) launch_theta_out(node_launch(ctx, *r), r->desc.fld + (size_t)(NF + THETA) * n);
-  for (int f = 0; f < NF; f++) {
+  const int nf = r->desc.nf;
+  if (mask >> nf) return fail(ctx, SG_ERR_INVALID, "field mask beyond the run's fields (the charges need an electrified run)");
+  if (mask & (1u << THETA)) launch_theta_out(node_launch(ctx, *r), field(r->desc, 1, THETA));
+  for (int f = 0; f < nf; f++) {
     if (!(mask & (1u << f))) continue;
     if (!host[f]) return fail(ctx, SG_ERR_INVALID, "null field pointer");
-    const float* src = r->desc.fld + (size_t)(f == THETA ? NF + THETA : f) * n;
+    const float* src = field(r->desc, f == THETA ? 1 : 0, f);
     CK(cudaMemcpyAsync(host[f], src, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
   }
   CK(cudaStreamSynchronize(ctx->stream));
@@ -901,7 +986,7 @@ int batch_fields(sg_context* ctx, const sg_run* runs, int n, uint32_t mask, floa
       if (!(mask & (1u << f))) continue;
       float* h = host[(size_t)k * NF + f];
       if (!h) return fail(ctx, SG_ERR_INVALID, "null field pointer");
-      float* dev = r->desc.fld + (size_t)(f == THETA ? NF + THETA : f) * nn;  // theta staged in set B
+      float* dev = field(r->desc, f == THETA ? 1 : 0, f);  // theta staged in set B
       if (write) CK(cudaMemcpyAsync(dev, h, nn * 4, cudaMemcpyHostToDevice, ctx->stream));
       else CK(cudaMemcpyAsync(h, dev, nn * 4, cudaMemcpyDeviceToHost, ctx->stream));
     }
@@ -1014,6 +1099,7 @@ static int batch_step_io(sg_context* ctx, const sg_run* runs, int n, uint32_t ma
     x.count = (int)((int64_t)n * (g + 1) / groups) - x.first;
     const std::vector<int> slots(all.begin() + x.first, all.begin() + x.first + x.count);
     if (!(x.P = get_plan(ctx, slots, &st))) return st;
+    if (x.P->elec) return fail(ctx, SG_ERR_UNSUPPORTED, "host round trips of electrified runs: step them with sg_batch_step (the lightning is host-stepped)");
     if ((st = ensure_graph(ctx, *x.P)) != SG_OK) return st;
     if ((st = pack_items(ctx, runs + x.first, x.count, mask, x.items, x.total)) != SG_OK) return st;
     x.off = total;
@@ -1144,6 +1230,7 @@ int sg_run_load_state(sg_context* ctx, sg_run run, const uint8_t* image, size_t 
   r->waterStart = h.water[4];
   // the model time and the time the rotation has held; the rotation recomputed from the fields (state.ts:74-76)
   const double tp[2] = {h.time, h.persisted};
+  r->time = h.time;
   CK(cudaMemcpyAsync(r->desc.rot + R_TIME, &tp[0], sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(r->desc.rot + R_PERSISTED, &tp[1], sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
@@ -1328,7 +1415,7 @@ int sg_run_retire(sg_context* ctx, sg_run run) {
   drop_packs_with(ctx, run);
   ctx->used -= r->bytes;
   ctx->pool.emplace(r->bytes, r->mem); ctx->pooled += r->bytes;
-  r->live = false; r->mem = nullptr;
+  r->live = false; r->mem = nullptr; r->lgt.reset();
   ctx->freeSlots.push_back(run);
   return SG_OK;
 }
@@ -1367,6 +1454,7 @@ int sg_time_steps(sg_context* ctx, const sg_run* runs, int n, int nsteps, int us
   for (int s = 0; s < nsteps; s++) {
     if (use_graph) CK(cudaGraphLaunch(P->exec, ctx->stream));
     else enqueue_step(ctx, *P, [](int) {});
+    if (P->elec) for (int slot : P->slots) if ((st = discharge_run(ctx, ctx->runs[slot], true)) != SG_OK) return st;
   }
   CK(cudaEventRecord(b, ctx->stream));
   CK(cudaEventSynchronize(b));
@@ -1414,6 +1502,67 @@ int sg_run_divergence(sg_context* ctx, sg_run run, double* max_abs_div) {
   CK(cudaMemcpyAsync(max_abs_div, ctx->d_scalar, 8, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   if (!std::isfinite(*max_abs_div)) return fail(ctx, SG_ERR_NONFINITE, "the run's velocities hold a non-finite value");
+  return SG_OK;
+}
+
+int sg_run_charge(sg_context* ctx, sg_run run, sg_charge_state* out) {
+  if (!ctx || !out) return SG_ERR_INVALID;
+  Run* r = find(ctx, run);
+  if (!r) return fail(ctx, SG_ERR_NOT_FOUND, "no run " + std::to_string(run));
+  cudaSetDevice(ctx->device);
+  std::memset(out, 0, sizeof(*out));
+  if (!r->lgt) return SG_OK;
+  double acc[A_COUNT];
+  CK(cudaMemcpyAsync(acc, r->desc.acc, sizeof(acc), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  out->ground = acc[A_CHG_GROUND]; out->separated = acc[A_CHG_SEPARATED]; out->ic = acc[A_CHG_IC];
+  out->cg_negative = acc[A_CHG_CG_NEG]; out->cg_positive = acc[A_CHG_CG_POS]; out->precipitation = acc[A_CHG_PRECIP];
+  out->conduction = acc[A_CHG_CONDUCTION]; out->flashes_ic = (int64_t)acc[A_FLASH_IC]; out->flashes_cg = (int64_t)acc[A_FLASH_CG];
+  out->last_flashes = (int32_t)r->lgt->last.size(); out->electrified = 1;
+  return SG_OK;
+}
+
+int sg_run_flashes(sg_context* ctx, sg_run run, sg_flash* out, int cap, int* count) {
+  if (!ctx || !count || cap < 0 || (cap > 0 && !out)) return SG_ERR_INVALID;
+  Run* r = find(ctx, run);
+  if (!r) return fail(ctx, SG_ERR_NOT_FOUND, "no run " + std::to_string(run));
+  *count = r->lgt ? (int)r->lgt->last.size() : 0;
+  for (int k = 0; k < *count && k < cap; k++) {
+    const FlashRecord& f = r->lgt->last[k];
+    sg_flash& o = out[k];
+    std::memset(&o, 0, sizeof(o));
+    o.time = f.time; o.potential = f.potential; o.charge = f.charge; o.moment = f.moment;
+    for (size_t j = 0; j < f.strokes.size() && j < 4; j++) o.stroke_charge[j] = f.strokes[j];
+    o.cg = f.cg ? 1 : 0; o.start = f.start; o.ground = f.ground; o.nodes = (int32_t)f.nodes.size(); o.strokes = (int32_t)f.strokes.size();
+  }
+  return SG_OK;
+}
+
+int sg_run_flash_channel(sg_context* ctx, sg_run run, int k, int32_t* nodes, int32_t* parent, int32_t* polarity, int cap) {
+  if (!ctx || cap < 0) return SG_ERR_INVALID;
+  Run* r = find(ctx, run);
+  if (!r) return fail(ctx, SG_ERR_NOT_FOUND, "no run " + std::to_string(run));
+  if (!r->lgt || k < 0 || k >= (int)r->lgt->last.size()) return fail(ctx, SG_ERR_INVALID, "no flash " + std::to_string(k) + " in the last step");
+  const FlashRecord& f = r->lgt->last[k];
+  const int m = std::min(cap, (int)f.nodes.size());
+  for (int c = 0; c < m; c++) {
+    if (nodes) nodes[c] = f.nodes[c];
+    if (parent) parent[c] = f.parent[c];
+    if (polarity) polarity[c] = f.polarity[c];
+  }
+  return SG_OK;
+}
+
+int sg_run_discharge(sg_context* ctx, sg_run run, double time, double dt) {
+  if (!ctx || !(dt > 0) || !std::isfinite(time)) return SG_ERR_INVALID;
+  Run* r = find(ctx, run);
+  if (!r) return fail(ctx, SG_ERR_NOT_FOUND, "no run " + std::to_string(run));
+  if (!r->lgt) return fail(ctx, SG_ERR_INVALID, "the run is not electrified");
+  cudaSetDevice(ctx->device);
+  std::string err;
+  const int st = lightning_discharge(ctx->stream, &r->grid, r->desc, *r->lgt, time, dt, flash_limit(dt), &err);
+  if (st != SG_OK) return fail(ctx, st, "lightning: " + err);
+  CK(cudaStreamSynchronize(ctx->stream));
   return SG_OK;
 }
 
@@ -1467,11 +1616,12 @@ int sg_debug_step_part(sg_context* ctx, sg_run run, int part) {
   return SG_OK;
 }
 int sg_debug_read_set(sg_context* ctx, sg_run run, int set, int field, float* host) {
-  if (!ctx || !host || set < 0 || set > 2 || field < 0 || field >= NF) return SG_ERR_INVALID;
+  if (!ctx || !host || set < 0 || set > 2 || field < 0) return SG_ERR_INVALID;
   Run* r = find(ctx, run);
   if (!r) return fail(ctx, SG_ERR_NOT_FOUND, "no run");
   size_t n = (size_t)r->nx * r->ny * r->nz;
-  CK(cudaMemcpyAsync(host, r->desc.fld + ((size_t)set * NF + field) * n, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  if (field >= r->desc.nf) return fail(ctx, SG_ERR_INVALID, "no such field in this run");
+  CK(cudaMemcpyAsync(host, sg::field(r->desc, set, field), n * 4, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   return SG_OK;
 }

@@ -14,7 +14,7 @@ from typing import Dict, Iterable, List, Optional, Sequence
 
 import numpy as np
 
-from .scenarios import CARRIED, RunSpec
+from .scenarios import CARRIED, CHARGES, RunSpec
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libstormgpu.so")
@@ -44,7 +44,18 @@ class SgSwitches(C.Structure):
                 ("frame_v", C.c_double)] + [(k, C.c_int32) for k in ("loading", "evaporation", "rain_formation",
                                                                          "anisotropic", "vertical_dz", "durran_klemp",
                                                                          "pressure_in_stages", "ice", "refine_projection",
-                                                                         "rotation")]
+                                                                         "rotation", "lightning", "corona", "lightning_seed",
+                                                                         "reserved2")]
+
+
+class SgChargeState(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("ground", "separated", "ic", "cg_negative", "cg_positive", "precipitation", "conduction")] + \
+               [("flashes_ic", C.c_int64), ("flashes_cg", C.c_int64), ("last_flashes", C.c_int32), ("electrified", C.c_int32)]
+
+
+class SgFlash(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("time", "potential", "charge", "moment")] + [("stroke_charge", C.c_double * 4)] + \
+               [(k, C.c_int32) for k in ("cg", "start", "ground", "nodes", "strokes", "reserved")]
 
 
 class SgStateInfo(C.Structure):
@@ -70,6 +81,7 @@ class SgCounters(C.Structure):
 
 _lib = None
 _lock = threading.Lock()
+ALL_FIELDS = tuple(CARRIED) + tuple(CHARGES)   # field ids of the C ABI (charges: electrified runs)
 _FP = C.POINTER(C.c_float)
 
 
@@ -138,6 +150,12 @@ def load():
             L.sg_run_read_swaths.argtypes = [vp, C.c_int32, _FP, _FP]
             L.sg_run_reset_swaths.argtypes = [vp, C.c_int32]
             L.sg_run_diagnostics.argtypes = [vp, C.c_int32, C.POINTER(SgDiagnostics)]
+            L.sg_run_bytes_electrified.restype = u64
+            L.sg_run_bytes_electrified.argtypes = [C.POINTER(SgGrid)]
+            L.sg_run_charge.argtypes = [vp, C.c_int32, C.POINTER(SgChargeState)]
+            L.sg_run_flashes.argtypes = [vp, C.c_int32, C.POINTER(SgFlash), i32, C.POINTER(C.c_int)]
+            L.sg_run_flash_channel.argtypes = [vp, C.c_int32, i32, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32), i32]
+            L.sg_run_discharge.argtypes = [vp, C.c_int32, C.c_double, C.c_double]
             _lib = L
     return _lib
 
@@ -157,18 +175,20 @@ class _Packed:
         self.base = SgBase(*[dp(a) for a in self.keep[3:]])
         self.switches = SgSwitches(sw.dt, sw.coriolis, sw.wind_relaxation, sw.sponge_rate, sw.sponge_start, sw.cs, sw.drag_cd(g),
                                    sw.frame_u, sw.frame_v, sw.loading, sw.evaporation, sw.rain_formation, sw.anisotropic,
-                                   sw.vertical_dz, sw.durran_klemp, sw.pressure_in_stages, 1, sw.refine_projection,
-                                   sw.rotation)
+                                   sw.vertical_dz, sw.durran_klemp, sw.pressure_in_stages, getattr(sw, "ice", 1),
+                                   sw.refine_projection, sw.rotation, getattr(sw, "lightning", 0), getattr(sw, "corona", 1),
+                                   getattr(sw, "lightning_seed", 43), 0)
         self.fields = [np.ascontiguousarray(spec.fields[k], dtype=np.float32).ravel() for k in CARRIED]
         self.ptrs = (_FP * len(CARRIED))(*[a.ctypes.data_as(_FP) for a in self.fields])
 
 
-def run_bytes(grid) -> int:
-    """Bytes of HBM one run of this grid takes in a context (sg_run_bytes): what admission by budget counts."""
+def run_bytes(grid, electrified: bool = False) -> int:
+    """Bytes of HBM one run of this grid takes in a context (sg_run_bytes; sg_run_bytes_electrified with its charge
+    carriers and lightning buffers): what admission by budget counts."""
     zs, dzs, hz = _f64(grid.zs), _f64(grid.dzs), _f64(grid.hz)
     dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
     g = SgGrid(grid.nx, grid.ny, grid.nz, 0, grid.dx, grid.dy, grid.height, dp(zs), dp(dzs), dp(hz))
-    return int(load().sg_run_bytes(C.byref(g)))
+    return int((load().sg_run_bytes_electrified if electrified else load().sg_run_bytes)(C.byref(g)))
 
 
 class Context:
@@ -335,6 +355,9 @@ class Run:
         self.id = rid.value
         self.time = 0.0
         self.live = True
+        charges = {k: v for k, v in spec.fields.items() if k in CHARGES}
+        if charges:
+            self.write(charges)
 
     def retire(self):
         if self.live:
@@ -349,9 +372,9 @@ class Run:
         names = list(names)
         out = out if out is not None else {k: np.empty(self.grid.n, np.float32) for k in names}
         mask = 0
-        ptrs = (_FP * len(CARRIED))()
+        ptrs = (_FP * len(ALL_FIELDS))()
         for k in names:
-            j = CARRIED.index(k)
+            j = ALL_FIELDS.index(k)
             mask |= 1 << j
             ptrs[j] = out[k].ctypes.data_as(_FP)
         self.ctx.check(load().sg_run_read_fields(self.ctx.h, self.id, mask, ptrs), "read fields")
@@ -359,10 +382,10 @@ class Run:
 
     def write(self, fields: Dict[str, np.ndarray]):
         mask = 0
-        ptrs = (_FP * len(CARRIED))()
+        ptrs = (_FP * len(ALL_FIELDS))()
         keep = []
         for k, a in fields.items():
-            j = CARRIED.index(k)
+            j = ALL_FIELDS.index(k)
             a = np.ascontiguousarray(a, dtype=np.float32).ravel()
             keep.append(a)
             mask |= 1 << j
@@ -387,6 +410,38 @@ class Run:
         if rc not in (0, 5):
             self.ctx.check(rc, "status")
         return {k: getattr(c, k) for k, _ in SgCounters._fields_ if k != "reserved"}
+
+    def charge(self) -> dict:
+        """The charge budget and flash counts (chargeGround, charge, flashCount, src/core/model.ts:218-241)."""
+        c = SgChargeState()
+        self.ctx.check(load().sg_run_charge(self.ctx.h, self.id, C.byref(c)), "charge")
+        return {k: getattr(c, k) for k, _ in SgChargeState._fields_}
+
+    def flashes(self, channels: bool = True) -> List[dict]:
+        """The last step's flashes (Flash records, src/core/lightning.ts:69-106), with their channels."""
+        count = C.c_int()
+        self.ctx.check(load().sg_run_flashes(self.ctx.h, self.id, None, 0, C.byref(count)), "flashes")
+        n = count.value
+        recs = (SgFlash * max(1, n))()
+        self.ctx.check(load().sg_run_flashes(self.ctx.h, self.id, recs, n, C.byref(count)), "flashes")
+        out = []
+        for k in range(n):
+            f = recs[k]
+            d = dict(time=f.time, kind="CG" if f.cg else "IC", start=f.start, ground=f.ground, potential=f.potential,
+                     charge=f.charge, moment=f.moment, strokes=np.array(list(f.stroke_charge)[:f.strokes]))
+            if channels:
+                m = f.nodes
+                nodes, parent, polarity = (np.empty(m, np.int32) for _ in range(3))
+                ip = C.POINTER(C.c_int32)
+                self.ctx.check(load().sg_run_flash_channel(self.ctx.h, self.id, k, nodes.ctypes.data_as(ip), parent.ctypes.data_as(ip),
+                                                           polarity.ctypes.data_as(ip), m), "flash channel")
+                d.update(nodes=nodes, parent=parent, polarity=polarity)
+            out.append(d)
+        return out
+
+    def discharge(self, time: float, dt: float):
+        """AtmosphereModel.discharge on the run's charge as it stands (src/core/model.ts:1537-1552), at model time `time`."""
+        self.ctx.check(load().sg_run_discharge(self.ctx.h, self.id, time, dt), "discharge")
 
     def debug_part(self, part: int):
         """Run one part of the step (1 beginStep, 2 dynamics, 3 physicsStep, 4 mixStep, 5 final projection)."""

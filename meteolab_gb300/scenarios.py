@@ -22,6 +22,8 @@ from .grid import Grid
 
 #: The transported fields in the order the step carries them (src/core/model.ts:1319-1335, ice on, no lightning).
 CARRIED = ("rain", "snow", "graupel", "hail", "u", "v", "w", "theta", "q", "cloud", "ice", "iceNumber", "cold")
+# the charge carriers of an electrified run, C/kg (field ids 13-16 of the C ABI; src/core/model.ts:210)
+CHARGES = ("chargeIce", "chargeGraupel", "chargeRain", "chargeAir")
 #: The fields the subgrid turbulence mixes (src/core/model.ts:1338-1344).
 MIXED = ("u", "v", "w", "theta", "q", "cloud", "ice", "iceNumber")
 SMAGORINSKY = 0.18

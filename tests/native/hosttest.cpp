@@ -9,10 +9,26 @@
 #include "../../meteolab_gb300/csrc/sg_fft.cuh"
 #include "../../meteolab_gb300/csrc/sg_physics.cuh"
 #include "../../meteolab_gb300/csrc/sg_tile_copies.cuh"
+#include "../../meteolab_gb300/csrc/sg_charge.cuh"
 
 using namespace sg;
 
 extern "C" {
+
+// the charging of the physics kernel (sg_charge.cuh), FP32
+float ht_takahashi(float tc, float lwc) { return charge::takahashi(tc, lwc); }
+float ht_charging(float tc, float rho, float cloud, float ice, float snow, float graupel, float hail, float snowFall, int wetG, int wetH, float crystals) {
+  return charge::chargingRate(tc, rho, cloud, ice, snow, graupel, hail, snowFall, wetG != 0, wetH != 0, crystals);
+}
+float ht_inductive(float tc, float rho, float cloud, float graupel, float hail, float ez, float rimerCharge, int wetG, int wetH) {
+  return charge::inductiveRate(tc, rho, cloud, graupel, hail, ez, rimerCharge, wetG != 0, wetH != 0);
+}
+void ht_transfer(float* c, const float* before, const float* after) {
+  float cc[4] = {c[0], c[1], c[2], c[3]};
+  const float b[4] = {before[0], before[1], before[2], before[3]}, a[4] = {after[0], after[1], after[2], after[3]};
+  charge::transferCharge(cc, b, a);
+  for (int k = 0; k < 4; k++) c[k] = cc[k];
+}
 
 float ht_weno(float a, float b, float c, float d, float e) { return weno5(a, b, c, d, e); }
 float ht_upwind(float a, float b, float c, float d, float e) { return upwind5(a, b, c, d, e); }

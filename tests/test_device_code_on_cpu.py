@@ -225,3 +225,58 @@ def test_bulk_tile_copies_cover_the_window_in_bounds(ht, nx, ny):
                     assert len(aux) == 2 * rows_on + 1 + (G * rows_on if s0 else 0)
                     total = G * int(ring[:, 3].sum()) + int(aux[:, 3].sum())
                     assert total == nb.value, (TX, TY, x0, y0, G, s0, total, nb.value)
+
+
+# ------------------------------------------------------------------ the charging (sg_charge.cuh)
+def test_takahashi_lookup_matches_oracle(ht):
+    ht.ht_takahashi.restype = C.c_float
+    ht.ht_takahashi.argtypes = [C.c_float, C.c_float]
+    rng = np.random.default_rng(3)
+    for tc, lwc in zip(rng.uniform(-42, 2, 400), np.exp(rng.uniform(np.log(.005), np.log(40), 400))):
+        tc, lwc = float(np.float32(tc)), float(np.float32(lwc))
+        ref = O.takahashi(tc, lwc)
+        assert abs(ht.ht_takahashi(tc, lwc) - ref) <= 1e-5 * max(1.0, abs(ref)), (tc, lwc)
+
+
+def test_charging_rates_match_oracle(ht):
+    """The device's FP32 Takahashi charging and inductive charging against the oracle's FP64, over mixed-phase states
+    (the model's own crystals, the snow's fall speed, both rimers, an upward and a downward field)."""
+    ht.ht_charging.restype = C.c_float
+    ht.ht_charging.argtypes = [C.c_float] * 8 + [C.c_int, C.c_int, C.c_float]
+    ht.ht_inductive.restype = C.c_float
+    ht.ht_inductive.argtypes = [C.c_float] * 7 + [C.c_int, C.c_int]
+    rng = np.random.default_rng(11)
+    checked = 0
+    for _ in range(600):
+        tc = float(np.float32(rng.uniform(-45, 3)))
+        rho = float(np.float32(rng.uniform(.4, 1.1)))
+        cloud, ice, snow, graupel, hail = (float(np.float32(v)) for v in rng.choice([0, 1], 5, p=[.15, .85]) * 10 ** rng.uniform(-6, -2.5, 5))
+        snow_fall = float(np.float32(rng.uniform(.3, 1.5)))
+        crystals = float(np.float32(10 ** rng.uniform(2, 5.5)))
+        wg, wh = (int(v) for v in rng.random(2) < .1)
+        ref = O.charging_rate(tc, rho, cloud, ice, snow, graupel, hail, snow_fall, wg, wh, crystals)
+        got = ht.ht_charging(tc, rho, cloud, ice, snow, graupel, hail, snow_fall, wg, wh, crystals)
+        assert abs(got - ref) <= 2e-4 * abs(ref) + 1e-20, (tc, rho, cloud, ice, snow, graupel, hail, got, ref)
+        ez = float(np.float32(rng.uniform(-8e4, 8e4)))
+        qr = float(np.float32(rng.uniform(-2e-9, 2e-9)))
+        ref = O.inductive_rate(tc, rho, cloud, graupel, hail, ez, qr, wg, wh)
+        got = ht.ht_inductive(tc, rho, cloud, graupel, hail, ez, qr, wg, wh)
+        assert abs(got - ref) <= 2e-4 * abs(ref) + 1e-22, (tc, got, ref)
+        checked += ref != 0
+    assert checked > 100
+
+
+def test_charge_transfer_matches_oracle_and_conserves(ht):
+    ht.ht_transfer.argtypes = [C.POINTER(C.c_float)] * 3
+    rng = np.random.default_rng(5)
+    for _ in range(500):
+        c = (rng.uniform(-5e-9, 5e-9, 4) * (rng.random(4) < .8)).astype(np.float32)
+        before = (10 ** rng.uniform(-6, -2.5, 4) * (rng.random(4) < .8)).astype(np.float32)
+        after = (before * rng.uniform(0, 2, 4) * (rng.random(4) < .9)).astype(np.float32)
+        ref = O.transfer_charge(c.astype(np.float64), before.astype(np.float64), after.astype(np.float64))
+        got = c.copy()
+        fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+        ht.ht_transfer(fp(got), fp(before), fp(after))
+        scale = float(np.max(np.abs(c))) + 1e-30
+        assert np.max(np.abs(got.astype(np.float64) - ref)) <= 1e-5 * scale
+        assert abs(float(np.sum(got.astype(np.float64))) - float(np.sum(c.astype(np.float64)))) <= 1e-5 * scale

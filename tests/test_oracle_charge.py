@@ -14,14 +14,9 @@ import numpy as np
 import pytest
 
 import pyoracle as O
-from meteolab_gb300.environment import Environment, SliderConfig
-from meteolab_gb300.grid import DEFAULT_GRID, create_grid
-from meteolab_gb300.scenarios import RunSpec, Switches, initial_fields
+from charge_cases import AIR, DT, GRID, mixed_phase, quiet_electrified, separated_charge, storm, total, with_fields
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-DT = 3.0
-# src/core/fixtures.ts:22-25: stable, unsaturated, sunless, no bubble
-QUIET = dict(lapseLow=6, lapseMid=6, lapseUpper=6, rhSurface=50, rhLow=40, rhMid=30, rhUpper=20)
 
 
 def close(a, b, digits):
@@ -133,37 +128,6 @@ def test_inductive_charging():  # :105-118
 
 
 # ------------------------------------------------------------------ lightning.test.ts
-GRID = create_grid(DEFAULT_GRID)
-AIR = Environment(SliderConfig(**QUIET), GRID).rho
-
-
-def storm(regions, grid=GRID, air=AIR):
-    """Gaussian charge regions over the domain centre, [height m, peak nC/m3], 2.5 km wide and 0.7 km deep: positive
-    on the ice carrier, negative on the graupel (lightning.test.ts:14-22), as FP32 carriers in C/kg."""
-    nx, ny, nz = grid.nx, grid.ny, grid.nz
-    zs = np.asarray(grid.zs)[:, None, None]
-    y = np.arange(ny)[None, :, None]
-    x = np.arange(nx)[None, None, :]
-    r2 = ((x - nx // 2) * grid.dx) ** 2 + ((y - ny // 2) * grid.dy) ** 2
-    air3 = np.asarray(air)[:, None, None]
-    acc = [np.zeros((nz, ny, nx), np.float32) for _ in range(4)]
-    for h, peak in regions:
-        k = 0 if peak > 0 else 1
-        term = peak * 1e-9 * np.exp(-r2 / 2500 ** 2 - ((zs - h) / 700) ** 2) / air3
-        acc[k] = (acc[k].astype(np.float64) + term).astype(np.float32)  # Float32Array +=
-    return [np.ascontiguousarray(a.ravel()) for a in acc]
-
-
-def total(carriers, grid=GRID, air=AIR):
-    s = 0.0
-    layer = grid.nx * grid.ny
-    for z in range(grid.nz):
-        w = air[z] * grid.dx * grid.dy * grid.hz[z]
-        for c in carriers:
-            s += float(np.sum(c[z * layer:(z + 1) * layer].astype(np.float64))) * w
-    return s
-
-
 def test_tripole_discharges_inside_the_cloud():  # lightning.test.ts:33-55
     carriers = storm([[10000, 2], [6500, -3.5], [3500, 1]])
     before = [c.copy() for c in carriers]
@@ -289,52 +253,15 @@ def test_corona_under_a_negative_charge():  # :139-157
 
 
 # ------------------------------------------------------------------ electrification.test.ts on the oracle's model
-def quiet_electrified(lightning=True, ice=True):
-    """A QUIET model (no bubble, no noise) with electrification switched on or off."""
-    grid = GRID
-    env = Environment(SliderConfig(**QUIET), grid)
-    sw = Switches(lightning=1 if lightning else 0)
-    spec = RunSpec(grid, env, sw, initial_fields(grid, env, 1, bubble=0.0, noise=0.0), 1, "quiet")
-    return spec
-
-
-def mixed_phase(spec, z0=5500, z1=7500):
-    """A block of mixed-phase cloud at the levels between z0 and z1 (electrification.test.ts:7-17)."""
-    g, env = spec.grid, spec.env
-    f = {k: v.copy() for k, v in spec.fields.items()}
-    nx, ny = g.nx, g.ny
-    for z in range(g.nz):
-        if not (z0 <= g.zs[z] <= z1):
-            continue
-        for y in range(ny // 2 - 3, ny // 2 + 3):
-            for x in range(nx // 2 - 3, nx // 2 + 3):
-                i = x + y * nx + z * g.layer
-                f["cloud"][i], f["ice"][i], f["snow"][i], f["graupel"][i] = 1e-3, 5e-4, 5e-4, 2e-3
-                t = float(f["theta"][i]) * env.exner[z] - 273.15
-                f["q"][i] = max(float(f["q"][i]), O.lib().orc_qsat(t, env.p[z]))
-    return f
-
-
 def model_with(spec, fields, fp64=False):
-    m = O.OracleModel(RunSpec(spec.grid, spec.env, spec.switches, fields, spec.seed, spec.label), fp64=fp64)
-    return m
-
-
-def separated_charge(m, spec):
-    g = spec.grid
-    s = 0.0
-    a, b, c = (m.get(k) for k in ("chargeIce", "chargeGraupel", "chargeRain"))
-    for z in range(g.nz):
-        sl = slice(z * g.layer, (z + 1) * g.layer)
-        s += float(np.sum(np.abs(a[sl]) + np.abs(b[sl]) + np.abs(c[sl]))) * spec.env.rho[z] * g.dx * g.dy * g.hz[z]
-    return s
+    return O.OracleModel(with_fields(spec, fields), fp64=fp64)
 
 
 def test_collisions_separate_charge_and_the_domain_stays_neutral():  # electrification.test.ts:20-33
     spec = quiet_electrified()
     m = model_with(spec, mixed_phase(spec))
     m.step(DT, 10)
-    sep = separated_charge(m, spec)
+    sep = separated_charge(m.get, spec)
     assert sep > 0
     graupel, ice = float(np.sum(m.get("chargeGraupel"))), float(np.sum(m.get("chargeIce")))
     assert abs(graupel) > 0 and np.sign(graupel) == -np.sign(ice)
