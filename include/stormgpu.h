@@ -257,6 +257,12 @@ int sg_run_flash_channel(sg_context* ctx, sg_run run, int k, int32_t* nodes, int
  * at model time `time`, at most flashLimit(dt) of them, then the conduction and corona over dt and the vertical field),
  * without a step: the seam of a caller that orders the step itself. The run's own time is not moved. */
 int sg_run_discharge(sg_context* ctx, sg_run run, double time, double dt);
+/* Diagnostics (no counterpart in the reference): the discharge's first search on the run's charge as it stands --
+ * the charge density (C/m3) and its potential (V), n FP64 values each (either may be null), the node of the strongest
+ * field and |E| / Einit there (-1 and 0: no field); last16 (nullable): the last flash's state record before the
+ * search (id, start node, front size, nodes, ground node, event, left the cloud, strokes, nodes before the last stage,
+ * potential, potential sum, neutralized, lowered, last stage's charge, flash charge, flash counter). Changes no field. */
+int sg_debug_lightning(sg_context* ctx, sg_run run, double* phi, double* rho, int32_t* best, double* ratio, double* last16);
 
 /* ---- stepping (replaces AtmosphereModel.step(dt) + time += dt, src/core/model.ts:873; gpuStep, src/gpu/step.ts:12) */
 int sg_run_step(sg_context* ctx, sg_run run, int nsteps);

@@ -477,6 +477,37 @@ static cudaError_t flash(cudaStream_t st, const RunDesc& R, LgtHost& H, int star
   return cudaSuccess;
 }
 
+int lightning_state(cudaStream_t st, LgtHost& H, double* out) {
+  LgtState S{};
+  if (read_state(st, H, S) != cudaSuccess) return SG_ERR_DEVICE;
+  const double v[16] = {(double)S.id, (double)S.start, (double)S.size, (double)S.nnodes, (double)S.ground, (double)S.event, (double)S.left,
+                        (double)S.strokes, (double)S.grown, S.potential, S.sum, S.neutralized, S.lowered, S.stage, S.charge, (double)H.flashId};
+  for (int k = 0; k < 16; k++) out[k] = v[k];
+  return SG_OK;
+}
+
+int lightning_probe(cudaStream_t st, const RunDesc& R, LgtHost& H, double* phi, double* rho, int* best, double* ratio) {
+  const LgtDev& L = H.dev;
+  const int nb = blocks(R.n, 256), ni = blocks(R.n - 2 * R.layer, 256);
+  k_lgt_cloudy<<<nb, 256, 0, st>>>(R, L);
+  k_lgt_rho<<<nb, 256, 0, st>>>(R, L);
+  elec_solve_launch(L.es, L.rho, L.phi, st);
+  k_lgt_search_reset<<<1, 32, 0, st>>>(L);
+  k_lgt_strongest<<<ni, 256, 0, st>>>(R, L, -1);
+  k_lgt_pick<<<ni, 256, 0, st>>>(R, L, -1);
+  LgtState S{};
+  cudaError_t e;
+  if ((e = read_state(st, H, S)) != cudaSuccess) return SG_ERR_DEVICE;
+  if (phi && (e = cudaMemcpyAsync(phi, L.phi, (size_t)R.n * 8, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return SG_ERR_DEVICE;
+  if (rho && (e = cudaMemcpyAsync(rho, L.rho, (size_t)R.n * 8, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return SG_ERR_DEVICE;
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess || (e = cudaGetLastError()) != cudaSuccess) return SG_ERR_DEVICE;
+  double r2;
+  std::memcpy(&r2, &S.maxBits, sizeof(double));
+  *best = S.maxBits ? S.best : -1;
+  *ratio = S.maxBits ? std::sqrt(r2) : 0;
+  return SG_OK;
+}
+
 int lightning_discharge(cudaStream_t st, const sg_grid* g, const RunDesc& R, LgtHost& H, double time, double dt, int limit, std::string* err) {
   const LgtDev& L = H.dev;
   const int nb = blocks(R.n, 256), ni = blocks(R.n - 2 * R.layer, 256);

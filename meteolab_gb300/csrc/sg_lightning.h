@@ -68,5 +68,11 @@ int lightning_init(cudaStream_t st, const sg_grid* g, const double* rho, LgtHost
 // The discharge after a step at model time `time` (the step's end) with step length dt: at most `limit` flashes, then
 // the conduction and corona over dt, then the vertical field. SG_OK, or SG_ERR_DEVICE with *err set.
 int lightning_discharge(cudaStream_t st, const sg_grid* g, const RunDesc& R, LgtHost& H, double time, double dt, int limit, std::string* err);
+// The discharge's first search alone (no flash): the charge density, its potential, the strongest field's node and
+// |E| / Einit there (-1 and 0 when there is no field) -- the diagnostics of sg_debug_lightning.
+int lightning_probe(cudaStream_t st, const RunDesc& R, LgtHost& H, double* phi, double* rho, int* best, double* ratio);
+// The last flash's state record: id, start, front size, nodes, ground, event, left, strokes, grown, potential, sum,
+// neutralized, lowered, the last stage's charge, the flash's charge, the flash counter.
+int lightning_state(cudaStream_t st, LgtHost& H, double* out16);
 
 }  // namespace sg

@@ -1553,6 +1553,19 @@ int sg_run_flash_channel(sg_context* ctx, sg_run run, int k, int32_t* nodes, int
   return SG_OK;
 }
 
+int sg_debug_lightning(sg_context* ctx, sg_run run, double* phi, double* rho, int32_t* best, double* ratio, double* last16) {
+  if (!ctx || !best || !ratio) return SG_ERR_INVALID;
+  Run* r = find(ctx, run);
+  if (!r) return fail(ctx, SG_ERR_NOT_FOUND, "no run " + std::to_string(run));
+  if (!r->lgt) return fail(ctx, SG_ERR_INVALID, "the run is not electrified");
+  cudaSetDevice(ctx->device);
+  if (last16 && lightning_state(ctx->stream, *r->lgt, last16) != SG_OK) return fail(ctx, SG_ERR_DEVICE, "lightning state");
+  int b = -1;
+  const int st = lightning_probe(ctx->stream, r->desc, *r->lgt, phi, rho, &b, ratio);
+  *best = b;
+  return st == SG_OK ? SG_OK : fail(ctx, st, "lightning probe");
+}
+
 int sg_run_discharge(sg_context* ctx, sg_run run, double time, double dt) {
   if (!ctx || !(dt > 0) || !std::isfinite(time)) return SG_ERR_INVALID;
   Run* r = find(ctx, run);

@@ -156,6 +156,8 @@ def load():
             L.sg_run_flashes.argtypes = [vp, C.c_int32, C.POINTER(SgFlash), i32, C.POINTER(C.c_int)]
             L.sg_run_flash_channel.argtypes = [vp, C.c_int32, i32, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32), i32]
             L.sg_run_discharge.argtypes = [vp, C.c_int32, C.c_double, C.c_double]
+            L.sg_debug_lightning.argtypes = [vp, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int32),
+                                             C.POINTER(C.c_double), C.POINTER(C.c_double)]
             _lib = L
     return _lib
 
@@ -438,6 +440,19 @@ class Run:
                 d.update(nodes=nodes, parent=parent, polarity=polarity)
             out.append(d)
         return out
+
+    LAST_FLASH = ("id", "start", "size", "nodes", "ground", "event", "left", "strokes", "grown", "potential", "sum",
+                  "neutralized", "lowered", "stage", "charge", "flashId")
+
+    def lightning_probe(self):
+        """The discharge's first search on the charge as it stands: (phi, rho, strongest node, |E| / Einit there, the
+        last flash's state record)."""
+        n = self.grid.n
+        phi, rho, best, ratio, last = np.empty(n), np.empty(n), C.c_int32(), C.c_double(), np.empty(16)
+        dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+        self.ctx.check(load().sg_debug_lightning(self.ctx.h, self.id, dp(phi), dp(rho), C.byref(best), C.byref(ratio), dp(last)),
+                       "lightning probe")
+        return phi, rho, best.value, ratio.value, dict(zip(self.LAST_FLASH, last))
 
     def discharge(self, time: float, dt: float):
         """AtmosphereModel.discharge on the run's charge as it stands (src/core/model.ts:1537-1552), at model time `time`."""

@@ -95,15 +95,16 @@ def separated_charge(get, spec):
     return s
 
 
-def tripole_with_cloud(regions):
+def tripole_with_cloud(regions, everywhere=False):
     """A QUIET electrified run's fields carrying `regions` of charge, with cloud water where the charge is (so the
-    channel knows the cloud by its mixing ratios as the model's lightning does, src/core/model.ts:1541)."""
+    channel knows the cloud by its mixing ratios as the model's lightning does, src/core/model.ts:1541), or
+    everywhere (then the channel knows clear air by its charge alone, as the reference's Lightning without cloud())."""
     spec = quiet_electrified()
     f = {k: v.copy() for k, v in spec.fields.items()}
     carriers = storm(regions)
     rho = np.repeat(np.asarray(spec.env.rho), GRID.layer)
     dens = np.abs(sum(c.astype(np.float64) for c in carriers)) * rho
-    f["cloud"] = np.where(dens > 2e-11, 1e-3, 0.0)
+    f["cloud"] = np.full(GRID.n, 1e-3) if everywhere else np.where(dens > 2e-11, 1e-3, 0.0)
     for name, c in zip(("chargeIce", "chargeGraupel", "chargeRain", "chargeAir"), carriers):
         f[name] = c
     return with_fields(spec, f)
