@@ -246,6 +246,44 @@ def cpu_baseline(states, steps: int = 30):
     return out
 
 
+def electrified_leg(ctx, members, runs, steps: int, build: int = 200, cpu_steps: int = 10):
+    """Electrification and lightning on: the first 16 ensemble members as the timed steps left them (developed storms),
+    electrified, their charge built over `build` untimed steps; then `steps` timed steps of the batch (device work and
+    the host-stepped flash stages included) beside the same states without electrification; flashes counted from the
+    runs' charge budgets. CPU: the oracle with lightning on from the same states (charges included), pool strategy."""
+    import dataclasses
+    from meteolab_gb300.scenarios import CARRIED, CHARGES, RunSpec
+    k = min(16, len(runs))
+    base = [RunSpec(m.grid, m.env, m.switches, r.read(), m.seed, m.label) for m, r in zip(members[:k], runs[:k])]
+    elec = [RunSpec(s.grid, s.env, dataclasses.replace(s.switches, lightning=1), s.fields, s.seed, s.label) for s in base]
+    er = [ctx.create(s) for s in elec]
+    ctx.time_steps(er, build)
+    before = [r.charge() for r in er]
+    ms = ctx.time_steps(er, steps)
+    after = [r.charge() for r in er]
+    flashes = sum(a["flashes_ic"] + a["flashes_cg"] - b["flashes_ic"] - b["flashes_cg"] for a, b in zip(after, before))
+    cg = sum(a["flashes_cg"] - b["flashes_cg"] for a, b in zip(after, before))
+    total_flashes = sum(a["flashes_ic"] + a["flashes_cg"] for a in after)
+    states = [RunSpec(s.grid, s.env, s.switches, r.read(list(CARRIED) + list(CHARGES)), s.seed, s.label) for s, r in zip(elec, er)]
+    for r in er:
+        r.retire()
+    pr = [ctx.create(s) for s in base]
+    ctx.time_steps(pr, 3)
+    ms_plain = ctx.time_steps(pr, steps)
+    for r in pr:
+        r.retire()
+    cells = sum(s.grid.n for s in elec)
+    threads = os.cpu_count() or 1
+    cpu = cpu_strategies(states[:threads], cpu_steps, threads)
+    best = max(cpu, key=lambda key: cpu[key][0])
+    return {"members": k, "grid": "40x32x50", "charge_build_steps": build, "timed_steps": steps,
+            "ms_per_step": ms / steps, "cell_steps_s": cells * steps / (ms * 1e-3),
+            "without_lightning_ms_per_step": ms_plain / steps, "flashes_timed": flashes, "cg_flashes_timed": cg,
+            "flashes_since_electrified": total_flashes,
+            "cpu_baseline": {"value": cpu[best][0], "unit": "cell-steps/s", "cores": threads, "kind": "port", "strategy": best,
+                             "sample": f"the same {min(threads, k)} electrified member states, {cpu_steps} steps, oracle with lightning on"}}
+
+
 def reference_arm(args, rank, pg):
     """--impl reference: the reference's algorithm on the host cores (the oracle port; no GPU, none of this package's
     device code) on a bounded sample of the workload: the first `threads` members of the same seeded 64-member ensemble,
@@ -478,6 +516,7 @@ def main():
     es.close()
 
     uneven = uneven_leg(ctx, max(5, args.steps // 2), args.spinup)
+    electrified = electrified_leg(ctx, members, runs, max(10, args.steps // 4)) if rank == 0 else None
     serving = None if args.quick else serving_leg(ctx, rate=4.0, count=32, quantum=10)
     # the serving configuration's range of arrival rates (0.5 to 8 runs/s), each with about 8-12 s of arrivals
     serving_rates = None if args.quick else [serving_leg(ctx, rate=r, count=c, quantum=10) for r, c in ((0.5, 6), (2.0, 16), (8.0, 64))]
@@ -517,6 +556,7 @@ def main():
         "batched_vs_plain_standard": value / world / plain["standard"]["graph_cell_steps_s"],
         "uneven_batch": uneven,
         "electric_solve": {"grid": "40x32x50", "ms_per_solve": electric_ms, "host_io_bytes": 2 * grid.n * 8},
+        "electrified": electrified,
         "serving": serving,
         "serving_rates": serving_rates,
         "kernels_ms_per_launch": {k: round(v[0], 5) for k, v in prof.items()},

@@ -16,6 +16,7 @@
 // Every loop is bounded: a grow launch adds at most MAX_CHANNEL nodes, a flash has at most STROKES + 2 stages, a step
 // at most flashLimit(dt) flashes.
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <climits>
 #include <cmath>
 #include <cstring>
@@ -87,63 +88,90 @@ __global__ void k_lgt_pick(const RunDesc R, const LgtDev L, int stamp) {
   if ((unsigned long long)__double_as_longlong(fieldRatio2(R, L, i)) == m) atomicMin(&L.st->best, i);
 }
 
-// ---------------------------------------------------------------- the channel (one thread's bookkeeping)
-// extend() (:389-404): the nodes beside channel node i (index c) go on the growth front with their shortest link.
-SG_D void extend(const RunDesc& R, const LgtDev& L, LgtState& S, int i, int c, int id) {
+// ---------------------------------------------------------------- the channel
+// extend() (:389-404) by one warp: lane l takes the l-th candidate of the reference's loop (level k from z - 1 up,
+// then dj, then di); the candidates are distinct nodes, so each lane keeps its node's shorter link on its own, and the
+// new links go on the growth front in the reference's order (a ballot over the lanes). All 32 lanes call it.
+SG_D void extendWarp(const RunDesc& R, const LgtDev& L, int i, int c, int id) {
+  const int lane = threadIdx.x & 31;
   const int nx = R.nx, ny = R.ny, nz = R.nz, layer = R.layer, z = i / layer, y = (i - z * layer) / nx, x = i - z * layer - y * nx;
-  for (int k = max(0, z - 1); k <= min(nz - 2, z + 1); k++) {
-    const double hz = lt(L, LT_ZS, k) - lt(L, LT_ZS, z), threshold = dmul(F_CRIT * .5, dadd(lt(L, LT_EINIT, z), lt(L, LT_EINIT, k)));
-    for (int dj = -1; dj <= 1; dj++)
-      for (int di = -1; di <= 1; di++) {
-        if (x + di < 0 || x + di >= nx || y + dj < 0 || y + dj >= ny) continue;
-        const int j = x + di + (y + dj) * nx + k * layer;
-        if (L.mark[j] == id || (k >= z && fabs(L.rho[j]) < RHO_MIN)) continue;
+  const int k0 = max(0, z - 1), k1 = min(nz - 2, z + 1);
+  bool fresh = false;
+  int j = -1;
+  if (lane < 27) {
+    const int k = k0 + lane / 9, dj = (lane % 9) / 3 - 1, di = lane % 3 - 1;
+    if (k <= k1 && x + di >= 0 && x + di < nx && y + dj >= 0 && y + dj < ny) {
+      j = x + di + (y + dj) * nx + k * layer;
+      if (!(L.mark[j] == id || (k >= z && fabs(L.rho[j]) < RHO_MIN))) {
+        const double hz = lt(L, LT_ZS, k) - lt(L, LT_ZS, z), threshold = dmul(F_CRIT * .5, dadd(lt(L, LT_EINIT, z), lt(L, LT_EINIT, k)));
         const double a = dmul((double)di, L.dx), b = dmul((double)dj, L.dy);
         const double s = dmul(__dsqrt_rn(dadd(dadd(dmul(a, a), dmul(b, b)), dmul(hz, hz))), threshold);
-        if (L.seen[j] != id) { L.seen[j] = id; L.frontier[S.size++] = j; }
-        else if (s >= L.scale[j]) continue;
-        L.scale[j] = s; L.link[j] = c;
+        if (L.seen[j] != id) { L.seen[j] = id; fresh = true; L.scale[j] = s; L.link[j] = c; }
+        else if (s < L.scale[j]) { L.scale[j] = s; L.link[j] = c; }
       }
+    }
   }
+  const unsigned mask = __ballot_sync(0xffffffffu, fresh);
+  volatile LgtState& V = *L.st;
+  const int size = V.size;
+  if (fresh) L.frontier[size + __popc(mask & ((1u << lane) - 1))] = j;
+  __syncwarp();
+  if (lane == 0) V.size = size + __popc(mask);
+  __syncwarp();
 }
-// add() of Lightning.flash (:294-304).
-SG_D void addNode(const RunDesc& R, const LgtDev& L, LgtState& S, int j, int from, int id) {
-  L.mark[j] = id; L.nodes[S.nnodes] = j; L.parent[S.nnodes] = from; S.nnodes++;
-  if (j < R.layer) { S.ground = j; S.before = S.potential; S.potential = 0; S.touched = 1; return; }
-  if (S.ground < 0) { S.sum = dadd(S.sum, L.phi[j]); S.potential = S.sum / (double)S.nnodes; }
-  extend(R, L, S, j, S.nnodes - 1, id);
+// add() of Lightning.flash (:294-304) by one warp (lane 0 the bookkeeping, all lanes the extension).
+SG_D void addNodeWarp(const RunDesc& R, const LgtDev& L, int j, int from, int id) {
+  volatile LgtState& V = *L.st;
+  if ((threadIdx.x & 31) == 0) {
+    const int nn = V.nnodes;
+    L.mark[j] = id; L.nodes[nn] = j; L.parent[nn] = from; V.nnodes = nn + 1;
+    if (j < R.layer) { V.ground = j; V.before = V.potential; V.potential = 0; V.touched = 1; }
+    else if (V.ground < 0) { const double sum = dadd(V.sum, L.phi[j]); V.sum = sum; V.potential = sum / (double)(nn + 1); }
+  }
+  __syncwarp();
+  if (j >= R.layer) extendWarp(R, L, j, V.nnodes - 1, id);
 }
 
 __global__ void k_lgt_flash_begin(const RunDesc R, const LgtDev L, int start, int id) {
-  if (threadIdx.x || blockIdx.x) return;
-  LgtState& S = *L.st;
-  S.size = 0; S.nnodes = 0; S.npol = 0; S.ground = -1; S.touched = 0; S.left = 0; S.event = 0; S.strokes = 0; S.nstrokes = 0;
-  S.sum = 0; S.potential = 0; S.before = 0; S.moment = 0; S.lowered = 0; S.neutralized = 0; S.stage = 0; S.needPotential = 0;
-  S.start = start; S.id = id;
-  addNode(R, L, S, start, -1, id);
+  if (blockIdx.x) return;
+  if (threadIdx.x == 0) {
+    LgtState& S = *L.st;
+    S.size = 0; S.nnodes = 0; S.npol = 0; S.ground = -1; S.touched = 0; S.left = 0; S.event = 0; S.strokes = 0; S.nstrokes = 0;
+    S.sum = 0; S.potential = 0; S.before = 0; S.moment = 0; S.lowered = 0; S.neutralized = 0; S.stage = 0; S.needPotential = 0;
+    S.start = start; S.id = id;
+  }
+  __syncwarp();
+  if (threadIdx.x < 32) addNodeWarp(R, L, start, -1, id);
 }
 
 // One stage's growth (:309-331): until no link exceeds the threshold, the channel leaves the cloud (the first time),
 // touches the ground, or has MAX_CHANNEL nodes. First, after a re-solve, the neutral channel's potential (:338).
+// A pick: every thread weights a contiguous part of the front; the parts' exclusive sums (warp scans, in order) and
+// the total; one random number; the part holding the first position where the pick less the weights before it is no
+// longer positive finds it; then warp 0 removes the link from the front, prunes the clear-air leader's other links (the
+// reference's swap-with-last order, its match flags formed by the block) and adds the node.
+constexpr int PRUNE_FLAGS = 16384;
 __global__ void __launch_bounds__(GROW_THREADS) k_lgt_grow(const RunDesc R, const LgtDev L, int id) {
-  __shared__ double part[GROW_THREADS];
+  __shared__ double wsum[GROW_THREADS / 32], wpre[GROW_THREADS / 32];
   __shared__ double pick;
-  __shared__ int pickN, stop;
-  LgtState& S = *L.st;
-  const int t = threadIdx.x, layer = R.layer;
+  __shared__ int pickN, stop, sJ, sFrom, sPrune;
+  __shared__ unsigned char flag[PRUNE_FLAGS];
+  volatile LgtState& V = *L.st;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5, layer = R.layer;
   if (t == 0) {
-    S.grown = S.nnodes; S.event = 0;
-    if (S.needPotential) {
+    V.grown = V.nnodes; V.event = 0;
+    if (V.needPotential) {
       double sum = 0;
-      for (int c = 0; c < S.nnodes; c++) sum = dadd(sum, L.phi[L.nodes[c]]);
-      S.sum = sum; S.potential = sum / (double)S.nnodes; S.needPotential = 0;
+      const int nn = V.nnodes;
+      for (int c = 0; c < nn; c++) sum = dadd(sum, L.phi[L.nodes[c]]);
+      V.sum = sum; V.potential = sum / (double)nn; V.needPotential = 0;
     }
   }
   __syncthreads();
   for (int iter = 0; iter < MAX_CHANNEL; iter++) {
-    if (S.nnodes >= MAX_CHANNEL) break;
-    const int size = S.size, ground = S.ground;
-    const double before = S.before, potential = S.potential;
+    if (V.nnodes >= MAX_CHANNEL) break;
+    const int size = V.size, ground = V.ground;
+    const double before = V.before, potential = V.potential;
     const int C = (size + GROW_THREADS - 1) / GROW_THREADS, f0 = min(size, t * C), f1 = min(size, f0 + C);
     double acc = 0;
     for (int f = f0; f < f1; f++) {
@@ -154,20 +182,24 @@ __global__ void __launch_bounds__(GROW_THREADS) k_lgt_grow(const RunDesc R, cons
       const double wp = w > 0 ? w : 0.0;
       L.weight[f] = wp; acc = dadd(acc, wp);
     }
-    part[t] = acc;
+    // exclusive sums of the parts in thread order: a shuffle scan in each warp, then over the warps' sums
+    double inc = acc;
+    for (int o = 1; o < 32; o <<= 1) { const double u = __shfl_up_sync(0xffffffffu, inc, o); if (lane >= o) inc = dadd(inc, u); }
+    double exc = __shfl_up_sync(0xffffffffu, inc, 1);
+    if (lane == 0) exc = 0;
+    if (lane == 31) wsum[warp] = inc;
     __syncthreads();
     if (t == 0) {
       double s = 0;
-      for (int k = 0; k < GROW_THREADS; k++) { const double v = part[k]; part[k] = s; s = dadd(s, v); }
-      pickN = INT_MAX;
+      for (int w = 0; w < GROW_THREADS / 32; w++) { wpre[w] = s; s = dadd(s, wsum[w]); }
+      pickN = INT_MAX; sPrune = -1;
       stop = s == 0;
-      if (!stop) pick = dmul(mulberry(S.rng), s);
+      if (!stop) { uint32_t r = V.rng; pick = dmul(mulberry(r), s); V.rng = r; }
     }
     __syncthreads();
     if (stop) break;
-    // the picked link: the first front position where the pick, less the weights up to it, is no longer positive
     if (f0 < f1) {
-      double p = pick - part[t];
+      double p = pick - dadd(wpre[warp], exc);
       if (p > 0)
         for (int f = f0; f < f1; f++) {
           p -= L.weight[f];
@@ -176,18 +208,39 @@ __global__ void __launch_bounds__(GROW_THREADS) k_lgt_grow(const RunDesc R, cons
     }
     __syncthreads();
     if (t == 0) {
-      int sz = S.size;
+      int sz = V.size;
       const int n = min(pickN, sz - 1), j = L.frontier[n], from = L.link[j];
-      if (!S.left && S.ground < 0 && clearAt(L, j)) { S.left = 1; S.event = 1; stop = 1; }  // the first step out of the cloud
+      if (!V.left && V.ground < 0 && clearAt(L, j)) { V.left = 1; V.event = 1; stop = 1; }  // the first step out of the cloud
       else {
         L.frontier[n] = L.frontier[--sz];
+        V.size = sz;
+        sJ = j; sFrom = from;
         // through clear air a leader does not branch: the other links from the same clear-air node leave the front
-        if (clearAt(L, L.nodes[from]))
-          for (int f = sz - 1; f >= 0; f--) if (L.link[L.frontier[f]] == from) L.frontier[f] = L.frontier[--sz];
-        S.size = sz;
-        addNode(R, L, S, j, from, id);
-        if (S.touched) { S.touched = 0; S.event = 1; stop = 1; }
+        sPrune = clearAt(L, L.nodes[from]) ? from : -1;
       }
+    }
+    __syncthreads();
+    if (stop) break;
+    if (sPrune >= 0) {
+      const int sz = V.size;
+      if (sz <= PRUNE_FLAGS) {
+        for (int f = t; f < sz; f += GROW_THREADS) flag[f] = L.link[L.frontier[f]] == sPrune;
+        __syncthreads();
+        if (t == 0) {
+          int m = sz;
+          for (int f = sz - 1; f >= 0; f--) if (flag[f]) L.frontier[f] = L.frontier[--m];
+          V.size = m;
+        }
+      } else if (t == 0) {
+        int m = sz;
+        for (int f = sz - 1; f >= 0; f--) if (L.link[L.frontier[f]] == sPrune) L.frontier[f] = L.frontier[--m];
+        V.size = m;
+      }
+      __syncthreads();
+    }
+    if (warp == 0) {
+      addNodeWarp(R, L, sJ, sFrom, id);
+      if (lane == 0 && V.touched) { V.touched = 0; V.event = 1; stop = 1; }
     }
     __syncthreads();
     if (stop) break;
@@ -443,40 +496,6 @@ static cudaError_t read_state(cudaStream_t st, const LgtHost& H, LgtState& S) {
   return cudaStreamSynchronize(st);
 }
 
-// One flash from `start` (Lightning.flash, :287-340): the stages, each grown and deposited on the device.
-static cudaError_t flash(cudaStream_t st, const RunDesc& R, LgtHost& H, int start, double time, int stamp, FlashRecord* out) {
-  const LgtDev& L = H.dev;
-  const int id = ++H.flashId, nb = blocks(R.n, 256);
-  k_lgt_flash_begin<<<1, 32, 0, st>>>(R, L, start, id);
-  LgtState S{};
-  cudaError_t e;
-  for (int stage = 0; stage < STROKES + 8; stage++) {
-    k_lgt_grow<<<1, GROW_THREADS, 0, st>>>(R, L, id);
-    k_lgt_deposit<<<1, DEP_THREADS, 0, st>>>(R, L);
-    if ((e = read_state(st, H, S)) != cudaSuccess) return e;
-    if (S.ground >= 0 && (S.strokes >= STROKES || (!S.event && S.nnodes == S.grown))) break;
-    if (S.ground < 0 && !S.event) break;
-    if (S.nnodes >= MAX_CHANNEL) break;
-    // the field of the charge as it now stands; before the contact the channel stays neutral on it
-    k_lgt_rho<<<nb, 256, 0, st>>>(R, L);
-    elec_solve_launch(L.es, L.rho, L.phi, st);
-  }
-  k_lgt_flash_end<<<1, 32, 0, st>>>(R, L, stamp);
-  if ((e = read_state(st, H, S)) != cudaSuccess) return e;
-  out->time = time; out->cg = S.ground >= 0; out->start = start; out->ground = S.ground; out->charge = S.charge;
-  out->potential = S.ground >= 0 ? S.before : S.potential; out->moment = S.ground >= 0 ? S.moment : 0;
-  out->strokes.assign(S.strokeQ, S.strokeQ + (S.ground >= 0 ? S.nstrokes : 0));
-  out->nodes.resize(S.nnodes); out->parent.resize(S.nnodes); out->polarity.resize(S.nnodes);
-  if (S.charge != 0 && S.nnodes > 0) {
-    if ((e = cudaMemcpyAsync(out->nodes.data(), L.nodes, S.nnodes * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(out->parent.data(), L.parent, S.nnodes * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(out->polarity.data(), L.polarity, S.nnodes * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
-        (e = cudaStreamSynchronize(st)) != cudaSuccess)
-      return e;
-  }
-  return cudaSuccess;
-}
-
 int lightning_state(cudaStream_t st, LgtHost& H, double* out) {
   LgtState S{};
   if (read_state(st, H, S) != cudaSuccess) return SG_ERR_DEVICE;
@@ -497,7 +516,7 @@ int lightning_probe(cudaStream_t st, const RunDesc& R, LgtHost& H, double* phi, 
   k_lgt_pick<<<ni, 256, 0, st>>>(R, L, -1);
   LgtState S{};
   cudaError_t e;
-  if ((e = read_state(st, H, S)) != cudaSuccess) return SG_ERR_DEVICE;
+  if (read_state(st, H, S) != cudaSuccess) return SG_ERR_DEVICE;
   if (phi && (e = cudaMemcpyAsync(phi, L.phi, (size_t)R.n * 8, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return SG_ERR_DEVICE;
   if (rho && (e = cudaMemcpyAsync(rho, L.rho, (size_t)R.n * 8, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return SG_ERR_DEVICE;
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess || (e = cudaGetLastError()) != cudaSuccess) return SG_ERR_DEVICE;
@@ -508,42 +527,152 @@ int lightning_probe(cudaStream_t st, const RunDesc& R, LgtHost& H, double* phi, 
   return SG_OK;
 }
 
-int lightning_discharge(cudaStream_t st, const sg_grid* g, const RunDesc& R, LgtHost& H, double time, double dt, int limit, std::string* err) {
-  const LgtDev& L = H.dev;
-  const int nb = blocks(R.n, 256), ni = blocks(R.n - 2 * R.layer, 256);
-  cudaError_t e = conduct_tables(st, g, H, dt);
-  if (e != cudaSuccess) { *err = cudaGetErrorString(e); return SG_ERR_DEVICE; }
-  H.last.clear();
-  const int stamp = ++H.flashId;
-  // the random numbers start afresh from the seed and the model time (:263)
-  const int32_t tenths = (int32_t)(int64_t)std::floor(time * 10 + .5);
-  const uint32_t rng = H.seed ^ (uint32_t)((uint32_t)tenths * 0x9E3779B1u);
-  k_lgt_seed<<<1, 32, 0, st>>>(L, rng);
-  k_lgt_cloudy<<<nb, 256, 0, st>>>(R, L);
-  for (int k = 0; k <= limit; k++) {
-    k_lgt_rho<<<nb, 256, 0, st>>>(R, L);
-    elec_solve_launch(L.es, L.rho, L.phi, st);
-    if (k == limit) break;
-    LgtState S{};
-    k_lgt_search_reset<<<1, 32, 0, st>>>(L);
-    k_lgt_strongest<<<ni, 256, 0, st>>>(R, L, stamp);
-    k_lgt_pick<<<ni, 256, 0, st>>>(R, L, stamp);
-    if ((e = read_state(st, H, S)) != cudaSuccess) { *err = cudaGetErrorString(e); return SG_ERR_DEVICE; }
-    double r2;
-    std::memcpy(&r2, &S.maxBits, sizeof(double));
-    if (S.maxBits == 0 || !(std::sqrt(r2) > 1)) break;
-    FlashRecord f;
-    if ((e = flash(st, R, H, S.best, time, stamp, &f)) != cudaSuccess) { *err = cudaGetErrorString(e); return SG_ERR_DEVICE; }
-    if (f.charge == 0) continue;
-    H.last.push_back(std::move(f));
-  }
-  // the ions drift in the field of the last solve, the ground gives corona; then the vertical field
-  k_lgt_sigma<<<nb, 256, 0, st>>>(R, L);
-  k_lgt_conduct<<<ni, 256, 0, st>>>(R, L, H.corona ? 1 : 0, dt);
-  k_lgt_conduct_end<<<1, 32, 0, st>>>(R, L, ni);
-  k_lgt_fieldz<<<ni, 256, 0, st>>>(R, L);
-  if ((e = cudaGetLastError()) != cudaSuccess) { *err = cudaGetErrorString(e); return SG_ERR_DEVICE; }
+LgtHost::~LgtHost() {
+  if (st) { cudaStreamSynchronize(st); cudaStreamDestroy(st); }
+  if (hs) cudaFreeHost(hs);
+  if (hchan) cudaFreeHost(hchan);
+}
+
+int lightning_host_buffers(LgtHost& H) {
+  if (!H.st && cudaStreamCreateWithFlags(&H.st, cudaStreamNonBlocking) != cudaSuccess) return SG_ERR_DEVICE;
+  if (!H.hs && cudaMallocHost(&H.hs, sizeof(LgtState)) != cudaSuccess) return SG_ERR_DEVICE;
+  if (!H.hchan && cudaMallocHost(&H.hchan, 3 * (size_t)MAX_CHANNEL * sizeof(int)) != cudaSuccess) return SG_ERR_DEVICE;
   return SG_OK;
+}
+
+namespace {
+
+// The search of pass k of Discharge (:264-268): the charge density and its field, then the strongest field; at the pass
+// after the last flash allowed, the conduction and the vertical field instead (:1547-1551).
+void launch_finish(const LgtJob& J) {
+  const LgtDev& L = J.H->dev;
+  const int nb = blocks(J.R.n, 256), ni = blocks(J.R.n - 2 * J.R.layer, 256);
+  k_lgt_sigma<<<nb, 256, 0, J.H->st>>>(J.R, L);
+  k_lgt_conduct<<<ni, 256, 0, J.H->st>>>(J.R, L, J.H->corona ? 1 : 0, J.dt);
+  k_lgt_conduct_end<<<1, 32, 0, J.H->st>>>(J.R, L, ni);
+  k_lgt_fieldz<<<ni, 256, 0, J.H->st>>>(J.R, L);
+}
+void launch_search(LgtJob& J) {
+  const LgtDev& L = J.H->dev;
+  const int nb = blocks(J.R.n, 256), ni = blocks(J.R.n - 2 * J.R.layer, 256);
+  cudaStream_t st = J.H->st;
+  k_lgt_rho<<<nb, 256, 0, st>>>(J.R, L);
+  elec_solve_launch(L.es, L.rho, L.phi, st);
+  if (J.k == J.limit) { launch_finish(J); J.phase = LgtJob::FINISHING; return; }
+  k_lgt_search_reset<<<1, 32, 0, st>>>(L);
+  k_lgt_strongest<<<ni, 256, 0, st>>>(J.R, L, J.stamp);
+  k_lgt_pick<<<ni, 256, 0, st>>>(J.R, L, J.stamp);
+  J.phase = LgtJob::SEARCH;
+}
+void launch_stage(LgtJob& J) {
+  k_lgt_grow<<<1, GROW_THREADS, 0, J.H->st>>>(J.R, J.H->dev, J.id);
+  k_lgt_deposit<<<1, DEP_THREADS, 0, J.H->st>>>(J.R, J.H->dev);
+  J.stage++;
+}
+
+// Advances a job by what its last round's state record says (Lightning.discharge and .flash, :259-340).
+cudaError_t advance(LgtJob& J) {
+  LgtHost& H = *J.H;
+  const LgtState& S = *H.hs;
+  cudaError_t e = cudaSuccess;
+  if (J.pending) {  // the flash that ended last round: its record (its channel was copied behind flash_end)
+    J.pending = false;
+    if (S.charge != 0) {
+      FlashRecord f;
+      f.time = J.time; f.cg = S.ground >= 0; f.start = J.start; f.ground = S.ground; f.charge = S.charge;
+      f.potential = S.ground >= 0 ? S.before : S.potential; f.moment = S.ground >= 0 ? S.moment : 0;
+      f.strokes.assign(S.strokeQ, S.strokeQ + (S.ground >= 0 ? S.nstrokes : 0));
+      const int m = J.copied;
+      f.nodes.assign(H.hchan, H.hchan + m); f.parent.assign(H.hchan + MAX_CHANNEL, H.hchan + MAX_CHANNEL + m);
+      f.polarity.assign(H.hchan + 2 * MAX_CHANNEL, H.hchan + 2 * MAX_CHANNEL + m);
+      H.last.push_back(std::move(f));
+    }
+  }
+  switch (J.phase) {
+    case LgtJob::SEARCH: {
+      double r2;
+      std::memcpy(&r2, &S.maxBits, sizeof(double));
+      if (S.maxBits == 0 || !(std::sqrt(r2) > 1)) { launch_finish(J); J.phase = LgtJob::DONE; break; }
+      J.start = S.best; J.id = ++H.flashId; J.stage = 0;
+      k_lgt_flash_begin<<<1, 32, 0, H.st>>>(J.R, H.dev, J.start, J.id);
+      launch_stage(J);
+      J.phase = LgtJob::FLASH;
+      break;
+    }
+    case LgtJob::FLASH: {
+      const bool end = (S.ground >= 0 && (S.strokes >= STROKES || (!S.event && S.nnodes == S.grown))) || (S.ground < 0 && !S.event) ||
+                       S.nnodes >= MAX_CHANNEL || J.stage >= STROKES + 8;
+      if (!end) {
+        // the field of the charge as it now stands; before the contact the channel stays neutral on it
+        k_lgt_rho<<<blocks(J.R.n, 256), 256, 0, H.st>>>(J.R, H.dev);
+        elec_solve_launch(H.dev.es, H.dev.rho, H.dev.phi, H.st);
+        launch_stage(J);
+        break;
+      }
+      k_lgt_flash_end<<<1, 32, 0, H.st>>>(J.R, H.dev, J.stamp);
+      J.copied = S.nnodes;
+      if ((e = cudaMemcpyAsync(H.hchan, H.dev.nodes, (size_t)S.nnodes * 4, cudaMemcpyDeviceToHost, H.st)) != cudaSuccess ||
+          (e = cudaMemcpyAsync(H.hchan + MAX_CHANNEL, H.dev.parent, (size_t)S.nnodes * 4, cudaMemcpyDeviceToHost, H.st)) != cudaSuccess ||
+          (e = cudaMemcpyAsync(H.hchan + 2 * MAX_CHANNEL, H.dev.polarity, (size_t)S.nnodes * 4, cudaMemcpyDeviceToHost, H.st)) != cudaSuccess)
+        return e;
+      J.pending = true;
+      J.k++;
+      launch_search(J);
+      break;
+    }
+    case LgtJob::FINISHING: J.phase = LgtJob::DONE; break;
+    case LgtJob::DONE: break;
+  }
+  return e;
+}
+
+}  // namespace
+
+// The discharges of several runs in lockstep, each on its own stream: a round launches every run's next piece of
+// work (a search, a flash stage, the end of a flash and the next search, the conduction), then reads every run's state
+// record once; the runs' single-block channel growths run side by side on the SMs.
+int lightning_discharge_many(LgtJob* jobs, int n, std::string* err) {
+  cudaError_t e = cudaSuccess;
+  for (int j = 0; j < n; j++) {
+    LgtJob& J = jobs[j];
+    LgtHost& H = *J.H;
+    if ((e = conduct_tables(H.st, J.g, H, J.dt)) != cudaSuccess) { *err = cudaGetErrorString(e); return SG_ERR_DEVICE; }
+    H.last.clear();
+    J.stamp = ++H.flashId; J.k = 0; J.pending = false;
+    // the random numbers start afresh from the seed and the model time (:263)
+    const int32_t tenths = (int32_t)(int64_t)std::floor(J.time * 10 + .5);
+    k_lgt_seed<<<1, 32, 0, H.st>>>(H.dev, H.seed ^ (uint32_t)((uint32_t)tenths * 0x9E3779B1u));
+    k_lgt_cloudy<<<blocks(J.R.n, 256), 256, 0, H.st>>>(J.R, H.dev);
+    launch_search(J);
+  }
+  int bound = 8;  // rounds: every flash at most STROKES + 9 stages and its end, every pass a search
+  for (int j = 0; j < n; j++) bound = std::max(bound, (jobs[j].limit + 2) * (STROKES + 12));
+  for (int round = 0; round < bound; round++) {
+    bool any = false;
+    for (int j = 0; j < n; j++) {
+      if (jobs[j].phase == LgtJob::DONE) continue;
+      any = true;
+      if ((e = cudaMemcpyAsync(jobs[j].H->hs, jobs[j].H->dev.st, sizeof(LgtState), cudaMemcpyDeviceToHost, jobs[j].H->st)) != cudaSuccess) break;
+    }
+    if (!any || e != cudaSuccess) break;
+    for (int j = 0; j < n && e == cudaSuccess; j++)
+      if (jobs[j].phase != LgtJob::DONE) e = cudaStreamSynchronize(jobs[j].H->st);
+    for (int j = 0; j < n && e == cudaSuccess; j++)
+      if (jobs[j].phase != LgtJob::DONE) e = advance(jobs[j]);
+    if (e != cudaSuccess) break;
+  }
+  for (int j = 0; j < n && e == cudaSuccess; j++) e = cudaStreamSynchronize(jobs[j].H->st);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) { *err = cudaGetErrorString(e); return SG_ERR_DEVICE; }
+  for (int j = 0; j < n; j++)
+    if (jobs[j].phase != LgtJob::DONE) { *err = "a discharge did not end within its bound of rounds"; return SG_ERR_DEVICE; }
+  return SG_OK;
+}
+
+int lightning_discharge(cudaStream_t, const sg_grid* g, const RunDesc& R, LgtHost& H, double time, double dt, int limit, std::string* err) {
+  LgtJob J;
+  J.g = g; J.R = R; J.H = &H; J.time = time; J.dt = dt; J.limit = limit;
+  return lightning_discharge_many(&J, 1, err);
 }
 
 }  // namespace sg

@@ -60,11 +60,33 @@ struct LgtHost {
   double dxy = 0, conductDt = 0;
   std::vector<double> tables;
   std::vector<FlashRecord> last;   // the flashes of the last discharge
+  cudaStream_t st = nullptr;       // the run's lightning stream
+  LgtState* hs = nullptr;          // pinned: the state record read each round
+  int* hchan = nullptr;            // pinned: a finished flash's channel (nodes, parents, polarities)
+  LgtHost() = default;
+  LgtHost(const LgtHost&) = delete;
+  LgtHost& operator=(const LgtHost&) = delete;
+  ~LgtHost();
+};
+
+// One run's discharge as the batch driver steps it.
+struct LgtJob {
+  const sg_grid* g = nullptr;
+  RunDesc R{};
+  LgtHost* H = nullptr;
+  double time = 0, dt = 0;
+  int limit = 0, k = 0, stamp = 0, stage = 0, start = -1, id = 0, copied = 0;
+  bool pending = false;            // a flash ended last round; its record is read this round
+  enum Phase { SEARCH, FLASH, FINISHING, DONE } phase = SEARCH;
 };
 
 size_t lightning_bytes(int nx, int ny, int nz);
 void lightning_bind(char* base, int nx, int ny, int nz, LgtDev& L);
 int lightning_init(cudaStream_t st, const sg_grid* g, const double* rho, LgtHost& H);
+// The run's lightning stream and pinned host buffers (once).
+int lightning_host_buffers(LgtHost& H);
+// The discharges of n runs together (lockstep rounds, a stream a run); each job's time is its flashes' model time.
+int lightning_discharge_many(LgtJob* jobs, int n, std::string* err);
 // The discharge after a step at model time `time` (the step's end) with step length dt: at most `limit` flashes, then
 // the conduction and corona over dt, then the vertical field. SG_OK, or SG_ERR_DEVICE with *err set.
 int lightning_discharge(cudaStream_t st, const sg_grid* g, const RunDesc& R, LgtHost& H, double time, double dt, int limit, std::string* err);

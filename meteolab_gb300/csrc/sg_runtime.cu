@@ -718,17 +718,29 @@ int slots_of(sg_context* ctx, const sg_run* runs, int n, std::vector<int>& slots
   return SG_OK;
 }
 
-// The lightning of an electrified run after its step: the flash time is the step's end (time + dt, src/core/model.ts:1542);
-// `advance`: the step moved the run's time by dt. Runs that failed or are not electrified are left alone.
-int discharge_run(sg_context* ctx, Run& r, bool advance) {
-  if (!r.lgt) return SG_OK;
-  if (advance) r.time += r.dt;
-  unsigned long long failed = 0;
-  CK(cudaMemcpyAsync(&failed, r.desc.cnt + C_FAILED, sizeof(failed), cudaMemcpyDeviceToHost, ctx->stream));
+// The lightning of a batch's electrified runs after their step (afterStep, src/core/model.ts:1130-1133), all of them
+// together: the flash time is the step's end (time + dt, :1542), so each run's time moves by its dt first. Runs that
+// failed are left alone.
+int discharge_batch(sg_context* ctx, const std::vector<int>& slots) {
+  std::vector<Run*> elec;
+  for (int s : slots) if (ctx->runs[s].lgt) elec.push_back(&ctx->runs[s]);
+  if (elec.empty()) return SG_OK;
+  std::vector<unsigned long long> failed(elec.size(), 0);
+  for (size_t k = 0; k < elec.size(); k++)
+    CK(cudaMemcpyAsync(&failed[k], elec[k]->desc.cnt + C_FAILED, sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
-  if (failed) return SG_OK;
+  std::vector<LgtJob> jobs;
+  for (size_t k = 0; k < elec.size(); k++) {
+    Run& r = *elec[k];
+    r.time += r.dt;
+    if (failed[k]) continue;
+    LgtJob J;
+    J.g = &r.grid; J.R = r.desc; J.H = r.lgt.get(); J.time = r.time; J.dt = r.dt; J.limit = flash_limit(r.dt);
+    jobs.push_back(J);
+  }
+  if (jobs.empty()) return SG_OK;
   std::string err;
-  const int st = lightning_discharge(ctx->stream, &r.grid, r.desc, *r.lgt, r.time, r.dt, flash_limit(r.dt), &err);
+  const int st = lightning_discharge_many(jobs.data(), (int)jobs.size(), &err);
   if (st != SG_OK) return fail(ctx, st, "lightning: " + err);
   return SG_OK;
 }
@@ -745,7 +757,7 @@ int batch_step(sg_context* ctx, const sg_run* runs, int n, int nsteps, bool wait
     // electrified runs: after each step their lightning (host-stepped flash stages, src/core/model.ts:1130-1133)
     for (int s = 0; s < nsteps; s++) {
       CK(cudaGraphLaunch(P->exec, ctx->stream));
-      for (int slot : P->slots) if ((st = discharge_run(ctx, ctx->runs[slot], true)) != SG_OK) return st;
+      if ((st = discharge_batch(ctx, P->slots)) != SG_OK) return st;
     }
   } else {
     for (int s = 0; s < nsteps; s++) CK(cudaGraphLaunch(P->exec, ctx->stream));
@@ -910,6 +922,7 @@ int sg_run_create(sg_context* ctx, const sg_grid* g, const sg_base_state* b, con
   if (elec) {
     const int e = lightning_init(ctx->stream, &r.grid, b->rho, *r.lgt);
     if (e) return fail(ctx, SG_ERR_DEVICE, std::string("lightning tables: ") + cudaGetErrorString((cudaError_t)e));
+    if (lightning_host_buffers(*r.lgt) != SG_OK) return fail(ctx, SG_ERR_DEVICE, "lightning stream and pinned buffers");
   }
   {
     const size_t n = (size_t)g->nx * g->ny * g->nz;
@@ -1454,7 +1467,7 @@ int sg_time_steps(sg_context* ctx, const sg_run* runs, int n, int nsteps, int us
   for (int s = 0; s < nsteps; s++) {
     if (use_graph) CK(cudaGraphLaunch(P->exec, ctx->stream));
     else enqueue_step(ctx, *P, [](int) {});
-    if (P->elec) for (int slot : P->slots) if ((st = discharge_run(ctx, ctx->runs[slot], true)) != SG_OK) return st;
+    if (P->elec && (st = discharge_batch(ctx, P->slots)) != SG_OK) return st;
   }
   CK(cudaEventRecord(b, ctx->stream));
   CK(cudaEventSynchronize(b));
