@@ -15,6 +15,14 @@
  *   retire(ctx, run), destroyContext(ctx)
  *   saveState(ctx, run, configJson: string, time, persisted) -> ArrayBuffer      (saveState, src/core/state.ts:43)
  *   loadState(ctx, run, image: ArrayBuffer) -> {version, time, persisted}        (readState + applyState, :55-83)
+ *   electrified runs (switches.lightning, with ice; switches.corona, switches.lightningSeed = config.seed + 1):
+ *   readCharges(ctx, run, charges: Float32Array[4]) / writeCharges(ctx, run, charges)   chargeIce, chargeGraupel,
+ *                                                             chargeRain, chargeAir (src/core/model.ts:210)
+ *   charge(ctx, run) -> {ground, separated, ic, cgNegative, cgPositive, precipitation, conduction, flashCount: {ic, cg}}
+ *   flashes(ctx, run) -> [{time, kind: 'IC'|'CG', start, ground, potential, charge, moment, strokes: number[],
+ *                          nodes, parent, polarity: Int32Array}]               (the last step's Flash records)
+ *   discharge(ctx, run, time, dt)                             (AtmosphereModel.discharge, :1537-1552, on the charge
+ *                                                             as it stands)
  */
 #include <node_api.h>
 #include <stdio.h>
@@ -94,6 +102,8 @@ static napi_value create_run(napi_env env, napi_callback_info info) {
   s.pressure_in_stages = (int32_t)get_num(env, argv[3], "pressureInStages"); s.ice = (int32_t)get_num(env, argv[3], "ice");
   s.refine_projection = (int32_t)get_num(env, argv[3], "refineProjection");
   s.rotation = (int32_t)get_num(env, argv[3], "rotation");
+  s.lightning = (int32_t)get_num(env, argv[3], "lightning"); s.corona = (int32_t)get_num(env, argv[3], "corona");
+  s.lightning_seed = (int32_t)get_num(env, argv[3], "lightningSeed");
   float* init[SG_NFIELDS];
   if (!fields_of(env, argv[4], init)) { napi_throw_type_error(env, NULL, "fields: 13 Float32Array"); return NULL; }
   sg_run run;
@@ -230,6 +240,102 @@ static napi_value fields_io(napi_env env, napi_callback_info info, int write) {
 static napi_value read_fields(napi_env env, napi_callback_info info) { return fields_io(env, info, 0); }
 static napi_value write_fields(napi_env env, napi_callback_info info) { return fields_io(env, info, 1); }
 
+static napi_value charges_io(napi_env env, napi_callback_info info, int write) {
+  size_t argc = 3; napi_value argv[3]; int32_t run;
+  CHECK(env, napi_get_cb_info(env, info, &argc, argv, NULL, NULL));
+  sg_context* ctx = ctx_of(env, argv[0]);
+  napi_get_value_int32(env, argv[1], &run);
+  float* f[SG_NFIELDS_ELECTRIFIED] = {0};
+  for (uint32_t k = 0; k < 4; k++) {
+    napi_value el; napi_typedarray_type type; size_t len; void* data; napi_value buf; size_t off;
+    if (napi_get_element(env, argv[2], k, &el) != napi_ok || napi_get_typedarray_info(env, el, &type, &len, &data, &buf, &off) != napi_ok ||
+        type != napi_float32_array) { napi_throw_type_error(env, NULL, "charges: 4 Float32Array"); return NULL; }
+    f[SG_CHARGE_ICE + k] = (float*)data;
+  }
+  int st = write ? sg_run_write_fields(ctx, run, SG_CHARGE_FIELDS, (const float* const*)f) : sg_run_read_fields(ctx, run, SG_CHARGE_FIELDS, f);
+  if (st) return throw_status(env, ctx, st);
+  return NULL;
+}
+static napi_value read_charges(napi_env env, napi_callback_info info) { return charges_io(env, info, 0); }
+static napi_value write_charges(napi_env env, napi_callback_info info) { return charges_io(env, info, 1); }
+
+static void set_num(napi_env env, napi_value o, const char* key, double x) { napi_value v; napi_create_double(env, x, &v); napi_set_named_property(env, o, key, v); }
+
+static napi_value charge(napi_env env, napi_callback_info info) {
+  size_t argc = 2; napi_value argv[2]; int32_t run;
+  CHECK(env, napi_get_cb_info(env, info, &argc, argv, NULL, NULL));
+  sg_context* ctx = ctx_of(env, argv[0]);
+  napi_get_value_int32(env, argv[1], &run);
+  sg_charge_state c;
+  int st = sg_run_charge(ctx, run, &c);
+  if (st) return throw_status(env, ctx, st);
+  napi_value o, fc;
+  CHECK(env, napi_create_object(env, &o));
+  set_num(env, o, "ground", c.ground); set_num(env, o, "separated", c.separated); set_num(env, o, "ic", c.ic);
+  set_num(env, o, "cgNegative", c.cg_negative); set_num(env, o, "cgPositive", c.cg_positive); set_num(env, o, "precipitation", c.precipitation);
+  set_num(env, o, "conduction", c.conduction);
+  CHECK(env, napi_create_object(env, &fc));
+  set_num(env, fc, "ic", (double)c.flashes_ic); set_num(env, fc, "cg", (double)c.flashes_cg);
+  napi_set_named_property(env, o, "flashCount", fc);
+  return o;
+}
+
+static napi_value int32_array(napi_env env, const int32_t* src, int n) {
+  napi_value ab, arr; void* data;
+  if (napi_create_arraybuffer(env, (size_t)n * 4, &data, &ab) != napi_ok) return NULL;
+  memcpy(data, src, (size_t)n * 4);
+  if (napi_create_typedarray(env, napi_int32_array, (size_t)n, ab, 0, &arr) != napi_ok) return NULL;
+  return arr;
+}
+
+static napi_value flashes(napi_env env, napi_callback_info info) {
+  size_t argc = 2; napi_value argv[2]; int32_t run;
+  CHECK(env, napi_get_cb_info(env, info, &argc, argv, NULL, NULL));
+  sg_context* ctx = ctx_of(env, argv[0]);
+  napi_get_value_int32(env, argv[1], &run);
+  int count = 0;
+  int st = sg_run_flashes(ctx, run, NULL, 0, &count);
+  if (st) return throw_status(env, ctx, st);
+  sg_flash* recs = (sg_flash*)calloc(count > 0 ? count : 1, sizeof(sg_flash));
+  int32_t* chan = (int32_t*)malloc(3 * 3000 * sizeof(int32_t));
+  st = sg_run_flashes(ctx, run, recs, count, &count);
+  napi_value list;
+  napi_create_array_with_length(env, (size_t)count, &list);
+  for (int k = 0; st == 0 && k < count; k++) {
+    const sg_flash* f = &recs[k];
+    st = sg_run_flash_channel(ctx, run, k, chan, chan + 3000, chan + 6000, 3000);
+    if (st) break;
+    napi_value o, kind, strokes, v;
+    napi_create_object(env, &o);
+    set_num(env, o, "time", f->time);
+    napi_create_string_utf8(env, f->cg ? "CG" : "IC", NAPI_AUTO_LENGTH, &kind); napi_set_named_property(env, o, "kind", kind);
+    set_num(env, o, "start", f->start); set_num(env, o, "ground", f->ground); set_num(env, o, "potential", f->potential);
+    set_num(env, o, "charge", f->charge); set_num(env, o, "moment", f->moment);
+    napi_create_array_with_length(env, (size_t)f->strokes, &strokes);
+    for (int j = 0; j < f->strokes && j < 4; j++) { napi_create_double(env, f->stroke_charge[j], &v); napi_set_element(env, strokes, (uint32_t)j, v); }
+    napi_set_named_property(env, o, "strokes", strokes);
+    napi_set_named_property(env, o, "nodes", int32_array(env, chan, f->nodes));
+    napi_set_named_property(env, o, "parent", int32_array(env, chan + 3000, f->nodes));
+    napi_set_named_property(env, o, "polarity", int32_array(env, chan + 6000, f->nodes));
+    napi_set_element(env, list, (uint32_t)k, o);
+  }
+  free(recs); free(chan);
+  if (st) return throw_status(env, ctx, st);
+  return list;
+}
+
+static napi_value discharge(napi_env env, napi_callback_info info) {
+  size_t argc = 4; napi_value argv[4]; int32_t run; double time = 0, dt = 0;
+  CHECK(env, napi_get_cb_info(env, info, &argc, argv, NULL, NULL));
+  sg_context* ctx = ctx_of(env, argv[0]);
+  napi_get_value_int32(env, argv[1], &run);
+  napi_get_value_double(env, argv[2], &time);
+  napi_get_value_double(env, argv[3], &dt);
+  int st = sg_run_discharge(ctx, run, time, dt);
+  if (st) return throw_status(env, ctx, st);
+  return NULL;
+}
+
 static napi_value status(napi_env env, napi_callback_info info) {
   size_t argc = 2; napi_value argv[2]; int32_t run;
   CHECK(env, napi_get_cb_info(env, info, &argc, argv, NULL, NULL));
@@ -311,6 +417,9 @@ static napi_value init(napi_env env, napi_value exports) {
     {"stepIo", 0, step_io, 0, 0, 0, napi_default, 0},
     {"electricCreate", 0, electric_create, 0, 0, 0, napi_default, 0}, {"electricSolve", 0, electric_solve, 0, 0, 0, napi_default, 0},
     {"electricDestroy", 0, electric_destroy, 0, 0, 0, napi_default, 0},
+    {"readCharges", 0, read_charges, 0, 0, 0, napi_default, 0}, {"writeCharges", 0, write_charges, 0, 0, 0, napi_default, 0},
+    {"charge", 0, charge, 0, 0, 0, napi_default, 0}, {"flashes", 0, flashes, 0, 0, 0, napi_default, 0},
+    {"discharge", 0, discharge, 0, 0, 0, napi_default, 0},
   };
   napi_define_properties(env, exports, sizeof d / sizeof d[0], d);
   return exports;

@@ -1192,7 +1192,11 @@ int sg_run_save_state(sg_context* ctx, sg_run run, const char* config_json, doub
   int st = sg_run_status(ctx, run, &c);
   if (st != SG_OK && st != SG_ERR_NONFINITE) return st;
   const double water[5] = {c.water_condensed, c.water_evaporated, c.water_rain_evaporated, c.water_surface, r->waterStart};
-  const std::string json = state::header_json(config_json, time, persisted, r->nx, r->ny, r->nz, water);
+  sg_charge_state cs;
+  if ((st = sg_run_charge(ctx, run, &cs)) != SG_OK) return st;
+  const double charge9[9] = {cs.ground, (double)cs.flashes_ic, (double)cs.flashes_cg, cs.separated, cs.ic, cs.cg_negative, cs.cg_positive,
+                             cs.precipitation, cs.conduction};
+  const std::string json = state::header_json(config_json, time, persisted, r->nx, r->ny, r->nz, water, r->lgt ? charge9 : nullptr);
   const size_t need = state::image_bytes(json.size(), state::VERSION, r->nx, r->ny, r->nz);
   *size = need;
   if (!out) return SG_OK;
@@ -1200,6 +1204,12 @@ int sg_run_save_state(sg_context* ctx, sg_run run, const char* config_json, doub
   const size_t n = (size_t)r->nx * r->ny * r->nz, layer = (size_t)r->nx * r->ny, off = state::data_offset(json.size());
   std::vector<float> fields((size_t)SG_NFIELDS * n), cols(3 * layer);
   if ((st = sg_batch_read_packed(ctx, &run, 1, SG_ALL_FIELDS, fields.data())) != SG_OK) return st;
+  std::vector<float> charges(r->lgt ? 4 * n : 0, 0.f);  // an electrified run's charge carriers
+  if (r->lgt) {
+    float* ptr[SG_NFIELDS_ELECTRIFIED] = {};
+    for (int k = 0; k < 4; k++) ptr[SG_CHARGE_ICE + k] = charges.data() + (size_t)k * n;
+    if ((st = sg_run_read_fields(ctx, run, SG_CHARGE_FIELDS, ptr)) != SG_OK) return st;
+  }
   if ((st = sg_run_read_columns(ctx, run, cols.data(), cols.data() + layer, cols.data() + 2 * layer)) != SG_OK) return st;
   std::memset(out, 0, off);
   std::memcpy(out, "MLAB", 4);
@@ -1210,7 +1220,9 @@ int sg_run_save_state(sg_context* ctx, sg_run run, const char* config_json, doub
   for (int k = 0; k < state::NSTATE; k++) {
     uint8_t* dst = out + off + (size_t)k * n * 4;
     const int f = state::carried_of(k);
-    if (f >= 0) std::memcpy(dst, fields.data() + (size_t)f * n, n * 4); else std::memset(dst, 0, n * 4);
+    if (f >= SG_CHARGE_ICE && r->lgt) std::memcpy(dst, charges.data() + (size_t)(f - SG_CHARGE_ICE) * n, n * 4);
+    else if (f >= 0 && f < SG_NFIELDS) std::memcpy(dst, fields.data() + (size_t)f * n, n * 4);
+    else std::memset(dst, 0, n * 4);
   }
   std::memcpy(out + off + (size_t)state::NSTATE * n * 4, cols.data(), 3 * layer * 4);
   return SG_OK;
@@ -1229,15 +1241,28 @@ int sg_run_load_state(sg_context* ctx, sg_run run, const uint8_t* image, size_t 
     return fail(ctx, SG_ERR_INVALID, "the file's grid is " + std::to_string(h.nx) + "x" + std::to_string(h.ny) + "x" + std::to_string(h.nz) +
                                          ", the run's " + std::to_string(r->nx) + "x" + std::to_string(r->ny) + "x" + std::to_string(r->nz));
   const size_t n = (size_t)r->nx * r->ny * r->nz, layer = (size_t)r->nx * r->ny;
-  std::vector<float> fields((size_t)SG_NFIELDS * n, 0.f), cols(3 * layer);
+  std::vector<float> fields((size_t)SG_NFIELDS * n, 0.f), cols(3 * layer), charges(4 * n, 0.f);
   for (int k = 0; k < h.nfields; k++) {
     const int f = state::carried_of(k);
-    if (f >= 0) std::memcpy(fields.data() + (size_t)f * n, image + h.data_offset + (size_t)k * n * 4, n * 4);
+    if (f >= 0 && f < SG_NFIELDS) std::memcpy(fields.data() + (size_t)f * n, image + h.data_offset + (size_t)k * n * 4, n * 4);
+    else if (f >= SG_CHARGE_ICE) std::memcpy(charges.data() + (size_t)(f - SG_CHARGE_ICE) * n, image + h.data_offset + (size_t)k * n * 4, n * 4);
   }
   std::memcpy(cols.data(), image + h.data_offset + (size_t)h.nfields * n * 4, 3 * layer * 4);
   int st = sg_batch_write_packed(ctx, &run, 1, SG_ALL_FIELDS, fields.data());
   if (st != SG_OK) return st;
   if ((st = sg_run_write_columns(ctx, run, cols.data(), cols.data() + layer, cols.data() + 2 * layer)) != SG_OK) return st;
+  if (r->lgt) {
+    // an electrified run: the file's charge (none in a version-1 file), its ground charge, flash counts and charge budget
+    // (state.ts:78-81); the flashes after the file's time forgotten (:82), the vertical field as a new model's (zero)
+    const float* ptr[SG_NFIELDS_ELECTRIFIED] = {};
+    for (int k = 0; k < 4; k++) ptr[SG_CHARGE_ICE + k] = charges.data() + (size_t)k * n;
+    if ((st = sg_run_write_fields(ctx, run, SG_CHARGE_FIELDS, ptr)) != SG_OK) return st;
+    const double acc[9] = {h.charge[0], h.charge[3], h.charge[4], h.charge[5], h.charge[6], h.charge[7], h.charge[8], h.charge[1], h.charge[2]};
+    static_assert(A_CHG_SEPARATED == A_CHG_GROUND + 1 && A_FLASH_CG == A_CHG_GROUND + 8, "the charge budget's slots in order");
+    CK(cudaMemcpyAsync(r->desc.acc + A_CHG_GROUND, acc, sizeof(acc), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemsetAsync(r->desc.ez, 0, n * 4, ctx->stream));
+    r->lgt->last.clear();
+  }
   // the water budget goes on from the file's flows and start (state.ts:77)
   CK(cudaMemcpyAsync(r->desc.acc + A_WATER, h.water, 3 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   r->waterStart = h.water[4];

@@ -94,10 +94,10 @@ struct Reader {
     double num[6];
     bool is_num[6] = {};
     double water[5] = {0, 0, 0, 0, 0};  // the budget's condensed, evaporated, rainEvaporated, surface, start (absent: 0)
+    double charge[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // chargeGround, flashCount ic and cg, the charge budget (absent: 0)
   };
-  // The header's "water" object: its four flows and its start when they are numbers.
-  bool water(int depth, Top* top) {
-    static const char* keys[5] = {"condensed", "evaporated", "rainEvaporated", "surface", "start"};
+  // A nested object of the header ("water", "flashCount", "charge"): the members named in keys, when numbers, into out.
+  bool numbers(int depth, const char* const* keys, int count, double* out) {
     p++; ws();
     if (p < e && *p == '}') { p++; return true; }
     for (;;) {
@@ -108,8 +108,8 @@ struct Reader {
       if (p >= e || *p != ':') return false;
       p++; ws();
       bool done = false;
-      for (int k = 0; k < 5 && !done; k++)
-        if (key == keys[k] && p < e && (*p == '-' || std::isdigit((unsigned char)*p))) { if (!num(&top->water[k])) return false; done = true; }
+      for (int k = 0; k < count && !done; k++)
+        if (key == keys[k] && p < e && (*p == '-' || std::isdigit((unsigned char)*p))) { if (!num(&out[k])) return false; done = true; }
       if (!done && !value(depth + 1)) return false;
       ws();
       if (p < e && *p == ',') { p++; continue; }
@@ -130,7 +130,13 @@ struct Reader {
       p++; ws();
       bool done = false;
       if (top) {
-        if (key == "water" && p < e && *p == '{') { if (!water(depth + 1, top)) return false; done = true; }
+        static const char* waterKeys[5] = {"condensed", "evaporated", "rainEvaporated", "surface", "start"};
+        static const char* flashKeys[2] = {"ic", "cg"};
+        static const char* chargeKeys[6] = {"separated", "ic", "cgNegative", "cgPositive", "precipitation", "conduction"};
+        if (key == "water" && p < e && *p == '{') { if (!numbers(depth + 1, waterKeys, 5, top->water)) return false; done = true; }
+        if (key == "flashCount" && p < e && *p == '{') { if (!numbers(depth + 1, flashKeys, 2, top->charge + 1)) return false; done = true; }
+        if (key == "charge" && p < e && *p == '{') { if (!numbers(depth + 1, chargeKeys, 6, top->charge + 3)) return false; done = true; }
+        if (key == "chargeGround" && p < e && (*p == '-' || std::isdigit((unsigned char)*p))) { if (!num(&top->charge[0])) return false; done = true; }
         if (key == "format") {
           if (p < e && *p == '"') { std::string v; if (!str(&v)) return false; top->format = v; top->format_is_string = true; done = true; }
           else top->format_is_string = false;
@@ -167,7 +173,7 @@ int carried_of(int k) {
   // STATE_FIELDS (state.ts:9): u v w theta q cloud rain cold ice snow graupel hail, chargeIce chargeGraupel chargeRain
   // chargeAir, iceNumber, rainNumber, graupelNumber graupelVolume hailNumber hailVolume
   static const int map[NSTATE] = {SG_U, SG_V, SG_W, SG_THETA, SG_Q, SG_CLOUD, SG_RAIN, SG_COLD, SG_ICE, SG_SNOW, SG_GRAUPEL, SG_HAIL,
-                                  -1, -1, -1, -1, SG_ICE_NUMBER, -1, -1, -1, -1, -1};
+                                  SG_CHARGE_ICE, SG_CHARGE_GRAUPEL, SG_CHARGE_RAIN, SG_CHARGE_AIR, SG_ICE_NUMBER, -1, -1, -1, -1, -1};
   return k >= 0 && k < NSTATE ? map[k] : -1;
 }
 
@@ -203,21 +209,25 @@ std::string parse(const uint8_t* buf, size_t len, Info& info) {
   info.nx = (int)top.num[3]; info.ny = (int)top.num[4]; info.nz = (int)top.num[5];
   info.nfields = fields_of(info.version);
   for (int k = 0; k < 5; k++) info.water[k] = top.water[k];
+  for (int k = 0; k < 9; k++) info.charge[k] = top.charge[k];
   info.data_offset = data_offset(length);
   if (len != image_bytes(length, info.version, info.nx, info.ny, info.nz)) return "the file's size does not match the grid";
   return "";
 }
 
-std::string header_json(const char* config, double time, double persisted, int nx, int ny, int nz, const double water[5]) {
+std::string header_json(const char* config, double time, double persisted, int nx, int ny, int nz, const double water[5], const double* charge) {
+  static const double none[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  const double* c = charge ? charge : none;
   std::string j = "{\"format\":\"meteolab-state\",\"version\":" + std::to_string(VERSION) + ",\"config\":";
   j += config && *config ? config : "null";
   j += ",\"time\":" + js_number(time) + ",\"persisted\":" + js_number(persisted);
   j += ",\"nx\":" + std::to_string(nx) + ",\"ny\":" + std::to_string(ny) + ",\"nz\":" + std::to_string(nz);
-  j += ",\"chargeGround\":0,\"flashCount\":{\"ic\":0,\"cg\":0}";
+  j += ",\"chargeGround\":" + js_number(c[0]) + ",\"flashCount\":{\"ic\":" + js_number(c[1]) + ",\"cg\":" + js_number(c[2]) + "}";
   j += ",\"water\":{\"condensed\":" + js_number(water[0]) + ",\"evaporated\":" + js_number(water[1]) + ",\"rainEvaporated\":" +
        js_number(water[2]) + ",\"surface\":" + js_number(water[3]) + ",\"start\":" + js_number(water[4]) + "}";
   j += ",\"added\":{\"heat\":0,\"vapour\":0,\"count\":0}";
-  j += ",\"charge\":{\"separated\":0,\"ic\":0,\"cgNegative\":0,\"cgPositive\":0,\"precipitation\":0,\"conduction\":0}}";
+  j += ",\"charge\":{\"separated\":" + js_number(c[3]) + ",\"ic\":" + js_number(c[4]) + ",\"cgNegative\":" + js_number(c[5]) +
+       ",\"cgPositive\":" + js_number(c[6]) + ",\"precipitation\":" + js_number(c[7]) + ",\"conduction\":" + js_number(c[8]) + "}}";
   return j;
 }
 

@@ -16,14 +16,16 @@ constexpr int NCOLUMNS = 3;       // STATE_COLUMNS: precipitation, hailGround, h
 
 // Fields a file of this version holds (state.ts:32): 12, 16, 17, 18, 22.
 int fields_of(int version);
-// The carried field (sg_field order) behind STATE_FIELDS[k], or -1 for the ones the configured step does not carry
-// (the four charge fields, the two-moment numbers and volumes).
+// The field (sg_field and sg_charge_field ids) behind STATE_FIELDS[k], or -1 for the ones the device step does not
+// carry (the two-moment numbers and volumes); the charges (13-16) are an electrified run's.
 int carried_of(int k);
 
 struct Info {
   int version = 0, nx = 0, ny = 0, nz = 0, nfields = 0;
   double time = 0, persisted = 0;
   double water[5] = {0, 0, 0, 0, 0};  // the water budget's flows (condensed, evaporated, rainEvaporated, surface) and start
+  // chargeGround, flashCount.ic, .cg, charge.separated, .ic, .cgNegative, .cgPositive, .precipitation, .conduction
+  double charge[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   size_t data_offset = 0;   // first float of the fields
 };
 
@@ -33,8 +35,10 @@ std::string parse(const uint8_t* buf, size_t len, Info& info);
 
 // The version-5 header of saveState (state.ts:43-53) for a run of this grid; `config` is the caller's SimConfig as
 // JSON text (null when absent), `water` the budget's condensed, evaporated, rainEvaporated and surface flows and its
-// start (the reservoirs' sum when the run began, AtmosphereModel.water.start).
-std::string header_json(const char* config, double time, double persisted, int nx, int ny, int nz, const double water[5]);
+// start (the reservoirs' sum when the run began, AtmosphereModel.water.start), `charge` (nullable: zeros) the nine
+// numbers of Info::charge.
+std::string header_json(const char* config, double time, double persisted, int nx, int ny, int nz, const double water[5],
+                        const double* charge = nullptr);
 
 // Whether `text` (null-terminated; null counts as valid) is one JSON value.
 bool json_valid(const char* text);

@@ -209,3 +209,52 @@ def test_electrification_changes_no_other_field(ctx):
     assert b.charge()["electrified"] == 1 and a.charge()["electrified"] == 0
     a.retire()
     b.retire()
+
+
+def test_electrified_state_saves_and_loads(ctx):
+    """A .meteolab file of an electrified run (state.ts:34-83): the four charge fields in STATE_FIELDS order, the ground
+    charge, flash counts and charge budget in the header; a run loaded from it has them all, saves the same bytes, and
+    two loaded runs go on flashing alike."""
+    import state_format as SF
+    spec = quiet_electrified()
+    g, rho = GRID, spec.env.rho
+    f = {k: v.copy() for k, v in spec.fields.items()}
+    zs = np.asarray(g.zs)[:, None, None]
+    y = np.arange(g.ny)[None, :, None]
+    x = np.arange(g.nx)[None, None, :]
+    r2 = ((x - g.nx // 2) * g.dx) ** 2 + ((y - g.ny // 2) * g.dy) ** 2
+    air = np.asarray(rho)[:, None, None]
+    f["chargeIce"] = (4e-9 * np.exp(-r2 / 2500 ** 2 - ((zs - 9000) / 700) ** 2) / air).astype(np.float32).ravel()
+    f["chargeGraupel"] = (-4e-9 * np.exp(-r2 / 2500 ** 2 - ((zs - 6500) / 700) ** 2) / air).astype(np.float32).ravel()
+    s2 = with_fields(spec, f)
+    r = ctx.create(s2)
+    r.step(2)
+    cfg = {"seed": 42, "lightning": True}
+    img = r.save_state(cfg, persisted=0.0)
+    header, fields, _ = SF.read_state(img)
+    got = r.read(list(CHARGES))
+    for k in CHARGES:
+        assert np.array_equal(fields[k], got[k]), k
+    st = r.charge()
+    assert st["flashes_ic"] + st["flashes_cg"] > 0
+    assert header["chargeGround"] == st["ground"]
+    assert header["flashCount"] == {"ic": st["flashes_ic"], "cg": st["flashes_cg"]}
+    assert header["charge"]["separated"] == st["separated"] and header["charge"]["conduction"] == st["conduction"]
+    a, b = ctx.create(s2), ctx.create(s2)
+    a.load_state(img)
+    b.load_state(img)
+    ga = a.read(list(CHARGES))
+    for k in CHARGES:
+        assert np.array_equal(ga[k], got[k]), k
+    sa = a.charge()
+    for k in ("ground", "separated", "ic", "cg_negative", "cg_positive", "precipitation", "conduction", "flashes_ic", "flashes_cg"):
+        assert sa[k] == st[k], k
+    assert a.save_state(cfg, persisted=0.0) == img
+    a.step(2)
+    b.step(2)
+    fa, fb = a.read(list(CARRIED) + list(CHARGES)), b.read(list(CARRIED) + list(CHARGES))
+    for k in fa:
+        assert np.array_equal(fa[k], fb[k]), k
+    assert [(q["kind"], q["start"], q["charge"]) for q in a.flashes(False)] == [(q["kind"], q["start"], q["charge"]) for q in b.flashes(False)]
+    for m in (r, a, b):
+        m.retire()
