@@ -83,6 +83,10 @@ class Switches:
     lightning: int = 0
     corona: int = 1
     lightning_seed: int = 43
+    # two-moment rain (AtmosphereModel.rainMoments 2, src/core/model.ts:842): the raindrop number carried with the rain;
+    # its collisional breakup 0 none (the default), 1 NSSL's, 2 Morrison's (:843, src/core/rain2m.ts:23-31)
+    rain_moments: int = 1
+    rain_breakup: int = 0
 
     def drag_cd(self, grid: Grid) -> float:
         return drag_coefficient(self.surface, 2 * float(grid.hz[0])) if self.drag else 0.0

@@ -48,6 +48,7 @@ template <class S> std::vector<S>* extraField(Model<S>* m, int id) {
     case 103: return &m->fallRain; case 104: return &m->fallSnow; case 105: return &m->fallGraupel; case 106: return &m->fallHail;
     case 107: return &m->condensate;
     case 108: return &m->fallChargeIce; case 109: return &m->fallChargeGraupel; case 110: return &m->fieldZ;
+    case 111: return &m->rainFallNumber;
   }
   return (id >= 0 && id < N_CARRIED) ? &m->f[id] : nullptr;
 }
@@ -166,6 +167,12 @@ void orc_set_lightning(void* p, int on, int corona, int seed) {
   auto set = [&](auto* m) { m->sw.lightning = on != 0; m->sw.corona = corona != 0; m->sw.lightningSeed = seed; };
   if (h->m32) set(h->m32); else set(h->m64);
 }
+// Two-moment rain (AtmosphereModel.rainMoments, src/core/model.ts:842) and its breakup: 0 none, 1 NSSL, 2 Morrison.
+void orc_set_rain2m(void* p, int moments, int breakup) {
+  Handle* h = (Handle*)p;
+  auto set = [&](auto* m) { m->sw.rainMoments = moments; m->sw.rainBreakup = breakup; };
+  if (h->m32) set(h->m32); else set(h->m64);
+}
 // out[11]: chargeGround, separated, ic, cgNegative, cgPositive, precipitation, conduction, flashes IC, flashes CG,
 // totalCharge, flashes of the last step.
 void orc_charge_state(void* p, double* out) {
@@ -228,6 +235,23 @@ void orc_lightning_fields(void* p, double* phi, double* rho, double* state) {
   if (state) { state[0] = L->l->fromGround; state[1] = L->l->conducted; }
 }
 int orc_flash_limit(double dt) { return flashLimit(dt); }
+
+// ---------------------------------------------------------------- two-moment rain (src/core/rain2m.test.ts)
+double orc_r2m_bounded(double q, double n, double rho) { return r2m::boundedNumber(q, n, rho); }
+double orc_r2m_mean_volume(double q, double n) { return r2m::meanVolume(q, n); }
+double orc_r2m_dn(double xv) { return r2m::dnOf(xv); }
+void orc_r2m_fall(double q, double n, double rho, double* out3) { r2m::fallSpeeds(q, n, rho, out3[0], out3[1]); out3[2] = r2m::fallSpeedZ(q, n, rho); }
+double orc_r2m_limits(int which) { return which == 0 ? r2m::XV_MIN : which == 1 ? r2m::XV_MAX : r2m::RAIN_MIN; }
+// v = [q, cloud, rain, number] FP32 cells, in place; returns the evaporated rain.
+double orc_r2m_processes(float* v, double tk, double p, double rho, double dt, int breakup, int evaporate) {
+  Arr<float> a = (Arr<float>)v;
+  return r2m::processes<float>(a, a + 1, a + 2, a + 3, 0, tk, p, rho, dt, breakup, evaporate != 0);
+}
+// v = [rain, number] FP32 cells, in place.
+void orc_r2m_number_change(float* v, double before, double rho, double meanMass) {
+  Arr<float> a = (Arr<float>)v;
+  r2m::numberChange<float>(a, a + 1, 0, before, rho, meanMass);
+}
 
 // ---------------------------------------------------------------- charging (src/core/charge.test.ts)
 double orc_critical_rar(double tc) { return criticalRar(tc); }

@@ -8,6 +8,7 @@
 #include <omp.h>
 #include "oracle_solvers.h"
 #include "oracle_elec.h"
+#include "oracle_rain2m.h"
 
 namespace orc {
 
@@ -21,30 +22,46 @@ struct Switches {
   // the lightning's random numbers are seeded with config.seed + 1 (:1538); corona over land (:1539).
   bool lightning = false, corona = true;
   int lightningSeed = 43;
+  // Two-moment rain (AtmosphereModel.rainMoments 2, src/core/model.ts:842; rain2m(), :905) and its breakup (:843).
+  int rainMoments = 1, rainBreakup = r2m::NONE;
 };
 
 enum FieldId { F_RAIN, F_SNOW, F_GRAUPEL, F_HAIL, F_U, F_V, F_W, F_THETA, F_Q, F_CLOUD, F_ICE, F_ICENUMBER, F_COLD,
-               F_CHARGE_ICE, F_CHARGE_GRAUPEL, F_CHARGE_RAIN, F_CHARGE_AIR, N_CARRIED };  // charges: src/core/model.ts:210
+               F_CHARGE_ICE, F_CHARGE_GRAUPEL, F_CHARGE_RAIN, F_CHARGE_AIR,  // charges: src/core/model.ts:210
+               F_RAIN_NUMBER, N_CARRIED };                                   // raindrops per kg (two-moment rain): :194
 
 // The microphysics part of physics(z) for node i (src/core/model.ts:1391-1471): Kessler rain, then with ice the
 // freezing, crystals, snow, graupel, hail, secondary ice and the mixed-phase saturation adjustment, else the warm
 // adjustment; the cold-pool indicator's share of the cooling. Returns the evaporated rain.
+// With two-moment rain (`rainNumber` given), its processes replace Kessler's and the drop number follows the rain the
+// ice processes take or give (:1391, :1402-1435).
 template <class S>
 double microphysicsNode(Arr<S> theta, Arr<S> q, Arr<S> cloud, Arr<S> rain, Arr<S> cold, Arr<S> ice, Arr<S> iceNumber, Arr<S> snow, Arr<S> graupel,
-                        Arr<S> hail, int i, double ex, double pz, double rhoZ, double rhoGround, double dt, const Switches& sw) {
-  double evap = !sw.rainFormation ? 0 : rainProcesses<S>(q, cloud, rain, i, (double)theta[i] * ex, pz, rhoZ, dt, sw.evaporation);
+                        Arr<S> hail, int i, double ex, double pz, double rhoZ, double rhoGround, double dt, const Switches& sw, Arr<S> rainNumber = nullptr) {
+  const bool two = rainNumber != nullptr;
+  double evap = !sw.rainFormation ? 0
+               : two ? r2m::processes<S>(q, cloud, rain, rainNumber, i, (double)theta[i] * ex, pz, rhoZ, dt, sw.rainBreakup, sw.evaporation)
+                     : rainProcesses<S>(q, cloud, rain, i, (double)theta[i] * ex, pz, rhoZ, dt, sw.evaporation);
   if (evap > 0) { double cool = LV / CP / ex * evap; theta[i] -= cool; cold[i] += cool; }
   double cond;
   if (sw.ice) {
+    double rainMark = rain[i];
     freezeRain<S>(theta, rain, graupel, i, ex);
+    if (two) { r2m::numberChange<S>(rain, rainNumber, i, rainMark, rhoZ, 0); rainMark = rain[i]; }
     settleCrystals<S>(ice, iceNumber, i);
     cold[i] += iceProcesses<S>(theta, q, ice, snow, iceNumber, i, ex, pz, rhoZ, dt);
     double iceBefore = ice[i], cloudBefore = cloud[i];
+    const double snowMass = two ? r2m::exponentialMeanMass(snow[i], N0S, RHO_S, rhoZ) : 0;
     cold[i] += snowProcesses<S>(theta, q, cloud, ice, snow, rain, i, ex, pz, rhoZ, rhoGround, dt);
+    if (two) { r2m::numberChange<S>(rain, rainNumber, i, rainMark, rhoZ, snowMass); rainMark = rain[i]; }
     double rainBefore = rain[i];
+    const double graupelMass = two ? r2m::exponentialMeanMass(graupel[i], N0G, RHO_G, rhoZ) : 0;
     cold[i] += graupelProcesses<S>(theta, q, cloud, ice, snow, rain, graupel, i, ex, pz, rhoZ, dt);
+    if (two) { r2m::numberChange<S>(rain, rainNumber, i, rainMark, rhoZ, graupelMass); rainMark = rain[i]; }
     double rainFrozen = (double)theta[i] * ex < 273.15 ? jmax(0, rainBefore - (double)rain[i]) : 0;
+    const double hailMass = two ? r2m::exponentialMeanMass(hail[i], N0H, RHO_H, rhoZ) : 0;
     cold[i] += hailProcesses<S>(theta, q, cloud, ice, snow, rain, graupel, hail, i, ex, pz, rhoZ, dt);
+    if (two) r2m::numberChange<S>(rain, rainNumber, i, rainMark, rhoZ, hailMass);
     if (iceBefore > 0) iceNumber[i] *= (double)ice[i] / iceBefore;
     double splinters = splintering((double)theta[i] * ex - 273.15) * SPLINTERS * jmax(0, cloudBefore - (double)cloud[i])
       + (rainFrozen > 0 ? fragmentsPerKg(std::pow(PI * RHO_W * N0R / (rhoZ * rainBefore), .25)) * rainFrozen : 0);
@@ -68,6 +85,7 @@ template <class S> struct Model {
   // electrification (src/core/model.ts:205-245): the carriers' fall speeds, the vertical field of the last solve, the
   // charge separated per level; the ground's charge, the budget, the flash counts and this step's flashes
   std::vector<S> fallChargeIce, fallChargeGraupel, fieldZ, levelCharge;
+  std::vector<S> rainFallNumber;  // two-moment rain: the number-weighted fall speed (:1224)
   double chargeGround = 0, chargeSeparated = 0, chargeIC = 0, chargeCgNegative = 0, chargeCgPositive = 0, chargePrecipitation = 0, chargeConduction = 0;
   long flashesIC = 0, flashesCG = 0;
   std::vector<Flash> lastFlashes;
@@ -94,7 +112,7 @@ template <class S> struct Model {
     for (int k = 0; k < N_CARRIED; k++) { f[k].assign(n, 0); stageStart[k].assign(n, 0); stageTend[k].assign(n, 0); }
     fallRain.assign(n, 0); fallSnow.assign(n, 0); fallGraupel.assign(n, 0); fallHail.assign(n, 0); condensate.assign(n, 0);
     precipitation.assign(layer, 0); hailGround.assign(layer, 0); hailSize.assign(layer, 0); levelWater.assign(nz * 4, 0);
-    fallChargeIce.assign(n, 0); fallChargeGraupel.assign(n, 0); fieldZ.assign(n, 0); levelCharge.assign(nz, 0);
+    fallChargeIce.assign(n, 0); fallChargeGraupel.assign(n, 0); fieldZ.assign(n, 0); levelCharge.assign(nz, 0); rainFallNumber.assign(n, 0);
     flux = FluxTransport(g, rho.data()); solver = PressureSolver(g, rho.data()); turb = Turbulence(g, rho.data());
     flux.g = &g; solver.g = &g; turb.g = &g;
     turb.anisotropic = sw.anisotropic; turb.verticalDz = sw.verticalDz; turb.durranKlemp = sw.durranKlemp;
@@ -121,6 +139,7 @@ template <class S> struct Model {
     std::vector<Carried> c;
     c.push_back({F_RAIN, true, true, 1});
     if (sw.ice) { c.push_back({F_SNOW, true, true, 1}); c.push_back({F_GRAUPEL, true, true, 1}); c.push_back({F_HAIL, true, true, 1}); }
+    if (rain2m()) c.push_back({F_RAIN_NUMBER, true, false, 1});  // :1323
     for (int k : {F_U, F_V, F_W, F_THETA}) c.push_back({k, false, false, 1});
     c.push_back({F_Q, true, true, 1}); c.push_back({F_CLOUD, true, true, 1});
     if (sw.ice) { c.push_back({F_ICE, true, true, 1}); c.push_back({F_ICENUMBER, true, false, 1}); }
@@ -129,6 +148,7 @@ template <class S> struct Model {
     return c;
   }
   bool electrified() const { return sw.ice && sw.lightning; }  // :1316
+  bool rain2m() const { return sw.rainMoments == 2; }             // :905 (the WENO transport is the only one here)
 
   // ---------------------------------------------------------- beginStep (src/core/model.ts:893-902)
   void updateGround() {  // :644-657 (the surface pattern, city and zones are zero in the device's configuration)
@@ -151,6 +171,10 @@ template <class S> struct Model {
     for (int i = k * layer, end = i + layer; i < end; i++) {
       fr[i] = fallSpeed(rain[i], rho[k], rho[0]); fs[i] = snowFallSpeed(snow[i], rho[k], rho[0]);
       fg[i] = graupelFallSpeed(graupel[i], rho[k]); fh[i] = hailFallSpeed(hail[i], rho[k]);
+    }
+    if (rain2m()) {  // :1224
+      Arr<S> num = F(F_RAIN_NUMBER), rfn = A(rainFallNumber);
+      for (int i = k * layer, end = i + layer; i < end; i++) { double vm, vn; r2m::fallSpeeds(rain[i], num[i], rho[k], vm, vn); fr[i] = vm; rfn[i] = vn; }
     }
     if (electrified()) {  // :1230-1234
       Arr<S> ice = F(F_ICE), ci = A(fallChargeIce), cg = A(fallChargeGraupel);
@@ -196,7 +220,7 @@ template <class S> struct Model {
   }
   void sedimentStep(double dt) {  // :928-932
     std::pair<int, std::vector<S>*> falls[4] = {{F_RAIN, &fallRain}, {F_SNOW, &fallSnow}, {F_GRAUPEL, &fallGraupel}, {F_HAIL, &fallHail}};
-    for (int j = 0; j < (sw.ice ? 4 : 1); j++) {
+    for (int j = rain2m() ? 1 : 0; j < (sw.ice ? 4 : 1); j++) {  // sedimented(): two-moment rain falls on its own (:907-911)
       Arr<S> field = F(falls[j].first), vt = A(*falls[j].second);
       int parts = fallParts(field, vt, dt);
       for (int q = 0; q < parts; q++) sedimentPart(field, vt, dt / parts);
@@ -214,7 +238,47 @@ template <class S> struct Model {
     updateGround();
     run(g.nz, [&](int k, int) { fall(k); });
     if (sw.ice) collectHail(dt);
+    if (rain2m()) sedimentRain2m(dt);  // :899
     sedimentStep(dt);
+  }
+  // sedimentRain2m / sediment2m (:944-988; NSSL sediment1d, infall 4): mass with its mass-weighted speed, number with its
+  // number-weighted one, and each sub-step the number kept between what the reflectivity (at its own speed) and a number
+  // carried at the mass's speed imply. Flat ground, no two-moment ice volume.
+  void sedimentRain2m(double dt) {
+    int nz = g.nz, layer = g.layer, n = g.n;
+    Arr<S> q = F(F_RAIN), num = F(F_RAIN_NUMBER), vm = A(fallRain), vn = A(rainFallNumber);
+    std::vector<double> refl(n), carriedN(n); std::vector<float> vzv(n);
+    double courant = 0;
+    for (int z = 0; z < nz; z++) for (int i = z * layer; i < (z + 1) * layer; i++) {
+      vzv[i] = (float)((double)q[i] > r2m::RAIN_MIN ? r2m::fallSpeedZ(q[i], num[i], rho[z]) : 0);
+      double h = g.hz[z];
+      courant = jmax(courant, jmax(dt * (double)vzv[i] / h, dt * (double)vm[i] / h));
+    }
+    const int parts = (int)jmax(1, std::ceil(courant / .8));
+    const double step = dt / parts, k6 = std::pow(6 / (PI * r2m::RHO_W2), 2);
+    for (int p = 0; p < parts; p++) {
+      for (int z = 0; z < nz; z++) for (int i = z * layer; i < (z + 1) * layer; i++) {
+        double rq = rho[z] * (double)q[i], rn = rho[z] * (double)num[i];
+        refl[i] = rq > 0 && rn > 0 ? r2m::G1 * k6 * rq * rq / rn : 0;
+        carriedN[i] = num[i];
+      }
+      for (int c = 0; c < layer; c++) deposit(c, rho[0] * (double)q[c] * (double)vm[c] * step, precipitation);
+      for (int z = 0; z < nz; z++) {
+        bool top = z < nz - 1; double level = rho[z] * g.hz[z];
+        for (int i = z * layer; i < (z + 1) * layer; i++) {
+          int a = i + layer; double m = level;
+          q[i] += step * ((top ? rho[z + 1] * (double)q[a] * (double)vm[a] : 0) - rho[z] * (double)q[i] * (double)vm[i]) / m;
+          num[i] += step * ((top ? rho[z + 1] * (double)num[a] * (double)vn[a] : 0) - rho[z] * (double)num[i] * (double)vn[i]) / m;
+          carriedN[i] += step * ((top ? rho[z + 1] * carriedN[a] * (double)vm[a] : 0) - rho[z] * carriedN[i] * (double)vm[i]) / m;
+          refl[i] += step * ((top ? refl[a] * (double)vzv[a] : 0) - refl[i] * (double)vzv[i]) / g.hz[z];
+        }
+      }
+      for (int z = 0; z < nz; z++) for (int i = z * layer; i < (z + 1) * layer; i++) {
+        if (!((double)q[i] > r2m::RAIN_MIN)) { if ((double)q[i] < 0) q[i] = 0.0; num[i] = 0.0; continue; }
+        double rq = rho[z] * (double)q[i], fromZ = refl[i] > 0 ? r2m::G1 * k6 * rq * rq / refl[i] / rho[z] : INFINITY;
+        num[i] = refl[i] > 0 ? jmax(jmin(fromZ, carriedN[i]), (double)num[i]) : jmax(carriedN[i], (double)num[i]);
+      }
+    }
   }
 
   // ---------------------------------------------------------- dynamics (src/core/model.ts:1029-1051)
@@ -311,7 +375,8 @@ template <class S> struct Model {
       double q0 = q[i];
       double before[4] = {0, 0, 0, 0};
       if (electric) { before[0] = (double)ice[i] + (double)snow[i]; before[1] = (double)graupel[i] + (double)hail[i]; before[2] = rain[i]; before[3] = cloud[i]; }
-      double evap = microphysicsNode<S>(theta, q, cloud, rain, cold, ice, iceNumber, snow, graupel, hail, i, ex, pz, rhoZ, rhoGround, dt, sw);
+      double evap = microphysicsNode<S>(theta, q, cloud, rain, cold, ice, iceNumber, snow, graupel, hail, i, ex, pz, rhoZ, rhoGround, dt, sw,
+                                        rain2m() ? F(F_RAIN_NUMBER) : nullptr);
       if (electric) {  // :1454-1469 (after the microphysics' last change to the carriers; only cold changes after it there)
         double after[4] = {(double)ice[i] + (double)snow[i], (double)graupel[i] + (double)hail[i], (double)rain[i], (double)cloud[i]};
         double now[4] = {cI[i], cG[i], cR[i], cA[i]};

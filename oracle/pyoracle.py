@@ -18,9 +18,10 @@ _lib = None
 
 CARRIED = ("rain", "snow", "graupel", "hail", "u", "v", "w", "theta", "q", "cloud", "ice", "iceNumber", "cold")
 CHARGES = ("chargeIce", "chargeGraupel", "chargeRain", "chargeAir")
+RAIN_NUMBER = "rainNumber"   # field id 17: raindrops per kg (two-moment rain)
 EXTRA = {"precipitation": 100, "hailGround": 101, "hailSize": 102, "fallSpeed": 103, "snowFall": 104,
          "graupelFall": 105, "hailFall": 106, "condensate": 107, "chargeFallIce": 108, "chargeFallGraupel": 109,
-         "fieldZ": 110}
+         "fieldZ": 110, "rainFallNumber": 111}
 
 _d = C.POINTER(C.c_double)
 _f = C.POINTER(C.c_float)
@@ -29,7 +30,8 @@ _f = C.POINTER(C.c_float)
 def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (plain g++/OpenMP)."""
     sources = [os.path.join(HERE, n) for n in ("oracle.cpp", "oracle_core.h", "oracle_solvers.h", "oracle_model.h", "oracle_diag.h",
-                                               "oracle_elec.h", os.path.join("..", "meteolab_gb300", "csrc", "sg_takahashi.h"))]
+                                               "oracle_elec.h", "oracle_rain2m.h",
+                                               os.path.join("..", "meteolab_gb300", "csrc", "sg_takahashi.h"))]
     if force or not os.path.exists(LIB_PATH) or any(os.path.getmtime(s) > os.path.getmtime(LIB_PATH) for s in sources):
         subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
     return LIB_PATH
@@ -83,6 +85,16 @@ def lib():
                                                      C.c_int, C.c_int, C.c_int, _d, _d, _d, _d, _f, _d, C.c_double, C.c_int]
             L.orc_set_lightning.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
             L.orc_charge_state.argtypes = [C.c_void_p, _d]
+            L.orc_set_rain2m.argtypes = [C.c_void_p, C.c_int, C.c_int]
+            for name, nargs in (("orc_r2m_bounded", 3), ("orc_r2m_mean_volume", 2), ("orc_r2m_dn", 1)):
+                getattr(L, name).restype = C.c_double
+                getattr(L, name).argtypes = [C.c_double] * nargs
+            L.orc_r2m_fall.argtypes = [C.c_double] * 3 + [_d]
+            L.orc_r2m_limits.restype = C.c_double
+            L.orc_r2m_limits.argtypes = [C.c_int]
+            L.orc_r2m_processes.restype = C.c_double
+            L.orc_r2m_processes.argtypes = [_f] + [C.c_double] * 4 + [C.c_int, C.c_int]
+            L.orc_r2m_number_change.argtypes = [_f, C.c_double, C.c_double, C.c_double]
             _i = C.POINTER(C.c_int)
             L.orc_flash.argtypes = [C.c_void_p, C.c_int, _d, _i, _i, _i, _d, C.c_int]
             L.orc_lightning_create.restype = C.c_void_p
@@ -152,6 +164,8 @@ class OracleModel:
         self.h = L.orc_create(1 if fp64 else 0, *args[:7], args[7], args[8], args[9], dp(env7), dp(sw), threads)
         self._keep = (keep, env7, sw)
         sw_ = spec.switches
+        if getattr(sw_, "rain_moments", 1) == 2:
+            L.orc_set_rain2m(self.h, 2, int(getattr(sw_, "rain_breakup", 0)))
         if getattr(sw_, "lightning", False):
             L.orc_set_lightning(self.h, 1, 1 if getattr(sw_, "corona", True) else 0, int(getattr(sw_, "lightning_seed", 43)))
         for name, arr in spec.fields.items():
@@ -171,6 +185,8 @@ class OracleModel:
             return CARRIED.index(name)
         if name in CHARGES:
             return len(CARRIED) + CHARGES.index(name)
+        if name == RAIN_NUMBER:
+            return len(CARRIED) + len(CHARGES)
         return EXTRA[name]
 
     def set(self, name: str, values: np.ndarray):
@@ -348,6 +364,44 @@ class OracleLightning:
         phi, rho, st = np.empty(n), np.empty(n), np.empty(2)
         lib().orc_lightning_fields(self.h, dp(phi), dp(rho), dp(st))
         return phi, rho, dict(fromGround=st[0], conducted=st[1])
+
+
+BREAKUP = {"none": 0, "nssl": 1, "morrison": 2}
+
+
+def r2m_bounded(q, n, rho):
+    return lib().orc_r2m_bounded(q, n, rho)
+
+
+def r2m_mean_volume(q, n):
+    return lib().orc_r2m_mean_volume(q, n)
+
+
+def r2m_dn(xv):
+    return lib().orc_r2m_dn(xv)
+
+
+def r2m_limits():
+    """(XV_MIN, XV_MAX, RAIN_MIN) of rain2m.ts."""
+    return tuple(lib().orc_r2m_limits(k) for k in range(3))
+
+
+def r2m_fall(q, n, rho):
+    """(mass-weighted, number-weighted, reflectivity-weighted) fall speeds."""
+    out = np.empty(3)
+    lib().orc_r2m_fall(q, n, rho, dp(out))
+    return tuple(out)
+
+
+def r2m_processes(cell: np.ndarray, tk, p, rho, dt, breakup="none", evaporate=True):
+    """rain2mProcesses on a float32 cell [q, cloud, rain, number] in place; returns the evaporated rain."""
+    assert cell.dtype == np.float32 and cell.size == 4
+    return lib().orc_r2m_processes(fp(cell), tk, p, rho, dt, BREAKUP[breakup], 1 if evaporate else 0)
+
+
+def r2m_number_change(cell: np.ndarray, before, rho, mean_mass):
+    """rainNumberChange on a float32 cell [rain, number] in place."""
+    lib().orc_r2m_number_change(fp(cell), before, rho, mean_mass)
 
 
 def flash_limit(dt: float) -> int:
