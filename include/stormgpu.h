@@ -42,8 +42,11 @@ enum sg_field {
 /* An electrified run (sg_switches.lightning with ice) also carries the charge on the ice-snow, graupel-hail, rain and
  * droplet-ion carriers, C per kg of air (AtmosphereModel.chargeIce, chargeGraupel, chargeRain, chargeAir,
  * src/core/model.ts:210), fields 13-16 of sg_run_read_fields / sg_run_write_fields (host[f] by field id). */
-enum sg_charge_field { SG_CHARGE_ICE = 13, SG_CHARGE_GRAUPEL, SG_CHARGE_RAIN, SG_CHARGE_AIR, SG_NFIELDS_ELECTRIFIED };
+/* A two-moment run (sg_switches.rain_moments 2) also carries the raindrops per kg of air (AtmosphereModel.rainNumber,
+ * :194), field 17. */
+enum sg_extra_field { SG_CHARGE_ICE = 13, SG_CHARGE_GRAUPEL, SG_CHARGE_RAIN, SG_CHARGE_AIR, SG_RAIN_NUMBER, SG_NFIELDS_EXTRA };
 #define SG_CHARGE_FIELDS (0xFu << SG_CHARGE_ICE)
+#define SG_NFIELDS_ELECTRIFIED SG_NFIELDS_EXTRA
 
 typedef struct sg_context sg_context;
 typedef int32_t sg_run;
@@ -95,6 +98,11 @@ typedef struct sg_switches {
   int32_t lightning;
   int32_t corona;          /* 1: the ground gives corona (over land; surfaceType 'water': 0, :1539) */
   int32_t lightning_seed;  /* the lightning's random numbers: config.seed + 1 (:1538) */
+  /* 2: two-moment rain after NSSL (AtmosphereModel.rainMoments, :842; src/core/rain2m.ts): the drop number carried,
+   * transported and falling with the rain (sedimentRain2m, :944-988), the NSSL warm-rain processes instead of Kessler's
+   * and the number following the rain the ice processes take or give; 1: one-moment rain (the configured step). */
+  int32_t rain_moments;
+  int32_t rain_breakup;    /* two-moment rain's collisional breakup (rainBreakup, :843): 0 none, 1 NSSL's, 2 Morrison's */
   int32_t reserved2;
 } sg_switches;
 
@@ -140,10 +148,10 @@ typedef struct sg_run_counters {
 int sg_context_create(int device, uint64_t hbm_budget_bytes, sg_context** out);
 int sg_context_destroy(sg_context* ctx);
 const char* sg_last_error(sg_context* ctx);
-/* Bytes of HBM one run of this grid takes (state, scratch, solver tables); an electrified run's (with its charge
- * carriers and lightning buffers). */
+/* Bytes of HBM one run of this grid takes (state, scratch, solver tables); a run with these switches (electrified:
+ * its charge carriers and lightning buffers; two-moment rain: its drop number). */
 uint64_t sg_run_bytes(const sg_grid* grid);
-uint64_t sg_run_bytes_electrified(const sg_grid* grid);
+uint64_t sg_run_bytes_for(const sg_grid* grid, const sg_switches* sw);
 
 /* ---- runs (replace `new AtmosphereModel(config, grid, profile)`, src/core/model.ts:329; fields as its arrays) */
 /* init[SG_NFIELDS] host arrays in sg_field order (theta is the full potential temperature, K). */

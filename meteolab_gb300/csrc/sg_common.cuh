@@ -2,7 +2,7 @@
 //
 // HBM layout of one run (all FP32 unless noted, n = nx*ny*nz nodes, node i = x + nx*(y + ny*z)):
 //   fld   3 sets x 13 fields x n      set A = the state between steps, B and C = RK3 stage / mixing scratch; an
-//                                     electrified run's 3 sets x 4 charge carriers x n after them
+//                                     electrified or two-moment run's 3 sets x 5 extra fields x n after them
 //   faces 4 x n                       projected face mass fluxes mx, my, mz and their divergence
 //   kmkh  2 x n                       eddy viscosities (vertical km, horizontal kh)
 //   phi   n                           face-projection potential
@@ -30,9 +30,10 @@ namespace sg {
 constexpr int NF = 13;  // carried fields
 enum Field { RAIN = 0, SNOW, GRAUPEL, HAIL, U, V, W, THETA, Q, CLOUD, ICE, ICENUM, COLD };
 // An electrified run also carries the charge on the ice-snow, graupel-hail, rain and droplet-ion carriers (C/kg,
-// src/core/model.ts:210): WENO fields without the positivity fix, not mixed (:1331, :1338-1344).
-constexpr int NFE = 17;
-enum ChargeField { CHARGE_ICE = 13, CHARGE_GRAUPEL, CHARGE_RAIN, CHARGE_AIR };
+// src/core/model.ts:210), a two-moment run the raindrop number (per kg, :194): WENO fields without the positivity fix,
+// not mixed (:1323, :1331, :1338-1344). Such a run's sets hold all five extra fields (NXE) after the 13 base fields'.
+constexpr int NXE = 5, NFE = NF + NXE;
+enum ExtraField { CHARGE_ICE = 13, CHARGE_GRAUPEL, CHARGE_RAIN, CHARGE_AIR, RAIN_NUMBER };
 // WENO5 for the water species and the cold-pool indicator, linear fifth-order upwind for u, v, w, theta
 // (src/core/model.ts:1320-1328).
 SG_HD bool monotone(int f) { return !(f == U || f == V || f == W || f == THETA); }
@@ -73,7 +74,7 @@ static_assert(sizeof(TriAB) == 16, "one 16-byte load a level");
 struct RunDesc {
   int nx, ny, nz, layer, n, nm, mh, ncells;
   int fx_nf, fy_nf, fx_rad[8], fy_rad[8];  // FFT radix plans of nx and ny
-  int slot, flags, nf, pad1;  // nf: fields a set (NF, or NFE for an electrified run)
+  int slot, flags, nf, breakup;  // nf: the run's field ids (NF, or NFE with the extra fields); breakup: two-moment rain's
   float dx, dy, inv_dx, inv_dy, dt, height;
   float inv_dx_lo, inv_dy_lo, inv_dt, inv_dt_lo;      // FP32 rounding errors of 1/dx, 1/dy; 1/dt as a pair
   float coriolis, keep, sponge_start, cs, drag, frame_u, frame_v, ue0, ve0, env_speed, lenH2, capH, rho0;
@@ -103,15 +104,16 @@ struct RunDesc {
   int core_lo, core_hi;                // the cloudy-core levels of countCores (:1653)
   float meso_zeta;                     // mesoCoreZeta(dx) (:129)
   float pad2;
-  // electrified runs (RF_ELEC): the step-start fall speeds [4][n] (ice-snow and graupel-hail charge carriers, rain,
-  // snow), the vertical field of the last solve [n] (V/m, for the inductive charging), the sedimentation's charge
-  // reaching the ground per work item
+  // electrified or two-moment runs: the step-start fall speeds [6][n] (ice-snow and graupel-hail charge carriers, rain,
+  // snow, rain's number- and reflectivity-weighted), the vertical field of the last solve [n] (V/m, for the inductive
+  // charging), the sedimentation's charge reaching the ground per work item
   float* vfall;
   float* ez;
   double* cpart;
 };
 enum RunFlags { RF_LOADING = 1, RF_EVAP = 2, RF_RAINFORM = 4, RF_ANISO = 8, RF_VDZ = 16, RF_DK = 32, RF_STAGES = 64, RF_ICE = 128,
-                RF_REFINE = 256, RF_ROTATION = 512, RF_ELEC = 1024 };
+                RF_REFINE = 256, RF_ROTATION = 512, RF_ELEC = 1024, RF_RAIN2M = 2048 };
+constexpr int RF_EXTRA = RF_ELEC | RF_RAIN2M;  // a run with the extra fields
 // diag columns: the UH column, the core sums, the swaths, the core labels; then the ground columns of a sample
 enum DiagColumn { DG_UH = 0, DG_COREW, DG_COREWZ, DG_GUST_MAX, DG_UH_MAX, DG_LABEL, DG_RATE, DG_HAIL, DG_GUST, DG_THV, DG_MASK, DG_COUNT };
 // rot layout (doubles): the rotation state (src/core/model.ts:263), the run's model time, then the step's keys and the
@@ -120,7 +122,8 @@ enum RotSlot { R_UH = 0, R_X, R_Y, R_ANTI, R_PERSISTED, R_UH01, R_UH03, R_LOW, R
                K_UH = 12, K_01, K_MIN, K_03,
                M_UP = 16, M_DOWN, M_CLOUD, M_TOP, M_THERMAL, M_COLD, R_COUNT = 24 };
 // scr layout
-enum Scratch { S_COURANT = 0, S_FILL = 4, S_CCOURANT = 11, S_COUNT = 16 };  // S_CCOURANT: the three falling charges
+// S_CCOURANT: the three falling charges; S_R2M: two-moment rain's fall (mass and reflectivity speeds)
+enum Scratch { S_COURANT = 0, S_FILL = 4, S_CCOURANT = 11, S_R2M = 14, S_COUNT = 16 };
 // cnt layout
 // C_TIMEOUT: a kernel's bounded wait for its own asynchronous copies ran out (the run is then failed too)
 enum Counter { C_CLIPPED = 0, C_STEPS = 1, C_FAILED = 2, C_TIMEOUT = 3, C_COUNT = 4 };
@@ -135,7 +138,7 @@ SG_HD float lvl(const RunDesc& R, int which, int z) { return R.lv[which * R.nz +
 // Set s of the 13 base fields is fld[s * 13 n ...]; an electrified run's charge carriers follow the three sets,
 // four fields a set, so the base fields keep their offsets (and the hot kernels their constant strides).
 SG_HD float* field(const RunDesc& R, int set, int f) {
-  return f < NF ? R.fld + ((size_t)set * NF + f) * R.n : R.fld + ((size_t)3 * NF + (size_t)set * (NFE - NF) + (f - NF)) * R.n;
+  return f < NF ? R.fld + ((size_t)set * NF + f) * R.n : R.fld + ((size_t)3 * NF + (size_t)set * NXE + (f - NF)) * R.n;
 }
 
 // ---- face reconstruction. Every operation is an explicitly rounded one (no contraction left to the compiler), so

@@ -18,6 +18,7 @@
 #include "sg_fft.cuh"
 #include "sg_physics.cuh"
 #include "sg_charge.cuh"
+#include "sg_rain2m.cuh"
 #include "sg_kernels.h"
 #include "sg_device.cuh"
 
@@ -171,27 +172,35 @@ __global__ void k_fall_courant(const RunDesc* __restrict__ runs, const int4* ite
       float m = warpMax(c[f]);
       if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMaxPos(R.scr + S_COURANT + f, m);
     }
-    if (R.flags & RF_ELEC) {
+    if (R.flags & RF_EXTRA) {
       // the charge carriers' fall speeds (:1230-1234) from the step-start water, with rain's and snow's own (the
-      // charge on rain falls with it; the charging reads the snow's), and the charges' Courant numbers
+      // charge on rain falls with it; the charging reads the snow's), and the charges' Courant numbers; two-moment
+      // rain's mass-, number- and reflectivity-weighted speeds from both moments (:1224) and its Courant number (:973)
       const size_t n = R.n;
-      const float *ice = field(R, 0, ICE), *cI = field(R, 0, CHARGE_ICE), *cG = field(R, 0, CHARGE_GRAUPEL), *cR = field(R, 0, CHARGE_RAIN);
-      float cc[3] = {0.f, 0.f, 0.f};
+      const bool elec = R.flags & RF_ELEC, two = R.flags & RF_RAIN2M;
+      const float *ice = field(R, 0, ICE), *num = field(R, 0, RAIN_NUMBER);
+      const float *cI = field(R, 0, CHARGE_ICE), *cG = field(R, 0, CHARGE_GRAUPEL), *cR = field(R, 0, CHARGE_RAIN);
+      float cc[4] = {0.f, 0.f, 0.f, 0.f};
       for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
         const int z = i / R.layer;
         const float rho = lvl(R, L_RHO, z), fsq = lvl(R, L_FALLSQ, z), k = R.dt * lvl(R, L_INV_HZ, z);
         const float a = rain[i], b = snow[i], g = graupel[i], h = hail[i], ic = ice[i];
-        const float vr = phys::rainFall(a, rho, fsq), vs = phys::snowFall(b, rho, fsq), vg = phys::graupelFall(g, rho), vh = phys::hailFall(h, rho);
+        float vr, vn = 0.f, vz = 0.f;
+        if (two) r2m::fallSpeeds(a, num[i], rho, vr, vn, vz); else vr = phys::rainFall(a, rho, fsq);
+        const float vs = phys::snowFall(b, rho, fsq), vg = phys::graupelFall(g, rho), vh = phys::hailFall(h, rho);
         const float is = ic + b, gh = g + h;
         const float vi = is > 0.f ? b * vs / is : 0.f, vgh = gh > 0.f ? (g * vg + h * vh) / gh : 0.f;
         R.vfall[i] = vi; R.vfall[n + i] = vgh; R.vfall[2 * n + i] = vr; R.vfall[3 * n + i] = vs;
-        if (cI[i] != 0.f) cc[0] = fmaxf(cc[0], k * vi);
-        if (cG[i] != 0.f) cc[1] = fmaxf(cc[1], k * vgh);
-        if (cR[i] != 0.f) cc[2] = fmaxf(cc[2], k * vr);
+        if (two) { R.vfall[4 * n + i] = vn; R.vfall[5 * n + i] = vz; cc[3] = fmaxf(cc[3], k * fmaxf(vz, vr)); }
+        if (elec) {
+          if (cI[i] != 0.f) cc[0] = fmaxf(cc[0], k * vi);
+          if (cG[i] != 0.f) cc[1] = fmaxf(cc[1], k * vgh);
+          if (cR[i] != 0.f) cc[2] = fmaxf(cc[2], k * vr);
+        }
       }
-      for (int f = 0; f < 3; f++) {
+      for (int f = 0; f < 4; f++) {
         float m = warpMax(cc[f]);
-        if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMaxPos(R.scr + S_CCOURANT + f, m);
+        if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMaxPos(R.scr + (f < 3 ? S_CCOURANT + f : S_R2M), m);
       }
     }
   }
@@ -223,7 +232,7 @@ __global__ void k_sediment(const RunDesc* __restrict__ runs, const int4* items, 
     float* precip = R.cols;
     float* hailGround = R.cols + layer;
     float* hailSize = R.cols + 2 * layer;
-    for (int f = 0; f < 4; f++) {
+    for (int f = (R.flags & RF_RAIN2M) ? 1 : 0; f < 4; f++) {  // sedimented(): two-moment rain falls on its own (:907-911)
       float* a = field(R, 0, f);
       const float courant = R.scr[S_COURANT + f];
       const int parts = max(1, (int)ceilf(courant / .8f));
@@ -297,6 +306,76 @@ __global__ void k_sediment(const RunDesc* __restrict__ runs, const int4* items, 
         double s = 0;
         for (int k = 0; k < SED_COLS; k++) s += gsum[k];
         R.cpart[items[it].y] = s;
+      }
+    }
+    __syncthreads();  // the level tables are restaged for the block's next item
+  }
+}
+
+// Two-moment rain's fall (sedimentRain2m / sediment2m, :944-988; NSSL sediment1d, infall 4), one thread a column: the
+// mass with its mass-weighted speed, the number with its number-weighted one, a reflectivity and a number carried at
+// the mass's speed beside them; every sub-step the number is kept between what those two imply. Bottom-up, so each
+// face uses the values above from before the sub-step; the ground flux into the rain gauge. Sub-steps by the faster of
+// the reflectivity's and the mass's speed over the run.
+__global__ void k_sediment_2m(const RunDesc* __restrict__ runs, const int4* items, int nitems) {
+  extern __shared__ float sm[];
+  FOR_ITEMS {
+    const RunDesc& R = runs[items[it].x];
+    if (R.cnt[C_FAILED] || !(R.flags & RF_RAIN2M)) continue;
+    const int nz = R.nz, layer = R.layer, t = threadIdx.x;
+    float* sq = sm;                     // [nz][SED_COLS] each: mass, number, carried number, reflectivity, the speeds
+    float* sn = sq + nz * SED_COLS;
+    float* sc = sn + nz * SED_COLS;
+    float* sr = sc + nz * SED_COLS;
+    float* vm = sr + nz * SED_COLS;
+    float* vn = vm + nz * SED_COLS;
+    float* vz = vn + nz * SED_COLS;
+    float* lrho = vz + nz * SED_COLS;   // [nz] rho0, 1/(rho0 h), 1/h
+    float* lk = lrho + nz;
+    float* lh = lk + nz;
+    for (int z = t; z < nz; z += blockDim.x) { lrho[z] = lvl(R, L_RHO, z); lk[z] = lvl(R, L_INV_RHO, z) * lvl(R, L_INV_HZ, z); lh[z] = lvl(R, L_INV_HZ, z); }
+    __syncthreads();
+    const int c = items[it].y * SED_COLS + t;
+    if (t < SED_COLS && c < layer) {
+      float* q = field(R, 0, RAIN);
+      float* num = field(R, 0, RAIN_NUMBER);
+      const size_t n = R.n;
+      bool any = false;
+      for (int z = 0; z < nz; z++) {
+        const int i = c + z * layer, s = z * SED_COLS + t;
+        sq[s] = q[i]; sn[s] = num[i]; vm[s] = R.vfall[2 * n + i]; vn[s] = R.vfall[4 * n + i]; vz[s] = R.vfall[5 * n + i];
+        any |= sq[s] != 0.f || sn[s] != 0.f;
+      }
+      if (any) {
+        const int parts = max(1, (int)ceilf(R.scr[S_R2M] / .8f));
+        const float step = R.dt / (float)parts;
+        float* precip = R.cols;
+        for (int p = 0; p < parts; p++) {
+          for (int z = 0; z < nz; z++) {
+            const int s = z * SED_COLS + t;
+            const float rq = lrho[z] * sq[s], rn = lrho[z] * sn[s];
+            sr[s] = rq > 0.f && rn > 0.f ? r2m::G1 * r2m::K6 * rq * rq / rn : 0.f;
+            sc[s] = sn[s];
+          }
+          precip[c] += R.rho0 * sq[t] * vm[t] * step;
+          float inQ = 0.f, inN = 0.f, inC = 0.f, inR = 0.f;  // the fluxes into level z from above, from before this sub-step
+          for (int z = nz - 1; z >= 0; z--) {
+            const int s = z * SED_COLS + t;
+            const float oq = lrho[z] * sq[s] * vm[s], on = lrho[z] * sn[s] * vn[s], oc = lrho[z] * sc[s] * vm[s], orr = sr[s] * vz[s];
+            sq[s] += step * (inQ - oq) * lk[z];
+            sn[s] += step * (inN - on) * lk[z];
+            sc[s] += step * (inC - oc) * lk[z];
+            sr[s] += step * (inR - orr) * lh[z];
+            inQ = oq; inN = on; inC = oc; inR = orr;
+          }
+          for (int z = 0; z < nz; z++) {
+            const int s = z * SED_COLS + t;
+            if (!(sq[s] > r2m::RAIN_MIN)) { if (sq[s] < 0.f) sq[s] = 0.f; sn[s] = 0.f; continue; }
+            const float rq = lrho[z] * sq[s];
+            sn[s] = sr[s] > 0.f ? fmaxf(fminf(r2m::G1 * r2m::K6 * rq * rq / sr[s] / lrho[z], sc[s]), sn[s]) : fmaxf(sc[s], sn[s]);
+          }
+        }
+        for (int z = 0; z < nz; z++) { const int i = c + z * layer, s = z * SED_COLS + t; q[i] = sq[s]; num[i] = sn[s]; }
       }
     }
     __syncthreads();  // the level tables are restaged for the block's next item
@@ -1273,7 +1352,7 @@ __global__ void __launch_bounds__(256, 3) k_physics(const RunDesc* __restrict__ 
 #pragma unroll
     for (int k = 0; k < NW; k++) whi[k] = wlo[k] = 0.f;
     bool bad = false;
-    const bool elec = ELEC && (R.flags & RF_ELEC);
+    const bool elec = ELEC && (R.flags & RF_ELEC);  // (ELEC: the kernel of a batch with extra fields)
     for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
       const int z = i / R.layer;
       auto fixed = [&](int kc, float x) { return x < 1e-10f ? 0.f : fmaf(x, fill[kc], x); };
@@ -1293,8 +1372,13 @@ __global__ void __launch_bounds__(256, 3) k_physics(const RunDesc* __restrict__ 
       const float q0 = s.q;
       float before[4];
       if constexpr (ELEC) if (elec) { before[0] = s.ice + s.snow; before[1] = s.graupel + s.hail; before[2] = s.rain; before[3] = s.cloud; }
-      float evap;
-      phys::microphysics(s, pl, dt, R.flags, evap);
+      float evap, rnum = 0.f;
+      if constexpr (ELEC) {
+        if (R.flags & RF_RAIN2M) {
+          rnum = field(R, in, RAIN_NUMBER)[i];
+          r2m::microphysics(s, rnum, pl, dt, R.flags, R.breakup, evap);
+        } else phys::microphysics(s, pl, dt, R.flags, evap);
+      } else phys::microphysics(s, pl, dt, R.flags, evap);
       if constexpr (ELEC) if (elec) {
         const float after[4] = {s.ice + s.snow, s.graupel + s.hail, s.rain, s.cloud};
         float c[4] = {field(R, in, CHARGE_ICE)[i], field(R, in, CHARGE_GRAUPEL)[i], field(R, in, CHARGE_RAIN)[i], field(R, in, CHARGE_AIR)[i]};
@@ -1330,6 +1414,7 @@ __global__ void __launch_bounds__(256, 3) k_physics(const RunDesc* __restrict__ 
       field(R, 0, COLD)[i] = s.cold;
       field(R, mid, U)[i] = u; field(R, mid, V)[i] = v; field(R, mid, W)[i] = w; field(R, mid, THETA)[i] = s.thp;
       field(R, mid, Q)[i] = s.q; field(R, mid, CLOUD)[i] = s.cloud; field(R, mid, ICE)[i] = s.ice; field(R, mid, ICENUM)[i] = s.inum;
+      if constexpr (ELEC) if (R.flags & RF_RAIN2M) field(R, 0, RAIN_NUMBER)[i] = rnum;  // not mixed: straight to set A
     }
     if (__syncthreads_or(bad) && threadIdx.x == 0) atomicExch(&R.cnt[C_FAILED], 1ull);
     size_t nch = (R.n + CHUNK - 1) / CHUNK;
@@ -1661,6 +1746,9 @@ void launch_pres_correct(const Launch& L, int set, int final_) {
 
 void launch_fill_partial(const Launch& L, int set) { k_fill_partial<<<GRID(L.n, L.cap), 128, 0, L.stream>>>(L.runs, L.items, L.n, set); }
 void launch_fill_final(const Launch& L) { k_fill_final<<<GRID(L.n, L.cap), 32, 0, L.stream>>>(L.runs, L.items, L.n); }
+void launch_sediment_2m(const Launch& L, int maxnz) {
+  k_sediment_2m<<<GRID(L.n, L.cap), SED_COLS, (7 * maxnz * SED_COLS + 3 * maxnz) * sizeof(float), L.stream>>>(L.runs, L.items, L.n);
+}
 void launch_physics(const Launch& L, int in, int mid, bool elec) {
   if (elec) k_physics<true><<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, in, mid);
   else k_physics<false><<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, in, mid);
@@ -1679,6 +1767,7 @@ cudaError_t set_smem_limits(int bytes) {
   if ((e = smem_limit(k_proj_div_xfft, bytes)) != cudaSuccess) return e;
   if ((e = smem_limit(k_proj_xifft, bytes)) != cudaSuccess) return e;
   if ((e = smem_limit(k_sediment, bytes)) != cudaSuccess) return e;
+  if ((e = smem_limit(k_sediment_2m, bytes)) != cudaSuccess) return e;
   if ((e = smem_limit(k_proj_div_fft2, bytes)) != cudaSuccess) return e;
   if ((e = smem_limit(k_proj_ifft2, bytes)) != cudaSuccess) return e;
   if ((e = smem_limit(k_refine_residual<0, 0>, bytes)) != cudaSuccess) return e;

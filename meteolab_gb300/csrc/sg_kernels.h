@@ -57,6 +57,7 @@ bool transport_bulk_ok(int TX, int TY, int min_nx, bool all_nx4);
 void launch_fill_partial(const Launch& L, int set);
 void launch_fill_final(const Launch& L);
 void launch_physics(const Launch& L, int in, int mid, bool elec);
+void launch_sediment_2m(const Launch& L, int maxnz);
 void launch_viscosity(const Launch& L, int set);
 // Mixing on (run, tile of TX x TY columns, z0, z1) items.
 void launch_mix(const Launch& L, int in, int TX, int TY);

@@ -37,12 +37,13 @@ struct Layout {
   size_t fld, faces, kmkh, phi, pres, pres2, spec, cols, lv, lv64, triF, triP, ab, twx, twy, scr, part, acc, cnt, items, diag, rot;
   size_t vfall = 0, ez = 0, cpart = 0, lgt = 0, total;  // electrified runs only
 };
-// One run's allocation; an electrified run's sets hold the four charge carriers too, and it has its fall speeds, the
-// vertical field and the lightning's buffers (sg_lightning.cu) after the rest.
-Layout layout(int nx, int ny, int nz, bool elec = false) {
+// One run's allocation (flags: its RF_ELEC / RF_RAIN2M); such a run's sets hold the extra fields too, and it has its
+// fall speeds and the vertical field after the rest, an electrified one also the lightning's buffers (sg_lightning.cu).
+Layout layout(int nx, int ny, int nz, int flags = 0) {
+  const bool extra = flags & RF_EXTRA, elec = flags & RF_ELEC;
   Layout L; size_t n = (size_t)nx * ny * nz, layer = (size_t)nx * ny, nm = nx / 2 + 1, nch = (n + CHUNK - 1) / CHUNK, o = 0;
   auto take = [&](size_t bytes) { size_t at = o; o += align(bytes); return at; };
-  L.fld = take(3 * (size_t)(elec ? NFE : NF) * n * 4); L.faces = take(4 * n * 4); L.kmkh = take(2 * n * 4); L.phi = take(n * 4);
+  L.fld = take(3 * (size_t)(extra ? NFE : NF) * n * 4); L.faces = take(4 * n * 4); L.kmkh = take(2 * n * 4); L.phi = take(n * 4);
   L.pres = take(layer * (nz - 1) * 4); L.pres2 = take(layer * (nz - 1) * 4); L.spec = take(nm * nz * ny * 8); L.cols = take(3 * layer * 4);
   L.lv = take((size_t)L_COUNT * nz * 4); L.lv64 = take((size_t)D_COUNT * nz * 8);
   L.triF = take(nm * nz * ny * 24); L.triP = take(nm * (nz - 1) * ny * 24); L.ab = take(nm * ny * 16);
@@ -50,10 +51,8 @@ Layout layout(int nx, int ny, int nz, bool elec = false) {
   L.acc = take(A_COUNT * 8); L.cnt = take(C_COUNT * 8);
   L.items = take(nch * 16);  // the run's own per-node work items (field conversions outside a batch plan)
   L.diag = take((size_t)DG_COUNT * layer * 4); L.rot = take(R_COUNT * 8);
-  if (elec) {
-    L.vfall = take(4 * n * 4); L.ez = take(n * 4); L.cpart = take(((layer + 63) / 64) * 8);
-    L.lgt = take(lightning_bytes(nx, ny, nz));
-  }
+  if (extra) { L.vfall = take(6 * n * 4); L.ez = take(n * 4); L.cpart = take(((layer + 63) / 64) * 8); }
+  if (elec) L.lgt = take(lightning_bytes(nx, ny, nz));
   L.total = o;
   return L;
 }
@@ -94,6 +93,8 @@ struct Plan {
   bool unrefined = false;                                             // some run does not (k_pres_correct<1> has work)
   bool rotation = false;                                              // some run tracks its rotation and swaths
   bool elec = false;                                                  // some run is electrified (charges, lightning)
+  bool extra = false;                                                 // some run has the extra fields (electrified or two-moment)
+  bool rain2m = false;                                                // some run has two-moment rain
   bool tuned = false;                                                 // TX, TY, wenoG chosen by timing
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -311,7 +312,10 @@ int validate(sg_context* ctx, const sg_grid* g, const sg_base_state* b, const sg
   if (g->nz > 128) return fail(ctx, SG_ERR_UNSUPPORTED, "nz > 128 levels");
   if (g->nx > 4096 || g->ny > 4096) return fail(ctx, SG_ERR_UNSUPPORTED, "nx or ny > 4096");
   // the kernels index a run's field sets with 32-bit element offsets
-  if ((size_t)g->nx * g->ny * g->nz * 3 * (sw->lightning ? NFE : NF) >= (1ull << 31)) return fail(ctx, SG_ERR_UNSUPPORTED, "grid beyond 55 million nodes");
+  if ((size_t)g->nx * g->ny * g->nz * 3 * ((sw->lightning || sw->rain_moments == 2) ? NFE : NF) >= (1ull << 31))
+    return fail(ctx, SG_ERR_UNSUPPORTED, "grid beyond 55 million nodes");
+  if (sw->rain_moments != 1 && sw->rain_moments != 2) return fail(ctx, SG_ERR_INVALID, "rain_moments must be 1 or 2");
+  if (sw->rain_breakup < 0 || sw->rain_breakup > 2) return fail(ctx, SG_ERR_INVALID, "rain_breakup must be 0 (none), 1 (NSSL) or 2 (Morrison)");
   int rad[8];
   if (fft_plan_factors(g->nx, rad) < 0 || fft_plan_factors(g->ny, rad) < 0) return fail(ctx, SG_ERR_UNSUPPORTED, "nx or ny has more than 8 prime factors");
   if (!(g->dx > 0 && g->dy > 0 && g->height > 0) || !g->zs || !g->dzs || !g->hz) return fail(ctx, SG_ERR_INVALID, "bad grid spacing or levels");
@@ -345,14 +349,15 @@ void transport_items(sg_context* ctx, const std::vector<int>& slots, int TX, int
   }
 }
 
-// The charge carriers of the electrified runs, one WENO field an item (groups 13-16), on the plan's tile.
+// The extra fields of the plan's runs, one WENO field an item on the plan's tile: the charge carriers of the
+// electrified runs (groups 13-16), the raindrop number of the two-moment ones (group 17).
 void charge_items(sg_context* ctx, const std::vector<int>& slots, int TX, int TY, std::vector<int4>& out) {
   out.clear();
   for (int s : slots) {
     const Run& r = ctx->runs[s];
-    if (!(r.desc.flags & RF_ELEC)) continue;
     const int tiles = ((r.nx + TX - 1) / TX) * ((r.ny + TY - 1) / TY);
-    for (int g = 13; g < 17; g++) for (int t = 0; t < tiles; t++) out.push_back(make_int4(s, g, t, 0));
+    if (r.desc.flags & RF_ELEC) for (int g = 13; g < 17; g++) for (int t = 0; t < tiles; t++) out.push_back(make_int4(s, g, t, 0));
+    if (r.desc.flags & RF_RAIN2M) for (int t = 0; t < tiles; t++) out.push_back(make_int4(s, 17, t, 0));
   }
 }
 
@@ -403,6 +408,8 @@ int build_plan(sg_context* ctx, const std::vector<int>& slots, Plan& P) {
     if (r.desc.flags & RF_REFINE) P.refine = true; else P.unrefined = true;
     if (r.desc.flags & RF_ROTATION) P.rotation = true;
     if (r.desc.flags & RF_ELEC) P.elec = true;
+    if (r.desc.flags & RF_EXTRA) P.extra = true;
+    if (r.desc.flags & RF_RAIN2M) P.rain2m = true;
   }
   // mixing items: (run, tile, z0, z1), the column in four level ranges
   P.mixTX = all40 ? 40 : 32; P.mixTY = 8;
@@ -584,6 +591,7 @@ void enqueue_part(sg_context* ctx, const Plan& P, int part, Hook hook) {
   if (part == 1) {
     launch_fall_courant(node); hook(0);
     launch_sediment(cols, P.maxnz); hook(1);
+    if (P.rain2m) launch_sediment_2m(cols, P.maxnz);
   } else if (part == 2) {
     enqueue_solve(ctx, P, PROJ_FACE, A, st, hook);
     launch_face_correct(node, A); hook(5);
@@ -595,7 +603,7 @@ void enqueue_part(sg_context* ctx, const Plan& P, int part, Hook hook) {
   } else if (part == 3) {
     launch_fill_partial(node, B); hook(11);
     launch_fill_final(runs); hook(12);
-    launch_physics(node, B, C, P.elec); hook(13);
+    launch_physics(node, B, C, P.extra); hook(13);
   } else if (part == 4) {
     launch_viscosity(node, C); hook(14);
     Launch mx = lx(ctx, P, FAM_MIX);
@@ -631,6 +639,7 @@ void enqueue_dynamics_graph(sg_context* ctx, const Plan& P) {
   cudaStreamWaitEvent(side, ev[0], 0);
   launch_fall_courant(nodeS);
   launch_sediment(colsS, P.maxnz);
+  if (P.rain2m) launch_sediment_2m(colsS, P.maxnz);
   cudaEventRecord(ev[6], side);  // the sedimented precipitation (the dynamics' stage-0 buoyancy loads it)
   enqueue_solve(ctx, P, PROJ_FACE, A, main, none);
   launch_face_correct(node, A);
@@ -859,7 +868,11 @@ int sg_context_fail(sg_context* ctx, int code, const char* message) { return fai
 extern "C" {
 
 uint64_t sg_run_bytes(const sg_grid* grid) { return grid ? layout(grid->nx, grid->ny, grid->nz).total : 0; }
-uint64_t sg_run_bytes_electrified(const sg_grid* grid) { return grid ? layout(grid->nx, grid->ny, grid->nz, true).total : 0; }
+uint64_t sg_run_bytes_for(const sg_grid* grid, const sg_switches* sw) {
+  if (!grid || !sw) return 0;
+  const int flags = (sw->lightning && sw->ice ? RF_ELEC : 0) | (sw->rain_moments == 2 ? RF_RAIN2M : 0);
+  return layout(grid->nx, grid->ny, grid->nz, flags).total;
+}
 
 int sg_run_create(sg_context* ctx, const sg_grid* g, const sg_base_state* b, const sg_switches* sw, const float* const* init, sg_run* out) {
   if (!ctx || !out) return SG_ERR_INVALID;
@@ -867,7 +880,8 @@ int sg_run_create(sg_context* ctx, const sg_grid* g, const sg_base_state* b, con
   if (st) return st;
   cudaSetDevice(ctx->device);
   const bool elec = sw->lightning && sw->ice;  // electrified() (src/core/model.ts:1316)
-  Layout Lo = layout(g->nx, g->ny, g->nz, elec);
+  const bool two = sw->rain_moments == 2;      // rain2m() (:905)
+  Layout Lo = layout(g->nx, g->ny, g->nz, (elec ? RF_ELEC : 0) | (two ? RF_RAIN2M : 0));
   // Admission by the HBM budget (pooled allocations of a retired run count as free).
   char* mem = nullptr;
   auto pit = ctx->pool.find(Lo.total);
@@ -893,8 +907,10 @@ int sg_run_create(sg_context* ctx, const sg_grid* g, const sg_base_state* b, con
   HostTables T; RunDesc& d = r.desc; d = RunDesc{};
   build_tables(g, b, sw, T, d);
   d.slot = slot;
-  d.nf = elec ? NFE : NF;
+  d.nf = elec || two ? NFE : NF;
   if (elec) d.flags |= RF_ELEC;
+  if (two) d.flags |= RF_RAIN2M;
+  d.breakup = sw->rain_breakup;
   d.fld = (float*)(mem + Lo.fld); d.faces = (float*)(mem + Lo.faces); d.kmkh = (float*)(mem + Lo.kmkh); d.phi = (float*)(mem + Lo.phi);
   d.pres = (float*)(mem + Lo.pres); d.pres2 = (float*)(mem + Lo.pres2); d.spec = (float2*)(mem + Lo.spec); d.cols = (float*)(mem + Lo.cols);
   d.lv = (const float*)(mem + Lo.lv); d.lv64 = (const double*)(mem + Lo.lv64); d.tri_face = (const TriAB*)(mem + Lo.triF);
@@ -903,8 +919,8 @@ int sg_run_create(sg_context* ctx, const sg_grid* g, const sg_base_state* b, con
   d.cnt = (unsigned long long*)(mem + Lo.cnt);
   d.diag = (float*)(mem + Lo.diag); d.rot = (double*)(mem + Lo.rot);
   r.lgt.reset();
+  if (elec || two) { d.vfall = (float*)(mem + Lo.vfall); d.ez = (float*)(mem + Lo.ez); d.cpart = (double*)(mem + Lo.cpart); }
   if (elec) {
-    d.vfall = (float*)(mem + Lo.vfall); d.ez = (float*)(mem + Lo.ez); d.cpart = (double*)(mem + Lo.cpart);
     r.lgt = std::make_unique<LgtHost>();
     lightning_bind(mem + Lo.lgt, g->nx, g->ny, g->nz, r.lgt->dev);
     r.lgt->seed = (uint32_t)sw->lightning_seed; r.lgt->corona = sw->corona != 0;
@@ -949,7 +965,8 @@ int sg_run_write_fields(sg_context* ctx, sg_run run, uint32_t mask, const float*
   cudaSetDevice(ctx->device);
   size_t n = (size_t)r->nx * r->ny * r->nz;
   const int nf = r->desc.nf;
-  if (mask >> nf) return fail(ctx, SG_ERR_INVALID, "field mask beyond the run's fields (the charges need an electrified run)");
+  if ((mask >> nf) || ((mask & SG_CHARGE_FIELDS) && !(r->desc.flags & RF_ELEC)) || ((mask & (1u << SG_RAIN_NUMBER)) && !(r->desc.flags & RF_RAIN2M)))
+    return fail(ctx, SG_ERR_INVALID, "field mask beyond the run's fields (the charges need an electrified run, the drop number two-moment rain)");
   for (int f = 0; f < nf; f++) {
     if (!(mask & (1u << f))) continue;
     if (!host[f]) return fail(ctx, SG_ERR_INVALID, "null field pointer");
@@ -969,7 +986,8 @@ int sg_run_read_fields(sg_context* ctx, sg_run run, uint32_t mask, float* const*
   cudaSetDevice(ctx->device);
   size_t n = (size_t)r->nx * r->ny * r->nz;
   const int nf = r->desc.nf;
-  if (mask >> nf) return fail(ctx, SG_ERR_INVALID, "field mask beyond the run's fields (the charges need an electrified run)");
+  if ((mask >> nf) || ((mask & SG_CHARGE_FIELDS) && !(r->desc.flags & RF_ELEC)) || ((mask & (1u << SG_RAIN_NUMBER)) && !(r->desc.flags & RF_RAIN2M)))
+    return fail(ctx, SG_ERR_INVALID, "field mask beyond the run's fields (the charges need an electrified run, the drop number two-moment rain)");
   if (mask & (1u << THETA)) launch_theta_out(node_launch(ctx, *r), field(r->desc, 1, THETA));
   for (int f = 0; f < nf; f++) {
     if (!(mask & (1u << f))) continue;
@@ -1204,11 +1222,13 @@ int sg_run_save_state(sg_context* ctx, sg_run run, const char* config_json, doub
   const size_t n = (size_t)r->nx * r->ny * r->nz, layer = (size_t)r->nx * r->ny, off = state::data_offset(json.size());
   std::vector<float> fields((size_t)SG_NFIELDS * n), cols(3 * layer);
   if ((st = sg_batch_read_packed(ctx, &run, 1, SG_ALL_FIELDS, fields.data())) != SG_OK) return st;
-  std::vector<float> charges(r->lgt ? 4 * n : 0, 0.f);  // an electrified run's charge carriers
-  if (r->lgt) {
-    float* ptr[SG_NFIELDS_ELECTRIFIED] = {};
-    for (int k = 0; k < 4; k++) ptr[SG_CHARGE_ICE + k] = charges.data() + (size_t)k * n;
-    if ((st = sg_run_read_fields(ctx, run, SG_CHARGE_FIELDS, ptr)) != SG_OK) return st;
+  // the extra fields the run carries (an electrified run's charges, a two-moment run's drop number)
+  std::vector<float> extra(5 * n, 0.f);
+  const uint32_t xmask = (r->lgt ? SG_CHARGE_FIELDS : 0u) | ((r->desc.flags & RF_RAIN2M) ? 1u << SG_RAIN_NUMBER : 0u);
+  if (xmask) {
+    float* ptr[SG_NFIELDS_EXTRA] = {};
+    for (int k = 0; k < 5; k++) ptr[SG_CHARGE_ICE + k] = extra.data() + (size_t)k * n;
+    if ((st = sg_run_read_fields(ctx, run, xmask, ptr)) != SG_OK) return st;
   }
   if ((st = sg_run_read_columns(ctx, run, cols.data(), cols.data() + layer, cols.data() + 2 * layer)) != SG_OK) return st;
   std::memset(out, 0, off);
@@ -1220,7 +1240,7 @@ int sg_run_save_state(sg_context* ctx, sg_run run, const char* config_json, doub
   for (int k = 0; k < state::NSTATE; k++) {
     uint8_t* dst = out + off + (size_t)k * n * 4;
     const int f = state::carried_of(k);
-    if (f >= SG_CHARGE_ICE && r->lgt) std::memcpy(dst, charges.data() + (size_t)(f - SG_CHARGE_ICE) * n, n * 4);
+    if (f >= SG_CHARGE_ICE) std::memcpy(dst, extra.data() + (size_t)(f - SG_CHARGE_ICE) * n, n * 4);
     else if (f >= 0 && f < SG_NFIELDS) std::memcpy(dst, fields.data() + (size_t)f * n, n * 4);
     else std::memset(dst, 0, n * 4);
   }
@@ -1241,21 +1261,28 @@ int sg_run_load_state(sg_context* ctx, sg_run run, const uint8_t* image, size_t 
     return fail(ctx, SG_ERR_INVALID, "the file's grid is " + std::to_string(h.nx) + "x" + std::to_string(h.ny) + "x" + std::to_string(h.nz) +
                                          ", the run's " + std::to_string(r->nx) + "x" + std::to_string(r->ny) + "x" + std::to_string(r->nz));
   const size_t n = (size_t)r->nx * r->ny * r->nz, layer = (size_t)r->nx * r->ny;
-  std::vector<float> fields((size_t)SG_NFIELDS * n, 0.f), cols(3 * layer), charges(4 * n, 0.f);
+  std::vector<float> fields((size_t)SG_NFIELDS * n, 0.f), cols(3 * layer), extra(5 * n, 0.f);
   for (int k = 0; k < h.nfields; k++) {
     const int f = state::carried_of(k);
     if (f >= 0 && f < SG_NFIELDS) std::memcpy(fields.data() + (size_t)f * n, image + h.data_offset + (size_t)k * n * 4, n * 4);
-    else if (f >= SG_CHARGE_ICE) std::memcpy(charges.data() + (size_t)(f - SG_CHARGE_ICE) * n, image + h.data_offset + (size_t)k * n * 4, n * 4);
+    else if (f >= SG_CHARGE_ICE) std::memcpy(extra.data() + (size_t)(f - SG_CHARGE_ICE) * n, image + h.data_offset + (size_t)k * n * 4, n * 4);
   }
   std::memcpy(cols.data(), image + h.data_offset + (size_t)h.nfields * n * 4, 3 * layer * 4);
   int st = sg_batch_write_packed(ctx, &run, 1, SG_ALL_FIELDS, fields.data());
   if (st != SG_OK) return st;
   if ((st = sg_run_write_columns(ctx, run, cols.data(), cols.data() + layer, cols.data() + 2 * layer)) != SG_OK) return st;
+  if (r->desc.flags & RF_RAIN2M) {
+    // a two-moment run: the file's drop number (none before version 4; the first step rebuilds it from the rain, as
+    // the reference's boundedNumber does for rain without a number, state.ts:13)
+    const float* ptr[SG_NFIELDS_EXTRA] = {};
+    ptr[SG_RAIN_NUMBER] = extra.data() + (size_t)(SG_RAIN_NUMBER - SG_CHARGE_ICE) * n;
+    if ((st = sg_run_write_fields(ctx, run, 1u << SG_RAIN_NUMBER, ptr)) != SG_OK) return st;
+  }
   if (r->lgt) {
     // an electrified run: the file's charge (none in a version-1 file), its ground charge, flash counts and charge budget
     // (state.ts:78-81); the flashes after the file's time forgotten (:82), the vertical field as a new model's (zero)
-    const float* ptr[SG_NFIELDS_ELECTRIFIED] = {};
-    for (int k = 0; k < 4; k++) ptr[SG_CHARGE_ICE + k] = charges.data() + (size_t)k * n;
+    const float* ptr[SG_NFIELDS_EXTRA] = {};
+    for (int k = 0; k < 4; k++) ptr[SG_CHARGE_ICE + k] = extra.data() + (size_t)k * n;
     if ((st = sg_run_write_fields(ctx, run, SG_CHARGE_FIELDS, ptr)) != SG_OK) return st;
     const double acc[9] = {h.charge[0], h.charge[3], h.charge[4], h.charge[5], h.charge[6], h.charge[7], h.charge[8], h.charge[1], h.charge[2]};
     static_assert(A_CHG_SEPARATED == A_CHG_GROUND + 1 && A_FLASH_CG == A_CHG_GROUND + 8, "the charge budget's slots in order");

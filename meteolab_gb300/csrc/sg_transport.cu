@@ -26,12 +26,14 @@ constexpr int TMAXC = 4;  // plane cells per thread: (TX + 6)(TY + 6) <= TMAXC *
 // face values, thb, qb, thv_env (dynamics).
 constexpr int tlv_rows(int kind) { return kind == TK_DYN ? 9 : 2; }
 // Field groups of the transport work items: 0-2 the WENO fields in threes, 3 the dynamics {u, v, w, theta'}, 4-12
-// the WENO fields one by one, 13-16 the charge carriers of an electrified run one by one.
-constexpr int TGROUPS = 17;
+// the WENO fields one by one, 13-16 the charge carriers of an electrified run and 17 the raindrop number of a
+// two-moment run, one by one.
+constexpr int TGROUPS = 18;
 __constant__ int TGROUP[TGROUPS][4] = {{RAIN, SNOW, GRAUPEL, -1}, {HAIL, Q, CLOUD, -1}, {ICE, ICENUM, COLD, -1}, {U, V, W, THETA},
                                        {RAIN, -1, -1, -1}, {SNOW, -1, -1, -1}, {GRAUPEL, -1, -1, -1}, {HAIL, -1, -1, -1},
                                        {Q, -1, -1, -1}, {CLOUD, -1, -1, -1}, {ICE, -1, -1, -1}, {ICENUM, -1, -1, -1}, {COLD, -1, -1, -1},
-                                       {CHARGE_ICE, -1, -1, -1}, {CHARGE_GRAUPEL, -1, -1, -1}, {CHARGE_RAIN, -1, -1, -1}, {CHARGE_AIR, -1, -1, -1}};
+                                       {CHARGE_ICE, -1, -1, -1}, {CHARGE_GRAUPEL, -1, -1, -1}, {CHARGE_RAIN, -1, -1, -1}, {CHARGE_AIR, -1, -1, -1},
+                                       {RAIN_NUMBER, -1, -1, -1}};
 
 // Two faces at once on the packed FP32 pipes (bit-identical per face to the scalar weno5 / upwind5).
 struct Op2 {
@@ -89,10 +91,10 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
   float* const fld = Rg.fld;
   int fo[G];
 #pragma unroll
-  // a charge carrier's sets follow the base fields' three, four fields a set: its offsets are shifted by `so` so the
-  // same set arithmetic addresses it
-  const bool chg = G == 1 && group >= 13;  // (charge carriers come one field an item)
-  const int so = chg ? (3 * NF - NF) * (int)n : 0, ss = chg ? (NFE - NF) * (int)n : NF * (int)n;
+  // an extra field's sets follow the base fields' three, NXE fields a set: its offsets are shifted by `so` so the same
+  // set arithmetic addresses it
+  const bool chg = G == 1 && group >= 13;  // (the extra fields come one an item)
+  const int so = chg ? (3 * NF - NF) * (int)n : 0, ss = chg ? NXE * (int)n : NF * (int)n;
   for (int g = 0; g < G; g++) fo[g] = TGROUP[group][g] * (int)n + so;
   const int qo = in_set * ss, oo = out_set * ss;
 #define QP(g) (fld + qo + fo[g])
@@ -352,10 +354,10 @@ __device__ __forceinline__ void transport_item_bulk(const RunDesc& Rg, int group
   float* const fld = Rg.fld;
   int fo[G];
 #pragma unroll
-  // a charge carrier's sets follow the base fields' three, four fields a set: its offsets are shifted by `so` so the
-  // same set arithmetic addresses it
-  const bool chg = G == 1 && group >= 13;  // (charge carriers come one field an item)
-  const int so = chg ? (3 * NF - NF) * (int)n : 0, ss = chg ? (NFE - NF) * (int)n : NF * (int)n;
+  // an extra field's sets follow the base fields' three, NXE fields a set: its offsets are shifted by `so` so the same
+  // set arithmetic addresses it
+  const bool chg = G == 1 && group >= 13;  // (the extra fields come one an item)
+  const int so = chg ? (3 * NF - NF) * (int)n : 0, ss = chg ? NXE * (int)n : NF * (int)n;
   for (int g = 0; g < G; g++) fo[g] = TGROUP[group][g] * (int)n + so;
   const int qo = in_set * ss, oo = out_set * ss;
   constexpr bool AUX_S0 = KIND == TK_WENO;

@@ -45,7 +45,7 @@ class SgSwitches(C.Structure):
                                                                          "anisotropic", "vertical_dz", "durran_klemp",
                                                                          "pressure_in_stages", "ice", "refine_projection",
                                                                          "rotation", "lightning", "corona", "lightning_seed",
-                                                                         "reserved2")]
+                                                                         "rain_moments", "rain_breakup", "reserved2")]
 
 
 class SgChargeState(C.Structure):
@@ -81,7 +81,7 @@ class SgCounters(C.Structure):
 
 _lib = None
 _lock = threading.Lock()
-ALL_FIELDS = tuple(CARRIED) + tuple(CHARGES)   # field ids of the C ABI (charges: electrified runs)
+ALL_FIELDS = tuple(CARRIED) + tuple(CHARGES) + ("rainNumber",)  # field ids of the C ABI (charges: electrified runs; drop number: two-moment)
 _FP = C.POINTER(C.c_float)
 
 
@@ -150,8 +150,8 @@ def load():
             L.sg_run_read_swaths.argtypes = [vp, C.c_int32, _FP, _FP]
             L.sg_run_reset_swaths.argtypes = [vp, C.c_int32]
             L.sg_run_diagnostics.argtypes = [vp, C.c_int32, C.POINTER(SgDiagnostics)]
-            L.sg_run_bytes_electrified.restype = u64
-            L.sg_run_bytes_electrified.argtypes = [C.POINTER(SgGrid)]
+            L.sg_run_bytes_for.restype = u64
+            L.sg_run_bytes_for.argtypes = [C.POINTER(SgGrid), C.POINTER(SgSwitches)]
             L.sg_run_charge.argtypes = [vp, C.c_int32, C.POINTER(SgChargeState)]
             L.sg_run_flashes.argtypes = [vp, C.c_int32, C.POINTER(SgFlash), i32, C.POINTER(C.c_int)]
             L.sg_run_flash_channel.argtypes = [vp, C.c_int32, i32, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32), i32]
@@ -166,6 +166,15 @@ def _f64(a) -> np.ndarray:
     return np.ascontiguousarray(a, dtype=np.float64)
 
 
+def _switches(sw, g) -> "SgSwitches":
+    """The POD sg_switches of a ``scenarios.Switches`` on grid g."""
+    return SgSwitches(sw.dt, sw.coriolis, sw.wind_relaxation, sw.sponge_rate, sw.sponge_start, sw.cs, sw.drag_cd(g),
+                      sw.frame_u, sw.frame_v, sw.loading, sw.evaporation, sw.rain_formation, sw.anisotropic,
+                      sw.vertical_dz, sw.durran_klemp, sw.pressure_in_stages, getattr(sw, "ice", 1),
+                      sw.refine_projection, sw.rotation, getattr(sw, "lightning", 0), getattr(sw, "corona", 1),
+                      getattr(sw, "lightning_seed", 43), getattr(sw, "rain_moments", 1), getattr(sw, "rain_breakup", 0), 0)
+
+
 class _Packed:
     """The C structs of one run spec with the arrays they point to kept alive."""
 
@@ -175,22 +184,21 @@ class _Packed:
         dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
         self.grid = SgGrid(g.nx, g.ny, g.nz, 0, g.dx, g.dy, g.height, dp(self.keep[0]), dp(self.keep[1]), dp(self.keep[2]))
         self.base = SgBase(*[dp(a) for a in self.keep[3:]])
-        self.switches = SgSwitches(sw.dt, sw.coriolis, sw.wind_relaxation, sw.sponge_rate, sw.sponge_start, sw.cs, sw.drag_cd(g),
-                                   sw.frame_u, sw.frame_v, sw.loading, sw.evaporation, sw.rain_formation, sw.anisotropic,
-                                   sw.vertical_dz, sw.durran_klemp, sw.pressure_in_stages, getattr(sw, "ice", 1),
-                                   sw.refine_projection, sw.rotation, getattr(sw, "lightning", 0), getattr(sw, "corona", 1),
-                                   getattr(sw, "lightning_seed", 43), 0)
+        self.switches = _switches(sw, g)
         self.fields = [np.ascontiguousarray(spec.fields[k], dtype=np.float32).ravel() for k in CARRIED]
         self.ptrs = (_FP * len(CARRIED))(*[a.ctypes.data_as(_FP) for a in self.fields])
 
 
-def run_bytes(grid, electrified: bool = False) -> int:
-    """Bytes of HBM one run of this grid takes in a context (sg_run_bytes; sg_run_bytes_electrified with its charge
-    carriers and lightning buffers): what admission by budget counts."""
+def run_bytes(grid, switches=None) -> int:
+    """Bytes of HBM one run of this grid takes in a context (sg_run_bytes; with `switches`, sg_run_bytes_for: an
+    electrified or two-moment run's extra fields and buffers): what admission by budget counts."""
     zs, dzs, hz = _f64(grid.zs), _f64(grid.dzs), _f64(grid.hz)
     dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
     g = SgGrid(grid.nx, grid.ny, grid.nz, 0, grid.dx, grid.dy, grid.height, dp(zs), dp(dzs), dp(hz))
-    return int((load().sg_run_bytes_electrified if electrified else load().sg_run_bytes)(C.byref(g)))
+    if switches is None:
+        return int(load().sg_run_bytes(C.byref(g)))
+    sw = _switches(switches, grid)
+    return int(load().sg_run_bytes_for(C.byref(g), C.byref(sw)))
 
 
 class Context:
@@ -357,9 +365,9 @@ class Run:
         self.id = rid.value
         self.time = 0.0
         self.live = True
-        charges = {k: v for k, v in spec.fields.items() if k in CHARGES}
-        if charges:
-            self.write(charges)
+        extra = {k: v for k, v in spec.fields.items() if k in CHARGES or k == "rainNumber"}
+        if extra:
+            self.write(extra)
 
     def retire(self):
         if self.live:

@@ -10,10 +10,23 @@
 #include "../../meteolab_gb300/csrc/sg_physics.cuh"
 #include "../../meteolab_gb300/csrc/sg_tile_copies.cuh"
 #include "../../meteolab_gb300/csrc/sg_charge.cuh"
+#include "../../meteolab_gb300/csrc/sg_rain2m.cuh"
 
 using namespace sg;
 
 extern "C" {
+
+// two-moment rain of the physics kernel (sg_rain2m.cuh), FP32: v = [q, cloud, rain, number] in place at temperature
+// tk (K), pressure p, density rho; returns the evaporated rain
+float ht_r2m_processes(float* v, double tk, double p, double rho, float dt, int breakup, int evaporate) {
+  phys::Level L = phys::makeLevel(tk, 1.0, p, rho, rho);
+  phys::Node s{0.f, (float)tk, L.tcb, v[0], v[1], v[2], 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  float number = v[3];
+  const float evap = r2m::processes(s, number, L, dt, breakup, evaporate != 0);
+  v[0] = s.q; v[1] = s.cloud; v[2] = s.rain; v[3] = number;
+  return evap;
+}
+void ht_r2m_fall(float q, float n, float rho, float* out) { r2m::fallSpeeds(q, n, rho, out[0], out[1], out[2]); }
 
 // the charging of the physics kernel (sg_charge.cuh), FP32
 float ht_takahashi(float tc, float lwc) { return charge::takahashi(tc, lwc); }

@@ -280,3 +280,37 @@ def test_charge_transfer_matches_oracle_and_conserves(ht):
         scale = float(np.max(np.abs(c))) + 1e-30
         assert np.max(np.abs(got.astype(np.float64) - ref)) <= 1e-5 * scale
         assert abs(float(np.sum(got.astype(np.float64))) - float(np.sum(c.astype(np.float64)))) <= 1e-5 * scale
+
+
+# ------------------------------------------------------------------ two-moment rain (sg_rain2m.cuh)
+def test_two_moment_rain_matches_oracle(ht):
+    """The device's FP32 two-moment rain processes and fall speeds against the oracle's FP64 (rain2m.ts), over warm
+    and cool, saturated and dry cells with and without cloud, for each breakup option."""
+    ht.ht_r2m_processes.restype = C.c_float
+    ht.ht_r2m_processes.argtypes = [C.POINTER(C.c_float), C.c_double, C.c_double, C.c_double, C.c_float, C.c_int, C.c_int]
+    ht.ht_r2m_fall.argtypes = [C.c_float, C.c_float, C.c_float, C.POINTER(C.c_float)]
+    rng = np.random.default_rng(21)
+    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+    for k in range(400):
+        tk = float(rng.uniform(255, 300))
+        p = float(rng.uniform(5e4, 1e5))
+        rho = p / (287 * tk)
+        qs = O.lib().orc_qsat(tk - 273.15, p)
+        q = qs * float(rng.uniform(.5, 1.02))
+        cloud = float(rng.choice([0.0, 10 ** rng.uniform(-5, -2.3)]))
+        rain = float(rng.choice([0.0, 10 ** rng.uniform(-7, -2.5)]))
+        number = float(O.r2m_bounded(rain, 10 ** rng.uniform(2, 6), rho)) if rain > 0 else 0.0
+        b = ("none", "nssl", "morrison")[k % 3]
+        ref = np.array([q, cloud, rain, number], np.float32)
+        got = ref.copy()
+        e_ref = O.r2m_processes(ref, tk, p, rho, 3.0, b)
+        e_got = ht.ht_r2m_processes(fp(got), tk, p, rho, 3.0, O.BREAKUP[b], 1)
+        for j, name in enumerate(("q", "cloud", "rain", "number")):
+            tol = 2e-4 * abs(float(ref[j])) + (1e-12 if j < 3 else 1e-3)
+            assert abs(float(got[j]) - float(ref[j])) <= tol, (k, name, float(got[j]), float(ref[j]), tk, p, cloud, rain)
+        assert abs(e_got - e_ref) <= 2e-4 * abs(e_ref) + 1e-13
+        if rain > 0:
+            out = np.empty(3, np.float32)
+            ht.ht_r2m_fall(np.float32(rain), np.float32(number), np.float32(rho), fp(out))
+            vm, vn, vz = O.r2m_fall(float(np.float32(rain)), float(np.float32(number)), float(np.float32(rho)))
+            assert abs(out[0] - vm) <= 1e-5 * vm + 1e-6 and abs(out[1] - vn) <= 1e-5 * vn + 1e-6 and abs(out[2] - vz) <= 1e-5 * vz + 1e-6
