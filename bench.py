@@ -284,6 +284,34 @@ def electrified_leg(ctx, members, runs, steps: int, build: int = 200, cpu_steps:
                              "sample": f"the same {min(threads, k)} electrified member states, {cpu_steps} steps, oracle with lightning on"}}
 
 
+def two_moment_leg(ctx, members, runs, steps: int, cpu_steps: int = 10):
+    """Two-moment rain: the ensemble's members as the timed steps left them, their drop number started as the
+    reference starts rain without one (Marshall-Palmer's), `steps` timed graph steps of the whole batch beside its
+    one-moment steps; CPU: the oracle with two-moment rain from the same states, pool strategy."""
+    import dataclasses
+    import numpy as np
+    from meteolab_gb300.scenarios import RunSpec, marshall_palmer_number
+    specs = []
+    for m, r in zip(members, runs):
+        f = r.read()
+        f["rainNumber"] = marshall_palmer_number(f["rain"], np.repeat(np.asarray(m.env.rho), m.grid.layer))
+        specs.append(RunSpec(m.grid, m.env, dataclasses.replace(m.switches, rain_moments=2), f, m.seed, m.label))
+    tr = [ctx.create(s) for s in specs]
+    ctx.time_steps(tr, 5)
+    ms = ctx.time_steps(tr, steps)
+    cells = sum(s.grid.n for s in specs)
+    states = [RunSpec(s.grid, s.env, s.switches, r.read(list(s.fields)), s.seed, s.label) for s, r in zip(specs, tr)]
+    for r in tr:
+        r.retire()
+    threads = os.cpu_count() or 1
+    cpu = cpu_strategies(states[:threads], cpu_steps, threads)
+    best = max(cpu, key=lambda key: cpu[key][0])
+    return {"members": len(specs), "grid": "40x32x50", "timed_steps": steps, "ms_per_step": ms / steps,
+            "cell_steps_s": cells * steps / (ms * 1e-3),
+            "cpu_baseline": {"value": cpu[best][0], "unit": "cell-steps/s", "cores": threads, "kind": "port", "strategy": best,
+                             "sample": f"{min(threads, len(states))} of the members, {cpu_steps} steps, oracle with two-moment rain"}}
+
+
 def reference_arm(args, rank, pg):
     """--impl reference: the reference's algorithm on the host cores (the oracle port; no GPU, none of this package's
     device code) on a bounded sample of the workload: the first `threads` members of the same seeded 64-member ensemble,
@@ -517,6 +545,7 @@ def main():
 
     uneven = uneven_leg(ctx, max(5, args.steps // 2), args.spinup)
     electrified = electrified_leg(ctx, members, runs, max(10, args.steps // 4)) if rank == 0 else None
+    two_moment = two_moment_leg(ctx, members, runs, max(10, args.steps // 4)) if rank == 0 else None
     serving = None if args.quick else serving_leg(ctx, rate=4.0, count=32, quantum=10)
     # the serving configuration's range of arrival rates (0.5 to 8 runs/s), each with about 8-12 s of arrivals
     serving_rates = None if args.quick else [serving_leg(ctx, rate=r, count=c, quantum=10) for r, c in ((0.5, 6), (2.0, 16), (8.0, 64))]
@@ -557,6 +586,7 @@ def main():
         "uneven_batch": uneven,
         "electric_solve": {"grid": "40x32x50", "ms_per_solve": electric_ms, "host_io_bytes": 2 * grid.n * 8},
         "electrified": electrified,
+        "two_moment": two_moment,
         "serving": serving,
         "serving_rates": serving_rates,
         "kernels_ms_per_launch": {k: round(v[0], 5) for k, v in prof.items()},

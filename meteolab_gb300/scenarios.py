@@ -279,3 +279,18 @@ def serving_requests(small: Grid, large: Grid, count: int, rate: float, seed: in
         spec = ensemble_members(grid, 1, seed=seed * 100 + k)[0]
         out.append((t, spec, int(rng.integers(400, 1201))))
     return out
+
+
+def marshall_palmer_number(rain: np.ndarray, rho: np.ndarray) -> np.ndarray:
+    """Raindrops per kg for rain (kg/kg) without a drop number, as two-moment rain starts it (boundedNumber with no
+    number, src/core/rain2m.ts:47-51): Marshall-Palmer's N0 / lambda, the mean drop kept between 80 um and a 6 mm
+    mass-weighted diameter. `rho` is each node's air density."""
+    q = np.asarray(rain, np.float64)
+    rho = np.asarray(rho, np.float64)
+    out = np.zeros_like(q)
+    wet = q > 1e-12
+    lam = (math.pi * 1000.0 * 8e6 / (rho[wet] * q[wet])) ** .25
+    n = 8e6 / lam / rho[wet]
+    xv = np.clip(q[wet] / (1000.0 * n), math.pi / 6 * 80e-6 ** 3, math.pi / 6 * 6e-3 ** 3 / (64 / 6))
+    out[wet] = q[wet] / (1000.0 * xv)
+    return out.astype(np.float32)

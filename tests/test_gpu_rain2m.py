@@ -18,7 +18,7 @@ import pytest
 import pyoracle as O
 from parity import FLOOR, developed_state, rel_l2
 from meteolab_gb300.grid import DEFAULT_GRID, create_grid
-from meteolab_gb300.scenarios import CARRIED, CHARGES, RunSpec, baseline_run
+from meteolab_gb300.scenarios import CARRIED, CHARGES, RunSpec, baseline_run, marshall_palmer_number
 
 pytestmark = pytest.mark.gpu
 DT = 3.0
@@ -40,8 +40,7 @@ def ctx():
 def storm2m():
     base = developed_state(baseline_run(GRID, seed=42), 300)
     f = dict(base.fields)
-    rho = np.repeat(np.asarray(base.env.rho), GRID.layer)
-    f["rainNumber"] = np.array([O.r2m_bounded(float(q), 0.0, float(r)) for q, r in zip(f["rain"], rho)], np.float32)
+    f["rainNumber"] = marshall_palmer_number(f["rain"], np.repeat(np.asarray(base.env.rho), GRID.layer))
     sw = dataclasses.replace(base.switches, rain_moments=2)
     return RunSpec(GRID, base.env, sw, f, base.seed, "storm2m")
 
@@ -77,7 +76,8 @@ def test_twenty_steps_match_the_oracle(ctx, storm2m):
 
 
 def test_rain_shaft_in_the_model(ctx):
-    """rain2m.test.ts:66-78: a 2 g/kg shaft from 2 to 4 km over a few columns; rain at the ground, the number in bounds."""
+    """rain2m.test.ts:66-78: a 2 g/kg shaft from 2 to 4 km over a few columns; rain at the ground, the number in bounds;
+    the rain at the ground and the fields against the oracle's (1e-4)."""
     base = baseline_run(GRID, seed=3, bubble=0.0)
     f = {k: v.copy() for k, v in base.fields.items()}
     f["rainNumber"] = np.zeros(GRID.n, np.float32)
@@ -87,9 +87,17 @@ def test_rain_shaft_in_the_model(ctx):
                 i = c + z * GRID.layer
                 f["rain"][i] = 2e-3
                 f["rainNumber"][i] = O.r2m_bounded(2e-3, 0, base.env.rho[z])
-    r = ctx.create(RunSpec(GRID, base.env, dataclasses.replace(base.switches, rain_moments=2), f, 3, "shaft"))
+    spec = RunSpec(GRID, base.env, dataclasses.replace(base.switches, rain_moments=2), f, 3, "shaft")
+    r = ctx.create(spec)
+    o = O.OracleModel(spec)
     r.step(200)
-    assert float(np.sum(r.columns()["precipitation"])) > 0
+    o.step(DT, 200)
+    prec = r.columns()["precipitation"]
+    assert float(np.sum(prec)) > 0
+    e = rel_l2(prec, o.get("precipitation"))
+    errs = {k: rel_l2(r.read([k])[k], o.get(k), FLOOR.get(k, 0.0)) for k in ("rain", "rainNumber", "q", "theta")}
+    print(f"\n2M shaft, 200 steps: precipitation {e:.2e}, " + ", ".join(f"{k} {v:.2e}" for k, v in errs.items()))
+    assert e < 1e-4 and all(v < 1e-4 for v in errs.values())
     got = r.read(["rain", "rainNumber"])
     xv_min, xv_max, _ = O.r2m_limits()
     assert (got["rainNumber"] >= 0).all()
