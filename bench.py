@@ -70,6 +70,8 @@ def parse():
     p.add_argument("--spinup", type=int, default=300, help="untimed steps before the warm-up (15 simulated minutes), so the "
                    "timed steps see a developed storm with cloud and precipitation rather than the quiescent start")
     p.add_argument("--quick", action="store_true", help="skip the serving and stress-grid legs")
+    p.add_argument("--moments", type=int, default=1, choices=[1, 2],
+                   help="with --ncu-window: the ensemble's rain one- or two-moment (the timed headline is one-moment)")
     p.add_argument("--ncu-window", action="store_true",
                    help="profiling driver: set up and spin up the ensemble, then run --steps eager steps between "
                         "cudaProfilerStart/Stop (for ncu --profile-from-start off) and exit without timing")
@@ -299,6 +301,7 @@ def two_moment_leg(ctx, members, runs, steps: int, cpu_steps: int = 10):
     tr = [ctx.create(s) for s in specs]
     ctx.time_steps(tr, 5)
     ms = ctx.time_steps(tr, steps)
+    prof = ctx.profile(tr, 2)
     cells = sum(s.grid.n for s in specs)
     states = [RunSpec(s.grid, s.env, s.switches, r.read(list(s.fields)), s.seed, s.label) for s, r in zip(specs, tr)]
     for r in tr:
@@ -308,6 +311,7 @@ def two_moment_leg(ctx, members, runs, steps: int, cpu_steps: int = 10):
     best = max(cpu, key=lambda key: cpu[key][0])
     return {"members": len(specs), "grid": "40x32x50", "timed_steps": steps, "ms_per_step": ms / steps,
             "cell_steps_s": cells * steps / (ms * 1e-3),
+            "kernels_ms_per_launch": {k: round(v[0], 5) for k, v in prof.items()},
             "cpu_baseline": {"value": cpu[best][0], "unit": "cell-steps/s", "cores": threads, "kind": "port", "strategy": best,
                              "sample": f"{min(threads, len(states))} of the members, {cpu_steps} steps, oracle with two-moment rain"}}
 
@@ -455,6 +459,17 @@ def main():
         ctx.time_steps(runs, args.spinup)
         ctx.set_transport_shape(0)  # tune the transport again, on the developed storms rather than the quiescent start
     if args.ncu_window:
+        if args.moments == 2:  # the same states with two-moment rain, the drop number started as Marshall-Palmer's
+            import dataclasses
+            from meteolab_gb300.scenarios import RunSpec, marshall_palmer_number
+            specs = []
+            for m, r in zip(members, runs):
+                f = r.read()
+                f["rainNumber"] = marshall_palmer_number(f["rain"], np.repeat(np.asarray(m.env.rho), m.grid.layer))
+                specs.append(RunSpec(m.grid, m.env, dataclasses.replace(m.switches, rain_moments=2), f, m.seed, m.label))
+            for r in runs:
+                r.retire()
+            runs = [ctx.create(s) for s in specs]
         ctx.time_steps(runs, 1, graph=False)  # plans and tuning outside the window
         torch.cuda.synchronize()
         torch.cuda.profiler.start()

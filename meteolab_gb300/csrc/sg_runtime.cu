@@ -458,8 +458,8 @@ void launch_transport_kinds(sg_context* ctx, const Plan& P, int in, int out, flo
     Launch L = lx(ctx, P, fams[k]);
     L.cap = L.n;
     if (L.n) launch_transport(L, k, P.wenoG, P.minb, in, out, frac, stage, P.TX, P.TY, P.bulk, ctx->edgeWarps);
-    if (k == 0) launch_charges(ctx, P, in, out, frac, stage, ctx->stream);
     hook(hookBase + k);
+    if (k == 0 && P.extra) { launch_charges(ctx, P, in, out, frac, stage, ctx->stream); hook(29); }
   }
 }
 
@@ -591,7 +591,7 @@ void enqueue_part(sg_context* ctx, const Plan& P, int part, Hook hook) {
   if (part == 1) {
     launch_fall_courant(node); hook(0);
     launch_sediment(cols, P.maxnz); hook(1);
-    if (P.rain2m) launch_sediment_2m(cols, P.maxnz);
+    if (P.rain2m) { launch_sediment_2m(cols, P.maxnz); hook(28); }
   } else if (part == 2) {
     enqueue_solve(ctx, P, PROJ_FACE, A, st, hook);
     launch_face_correct(node, A); hook(5);
@@ -673,12 +673,12 @@ void enqueue_step_graph(sg_context* ctx, const Plan& P) {
   enqueue_dynamics_graph(ctx, P);
   for (int part = 3; part <= 5; part++) enqueue_part(ctx, P, part, none);
 }
-const int NKERNELS = 28;
+const int NKERNELS = 30;
 const char* KERNEL_NAMES[NKERNELS] = {"fall_courant", "sediment", "face_div_xfft", "face_modes", "face_xifft", "face_correct", "transport",
                                       "pres_div_xfft", "pres_modes", "pres_xifft", "pres_correct", "fill_partial", "fill_final", "physics",
                                       "viscosity", "mix", "pres_correct_final", "step_end", "transport_weno", "transport_dynamics",
                                       "refine_residual", "refine_unused", "refine_div_xfft", "refine_modes", "refine_xifft", "refine_correct",
-                                      "rotation_columns", "rotation_summary"};
+                                      "rotation_columns", "rotation_summary", "sediment_2m", "transport_extra"};
 
 Plan* get_plan(sg_context* ctx, const std::vector<int>& slots, int* status) {
   auto it = ctx->plans.find(slots);
