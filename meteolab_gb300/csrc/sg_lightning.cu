@@ -92,7 +92,7 @@ __global__ void k_lgt_pick(const RunDesc R, const LgtDev L, int stamp) {
 // extend() (:389-404) by one warp: lane l takes the l-th candidate of the reference's loop (level k from z - 1 up,
 // then dj, then di); the candidates are distinct nodes, so each lane keeps its node's shorter link on its own, and the
 // new links go on the growth front in the reference's order (a ballot over the lanes). All 32 lanes call it.
-SG_D void extendWarp(const RunDesc& R, const LgtDev& L, int i, int c, int id) {
+SG_D void extendWarp(const RunDesc& R, const LgtDev& L, volatile LgtState& V, int i, int c, int id) {
   const int lane = threadIdx.x & 31;
   const int nx = R.nx, ny = R.ny, nz = R.nz, layer = R.layer, z = i / layer, y = (i - z * layer) / nx, x = i - z * layer - y * nx;
   const int k0 = max(0, z - 1), k1 = min(nz - 2, z + 1);
@@ -112,16 +112,15 @@ SG_D void extendWarp(const RunDesc& R, const LgtDev& L, int i, int c, int id) {
     }
   }
   const unsigned mask = __ballot_sync(0xffffffffu, fresh);
-  volatile LgtState& V = *L.st;
   const int size = V.size;
   if (fresh) L.frontier[size + __popc(mask & ((1u << lane) - 1))] = j;
   __syncwarp();
   if (lane == 0) V.size = size + __popc(mask);
   __syncwarp();
 }
-// add() of Lightning.flash (:294-304) by one warp (lane 0 the bookkeeping, all lanes the extension).
-SG_D void addNodeWarp(const RunDesc& R, const LgtDev& L, int j, int from, int id) {
-  volatile LgtState& V = *L.st;
+// add() of Lightning.flash (:294-304) by one warp (lane 0 the bookkeeping, all lanes the extension), on the block's
+// copy of the state record.
+SG_D void addNodeWarp(const RunDesc& R, const LgtDev& L, volatile LgtState& V, int j, int from, int id) {
   if ((threadIdx.x & 31) == 0) {
     const int nn = V.nnodes;
     L.mark[j] = id; L.nodes[nn] = j; L.parent[nn] = from; V.nnodes = nn + 1;
@@ -129,19 +128,34 @@ SG_D void addNodeWarp(const RunDesc& R, const LgtDev& L, int j, int from, int id
     else if (V.ground < 0) { const double sum = dadd(V.sum, L.phi[j]); V.sum = sum; V.potential = sum / (double)(nn + 1); }
   }
   __syncwarp();
-  if (j >= R.layer) extendWarp(R, L, j, V.nnodes - 1, id);
+  if (j >= R.layer) extendWarp(R, L, V, j, V.nnodes - 1, id);
+}
+
+// The state record in shared memory for a kernel's run (a copy in, its changes out): the channel's bookkeeping reads
+// and writes it every node, a round trip to L2 each time in global memory.
+static_assert(sizeof(LgtState) % 4 == 0, "the state record copies as words");
+SG_D void stateIn(LgtState& sh, const LgtDev& L, int t, int threads) {
+  for (int k = t; k < (int)(sizeof(LgtState) / 4); k += threads) reinterpret_cast<int*>(&sh)[k] = reinterpret_cast<const int*>(L.st)[k];
+}
+SG_D void stateOut(const LgtState& sh, const LgtDev& L, int t, int threads) {
+  for (int k = t; k < (int)(sizeof(LgtState) / 4); k += threads) reinterpret_cast<int*>(L.st)[k] = reinterpret_cast<const int*>(&sh)[k];
 }
 
 __global__ void k_lgt_flash_begin(const RunDesc R, const LgtDev L, int start, int id) {
-  if (blockIdx.x) return;
+  __shared__ LgtState sh;
+  if (blockIdx.x || threadIdx.x >= 32) return;
+  stateIn(sh, L, threadIdx.x, 32);
+  __syncwarp();
   if (threadIdx.x == 0) {
-    LgtState& S = *L.st;
+    LgtState& S = sh;
     S.size = 0; S.nnodes = 0; S.npol = 0; S.ground = -1; S.touched = 0; S.left = 0; S.event = 0; S.strokes = 0; S.nstrokes = 0;
     S.sum = 0; S.potential = 0; S.before = 0; S.moment = 0; S.lowered = 0; S.neutralized = 0; S.stage = 0; S.needPotential = 0;
     S.start = start; S.id = id;
   }
   __syncwarp();
-  if (threadIdx.x < 32) addNodeWarp(R, L, start, -1, id);
+  addNodeWarp(R, L, sh, start, -1, id);
+  __syncwarp();
+  stateOut(sh, L, threadIdx.x, 32);
 }
 
 // One stage's growth (:309-331): until no link exceeds the threshold, the channel leaves the cloud (the first time),
@@ -156,8 +170,11 @@ __global__ void __launch_bounds__(GROW_THREADS) k_lgt_grow(const RunDesc R, cons
   __shared__ double pick;
   __shared__ int pickN, stop, sJ, sFrom, sPrune;
   __shared__ unsigned char flag[PRUNE_FLAGS];
-  volatile LgtState& V = *L.st;
+  __shared__ LgtState sh;
+  volatile LgtState& V = sh;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5, layer = R.layer;
+  stateIn(sh, L, t, GROW_THREADS);
+  __syncthreads();
   if (t == 0) {
     V.grown = V.nnodes; V.event = 0;
     if (V.needPotential) {
@@ -239,12 +256,14 @@ __global__ void __launch_bounds__(GROW_THREADS) k_lgt_grow(const RunDesc R, cons
       __syncthreads();
     }
     if (warp == 0) {
-      addNodeWarp(R, L, sJ, sFrom, id);
+      addNodeWarp(R, L, sh, sJ, sFrom, id);
       if (lane == 0 && V.touched) { V.touched = 0; V.event = 1; stop = 1; }
     }
     __syncthreads();
     if (stop) break;
   }
+  __syncthreads();
+  stateOut(sh, L, t, GROW_THREADS);
 }
 
 // deposit() (:352-381) and neutralize() (:410-418) of one stage, one block: each channel node gets its capacitance

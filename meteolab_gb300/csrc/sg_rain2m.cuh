@@ -35,6 +35,9 @@ SG_HD void fallSpeeds(float q, float n, float rho, float& vm, float& vn, float& 
 // rain2mProcesses (:76-146) on the node; returns the evaporated rain (the caller cools the air).
 SG_HD float processes(phys::Node& s, float& number, const phys::Level& L, float dt, int breakup, bool evaporate) {
   const float rho = L.rho, tk = tcOf(s, L.exner) + T0, qc = s.cloud, qr = s.rain;
+  // neither cloud water nor rain: nothing forms, collects or evaporates; the reference's arithmetic leaves the rain as
+  // it is (negative tails to zero) and the number zero
+  if (!(qc > 1e-9f) && !(qr > RAIN_MIN)) { s.rain = fmaxf(0.f, qr); number = 0.f; return 0.f; }
   float nr = qr > RAIN_MIN ? boundedNumber(qr, number, rho) * rho : 0.f;
   float autoM = 0.f, autoN = 0.f, accretion = 0.f;
   const float nc = CLOUD_DROPLETS * rho / RHO_00;
