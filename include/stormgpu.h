@@ -103,7 +103,11 @@ typedef struct sg_switches {
    * and the number following the rain the ice processes take or give; 1: one-moment rain (the configured step). */
   int32_t rain_moments;
   int32_t rain_breakup;    /* two-moment rain's collisional breakup (rainBreakup, :843): 0 none, 1 NSSL's, 2 Morrison's */
-  int32_t reserved2;
+  /* 2: two-moment graupel and hail after NSSL (AtmosphereModel.iceMoments, :839-840; src/core/ice2m.ts), with the ice
+   * microphysics and two-moment rain only (ice2m(), :914; SimConfig.moments 2 sets both, :331): their number and
+   * particle volume carried, transported and falling with the mass (sedimentIce2m, :916-921), their processes instead
+   * of the one-moment graupel and hail ones, the charging by their own distributions; 1: one-moment graupel and hail. */
+  int32_t ice_moments;
 } sg_switches;
 
 /* The charge budget of an electrified run since it began (AtmosphereModel.chargeGround, .charge, .flashCount,

@@ -15,6 +15,8 @@
  *   retire(ctx, run), destroyContext(ctx)
  *   saveState(ctx, run, configJson: string, time, persisted) -> ArrayBuffer      (saveState, src/core/state.ts:43)
  *   loadState(ctx, run, image: ArrayBuffer) -> {version, time, persisted}        (readState + applyState, :55-83)
+ *   two-moment runs: switches.rainMoments 2 (and rainBreakup), switches.iceMoments 2 (with ice and two-moment rain); their
+ *   numbers and volumes through readCharges-like calls are not bound here: they travel in state files (saveState)
  *   electrified runs (switches.lightning, with ice; switches.corona, switches.lightningSeed = config.seed + 1):
  *   readCharges(ctx, run, charges: Float32Array[4]) / writeCharges(ctx, run, charges)   chargeIce, chargeGraupel,
  *                                                             chargeRain, chargeAir (src/core/model.ts:210)
@@ -45,6 +47,13 @@ static napi_value throw_status(napi_env env, sg_context* ctx, int st) {
 static double get_num(napi_env env, napi_value obj, const char* key) {
   napi_value v; double d = 0;
   if (napi_get_named_property(env, obj, key, &v) == napi_ok) napi_get_value_double(env, v, &d);
+  return d;
+}
+
+/* A number property, or `otherwise` where the object has none (an optional setting). */
+static double get_num_or(napi_env env, napi_value obj, const char* key, double otherwise) {
+  napi_value v; double d;
+  if (napi_get_named_property(env, obj, key, &v) != napi_ok || napi_get_value_double(env, v, &d) != napi_ok) return otherwise;
   return d;
 }
 
@@ -104,6 +113,10 @@ static napi_value create_run(napi_env env, napi_callback_info info) {
   s.rotation = (int32_t)get_num(env, argv[3], "rotation");
   s.lightning = (int32_t)get_num(env, argv[3], "lightning"); s.corona = (int32_t)get_num(env, argv[3], "corona");
   s.lightning_seed = (int32_t)get_num(env, argv[3], "lightningSeed");
+  /* the model's moments (AtmosphereModel.rainMoments / iceMoments, rainBreakup 0 none, 1 NSSL, 2 Morrison; 1, 1, 0 when
+   * not given) */
+  s.rain_moments = (int32_t)get_num_or(env, argv[3], "rainMoments", 1); s.ice_moments = (int32_t)get_num_or(env, argv[3], "iceMoments", 1);
+  s.rain_breakup = (int32_t)get_num_or(env, argv[3], "rainBreakup", 0);
   float* init[SG_NFIELDS];
   if (!fields_of(env, argv[4], init)) { napi_throw_type_error(env, NULL, "fields: 13 Float32Array"); return NULL; }
   sg_run run;

@@ -45,7 +45,7 @@ class SgSwitches(C.Structure):
                                                                          "anisotropic", "vertical_dz", "durran_klemp",
                                                                          "pressure_in_stages", "ice", "refine_projection",
                                                                          "rotation", "lightning", "corona", "lightning_seed",
-                                                                         "rain_moments", "rain_breakup", "reserved2")]
+                                                                         "rain_moments", "rain_breakup", "ice_moments")]
 
 
 class SgChargeState(C.Structure):
@@ -172,7 +172,8 @@ def _switches(sw, g) -> "SgSwitches":
                       sw.frame_u, sw.frame_v, sw.loading, sw.evaporation, sw.rain_formation, sw.anisotropic,
                       sw.vertical_dz, sw.durran_klemp, sw.pressure_in_stages, getattr(sw, "ice", 1),
                       sw.refine_projection, sw.rotation, getattr(sw, "lightning", 0), getattr(sw, "corona", 1),
-                      getattr(sw, "lightning_seed", 43), getattr(sw, "rain_moments", 1), getattr(sw, "rain_breakup", 0), 0)
+                      getattr(sw, "lightning_seed", 43), getattr(sw, "rain_moments", 1), getattr(sw, "rain_breakup", 0),
+                      getattr(sw, "ice_moments", 1))
 
 
 class _Packed:

@@ -87,6 +87,9 @@ class Switches:
     # its collisional breakup 0 none (the default), 1 NSSL's, 2 Morrison's (:843, src/core/rain2m.ts:23-31)
     rain_moments: int = 1
     rain_breakup: int = 0
+    # two-moment graupel and hail (AtmosphereModel.iceMoments 2, src/core/model.ts:839-840; with the ice microphysics and
+    # two-moment rain only, :914): their number and particle volume carried with their mass (src/core/ice2m.ts)
+    ice_moments: int = 1
 
     def drag_cd(self, grid: Grid) -> float:
         return drag_coefficient(self.surface, 2 * float(grid.hz[0])) if self.drag else 0.0

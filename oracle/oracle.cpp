@@ -49,6 +49,7 @@ template <class S> std::vector<S>* extraField(Model<S>* m, int id) {
     case 107: return &m->condensate;
     case 108: return &m->fallChargeIce; case 109: return &m->fallChargeGraupel; case 110: return &m->fieldZ;
     case 111: return &m->rainFallNumber;
+    case 112: return &m->graupelFallNumber; case 113: return &m->hailFallNumber;
   }
   return (id >= 0 && id < N_CARRIED) ? &m->f[id] : nullptr;
 }
@@ -71,9 +72,10 @@ void orc_set_threads(void* p, int threads) {
   if (h->m32) h->m32->nthreads = std::min(threads, (int)h->m32->dscr.size());
   if (h->m64) h->m64->nthreads = std::min(threads, (int)h->m64->dscr.size());
 }
-// Field ids: 0..16 carried (rain, snow, graupel, hail, u, v, w, theta, q, cloud, ice, iceNumber, cold, chargeIce,
-// chargeGraupel, chargeRain, chargeAir); 100 precipitation, 101 hailGround, 102 hailSize, 103-106 fall speeds,
-// 107 condensate, 108-109 the charge carriers' fall speeds, 110 the vertical field (fieldZ).
+// Field ids: 0..21 carried (rain, snow, graupel, hail, u, v, w, theta, q, cloud, ice, iceNumber, cold, chargeIce,
+// chargeGraupel, chargeRain, chargeAir, rainNumber, graupelNumber, graupelVolume, hailNumber, hailVolume); 100
+// precipitation, 101 hailGround, 102 hailSize, 103-106 fall speeds, 107 condensate, 108-109 the charge carriers' fall
+// speeds, 110 the vertical field (fieldZ), 111-113 the number-weighted fall speeds of rain, graupel and hail.
 int orc_set_field(void* p, int id, const double* src, long count) {
   Handle* h = (Handle*)p;
   if (h->m32) { auto* v = extraField(h->m32, id); if (!v || (long)v->size() != count) return -1; for (long i = 0; i < count; i++) (*v)[i] = (float)src[i]; }
@@ -173,6 +175,12 @@ void orc_set_rain2m(void* p, int moments, int breakup) {
   auto set = [&](auto* m) { m->sw.rainMoments = moments; m->sw.rainBreakup = breakup; };
   if (h->m32) set(h->m32); else set(h->m64);
 }
+// Two-moment graupel and hail (AtmosphereModel.iceMoments, src/core/model.ts:839-840; with two-moment rain and ice only).
+void orc_set_ice2m(void* p, int moments) {
+  Handle* h = (Handle*)p;
+  auto set = [&](auto* m) { m->sw.iceMoments = moments; };
+  if (h->m32) set(h->m32); else set(h->m64);
+}
 // out[11]: chargeGround, separated, ic, cgNegative, cgPositive, precipitation, conduction, flashes IC, flashes CG,
 // totalCharge, flashes of the last step.
 void orc_charge_state(void* p, double* out) {
@@ -251,6 +259,45 @@ double orc_r2m_processes(float* v, double tk, double p, double rho, double dt, i
 void orc_r2m_number_change(float* v, double before, double rho, double meanMass) {
   Arr<float> a = (Arr<float>)v;
   r2m::numberChange<float>(a, a + 1, 0, before, rho, meanMass);
+}
+
+// ---------------------------------------------------------------- two-moment graupel and hail (src/core/ice2m.test.ts)
+double orc_i2m_gamma(double x) { return i2m::gammaFn(x); }
+double orc_i2m_upper_gamma(int n, double x) { return i2m::upperGamma(n, x); }
+static const i2m::IceClass& i2mClass(int c) { return c == 0 ? i2m::GRAUPEL_2M : i2m::HAIL_2M; }
+void orc_i2m_fall_law(double rhoX, double* ab) { i2m::fallLaw(rhoX, ab[0], ab[1]); }
+double orc_i2m_density(int c, double q, double vol) { return i2m::densityOf(i2mClass(c), q, vol); }
+double orc_i2m_bounded(int c, double q, double n, double vol) { return i2m::boundedIceNumber(i2mClass(c), q, n, vol); }
+double orc_i2m_moment_speed(int c, double q, double n, double vol, double rho, int k) { return i2m::momentSpeed(i2mClass(c), q, n, vol, rho, k); }
+double orc_i2m_largest(int c, double q, double n, double vol, double rho) { return i2m::largestDiameter(i2mClass(c), q, n, vol, rho); }
+double orc_i2m_reflectivity_factor(int c) { return i2m::reflectivityFactor(i2mClass(c).alpha); }
+// out5 = n, d1, d2, fall, d2v; returns 0 without the class (null in the reference).
+int orc_i2m_rimer_moments(int c, double q, double n, double vol, double rho, double* out5) {
+  RimerMoments m;
+  if (!i2m::rimerMoments(i2mClass(c), q, n, vol, rho, m)) return 0;
+  out5[0] = m.n; out5[1] = m.d1; out5[2] = m.d2; out5[3] = m.fall; out5[4] = m.d2v;
+  return 1;
+}
+// The Seifert-Beheng sweep coefficients of a class (0 graupel, 1 hail) with the droplets (y 0) or an exponential class
+// (y 1) for moment k: out3 = delbk(x, 0), delabk(x, y, k), delbk(y, k).
+void orc_i2m_sweep_coefficients(int c, int y, int k, double* out3) {
+  i2m::MassShape x = i2m::diameterShape(i2mClass(c).alpha), ys = y == 0 ? i2m::DROPLETS : i2m::diameterShape(0);
+  out3[0] = i2m::delbk(x, 0); out3[1] = i2m::delabk(x, ys, k); out3[2] = i2m::delbk(ys, k);
+}
+// v = 14 FP32 cells in Ice2mFields order (theta, q, cloud, ice, iceNumber, snow, rain, rainNumber, graupel, graupelNumber,
+// graupelVolume, hail, hailNumber, hailVolume), in place; out3 = cooling, wetG, wetH.
+void orc_i2m_processes(float* v, double exner, double p, double rho, double dt, double* out3) {
+  Arr<float> a = (Arr<float>)v;
+  i2m::Fields<float> f = {a, a + 1, a + 2, a + 3, a + 4, a + 5, a + 6, a + 7, a + 8, a + 9, a + 10, a + 11, a + 12, a + 13};
+  i2m::Result r = i2m::processes<float>(f, 0, exner, p, rho, dt);
+  out3[0] = r.cooling; out3[1] = r.wetG; out3[2] = r.wetH;
+}
+// chargingRate with optional two-moment moments (m10 = graupel's five then hail's five; has2 flags which are given).
+double orc_charging_rate_2m(double tc, double rho, double cloud, double ice, double snow, double graupel, double hail, double snowFall, int wetG, int wetH,
+                            double crystals, const double* m10, const int* has2) {
+  RimerMoments m[2]; bool has[2] = {has2[0] != 0, has2[1] != 0};
+  for (int j = 0; j < 2; j++) m[j] = {m10[5 * j], m10[5 * j + 1], m10[5 * j + 2], m10[5 * j + 3], m10[5 * j + 4]};
+  return chargingRate(tc, rho, cloud, ice, snow, graupel, hail, snowFall, wetG != 0, wetH != 0, crystals, true, m, has);
 }
 
 // ---------------------------------------------------------------- charging (src/core/charge.test.ts)

@@ -85,8 +85,10 @@ inline double rimerRate(const RimerMoments& m, double tc, double water, double r
 }
 
 // :136-151. `crystals` < 0 stands for "not given" (the reference's undefined): the number is then estimated from the mass.
+// `twoMoment` (ice2m.ts rimerMoments of graupel and hail, a null pointer or a false flag for "none") replaces the
+// exponential moments of a rimer that has them (:153-155; a missing entry falls back to the fixed intercept's).
 inline double chargingRate(double tc, double rho, double cloud, double ice, double snow, double graupel, double hail, double snowFall, bool wetGraupel = false,
-                           bool wetHail = false, double crystals = -1, bool tak = true) {
+                           bool wetHail = false, double crystals = -1, bool tak = true, const RimerMoments* twoMoment = nullptr, const bool* twoHas = nullptr) {
   if (tc >= 0 || tc < (tak ? -40 : CHARGING_COLDEST) || cloud <= 0 || ice + snow <= 0 || graupel + hail <= 0) return 0;
   double rebound = tak ? .5 * (1 - .1 * std::exp(.1 * tc)) : 1 - std::exp(.09 * tc), water = rho * cloud * 1000;
   bool given = crystals >= 0;
@@ -96,13 +98,14 @@ inline double chargingRate(double tc, double rho, double cloud, double ice, doub
   double snowSlope = snow > 0 ? std::pow(PI * RHO_S * N0S / (rho * snow), .25) : 0, ns = snow > 0 ? N0S / snowSlope : 0,
          ds = snow > 0 ? (tak ? 1.8171 : 1) / snowSlope : 0;
   double rate = 0, table = tak ? takahashiCharge(tc, water) : 0;
-  if (graupel > 0 && !wetGraupel) rate += rimerRate(exponentialMoments(N0G, RHO_G, graupel, rho), tc, water, rebound, ni, di, ns, ds, snowFall, table, tak);
-  if (hail > 0 && !wetHail) rate += rimerRate(exponentialMoments(N0H, RHO_H, hail, rho), tc, water, rebound, ni, di, ns, ds, snowFall, table, tak);
+  auto momentsOf = [&](int j, double n0, double dens, double q) { return twoMoment && twoHas[j] ? twoMoment[j] : exponentialMoments(n0, dens, q, rho); };
+  if (graupel > 0 && !wetGraupel) rate += rimerRate(momentsOf(0, N0G, RHO_G, graupel), tc, water, rebound, ni, di, ns, ds, snowFall, table, tak);
+  if (hail > 0 && !wetHail) rate += rimerRate(momentsOf(1, N0H, RHO_H, hail), tc, water, rebound, ni, di, ns, ds, snowFall, table, tak);
   return rate;
 }
 
 inline double inductiveRate(double tc, double rho, double cloud, double graupel, double hail, double ez, double rimerCharge, bool wetGraupel = false,
-                            bool wetHail = false) {  // :187-200
+                            bool wetHail = false, const RimerMoments* twoMoment = nullptr, const bool* twoHas = nullptr) {  // :187-200
   if (tc >= 0 || cloud <= 0) return 0;
   double d = DROPLET_SIZE, droplets = rho * cloud / (PI / 6 * 1000 * std::pow(d, 3)), k = COLLECTION_EFFICIENCY * DROPLET_REBOUND * droplets;
   double polarize = 0, mass = 0, massFall = 0;
@@ -110,7 +113,7 @@ inline double inductiveRate(double tc, double rho, double cloud, double graupel,
   const bool wet[2] = {wetGraupel, wetHail};
   for (int j = 0; j < 2; j++) {
     if (q[j] <= 1e-9 || wet[j]) continue;
-    RimerMoments m = exponentialMoments(n0[j], dens[j], q[j], rho);
+    RimerMoments m = twoMoment && twoHas[j] ? twoMoment[j] : exponentialMoments(n0[j], dens[j], q[j], rho);
     polarize += std::pow(PI, 4) / 8 * EPSILON0 * ez * CONTACT_COS * d * d * m.d2v;
     mass += q[j]; massFall += q[j] * m.fall;
   }

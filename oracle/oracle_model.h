@@ -9,6 +9,7 @@
 #include "oracle_solvers.h"
 #include "oracle_elec.h"
 #include "oracle_rain2m.h"
+#include "oracle_ice2m.h"
 
 namespace orc {
 
@@ -24,20 +25,27 @@ struct Switches {
   int lightningSeed = 43;
   // Two-moment rain (AtmosphereModel.rainMoments 2, src/core/model.ts:842; rain2m(), :905) and its breakup (:843).
   int rainMoments = 1, rainBreakup = r2m::NONE;
+  // Two-moment graupel and hail (iceMoments 2, :839-840; ice2m(), :914: with the ice microphysics and two-moment rain).
+  int iceMoments = 1;
 };
 
 enum FieldId { F_RAIN, F_SNOW, F_GRAUPEL, F_HAIL, F_U, F_V, F_W, F_THETA, F_Q, F_CLOUD, F_ICE, F_ICENUMBER, F_COLD,
                F_CHARGE_ICE, F_CHARGE_GRAUPEL, F_CHARGE_RAIN, F_CHARGE_AIR,  // charges: src/core/model.ts:210
-               F_RAIN_NUMBER, N_CARRIED };                                   // raindrops per kg (two-moment rain): :194
+               F_RAIN_NUMBER,                                                // raindrops per kg (two-moment rain): :194
+               F_GRAUPEL_NUMBER, F_GRAUPEL_VOLUME, F_HAIL_NUMBER, F_HAIL_VOLUME,  // two-moment graupel and hail: :202
+               N_CARRIED };
 
 // The microphysics part of physics(z) for node i (src/core/model.ts:1391-1471): Kessler rain, then with ice the
 // freezing, crystals, snow, graupel, hail, secondary ice and the mixed-phase saturation adjustment, else the warm
 // adjustment; the cold-pool indicator's share of the cooling. Returns the evaporated rain.
 // With two-moment rain (`rainNumber` given), its processes replace Kessler's and the drop number follows the rain the
-// ice processes take or give (:1391, :1402-1435).
+// ice processes take or give (:1391, :1402-1435). With two-moment graupel and hail as well (`ice2m` given, its
+// rainNumber the same array), their processes replace the one-moment graupel and hail ones (:1420-1426) and `wet2m`
+// receives their cooling and wet growth.
 template <class S>
 double microphysicsNode(Arr<S> theta, Arr<S> q, Arr<S> cloud, Arr<S> rain, Arr<S> cold, Arr<S> ice, Arr<S> iceNumber, Arr<S> snow, Arr<S> graupel,
-                        Arr<S> hail, int i, double ex, double pz, double rhoZ, double rhoGround, double dt, const Switches& sw, Arr<S> rainNumber = nullptr) {
+                        Arr<S> hail, int i, double ex, double pz, double rhoZ, double rhoGround, double dt, const Switches& sw, Arr<S> rainNumber = nullptr,
+                        const i2m::Fields<S>* ice2m = nullptr, i2m::Result* wet2m = nullptr) {
   const bool two = rainNumber != nullptr;
   double evap = !sw.rainFormation ? 0
                : two ? r2m::processes<S>(q, cloud, rain, rainNumber, i, (double)theta[i] * ex, pz, rhoZ, dt, sw.rainBreakup, sw.evaporation)
@@ -46,7 +54,12 @@ double microphysicsNode(Arr<S> theta, Arr<S> q, Arr<S> cloud, Arr<S> rain, Arr<S
   double cond;
   if (sw.ice) {
     double rainMark = rain[i];
+    const double frozenDrops = two ? (double)rainNumber[i] : 0, graupelMark = graupel[i];
     freezeRain<S>(theta, rain, graupel, i, ex);
+    // two-moment graupel: the drops frozen at once become as many particles of 900 kg/m3 (:1404)
+    if (ice2m && (double)graupel[i] > graupelMark) {
+      ice2m->graupelNumber[i] += rainMark > 0 ? frozenDrops * (1 - (double)rain[i] / rainMark) : 0; ice2m->graupelVolume[i] += ((double)graupel[i] - graupelMark) / 900;
+    }
     if (two) { r2m::numberChange<S>(rain, rainNumber, i, rainMark, rhoZ, 0); rainMark = rain[i]; }
     settleCrystals<S>(ice, iceNumber, i);
     cold[i] += iceProcesses<S>(theta, q, ice, snow, iceNumber, i, ex, pz, rhoZ, dt);
@@ -54,14 +67,21 @@ double microphysicsNode(Arr<S> theta, Arr<S> q, Arr<S> cloud, Arr<S> rain, Arr<S
     const double snowMass = two ? r2m::exponentialMeanMass(snow[i], N0S, RHO_S, rhoZ) : 0;
     cold[i] += snowProcesses<S>(theta, q, cloud, ice, snow, rain, i, ex, pz, rhoZ, rhoGround, dt);
     if (two) { r2m::numberChange<S>(rain, rainNumber, i, rainMark, rhoZ, snowMass); rainMark = rain[i]; }
-    double rainBefore = rain[i];
-    const double graupelMass = two ? r2m::exponentialMeanMass(graupel[i], N0G, RHO_G, rhoZ) : 0;
-    cold[i] += graupelProcesses<S>(theta, q, cloud, ice, snow, rain, graupel, i, ex, pz, rhoZ, dt);
-    if (two) { r2m::numberChange<S>(rain, rainNumber, i, rainMark, rhoZ, graupelMass); rainMark = rain[i]; }
-    double rainFrozen = (double)theta[i] * ex < 273.15 ? jmax(0, rainBefore - (double)rain[i]) : 0;
-    const double hailMass = two ? r2m::exponentialMeanMass(hail[i], N0H, RHO_H, rhoZ) : 0;
-    cold[i] += hailProcesses<S>(theta, q, cloud, ice, snow, rain, graupel, hail, i, ex, pz, rhoZ, dt);
-    if (two) r2m::numberChange<S>(rain, rainNumber, i, rainMark, rhoZ, hailMass);
+    // (the one-moment snow gives no graupel with RIMED_SNOW_TO_GRAUPEL off, so :1417 never applies)
+    double rainBefore = rain[i], rainFrozen;
+    if (ice2m) {  // :1421-1426
+      i2m::Result r = i2m::processes<S>(*ice2m, i, ex, pz, rhoZ, dt); cold[i] += r.cooling;
+      if (wet2m) *wet2m = r;
+      rainFrozen = (double)theta[i] * ex < 273.15 ? jmax(0, rainBefore - (double)rain[i]) : 0;
+    } else {
+      const double graupelMass = two ? r2m::exponentialMeanMass(graupel[i], N0G, RHO_G, rhoZ) : 0;
+      cold[i] += graupelProcesses<S>(theta, q, cloud, ice, snow, rain, graupel, i, ex, pz, rhoZ, dt);
+      if (two) { r2m::numberChange<S>(rain, rainNumber, i, rainMark, rhoZ, graupelMass); rainMark = rain[i]; }
+      rainFrozen = (double)theta[i] * ex < 273.15 ? jmax(0, rainBefore - (double)rain[i]) : 0;
+      const double hailMass = two ? r2m::exponentialMeanMass(hail[i], N0H, RHO_H, rhoZ) : 0;
+      cold[i] += hailProcesses<S>(theta, q, cloud, ice, snow, rain, graupel, hail, i, ex, pz, rhoZ, dt);
+      if (two) r2m::numberChange<S>(rain, rainNumber, i, rainMark, rhoZ, hailMass);
+    }
     if (iceBefore > 0) iceNumber[i] *= (double)ice[i] / iceBefore;
     double splinters = splintering((double)theta[i] * ex - 273.15) * SPLINTERS * jmax(0, cloudBefore - (double)cloud[i])
       + (rainFrozen > 0 ? fragmentsPerKg(std::pow(PI * RHO_W * N0R / (rhoZ * rainBefore), .25)) * rainFrozen : 0);
@@ -86,6 +106,7 @@ template <class S> struct Model {
   // charge separated per level; the ground's charge, the budget, the flash counts and this step's flashes
   std::vector<S> fallChargeIce, fallChargeGraupel, fieldZ, levelCharge;
   std::vector<S> rainFallNumber;  // two-moment rain: the number-weighted fall speed (:1224)
+  std::vector<S> graupelFallNumber, hailFallNumber;  // two-moment graupel and hail: their number-weighted fall speeds (:1227-1228)
   double chargeGround = 0, chargeSeparated = 0, chargeIC = 0, chargeCgNegative = 0, chargeCgPositive = 0, chargePrecipitation = 0, chargeConduction = 0;
   long flashesIC = 0, flashesCG = 0;
   std::vector<Flash> lastFlashes;
@@ -113,6 +134,7 @@ template <class S> struct Model {
     fallRain.assign(n, 0); fallSnow.assign(n, 0); fallGraupel.assign(n, 0); fallHail.assign(n, 0); condensate.assign(n, 0);
     precipitation.assign(layer, 0); hailGround.assign(layer, 0); hailSize.assign(layer, 0); levelWater.assign(nz * 4, 0);
     fallChargeIce.assign(n, 0); fallChargeGraupel.assign(n, 0); fieldZ.assign(n, 0); levelCharge.assign(nz, 0); rainFallNumber.assign(n, 0);
+    graupelFallNumber.assign(n, 0); hailFallNumber.assign(n, 0);
     flux = FluxTransport(g, rho.data()); solver = PressureSolver(g, rho.data()); turb = Turbulence(g, rho.data());
     flux.g = &g; solver.g = &g; turb.g = &g;
     turb.anisotropic = sw.anisotropic; turb.verticalDz = sw.verticalDz; turb.durranKlemp = sw.durranKlemp;
@@ -140,6 +162,7 @@ template <class S> struct Model {
     c.push_back({F_RAIN, true, true, 1});
     if (sw.ice) { c.push_back({F_SNOW, true, true, 1}); c.push_back({F_GRAUPEL, true, true, 1}); c.push_back({F_HAIL, true, true, 1}); }
     if (rain2m()) c.push_back({F_RAIN_NUMBER, true, false, 1});  // :1323
+    if (ice2m()) for (int k : {F_GRAUPEL_NUMBER, F_GRAUPEL_VOLUME, F_HAIL_NUMBER, F_HAIL_VOLUME}) c.push_back({k, true, false, 1});  // :1324
     for (int k : {F_U, F_V, F_W, F_THETA}) c.push_back({k, false, false, 1});
     c.push_back({F_Q, true, true, 1}); c.push_back({F_CLOUD, true, true, 1});
     if (sw.ice) { c.push_back({F_ICE, true, true, 1}); c.push_back({F_ICENUMBER, true, false, 1}); }
@@ -149,6 +172,11 @@ template <class S> struct Model {
   }
   bool electrified() const { return sw.ice && sw.lightning; }  // :1316
   bool rain2m() const { return sw.rainMoments == 2; }             // :905 (the WENO transport is the only one here)
+  bool ice2m() const { return sw.iceMoments == 2 && sw.ice && rain2m(); }  // :914
+  i2m::Fields<S> fields2m() {
+    return {F(F_THETA), F(F_Q), F(F_CLOUD), F(F_ICE), F(F_ICENUMBER), F(F_SNOW), F(F_RAIN), F(F_RAIN_NUMBER), F(F_GRAUPEL), F(F_GRAUPEL_NUMBER),
+            F(F_GRAUPEL_VOLUME), F(F_HAIL), F(F_HAIL_NUMBER), F(F_HAIL_VOLUME)};
+  }
 
   // ---------------------------------------------------------- beginStep (src/core/model.ts:893-902)
   void updateGround() {  // :644-657 (the surface pattern, city and zones are zero in the device's configuration)
@@ -176,6 +204,13 @@ template <class S> struct Model {
       Arr<S> num = F(F_RAIN_NUMBER), rfn = A(rainFallNumber);
       for (int i = k * layer, end = i + layer; i < end; i++) { double vm, vn; r2m::fallSpeeds(rain[i], num[i], rho[k], vm, vn); fr[i] = vm; rfn[i] = vn; }
     }
+    if (ice2m()) {  // :1226-1229
+      Arr<S> gn = F(F_GRAUPEL_NUMBER), gv = F(F_GRAUPEL_VOLUME), hn = F(F_HAIL_NUMBER), hv = F(F_HAIL_VOLUME), gfn = A(graupelFallNumber), hfn = A(hailFallNumber);
+      for (int i = k * layer, end = i + layer; i < end; i++) {
+        fg[i] = i2m::momentSpeed(i2m::GRAUPEL_2M, graupel[i], gn[i], gv[i], rho[k], 3); gfn[i] = i2m::momentSpeed(i2m::GRAUPEL_2M, graupel[i], gn[i], gv[i], rho[k], 0);
+        fh[i] = i2m::momentSpeed(i2m::HAIL_2M, hail[i], hn[i], hv[i], rho[k], 3); hfn[i] = i2m::momentSpeed(i2m::HAIL_2M, hail[i], hn[i], hv[i], rho[k], 0);
+      }
+    }
     if (electrified()) {  // :1230-1234
       Arr<S> ice = F(F_ICE), ci = A(fallChargeIce), cg = A(fallChargeGraupel);
       for (int i = k * layer, end = i + layer; i < end; i++) {
@@ -191,7 +226,7 @@ template <class S> struct Model {
       int i = b; double h = hail[i];
       if (!(h > 1e-9)) continue;
       deposit(b, rho[0] * h * (double)fh[i] * dt, hailGround);
-      double size = hailMaxDiameter(hail[i], rho[0]) * 1000;
+      double size = (ice2m() ? i2m::largestDiameter(i2m::HAIL_2M, hail[i], F(F_HAIL_NUMBER)[i], F(F_HAIL_VOLUME)[i], rho[0]) : hailMaxDiameter(hail[i], rho[0])) * 1000;  // largestHail :709-711
       for (int j = 0; j < 4; j++) if (groundWeight[b * 4 + j] > 0) { int c = groundCell[b * 4 + j]; hs[c] = jmax(hs[c], size); }
     }
   }
@@ -221,6 +256,7 @@ template <class S> struct Model {
   void sedimentStep(double dt) {  // :928-932
     std::pair<int, std::vector<S>*> falls[4] = {{F_RAIN, &fallRain}, {F_SNOW, &fallSnow}, {F_GRAUPEL, &fallGraupel}, {F_HAIL, &fallHail}};
     for (int j = rain2m() ? 1 : 0; j < (sw.ice ? 4 : 1); j++) {  // sedimented(): two-moment rain falls on its own (:907-911)
+      if (ice2m() && j >= 2) continue;                            // and so do two-moment graupel and hail
       Arr<S> field = F(falls[j].first), vt = A(*falls[j].second);
       int parts = fallParts(field, vt, dt);
       for (int q = 0; q < parts; q++) sedimentPart(field, vt, dt / parts);
@@ -239,27 +275,35 @@ template <class S> struct Model {
     run(g.nz, [&](int k, int) { fall(k); });
     if (sw.ice) collectHail(dt);
     if (rain2m()) sedimentRain2m(dt);  // :899
+    if (ice2m()) {                     // :900
+      sediment2m(dt, F(F_GRAUPEL), F(F_GRAUPEL_NUMBER), F(F_GRAUPEL_VOLUME), A(fallGraupel), A(graupelFallNumber), &i2m::GRAUPEL_2M);
+      sediment2m(dt, F(F_HAIL), F(F_HAIL_NUMBER), F(F_HAIL_VOLUME), A(fallHail), A(hailFallNumber), &i2m::HAIL_2M);
+    }
     sedimentStep(dt);
   }
-  // sedimentRain2m / sediment2m (:944-988; NSSL sediment1d, infall 4): mass with its mass-weighted speed, number with its
-  // number-weighted one, and each sub-step the number kept between what the reflectivity (at its own speed) and a number
-  // carried at the mass's speed imply. Flat ground, no two-moment ice volume.
-  void sedimentRain2m(double dt) {
+  // sedimentRain2m / sedimentIce2m / sediment2m (:916-988; NSSL sediment1d, infall 4): mass with its mass-weighted speed,
+  // number with its number-weighted one, a two-moment ice class's volume with the mass, and each sub-step the number
+  // kept between what the reflectivity (at its own speed) and a number carried at the mass's speed imply. Flat ground.
+  void sedimentRain2m(double dt) { sediment2m(dt, F(F_RAIN), F(F_RAIN_NUMBER), nullptr, A(fallRain), A(rainFallNumber), nullptr); }
+  void sediment2m(double dt, Arr<S> q, Arr<S> num, Arr<S> vol, Arr<S> vm, Arr<S> vn, const i2m::IceClass* c) {
     int nz = g.nz, layer = g.layer, n = g.n;
-    Arr<S> q = F(F_RAIN), num = F(F_RAIN_NUMBER), vm = A(fallRain), vn = A(rainFallNumber);
+    const double qMin = c ? i2m::ICE2M_MIN : r2m::RAIN_MIN, g1 = c ? i2m::reflectivityFactor(c->alpha) : r2m::G1;
+    // the reflectivity's particle density: water's, or the class's own now, bounded to 170-900 kg/m3 (:920)
+    auto k6of = [&](int i) { double rx = c ? jmin(900, jmax(170, i2m::densityOf(*c, q[i], vol[i]))) : r2m::RHO_W2; return std::pow(6 / (PI * rx), 2); };
     std::vector<double> refl(n), carriedN(n); std::vector<float> vzv(n);
     double courant = 0;
     for (int z = 0; z < nz; z++) for (int i = z * layer; i < (z + 1) * layer; i++) {
-      vzv[i] = (float)((double)q[i] > r2m::RAIN_MIN ? r2m::fallSpeedZ(q[i], num[i], rho[z]) : 0);
+      vzv[i] = (float)(c ? ((double)q[i] > qMin ? i2m::momentSpeed(*c, q[i], num[i], vol[i], rho[z], 6) : 0)
+                         : ((double)q[i] > qMin ? r2m::fallSpeedZ(q[i], num[i], rho[z]) : 0));
       double h = g.hz[z];
       courant = jmax(courant, jmax(dt * (double)vzv[i] / h, dt * (double)vm[i] / h));
     }
     const int parts = (int)jmax(1, std::ceil(courant / .8));
-    const double step = dt / parts, k6 = std::pow(6 / (PI * r2m::RHO_W2), 2);
+    const double step = dt / parts;
     for (int p = 0; p < parts; p++) {
       for (int z = 0; z < nz; z++) for (int i = z * layer; i < (z + 1) * layer; i++) {
-        double rq = rho[z] * (double)q[i], rn = rho[z] * (double)num[i];
-        refl[i] = rq > 0 && rn > 0 ? r2m::G1 * k6 * rq * rq / rn : 0;
+        double rq = rho[z] * (double)q[i], rn = rho[z] * (double)num[i], k6 = k6of(i);
+        refl[i] = rq > 0 && rn > 0 ? g1 * k6 * rq * rq / rn : 0;
         carriedN[i] = num[i];
       }
       for (int c = 0; c < layer; c++) deposit(c, rho[0] * (double)q[c] * (double)vm[c] * step, precipitation);
@@ -268,14 +312,15 @@ template <class S> struct Model {
         for (int i = z * layer; i < (z + 1) * layer; i++) {
           int a = i + layer; double m = level;
           q[i] += step * ((top ? rho[z + 1] * (double)q[a] * (double)vm[a] : 0) - rho[z] * (double)q[i] * (double)vm[i]) / m;
+          if (vol) vol[i] += step * ((top ? rho[z + 1] * (double)vol[a] * (double)vm[a] : 0) - rho[z] * (double)vol[i] * (double)vm[i]) / m;
           num[i] += step * ((top ? rho[z + 1] * (double)num[a] * (double)vn[a] : 0) - rho[z] * (double)num[i] * (double)vn[i]) / m;
           carriedN[i] += step * ((top ? rho[z + 1] * carriedN[a] * (double)vm[a] : 0) - rho[z] * carriedN[i] * (double)vm[i]) / m;
           refl[i] += step * ((top ? refl[a] * (double)vzv[a] : 0) - refl[i] * (double)vzv[i]) / g.hz[z];
         }
       }
       for (int z = 0; z < nz; z++) for (int i = z * layer; i < (z + 1) * layer; i++) {
-        if (!((double)q[i] > r2m::RAIN_MIN)) { if ((double)q[i] < 0) q[i] = 0.0; num[i] = 0.0; continue; }
-        double rq = rho[z] * (double)q[i], fromZ = refl[i] > 0 ? r2m::G1 * k6 * rq * rq / refl[i] / rho[z] : INFINITY;
+        if (!((double)q[i] > qMin)) { if ((double)q[i] < 0) q[i] = 0.0; num[i] = 0.0; if (vol) vol[i] = 0.0; continue; }
+        double rq = rho[z] * (double)q[i], k6 = k6of(i), fromZ = refl[i] > 0 ? g1 * k6 * rq * rq / refl[i] / rho[z] : INFINITY;
         num[i] = refl[i] > 0 ? jmax(jmin(fromZ, carriedN[i]), (double)num[i]) : jmax(carriedN[i], (double)num[i]);
       }
     }
@@ -369,23 +414,32 @@ template <class S> struct Model {
     Arr<S> ice = F(F_ICE), iceNumber = F(F_ICENUMBER), snow = F(F_SNOW), graupel = F(F_GRAUPEL), hail = F(F_HAIL);
     double rhoGround = rho[0], f = sw.coriolis, keep = std::exp(-sw.windRelaxation * dt), H = g.height;
     double alt = g.zs[z], pz = p[z], rhoZ = rho[z], ex = exner[z], ue = uEnv[z], ve = vEnv[z], thEnv = thetaEnv[z];
-    const bool electric = electrified(); double wCharge = 0;
+    const bool electric = electrified(), two2m = ice2m(); double wCharge = 0;
+    const i2m::Fields<S> f2m = fields2m();
     Arr<S> cI = F(F_CHARGE_ICE), cG = F(F_CHARGE_GRAUPEL), cR = F(F_CHARGE_RAIN), cA = F(F_CHARGE_AIR), snowFall = A(fallSnow), ez = A(fieldZ);
     for (int y = 0; y < ny; y++) for (int x = 0, i = z * layer + y * nx; x < nx; x++, i++) {
       double q0 = q[i];
       double before[4] = {0, 0, 0, 0};
       if (electric) { before[0] = (double)ice[i] + (double)snow[i]; before[1] = (double)graupel[i] + (double)hail[i]; before[2] = rain[i]; before[3] = cloud[i]; }
+      i2m::Result wet2m = {0, false, false};
       double evap = microphysicsNode<S>(theta, q, cloud, rain, cold, ice, iceNumber, snow, graupel, hail, i, ex, pz, rhoZ, rhoGround, dt, sw,
-                                        rain2m() ? F(F_RAIN_NUMBER) : nullptr);
+                                        rain2m() ? F(F_RAIN_NUMBER) : nullptr, two2m ? &f2m : nullptr, &wet2m);
       if (electric) {  // :1454-1469 (after the microphysics' last change to the carriers; only cold changes after it there)
         double after[4] = {(double)ice[i] + (double)snow[i], (double)graupel[i] + (double)hail[i], (double)rain[i], (double)cloud[i]};
         double now[4] = {cI[i], cG[i], cR[i], cA[i]};
         if (now[0] != 0 || now[1] != 0 || now[2] != 0 || now[3] != 0) transferCharge(now, before, after);
         double tc = (double)theta[i] * ex - 273.15;
-        bool wetG = wetGrowing(graupel[i], N0G, RHO_G, tc, q[i], pz, rhoZ, cloud[i], rain[i], ice[i], snow[i]);
-        bool wetH = wetGrowing(hail[i], N0H, RHO_H, tc, q[i], pz, rhoZ, cloud[i], rain[i], ice[i], snow[i]);
-        double separated = chargingRate(tc, rhoZ, cloud[i], ice[i], snow[i], graupel[i], hail[i], snowFall[i], wetG, wetH, (double)iceNumber[i] * rhoZ, true) * dt / rhoZ;
-        double induced = inductiveRate(tc, rhoZ, cloud[i], graupel[i], hail[i], ez[i], (now[1] + separated) * rhoZ, wetG, wetH) * dt / rhoZ;
+        bool wetG = two2m ? wet2m.wetG : wetGrowing(graupel[i], N0G, RHO_G, tc, q[i], pz, rhoZ, cloud[i], rain[i], ice[i], snow[i]);
+        bool wetH = two2m ? wet2m.wetH : wetGrowing(hail[i], N0H, RHO_H, tc, q[i], pz, rhoZ, cloud[i], rain[i], ice[i], snow[i]);
+        // two-moment graupel and hail charge by their own distributions (:1462-1466)
+        RimerMoments mom[2]; bool has[2] = {false, false};
+        if (two2m) {
+          has[0] = i2m::rimerMoments(i2m::GRAUPEL_2M, graupel[i], f2m.graupelNumber[i], f2m.graupelVolume[i], rhoZ, mom[0]);
+          has[1] = i2m::rimerMoments(i2m::HAIL_2M, hail[i], f2m.hailNumber[i], f2m.hailVolume[i], rhoZ, mom[1]);
+        }
+        double separated = chargingRate(tc, rhoZ, cloud[i], ice[i], snow[i], graupel[i], hail[i], snowFall[i], wetG, wetH, (double)iceNumber[i] * rhoZ, true,
+                                        two2m ? mom : nullptr, has) * dt / rhoZ;
+        double induced = inductiveRate(tc, rhoZ, cloud[i], graupel[i], hail[i], ez[i], (now[1] + separated) * rhoZ, wetG, wetH, two2m ? mom : nullptr, has) * dt / rhoZ;
         cI[i] = now[0] - separated; cG[i] = now[1] + separated + induced; cR[i] = now[2]; cA[i] = now[3] - induced;
         wCharge += std::fabs(separated) + std::fabs(induced);
       }

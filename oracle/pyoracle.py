@@ -19,9 +19,10 @@ _lib = None
 CARRIED = ("rain", "snow", "graupel", "hail", "u", "v", "w", "theta", "q", "cloud", "ice", "iceNumber", "cold")
 CHARGES = ("chargeIce", "chargeGraupel", "chargeRain", "chargeAir")
 RAIN_NUMBER = "rainNumber"   # field id 17: raindrops per kg (two-moment rain)
+ICE2M = ("graupelNumber", "graupelVolume", "hailNumber", "hailVolume")   # field ids 18-21 (two-moment graupel and hail)
 EXTRA = {"precipitation": 100, "hailGround": 101, "hailSize": 102, "fallSpeed": 103, "snowFall": 104,
          "graupelFall": 105, "hailFall": 106, "condensate": 107, "chargeFallIce": 108, "chargeFallGraupel": 109,
-         "fieldZ": 110, "rainFallNumber": 111}
+         "fieldZ": 110, "rainFallNumber": 111, "graupelFallNumber": 112, "hailFallNumber": 113}
 
 _d = C.POINTER(C.c_double)
 _f = C.POINTER(C.c_float)
@@ -95,7 +96,23 @@ def lib():
             L.orc_r2m_processes.restype = C.c_double
             L.orc_r2m_processes.argtypes = [_f] + [C.c_double] * 4 + [C.c_int, C.c_int]
             L.orc_r2m_number_change.argtypes = [_f, C.c_double, C.c_double, C.c_double]
+            L.orc_set_ice2m.argtypes = [C.c_void_p, C.c_int]
+            for name, args in (("orc_i2m_gamma", [C.c_double]), ("orc_i2m_upper_gamma", [C.c_int, C.c_double]),
+                               ("orc_i2m_density", [C.c_int, C.c_double, C.c_double]),
+                               ("orc_i2m_bounded", [C.c_int] + [C.c_double] * 3),
+                               ("orc_i2m_moment_speed", [C.c_int] + [C.c_double] * 4 + [C.c_int]),
+                               ("orc_i2m_largest", [C.c_int] + [C.c_double] * 4),
+                               ("orc_i2m_reflectivity_factor", [C.c_int])):
+                getattr(L, name).restype = C.c_double
+                getattr(L, name).argtypes = args
+            L.orc_i2m_fall_law.argtypes = [C.c_double, _d]
+            L.orc_i2m_rimer_moments.restype = C.c_int
+            L.orc_i2m_rimer_moments.argtypes = [C.c_int] + [C.c_double] * 4 + [_d]
+            L.orc_i2m_sweep_coefficients.argtypes = [C.c_int, C.c_int, C.c_int, _d]
+            L.orc_i2m_processes.argtypes = [_f] + [C.c_double] * 4 + [_d]
             _i = C.POINTER(C.c_int)
+            L.orc_charging_rate_2m.restype = C.c_double
+            L.orc_charging_rate_2m.argtypes = [C.c_double] * 8 + [C.c_int, C.c_int, C.c_double, _d, _i]
             L.orc_flash.argtypes = [C.c_void_p, C.c_int, _d, _i, _i, _i, _d, C.c_int]
             L.orc_lightning_create.restype = C.c_void_p
             L.orc_lightning_create.argtypes = grid_args + [_d, C.c_int]
@@ -166,6 +183,8 @@ class OracleModel:
         sw_ = spec.switches
         if getattr(sw_, "rain_moments", 1) == 2:
             L.orc_set_rain2m(self.h, 2, int(getattr(sw_, "rain_breakup", 0)))
+        if getattr(sw_, "ice_moments", 1) == 2:
+            L.orc_set_ice2m(self.h, 2)
         if getattr(sw_, "lightning", False):
             L.orc_set_lightning(self.h, 1, 1 if getattr(sw_, "corona", True) else 0, int(getattr(sw_, "lightning_seed", 43)))
         for name, arr in spec.fields.items():
@@ -187,6 +206,8 @@ class OracleModel:
             return len(CARRIED) + CHARGES.index(name)
         if name == RAIN_NUMBER:
             return len(CARRIED) + len(CHARGES)
+        if name in ICE2M:
+            return len(CARRIED) + len(CHARGES) + 1 + ICE2M.index(name)
         return EXTRA[name]
 
     def set(self, name: str, values: np.ndarray):
@@ -442,3 +463,79 @@ def transfer_charge(charge, before, after):
     c, b, a = f64(charge).copy(), f64(before), f64(after)
     lib().orc_transfer_charge(dp(c), dp(b), dp(a))
     return c
+
+
+# ---------------------------------------------------------------- two-moment graupel and hail (src/core/ice2m.ts)
+ICE_CLASS = {"graupel": 0, "hail": 1}
+I2M_ORDER = ("theta", "q", "cloud", "ice", "iceNumber", "snow", "rain", "rainNumber", "graupel", "graupelNumber",
+             "graupelVolume", "hail", "hailNumber", "hailVolume")
+
+
+def i2m_gamma(x):
+    return lib().orc_i2m_gamma(x)
+
+
+def i2m_upper_gamma(n, x):
+    return lib().orc_i2m_upper_gamma(n, x)
+
+
+def i2m_fall_law(rho_x):
+    out = np.zeros(2)
+    lib().orc_i2m_fall_law(rho_x, dp(out))
+    return float(out[0]), float(out[1])
+
+
+def i2m_density(c, q, vol):
+    return lib().orc_i2m_density(ICE_CLASS[c], q, vol)
+
+
+def i2m_bounded(c, q, n, vol):
+    return lib().orc_i2m_bounded(ICE_CLASS[c], q, n, vol)
+
+
+def i2m_moment_speed(c, q, n, vol, rho, k):
+    return lib().orc_i2m_moment_speed(ICE_CLASS[c], q, n, vol, rho, k)
+
+
+def i2m_largest(c, q, n, vol, rho):
+    return lib().orc_i2m_largest(ICE_CLASS[c], q, n, vol, rho)
+
+
+def i2m_reflectivity_factor(c):
+    return lib().orc_i2m_reflectivity_factor(ICE_CLASS[c])
+
+
+def i2m_rimer_moments(c, q, n, vol, rho):
+    """(n, d1, d2, fall, d2v) per m3, or None without the class."""
+    out = np.zeros(5)
+    return tuple(float(x) for x in out) if lib().orc_i2m_rimer_moments(ICE_CLASS[c], q, n, vol, rho, dp(out)) else None
+
+
+def i2m_sweep_coefficients(c, y, k):
+    """delbk(x, 0), delabk(x, y, k), delbk(y, k) for class c and y "droplets" or "exponential"."""
+    out = np.zeros(3)
+    lib().orc_i2m_sweep_coefficients(ICE_CLASS[c], 0 if y == "droplets" else 1, k, dp(out))
+    return tuple(float(x) for x in out)
+
+
+def i2m_node(**values) -> np.ndarray:
+    """An FP32 cell vector in ice2mProcesses' field order, zero where not given."""
+    return np.array([values.get(k, 0.0) for k in I2M_ORDER], np.float32)
+
+
+def i2m_processes(cell: np.ndarray, exner, p, rho, dt):
+    """ice2mProcesses on one node's cells (in place); returns (cooling, wetG, wetH)."""
+    assert cell.dtype == np.float32 and cell.size == 14
+    out = np.zeros(3)
+    lib().orc_i2m_processes(fp(cell), exner, p, rho, dt, dp(out))
+    return float(out[0]), bool(out[1]), bool(out[2])
+
+
+def charging_rate_2m(tc, rho, cloud, ice, snow, graupel, hail, snow_fall, wet_g=False, wet_h=False, crystals=-1.0, moments=(None, None)):
+    """chargingRate (Takahashi) with the two-moment moments of graupel and hail where given."""
+    m = np.zeros(10)
+    has = (C.c_int * 2)(*(0 if x is None else 1 for x in moments))
+    for j, x in enumerate(moments):
+        if x is not None:
+            m[5 * j:5 * j + 5] = x
+    return lib().orc_charging_rate_2m(tc, rho, cloud, ice, snow, graupel, hail, snow_fall, int(wet_g), int(wet_h), crystals, dp(m), has)
