@@ -71,7 +71,7 @@ def parse():
                    "timed steps see a developed storm with cloud and precipitation rather than the quiescent start")
     p.add_argument("--quick", action="store_true", help="skip the serving and stress-grid legs")
     p.add_argument("--moments", type=int, default=1, choices=[1, 2],
-                   help="with --ncu-window: the ensemble's rain one- or two-moment (the timed headline is one-moment)")
+                   help="with --ncu-window: the ensemble in the one- or two-moment configuration (two-moment rain, graupel and hail; the timed headline is one-moment)")
     p.add_argument("--ncu-window", action="store_true",
                    help="profiling driver: set up and spin up the ensemble, then run --steps eager steps between "
                         "cudaProfilerStart/Stop (for ncu --profile-from-start off) and exit without timing")
@@ -286,18 +286,29 @@ def electrified_leg(ctx, members, runs, steps: int, build: int = 200, cpu_steps:
                              "sample": f"the same {min(threads, k)} electrified member states, {cpu_steps} steps, oracle with lightning on"}}
 
 
-def two_moment_leg(ctx, members, runs, steps: int, cpu_steps: int = 10):
-    """Two-moment rain: the ensemble's members as the timed steps left them, their drop number started as the
-    reference starts rain without one (Marshall-Palmer's), `steps` timed graph steps of the whole batch beside its
-    one-moment steps; CPU: the oracle with two-moment rain from the same states, pool strategy."""
+def two_moment_specs(members, runs):
+    """The ensemble's members as the timed steps left them, in the reference's two-moment configuration (SimConfig.moments
+    2: two-moment rain, graupel and hail, src/core/model.ts:331): the drop number started as the reference starts rain
+    without one (Marshall-Palmer's), graupel's and hail's number and volume as the one-moment classes of the same mass."""
     import dataclasses
     import numpy as np
-    from meteolab_gb300.scenarios import RunSpec, marshall_palmer_number
+    from meteolab_gb300.scenarios import RunSpec, exponential_ice_moments, marshall_palmer_number
     specs = []
     for m, r in zip(members, runs):
         f = r.read()
-        f["rainNumber"] = marshall_palmer_number(f["rain"], np.repeat(np.asarray(m.env.rho), m.grid.layer))
-        specs.append(RunSpec(m.grid, m.env, dataclasses.replace(m.switches, rain_moments=2), f, m.seed, m.label))
+        rho = np.repeat(np.asarray(m.env.rho), m.grid.layer)
+        f["rainNumber"] = marshall_palmer_number(f["rain"], rho)
+        for kind in ("graupel", "hail"):
+            f[kind + "Number"], f[kind + "Volume"] = exponential_ice_moments(f[kind], rho, kind)
+        specs.append(RunSpec(m.grid, m.env, dataclasses.replace(m.switches, rain_moments=2, ice_moments=2), f, m.seed, m.label))
+    return specs
+
+
+def two_moment_leg(ctx, members, runs, steps: int, cpu_steps: int = 10):
+    """The two-moment configuration (two_moment_specs) of the ensemble: `steps` timed graph steps of the whole batch
+    beside its one-moment steps; CPU: the oracle in the same configuration from the same states, pool strategy."""
+    from meteolab_gb300.scenarios import RunSpec
+    specs = two_moment_specs(members, runs)
     tr = [ctx.create(s) for s in specs]
     ctx.time_steps(tr, 5)
     ms = ctx.time_steps(tr, steps)
@@ -309,11 +320,12 @@ def two_moment_leg(ctx, members, runs, steps: int, cpu_steps: int = 10):
     threads = os.cpu_count() or 1
     cpu = cpu_strategies(states[:threads], cpu_steps, threads)
     best = max(cpu, key=lambda key: cpu[key][0])
-    return {"members": len(specs), "grid": "40x32x50", "timed_steps": steps, "ms_per_step": ms / steps,
+    return {"members": len(specs), "grid": "40x32x50", "config": "SimConfig.moments 2: two-moment rain, graupel and hail",
+            "timed_steps": steps, "ms_per_step": ms / steps,
             "cell_steps_s": cells * steps / (ms * 1e-3),
             "kernels_ms_per_launch": {k: round(v[0], 5) for k, v in prof.items()},
             "cpu_baseline": {"value": cpu[best][0], "unit": "cell-steps/s", "cores": threads, "kind": "port", "strategy": best,
-                             "sample": f"{min(threads, len(states))} of the members, {cpu_steps} steps, oracle with two-moment rain"}}
+                             "sample": f"{min(threads, len(states))} of the members, {cpu_steps} steps, oracle in the two-moment configuration"}}
 
 
 def reference_arm(args, rank, pg):
@@ -459,14 +471,8 @@ def main():
         ctx.time_steps(runs, args.spinup)
         ctx.set_transport_shape(0)  # tune the transport again, on the developed storms rather than the quiescent start
     if args.ncu_window:
-        if args.moments == 2:  # the same states with two-moment rain, the drop number started as Marshall-Palmer's
-            import dataclasses
-            from meteolab_gb300.scenarios import RunSpec, marshall_palmer_number
-            specs = []
-            for m, r in zip(members, runs):
-                f = r.read()
-                f["rainNumber"] = marshall_palmer_number(f["rain"], np.repeat(np.asarray(m.env.rho), m.grid.layer))
-                specs.append(RunSpec(m.grid, m.env, dataclasses.replace(m.switches, rain_moments=2), f, m.seed, m.label))
+        if args.moments == 2:  # the same states in the two-moment configuration (two_moment_specs)
+            specs = two_moment_specs(members, runs)
             for r in runs:
                 r.retire()
             runs = [ctx.create(s) for s in specs]

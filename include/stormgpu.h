@@ -43,9 +43,14 @@ enum sg_field {
  * droplet-ion carriers, C per kg of air (AtmosphereModel.chargeIce, chargeGraupel, chargeRain, chargeAir,
  * src/core/model.ts:210), fields 13-16 of sg_run_read_fields / sg_run_write_fields (host[f] by field id). */
 /* A two-moment run (sg_switches.rain_moments 2) also carries the raindrops per kg of air (AtmosphereModel.rainNumber,
- * :194), field 17. */
-enum sg_extra_field { SG_CHARGE_ICE = 13, SG_CHARGE_GRAUPEL, SG_CHARGE_RAIN, SG_CHARGE_AIR, SG_RAIN_NUMBER, SG_NFIELDS_EXTRA };
+ * :194), field 17; with two-moment graupel and hail (sg_switches.ice_moments 2) also their particles per kg of air and
+ * their particle volume, m3 per kg (graupelNumber, graupelVolume, hailNumber, hailVolume, :202), fields 18-21. */
+enum sg_extra_field {
+  SG_CHARGE_ICE = 13, SG_CHARGE_GRAUPEL, SG_CHARGE_RAIN, SG_CHARGE_AIR, SG_RAIN_NUMBER,
+  SG_GRAUPEL_NUMBER, SG_GRAUPEL_VOLUME, SG_HAIL_NUMBER, SG_HAIL_VOLUME, SG_NFIELDS_EXTRA
+};
 #define SG_CHARGE_FIELDS (0xFu << SG_CHARGE_ICE)
+#define SG_ICE2M_FIELDS (0xFu << SG_GRAUPEL_NUMBER)
 #define SG_NFIELDS_ELECTRIFIED SG_NFIELDS_EXTRA
 
 typedef struct sg_context sg_context;

@@ -85,9 +85,10 @@ SG_HD float rimerRate(const Moments& m, float table, float rebound, float ni, fl
 }
 
 // chargingRate (charge.ts:136-151), Takahashi scheme, the model's own crystals (`crystals` per m3): the charge
-// separation rate, C m^-3 s^-1, gained by the graupel-hail carrier.
+// separation rate, C m^-3 s^-1, gained by the graupel-hail carrier. `two` (graupel's, hail's) with the bits of `has`:
+// two-moment classes' own moments (ice2m.ts rimerMoments), taken instead of the fixed intercept's where given (:153-155).
 SG_HD float chargingRate(float tc, float rho, float cloud, float ice, float snow, float graupel, float hail, float snowFall, bool wetG, bool wetH,
-                         float crystals) {
+                         float crystals, const Moments* two = nullptr, int has = 0) {
   if (tc >= 0.f || tc < -40.f || cloud <= 0.f || ice + snow <= 0.f || graupel + hail <= 0.f) return 0.f;
   const float rebound = .5f * (1.f - .1f * expf(.1f * tc)), water = rho * cloud * 1000.f;
   const float ni = ice <= 0.f ? 0.f : crystals;
@@ -97,22 +98,23 @@ SG_HD float chargingRate(float tc, float rho, float cloud, float ice, float snow
   if (snow > 0.f) { const float slope = root4(PI * RHO_S * N0S / (rho * snow)); ns = N0S / slope; ds = 1.8171f / slope; }
   const float table = takahashi(tc, water);
   float rate = 0.f;
-  if (graupel > 0.f && !wetG) rate += rimerRate(moments(N0G, RHO_G, graupel, rho), table, rebound, ni, di, ns, ds, snowFall);
-  if (hail > 0.f && !wetH) rate += rimerRate(moments(N0H, RHO_H, hail, rho), table, rebound, ni, di, ns, ds, snowFall);
+  if (graupel > 0.f && !wetG) rate += rimerRate((has & 1) ? two[0] : moments(N0G, RHO_G, graupel, rho), table, rebound, ni, di, ns, ds, snowFall);
+  if (hail > 0.f && !wetH) rate += rimerRate((has & 2) ? two[1] : moments(N0H, RHO_H, hail, rho), table, rebound, ni, di, ns, ds, snowFall);
   return rate;
 }
 
 // inductiveRate (charge.ts:187-200): C m^-3 s^-1 gained by the graupel-hail carrier (the droplets get the opposite).
-SG_HD float inductiveRate(float tc, float rho, float cloud, float graupel, float hail, float ez, float rimerCharge, bool wetG, bool wetH) {
+SG_HD float inductiveRate(float tc, float rho, float cloud, float graupel, float hail, float ez, float rimerCharge, bool wetG, bool wetH,
+                          const Moments* two = nullptr, int has = 0) {
   if (tc >= 0.f || cloud <= 0.f) return 0.f;
   const float d = DROPLET_SIZE, droplets = rho * cloud / DROPLET_KG, k = COLLECTION_EFFICIENCY * DROPLET_REBOUND * droplets;
   float polarize = 0.f, mass = 0.f, massFall = 0.f;
   if (graupel > 1e-9f && !wetG) {
-    const Moments m = moments(N0G, RHO_G, graupel, rho);
+    const Moments m = (has & 1) ? two[0] : moments(N0G, RHO_G, graupel, rho);
     polarize += PI4_8 * EPSILON0 * ez * CONTACT_COS * d * d * m.d2v; mass += graupel; massFall += graupel * m.fall;
   }
   if (hail > 1e-9f && !wetH) {
-    const Moments m = moments(N0H, RHO_H, hail, rho);
+    const Moments m = (has & 2) ? two[1] : moments(N0H, RHO_H, hail, rho);
     polarize += PI4_8 * EPSILON0 * ez * CONTACT_COS * d * d * m.d2v; mass += hail; massFall += hail * m.fall;
   }
   if (mass == 0.f) return 0.f;

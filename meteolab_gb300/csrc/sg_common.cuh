@@ -30,10 +30,11 @@ namespace sg {
 constexpr int NF = 13;  // carried fields
 enum Field { RAIN = 0, SNOW, GRAUPEL, HAIL, U, V, W, THETA, Q, CLOUD, ICE, ICENUM, COLD };
 // An electrified run also carries the charge on the ice-snow, graupel-hail, rain and droplet-ion carriers (C/kg,
-// src/core/model.ts:210), a two-moment run the raindrop number (per kg, :194): WENO fields without the positivity fix,
-// not mixed (:1323, :1331, :1338-1344). Such a run's sets hold all five extra fields (NXE) after the 13 base fields'.
-constexpr int NXE = 5, NFE = NF + NXE;
-enum ExtraField { CHARGE_ICE = 13, CHARGE_GRAUPEL, CHARGE_RAIN, CHARGE_AIR, RAIN_NUMBER };
+// src/core/model.ts:210), a two-moment run the raindrop number (per kg, :194) and with two-moment graupel and hail
+// their number and particle volume (:202): WENO fields without the positivity fix, not mixed (:1323-1324, :1331,
+// :1338-1344). Such a run's sets hold all nine extra fields (NXE) after the 13 base fields'.
+constexpr int NXE = 9, NFE = NF + NXE;
+enum ExtraField { CHARGE_ICE = 13, CHARGE_GRAUPEL, CHARGE_RAIN, CHARGE_AIR, RAIN_NUMBER, GRAUPEL_NUMBER, GRAUPEL_VOLUME, HAIL_NUMBER, HAIL_VOLUME };
 // WENO5 for the water species and the cold-pool indicator, linear fifth-order upwind for u, v, w, theta
 // (src/core/model.ts:1320-1328).
 SG_HD bool monotone(int f) { return !(f == U || f == V || f == W || f == THETA); }
@@ -105,15 +106,19 @@ struct RunDesc {
   float meso_zeta;                     // mesoCoreZeta(dx) (:129)
   float pad2;
   // electrified or two-moment runs: the step-start fall speeds [6][n] (ice-snow and graupel-hail charge carriers, rain,
-  // snow, rain's number- and reflectivity-weighted), the vertical field of the last solve [n] (V/m, for the inductive
-  // charging), the sedimentation's charge reaching the ground per work item
+  // snow, rain's number- and reflectivity-weighted), with two-moment graupel and hail [12][n] (then also graupel's mass-,
+  // number- and reflectivity-weighted, and hail's: V_MASS_G...), the vertical field of the last solve [n] (V/m, for the
+  // inductive charging), the sedimentation's charge reaching the ground per work item
   float* vfall;
   float* ez;
   double* cpart;
 };
 enum RunFlags { RF_LOADING = 1, RF_EVAP = 2, RF_RAINFORM = 4, RF_ANISO = 8, RF_VDZ = 16, RF_DK = 32, RF_STAGES = 64, RF_ICE = 128,
-                RF_REFINE = 256, RF_ROTATION = 512, RF_ELEC = 1024, RF_RAIN2M = 2048 };
-constexpr int RF_EXTRA = RF_ELEC | RF_RAIN2M;  // a run with the extra fields
+                RF_REFINE = 256, RF_ROTATION = 512, RF_ELEC = 1024, RF_RAIN2M = 2048, RF_ICE2M = 4096 };
+constexpr int RF_EXTRA = RF_ELEC | RF_RAIN2M | RF_ICE2M;  // a run with the extra fields
+// vfall rows: the charge carriers', rain's mass-, snow's, rain's number- and reflectivity-weighted speeds; then
+// two-moment graupel's and hail's mass-, number- and reflectivity-weighted ones
+enum FallRow { V_CHG_ICE = 0, V_CHG_GRAUPEL, V_RAIN, V_SNOW, V_RAIN_N, V_RAIN_Z, V_GRAUPEL, V_GRAUPEL_N, V_GRAUPEL_Z, V_HAIL, V_HAIL_N, V_HAIL_Z };
 // diag columns: the UH column, the core sums, the swaths, the core labels; then the ground columns of a sample
 enum DiagColumn { DG_UH = 0, DG_COREW, DG_COREWZ, DG_GUST_MAX, DG_UH_MAX, DG_LABEL, DG_RATE, DG_HAIL, DG_GUST, DG_THV, DG_MASK, DG_COUNT };
 // rot layout (doubles): the rotation state (src/core/model.ts:263), the run's model time, then the step's keys and the
@@ -122,8 +127,9 @@ enum RotSlot { R_UH = 0, R_X, R_Y, R_ANTI, R_PERSISTED, R_UH01, R_UH03, R_LOW, R
                K_UH = 12, K_01, K_MIN, K_03,
                M_UP = 16, M_DOWN, M_CLOUD, M_TOP, M_THERMAL, M_COLD, R_COUNT = 24 };
 // scr layout
-// S_CCOURANT: the three falling charges; S_R2M: two-moment rain's fall (mass and reflectivity speeds)
-enum Scratch { S_COURANT = 0, S_FILL = 4, S_CCOURANT = 11, S_R2M = 14, S_COUNT = 16 };
+// S_CCOURANT: the three falling charges; S_R2M, S_G2M, S_H2M: two-moment rain's, graupel's and hail's fall (mass and
+// reflectivity speeds)
+enum Scratch { S_COURANT = 0, S_FILL = 4, S_CCOURANT = 11, S_R2M = 14, S_G2M = 15, S_H2M = 16, S_COUNT = 18 };
 // cnt layout
 // C_TIMEOUT: a kernel's bounded wait for its own asynchronous copies ran out (the run is then failed too)
 enum Counter { C_CLIPPED = 0, C_STEPS = 1, C_FAILED = 2, C_TIMEOUT = 3, C_COUNT = 4 };

@@ -19,6 +19,7 @@
 #include "sg_physics.cuh"
 #include "sg_charge.cuh"
 #include "sg_rain2m.cuh"
+#include "sg_ice2m.cuh"
 #include "sg_kernels.h"
 #include "sg_device.cuh"
 
@@ -175,32 +176,44 @@ __global__ void k_fall_courant(const RunDesc* __restrict__ runs, const int4* ite
     if (R.flags & RF_EXTRA) {
       // the charge carriers' fall speeds (:1230-1234) from the step-start water, with rain's and snow's own (the
       // charge on rain falls with it; the charging reads the snow's), and the charges' Courant numbers; two-moment
-      // rain's mass-, number- and reflectivity-weighted speeds from both moments (:1224) and its Courant number (:973)
+      // rain's mass-, number- and reflectivity-weighted speeds from both moments (:1224) and its Courant number (:973);
+      // two-moment graupel's and hail's from their moments and density (:1226-1229), which the graupel-hail carrier
+      // falls with too
       const size_t n = R.n;
-      const bool elec = R.flags & RF_ELEC, two = R.flags & RF_RAIN2M;
+      const bool elec = R.flags & RF_ELEC, two = R.flags & RF_RAIN2M, ice2 = R.flags & RF_ICE2M;
       const float *ice = field(R, 0, ICE), *num = field(R, 0, RAIN_NUMBER);
       const float *cI = field(R, 0, CHARGE_ICE), *cG = field(R, 0, CHARGE_GRAUPEL), *cR = field(R, 0, CHARGE_RAIN);
-      float cc[4] = {0.f, 0.f, 0.f, 0.f};
+      const float *gn = field(R, 0, GRAUPEL_NUMBER), *gv = field(R, 0, GRAUPEL_VOLUME), *hn = field(R, 0, HAIL_NUMBER), *hv = field(R, 0, HAIL_VOLUME);
+      float cc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
       for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
         const int z = i / R.layer;
         const float rho = lvl(R, L_RHO, z), fsq = lvl(R, L_FALLSQ, z), k = R.dt * lvl(R, L_INV_HZ, z);
         const float a = rain[i], b = snow[i], g = graupel[i], h = hail[i], ic = ice[i];
         float vr, vn = 0.f, vz = 0.f;
         if (two) r2m::fallSpeeds(a, num[i], rho, vr, vn, vz); else vr = phys::rainFall(a, rho, fsq);
-        const float vs = phys::snowFall(b, rho, fsq), vg = phys::graupelFall(g, rho), vh = phys::hailFall(h, rho);
+        const float vs = phys::snowFall(b, rho, fsq);
+        float vg, vh;
+        if (ice2) {
+          float vgn, vgz, vhn, vhz;
+          i2m::momentSpeeds(i2m::GRAUPEL_2M(), g, gn[i], gv[i], rho, vg, vgn, vgz);
+          i2m::momentSpeeds(i2m::HAIL_2M(), h, hn[i], hv[i], rho, vh, vhn, vhz);
+          R.vfall[V_GRAUPEL * n + i] = vg; R.vfall[V_GRAUPEL_N * n + i] = vgn; R.vfall[V_GRAUPEL_Z * n + i] = vgz;
+          R.vfall[V_HAIL * n + i] = vh; R.vfall[V_HAIL_N * n + i] = vhn; R.vfall[V_HAIL_Z * n + i] = vhz;
+          cc[4] = fmaxf(cc[4], k * fmaxf(vgz, vg)); cc[5] = fmaxf(cc[5], k * fmaxf(vhz, vh));
+        } else { vg = phys::graupelFall(g, rho); vh = phys::hailFall(h, rho); }
         const float is = ic + b, gh = g + h;
         const float vi = is > 0.f ? b * vs / is : 0.f, vgh = gh > 0.f ? (g * vg + h * vh) / gh : 0.f;
-        R.vfall[i] = vi; R.vfall[n + i] = vgh; R.vfall[2 * n + i] = vr; R.vfall[3 * n + i] = vs;
-        if (two) { R.vfall[4 * n + i] = vn; R.vfall[5 * n + i] = vz; cc[3] = fmaxf(cc[3], k * fmaxf(vz, vr)); }
+        R.vfall[V_CHG_ICE * n + i] = vi; R.vfall[V_CHG_GRAUPEL * n + i] = vgh; R.vfall[V_RAIN * n + i] = vr; R.vfall[V_SNOW * n + i] = vs;
+        if (two) { R.vfall[V_RAIN_N * n + i] = vn; R.vfall[V_RAIN_Z * n + i] = vz; cc[3] = fmaxf(cc[3], k * fmaxf(vz, vr)); }
         if (elec) {
           if (cI[i] != 0.f) cc[0] = fmaxf(cc[0], k * vi);
           if (cG[i] != 0.f) cc[1] = fmaxf(cc[1], k * vgh);
           if (cR[i] != 0.f) cc[2] = fmaxf(cc[2], k * vr);
         }
       }
-      for (int f = 0; f < 4; f++) {
+      for (int f = 0; f < 6; f++) {
         float m = warpMax(cc[f]);
-        if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMaxPos(R.scr + (f < 3 ? S_CCOURANT + f : S_R2M), m);
+        if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMaxPos(R.scr + (f < 3 ? S_CCOURANT + f : f == 3 ? S_R2M : f == 4 ? S_G2M : S_H2M), m);
       }
     }
   }
@@ -232,7 +245,9 @@ __global__ void k_sediment(const RunDesc* __restrict__ runs, const int4* items, 
     float* precip = R.cols;
     float* hailGround = R.cols + layer;
     float* hailSize = R.cols + 2 * layer;
-    for (int f = (R.flags & RF_RAIN2M) ? 1 : 0; f < 4; f++) {  // sedimented(): two-moment rain falls on its own (:907-911)
+    // sedimented(): two-moment rain, graupel and hail fall on their own (:907-911)
+    const int fEnd = (R.flags & RF_ICE2M) ? GRAUPEL : 4;
+    for (int f = (R.flags & RF_RAIN2M) ? 1 : 0; f < fEnd; f++) {
       float* a = field(R, 0, f);
       const float courant = R.scr[S_COURANT + f];
       const int parts = max(1, (int)ceilf(courant / .8f));
@@ -278,7 +293,7 @@ __global__ void k_sediment(const RunDesc* __restrict__ runs, const int4* items, 
       const float dxy = R.dx * R.dy;
       for (int j = 0; j < 3; j++) {
         float* a = field(R, 0, CHARGE_ICE + j);
-        const float* vt = R.vfall + (size_t)j * R.n;
+        const float* vt = R.vfall + (size_t)(j == 2 ? V_RAIN : j) * R.n;
         const int parts = max(1, (int)ceilf(R.scr[S_CCOURANT + j] / .8f));
         if (!on) continue;
         bool any = false;
@@ -312,70 +327,102 @@ __global__ void k_sediment(const RunDesc* __restrict__ runs, const int4* items, 
   }
 }
 
-// Two-moment rain's fall (sedimentRain2m / sediment2m, :944-988; NSSL sediment1d, infall 4), one thread a column: the
-// mass with its mass-weighted speed, the number with its number-weighted one, a reflectivity and a number carried at
+// Two-moment fall (sedimentRain2m / sedimentIce2m / sediment2m, :898-988; NSSL sediment1d, infall 4), one thread a
+// column, for two-moment rain and then two-moment graupel and hail: the mass with its mass-weighted speed, the number
+// with its number-weighted one, an ice class's particle volume with the mass, a reflectivity and a number carried at
 // the mass's speed beside them; every sub-step the number is kept between what those two imply. Bottom-up, so each
 // face uses the values above from before the sub-step; the ground flux into the rain gauge. Sub-steps by the faster of
-// the reflectivity's and the mass's speed over the run.
+// the reflectivity's and the mass's speed over the run. Before two-moment hail falls, the hail reaching the ground and
+// its largest stones (collectHail, :697-711, with the two-moment speed and tail).
 __global__ void k_sediment_2m(const RunDesc* __restrict__ runs, const int4* items, int nitems) {
   extern __shared__ float sm[];
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
     if (R.cnt[C_FAILED] || !(R.flags & RF_RAIN2M)) continue;
     const int nz = R.nz, layer = R.layer, t = threadIdx.x;
-    float* sq = sm;                     // [nz][SED_COLS] each: mass, number, carried number, reflectivity, the speeds
+    float* sq = sm;                     // [nz][SED_COLS] each: mass, number, carried number, reflectivity, the speeds, volume
     float* sn = sq + nz * SED_COLS;
     float* sc = sn + nz * SED_COLS;
     float* sr = sc + nz * SED_COLS;
     float* vm = sr + nz * SED_COLS;
     float* vn = vm + nz * SED_COLS;
     float* vz = vn + nz * SED_COLS;
-    float* lrho = vz + nz * SED_COLS;   // [nz] rho0, 1/(rho0 h), 1/h
+    float* sv = vz + nz * SED_COLS;
+    float* lrho = sv + nz * SED_COLS;   // [nz] rho0, 1/(rho0 h), 1/h
     float* lk = lrho + nz;
     float* lh = lk + nz;
     for (int z = t; z < nz; z += blockDim.x) { lrho[z] = lvl(R, L_RHO, z); lk[z] = lvl(R, L_INV_RHO, z) * lvl(R, L_INV_HZ, z); lh[z] = lvl(R, L_INV_HZ, z); }
     __syncthreads();
     const int c = items[it].y * SED_COLS + t;
+    const int classes = (R.flags & RF_ICE2M) ? 3 : 1;
     if (t < SED_COLS && c < layer) {
-      float* q = field(R, 0, RAIN);
-      float* num = field(R, 0, RAIN_NUMBER);
       const size_t n = R.n;
-      bool any = false;
-      for (int z = 0; z < nz; z++) {
-        const int i = c + z * layer, s = z * SED_COLS + t;
-        sq[s] = q[i]; sn[s] = num[i]; vm[s] = R.vfall[2 * n + i]; vn[s] = R.vfall[4 * n + i]; vz[s] = R.vfall[5 * n + i];
-        any |= sq[s] != 0.f || sn[s] != 0.f;
-      }
-      if (any) {
-        const int parts = max(1, (int)ceilf(R.scr[S_R2M] / .8f));
+      for (int k = 0; k < classes; k++) {
+        // class k: rain (the drops' density, reflectivity factor G1), graupel, hail (their own density, bounded to
+        // 170-900 kg/m3 for the reflectivity, :920, and factor)
+        const bool ice = k > 0;
+        const i2m::IceClass cl = k == 1 ? i2m::GRAUPEL_2M() : i2m::HAIL_2M();
+        float* q = field(R, 0, k == 0 ? RAIN : k == 1 ? GRAUPEL : HAIL);
+        float* num = field(R, 0, k == 0 ? RAIN_NUMBER : k == 1 ? GRAUPEL_NUMBER : HAIL_NUMBER);
+        float* vol = ice ? field(R, 0, k == 1 ? GRAUPEL_VOLUME : HAIL_VOLUME) : nullptr;
+        const float* fm = R.vfall + (size_t)(k == 0 ? V_RAIN : k == 1 ? V_GRAUPEL : V_HAIL) * n;
+        const float* fn = R.vfall + (size_t)(k == 0 ? V_RAIN_N : k == 1 ? V_GRAUPEL_N : V_HAIL_N) * n;
+        const float* fz = R.vfall + (size_t)(k == 0 ? V_RAIN_Z : k == 1 ? V_GRAUPEL_Z : V_HAIL_Z) * n;
+        const float g1 = ice ? cl.g1 : r2m::G1;
+        auto k6 = [&](float qq, float vv) {
+          if (!ice) return r2m::K6;
+          const float d = 6.f / (phys::PI * fminf(900.f, fmaxf(170.f, i2m::densityOf(cl, qq, vv))));
+          return d * d;
+        };
+        if (k == 2) {
+          const float h = q[c];
+          if (h > 1e-9f) {
+            R.cols[layer + c] += R.rho0 * h * fm[c] * R.dt;
+            R.cols[2 * layer + c] = fmaxf(R.cols[2 * layer + c], i2m::largestDiameter(i2m::HAIL_2M(), h, num[c], vol[c], R.rho0) * 1000.f);
+          }
+        }
+        bool any = false;
+        for (int z = 0; z < nz; z++) {
+          const int i = c + z * layer, s = z * SED_COLS + t;
+          sq[s] = q[i]; sn[s] = num[i]; vm[s] = fm[i]; vn[s] = fn[i]; vz[s] = fz[i]; sv[s] = ice ? vol[i] : 0.f;
+          any |= sq[s] != 0.f || sn[s] != 0.f || sv[s] != 0.f;
+        }
+        if (!any) continue;
+        const int parts = max(1, (int)ceilf(R.scr[k == 0 ? S_R2M : k == 1 ? S_G2M : S_H2M] / .8f));
         const float step = R.dt / (float)parts;
         float* precip = R.cols;
         for (int p = 0; p < parts; p++) {
           for (int z = 0; z < nz; z++) {
             const int s = z * SED_COLS + t;
             const float rq = lrho[z] * sq[s], rn = lrho[z] * sn[s];
-            sr[s] = rq > 0.f && rn > 0.f ? r2m::G1 * r2m::K6 * rq * rq / rn : 0.f;
+            sr[s] = rq > 0.f && rn > 0.f ? g1 * k6(sq[s], sv[s]) * rq * rq / rn : 0.f;
             sc[s] = sn[s];
           }
           precip[c] += R.rho0 * sq[t] * vm[t] * step;
-          float inQ = 0.f, inN = 0.f, inC = 0.f, inR = 0.f;  // the fluxes into level z from above, from before this sub-step
+          float inQ = 0.f, inN = 0.f, inC = 0.f, inR = 0.f, inV = 0.f;  // the fluxes into level z from above, from before this sub-step
           for (int z = nz - 1; z >= 0; z--) {
             const int s = z * SED_COLS + t;
             const float oq = lrho[z] * sq[s] * vm[s], on = lrho[z] * sn[s] * vn[s], oc = lrho[z] * sc[s] * vm[s], orr = sr[s] * vz[s];
+            const float ov = lrho[z] * sv[s] * vm[s];
             sq[s] += step * (inQ - oq) * lk[z];
+            sv[s] += step * (inV - ov) * lk[z];
             sn[s] += step * (inN - on) * lk[z];
             sc[s] += step * (inC - oc) * lk[z];
             sr[s] += step * (inR - orr) * lh[z];
-            inQ = oq; inN = on; inC = oc; inR = orr;
+            inQ = oq; inN = on; inC = oc; inR = orr; inV = ov;
           }
           for (int z = 0; z < nz; z++) {
             const int s = z * SED_COLS + t;
-            if (!(sq[s] > r2m::RAIN_MIN)) { if (sq[s] < 0.f) sq[s] = 0.f; sn[s] = 0.f; continue; }
+            if (!(sq[s] > r2m::RAIN_MIN)) { if (sq[s] < 0.f) sq[s] = 0.f; sn[s] = 0.f; sv[s] = 0.f; continue; }
             const float rq = lrho[z] * sq[s];
-            sn[s] = sr[s] > 0.f ? fmaxf(fminf(r2m::G1 * r2m::K6 * rq * rq / sr[s] / lrho[z], sc[s]), sn[s]) : fmaxf(sc[s], sn[s]);
+            sn[s] = sr[s] > 0.f ? fmaxf(fminf(g1 * k6(sq[s], sv[s]) * rq * rq / sr[s] / lrho[z], sc[s]), sn[s]) : fmaxf(sc[s], sn[s]);
           }
         }
-        for (int z = 0; z < nz; z++) { const int i = c + z * layer, s = z * SED_COLS + t; q[i] = sq[s]; num[i] = sn[s]; }
+        for (int z = 0; z < nz; z++) {
+          const int i = c + z * layer, s = z * SED_COLS + t;
+          q[i] = sq[s]; num[i] = sn[s];
+          if (ice) vol[i] = sv[s];
+        }
       }
     }
     __syncthreads();  // the level tables are restaged for the block's next item
@@ -1338,7 +1385,7 @@ __global__ void k_fill_final(const RunDesc* __restrict__ runs, const int4* items
 // ELEC: the kernel of a batch with electrified runs, which also moves their charge with the water and charges the
 // graupel and crystals after the microphysics (:1454-1469); the charges go to set A (they are not mixed).
 template <bool ELEC>
-__global__ void __launch_bounds__(256, 3) k_physics(const RunDesc* __restrict__ runs, const int4* items, int nitems, int in, int mid) {
+__global__ void __launch_bounds__(256, ELEC ? 2 : 3) k_physics(const RunDesc* __restrict__ runs, const int4* items, int nitems, int in, int mid) {
   __shared__ double sh[32 * 4];
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
@@ -1373,8 +1420,14 @@ __global__ void __launch_bounds__(256, 3) k_physics(const RunDesc* __restrict__ 
       float before[4];
       if constexpr (ELEC) if (elec) { before[0] = s.ice + s.snow; before[1] = s.graupel + s.hail; before[2] = s.rain; before[3] = s.cloud; }
       float evap, rnum = 0.f;
+      i2m::Fields f2m = {0.f, 0.f, 0.f, 0.f};
+      bool wet2G = false, wet2H = false;
       if constexpr (ELEC) {
-        if (R.flags & RF_RAIN2M) {
+        if (R.flags & RF_ICE2M) {
+          rnum = field(R, in, RAIN_NUMBER)[i];
+          f2m = {field(R, in, GRAUPEL_NUMBER)[i], field(R, in, GRAUPEL_VOLUME)[i], field(R, in, HAIL_NUMBER)[i], field(R, in, HAIL_VOLUME)[i]};
+          i2m::microphysics(s, rnum, f2m, pl, dt, R.flags, R.breakup, evap, wet2G, wet2H);
+        } else if (R.flags & RF_RAIN2M) {
           rnum = field(R, in, RAIN_NUMBER)[i];
           r2m::microphysics(s, rnum, pl, dt, R.flags, R.breakup, evap);
         } else phys::microphysics(s, pl, dt, R.flags, evap);
@@ -1384,9 +1437,20 @@ __global__ void __launch_bounds__(256, 3) k_physics(const RunDesc* __restrict__ 
         float c[4] = {field(R, in, CHARGE_ICE)[i], field(R, in, CHARGE_GRAUPEL)[i], field(R, in, CHARGE_RAIN)[i], field(R, in, CHARGE_AIR)[i]};
         if (c[0] != 0.f || c[1] != 0.f || c[2] != 0.f || c[3] != 0.f) charge::transferCharge(c, before, after);
         const float tc = phys::tcOf(s, pl.exner), rho = pl.rho;
-        const bool wetG = charge::wetGrowing(s.graupel, phys::N0G, phys::RHO_G, tc, s, pl), wetH = charge::wetGrowing(s.hail, phys::N0H, phys::RHO_H, tc, s, pl);
-        const float separated = charge::chargingRate(tc, rho, s.cloud, s.ice, s.snow, s.graupel, s.hail, R.vfall[3 * (size_t)R.n + i], wetG, wetH, s.inum * rho) * dt / rho;
-        const float induced = charge::inductiveRate(tc, rho, s.cloud, s.graupel, s.hail, R.ez[i], (c[1] + separated) * rho, wetG, wetH) * dt / rho;
+        // two-moment graupel and hail: their wet growth from their processes, their charging by their own moments
+        // (:1461-1466; a class without particles charges by the fixed intercept's)
+        bool wetG, wetH;
+        charge::Moments two[2];
+        int has = 0;
+        if (R.flags & RF_ICE2M) {
+          wetG = wet2G; wetH = wet2H;
+          if (i2m::rimerMoments(i2m::GRAUPEL_2M(), s.graupel, f2m.gn, f2m.gv, rho, two[0])) has |= 1;
+          if (i2m::rimerMoments(i2m::HAIL_2M(), s.hail, f2m.hn, f2m.hv, rho, two[1])) has |= 2;
+        } else {
+          wetG = charge::wetGrowing(s.graupel, phys::N0G, phys::RHO_G, tc, s, pl); wetH = charge::wetGrowing(s.hail, phys::N0H, phys::RHO_H, tc, s, pl);
+        }
+        const float separated = charge::chargingRate(tc, rho, s.cloud, s.ice, s.snow, s.graupel, s.hail, R.vfall[V_SNOW * (size_t)R.n + i], wetG, wetH, s.inum * rho, two, has) * dt / rho;
+        const float induced = charge::inductiveRate(tc, rho, s.cloud, s.graupel, s.hail, R.ez[i], (c[1] + separated) * rho, wetG, wetH, two, has) * dt / rho;
         field(R, 0, CHARGE_ICE)[i] = c[0] - separated; field(R, 0, CHARGE_GRAUPEL)[i] = c[1] + separated + induced;
         field(R, 0, CHARGE_RAIN)[i] = c[2]; field(R, 0, CHARGE_AIR)[i] = c[3] - induced;
         df_add_prod(whi[NW - 1], wlo[NW - 1], lvl(R, L_NODEMASS, z), lvl(R, L_NODEMASS_LO, z), fabsf(separated) + fabsf(induced));
@@ -1415,6 +1479,9 @@ __global__ void __launch_bounds__(256, 3) k_physics(const RunDesc* __restrict__ 
       field(R, mid, U)[i] = u; field(R, mid, V)[i] = v; field(R, mid, W)[i] = w; field(R, mid, THETA)[i] = s.thp;
       field(R, mid, Q)[i] = s.q; field(R, mid, CLOUD)[i] = s.cloud; field(R, mid, ICE)[i] = s.ice; field(R, mid, ICENUM)[i] = s.inum;
       if constexpr (ELEC) if (R.flags & RF_RAIN2M) field(R, 0, RAIN_NUMBER)[i] = rnum;  // not mixed: straight to set A
+      if constexpr (ELEC) if (R.flags & RF_ICE2M) {
+        field(R, 0, GRAUPEL_NUMBER)[i] = f2m.gn; field(R, 0, GRAUPEL_VOLUME)[i] = f2m.gv; field(R, 0, HAIL_NUMBER)[i] = f2m.hn; field(R, 0, HAIL_VOLUME)[i] = f2m.hv;
+      }
     }
     if (__syncthreads_or(bad) && threadIdx.x == 0) atomicExch(&R.cnt[C_FAILED], 1ull);
     size_t nch = (R.n + CHUNK - 1) / CHUNK;
@@ -1747,7 +1814,7 @@ void launch_pres_correct(const Launch& L, int set, int final_) {
 void launch_fill_partial(const Launch& L, int set) { k_fill_partial<<<GRID(L.n, L.cap), 128, 0, L.stream>>>(L.runs, L.items, L.n, set); }
 void launch_fill_final(const Launch& L) { k_fill_final<<<GRID(L.n, L.cap), 32, 0, L.stream>>>(L.runs, L.items, L.n); }
 void launch_sediment_2m(const Launch& L, int maxnz) {
-  k_sediment_2m<<<GRID(L.n, L.cap), SED_COLS, (7 * maxnz * SED_COLS + 3 * maxnz) * sizeof(float), L.stream>>>(L.runs, L.items, L.n);
+  k_sediment_2m<<<GRID(L.n, L.cap), SED_COLS, (8 * maxnz * SED_COLS + 3 * maxnz) * sizeof(float), L.stream>>>(L.runs, L.items, L.n);
 }
 void launch_physics(const Launch& L, int in, int mid, bool elec) {
   if (elec) k_physics<true><<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, in, mid);
@@ -1760,6 +1827,10 @@ void launch_mix(const Launch& L, int in, int TX, int TY) {
 }
 void launch_step_end(const Launch& L) { k_step_end<<<GRID(L.n, L.cap), 64, 0, L.stream>>>(L.runs, L.items, L.n); }
 void launch_divergence_max(const Launch& L, int set, double* out) { k_divergence_max<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set, out); }
+
+// The constant tables the kernels read that are made on the host: the Seifert-Beheng sweep coefficients of two-moment
+// graupel and hail (FP64, then rounded).
+cudaError_t upload_tables() { return cudaMemcpyToSymbol(i2m::c_sweep, &i2m::h_sweep, sizeof(i2m::SweepTable)); }
 
 cudaError_t set_smem_limits(int bytes) {
   cudaError_t e;

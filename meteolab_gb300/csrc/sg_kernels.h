@@ -70,6 +70,7 @@ void launch_rotation_columns(const Launch& cols, int refresh);
 void launch_rotation_summary(const Launch& runs, int refresh);
 void launch_diag_sample(const Launch& L);
 cudaError_t set_smem_limits(int bytes);
+cudaError_t upload_tables();
 // With `device` current: loads the module of sg_divergence_max_static and resolves its static scratch (sg_static.cu).
 int static_prepare(int device);
 cudaError_t set_transport_smem_limits(int bytes);  // (sg_transport.cu)

@@ -51,7 +51,7 @@ Layout layout(int nx, int ny, int nz, int flags = 0) {
   L.acc = take(A_COUNT * 8); L.cnt = take(C_COUNT * 8);
   L.items = take(nch * 16);  // the run's own per-node work items (field conversions outside a batch plan)
   L.diag = take((size_t)DG_COUNT * layer * 4); L.rot = take(R_COUNT * 8);
-  if (extra) { L.vfall = take(6 * n * 4); L.ez = take(n * 4); L.cpart = take(((layer + 63) / 64) * 8); }
+  if (extra) { L.vfall = take(((flags & RF_ICE2M) ? 12 : 6) * n * 4); L.ez = take(n * 4); L.cpart = take(((layer + 63) / 64) * 8); }
   if (elec) L.lgt = take(lightning_bytes(nx, ny, nz));
   L.total = o;
   return L;
@@ -316,6 +316,7 @@ int validate(sg_context* ctx, const sg_grid* g, const sg_base_state* b, const sg
     return fail(ctx, SG_ERR_UNSUPPORTED, "grid beyond 55 million nodes");
   if (sw->rain_moments != 1 && sw->rain_moments != 2) return fail(ctx, SG_ERR_INVALID, "rain_moments must be 1 or 2");
   if (sw->rain_breakup < 0 || sw->rain_breakup > 2) return fail(ctx, SG_ERR_INVALID, "rain_breakup must be 0 (none), 1 (NSSL) or 2 (Morrison)");
+  if (sw->ice_moments != 1 && sw->ice_moments != 2) return fail(ctx, SG_ERR_INVALID, "ice_moments must be 1 or 2");
   int rad[8];
   if (fft_plan_factors(g->nx, rad) < 0 || fft_plan_factors(g->ny, rad) < 0) return fail(ctx, SG_ERR_UNSUPPORTED, "nx or ny has more than 8 prime factors");
   if (!(g->dx > 0 && g->dy > 0 && g->height > 0) || !g->zs || !g->dzs || !g->hz) return fail(ctx, SG_ERR_INVALID, "bad grid spacing or levels");
@@ -358,6 +359,7 @@ void charge_items(sg_context* ctx, const std::vector<int>& slots, int TX, int TY
     const int tiles = ((r.nx + TX - 1) / TX) * ((r.ny + TY - 1) / TY);
     if (r.desc.flags & RF_ELEC) for (int g = 13; g < 17; g++) for (int t = 0; t < tiles; t++) out.push_back(make_int4(s, g, t, 0));
     if (r.desc.flags & RF_RAIN2M) for (int t = 0; t < tiles; t++) out.push_back(make_int4(s, 17, t, 0));
+    if (r.desc.flags & RF_ICE2M) for (int g = 18; g < 22; g++) for (int t = 0; t < tiles; t++) out.push_back(make_int4(s, g, t, 0));
   }
 }
 
@@ -822,7 +824,7 @@ int sg_context_create(int device, uint64_t hbm_budget_bytes, sg_context** out) {
   if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess ||
       (e = cudaMalloc(&ctx->d_runs, MAX_SLOTS * sizeof(RunDesc))) != cudaSuccess ||
       (e = cudaMalloc(&ctx->d_scalar, 64 * sizeof(double))) != cudaSuccess ||
-      (e = set_smem_limits(ctx->maxSmem)) != cudaSuccess) {
+      (e = set_smem_limits(ctx->maxSmem)) != cudaSuccess || (e = upload_tables()) != cudaSuccess) {
     delete ctx; return SG_ERR_DEVICE;
   }
   for (int k = 0; k < 2; k++)
@@ -867,11 +869,18 @@ cudaStream_t sg_context_stream(sg_context* ctx) { return ctx->stream; }
 int sg_context_fail(sg_context* ctx, int code, const char* message) { return fail(ctx, code, message); }
 extern "C" {
 
+}  // extern "C"
+// The extra-field flags of a run: electrified() (src/core/model.ts:1316), rain2m() (:905), ice2m() (:914).
+static int run_flags(const sg_switches* sw) {
+  const bool two = sw->rain_moments == 2;
+  return (sw->lightning && sw->ice ? RF_ELEC : 0) | (two ? RF_RAIN2M : 0) | (two && sw->ice && sw->ice_moments == 2 ? RF_ICE2M : 0);
+}
+extern "C" {
+
 uint64_t sg_run_bytes(const sg_grid* grid) { return grid ? layout(grid->nx, grid->ny, grid->nz).total : 0; }
 uint64_t sg_run_bytes_for(const sg_grid* grid, const sg_switches* sw) {
   if (!grid || !sw) return 0;
-  const int flags = (sw->lightning && sw->ice ? RF_ELEC : 0) | (sw->rain_moments == 2 ? RF_RAIN2M : 0);
-  return layout(grid->nx, grid->ny, grid->nz, flags).total;
+  return layout(grid->nx, grid->ny, grid->nz, run_flags(sw)).total;
 }
 
 int sg_run_create(sg_context* ctx, const sg_grid* g, const sg_base_state* b, const sg_switches* sw, const float* const* init, sg_run* out) {
@@ -879,9 +888,9 @@ int sg_run_create(sg_context* ctx, const sg_grid* g, const sg_base_state* b, con
   int st = validate(ctx, g, b, sw);
   if (st) return st;
   cudaSetDevice(ctx->device);
-  const bool elec = sw->lightning && sw->ice;  // electrified() (src/core/model.ts:1316)
-  const bool two = sw->rain_moments == 2;      // rain2m() (:905)
-  Layout Lo = layout(g->nx, g->ny, g->nz, (elec ? RF_ELEC : 0) | (two ? RF_RAIN2M : 0));
+  const int xflags = run_flags(sw);
+  const bool elec = xflags & RF_ELEC, two = xflags & RF_RAIN2M;
+  Layout Lo = layout(g->nx, g->ny, g->nz, xflags);
   // Admission by the HBM budget (pooled allocations of a retired run count as free).
   char* mem = nullptr;
   auto pit = ctx->pool.find(Lo.total);
@@ -908,8 +917,7 @@ int sg_run_create(sg_context* ctx, const sg_grid* g, const sg_base_state* b, con
   build_tables(g, b, sw, T, d);
   d.slot = slot;
   d.nf = elec || two ? NFE : NF;
-  if (elec) d.flags |= RF_ELEC;
-  if (two) d.flags |= RF_RAIN2M;
+  d.flags |= xflags;
   d.breakup = sw->rain_breakup;
   d.fld = (float*)(mem + Lo.fld); d.faces = (float*)(mem + Lo.faces); d.kmkh = (float*)(mem + Lo.kmkh); d.phi = (float*)(mem + Lo.phi);
   d.pres = (float*)(mem + Lo.pres); d.pres2 = (float*)(mem + Lo.pres2); d.spec = (float2*)(mem + Lo.spec); d.cols = (float*)(mem + Lo.cols);
@@ -958,6 +966,13 @@ int sg_run_create(sg_context* ctx, const sg_grid* g, const sg_base_state* b, con
   return SG_OK;
 }
 
+// Whether a field mask names only fields the run carries.
+static bool mask_fits(const Run& r, uint32_t mask) {
+  const int f = r.desc.flags;
+  return !(mask >> r.desc.nf) && !((mask & SG_CHARGE_FIELDS) && !(f & RF_ELEC)) && !((mask & (1u << SG_RAIN_NUMBER)) && !(f & RF_RAIN2M)) &&
+         !((mask & SG_ICE2M_FIELDS) && !(f & RF_ICE2M));
+}
+
 int sg_run_write_fields(sg_context* ctx, sg_run run, uint32_t mask, const float* const* host) {
   if (!ctx || !host) return SG_ERR_INVALID;
   Run* r = find(ctx, run);
@@ -965,8 +980,9 @@ int sg_run_write_fields(sg_context* ctx, sg_run run, uint32_t mask, const float*
   cudaSetDevice(ctx->device);
   size_t n = (size_t)r->nx * r->ny * r->nz;
   const int nf = r->desc.nf;
-  if ((mask >> nf) || ((mask & SG_CHARGE_FIELDS) && !(r->desc.flags & RF_ELEC)) || ((mask & (1u << SG_RAIN_NUMBER)) && !(r->desc.flags & RF_RAIN2M)))
-    return fail(ctx, SG_ERR_INVALID, "field mask beyond the run's fields (the charges need an electrified run, the drop number two-moment rain)");
+  if (!mask_fits(*r, mask))
+    return fail(ctx, SG_ERR_INVALID, "field mask beyond the run's fields (the charges need an electrified run, the drop number two-moment rain, "
+                                     "the graupel and hail numbers and volumes two-moment ice)");
   for (int f = 0; f < nf; f++) {
     if (!(mask & (1u << f))) continue;
     if (!host[f]) return fail(ctx, SG_ERR_INVALID, "null field pointer");
@@ -986,8 +1002,9 @@ int sg_run_read_fields(sg_context* ctx, sg_run run, uint32_t mask, float* const*
   cudaSetDevice(ctx->device);
   size_t n = (size_t)r->nx * r->ny * r->nz;
   const int nf = r->desc.nf;
-  if ((mask >> nf) || ((mask & SG_CHARGE_FIELDS) && !(r->desc.flags & RF_ELEC)) || ((mask & (1u << SG_RAIN_NUMBER)) && !(r->desc.flags & RF_RAIN2M)))
-    return fail(ctx, SG_ERR_INVALID, "field mask beyond the run's fields (the charges need an electrified run, the drop number two-moment rain)");
+  if (!mask_fits(*r, mask))
+    return fail(ctx, SG_ERR_INVALID, "field mask beyond the run's fields (the charges need an electrified run, the drop number two-moment rain, "
+                                     "the graupel and hail numbers and volumes two-moment ice)");
   if (mask & (1u << THETA)) launch_theta_out(node_launch(ctx, *r), field(r->desc, 1, THETA));
   for (int f = 0; f < nf; f++) {
     if (!(mask & (1u << f))) continue;
@@ -1222,12 +1239,15 @@ int sg_run_save_state(sg_context* ctx, sg_run run, const char* config_json, doub
   const size_t n = (size_t)r->nx * r->ny * r->nz, layer = (size_t)r->nx * r->ny, off = state::data_offset(json.size());
   std::vector<float> fields((size_t)SG_NFIELDS * n), cols(3 * layer);
   if ((st = sg_batch_read_packed(ctx, &run, 1, SG_ALL_FIELDS, fields.data())) != SG_OK) return st;
-  // the extra fields the run carries (an electrified run's charges, a two-moment run's drop number)
-  std::vector<float> extra(5 * n, 0.f);
-  const uint32_t xmask = (r->lgt ? SG_CHARGE_FIELDS : 0u) | ((r->desc.flags & RF_RAIN2M) ? 1u << SG_RAIN_NUMBER : 0u);
+  // the extra fields the run carries (an electrified run's charges, a two-moment run's drop number, graupel and hail
+  // numbers and volumes)
+  constexpr int NX = SG_NFIELDS_EXTRA - SG_CHARGE_ICE;
+  std::vector<float> extra(NX * n, 0.f);
+  const uint32_t xmask = (r->lgt ? SG_CHARGE_FIELDS : 0u) | ((r->desc.flags & RF_RAIN2M) ? 1u << SG_RAIN_NUMBER : 0u) |
+                         ((r->desc.flags & RF_ICE2M) ? SG_ICE2M_FIELDS : 0u);
   if (xmask) {
     float* ptr[SG_NFIELDS_EXTRA] = {};
-    for (int k = 0; k < 5; k++) ptr[SG_CHARGE_ICE + k] = extra.data() + (size_t)k * n;
+    for (int k = 0; k < NX; k++) ptr[SG_CHARGE_ICE + k] = extra.data() + (size_t)k * n;
     if ((st = sg_run_read_fields(ctx, run, xmask, ptr)) != SG_OK) return st;
   }
   if ((st = sg_run_read_columns(ctx, run, cols.data(), cols.data() + layer, cols.data() + 2 * layer)) != SG_OK) return st;
@@ -1261,7 +1281,7 @@ int sg_run_load_state(sg_context* ctx, sg_run run, const uint8_t* image, size_t 
     return fail(ctx, SG_ERR_INVALID, "the file's grid is " + std::to_string(h.nx) + "x" + std::to_string(h.ny) + "x" + std::to_string(h.nz) +
                                          ", the run's " + std::to_string(r->nx) + "x" + std::to_string(r->ny) + "x" + std::to_string(r->nz));
   const size_t n = (size_t)r->nx * r->ny * r->nz, layer = (size_t)r->nx * r->ny;
-  std::vector<float> fields((size_t)SG_NFIELDS * n, 0.f), cols(3 * layer), extra(5 * n, 0.f);
+  std::vector<float> fields((size_t)SG_NFIELDS * n, 0.f), cols(3 * layer), extra((size_t)(SG_NFIELDS_EXTRA - SG_CHARGE_ICE) * n, 0.f);
   for (int k = 0; k < h.nfields; k++) {
     const int f = state::carried_of(k);
     if (f >= 0 && f < SG_NFIELDS) std::memcpy(fields.data() + (size_t)f * n, image + h.data_offset + (size_t)k * n * 4, n * 4);
@@ -1277,6 +1297,13 @@ int sg_run_load_state(sg_context* ctx, sg_run run, const uint8_t* image, size_t 
     const float* ptr[SG_NFIELDS_EXTRA] = {};
     ptr[SG_RAIN_NUMBER] = extra.data() + (size_t)(SG_RAIN_NUMBER - SG_CHARGE_ICE) * n;
     if ((st = sg_run_write_fields(ctx, run, 1u << SG_RAIN_NUMBER, ptr)) != SG_OK) return st;
+  }
+  if (r->desc.flags & RF_ICE2M) {
+    // two-moment graupel and hail: the file's numbers and volumes (none before version 5: the first step's bounding
+    // rebuilds them from the mass, as boundedIceNumber and the class's density without a volume do, state.ts:14)
+    const float* ptr[SG_NFIELDS_EXTRA] = {};
+    for (int k = SG_GRAUPEL_NUMBER; k <= SG_HAIL_VOLUME; k++) ptr[k] = extra.data() + (size_t)(k - SG_CHARGE_ICE) * n;
+    if ((st = sg_run_write_fields(ctx, run, SG_ICE2M_FIELDS, ptr)) != SG_OK) return st;
   }
   if (r->lgt) {
     // an electrified run: the file's charge (none in a version-1 file), its ground charge, flash counts and charge budget

@@ -173,7 +173,8 @@ int carried_of(int k) {
   // STATE_FIELDS (state.ts:9): u v w theta q cloud rain cold ice snow graupel hail, chargeIce chargeGraupel chargeRain
   // chargeAir, iceNumber, rainNumber, graupelNumber graupelVolume hailNumber hailVolume
   static const int map[NSTATE] = {SG_U, SG_V, SG_W, SG_THETA, SG_Q, SG_CLOUD, SG_RAIN, SG_COLD, SG_ICE, SG_SNOW, SG_GRAUPEL, SG_HAIL,
-                                  SG_CHARGE_ICE, SG_CHARGE_GRAUPEL, SG_CHARGE_RAIN, SG_CHARGE_AIR, SG_ICE_NUMBER, SG_RAIN_NUMBER, -1, -1, -1, -1};
+                                  SG_CHARGE_ICE, SG_CHARGE_GRAUPEL, SG_CHARGE_RAIN, SG_CHARGE_AIR, SG_ICE_NUMBER, SG_RAIN_NUMBER,
+                                  SG_GRAUPEL_NUMBER, SG_GRAUPEL_VOLUME, SG_HAIL_NUMBER, SG_HAIL_VOLUME};
   return k >= 0 && k < NSTATE ? map[k] : -1;
 }
 

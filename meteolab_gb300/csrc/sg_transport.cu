@@ -26,14 +26,15 @@ constexpr int TMAXC = 4;  // plane cells per thread: (TX + 6)(TY + 6) <= TMAXC *
 // face values, thb, qb, thv_env (dynamics).
 constexpr int tlv_rows(int kind) { return kind == TK_DYN ? 9 : 2; }
 // Field groups of the transport work items: 0-2 the WENO fields in threes, 3 the dynamics {u, v, w, theta'}, 4-12
-// the WENO fields one by one, 13-16 the charge carriers of an electrified run and 17 the raindrop number of a
-// two-moment run, one by one.
-constexpr int TGROUPS = 18;
+// the WENO fields one by one, 13-16 the charge carriers of an electrified run, 17 the raindrop number of a two-moment
+// run and 18-21 the graupel and hail numbers and volumes of a two-moment ice run, one by one.
+constexpr int TGROUPS = 22;
 __constant__ int TGROUP[TGROUPS][4] = {{RAIN, SNOW, GRAUPEL, -1}, {HAIL, Q, CLOUD, -1}, {ICE, ICENUM, COLD, -1}, {U, V, W, THETA},
                                        {RAIN, -1, -1, -1}, {SNOW, -1, -1, -1}, {GRAUPEL, -1, -1, -1}, {HAIL, -1, -1, -1},
                                        {Q, -1, -1, -1}, {CLOUD, -1, -1, -1}, {ICE, -1, -1, -1}, {ICENUM, -1, -1, -1}, {COLD, -1, -1, -1},
                                        {CHARGE_ICE, -1, -1, -1}, {CHARGE_GRAUPEL, -1, -1, -1}, {CHARGE_RAIN, -1, -1, -1}, {CHARGE_AIR, -1, -1, -1},
-                                       {RAIN_NUMBER, -1, -1, -1}};
+                                       {RAIN_NUMBER, -1, -1, -1}, {GRAUPEL_NUMBER, -1, -1, -1}, {GRAUPEL_VOLUME, -1, -1, -1},
+                                       {HAIL_NUMBER, -1, -1, -1}, {HAIL_VOLUME, -1, -1, -1}};
 
 // Two faces at once on the packed FP32 pipes (bit-identical per face to the scalar weno5 / upwind5).
 struct Op2 {

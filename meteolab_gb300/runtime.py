@@ -14,7 +14,7 @@ from typing import Dict, Iterable, List, Optional, Sequence
 
 import numpy as np
 
-from .scenarios import CARRIED, CHARGES, RunSpec
+from .scenarios import CARRIED, CHARGES, ICE2M, RunSpec
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libstormgpu.so")
@@ -81,7 +81,9 @@ class SgCounters(C.Structure):
 
 _lib = None
 _lock = threading.Lock()
-ALL_FIELDS = tuple(CARRIED) + tuple(CHARGES) + ("rainNumber",)  # field ids of the C ABI (charges: electrified runs; drop number: two-moment)
+# field ids of the C ABI (charges: electrified runs; drop number: two-moment rain; graupel and hail numbers and volumes:
+# two-moment ice)
+ALL_FIELDS = tuple(CARRIED) + tuple(CHARGES) + ("rainNumber",) + tuple(ICE2M)
 _FP = C.POINTER(C.c_float)
 
 
@@ -366,7 +368,7 @@ class Run:
         self.id = rid.value
         self.time = 0.0
         self.live = True
-        extra = {k: v for k, v in spec.fields.items() if k in CHARGES or k == "rainNumber"}
+        extra = {k: v for k, v in spec.fields.items() if k in CHARGES or k == "rainNumber" or k in ICE2M}
         if extra:
             self.write(extra)
 

@@ -24,6 +24,8 @@ from .grid import Grid
 CARRIED = ("rain", "snow", "graupel", "hail", "u", "v", "w", "theta", "q", "cloud", "ice", "iceNumber", "cold")
 # the charge carriers of an electrified run, C/kg (field ids 13-16 of the C ABI; src/core/model.ts:210)
 CHARGES = ("chargeIce", "chargeGraupel", "chargeRain", "chargeAir")
+# two-moment graupel and hail (src/core/model.ts:202): particles per kg and particle volume, m3 per kg
+ICE2M = ("graupelNumber", "graupelVolume", "hailNumber", "hailVolume")
 #: The fields the subgrid turbulence mixes (src/core/model.ts:1338-1344).
 MIXED = ("u", "v", "w", "theta", "q", "cloud", "ice", "iceNumber")
 SMAGORINSKY = 0.18
@@ -297,3 +299,19 @@ def marshall_palmer_number(rain: np.ndarray, rho: np.ndarray) -> np.ndarray:
     xv = np.clip(q[wet] / (1000.0 * n), math.pi / 6 * 80e-6 ** 3, math.pi / 6 * 6e-3 ** 3 / (64 / 6))
     out[wet] = q[wet] / (1000.0 * xv)
     return out.astype(np.float32)
+
+
+def exponential_ice_moments(q: np.ndarray, rho: np.ndarray, kind: str):
+    """Number (per kg) and particle volume (m3 per kg) of two-moment graupel or hail started as the one-moment class of the
+    same mass: the exponential distribution of its fixed intercept and density (graupel N0 4e4 m^-4 at 400 kg/m3, hail
+    N0 4e4 at 900; src/core/graupel.ts, hail.ts), so the number is N0 / lambda and the volume q / density, as the
+    reference's own comparison of the two schemes sets it (ice2m.test.ts:92-98). `rho` is each node's air density."""
+    n0, density = {"graupel": (4e4, 400.0), "hail": (4e4, 900.0)}[kind]
+    q = np.asarray(q, np.float64)
+    rho = np.asarray(rho, np.float64)
+    number, volume = np.zeros_like(q), np.zeros_like(q)
+    some = q > 1e-12
+    lam = (math.pi * density * n0 / (rho[some] * q[some])) ** .25
+    number[some] = n0 / lam / rho[some]
+    volume[some] = q[some] / density
+    return number.astype(np.float32), volume.astype(np.float32)

@@ -359,6 +359,19 @@ double orc_microphysics(float* v, double exner, double p, double rho, double rho
   return microphysicsNode<float>(a, a + 1, a + 2, a + 3, a + 9, a + 4, a + 5, a + 6, a + 7, a + 8, 0, exner, p, rho, rhoGround, dt, sw);
 }
 
+// The microphysics of a node with two-moment rain, graupel and hail: v = theta, q, cloud, rain, ice, iceNumber, snow,
+// graupel, hail, cold, rainNumber, graupelNumber, graupelVolume, hailNumber, hailVolume (FP32 cells, in place); flags as
+// orc_microphysics (ice on); wet2 = graupel's and hail's wet growth. Returns the evaporated rain.
+double orc_microphysics_2m(float* v, double exner, double p, double rho, double rhoGround, double dt, int flags, int* wet2) {
+  Switches sw; sw.ice = true; sw.evaporation = (flags & 2) != 0; sw.rainFormation = (flags & 4) != 0; sw.rainMoments = 2; sw.iceMoments = 2;
+  Arr<float> a = (Arr<float>)v;
+  i2m::Fields<float> f = {a, a + 1, a + 2, a + 4, a + 5, a + 6, a + 3, a + 10, a + 7, a + 11, a + 12, a + 8, a + 13, a + 14};
+  i2m::Result r = {0, false, false};
+  double e = microphysicsNode<float>(a, a + 1, a + 2, a + 3, a + 9, a + 4, a + 5, a + 6, a + 7, a + 8, 0, exner, p, rho, rhoGround, dt, sw, a + 10, &f, &r);
+  wet2[0] = r.wetG; wet2[1] = r.wetH;
+  return e;
+}
+
 // The same on FP64 cells (the pure FP64 oracle's arithmetic and storage).
 double orc_microphysics64(double* v, double exner, double p, double rho, double rhoGround, double dt, int flags) {
   Switches sw; sw.ice = flags & 1; sw.evaporation = (flags & 2) != 0; sw.rainFormation = (flags & 4) != 0;

@@ -75,6 +75,8 @@ def lib():
             L.orc_cell.argtypes = [C.c_int, _f, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double]
             L.orc_microphysics.restype = C.c_double
             L.orc_microphysics.argtypes = [_f, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int]
+            L.orc_microphysics_2m.restype = C.c_double
+            L.orc_microphysics_2m.argtypes = [_f, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, C.POINTER(C.c_int)]
             L.orc_microphysics64.restype = C.c_double
             L.orc_microphysics64.argtypes = [_d, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int]
             L.orc_fft.argtypes = [C.c_int, _d, _d, C.c_int]

@@ -11,6 +11,7 @@
 #include "../../meteolab_gb300/csrc/sg_tile_copies.cuh"
 #include "../../meteolab_gb300/csrc/sg_charge.cuh"
 #include "../../meteolab_gb300/csrc/sg_rain2m.cuh"
+#include "../../meteolab_gb300/csrc/sg_ice2m.cuh"
 
 using namespace sg;
 
@@ -27,6 +28,38 @@ float ht_r2m_processes(float* v, double tk, double p, double rho, float dt, int 
   return evap;
 }
 void ht_r2m_fall(float q, float n, float rho, float* out) { r2m::fallSpeeds(q, n, rho, out[0], out[1], out[2]); }
+
+// two-moment graupel and hail (sg_ice2m.cuh), FP32; class c 0 graupel, 1 hail
+static i2m::IceClass cls(int c) { return c == 0 ? i2m::GRAUPEL_2M() : i2m::HAIL_2M(); }
+void ht_i2m_speeds(int c, float q, float n, float vol, float rho, float* out3) { i2m::momentSpeeds(cls(c), q, n, vol, rho, out3[0], out3[1], out3[2]); }
+float ht_i2m_largest(int c, float q, float n, float vol, float rho) { return i2m::largestDiameter(cls(c), q, n, vol, rho); }
+int ht_i2m_rimer(int c, float q, float n, float vol, float rho, float* out5) {
+  charge::Moments m;
+  if (!i2m::rimerMoments(cls(c), q, n, vol, rho, m)) return 0;
+  out5[0] = m.n; out5[1] = m.d1; out5[2] = m.d2; out5[3] = m.fall; out5[4] = m.d2v;
+  return 1;
+}
+void ht_i2m_sweep(int c, int pair, float* out3) { out3[0] = i2m::h_sweep.a[c][pair]; out3[1] = i2m::h_sweep.b[c][pair]; out3[2] = i2m::h_sweep.c[c][pair]; }
+// the node's microphysics with two-moment rain, graupel and hail: v = thp, thb, q, cloud, rain, ice, inum, snow, graupel,
+// hail, cold, rainNumber, graupelNumber, graupelVolume, hailNumber, hailVolume (in place); wet2 = wet growth
+float ht_microphysics_2m(float* v, double exner, double p, double rho, double rho0, float dt, int flags, int* wet2) {
+  phys::Level L = phys::makeLevel((double)v[1], exner, p, rho, rho0);
+  phys::Node s{v[0], v[1], L.tcb, v[2], v[3], v[4], v[5], v[6], v[7], v[8], v[9], v[10]};
+  float rn = v[11], evap = 0.f;
+  i2m::Fields f = {v[12], v[13], v[14], v[15]};
+  bool wg = false, wh = false;
+  i2m::microphysics(s, rn, f, L, dt, flags, 0, evap, wg, wh);
+  v[0] = s.thp; v[2] = s.q; v[3] = s.cloud; v[4] = s.rain; v[5] = s.ice; v[6] = s.inum; v[7] = s.snow; v[8] = s.graupel; v[9] = s.hail; v[10] = s.cold;
+  v[11] = rn; v[12] = f.gn; v[13] = f.gv; v[14] = f.hn; v[15] = f.hv;
+  wet2[0] = wg; wet2[1] = wh;
+  return evap;
+}
+float ht_charging_2m(float tc, float rho, float cloud, float ice, float snow, float graupel, float hail, float snowFall, float crystals,
+                     const float* m10, int has) {
+  charge::Moments two[2];
+  for (int j = 0; j < 2; j++) two[j] = {m10[5 * j], m10[5 * j + 1], m10[5 * j + 2], m10[5 * j + 3], m10[5 * j + 4]};
+  return charge::chargingRate(tc, rho, cloud, ice, snow, graupel, hail, snowFall, false, false, crystals, two, has);
+}
 
 // the charging of the physics kernel (sg_charge.cuh), FP32
 float ht_takahashi(float tc, float lwc) { return charge::takahashi(tc, lwc); }
