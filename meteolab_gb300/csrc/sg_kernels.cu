@@ -327,105 +327,118 @@ __global__ void k_sediment(const RunDesc* __restrict__ runs, const int4* items, 
   }
 }
 
-// Two-moment fall (sedimentRain2m / sedimentIce2m / sediment2m, :898-988; NSSL sediment1d, infall 4), one thread a
-// column, for two-moment rain and then two-moment graupel and hail: the mass with its mass-weighted speed, the number
-// with its number-weighted one, an ice class's particle volume with the mass, a reflectivity and a number carried at
-// the mass's speed beside them; every sub-step the number is kept between what those two imply. Bottom-up, so each
-// face uses the values above from before the sub-step; the ground flux into the rain gauge. Sub-steps by the faster of
-// the reflectivity's and the mass's speed over the run. Before two-moment hail falls, the hail reaching the ground and
-// its largest stones (collectHail, :697-711, with the two-moment speed and tail).
-__global__ void k_sediment_2m(const RunDesc* __restrict__ runs, const int4* items, int nitems) {
-  extern __shared__ float sm[];
+// Two-moment fall (sedimentRain2m / sedimentIce2m / sediment2m, :898-988; NSSL sediment1d, infall 4) for two-moment
+// rain and then two-moment graupel and hail: the mass with its mass-weighted speed, the number with its number-weighted
+// one, an ice class's particle volume with the mass, a reflectivity and a number carried at the mass's speed beside
+// them; every sub-step the number is kept between what those two imply. A warp a column, level z in lane z % 32 (slot
+// z / 32, K slots), every value in registers: a level's update reads only its own and the level above's values from
+// before the sub-step (the reference's bottom-up loop), so the level above's out-fluxes come by one warp shuffle. The
+// ground flux into the rain gauge (lane 0, level 0, in sub-step order). Sub-steps by the faster of the reflectivity's
+// and the mass's speed over the run. Before two-moment hail falls, the hail reaching the ground and its largest stones
+// (collectHail, :697-711, with the two-moment speed and tail).
+constexpr int SED2_WARPS = 8;
+template <int K>
+__global__ void __launch_bounds__(SED2_WARPS * 32) k_sediment_2m(const RunDesc* __restrict__ runs, const int4* items, int nitems) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  constexpr unsigned FULL = 0xffffffffu;
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
     if (R.cnt[C_FAILED] || !(R.flags & RF_RAIN2M)) continue;
-    const int nz = R.nz, layer = R.layer, t = threadIdx.x;
-    float* sq = sm;                     // [nz][SED_COLS] each: mass, number, carried number, reflectivity, the speeds, volume
-    float* sn = sq + nz * SED_COLS;
-    float* sc = sn + nz * SED_COLS;
-    float* sr = sc + nz * SED_COLS;
-    float* vm = sr + nz * SED_COLS;
-    float* vn = vm + nz * SED_COLS;
-    float* vz = vn + nz * SED_COLS;
-    float* sv = vz + nz * SED_COLS;
-    float* lrho = sv + nz * SED_COLS;   // [nz] rho0, 1/(rho0 h), 1/h
-    float* lk = lrho + nz;
-    float* lh = lk + nz;
-    for (int z = t; z < nz; z += blockDim.x) { lrho[z] = lvl(R, L_RHO, z); lk[z] = lvl(R, L_INV_RHO, z) * lvl(R, L_INV_HZ, z); lh[z] = lvl(R, L_INV_HZ, z); }
-    __syncthreads();
-    const int c = items[it].y * SED_COLS + t;
+    const int nz = R.nz, layer = R.layer;
+    const size_t n = R.n;
     const int classes = (R.flags & RF_ICE2M) ? 3 : 1;
-    if (t < SED_COLS && c < layer) {
-      const size_t n = R.n;
+    float rho[K], lk[K], lh[K];
+#pragma unroll
+    for (int j = 0; j < K; j++) {
+      const int z = lane + 32 * j;
+      rho[j] = z < nz ? lvl(R, L_RHO, z) : 0.f;
+      lk[j] = z < nz ? lvl(R, L_INV_RHO, z) * lvl(R, L_INV_HZ, z) : 0.f;
+      lh[j] = z < nz ? lvl(R, L_INV_HZ, z) : 0.f;
+    }
+    for (int cc = wid; cc < SED_COLS; cc += SED2_WARPS) {
+      const int c = items[it].y * SED_COLS + cc;
+      if (c >= layer) break;
       for (int k = 0; k < classes; k++) {
         // class k: rain (the drops' density, reflectivity factor G1), graupel, hail (their own density, bounded to
         // 170-900 kg/m3 for the reflectivity, :920, and factor)
         const bool ice = k > 0;
         const i2m::IceClass cl = k == 1 ? i2m::GRAUPEL_2M() : i2m::HAIL_2M();
-        float* q = field(R, 0, k == 0 ? RAIN : k == 1 ? GRAUPEL : HAIL);
-        float* num = field(R, 0, k == 0 ? RAIN_NUMBER : k == 1 ? GRAUPEL_NUMBER : HAIL_NUMBER);
-        float* vol = ice ? field(R, 0, k == 1 ? GRAUPEL_VOLUME : HAIL_VOLUME) : nullptr;
-        const float* fm = R.vfall + (size_t)(k == 0 ? V_RAIN : k == 1 ? V_GRAUPEL : V_HAIL) * n;
-        const float* fn = R.vfall + (size_t)(k == 0 ? V_RAIN_N : k == 1 ? V_GRAUPEL_N : V_HAIL_N) * n;
-        const float* fz = R.vfall + (size_t)(k == 0 ? V_RAIN_Z : k == 1 ? V_GRAUPEL_Z : V_HAIL_Z) * n;
+        float* Q = field(R, 0, k == 0 ? RAIN : k == 1 ? GRAUPEL : HAIL);
+        float* N = field(R, 0, k == 0 ? RAIN_NUMBER : k == 1 ? GRAUPEL_NUMBER : HAIL_NUMBER);
+        float* V = ice ? field(R, 0, k == 1 ? GRAUPEL_VOLUME : HAIL_VOLUME) : nullptr;
+        const float* FM = R.vfall + (size_t)(k == 0 ? V_RAIN : k == 1 ? V_GRAUPEL : V_HAIL) * n;
+        const float* FN = R.vfall + (size_t)(k == 0 ? V_RAIN_N : k == 1 ? V_GRAUPEL_N : V_HAIL_N) * n;
+        const float* FZ = R.vfall + (size_t)(k == 0 ? V_RAIN_Z : k == 1 ? V_GRAUPEL_Z : V_HAIL_Z) * n;
         const float g1 = ice ? cl.g1 : r2m::G1;
         auto k6 = [&](float qq, float vv) {
           if (!ice) return r2m::K6;
           const float d = 6.f / (phys::PI * fminf(900.f, fmaxf(170.f, i2m::densityOf(cl, qq, vv))));
           return d * d;
         };
-        if (k == 2) {
-          const float h = q[c];
+        if (k == 2 && lane == 0) {
+          const float h = Q[c];
           if (h > 1e-9f) {
-            R.cols[layer + c] += R.rho0 * h * fm[c] * R.dt;
-            R.cols[2 * layer + c] = fmaxf(R.cols[2 * layer + c], i2m::largestDiameter(i2m::HAIL_2M(), h, num[c], vol[c], R.rho0) * 1000.f);
+            R.cols[layer + c] += R.rho0 * h * FM[c] * R.dt;
+            R.cols[2 * layer + c] = fmaxf(R.cols[2 * layer + c], i2m::largestDiameter(i2m::HAIL_2M(), h, N[c], V[c], R.rho0) * 1000.f);
           }
         }
+        float q[K], num[K], vol[K], vm[K], vn[K], vz[K];
         bool any = false;
-        for (int z = 0; z < nz; z++) {
-          const int i = c + z * layer, s = z * SED_COLS + t;
-          sq[s] = q[i]; sn[s] = num[i]; vm[s] = fm[i]; vn[s] = fn[i]; vz[s] = fz[i]; sv[s] = ice ? vol[i] : 0.f;
-          any |= sq[s] != 0.f || sn[s] != 0.f || sv[s] != 0.f;
+#pragma unroll
+        for (int j = 0; j < K; j++) {
+          const int z = lane + 32 * j, i = c + z * layer;
+          const bool in = z < nz;
+          q[j] = in ? Q[i] : 0.f; num[j] = in ? N[i] : 0.f; vol[j] = in && ice ? V[i] : 0.f;
+          vm[j] = in ? FM[i] : 0.f; vn[j] = in ? FN[i] : 0.f; vz[j] = in ? FZ[i] : 0.f;
+          any |= q[j] != 0.f || num[j] != 0.f || vol[j] != 0.f;
         }
-        if (!any) continue;
+        if (!__any_sync(FULL, any)) continue;
         const int parts = max(1, (int)ceilf(R.scr[k == 0 ? S_R2M : k == 1 ? S_G2M : S_H2M] / .8f));
         const float step = R.dt / (float)parts;
-        float* precip = R.cols;
         for (int p = 0; p < parts; p++) {
-          for (int z = 0; z < nz; z++) {
-            const int s = z * SED_COLS + t;
-            const float rq = lrho[z] * sq[s], rn = lrho[z] * sn[s];
-            sr[s] = rq > 0.f && rn > 0.f ? g1 * k6(sq[s], sv[s]) * rq * rq / rn : 0.f;
-            sc[s] = sn[s];
+          float refl[K], carried[K];
+#pragma unroll
+          for (int j = 0; j < K; j++) {
+            const float rq = rho[j] * q[j], rn = rho[j] * num[j];
+            refl[j] = rq > 0.f && rn > 0.f ? g1 * k6(q[j], vol[j]) * rq * rq / rn : 0.f;
+            carried[j] = num[j];
           }
-          precip[c] += R.rho0 * sq[t] * vm[t] * step;
-          float inQ = 0.f, inN = 0.f, inC = 0.f, inR = 0.f, inV = 0.f;  // the fluxes into level z from above, from before this sub-step
-          for (int z = nz - 1; z >= 0; z--) {
-            const int s = z * SED_COLS + t;
-            const float oq = lrho[z] * sq[s] * vm[s], on = lrho[z] * sn[s] * vn[s], oc = lrho[z] * sc[s] * vm[s], orr = sr[s] * vz[s];
-            const float ov = lrho[z] * sv[s] * vm[s];
-            sq[s] += step * (inQ - oq) * lk[z];
-            sv[s] += step * (inV - ov) * lk[z];
-            sn[s] += step * (inN - on) * lk[z];
-            sc[s] += step * (inC - oc) * lk[z];
-            sr[s] += step * (inR - orr) * lh[z];
-            inQ = oq; inN = on; inC = oc; inR = orr; inV = ov;
+          if (lane == 0) R.cols[c] += R.rho0 * q[0] * vm[0] * step;
+          // each level's out-fluxes from before the sub-step; the level above's into this one (none past the top)
+          float oq[K], on[K], oc[K], orr[K], ov[K];
+#pragma unroll
+          for (int j = 0; j < K; j++) {
+            oq[j] = rho[j] * q[j] * vm[j]; on[j] = rho[j] * num[j] * vn[j]; oc[j] = rho[j] * carried[j] * vm[j];
+            orr[j] = refl[j] * vz[j]; ov[j] = rho[j] * vol[j] * vm[j];
           }
-          for (int z = 0; z < nz; z++) {
-            const int s = z * SED_COLS + t;
-            if (!(sq[s] > r2m::RAIN_MIN)) { if (sq[s] < 0.f) sq[s] = 0.f; sn[s] = 0.f; sv[s] = 0.f; continue; }
-            const float rq = lrho[z] * sq[s];
-            sn[s] = sr[s] > 0.f ? fmaxf(fminf(g1 * k6(sq[s], sv[s]) * rq * rq / sr[s] / lrho[z], sc[s]), sn[s]) : fmaxf(sc[s], sn[s]);
+          auto above = [&](const float (&o)[K], int j) {
+            const float next = __shfl_down_sync(FULL, o[j], 1);
+            const float wrap = __shfl_sync(FULL, j + 1 < K ? o[j + 1 < K ? j + 1 : j] : 0.f, 0);
+            return lane < 31 ? next : (j + 1 < K ? wrap : 0.f);
+          };
+#pragma unroll
+          for (int j = 0; j < K; j++) {
+            const float iq = above(oq, j), in_ = above(on, j), ic = above(oc, j), ir = above(orr, j), iv = above(ov, j);
+            q[j] += step * (iq - oq[j]) * lk[j];
+            vol[j] += step * (iv - ov[j]) * lk[j];
+            num[j] += step * (in_ - on[j]) * lk[j];
+            carried[j] += step * (ic - oc[j]) * lk[j];
+            refl[j] += step * (ir - orr[j]) * lh[j];
+          }
+#pragma unroll
+          for (int j = 0; j < K; j++) {
+            if (!(q[j] > r2m::RAIN_MIN)) { if (q[j] < 0.f) q[j] = 0.f; num[j] = 0.f; vol[j] = 0.f; continue; }
+            const float rq = rho[j] * q[j];
+            num[j] = refl[j] > 0.f ? fmaxf(fminf(g1 * k6(q[j], vol[j]) * rq * rq / refl[j] / rho[j], carried[j]), num[j]) : fmaxf(carried[j], num[j]);
           }
         }
-        for (int z = 0; z < nz; z++) {
-          const int i = c + z * layer, s = z * SED_COLS + t;
-          q[i] = sq[s]; num[i] = sn[s];
-          if (ice) vol[i] = sv[s];
+#pragma unroll
+        for (int j = 0; j < K; j++) {
+          const int z = lane + 32 * j, i = c + z * layer;
+          if (z < nz) { Q[i] = q[j]; N[i] = num[j]; if (ice) V[i] = vol[j]; }
         }
       }
     }
-    __syncthreads();  // the level tables are restaged for the block's next item
   }
 }
 
@@ -1814,7 +1827,11 @@ void launch_pres_correct(const Launch& L, int set, int final_) {
 void launch_fill_partial(const Launch& L, int set) { k_fill_partial<<<GRID(L.n, L.cap), 128, 0, L.stream>>>(L.runs, L.items, L.n, set); }
 void launch_fill_final(const Launch& L) { k_fill_final<<<GRID(L.n, L.cap), 32, 0, L.stream>>>(L.runs, L.items, L.n); }
 void launch_sediment_2m(const Launch& L, int maxnz) {
-  k_sediment_2m<<<GRID(L.n, L.cap), SED_COLS, (8 * maxnz * SED_COLS + 3 * maxnz) * sizeof(float), L.stream>>>(L.runs, L.items, L.n);
+  const int K = (maxnz + 31) / 32;  // level slots a lane (nz <= 128)
+  if (K <= 1) k_sediment_2m<1><<<GRID(L.n, L.cap), SED2_WARPS * 32, 0, L.stream>>>(L.runs, L.items, L.n);
+  else if (K == 2) k_sediment_2m<2><<<GRID(L.n, L.cap), SED2_WARPS * 32, 0, L.stream>>>(L.runs, L.items, L.n);
+  else if (K == 3) k_sediment_2m<3><<<GRID(L.n, L.cap), SED2_WARPS * 32, 0, L.stream>>>(L.runs, L.items, L.n);
+  else k_sediment_2m<4><<<GRID(L.n, L.cap), SED2_WARPS * 32, 0, L.stream>>>(L.runs, L.items, L.n);
 }
 void launch_physics(const Launch& L, int in, int mid, bool elec) {
   if (elec) k_physics<true><<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, in, mid);
@@ -1838,7 +1855,6 @@ cudaError_t set_smem_limits(int bytes) {
   if ((e = smem_limit(k_proj_div_xfft, bytes)) != cudaSuccess) return e;
   if ((e = smem_limit(k_proj_xifft, bytes)) != cudaSuccess) return e;
   if ((e = smem_limit(k_sediment, bytes)) != cudaSuccess) return e;
-  if ((e = smem_limit(k_sediment_2m, bytes)) != cudaSuccess) return e;
   if ((e = smem_limit(k_proj_div_fft2, bytes)) != cudaSuccess) return e;
   if ((e = smem_limit(k_proj_ifft2, bytes)) != cudaSuccess) return e;
   if ((e = smem_limit(k_refine_residual<0, 0>, bytes)) != cudaSuccess) return e;
