@@ -63,7 +63,7 @@ STEP_BYTES_PER_CELL = 32 + 72 + 464 + 252 + 64 + 104 + 36 + 72
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=100)
+    p.add_argument("--steps", type=int, default=400)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--members", type=int, default=MEMBERS)
@@ -121,7 +121,7 @@ class Clocks:
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, device: int):
-        self.device, self.proc, self.lines = device, None, []
+        self.device, self.proc, self.lines, self.first = device, None, [], 0
 
     def __enter__(self):
         try:
@@ -129,6 +129,11 @@ class Clocks:
                                           "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.reader = threading.Thread(target=lambda: self.lines.extend(self.proc.stdout), daemon=True)
             self.reader.start()
+            # the timed region starts once sampling has (nvidia-smi takes a moment to print its first line)
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 3.0 and self.proc.poll() is None:
+                time.sleep(.02)
+            self.first = len(self.lines)  # samples from here on fall in the timed region
         except Exception:
             self.proc = None
         return self
@@ -145,7 +150,8 @@ class Clocks:
     def summary(self):
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.lines:
+        lines = self.lines[self.first:] or self.lines[-1:]  # (a region shorter than the sampling interval: the last sample)
+        for line in lines:
             f = [x.strip() for x in line.split(",")]
             if len(f) < 9:
                 continue
