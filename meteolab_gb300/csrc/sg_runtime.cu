@@ -105,7 +105,7 @@ struct Plan {
   }
 };
 enum Family { FAM_NODE, FAM_COLS, FAM_ROWS_FACE, FAM_ROWS_PRES, FAM_MODES, FAM_RUNS, FAM_CELLS, FAM_T_WENO, FAM_T_DYN, FAM_MIX,
-              FAM_REFINE, FAM_T_CHG, FAM_COUNT };
+              FAM_REFINE, FAM_T_CHG, FAM_T_CHG3, FAM_COUNT };
 
 }  // namespace
 
@@ -352,14 +352,25 @@ void transport_items(sg_context* ctx, const std::vector<int>& slots, int TX, int
 
 // The extra fields of the plan's runs, one WENO field an item on the plan's tile: the charge carriers of the
 // electrified runs (groups 13-16), the raindrop number of the two-moment ones (group 17).
-void charge_items(sg_context* ctx, const std::vector<int>& slots, int TX, int TY, std::vector<int4>& out) {
-  out.clear();
+// The extra fields' transport items: three fields an item where a run carries a whole triple (groups 22: the first
+// three charge carriers, 23: the drop number with graupel's number and volume, 24: hail's number and volume with the
+// ions' charge), the rest one an item (groups 13-21).
+void charge_items(sg_context* ctx, const std::vector<int>& slots, int TX, int TY, std::vector<int4>& out, std::vector<int4>& out3) {
+  out.clear(); out3.clear();
   for (int s : slots) {
     const Run& r = ctx->runs[s];
     const int tiles = ((r.nx + TX - 1) / TX) * ((r.ny + TY - 1) / TY);
-    if (r.desc.flags & RF_ELEC) for (int g = 13; g < 17; g++) for (int t = 0; t < tiles; t++) out.push_back(make_int4(s, g, t, 0));
-    if (r.desc.flags & RF_RAIN2M) for (int t = 0; t < tiles; t++) out.push_back(make_int4(s, 17, t, 0));
-    if (r.desc.flags & RF_ICE2M) for (int g = 18; g < 22; g++) for (int t = 0; t < tiles; t++) out.push_back(make_int4(s, g, t, 0));
+    const bool elec = r.desc.flags & RF_ELEC, rain2 = r.desc.flags & RF_RAIN2M, ice2 = r.desc.flags & RF_ICE2M;
+    std::vector<int> ones, threes;
+    if (elec) threes.push_back(22);
+    if (ice2) threes.push_back(23); else if (rain2) ones.push_back(17);
+    if (elec && ice2) threes.push_back(24);
+    else {
+      if (elec) ones.push_back(16);
+      if (ice2) { ones.push_back(20); ones.push_back(21); }
+    }
+    for (int g : threes) for (int t = 0; t < tiles; t++) out3.push_back(make_int4(s, g, t, 0));
+    for (int g : ones) for (int t = 0; t < tiles; t++) out.push_back(make_int4(s, g, t, 0));
   }
 }
 
@@ -434,7 +445,7 @@ int build_plan(sg_context* ctx, const std::vector<int>& slots, Plan& P) {
   P.bulk = P.minb == 2 && ctx->bulk && transport_bulk_ok(P.TX, P.TY, P.minnx, P.nx4) &&
            std::max(transport_smem_bulk(TK_WENO, P.wenoG, P.TX, P.TY), transport_smem_bulk(TK_DYN, 4, P.TX, P.TY)) <= (size_t)ctx->maxSmem;
   transport_items(ctx, slots, P.TX, P.TY, P.wenoG, all + FAM_T_WENO);
-  charge_items(ctx, slots, P.TX, P.TY, all[FAM_T_CHG]);
+  charge_items(ctx, slots, P.TX, P.TY, all[FAM_T_CHG], all[FAM_T_CHG3]);
   int st = upload_items(ctx, P, all);
   if (st != SG_OK) return st;
   return ctx->autotune && !ctx->pinned[0] ? autotune_transport(ctx, P) : SG_OK;
@@ -444,8 +455,12 @@ Launch lx(sg_context* ctx, const Plan& P, int fam, int capPerSm = 8) {
   return Launch{ctx->d_runs, P.items + P.off[fam], P.cnt[fam], ctx->sms * capPerSm, ctx->stream};
 }
 
-// The charge carriers' WENO transport of one RK3 stage (electrified runs; per-thread copies, one field an item).
+// The extra fields' WENO transport of one RK3 stage (electrified and two-moment runs; per-thread copies): the items of
+// three fields, then those of one.
 void launch_charges(sg_context* ctx, const Plan& P, int in, int out, float frac, int stage, cudaStream_t stream) {
+  Launch C3 = lx(ctx, P, FAM_T_CHG3);
+  C3.cap = C3.n; C3.stream = stream;
+  if (C3.n) launch_transport(C3, TK_WENO, 3, P.minb, in, out, frac, stage, P.TX, P.TY, false, false);  // (no edge warps: see the kernel)
   Launch C = lx(ctx, P, FAM_T_CHG);
   C.cap = C.n; C.stream = stream;
   if (C.n) launch_transport(C, TK_WENO, 1, P.minb, in, out, frac, stage, P.TX, P.TY, false, ctx->edgeWarps);
@@ -530,12 +545,12 @@ int autotune_transport(sg_context* ctx, Plan& P) {
   P.TX = best[0]; P.TY = best[1]; P.wenoG = best[2]; P.minb = best[3]; P.bulk = best[4] != 0; P.tuned = true;
   std::vector<int4> all[FAM_COUNT];
   for (int f = 0; f < FAM_COUNT; f++) {  // keep the other families, rebuild the transport ones
-    if (f == FAM_T_WENO || f == FAM_T_DYN || f == FAM_T_CHG) continue;
+    if (f == FAM_T_WENO || f == FAM_T_DYN || f == FAM_T_CHG || f == FAM_T_CHG3) continue;
     all[f].resize(P.cnt[f]);
     if (P.cnt[f]) CK(cudaMemcpy(all[f].data(), P.items + P.off[f], P.cnt[f] * sizeof(int4), cudaMemcpyDeviceToHost));
   }
   transport_items(ctx, P.slots, P.TX, P.TY, P.wenoG, all + FAM_T_WENO);
-  charge_items(ctx, P.slots, P.TX, P.TY, all[FAM_T_CHG]);
+  charge_items(ctx, P.slots, P.TX, P.TY, all[FAM_T_CHG], all[FAM_T_CHG3]);
   return upload_items(ctx, P, all);
 }
 

@@ -27,14 +27,18 @@ constexpr int TMAXC = 4;  // plane cells per thread: (TX + 6)(TY + 6) <= TMAXC *
 constexpr int tlv_rows(int kind) { return kind == TK_DYN ? 9 : 2; }
 // Field groups of the transport work items: 0-2 the WENO fields in threes, 3 the dynamics {u, v, w, theta'}, 4-12
 // the WENO fields one by one, 13-16 the charge carriers of an electrified run, 17 the raindrop number of a two-moment
-// run and 18-21 the graupel and hail numbers and volumes of a two-moment ice run, one by one.
-constexpr int TGROUPS = 22;
+// run and 18-21 the graupel and hail numbers and volumes of a two-moment ice run, one by one; 22-24 extra fields in
+// threes (the first three charge carriers; the drop number with graupel's number and volume; hail's number and volume
+// with the ions' charge).
+constexpr int TGROUPS = 25;
 __constant__ int TGROUP[TGROUPS][4] = {{RAIN, SNOW, GRAUPEL, -1}, {HAIL, Q, CLOUD, -1}, {ICE, ICENUM, COLD, -1}, {U, V, W, THETA},
                                        {RAIN, -1, -1, -1}, {SNOW, -1, -1, -1}, {GRAUPEL, -1, -1, -1}, {HAIL, -1, -1, -1},
                                        {Q, -1, -1, -1}, {CLOUD, -1, -1, -1}, {ICE, -1, -1, -1}, {ICENUM, -1, -1, -1}, {COLD, -1, -1, -1},
                                        {CHARGE_ICE, -1, -1, -1}, {CHARGE_GRAUPEL, -1, -1, -1}, {CHARGE_RAIN, -1, -1, -1}, {CHARGE_AIR, -1, -1, -1},
                                        {RAIN_NUMBER, -1, -1, -1}, {GRAUPEL_NUMBER, -1, -1, -1}, {GRAUPEL_VOLUME, -1, -1, -1},
-                                       {HAIL_NUMBER, -1, -1, -1}, {HAIL_VOLUME, -1, -1, -1}};
+                                       {HAIL_NUMBER, -1, -1, -1}, {HAIL_VOLUME, -1, -1, -1},
+                                       {CHARGE_ICE, CHARGE_GRAUPEL, CHARGE_RAIN, -1}, {RAIN_NUMBER, GRAUPEL_NUMBER, GRAUPEL_VOLUME, -1},
+                                       {HAIL_NUMBER, HAIL_VOLUME, CHARGE_AIR, -1}};
 
 // Two faces at once on the packed FP32 pipes (bit-identical per face to the scalar weno5 / upwind5).
 struct Op2 {
@@ -94,7 +98,8 @@ __device__ __forceinline__ void transport_item(const RunDesc& Rg, int group, int
 #pragma unroll
   // an extra field's sets follow the base fields' three, NXE fields a set: its offsets are shifted by `so` so the same
   // set arithmetic addresses it
-  const bool chg = G == 1 && group >= 13;  // (the extra fields come one an item)
+  // (extra fields come one an item, or three an item without the edge warps: the base kernels keep compile-time offsets)
+  const bool chg = (G == 1 || !EW) && group >= 13;
   const int so = chg ? (3 * NF - NF) * (int)n : 0, ss = chg ? NXE * (int)n : NF * (int)n;
   for (int g = 0; g < G; g++) fo[g] = TGROUP[group][g] * (int)n + so;
   const int qo = in_set * ss, oo = out_set * ss;
@@ -357,7 +362,7 @@ __device__ __forceinline__ void transport_item_bulk(const RunDesc& Rg, int group
 #pragma unroll
   // an extra field's sets follow the base fields' three, NXE fields a set: its offsets are shifted by `so` so the same
   // set arithmetic addresses it
-  const bool chg = G == 1 && group >= 13;  // (the extra fields come one an item)
+  const bool chg = G == 1 && group >= 13;  // (the bulk kernels carry no extra fields: only G == 1 could)
   const int so = chg ? (3 * NF - NF) * (int)n : 0, ss = chg ? NXE * (int)n : NF * (int)n;
   for (int g = 0; g < G; g++) fo[g] = TGROUP[group][g] * (int)n + so;
   const int qo = in_set * ss, oo = out_set * ss;
