@@ -63,7 +63,7 @@ STEP_BYTES_PER_CELL = 32 + 72 + 464 + 252 + 64 + 104 + 36 + 72
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=400)
+    p.add_argument("--steps", type=int, default=100)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--members", type=int, default=MEMBERS)
@@ -116,14 +116,50 @@ def allmax(pg, x: float) -> float:
 
 
 class Clocks:
-    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+    """SM clock and clock-event (throttle) reasons sampled during the timed region: through NVML's read-only queries
+    every few milliseconds on a sampling thread (the timed call releases the GIL), so even a region of a few tens of
+    milliseconds has samples; nvidia-smi at 200 ms where NVML cannot be loaded."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # NVML clock-event reason bits (nvml.h): SW power cap, HW slowdown, SW thermal, HW thermal
+    BITS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8, "sw_thermal_slowdown": 0x20, "hw_thermal_slowdown": 0x40}
 
     def __init__(self, device: int):
         self.device, self.proc, self.lines, self.first = device, None, [], 0
+        self.nvml, self.samples, self.max_mhz, self.stop = None, [], None, threading.Event()
+
+    def _nvml_open(self):
+        import ctypes
+        lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            return None
+        handle = ctypes.c_void_p()
+        if lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(self.device), ctypes.byref(handle)) != 0:
+            return None
+        mx = ctypes.c_uint()
+        if lib.nvmlDeviceGetMaxClockInfo(handle, 1, ctypes.byref(mx)) == 0:  # 1: NVML_CLOCK_SM
+            self.max_mhz = float(mx.value)
+        reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        return lib, handle, reasons
+
+    def _nvml_loop(self):
+        import ctypes
+        lib, handle, reasons = self.nvml
+        clk, rs = ctypes.c_uint(), ctypes.c_ulonglong()
+        while not self.stop.is_set():
+            if lib.nvmlDeviceGetClockInfo(handle, 1, ctypes.byref(clk)) == 0 and reasons(handle, ctypes.byref(rs)) == 0:
+                self.samples.append((float(clk.value), int(rs.value)))
+            time.sleep(.005)
 
     def __enter__(self):
+        try:
+            self.nvml = self._nvml_open()
+        except Exception:
+            self.nvml = None
+        if self.nvml:
+            self.reader = threading.Thread(target=self._nvml_loop, daemon=True)
+            self.reader.start()
+            return self
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
                                           "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
@@ -139,6 +175,13 @@ class Clocks:
         return self
 
     def __exit__(self, *exc):
+        if self.nvml:
+            self.stop.set()
+            self.reader.join(timeout=2)
+            try:
+                self.nvml[0].nvmlShutdown()
+            except Exception:
+                pass
         if self.proc:
             self.proc.terminate()
             try:
@@ -148,6 +191,11 @@ class Clocks:
             self.reader.join(timeout=2)
 
     def summary(self):
+        if self.nvml:
+            sm = [c for c, _ in self.samples]
+            reasons = sorted(n for n, b in self.BITS.items() if any(r & b for _, r in self.samples))
+            return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": self.max_mhz, "reasons": reasons,
+                    "samples": len(sm), "source": "nvml, 5 ms"}
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         lines = self.lines[self.first:] or self.lines[-1:]  # (a region shorter than the sampling interval: the last sample)
@@ -162,7 +210,8 @@ class Clocks:
             for k, n in enumerate(names):
                 if f[5 + k].lower() == "active":
                     reasons.add(n)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm),
+                "source": "nvidia-smi, 200 ms"}
 
 
 def peaks():
