@@ -15,8 +15,9 @@
  *   retire(ctx, run), destroyContext(ctx)
  *   saveState(ctx, run, configJson: string, time, persisted) -> ArrayBuffer      (saveState, src/core/state.ts:43)
  *   loadState(ctx, run, image: ArrayBuffer) -> {version, time, persisted}        (readState + applyState, :55-83)
- *   two-moment runs: switches.rainMoments 2 (and rainBreakup), switches.iceMoments 2 (with ice and two-moment rain); their
- *   numbers and volumes through readCharges-like calls are not bound here: they travel in state files (saveState)
+ *   two-moment runs: switches.rainMoments 2 (and rainBreakup), switches.iceMoments 2 (with ice and two-moment rain):
+ *   readMoments(ctx, run, fields: Float32Array[1 or 5]) / writeMoments(ctx, run, fields)   rainNumber, then graupelNumber,
+ *                                                             graupelVolume, hailNumber, hailVolume (src/core/model.ts:194-202)
  *   electrified runs (switches.lightning, with ice; switches.corona, switches.lightningSeed = config.seed + 1):
  *   readCharges(ctx, run, charges: Float32Array[4]) / writeCharges(ctx, run, charges)   chargeIce, chargeGraupel,
  *                                                             chargeRain, chargeAir (src/core/model.ts:210)
@@ -253,22 +254,35 @@ static napi_value fields_io(napi_env env, napi_callback_info info, int write) {
 static napi_value read_fields(napi_env env, napi_callback_info info) { return fields_io(env, info, 0); }
 static napi_value write_fields(napi_env env, napi_callback_info info) { return fields_io(env, info, 1); }
 
-static napi_value charges_io(napi_env env, napi_callback_info info, int write) {
-  size_t argc = 3; napi_value argv[3]; int32_t run;
+/* The extra fields first .. first + count - 1 (a JS array of that many Float32Arrays; `most` of them at most, `least`
+ * at least) from or into the run. */
+static napi_value extras_io(napi_env env, napi_callback_info info, int write, int first, uint32_t least, uint32_t most, const char* what) {
+  size_t argc = 3; napi_value argv[3]; int32_t run; uint32_t count = 0;
   CHECK(env, napi_get_cb_info(env, info, &argc, argv, NULL, NULL));
   sg_context* ctx = ctx_of(env, argv[0]);
   napi_get_value_int32(env, argv[1], &run);
-  float* f[SG_NFIELDS_ELECTRIFIED] = {0};
-  for (uint32_t k = 0; k < 4; k++) {
+  if (napi_get_array_length(env, argv[2], &count) != napi_ok || count < least || count > most) { napi_throw_type_error(env, NULL, what); return NULL; }
+  float* f[SG_NFIELDS_EXTRA] = {0};
+  uint32_t mask = 0;
+  for (uint32_t k = 0; k < count; k++) {
     napi_value el; napi_typedarray_type type; size_t len; void* data; napi_value buf; size_t off;
     if (napi_get_element(env, argv[2], k, &el) != napi_ok || napi_get_typedarray_info(env, el, &type, &len, &data, &buf, &off) != napi_ok ||
-        type != napi_float32_array) { napi_throw_type_error(env, NULL, "charges: 4 Float32Array"); return NULL; }
-    f[SG_CHARGE_ICE + k] = (float*)data;
+        type != napi_float32_array) { napi_throw_type_error(env, NULL, what); return NULL; }
+    f[first + k] = (float*)data;
+    mask |= 1u << (first + k);
   }
-  int st = write ? sg_run_write_fields(ctx, run, SG_CHARGE_FIELDS, (const float* const*)f) : sg_run_read_fields(ctx, run, SG_CHARGE_FIELDS, f);
+  int st = write ? sg_run_write_fields(ctx, run, mask, (const float* const*)f) : sg_run_read_fields(ctx, run, mask, f);
   if (st) return throw_status(env, ctx, st);
   return NULL;
 }
+static napi_value charges_io(napi_env env, napi_callback_info info, int write) {
+  return extras_io(env, info, write, SG_CHARGE_ICE, 4, 4, "charges: 4 Float32Array");
+}
+static napi_value moments_io(napi_env env, napi_callback_info info, int write) {
+  return extras_io(env, info, write, SG_RAIN_NUMBER, 1, 5, "moments: 1 or 5 Float32Array (rainNumber, then graupelNumber, graupelVolume, hailNumber, hailVolume)");
+}
+static napi_value read_moments(napi_env env, napi_callback_info info) { return moments_io(env, info, 0); }
+static napi_value write_moments(napi_env env, napi_callback_info info) { return moments_io(env, info, 1); }
 static napi_value read_charges(napi_env env, napi_callback_info info) { return charges_io(env, info, 0); }
 static napi_value write_charges(napi_env env, napi_callback_info info) { return charges_io(env, info, 1); }
 
@@ -431,6 +445,7 @@ static napi_value init(napi_env env, napi_value exports) {
     {"electricCreate", 0, electric_create, 0, 0, 0, napi_default, 0}, {"electricSolve", 0, electric_solve, 0, 0, 0, napi_default, 0},
     {"electricDestroy", 0, electric_destroy, 0, 0, 0, napi_default, 0},
     {"readCharges", 0, read_charges, 0, 0, 0, napi_default, 0}, {"writeCharges", 0, write_charges, 0, 0, 0, napi_default, 0},
+    {"readMoments", 0, read_moments, 0, 0, 0, napi_default, 0}, {"writeMoments", 0, write_moments, 0, 0, 0, napi_default, 0},
     {"charge", 0, charge, 0, 0, 0, napi_default, 0}, {"flashes", 0, flashes, 0, 0, 0, napi_default, 0},
     {"discharge", 0, discharge, 0, 0, 0, napi_default, 0},
   };

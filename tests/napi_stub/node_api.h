@@ -58,6 +58,7 @@ napi_status napi_get_value_string_utf8(napi_env env, napi_value value, char* buf
 napi_status napi_get_named_property(napi_env env, napi_value object, const char* utf8name, napi_value* result);
 napi_status napi_set_named_property(napi_env env, napi_value object, const char* utf8name, napi_value value);
 napi_status napi_get_element(napi_env env, napi_value object, uint32_t index, napi_value* result);
+napi_status napi_get_array_length(napi_env env, napi_value value, uint32_t* result);
 napi_status napi_set_element(napi_env env, napi_value object, uint32_t index, napi_value value);
 napi_status napi_create_array_with_length(napi_env env, size_t length, napi_value* result);
 napi_status napi_create_typedarray(napi_env env, napi_typedarray_type type, size_t length, napi_value arraybuffer, size_t byte_offset,
