@@ -59,3 +59,24 @@ def test_reference_arm_prints_on_rank_zero_only(capsys):
         gpus, steps, warmup, members = 2, 1, 0, 64
     bench.reference_arm(A, 1, None)
     assert capsys.readouterr().out == ""
+
+
+def test_clock_summary_reads_the_reason_bits_and_the_timed_samples():
+    """The clock record of the timed region: NVML samples (SM MHz, clock-event reason bits) give the median and the
+    reasons that were active at any sample; nvidia-smi lines count only from the region's start."""
+    sys.path.insert(0, ROOT)
+    import bench
+    c = bench.Clocks(0)
+    c.nvml, c.max_mhz = ("lib", None, None), 2070.0
+    c.samples = [(2070.0, 0), (2070.0, 0x4), (1980.0, 0x4 | 0x1), (2070.0, 0)]
+    s = c.summary()
+    assert s["sm_mhz"] == 2070.0 and s["sm_max_mhz"] == 2070.0 and s["reasons"] == ["sw_power_cap"] and s["samples"] == 4
+    c.samples.append((1500.0, 0x40))
+    assert bench.Clocks.summary(c)["reasons"] == ["hw_thermal_slowdown", "sw_power_cap"]
+    smi = bench.Clocks(0)
+    smi.lines = ["0, 1200, 2070, 300, Not Active, Not Active, Not Active, Not Active, Not Active",
+                 "0, 2070, 2070, 900, Active, Not Active, Not Active, Not Active, Active",
+                 "0, 2065, 2070, 950, Not Active, Not Active, Not Active, Not Active, Not Active"]
+    smi.first = 1  # the idle sample before the region is left out
+    s = smi.summary()
+    assert s["samples"] == 2 and s["sm_mhz"] == (2070 + 2065) / 2 and s["reasons"] == ["sw_power_cap"]
