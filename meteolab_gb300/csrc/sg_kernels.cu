@@ -1834,6 +1834,7 @@ void launch_sediment_2m(const Launch& L, int maxnz) {
   else k_sediment_2m<4><<<GRID(L.n, L.cap), SED2_WARPS * 32, 0, L.stream>>>(L.runs, L.items, L.n);
 }
 void launch_physics(const Launch& L, int in, int mid, bool elec) {
+  if (L.n == 0) return;
   if (elec) k_physics<true><<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, in, mid);
   else k_physics<false><<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, in, mid);
 }

@@ -183,3 +183,28 @@ def test_numbers_and_volumes_through_a_state_file(ctx, storm):
     assert a.save_state({"moments": 2}, persisted=0.0) == img
     r.retire()
     a.retire()
+
+
+def test_mixed_batch_gives_each_run_its_own_bits(ctx, storm):
+    """A one-moment run, a two-moment run (rain, graupel and hail) and an electrified two-moment run stepped together in
+    one batch (one plan: the extras' kernels, the two-moment fall and the lightning beside the plain run's work) give
+    each run exactly the fields, numbers and charges it has stepped alone."""
+    plain = RunSpec(GRID, storm.env, dataclasses.replace(storm.switches, rain_moments=1, ice_moments=1),
+                    {k: v for k, v in storm.fields.items() if k in CARRIED}, storm.seed, "plain")
+    elec = RunSpec(GRID, storm.env, dataclasses.replace(storm.switches, lightning=1), storm.fields, storm.seed, "storm2m-ice+e")
+    specs = (plain, storm, elec)
+    names = (list(CARRIED), list(FIELDS), list(FIELDS) + list(CHARGES))
+    alone = []
+    for s, nm in zip(specs, names):
+        r = ctx.create(s)
+        r.step(3)
+        alone.append(r.read(nm))
+        r.retire()
+    runs = [ctx.create(s) for s in specs]
+    ctx.batch_step(runs, 3)
+    for r, a, nm in zip(runs, alone, names):
+        b = r.read(nm)
+        assert r.status()["failed"] == 0
+        for k in nm:
+            assert np.array_equal(a[k], b[k]), (r.spec.label, k)
+        r.retire()
