@@ -78,7 +78,7 @@ struct Run {
 struct Plan {
   std::vector<int> slots;
   int4* items = nullptr;  // device
-  int off[16] = {0}, cnt[16] = {0};
+  int off[24] = {0}, cnt[24] = {0};
   int maxnx = 0, maxny = 0, maxnz = 0, TX = 40, TY = 8, wenoG = 3;  // transport tile and WENO fields per item
   int minb = 2;                                                       // WENO transport blocks per SM (register budget)
   int minnx = 1 << 30;                                                // the narrowest grid of the plan
@@ -87,7 +87,8 @@ struct Plan {
   int yc = 32;                                                        // layer rows per x-transform item
   int mixTX = 32, mixTY = 8;                                          // mixing tile
   int refTX = 16, refTY = 8;                                          // refinement tile
-  bool layerfft = false;                                              // 2-D transforms per layer (see enqueue_part)
+  bool layerAny = false, rowAny = false;                              // some run takes the 2-D layer transforms / the row path
+  int rowMaxnx = 0, rowMaxny = 0;                                     // the widest grid of the row path
   size_t fftSmem = 0;                                                 // their shared memory: the largest over the runs
   bool refine = false;                                                // some run refines its final projection
   bool unrefined = false;                                             // some run does not (k_pres_correct<1> has work)
@@ -105,7 +106,7 @@ struct Plan {
   }
 };
 enum Family { FAM_NODE, FAM_COLS, FAM_ROWS_FACE, FAM_ROWS_PRES, FAM_MODES, FAM_RUNS, FAM_CELLS, FAM_T_WENO, FAM_T_DYN, FAM_MIX,
-              FAM_REFINE, FAM_T_CHG, FAM_T_CHG3, FAM_PHYS, FAM_PHYS_X, FAM_COUNT };
+              FAM_REFINE, FAM_T_CHG, FAM_T_CHG3, FAM_PHYS, FAM_PHYS_X, FAM_LROWS_FACE, FAM_LROWS_PRES, FAM_LMODES, FAM_COUNT };
 
 }  // namespace
 
@@ -401,12 +402,16 @@ int build_plan(sg_context* ctx, const std::vector<int>& slots, Plan& P) {
   P.TX = all40 ? 40 : 32;
   P.TY = 8;
   P.wenoG = 3;
-  // Spectral solves: when a layer's spectrum fits in shared memory (the 40x32 and 80x64 grids), whole layers are
-  // transformed in 2-D and the mode kernel is a pure FP64 sweep; otherwise rows of 16 or 32 are x-transformed and
-  // the mode kernel transforms along y around its sweep.
-  P.layerfft = !ctx->rowsOnly && layer_fft_smem(P.maxnx, P.maxny) <= (size_t)std::min(ctx->maxSmem, 100 * 1024);
-  P.yc = P.layerfft ? P.maxny : std::min(P.maxnx > 128 ? 16 : 32, (P.maxny + 1) / 2 * 2);
-  for (int s : slots) P.fftSmem = std::max(P.fftSmem, layer_fft_smem_run(ctx->runs[s].nx, ctx->runs[s].ny));
+  // Spectral solves, chosen run by run (so a run's bits do not depend on its batch): when a layer's spectrum fits in
+  // shared memory (the 40x32 and 80x64 grids), whole layers are transformed in 2-D and the mode kernel is a pure FP64
+  // sweep; otherwise rows of 16 or 32 are x-transformed and the mode kernel transforms along y around its sweep.
+  auto layerPath = [&](const Run& r) { return !ctx->rowsOnly && layer_fft_smem(r.nx, r.ny) <= (size_t)std::min(ctx->maxSmem, 100 * 1024); };
+  for (int s : slots) {
+    const Run& r = ctx->runs[s];
+    if (layerPath(r)) { P.layerAny = true; P.fftSmem = std::max(P.fftSmem, layer_fft_smem_run(r.nx, r.ny)); }
+    else { P.rowAny = true; P.rowMaxnx = std::max(P.rowMaxnx, r.nx); P.rowMaxny = std::max(P.rowMaxny, r.ny); }
+  }
+  P.yc = P.rowAny ? std::min(P.rowMaxnx > 128 ? 16 : 32, (P.rowMaxny + 1) / 2 * 2) : 32;
   for (int s : slots) {
     const Run& r = ctx->runs[s];
     int n = r.nx * r.ny * r.nz, nch = (n + CHUNK - 1) / CHUNK, layer = r.nx * r.ny;
@@ -416,9 +421,15 @@ int build_plan(sg_context* ctx, const std::vector<int>& slots, Plan& P) {
     int ncc = (r.nx * r.ny * (r.nz - 1) + CHUNK - 1) / CHUNK;
     for (int c = 0; c < ncc; c++) all[FAM_CELLS].push_back(make_int4(s, c, 0, 0));
     for (int c = 0; c < (layer + 63) / 64; c++) all[FAM_COLS].push_back(make_int4(s, c, 0, 0));
-    for (int k = 0; k < r.nz; k++) for (int y = 0; y < r.ny; y += P.yc) all[FAM_ROWS_FACE].push_back(make_int4(s, k, y, 0));
-    for (int k = 0; k < r.nz - 1; k++) for (int y = 0; y < r.ny; y += P.yc) all[FAM_ROWS_PRES].push_back(make_int4(s, k, y, 0));
-    for (int m = 0; m < r.nx / 2 + 1; m++) all[FAM_MODES].push_back(make_int4(s, m, 0, 0));
+    if (layerPath(r)) {  // a layer an item
+      for (int k = 0; k < r.nz; k++) all[FAM_LROWS_FACE].push_back(make_int4(s, k, 0, 0));
+      for (int k = 0; k < r.nz - 1; k++) all[FAM_LROWS_PRES].push_back(make_int4(s, k, 0, 0));
+      for (int m = 0; m < r.nx / 2 + 1; m++) all[FAM_LMODES].push_back(make_int4(s, m, 0, 0));
+    } else {
+      for (int k = 0; k < r.nz; k++) for (int y = 0; y < r.ny; y += P.yc) all[FAM_ROWS_FACE].push_back(make_int4(s, k, y, 0));
+      for (int k = 0; k < r.nz - 1; k++) for (int y = 0; y < r.ny; y += P.yc) all[FAM_ROWS_PRES].push_back(make_int4(s, k, y, 0));
+      for (int m = 0; m < r.nx / 2 + 1; m++) all[FAM_MODES].push_back(make_int4(s, m, 0, 0));
+    }
     all[FAM_RUNS].push_back(make_int4(s, 0, 0, 0));
     if (r.desc.flags & RF_REFINE) P.refine = true; else P.unrefined = true;
     if (r.desc.flags & RF_ROTATION) P.rotation = true;
@@ -560,21 +571,26 @@ int autotune_transport(sg_context* ctx, Plan& P) {
 // plan's rows and modes, on the stream of `rows`.
 template <class Hook>
 void enqueue_solve(sg_context* ctx, const Plan& P, int mode, int set, cudaStream_t stream, Hook hook) {
-  Launch rows = lx(ctx, P, mode == PROJ_FACE ? FAM_ROWS_FACE : FAM_ROWS_PRES), modes = lx(ctx, P, FAM_MODES);
-  rows.cap = rows.n;
-  modes.cap = modes.n;  // one block per wavenumber: its column solves are serial in z, so spread them over the SMs
-  rows.stream = modes.stream = stream;
   const int h = mode == PROJ_FACE ? 2 : mode == PROJ_PRES ? 7 : 22;  // profile ids of the three stages
-  if (P.layerfft) {
+  if (P.layerAny) {  // the runs whose layers transform in 2-D
+    Launch rows = lx(ctx, P, mode == PROJ_FACE ? FAM_LROWS_FACE : FAM_LROWS_PRES), modes = lx(ctx, P, FAM_LMODES);
+    rows.cap = rows.n;
+    modes.cap = modes.n;  // one block per wavenumber: its column solves are serial in z, so spread them over the SMs
+    rows.stream = modes.stream = stream;
     launch_proj_div_fft2(rows, mode, set, P.fftSmem); hook(h);
     launch_proj_sweep(modes, mode, P.maxny); hook(h + 1);
     launch_proj_ifft2(rows, mode, P.fftSmem); hook(h + 2);
-  } else {
-    const int mthreads = std::min(512, std::max(64, (2 * P.maxny + 31) / 32 * 32));
+  }
+  if (P.rowAny) {  // the runs of the row path
+    Launch rows = lx(ctx, P, mode == PROJ_FACE ? FAM_ROWS_FACE : FAM_ROWS_PRES), modes = lx(ctx, P, FAM_MODES);
+    rows.cap = rows.n;
+    modes.cap = modes.n;
+    rows.stream = modes.stream = stream;
+    const int mthreads = std::min(512, std::max(64, (2 * P.rowMaxny + 31) / 32 * 32));
     const int mbudget = std::min(ctx->maxSmem, 200 * 1024);
-    launch_proj_div_xfft(rows, mode, set, P.yc, P.maxnx); hook(h);
-    launch_proj_modes(modes, mode, P.maxnz, P.maxny, mthreads, mbudget); hook(h + 1);
-    launch_proj_xifft(rows, mode, P.yc, P.maxnx); hook(h + 2);
+    launch_proj_div_xfft(rows, mode, set, P.yc, P.rowMaxnx); hook(h);
+    launch_proj_modes(modes, mode, P.maxnz, P.rowMaxny, mthreads, mbudget); hook(h + 1);
+    launch_proj_xifft(rows, mode, P.yc, P.rowMaxnx); hook(h + 2);
   }
 }
 

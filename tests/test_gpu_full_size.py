@@ -63,16 +63,20 @@ def test_a_full_size_run_keeps_the_invariants(ctx, opts, label):
 
 
 def test_the_stress_grid_is_the_same_alone_and_in_a_batch(ctx):
+    """The stress run (the row-transform path) and a large run (the 2-D layer transforms) each give the bits they get
+    alone when batched together: the spectral path is chosen run by run, not by the batch's widest grid."""
     big = baseline_run(create_grid(STRESS_GRID), seed=6, bubble=2.0)
     small = baseline_run(create_grid(LARGE_GRID), seed=7)
-    a = ctx.create(big)
+    a, b = ctx.create(big), ctx.create(small)
     a.step(5)
+    b.step(5)
     x, y = ctx.create(big), ctx.create(small)
     ctx.batch_step([x, y], 5)
-    fa, fx = a.read(), x.read()
+    fa, fb, fx, fy = a.read(), b.read(), x.read(), y.read()
     for k in CARRIED:
-        assert np.array_equal(fa[k], fx[k]), k
-    for run in (a, x, y):
+        assert np.array_equal(fa[k], fx[k]), ("stress", k)
+        assert np.array_equal(fb[k], fy[k]), ("large", k)
+    for run in (a, b, x, y):
         run.retire()
 
 
