@@ -76,7 +76,7 @@ struct LgtJob {
   LgtHost* H = nullptr;
   double time = 0, dt = 0;
   int limit = 0, k = 0, stamp = 0, stage = 0, start = -1, id = 0, copied = 0;
-  bool pending = false;            // a flash ended last round; its record is read this round
+  bool pending = false;            // a flash ended in the previous discharge round; its record is read in this one
   enum Phase { SEARCH, FLASH, FINISHING, DONE } phase = SEARCH;
 };
 
