@@ -74,3 +74,19 @@ def test_static_check_refuses_short_level_arrays():
     g = create_grid(DEFAULT_GRID)
     with pytest.raises(ValueError, match="levels"):
         divergence_max_static(0, 0, 0, 0, g, [1.0] * (g.nz - 1))
+
+
+def test_run_bytes_grow_with_the_extra_fields(lib):
+    """What admission by budget counts (sg_run_bytes_for, host arithmetic only): the extra field sets and fall speeds
+    of a two-moment run, twice the fall speeds with two-moment graupel and hail, the lightning's buffers on top; the
+    graupel and hail moments need two-moment rain and the ice microphysics (ice2m(), src/core/model.ts:914)."""
+    from meteolab_gb300 import runtime
+    from meteolab_gb300.grid import DEFAULT_GRID, create_grid
+    from meteolab_gb300.scenarios import Switches
+    g = create_grid(DEFAULT_GRID)
+    plain, rain2, ice2 = (runtime.run_bytes(g, Switches(rain_moments=r, ice_moments=i)) for r, i in ((1, 1), (2, 1), (2, 2)))
+    elec_ice2 = runtime.run_bytes(g, Switches(rain_moments=2, ice_moments=2, lightning=1))
+    assert plain == runtime.run_bytes(g) < rain2 < ice2 < elec_ice2
+    assert ice2 - rain2 >= 6 * g.n * 4  # graupel's and hail's three speeds each
+    assert runtime.run_bytes(g, Switches(rain_moments=1, ice_moments=2)) == plain
+    assert runtime.run_bytes(g, Switches(rain_moments=2, ice_moments=2, ice=0)) == rain2
