@@ -1395,10 +1395,12 @@ __global__ void k_fill_final(const RunDesc* __restrict__ runs, const int4* items
 // Per node: the positivity fix and the cold decay ('finish', :1253-1258), then physics(z) (:1347-1531): microphysics,
 // Coriolis and wind relaxation, surface fluxes (none in the single-storm mode), cold clamp, Rayleigh sponge.
 // In: set `in` (final RK3 values). Out: rain, snow, graupel, hail, cold -> set A; the mixed fields -> set `mid`.
-// ELEC: the kernel of a batch with electrified runs, which also moves their charge with the water and charges the
-// graupel and crystals after the microphysics (:1454-1469); the charges go to set A (they are not mixed).
-template <bool ELEC>
-__global__ void __launch_bounds__(256, ELEC ? 2 : 3) k_physics(const RunDesc* __restrict__ runs, const int4* items, int nitems, int in, int mid) {
+// A variant for each kind of run, so each runs only its own code (the plan launches each on its runs' items): ELEC, an
+// electrified run's, which also moves the charge with the water and charges the graupel and crystals after the
+// microphysics (:1454-1469; the charges go to set A, they are not mixed); MOM 1 one-moment microphysics, 2 two-moment
+// rain, 3 two-moment rain, graupel and hail (their numbers and volumes to set A).
+template <bool ELEC, int MOM>
+__global__ void __launch_bounds__(256, (ELEC || MOM == 3) ? 2 : 3) k_physics(const RunDesc* __restrict__ runs, const int4* items, int nitems, int in, int mid) {
   __shared__ double sh[32 * 4];
   FOR_ITEMS {
     const RunDesc& R = runs[items[it].x];
@@ -1412,7 +1414,7 @@ __global__ void __launch_bounds__(256, ELEC ? 2 : 3) k_physics(const RunDesc* __
 #pragma unroll
     for (int k = 0; k < NW; k++) whi[k] = wlo[k] = 0.f;
     bool bad = false;
-    const bool elec = ELEC && (R.flags & RF_ELEC);  // (ELEC: the kernel of a batch with extra fields)
+    constexpr bool elec = ELEC;
     for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
       const int z = i / R.layer;
       auto fixed = [&](int kc, float x) { return x < 1e-10f ? 0.f : fmaf(x, fill[kc], x); };
@@ -1435,15 +1437,13 @@ __global__ void __launch_bounds__(256, ELEC ? 2 : 3) k_physics(const RunDesc* __
       float evap, rnum = 0.f;
       i2m::Fields f2m = {0.f, 0.f, 0.f, 0.f};
       bool wet2G = false, wet2H = false;
-      if constexpr (ELEC) {
-        if (R.flags & RF_ICE2M) {
-          rnum = field(R, in, RAIN_NUMBER)[i];
-          f2m = {field(R, in, GRAUPEL_NUMBER)[i], field(R, in, GRAUPEL_VOLUME)[i], field(R, in, HAIL_NUMBER)[i], field(R, in, HAIL_VOLUME)[i]};
-          i2m::microphysics(s, rnum, f2m, pl, dt, R.flags, R.breakup, evap, wet2G, wet2H);
-        } else if (R.flags & RF_RAIN2M) {
-          rnum = field(R, in, RAIN_NUMBER)[i];
-          r2m::microphysics(s, rnum, pl, dt, R.flags, R.breakup, evap);
-        } else phys::microphysics(s, pl, dt, R.flags, evap);
+      if constexpr (MOM == 3) {
+        rnum = field(R, in, RAIN_NUMBER)[i];
+        f2m = {field(R, in, GRAUPEL_NUMBER)[i], field(R, in, GRAUPEL_VOLUME)[i], field(R, in, HAIL_NUMBER)[i], field(R, in, HAIL_VOLUME)[i]};
+        i2m::microphysics(s, rnum, f2m, pl, dt, R.flags, R.breakup, evap, wet2G, wet2H);
+      } else if constexpr (MOM == 2) {
+        rnum = field(R, in, RAIN_NUMBER)[i];
+        r2m::microphysics(s, rnum, pl, dt, R.flags, R.breakup, evap);
       } else phys::microphysics(s, pl, dt, R.flags, evap);
       if constexpr (ELEC) if (elec) {
         const float after[4] = {s.ice + s.snow, s.graupel + s.hail, s.rain, s.cloud};
@@ -1455,7 +1455,7 @@ __global__ void __launch_bounds__(256, ELEC ? 2 : 3) k_physics(const RunDesc* __
         bool wetG, wetH;
         charge::Moments two[2];
         int has = 0;
-        if (R.flags & RF_ICE2M) {
+        if constexpr (MOM == 3) {
           wetG = wet2G; wetH = wet2H;
           if (i2m::rimerMoments(i2m::GRAUPEL_2M(), s.graupel, f2m.gn, f2m.gv, rho, two[0])) has |= 1;
           if (i2m::rimerMoments(i2m::HAIL_2M(), s.hail, f2m.hn, f2m.hv, rho, two[1])) has |= 2;
@@ -1491,8 +1491,8 @@ __global__ void __launch_bounds__(256, ELEC ? 2 : 3) k_physics(const RunDesc* __
       field(R, 0, COLD)[i] = s.cold;
       field(R, mid, U)[i] = u; field(R, mid, V)[i] = v; field(R, mid, W)[i] = w; field(R, mid, THETA)[i] = s.thp;
       field(R, mid, Q)[i] = s.q; field(R, mid, CLOUD)[i] = s.cloud; field(R, mid, ICE)[i] = s.ice; field(R, mid, ICENUM)[i] = s.inum;
-      if constexpr (ELEC) if (R.flags & RF_RAIN2M) field(R, 0, RAIN_NUMBER)[i] = rnum;  // not mixed: straight to set A
-      if constexpr (ELEC) if (R.flags & RF_ICE2M) {
+      if constexpr (MOM >= 2) field(R, 0, RAIN_NUMBER)[i] = rnum;  // not mixed: straight to set A
+      if constexpr (MOM == 3) {
         field(R, 0, GRAUPEL_NUMBER)[i] = f2m.gn; field(R, 0, GRAUPEL_VOLUME)[i] = f2m.gv; field(R, 0, HAIL_NUMBER)[i] = f2m.hn; field(R, 0, HAIL_VOLUME)[i] = f2m.hv;
       }
     }
@@ -1833,10 +1833,16 @@ void launch_sediment_2m(const Launch& L, int maxnz) {
   else if (K == 3) k_sediment_2m<3><<<GRID(L.n, L.cap), SED2_WARPS * 32, 0, L.stream>>>(L.runs, L.items, L.n);
   else k_sediment_2m<4><<<GRID(L.n, L.cap), SED2_WARPS * 32, 0, L.stream>>>(L.runs, L.items, L.n);
 }
-void launch_physics(const Launch& L, int in, int mid, bool elec) {
+void launch_physics(const Launch& L, int in, int mid, int variant) {
   if (L.n == 0) return;
-  if (elec) k_physics<true><<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, in, mid);
-  else k_physics<false><<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, in, mid);
+  switch (variant) {  // (electrified ? 3 : 0) + moments - 1
+    case 0: k_physics<false, 1><<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, in, mid); break;
+    case 1: k_physics<false, 2><<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, in, mid); break;
+    case 2: k_physics<false, 3><<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, in, mid); break;
+    case 3: k_physics<true, 1><<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, in, mid); break;
+    case 4: k_physics<true, 2><<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, in, mid); break;
+    default: k_physics<true, 3><<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, in, mid); break;
+  }
 }
 void launch_viscosity(const Launch& L, int set) { k_viscosity<<<GRID(L.n, L.cap), 256, 0, L.stream>>>(L.runs, L.items, L.n, set); }
 size_t mix_smem(int TX, int TY) { return (size_t)2 * (NMIX + 1) * (TX + 2) * (TY + 2) * sizeof(float); }

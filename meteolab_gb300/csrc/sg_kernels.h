@@ -56,7 +56,8 @@ size_t transport_smem_bulk(int kind, int G, int TX, int TY);
 bool transport_bulk_ok(int TX, int TY, int min_nx, bool all_nx4);
 void launch_fill_partial(const Launch& L, int set);
 void launch_fill_final(const Launch& L);
-void launch_physics(const Launch& L, int in, int mid, bool elec);
+// variant: (electrified ? 3 : 0) + moments - 1 (1 one-moment, 2 two-moment rain, 3 two-moment rain, graupel and hail)
+void launch_physics(const Launch& L, int in, int mid, int variant);
 void launch_sediment_2m(const Launch& L, int maxnz);
 void launch_viscosity(const Launch& L, int set);
 // Mixing on (run, tile of TX x TY columns, z0, z1) items.

@@ -106,7 +106,7 @@ struct Plan {
   }
 };
 enum Family { FAM_NODE, FAM_COLS, FAM_ROWS_FACE, FAM_ROWS_PRES, FAM_MODES, FAM_RUNS, FAM_CELLS, FAM_T_WENO, FAM_T_DYN, FAM_MIX,
-              FAM_REFINE, FAM_T_CHG, FAM_T_CHG3, FAM_PHYS, FAM_PHYS_X, FAM_LROWS_FACE, FAM_LROWS_PRES, FAM_LMODES, FAM_COUNT };
+              FAM_REFINE, FAM_T_CHG, FAM_T_CHG3, FAM_PHYS, FAM_PHYS_LAST = FAM_PHYS + 5, FAM_LROWS_FACE, FAM_LROWS_PRES, FAM_LMODES, FAM_COUNT };
 
 }  // namespace
 
@@ -375,6 +375,11 @@ void charge_items(sg_context* ctx, const std::vector<int>& slots, int TX, int TY
   }
 }
 
+// The physics kernel variant of a run: (electrified ? 3 : 0) + its moments - 1 (k_physics<ELEC, MOM>).
+int physics_variant(int flags) {
+  return ((flags & RF_ELEC) ? 3 : 0) + ((flags & RF_ICE2M) ? 2 : (flags & RF_RAIN2M) ? 1 : 0);
+}
+
 int upload_items(sg_context* ctx, Plan& P, std::vector<int4>* all) {
   std::vector<int4> flat;
   for (int f = 0; f < FAM_COUNT; f++) { P.off[f] = (int)flat.size(); P.cnt[f] = (int)all[f].size(); flat.insert(flat.end(), all[f].begin(), all[f].end()); }
@@ -416,8 +421,8 @@ int build_plan(sg_context* ctx, const std::vector<int>& slots, Plan& P) {
     const Run& r = ctx->runs[s];
     int n = r.nx * r.ny * r.nz, nch = (n + CHUNK - 1) / CHUNK, layer = r.nx * r.ny;
     for (int c = 0; c < nch; c++) all[FAM_NODE].push_back(make_int4(s, c, 0, 0));
-    // the physics' node chunks by kernel: a run takes the same physics kernel whatever batch it is in
-    for (int c = 0; c < nch; c++) all[(r.desc.flags & RF_EXTRA) ? FAM_PHYS_X : FAM_PHYS].push_back(make_int4(s, c, 0, 0));
+    // the physics' node chunks by kernel variant: a run takes the same physics code whatever batch it is in
+    for (int c = 0; c < nch; c++) all[FAM_PHYS + physics_variant(r.desc.flags)].push_back(make_int4(s, c, 0, 0));
     int ncc = (r.nx * r.ny * (r.nz - 1) + CHUNK - 1) / CHUNK;
     for (int c = 0; c < ncc; c++) all[FAM_CELLS].push_back(make_int4(s, c, 0, 0));
     for (int c = 0; c < (layer + 63) / 64; c++) all[FAM_COLS].push_back(make_int4(s, c, 0, 0));
@@ -638,8 +643,8 @@ void enqueue_part(sg_context* ctx, const Plan& P, int part, Hook hook) {
   } else if (part == 3) {
     launch_fill_partial(node, B); hook(11);
     launch_fill_final(runs); hook(12);
-    launch_physics(lx(ctx, P, FAM_PHYS), B, C, false);
-    launch_physics(lx(ctx, P, FAM_PHYS_X), B, C, true); hook(13);
+    for (int v = 0; v < 6; v++) launch_physics(lx(ctx, P, FAM_PHYS + v), B, C, v);
+    hook(13);
   } else if (part == 4) {
     launch_viscosity(node, C); hook(14);
     Launch mx = lx(ctx, P, FAM_MIX);
