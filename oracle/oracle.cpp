@@ -2,6 +2,7 @@
 // see oracle_core.h). Loaded by oracle/pyoracle.py for tests/, __graft_entry__.smoke() and bench.py's CPU legs.
 #include "oracle_model.h"
 #include "oracle_diag.h"
+#include "oracle_terrain.h"
 
 using namespace orc;
 
@@ -421,6 +422,45 @@ void orc_turbulence(int nx, int ny, int nz, double dx, double dy, double dz, dou
   if (km) { std::memcpy(km, t.km.data(), g.n * 8); std::memcpy(kh, t.kh.data(), g.n * 8); }
   std::vector<float> tmp(g.n);
   if (a) for (int s = 0; s < steps; s++) t.mix<float>((Arr<float>)a, base, factor, dt, tmp);
+}
+
+// Terrain (terrain.ts): the heights of a form (kind 0 hill, 1 ridge, 2 plateau, 3 schar; NaN for an absent option).
+void orc_terrain_heights(int nx, int ny, int nz, double dx, double dy, double dz, double height, const double* zs, const double* dzs, const double* hz,
+                         int kind, double top, double width, double x, double y, double heading, double wavelength, float* out) {
+  GridSpec g = makeGrid(nx, ny, nz, dx, dy, dz, height, zs, dzs, hz);
+  std::vector<float> h = terrain::heights(terrain::Form{kind, top, width, x, y, heading, wavelength}, g);
+  std::memcpy(out, h.data(), h.size() * 4);
+}
+// The cut-cell geometry of ground heights: solid mask, ground levels, node heights, face apertures, slope areas.
+void orc_terrain_geometry(int nx, int ny, int nz, double dx, double dy, double dz, double height, const double* zs, const double* dzs, const double* hz,
+                          const float* ground, uint8_t* solid, int* levels, double* heights, double* ax, double* ay, float* slope) {
+  GridSpec g = makeGrid(nx, ny, nz, dx, dy, dz, height, zs, dzs, hz);
+  std::vector<uint8_t> s = terrain::solidMask(g, ground);
+  std::memcpy(solid, s.data(), s.size());
+  std::vector<int> lv = terrain::groundLevels(g, s.data());
+  std::memcpy(levels, lv.data(), lv.size() * 4);
+  std::vector<double> h = terrain::nodeHeights(g, s.data(), ground);
+  std::memcpy(heights, h.data(), h.size() * 8);
+  std::vector<double> a, b;
+  terrain::faceApertures(g, s.data(), ground, a, b);
+  std::memcpy(ax, a.data(), a.size() * 8); std::memcpy(ay, b.data(), b.size() * 8);
+  std::vector<float> sl = terrain::slopeArea(g, ground);
+  std::memcpy(slope, sl.data(), sl.size() * 4);
+}
+// MaskedProjection over ground heights: mask, the cut cells' divergence before, project, the divergence after.
+// stats = {iterations, residual}; dropped (cells) the cells without a row.
+void orc_masked_project(int nx, int ny, int nz, double dx, double dy, double dz, double height, const double* zs, const double* dzs, const double* hz,
+                        const double* rho, const float* ground, double tolerance, int maxIterations, float* u, float* v, float* w, double dt,
+                        double* pressure, double* before, double* after, double* stats, uint8_t* dropped) {
+  GridSpec g = makeGrid(nx, ny, nz, dx, dy, dz, height, zs, dzs, hz);
+  PressureSolver s(g, rho);
+  terrain::MaskedProjection m(g, s, ground, tolerance, maxIterations);
+  m.mask(u, v, w);
+  m.divergence(u, v, w, before);
+  m.project(u, v, w, dt, pressure);
+  m.divergence(u, v, w, after);
+  stats[0] = m.iterations; stats[1] = m.residual;
+  std::memcpy(dropped, m.dropped.data(), m.dropped.size());
 }
 
 }  // extern "C"

@@ -31,7 +31,7 @@ _f = C.POINTER(C.c_float)
 def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (plain g++/OpenMP)."""
     sources = [os.path.join(HERE, n) for n in ("oracle.cpp", "oracle_core.h", "oracle_solvers.h", "oracle_model.h", "oracle_diag.h",
-                                               "oracle_elec.h", "oracle_rain2m.h",
+                                               "oracle_elec.h", "oracle_rain2m.h", "oracle_ice2m.h", "oracle_terrain.h",
                                                os.path.join("..", "meteolab_gb300", "csrc", "sg_takahashi.h"))]
     if force or not os.path.exists(LIB_PATH) or any(os.path.getmtime(s) > os.path.getmtime(LIB_PATH) for s in sources):
         subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
@@ -139,6 +139,10 @@ def lib():
             L.orc_inductive_rate.restype = C.c_double
             L.orc_inductive_rate.argtypes = [C.c_double] * 7 + [C.c_int, C.c_int]
             L.orc_transfer_charge.argtypes = [_d, _d, _d]
+            _u8 = C.POINTER(C.c_uint8)
+            L.orc_terrain_heights.argtypes = grid_args + [C.c_int] + [C.c_double] * 6 + [_f]
+            L.orc_terrain_geometry.argtypes = grid_args + [_f, _u8, _i, _d, _d, _d, _f]
+            L.orc_masked_project.argtypes = grid_args + [_d, _f, C.c_double, C.c_int, _f, _f, _f, C.c_double, _d, _d, _d, _d, _u8]
             _lib = L
     return _lib
 
@@ -541,3 +545,45 @@ def charging_rate_2m(tc, rho, cloud, ice, snow, graupel, hail, snow_fall, wet_g=
         if x is not None:
             m[5 * j:5 * j + 5] = x
     return lib().orc_charging_rate_2m(tc, rho, cloud, ice, snow, graupel, hail, snow_fall, int(wet_g), int(wet_h), crystals, dp(m), has)
+
+
+TERRAIN_KINDS = {"hill": 0, "ridge": 1, "plateau": 2, "schar": 3}
+
+
+def terrain_heights(grid, kind: str, height: float, width: float, x=None, y=None, heading=None, wavelength=None) -> np.ndarray:
+    """terrainHeights (src/core/terrain.ts:37-63): the ground height of every column, m, float32 [ny*nx]."""
+    L = lib()
+    args, keep = grid_args(grid)
+    out = np.zeros(grid.nx * grid.ny, np.float32)
+    opt = [float("nan") if a is None else float(a) for a in (x, y, heading, wavelength)]
+    L.orc_terrain_heights(*args, TERRAIN_KINDS[kind], height, width, *opt, fp(out))
+    return out
+
+
+def terrain_geometry(grid, ground: np.ndarray) -> Dict[str, np.ndarray]:
+    """solidMask, groundLevels, nodeHeights, faceApertures and slopeArea (src/core/terrain.ts:80-150) of ground heights."""
+    L = lib()
+    args, keep = grid_args(grid)
+    g = np.ascontiguousarray(ground, dtype=np.float32)
+    n, layer = grid.nx * grid.ny * grid.nz, grid.nx * grid.ny
+    out = {"solid": np.zeros(n, np.uint8), "levels": np.zeros(layer, np.int32), "heights": np.zeros(n), "ax": np.zeros(n),
+           "ay": np.zeros(n), "slope": np.zeros(layer, np.float32)}
+    L.orc_terrain_geometry(*args, fp(g), out["solid"].ctypes.data_as(C.POINTER(C.c_uint8)), out["levels"].ctypes.data_as(C.POINTER(C.c_int)),
+                           dp(out["heights"]), dp(out["ax"]), dp(out["ay"]), fp(out["slope"]))
+    return out
+
+
+def masked_project(grid, rho, ground, u, v, w, dt, pressure=None, tolerance=1e-6, max_iterations=200):
+    """MaskedProjection (src/core/terrain.ts:168-363) as the reference's test drives it (terrain.test.ts:23-45): mask,
+    the cut cells' divergence before, project in place, the divergence after. Returns (u, v, w, pressure, before, after,
+    iterations, residual, dropped)."""
+    L = lib()
+    args, keep = grid_args(grid)
+    cells = grid.nx * grid.ny * (grid.nz - 1)
+    uu, vv, ww = (np.array(a, dtype=np.float32, copy=True) for a in (u, v, w))
+    p = np.zeros(cells) if pressure is None else np.array(pressure, dtype=np.float64, copy=True)
+    before, after, stats, dropped = np.zeros(cells), np.zeros(cells), np.zeros(2), np.zeros(cells, np.uint8)
+    r, g = f64(rho), np.ascontiguousarray(ground, dtype=np.float32)
+    L.orc_masked_project(*args, dp(r), fp(g), tolerance, max_iterations, fp(uu), fp(vv), fp(ww), dt, dp(p), dp(before), dp(after),
+                         dp(stats), dropped.ctypes.data_as(C.POINTER(C.c_uint8)))
+    return uu, vv, ww, p, before, after, int(stats[0]), float(stats[1]), dropped
