@@ -211,6 +211,41 @@ int sg_electric_create(sg_context* ctx, const sg_grid* grid, sg_electric** out);
 int sg_electric_solve(sg_electric* solver, const double* rho, double* phi);
 int sg_electric_destroy(sg_electric* solver);
 
+/* ---- terrain (src/core/terrain.ts): the ground as cut cells in the flat grid, and the projection that keeps the air
+ * out of it. A form (TerrainConfig, terrain.ts:16-27): heights and widths in km, the centre in km from the domain's
+ * south-west corner, the ridge's heading in degrees clockwise from north, the Schar ridges' wavelength in km; NaN for
+ * an absent option (the reference's defaults: the middle, north-south, 4 km). */
+enum sg_terrain_kind { SG_TERRAIN_HILL = 0, SG_TERRAIN_RIDGE = 1, SG_TERRAIN_PLATEAU = 2, SG_TERRAIN_SCHAR = 3 };
+typedef struct sg_terrain {
+  int32_t kind, reserved;
+  double height, width, x, y, heading, wavelength;
+} sg_terrain;
+/* terrainHeights (terrain.ts:37-63): the ground height of every column, m, into out[nx*ny]. Host arithmetic only. */
+int sg_terrain_heights(const sg_grid* grid, const sg_terrain* form, float* out);
+/* The cut-cell geometry of ground heights ground[nx*ny] (m), host arithmetic only; every output nullable:
+ * solidMask (:80-84) solid[n], groundLevels (:87-91) levels[nx*ny], nodeHeights (:101-105) heights[n],
+ * faceApertures (:119-134) ax[n] and ay[n], slopeArea (:141-150) slope[nx*ny]. */
+int sg_terrain_geometry(const sg_grid* grid, const float* ground, uint8_t* solid, int32_t* levels, double* heights, double* ax,
+                        double* ay, float* slope);
+/* MaskedProjection (terrain.ts:168-363) on the device: the node mass flux rho0 u made divergence-free over the dual
+ * cells cut by the ground, by preconditioned conjugate gradients (the flat spectral solve as the preconditioner) to
+ * `tolerance` of the first residual in at most `max_iterations`, FP64 throughout. sg_masked_create replaces
+ * `new MaskedProjection(grid, new PressureSolver(grid, rho), ground, tolerance, maxIterations)` (rho: nz base-state
+ * densities; ground: nx*ny heights, m); sg_masked_project replaces `project(u, v, w, dt, pressure)`: u, v, w host
+ * arrays of n floats projected in place, pressure the host array of nx*ny*(nz-1) cell values, the first guess in and
+ * the result out; sg_masked_mask and sg_masked_divergence replace `mask` and `divergence` (out: nx*ny*(nz-1));
+ * sg_masked_stats gives `iterations` and `residual` of the last projection and sg_masked_dropped the cells without a
+ * row (`dropped`, nullable outputs). */
+typedef struct sg_masked sg_masked;
+int sg_masked_create(sg_context* ctx, const sg_grid* grid, const double* rho, const float* ground, double tolerance, int max_iterations,
+                     sg_masked** out);
+int sg_masked_project(sg_masked* m, float* u, float* v, float* w, double dt, double* pressure);
+int sg_masked_mask(sg_masked* m, float* u, float* v, float* w);
+int sg_masked_divergence(sg_masked* m, const float* u, const float* v, const float* w, double* out);
+int sg_masked_stats(sg_masked* m, int32_t* iterations, double* residual);
+int sg_masked_dropped(sg_masked* m, uint8_t* dropped);
+int sg_masked_destroy(sg_masked* m);
+
 /* ---- per-run diagnostics (runs with switches.rotation). The rotation state after the last step (RotationState,
  * src/core/model.ts:263; the reference's field names) and the model time the device keeps for the swaths' ground shift. */
 typedef struct sg_rotation {

@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libstormgpu.so")
 OBJDIR = os.path.join(HERE, "_build")
 SOURCES = ["sg_kernels.cu", "sg_transport.cu", "sg_diag.cu", "sg_runtime.cu", "sg_static.cu", "sg_state.cu", "sg_electric.cu",
-           "sg_lightning.cu"]
+           "sg_lightning.cu", "sg_masked.cu"]
 HEADERS = ["sg_common.cuh", "sg_device.cuh", "sg_fft.cuh", "sg_physics.cuh", "sg_kernels.h", "sg_state.h", "sg_tile_copies.cuh",
            "sg_charge.cuh", "sg_takahashi.h", "sg_elec_solve.cuh", "sg_lightning.h", "sg_rain2m.cuh", "sg_ice2m.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

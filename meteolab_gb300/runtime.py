@@ -34,6 +34,11 @@ class SgGrid(C.Structure):
                 ("zs", C.POINTER(C.c_double)), ("dzs", C.POINTER(C.c_double)), ("hz", C.POINTER(C.c_double))]
 
 
+class SgTerrain(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("reserved", C.c_int32), ("height", C.c_double), ("width", C.c_double), ("x", C.c_double),
+                ("y", C.c_double), ("heading", C.c_double), ("wavelength", C.c_double)]
+
+
 class SgBase(C.Structure):
     _fields_ = [(k, C.POINTER(C.c_double)) for k in ("p", "exner", "theta", "q", "u", "v", "rho")]
 
@@ -126,6 +131,17 @@ def load():
             L.sg_electric_create.argtypes = [vp, C.POINTER(SgGrid), C.POINTER(vp)]
             L.sg_electric_solve.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
             L.sg_electric_destroy.argtypes = [vp]
+            _U8 = C.POINTER(C.c_uint8)
+            L.sg_terrain_heights.argtypes = [C.POINTER(SgGrid), C.POINTER(SgTerrain), _FP]
+            L.sg_terrain_geometry.argtypes = [C.POINTER(SgGrid), _FP, _U8, C.POINTER(C.c_int32), C.POINTER(C.c_double),
+                                              C.POINTER(C.c_double), C.POINTER(C.c_double), _FP]
+            L.sg_masked_create.argtypes = [vp, C.POINTER(SgGrid), C.POINTER(C.c_double), _FP, C.c_double, i32, C.POINTER(vp)]
+            L.sg_masked_project.argtypes = [vp, _FP, _FP, _FP, C.c_double, C.POINTER(C.c_double)]
+            L.sg_masked_mask.argtypes = [vp, _FP, _FP, _FP]
+            L.sg_masked_divergence.argtypes = [vp, _FP, _FP, _FP, C.POINTER(C.c_double)]
+            L.sg_masked_stats.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_double)]
+            L.sg_masked_dropped.argtypes = [vp, _U8]
+            L.sg_masked_destroy.argtypes = [vp]
             L.sg_batch_read_packed.argtypes = [vp, C.POINTER(C.c_int32), i32, C.c_uint32, _FP]
             L.sg_batch_step_io.argtypes = [vp, C.POINTER(C.c_int32), i32, C.c_uint32, _FP, i32, i32]
             L.sg_batch_step_round_trips.argtypes = [vp, C.POINTER(C.c_int32), i32, C.c_uint32, _FP, i32, i32]
@@ -679,6 +695,118 @@ class ElectricSolver:
     def close(self):
         if getattr(self, "h", None):
             load().sg_electric_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+TERRAIN_KINDS = {"hill": 0, "ridge": 1, "plateau": 2, "schar": 3}
+
+
+def _grid_struct(grid):
+    keep = (_f64(grid.zs), _f64(grid.dzs), _f64(grid.hz))
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    return SgGrid(grid.nx, grid.ny, grid.nz, 0, grid.dx, grid.dy, grid.height, dp(keep[0]), dp(keep[1]), dp(keep[2])), keep
+
+
+def terrain_heights(terrain: dict, grid) -> np.ndarray:
+    """terrainHeights (src/core/terrain.ts:37-63): the ground height of every column, m, float32 [ny*nx], of a terrain
+    form as SimConfig.terrain gives it: {kind: 'hill'|'ridge'|'plateau'|'schar', height, width (km), optional x, y (km),
+    heading (degrees), wavelength (km)}."""
+    nan = float("nan")
+    t = SgTerrain(TERRAIN_KINDS[terrain["kind"]], 0, float(terrain["height"]), float(terrain["width"]),
+                  *(float(terrain[k]) if terrain.get(k) is not None else nan for k in ("x", "y", "heading", "wavelength")))
+    g, keep = _grid_struct(grid)
+    out = np.zeros(grid.nx * grid.ny, np.float32)
+    if load().sg_terrain_heights(C.byref(g), C.byref(t), out.ctypes.data_as(_FP)) != 0:
+        raise StormGpuError(1, "terrain heights: an invalid grid or form")
+    return out
+
+
+def terrain_geometry(grid, ground) -> dict:
+    """The cut cells of ground heights (terrain.ts): solidMask, groundLevels, nodeHeights, faceApertures (ax, ay) and
+    slopeArea, computed by the library on the host."""
+    g, keep = _grid_struct(grid)
+    h = np.ascontiguousarray(ground, dtype=np.float32)
+    n, layer = grid.nx * grid.ny * grid.nz, grid.nx * grid.ny
+    if h.size != layer:
+        raise ValueError(f"ground must hold {layer} heights")
+    out = {"solid": np.zeros(n, np.uint8), "levels": np.zeros(layer, np.int32), "heights": np.zeros(n), "ax": np.zeros(n),
+           "ay": np.zeros(n), "slope": np.zeros(layer, np.float32)}
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    if load().sg_terrain_geometry(C.byref(g), h.ctypes.data_as(_FP), out["solid"].ctypes.data_as(C.POINTER(C.c_uint8)),
+                                  out["levels"].ctypes.data_as(C.POINTER(C.c_int32)), dp(out["heights"]), dp(out["ax"]), dp(out["ay"]),
+                                  out["slope"].ctypes.data_as(_FP)) != 0:
+        raise StormGpuError(1, "terrain geometry: an invalid grid or ground")
+    return out
+
+
+class MaskedProjection:
+    """The reference's MaskedProjection (src/core/terrain.ts:168-363) on the device: ``project(u, v, w, dt, pressure)``
+    makes the node mass flux rho0 u divergence-free over the dual cells cut by the ground, in place, by preconditioned
+    conjugate gradients around the flat spectral solve; ``pressure`` (nx*ny*(nz-1) cells) is the first guess and gets
+    the result. ``mask``, ``divergence``, ``iterations``, ``residual`` and ``dropped`` as the reference's."""
+
+    def __init__(self, ctx: Context, grid, rho, ground, tolerance: float = 1e-6, max_iterations: int = 200):
+        self.ctx, self.grid = ctx, grid
+        self._g, self._keep = _grid_struct(grid)
+        r = _f64(rho)
+        h = np.ascontiguousarray(ground, dtype=np.float32)
+        if r.size != grid.nz or h.size != grid.nx * grid.ny:
+            raise ValueError(f"rho needs {grid.nz} levels and ground {grid.nx * grid.ny} columns")
+        hnd = C.c_void_p()
+        ctx.check(load().sg_masked_create(ctx.h, C.byref(self._g), r.ctypes.data_as(C.POINTER(C.c_double)), h.ctypes.data_as(_FP),
+                                          tolerance, max_iterations, C.byref(hnd)), "masked projection")
+        self.h = hnd
+        self.cells = grid.nx * grid.ny * (grid.nz - 1)
+
+    def _fields(self, *arrays):
+        n = self.grid.nx * self.grid.ny * self.grid.nz
+        for a in arrays:
+            if a.dtype != np.float32 or not a.flags.c_contiguous or a.size != n:
+                raise ValueError(f"u, v and w must be contiguous float32 arrays of {n}")
+        return [a.ctypes.data_as(_FP) for a in arrays]
+
+    def project(self, u: np.ndarray, v: np.ndarray, w: np.ndarray, dt: float, pressure: np.ndarray) -> None:
+        if pressure.dtype != np.float64 or not pressure.flags.c_contiguous or pressure.size != self.cells:
+            raise ValueError(f"pressure must be a contiguous float64 array of {self.cells}")
+        self.ctx.check(load().sg_masked_project(self.h, *self._fields(u, v, w), dt, pressure.ctypes.data_as(C.POINTER(C.c_double))),
+                       "masked projection")
+
+    def mask(self, u: np.ndarray, v: np.ndarray, w: np.ndarray) -> None:
+        self.ctx.check(load().sg_masked_mask(self.h, *self._fields(u, v, w)), "masked projection")
+
+    def divergence(self, u: np.ndarray, v: np.ndarray, w: np.ndarray, out: Optional[np.ndarray] = None) -> np.ndarray:
+        out = np.empty(self.cells) if out is None else out
+        self.ctx.check(load().sg_masked_divergence(self.h, *self._fields(u, v, w), out.ctypes.data_as(C.POINTER(C.c_double))),
+                       "masked projection")
+        return out
+
+    @property
+    def iterations(self) -> int:
+        it = C.c_int32()
+        load().sg_masked_stats(self.h, C.byref(it), None)
+        return int(it.value)
+
+    @property
+    def residual(self) -> float:
+        r = C.c_double()
+        load().sg_masked_stats(self.h, None, C.byref(r))
+        return float(r.value)
+
+    @property
+    def dropped(self) -> np.ndarray:
+        out = np.zeros(self.cells, np.uint8)
+        load().sg_masked_dropped(self.h, out.ctypes.data_as(C.POINTER(C.c_uint8)))
+        return out
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().sg_masked_destroy(self.h)
             self.h = None
 
     def __del__(self):
