@@ -27,6 +27,7 @@
  *   discharge(ctx, run, time, dt)                             (AtmosphereModel.discharge, :1537-1552, on the charge
  *                                                             as it stands)
  */
+#include <math.h>
 #include <node_api.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -240,6 +241,100 @@ static napi_value electric_destroy(napi_env env, napi_callback_info info) {
   return NULL;
 }
 
+static void read_grid(napi_env env, napi_value obj, sg_grid* g) {
+  memset(g, 0, sizeof *g);
+  g->nx = (int32_t)get_num(env, obj, "nx"); g->ny = (int32_t)get_num(env, obj, "ny"); g->nz = (int32_t)get_num(env, obj, "nz");
+  g->dx = get_num(env, obj, "dx"); g->dy = get_num(env, obj, "dy"); g->height = get_num(env, obj, "height");
+  g->zs = typed_data(env, obj, "zs", NULL); g->dzs = typed_data(env, obj, "dzs", NULL); g->hz = typed_data(env, obj, "hz", NULL);
+}
+
+/* terrainHeights(grid, form) -> Float32Array: terrainHeights(form, grid) (src/core/terrain.ts:37-63); form as
+ * SimConfig.terrain: {kind: 'hill'|'ridge'|'plateau'|'schar', height, width, x?, y?, heading?, wavelength?}. */
+static napi_value terrain_heights_js(napi_env env, napi_callback_info info) {
+  size_t argc = 2; napi_value argv[2];
+  CHECK(env, napi_get_cb_info(env, info, &argc, argv, NULL, NULL));
+  sg_grid g; read_grid(env, argv[0], &g);
+  sg_terrain t; memset(&t, 0, sizeof t);
+  napi_value kind; char name[16] = {0}; size_t len = 0;
+  if (napi_get_named_property(env, argv[1], "kind", &kind) != napi_ok || napi_get_value_string_utf8(env, kind, name, sizeof name, &len) != napi_ok) {
+    napi_throw_type_error(env, NULL, "terrain: kind"); return NULL;
+  }
+  t.kind = !strcmp(name, "hill") ? SG_TERRAIN_HILL : !strcmp(name, "ridge") ? SG_TERRAIN_RIDGE : !strcmp(name, "plateau") ? SG_TERRAIN_PLATEAU
+         : !strcmp(name, "schar") ? SG_TERRAIN_SCHAR : -1;
+  t.height = get_num(env, argv[1], "height"); t.width = get_num(env, argv[1], "width");
+  t.x = get_num_or(env, argv[1], "x", NAN); t.y = get_num_or(env, argv[1], "y", NAN);
+  t.heading = get_num_or(env, argv[1], "heading", NAN); t.wavelength = get_num_or(env, argv[1], "wavelength", NAN);
+  const size_t columns = (size_t)(g.nx > 0 ? g.nx : 0) * (size_t)(g.ny > 0 ? g.ny : 0);
+  void* data = NULL; napi_value ab, out;
+  CHECK(env, napi_create_arraybuffer(env, columns * 4, &data, &ab));
+  CHECK(env, napi_create_typedarray(env, napi_float32_array, columns, ab, 0, &out));
+  if (sg_terrain_heights(&g, &t, (float*)data)) { napi_throw_error(env, NULL, "terrain: an invalid grid or form"); return NULL; }
+  return out;
+}
+
+/* maskedCreate(ctx, grid, rho: Float64Array, ground: Float32Array, tolerance = 1e-6, maxIterations = 200) -> handle:
+ * `new MaskedProjection(grid, new PressureSolver(grid, rho), ground, tolerance, maxIterations)` (terrain.ts:190). */
+static napi_value masked_create(napi_env env, napi_callback_info info) {
+  size_t argc = 6; napi_value argv[6];
+  CHECK(env, napi_get_cb_info(env, info, &argc, argv, NULL, NULL));
+  if (argc < 4) { napi_throw_type_error(env, NULL, "maskedCreate(ctx, grid, rho, ground, tolerance?, maxIterations?)"); return NULL; }
+  sg_context* ctx = ctx_of(env, argv[0]);
+  sg_grid g; read_grid(env, argv[1], &g);
+  napi_typedarray_type type; size_t len; void* rho; void* ground; napi_value buf; size_t off;
+  if (napi_get_typedarray_info(env, argv[2], &type, &len, &rho, &buf, &off) != napi_ok || type != napi_float64_array ||
+      napi_get_typedarray_info(env, argv[3], &type, &len, &ground, &buf, &off) != napi_ok || type != napi_float32_array) {
+    napi_throw_type_error(env, NULL, "rho: Float64Array, ground: Float32Array"); return NULL;
+  }
+  double tolerance = 1e-6, iterations = 200;
+  if (argc > 4) napi_get_value_double(env, argv[4], &tolerance);
+  if (argc > 5) napi_get_value_double(env, argv[5], &iterations);
+  sg_masked* m = NULL;
+  int st = sg_masked_create(ctx, &g, (const double*)rho, (const float*)ground, tolerance, (int)iterations, &m);
+  if (st) return throw_status(env, ctx, st);
+  napi_value ext;
+  CHECK(env, napi_create_external(env, m, NULL, NULL, &ext));
+  return ext;
+}
+
+/* maskedProject(ctx, m, u, v, w: Float32Array, dt, pressure: Float64Array) -> {iterations, residual}:
+ * MaskedProjection.project(u, v, w, dt, pressure) (terrain.ts:303-337), synchronous as the reference's. */
+static napi_value masked_project(napi_env env, napi_callback_info info) {
+  size_t argc = 7; napi_value argv[7];
+  CHECK(env, napi_get_cb_info(env, info, &argc, argv, NULL, NULL));
+  if (argc < 7) { napi_throw_type_error(env, NULL, "maskedProject(ctx, m, u, v, w, dt, pressure)"); return NULL; }
+  sg_context* ctx = ctx_of(env, argv[0]);
+  void* m = NULL; napi_get_value_external(env, argv[1], &m);
+  void* f[3]; void* p; napi_typedarray_type type; size_t len; napi_value buf; size_t off;
+  for (int k = 0; k < 3; k++)
+    if (napi_get_typedarray_info(env, argv[2 + k], &type, &len, &f[k], &buf, &off) != napi_ok || type != napi_float32_array) {
+      napi_throw_type_error(env, NULL, "u, v, w: Float32Array"); return NULL;
+    }
+  if (napi_get_typedarray_info(env, argv[6], &type, &len, &p, &buf, &off) != napi_ok || type != napi_float64_array) {
+    napi_throw_type_error(env, NULL, "pressure: Float64Array"); return NULL;
+  }
+  double dt = 0;
+  napi_get_value_double(env, argv[5], &dt);
+  int st = sg_masked_project((sg_masked*)m, (float*)f[0], (float*)f[1], (float*)f[2], dt, (double*)p);
+  if (st) return throw_status(env, ctx, st);
+  int32_t iterations = 0; double residual = 0;
+  sg_masked_stats((sg_masked*)m, &iterations, &residual);
+  napi_value out, a, b;
+  CHECK(env, napi_create_object(env, &out));
+  CHECK(env, napi_create_int32(env, iterations, &a));
+  CHECK(env, napi_create_double(env, residual, &b));
+  CHECK(env, napi_set_named_property(env, out, "iterations", a));
+  CHECK(env, napi_set_named_property(env, out, "residual", b));
+  return out;
+}
+
+static napi_value masked_destroy(napi_env env, napi_callback_info info) {
+  size_t argc = 1; napi_value argv[1];
+  CHECK(env, napi_get_cb_info(env, info, &argc, argv, NULL, NULL));
+  void* m = NULL; napi_get_value_external(env, argv[0], &m);
+  sg_masked_destroy((sg_masked*)m);
+  return NULL;
+}
+
 static napi_value fields_io(napi_env env, napi_callback_info info, int write) {
   size_t argc = 3; napi_value argv[3]; int32_t run;
   CHECK(env, napi_get_cb_info(env, info, &argc, argv, NULL, NULL));
@@ -444,6 +539,8 @@ static napi_value init(napi_env env, napi_value exports) {
     {"stepIo", 0, step_io, 0, 0, 0, napi_default, 0},
     {"electricCreate", 0, electric_create, 0, 0, 0, napi_default, 0}, {"electricSolve", 0, electric_solve, 0, 0, 0, napi_default, 0},
     {"electricDestroy", 0, electric_destroy, 0, 0, 0, napi_default, 0},
+    {"terrainHeights", 0, terrain_heights_js, 0, 0, 0, napi_default, 0}, {"maskedCreate", 0, masked_create, 0, 0, 0, napi_default, 0},
+    {"maskedProject", 0, masked_project, 0, 0, 0, napi_default, 0}, {"maskedDestroy", 0, masked_destroy, 0, 0, 0, napi_default, 0},
     {"readCharges", 0, read_charges, 0, 0, 0, napi_default, 0}, {"writeCharges", 0, write_charges, 0, 0, 0, napi_default, 0},
     {"readMoments", 0, read_moments, 0, 0, 0, napi_default, 0}, {"writeMoments", 0, write_moments, 0, 0, 0, napi_default, 0},
     {"charge", 0, charge, 0, 0, 0, napi_default, 0}, {"flashes", 0, flashes, 0, 0, 0, napi_default, 0},
