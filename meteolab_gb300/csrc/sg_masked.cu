@@ -371,26 +371,45 @@ __global__ void k_mp_ydft(const double2* __restrict__ in, double2* __restrict__ 
 
 // One mode a thread, the reference's Thomas sweep over the cell layers (pressure.ts:118-140) with the rows' lower
 // coefficients and pivots from the host; the forward values kept in place for the back substitution. A mode the
-// reference zeroes, and the pinned lowest cell of the uniform mode, have an infinite pivot.
+// reference zeroes, and the pinned lowest cell of the uniform mode, have an infinite pivot. The recurrence is a
+// dependent chain of FP64 divides: each eight layers' coefficients and right-hand sides are loaded before their eight
+// steps, so a step waits on the divide, not on memory.
+constexpr int THOMAS_AHEAD = 8;
 __global__ void k_mp_thomas(double2* __restrict__ S2, const double* __restrict__ lo, const double* __restrict__ cp,
                             const double* __restrict__ piv, int nc, int modes, const MpState* __restrict__ st, int skip) {
   if (st && (st->done & skip)) return;
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= modes) return;
   double2 d = make_double2(0, 0);
-  for (int k = 0; k < nc; k++) {
-    const size_t at = (size_t)k * modes + g;
-    const double2 r = S2[at];
-    const double a = lo[at], m = piv[at];
-    d = make_double2((r.x - a * d.x) / m, (r.y - a * d.y) / m);
-    S2[at] = d;
+  for (int k0 = 0; k0 < nc; k0 += THOMAS_AHEAD) {
+    double2 r[THOMAS_AHEAD];
+    double a[THOMAS_AHEAD], m[THOMAS_AHEAD];
+#pragma unroll
+    for (int q = 0; q < THOMAS_AHEAD; q++) {
+      const size_t at = (size_t)min(k0 + q, nc - 1) * modes + g;
+      r[q] = S2[at]; a[q] = lo[at]; m[q] = piv[at];
+    }
+#pragma unroll
+    for (int q = 0; q < THOMAS_AHEAD; q++)
+      if (k0 + q < nc) {
+        d = make_double2((r[q].x - a[q] * d.x) / m[q], (r[q].y - a[q] * d.y) / m[q]);
+        S2[(size_t)(k0 + q) * modes + g] = d;
+      }
   }
-  for (int k = nc - 2; k >= 0; k--) {
-    const size_t at = (size_t)k * modes + g;
-    const double c = cp[at];
-    const double2 v = S2[at];
-    d = make_double2(v.x - c * d.x, v.y - c * d.y);
-    S2[at] = d;
+  for (int k1 = nc - 2; k1 >= 0; k1 -= THOMAS_AHEAD) {
+    double2 v[THOMAS_AHEAD];
+    double c[THOMAS_AHEAD];
+#pragma unroll
+    for (int q = 0; q < THOMAS_AHEAD; q++) {
+      const size_t at = (size_t)max(k1 - q, 0) * modes + g;
+      v[q] = S2[at]; c[q] = cp[at];
+    }
+#pragma unroll
+    for (int q = 0; q < THOMAS_AHEAD; q++)
+      if (k1 - q >= 0) {
+        d = make_double2(v[q].x - c[q] * d.x, v[q].y - c[q] * d.y);
+        S2[(size_t)(k1 - q) * modes + g] = d;
+      }
   }
 }
 
