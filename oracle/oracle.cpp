@@ -463,4 +463,22 @@ void orc_masked_project(int nx, int ny, int nz, double dx, double dy, double dz,
   std::memcpy(dropped, m.dropped.data(), m.dropped.size());
 }
 
+// FluxTransport.setTerrain + setVelocityMasked (advection.ts:78-153) of float velocities over ground heights (the
+// model's set-up, model.ts:366-377: nodeHeights and faceApertures of the ground); faces and their divergence out,
+// stats = {iterations, residual}.
+void orc_masked_faces(int nx, int ny, int nz, double dx, double dy, double dz, double height, const double* zs, const double* dzs, const double* hz,
+                      const double* rho, const float* ground, double tolerance, int maxIterations, const float* u, const float* v, const float* w,
+                      double* mx, double* my, double* mz, double* div, double* stats) {
+  GridSpec g = makeGrid(nx, ny, nz, dx, dy, dz, height, zs, dzs, hz);
+  FluxTransport t(g, rho);
+  std::vector<uint8_t> solid = terrain::solidMask(g, ground);
+  std::vector<double> heights = terrain::nodeHeights(g, solid.data(), ground), ax, ay;
+  terrain::faceApertures(g, solid.data(), ground, ax, ay);
+  terrain::MaskedFaces m(g, t, solid.data(), heights.data(), ax, ay);
+  m.setVelocityMasked<float>((Arr<float>)u, (Arr<float>)v, (Arr<float>)w, tolerance, maxIterations);
+  std::memcpy(mx, t.mx.data(), g.n * 8); std::memcpy(my, t.my.data(), g.n * 8); std::memcpy(mz, t.mz.data(), g.n * 8);
+  std::memcpy(div, t.div.data(), g.n * 8);
+  stats[0] = m.iterations; stats[1] = m.residual;
+}
+
 }  // extern "C"

@@ -2,7 +2,8 @@
 // compared with, never linked into the product. Restates src/core/terrain.ts: the ground heights of a terrain form
 // (terrainHeights :37-63), the cut-cell geometry (volumeTop :72, solidMask :80-84, groundLevels :87-91, nodeHeights
 // :101-105, faceApertures :119-134, slopeArea :141-150) and MaskedProjection (:168-363), the cut-cell projection
-// solved by preconditioned conjugate gradients around the flat spectral solve (PressureSolver, oracle_solvers.h).
+// solved by preconditioned conjugate gradients around the flat spectral solve (PressureSolver, oracle_solvers.h); and
+// the transport's faces with terrain (src/core/advection.ts:78-184, MaskedFaces: setTerrain, setVelocityMasked).
 // JS semantics: doubles, Float32Array stores rounded to float, sums in the reference's order.
 #pragma once
 #include <cstdint>
@@ -274,6 +275,110 @@ struct MaskedProjection {
     for (int kk = 0; kk < g.nz; kk++) gradientPart(kk);
     for (size_t i = 0; i < (size_t)g.n; i++) { u[i] = (float)((double)u[i] + tu[i]); v[i] = (float)((double)v[i] + tv[i]); w[i] = (float)((double)w[i] + tw[i]); }
     mask(u, v, w);
+  }
+};
+
+// src/core/advection.ts:78-90, :96-105, :115-184: the transport's face fluxes with terrain. setTerrain's open faces
+// (bit 1 to x + 1, 2 to y + 1, 4 to z + 1: both nodes fluid) and node heights (1 in the ground), the apertures'
+// divergence, and setVelocityMasked: the faces of the node velocity, shut next to the ground, made divergence-free over
+// the fluid nodes by PCG on S phi = -h div(M rho0 grad phi) with the flat face solve as the preconditioner.
+struct MaskedFaces {
+  const GridSpec& g;
+  FluxTransport& t;
+  std::vector<uint8_t> open;
+  std::vector<double> hn, ax, ay, q, r, zz, d, sd, b, fx, fy, fz;
+  int iterations = 0; double residual = 0;
+  DftScratch ds; ModeScratch ms;
+
+  MaskedFaces(const GridSpec& grid, FluxTransport& tr, const uint8_t* solid, const double* heights, const std::vector<double>& apX,
+              const std::vector<double>& apY)
+      : g(grid), t(tr), ax(apX), ay(apY), ds(grid.nx, grid.ny), ms(grid.nz) {
+    const size_t n = g.n;
+    open.assign(n, 0); hn.assign(n, 0);
+    for (auto* a : {&q, &r, &zz, &d, &sd, &b, &fx, &fy, &fz}) a->assign(n, 0);
+    for (size_t i = 0; i < n; i++) hn[i] = solid[i] ? 1 : heights[i];
+    for (int z = 0, i = 0; z < g.nz; z++)
+      for (int y = 0; y < g.ny; y++)
+        for (int x = 0; x < g.nx; x++, i++) {
+          if (solid[i]) continue;
+          const int l = z * g.layer, e = g.xo[3][x] + y * g.nx + l, north = x + g.yo[3][y] + l;
+          if (!solid[e]) open[i] |= 1;
+          if (!solid[north]) open[i] |= 2;
+          if (z < g.nz - 1 && !solid[i + g.layer]) open[i] |= 4;
+        }
+  }
+
+  void terrainDivergence(double* out, const double* gx, const double* gy, const double* gz) const {  // :96-105
+    for (int z = 0, i = 0; z < g.nz; z++) {
+      const int l = z * g.layer;
+      for (int y = 0; y < g.ny; y++)
+        for (int x = 0; x < g.nx; x++, i++) {
+          const int w = g.xo[1][x] + y * g.nx + l, s = x + g.yo[1][y] + l;
+          out[i] = (ax[i] * gx[i] - ax[w] * gx[w]) / g.dx + (ay[i] * gy[i] - ay[s] * gy[s]) / g.dy + (gz[i] - (z > 0 ? gz[i - g.layer] : 0));
+        }
+    }
+  }
+
+  void maskedGradient(const double* phi, double sign, double* gx, double* gy, double* gz) const {  // :156-167
+    for (int z = 0, i = 0; z < g.nz; z++) {
+      const int l = z * g.layer; const double rr = t.rho[z], rUp = z < g.nz - 1 ? (t.rho[z] + t.rho[z + 1]) / 2 : 0;
+      for (int y = 0; y < g.ny; y++)
+        for (int x = 0; x < g.nx; x++, i++) {
+          const uint8_t o = open[i];
+          gx[i] += o & 1 ? sign * rr * (phi[g.xo[3][x] + y * g.nx + l] - phi[i]) / g.dx : 0;
+          gy[i] += o & 2 ? sign * rr * (phi[x + g.yo[3][y] + l] - phi[i]) / g.dy : 0;
+          gz[i] += o & 4 ? sign * rUp * (phi[i + g.layer] - phi[i]) / g.dzs[z] : 0;
+        }
+    }
+  }
+
+  void applyMasked(const double* dd, double* out) {  // :170-176
+    std::fill(fx.begin(), fx.end(), 0.0); std::fill(fy.begin(), fy.end(), 0.0); std::fill(fz.begin(), fz.end(), 0.0);
+    maskedGradient(dd, 1, fx.data(), fy.data(), fz.data());
+    terrainDivergence(out, fx.data(), fy.data(), fz.data());
+    for (size_t i = 0; i < (size_t)g.n; i++) out[i] = -out[i];
+  }
+
+  void flatSolve(const double* rv, double* out) {  // :179-184
+    for (size_t i = 0; i < (size_t)g.n; i++) t.div[i] = -rv[i] / g.hz[i / g.layer];
+    t.forward(0, g.nz, ds); t.modes(0, g.ny, ms); t.inverse(0, g.nz, ds);
+    std::copy(t.phi.begin(), t.phi.end(), out);
+  }
+
+  template <class S> void setVelocityMasked(Arr<S> u, Arr<S> v, Arr<S> w, double tolerance = 1e-10, int maxIterations = 400) {  // :115-153
+    const size_t n = g.n;
+    t.faces<S>(u, v, w, 0, g.nz);
+    for (size_t i = 0; i < n; i++) { if (!(open[i] & 1)) t.mx[i] = 0; if (!(open[i] & 2)) t.my[i] = 0; if (!(open[i] & 4)) t.mz[i] = 0; }
+    terrainDivergence(b.data(), t.mx.data(), t.my.data(), t.mz.data());
+    double bb = 0;
+    for (size_t i = 0; i < n; i++) { b[i] = -b[i]; bb += b[i] * b[i]; }
+    std::fill(q.begin(), q.end(), 0.0);
+    if (bb > 0) {
+      r = b;
+      flatSolve(r.data(), zz.data());
+      double rz = 0;
+      for (size_t i = 0; i < n; i++) { d[i] = zz[i]; rz += r[i] * zz[i]; }
+      int k = 0; double rr = bb;
+      for (; k < maxIterations && rr > tolerance * tolerance * bb; k++) {
+        applyMasked(d.data(), sd.data());
+        double dsd = 0;
+        for (size_t i = 0; i < n; i++) dsd += d[i] * sd[i];
+        if (!(dsd > 0)) break;
+        const double alpha = rz / dsd;
+        rr = 0;
+        for (size_t i = 0; i < n; i++) { q[i] += alpha * d[i]; r[i] -= alpha * sd[i]; rr += r[i] * r[i]; }
+        flatSolve(r.data(), zz.data());
+        double rzNew = 0;
+        for (size_t i = 0; i < n; i++) rzNew += r[i] * zz[i];
+        const double beta = rzNew / rz;
+        rz = rzNew;
+        for (size_t i = 0; i < n; i++) d[i] = zz[i] + beta * d[i];
+      }
+      iterations = k; residual = std::sqrt(rr / bb);
+    } else { iterations = 0; residual = 0; }
+    maskedGradient(q.data(), -1, t.mx.data(), t.my.data(), t.mz.data());
+    terrainDivergence(t.div.data(), t.mx.data(), t.my.data(), t.mz.data());
+    for (size_t i = 0; i < n; i++) t.div[i] /= hn[i];
   }
 };
 

@@ -142,6 +142,7 @@ def lib():
             _u8 = C.POINTER(C.c_uint8)
             L.orc_terrain_heights.argtypes = grid_args + [C.c_int] + [C.c_double] * 6 + [_f]
             L.orc_terrain_geometry.argtypes = grid_args + [_f, _u8, _i, _d, _d, _d, _f]
+            L.orc_masked_faces.argtypes = grid_args + [_d, _f, C.c_double, C.c_int, _f, _f, _f, _d, _d, _d, _d, _d]
             L.orc_masked_project.argtypes = grid_args + [_d, _f, C.c_double, C.c_int, _f, _f, _f, C.c_double, _d, _d, _d, _d, _u8]
             _lib = L
     return _lib
@@ -587,3 +588,16 @@ def masked_project(grid, rho, ground, u, v, w, dt, pressure=None, tolerance=1e-6
     L.orc_masked_project(*args, dp(r), fp(g), tolerance, max_iterations, fp(uu), fp(vv), fp(ww), dt, dp(p), dp(before), dp(after),
                          dp(stats), dropped.ctypes.data_as(C.POINTER(C.c_uint8)))
     return uu, vv, ww, p, before, after, int(stats[0]), float(stats[1]), dropped
+
+
+def masked_faces(grid, rho, ground, u, v, w, tolerance=1e-10, max_iterations=400):
+    """FluxTransport.setVelocityMasked (src/core/advection.ts:115-153) with the model's terrain set-up (model.ts:366-377):
+    the projected face mass fluxes mx, my, mz, their divergence over the node heights, iterations and residual."""
+    L = lib()
+    args, keep = grid_args(grid)
+    n = grid.nx * grid.ny * grid.nz
+    mx, my, mz, div, stats = np.zeros(n), np.zeros(n), np.zeros(n), np.zeros(n), np.zeros(2)
+    uu, vv, ww = (np.ascontiguousarray(a, dtype=np.float32) for a in (u, v, w))
+    L.orc_masked_faces(*args, dp(f64(rho)), fp(np.ascontiguousarray(ground, dtype=np.float32)), tolerance, max_iterations, fp(uu), fp(vv), fp(ww),
+                       dp(mx), dp(my), dp(mz), dp(div), dp(stats))
+    return mx, my, mz, div, int(stats[0]), float(stats[1])

@@ -119,3 +119,50 @@ def test_a_flat_ground_projects_as_without_terrain():
     args, keep = O.grid_args(GRID)
     O.lib().orc_pressure_project(*args, O.dp(O.f64(rho)), O.fp(pu), O.fp(pv), O.fp(pw), DT, O.dp(d0), O.dp(d1), O.dp(pp))
     assert np.array_equal(mu, pu) and np.array_equal(mv, pv) and np.array_equal(mw, pw) and np.array_equal(p, pp)
+
+
+def schar_case():
+    """terrain.test.ts:200-206: a 96 x 4 x 40 grid (48 x 2 x 15 km), a Schar ridge 100 m high (5 km envelope, 4 km
+    waves), a uniform 10 m/s westerly."""
+    g = create_grid(GridOptions(96, 4, 40, 48_000, 2_000, 15_000, bottom_spacing=100))
+    rho = 1.2 * np.exp(-np.asarray(g.zs) / 9000)
+    return g, rho, O.terrain_heights(g, "schar", .1, 5, wavelength=4)
+
+
+def test_the_transport_sees_the_ridge_the_projection_sees():  # terrain.test.ts:200-226
+    g, rho, h = schar_case()
+    n, layer = g.nx * g.ny * g.nz, g.nx * g.ny
+    U = np.full(n, 10, np.float32)
+    zero = np.zeros(n, np.float32)
+    u, v, w, *_ = O.masked_project(g, rho, h, U, zero, zero, 1.0)
+    mx, my, mz, div, iterations, residual = O.masked_faces(g, rho, h, U, zero, zero)
+    assert 0 < iterations < 400 and residual <= 1e-10
+    for height in (1400, 2200, 3200):
+        z = next(k for k, q in enumerate(g.zs) if q >= height)
+        node = (w[z * layer:(z + 1) * layer].astype(float) + w[(z + 1) * layer:(z + 2) * layer]) / 2
+        face = mz[z * layer:(z + 1) * layer] / ((rho[z] + rho[z + 1]) / 2)
+        ratio = float(face @ node) / float(node @ node)
+        assert (node @ node) > 0 and .98 < ratio < 1.03
+
+
+def test_the_faces_into_the_ground_are_shut_and_the_rest_divergence_free():
+    """setVelocityMasked (advection.ts:115-153) over a hill: no flux through a face next to a solid node, and the faces'
+    divergence over the node heights down to the tolerance of the first (the water cannot cross the ground)."""
+    rho, h, u, v, w = hill_case()
+    g = GRID
+    n, layer, nx = g.nx * g.ny * g.nz, g.nx * g.ny, g.nx
+    rng = np.random.default_rng(5)
+    w = rng.normal(0, 1, n).astype(np.float32)
+    solid = O.terrain_geometry(g, h)["solid"]
+    mx, my, mz, div, iterations, residual = O.masked_faces(g, rho, h, u, v, w)
+    assert iterations > 0 and residual <= 1e-10
+    i = np.arange(n)
+    c = i % layer
+    east = (c % nx + 1) % nx + (c // nx) * nx + (i // layer) * layer
+    north = c % nx + ((c // nx + 1) % g.ny) * nx + (i // layer) * layer
+    up = np.minimum(i + layer, n - 1)
+    assert (mx[(solid == 1) | (solid[east] == 1)] == 0).all() and (my[(solid == 1) | (solid[north] == 1)] == 0).all()
+    assert (mz[(solid == 1) | (solid[up] == 1) | (i >= n - layer)] == 0).all()
+    fluid = solid == 0
+    faces0 = O.masked_faces(g, rho, h, u, v, w, max_iterations=0)
+    assert np.abs(div[fluid]).max() < 1e-7 * np.abs(faces0[3][fluid]).max()
