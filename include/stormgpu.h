@@ -245,6 +245,20 @@ int sg_masked_divergence(sg_masked* m, const float* u, const float* v, const flo
 int sg_masked_stats(sg_masked* m, int32_t* iterations, double* residual);
 int sg_masked_dropped(sg_masked* m, uint8_t* dropped);
 int sg_masked_destroy(sg_masked* m);
+/* The transport's face fluxes with terrain (FluxTransport.setTerrain and setVelocityMasked, src/core/advection.ts:78-184)
+ * on the device: the face mass fluxes of the node velocity, shut next to the ground and made divergence-free over the
+ * fluid nodes with the faces' open heights, by preconditioned conjugate gradients (the flat face solve as the
+ * preconditioner) to `tolerance` of the first residual in at most `max_iterations` (the reference's 1e-10 and 400), FP64.
+ * sg_faces_create replaces `new FluxTransport(grid, rho)` with `setTerrain(solid, nodeHeights, faceApertures)` of the
+ * ground heights (as the model sets it up, src/core/model.ts:366-377); sg_faces_set_velocity replaces
+ * `setVelocityMasked(u, v, w)` and reading `mx`, `my`, `mz`, `div` (host arrays of n doubles, each nullable);
+ * sg_faces_stats gives `maskedIterations` and `maskedResidual`. */
+typedef struct sg_faces sg_faces;
+int sg_faces_create(sg_context* ctx, const sg_grid* grid, const double* rho, const float* ground, double tolerance, int max_iterations,
+                    sg_faces** out);
+int sg_faces_set_velocity(sg_faces* f, const float* u, const float* v, const float* w, double* mx, double* my, double* mz, double* div);
+int sg_faces_stats(sg_faces* f, int32_t* iterations, double* residual);
+int sg_faces_destroy(sg_faces* f);
 
 /* ---- per-run diagnostics (runs with switches.rotation). The rotation state after the last step (RotationState,
  * src/core/model.ts:263; the reference's field names) and the model time the device keeps for the swaths' ground shift. */

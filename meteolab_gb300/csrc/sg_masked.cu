@@ -148,10 +148,10 @@ void slope_area(const HostGrid& g, const float* h, float* area) {
 // 2 a zero right-hand side (nothing to project).
 struct MpState {
   double bb, tol2bb, rz, rr, alpha, beta, tolerance;
-  int k, done, maxIt, pad;
+  int k, done, maxIt, keepBB;
 };
 enum { STOP = 1, ZERO = 2, ANY = 3 };
-enum { R_BB, R_RZ0, R_RR, R_DSD, R_RZN };
+enum { R_BB, R_RZ0, R_RR, R_DSD, R_RZN, R_RR_KEEP, R_TEST };
 
 struct Geo {
   const uint8_t *solid, *wall, *dropped;
@@ -306,7 +306,7 @@ __global__ void __launch_bounds__(TPB) k_mp_reduce(MpState* __restrict__ st, con
   const double s = block_sum(v, sh);
   if (threadIdx.x != 0) return;
   if (OP == R_BB) {
-    st->bb = s; st->tol2bb = st->tolerance * st->tolerance * s; st->rr = 0; st->k = 0;
+    st->bb = s; st->tol2bb = st->tolerance * st->tolerance * s; st->rr = st->keepBB ? s : 0; st->k = 0;
     if (!(s > 0)) st->done = ZERO;
   } else if (OP == R_RZ0) {
     st->rz = s;
@@ -314,6 +314,10 @@ __global__ void __launch_bounds__(TPB) k_mp_reduce(MpState* __restrict__ st, con
   } else if (OP == R_RR) {
     st->rr = s;
     if (s <= st->tol2bb) st->done = STOP;
+  } else if (OP == R_RR_KEEP) {
+    st->rr = s;
+  } else if (OP == R_TEST) {
+    if (!(st->rr > st->tol2bb)) st->done = STOP;
   } else if (OP == R_DSD) {
     if (!(s > 0)) st->done = STOP;
     else st->alpha = st->rz / s;
@@ -324,13 +328,14 @@ __global__ void __launch_bounds__(TPB) k_mp_reduce(MpState* __restrict__ st, con
 }
 
 // Forward x-DFT of each cell row of scale * src: S1[k][m][y], m <= nx / 2.
-__global__ void k_mp_xdft(const double* __restrict__ src, double scale, double2* __restrict__ S1, const double2* __restrict__ twx, Geo g,
-                          int mh, const MpState* __restrict__ st, int skip) {
+// With `per` (the face solve): row = scale * src / per[k], the right-hand side over each level's height.
+__global__ void k_mp_xdft(const double* __restrict__ src, double scale, const double* __restrict__ per, double2* __restrict__ S1,
+                          const double2* __restrict__ twx, Geo g, int mh, const MpState* __restrict__ st, int skip) {
   extern __shared__ double row[];
   if (st && (st->done & skip)) return;
   const int y = blockIdx.x, k = blockIdx.y, nx = g.nx;
   const double* s = src + (size_t)k * g.layer + (size_t)y * nx;
-  for (int x = threadIdx.x; x < nx; x += blockDim.x) row[x] = scale * s[x];
+  for (int x = threadIdx.x; x < nx; x += blockDim.x) row[x] = per ? scale * s[x] / per[k] : scale * s[x];
   __syncthreads();
   for (int m = threadIdx.x; m <= mh; m += blockDim.x) {
     double re = 0, im = 0;
@@ -370,13 +375,15 @@ __global__ void k_mp_ydft(const double2* __restrict__ in, double2* __restrict__ 
 }
 
 // One mode a thread, the reference's Thomas sweep over the cell layers (pressure.ts:118-140) with the rows' lower
-// coefficients and pivots from the host; the forward values kept in place for the back substitution. A mode the
+// coefficients and pivots from the host (the face solve's right-hand sides times each level's height, rs); the forward
+// values kept in place for the back substitution. A mode the
 // reference zeroes, and the pinned lowest cell of the uniform mode, have an infinite pivot. The recurrence is a
 // dependent chain of FP64 divides: each eight layers' coefficients and right-hand sides are loaded before their eight
 // steps, so a step waits on the divide, not on memory.
 constexpr int THOMAS_AHEAD = 8;
 __global__ void k_mp_thomas(double2* __restrict__ S2, const double* __restrict__ lo, const double* __restrict__ cp,
-                            const double* __restrict__ piv, int nc, int modes, const MpState* __restrict__ st, int skip) {
+                            const double* __restrict__ piv, const double* __restrict__ rs, int nc, int modes, const MpState* __restrict__ st,
+                            int skip) {
   if (st && (st->done & skip)) return;
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= modes) return;
@@ -388,6 +395,7 @@ __global__ void k_mp_thomas(double2* __restrict__ S2, const double* __restrict__
     for (int q = 0; q < THOMAS_AHEAD; q++) {
       const size_t at = (size_t)min(k0 + q, nc - 1) * modes + g;
       r[q] = S2[at]; a[q] = lo[at]; m[q] = piv[at];
+      if (rs) { const double h = rs[min(k0 + q, nc - 1)]; r[q] = make_double2(h * r[q].x, h * r[q].y); }
     }
 #pragma unroll
     for (int q = 0; q < THOMAS_AHEAD; q++)
@@ -413,9 +421,10 @@ __global__ void k_mp_thomas(double2* __restrict__ S2, const double* __restrict__
   }
 }
 
-// Inverse x-DFT of each cell row from its half spectrum, / (nx ny). MASKED: the preconditioner's z = V phi, zero in the
-// dropped cells (:355), with the r.z partials; else the plain solution (the flat solve's pressure).
-template <bool MASKED>
+// Inverse x-DFT of each cell row from its half spectrum, / (nx ny). MODE 1: the preconditioner's z = V phi, zero in the
+// dropped cells (:355), with the r.z partials; 2: the plain solution with the r.z partials (the face solve's); 0: the
+// plain solution (the flat solve's pressure).
+template <int MODE>
 __global__ void k_mp_xidft(const double2* __restrict__ S1, double* __restrict__ out, const double* __restrict__ r, double* __restrict__ part,
                            const double2* __restrict__ twx, Geo g, int mh, const MpState* __restrict__ st, int skip) {
   extern __shared__ double2 zs[];
@@ -437,13 +446,11 @@ __global__ void k_mp_xidft(const double2* __restrict__ S1, double* __restrict__ 
     }
     const size_t c = (size_t)k * g.layer + (size_t)y * nx + x;
     double val = v * scale;
-    if (MASKED) {
-      val = g.dropped[c] ? 0 : val * g.dzs[k];
-      dot += r[c] * val;
-    }
+    if (MODE == 1) val = g.dropped[c] ? 0 : val * g.dzs[k];
+    if (MODE) dot += r[c] * val;
     out[c] = val;
   }
-  if (MASKED) {
+  if (MODE) {
     const double s = block_sum(dot, sh);
     if (threadIdx.x == 0) part[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = s;
   }
@@ -507,6 +514,106 @@ __global__ void k_mp_flat_correct(const double* __restrict__ p, float* __restric
   }
 }
 
+// ---------------------------------------------------------------- the transport's faces with terrain
+// (FluxTransport.setTerrain and setVelocityMasked, src/core/advection.ts:78-184): node vectors [n].
+
+struct FaceGeo {
+  const uint8_t* open;  // bit 1 the face to x + 1, 2 to y + 1, 4 to z + 1: both nodes fluid
+  const double *ax, *ay, *hn, *rho, *dzs;
+  int nx, ny, nz, layer;
+  size_t n;
+  double dx, dy;
+};
+
+struct Node {
+  int x, y, z;
+  size_t l, e, w, no, so;
+};
+__device__ __forceinline__ Node node_of(size_t i, const FaceGeo& g) {
+  Node a;
+  a.z = (int)(i / g.layer);
+  const int rem = (int)(i - (size_t)a.z * g.layer);
+  a.y = rem / g.nx; a.x = rem - a.y * g.nx;
+  a.l = (size_t)a.z * g.layer;
+  a.e = (size_t)(a.x + 1 == g.nx ? 0 : a.x + 1) + (size_t)a.y * g.nx + a.l;
+  a.w = (size_t)(a.x == 0 ? g.nx - 1 : a.x - 1) + (size_t)a.y * g.nx + a.l;
+  a.no = (size_t)a.x + (size_t)(a.y + 1 == g.ny ? 0 : a.y + 1) * g.nx + a.l;
+  a.so = (size_t)a.x + (size_t)(a.y == 0 ? g.ny - 1 : a.y - 1) * g.nx + a.l;
+  return a;
+}
+
+// faces (advection.ts:190-200) of the node velocity, shut where a face is not open (:120).
+__global__ void k_tm_faces(const float* __restrict__ u, const float* __restrict__ v, const float* __restrict__ w, double* __restrict__ mx,
+                           double* __restrict__ my, double* __restrict__ mz, FaceGeo g) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.n) return;
+  const Node a = node_of(i, g);
+  const uint8_t o = g.open[i];
+  const double r = g.rho[a.z];
+  mx[i] = o & 1 ? r * ((double)u[i] + (double)u[a.e]) / 2 : 0;
+  my[i] = o & 2 ? r * ((double)v[i] + (double)v[a.no]) / 2 : 0;
+  mz[i] = o & 4 ? (g.rho[a.z] + g.rho[a.z + 1]) / 2 * ((double)w[i] + (double)w[i + g.layer]) / 2 : 0;
+}
+
+// The apertures' divergence of the face fluxes (:96-105): MODE 0 b = -(h div) with the b.b partials, 1 div = h div / hn.
+template <int MODE>
+__global__ void __launch_bounds__(TPB) k_tm_tdiv(const double* __restrict__ mx, const double* __restrict__ my, const double* __restrict__ mz,
+                                                 double* __restrict__ out, double* __restrict__ part, FaceGeo g) {
+  __shared__ double sh[32];
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double dot = 0;
+  if (i < g.n) {
+    const Node a = node_of(i, g);
+    double v = (g.ax[i] * mx[i] - g.ax[a.w] * mx[a.w]) / g.dx + (g.ay[i] * my[i] - g.ay[a.so] * my[a.so]) / g.dy +
+               (mz[i] - (a.z > 0 ? mz[i - g.layer] : 0));
+    if (MODE == 0) { v = -v; dot = v * v; }
+    else v = v / g.hn[i];
+    out[i] = v;
+  }
+  if (MODE == 0) {
+    const double s = block_sum(dot, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+  }
+}
+
+// S d = -h div(M rho0 grad d) (:170-176) at each node from d at it and its six neighbours (each face flux as the
+// reference forms it), with the d.Sd partials.
+__global__ void __launch_bounds__(TPB) k_tm_apply(const double* __restrict__ d, double* __restrict__ out, double* __restrict__ part, FaceGeo g,
+                                                  const MpState* __restrict__ st) {
+  __shared__ double sh[32];
+  if (st->done) return;
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double dot = 0;
+  if (i < g.n) {
+    const Node a = node_of(i, g);
+    const double r = g.rho[a.z], di = d[i];
+    const uint8_t oi = g.open[i];
+    const double fxi = oi & 1 ? r * (d[a.e] - di) / g.dx : 0, fxw = g.open[a.w] & 1 ? r * (di - d[a.w]) / g.dx : 0;
+    const double fyi = oi & 2 ? r * (d[a.no] - di) / g.dy : 0, fys = g.open[a.so] & 2 ? r * (di - d[a.so]) / g.dy : 0;
+    const double fzi = oi & 4 ? (g.rho[a.z] + g.rho[a.z + 1]) / 2 * (d[i + g.layer] - di) / g.dzs[a.z] : 0;
+    const double fzb = a.z > 0 && (g.open[i - g.layer] & 4) ? (g.rho[a.z - 1] + g.rho[a.z]) / 2 * (di - d[i - g.layer]) / g.dzs[a.z - 1] : 0;
+    const double v = -((g.ax[i] * fxi - g.ax[a.w] * fxw) / g.dx + (g.ay[i] * fyi - g.ay[a.so] * fys) / g.dy + (fzi - fzb));
+    out[i] = v;
+    dot = di * v;
+  }
+  const double s = block_sum(dot, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// The fluxes lose M rho0 grad(q) (:150).
+__global__ void k_tm_correct(const double* __restrict__ q, double* __restrict__ mx, double* __restrict__ my, double* __restrict__ mz, FaceGeo g,
+                             const MpState* __restrict__ st) {
+  if (st->done & ZERO) return;
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.n) return;
+  const Node a = node_of(i, g);
+  const uint8_t o = g.open[i];
+  const double r = g.rho[a.z], qi = q[i];
+  mx[i] += o & 1 ? -r * (q[a.e] - qi) / g.dx : 0;
+  my[i] += o & 2 ? -r * (q[a.no] - qi) / g.dy : 0;
+  mz[i] += o & 4 ? -((g.rho[a.z] + g.rho[a.z + 1]) / 2) * (q[i + g.layer] - qi) / g.dzs[a.z] : 0;
+}
+
 int blocks(size_t count) { return (int)((count + TPB - 1) / TPB); }
 int threads_for(int count) { return std::min(256, std::max(32, (count + 31) / 32 * 32)); }
 
@@ -531,19 +638,63 @@ struct sg_masked {
   double residual = 0;
 };
 
+struct sg_faces {
+  sg_context* ctx = nullptr;
+  FaceGeo fg{};
+  Geo geo{};  // the node vectors as the shared kernels see them: cells = n, nc = nz
+  int mh = 0, modes = 0, maxIt = 400;
+  double tolerance = 1e-10;
+  char* mem = nullptr;
+  float *u = nullptr, *v = nullptr, *w = nullptr;
+  double *mx = nullptr, *my = nullptr, *mz = nullptr, *div = nullptr, *b = nullptr, *q = nullptr, *r = nullptr, *z = nullptr, *d = nullptr,
+         *sd = nullptr, *pDot = nullptr, *pRR = nullptr, *lo = nullptr, *cp = nullptr, *piv = nullptr, *hz = nullptr;
+  double2 *S1 = nullptr, *S2 = nullptr, *twx = nullptr, *twy = nullptr;
+  MpState* st = nullptr;
+  cudaGraphExec_t chunk = nullptr;
+  int iterations = 0;
+  double residual = 0;
+};
+
 namespace {
 
 constexpr int CHUNK = 8;
+
+// The face solve's preconditioner (flatSolve, advection.ts:179-184): div = -r / h, the flat face solve (forward,
+// modes with the right-hand sides times h, inverse) into z, with the r.z partials.
+void enqueue_face_precondition(sg_faces* f, cudaStream_t s, int skip) {
+  const Geo& g = f->geo;
+  const int nx = g.nx, ny = g.ny, nz = g.nc, mh = f->mh;
+  k_mp_xdft<<<dim3(ny, nz), threads_for(mh + 1), (size_t)nx * 8, s>>>(f->r, -1.0, f->hz, f->S1, f->twx, g, mh, f->st, skip);
+  k_mp_ydft<<<dim3(mh + 1, nz), threads_for(ny), (size_t)ny * 16, s>>>(f->S1, f->S2, f->twy, ny, mh, -1.0, f->st, skip);
+  k_mp_thomas<<<(f->modes + 63) / 64, 64, 0, s>>>(f->S2, f->lo, f->cp, f->piv, f->hz, nz, f->modes, f->st, skip);
+  k_mp_ydft<<<dim3(mh + 1, nz), threads_for(ny), (size_t)ny * 16, s>>>(f->S2, f->S1, f->twy, ny, mh, 1.0, f->st, skip);
+  k_mp_xidft<2><<<dim3(ny, nz), threads_for(nx), (size_t)(mh + 1) * 16, s>>>(f->S1, f->z, f->r, f->pDot, f->twx, g, mh, f->st, skip);
+}
+
+// One iteration of setVelocityMasked's loop (:127-145): the test on the last update's r.r, S d and d.Sd, alpha, the
+// update with its r.r kept, the preconditioner, beta, the new direction.
+void enqueue_face_iteration(sg_faces* f, cudaStream_t s) {
+  const Geo& g = f->geo;
+  const int nb = blocks(g.cells);
+  k_mp_reduce<R_TEST><<<1, TPB, 0, s>>>(f->st, f->pRR, 0, ANY);
+  k_tm_apply<<<nb, TPB, 0, s>>>(f->d, f->sd, f->pDot, f->fg, f->st);
+  k_mp_reduce<R_DSD><<<1, TPB, 0, s>>>(f->st, f->pDot, nb, ANY);
+  k_mp_update<<<nb, TPB, 0, s>>>(f->q, f->r, f->d, f->sd, f->pRR, g, f->st);
+  k_mp_reduce<R_RR_KEEP><<<1, TPB, 0, s>>>(f->st, f->pRR, nb, ANY);
+  enqueue_face_precondition(f, s, ANY);
+  k_mp_reduce<R_RZN><<<1, TPB, 0, s>>>(f->st, f->pDot, g.ny * g.nc, ANY);
+  k_mp_dir<<<nb, TPB, 0, s>>>(f->d, f->z, g, f->st, 0);
+}
 
 // The preconditioner z = P S0^-1 P r (:351-356): the flat solve of -r, z = V phi, with the r.z partials.
 void enqueue_precondition(sg_masked* m, cudaStream_t s, int skip) {
   const Geo& g = m->geo;
   const int nx = g.nx, ny = g.ny, nc = g.nc, mh = m->mh;
-  k_mp_xdft<<<dim3(ny, nc), threads_for(mh + 1), (size_t)nx * 8, s>>>(m->r, -1.0, m->S1, m->twx, g, mh, m->st, skip);
+  k_mp_xdft<<<dim3(ny, nc), threads_for(mh + 1), (size_t)nx * 8, s>>>(m->r, -1.0, nullptr, m->S1, m->twx, g, mh, m->st, skip);
   k_mp_ydft<<<dim3(mh + 1, nc), threads_for(ny), (size_t)ny * 16, s>>>(m->S1, m->S2, m->twy, ny, mh, -1.0, m->st, skip);
-  k_mp_thomas<<<(m->modes + 63) / 64, 64, 0, s>>>(m->S2, m->lo, m->cp, m->piv, nc, m->modes, m->st, skip);
+  k_mp_thomas<<<(m->modes + 63) / 64, 64, 0, s>>>(m->S2, m->lo, m->cp, m->piv, nullptr, nc, m->modes, m->st, skip);
   k_mp_ydft<<<dim3(mh + 1, nc), threads_for(ny), (size_t)ny * 16, s>>>(m->S2, m->S1, m->twy, ny, mh, 1.0, m->st, skip);
-  k_mp_xidft<true><<<dim3(ny, nc), threads_for(nx), (size_t)(mh + 1) * 16, s>>>(m->S1, m->z, m->r, m->pDot, m->twx, g, mh, m->st, skip);
+  k_mp_xidft<1><<<dim3(ny, nc), threads_for(nx), (size_t)(mh + 1) * 16, s>>>(m->S1, m->z, m->r, m->pDot, m->twx, g, mh, m->st, skip);
 }
 
 // One iteration of the loop (:314-329).
@@ -783,11 +934,11 @@ int sg_masked_project(sg_masked* m, float* u, float* v, float* w, double dt, dou
   if (!m->any) {
     // No terrain at all: the flat projection exactly (:336-339); the pressure is the flat solve's, not a first guess.
     k_mp_flat_div<<<cb, TPB, 0, s>>>(m->u, m->v, m->w, m->b, dt, g);
-    k_mp_xdft<<<dim3(ny, nc), threads_for(mh + 1), (size_t)nx * 8, s>>>(m->b, 1.0, m->S1, m->twx, g, mh, nullptr, 0);
+    k_mp_xdft<<<dim3(ny, nc), threads_for(mh + 1), (size_t)nx * 8, s>>>(m->b, 1.0, nullptr, m->S1, m->twx, g, mh, nullptr, 0);
     k_mp_ydft<<<dim3(mh + 1, nc), threads_for(ny), (size_t)ny * 16, s>>>(m->S1, m->S2, m->twy, ny, mh, -1.0, nullptr, 0);
-    k_mp_thomas<<<(m->modes + 63) / 64, 64, 0, s>>>(m->S2, m->lo, m->cp, m->piv, nc, m->modes, nullptr, 0);
+    k_mp_thomas<<<(m->modes + 63) / 64, 64, 0, s>>>(m->S2, m->lo, m->cp, m->piv, nullptr, nc, m->modes, nullptr, 0);
     k_mp_ydft<<<dim3(mh + 1, nc), threads_for(ny), (size_t)ny * 16, s>>>(m->S2, m->S1, m->twy, ny, mh, 1.0, nullptr, 0);
-    k_mp_xidft<false><<<dim3(ny, nc), threads_for(nx), (size_t)(mh + 1) * 16, s>>>(m->S1, m->p, nullptr, nullptr, m->twx, g, mh, nullptr, 0);
+    k_mp_xidft<0><<<dim3(ny, nc), threads_for(nx), (size_t)(mh + 1) * 16, s>>>(m->S1, m->p, nullptr, nullptr, m->twx, g, mh, nullptr, 0);
     k_mp_flat_correct<<<nb, TPB, 0, s>>>(m->p, m->u, m->v, m->w, dt, g);
   } else {
     MpState init{};
@@ -849,6 +1000,194 @@ int sg_masked_stats(sg_masked* m, int32_t* iterations, double* residual) {
 int sg_masked_dropped(sg_masked* m, uint8_t* dropped) {
   if (!m || !dropped) return SG_ERR_INVALID;
   std::memcpy(dropped, m->dropped.data(), m->dropped.size());
+  return SG_OK;
+}
+
+int sg_faces_create(sg_context* ctx, const sg_grid* grid, const double* rho, const float* ground, double tolerance, int max_iterations,
+                    sg_faces** out) {
+  if (!ctx || !out) return SG_ERR_INVALID;
+  *out = nullptr;
+  HostGrid g;
+  if (!host_grid(grid, g) || !rho || !ground)
+    return sg_context_fail(ctx, SG_ERR_INVALID, "masked faces: a grid with nx, ny >= 1, nz >= 3, dx, dy > 0, its level arrays, rho and the ground");
+  if (g.nx > 2048 || g.ny > 2048) return sg_context_fail(ctx, SG_ERR_INVALID, "masked faces: nx and ny at most 2048");
+  if (g.n > (size_t)1 << 30) return sg_context_fail(ctx, SG_ERR_INVALID, "masked faces: at most 2^30 nodes");
+  if (!(tolerance >= 0) || max_iterations < 0) return sg_context_fail(ctx, SG_ERR_INVALID, "masked faces: tolerance >= 0, max_iterations >= 0");
+  for (int k = 0; k < g.nz; k++)
+    if (!(g.hz[k] > 0) || (k < g.nz - 1 && !(g.dzs[k] > 0)) || !(rho[k] > 0))
+      return sg_context_fail(ctx, SG_ERR_INVALID, "masked faces: level spacings and densities must be positive");
+  for (int c = 0; c < g.layer; c++)
+    if (!std::isfinite(ground[c])) return sg_context_fail(ctx, SG_ERR_INVALID, "masked faces: finite ground heights");
+  if (cudaSetDevice(sg_context_device(ctx)) != cudaSuccess) return sg_context_fail(ctx, SG_ERR_DEVICE, "masked faces: cudaSetDevice");
+  const int nx = g.nx, ny = g.ny, nz = g.nz, layer = g.layer, mh = nx / 2, modes = (mh + 1) * ny;
+  const size_t n = g.n, spec = (size_t)nz * modes;
+
+  // setTerrain (advection.ts:78-90) with the model's geometry (model.ts:366-377): open faces, node heights (1 in the
+  // ground), the faces' open heights.
+  std::vector<uint8_t> solid(n), open(n, 0);
+  std::vector<int32_t> levels(layer);
+  std::vector<double> heights(n), hn(n), ax(n), ay(n);
+  solid_levels(g, ground, solid.data(), levels.data());
+  node_heights(g, solid.data(), levels.data(), ground, heights.data());
+  face_apertures(g, solid.data(), ground, ax.data(), ay.data());
+  for (size_t i = 0; i < n; i++) hn[i] = solid[i] ? 1 : heights[i];
+  for (int z = 0; z < nz; z++)
+    for (int y = 0; y < ny; y++)
+      for (int x = 0; x < nx; x++) {
+        const size_t i = x + (size_t)nx * y + (size_t)layer * z, l = (size_t)layer * z;
+        if (solid[i]) continue;
+        if (!solid[(x + 1) % nx + (size_t)nx * y + l]) open[i] |= 1;
+        if (!solid[x + (size_t)nx * ((y + 1) % ny) + l]) open[i] |= 2;
+        if (z < nz - 1 && !solid[i + layer]) open[i] |= 4;
+      }
+
+  // The flat face solve's rows per mode (advection.ts:222-241): each level's lower coefficient, pivot and cp in the
+  // reference's order; the uniform mode's pinned lowest level with an infinite pivot.
+  std::vector<double> tlo(spec, 0.0), tcp(spec, 0.0), tpiv(spec, 0.0);
+  auto face = [&](int k) { return k < 0 || k >= nz - 1 ? 0.0 : (rho[k] + rho[k + 1]) / 2; };
+  for (int m = 0; m <= mh; m++)
+    for (int q = 0; q < ny; q++) {
+      const double lam = m == 0 && q == 0 ? 0
+                                          : 4 * std::pow(std::sin(PI_ * m / nx), 2) / (g.dx * g.dx) + 4 * std::pow(std::sin(PI_ * q / ny), 2) / (g.dy * g.dy);
+      const bool pinned = lam == 0;
+      const size_t mode = (size_t)m * ny + q;
+      double cprev = 0;
+      for (int k = 0; k < nz; k++) {
+        double lo = k > 0 ? face(k - 1) / g.dzs[k - 1] : 0, up = k < nz - 1 ? face(k) / g.dzs[k] : 0, di = -rho[k] * g.hz[k] * lam - lo - up;
+        bool zero = false;
+        if (pinned && k == 0) { lo = 0; di = 1; up = 0; zero = true; }
+        if (pinned && k == 1) lo = 0;
+        const double piv = k == 0 ? di : di - lo * cprev;
+        cprev = up / piv;
+        const size_t at = (size_t)k * modes + mode;
+        tlo[at] = lo; tcp[at] = cprev; tpiv[at] = zero ? INFINITY : piv;
+      }
+    }
+  std::vector<double2> tx(nx), ty(ny);
+  for (int t = 0; t < nx; t++) tx[t] = make_double2(std::cos(2 * PI_ * t / nx), std::sin(2 * PI_ * t / nx));
+  for (int t = 0; t < ny; t++) ty[t] = make_double2(std::cos(2 * PI_ * t / ny), std::sin(2 * PI_ * t / ny));
+
+  auto al = [](size_t bytes) { return (bytes + 255) / 256 * 256; };
+  const size_t nparts = std::max((size_t)blocks(n), (size_t)ny * nz);
+  size_t off = 0;
+  auto take = [&](size_t bytes) { const size_t o = off; off += al(bytes); return o; };
+  const size_t oU = take(n * 4), oV = take(n * 4), oW = take(n * 4), oMx = take(n * 8), oMy = take(n * 8), oMz = take(n * 8), oDiv = take(n * 8),
+               oB = take(n * 8), oQ = take(n * 8), oR = take(n * 8), oZ = take(n * 8), oD = take(n * 8), oSd = take(n * 8), oPd = take(nparts * 8),
+               oPr = take(nparts * 8), oLo = take(spec * 8), oCp = take(spec * 8), oPv = take(spec * 8), oS1 = take(spec * 16), oS2 = take(spec * 16),
+               oTx = take((size_t)nx * 16), oTy = take((size_t)ny * 16), oSt = take(sizeof(MpState)), oOpen = take(n), oAx = take(n * 8),
+               oAy = take(n * 8), oHn = take(n * 8), oRho = take((size_t)nz * 8), oDz = take((size_t)nz * 8), oHz = take((size_t)nz * 8), total = off;
+  auto* f = new sg_faces;
+  f->ctx = ctx; f->mh = mh; f->modes = modes; f->maxIt = max_iterations; f->tolerance = tolerance;
+  cudaError_t e = cudaMalloc(&f->mem, total);
+  if (e != cudaSuccess) { delete f; cudaGetLastError(); return sg_context_fail(ctx, SG_ERR_BUDGET, "masked faces: device memory"); }
+  char* M = f->mem;
+  f->u = (float*)(M + oU); f->v = (float*)(M + oV); f->w = (float*)(M + oW);
+  f->mx = (double*)(M + oMx); f->my = (double*)(M + oMy); f->mz = (double*)(M + oMz); f->div = (double*)(M + oDiv); f->b = (double*)(M + oB);
+  f->q = (double*)(M + oQ); f->r = (double*)(M + oR); f->z = (double*)(M + oZ); f->d = (double*)(M + oD); f->sd = (double*)(M + oSd);
+  f->pDot = (double*)(M + oPd); f->pRR = (double*)(M + oPr); f->lo = (double*)(M + oLo); f->cp = (double*)(M + oCp); f->piv = (double*)(M + oPv);
+  f->S1 = (double2*)(M + oS1); f->S2 = (double2*)(M + oS2); f->twx = (double2*)(M + oTx); f->twy = (double2*)(M + oTy); f->st = (MpState*)(M + oSt);
+  f->hz = (double*)(M + oHz);
+  FaceGeo& F = f->fg;
+  F.open = (const uint8_t*)(M + oOpen); F.ax = (const double*)(M + oAx); F.ay = (const double*)(M + oAy); F.hn = (const double*)(M + oHn);
+  F.rho = (const double*)(M + oRho); F.dzs = (const double*)(M + oDz);
+  F.nx = nx; F.ny = ny; F.nz = nz; F.layer = layer; F.n = n; F.dx = g.dx; F.dy = g.dy;
+  Geo& G = f->geo;
+  G.nx = nx; G.ny = ny; G.nz = nz; G.layer = layer; G.nc = nz; G.n = n; G.cells = n; G.dx = g.dx; G.dy = g.dy;
+  cudaStream_t st = sg_context_stream(ctx);
+  std::vector<double> dz(nz, 0.0);
+  std::copy(g.dzs, g.dzs + nz - 1, dz.begin());
+  struct Up { size_t off; const void* src; size_t bytes; };
+  const Up ups[] = {{oLo, tlo.data(), spec * 8}, {oCp, tcp.data(), spec * 8}, {oPv, tpiv.data(), spec * 8}, {oTx, tx.data(), (size_t)nx * 16},
+                    {oTy, ty.data(), (size_t)ny * 16}, {oOpen, open.data(), n}, {oAx, ax.data(), n * 8}, {oAy, ay.data(), n * 8},
+                    {oHn, hn.data(), n * 8}, {oRho, rho, (size_t)nz * 8}, {oDz, dz.data(), (size_t)nz * 8}, {oHz, g.hz, (size_t)nz * 8}};
+  for (const Up& up : ups)
+    if ((e = cudaMemcpyAsync(M + up.off, up.src, up.bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess) break;
+  if (e == cudaSuccess) e = cudaMemsetAsync(f->d, 0, n * 8, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    cudaFree(f->mem); delete f;
+    return sg_context_fail(ctx, SG_ERR_DEVICE, (std::string("masked faces: ") + cudaGetErrorString(e)).c_str());
+  }
+  *out = f;
+  return SG_OK;
+}
+
+int sg_faces_set_velocity(sg_faces* f, const float* u, const float* v, const float* w, double* mx, double* my, double* mz, double* div) {
+  if (!f) return SG_ERR_INVALID;
+  if (!u || !v || !w) return sg_context_fail(f->ctx, SG_ERR_INVALID, "masked faces: u, v and w buffers");
+  cudaSetDevice(sg_context_device(f->ctx));
+  cudaStream_t s = sg_context_stream(f->ctx);
+  const Geo& g = f->geo;
+  const size_t n = g.n;
+  const int nb = blocks(n);
+  auto fail_f = [&](const char* what, cudaError_t e) {
+    return sg_context_fail(f->ctx, SG_ERR_DEVICE, (std::string("masked faces: ") + what + ": " + cudaGetErrorString(e)).c_str());
+  };
+  cudaError_t e;
+  const float* host[3] = {u, v, w};
+  float* dev[3] = {f->u, f->v, f->w};
+  for (int k = 0; k < 3; k++)
+    if ((e = cudaMemcpyAsync(dev[k], host[k], n * 4, cudaMemcpyHostToDevice, s)) != cudaSuccess) return fail_f("copy in", e);
+  MpState init{};
+  init.tolerance = f->tolerance; init.maxIt = f->maxIt; init.keepBB = 1;
+  if ((e = cudaMemcpyAsync(f->st, &init, sizeof(MpState), cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+      (e = cudaMemsetAsync(f->q, 0, n * 8, s)) != cudaSuccess)
+    return fail_f("state", e);
+  // faces, shut next to the ground; b = -h div, bb (= the first rr); r = b; z = S0^-1 r, rz; d = z (:117-126).
+  k_tm_faces<<<nb, TPB, 0, s>>>(f->u, f->v, f->w, f->mx, f->my, f->mz, f->fg);
+  k_tm_tdiv<0><<<nb, TPB, 0, s>>>(f->mx, f->my, f->mz, f->b, f->pRR, f->fg);
+  k_mp_reduce<R_BB><<<1, TPB, 0, s>>>(f->st, f->pRR, nb, 0);
+  if ((e = cudaMemcpyAsync(f->r, f->b, n * 8, cudaMemcpyDeviceToDevice, s)) != cudaSuccess) return fail_f("copy", e);
+  enqueue_face_precondition(f, s, ZERO);
+  k_mp_reduce<R_RZ0><<<1, TPB, 0, s>>>(f->st, f->pDot, g.ny * g.nc, ZERO);
+  k_mp_dir<<<nb, TPB, 0, s>>>(f->d, f->z, g, f->st, 1);
+  if ((e = cudaGetLastError()) != cudaSuccess) return fail_f("launch", e);
+  if (!f->chunk) {
+    cudaGraph_t graph = nullptr;
+    if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return fail_f("capture", e);
+    for (int it = 0; it < CHUNK; it++) enqueue_face_iteration(f, s);
+    e = cudaStreamEndCapture(s, &graph);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&f->chunk, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (e != cudaSuccess) { f->chunk = nullptr; return fail_f("graph", e); }
+  }
+  int done = 0;
+  for (int c = 0;; c++) {
+    if ((e = cudaMemcpyAsync(&done, &f->st->done, 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess || (e = cudaStreamSynchronize(s)) != cudaSuccess)
+      return fail_f("solve", e);
+    if (done || c > f->maxIt / CHUNK + 1) break;
+    if ((e = cudaGraphLaunch(f->chunk, s)) != cudaSuccess) return fail_f("graph launch", e);
+  }
+  if (!done) return sg_context_fail(f->ctx, SG_ERR_DEVICE, "masked faces: the iterations did not stop");
+  // The fluxes lose M rho0 grad(q); div the apertures' divergence over the node heights (:150-152).
+  k_tm_correct<<<nb, TPB, 0, s>>>(f->q, f->mx, f->my, f->mz, f->fg, f->st);
+  k_tm_tdiv<1><<<nb, TPB, 0, s>>>(f->mx, f->my, f->mz, f->div, nullptr, f->fg);
+  MpState fin{};
+  if ((e = cudaMemcpyAsync(&fin, f->st, sizeof(MpState), cudaMemcpyDeviceToHost, s)) != cudaSuccess) return fail_f("state", e);
+  double* outs[4] = {mx, my, mz, div};
+  const double* devs[4] = {f->mx, f->my, f->mz, f->div};
+  for (int k = 0; k < 4; k++)
+    if (outs[k] && (e = cudaMemcpyAsync(outs[k], devs[k], n * 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return fail_f("copy out", e);
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess || (e = cudaGetLastError()) != cudaSuccess) return fail_f("faces", e);
+  if (fin.done == ZERO) { f->iterations = 0; f->residual = 0; }
+  else { f->iterations = fin.k; f->residual = std::sqrt(fin.rr / fin.bb); }
+  return SG_OK;
+}
+
+int sg_faces_stats(sg_faces* f, int32_t* iterations, double* residual) {
+  if (!f) return SG_ERR_INVALID;
+  if (iterations) *iterations = f->iterations;
+  if (residual) *residual = f->residual;
+  return SG_OK;
+}
+
+int sg_faces_destroy(sg_faces* f) {
+  if (!f) return SG_ERR_INVALID;
+  cudaSetDevice(sg_context_device(f->ctx));
+  cudaStreamSynchronize(sg_context_stream(f->ctx));
+  if (f->chunk) cudaGraphExecDestroy(f->chunk);
+  cudaFree(f->mem);
+  delete f;
   return SG_OK;
 }
 

@@ -142,6 +142,11 @@ def load():
             L.sg_masked_stats.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_double)]
             L.sg_masked_dropped.argtypes = [vp, _U8]
             L.sg_masked_destroy.argtypes = [vp]
+            _D = C.POINTER(C.c_double)
+            L.sg_faces_create.argtypes = [vp, C.POINTER(SgGrid), _D, _FP, C.c_double, i32, C.POINTER(vp)]
+            L.sg_faces_set_velocity.argtypes = [vp, _FP, _FP, _FP, _D, _D, _D, _D]
+            L.sg_faces_stats.argtypes = [vp, C.POINTER(C.c_int32), _D]
+            L.sg_faces_destroy.argtypes = [vp]
             L.sg_batch_read_packed.argtypes = [vp, C.POINTER(C.c_int32), i32, C.c_uint32, _FP]
             L.sg_batch_step_io.argtypes = [vp, C.POINTER(C.c_int32), i32, C.c_uint32, _FP, i32, i32]
             L.sg_batch_step_round_trips.argtypes = [vp, C.POINTER(C.c_int32), i32, C.c_uint32, _FP, i32, i32]
@@ -807,6 +812,59 @@ class MaskedProjection:
     def close(self):
         if getattr(self, "h", None):
             load().sg_masked_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class TerrainFaces:
+    """The reference's transport faces with terrain (FluxTransport.setTerrain and setVelocityMasked,
+    src/core/advection.ts:78-184) on the device: ``set_velocity_masked(u, v, w)`` returns the face mass fluxes
+    (mx, my, mz) of the node velocity, shut next to the ground and divergence-free over the fluid nodes with the faces'
+    open heights, and their divergence over the node heights (div); ``iterations`` and ``residual`` as the reference's
+    maskedIterations and maskedResidual."""
+
+    def __init__(self, ctx: Context, grid, rho, ground, tolerance: float = 1e-10, max_iterations: int = 400):
+        self.ctx, self.grid = ctx, grid
+        self._g, self._keep = _grid_struct(grid)
+        r = _f64(rho)
+        h = np.ascontiguousarray(ground, dtype=np.float32)
+        if r.size != grid.nz or h.size != grid.nx * grid.ny:
+            raise ValueError(f"rho needs {grid.nz} levels and ground {grid.nx * grid.ny} columns")
+        hnd = C.c_void_p()
+        ctx.check(load().sg_faces_create(ctx.h, C.byref(self._g), r.ctypes.data_as(C.POINTER(C.c_double)), h.ctypes.data_as(_FP),
+                                         tolerance, max_iterations, C.byref(hnd)), "masked faces")
+        self.h = hnd
+
+    def set_velocity_masked(self, u: np.ndarray, v: np.ndarray, w: np.ndarray):
+        n = self.grid.nx * self.grid.ny * self.grid.nz
+        fields = [np.ascontiguousarray(a, dtype=np.float32) for a in (u, v, w)]
+        if any(a.size != n for a in fields):
+            raise ValueError(f"u, v and w must hold {n} values")
+        out = [np.empty(n) for _ in range(4)]
+        dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+        self.ctx.check(load().sg_faces_set_velocity(self.h, *[a.ctypes.data_as(_FP) for a in fields], *[dp(a) for a in out]), "masked faces")
+        return tuple(out)
+
+    @property
+    def iterations(self) -> int:
+        it = C.c_int32()
+        load().sg_faces_stats(self.h, C.byref(it), None)
+        return int(it.value)
+
+    @property
+    def residual(self) -> float:
+        r = C.c_double()
+        load().sg_faces_stats(self.h, None, C.byref(r))
+        return float(r.value)
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().sg_faces_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -137,3 +137,65 @@ def test_calm_air_and_a_short_solve(ctx):
     m, (du, dv, dw, dp), ref = both(ctx, g, h, u, zero, zero, np.zeros(cells), max_iterations=3)
     assert m.iterations == 3 and ref[6] == 3
     assert abs(m.residual - ref[7]) < 1e-6 * ref[7] and rel(dw, ref[2]) < 1e-5
+
+
+def faces_both(ctx, grid, ground, u, v, w, **kw):
+    from meteolab_gb300.runtime import TerrainFaces
+    f = TerrainFaces(ctx, grid, density(grid), ground, **kw)
+    mine = f.set_velocity_masked(u, v, w)
+    ref = O.masked_faces(grid, density(grid), ground, u, v, w, **kw)
+    return f, mine, ref
+
+
+def test_transport_faces_over_a_hill_match_the_oracle(ctx):
+    """setVelocityMasked (advection.ts:115-153) on the device against the oracle: a westerly with random vertical
+    motion over the hill; the faces into the ground shut, the fluid nodes' divergence at the solve's tolerance."""
+    from meteolab_gb300.runtime import terrain_geometry, terrain_heights
+    g = TEST_GRID
+    n, layer, nx = g.nx * g.ny * g.nz, g.nx * g.ny, g.nx
+    h = terrain_heights({"kind": "hill", "height": 1, "width": 5}, g)
+    rng = np.random.default_rng(5)
+    u = np.full(n, 10, np.float32)
+    v = np.zeros(n, np.float32)
+    w = rng.normal(0, 1, n).astype(np.float32)
+    f, (mx, my, mz, div), (rmx, rmy, rmz, rdiv, iterations, residual) = faces_both(ctx, g, h, u, v, w)
+    assert abs(f.iterations - iterations) <= 1 and f.residual <= 1e-10
+    assert rel(mx, rmx) < 1e-8 and rel(my, rmy) < 1e-8 and rel(mz, rmz) < 1e-8
+    solid = terrain_geometry(g, h)["solid"]
+    i = np.arange(n)
+    c = i % layer
+    east = (c % nx + 1) % nx + (c // nx) * nx + (i // layer) * layer
+    assert (mx[(solid == 1) | (solid[east] == 1)] == 0).all()
+    fluid = solid == 0
+    assert np.abs(div[fluid]).max() < 1e-6 * np.abs(rmz).max() / min(g.hz)
+
+
+def test_the_transport_sees_the_ridge_the_projection_sees_on_the_device(ctx):  # terrain.test.ts:200-226
+    from meteolab_gb300.runtime import MaskedProjection, terrain_heights
+    g = create_grid(GridOptions(96, 4, 40, 48_000, 2_000, 15_000, bottom_spacing=100))
+    h = terrain_heights({"kind": "schar", "height": .1, "width": 5, "wavelength": 4}, g)
+    n, layer, rho = g.nx * g.ny * g.nz, g.nx * g.ny, density(g)
+    u, v, w = np.full(n, 10, np.float32), np.zeros(n, np.float32), np.zeros(n, np.float32)
+    m = MaskedProjection(ctx, g, rho, h)
+    m.project(u, v, w, 1.0, np.zeros(layer * (g.nz - 1)))
+    f, (mx, my, mz, div), ref = faces_both(ctx, g, h, np.full(n, 10, np.float32), np.zeros(n, np.float32), np.zeros(n, np.float32))
+    for height in (1400, 2200, 3200):
+        z = next(k for k, q in enumerate(g.zs) if q >= height)
+        node = (w[z * layer:(z + 1) * layer].astype(float) + w[(z + 1) * layer:(z + 2) * layer]) / 2
+        face = mz[z * layer:(z + 1) * layer] / ((rho[z] + rho[z + 1]) / 2)
+        assert (node @ node) > 0 and .98 < float(face @ node) / float(node @ node) < 1.03
+    assert rel(mz, ref[2]) < 1e-8
+
+
+def test_transport_faces_short_solve_and_calm_air(ctx):
+    """Three iterations at most stop at three with the oracle's residual; calm air has nothing to project."""
+    from meteolab_gb300.runtime import terrain_heights
+    g = TEST_GRID
+    n = g.nx * g.ny * g.nz
+    h = terrain_heights({"kind": "plateau", "height": .5, "width": 8}, g)
+    zero = np.zeros(n, np.float32)
+    f, mine, ref = faces_both(ctx, g, h, zero, zero, zero)
+    assert f.iterations == 0 and f.residual == 0 and ref[4] == 0 and not any(a.any() for a in mine)
+    u = np.full(n, 10, np.float32)
+    f, mine, ref = faces_both(ctx, g, h, u, zero, zero, max_iterations=3)
+    assert f.iterations == 3 and ref[4] == 3 and abs(f.residual - ref[5]) < 1e-6 * ref[5] and rel(mine[2], ref[2]) < 1e-8
