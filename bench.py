@@ -421,6 +421,40 @@ def reference_arm(args, rank, pg):
     print(json.dumps(line), flush=True)
 
 
+def terrain_leg(ctx, grid, calls: int = 10):
+    """The terrain's two masked solves on the standard grid over a 1 km hill (5 km half-width), a 10 +- 2 m/s westerly
+    with random vertical motion: MaskedProjection.project (the pressure, to 1e-6) and the transport's
+    setVelocityMasked (the faces, to 1e-10), each one call with its host copies; median wall time of `calls` calls
+    after one warm-up, with the iterations each took."""
+    import numpy as np
+    from meteolab_gb300.runtime import MaskedProjection, TerrainFaces, terrain_heights
+    try:
+        h = terrain_heights({"kind": "hill", "height": 1, "width": 5}, grid)
+        rho = 1.2 * np.exp(-np.asarray(grid.zs) / 9000)
+        rng = np.random.default_rng(1)
+        u0 = (10 + rng.normal(0, 2, grid.n)).astype(np.float32)
+        v0 = rng.normal(0, 2, grid.n).astype(np.float32)
+        w0 = rng.normal(0, 1, grid.n).astype(np.float32)
+        cells = grid.nx * grid.ny * (grid.nz - 1)
+        m, f = MaskedProjection(ctx, grid, rho, h), TerrainFaces(ctx, grid, rho, h)
+        proj, faces = [], []
+        for k in range(calls + 1):
+            u, v, w, p = u0.copy(), v0.copy(), w0.copy(), np.zeros(cells)
+            t0 = time.perf_counter()
+            m.project(u, v, w, 3.0, p)
+            proj.append(time.perf_counter() - t0)
+            t0 = time.perf_counter()
+            f.set_velocity_masked(u0, v0, w0)
+            faces.append(time.perf_counter() - t0)
+        out = {"grid": "40x32x50", "form": "hill 1 km, half-width 5 km",
+               "projection": {"ms_per_call": 1e3 * float(np.median(proj[1:])), "iterations": m.iterations, "residual": m.residual},
+               "faces": {"ms_per_call": 1e3 * float(np.median(faces[1:])), "iterations": f.iterations, "residual": f.residual}}
+        m.close(); f.close()
+        return out
+    except Exception as e:  # the headline does not depend on this leg
+        return {"error": str(e)}
+
+
 def serving_leg(ctx, rate: float, count: int, quantum: int):
     """The serving configuration: an open Poisson stream of requests (seeded soundings, standard or large grid 3:1,
     400-1200 steps) through the continuous-batching loop. Time-to-completion runs from a request's arrival to its
@@ -619,6 +653,8 @@ def main():
     electric_ms = (time.perf_counter() - t0) / k * 1e3
     es.close()
 
+    terrain = terrain_leg(ctx, grid)
+
     uneven = uneven_leg(ctx, max(5, args.steps // 2), args.spinup)
     electrified = electrified_leg(ctx, members, runs, max(10, args.steps // 4)) if rank == 0 else None
     two_moment = two_moment_leg(ctx, members, runs, max(10, args.steps // 4)) if rank == 0 else None
@@ -661,6 +697,7 @@ def main():
         "batched_vs_plain_standard": value / world / plain["standard"]["graph_cell_steps_s"],
         "uneven_batch": uneven,
         "electric_solve": {"grid": "40x32x50", "ms_per_solve": electric_ms, "host_io_bytes": 2 * grid.n * 8},
+        "terrain": terrain,
         "electrified": electrified,
         "two_moment": two_moment,
         "serving": serving,
