@@ -3,11 +3,13 @@
 // slopeArea :141-150), and MaskedProjection (:168-363) on the device: the node mass flux rho0 u made divergence-free
 // over the dual cells cut by the ground. The masked operator S = -D M (rho0 H)^-1 D^T is solved by preconditioned
 // conjugate gradients with the flat operator's spectral inverse (PressureSolver.solve, src/core/pressure.ts:95-140) as
-// the preconditioner, all in FP64 as the reference.
+// the preconditioner, all in FP64 as the reference. The transport's faces with terrain (FluxTransport.setTerrain and
+// setVelocityMasked, src/core/advection.ts:78-184) are solved the same way over node vectors, with the flat face solve
+// as the preconditioner (sg_faces_*).
 //
 // Layout: velocities FP32 [n] (node x + nx (y + ny z)); the cells' vectors FP64 [nc * nx * ny], nc = nz - 1 (cell
 // x + nx (y + ny k) between node levels k and k + 1); spectra FP64 complex [nc][nx/2 + 1][ny]. One CG iteration is
-// nine launches: the cut cells' gradient of the search direction (a thread per node), its divergence fused with the
+// twelve launches: the cut cells' gradient of the search direction (a thread per node), its divergence fused with the
 // d.Sd partial sums (a thread per cell), the q/r update fused with the r.r partials, the preconditioner (x-DFT per row,
 // y-DFT per column, a Thomas sweep per mode over the levels, y- and x-inverse, the last fused with the r.z partials),
 // the direction update, and one-block reductions that finish each dot product in a fixed order (the result does not
